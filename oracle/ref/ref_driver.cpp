@@ -1,0 +1,263 @@
+// oracle/ref/ref_driver.cpp -- TEST INFRASTRUCTURE ONLY.
+//
+// C entry points (vref_*, declared in oracle/vibe_oracle.h) over the
+// reference's own compiled classes: grid::Grid, dyn::ReferenceState,
+// dyn::State, dyn::Equations, dyn::Advection, dyn::Damping,
+// timeint::AcousticSubstepper and driver::init_warm_bubble. Built by
+// oracle/Makefile (target `ref`) into oracle/_ref/ only.
+//
+// Restated glue (the reference's versions do not compile, see the notes):
+//   * vref_rk3_step follows RungeKutta3Integrator::step
+//     (src/time/runge_kutta.cpp:77-119). The shipped code calls
+//     State::add_scaled(Real, const Tendency&), which does not exist
+//     (runge_kutta.cpp:92 vs include/vibe/dyn/state.hpp:137-139); here that
+//     update is expanded field by field over the 12 species.
+//   * the acoustic substep follows runge_kutta.cpp:65-75 verbatim.
+//   * weno_scalars=1 replaces the non-conservative scalar advection of theta
+//     and the moisture species (src/dyn/equations.cpp:129-137) with
+//     Advection::scalar in WENO5 flux form (src/dyn/advection.cpp:144-187)
+//     and re-applies the positivity clip (equations.cpp:139-149).
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "../vibe_oracle.h"
+#include "vibe/common/constants.hpp"
+#include "vibe/config/config.hpp"
+#include "vibe/driver/initial_conditions.hpp"
+#include "vibe/dyn/advection.hpp"
+#include "vibe/dyn/equations.hpp"
+#include "vibe/dyn/reference_state.hpp"
+#include "vibe/dyn/state.hpp"
+#include "vibe/dyn/tendency.hpp"
+#include "vibe/grid/decomposition.hpp"
+#include "vibe/grid/geometry.hpp"
+#include "vibe/time/acoustic_substep.hpp"
+
+using namespace vibe;
+
+struct vref_model {
+  vo_setup setup{};
+  config::ModelConfig cfg;
+  std::unique_ptr<grid::Grid> grid;
+  std::unique_ptr<dyn::ReferenceState> ref;
+  std::unique_ptr<dyn::State> state;
+  std::unique_ptr<dyn::Equations> eq;
+  std::unique_ptr<dyn::Advection> weno;
+  std::unique_ptr<dyn::Tendency> slow, scratch;
+};
+
+namespace {
+
+const char* advection_name(int a) {
+  switch (a) {
+    case 4: return "central4";
+    case 6: return "central6";
+    case 5: return "weno5";
+    default: return "central2";
+  }
+}
+
+const grid::Field<Real>& reffield(const vref_model* m, int which) {
+  switch (which) {
+    case VO_THETA0: return m->ref->theta0();
+    case VO_PI0: return m->ref->pi0();
+    case VO_RHO0: return m->ref->rho0();
+    case VO_P0: return m->ref->p0();
+    default: return m->ref->qv0();
+  }
+}
+
+void slow_tendency(vref_model* m, dyn::State& s, dyn::Tendency& d) {
+  m->eq->tendencies(s, d);
+  if (!m->setup.weno_scalars) return;
+  const grid::Grid& g = *m->grid;
+  m->weno->scalar(s.theta(), s.u(), s.v(), s.w(), s.rho(), d.theta());
+  const int last = m->setup.moist ? static_cast<int>(dyn::Species::Qg)
+                                  : static_cast<int>(dyn::Species::Qv);
+  for (int sp = static_cast<int>(dyn::Species::Qv); sp <= last; ++sp) {
+    const auto species = static_cast<dyn::Species>(sp);
+    m->weno->scalar(s.field(species), s.u(), s.v(), s.w(), s.rho(), d.field(species));
+  }
+  for (int sp = static_cast<int>(dyn::Species::Qv); sp <= static_cast<int>(dyn::Species::Qg); ++sp) {
+    const auto species = static_cast<dyn::Species>(sp);
+    const grid::Field<Real>& q = s.field(species);
+    grid::Field<Real>& dq = d.field(species);
+    for (Int k = 0; k < g.nz(); ++k)
+      for (Int j = 0; j < g.ny(); ++j)
+        for (Int i = 0; i < g.nx(); ++i)
+          if (q(i, j, k) <= Real(0) && dq(i, j, k) < Real(0)) dq(i, j, k) = Real(0);
+  }
+}
+
+void acoustic_substep(vref_model* m, dyn::State& s, Real dtau) {
+  dyn::Tendency& sc = *m->scratch;
+  m->eq->acoustic_tendencies(s, sc);
+  s.rho().add_scaled(dtau, sc.rho());
+  s.pi().add_scaled(dtau, sc.pi());
+  m->eq->acoustic_tendencies(s, sc);
+  s.u().add_scaled(dtau, sc.u());
+  s.v().add_scaled(dtau, sc.v());
+  s.w().add_scaled(dtau, sc.w());
+}
+
+}  // namespace
+
+extern "C" {
+
+vref_model* vref_create(const vo_setup* su) {
+  auto* m = new vref_model();
+  m->setup = *su;
+  grid::Geometry geo;
+  geo.nx = su->nx;
+  geo.ny = su->ny;
+  geo.nz = su->nz;
+  geo.dx = su->dx;
+  geo.dy = su->dy;
+  geo.z_top = su->z_top;
+  geo.zeta = grid::make_stretched_zeta(su->nz, su->zeta_first, su->zeta_stretch);
+  if (su->terrain_kind == 1) {
+    geo.zs.assign(static_cast<Size>(su->nx) * static_cast<Size>(su->ny), Real(0));
+    for (Int j = 0; j < su->ny; ++j)
+      for (Int i = 0; i < su->nx; ++i) {
+        const Real x = (static_cast<Real>(i) + Real(0.5)) * su->dx - su->hill_xc;
+        const Real y = (static_cast<Real>(j) + Real(0.5)) * su->dy - su->hill_yc;
+        geo.zs[static_cast<Size>(j) * su->nx + i] =
+            su->hill_h * std::exp(-(x * x + y * y) / (su->hill_a * su->hill_a));
+      }
+  }
+  geo.name = "oracle";
+  auto dec = grid::Decomposition::make(su->nx, su->ny, su->nz, 1, 1, VO_HALO, false, false);
+  m->grid = std::make_unique<grid::Grid>(geo, dec);
+  const grid::Grid& g = *m->grid;
+
+  if (su->ref_kind == 1) {
+    std::vector<Real> z, th;
+    const int np = static_cast<int>(std::ceil(su->z_top / su->profile_dz)) + 2;
+    for (int p = 0; p < np; ++p) {
+      const Real zz = static_cast<Real>(p) * su->profile_dz;
+      z.push_back(zz);
+      th.push_back(su->theta0 * std::exp(su->bv_n * su->bv_n * zz / kGravity));
+    }
+    m->ref = std::make_unique<dyn::ReferenceState>(
+        dyn::ReferenceState::from_profile(g, z, th, su->p_surf));
+  } else {
+    m->ref = std::make_unique<dyn::ReferenceState>(
+        dyn::ReferenceState::isothermal(g, su->theta0, su->p_surf));
+  }
+
+  auto& c = m->cfg;
+  c.numerics.advection = advection_name(su->advection);
+  c.numerics.flux_form = true;
+  c.numerics.coriolis = su->coriolis == 0 ? "none" : (su->coriolis == 2 ? "betaplane" : "fplane");
+  c.numerics.fplane_latitude = su->latitude;
+  c.numerics.sponge_alpha = su->sponge_alpha;
+  c.numerics.sponge_start_fraction = su->sponge_start_fraction;
+  c.numerics.divergence_damping = su->divergence_damping;
+  c.numerics.divergence_order = su->divergence_order;
+  c.physics.microphysics = su->moist ? "kessler" : "none";
+  m->eq = std::make_unique<dyn::Equations>(g, *m->ref, c);
+  m->weno = std::make_unique<dyn::Advection>(g, dyn::AdvectionScheme::WENO5, true);
+  m->slow = std::make_unique<dyn::Tendency>(g);
+  m->scratch = std::make_unique<dyn::Tendency>(g);
+
+  m->state = std::make_unique<dyn::State>(g);
+  m->state->set_reference(m->ref.get());
+  driver::IcOptions opt;
+  opt.bubble_amplitude = su->bubble_amplitude;
+  opt.bubble_radius_x = su->bubble_radius_x;
+  opt.bubble_radius_z = su->bubble_radius_z;
+  opt.bubble_xc = su->bubble_xc;
+  opt.bubble_yc = su->bubble_yc;
+  opt.bubble_zc = su->bubble_zc;
+  opt.qv_surface = su->qv_surface;
+  opt.qv_decay_height = su->qv_decay_height;
+  opt.u_background = su->u_background;
+  opt.shear_u = su->shear_u;
+  driver::init_warm_bubble(g, *m->ref, *m->state, opt);
+  return m;
+}
+
+void vref_destroy(vref_model* m) { delete m; }
+
+size_t vref_storage_size(const vref_model* m, int species) {
+  return m->state->field(static_cast<dyn::Species>(species)).size();
+}
+
+void vref_get_field(const vref_model* m, int species, double* out) {
+  const auto& f = m->state->field(static_cast<dyn::Species>(species)).storage();
+  std::memcpy(out, f.data(), f.size() * sizeof(double));
+}
+
+void vref_set_field(vref_model* m, int species, const double* in) {
+  auto& f = m->state->field(static_cast<dyn::Species>(species)).storage();
+  std::memcpy(f.data(), in, f.size() * sizeof(double));
+}
+
+void vref_get_reffield(const vref_model* m, int which, double* out) {
+  const auto& f = reffield(m, which).storage();
+  std::memcpy(out, f.data(), f.size() * sizeof(double));
+}
+
+void vref_get_zeta(const vref_model* m, double* out) {
+  const auto& z = m->grid->geom().zeta;
+  std::memcpy(out, z.data(), z.size() * sizeof(double));
+}
+
+void vref_get_terrain(const vref_model* m, double* out) {
+  const grid::Grid& g = *m->grid;
+  for (Int j = 0; j < g.ny(); ++j)
+    for (Int i = 0; i < g.nx(); ++i) out[static_cast<Size>(j) * g.nx() + i] = g.terrain(i, j);
+}
+
+void vref_get_sponge(const vref_model* m, double* out) {
+  const auto& sp = m->eq->damping().sponge_profile();
+  std::memcpy(out, sp.data(), sp.size() * sizeof(double));
+}
+
+int vref_rk3_step(vref_model* m, double dt, int n_sub_in) {
+  dyn::State& s = *m->state;
+  const int n_sub = std::max(n_sub_in, 1);
+  const dyn::State s0 = s.clone();
+  const Real dt_stage[3] = {dt / Real(3), dt / Real(2), dt};
+  for (int stage = 0; stage < 3; ++stage) {
+    slow_tendency(m, s, *m->slow);
+    s = s0;
+    for (int sp = 0; sp < dyn::kNumSpecies; ++sp) {
+      const auto species = static_cast<dyn::Species>(sp);
+      s.field(species).add_scaled(dt_stage[stage], m->slow->field(species));
+    }
+    const Real dtau_stage = dt_stage[stage] / static_cast<Real>(n_sub);
+    for (int n = 0; n < n_sub; ++n) acoustic_substep(m, s, dtau_stage);
+    if (s.has_nonfinite()) return 1;
+  }
+  m->eq->damping().apply_sponge(s, *m->ref, dt);
+  s.step += 1;
+  return 0;
+}
+
+void vref_slow_tendency(vref_model* m, double* const* out) {
+  slow_tendency(m, *m->state, *m->slow);
+  for (int sp = 0; sp < dyn::kNumSpecies; ++sp) {
+    const auto& f = m->slow->field(static_cast<dyn::Species>(sp)).storage();
+    std::memcpy(out[sp], f.data(), f.size() * sizeof(double));
+  }
+}
+
+void vref_acoustic_substep(vref_model* m, double dtau) { acoustic_substep(m, *m->state, dtau); }
+
+void vref_hevi_substep(vref_model* m, double dtau) {
+  timeint::AcousticOptions opt;
+  opt.vertical_implicit = true;
+  timeint::AcousticSubstepper sub(*m->grid, opt);
+  sub.step(*m->state, dtau, *m->ref);
+}
+
+void vref_sponge(vref_model* m, double dt) {
+  m->eq->damping().apply_sponge(*m->state, *m->ref, dt);
+}
+
+}  // extern "C"

@@ -1,0 +1,1178 @@
+/* oracle/vibe_oracle.c -- TEST INFRASTRUCTURE ONLY.
+ *
+ * Plain-C, serial, FP64 restatement of the VIBE-Model dynamics step as the
+ * reference's source computes it. Every routine cites the reference
+ * file:line it follows and keeps that code's floating-point operation order,
+ * so that, built with -ffp-contract=off, it reproduces the reference compiled
+ * unchanged (oracle/_ref) bit for bit in pgf_perturbation=0 mode.
+ *
+ * Used only by tests/, __graft_entry__.smoke() and bench.py's CPU-baseline
+ * leg, always as the checker -- never on the product path.
+ */
+#include "vibe_oracle.h"
+
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+
+/* include/vibe/common/constants.hpp:16-60 */
+#define K_GRAVITY 9.80665
+#define K_RD 287.05
+#define K_CP 1004.64
+#define K_CV 717.63
+#define K_EPS_VAP 0.62197
+#define K_P0 100000.0
+#define K_PI 3.14159265358979323846
+#define K_OMEGA 7.2921159e-5
+#define K_EARTH_RADIUS 6.371229e6
+#define K_DEG2RAD (K_PI / 180.0)
+#define K_BUOY_MOIST 0.608 /* equations.cpp:40 */
+
+/* std::max / std::min / clamp semantics (include/vibe/common/types.hpp:83) */
+static inline double dmax(double a, double b) { return (a < b) ? b : a; }
+static inline double dmin(double a, double b) { return (b < a) ? b : a; }
+static inline int imax(int a, int b) { return (a < b) ? b : a; }
+static inline int imin(int a, int b) { return (b < a) ? b : a; }
+static inline int iclamp(int v, int lo, int hi) { return v < lo ? lo : (v > hi ? hi : v); }
+static inline double sqr(double x) { return x * x; }
+static inline double lerp(double a, double b, double w) { return a + w * (b - a); }
+
+/* ------------------------------------------------------------------------ */
+/* field storage: include/vibe/grid/field.hpp:40-96                          */
+/* ------------------------------------------------------------------------ */
+typedef struct {
+  int nx, ny, nz;    /* grid interior sizes (same for every stagger) */
+  int nsx, nsy, nsz; /* storage sizes incl. halo and the +1 face     */
+  double *d;
+} fld;
+
+static void fld_alloc(fld *f, int nx, int ny, int nz, int stagger) {
+  f->nx = nx; f->ny = ny; f->nz = nz;
+  f->nsx = nx + 2 * VO_HALO + (stagger == 1);
+  f->nsy = ny + 2 * VO_HALO + (stagger == 2);
+  f->nsz = nz + 2 * VO_HALO + (stagger == 3);
+  f->d = (double *)calloc((size_t)f->nsx * f->nsy * f->nsz, sizeof(double));
+}
+static size_t fld_size(const fld *f) { return (size_t)f->nsx * f->nsy * f->nsz; }
+static void fld_zero(fld *f) { memset(f->d, 0, fld_size(f) * sizeof(double)); }
+/* FieldT::offset (field.hpp:77-81) */
+#define AT(f, i, j, k) \
+  ((f).d[(size_t)((((k) + VO_HALO) * (f).nsy + ((j) + VO_HALO)) * (f).nsx + ((i) + VO_HALO))])
+/* FieldT::clamp_at (field.hpp:91-96): clamps to the CELL interior for every stagger */
+static inline double CL(const fld *f, int i, int j, int k) {
+  return AT(*f, iclamp(i, 0, f->nx - 1), iclamp(j, 0, f->ny - 1), iclamp(k, 0, f->nz - 1));
+}
+
+static int stagger_of(int sp) { return sp == VO_U ? 1 : sp == VO_V ? 2 : sp == VO_W ? 3 : 0; }
+
+struct vo_model {
+  vo_setup s;
+  int nx, ny, nz;
+  double *zeta;   /* nz+1 */
+  double *zs;     /* nx*ny terrain */
+  double *sponge; /* nz */
+  fld st[VO_NSPECIES];
+  fld s0[VO_NSPECIES];
+  fld slow[VO_NSPECIES];
+  fld scr[VO_NSPECIES];
+  fld ref[5];     /* theta0, pi0, rho0, p0, qv0 */
+  double f0, beta;
+};
+
+/* ------------------------------------------------------------------------ */
+/* grid metrics: src/grid/geometry.cpp                                      */
+/* ------------------------------------------------------------------------ */
+
+/* make_stretched_zeta, geometry.cpp:39-60 */
+static void make_stretched_zeta(int nz, double first, double stretch, double *zeta) {
+  double *dz = (double *)malloc(sizeof(double) * (size_t)nz);
+  double total = 0.0, h = first, acc = 0.0;
+  for (int k = 0; k < nz; ++k) { dz[k] = h; total += h; h *= stretch; }
+  zeta[0] = 0.0;
+  for (int k = 0; k < nz; ++k) { acc += dz[k]; zeta[k + 1] = acc / total; }
+  zeta[nz] = 1.0;
+  free(dz);
+}
+
+/* Grid::dzeta, geometry.cpp:242-245 */
+static inline double g_dzeta(const vo_model *m, int k) {
+  const int kk = iclamp(k, 0, m->nz - 1);
+  return m->zeta[kk + 1] - m->zeta[kk];
+}
+/* Grid::terrain, geometry.cpp:247-253 */
+static inline double g_terrain(const vo_model *m, int i, int j) {
+  return m->zs[(size_t)iclamp(j, 0, m->ny - 1) * m->nx + iclamp(i, 0, m->nx - 1)];
+}
+/* zeta_at, geometry.cpp:20-31 */
+static double zeta_at(const vo_model *m, double kk) {
+  const int nz = m->nz;
+  if (kk <= 0.0) return m->zeta[0];
+  if (kk >= (double)nz) return m->zeta[nz];
+  const int k0 = (int)floor(kk);
+  const double frac = kk - (double)k0;
+  if (frac == 0.0) return m->zeta[k0];
+  if (fabs(frac - 0.5) < 1e-12) return 0.5 * (m->zeta[k0] + m->zeta[k0 + 1]);
+  return lerp(m->zeta[k0], m->zeta[k0 + 1], frac);
+}
+/* Grid::height, geometry.cpp:260-263; z_center/z_interface geometry.hpp:135-139 */
+static double g_height(const vo_model *m, int i, int j, double kk) {
+  const double zs = g_terrain(m, i, j);
+  return zs + zeta_at(m, kk) * (m->s.z_top - zs);
+}
+static double g_zc(const vo_model *m, int i, int j, int k) { return g_height(m, i, j, (double)k + 0.5); }
+
+/* ------------------------------------------------------------------------ */
+/* reference state: src/dyn/reference_state.cpp                             */
+/* ------------------------------------------------------------------------ */
+static double density_from(double pi0, double theta0) { /* :26-28 */
+  return K_P0 * pow(pi0, K_CV / K_RD) / (K_RD * theta0);
+}
+static double pressure_from(double pi0) { return K_P0 * pow(pi0, K_CP / K_RD); } /* :31 */
+
+static void ref_isothermal(vo_model *m) { /* :35-59 */
+  const double th = m->s.theta0;
+  const double pi_surf = pow(m->s.p_surf / K_P0, K_RD / K_CP);
+  for (int k = 0; k < m->nz; ++k)
+    for (int j = 0; j < m->ny; ++j)
+      for (int i = 0; i < m->nx; ++i) {
+        const double z = g_zc(m, i, j, k);
+        const double pi = pi_surf - K_GRAVITY * z / (K_CP * th);
+        AT(m->ref[VO_THETA0], i, j, k) = th;
+        AT(m->ref[VO_PI0], i, j, k) = pi;
+        AT(m->ref[VO_P0], i, j, k) = pressure_from(pi);
+        AT(m->ref[VO_RHO0], i, j, k) = density_from(pi, th);
+        AT(m->ref[VO_QV0], i, j, k) = 0.0;
+      }
+}
+
+static void ref_from_profile(vo_model *m) { /* :61-110 */
+  const int np = (int)ceil(m->s.z_top / m->s.profile_dz) + 2;
+  double *z = (double *)malloc(sizeof(double) * (size_t)np);
+  double *th = (double *)malloc(sizeof(double) * (size_t)np);
+  double *zi = (double *)malloc(sizeof(double) * (size_t)(m->nz + 1));
+  for (int p = 0; p < np; ++p) {
+    z[p] = (double)p * m->s.profile_dz;
+    th[p] = m->s.theta0 * exp(m->s.bv_n * m->s.bv_n * z[p] / K_GRAVITY);
+  }
+  const double pi_surf = pow(m->s.p_surf / K_P0, K_RD / K_CP);
+#define THETA_AT(zz, out)                                                   \
+  do {                                                                      \
+    const double zz_ = (zz);                                                \
+    if (zz_ <= z[0]) { out = th[0]; }                                       \
+    else if (zz_ >= z[np - 1]) { out = th[np - 1]; }                        \
+    else {                                                                  \
+      size_t kk_ = 0;                                                       \
+      while (kk_ + 2 < (size_t)np && z[kk_ + 1] < zz_) ++kk_;               \
+      const double w_ = (z[kk_ + 1] - z[kk_] > 0.0)                         \
+                            ? (zz_ - z[kk_]) / (z[kk_ + 1] - z[kk_]) : 0.0; \
+      out = lerp(th[kk_], th[kk_ + 1], w_);                                 \
+    }                                                                       \
+  } while (0)
+  for (int j = 0; j < m->ny; ++j)
+    for (int i = 0; i < m->nx; ++i) {
+      for (int k = 0; k <= m->nz; ++k) zi[k] = g_height(m, i, j, (double)k);
+      double pi = pi_surf, th_surf;
+      THETA_AT(zi[0], th_surf);
+      AT(m->ref[VO_THETA0], i, j, 0) = th_surf;
+      for (int k = 0; k < m->nz; ++k) {
+        double th_lo, th_hi;
+        THETA_AT(zi[k], th_lo);
+        THETA_AT(zi[k + 1], th_hi);
+        const double th_mid = 0.5 * (th_lo + th_hi);
+        const double dz = zi[k + 1] - zi[k];
+        pi -= K_GRAVITY * dz / (K_CP * th_mid);
+        const double th_c = 0.5 * (th_lo + th_hi);
+        AT(m->ref[VO_THETA0], i, j, k) = th_c;
+        AT(m->ref[VO_PI0], i, j, k) = pi;
+        AT(m->ref[VO_P0], i, j, k) = pressure_from(pi);
+        AT(m->ref[VO_RHO0], i, j, k) = density_from(pi, th_c);
+        AT(m->ref[VO_QV0], i, j, k) = 0.0;
+      }
+    }
+#undef THETA_AT
+  free(z); free(th); free(zi);
+}
+
+/* ------------------------------------------------------------------------ */
+/* initial conditions: src/driver/initial_conditions.cpp                     */
+/* ------------------------------------------------------------------------ */
+static void enforce_state_equation(vo_model *m) { /* :110-121 */
+  for (int k = 0; k < m->nz; ++k)
+    for (int j = 0; j < m->ny; ++j)
+      for (int i = 0; i < m->nx; ++i) {
+        const double qv = dmax(AT(m->st[VO_QV], i, j, k), 0.0);
+        const double gamma_f = (1.0 + qv / K_EPS_VAP) / (1.0 + qv);
+        const double val = AT(m->st[VO_RHO], i, j, k) * K_RD * AT(m->st[VO_THETA], i, j, k) * gamma_f / K_P0;
+        if (val > 0.0) AT(m->st[VO_PI], i, j, k) = pow(val, K_RD / K_CV);
+      }
+}
+
+static void init_warm_bubble(vo_model *m) { /* :136-159 with fill_base_state :66-91 */
+  const vo_setup *s = &m->s;
+  for (int k = 0; k < m->nz; ++k)
+    for (int j = 0; j < m->ny; ++j)
+      for (int i = 0; i < m->nx; ++i) {
+        const double z = g_zc(m, i, j, k);
+        AT(m->st[VO_THETA], i, j, k) = AT(m->ref[VO_THETA0], i, j, k);
+        AT(m->st[VO_PI], i, j, k) = AT(m->ref[VO_PI0], i, j, k);
+        AT(m->st[VO_RHO], i, j, k) = AT(m->ref[VO_RHO0], i, j, k);
+        AT(m->st[VO_QV], i, j, k) = s->qv_surface * exp(-dmax(z, 0.0) / s->qv_decay_height);
+        for (int sp = VO_QC; sp <= VO_QG; ++sp) AT(m->st[sp], i, j, k) = 0.0;
+      }
+  fld_zero(&m->st[VO_U]); fld_zero(&m->st[VO_V]); fld_zero(&m->st[VO_W]);
+  const double xc = (s->bubble_xc != 0.0) ? s->bubble_xc : 0.5 * 0.0 + 0.5 * (double)m->nx * s->dx;
+  const double yc = (s->bubble_yc != 0.0) ? s->bubble_yc : 0.5 * (double)m->ny * s->dy;
+  for (int k = 0; k < m->nz; ++k)
+    for (int j = 0; j < m->ny; ++j)
+      for (int i = 0; i < m->nx; ++i) {
+        const double x = (0 + (double)i + 0.5) * s->dx;
+        const double y = (0 + (double)j + 0.5) * s->dy;
+        const double z = g_zc(m, i, j, k);
+        const double r2 = sqr((x - xc) / s->bubble_radius_x) + sqr((y - yc) / s->bubble_radius_x) +
+                          sqr((z - s->bubble_zc) / s->bubble_radius_z);
+        if (r2 < 1.0) {
+          const double c = cos(0.5 * K_PI * sqrt(r2));
+          AT(m->st[VO_THETA], i, j, k) += s->bubble_amplitude * c * c;
+        }
+      }
+  /* apply_shear :94-102 */
+  for (int k = 0; k < m->nz; ++k)
+    for (int j = 0; j < m->ny; ++j)
+      for (int i = 0; i <= m->nx; ++i) {
+        const double z = g_zc(m, imin(i, m->nx - 1), j, k);
+        AT(m->st[VO_U], i, j, k) = s->u_background + s->shear_u * z;
+      }
+  enforce_state_equation(m);
+}
+
+/* ------------------------------------------------------------------------ */
+/* advection: src/dyn/advection.cpp                                          */
+/* ------------------------------------------------------------------------ */
+
+/* Advection::weno5_reconstruct, advection.cpp:62-98 */
+static void weno5(double qm2, double qm1, double q0, double q1, double q2, double *ql, double *qr) {
+  const double eps = 1e-6;
+  const double d0 = 0.1, d1 = 0.6, d2 = 0.3;
+  const double v0 = (2.0 * qm2 - 7.0 * qm1 + 11.0 * q0) / 6.0;
+  const double v1 = (-qm1 + 5.0 * q0 + 2.0 * q1) / 6.0;
+  const double v2 = (2.0 * q0 + 5.0 * q1 - q2) / 6.0;
+  const double b0 = (13.0 / 12.0) * sqr(qm2 - 2.0 * qm1 + q0) + 0.25 * sqr(qm2 - 4.0 * qm1 + 3.0 * q0);
+  const double b1 = (13.0 / 12.0) * sqr(qm1 - 2.0 * q0 + q1) + 0.25 * sqr(qm1 - q1);
+  const double b2 = (13.0 / 12.0) * sqr(q0 - 2.0 * q1 + q2) + 0.25 * sqr(3.0 * q0 - 4.0 * q1 + q2);
+  const double a0 = d0 / sqr(eps + b0);
+  const double a1 = d1 / sqr(eps + b1);
+  const double a2 = d2 / sqr(eps + b2);
+  const double wsum = a0 + a1 + a2;
+  *ql = (a0 * v0 + a1 * v1 + a2 * v2) / wsum;
+  const double u0 = (2.0 * q2 - 7.0 * q1 + 11.0 * q0) / 6.0;
+  const double u1 = (-q1 + 5.0 * q0 + 2.0 * qm1) / 6.0;
+  const double u2 = (2.0 * q0 + 5.0 * qm1 - qm2) / 6.0;
+  const double g0 = (13.0 / 12.0) * sqr(q2 - 2.0 * q1 + q0) + 0.25 * sqr(q2 - 4.0 * q1 + 3.0 * q0);
+  const double g1 = (13.0 / 12.0) * sqr(q1 - 2.0 * q0 + qm1) + 0.25 * sqr(q1 - qm1);
+  const double g2 = (13.0 / 12.0) * sqr(q0 - 2.0 * qm1 + qm2) + 0.25 * sqr(3.0 * q0 - 4.0 * qm1 + qm2);
+  const double c0 = d0 / sqr(eps + g0);
+  const double c1 = d1 / sqr(eps + g1);
+  const double c2 = d2 / sqr(eps + g2);
+  const double wsum2 = c0 + c1 + c2;
+  *qr = (c0 * u0 + c1 * u1 + c2 * u2) / wsum2;
+}
+
+/* reconstruct_face lambda with local Lax-Friedrichs split, advection.cpp:151-156 */
+static inline double weno_face(double qm2, double qm1, double q0, double q1, double q2, double vel) {
+  double ql, qr;
+  weno5(qm2, qm1, q0, q1, q2, &ql, &qr);
+  const double alpha = dmax(fabs(vel), 1e-3);
+  return 0.5 * (vel * (ql + qr) - alpha * (qr - ql));
+}
+
+/* Advection::scalar, WENO5 branch, advection.cpp:144-187 */
+static void advect_weno5(const vo_model *m, const fld *q, const fld *u, const fld *v, const fld *w, fld *dq) {
+  const int nx = m->nx, ny = m->ny, nz = m->nz;
+  for (int k = 0; k < nz; ++k)
+    for (int j = 0; j < ny; ++j)
+      for (int i = 0; i < nx; ++i) {
+        const double dx = m->s.dx, dy = m->s.dy;
+        const double dz = g_dzeta(m, k) * (m->s.z_top - g_terrain(m, i, j));
+        const double fe = weno_face(CL(q, i - 2, j, k), CL(q, i - 1, j, k), AT(*q, i, j, k),
+                                    CL(q, i + 1, j, k), CL(q, i + 2, j, k), AT(*u, i + 1, j, k));
+        const double fw = weno_face(CL(q, i - 3, j, k), CL(q, i - 2, j, k), CL(q, i - 1, j, k),
+                                    AT(*q, i, j, k), CL(q, i + 1, j, k), AT(*u, i, j, k));
+        const double fn = weno_face(CL(q, i, j - 2, k), CL(q, i, j - 1, k), AT(*q, i, j, k),
+                                    CL(q, i, j + 1, k), CL(q, i, j + 2, k), AT(*v, i, j + 1, k));
+        const double fs = weno_face(CL(q, i, j - 3, k), CL(q, i, j - 2, k), CL(q, i, j - 1, k),
+                                    AT(*q, i, j, k), CL(q, i, j + 1, k), AT(*v, i, j, k));
+        double ft = 0.0, fb = 0.0;
+        if (k + 2 < nz || k >= 2) {
+          ft = weno_face(CL(q, i, j, k - 2), CL(q, i, j, k - 1), AT(*q, i, j, k),
+                         CL(q, i, j, k + 1), CL(q, i, j, k + 2), AT(*w, i, j, k + 1));
+          fb = weno_face(CL(q, i, j, k - 3), CL(q, i, j, k - 2), CL(q, i, j, k - 1),
+                         AT(*q, i, j, k), CL(q, i, j, k + 1), AT(*w, i, j, k));
+        }
+        AT(*dq, i, j, k) = -(fe - fw) / dx - (fn - fs) / dy - (ft - fb) / dz;
+        if (m->s.weno_advective) {
+          double div = (AT(*u, i + 1, j, k) - AT(*u, i, j, k)) / dx + (AT(*v, i, j + 1, k) - AT(*v, i, j, k)) / dy;
+          if (k + 2 < nz || k >= 2) div += (AT(*w, i, j, k + 1) - AT(*w, i, j, k)) / dz;
+          AT(*dq, i, j, k) += AT(*q, i, j, k) * div;
+        }
+      }
+}
+
+/* grad_x / grad_y, advection.cpp:106-136 */
+static inline double grad_x(const fld *q, int i, int j, int k, double inv_dx, int order) {
+  switch (order) {
+    case 4:
+      return (CL(q, i - 2, j, k) - 8.0 * CL(q, i - 1, j, k) + 8.0 * CL(q, i + 1, j, k) - CL(q, i + 2, j, k)) *
+             (inv_dx / 12.0);
+    case 6:
+      return (-CL(q, i - 3, j, k) + 9.0 * CL(q, i - 2, j, k) - 45.0 * CL(q, i - 1, j, k) +
+              45.0 * CL(q, i + 1, j, k) - 9.0 * CL(q, i + 2, j, k) + CL(q, i + 3, j, k)) *
+             (inv_dx / 60.0);
+    default:
+      return (CL(q, i + 1, j, k) - CL(q, i - 1, j, k)) * (0.5 * inv_dx);
+  }
+}
+static inline double grad_y(const fld *q, int i, int j, int k, double inv_dy, int order) {
+  switch (order) {
+    case 4:
+      return (CL(q, i, j - 2, k) - 8.0 * CL(q, i, j - 1, k) + 8.0 * CL(q, i, j + 1, k) - CL(q, i, j + 2, k)) *
+             (inv_dy / 12.0);
+    case 6:
+      return (-CL(q, i, j - 3, k) + 9.0 * CL(q, i, j - 2, k) - 45.0 * CL(q, i, j - 1, k) +
+              45.0 * CL(q, i, j + 1, k) - 9.0 * CL(q, i, j + 2, k) + CL(q, i, j + 3, k)) *
+             (inv_dy / 60.0);
+    default:
+      return (CL(q, i, j + 1, k) - CL(q, i, j - 1, k)) * (0.5 * inv_dy);
+  }
+}
+
+/* Advection constructor order_ (advection.cpp:44-52): weno5 -> 5, which the
+ * switches above treat as 2nd order. */
+static int adv_order(const vo_model *m) { return m->s.advection; }
+
+/* Advection::scalar_nonconservative, advection.cpp:224-244 */
+static void advect_nonconservative(const vo_model *m, const fld *q, const fld *u, const fld *v, const fld *w, fld *dq) {
+  const int order = adv_order(m);
+  for (int k = 0; k < m->nz; ++k)
+    for (int j = 0; j < m->ny; ++j)
+      for (int i = 0; i < m->nx; ++i) {
+        const double dx = m->s.dx, dy = m->s.dy;
+        const double scale = m->s.z_top - g_terrain(m, i, j);
+        const double dz = g_dzeta(m, k) * scale;
+        const double ua = 0.5 * (AT(*u, i, j, k) + AT(*u, i + 1, j, k));
+        const double va = 0.5 * (AT(*v, i, j, k) + AT(*v, i, j + 1, k));
+        const double wa = 0.5 * (AT(*w, i, j, k) + AT(*w, i, j, k + 1));
+        AT(*dq, i, j, k) = -(ua * grad_x(q, i, j, k, 1.0 / dx, order) + va * grad_y(q, i, j, k, 1.0 / dy, order) +
+                             wa * (CL(q, i, j, k + 1) - CL(q, i, j, k - 1)) * (0.5 / dz));
+      }
+}
+
+/* Advection::momentum, advection.cpp:250-319 */
+static void advect_momentum(const vo_model *m, fld *st, fld *d) {
+  const int nx = m->nx, ny = m->ny, nz = m->nz;
+  const fld *u = &st[VO_U], *v = &st[VO_V], *w = &st[VO_W];
+  fld *du = &d[VO_U], *dv = &d[VO_V], *dw = &d[VO_W];
+  for (int k = 0; k < nz; ++k)
+    for (int j = 0; j < ny; ++j)
+      for (int i = 0; i <= nx; ++i) {
+        const int ip = imin(i, nx - 1);
+        const double dx = m->s.dx, dy = m->s.dy;
+        const double scale = m->s.z_top - g_terrain(m, ip, j);
+        const double dz = g_dzeta(m, imin(k, nz - 1)) * scale;
+        const double uc = 0.5 * (AT(*u, imax(i - 1, 0), j, k) + AT(*u, ip, j, k));
+        const double ux = (AT(*u, ip, j, k) - AT(*u, imax(i - 1, 0), j, k)) / dx;
+        const double uy = (AT(*u, ip, imin(j + 1, ny - 1), k) - AT(*u, ip, imax(j - 1, 0), k)) / (2.0 * dy);
+        const double uz = (AT(*u, ip, j, imin(k + 1, nz - 1)) - AT(*u, ip, j, imax(k - 1, 0))) / (2.0 * dz);
+        const double vc = 0.25 * (AT(*v, imax(i - 1, 0), imax(j - 1, 0), k) + AT(*v, ip, imax(j - 1, 0), k) +
+                                  AT(*v, imax(i - 1, 0), j, k) + AT(*v, ip, j, k));
+        const double wc = 0.5 * (AT(*w, ip, j, k) + AT(*w, ip, j, imin(k + 1, nz - 1)));
+        AT(*du, i, j, k) -= uc * ux + vc * uy + wc * uz;
+      }
+  for (int k = 0; k < nz; ++k)
+    for (int j = 0; j <= ny; ++j)
+      for (int i = 0; i < nx; ++i) {
+        const int jp = imin(j, ny - 1);
+        const double dx = m->s.dx, dy = m->s.dy;
+        const double scale = m->s.z_top - g_terrain(m, i, jp);
+        const double dz = g_dzeta(m, imin(k, nz - 1)) * scale;
+        const double vc = 0.5 * (AT(*v, i, imax(j - 1, 0), k) + AT(*v, i, jp, k));
+        const double vy = (AT(*v, i, jp, k) - AT(*v, i, imax(j - 1, 0), k)) / dy;
+        const double vx = (AT(*v, imin(i + 1, nx - 1), jp, k) - AT(*v, imax(i - 1, 0), jp, k)) / (2.0 * dx);
+        const double vz = (AT(*v, i, jp, imin(k + 1, nz - 1)) - AT(*v, i, jp, imax(k - 1, 0))) / (2.0 * dz);
+        const double uc = 0.25 * (AT(*u, imax(i - 1, 0), imax(j - 1, 0), k) + AT(*u, i, imax(j - 1, 0), k) +
+                                  AT(*u, imax(i - 1, 0), jp, k) + AT(*u, i, jp, k));
+        const double wc = 0.5 * (AT(*w, i, jp, k) + AT(*w, i, jp, imin(k + 1, nz - 1)));
+        AT(*dv, i, j, k) -= uc * vx + vc * vy + wc * vz;
+      }
+  for (int k = 0; k <= nz; ++k)
+    for (int j = 0; j < ny; ++j)
+      for (int i = 0; i < nx; ++i) {
+        const int kc = imin(imax(k, 0), nz - 1);
+        const double dx = m->s.dx, dy = m->s.dy;
+        const double scale = m->s.z_top - g_terrain(m, i, j);
+        const double dz = g_dzeta(m, kc) * scale;
+        const double wc = 0.5 * (AT(*w, i, j, kc) + AT(*w, i, j, imin(k, nz)));
+        const double wz = (AT(*w, i, j, imin(k, nz)) - AT(*w, i, j, imax(k - 1, 0))) / dz;
+        const double wx = (AT(*w, imin(i + 1, nx - 1), j, imin(k, nz)) - AT(*w, imax(i - 1, 0), j, imin(k, nz))) / (2.0 * dx);
+        const double wy = (AT(*w, i, imin(j + 1, ny - 1), imin(k, nz)) - AT(*w, i, imax(j - 1, 0), imin(k, nz))) / (2.0 * dy);
+        const double uc = 0.5 * (AT(*u, i, j, kc) + AT(*u, i + 1, j, kc));
+        const double vc = 0.5 * (AT(*v, i, j, kc) + AT(*v, i, j + 1, kc));
+        AT(*dw, i, j, k) -= uc * wx + vc * wy + wc * wz;
+      }
+}
+
+/* Coriolis::f_at / apply, coriolis.cpp:25-70 */
+static double cor_f(const vo_model *m, int j) {
+  if (m->s.coriolis != 2) return m->f0;
+  const double y = (0.0 + (double)j + 0.5) * m->s.dy;
+  const double y0 = 0.5 * (double)m->ny * m->s.dy;
+  return m->f0 + m->beta * (y - y0);
+}
+static void coriolis_apply(const vo_model *m, fld *st, fld *d) {
+  if (m->s.coriolis == 0) return;
+  const int nx = m->nx, ny = m->ny, nz = m->nz;
+  const fld *u = &st[VO_U], *v = &st[VO_V];
+  for (int k = 0; k < nz; ++k)
+    for (int j = 0; j < ny; ++j)
+      for (int i = 0; i <= nx; ++i) {
+        const double v_at_u = 0.25 * (AT(*v, imax(i - 1, 0), imax(j - 1, 0), k) + AT(*v, imin(i, nx - 1), imax(j - 1, 0), k) +
+                                      AT(*v, imax(i - 1, 0), j, k) + AT(*v, imin(i, nx - 1), j, k));
+        AT(d[VO_U], i, j, k) += cor_f(m, j) * v_at_u;
+      }
+  for (int k = 0; k < nz; ++k)
+    for (int j = 0; j <= ny; ++j)
+      for (int i = 0; i < nx; ++i) {
+        const double u_at_v = 0.25 * (AT(*u, imax(i - 1, 0), imax(j - 1, 0), k) + AT(*u, i, imax(j - 1, 0), k) +
+                                      AT(*u, imax(i - 1, 0), imin(j, ny - 1), k) + AT(*u, i, imin(j, ny - 1), k));
+        AT(d[VO_V], i, j, k) -= cor_f(m, j) * u_at_v;
+      }
+}
+
+/* Damping::tendencies (divergence damping), damping.cpp:43-74 */
+static double lap2(const vo_model *m, const fld *f, int i, int j, int k) {
+  const double dx = m->s.dx, dy = m->s.dy;
+  return (CL(f, i + 1, j, k) - 2.0 * AT(*f, i, j, k) + CL(f, i - 1, j, k)) / (dx * dx) +
+         (CL(f, i, j + 1, k) - 2.0 * AT(*f, i, j, k) + CL(f, i, j - 1, k)) / (dy * dy);
+}
+static void damping_tendencies(const vo_model *m, fld *st, fld *d) {
+  if (m->s.divergence_damping <= 0.0) return;
+  const double nu = m->s.divergence_damping;
+  const fld *pi = &st[VO_PI];
+  if (m->s.divergence_order <= 2) {
+    for (int k = 0; k < m->nz; ++k)
+      for (int j = 0; j < m->ny; ++j)
+        for (int i = 0; i < m->nx; ++i) AT(d[VO_PI], i, j, k) -= nu * lap2(m, pi, i, j, k);
+  } else {
+    fld tmp;
+    fld_alloc(&tmp, m->nx, m->ny, m->nz, 0);
+    for (int k = 0; k < m->nz; ++k)
+      for (int j = 0; j < m->ny; ++j)
+        for (int i = 0; i < m->nx; ++i) AT(tmp, i, j, k) = lap2(m, pi, i, j, k);
+    for (int k = 0; k < m->nz; ++k)
+      for (int j = 0; j < m->ny; ++j)
+        for (int i = 0; i < m->nx; ++i) AT(d[VO_PI], i, j, k) -= nu * lap2(m, &tmp, i, j, k);
+    free(tmp.d);
+  }
+}
+
+/* Exner difference used by every pressure-gradient term: total pi as the
+ * reference code computes it, or pi' = pi - pi0 in the documented form. */
+static inline double dpi(const vo_model *m, const fld *pi, int ia, int ja, int ka, int ib, int jb, int kb) {
+  if (!m->s.pgf_perturbation) return AT(*pi, ia, ja, ka) - AT(*pi, ib, jb, kb);
+  return (AT(*pi, ia, ja, ka) - AT(m->ref[VO_PI0], ia, ja, ka)) -
+         (AT(*pi, ib, jb, kb) - AT(m->ref[VO_PI0], ib, jb, kb));
+}
+
+/* Equations::tendencies, equations.cpp:60-150 (+ the O-WENO override of the
+ * scalar advection when weno_scalars is set). */
+static void slow_tendency(vo_model *m, fld *st, fld *d) {
+  const int nx = m->nx, ny = m->ny, nz = m->nz;
+  for (int sp = 0; sp < VO_NSPECIES; ++sp) fld_zero(&d[sp]);
+  advect_momentum(m, st, d);
+  coriolis_apply(m, st, d);
+  damping_tendencies(m, st, d);
+  const fld *th = &st[VO_THETA], *pi = &st[VO_PI], *rho = &st[VO_RHO];
+  for (int k = 0; k < nz; ++k) /* :72-80 */
+    for (int j = 0; j < ny; ++j)
+      for (int i = 0; i <= nx; ++i) {
+        const int ip = imin(i, nx - 1), im = imax(i - 1, 0);
+        const double dx = m->s.dx;
+        const double t = 0.5 * (AT(*th, im, j, k) + AT(*th, ip, j, k));
+        AT(d[VO_U], i, j, k) -= K_CP * t * dpi(m, pi, ip, j, k, im, j, k) / dx;
+      }
+  for (int k = 0; k < nz; ++k) /* :81-89 */
+    for (int j = 0; j <= ny; ++j)
+      for (int i = 0; i < nx; ++i) {
+        const int jp = imin(j, ny - 1), jm = imax(j - 1, 0);
+        const double dy = m->s.dy;
+        const double t = 0.5 * (AT(*th, i, jm, k) + AT(*th, i, jp, k));
+        AT(d[VO_V], i, j, k) -= K_CP * t * dpi(m, pi, i, jp, k, i, jm, k) / dy;
+      }
+  for (int k = 0; k <= nz; ++k) /* :91-110 */
+    for (int j = 0; j < ny; ++j)
+      for (int i = 0; i < nx; ++i) {
+        const int kc = imin(imax(k, 0), nz - 1), km = imax(k - 1, 0);
+        const double scale = m->s.z_top - g_terrain(m, i, j);
+        const double dz = dmax(g_dzeta(m, kc) * scale, 1.0);
+        const double t = 0.5 * (AT(*th, i, j, km) + AT(*th, i, j, kc));
+        AT(d[VO_W], i, j, k) -= K_CP * t * dpi(m, pi, i, j, kc, i, j, km) / dz;
+        const double th0 = AT(m->ref[VO_THETA0], i, j, kc);
+        const double thp = AT(*th, i, j, kc) - th0;
+        const double qcond = AT(st[VO_QC], i, j, kc) + AT(st[VO_QR], i, j, kc) + AT(st[VO_QI], i, j, kc) +
+                             AT(st[VO_QS], i, j, kc) + AT(st[VO_QG], i, j, kc);
+        AT(d[VO_W], i, j, k) += K_GRAVITY * (thp / dmax(th0, 1.0) + K_BUOY_MOIST * AT(st[VO_QV], i, j, kc) - qcond);
+      }
+  for (int k = 0; k < nz; ++k) /* :112-127 */
+    for (int j = 0; j < ny; ++j)
+      for (int i = 0; i < nx; ++i) {
+        const double dx = m->s.dx, dy = m->s.dy;
+        const double scale = m->s.z_top - g_terrain(m, i, j);
+        const double dz = dmax(g_dzeta(m, k) * scale, 1.0);
+        const double fx = AT(st[VO_U], i + 1, j, k) * 0.5 * (AT(*rho, i, j, k) + AT(*rho, i + 1, j, k)) -
+                          AT(st[VO_U], i, j, k) * 0.5 * (AT(*rho, imax(i - 1, 0), j, k) + AT(*rho, i, j, k));
+        const double fy = AT(st[VO_V], i, j + 1, k) * 0.5 * (AT(*rho, i, j, k) + AT(*rho, i, j + 1, k)) -
+                          AT(st[VO_V], i, j, k) * 0.5 * (AT(*rho, i, imax(j - 1, 0), k) + AT(*rho, i, j, k));
+        const double fz = AT(st[VO_W], i, j, k + 1) * 0.5 * (AT(*rho, i, j, k) + AT(*rho, i, j, imin(k + 1, nz - 1))) -
+                          AT(st[VO_W], i, j, k) * 0.5 * (AT(*rho, i, j, imax(k - 1, 0)) + AT(*rho, i, j, k));
+        AT(d[VO_RHO], i, j, k) = -(fx / dx + fy / dy + fz / dz);
+      }
+  const int last = m->s.moist ? VO_QG : VO_QV;
+  for (int sp = VO_THETA; sp <= last; ++sp) { /* :129-137 */
+    if (sp == VO_PI) continue;
+    if (m->s.weno_scalars)
+      advect_weno5(m, &st[sp], &st[VO_U], &st[VO_V], &st[VO_W], &d[sp]);
+    else
+      advect_nonconservative(m, &st[sp], &st[VO_U], &st[VO_V], &st[VO_W], &d[sp]);
+  }
+  for (int sp = VO_QV; sp <= VO_QG; ++sp) /* :139-149 */
+    for (int k = 0; k < nz; ++k)
+      for (int j = 0; j < ny; ++j)
+        for (int i = 0; i < nx; ++i)
+          if (AT(st[sp], i, j, k) <= 0.0 && AT(d[sp], i, j, k) < 0.0) AT(d[sp], i, j, k) = 0.0;
+}
+
+static void acoustic_tendencies(vo_model *m, fld *st, fld *d);
+
+/* split_fast composition: remove the terms the substeps integrate
+ * (acoustic_tendencies of the same input state) from the slow tendency of
+ * u, v, w and rho. */
+static void slow_tendency_split(vo_model *m, fld *st, fld *d) {
+  slow_tendency(m, st, d);
+  if (!m->s.split_fast) return;
+  acoustic_tendencies(m, st, m->scr);
+  const int sps[4] = {VO_U, VO_V, VO_W, VO_RHO};
+  for (int q = 0; q < 4; ++q) {
+    const size_t n = fld_size(&d[sps[q]]);
+    for (size_t e = 0; e < n; ++e) d[sps[q]].d[e] -= m->scr[sps[q]].d[e];
+  }
+}
+
+/* linear mass divergence -div(rho0 u) with the reference's rho0 clamps,
+ * equations.cpp:187-200 (identical in acoustic_substep.cpp:71-85) */
+static double mass_div0(const vo_model *m, const fld *st, int i, int j, int k) {
+  const int nx = m->nx, ny = m->ny, nz = m->nz;
+  const fld *r0 = &m->ref[VO_RHO0];
+  const double dx = m->s.dx, dy = m->s.dy;
+  const double scale = m->s.z_top - g_terrain(m, i, j);
+  const double dz = dmax(g_dzeta(m, k) * scale, 1.0);
+  const double fx = AT(st[VO_U], i + 1, j, k) * 0.5 * (AT(*r0, i, j, k) + AT(*r0, imin(i + 1, nx - 1), j, k)) -
+                    AT(st[VO_U], i, j, k) * 0.5 * (AT(*r0, imax(i - 1, 0), j, k) + AT(*r0, i, j, k));
+  const double fy = AT(st[VO_V], i, j + 1, k) * 0.5 * (AT(*r0, i, j, k) + AT(*r0, i, imin(j + 1, ny - 1), k)) -
+                    AT(st[VO_V], i, j, k) * 0.5 * (AT(*r0, i, imax(j - 1, 0), k) + AT(*r0, i, j, k));
+  const double fz = AT(st[VO_W], i, j, k + 1) * 0.5 * (AT(*r0, i, j, k) + AT(*r0, i, j, imin(k + 1, nz - 1))) -
+                    AT(st[VO_W], i, j, k) * 0.5 * (AT(*r0, i, j, imax(k - 1, 0)) + AT(*r0, i, j, k));
+  return -(fx / dx + fy / dy + fz / dz);
+}
+
+/* Equations::acoustic_tendencies, equations.cpp:152-209 */
+static void acoustic_tendencies(vo_model *m, fld *st, fld *d) {
+  const int nx = m->nx, ny = m->ny, nz = m->nz;
+  const fld *th0 = &m->ref[VO_THETA0], *pi = &st[VO_PI];
+  for (int sp = 0; sp < VO_NSPECIES; ++sp) fld_zero(&d[sp]);
+  for (int k = 0; k < nz; ++k)
+    for (int j = 0; j < ny; ++j)
+      for (int i = 0; i <= nx; ++i) {
+        const int ip = imin(i, nx - 1), im = imax(i - 1, 0);
+        const double t0 = 0.5 * (AT(*th0, im, j, k) + AT(*th0, ip, j, k));
+        AT(d[VO_U], i, j, k) = -K_CP * t0 * dpi(m, pi, ip, j, k, im, j, k) / m->s.dx;
+      }
+  for (int k = 0; k < nz; ++k)
+    for (int j = 0; j <= ny; ++j)
+      for (int i = 0; i < nx; ++i) {
+        const int jp = imin(j, ny - 1), jm = imax(j - 1, 0);
+        const double t0 = 0.5 * (AT(*th0, i, jm, k) + AT(*th0, i, jp, k));
+        AT(d[VO_V], i, j, k) = -K_CP * t0 * dpi(m, pi, i, jp, k, i, jm, k) / m->s.dy;
+      }
+  for (int k = 0; k <= nz; ++k)
+    for (int j = 0; j < ny; ++j)
+      for (int i = 0; i < nx; ++i) {
+        const int kc = imin(imax(k, 0), nz - 1), km = imax(k - 1, 0);
+        const double scale = m->s.z_top - g_terrain(m, i, j);
+        const double dz = dmax(g_dzeta(m, kc) * scale, 1.0);
+        const double t0 = 0.5 * (AT(*th0, i, j, km) + AT(*th0, i, j, kc));
+        AT(d[VO_W], i, j, k) = -K_CP * t0 * dpi(m, pi, i, j, kc, i, j, km) / dz;
+      }
+  for (int k = 0; k < nz; ++k)
+    for (int j = 0; j < ny; ++j)
+      for (int i = 0; i < nx; ++i) AT(d[VO_RHO], i, j, k) = mass_div0(m, st, i, j, k);
+  for (int k = 0; k < nz; ++k)
+    for (int j = 0; j < ny; ++j)
+      for (int i = 0; i < nx; ++i) {
+        const double r0 = dmax(AT(m->ref[VO_RHO0], i, j, k), 1e-8);
+        AT(d[VO_PI], i, j, k) = (K_RD / K_CV) * (AT(m->ref[VO_PI0], i, j, k) / r0) * AT(d[VO_RHO], i, j, k);
+      }
+}
+
+static void add_scaled(fld *f, double a, const fld *x) { /* FieldT::add_scaled, field.hpp:108-111 */
+  const size_t n = fld_size(f);
+  for (size_t q = 0; q < n; ++q) f->d[q] += a * x->d[q];
+}
+
+/* RungeKutta3Integrator::acoustic_substep, runge_kutta.cpp:65-75 */
+static void fb_substep(vo_model *m, double dtau) {
+  acoustic_tendencies(m, m->st, m->scr);
+  add_scaled(&m->st[VO_RHO], dtau, &m->scr[VO_RHO]);
+  add_scaled(&m->st[VO_PI], dtau, &m->scr[VO_PI]);
+  acoustic_tendencies(m, m->st, m->scr);
+  add_scaled(&m->st[VO_U], dtau, &m->scr[VO_U]);
+  add_scaled(&m->st[VO_V], dtau, &m->scr[VO_V]);
+  add_scaled(&m->st[VO_W], dtau, &m->scr[VO_W]);
+}
+
+/* ------------------------------------------------------------------------ */
+/* tridiagonal solves                                                        */
+/* ------------------------------------------------------------------------ */
+
+/* thomas_solve, helmholtz.cpp:57-86 (n>=2 branch; returns 1 on a pivot below
+ * 1e-300, where the reference throws NumericalError) */
+static int thomas(const double *a, const double *b, const double *c, const double *d, int n,
+                  double *x, double *cp, double *dp) {
+  if (n == 1) { x[0] = d[0] / b[0]; return 0; }
+  double denom = b[0];
+  if (!(fabs(denom) > 0.0)) return 1;
+  cp[0] = c[0] / denom;
+  dp[0] = d[0] / denom;
+  for (int k = 1; k < n; ++k) {
+    denom = b[k] - a[k - 1] * cp[k - 1];
+    if (fabs(denom) < 1e-300) return 1;
+    dp[k] = (d[k] - a[k - 1] * dp[k - 1]) / denom;
+    if (k < n - 1) cp[k] = c[k] / denom;
+  }
+  x[n - 1] = dp[n - 1];
+  for (int k = n - 1; k-- > 0;) x[k] = dp[k] - cp[k] * x[k + 1];
+  return 0;
+}
+
+/* AcousticSubstepper: update_coefficients :38-65, update_mass_and_pressure
+ * :67-94, update_momentum :96-124, solve_vertical_implicit :126-137, step
+ * :139-149 (src/time/acoustic_substep.cpp) */
+static void ref_hevi_substep(vo_model *m, double dtau) {
+  const int nx = m->nx, ny = m->ny, nz = m->nz;
+  fld *st = m->st;
+  const fld *r0f = &m->ref[VO_RHO0], *th0f = &m->ref[VO_THETA0], *pi0f = &m->ref[VO_PI0];
+  /* update_mass_and_pressure */
+  fld drho;
+  fld_alloc(&drho, nx, ny, nz, 0);
+  for (int k = 0; k < nz; ++k)
+    for (int j = 0; j < ny; ++j)
+      for (int i = 0; i < nx; ++i) {
+        const double dx = m->s.dx, dy = m->s.dy;
+        const double scale = m->s.z_top - g_terrain(m, i, j);
+        const double dz = dmax(g_dzeta(m, k) * scale, 1.0);
+        const double r0 = AT(*r0f, i, j, k);
+        const double fx = AT(st[VO_U], i + 1, j, k) * 0.5 * (r0 + AT(*r0f, imin(i + 1, nx - 1), j, k)) -
+                          AT(st[VO_U], i, j, k) * 0.5 * (AT(*r0f, imax(i - 1, 0), j, k) + r0);
+        const double fy = AT(st[VO_V], i, j + 1, k) * 0.5 * (r0 + AT(*r0f, i, imin(j + 1, ny - 1), k)) -
+                          AT(st[VO_V], i, j, k) * 0.5 * (AT(*r0f, i, imax(j - 1, 0), k) + r0);
+        const double fz = AT(st[VO_W], i, j, k + 1) * 0.5 * (r0 + AT(*r0f, i, j, imin(k + 1, nz - 1))) -
+                          AT(st[VO_W], i, j, k) * 0.5 * (AT(*r0f, i, j, imax(k - 1, 0)) + r0);
+        AT(drho, i, j, k) = -(fx / dx + fy / dy + fz / dz);
+      }
+  for (int k = 0; k < nz; ++k)
+    for (int j = 0; j < ny; ++j)
+      for (int i = 0; i < nx; ++i) {
+        const double r0 = dmax(AT(*r0f, i, j, k), 1e-8);
+        AT(st[VO_RHO], i, j, k) += dtau * AT(drho, i, j, k);
+        AT(st[VO_PI], i, j, k) += dtau * (K_RD / K_CV) * (AT(*pi0f, i, j, k) / r0) * AT(drho, i, j, k);
+      }
+  free(drho.d);
+  /* update_coefficients from column (0,0) */
+  double *ta = (double *)calloc((size_t)(nz > 1 ? nz - 1 : 1), sizeof(double));
+  double *tb = (double *)calloc((size_t)nz, sizeof(double));
+  double *tc = (double *)calloc((size_t)(nz > 1 ? nz - 1 : 1), sizeof(double));
+  double *rhs = (double *)calloc((size_t)nz, sizeof(double));
+  double *sol = (double *)calloc((size_t)nz, sizeof(double));
+  double *cp = (double *)calloc((size_t)nz, sizeof(double));
+  double *dp = (double *)calloc((size_t)nz, sizeof(double));
+  const double half = 0.5 * dtau;
+  for (int k = 0; k < nz; ++k) {
+    const double scale = m->s.z_top - g_terrain(m, 0, 0);
+    const double dz = dmax(g_dzeta(m, k) * scale, 1.0);
+    const double rho0 = AT(*r0f, 0, 0, k);
+    const double th0 = AT(*th0f, 0, 0, k);
+    const double cs2 = (K_CP / K_CV) * K_RD * AT(*th0f, 0, 0, k) * AT(*pi0f, 0, 0, k); /* sound_speed2 :149-153 */
+    const double a_k = half * half * K_CP * th0 * rho0 / (dz * dz);
+    const double a_kp1 = (k < nz - 1) ? half * half * K_CP * AT(*th0f, 0, 0, k + 1) * AT(*r0f, 0, 0, k + 1) / (dz * dz) : a_k;
+    const double b0 = 1.0 / dmax(rho0 * cs2, 1e-12);
+    tb[k] = b0 + a_k + a_kp1;
+    if (k < nz - 1) tc[k] = -a_kp1;
+    if (k > 0) ta[k - 1] = -a_k;
+  }
+  /* solve_vertical_implicit */
+  for (int j = 0; j < ny; ++j)
+    for (int i = 0; i < nx; ++i) {
+      for (int k = 0; k < nz; ++k) rhs[k] = AT(st[VO_PI], i, j, k);
+      thomas(ta, tb, tc, rhs, nz, sol, cp, dp);
+      for (int k = 0; k < nz; ++k) AT(st[VO_PI], i, j, k) = sol[k];
+    }
+  free(ta); free(tb); free(tc); free(rhs); free(sol); free(cp); free(dp);
+  /* update_momentum */
+  for (int k = 0; k < nz; ++k)
+    for (int j = 0; j < ny; ++j)
+      for (int i = 0; i <= nx; ++i) {
+        const int ip = imin(i, nx - 1), im = imax(i - 1, 0);
+        const double dx = m->s.dx;
+        const double t0 = 0.5 * (AT(*th0f, im, j, k) + AT(*th0f, ip, j, k));
+        AT(st[VO_U], i, j, k) -= dtau * K_CP * t0 * (AT(st[VO_PI], ip, j, k) - AT(st[VO_PI], im, j, k)) / dx;
+      }
+  for (int k = 0; k < nz; ++k)
+    for (int j = 0; j <= ny; ++j)
+      for (int i = 0; i < nx; ++i) {
+        const int jp = imin(j, ny - 1), jm = imax(j - 1, 0);
+        const double dy = m->s.dy;
+        const double t0 = 0.5 * (AT(*th0f, i, jm, k) + AT(*th0f, i, jp, k));
+        AT(st[VO_V], i, j, k) -= dtau * K_CP * t0 * (AT(st[VO_PI], i, jp, k) - AT(st[VO_PI], i, jm, k)) / dy;
+      }
+  for (int k = 0; k <= nz; ++k)
+    for (int j = 0; j < ny; ++j)
+      for (int i = 0; i < nx; ++i) {
+        const int kc = imin(imax(k, 0), nz - 1), km = imax(k - 1, 0);
+        const double scale = m->s.z_top - g_terrain(m, i, j);
+        const double dz = dmax(g_dzeta(m, kc) * scale, 1.0);
+        const double t0 = 0.5 * (AT(*th0f, i, j, km) + AT(*th0f, i, j, kc));
+        AT(st[VO_W], i, j, k) -= dtau * K_CP * t0 * (AT(st[VO_PI], i, j, kc) - AT(st[VO_PI], i, j, km)) / dz;
+      }
+}
+
+/* Vertically implicit acoustic substep written consistently with the
+ * explicit operator above (no reference counterpart; its own restatement).
+ * With weight b = hevi_beta, rho0 face values r_f = 0.5*(rho0(k-1)+rho0(k))
+ * (clamped as in mass_div0), face thetas t_f and face spacings
+ * dzf_k = max(dzeta(min(k,nz-1))*scale, 1) as in acoustic_tendencies:
+ *   Dh   = horizontal part of mass_div0 with the old u, v
+ *   G_k  = (pi'_k - pi'_{k-1}) / dzf_k on interior faces, 0 on k = 0, nz
+ *   w~   = w - dtau*(1-b)*cp*t_f*G(pi'_old)
+ *   pi*  = pi + dtau*kappa*(Dh + (1-b)*Dv(w_old) + b*Dv(w~))
+ *   (1 + c_k(T_k + T_{k+1})) x_k - c_k T_k x_{k-1} - c_k T_{k+1} x_{k+1} = pi*_k - P0_k
+ *   with c_k = (dtau*b)^2*kappa_k/dz_k, T_f = r_f*cp*t_f/dzf_f (T_0 = T_nz = 0),
+ *   x = pi'_new, P0 = pi0 (perturbation form) or 0 (total form);
+ *   w_new = w~ - dtau*b*cp*t_f*G(x);  rho_new = rho + dtau*(Dh + (1-b)Dv(w_old) + b Dv(w_new));
+ *   u, v backward with the new pi as in the explicit substep. */
+static void cons_hevi_substep(vo_model *m, double dtau) {
+  const int nx = m->nx, ny = m->ny, nz = m->nz;
+  fld *st = m->st;
+  const fld *r0f = &m->ref[VO_RHO0], *th0f = &m->ref[VO_THETA0], *pi0f = &m->ref[VO_PI0];
+  const double b = m->s.hevi_beta, ob = 1.0 - b;
+  const int pert = m->s.pgf_perturbation;
+  double *T = (double *)calloc((size_t)nz + 1, sizeof(double));
+  double *rf = (double *)calloc((size_t)nz + 1, sizeof(double));
+  double *tf = (double *)calloc((size_t)nz + 1, sizeof(double));
+  double *dzf = (double *)calloc((size_t)nz + 1, sizeof(double));
+  double *G = (double *)calloc((size_t)nz + 1, sizeof(double));
+  double *wt = (double *)calloc((size_t)nz + 1, sizeof(double));
+  double *wn = (double *)calloc((size_t)nz + 1, sizeof(double));
+  double *Dh = (double *)calloc((size_t)nz, sizeof(double));
+  double *dzc = (double *)calloc((size_t)nz, sizeof(double));
+  double *kap = (double *)calloc((size_t)nz, sizeof(double));
+  double *ta = (double *)calloc((size_t)nz, sizeof(double));
+  double *tb = (double *)calloc((size_t)nz, sizeof(double));
+  double *tc = (double *)calloc((size_t)nz, sizeof(double));
+  double *rhs = (double *)calloc((size_t)nz, sizeof(double));
+  double *x = (double *)calloc((size_t)nz, sizeof(double));
+  double *cp = (double *)calloc((size_t)nz, sizeof(double));
+  double *dp = (double *)calloc((size_t)nz, sizeof(double));
+  fld pin; /* new pi for the horizontal momentum update */
+  fld_alloc(&pin, nx, ny, nz, 0);
+  for (int j = 0; j < ny; ++j)
+    for (int i = 0; i < nx; ++i) {
+      const double scale = m->s.z_top - g_terrain(m, i, j);
+      for (int k = 0; k < nz; ++k) {
+        dzc[k] = dmax(g_dzeta(m, k) * scale, 1.0);
+        kap[k] = (K_RD / K_CV) * (AT(*pi0f, i, j, k) / dmax(AT(*r0f, i, j, k), 1e-8));
+        const double r0 = AT(*r0f, i, j, k);
+        const double fx = AT(st[VO_U], i + 1, j, k) * 0.5 * (r0 + AT(*r0f, imin(i + 1, nx - 1), j, k)) -
+                          AT(st[VO_U], i, j, k) * 0.5 * (AT(*r0f, imax(i - 1, 0), j, k) + r0);
+        const double fy = AT(st[VO_V], i, j + 1, k) * 0.5 * (r0 + AT(*r0f, i, imin(j + 1, ny - 1), k)) -
+                          AT(st[VO_V], i, j, k) * 0.5 * (AT(*r0f, i, imax(j - 1, 0), k) + r0);
+        Dh[k] = -(fx / m->s.dx + fy / m->s.dy);
+      }
+      for (int k = 0; k <= nz; ++k) {
+        const int kc = imin(k, nz - 1), km = imax(k - 1, 0);
+        rf[k] = 0.5 * (AT(*r0f, i, j, km) + AT(*r0f, i, j, kc));
+        tf[k] = 0.5 * (AT(*th0f, i, j, km) + AT(*th0f, i, j, kc));
+        dzf[k] = dmax(g_dzeta(m, kc) * scale, 1.0);
+        if (k == 0 || k == nz) {
+          G[k] = 0.0; T[k] = 0.0;
+        } else {
+          const double pa = AT(st[VO_PI], i, j, kc) - (pert ? AT(*pi0f, i, j, kc) : 0.0);
+          const double pb = AT(st[VO_PI], i, j, km) - (pert ? AT(*pi0f, i, j, km) : 0.0);
+          G[k] = (pa - pb) / dzf[k];
+          T[k] = rf[k] * K_CP * tf[k] / dzf[k];
+        }
+        wt[k] = AT(st[VO_W], i, j, k) - dtau * ob * K_CP * tf[k] * G[k];
+      }
+      for (int k = 0; k < nz; ++k) {
+        const double dv_old = -(rf[k + 1] * AT(st[VO_W], i, j, k + 1) - rf[k] * AT(st[VO_W], i, j, k)) / dzc[k];
+        const double dv_t = -(rf[k + 1] * wt[k + 1] - rf[k] * wt[k]) / dzc[k];
+        const double pstar = AT(st[VO_PI], i, j, k) + dtau * kap[k] * (Dh[k] + ob * dv_old + b * dv_t);
+        const double ck = (dtau * b) * (dtau * b) * kap[k] / dzc[k];
+        ta[k] = -ck * T[k];
+        tc[k] = -ck * T[k + 1];
+        tb[k] = 1.0 + ck * (T[k] + T[k + 1]);
+        rhs[k] = pstar - (pert ? AT(*pi0f, i, j, k) : 0.0);
+      }
+      thomas(ta + 1, tb, tc, rhs, nz, x, cp, dp);
+      for (int k = 0; k <= nz; ++k) {
+        double g = 0.0;
+        if (k > 0 && k < nz) g = (x[k] - x[k - 1]) / dzf[k];
+        wn[k] = wt[k] - dtau * b * K_CP * tf[k] * g;
+      }
+      for (int k = 0; k < nz; ++k) {
+        const double dv_old = -(rf[k + 1] * AT(st[VO_W], i, j, k + 1) - rf[k] * AT(st[VO_W], i, j, k)) / dzc[k];
+        const double dv_new = -(rf[k + 1] * wn[k + 1] - rf[k] * wn[k]) / dzc[k];
+        AT(st[VO_RHO], i, j, k) += dtau * (Dh[k] + ob * dv_old + b * dv_new);
+        AT(pin, i, j, k) = x[k] + (pert ? AT(*pi0f, i, j, k) : 0.0);
+      }
+      for (int k = 0; k <= nz; ++k) AT(st[VO_W], i, j, k) = wn[k];
+    }
+  for (int k = 0; k < nz; ++k)
+    for (int j = 0; j < ny; ++j)
+      for (int i = 0; i < nx; ++i) AT(st[VO_PI], i, j, k) = AT(pin, i, j, k);
+  free(pin.d);
+  for (int k = 0; k < nz; ++k) /* backward horizontal momentum, as equations.cpp:157-174 */
+    for (int j = 0; j < ny; ++j)
+      for (int i = 0; i <= nx; ++i) {
+        const int ip = imin(i, nx - 1), im = imax(i - 1, 0);
+        const double t0 = 0.5 * (AT(*th0f, im, j, k) + AT(*th0f, ip, j, k));
+        AT(st[VO_U], i, j, k) += dtau * (-K_CP * t0 * dpi(m, &st[VO_PI], ip, j, k, im, j, k) / m->s.dx);
+      }
+  for (int k = 0; k < nz; ++k)
+    for (int j = 0; j <= ny; ++j)
+      for (int i = 0; i < nx; ++i) {
+        const int jp = imin(j, ny - 1), jm = imax(j - 1, 0);
+        const double t0 = 0.5 * (AT(*th0f, i, jm, k) + AT(*th0f, i, jp, k));
+        AT(st[VO_V], i, j, k) += dtau * (-K_CP * t0 * dpi(m, &st[VO_PI], i, jp, k, i, jm, k) / m->s.dy);
+      }
+  free(T); free(rf); free(tf); free(dzf); free(G); free(wt); free(wn); free(Dh); free(dzc);
+  free(kap); free(ta); free(tb); free(tc); free(rhs); free(x); free(cp); free(dp);
+}
+
+/* Damping::apply_sponge, damping.cpp:76-140 */
+static void sponge_apply(vo_model *m, double dt) {
+  const int nx = m->nx, ny = m->ny, nz = m->nz;
+  int kmin = nz;
+  for (int k = 0; k < nz; ++k)
+    if (m->sponge[k] > 0.0) { kmin = k; break; }
+  if (kmin >= nz) return;
+#define ALPHA_AT(k) (m->sponge[imin((k), nz - 1)])
+  for (int k = kmin; k < nz; ++k) { /* u */
+    const double a = ALPHA_AT(k);
+    if (a <= 0.0) continue;
+    const double w = 1.0 / (1.0 + dt * a);
+    for (int j = 0; j < ny; ++j)
+      for (int i = 0; i <= nx; ++i) AT(m->st[VO_U], i, j, k) = w * AT(m->st[VO_U], i, j, k);
+  }
+  for (int k = kmin; k < nz; ++k) { /* v */
+    const double a = ALPHA_AT(k);
+    if (a <= 0.0) continue;
+    const double w = 1.0 / (1.0 + dt * a);
+    for (int j = 0; j <= ny; ++j)
+      for (int i = 0; i < nx; ++i) AT(m->st[VO_V], i, j, k) = w * AT(m->st[VO_V], i, j, k);
+  }
+  for (int k = kmin; k <= nz; ++k) { /* w */
+    const double a = ALPHA_AT(k);
+    if (a <= 0.0) continue;
+    const double w = 1.0 / (1.0 + dt * a);
+    for (int j = 0; j < ny; ++j)
+      for (int i = 0; i < nx; ++i) AT(m->st[VO_W], i, j, k) = w * AT(m->st[VO_W], i, j, k);
+  }
+  const int cells[3] = {VO_RHO, VO_THETA, VO_PI};
+  const int tgts[3] = {VO_RHO0, VO_THETA0, VO_PI0};
+  for (int c = 0; c < 3; ++c)
+    for (int k = kmin; k < nz; ++k) {
+      const double a = ALPHA_AT(k);
+      if (a <= 0.0) continue;
+      const double w = 1.0 / (1.0 + dt * a);
+      for (int j = 0; j < ny; ++j)
+        for (int i = 0; i < nx; ++i) {
+          const double tgt = AT(m->ref[tgts[c]], i, j, k);
+          AT(m->st[cells[c]], i, j, k) = w * (AT(m->st[cells[c]], i, j, k) + dt * a * tgt);
+        }
+    }
+#undef ALPHA_AT
+}
+
+static int has_nonfinite(const vo_model *m) { /* State::has_nonfinite, state.cpp:96-101 */
+  for (int sp = 0; sp < VO_NSPECIES; ++sp) {
+    const size_t n = fld_size(&m->st[sp]);
+    for (size_t q = 0; q < n; ++q)
+      if (!isfinite(m->st[sp].d[q])) return 1;
+  }
+  return 0;
+}
+
+/* ------------------------------------------------------------------------ */
+/* public entry points                                                      */
+/* ------------------------------------------------------------------------ */
+void vo_setup_defaults(vo_setup *s) {
+  memset(s, 0, sizeof(*s));
+  s->nx = 64; s->ny = 64; s->nz = 40;
+  s->dx = 250.0; s->dy = 250.0; s->z_top = 10000.0;
+  s->zeta_first = 1.0; s->zeta_stretch = 1.0;
+  s->ref_kind = 0; s->theta0 = 300.0; s->p_surf = 100000.0; s->bv_n = 0.01; s->profile_dz = 250.0;
+  s->bubble_amplitude = 2.0; s->bubble_radius_x = 2000.0; s->bubble_radius_z = 2000.0;
+  s->bubble_xc = 8000.0; s->bubble_yc = 8000.0; s->bubble_zc = 2000.0;
+  s->qv_surface = 0.014; s->qv_decay_height = 3000.0;
+  s->advection = 5; s->weno_scalars = 1; s->moist = 0; s->coriolis = 0; s->latitude = 45.0;
+  s->sponge_alpha = 0.2; s->sponge_start_fraction = 0.8;
+  s->divergence_damping = 0.0; s->divergence_order = 2;
+  s->pgf_perturbation = 1; s->acoustic_mode = 0; s->hevi_beta = 0.5; s->split_fast = 1; s->weno_advective = 1;
+}
+
+vo_model *vo_create(const vo_setup *su) {
+  vo_model *m = (vo_model *)calloc(1, sizeof(vo_model));
+  m->s = *su;
+  m->nx = su->nx; m->ny = su->ny; m->nz = su->nz;
+  const int nx = m->nx, ny = m->ny, nz = m->nz;
+  m->zeta = (double *)calloc((size_t)nz + 1, sizeof(double));
+  make_stretched_zeta(nz, su->zeta_first, su->zeta_stretch, m->zeta);
+  m->zs = (double *)calloc((size_t)nx * ny, sizeof(double));
+  if (su->terrain_kind == 1) /* Gaussian hill at cell centres (build-defined case) */
+    for (int j = 0; j < ny; ++j)
+      for (int i = 0; i < nx; ++i) {
+        const double x = ((double)i + 0.5) * su->dx - su->hill_xc;
+        const double y = ((double)j + 0.5) * su->dy - su->hill_yc;
+        m->zs[(size_t)j * nx + i] = su->hill_h * exp(-(x * x + y * y) / (su->hill_a * su->hill_a));
+      }
+  for (int sp = 0; sp < VO_NSPECIES; ++sp) {
+    fld_alloc(&m->st[sp], nx, ny, nz, stagger_of(sp));
+    fld_alloc(&m->s0[sp], nx, ny, nz, stagger_of(sp));
+    fld_alloc(&m->slow[sp], nx, ny, nz, stagger_of(sp));
+    fld_alloc(&m->scr[sp], nx, ny, nz, stagger_of(sp));
+  }
+  for (int r = 0; r < 5; ++r) fld_alloc(&m->ref[r], nx, ny, nz, 0);
+  if (su->ref_kind == 1) ref_from_profile(m); else ref_isothermal(m);
+  /* Damping constructor sponge profile, damping.cpp:24-41 */
+  m->sponge = (double *)calloc((size_t)nz, sizeof(double));
+  {
+    const double zs0 = su->sponge_start_fraction * su->z_top;
+    for (int k = 0; k < nz; ++k) {
+      const double z = g_zc(m, 0, 0, k);
+      if (z <= zs0) { m->sponge[k] = 0.0; continue; }
+      const double t = (z - zs0) / dmax(su->z_top - zs0, 1.0);
+      const double sn = sin(0.5 * K_PI * (t < 0.0 ? 0.0 : (t > 1.0 ? 1.0 : t)));
+      m->sponge[k] = su->sponge_alpha * sn * sn;
+    }
+  }
+  /* Coriolis constructor, coriolis.cpp:25-32 */
+  m->f0 = 2.0 * K_OMEGA * sin(su->latitude * K_DEG2RAD);
+  m->beta = 2.0 * K_OMEGA * cos(su->latitude * K_DEG2RAD) / K_EARTH_RADIUS;
+  init_warm_bubble(m);
+  return m;
+}
+
+void vo_destroy(vo_model *m) {
+  if (!m) return;
+  for (int sp = 0; sp < VO_NSPECIES; ++sp) {
+    free(m->st[sp].d); free(m->s0[sp].d); free(m->slow[sp].d); free(m->scr[sp].d);
+  }
+  for (int r = 0; r < 5; ++r) free(m->ref[r].d);
+  free(m->zeta); free(m->zs); free(m->sponge);
+  free(m);
+}
+
+size_t vo_storage_size(const vo_model *m, int species) { return fld_size(&m->st[species]); }
+void vo_get_field(const vo_model *m, int sp, double *out) {
+  memcpy(out, m->st[sp].d, fld_size(&m->st[sp]) * sizeof(double));
+}
+void vo_set_field(vo_model *m, int sp, const double *in) {
+  memcpy(m->st[sp].d, in, fld_size(&m->st[sp]) * sizeof(double));
+}
+void vo_get_reffield(const vo_model *m, int which, double *out) {
+  memcpy(out, m->ref[which].d, fld_size(&m->ref[which]) * sizeof(double));
+}
+void vo_get_zeta(const vo_model *m, double *out) { memcpy(out, m->zeta, sizeof(double) * (size_t)(m->nz + 1)); }
+void vo_get_terrain(const vo_model *m, double *out) { memcpy(out, m->zs, sizeof(double) * (size_t)m->nx * m->ny); }
+void vo_get_sponge(const vo_model *m, double *out) { memcpy(out, m->sponge, sizeof(double) * (size_t)m->nz); }
+
+void vo_acoustic_substep(vo_model *m, double dtau) { fb_substep(m, dtau); }
+void vo_hevi_substep(vo_model *m, double dtau) {
+  if (m->s.acoustic_mode == 1) ref_hevi_substep(m, dtau); else cons_hevi_substep(m, dtau);
+}
+void vo_sponge(vo_model *m, double dt) { sponge_apply(m, dt); }
+
+void vo_slow_tendency(vo_model *m, double *const *out) {
+  slow_tendency_split(m, m->st, m->slow);
+  for (int sp = 0; sp < VO_NSPECIES; ++sp)
+    memcpy(out[sp], m->slow[sp].d, fld_size(&m->slow[sp]) * sizeof(double));
+}
+
+/* RungeKutta3Integrator::step, runge_kutta.cpp:77-119, with
+ * State::add_scaled(Real, Tendency) expanded field by field */
+int vo_rk3_step(vo_model *m, double dt, int n_sub_in) {
+  const int n_sub = n_sub_in > 1 ? n_sub_in : 1;
+  for (int sp = 0; sp < VO_NSPECIES; ++sp)
+    memcpy(m->s0[sp].d, m->st[sp].d, fld_size(&m->st[sp]) * sizeof(double));
+  const double dt_stage[3] = {dt / 3.0, dt / 2.0, dt};
+  for (int stage = 0; stage < 3; ++stage) {
+    slow_tendency_split(m, m->st, m->slow);
+    for (int sp = 0; sp < VO_NSPECIES; ++sp) {
+      memcpy(m->st[sp].d, m->s0[sp].d, fld_size(&m->st[sp]) * sizeof(double));
+      add_scaled(&m->st[sp], dt_stage[stage], &m->slow[sp]);
+    }
+    const double dtau = dt_stage[stage] / (double)n_sub;
+    for (int n = 0; n < n_sub; ++n) {
+      if (m->s.acoustic_mode == 0) fb_substep(m, dtau);
+      else vo_hevi_substep(m, dtau);
+    }
+    if (has_nonfinite(m)) return 1;
+  }
+  sponge_apply(m, dt);
+  return 0;
+}
+
+/* ------------------------------------------------------------------------ */
+/* C-ABI kernels: src/common/c_kernels.c                                     */
+/* ------------------------------------------------------------------------ */
+int vo_tridiagonal_solve(const double *a, const double *b, const double *c, const double *d, int n,
+                         double *x, double *ws) {
+  /* argument checks and n==1 branch: c_kernels.c:22-29 */
+  if (n <= 0 || b == NULL || d == NULL || x == NULL || ws == NULL) return 2;
+  if (n == 1) {
+    if (b[0] == 0.0) return 1;
+    x[0] = d[0] / b[0];
+    return 0;
+  }
+  /* contract c_kernels.h:38-55 (NULL a/c = 0) solved with the recurrence of
+   * thomas_solve, helmholtz.cpp:71-85; ws holds the modified super-diagonal */
+  double denom = b[0];
+  if (denom == 0.0) return 1;
+  ws[0] = (c != NULL ? c[0] : 0.0) / denom;
+  x[0] = d[0] / denom;
+  for (int k = 1; k < n; ++k) {
+    const double am = (a != NULL) ? a[k - 1] : 0.0;
+    denom = b[k] - am * ws[k - 1];
+    if (denom == 0.0) return 1;
+    x[k] = (d[k] - am * x[k - 1]) / denom;
+    if (k < n - 1) ws[k] = (c != NULL ? c[k] : 0.0) / denom;
+  }
+  for (int k = n - 1; k-- > 0;) x[k] = x[k] - ws[k] * x[k + 1];
+  return 0;
+}
+
+void vo_weno5_reconstruct(double qm2, double qm1, double q0, double q1, double q2, double *q_left,
+                          double *q_right) {
+  if (q_left == NULL || q_right == NULL) return; /* c_kernels.c:71 */
+  weno5(qm2, qm1, q0, q1, q2, q_left, q_right);   /* c_kernels.c:64-104 == advection.cpp:62-98 */
+}
+
+double vo_bilinear(const double *f, int halo, int nsx, int nsy, int nz, double xi, double yj, int k) {
+  /* c_kernels.c:108-144 */
+  const int nxi = nsx - 2 * halo, nyi = nsy - 2 * halo;
+  if (f == NULL || nz <= 0) return 0.0;
+  if (k < 0) k = 0;
+  if (k >= nz) k = nz - 1;
+  const int i0 = (int)floor(xi), j0 = (int)floor(yj);
+  const double wx = xi - (double)i0, wy = yj - (double)j0;
+  int ia = i0, ib = i0 + 1, ja = j0, jb = j0 + 1;
+  ia = iclamp(ia, 0, nxi - 1); ib = iclamp(ib, 0, nxi - 1);
+  ja = iclamp(ja, 0, nyi - 1); jb = iclamp(jb, 0, nyi - 1);
+#define F_AT(I, J) f[(((size_t)(k + halo) * (size_t)nsy + (size_t)((J) + halo)) * (size_t)nsx) + (size_t)((I) + halo)]
+  const double q00 = F_AT(ia, ja), q10 = F_AT(ib, ja), q01 = F_AT(ia, jb), q11 = F_AT(ib, jb);
+#undef F_AT
+  return (q00 + wx * (q10 - q00)) + wy * ((q01 + wx * (q11 - q01)) - (q00 + wx * (q10 - q00)));
+}
+
+double vo_cfl_scan(const double *u, const double *v, const double *w, const double *dzeta, const double *zs,
+                   int nx, int ny, int nz, double dx, double dy, double z_top, double dt, double *max_wind_out,
+                   double *min_dz_out) {
+  /* c_kernels.c:148-186 */
+  double worst = 0.0, max_wind = 0.0, min_dz = 1e30;
+  const size_t nxy = (size_t)nx * (size_t)ny;
+  if (u == NULL || v == NULL || w == NULL || dzeta == NULL) return 0.0;
+  for (int k = 0; k < nz; ++k)
+    for (int j = 0; j < ny; ++j)
+      for (int i = 0; i < nx; ++i) {
+        const size_t idx = (size_t)k * nxy + (size_t)j * (size_t)nx + (size_t)i;
+        const double uu = u[idx], vv = v[idx], ww = w[idx];
+        const double scale = (zs != NULL) ? (z_top - zs[(size_t)j * (size_t)nx + (size_t)i]) : z_top;
+        double dz = dzeta[k] * scale;
+        if (dz < 1.0) dz = 1.0;
+        if (dz < min_dz) min_dz = dz;
+        const double speed = sqrt(uu * uu + vv * vv + ww * ww);
+        if (speed > max_wind) max_wind = speed;
+        const double cfl = dt * (fabs(uu) / dx + fabs(vv) / dy + fabs(ww) / dz);
+        if (cfl > worst) worst = cfl;
+      }
+  if (max_wind_out != NULL) *max_wind_out = max_wind;
+  if (min_dz_out != NULL) *min_dz_out = (min_dz > 1e29) ? 0.0 : min_dz;
+  return worst;
+}
+
+double vo_neumaier_sum(const double *x, size_t n) { /* c_kernels.c:190-205 */
+  double sum = 0.0, c = 0.0;
+  if (x == NULL) return 0.0;
+  for (size_t i = 0; i < n; ++i) {
+    const double t = sum + x[i];
+    if (fabs(sum) >= fabs(x[i])) c += (sum - t) + x[i];
+    else c += (x[i] - t) + sum;
+    sum = t;
+  }
+  return sum + c;
+}
+
+void vo_advect_scalar_flux(const double *q, const double *rho, const double *u, const double *v, const double *w,
+                           const double *dzeta, const double *zs, int nx, int ny, int nz, double dx, double dy,
+                           double z_top, double *dqdt) {
+  /* c_kernels.c:209-286 */
+  const size_t nxy = (size_t)nx * (size_t)ny;
+  const double inv_dx = 1.0 / dx, inv_dy = 1.0 / dy;
+  if (q == NULL || rho == NULL || u == NULL || v == NULL || w == NULL || dzeta == NULL || dqdt == NULL) return;
+  for (int k = 0; k < nz; ++k) {
+    const size_t base_k = (size_t)k * nxy;
+    for (int j = 0; j < ny; ++j)
+      for (int i = 0; i < nx; ++i) {
+        const size_t idx = base_k + (size_t)j * (size_t)nx + (size_t)i;
+        const double scale = (zs != NULL) ? (z_top - zs[(size_t)j * (size_t)nx + (size_t)i]) : z_top;
+        double dz = dzeta[k] * scale;
+        double fxE, fxW, fyN, fyS, fzT, fzB;
+        if (dz < 1.0) dz = 1.0;
+        {
+          const size_t e = base_k + (size_t)j * (size_t)nx + (size_t)((i + 1) % nx);
+          const size_t c = idx;
+          const size_t ws = base_k + (size_t)j * (size_t)nx + (size_t)((i + nx - 1) % nx);
+          fxE = u[e] * (0.5 * (rho[c] + rho[e])) * (0.5 * (q[c] + q[e]));
+          fxW = u[c] * (0.5 * (rho[ws] + rho[c])) * (0.5 * (q[ws] + q[c]));
+        }
+        {
+          const size_t e = base_k + (size_t)((j + 1) % ny) * (size_t)nx + (size_t)i;
+          const size_t c = idx;
+          const size_t s = base_k + (size_t)((j + ny - 1) % ny) * (size_t)nx + (size_t)i;
+          fyN = v[e] * (0.5 * (rho[c] + rho[e])) * (0.5 * (q[c] + q[e]));
+          fyS = v[c] * (0.5 * (rho[s] + rho[c])) * (0.5 * (q[s] + q[c]));
+        }
+        if (k > 0 && k + 1 < nz) {
+          const size_t t = base_k + nxy + (size_t)j * (size_t)nx + (size_t)i;
+          const size_t c = idx;
+          const size_t b = base_k - nxy + (size_t)j * (size_t)nx + (size_t)i;
+          fzT = w[t] * (0.5 * (rho[c] + rho[t])) * (0.5 * (q[c] + q[t]));
+          fzB = w[c] * (0.5 * (rho[b] + rho[c])) * (0.5 * (q[b] + q[c]));
+        } else {
+          fzT = 0.0;
+          fzB = 0.0;
+        }
+        const double div = (fxE - fxW) * inv_dx + (fyN - fyS) * inv_dy + (fzT - fzB) / dz;
+        const double rr = (rho[idx] > 1e-12) ? rho[idx] : 1e-12;
+        dqdt[idx] = -div / rr;
+      }
+  }
+}

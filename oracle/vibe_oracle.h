@@ -1,0 +1,159 @@
+/* oracle/vibe_oracle.h -- TEST INFRASTRUCTURE ONLY.
+ *
+ * CPU oracle for the VIBE-Model dynamics step. Two implementations share this
+ * interface:
+ *   - vo_*   : oracle/vibe_oracle.c, a plain-C restatement of the reference's
+ *              serial FP64 algorithm (each function cites the reference
+ *              file:line it follows). Builds anywhere with gcc.
+ *   - vref_* : oracle/ref/ref_driver.cpp, linked against the reference's own
+ *              sources compiled unchanged (oracle/_ref/libvibe_ref.so).
+ *              Only buildable where the reference tree is present.
+ * Only tests, the smoke check and bench.py's CPU-baseline leg may use either.
+ *
+ * Data layout = the reference's grid::FieldT storage (field.hpp:6-11,77-81):
+ *   offset(i,j,k) = ((k+h)*nsy + (j+h))*nsx + (i+h), halo h = 4,
+ *   nsx = nx+2h (+1 for u), nsy = ny+2h (+1 for v), nsz = nz+2h (+1 for w).
+ * Species order = dyn::Species (state.hpp:53-55):
+ *   u v w rho theta pi qv qc qr qi qs qg.
+ */
+#ifndef VIBE_ORACLE_H
+#define VIBE_ORACLE_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define VO_NSPECIES 12
+#define VO_HALO 4
+
+enum vo_species { VO_U = 0, VO_V, VO_W, VO_RHO, VO_THETA, VO_PI, VO_QV,
+                  VO_QC, VO_QR, VO_QI, VO_QS, VO_QG };
+
+/* Reference-state fields (reference_state.hpp): theta0, pi0, rho0, p0, qv0. */
+enum vo_reffield { VO_THETA0 = 0, VO_PI0, VO_RHO0, VO_P0, VO_QV0 };
+
+/* Case description shared by the oracle, the reference-linked driver and the
+ * GPU library's set-up code (same field meaning in all three). */
+typedef struct vo_setup {
+  int nx, ny, nz;
+  double dx, dy, z_top;
+  /* vertical levels: geometry.cpp:39-60 make_stretched_zeta(nz, first, stretch) */
+  double zeta_first, zeta_stretch;
+  /* terrain: 0 flat, 1 Gaussian hill h*exp(-r^2/a^2) centred at (hx, hy) */
+  int terrain_kind;
+  double hill_h, hill_a, hill_xc, hill_yc;
+  /* reference state: 0 = ReferenceState::isothermal(theta0, p_surf)
+   *                  1 = ReferenceState::from_profile of theta0*exp(N^2 z/g)
+   *                      sampled every profile_dz metres up to z_top + profile_dz */
+  int ref_kind;
+  double theta0, p_surf, bv_n, profile_dz;
+  /* warm bubble (initial_conditions.cpp:136-159) + IcOptions defaults */
+  double bubble_amplitude, bubble_radius_x, bubble_radius_z;
+  double bubble_xc, bubble_yc, bubble_zc;
+  double qv_surface, qv_decay_height;
+  double u_background, shear_u;
+  /* numerics (config.hpp:55-68) */
+  int advection;        /* 2, 4, 6 central; 5 = weno5 (falls to 2nd order in
+                           scalar_nonconservative, advection.cpp:106-120) */
+  int weno_scalars;     /* 1: theta/q use Advection::scalar WENO5 flux form */
+  int moist;            /* microphysics != "none" */
+  int coriolis;         /* 0 none, 1 f-plane, 2 beta-plane */
+  double latitude;
+  double sponge_alpha, sponge_start_fraction;
+  double divergence_damping;
+  int divergence_order;
+  /* --- compositions the reference does not provide (not read by vref_*) ---
+   * pgf_perturbation: 0 = pressure-gradient terms act on the total Exner
+   *   function, as src/dyn/equations.cpp:79,88,101,164,173,183 compute;
+   *   1 = they act on pi' = pi - pi0, the form the reference documents
+   *   (include/vibe/dyn/equations.hpp:9-16, docs/design/04_time_integration.md
+   *   sec. 2.2). Only 1 keeps a resting atmosphere at rest.
+   * acoustic_mode: 0 = explicit forward-backward substep
+   *   (runge_kutta.cpp:65-75); 1 = the reference's HEVI substep
+   *   (acoustic_substep.cpp:139-149, dimensionally inconsistent, kernel-level
+   *   use only); 2 = vertically implicit (Crank-Nicolson weight hevi_beta)
+   *   substep written consistently with the explicit operator.
+   */
+  int pgf_perturbation;
+  int acoustic_mode;
+  double hevi_beta;
+  /* split_fast: 0 = the slow tendency keeps the pressure-gradient and the
+   *   linear mass-divergence terms that the acoustic substeps integrate again
+   *   (runge_kutta.cpp:88-100 as written: fast terms counted twice, explicit
+   *   at the full stage step); 1 = those terms (acoustic_tendencies of the
+   *   stage input state, equations.cpp:152-200) are removed from the slow
+   *   tendency of u, v, w and rho, so the substeps integrate them once
+   *   (docs/design/04_time_integration.md sec. 2.1-2.2). */
+  int split_fast;
+  /* weno_advective: 1 = the WENO5 flux-form scalar tendency
+   *   (advection.cpp:144-187: -div(u q), no density weight) gets + q div(u)
+   *   with the same face winds and spacings, giving the advective form
+   *   dq/dt = -u.grad(q) that equations.cpp:8-11 documents; a constant field
+   *   then has zero tendency even where the flow is divergent. */
+  int weno_advective;
+} vo_setup;
+
+/* Fill *s with the Config-1 warm-bubble case on an nx x ny x nz grid. */
+void vo_setup_defaults(vo_setup *s);
+
+/* ---- plain-C restatement (oracle/vibe_oracle.c) ---- */
+typedef struct vo_model vo_model;
+vo_model *vo_create(const vo_setup *s);
+void vo_destroy(vo_model *m);
+size_t vo_storage_size(const vo_model *m, int species);
+void vo_get_field(const vo_model *m, int species, double *out);
+void vo_set_field(vo_model *m, int species, const double *in);
+void vo_get_reffield(const vo_model *m, int which, double *out);
+void vo_get_zeta(const vo_model *m, double *out);      /* nz+1 */
+void vo_get_terrain(const vo_model *m, double *out);   /* nx*ny */
+void vo_get_sponge(const vo_model *m, double *out);    /* nz */
+int  vo_rk3_step(vo_model *m, double dt, int n_sub);   /* 0 ok, 1 non-finite */
+void vo_slow_tendency(vo_model *m, double *const *out);/* 12 storage arrays */
+void vo_acoustic_substep(vo_model *m, double dtau);
+void vo_hevi_substep(vo_model *m, double dtau);
+void vo_sponge(vo_model *m, double dt);
+
+/* C-ABI kernels restated (src/common/c_kernels.c). vo_tridiagonal_solve
+ * follows the documented contract (c_kernels.h:38-55) with the textbook
+ * recurrence of thomas_solve (helmholtz.cpp:57-86): the shipped
+ * c_kernels.c:18-60 does not solve the system it documents. */
+int vo_tridiagonal_solve(const double *a, const double *b, const double *c,
+                         const double *d, int n, double *x, double *ws);
+void vo_weno5_reconstruct(double qm2, double qm1, double q0, double q1,
+                          double q2, double *q_left, double *q_right);
+double vo_bilinear(const double *f, int halo, int nsx, int nsy, int nz,
+                   double xi, double yj, int k);
+double vo_cfl_scan(const double *u, const double *v, const double *w,
+                   const double *dzeta, const double *zs, int nx, int ny,
+                   int nz, double dx, double dy, double z_top, double dt,
+                   double *max_wind_out, double *min_dz_out);
+double vo_neumaier_sum(const double *x, size_t n);
+void vo_advect_scalar_flux(const double *q, const double *rho, const double *u,
+                           const double *v, const double *w, const double *dzeta,
+                           const double *zs, int nx, int ny, int nz, double dx,
+                           double dy, double z_top, double *dqdt);
+
+/* ---- reference-linked driver (oracle/ref/ref_driver.cpp) ---- */
+typedef struct vref_model vref_model;
+vref_model *vref_create(const vo_setup *s);
+void vref_destroy(vref_model *m);
+size_t vref_storage_size(const vref_model *m, int species);
+void vref_get_field(const vref_model *m, int species, double *out);
+void vref_set_field(vref_model *m, int species, const double *in);
+void vref_get_reffield(const vref_model *m, int which, double *out);
+void vref_get_zeta(const vref_model *m, double *out);
+void vref_get_terrain(const vref_model *m, double *out);
+void vref_get_sponge(const vref_model *m, double *out);
+int  vref_rk3_step(vref_model *m, double dt, int n_sub);
+void vref_slow_tendency(vref_model *m, double *const *out);
+void vref_acoustic_substep(vref_model *m, double dtau);
+void vref_hevi_substep(vref_model *m, double dtau);
+void vref_sponge(vref_model *m, double dt);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

@@ -1,0 +1,217 @@
+"""ctypes view of the CPU oracle (oracle/vibe_oracle.h) for the tests.
+
+Two interchangeable back ends share one interface:
+  * ``port``: oracle/liboracle.so, the plain-C restatement of the reference
+    step (builds anywhere);
+  * ``ref``: oracle/_ref/libvibe_ref.so, the reference's own sources compiled
+    unchanged plus a thin driver (only where the reference tree was present
+    at build time).
+This module is test infrastructure: nothing on the product path imports it.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+ORACLE_DIR = os.path.join(ROOT, "oracle")
+PORT_SO = os.path.join(ORACLE_DIR, "liboracle.so")
+REF_SO = os.path.join(ORACLE_DIR, "_ref", "libvibe_ref.so")
+
+SPECIES = ["u", "v", "w", "rho", "theta", "pi", "qv", "qc", "qr", "qi", "qs", "qg"]
+NSPECIES = 12
+HALO = 4
+REFFIELDS = ["theta0", "pi0", "rho0", "p0", "qv0"]
+
+_D, _I = ctypes.c_double, ctypes.c_int
+
+
+class Setup(ctypes.Structure):
+    """Mirror of ``vo_setup`` (same field order)."""
+
+    _fields_ = [
+        ("nx", _I), ("ny", _I), ("nz", _I),
+        ("dx", _D), ("dy", _D), ("z_top", _D),
+        ("zeta_first", _D), ("zeta_stretch", _D),
+        ("terrain_kind", _I), ("hill_h", _D), ("hill_a", _D), ("hill_xc", _D), ("hill_yc", _D),
+        ("ref_kind", _I), ("theta0", _D), ("p_surf", _D), ("bv_n", _D), ("profile_dz", _D),
+        ("bubble_amplitude", _D), ("bubble_radius_x", _D), ("bubble_radius_z", _D),
+        ("bubble_xc", _D), ("bubble_yc", _D), ("bubble_zc", _D),
+        ("qv_surface", _D), ("qv_decay_height", _D),
+        ("u_background", _D), ("shear_u", _D),
+        ("advection", _I), ("weno_scalars", _I), ("moist", _I),
+        ("coriolis", _I), ("latitude", _D),
+        ("sponge_alpha", _D), ("sponge_start_fraction", _D),
+        ("divergence_damping", _D), ("divergence_order", _I),
+        ("pgf_perturbation", _I), ("acoustic_mode", _I), ("hevi_beta", _D),
+        ("split_fast", _I), ("weno_advective", _I),
+    ]
+
+    def copy(self, **kw):
+        s = Setup()
+        ctypes.pointer(s)[0] = self
+        for k, v in kw.items():
+            setattr(s, k, v)
+        return s
+
+
+def storage_shape(setup, species):
+    """(nsz, nsy, nsx) of a species' halo'd storage (field.hpp:40-53)."""
+    h2 = 2 * HALO
+    return (setup.nz + h2 + (species == 2), setup.ny + h2 + (species == 1),
+            setup.nx + h2 + (species == 0))
+
+
+def interior(setup, species, arr):
+    """View of the interior points incl. the extra face (State::pack order)."""
+    a = arr.reshape(storage_shape(setup, species))
+    nx, ny, nz = setup.nx, setup.ny, setup.nz
+    return a[HALO:HALO + nz + (species == 2), HALO:HALO + ny + (species == 1),
+             HALO:HALO + nx + (species == 0)]
+
+
+_libs = {}
+
+
+def _load(kind):
+    if kind in _libs:
+        return _libs[kind]
+    path = PORT_SO if kind == "port" else REF_SO
+    lib = ctypes.CDLL(path)
+    p = "vo_" if kind == "port" else "vref_"
+    vp = ctypes.c_void_p
+    dp = ctypes.POINTER(ctypes.c_double)
+    sig = {
+        "create": (vp, [ctypes.POINTER(Setup)]),
+        "destroy": (None, [vp]),
+        "storage_size": (ctypes.c_size_t, [vp, _I]),
+        "get_field": (None, [vp, _I, vp]),
+        "set_field": (None, [vp, _I, vp]),
+        "get_reffield": (None, [vp, _I, vp]),
+        "get_zeta": (None, [vp, vp]),
+        "get_terrain": (None, [vp, vp]),
+        "get_sponge": (None, [vp, vp]),
+        "rk3_step": (_I, [vp, _D, _I]),
+        "slow_tendency": (None, [vp, ctypes.POINTER(dp)]),
+        "acoustic_substep": (None, [vp, _D]),
+        "hevi_substep": (None, [vp, _D]),
+        "sponge": (None, [vp, _D]),
+    }
+    fns = {}
+    for name, (res, args) in sig.items():
+        f = getattr(lib, p + name)
+        f.restype = res
+        f.argtypes = args
+        fns[name] = f
+    if kind == "port":
+        lib.vo_setup_defaults.argtypes = [ctypes.POINTER(Setup)]
+        lib.vo_setup_defaults.restype = None
+        lib.vo_tridiagonal_solve.restype = _I
+        lib.vo_tridiagonal_solve.argtypes = [vp, vp, vp, vp, _I, vp, vp]
+        lib.vo_weno5_reconstruct.restype = None
+        lib.vo_weno5_reconstruct.argtypes = [_D, _D, _D, _D, _D, dp, dp]
+        lib.vo_bilinear.restype = _D
+        lib.vo_bilinear.argtypes = [vp, _I, _I, _I, _I, _D, _D, _I]
+        lib.vo_cfl_scan.restype = _D
+        lib.vo_cfl_scan.argtypes = [vp, vp, vp, vp, vp, _I, _I, _I, _D, _D, _D, _D, dp, dp]
+        lib.vo_neumaier_sum.restype = _D
+        lib.vo_neumaier_sum.argtypes = [vp, ctypes.c_size_t]
+        lib.vo_advect_scalar_flux.restype = None
+        lib.vo_advect_scalar_flux.argtypes = [vp] * 7 + [_I, _I, _I, _D, _D, _D, vp]
+    _libs[kind] = (lib, fns)
+    return _libs[kind]
+
+
+def port_lib():
+    return _load("port")[0]
+
+
+def ref_available():
+    return os.path.exists(REF_SO)
+
+
+def defaults():
+    """Config-1 warm bubble (64x64x40, dx=dy=dz=250 m, theta0=300 K)."""
+    s = Setup()
+    port_lib().vo_setup_defaults(ctypes.byref(s))
+    return s
+
+
+class Model:
+    """One oracle model instance (``kind`` = 'port' or 'ref')."""
+
+    def __init__(self, setup, kind="port"):
+        self.kind = kind
+        self.setup = setup.copy()
+        self._lib, self._f = _load(kind)
+        self.h = self._f["create"](ctypes.byref(self.setup))
+
+    def close(self):
+        if self.h:
+            self._f["destroy"](self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def size(self, sp):
+        return int(self._f["storage_size"](self.h, sp))
+
+    def get(self, sp):
+        a = np.empty(self.size(sp))
+        self._f["get_field"](self.h, sp, a.ctypes.data)
+        return a
+
+    def set(self, sp, arr):
+        a = np.ascontiguousarray(arr, dtype=np.float64).ravel()
+        assert a.size == self.size(sp)
+        self._f["set_field"](self.h, sp, a.ctypes.data)
+
+    def state(self):
+        return [self.get(sp) for sp in range(NSPECIES)]
+
+    def set_state(self, st):
+        for sp, a in enumerate(st):
+            self.set(sp, a)
+
+    def reffield(self, which):
+        a = np.empty(self.size(3))
+        self._f["get_reffield"](self.h, which, a.ctypes.data)
+        return a
+
+    def zeta(self):
+        a = np.empty(self.setup.nz + 1)
+        self._f["get_zeta"](self.h, a.ctypes.data)
+        return a
+
+    def terrain(self):
+        a = np.empty(self.setup.nx * self.setup.ny)
+        self._f["get_terrain"](self.h, a.ctypes.data)
+        return a
+
+    def sponge_profile(self):
+        a = np.empty(self.setup.nz)
+        self._f["get_sponge"](self.h, a.ctypes.data)
+        return a
+
+    def rk3_step(self, dt, n_sub):
+        return int(self._f["rk3_step"](self.h, dt, n_sub))
+
+    def slow_tendency(self):
+        outs = [np.empty(self.size(sp)) for sp in range(NSPECIES)]
+        ptrs = (ctypes.POINTER(ctypes.c_double) * NSPECIES)(
+            *[o.ctypes.data_as(ctypes.POINTER(ctypes.c_double)) for o in outs])
+        self._f["slow_tendency"](self.h, ptrs)
+        return outs
+
+    def acoustic_substep(self, dtau):
+        self._f["acoustic_substep"](self.h, dtau)
+
+    def hevi_substep(self, dtau):
+        self._f["hevi_substep"](self.h, dtau)
+
+    def sponge(self, dt):
+        self._f["sponge"](self.h, dt)
