@@ -1,0 +1,120 @@
+/* include/vibe_c_kernels.h
+ *
+ * Drop-in replacement for the reference's C11 hot-kernel ABI
+ * (include/vibe/common/c_kernels.h:29-117): same symbol names, argument
+ * meaning, NULL handling and return codes, so a caller linked against the
+ * reference's libvibe links against libvibe_gb300.so unchanged. The work runs
+ * on the GPU (sm_103a): the host-pointer entry points stage their arrays
+ * through device memory on an internal stream; the *_dev entry points take
+ * device pointers and a stream and never copy.
+ *
+ * Conventions kept from c_kernels.h:13-19: all scalars double; errors are
+ * return codes, never errno; no global state visible to the caller.
+ * Differences, each deliberate:
+ *   - vibe_tridiagonal_solve_f64 solves the system its contract documents
+ *     (c_kernels.h:38-55). The shipped c_kernels.c:18-60 does not: on the
+ *     reference's own test matrix diag(1,-4,1) it leaves a residual of 9e-2.
+ *   - device failures return VIBE_C_ERR_DEVICE (new code 3); void/double
+ *     functions report them through vibe_c_last_error().
+ */
+#ifndef VIBE_GB300_C_KERNELS_H
+#define VIBE_GB300_C_KERNELS_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define VIBE_C_OK 0
+#define VIBE_C_ERR_SINGULAR 1
+#define VIBE_C_ERR_BAD_ARG 2
+#define VIBE_C_ERR_DEVICE 3
+
+typedef struct CUstream_st *vibe_stream_t; /* == cudaStream_t */
+
+/* Replaces c_kernels.h:54-55 (vibe_tridiagonal_solve_f64). Solves
+ * a[k] x[k-1] + b[k] x[k] + c[k] x[k+1] = d[k], k = 0..n-1; a, c have n-1
+ * entries (a[k-1] is row k's sub-diagonal) and may be NULL (= 0). ws (n) is
+ * caller workspace, as in the reference; its contents on return are
+ * unspecified. Returns VIBE_C_OK, VIBE_C_ERR_SINGULAR on a zero pivot,
+ * VIBE_C_ERR_BAD_ARG, or VIBE_C_ERR_DEVICE. */
+int vibe_tridiagonal_solve_f64(const double *a, const double *b, const double *c,
+                               const double *d, int n, double *x, double *ws);
+
+/* Replaces c_kernels.h:65-66. WENO5 left/right face reconstruction
+ * (d = 0.1/0.6/0.3, eps = 1e-6). Silently returns when an output is NULL. */
+void vibe_weno5_reconstruct_f64(double qm2, double qm1, double q0, double q1,
+                                double q2, double *q_left, double *q_right);
+
+/* Replaces c_kernels.h:77-78. Bilinear sample of a halo'd FieldT-layout
+ * array at fractional cell index (xi, yj), level k, clamped to the interior.
+ * Returns 0 for NULL f or nz <= 0. */
+double vibe_bilinear_f64(const double *f, int halo, int nsx, int nsy, int nz,
+                         double xi, double yj, int k);
+
+/* Replaces c_kernels.h:89-92. Max over cells of
+ * dt*(|u|/dx + |v|/dy + |w|/max(dzeta[k]*(z_top - zs), 1)); also the max wind
+ * speed and the min dz (0 when none). zs may be NULL (flat). Returns 0 when
+ * u, v, w or dzeta is NULL. */
+double vibe_cfl_scan_f64(const double *u, const double *v, const double *w,
+                         const double *dzeta, const double *zs, int nx, int ny,
+                         int nz, double dx, double dy, double z_top, double dt,
+                         double *max_wind_out, double *min_dz_out);
+
+/* Replaces c_kernels.h:101. Compensated (Neumaier) sum of n doubles. The
+ * device reduction compensates per thread, per warp and across blocks, so the
+ * result carries the same O(eps) error bound as the serial loop (not the same
+ * bits). Returns 0 for NULL x. */
+double vibe_neumaier_sum_f64(const double *x, size_t n);
+
+/* Replaces c_kernels.h:113-117. Second-order flux-form advection on
+ * collocated, halo-free, i-fastest arrays, periodic in x and y, zero vertical
+ * flux on the first and last level. Silently returns on NULL arguments. */
+void vibe_advect_scalar_flux_f64(const double *q, const double *rho,
+                                 const double *u, const double *v, const double *w,
+                                 const double *dzeta, const double *zs, int nx,
+                                 int ny, int nz, double dx, double dy,
+                                 double z_top, double *dqdt);
+
+/* ---- device-pointer and batched forms (no reference counterpart; the same
+ * arithmetic as the host entry points above) ---- */
+
+/* n_sys independent systems of size n, each stored contiguously
+ * (system s uses a + s*(n-1), b + s*n, ...). One thread per system.
+ * status (device, n_sys ints) receives the per-system return code; may be
+ * NULL. Returns VIBE_C_OK or VIBE_C_ERR_BAD_ARG/VIBE_C_ERR_DEVICE (launch). */
+int vibe_tridiagonal_solve_batched_f64_dev(const double *a, const double *b,
+                                           const double *c, const double *d,
+                                           int n, int n_sys, double *x,
+                                           int *status, vibe_stream_t stream);
+/* Host-pointer batched form; returns the first non-zero per-system code. */
+int vibe_tridiagonal_solve_batched_f64(const double *a, const double *b,
+                                       const double *c, const double *d, int n,
+                                       int n_sys, double *x);
+/* Batched WENO5: q holds 5*n values (stencils q[5e..5e+4]). */
+int vibe_weno5_reconstruct_batched_f64_dev(const double *q, size_t n,
+                                           double *q_left, double *q_right,
+                                           vibe_stream_t stream);
+int vibe_cfl_scan_f64_dev(const double *u, const double *v, const double *w,
+                          const double *dzeta, const double *zs, int nx, int ny,
+                          int nz, double dx, double dy, double z_top, double dt,
+                          double *out3 /* device: cfl, max_wind, min_dz */,
+                          vibe_stream_t stream);
+int vibe_neumaier_sum_f64_dev(const double *x, size_t n, double *out /* device */,
+                              vibe_stream_t stream);
+int vibe_advect_scalar_flux_f64_dev(const double *q, const double *rho,
+                                    const double *u, const double *v,
+                                    const double *w, const double *dzeta,
+                                    const double *zs, int nx, int ny, int nz,
+                                    double dx, double dy, double z_top,
+                                    double *dqdt, vibe_stream_t stream);
+
+/* Message of the last device failure seen by this thread ("" if none). */
+const char *vibe_c_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

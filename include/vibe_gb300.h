@@ -1,0 +1,142 @@
+/* include/vibe_gb300.h
+ *
+ * C ABI of the GB300 dynamics step: the device-resident counterpart of the
+ * reference's C++ stepper interfaces. Each entry point names the reference
+ * interface it replaces:
+ *   vibe_gb300_model_create     RungeKutta3Integrator ctor (include/vibe/time/
+ *                               runge_kutta.hpp:53-56) + Grid/ReferenceState/
+ *                               State set-up (geometry.hpp:89-161,
+ *                               reference_state.hpp:36-49, state.hpp:98-103)
+ *                               + driver::init_warm_bubble
+ *                               (initial_conditions.hpp:84-85)
+ *   vibe_gb300_step             Integrator::step(State&, const StepContext&)
+ *                               (include/vibe/time/integrator.hpp:65), n times
+ *   vibe_gb300_slow_tendency    Equations::tendencies (equations.hpp:67)
+ *   vibe_gb300_acoustic_substep RungeKutta3Integrator::acoustic_substep
+ *                               (runge_kutta.hpp:62-63)
+ *   vibe_gb300_hevi_substep     AcousticSubstepper::step (acoustic_substep.hpp:59)
+ *   vibe_gb300_sponge           Damping::apply_sponge (damping.hpp:36)
+ *   vibe_gb300_get/set_field    FieldT::storage() of a State species
+ *                               (field.hpp:73-74), same halo'd layout
+ * Errors: every int-returning call returns 0 on success and a negative
+ * VIBE_GB300_E* code otherwise (the reference throws NumericalError /
+ * VIBE_CHECK failures instead); vibe_gb300_last_error() gives the message.
+ * Threading: one model is not thread-safe (as the reference's integrators);
+ * separate models may be used from separate threads. All device work of a
+ * model runs on its own CUDA stream.
+ */
+#ifndef VIBE_GB300_H
+#define VIBE_GB300_H
+
+#include <stddef.h>
+
+#include "vibe_c_kernels.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define VIBE_GB300_OK 0
+#define VIBE_GB300_EBADARG (-1)
+#define VIBE_GB300_EDEVICE (-2)
+#define VIBE_GB300_ENONFINITE (-3) /* RK3 non-finite check, runge_kutta.cpp:103-106 */
+#define VIBE_GB300_ESINGULAR (-4)  /* Thomas pivot < 1e-300, helmholtz.cpp:78-80 */
+#define VIBE_GB300_EUNSUPPORTED (-5)
+
+#define VIBE_GB300_FP64 0  /* all arithmetic FP64 */
+#define VIBE_GB300_MIXED 1 /* FP64 state, FP32 tendencies and substeps */
+
+/* Species order of dyn::Species (include/vibe/dyn/state.hpp:53-55). */
+enum vibe_gb300_species {
+  VIBE_U = 0, VIBE_V, VIBE_W, VIBE_RHO, VIBE_THETA, VIBE_PI, VIBE_QV,
+  VIBE_QC, VIBE_QR, VIBE_QI, VIBE_QS, VIBE_QG, VIBE_NSPECIES
+};
+
+/* Case and numerics description. Field meaning as in config.hpp:26-68,
+ * IcOptions (initial_conditions.hpp:49-74) and ReferenceState; the last
+ * four fields select compositions the reference does not provide (see
+ * the design doc). Plain C struct, no defaults: fill with
+ * vibe_gb300_setup_defaults() first. */
+typedef struct vibe_gb300_setup {
+  int nx, ny, nz;
+  double dx, dy, z_top;
+  double zeta_first, zeta_stretch;  /* make_stretched_zeta(nz, first, stretch) */
+  int terrain_kind;                 /* 0 flat, 1 Gaussian hill */
+  double hill_h, hill_a, hill_xc, hill_yc;
+  int ref_kind;                     /* 0 isothermal(theta0), 1 theta0*exp(N^2 z/g) profile */
+  double theta0, p_surf, bv_n, profile_dz;
+  double bubble_amplitude, bubble_radius_x, bubble_radius_z;
+  double bubble_xc, bubble_yc, bubble_zc;
+  double qv_surface, qv_decay_height;
+  double u_background, shear_u;
+  int advection;                    /* 2, 4, 6 central; 5 weno5 */
+  int weno_scalars;                 /* theta/q by WENO5 flux form */
+  int moist;
+  int coriolis;                     /* 0 none, 1 f-plane, 2 beta-plane */
+  double latitude;
+  double sponge_alpha, sponge_start_fraction;
+  double divergence_damping;
+  int divergence_order;
+  int pgf_perturbation;             /* pressure gradient on pi - pi0 */
+  int acoustic_mode;                /* 0 explicit FB, 1 reference HEVI, 2 consistent HEVI */
+  double hevi_beta;
+  int split_fast;                   /* fast terms integrated only by the substeps */
+  int weno_advective;               /* WENO5 flux form + q div(u) */
+} vibe_gb300_setup;
+
+typedef struct vibe_gb300_model vibe_gb300_model;
+
+void vibe_gb300_setup_defaults(vibe_gb300_setup *s);
+
+/* Builds grid metrics, reference state and the warm-bubble initial state on
+ * the host (same formulas as the reference), uploads them and allocates all
+ * device buffers. precision: VIBE_GB300_FP64 or VIBE_GB300_MIXED (the mixed
+ * path needs flat terrain, a horizontally uniform reference state,
+ * pgf_perturbation = 1 and split_fast = 1). */
+int vibe_gb300_model_create(const vibe_gb300_setup *s, int precision,
+                            vibe_gb300_model **out);
+void vibe_gb300_model_destroy(vibe_gb300_model *m);
+
+/* Number of doubles in the FieldT storage of a species (halo 4). */
+size_t vibe_gb300_storage_size(const vibe_gb300_model *m, int species);
+/* Copy a species between the device state and a host array in FieldT
+ * storage layout. get writes zeros into halo points other than the east/
+ * north ghost line the step reads (the serial reference never fills them). */
+int vibe_gb300_get_field(vibe_gb300_model *m, int species, double *host);
+int vibe_gb300_set_field(vibe_gb300_model *m, int species, const double *host);
+/* Reference-state field (0 theta0, 1 pi0, 2 rho0, 3 p0, 4 qv0), zeta
+ * (nz+1), terrain (nx*ny) and sponge profile (nz) as built on the host. */
+int vibe_gb300_get_reffield(const vibe_gb300_model *m, int which, double *host);
+int vibe_gb300_get_zeta(const vibe_gb300_model *m, double *host);
+int vibe_gb300_get_terrain(const vibe_gb300_model *m, double *host);
+int vibe_gb300_get_sponge(const vibe_gb300_model *m, double *host);
+
+/* n_steps RK3 steps of length dt with n_sub acoustic substeps per stage.
+ * Blocks until done; returns VIBE_GB300_ENONFINITE if a stage produced a
+ * non-finite value. */
+int vibe_gb300_step(vibe_gb300_model *m, double dt, int n_sub, int n_steps);
+/* Enqueue only (no host synchronisation); vibe_gb300_sync returns the
+ * status of everything enqueued since the previous sync. */
+int vibe_gb300_step_async(vibe_gb300_model *m, double dt, int n_sub, int n_steps);
+int vibe_gb300_sync(vibe_gb300_model *m);
+
+/* Kernel-level entry points (FP64 path only for the tendency). */
+int vibe_gb300_slow_tendency(vibe_gb300_model *m, double *const *host_out);
+int vibe_gb300_acoustic_substep(vibe_gb300_model *m, double dtau);
+int vibe_gb300_hevi_substep(vibe_gb300_model *m, double dtau);
+int vibe_gb300_sponge(vibe_gb300_model *m, double dt);
+
+/* Device pointer of a species in the device layout
+ * idx = (k*(ny+1) + j)*pitch + i, and that pitch. */
+int vibe_gb300_device_field(vibe_gb300_model *m, int species, double **ptr, int *pitch);
+vibe_stream_t vibe_gb300_stream(vibe_gb300_model *m);
+/* Number of kernels this model launches per step for (dt, n_sub). */
+int vibe_gb300_launches_per_step(const vibe_gb300_model *m, int n_sub);
+
+const char *vibe_gb300_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

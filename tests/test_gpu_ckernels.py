@@ -1,0 +1,181 @@
+"""GPU C-ABI kernels (include/vibe_c_kernels.h) against the reference's own
+known-answer tests (tests/unit/test_common.cpp:163-266,
+tests/unit/test_time.cpp:53-100, tests/unit/test_gpu_precision.cpp) and
+against the oracle on seeded inputs."""
+import ctypes
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+# ---- known answers from the reference's tests --------------------------------
+def test_thomas_residual_diag_1_m4_1(vg):
+    """test_common.cpp:163-175: diag(1,-4,1), d = 1, residual <= 1e-10 (the
+    reference's own c_kernels.c fails this with 9e-2)."""
+    n = 24
+    a = np.ones(n - 1)
+    c = np.ones(n - 1)
+    b = np.full(n, -4.0)
+    d = np.ones(n)
+    rc, x = vg.tridiagonal_solve(a, b, c, d)
+    assert rc == 0
+    lhs = -4.0 * x
+    lhs[1:] += x[:-1]
+    lhs[:-1] += x[1:]
+    assert np.abs(lhs - 1.0).max() <= 1e-10
+
+
+def test_thomas_singular_and_bad_args(vg):
+    """test_common.cpp:177-186."""
+    lib = vg.lib
+    b = np.zeros(2)
+    d = np.ones(2)
+    x = np.zeros(2)
+    ws = np.zeros(2)
+    assert lib.vibe_tridiagonal_solve_f64(None, b.ctypes.data, None, d.ctypes.data, 2, x.ctypes.data,
+                                          ws.ctypes.data) == 1
+    assert lib.vibe_tridiagonal_solve_f64(None, None, None, None, 2, x.ctypes.data, ws.ctypes.data) == 2
+    assert lib.vibe_tridiagonal_solve_f64(None, b.ctypes.data, None, d.ctypes.data, 0, x.ctypes.data,
+                                          ws.ctypes.data) == 2
+
+
+def test_thomas_mms_and_variable_coefficients(vg, oc):
+    """test_time.cpp:53-88 pattern; variable coefficients vs the oracle."""
+    n = 24
+    j = np.arange(n)
+    b = 4.0 + 0.1 * j
+    d = np.sin(0.3 * j)
+    a = np.full(n - 1, -1.0)
+    c = np.full(n - 1, -1.2)
+    rc, x = vg.tridiagonal_solve(a, b, c, d)
+    assert rc == 0
+    xo = np.zeros(n)
+    ws = np.zeros(n)
+    L = oc.port_lib()
+    assert L.vo_tridiagonal_solve(a.ctypes.data, b.ctypes.data, c.ctypes.data, d.ctypes.data, n, xo.ctypes.data,
+                                  ws.ctypes.data) == 0
+    assert np.abs(x - xo).max() <= 1e-12 * np.abs(xo).max()
+
+
+def test_thomas_batched_matches_oracle(vg, oc):
+    rng = np.random.default_rng(7)
+    n_sys, n = 1000, 60
+    b = 4.0 + rng.random((n_sys, n))
+    a = -rng.random((n_sys, n - 1))
+    c = -rng.random((n_sys, n - 1))
+    d = rng.standard_normal((n_sys, n))
+    rc, x = vg.tridiagonal_solve_batched(a, b, c, d)
+    assert rc == 0
+    L = oc.port_lib()
+    for s in (0, 17, 999):
+        xo = np.zeros(n)
+        ws = np.zeros(n)
+        aa, bb, cc, dd = (np.ascontiguousarray(v[s]) for v in (a, b, c, d))
+        L.vo_tridiagonal_solve(aa.ctypes.data, bb.ctypes.data, cc.ctypes.data, dd.ctypes.data, n, xo.ctypes.data,
+                               ws.ctypes.data)
+        assert np.abs(x[s] - xo).max() <= 1e-12 * np.abs(xo).max()
+
+
+def test_weno5_known_answers(vg, oc):
+    """test_common.cpp:188-205: exact on constants, bounded on monotone data."""
+    ql, qr = vg.weno5_reconstruct(3.5, 3.5, 3.5, 3.5, 3.5)
+    assert abs(ql - 3.5) <= 1e-12 and abs(qr - 3.5) <= 1e-12
+    ql, qr = vg.weno5_reconstruct(0.2, -0.4, 1.1, 0.9, 2.3)
+    assert -0.4 <= ql <= 2.3 and -0.4 <= qr <= 2.3
+    L = oc.port_lib()
+    a, b = ctypes.c_double(), ctypes.c_double()
+    L.vo_weno5_reconstruct(0.2, -0.4, 1.1, 0.9, 2.3, ctypes.byref(a), ctypes.byref(b))
+    assert abs(ql - a.value) <= 1e-14 and abs(qr - b.value) <= 1e-14
+
+
+def test_bilinear_known_answers(vg):
+    """test_common.cpp:207-226."""
+    halo, nx, ny, nz = 2, 5, 4, 2
+    nsx, nsy = nx + 2 * halo, ny + 2 * halo
+    f = np.zeros((nz + 2 * halo, nsy, nsx))
+    for k in range(nz):
+        for j in range(ny):
+            for i in range(nx):
+                f[k + halo, j + halo, i + halo] = 10.0 * i + j + 100.0 * k
+    assert abs(vg.bilinear(f, halo, nsx, nsy, nz, 2.0, 1.0, 1) - 121.0) <= 1e-12
+    assert abs(vg.bilinear(f, halo, nsx, nsy, nz, 1.5, 1.0, 0) - 16.0) <= 1e-12
+    assert abs(vg.bilinear(f, halo, nsx, nsy, nz, -50.0, -50.0, 0) - 0.0) <= 1e-12
+
+
+def test_cfl_scan_known_answers(vg):
+    """test_common.cpp:228-242: linear in dt, hand value 0.02, min dz 1000."""
+    nx, ny, nz = 4, 3, 3
+    u = np.full(nx * ny * nz, 20.0)
+    v = np.zeros_like(u)
+    w = np.zeros_like(u)
+    dzeta = np.array([0.05, 0.10, 0.20])
+    c1, mw, mdz = vg.cfl_scan(u, v, w, dzeta, None, nx, ny, nz, 1000.0, 1000.0, 20000.0, 1.0)
+    c2, _, _ = vg.cfl_scan(u, v, w, dzeta, None, nx, ny, nz, 1000.0, 1000.0, 20000.0, 2.0)
+    assert abs(c2 - 2.0 * c1) <= 1e-12
+    assert abs(mw - 20.0) <= 1e-12
+    assert abs(mdz - 0.05 * 20000.0) <= 1e-9
+    assert abs(c1 - 20.0 / 1000.0) <= 1e-12
+
+
+def test_cfl_scan_matches_oracle_with_terrain(vg, oc):
+    rng = np.random.default_rng(3)
+    nx, ny, nz = 37, 23, 19
+    n = nx * ny * nz
+    u, v, w = (rng.standard_normal(n) * s for s in (15.0, 10.0, 2.0))
+    dzeta = rng.random(nz) * 0.1 + 1e-3
+    zs = rng.random(nx * ny) * 500.0
+    r, mw, mdz = vg.cfl_scan(u, v, w, dzeta, zs, nx, ny, nz, 1000.0, 800.0, 20000.0, 6.0)
+    L = oc.port_lib()
+    a, b = ctypes.c_double(), ctypes.c_double()
+    ro = L.vo_cfl_scan(u.ctypes.data, v.ctypes.data, w.ctypes.data, dzeta.ctypes.data, zs.ctypes.data, nx, ny, nz,
+                       1000.0, 800.0, 20000.0, 6.0, ctypes.byref(a), ctypes.byref(b))
+    assert r == ro and mw == a.value and mdz == b.value  # max/min are exact
+
+
+def test_neumaier_cancellation(vg):
+    """test_common.cpp:244-254: [1e16, 1 x 9998, -1e16] sums to 9998."""
+    n = 10000
+    x = np.ones(n)
+    x[0] = 1e16
+    x[-1] = -1e16
+    assert abs(vg.neumaier_sum(x) - (n - 2)) <= 1e-6
+    assert abs(vg.neumaier_sum(np.ones(1_000_000)) - 1e6) <= 1e-3  # test_gpu_precision.cpp reduce on 1e6 ones
+
+
+def test_neumaier_matches_oracle(vg, oc):
+    rng = np.random.default_rng(11)
+    x = rng.standard_normal(3_000_017) * 10.0 ** rng.integers(-8, 8, 3_000_017)
+    L = oc.port_lib()
+    ref = L.vo_neumaier_sum(x.ctypes.data, x.size)
+    got = vg.neumaier_sum(x)
+    assert abs(got - ref) <= 1e-12 * np.abs(x).sum()
+    assert vg.neumaier_sum(np.zeros(0)) == 0.0
+
+
+def test_flux_advection_constant_is_zero(vg):
+    """test_common.cpp:256-266."""
+    nx, ny, nz = 6, 5, 4
+    n = nx * ny * nz
+    q, rho, u, v, w = (np.full(n, val) for val in (3.0, 1.2, 7.0, -3.0, 0.5))
+    dzeta = np.array([0.05, 0.08, 0.12, 0.2])
+    dq = vg.advect_scalar_flux(q, rho, u, v, w, dzeta, None, nx, ny, nz, 1000.0, 1000.0, 20000.0)
+    assert np.abs(dq).max() <= 1e-10
+
+
+def test_flux_advection_matches_oracle(vg, oc):
+    rng = np.random.default_rng(5)
+    nx, ny, nz = 33, 17, 9
+    n = nx * ny * nz
+    q = rng.random(n)
+    rho = 1.0 + 0.1 * rng.random(n)
+    u, v, w = (rng.standard_normal(n) for _ in range(3))
+    dzeta = rng.random(nz) * 0.1 + 0.01
+    zs = rng.random(nx * ny) * 300.0
+    dq = vg.advect_scalar_flux(q, rho, u, v, w, dzeta, zs, nx, ny, nz, 900.0, 1100.0, 15000.0)
+    out = np.zeros(n)
+    oc.port_lib().vo_advect_scalar_flux(q.ctypes.data, rho.ctypes.data, u.ctypes.data, v.ctypes.data, w.ctypes.data,
+                                        dzeta.ctypes.data, zs.ctypes.data, nx, ny, nz, 900.0, 1100.0, 15000.0,
+                                        out.ctypes.data)
+    assert np.abs(dq - out).max() <= 1e-12 * np.abs(out).max()

@@ -1,0 +1,223 @@
+"""GPU parity of the dynamics step against the CPU oracle (oracle/vibe_oracle.c,
+itself pinned bit for bit to the reference compiled unchanged).
+
+Tolerances (relative to each field's max |value| over the compared points):
+  FP64 GPU path    <= 1e-12 per step / per kernel
+  mixed GPU path   <= 1e-5  per step
+Integer/index work (the set-up on the host) must be bit-exact.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+TOL64 = 1e-12
+TOLMX = 1e-5
+
+
+def small_setup(vg, **kw):
+    base = dict(nx=20, ny=16, nz=12, dx=250.0, dy=250.0, z_top=3000.0, zeta_first=1.0, zeta_stretch=1.08,
+                bubble_xc=2500.0, bubble_yc=2000.0, bubble_zc=1000.0, bubble_radius_x=1500.0,
+                bubble_radius_z=1000.0, u_background=5.0, shear_u=0.001)
+    base.update(kw)
+    return vg.Setup.defaults(**base)
+
+
+def oracle_setup(oc, s):
+    t = oc.Setup()
+    for name, _ in oc.Setup._fields_:
+        setattr(t, name, getattr(s, name))
+    return t
+
+
+def rel_err(vg, s, sp, got, ref):
+    g = vg.interior(s, sp, got)
+    r = vg.interior(s, sp, ref)
+    scale = np.abs(r).max()
+    if scale == 0.0:
+        return float(np.abs(g).max())
+    return float(np.abs(g - r).max() / scale)
+
+
+def assert_state_close(vg, s, got, ref, tol, species=range(7), what=""):
+    errs = {vg.SPECIES[sp]: rel_err(vg, s, sp, got[sp], ref[sp]) for sp in species}
+    bad = {k: v for k, v in errs.items() if not v <= tol}
+    assert not bad, "%s: relative error above %g: %s (all: %s)" % (what, tol, bad, errs)
+    return errs
+
+
+SCHEMES = [
+    dict(advection=2, weno_scalars=0, pgf_perturbation=0, split_fast=0, weno_advective=0),
+    dict(advection=4, weno_scalars=0, pgf_perturbation=0, split_fast=0, coriolis=1),
+    dict(advection=6, weno_scalars=0, pgf_perturbation=1, split_fast=1, coriolis=2, moist=1, qv_surface=0.01),
+    dict(advection=5, weno_scalars=1, pgf_perturbation=0, split_fast=0, weno_advective=0, ref_kind=1),
+    dict(advection=5, weno_scalars=1, pgf_perturbation=1, split_fast=1, weno_advective=1,
+         divergence_damping=50.0, divergence_order=4),
+    dict(advection=2, weno_scalars=0, divergence_damping=50.0, divergence_order=2, moist=1),
+]
+
+
+def test_setup_bit_exact(vg, oc):
+    s = small_setup(vg, ref_kind=1)
+    with vg.Model(s, vg.FP64) as m:
+        o = oc.Model(oracle_setup(oc, s), "port")
+        for sp in range(12):
+            assert np.array_equal(m.get(sp), o.get(sp)), vg.SPECIES[sp]
+        for r in range(5):
+            assert np.array_equal(m.reffield(r), o.reffield(r))
+        assert np.array_equal(m.zeta(), o.zeta())
+        assert np.array_equal(m.sponge_profile(), o.sponge_profile())
+
+
+@pytest.mark.parametrize("scheme", range(len(SCHEMES)))
+def test_slow_tendency_fp64(vg, oc, scheme):
+    s = small_setup(vg, **SCHEMES[scheme])
+    with vg.Model(s, vg.FP64) as m:
+        o = oc.Model(oracle_setup(oc, s), "port")
+        assert_state_close(vg, s, m.slow_tendency(), o.slow_tendency(), TOL64, range(12), "slow tendency")
+
+
+@pytest.mark.parametrize("pgf", [0, 1])
+def test_acoustic_substep_fp64(vg, oc, pgf):
+    s = small_setup(vg, pgf_perturbation=pgf)
+    with vg.Model(s, vg.FP64) as m:
+        o = oc.Model(oracle_setup(oc, s), "port")
+        for _ in range(3):
+            m.acoustic_substep(0.3)
+            o.acoustic_substep(0.3)
+        assert_state_close(vg, s, m.state(), o.state(), TOL64, range(7), "FB substep")
+
+
+def test_reference_hevi_substep_fp64(vg, oc):
+    s = small_setup(vg, acoustic_mode=1, pgf_perturbation=0)
+    with vg.Model(s, vg.FP64) as m:
+        o = oc.Model(oracle_setup(oc, s), "port")
+        for _ in range(2):
+            m.hevi_substep(0.7)
+            o.hevi_substep(0.7)
+        assert_state_close(vg, s, m.state(), o.state(), TOL64, range(7), "reference HEVI substep")
+
+
+@pytest.mark.parametrize("beta", [0.5, 0.6])
+def test_consistent_hevi_substep_fp64(vg, oc, beta):
+    s = small_setup(vg, acoustic_mode=2, hevi_beta=beta)
+    with vg.Model(s, vg.FP64) as m:
+        o = oc.Model(oracle_setup(oc, s), "port")
+        for _ in range(3):
+            m.hevi_substep(1.0)
+            o.hevi_substep(1.0)
+        assert_state_close(vg, s, m.state(), o.state(), TOL64, range(7), "consistent HEVI substep")
+
+
+def test_sponge_fp64(vg, oc):
+    s = small_setup(vg, sponge_alpha=0.3, sponge_start_fraction=0.5)
+    with vg.Model(s, vg.FP64) as m:
+        o = oc.Model(oracle_setup(oc, s), "port")
+        m.sponge(6.0)
+        o.sponge(6.0)
+        assert_state_close(vg, s, m.state(), o.state(), TOL64, range(7), "sponge")
+
+
+STEP_CASES = [
+    dict(pgf_perturbation=0, split_fast=0, weno_scalars=0, advection=2, weno_advective=0),  # reference composition
+    dict(pgf_perturbation=0, split_fast=0, weno_scalars=1, advection=5, weno_advective=0),  # O-WENO
+    dict(),                                                                                  # stable, FB
+    dict(acoustic_mode=2, ref_kind=1),                                                        # stable, HEVI
+    dict(acoustic_mode=1, pgf_perturbation=0, split_fast=0),                                  # O-HEVI
+]
+
+
+@pytest.mark.parametrize("case", range(len(STEP_CASES)))
+def test_rk3_step_fp64(vg, oc, case):
+    s = small_setup(vg, **STEP_CASES[case])
+    with vg.Model(s, vg.FP64) as m:
+        o = oc.Model(oracle_setup(oc, s), "port")
+        m.step(2.0, 4, 1)
+        assert o.rk3_step(2.0, 4) == 0
+        assert_state_close(vg, s, m.state(), o.state(), TOL64, range(12), "rk3 step")
+
+
+@pytest.mark.parametrize("case", [2, 3])
+def test_rk3_step_mixed(vg, oc, case):
+    s = small_setup(vg, **STEP_CASES[case])
+    with vg.Model(s, vg.MIXED) as m:
+        o = oc.Model(oracle_setup(oc, s), "port")
+        m.step(2.0, 4, 1)
+        assert o.rk3_step(2.0, 4) == 0
+        assert_state_close(vg, s, m.state(), o.state(), TOLMX, range(7), "mixed rk3 step")
+
+
+def test_mixed_many_steps_track_fp64(vg):
+    """Mixed vs FP64 GPU over 10 steps of a HEVI case (error growth bound)."""
+    s = small_setup(vg, acoustic_mode=2, ref_kind=1, nx=24, ny=24, nz=20, dx=1000.0, dy=1000.0, z_top=10000.0,
+                    bubble_xc=12000.0, bubble_yc=12000.0, bubble_zc=3000.0, bubble_radius_x=4000.0,
+                    bubble_radius_z=2000.0, bubble_amplitude=3.0, u_background=10.0, shear_u=0.0)
+    with vg.Model(s, vg.FP64) as a, vg.Model(s, vg.MIXED) as b:
+        a.step(6.0, 6, 10)
+        b.step(6.0, 6, 10)
+        errs = assert_state_close(vg, s, b.state(), a.state(), 1e-4, range(7), "10 mixed steps")
+        print("mixed vs fp64 after 10 steps:", errs)
+
+
+@pytest.mark.parametrize("dims", [(13, 7, 5), (9, 11, 3), (5, 4, 2), (1, 6, 4)])
+def test_ragged_and_tiny_grids(vg, oc, dims):
+    nx, ny, nz = dims
+    s = small_setup(vg, nx=nx, ny=ny, nz=nz, bubble_xc=nx * 125.0, bubble_yc=ny * 125.0, bubble_zc=500.0)
+    for prec, tol, case in ((vg.FP64, TOL64, 2), (vg.FP64, TOL64, 0), (vg.MIXED, TOLMX, 2)):
+        t = small_setup(vg, nx=nx, ny=ny, nz=nz, bubble_xc=nx * 125.0, bubble_yc=ny * 125.0, bubble_zc=500.0,
+                        **STEP_CASES[case])
+        with vg.Model(t, prec) as m:
+            o = oc.Model(oracle_setup(oc, t), "port")
+            m.step(1.0, 2, 1)
+            assert o.rk3_step(1.0, 2) == 0
+            assert_state_close(vg, t, m.state(), o.state(), tol, range(7), "grid %s prec %d" % (dims, prec))
+
+
+def test_halo_ghost_line_is_read(vg, oc):
+    """The reference reads rho at i = nx and j = ny without a clamp
+    (equations.cpp:120-123); a non-zero halo there must change the result
+    the same way on both sides."""
+    s = small_setup(vg, **STEP_CASES[0])
+    with vg.Model(s, vg.FP64) as m:
+        o = oc.Model(oracle_setup(oc, s), "port")
+        rho = o.get(3)
+        a = rho.reshape(vg.storage_shape(s, 3))
+        a[4:4 + s.nz, 4:4 + s.ny, 4 + s.nx] = 1.1    # east ghost column
+        a[4:4 + s.nz, 4 + s.ny, 4:4 + s.nx] = 0.9    # north ghost row
+        o.set(3, a)
+        m.set(3, a)
+        assert_state_close(vg, s, m.slow_tendency(), o.slow_tendency(), TOL64, [3], "ghost line")
+
+
+def test_nonfinite_state_is_reported(vg):
+    s = small_setup(vg)
+    for prec in (vg.FP64, vg.MIXED):
+        with vg.Model(s, prec) as m:
+            th = m.get(4)
+            th.reshape(vg.storage_shape(s, 4))[6, 6, 6] = np.nan
+            m.set(4, th)
+            with pytest.raises(vg.VibeError) as e:
+                m.step(2.0, 4, 1)
+            assert e.value.code == -3
+            # the model stays usable after the error
+            m.set(4, np.nan_to_num(th, nan=300.0))
+
+
+def test_mixed_rejects_unsupported_setups(vg):
+    with pytest.raises(vg.VibeError) as e:
+        vg.Model(small_setup(vg, terrain_kind=1, hill_h=300.0, hill_a=1000.0, hill_xc=2500.0, hill_yc=2000.0),
+                 vg.MIXED)
+    assert e.value.code == -5
+    with pytest.raises(vg.VibeError):
+        vg.Model(small_setup(vg, split_fast=0), vg.MIXED)
+
+
+def test_terrain_fp64_step(vg, oc):
+    s = small_setup(vg, terrain_kind=1, hill_h=300.0, hill_a=1000.0, hill_xc=2500.0, hill_yc=2000.0,
+                    acoustic_mode=2, ref_kind=1)
+    with vg.Model(s, vg.FP64) as m:
+        o = oc.Model(oracle_setup(oc, s), "port")
+        assert np.array_equal(m.terrain(), o.terrain())
+        m.step(2.0, 3, 1)
+        assert o.rk3_step(2.0, 3) == 0
+        assert_state_close(vg, s, m.state(), o.state(), TOL64, range(7), "terrain step")

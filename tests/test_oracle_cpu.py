@@ -1,0 +1,157 @@
+"""CPU tests of the oracle: the plain-C restatement against the reference
+compiled unchanged (bit for bit) where the reference tree was available at
+build time, against the committed golden fixtures everywhere, and the
+reference's own known-answer tests for the C ABI."""
+import ctypes
+import os
+
+import numpy as np
+import pytest
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def small(oc, **kw):
+    s = oc.defaults()
+    base = dict(nx=20, ny=16, nz=12, dx=250.0, dy=250.0, z_top=3000.0, zeta_first=1.0, zeta_stretch=1.08,
+                bubble_xc=2500.0, bubble_yc=2000.0, bubble_zc=1000.0, bubble_radius_x=1500.0,
+                bubble_radius_z=1000.0, u_background=5.0, shear_u=0.001,
+                pgf_perturbation=0, split_fast=0, weno_advective=0, acoustic_mode=0)
+    base.update(kw)
+    for k, v in base.items():
+        setattr(s, k, v)
+    return s
+
+
+REF_CASES = [dict(advection=a, weno_scalars=w, coriolis=c, ref_kind=r, moist=mo,
+                  divergence_damping=dd, divergence_order=do)
+             for (a, w, c, r, mo, dd, do) in [(2, 0, 0, 0, 0, 0.0, 2), (4, 0, 1, 1, 0, 100.0, 2),
+                                              (6, 0, 2, 0, 1, 0.0, 2), (5, 1, 0, 1, 0, 50.0, 4),
+                                              (5, 1, 1, 0, 1, 0.0, 2)]]
+
+
+@pytest.mark.skipif(not os.path.exists(os.path.join(os.path.dirname(GOLDEN), "..", "oracle", "_ref",
+                                                    "libvibe_ref.so")),
+                    reason="reference-linked oracle not built (reference tree absent)")
+@pytest.mark.parametrize("case", range(len(REF_CASES)))
+def test_port_is_bit_exact_to_reference(oc, case):
+    s = small(oc, **REF_CASES[case])
+    a, b = oc.Model(s, "port"), oc.Model(s, "ref")
+    for sp in range(12):
+        assert np.array_equal(a.get(sp), b.get(sp))
+    for r in range(5):
+        assert np.array_equal(a.reffield(r), b.reffield(r))
+    assert np.array_equal(a.sponge_profile(), b.sponge_profile())
+    for x, y in zip(a.slow_tendency(), b.slow_tendency()):
+        assert np.array_equal(x, y)
+    a.acoustic_substep(0.2)
+    b.acoustic_substep(0.2)
+    assert a.rk3_step(2.0, 3) == b.rk3_step(2.0, 3) == 0
+    for sp in range(12):
+        assert np.array_equal(a.get(sp), b.get(sp)), oc.SPECIES[sp]
+    t = small(oc, acoustic_mode=1)
+    a, b = oc.Model(t, "port"), oc.Model(t, "ref")
+    a.hevi_substep(0.7)
+    b.hevi_substep(0.7)
+    a.sponge(6.0)
+    b.sponge(6.0)
+    for sp in range(12):
+        assert np.array_equal(a.get(sp), b.get(sp))
+
+
+def _golden(name):
+    path = os.path.join(GOLDEN, name + ".npz")
+    if not os.path.exists(path):
+        pytest.skip("golden fixture %s missing" % name)
+    return np.load(path)
+
+
+def test_port_matches_golden_steps(oc):
+    """Fixtures written by tests/golden/make_golden.py from the reference
+    compiled unchanged (oracle/_ref): the port must reproduce them bit for
+    bit on this machine's libm (x86 and Arm glibc agree on these inputs)."""
+    g = _golden("ref_steps")
+    for case in range(int(g["ncases"])):
+        s = small(oc, **{k: g["case%d_%s" % (case, k)].item() for k in g["keys"]})
+        m = oc.Model(s, "port")
+        for n in range(int(g["case%d_nsteps" % case])):
+            assert m.rk3_step(float(g["dt"]), int(g["nsub"])) == 0
+        for sp in range(7):
+            got = oc.interior(s, sp, m.get(sp))
+            ref = g["case%d_sp%d" % (case, sp)]
+            assert np.allclose(got, ref, rtol=0, atol=1e-13 * max(np.abs(ref).max(), 1e-300)), (case, sp)
+
+
+def test_port_matches_golden_kernels(oc):
+    g = _golden("ref_kernels")
+    s = small(oc, acoustic_mode=1)
+    m = oc.Model(s, "port")
+    tend = m.slow_tendency()
+    for sp in range(7):
+        assert np.array_equal(oc.interior(s, sp, tend[sp]), g["tend_sp%d" % sp])
+    m.hevi_substep(0.7)
+    for sp in range(7):
+        assert np.array_equal(oc.interior(s, sp, m.get(sp)), g["hevi_sp%d" % sp])
+
+
+def test_reference_composition_diverges_and_documented_one_does_not(oc):
+    """The reference's own composition (total-Exner pressure gradient, fast
+    terms counted twice) blows up within a few steps on a warm bubble; the
+    documented composition (pi', fast terms once, advective WENO5) stays
+    bounded. 32x32x20 at 250 m keeps this a few seconds."""
+    base = dict(nx=32, ny=32, nz=20, dx=250.0, dy=250.0, z_top=5000.0, zeta_first=1.0, zeta_stretch=1.0,
+                bubble_xc=4000.0, bubble_yc=4000.0, bubble_zc=1500.0, qv_surface=0.0, u_background=0.0,
+                shear_u=0.0, advection=5, weno_scalars=1)
+    bad = oc.Model(small(oc, **base), "port")
+    rcs = [bad.rk3_step(2.0, 6) for _ in range(12)]
+    assert 1 in rcs
+    good_s = small(oc, **base, pgf_perturbation=1, split_fast=1, weno_advective=1)
+    good = oc.Model(good_s, "port")
+    for _ in range(12):
+        assert good.rk3_step(2.0, 6) == 0
+    w = oc.interior(good_s, 2, good.get(2))
+    assert np.abs(w).max() < 5.0
+
+
+# ---- C-ABI known answers on the oracle (test_common.cpp:163-266) -------------
+def test_oracle_c_abi_known_answers(oc):
+    L = oc.port_lib()
+    n = 24
+    a, c, b, d = np.ones(n - 1), np.ones(n - 1), np.full(n, -4.0), np.ones(n)
+    x, ws = np.zeros(n), np.zeros(n)
+    assert L.vo_tridiagonal_solve(a.ctypes.data, b.ctypes.data, c.ctypes.data, d.ctypes.data, n, x.ctypes.data,
+                                  ws.ctypes.data) == 0
+    lhs = -4.0 * x
+    lhs[1:] += x[:-1]
+    lhs[:-1] += x[1:]
+    assert np.abs(lhs - 1).max() <= 1e-10
+    z = np.zeros(2)
+    o = np.ones(2)
+    assert L.vo_tridiagonal_solve(None, z.ctypes.data, None, o.ctypes.data, 2, x.ctypes.data, ws.ctypes.data) == 1
+    assert L.vo_tridiagonal_solve(None, None, None, None, 2, x.ctypes.data, ws.ctypes.data) == 2
+    ql, qr = ctypes.c_double(), ctypes.c_double()
+    L.vo_weno5_reconstruct(3.5, 3.5, 3.5, 3.5, 3.5, ctypes.byref(ql), ctypes.byref(qr))
+    assert abs(ql.value - 3.5) <= 1e-12 and abs(qr.value - 3.5) <= 1e-12
+    xs = np.ones(10000)
+    xs[0], xs[-1] = 1e16, -1e16
+    assert abs(L.vo_neumaier_sum(xs.ctypes.data, xs.size) - 9998.0) <= 1e-6
+
+
+@pytest.mark.skipif(not os.path.exists(os.path.join(os.path.dirname(GOLDEN), "..", "oracle", "_ref",
+                                                    "libvibe_ref.so")),
+                    reason="reference-linked oracle not built (reference tree absent)")
+def test_reference_c_thomas_is_wrong_port_is_right(oc):
+    """The shipped vibe_tridiagonal_solve_f64 (c_kernels.c:18-60) misses its
+    own contract; the oracle follows the contract."""
+    ref = ctypes.CDLL(oc.REF_SO)
+    ref.vibe_tridiagonal_solve_f64.restype = ctypes.c_int
+    ref.vibe_tridiagonal_solve_f64.argtypes = [ctypes.c_void_p] * 4 + [ctypes.c_int] + [ctypes.c_void_p] * 2
+    n = 24
+    a, c, b, d = np.ones(n - 1), np.ones(n - 1), np.full(n, -4.0), np.ones(n)
+    x, ws = np.zeros(n), np.zeros(n)
+    ref.vibe_tridiagonal_solve_f64(a.ctypes.data, b.ctypes.data, c.ctypes.data, d.ctypes.data, n, x.ctypes.data,
+                                   ws.ctypes.data)
+    lhs = -4.0 * x
+    lhs[1:] += x[:-1]
+    lhs[:-1] += x[1:]
+    assert np.abs(lhs - 1).max() > 1e-2

@@ -1,0 +1,852 @@
+// vibe-model_gb300/csrc/model.cu
+//
+// Host side of the GB300 dynamics step: case set-up (grid metrics,
+// reference state, initial state -- computed once on the host with the
+// reference's formulas), device buffers, the per-step kernel schedule for
+// both precisions, and the C ABI declared in include/vibe_gb300.h.
+// Nothing here computes the step on the CPU: every state update is a kernel.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "step_kernels.cuh"
+#include "vibe_gb300.h"
+
+using namespace vgb;
+
+namespace {
+thread_local std::string g_err;
+int fail(int code, const std::string& msg) {
+  g_err = msg;
+  return code;
+}
+#define CUDA_OK(call)                                                                          \
+  do {                                                                                         \
+    cudaError_t e_ = (call);                                                                   \
+    if (e_ != cudaSuccess) return fail(VIBE_GB300_EDEVICE, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
+constexpr int H = 4;  // halo width of the reference's FieldT (driver.cpp:157-159)
+
+struct HostSetup {
+  std::vector<double> zeta, zs, sponge;
+  std::vector<double> ref[5];  // FieldT storage of theta0, pi0, rho0, p0, qv0
+  std::vector<double> st[NSPECIES];
+};
+}  // namespace
+
+struct vibe_gb300_model {
+  vibe_gb300_setup su{};
+  int precision = 0;
+  Dims d{};
+  Metric met{};
+  Flags fl{};
+  Tab tab{};
+  cudaStream_t stream = nullptr;
+  HostSetup hs;
+  int nsx[NSPECIES], nsy[NSPECIES], nsz[NSPECIES];
+  bool uniform = true;
+  // device memory (one allocation per buffer)
+  std::vector<void*> allocs;
+  double* S[2][NSPECIES] = {};
+  int cur = 0;
+  double* tend[NSPECIES] = {};
+  double* tmp[NSPECIES] = {};
+  double* scratch = nullptr;
+  double *d_dzeta = nullptr, *d_scale = nullptr, *d_sponge = nullptr;
+  double *d_th0 = nullptr, *d_pi0 = nullptr, *d_rho0 = nullptr;
+  double* d_stage_in = nullptr;   // staging for FieldT <-> device layout
+  double* d_tri = nullptr;        // reference HEVI coefficients (3*nz)
+  float* W0[NSPECIES] = {};
+  float* WSt[2][NSPECIES] = {};
+  float* WA[NSPECIES] = {};
+  float* WB[NSPECIES] = {};
+  float* d_ftab = nullptr;        // FP32 tables
+  double* d_dtab = nullptr;       // FP64 tables
+  float* d_lu = nullptr;          // 3 stages x 3*nz
+  double* d_spid = nullptr;       // identity sponge tables (nz+1 weights, nz+1 zeros)
+  float* d_spif = nullptr;
+  unsigned* d_err = nullptr;
+  unsigned* h_err = nullptr;      // pinned
+  double* h_pin = nullptr;        // pinned staging
+  size_t pin_n = 0;
+  double cfg_dt = -1.0;
+  int cfg_nsub = -1;
+  int kmin = 0;
+  std::vector<float> ftab_host;
+  std::vector<double> dtab_host;
+};
+
+namespace {
+
+size_t storage_count(const vibe_gb300_model* m, int q) {
+  return (size_t)m->nsx[q] * m->nsy[q] * m->nsz[q];
+}
+__host__ __device__ inline size_t soff(int nsx, int nsy, int i, int j, int k) {
+  return ((size_t)(k + H) * nsy + (size_t)(j + H)) * nsx + (size_t)(i + H);
+}
+
+// ---- host set-up, same formulas as the reference --------------------------
+
+// make_stretched_zeta, src/grid/geometry.cpp:39-60
+void make_zeta(int nz, double first, double stretch, std::vector<double>& zeta) {
+  std::vector<double> dz(nz);
+  double total = 0.0, h = first, acc = 0.0;
+  for (int k = 0; k < nz; ++k) { dz[k] = h; total += h; h *= stretch; }
+  zeta.assign(nz + 1, 0.0);
+  for (int k = 0; k < nz; ++k) { acc += dz[k]; zeta[k + 1] = acc / total; }
+  zeta[nz] = 1.0;
+}
+
+struct Geo {
+  const vibe_gb300_setup* s;
+  const std::vector<double>* zeta;
+  const std::vector<double>* zs;
+  double terrain(int i, int j) const {  // geometry.cpp:247-253
+    return (*zs)[(size_t)iclamp(j, 0, s->ny - 1) * s->nx + iclamp(i, 0, s->nx - 1)];
+  }
+  double zeta_at(double kk) const {  // geometry.cpp:20-31
+    const int nz = s->nz;
+    if (kk <= 0.0) return (*zeta)[0];
+    if (kk >= (double)nz) return (*zeta)[nz];
+    const int k0 = (int)std::floor(kk);
+    const double frac = kk - (double)k0;
+    if (frac == 0.0) return (*zeta)[k0];
+    if (std::fabs(frac - 0.5) < 1e-12) return 0.5 * ((*zeta)[k0] + (*zeta)[k0 + 1]);
+    return (*zeta)[k0] + frac * ((*zeta)[k0 + 1] - (*zeta)[k0]);
+  }
+  double height(int i, int j, double kk) const {  // geometry.cpp:260-263
+    const double z0 = terrain(i, j);
+    return z0 + zeta_at(kk) * (s->z_top - z0);
+  }
+  double zc(int i, int j, int k) const { return height(i, j, (double)k + 0.5); }
+};
+
+double density_from(double pi0, double th0) { return kP0 * std::pow(pi0, kCv / kRd) / (kRd * th0); }  // reference_state.cpp:26-28
+double pressure_from(double pi0) { return kP0 * std::pow(pi0, kCp / kRd); }                            // :31
+
+void host_setup(vibe_gb300_model* m) {
+  const vibe_gb300_setup& s = m->su;
+  const int nx = s.nx, ny = s.ny, nz = s.nz;
+  HostSetup& hs = m->hs;
+  make_zeta(nz, s.zeta_first, s.zeta_stretch, hs.zeta);
+  hs.zs.assign((size_t)nx * ny, 0.0);
+  if (s.terrain_kind == 1)
+    for (int j = 0; j < ny; ++j)
+      for (int i = 0; i < nx; ++i) {
+        const double x = ((double)i + 0.5) * s.dx - s.hill_xc;
+        const double y = ((double)j + 0.5) * s.dy - s.hill_yc;
+        hs.zs[(size_t)j * nx + i] = s.hill_h * std::exp(-(x * x + y * y) / (s.hill_a * s.hill_a));
+      }
+  Geo g{&s, &hs.zeta, &hs.zs};
+  const int cx = m->nsx[RHO], cy = m->nsy[RHO];
+  for (auto& r : hs.ref) r.assign(storage_count(m, RHO), 0.0);
+  auto R = [&](int w, int i, int j, int k) -> double& { return hs.ref[w][soff(cx, cy, i, j, k)]; };
+  const double pi_surf = std::pow(s.p_surf / kP0, kRd / kCp);
+  if (s.ref_kind == 1) {  // ReferenceState::from_profile, reference_state.cpp:61-110
+    const int np = (int)std::ceil(s.z_top / s.profile_dz) + 2;
+    std::vector<double> z(np), th(np), zi(nz + 1);
+    for (int p = 0; p < np; ++p) {
+      z[p] = (double)p * s.profile_dz;
+      th[p] = s.theta0 * std::exp(s.bv_n * s.bv_n * z[p] / kG);
+    }
+    auto theta_at = [&](double zz) {
+      if (zz <= z.front()) return th.front();
+      if (zz >= z.back()) return th.back();
+      size_t k = 0;
+      while (k + 2 < z.size() && z[k + 1] < zz) ++k;
+      const double w = (z[k + 1] - z[k] > 0.0) ? (zz - z[k]) / (z[k + 1] - z[k]) : 0.0;
+      return th[k] + w * (th[k + 1] - th[k]);
+    };
+    for (int j = 0; j < ny; ++j)
+      for (int i = 0; i < nx; ++i) {
+        for (int k = 0; k <= nz; ++k) zi[k] = g.height(i, j, (double)k);
+        double pi = pi_surf;
+        R(0, i, j, 0) = theta_at(zi[0]);
+        for (int k = 0; k < nz; ++k) {
+          const double th_lo = theta_at(zi[k]), th_hi = theta_at(zi[k + 1]);
+          const double th_mid = 0.5 * (th_lo + th_hi);
+          const double dz = zi[k + 1] - zi[k];
+          pi -= kG * dz / (kCp * th_mid);
+          const double th_c = 0.5 * (th_lo + th_hi);
+          R(0, i, j, k) = th_c;
+          R(1, i, j, k) = pi;
+          R(3, i, j, k) = pressure_from(pi);
+          R(2, i, j, k) = density_from(pi, th_c);
+          R(4, i, j, k) = 0.0;
+        }
+      }
+  } else {  // ReferenceState::isothermal, reference_state.cpp:35-59
+    for (int k = 0; k < nz; ++k)
+      for (int j = 0; j < ny; ++j)
+        for (int i = 0; i < nx; ++i) {
+          const double z = g.zc(i, j, k);
+          const double pi = pi_surf - kG * z / (kCp * s.theta0);
+          R(0, i, j, k) = s.theta0;
+          R(1, i, j, k) = pi;
+          R(3, i, j, k) = pressure_from(pi);
+          R(2, i, j, k) = density_from(pi, s.theta0);
+          R(4, i, j, k) = 0.0;
+        }
+  }
+  // Damping constructor sponge profile, damping.cpp:24-41
+  hs.sponge.assign(nz, 0.0);
+  {
+    const double zs0 = s.sponge_start_fraction * s.z_top;
+    for (int k = 0; k < nz; ++k) {
+      const double z = g.zc(0, 0, k);
+      if (z <= zs0) continue;
+      const double t = (z - zs0) / dmax(s.z_top - zs0, 1.0);
+      const double sn = std::sin(0.5 * kPi * (t < 0.0 ? 0.0 : (t > 1.0 ? 1.0 : t)));
+      hs.sponge[k] = s.sponge_alpha * sn * sn;
+    }
+  }
+  // init_warm_bubble, initial_conditions.cpp:136-159 (fill_base_state :66-91,
+  // apply_shear :94-102, enforce_state_equation :110-121)
+  for (int q = 0; q < NSPECIES; ++q) hs.st[q].assign(storage_count(m, q), 0.0);
+  auto S = [&](int q, int i, int j, int k) -> double& { return hs.st[q][soff(m->nsx[q], m->nsy[q], i, j, k)]; };
+  for (int k = 0; k < nz; ++k)
+    for (int j = 0; j < ny; ++j)
+      for (int i = 0; i < nx; ++i) {
+        const double z = g.zc(i, j, k);
+        S(THETA, i, j, k) = R(0, i, j, k);
+        S(PI, i, j, k) = R(1, i, j, k);
+        S(RHO, i, j, k) = R(2, i, j, k);
+        S(QV, i, j, k) = s.qv_surface * std::exp(-dmax(z, 0.0) / s.qv_decay_height);
+      }
+  const double xc = (s.bubble_xc != 0.0) ? s.bubble_xc : 0.5 * 0.0 + 0.5 * (double)nx * s.dx;
+  const double yc = (s.bubble_yc != 0.0) ? s.bubble_yc : 0.5 * (double)ny * s.dy;
+  for (int k = 0; k < nz; ++k)
+    for (int j = 0; j < ny; ++j)
+      for (int i = 0; i < nx; ++i) {
+        const double x = (0 + (double)i + 0.5) * s.dx, y = (0 + (double)j + 0.5) * s.dy;
+        const double z = g.zc(i, j, k);
+        const double ax = (x - xc) / s.bubble_radius_x, ay = (y - yc) / s.bubble_radius_x,
+                     az = (z - s.bubble_zc) / s.bubble_radius_z;
+        const double r2 = ax * ax + ay * ay + az * az;
+        if (r2 < 1.0) {
+          const double c = std::cos(0.5 * kPi * std::sqrt(r2));
+          S(THETA, i, j, k) += s.bubble_amplitude * c * c;
+        }
+      }
+  for (int k = 0; k < nz; ++k)
+    for (int j = 0; j < ny; ++j)
+      for (int i = 0; i <= nx; ++i) S(U, i, j, k) = s.u_background + s.shear_u * g.zc(imin(i, nx - 1), j, k);
+  for (int k = 0; k < nz; ++k)
+    for (int j = 0; j < ny; ++j)
+      for (int i = 0; i < nx; ++i) {
+        const double qv = dmax(S(QV, i, j, k), 0.0);
+        const double gamma_f = (1.0 + qv / kEpsVap) / (1.0 + qv);
+        const double val = S(RHO, i, j, k) * kRd * S(THETA, i, j, k) * gamma_f / kP0;
+        if (val > 0.0) S(PI, i, j, k) = std::pow(val, kRd / kCv);
+      }
+}
+
+// ---- device buffers -------------------------------------------------------
+template <class T>
+int dalloc(vibe_gb300_model* m, T** p, size_t n) {
+  void* v = nullptr;
+  CUDA_OK(cudaMalloc(&v, n * sizeof(T) + 256));
+  CUDA_OK(cudaMemsetAsync(v, 0, n * sizeof(T) + 256, m->stream));
+  m->allocs.push_back(v);
+  *p = (T*)v;
+  return 0;
+}
+
+// FieldT storage <-> device layout
+__global__ void k_pack(Dims d, int nsx, int nsy, int ni, int nj, int nk, const double* __restrict__ src,
+                       double* __restrict__ dst) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y, k = blockIdx.z;
+  if (i >= ni || j >= nj || k >= nk) return;
+  dst[d.idx(i, j, k)] = src[soff(nsx, nsy, i, j, k)];
+}
+__global__ void k_unpack(Dims d, int nsx, int nsy, int nsz, int ni, int nj, int nk, const double* __restrict__ src,
+                         double* __restrict__ dst) {
+  const size_t n = (size_t)nsx * nsy * nsz;
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x) {
+    const int ii = (int)(e % nsx) - H;
+    const int jj = (int)((e / nsx) % nsy) - H;
+    const int kk = (int)(e / ((size_t)nsx * nsy)) - H;
+    double v = 0.0;
+    if (ii >= 0 && ii < ni && jj >= 0 && jj < nj && kk >= 0 && kk < nk) v = src[d.idx(ii, jj, kk)];
+    dst[e] = v;
+  }
+}
+
+void box_of(const vibe_gb300_model* m, int q, int& ni, int& nj, int& nk) {
+  ni = m->d.nx + 1;
+  nj = m->d.ny + 1;
+  nk = m->d.nz + (q == W);
+}
+
+int upload_storage(vibe_gb300_model* m, int q, const double* host, double* const* dsts, int ndst) {
+  const size_t n = storage_count(m, q);
+  CUDA_OK(cudaMemcpyAsync(m->d_stage_in, host, n * sizeof(double), cudaMemcpyHostToDevice, m->stream));
+  int ni, nj, nk;
+  box_of(m, q, ni, nj, nk);
+  const dim3 b(32, 4);
+  for (int t = 0; t < ndst; ++t)
+    k_pack<<<dim3((ni + 31) / 32, (nj + 3) / 4, nk), b, 0, m->stream>>>(m->d, m->nsx[q], m->nsy[q], ni, nj, nk,
+                                                                         m->d_stage_in, dsts[t]);
+  CUDA_OK(cudaGetLastError());
+  return 0;
+}
+
+// ---- FP32 tables of the mixed path / stage coefficients ---------------------
+int build_tables(vibe_gb300_model* m) {
+  const int nz = m->d.nz;
+  const auto& hs = m->hs;
+  const int cx = m->nsx[RHO], cy = m->nsy[RHO];
+  auto R = [&](int w, int k) { return hs.ref[w][soff(cx, cy, 0, 0, k)]; };
+  std::vector<double> r0(nz), t0(nz), p0(nz);
+  for (int k = 0; k < nz; ++k) { t0[k] = R(0, k); p0[k] = R(1, k); r0[k] = R(2, k); }
+  const double zt = m->su.z_top;
+  auto dzeta = [&](int k) { const int kk = iclamp(k, 0, nz - 1); return hs.zeta[kk + 1] - hs.zeta[kk]; };
+  std::vector<float>& f = m->ftab_host;
+  f.assign((size_t)20 * (nz + 1) + 6 * (size_t)nz + 64, 0.f);
+  size_t o = 0;
+  auto put = [&](const float** dst, size_t n) { size_t at = o; o += n; return at; };
+  size_t o_r0c = put(nullptr, nz), o_rfz = put(nullptr, nz + 1), o_t0c = put(nullptr, nz), o_tfz = put(nullptr, nz + 1);
+  size_t o_kap = put(nullptr, nz), o_idzc = put(nullptr, nz), o_idzw = put(nullptr, nz + 1), o_idza = put(nullptr, nz);
+  size_t o_thi = put(nullptr, nz), o_t0d = put(nullptr, 6 * (size_t)nz), o_spw = put(nullptr, nz + 1);
+  for (int k = 0; k < nz; ++k) {
+    f[o_r0c + k] = (float)r0[k];
+    f[o_t0c + k] = (float)t0[k];
+    f[o_kap + k] = (float)((kRd / kCv) * (p0[k] / dmax(r0[k], 1e-8)));
+    f[o_idzc + k] = (float)(1.0 / dmax(dzeta(k) * zt, 1.0));
+    f[o_idza + k] = (float)(1.0 / (dzeta(k) * zt));
+    f[o_thi + k] = (float)(1.0 / dmax(t0[k], 1.0));
+    for (int mm = -3; mm <= 2; ++mm) f[o_t0d + 6 * (size_t)k + (mm + 3)] = (float)(t0[iclamp(k + mm, 0, nz - 1)] - t0[k]);
+  }
+  for (int k = 0; k <= nz; ++k) {
+    const int kc = imin(k, nz - 1), km = imax(k - 1, 0);
+    f[o_rfz + k] = (float)(0.5 * (r0[km] + r0[kc]));
+    f[o_tfz + k] = (float)(0.5 * (t0[km] + t0[kc]));
+    f[o_idzw + k] = (float)(1.0 / dmax(dzeta(kc) * zt, 1.0));
+    f[o_spw + k] = 1.f;
+  }
+  const size_t nft = o;
+  if (dalloc(m, &m->d_ftab, nft)) return VIBE_GB300_EDEVICE;
+  CUDA_OK(cudaMemcpy(m->d_ftab, f.data(), nft * sizeof(float), cudaMemcpyHostToDevice));
+  Tab& t = m->tab;
+  t.r0c = m->d_ftab + o_r0c; t.rfz = m->d_ftab + o_rfz; t.t0c = m->d_ftab + o_t0c; t.tfz = m->d_ftab + o_tfz;
+  t.kap = m->d_ftab + o_kap; t.idzc = m->d_ftab + o_idzc; t.idzw = m->d_ftab + o_idzw; t.idza = m->d_ftab + o_idza;
+  t.th0inv = m->d_ftab + o_thi; t.t0d = m->d_ftab + o_t0d; t.spw = m->d_ftab + o_spw;
+  // FP64: spwd(nz+1), spdt(nz+1), r0, t0, p0 (nz each)
+  std::vector<double>& dt = m->dtab_host;
+  dt.assign(2 * (size_t)(nz + 1) + 3 * (size_t)nz, 0.0);
+  for (int k = 0; k <= nz; ++k) dt[k] = 1.0;
+  for (int k = 0; k < nz; ++k) {
+    dt[2 * (nz + 1) + k] = r0[k];
+    dt[2 * (nz + 1) + nz + k] = t0[k];
+    dt[2 * (nz + 1) + 2 * nz + k] = p0[k];
+  }
+  if (dalloc(m, &m->d_dtab, dt.size())) return VIBE_GB300_EDEVICE;
+  CUDA_OK(cudaMemcpy(m->d_dtab, dt.data(), dt.size() * sizeof(double), cudaMemcpyHostToDevice));
+  t.spwd = m->d_dtab;
+  t.spdt = m->d_dtab + (nz + 1);
+  t.r0d = m->d_dtab + 2 * (nz + 1);
+  t.t0dd = t.r0d + nz;
+  t.p0d = t.r0d + 2 * nz;
+  t.dx_inv = (float)(1.0 / m->su.dx);
+  t.dy_inv = (float)(1.0 / m->su.dy);
+  t.f0 = (float)m->met.f0;
+  t.beta = (float)m->met.beta;
+  t.dy = (float)m->su.dy;
+  // identity sponge tables for single substep folds
+  std::vector<double> idt(2 * (size_t)(nz + 1), 0.0);
+  for (int k = 0; k <= nz; ++k) idt[k] = 1.0;
+  if (dalloc(m, &m->d_spid, idt.size())) return VIBE_GB300_EDEVICE;
+  CUDA_OK(cudaMemcpy(m->d_spid, idt.data(), idt.size() * sizeof(double), cudaMemcpyHostToDevice));
+  std::vector<float> idf(nz + 1, 1.f);
+  if (dalloc(m, &m->d_spif, idf.size())) return VIBE_GB300_EDEVICE;
+  CUDA_OK(cudaMemcpy(m->d_spif, idf.data(), idf.size() * sizeof(float), cudaMemcpyHostToDevice));
+  return 0;
+}
+
+// dt/n_sub dependent coefficients: sponge weights (damping.cpp:94,98), the
+// LU factors of the consistent HEVI matrix for the three stage substep
+// lengths, and the reference HEVI coefficients are built per call.
+int configure_dt(vibe_gb300_model* m, double dt, int n_sub) {
+  if (dt == m->cfg_dt && n_sub == m->cfg_nsub) return 0;
+  const int nz = m->d.nz;
+  const auto& sp = m->hs.sponge;
+  std::vector<double>& d = m->dtab_host;
+  std::vector<float>& f = m->ftab_host;
+  const size_t o_spw = (size_t)nz + (nz + 1) + nz + (nz + 1) + nz + nz + (nz + 1) + nz + nz + 6 * (size_t)nz;
+  for (int k = 0; k <= nz; ++k) {
+    const double a = sp[imin(k, nz - 1)];
+    const double w = (a > 0.0) ? 1.0 / (1.0 + dt * a) : 1.0;
+    d[k] = w;
+    d[nz + 1 + k] = (a > 0.0) ? dt * a : 0.0;
+    f[o_spw + k] = (float)w;
+  }
+  CUDA_OK(cudaMemcpyAsync(m->d_dtab, d.data(), 2 * (size_t)(nz + 1) * sizeof(double), cudaMemcpyHostToDevice, m->stream));
+  CUDA_OK(cudaMemcpyAsync(m->d_ftab + o_spw, f.data() + o_spw, (nz + 1) * sizeof(float), cudaMemcpyHostToDevice, m->stream));
+  m->kmin = nz + 1;
+  for (int k = 0; k < nz; ++k)
+    if (sp[k] > 0.0) { m->kmin = k; break; }
+  if (m->precision == VIBE_GB300_MIXED) {
+    // consistent HEVI matrix (uniform column): a_k = -c_k T_k,
+    // c_k = -c_k T_{k+1}, b_k = 1 + c_k (T_k + T_{k+1}) with
+    // c_k = (dtau*beta)^2 kappa_k / dz_k, T_f = rho0_f cp theta0_f / dzf_f
+    const auto& hs = m->hs;
+    const int cx = m->nsx[RHO], cy = m->nsy[RHO];
+    auto R = [&](int w, int k) { return hs.ref[w][soff(cx, cy, 0, 0, k)]; };
+    auto dzeta = [&](int k) { const int kk = iclamp(k, 0, nz - 1); return hs.zeta[kk + 1] - hs.zeta[kk]; };
+    const double zt = m->su.z_top, b = m->su.hevi_beta;
+    std::vector<double> T(nz + 1, 0.0);
+    for (int k = 1; k < nz; ++k) {
+      const double rf = 0.5 * (R(2, k - 1) + R(2, k)), tf = 0.5 * (R(0, k - 1) + R(0, k));
+      T[k] = rf * kCp * tf / dmax(dzeta(k) * zt, 1.0);
+    }
+    std::vector<float> lu(9 * (size_t)nz, 0.f);
+    const double dts[3] = {dt / 3.0, dt / 2.0, dt};
+    for (int s = 0; s < 3; ++s) {
+      const double dtau = dts[s] / (double)(n_sub > 1 ? n_sub : 1);
+      double cprev = 0.0;
+      for (int k = 0; k < nz; ++k) {
+        const double kap = (kRd / kCv) * (R(1, k) / dmax(R(2, k), 1e-8));
+        const double ck = (dtau * b) * (dtau * b) * kap / dmax(dzeta(k) * zt, 1.0);
+        const double a = -ck * T[k], c = -ck * T[k + 1], bb = 1.0 + ck * (T[k] + T[k + 1]);
+        const double den = (k == 0) ? bb : bb - a * cprev;
+        cprev = (k < nz - 1) ? c / den : 0.0;
+        lu[s * 3 * (size_t)nz + k] = (float)a;
+        lu[s * 3 * (size_t)nz + nz + k] = (float)cprev;
+        lu[s * 3 * (size_t)nz + 2 * nz + k] = (float)(1.0 / den);
+      }
+    }
+    CUDA_OK(cudaMemcpyAsync(m->d_lu, lu.data(), lu.size() * sizeof(float), cudaMemcpyHostToDevice, m->stream));
+    CUDA_OK(cudaStreamSynchronize(m->stream));
+  }
+  m->cfg_dt = dt;
+  m->cfg_nsub = n_sub;
+  return 0;
+}
+
+// reference HEVI coefficients from column (0,0), acoustic_substep.cpp:38-65
+int ref_hevi_coefficients(vibe_gb300_model* m, double dtau) {
+  const int nz = m->d.nz;
+  const auto& hs = m->hs;
+  const int cx = m->nsx[RHO], cy = m->nsy[RHO];
+  auto R = [&](int w, int k) { return hs.ref[w][soff(cx, cy, 0, 0, k)]; };
+  std::vector<double> tri(3 * (size_t)nz, 0.0);
+  double* ta = tri.data();
+  double* tb = ta + nz;
+  double* tc = tb + nz;
+  const double half = 0.5 * dtau;
+  for (int k = 0; k < nz; ++k) {
+    const double scale = m->su.z_top - hs.zs[0];
+    const double dz = dmax((hs.zeta[k + 1] - hs.zeta[k]) * scale, 1.0);
+    const double rho0 = R(2, k), th0 = R(0, k);
+    const double cs2 = (kCp / kCv) * kRd * R(0, k) * R(1, k);
+    const double a_k = half * half * kCp * th0 * rho0 / (dz * dz);
+    const double a_kp1 = (k < nz - 1) ? half * half * kCp * R(0, k + 1) * R(2, k + 1) / (dz * dz) : a_k;
+    const double b0 = 1.0 / dmax(rho0 * cs2, 1e-12);
+    tb[k] = b0 + a_k + a_kp1;
+    if (k < nz - 1) tc[k] = -a_kp1;
+    if (k > 0) ta[k - 1] = -a_k;
+  }
+  CUDA_OK(cudaMemcpyAsync(m->d_tri, tri.data(), tri.size() * sizeof(double), cudaMemcpyHostToDevice, m->stream));
+  CUDA_OK(cudaStreamSynchronize(m->stream));
+  return 0;
+}
+
+WS ws_of(float* const* a) {
+  WS w;
+  for (int q = 0; q < NSPECIES; ++q) w.f[q] = a[q];
+  return w;
+}
+// fields u..pi from `sub`, the rest from `stage`
+WS ws_compose(float* const* sub, float* const* stage) {
+  WS w;
+  for (int q = 0; q < NSPECIES; ++q) w.f[q] = (q <= PI) ? sub[q] : stage[q];
+  return w;
+}
+
+int enqueue_steps(vibe_gb300_model* m, double dt, int n_sub_in, int n_steps) {
+  const int n_sub = n_sub_in > 1 ? n_sub_in : 1;
+  if (int rc = configure_dt(m, dt, n_sub)) return rc;
+  const double dts[3] = {dt / 3.0, dt / 2.0, dt};
+  const Dims& d = m->d;
+  for (int step = 0; step < n_steps; ++step) {
+    double** S0 = m->S[m->cur];
+    double** S1 = m->S[1 - m->cur];
+    if (m->precision == VIBE_GB300_FP64) {
+      for (int stage = 0; stage < 3; ++stage) {
+        double** src = (stage == 0) ? S0 : S1;
+        fp64_slow_tendency(d, m->met, m->fl, src, m->tend, m->scratch, m->stream);
+        fp64_stage_update(d, S0, m->tend, dts[stage], S1, m->stream);
+        const double dtau = dts[stage] / (double)n_sub;
+        if (m->fl.acoustic_mode == 1)
+          if (int rc = ref_hevi_coefficients(m, dtau)) return rc;
+        for (int n = 0; n < n_sub; ++n) {
+          if (m->fl.acoustic_mode == 0) fp64_fb_substep(d, m->met, m->fl, S1, dtau, m->stream);
+          else if (m->fl.acoustic_mode == 1)
+            fp64_ref_hevi_substep(d, m->met, S1, dtau, m->d_tri, m->d_tri + d.nz, m->d_tri + 2 * d.nz, m->scratch,
+                                  m->d_err, m->stream);
+          else fp64_cons_hevi_substep(d, m->met, m->fl, S1, m->tmp, m->scratch, dtau, m->d_err, m->stream);
+        }
+        fp64_nonfinite(d, S1, m->d_err, m->stream);
+      }
+      fp64_sponge(d, m->met, S1, m->kmin, dt, m->stream);
+    } else {
+      const WS w0 = ws_of(m->W0);
+      float** final_sub = nullptr;
+      for (int stage = 0; stage < 3; ++stage) {
+        float** st_out = m->WSt[stage & 1];
+        const WS win = (stage == 0) ? w0 : ws_compose(final_sub, m->WSt[(stage - 1) & 1]);
+        mixed_stage(d, m->tab, m->fl, win, w0, ws_of(st_out), S0, S1, dts[stage], stage == 2, m->d_err, m->stream);
+        const float dtau = (float)(dts[stage] / (double)n_sub);
+        float** in = st_out;
+        for (int n = 0; n < n_sub; ++n) {
+          float** out = (n & 1) ? m->WB : m->WA;
+          if (m->fl.acoustic_mode == 2)
+            mixed_hevi_substep(d, m->tab, m->fl, ws_of(in), ws_of(out), dtau, m->d_lu + (size_t)stage * 3 * d.nz,
+                               m->d_err, m->stream);
+          else mixed_fb_substep(d, m->tab, m->fl, ws_of(in), ws_of(out), dtau, m->stream);
+          in = out;
+        }
+        final_sub = in;
+      }
+      mixed_finish(d, m->tab, m->fl, ws_of(final_sub), ws_of(m->WSt[0]), w0, S1, dt, m->kmin, m->d_err, m->stream);
+    }
+    m->cur = 1 - m->cur;
+  }
+  CUDA_OK(cudaGetLastError());
+  return 0;
+}
+
+int read_status(vibe_gb300_model* m) {
+  CUDA_OK(cudaMemcpyAsync(m->h_err, m->d_err, sizeof(unsigned), cudaMemcpyDeviceToHost, m->stream));
+  CUDA_OK(cudaStreamSynchronize(m->stream));
+  const unsigned e = *m->h_err;
+  CUDA_OK(cudaMemsetAsync(m->d_err, 0, sizeof(unsigned), m->stream));
+  if (e & kErrSingular) return fail(VIBE_GB300_ESINGULAR, "tridiagonal pivot below 1e-300");
+  if (e & kErrNonFinite) return fail(VIBE_GB300_ENONFINITE, "non-finite value in the state");
+  return 0;
+}
+
+int sync_working(vibe_gb300_model* m) {
+  if (m->precision != VIBE_GB300_MIXED) return 0;
+  mixed_to_working(m->d, m->tab, m->S[m->cur], ws_of(m->W0), m->stream);
+  CUDA_OK(cudaGetLastError());
+  return 0;
+}
+
+}  // namespace
+
+// ===========================================================================
+// C ABI
+// ===========================================================================
+extern "C" {
+
+const char* vibe_gb300_last_error(void) { return g_err.c_str(); }
+
+void vibe_gb300_setup_defaults(vibe_gb300_setup* s) {
+  std::memset(s, 0, sizeof(*s));
+  s->nx = 64; s->ny = 64; s->nz = 40;
+  s->dx = 250.0; s->dy = 250.0; s->z_top = 10000.0;
+  s->zeta_first = 1.0; s->zeta_stretch = 1.0;
+  s->ref_kind = 0; s->theta0 = 300.0; s->p_surf = 100000.0; s->bv_n = 0.01; s->profile_dz = 250.0;
+  s->bubble_amplitude = 2.0; s->bubble_radius_x = 2000.0; s->bubble_radius_z = 2000.0;
+  s->bubble_xc = 8000.0; s->bubble_yc = 8000.0; s->bubble_zc = 2000.0;
+  s->qv_surface = 0.014; s->qv_decay_height = 3000.0;
+  s->advection = 5; s->weno_scalars = 1; s->moist = 0; s->coriolis = 0; s->latitude = 45.0;
+  s->sponge_alpha = 0.2; s->sponge_start_fraction = 0.8;
+  s->divergence_damping = 0.0; s->divergence_order = 2;
+  s->pgf_perturbation = 1; s->acoustic_mode = 0; s->hevi_beta = 0.5; s->split_fast = 1; s->weno_advective = 1;
+}
+
+int vibe_gb300_model_create(const vibe_gb300_setup* s, int precision, vibe_gb300_model** out) {
+  if (!s || !out) return fail(VIBE_GB300_EBADARG, "null argument");
+  *out = nullptr;
+  if (s->nx < 1 || s->ny < 1 || s->nz < 1 || !(s->dx > 0) || !(s->dy > 0) || !(s->z_top > 0))
+    return fail(VIBE_GB300_EBADARG, "grid sizes and spacings must be positive");
+  if (precision != VIBE_GB300_FP64 && precision != VIBE_GB300_MIXED)
+    return fail(VIBE_GB300_EBADARG, "precision must be VIBE_GB300_FP64 or VIBE_GB300_MIXED");
+  if (s->acoustic_mode < 0 || s->acoustic_mode > 2) return fail(VIBE_GB300_EBADARG, "acoustic_mode must be 0, 1 or 2");
+  auto* m = new vibe_gb300_model();
+  m->su = *s;
+  m->precision = precision;
+  auto bail = [&](int rc) { vibe_gb300_model_destroy(m); return rc; };
+  const int nx = s->nx, ny = s->ny, nz = s->nz;
+  for (int q = 0; q < NSPECIES; ++q) {
+    m->nsx[q] = nx + 2 * H + (q == U);
+    m->nsy[q] = ny + 2 * H + (q == V);
+    m->nsz[q] = nz + 2 * H + (q == W);
+  }
+  m->d.nx = nx; m->d.ny = ny; m->d.nz = nz;
+  m->d.P = ((nx + 1) + 7) / 8 * 8;
+  m->d.NY1 = ny + 1;
+  m->d.plane = (size_t)m->d.NY1 * m->d.P;
+  Flags& fl = m->fl;
+  fl.advection = s->advection; fl.weno_scalars = s->weno_scalars; fl.weno_advective = s->weno_advective;
+  fl.moist = s->moist; fl.coriolis = s->coriolis; fl.div_damp = s->divergence_damping;
+  fl.div_order = s->divergence_order; fl.pgf_pert = s->pgf_perturbation; fl.split_fast = s->split_fast;
+  fl.acoustic_mode = s->acoustic_mode; fl.hevi_beta = s->hevi_beta;
+  host_setup(m);
+  // horizontally uniform reference state on flat terrain?
+  {
+    const int cx = m->nsx[RHO], cy = m->nsy[RHO];
+    for (size_t e = 0; e < m->hs.zs.size() && m->uniform; ++e) m->uniform = (m->hs.zs[e] == 0.0);
+    for (int w = 0; w < 3 && m->uniform; ++w)
+      for (int k = 0; k < nz && m->uniform; ++k)
+        for (int j = 0; j < ny && m->uniform; ++j)
+          for (int i = 0; i < nx && m->uniform; ++i)
+            m->uniform = (m->hs.ref[w][soff(cx, cy, i, j, k)] == m->hs.ref[w][soff(cx, cy, 0, 0, k)]);
+  }
+  if (precision == VIBE_GB300_MIXED) {
+    if (!m->uniform) return bail(fail(VIBE_GB300_EUNSUPPORTED, "mixed path needs flat terrain and a horizontally uniform reference state"));
+    if (!s->pgf_perturbation || !s->split_fast)
+      return bail(fail(VIBE_GB300_EUNSUPPORTED, "mixed path needs pgf_perturbation=1 and split_fast=1"));
+    if (s->acoustic_mode == 1) return bail(fail(VIBE_GB300_EUNSUPPORTED, "mixed path supports acoustic_mode 0 and 2"));
+    if (s->divergence_damping > 0.0 && s->divergence_order > 2)
+      return bail(fail(VIBE_GB300_EUNSUPPORTED, "mixed path supports 2nd-order divergence damping only"));
+  }
+  m->met.f0 = 2.0 * kOmega * std::sin(s->latitude * (kPi / 180.0));
+  m->met.beta = 2.0 * kOmega * std::cos(s->latitude * (kPi / 180.0)) / kEarthRadius;
+  if (cudaStreamCreateWithFlags(&m->stream, cudaStreamNonBlocking) != cudaSuccess)
+    return bail(fail(VIBE_GB300_EDEVICE, "cudaStreamCreate failed (no CUDA device?)"));
+  const size_t nfield = m->d.plane * (size_t)(nz + 1);
+  size_t max_storage = 0;
+  for (int q = 0; q < NSPECIES; ++q) max_storage = std::max(max_storage, storage_count(m, q));
+  int rc = 0;
+  for (int b = 0; b < 2 && !rc; ++b)
+    for (int q = 0; q < NSPECIES && !rc; ++q) rc = dalloc(m, &m->S[b][q], nfield);
+  rc = rc ? rc : dalloc(m, &m->d_stage_in, max_storage);
+  rc = rc ? rc : dalloc(m, &m->d_dzeta, (size_t)nz);
+  rc = rc ? rc : dalloc(m, &m->d_scale, (size_t)nx * ny);
+  rc = rc ? rc : dalloc(m, &m->d_sponge, (size_t)nz);
+  rc = rc ? rc : dalloc(m, &m->d_th0, nfield);
+  rc = rc ? rc : dalloc(m, &m->d_pi0, nfield);
+  rc = rc ? rc : dalloc(m, &m->d_rho0, nfield);
+  rc = rc ? rc : dalloc(m, &m->d_err, (size_t)1);
+  rc = rc ? rc : dalloc(m, &m->d_tri, 3 * (size_t)nz);
+  if (!rc && precision == VIBE_GB300_FP64) {
+    for (int q = 0; q < NSPECIES && !rc; ++q) rc = dalloc(m, &m->tend[q], nfield);
+    for (int q = 0; q < NSPECIES && !rc; ++q) rc = (q == W || q == RHO || q == PI) ? dalloc(m, &m->tmp[q], nfield) : 0;
+    const size_t scr = std::max(m->d.plane * (size_t)nz + (size_t)nx * ny * 2 * nz, (size_t)nx * ny * (5 * (size_t)nz + 2));
+    rc = rc ? rc : dalloc(m, &m->scratch, std::max(scr, nfield));
+  }
+  if (!rc && precision == VIBE_GB300_MIXED) {
+    for (int q = 0; q < NSPECIES && !rc; ++q) rc = dalloc(m, &m->W0[q], nfield);
+    for (int b = 0; b < 2 && !rc; ++b)
+      for (int q = 0; q < NSPECIES && !rc; ++q) rc = dalloc(m, &m->WSt[b][q], nfield);
+    for (int q = 0; q <= PI && !rc; ++q) rc = dalloc(m, &m->WA[q], nfield);
+    for (int q = 0; q <= PI && !rc; ++q) rc = dalloc(m, &m->WB[q], nfield);
+    rc = rc ? rc : dalloc(m, &m->d_lu, 9 * (size_t)nz);
+  }
+  if (rc) return bail(rc);
+  if (cudaMallocHost(&m->h_err, sizeof(unsigned)) != cudaSuccess) return bail(fail(VIBE_GB300_EDEVICE, "cudaMallocHost failed"));
+  *m->h_err = 0;
+  // metrics
+  std::vector<double> dz(nz), sc((size_t)nx * ny);
+  for (int k = 0; k < nz; ++k) dz[k] = m->hs.zeta[k + 1] - m->hs.zeta[k];
+  for (size_t e = 0; e < sc.size(); ++e) sc[e] = s->z_top - m->hs.zs[e];
+  if (cudaMemcpy(m->d_dzeta, dz.data(), nz * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess ||
+      cudaMemcpy(m->d_scale, sc.data(), sc.size() * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess ||
+      cudaMemcpy(m->d_sponge, m->hs.sponge.data(), nz * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess)
+    return bail(fail(VIBE_GB300_EDEVICE, "metric upload failed"));
+  m->met.dx = s->dx; m->met.dy = s->dy; m->met.z_top = s->z_top;
+  m->met.dzeta = m->d_dzeta; m->met.scale = m->d_scale; m->met.sponge = m->d_sponge;
+  m->met.th0 = m->d_th0; m->met.pi0 = m->d_pi0; m->met.rho0 = m->d_rho0;
+  {
+    double* dst[1];
+    dst[0] = m->d_th0;
+    if ((rc = upload_storage(m, RHO, m->hs.ref[0].data(), dst, 1))) return bail(rc);
+    CUDA_OK(cudaStreamSynchronize(m->stream));
+    dst[0] = m->d_pi0;
+    if ((rc = upload_storage(m, RHO, m->hs.ref[1].data(), dst, 1))) return bail(rc);
+    CUDA_OK(cudaStreamSynchronize(m->stream));
+    dst[0] = m->d_rho0;
+    if ((rc = upload_storage(m, RHO, m->hs.ref[2].data(), dst, 1))) return bail(rc);
+    CUDA_OK(cudaStreamSynchronize(m->stream));
+  }
+  if (m->uniform)
+    if ((rc = build_tables(m))) return bail(rc);
+  for (int q = 0; q < NSPECIES; ++q)
+    if ((rc = vibe_gb300_set_field(m, q, m->hs.st[q].data()))) return bail(rc);
+  *out = m;
+  return 0;
+}
+
+void vibe_gb300_model_destroy(vibe_gb300_model* m) {
+  if (!m) return;
+  if (m->stream) cudaStreamSynchronize(m->stream);
+  for (void* p : m->allocs) cudaFree(p);
+  if (m->h_err) cudaFreeHost(m->h_err);
+  if (m->h_pin) cudaFreeHost(m->h_pin);
+  if (m->stream) cudaStreamDestroy(m->stream);
+  delete m;
+}
+
+size_t vibe_gb300_storage_size(const vibe_gb300_model* m, int species) {
+  if (!m || species < 0 || species >= NSPECIES) return 0;
+  return storage_count(m, species);
+}
+
+int vibe_gb300_set_field(vibe_gb300_model* m, int q, const double* host) {
+  if (!m || !host || q < 0 || q >= NSPECIES) return fail(VIBE_GB300_EBADARG, "bad argument");
+  double* dst[2] = {m->S[0][q], m->S[1][q]};
+  if (int rc = upload_storage(m, q, host, dst, 2)) return rc;
+  if (int rc = sync_working(m)) return rc;
+  CUDA_OK(cudaStreamSynchronize(m->stream));
+  if (m->precision == VIBE_GB300_MIXED) {
+    // every FP32 buffer starts from the same values (ghost line included)
+    const size_t n = m->d.plane * (size_t)(m->d.nz + 1) * sizeof(float);
+    for (int b = 0; b < 2; ++b) CUDA_OK(cudaMemcpyAsync(m->WSt[b][q], m->W0[q], n, cudaMemcpyDeviceToDevice, m->stream));
+    if (q <= PI) {
+      CUDA_OK(cudaMemcpyAsync(m->WA[q], m->W0[q], n, cudaMemcpyDeviceToDevice, m->stream));
+      CUDA_OK(cudaMemcpyAsync(m->WB[q], m->W0[q], n, cudaMemcpyDeviceToDevice, m->stream));
+    }
+    CUDA_OK(cudaStreamSynchronize(m->stream));
+  }
+  return 0;
+}
+
+int vibe_gb300_get_field(vibe_gb300_model* m, int q, double* host) {
+  if (!m || !host || q < 0 || q >= NSPECIES) return fail(VIBE_GB300_EBADARG, "bad argument");
+  const size_t n = storage_count(m, q);
+  int ni, nj, nk;
+  box_of(m, q, ni, nj, nk);
+  k_unpack<<<1024, 256, 0, m->stream>>>(m->d, m->nsx[q], m->nsy[q], m->nsz[q], ni, nj, nk, m->S[m->cur][q],
+                                        m->d_stage_in);
+  CUDA_OK(cudaGetLastError());
+  CUDA_OK(cudaMemcpyAsync(host, m->d_stage_in, n * sizeof(double), cudaMemcpyDeviceToHost, m->stream));
+  CUDA_OK(cudaStreamSynchronize(m->stream));
+  return 0;
+}
+
+int vibe_gb300_get_reffield(const vibe_gb300_model* m, int which, double* host) {
+  if (!m || !host || which < 0 || which > 4) return fail(VIBE_GB300_EBADARG, "bad argument");
+  std::memcpy(host, m->hs.ref[which].data(), m->hs.ref[which].size() * sizeof(double));
+  return 0;
+}
+int vibe_gb300_get_zeta(const vibe_gb300_model* m, double* host) {
+  if (!m || !host) return fail(VIBE_GB300_EBADARG, "bad argument");
+  std::memcpy(host, m->hs.zeta.data(), m->hs.zeta.size() * sizeof(double));
+  return 0;
+}
+int vibe_gb300_get_terrain(const vibe_gb300_model* m, double* host) {
+  if (!m || !host) return fail(VIBE_GB300_EBADARG, "bad argument");
+  std::memcpy(host, m->hs.zs.data(), m->hs.zs.size() * sizeof(double));
+  return 0;
+}
+int vibe_gb300_get_sponge(const vibe_gb300_model* m, double* host) {
+  if (!m || !host) return fail(VIBE_GB300_EBADARG, "bad argument");
+  std::memcpy(host, m->hs.sponge.data(), m->hs.sponge.size() * sizeof(double));
+  return 0;
+}
+
+int vibe_gb300_step_async(vibe_gb300_model* m, double dt, int n_sub, int n_steps) {
+  if (!m || n_steps < 0 || !(dt > 0)) return fail(VIBE_GB300_EBADARG, "bad argument");
+  return enqueue_steps(m, dt, n_sub, n_steps);
+}
+
+int vibe_gb300_sync(vibe_gb300_model* m) {
+  if (!m) return fail(VIBE_GB300_EBADARG, "bad argument");
+  return read_status(m);
+}
+
+int vibe_gb300_step(vibe_gb300_model* m, double dt, int n_sub, int n_steps) {
+  if (int rc = vibe_gb300_step_async(m, dt, n_sub, n_steps)) return rc;
+  return read_status(m);
+}
+
+int vibe_gb300_slow_tendency(vibe_gb300_model* m, double* const* host_out) {
+  if (!m || !host_out) return fail(VIBE_GB300_EBADARG, "bad argument");
+  if (m->precision != VIBE_GB300_FP64) return fail(VIBE_GB300_EUNSUPPORTED, "slow tendency output is FP64-path only");
+  fp64_slow_tendency(m->d, m->met, m->fl, m->S[m->cur], m->tend, m->scratch, m->stream);
+  for (int q = 0; q < NSPECIES; ++q) {
+    int ni, nj, nk;
+    box_of(m, q, ni, nj, nk);
+    if (q == U) nj = m->d.ny;
+    else if (q == V) ni = m->d.nx;
+    else if (q == W) { ni = m->d.nx; nj = m->d.ny; }
+    else { ni = m->d.nx; nj = m->d.ny; }
+    k_unpack<<<1024, 256, 0, m->stream>>>(m->d, m->nsx[q], m->nsy[q], m->nsz[q], ni, nj, nk, m->tend[q], m->d_stage_in);
+    CUDA_OK(cudaMemcpyAsync(host_out[q], m->d_stage_in, storage_count(m, q) * sizeof(double), cudaMemcpyDeviceToHost,
+                            m->stream));
+    CUDA_OK(cudaStreamSynchronize(m->stream));
+  }
+  CUDA_OK(cudaGetLastError());
+  return 0;
+}
+
+int vibe_gb300_acoustic_substep(vibe_gb300_model* m, double dtau) {
+  if (!m) return fail(VIBE_GB300_EBADARG, "bad argument");
+  if (m->precision == VIBE_GB300_FP64) {
+    fp64_fb_substep(m->d, m->met, m->fl, m->S[m->cur], dtau, m->stream);
+  } else {
+    if (int rc = sync_working(m)) return rc;
+    mixed_fb_substep(m->d, m->tab, m->fl, ws_of(m->W0), ws_of(m->WA), (float)dtau, m->stream);
+    Tab id = m->tab;
+    id.spwd = m->d_spid; id.spdt = m->d_spid + (m->d.nz + 1); id.spw = m->d_spif;
+    mixed_finish(m->d, id, m->fl, ws_compose(m->WA, m->W0), ws_of(m->W0), ws_of(m->WSt[1]), m->S[m->cur], 0.0, 0,
+                 m->d_err, m->stream);
+  }
+  CUDA_OK(cudaGetLastError());
+  return read_status(m);
+}
+
+int vibe_gb300_hevi_substep(vibe_gb300_model* m, double dtau) {
+  if (!m) return fail(VIBE_GB300_EBADARG, "bad argument");
+  if (m->fl.acoustic_mode == 0) return fail(VIBE_GB300_EBADARG, "acoustic_mode 0 has no HEVI substep");
+  if (m->precision == VIBE_GB300_FP64) {
+    if (m->fl.acoustic_mode == 1) {
+      if (int rc = ref_hevi_coefficients(m, dtau)) return rc;
+      fp64_ref_hevi_substep(m->d, m->met, m->S[m->cur], dtau, m->d_tri, m->d_tri + m->d.nz, m->d_tri + 2 * m->d.nz,
+                            m->scratch, m->d_err, m->stream);
+    } else {
+      fp64_cons_hevi_substep(m->d, m->met, m->fl, m->S[m->cur], m->tmp, m->scratch, dtau, m->d_err, m->stream);
+    }
+  } else {
+    // single substep: factors for this dtau in stage slot 0
+    const double dt_equiv = 3.0 * dtau;  // stage 0 uses dt/3 with n_sub = 1
+    m->cfg_dt = -1.0;
+    if (int rc = configure_dt(m, dt_equiv, 1)) return rc;
+    if (int rc = sync_working(m)) return rc;
+    mixed_hevi_substep(m->d, m->tab, m->fl, ws_of(m->W0), ws_of(m->WA), (float)dtau, m->d_lu, m->d_err, m->stream);
+    Tab id = m->tab;
+    id.spwd = m->d_spid; id.spdt = m->d_spid + (m->d.nz + 1); id.spw = m->d_spif;
+    mixed_finish(m->d, id, m->fl, ws_compose(m->WA, m->W0), ws_of(m->W0), ws_of(m->WSt[1]), m->S[m->cur], 0.0, 0,
+                 m->d_err, m->stream);
+    m->cfg_dt = -1.0;
+  }
+  CUDA_OK(cudaGetLastError());
+  return read_status(m);
+}
+
+int vibe_gb300_sponge(vibe_gb300_model* m, double dt) {
+  if (!m) return fail(VIBE_GB300_EBADARG, "bad argument");
+  int kmin = m->d.nz + 1;
+  for (int k = 0; k < m->d.nz; ++k)
+    if (m->hs.sponge[k] > 0.0) { kmin = k; break; }
+  fp64_sponge(m->d, m->met, m->S[m->cur], kmin, dt, m->stream);
+  if (int rc = sync_working(m)) return rc;
+  CUDA_OK(cudaGetLastError());
+  return read_status(m);
+}
+
+int vibe_gb300_device_field(vibe_gb300_model* m, int q, double** ptr, int* pitch) {
+  if (!m || !ptr || q < 0 || q >= NSPECIES) return fail(VIBE_GB300_EBADARG, "bad argument");
+  *ptr = m->S[m->cur][q];
+  if (pitch) *pitch = m->d.P;
+  return 0;
+}
+
+vibe_stream_t vibe_gb300_stream(vibe_gb300_model* m) { return m ? (vibe_stream_t)m->stream : nullptr; }
+
+int vibe_gb300_launches_per_step(const vibe_gb300_model* m, int n_sub) {
+  if (!m) return 0;
+  n_sub = n_sub > 1 ? n_sub : 1;
+  if (m->precision == VIBE_GB300_MIXED) return 3 * (1 + 2 * n_sub) + 1;
+  const int tend = 4 + ((m->fl.div_damp > 0.0 && m->fl.div_order > 2) ? 1 : 0);
+  const int sub = (m->fl.acoustic_mode == 0) ? 2 : (m->fl.acoustic_mode == 1 ? 4 : 2);
+  return 3 * (tend + NSPECIES + n_sub * sub + 1) + 1;
+}
+
+}  // extern "C"

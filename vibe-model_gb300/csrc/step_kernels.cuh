@@ -1,0 +1,59 @@
+// vibe-model_gb300/csrc/step_kernels.cuh -- launchers of the step kernels.
+#pragma once
+#include "vibe_internal.cuh"
+
+namespace vgb {
+
+// ---- FP64 path (step_fp64.cu) ----
+void fp64_slow_tendency(const Dims& d, const Metric& m, const Flags& fl, double* const* st, double* const* tend,
+                        double* lap_scratch, cudaStream_t stream);
+void fp64_stage_update(const Dims& d, double* const* s0, double* const* tend, double a, double* const* out,
+                       cudaStream_t stream);
+void fp64_fb_substep(const Dims& d, const Metric& m, const Flags& fl, double* const* st, double dtau,
+                     cudaStream_t stream);
+void fp64_ref_hevi_substep(const Dims& d, const Metric& m, double* const* st, double dtau, const double* ta,
+                           const double* tb, const double* tc, double* scratch, unsigned* err, cudaStream_t stream);
+void fp64_cons_hevi_substep(const Dims& d, const Metric& m, const Flags& fl, double* const* st, double* const* tmp,
+                            double* scratch, double dtau, unsigned* err, cudaStream_t stream);
+void fp64_sponge(const Dims& d, const Metric& m, double* const* st, int kmin, double dt, cudaStream_t stream);
+void fp64_nonfinite(const Dims& d, double* const* st, unsigned* err, cudaStream_t stream);
+
+// ---- mixed path (step_mixed.cu): FP64 state, FP32 working state ----
+// Horizontally uniform reference state on flat terrain: every coefficient
+// is a function of k only and lives in these FP32 tables (device).
+struct Tab {
+  const float* r0c;    // nz   rho0(k)
+  const float* rfz;    // nz+1 0.5*(rho0(max(k-1,0)) + rho0(min(k,nz-1)))
+  const float* t0c;    // nz   theta0(k)
+  const float* tfz;    // nz+1 0.5*(theta0(max(k-1,0)) + theta0(min(k,nz-1)))
+  const float* kap;    // nz   (Rd/cv) * pi0 / max(rho0, 1e-8)
+  const float* idzc;   // nz   1/max(dzeta(k)*z_top, 1)        (mass divergence)
+  const float* idzw;   // nz+1 1/max(dzeta(min(k,nz-1))*z_top, 1) (w pressure gradient)
+  const float* idza;   // nz   1/(dzeta(k)*z_top)               (advection)
+  const float* th0inv; // nz   1/max(theta0(k), 1)
+  const float* t0d;    // 6*nz theta0(clamp(k+m)) - theta0(k), m = -3..2 (WENO shift)
+  const float* spw;    // nz+1 sponge weight 1/(1+dt*alpha(min(k,nz-1))) for the current dt
+  const double* spwd;  // nz+1 the same weight in FP64 (damping.cpp:94)
+  const double* spdt;  // nz+1 dt*alpha(min(k,nz-1)) in FP64 (damping.cpp:98)
+  const double* r0d;   // nz   rho0 (FP64)
+  const double* t0dd;  // nz   theta0 (FP64)
+  const double* p0d;   // nz   pi0 (FP64)
+  float dx_inv, dy_inv, f0, beta, dy;
+};
+
+struct WS {          // FP32 working state (perturbation form)
+  float* f[NSPECIES]; // u v w rho' theta' pi' qv qc..qg
+};
+
+void mixed_stage(const Dims& d, const Tab& t, const Flags& fl, const WS& win, const WS& w0, const WS& wout,
+                 double* const* s0, double* const* ss, double dt_stage, bool write_fp64, unsigned* err,
+                 cudaStream_t stream);
+void mixed_fb_substep(const Dims& d, const Tab& t, const Flags& fl, const WS& win, const WS& wout, float dtau,
+                      cudaStream_t stream);
+void mixed_hevi_substep(const Dims& d, const Tab& t, const Flags& fl, const WS& win, const WS& wout, float dtau,
+                        const float* lu /* 3*nz: a, cprime, inv_denom */, unsigned* err, cudaStream_t stream);
+void mixed_finish(const Dims& d, const Tab& t, const Flags& fl, const WS& wfin, const WS& wst, const WS& w0,
+                  double* const* ss, double dt, int kmin, unsigned* err, cudaStream_t stream);
+void mixed_to_working(const Dims& d, const Tab& t, double* const* s, const WS& w, cudaStream_t stream);
+
+}  // namespace vgb

@@ -1,0 +1,296 @@
+"""Python host binding of libvibe_gb300.so (include/vibe_gb300.h,
+include/vibe_c_kernels.h).
+
+Mirrors the reference's stepper interface for this path:
+``Model`` ~ RungeKutta3Integrator + the State it advances
+(include/vibe/time/runge_kutta.hpp:46-80, include/vibe/dyn/state.hpp:98-166),
+``Model.step(dt, n_sub)`` ~ ``Integrator::step(State&, StepContext)``
+(include/vibe/time/integrator.hpp:65), fields exchanged in the reference's
+halo'd FieldT storage layout. Failures raise, as the reference's
+NumericalError / VIBE_CHECK do. Importing this module fails loudly when the
+CUDA library has not been built: there is no CPU path.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libvibe_gb300.so")
+
+SPECIES = ["u", "v", "w", "rho", "theta", "pi", "qv", "qc", "qr", "qi", "qs", "qg"]
+NSPECIES = 12
+HALO = 4
+FP64, MIXED = 0, 1
+_D, _I = ctypes.c_double, ctypes.c_int
+
+if not os.path.exists(LIB_PATH):
+    raise ImportError("libvibe_gb300.so is not built (run vibe-model_gb300/build.py); "
+                      "the dynamics step has no CPU implementation")
+lib = ctypes.CDLL(LIB_PATH)
+
+
+class Setup(ctypes.Structure):
+    """Mirror of ``vibe_gb300_setup``."""
+
+    _fields_ = [
+        ("nx", _I), ("ny", _I), ("nz", _I),
+        ("dx", _D), ("dy", _D), ("z_top", _D),
+        ("zeta_first", _D), ("zeta_stretch", _D),
+        ("terrain_kind", _I), ("hill_h", _D), ("hill_a", _D), ("hill_xc", _D), ("hill_yc", _D),
+        ("ref_kind", _I), ("theta0", _D), ("p_surf", _D), ("bv_n", _D), ("profile_dz", _D),
+        ("bubble_amplitude", _D), ("bubble_radius_x", _D), ("bubble_radius_z", _D),
+        ("bubble_xc", _D), ("bubble_yc", _D), ("bubble_zc", _D),
+        ("qv_surface", _D), ("qv_decay_height", _D),
+        ("u_background", _D), ("shear_u", _D),
+        ("advection", _I), ("weno_scalars", _I), ("moist", _I),
+        ("coriolis", _I), ("latitude", _D),
+        ("sponge_alpha", _D), ("sponge_start_fraction", _D),
+        ("divergence_damping", _D), ("divergence_order", _I),
+        ("pgf_perturbation", _I), ("acoustic_mode", _I), ("hevi_beta", _D),
+        ("split_fast", _I), ("weno_advective", _I),
+    ]
+
+    @classmethod
+    def defaults(cls, **kw):
+        s = cls()
+        lib.vibe_gb300_setup_defaults(ctypes.byref(s))
+        for k, v in kw.items():
+            if not hasattr(s, k):
+                raise AttributeError(k)
+            setattr(s, k, v)
+        return s
+
+    def as_dict(self):
+        return {name: getattr(self, name) for name, _ in self._fields_}
+
+
+_vp = ctypes.c_void_p
+_dp = ctypes.POINTER(ctypes.c_double)
+_sigs = {
+    "vibe_gb300_setup_defaults": (None, [ctypes.POINTER(Setup)]),
+    "vibe_gb300_model_create": (_I, [ctypes.POINTER(Setup), _I, ctypes.POINTER(_vp)]),
+    "vibe_gb300_model_destroy": (None, [_vp]),
+    "vibe_gb300_storage_size": (ctypes.c_size_t, [_vp, _I]),
+    "vibe_gb300_get_field": (_I, [_vp, _I, _vp]),
+    "vibe_gb300_set_field": (_I, [_vp, _I, _vp]),
+    "vibe_gb300_get_reffield": (_I, [_vp, _I, _vp]),
+    "vibe_gb300_get_zeta": (_I, [_vp, _vp]),
+    "vibe_gb300_get_terrain": (_I, [_vp, _vp]),
+    "vibe_gb300_get_sponge": (_I, [_vp, _vp]),
+    "vibe_gb300_step": (_I, [_vp, _D, _I, _I]),
+    "vibe_gb300_step_async": (_I, [_vp, _D, _I, _I]),
+    "vibe_gb300_sync": (_I, [_vp]),
+    "vibe_gb300_slow_tendency": (_I, [_vp, ctypes.POINTER(_dp)]),
+    "vibe_gb300_acoustic_substep": (_I, [_vp, _D]),
+    "vibe_gb300_hevi_substep": (_I, [_vp, _D]),
+    "vibe_gb300_sponge": (_I, [_vp, _D]),
+    "vibe_gb300_device_field": (_I, [_vp, _I, ctypes.POINTER(_dp), ctypes.POINTER(_I)]),
+    "vibe_gb300_stream": (_vp, [_vp]),
+    "vibe_gb300_launches_per_step": (_I, [_vp, _I]),
+    "vibe_gb300_last_error": (ctypes.c_char_p, []),
+    # C-ABI kernels (include/vibe_c_kernels.h)
+    "vibe_tridiagonal_solve_f64": (_I, [_vp, _vp, _vp, _vp, _I, _vp, _vp]),
+    "vibe_tridiagonal_solve_batched_f64": (_I, [_vp, _vp, _vp, _vp, _I, _I, _vp]),
+    "vibe_weno5_reconstruct_f64": (None, [_D, _D, _D, _D, _D, _dp, _dp]),
+    "vibe_bilinear_f64": (_D, [_vp, _I, _I, _I, _I, _D, _D, _I]),
+    "vibe_cfl_scan_f64": (_D, [_vp, _vp, _vp, _vp, _vp, _I, _I, _I, _D, _D, _D, _D, _dp, _dp]),
+    "vibe_neumaier_sum_f64": (_D, [_vp, ctypes.c_size_t]),
+    "vibe_advect_scalar_flux_f64": (None, [_vp] * 7 + [_I, _I, _I, _D, _D, _D, _vp]),
+    "vibe_c_last_error": (ctypes.c_char_p, []),
+}
+for _name, (_res, _args) in _sigs.items():
+    _f = getattr(lib, _name)
+    _f.restype = _res
+    _f.argtypes = _args
+
+ERRORS = {-1: "bad argument", -2: "device error", -3: "non-finite state", -4: "singular tridiagonal",
+          -5: "unsupported"}
+
+
+class VibeError(RuntimeError):
+    """Raised for any non-zero status (the reference throws NumericalError)."""
+
+    def __init__(self, code, msg):
+        super().__init__("%s (%d): %s" % (ERRORS.get(code, "error"), code, msg))
+        self.code = code
+
+
+def _check(rc):
+    if rc != 0:
+        raise VibeError(rc, lib.vibe_gb300_last_error().decode())
+    return rc
+
+
+def storage_shape(setup, species):
+    """(nsz, nsy, nsx) of a species' FieldT storage (field.hpp:40-53)."""
+    h2 = 2 * HALO
+    return (setup.nz + h2 + (species == 2), setup.ny + h2 + (species == 1),
+            setup.nx + h2 + (species == 0))
+
+
+def interior(setup, species, arr):
+    """Interior points incl. the extra face of a storage array."""
+    a = np.asarray(arr).reshape(storage_shape(setup, species))
+    return a[HALO:HALO + setup.nz + (species == 2), HALO:HALO + setup.ny + (species == 1),
+             HALO:HALO + setup.nx + (species == 0)]
+
+
+class Model:
+    """A device-resident state plus its RK3 integrator."""
+
+    def __init__(self, setup, precision=FP64):
+        self.setup = setup
+        self.precision = precision
+        h = _vp()
+        _check(lib.vibe_gb300_model_create(ctypes.byref(setup), precision, ctypes.byref(h)))
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib.vibe_gb300_model_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def size(self, sp):
+        return int(lib.vibe_gb300_storage_size(self.h, sp))
+
+    def get(self, sp):
+        a = np.empty(self.size(sp))
+        _check(lib.vibe_gb300_get_field(self.h, sp, a.ctypes.data))
+        return a
+
+    def set(self, sp, arr):
+        a = np.ascontiguousarray(arr, dtype=np.float64).ravel()
+        if a.size != self.size(sp):
+            raise ValueError("species %d expects %d values, got %d" % (sp, self.size(sp), a.size))
+        _check(lib.vibe_gb300_set_field(self.h, sp, a.ctypes.data))
+
+    def state(self):
+        return [self.get(sp) for sp in range(NSPECIES)]
+
+    def set_state(self, st):
+        for sp, a in enumerate(st):
+            self.set(sp, a)
+
+    def reffield(self, which):
+        a = np.empty(self.size(3))
+        _check(lib.vibe_gb300_get_reffield(self.h, which, a.ctypes.data))
+        return a
+
+    def zeta(self):
+        a = np.empty(self.setup.nz + 1)
+        _check(lib.vibe_gb300_get_zeta(self.h, a.ctypes.data))
+        return a
+
+    def terrain(self):
+        a = np.empty(self.setup.nx * self.setup.ny)
+        _check(lib.vibe_gb300_get_terrain(self.h, a.ctypes.data))
+        return a
+
+    def sponge_profile(self):
+        a = np.empty(self.setup.nz)
+        _check(lib.vibe_gb300_get_sponge(self.h, a.ctypes.data))
+        return a
+
+    def step(self, dt, n_sub, n_steps=1):
+        return _check(lib.vibe_gb300_step(self.h, dt, n_sub, n_steps))
+
+    def step_async(self, dt, n_sub, n_steps=1):
+        return _check(lib.vibe_gb300_step_async(self.h, dt, n_sub, n_steps))
+
+    def sync(self):
+        return _check(lib.vibe_gb300_sync(self.h))
+
+    def slow_tendency(self):
+        outs = [np.empty(self.size(sp)) for sp in range(NSPECIES)]
+        ptrs = (_dp * NSPECIES)(*[o.ctypes.data_as(_dp) for o in outs])
+        _check(lib.vibe_gb300_slow_tendency(self.h, ptrs))
+        return outs
+
+    def acoustic_substep(self, dtau):
+        _check(lib.vibe_gb300_acoustic_substep(self.h, dtau))
+
+    def hevi_substep(self, dtau):
+        _check(lib.vibe_gb300_hevi_substep(self.h, dtau))
+
+    def sponge(self, dt):
+        _check(lib.vibe_gb300_sponge(self.h, dt))
+
+    def stream(self):
+        return lib.vibe_gb300_stream(self.h)
+
+    def launches_per_step(self, n_sub):
+        return int(lib.vibe_gb300_launches_per_step(self.h, n_sub))
+
+
+# ---- C-ABI kernels (names as in the reference's c_kernels.h) ----------------
+def _ptr(a):
+    return None if a is None else np.ascontiguousarray(a, dtype=np.float64).ctypes.data
+
+
+def tridiagonal_solve(a, b, c, d):
+    """vibe_tridiagonal_solve_f64: returns (rc, x)."""
+    b = np.ascontiguousarray(b, dtype=np.float64)
+    n = b.size
+    keep = [np.ascontiguousarray(v, dtype=np.float64) if v is not None else None for v in (a, c, d)]
+    x = np.zeros(n)
+    ws = np.zeros(max(n, 1))
+    rc = lib.vibe_tridiagonal_solve_f64(_ptr(keep[0]), b.ctypes.data, _ptr(keep[1]), keep[2].ctypes.data, n,
+                                        x.ctypes.data, ws.ctypes.data)
+    return rc, x
+
+
+def tridiagonal_solve_batched(a, b, c, d):
+    """n_sys systems as rows of b, d (n_sys, n) and a, c (n_sys, n-1)."""
+    b = np.ascontiguousarray(b, dtype=np.float64)
+    n_sys, n = b.shape
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    c = np.ascontiguousarray(c, dtype=np.float64)
+    d = np.ascontiguousarray(d, dtype=np.float64)
+    x = np.zeros_like(b)
+    rc = lib.vibe_tridiagonal_solve_batched_f64(a.ctypes.data, b.ctypes.data, c.ctypes.data, d.ctypes.data, n, n_sys,
+                                                x.ctypes.data)
+    return rc, x
+
+
+def weno5_reconstruct(qm2, qm1, q0, q1, q2):
+    ql, qr = ctypes.c_double(), ctypes.c_double()
+    lib.vibe_weno5_reconstruct_f64(qm2, qm1, q0, q1, q2, ctypes.byref(ql), ctypes.byref(qr))
+    return ql.value, qr.value
+
+
+def bilinear(f, halo, nsx, nsy, nz, xi, yj, k):
+    f = np.ascontiguousarray(f, dtype=np.float64)
+    return lib.vibe_bilinear_f64(f.ctypes.data, halo, nsx, nsy, nz, xi, yj, k)
+
+
+def cfl_scan(u, v, w, dzeta, zs, nx, ny, nz, dx, dy, z_top, dt):
+    keep = [np.ascontiguousarray(a, dtype=np.float64) if a is not None else None for a in (u, v, w, dzeta, zs)]
+    mw, mdz = ctypes.c_double(), ctypes.c_double()
+    r = lib.vibe_cfl_scan_f64(*[_ptr(k) for k in keep], nx, ny, nz, dx, dy, z_top, dt, ctypes.byref(mw),
+                              ctypes.byref(mdz))
+    return r, mw.value, mdz.value
+
+
+def neumaier_sum(x):
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    return lib.vibe_neumaier_sum_f64(x.ctypes.data, x.size)
+
+
+def advect_scalar_flux(q, rho, u, v, w, dzeta, zs, nx, ny, nz, dx, dy, z_top):
+    keep = [np.ascontiguousarray(a, dtype=np.float64) if a is not None else None for a in (q, rho, u, v, w, dzeta, zs)]
+    out = np.full(nx * ny * nz, np.nan)
+    lib.vibe_advect_scalar_flux_f64(*[_ptr(k) for k in keep], nx, ny, nz, dx, dy, z_top, out.ctypes.data)
+    return out
