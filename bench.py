@@ -1,0 +1,365 @@
+#!/usr/bin/env python
+"""Throughput of the GB300 dynamics step (cell-updates/s) on the
+512 x 512 x 80 single-domain case.
+
+Workload (synthetic, seeded): dx = dy = 1 km; 80 levels stretched from a
+50 m first layer over a 20 km top (ratio 1.0341247533415947: with a 50 m
+first layer and 20 km depth, geometric stretching over 80 levels ends at
+708 m, not 500 m); theta0 = 300 K with N = 0.01 1/s; uniform u = 10 m/s;
+theta' ~ U(-0.5, 0.5) K below 1 km plus 20 warm bubbles (1-3 K, radius
+1-4 km, centres uniform in x, y and in 1-5 km height); WENO5 scalars,
+2nd-order momentum (the reference has no 4th-order momentum advection);
+dt = 6 s, 6 acoustic substeps per RK stage with the vertically implicit
+substep; pi' pressure gradient and fast terms integrated once.
+
+One step = one SSP-RK3 step: 3 stages + 18 acoustic substeps + sponge.
+`value` is the mixed-precision (FP64 state, FP32 compute) path; the plain
+FP64 path is measured beside it. Inputs (1.7 GB of FP64 state) are far
+larger than the 129 MB L2, so no flush is needed between steps.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+Under torchrun every rank advances its own replica (an ensemble member):
+weak scaling, no collective on the data path.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "vibe-model_gb300")
+sys.path.insert(0, PKG)
+
+NX, NY, NZ = 512, 512, 80
+DT, NSUB = 6.0, 6
+STRETCH = 1.0341247533415947
+METRIC = "dyn-step cell-updates/s, mixed vs FP64 on 1 GB300 at stated error vs FP64"
+UNIT = "cell-updates/s"
+HBM_FALLBACK = 6800.0
+
+
+CASE = dict(nz=NZ, dx=1000.0, dy=1000.0, z_top=20000.0, zeta_first=1.0, zeta_stretch=STRETCH,
+            ref_kind=1, theta0=300.0, bv_n=0.01, profile_dz=250.0, bubble_amplitude=0.0,
+            qv_surface=0.0, u_background=10.0, shear_u=0.0,
+            advection=5, weno_scalars=1, weno_advective=1, pgf_perturbation=1, split_fast=1,
+            acoustic_mode=2, hevi_beta=0.5, moist=0, coriolis=0)
+
+
+def case_setup(vg_setup_cls, nx=NX, ny=NY):
+    return vg_setup_cls.defaults(nx=nx, ny=ny, **CASE)
+
+
+def perturbed_state(setup, theta, rho, zeta, seed=1, nx_full=NX, ny_full=NY, x_off=0, y_off=0):
+    """theta/pi storage arrays with the seeded perturbations (numpy set-up)."""
+    rng = np.random.default_rng(seed)
+    h = 4
+    th = theta.reshape(setup.nz + 8, setup.ny + 8, setup.nx + 8).copy()
+    r = rho.reshape(setup.nz + 8, setup.ny + 8, setup.nx + 8)
+    zc = 0.5 * (zeta[:-1] + zeta[1:]) * setup.z_top
+    noise = rng.uniform(-0.5, 0.5, size=(NZ, ny_full, nx_full))
+    low = zc < 1000.0
+    x = (np.arange(setup.nx) + x_off + 0.5) * setup.dx
+    y = (np.arange(setup.ny) + y_off + 0.5) * setup.dy
+    interior = th[h:h + NZ, h:h + setup.ny, h:h + setup.nx]
+    interior[low] += noise[low][:, y_off:y_off + setup.ny, x_off:x_off + setup.nx]
+    amp = rng.uniform(1.0, 3.0, 20)
+    rad = rng.uniform(1000.0, 4000.0, 20)
+    xc = rng.uniform(0.0, nx_full * setup.dx, 20)
+    yc = rng.uniform(0.0, ny_full * setup.dy, 20)
+    zcen = rng.uniform(1000.0, 5000.0, 20)
+    for b in range(20):  # cos^2 bubbles as init_warm_bubble (initial_conditions.cpp:144-156)
+        ix = np.nonzero(np.abs(x - xc[b]) < rad[b])[0]
+        iy = np.nonzero(np.abs(y - yc[b]) < rad[b])[0]
+        iz = np.nonzero(np.abs(zc - zcen[b]) < rad[b])[0]
+        if not (ix.size and iy.size and iz.size):
+            continue
+        Z, Y, X = np.meshgrid(zc[iz], y[iy], x[ix], indexing="ij")
+        r2 = ((X - xc[b]) / rad[b]) ** 2 + ((Y - yc[b]) / rad[b]) ** 2 + ((Z - zcen[b]) / rad[b]) ** 2
+        c = np.cos(0.5 * np.pi * np.sqrt(np.minimum(r2, 1.0)))
+        sub = interior[iz[0]:iz[-1] + 1, iy[0]:iy[-1] + 1, ix[0]:ix[-1] + 1]
+        sub += np.where(r2 < 1.0, amp[b] * c * c, 0.0)
+    # enforce_state_equation (initial_conditions.cpp:110-121), dry: gamma_f = 1
+    val = r[h:h + NZ, h:h + setup.ny, h:h + setup.nx] * 287.05 * interior / 100000.0
+    pi = np.zeros_like(th)
+    pi[h:h + NZ, h:h + setup.ny, h:h + setup.nx] = np.power(val, 287.05 / 717.63)
+    return th.ravel(), pi.ravel()
+
+
+class ClockSampler:
+    """nvidia-smi samples of SM clock and throttle reasons during a region."""
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.rows = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+            time.sleep(0.3)
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) == 7:
+                self.rows.append(parts)
+
+    def __exit__(self, *exc):
+        if self.proc:
+            time.sleep(0.2)
+            self.proc.terminate()
+            self.proc.wait(timeout=5)
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        sm = [float(r[0]) for r in self.rows if r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[c] for r in self.rows for c in range(4) if r[3 + c].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.rows)}
+
+
+def measured_peak():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return HBM_FALLBACK, "fallback"
+
+
+def traffic_of(kernel):
+    """DRAM bytes per launch from the committed ncu summary, or None."""
+    p = os.path.join(ROOT, "profiles", "dram_traffic.json")
+    try:
+        with open(p) as f:
+            return json.load(f).get(kernel)
+    except (OSError, ValueError):
+        return None
+
+
+# ---- CPU baseline / reference arm (oracle port on host cores) ---------------
+def _oracle():
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import oracle_ctypes as oc
+    if not os.path.exists(oc.PORT_SO):
+        subprocess.run(["make", "-C", oc.ORACLE_DIR, "-s"], check=True)
+    return oc
+
+
+def cpu_sample_run(args):
+    """One worker: steps a horizontal sample of the workload on the oracle
+    port (the reference's serial FP64 algorithm). Returns (cells, seconds)."""
+    nx, ny, steps, warmup, seed = args
+    oc = _oracle()
+    s = oc.defaults()
+    for k, v in dict(CASE, nx=nx, ny=ny).items():
+        setattr(s, k, v)
+    m = oc.Model(s, "port")
+    th, pi = perturbed_state(s, m.get(4), m.get(3), m.zeta(), seed=seed, x_off=0, y_off=0)
+    m.set(4, th)
+    m.set(5, pi)
+    for _i in range(warmup):
+        m.rk3_step(DT, NSUB)
+    t0 = time.perf_counter()
+    for _i in range(steps):
+        m.rk3_step(DT, NSUB)
+    return nx * ny * NZ * steps, time.perf_counter() - t0
+
+
+def reference_arm(args):
+    import multiprocessing as mp
+    cores = os.cpu_count() or 1
+    nx = ny = 64
+    steps, warmup = args.steps, args.warmup
+    with mp.get_context("spawn").Pool(cores) as pool:
+        t0 = time.perf_counter()
+        res = pool.map(cpu_sample_run, [(nx, ny, steps, warmup, 1 + p) for p in range(cores)])
+        wall = time.perf_counter() - t0
+    cells = sum(r[0] for r in res)
+    secs = max(r[1] for r in res)
+    value = cells / secs
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": steps, "warmup": warmup, "ms_per_step": 1e3 * secs / steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": "512x512x80 single domain, dx=1km, dt=6s, 6 substeps/stage (per-core sample %dx%dx%d)"
+                   % (nx, ny, NZ), "sample_per_core": [nx, ny, NZ]},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": "%d independent %dx%dx%d horizontal samples of the workload, one per core, "
+                                   "%d timed steps each (wall %.1f s)" % (cores, nx, ny, NZ, steps, wall)},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
+# ---- GPU arm -----------------------------------------------------------------
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+
+    if args.impl == "reference":
+        if rank == 0:
+            reference_arm(args)
+        return
+
+    # CPU baseline first (rank 0 at N=1 only), before any CUDA work
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cells, secs = cpu_sample_run((128, 128, 2, 0, 1))
+        cpu = {"value": cells / secs, "unit": UNIT, "cores": 1, "kind": "port",
+               "sample": "128x128x80 horizontal sample of the workload, 2 RK3 steps, single thread (%.1f s)" % secs}
+
+    import torch
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    def max_over_ranks(x):
+        if dist is None:
+            return x
+        t = torch.tensor([x], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    import vibe_gb300 as vg
+    setup = case_setup(vg.Setup)
+    cells = NX * NY * NZ
+
+    def make(prec):
+        m = vg.Model(setup, prec)
+        th, pi = perturbed_state(setup, m.get(4), m.get(3), m.zeta(), seed=1 + rank)
+        m.set(4, th)
+        m.set(5, pi)
+        return m
+
+    def timed_steps(m, k):
+        ext = torch.cuda.ExternalStream(m.stream())
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        barrier()
+        e0.record(ext)
+        m.step_async(DT, NSUB, k)
+        e1.record(ext)
+        m.sync()
+        barrier()
+        return e0.elapsed_time(e1)
+
+    # ---- mixed path (the headline) ----
+    mx = make(vg.MIXED)
+    mx.step(DT, NSUB, args.warmup)
+    mx.set_kernel_timing(True)
+    with ClockSampler(local) as clk:
+        ms_mx = timed_steps(mx, args.steps)
+    ktimes = mx.kernel_times()
+    mx.set_kernel_timing(False)
+    ms_mx = max_over_ranks(ms_mx)
+    launches = mx.launches_per_step(NSUB) * args.steps
+
+    # ---- end to end through the public API with host buffers ----
+    pinned = [torch.empty(mx.size(sp), dtype=torch.float64, pin_memory=True) for sp in range(7)]
+    ptrs = [p.data_ptr() for p in pinned]
+    mx.get_state_ptrs(ptrs)
+    mx.sync()
+    e2e_steps = max(3, args.steps // 4)
+    ext = torch.cuda.ExternalStream(mx.stream())
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    barrier()
+    e0.record(ext)
+    for _ in range(e2e_steps):
+        mx.set_state_ptrs(ptrs)
+        mx.step_async(DT, NSUB, 1)
+        mx.get_state_ptrs(ptrs)
+    e1.record(ext)
+    mx.sync()
+    barrier()
+    ms_e2e = max_over_ranks(e0.elapsed_time(e1))
+    h2d = sum(mx.size(sp) for sp in range(7)) * 8
+    mx.close()
+
+    # ---- plain FP64 path ----
+    f64 = make(vg.FP64)
+    f64.step(DT, NSUB, 1)
+    k64 = max(2, args.steps // 10)
+    ms_64 = max_over_ranks(timed_steps(f64, k64))
+    f64.close()
+
+    value = world * cells * args.steps / (ms_mx * 1e-3)
+    value64 = world * cells * k64 / (ms_64 * 1e-3)
+    e2e = world * cells * e2e_steps / (ms_e2e * 1e-3)
+
+    # roofline of the dominant kernel class (live CUDA-event times)
+    peak, peak_kind = measured_peak()
+    per_cell = {0: (84.0 * 2 + 196.0) / 3.0, 1: 32.0, 2: 156.0, 3: 20.0}
+    names = {0: "k_mx_stage", 1: "k_mx_hevi_col", 2: "k_mx_finish", 3: "k_mx_fb_mom(u,v)"}
+    dom = max(ktimes, key=lambda c: ktimes[c][0])
+    tot_ms, spans = ktimes[dom]
+    avg_s = tot_ms / max(spans, 1) * 1e-3
+    bytes_launch = per_cell[dom] * cells
+    achieved = bytes_launch / avg_s / 1e9
+    share = {names[c]: round(ktimes[c][0] / max(sum(v[0] for v in ktimes.values()), 1e-9), 4) for c in ktimes}
+
+    if rank != 0:
+        return
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_mx / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64-state/f32-compute", "data": "synthetic",
+        "config": {"workload": "512x512x80 single domain (dx=1 km, stretched dz 50->708 m, 20 km top), WENO5 "
+                               "scalars, dt=6 s, 6 HEVI substeps per RK3 stage",
+                   "cells": cells, "dt_s": DT, "substeps_per_stage": NSUB, "precision": "mixed",
+                   "l2": "inputs (1.7 GB state) >> 129 MB L2; no flush", "parallelism": "replica per GPU"},
+        "fp64_value": value64, "fp64_ms_per_step": ms_64 / k64, "mixed_over_fp64": value / value64,
+        "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": h2d,
+                "note": "set_state (7 species, pinned host, FieldT layout) + step + get_state per step"},
+        "roofline": {"bound": "hbm", "kernel": names[dom], "achieved": achieved, "peak": peak,
+                     "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind,
+                     "traffic": traffic_of(names[dom]), "algorithmic_bytes_per_launch": bytes_launch,
+                     "avg_launch_ms": avg_s * 1e3, "launches": spans, "time_share": share},
+        "step_roofline": {"bytes_per_cell_update": 1944, "achieved": 1944.0 * value / world / 1e9,
+                          "peak": peak, "unit": "GB/s", "frac": 1944.0 * value / world / 1e9 / peak},
+        "gpu_launches": launches,
+        "clocks": clk.summary(),
+    }
+    if cpu is not None:
+        line["cpu_baseline"] = cpu
+    print(json.dumps(line))
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -45,6 +45,7 @@ extern "C" {
 
 #define VIBE_GB300_FP64 0  /* all arithmetic FP64 */
 #define VIBE_GB300_MIXED 1 /* FP64 state, FP32 tendencies and substeps */
+#define VIBE_GB300_FP64_EXACT 2 /* FP64 without FMA contraction: the reference's bits */
 
 /* Species order of dyn::Species (include/vibe/dyn/state.hpp:53-55). */
 enum vibe_gb300_species {
@@ -125,6 +126,20 @@ int vibe_gb300_slow_tendency(vibe_gb300_model *m, double *const *host_out);
 int vibe_gb300_acoustic_substep(vibe_gb300_model *m, double dtau);
 int vibe_gb300_hevi_substep(vibe_gb300_model *m, double dtau);
 int vibe_gb300_sponge(vibe_gb300_model *m, double dt);
+
+/* Bulk forms of set/get_field over species 0..nspecies-1 (NULL entries are
+ * skipped). Asynchronous on the model stream: host arrays must stay valid
+ * until vibe_gb300_sync(); pinned host memory makes the copies overlap. */
+int vibe_gb300_set_state(vibe_gb300_model *m, const double *const *host, int nspecies);
+int vibe_gb300_get_state(vibe_gb300_model *m, double *const *host, int nspecies);
+
+/* Optional timing of kernel classes with CUDA events on the model stream
+ * (0 = RK stage kernels, 1 = acoustic substep column/mass kernels,
+ * 2 = finish/sponge/checks, 3 = horizontal momentum of the HEVI substep).
+ * kernel_times returns the accumulated milliseconds and event-pair counts
+ * since timing was enabled. */
+int vibe_gb300_set_kernel_timing(vibe_gb300_model *m, int enable);
+int vibe_gb300_kernel_times(vibe_gb300_model *m, double *ms, long *count, int nclass);
 
 /* Device pointer of a species in the device layout
  * idx = (k*(ny+1) + j)*pitch + i, and that pitch. */

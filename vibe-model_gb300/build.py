@@ -16,7 +16,12 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libvibe_gb300.so")
-SOURCES = ["step_fp64.cu", "step_mixed.cu", "model.cu", "ckern.cu"]
+# (source, object, extra flags)
+SOURCES = [("step_fp64.cu", "step_fp64.o", []),
+           ("step_fp64.cu", "step_fp64_exact.o", ["-DVGB_FP64_EXACT", "--fmad=false"]),
+           ("step_mixed.cu", "step_mixed.o", []),
+           ("model.cu", "model.o", []),
+           ("ckern.cu", "ckern.o", [])]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -44,12 +49,12 @@ def build(verbose=False, force=False):
     headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cuh", ".h"))]
     headers += [os.path.join(ROOT, "include", f) for f in os.listdir(os.path.join(ROOT, "include"))]
     objs, jobs = [], []
-    for src in SOURCES:
+    for src, obj, extra in SOURCES:
         s = os.path.join(CSRC, src)
-        o = os.path.join(BUILD, src + ".o")
+        o = os.path.join(BUILD, obj)
         objs.append(o)
-        if force or _stale(o, [s] + headers):
-            jobs.append([nvcc()] + _flags() + ["-c", s, "-o", o])
+        if force or _stale(o, [s] + headers + [os.path.abspath(__file__)]):
+            jobs.append([nvcc()] + _flags() + extra + ["-c", s, "-o", o])
 
     def run(cmd):
         r = subprocess.run(cmd, capture_output=True, text=True)

@@ -37,8 +37,25 @@ struct HostSetup {
 };
 }  // namespace
 
+// FP64 launchers of one build variant (FMA-contracted or bit-exact)
+struct Fp64Ops {
+  decltype(&fp64_slow_tendency) slow_tendency;
+  decltype(&fp64_stage_update) stage_update;
+  decltype(&fp64_fb_substep) fb_substep;
+  decltype(&fp64_ref_hevi_substep) ref_hevi_substep;
+  decltype(&fp64_cons_hevi_substep) cons_hevi_substep;
+  decltype(&fp64_sponge) sponge;
+  decltype(&fp64_nonfinite) nonfinite;
+};
+static const Fp64Ops kFp64Fast = {fp64_slow_tendency, fp64_stage_update, fp64_fb_substep, fp64_ref_hevi_substep,
+                                  fp64_cons_hevi_substep, fp64_sponge, fp64_nonfinite};
+static const Fp64Ops kFp64Exact = {fp64_slow_tendency_exact, fp64_stage_update_exact, fp64_fb_substep_exact,
+                                   fp64_ref_hevi_substep_exact, fp64_cons_hevi_substep_exact, fp64_sponge_exact,
+                                   fp64_nonfinite_exact};
+
 struct vibe_gb300_model {
   vibe_gb300_setup su{};
+  const Fp64Ops* f64 = &kFp64Fast;
   int precision = 0;
   Dims d{};
   Metric met{};
@@ -77,6 +94,13 @@ struct vibe_gb300_model {
   int kmin = 0;
   std::vector<float> ftab_host;
   std::vector<double> dtab_host;
+  // optional per-kernel-class timing with CUDA events on the model stream
+  bool timing = false;
+  static constexpr int kClasses = 4;  // 0 stage, 1 substep (all kernels), 2 finish/sponge, 3 other
+  std::vector<cudaEvent_t> ev_pool;
+  std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> ev_open;
+  double class_ms[kClasses] = {};
+  long class_n[kClasses] = {};
 };
 
 namespace {
@@ -376,15 +400,20 @@ int configure_dt(vibe_gb300_model* m, double dt, int n_sub) {
   std::vector<double>& d = m->dtab_host;
   std::vector<float>& f = m->ftab_host;
   const size_t o_spw = (size_t)nz + (nz + 1) + nz + (nz + 1) + nz + nz + (nz + 1) + nz + nz + 6 * (size_t)nz;
-  for (int k = 0; k <= nz; ++k) {
-    const double a = sp[imin(k, nz - 1)];
-    const double w = (a > 0.0) ? 1.0 / (1.0 + dt * a) : 1.0;
-    d[k] = w;
-    d[nz + 1 + k] = (a > 0.0) ? dt * a : 0.0;
-    f[o_spw + k] = (float)w;
+  if (m->uniform) {  // per-level sponge tables of the mixed path
+    for (int k = 0; k <= nz; ++k) {
+      const double a = sp[imin(k, nz - 1)];
+      const double w = (a > 0.0) ? 1.0 / (1.0 + dt * a) : 1.0;
+      d[k] = w;
+      d[nz + 1 + k] = (a > 0.0) ? dt * a : 0.0;
+      f[o_spw + k] = (float)w;
+    }
+    CUDA_OK(cudaMemcpyAsync(m->d_dtab, d.data(), 2 * (size_t)(nz + 1) * sizeof(double), cudaMemcpyHostToDevice,
+                            m->stream));
+    CUDA_OK(cudaMemcpyAsync(m->d_ftab + o_spw, f.data() + o_spw, (nz + 1) * sizeof(float), cudaMemcpyHostToDevice,
+                            m->stream));
+    CUDA_OK(cudaStreamSynchronize(m->stream));
   }
-  CUDA_OK(cudaMemcpyAsync(m->d_dtab, d.data(), 2 * (size_t)(nz + 1) * sizeof(double), cudaMemcpyHostToDevice, m->stream));
-  CUDA_OK(cudaMemcpyAsync(m->d_ftab + o_spw, f.data() + o_spw, (nz + 1) * sizeof(float), cudaMemcpyHostToDevice, m->stream));
   m->kmin = nz + 1;
   for (int k = 0; k < nz; ++k)
     if (sp[k] > 0.0) { m->kmin = k; break; }
@@ -459,11 +488,52 @@ WS ws_of(float* const* a) {
   for (int q = 0; q < NSPECIES; ++q) w.f[q] = a[q];
   return w;
 }
-// fields u..pi from `sub`, the rest from `stage`
+// the fields the acoustic substeps update (u, v, w, rho, pi); theta sits
+// between rho and pi in the species order, so a range test would be wrong
+inline bool acoustic_field(int q) { return q == U || q == V || q == W || q == RHO || q == PI; }
+// acoustic fields from `sub`, the rest from `stage`
 WS ws_compose(float* const* sub, float* const* stage) {
   WS w;
-  for (int q = 0; q < NSPECIES; ++q) w.f[q] = (q <= PI) ? sub[q] : stage[q];
+  for (int q = 0; q < NSPECIES; ++q) w.f[q] = acoustic_field(q) ? sub[q] : stage[q];
   return w;
+}
+
+cudaEvent_t take_event(vibe_gb300_model* m) {
+  cudaEvent_t e;
+  if (!m->ev_pool.empty()) {
+    e = m->ev_pool.back();
+    m->ev_pool.pop_back();
+  } else {
+    cudaEventCreate(&e);
+  }
+  return e;
+}
+struct Span {  // brackets the launches of one kernel class with two events
+  vibe_gb300_model* m;
+  int cls;
+  cudaEvent_t a = nullptr;
+  Span(vibe_gb300_model* mm, int c) : m(mm), cls(c) {
+    if (!m->timing) return;
+    a = take_event(m);
+    cudaEventRecord(a, m->stream);
+  }
+  ~Span() {
+    if (!a) return;
+    cudaEvent_t b = take_event(m);
+    cudaEventRecord(b, m->stream);
+    m->ev_open.push_back({cls, {a, b}});
+  }
+};
+void collect_timing(vibe_gb300_model* m) {  // after a stream sync
+  for (auto& o : m->ev_open) {
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, o.second.first, o.second.second);
+    m->class_ms[o.first] += ms;
+    m->class_n[o.first] += 1;
+    m->ev_pool.push_back(o.second.first);
+    m->ev_pool.push_back(o.second.second);
+  }
+  m->ev_open.clear();
 }
 
 int enqueue_steps(vibe_gb300_model* m, double dt, int n_sub_in, int n_steps) {
@@ -477,40 +547,58 @@ int enqueue_steps(vibe_gb300_model* m, double dt, int n_sub_in, int n_steps) {
     if (m->precision == VIBE_GB300_FP64) {
       for (int stage = 0; stage < 3; ++stage) {
         double** src = (stage == 0) ? S0 : S1;
-        fp64_slow_tendency(d, m->met, m->fl, src, m->tend, m->scratch, m->stream);
-        fp64_stage_update(d, S0, m->tend, dts[stage], S1, m->stream);
+        {
+          Span sp(m, 0);
+          m->f64->slow_tendency(d, m->met, m->fl, src, m->tend, m->scratch, m->stream);
+          m->f64->stage_update(d, S0, m->tend, dts[stage], S1, m->stream);
+        }
         const double dtau = dts[stage] / (double)n_sub;
         if (m->fl.acoustic_mode == 1)
           if (int rc = ref_hevi_coefficients(m, dtau)) return rc;
         for (int n = 0; n < n_sub; ++n) {
-          if (m->fl.acoustic_mode == 0) fp64_fb_substep(d, m->met, m->fl, S1, dtau, m->stream);
+          Span sp(m, 1);
+          if (m->fl.acoustic_mode == 0) m->f64->fb_substep(d, m->met, m->fl, S1, dtau, m->stream);
           else if (m->fl.acoustic_mode == 1)
-            fp64_ref_hevi_substep(d, m->met, S1, dtau, m->d_tri, m->d_tri + d.nz, m->d_tri + 2 * d.nz, m->scratch,
+            m->f64->ref_hevi_substep(d, m->met, S1, dtau, m->d_tri, m->d_tri + d.nz, m->d_tri + 2 * d.nz, m->scratch,
                                   m->d_err, m->stream);
-          else fp64_cons_hevi_substep(d, m->met, m->fl, S1, m->tmp, m->scratch, dtau, m->d_err, m->stream);
+          else m->f64->cons_hevi_substep(d, m->met, m->fl, S1, m->tmp, m->scratch, dtau, m->d_err, m->stream);
         }
-        fp64_nonfinite(d, S1, m->d_err, m->stream);
+        Span sp(m, 2);
+        m->f64->nonfinite(d, S1, m->d_err, m->stream);
       }
-      fp64_sponge(d, m->met, S1, m->kmin, dt, m->stream);
+      Span sp(m, 2);
+      m->f64->sponge(d, m->met, S1, m->kmin, dt, m->stream);
     } else {
       const WS w0 = ws_of(m->W0);
       float** final_sub = nullptr;
       for (int stage = 0; stage < 3; ++stage) {
         float** st_out = m->WSt[stage & 1];
         const WS win = (stage == 0) ? w0 : ws_compose(final_sub, m->WSt[(stage - 1) & 1]);
-        mixed_stage(d, m->tab, m->fl, win, w0, ws_of(st_out), S0, S1, dts[stage], stage == 2, m->d_err, m->stream);
+        {
+          Span sp(m, 0);
+          mixed_stage(d, m->tab, m->fl, win, w0, ws_of(st_out), S0, S1, dts[stage], stage == 2, m->d_err, m->stream);
+        }
         const float dtau = (float)(dts[stage] / (double)n_sub);
         float** in = st_out;
         for (int n = 0; n < n_sub; ++n) {
           float** out = (n & 1) ? m->WB : m->WA;
-          if (m->fl.acoustic_mode == 2)
-            mixed_hevi_substep(d, m->tab, m->fl, ws_of(in), ws_of(out), dtau, m->d_lu + (size_t)stage * 3 * d.nz,
-                               m->d_err, m->stream);
-          else mixed_fb_substep(d, m->tab, m->fl, ws_of(in), ws_of(out), dtau, m->stream);
+          if (m->fl.acoustic_mode == 2) {
+            {
+              Span sp(m, 1);
+              mixed_hevi_column(d, m->tab, m->fl, ws_of(in), ws_of(out), dtau, m->d_lu + (size_t)stage * 3 * d.nz,
+                                m->stream);
+            }
+            Span sp(m, 3);
+            mixed_uv_backward(d, m->tab, ws_of(in), ws_of(out), dtau, m->stream);
+          } else {
+            Span sp(m, 1);
+            mixed_fb_substep(d, m->tab, m->fl, ws_of(in), ws_of(out), dtau, m->stream);
+          }
           in = out;
         }
         final_sub = in;
       }
+      Span sp(m, 2);
       mixed_finish(d, m->tab, m->fl, ws_of(final_sub), ws_of(m->WSt[0]), w0, S1, dt, m->kmin, m->d_err, m->stream);
     }
     m->cur = 1 - m->cur;
@@ -522,6 +610,7 @@ int enqueue_steps(vibe_gb300_model* m, double dt, int n_sub_in, int n_steps) {
 int read_status(vibe_gb300_model* m) {
   CUDA_OK(cudaMemcpyAsync(m->h_err, m->d_err, sizeof(unsigned), cudaMemcpyDeviceToHost, m->stream));
   CUDA_OK(cudaStreamSynchronize(m->stream));
+  collect_timing(m);
   const unsigned e = *m->h_err;
   CUDA_OK(cudaMemsetAsync(m->d_err, 0, sizeof(unsigned), m->stream));
   if (e & kErrSingular) return fail(VIBE_GB300_ESINGULAR, "tridiagonal pivot below 1e-300");
@@ -565,11 +654,13 @@ int vibe_gb300_model_create(const vibe_gb300_setup* s, int precision, vibe_gb300
   *out = nullptr;
   if (s->nx < 1 || s->ny < 1 || s->nz < 1 || !(s->dx > 0) || !(s->dy > 0) || !(s->z_top > 0))
     return fail(VIBE_GB300_EBADARG, "grid sizes and spacings must be positive");
-  if (precision != VIBE_GB300_FP64 && precision != VIBE_GB300_MIXED)
-    return fail(VIBE_GB300_EBADARG, "precision must be VIBE_GB300_FP64 or VIBE_GB300_MIXED");
+  if (precision != VIBE_GB300_FP64 && precision != VIBE_GB300_MIXED && precision != VIBE_GB300_FP64_EXACT)
+    return fail(VIBE_GB300_EBADARG, "precision must be VIBE_GB300_FP64, _MIXED or _FP64_EXACT");
   if (s->acoustic_mode < 0 || s->acoustic_mode > 2) return fail(VIBE_GB300_EBADARG, "acoustic_mode must be 0, 1 or 2");
   auto* m = new vibe_gb300_model();
   m->su = *s;
+  m->f64 = (precision == VIBE_GB300_FP64_EXACT) ? &kFp64Exact : &kFp64Fast;
+  if (precision == VIBE_GB300_FP64_EXACT) precision = VIBE_GB300_FP64;  // same buffers and schedule
   m->precision = precision;
   auto bail = [&](int rc) { vibe_gb300_model_destroy(m); return rc; };
   const int nx = s->nx, ny = s->ny, nz = s->nz;
@@ -635,8 +726,8 @@ int vibe_gb300_model_create(const vibe_gb300_setup* s, int precision, vibe_gb300
     for (int q = 0; q < NSPECIES && !rc; ++q) rc = dalloc(m, &m->W0[q], nfield);
     for (int b = 0; b < 2 && !rc; ++b)
       for (int q = 0; q < NSPECIES && !rc; ++q) rc = dalloc(m, &m->WSt[b][q], nfield);
-    for (int q = 0; q <= PI && !rc; ++q) rc = dalloc(m, &m->WA[q], nfield);
-    for (int q = 0; q <= PI && !rc; ++q) rc = dalloc(m, &m->WB[q], nfield);
+    for (int q = 0; q < NSPECIES && !rc; ++q) rc = acoustic_field(q) ? dalloc(m, &m->WA[q], nfield) : 0;
+    for (int q = 0; q < NSPECIES && !rc; ++q) rc = acoustic_field(q) ? dalloc(m, &m->WB[q], nfield) : 0;
     rc = rc ? rc : dalloc(m, &m->d_lu, 9 * (size_t)nz);
   }
   if (rc) return bail(rc);
@@ -676,6 +767,8 @@ int vibe_gb300_model_create(const vibe_gb300_setup* s, int precision, vibe_gb300
 void vibe_gb300_model_destroy(vibe_gb300_model* m) {
   if (!m) return;
   if (m->stream) cudaStreamSynchronize(m->stream);
+  collect_timing(m);
+  for (cudaEvent_t e : m->ev_pool) cudaEventDestroy(e);
   for (void* p : m->allocs) cudaFree(p);
   if (m->h_err) cudaFreeHost(m->h_err);
   if (m->h_pin) cudaFreeHost(m->h_pin);
@@ -698,7 +791,7 @@ int vibe_gb300_set_field(vibe_gb300_model* m, int q, const double* host) {
     // every FP32 buffer starts from the same values (ghost line included)
     const size_t n = m->d.plane * (size_t)(m->d.nz + 1) * sizeof(float);
     for (int b = 0; b < 2; ++b) CUDA_OK(cudaMemcpyAsync(m->WSt[b][q], m->W0[q], n, cudaMemcpyDeviceToDevice, m->stream));
-    if (q <= PI) {
+    if (acoustic_field(q)) {
       CUDA_OK(cudaMemcpyAsync(m->WA[q], m->W0[q], n, cudaMemcpyDeviceToDevice, m->stream));
       CUDA_OK(cudaMemcpyAsync(m->WB[q], m->W0[q], n, cudaMemcpyDeviceToDevice, m->stream));
     }
@@ -758,8 +851,29 @@ int vibe_gb300_step(vibe_gb300_model* m, double dt, int n_sub, int n_steps) {
 
 int vibe_gb300_slow_tendency(vibe_gb300_model* m, double* const* host_out) {
   if (!m || !host_out) return fail(VIBE_GB300_EBADARG, "bad argument");
-  if (m->precision != VIBE_GB300_FP64) return fail(VIBE_GB300_EUNSUPPORTED, "slow tendency output is FP64-path only");
-  fp64_slow_tendency(m->d, m->met, m->fl, m->S[m->cur], m->tend, m->scratch, m->stream);
+  if (m->precision == VIBE_GB300_MIXED) {
+    // the stage kernel with no base state writes the raw FP32 tendency
+    if (int rc = sync_working(m)) return rc;
+    WS none;
+    for (int q = 0; q < NSPECIES; ++q) none.f[q] = nullptr;
+    mixed_stage(m->d, m->tab, m->fl, ws_of(m->W0), none, ws_of(m->WSt[1]), nullptr, nullptr, 1.0, false, m->d_err,
+                 m->stream);
+    for (int q = 0; q < NSPECIES; ++q) {
+      int ni = m->d.nx + (q == U), nj = m->d.ny + (q == V), nk = m->d.nz + (q == W);
+      const bool active = q <= QV || m->fl.moist;
+      if (!active) { ni = 0; }
+      mixed_unpack_f32(m->d, m->nsx[q], m->nsy[q], m->nsz[q], ni, nj, nk, m->WSt[1][q], m->d_stage_in, m->stream);
+      CUDA_OK(cudaMemcpyAsync(host_out[q], m->d_stage_in, storage_count(m, q) * sizeof(double), cudaMemcpyDeviceToHost,
+                              m->stream));
+      CUDA_OK(cudaStreamSynchronize(m->stream));
+    }
+    // WSt[1] now holds tendencies: restore its ghost line / inactive species
+    const size_t n = m->d.plane * (size_t)(m->d.nz + 1) * sizeof(float);
+    for (int q = 0; q < NSPECIES; ++q) CUDA_OK(cudaMemcpyAsync(m->WSt[1][q], m->W0[q], n, cudaMemcpyDeviceToDevice, m->stream));
+    CUDA_OK(cudaStreamSynchronize(m->stream));
+    return read_status(m);
+  }
+  m->f64->slow_tendency(m->d, m->met, m->fl, m->S[m->cur], m->tend, m->scratch, m->stream);
   for (int q = 0; q < NSPECIES; ++q) {
     int ni, nj, nk;
     box_of(m, q, ni, nj, nk);
@@ -779,7 +893,7 @@ int vibe_gb300_slow_tendency(vibe_gb300_model* m, double* const* host_out) {
 int vibe_gb300_acoustic_substep(vibe_gb300_model* m, double dtau) {
   if (!m) return fail(VIBE_GB300_EBADARG, "bad argument");
   if (m->precision == VIBE_GB300_FP64) {
-    fp64_fb_substep(m->d, m->met, m->fl, m->S[m->cur], dtau, m->stream);
+    m->f64->fb_substep(m->d, m->met, m->fl, m->S[m->cur], dtau, m->stream);
   } else {
     if (int rc = sync_working(m)) return rc;
     mixed_fb_substep(m->d, m->tab, m->fl, ws_of(m->W0), ws_of(m->WA), (float)dtau, m->stream);
@@ -798,10 +912,10 @@ int vibe_gb300_hevi_substep(vibe_gb300_model* m, double dtau) {
   if (m->precision == VIBE_GB300_FP64) {
     if (m->fl.acoustic_mode == 1) {
       if (int rc = ref_hevi_coefficients(m, dtau)) return rc;
-      fp64_ref_hevi_substep(m->d, m->met, m->S[m->cur], dtau, m->d_tri, m->d_tri + m->d.nz, m->d_tri + 2 * m->d.nz,
+      m->f64->ref_hevi_substep(m->d, m->met, m->S[m->cur], dtau, m->d_tri, m->d_tri + m->d.nz, m->d_tri + 2 * m->d.nz,
                             m->scratch, m->d_err, m->stream);
     } else {
-      fp64_cons_hevi_substep(m->d, m->met, m->fl, m->S[m->cur], m->tmp, m->scratch, dtau, m->d_err, m->stream);
+      m->f64->cons_hevi_substep(m->d, m->met, m->fl, m->S[m->cur], m->tmp, m->scratch, dtau, m->d_err, m->stream);
     }
   } else {
     // single substep: factors for this dtau in stage slot 0
@@ -825,10 +939,67 @@ int vibe_gb300_sponge(vibe_gb300_model* m, double dt) {
   int kmin = m->d.nz + 1;
   for (int k = 0; k < m->d.nz; ++k)
     if (m->hs.sponge[k] > 0.0) { kmin = k; break; }
-  fp64_sponge(m->d, m->met, m->S[m->cur], kmin, dt, m->stream);
+  m->f64->sponge(m->d, m->met, m->S[m->cur], kmin, dt, m->stream);
   if (int rc = sync_working(m)) return rc;
   CUDA_OK(cudaGetLastError());
   return read_status(m);
+}
+
+int vibe_gb300_set_state(vibe_gb300_model* m, const double* const* host, int nspecies) {
+  if (!m || !host || nspecies < 1 || nspecies > NSPECIES) return fail(VIBE_GB300_EBADARG, "bad argument");
+  for (int q = 0; q < nspecies; ++q) {
+    if (!host[q]) continue;
+    double* dst[2] = {m->S[0][q], m->S[1][q]};
+    if (int rc = upload_storage(m, q, host[q], dst, 2)) return rc;
+  }
+  if (m->precision == VIBE_GB300_MIXED) {
+    if (int rc = sync_working(m)) return rc;
+    // the ghost line of rho' and inactive species live in every FP32 buffer
+    const size_t n = m->d.plane * (size_t)(m->d.nz + 1) * sizeof(float);
+    const int last = m->fl.moist ? QG : QV;
+    for (int q = 0; q < nspecies; ++q) {
+      if (!host[q] || !(q == RHO || q > last)) continue;
+      for (int b = 0; b < 2; ++b) CUDA_OK(cudaMemcpyAsync(m->WSt[b][q], m->W0[q], n, cudaMemcpyDeviceToDevice, m->stream));
+      if (acoustic_field(q)) {
+        CUDA_OK(cudaMemcpyAsync(m->WA[q], m->W0[q], n, cudaMemcpyDeviceToDevice, m->stream));
+        CUDA_OK(cudaMemcpyAsync(m->WB[q], m->W0[q], n, cudaMemcpyDeviceToDevice, m->stream));
+      }
+    }
+  }
+  CUDA_OK(cudaGetLastError());
+  return 0;
+}
+
+int vibe_gb300_get_state(vibe_gb300_model* m, double* const* host, int nspecies) {
+  if (!m || !host || nspecies < 1 || nspecies > NSPECIES) return fail(VIBE_GB300_EBADARG, "bad argument");
+  for (int q = 0; q < nspecies; ++q) {
+    if (!host[q]) continue;
+    int ni, nj, nk;
+    box_of(m, q, ni, nj, nk);
+    k_unpack<<<1024, 256, 0, m->stream>>>(m->d, m->nsx[q], m->nsy[q], m->nsz[q], ni, nj, nk, m->S[m->cur][q],
+                                          m->d_stage_in);
+    CUDA_OK(cudaMemcpyAsync(host[q], m->d_stage_in, storage_count(m, q) * sizeof(double), cudaMemcpyDeviceToHost,
+                            m->stream));
+  }
+  CUDA_OK(cudaGetLastError());
+  return 0;
+}
+
+int vibe_gb300_set_kernel_timing(vibe_gb300_model* m, int enable) {
+  if (!m) return fail(VIBE_GB300_EBADARG, "bad argument");
+  CUDA_OK(cudaStreamSynchronize(m->stream));
+  collect_timing(m);
+  m->timing = enable != 0;
+  for (int c = 0; c < vibe_gb300_model::kClasses; ++c) { m->class_ms[c] = 0.0; m->class_n[c] = 0; }
+  return 0;
+}
+
+int vibe_gb300_kernel_times(vibe_gb300_model* m, double* ms, long* count, int nclass) {
+  if (!m || !ms || !count) return fail(VIBE_GB300_EBADARG, "bad argument");
+  CUDA_OK(cudaStreamSynchronize(m->stream));
+  collect_timing(m);
+  for (int c = 0; c < nclass && c < vibe_gb300_model::kClasses; ++c) { ms[c] = m->class_ms[c]; count[c] = m->class_n[c]; }
+  return 0;
 }
 
 int vibe_gb300_device_field(vibe_gb300_model* m, int q, double** ptr, int* pitch) {

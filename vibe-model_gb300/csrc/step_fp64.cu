@@ -8,6 +8,16 @@
 // exact baseline the mixed path is measured against.
 #include "step_kernels.cuh"
 
+// Built twice: as is (FMA contraction on, the fast FP64 path) and with
+// -DVGB_FP64_EXACT --fmad=false, which keeps every multiply and add
+// separately rounded in the reference's operation order, so results equal
+// the serial reference bit for bit.
+#ifdef VGB_FP64_EXACT
+#define FP64_FN(name) name##_exact
+#else
+#define FP64_FN(name) name
+#endif
+
 namespace vgb {
 namespace {
 
@@ -617,7 +627,7 @@ static MS to_ms(double* const* f) {
   return s;
 }
 
-void fp64_slow_tendency(const Dims& d, const Metric& m, const Flags& fl, double* const* st, double* const* tend,
+void FP64_FN(fp64_slow_tendency)(const Dims& d, const Metric& m, const Flags& fl, double* const* st, double* const* tend,
                         double* lap_scratch, cudaStream_t stream) {
   const CS s = to_cs(st);
   k_tend_u<<<grid3(d, d.nx + 1, d.ny, d.nz, kBlk), kBlk, 0, stream>>>(d, m, fl, s, tend[U]);
@@ -631,7 +641,7 @@ void fp64_slow_tendency(const Dims& d, const Metric& m, const Flags& fl, double*
   k_tend_cells<<<grid3(d, d.nx, d.ny, d.nz, kBlk), kBlk, 0, stream>>>(d, m, fl, s, to_ms(tend), lapf);
 }
 
-void fp64_stage_update(const Dims& d, double* const* s0, double* const* tend, double a, double* const* out,
+void FP64_FN(fp64_stage_update)(const Dims& d, double* const* s0, double* const* tend, double a, double* const* out,
                        cudaStream_t stream) {
   for (int q = 0; q < NSPECIES; ++q) {
     const int ni = d.nx + (q == U), nj = d.ny + (q == V), nk = d.nz + (q == W);
@@ -639,14 +649,14 @@ void fp64_stage_update(const Dims& d, double* const* s0, double* const* tend, do
   }
 }
 
-void fp64_fb_substep(const Dims& d, const Metric& m, const Flags& fl, double* const* st, double dtau,
+void FP64_FN(fp64_fb_substep)(const Dims& d, const Metric& m, const Flags& fl, double* const* st, double dtau,
                      cudaStream_t stream) {
   const CS s = to_cs(st);
   k_fb_mass<<<grid3(d, d.nx, d.ny, d.nz, kBlk), kBlk, 0, stream>>>(d, m, s, st[RHO], st[PI], dtau);
   k_fb_mom<<<grid3(d, d.nx + 1, d.ny + 1, d.nz + 1, kBlk), kBlk, 0, stream>>>(d, m, fl, s, st[U], st[V], st[W], dtau);
 }
 
-void fp64_ref_hevi_substep(const Dims& d, const Metric& m, double* const* st, double dtau, const double* ta,
+void FP64_FN(fp64_ref_hevi_substep)(const Dims& d, const Metric& m, double* const* st, double dtau, const double* ta,
                            const double* tb, const double* tc, double* scratch, unsigned* err, cudaStream_t stream) {
   const CS s = to_cs(st);
   double* drho = scratch;
@@ -658,7 +668,7 @@ void fp64_ref_hevi_substep(const Dims& d, const Metric& m, double* const* st, do
   k_rhevi_mom<<<grid3(d, d.nx + 1, d.ny + 1, d.nz + 1, kBlk), kBlk, 0, stream>>>(d, m, s, st[U], st[V], st[W], dtau);
 }
 
-void fp64_cons_hevi_substep(const Dims& d, const Metric& m, const Flags& fl, double* const* st, double* const* tmp,
+void FP64_FN(fp64_cons_hevi_substep)(const Dims& d, const Metric& m, const Flags& fl, double* const* st, double* const* tmp,
                             double* scratch, double dtau, unsigned* err, cudaStream_t stream) {
   // column solve reads the old state, writes w/rho/pi into tmp, copied back
   const CS s = to_cs(st);
@@ -672,12 +682,12 @@ void fp64_cons_hevi_substep(const Dims& d, const Metric& m, const Flags& fl, dou
   k_uv_backward<<<grid3(d, d.nx + 1, d.ny + 1, d.nz, kBlk), kBlk, 0, stream>>>(d, m, fl, s, st[U], st[V], dtau);
 }
 
-void fp64_sponge(const Dims& d, const Metric& m, double* const* st, int kmin, double dt, cudaStream_t stream) {
+void FP64_FN(fp64_sponge)(const Dims& d, const Metric& m, double* const* st, int kmin, double dt, cudaStream_t stream) {
   if (kmin > d.nz) return;
   k_sponge<<<grid3(d, d.nx + 1, d.ny + 1, d.nz + 1 - kmin, kBlk), kBlk, 0, stream>>>(d, m, to_ms(st), kmin, dt);
 }
 
-void fp64_nonfinite(const Dims& d, double* const* st, unsigned* err, cudaStream_t stream) {
+void FP64_FN(fp64_nonfinite)(const Dims& d, double* const* st, unsigned* err, cudaStream_t stream) {
   k_nonfinite<<<grid3(d, d.nx + 1, d.ny + 1, d.nz + 1, kBlk), kBlk, 0, stream>>>(d, to_cs(st), err);
 }
 

@@ -18,6 +18,20 @@ void fp64_cons_hevi_substep(const Dims& d, const Metric& m, const Flags& fl, dou
 void fp64_sponge(const Dims& d, const Metric& m, double* const* st, int kmin, double dt, cudaStream_t stream);
 void fp64_nonfinite(const Dims& d, double* const* st, unsigned* err, cudaStream_t stream);
 
+// ---- bit-exact FP64 path (step_fp64.cu built with --fmad=false) ----
+void fp64_slow_tendency_exact(const Dims& d, const Metric& m, const Flags& fl, double* const* st, double* const* tend,
+                        double* lap_scratch, cudaStream_t stream);
+void fp64_stage_update_exact(const Dims& d, double* const* s0, double* const* tend, double a, double* const* out,
+                       cudaStream_t stream);
+void fp64_fb_substep_exact(const Dims& d, const Metric& m, const Flags& fl, double* const* st, double dtau,
+                     cudaStream_t stream);
+void fp64_ref_hevi_substep_exact(const Dims& d, const Metric& m, double* const* st, double dtau, const double* ta,
+                           const double* tb, const double* tc, double* scratch, unsigned* err, cudaStream_t stream);
+void fp64_cons_hevi_substep_exact(const Dims& d, const Metric& m, const Flags& fl, double* const* st, double* const* tmp,
+                            double* scratch, double dtau, unsigned* err, cudaStream_t stream);
+void fp64_sponge_exact(const Dims& d, const Metric& m, double* const* st, int kmin, double dt, cudaStream_t stream);
+void fp64_nonfinite_exact(const Dims& d, double* const* st, unsigned* err, cudaStream_t stream);
+
 // ---- mixed path (step_mixed.cu): FP64 state, FP32 working state ----
 // Horizontally uniform reference state on flat terrain: every coefficient
 // is a function of k only and lives in these FP32 tables (device).
@@ -52,8 +66,13 @@ void mixed_fb_substep(const Dims& d, const Tab& t, const Flags& fl, const WS& wi
                       cudaStream_t stream);
 void mixed_hevi_substep(const Dims& d, const Tab& t, const Flags& fl, const WS& win, const WS& wout, float dtau,
                         const float* lu /* 3*nz: a, cprime, inv_denom */, unsigned* err, cudaStream_t stream);
+void mixed_hevi_column(const Dims& d, const Tab& t, const Flags& fl, const WS& win, const WS& wout, float dtau,
+                       const float* lu, cudaStream_t stream);
+void mixed_uv_backward(const Dims& d, const Tab& t, const WS& win, const WS& wout, float dtau, cudaStream_t stream);
 void mixed_finish(const Dims& d, const Tab& t, const Flags& fl, const WS& wfin, const WS& wst, const WS& w0,
                   double* const* ss, double dt, int kmin, unsigned* err, cudaStream_t stream);
+void mixed_unpack_f32(const Dims& d, int nsx, int nsy, int nsz, int ni, int nj, int nk, const float* src, double* dst,
+                      cudaStream_t stream);
 void mixed_to_working(const Dims& d, const Tab& t, double* const* s, const WS& w, cudaStream_t stream);
 
 }  // namespace vgb

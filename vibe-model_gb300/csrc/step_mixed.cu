@@ -132,7 +132,7 @@ __global__ void __launch_bounds__(128) k_mx_stage(Dims d, Tab t, Flags fl, WS wi
   const size_t c = IX(i, j, k);
   bool bad = false;
   auto emit = [&](int q, float r) {
-    const float o = w0.f[q][c] + dts * r;
+    const float o = (w0.f[q] != nullptr) ? w0.f[q][c] + dts * r : r;  // no base: raw tendency
     wout.f[q][c] = o;
     bad |= !isfinite(o);
     if (kFP64Out) ss.f[q][c] = s0.f[q][c] + dtd * (double)r;
@@ -375,6 +375,18 @@ __global__ void k_mx_finish(Dims d, Tab t, Flags fl, WS wfin, WS wst, WS w0, MS6
   if (bad) atomicOr(err, (unsigned)kErrNonFinite);
 }
 
+// FP32 field (device layout) -> FP64 FieldT storage (zeros outside the box)
+__global__ void k_mx_unpack_f32(Dims d, int nsx, int nsy, int nsz, int ni, int nj, int nk, const float* __restrict__ src,
+                                double* __restrict__ dst) {
+  const size_t n = (size_t)nsx * nsy * nsz;
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x) {
+    const int ii = (int)(e % nsx) - 4, jj = (int)((e / nsx) % nsy) - 4, kk = (int)(e / ((size_t)nsx * nsy)) - 4;
+    double v = 0.0;
+    if (ii >= 0 && ii < ni && jj >= 0 && jj < nj && kk >= 0 && kk < nk) v = (double)src[d.idx(ii, jj, kk)];
+    dst[e] = v;
+  }
+}
+
 // FP64 state -> FP32 working copy in perturbation form, incl. ghosts.
 __global__ void k_mx_to_working(Dims d, Tab t, CS64 s, WS w) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -427,15 +439,29 @@ void mixed_fb_substep(const Dims& d, const Tab& t, const Flags& fl, const WS& wi
   k_mx_fb_mom<<<g3(d.nx + 1, d.ny + 1, d.nz + 1, b), b, 0, stream>>>(d, t, win, wout, dtau, 1);
 }
 
+void mixed_hevi_column(const Dims& d, const Tab& t, const Flags& fl, const WS& win, const WS& wout, float dtau,
+                       const float* lu, cudaStream_t stream) {
+  const dim3 bc(32, 2);
+  const size_t smem = (size_t)(3 * d.nz + 1) * bc.x * bc.y * sizeof(float);
+  static size_t smem_set = 0;  // opt in above 48 KB once per size
+  if (smem > 48 * 1024 && smem > smem_set) {
+    cudaFuncSetAttribute(k_mx_hevi_col, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    smem_set = smem;
+  }
+  k_mx_hevi_col<<<dim3((d.nx + bc.x - 1) / bc.x, (d.ny + bc.y - 1) / bc.y), bc, smem, stream>>>(d, t, fl, win, wout,
+                                                                                               dtau, lu);
+}
+
+void mixed_uv_backward(const Dims& d, const Tab& t, const WS& win, const WS& wout, float dtau, cudaStream_t stream) {
+  const dim3 b(32, 4);
+  k_mx_fb_mom<<<g3(d.nx + 1, d.ny + 1, d.nz, b), b, 0, stream>>>(d, t, win, wout, dtau, 0);
+}
+
 void mixed_hevi_substep(const Dims& d, const Tab& t, const Flags& fl, const WS& win, const WS& wout, float dtau,
                         const float* lu, unsigned* err, cudaStream_t stream) {
   (void)err;
-  const dim3 bc(32, 2);
-  const size_t smem = (size_t)(3 * d.nz + 1) * bc.x * bc.y * sizeof(float);
-  k_mx_hevi_col<<<dim3((d.nx + bc.x - 1) / bc.x, (d.ny + bc.y - 1) / bc.y), bc, smem, stream>>>(d, t, fl, win, wout,
-                                                                                               dtau, lu);
-  const dim3 b(32, 4);
-  k_mx_fb_mom<<<g3(d.nx + 1, d.ny + 1, d.nz, b), b, 0, stream>>>(d, t, win, wout, dtau, 0);
+  mixed_hevi_column(d, t, fl, win, wout, dtau, lu, stream);
+  mixed_uv_backward(d, t, win, wout, dtau, stream);
 }
 
 void mixed_finish(const Dims& d, const Tab& t, const Flags& fl, const WS& wfin, const WS& wst, const WS& w0,
@@ -443,6 +469,11 @@ void mixed_finish(const Dims& d, const Tab& t, const Flags& fl, const WS& wfin, 
   (void)dt; (void)kmin;
   const dim3 b(32, 4);
   k_mx_finish<<<g3(d.nx + 1, d.ny + 1, d.nz + 1, b), b, 0, stream>>>(d, t, fl, wfin, wst, w0, ms64(ss), err);
+}
+
+void mixed_unpack_f32(const Dims& d, int nsx, int nsy, int nsz, int ni, int nj, int nk, const float* src, double* dst,
+                      cudaStream_t stream) {
+  k_mx_unpack_f32<<<1024, 256, 0, stream>>>(d, nsx, nsy, nsz, ni, nj, nk, src, dst);
 }
 
 void mixed_to_working(const Dims& d, const Tab& t, double* const* s, const WS& w, cudaStream_t stream) {

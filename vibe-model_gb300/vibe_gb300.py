@@ -21,7 +21,7 @@ LIB_PATH = os.path.join(HERE, "libvibe_gb300.so")
 SPECIES = ["u", "v", "w", "rho", "theta", "pi", "qv", "qc", "qr", "qi", "qs", "qg"]
 NSPECIES = 12
 HALO = 4
-FP64, MIXED = 0, 1
+FP64, MIXED, FP64_EXACT = 0, 1, 2
 _D, _I = ctypes.c_double, ctypes.c_int
 
 if not os.path.exists(LIB_PATH):
@@ -86,6 +86,10 @@ _sigs = {
     "vibe_gb300_hevi_substep": (_I, [_vp, _D]),
     "vibe_gb300_sponge": (_I, [_vp, _D]),
     "vibe_gb300_device_field": (_I, [_vp, _I, ctypes.POINTER(_dp), ctypes.POINTER(_I)]),
+    "vibe_gb300_set_state": (_I, [_vp, ctypes.POINTER(_dp), _I]),
+    "vibe_gb300_get_state": (_I, [_vp, ctypes.POINTER(_dp), _I]),
+    "vibe_gb300_set_kernel_timing": (_I, [_vp, _I]),
+    "vibe_gb300_kernel_times": (_I, [_vp, _dp, ctypes.POINTER(ctypes.c_long), _I]),
     "vibe_gb300_stream": (_vp, [_vp]),
     "vibe_gb300_launches_per_step": (_I, [_vp, _I]),
     "vibe_gb300_last_error": (ctypes.c_char_p, []),
@@ -227,6 +231,25 @@ class Model:
 
     def sponge(self, dt):
         _check(lib.vibe_gb300_sponge(self.h, dt))
+
+    def set_state_ptrs(self, ptrs):
+        """Asynchronous bulk upload from host addresses (ints; None skips)."""
+        arr = (_dp * len(ptrs))(*[ctypes.cast(p, _dp) if p else None for p in ptrs])
+        _check(lib.vibe_gb300_set_state(self.h, arr, len(ptrs)))
+
+    def get_state_ptrs(self, ptrs):
+        arr = (_dp * len(ptrs))(*[ctypes.cast(p, _dp) if p else None for p in ptrs])
+        _check(lib.vibe_gb300_get_state(self.h, arr, len(ptrs)))
+
+    def set_kernel_timing(self, on):
+        _check(lib.vibe_gb300_set_kernel_timing(self.h, 1 if on else 0))
+
+    def kernel_times(self):
+        """{class: (total_ms, n_spans)} for 0 stage, 1 substep, 2 finish."""
+        ms = (ctypes.c_double * 4)()
+        n = (ctypes.c_long * 4)()
+        _check(lib.vibe_gb300_kernel_times(self.h, ms, n, 4))
+        return {c: (ms[c], n[c]) for c in range(4)}
 
     def stream(self):
         return lib.vibe_gb300_stream(self.h)
