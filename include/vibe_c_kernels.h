@@ -88,6 +88,23 @@ int vibe_tridiagonal_solve_batched_f64_dev(const double *a, const double *b,
                                            const double *c, const double *d,
                                            int n, int n_sys, double *x,
                                            int *status, vibe_stream_t stream);
+/* Allocation-free form of vibe_tridiagonal_solve_batched_f64_dev; it has no
+ * counterpart in the reference. For callers that may not allocate device
+ * memory (a host model whose own allocator owns the device memory, or a
+ * time-critical loop where cudaMalloc/cudaFree would synchronise the device):
+ * the per-system workspace lives in a fixed device array of 2^18 doubles
+ * (2 MiB, held on every GPU that loads the library until exit), so
+ * n * n_sys must not exceed 262144 (larger requests return
+ * VIBE_C_ERR_BAD_ARG; vibe_c_last_error() says why). Inputs and outputs are
+ * device pointers as in the _dev form. The first call on each device
+ * resolves the array's device address (cudaGetSymbolAddress); make that
+ * first call before any stream capture. All calls share the one array:
+ * calls whose kernels can overlap on the GPU (different streams, no
+ * ordering between them) race on it. */
+int vibe_tridiagonal_solve_batched_f64_dev_noalloc(const double *a, const double *b,
+                                                   const double *c, const double *d,
+                                                   int n, int n_sys, double *x,
+                                                   int *status, vibe_stream_t stream);
 /* Host-pointer batched form; returns the first non-zero per-system code. */
 int vibe_tridiagonal_solve_batched_f64(const double *a, const double *b,
                                        const double *c, const double *d, int n,

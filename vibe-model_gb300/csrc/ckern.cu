@@ -312,6 +312,24 @@ __global__ void k_flux_adv(const double* __restrict__ q, const double* __restric
   }
 }
 
+// ---- allocation-free batched Thomas ------------------------------------
+// Some callers of this library may not allocate device memory at all: a host
+// model whose own allocator has reserved the device's memory and forbids any
+// other allocation, or a time-critical step loop in which a cudaMalloc or
+// cudaFree (both can synchronise the whole device) is not acceptable. For
+// them, vibe_tridiagonal_solve_batched_f64_dev_noalloc keeps its Thomas
+// workspace (the modified super-diagonal, n doubles per system) in this
+// fixed device array instead of the allocated scratch buffer. The array is
+// sized here, once, and every GPU that loads the library holds it until the
+// process exits.
+constexpr size_t kNoAllocThomasDoubles = (size_t)1 << 18;  // 2 MiB: n * n_sys <= 262144
+static __device__ __align__(256) double g_noalloc_thomas_work[kNoAllocThomasDoubles];
+// Device address of that array per device. Host code only sees a host-side
+// stand-in for the symbol; the address a kernel may use comes from
+// cudaGetSymbolAddress, called with the device current.
+std::mutex g_noalloc_mu;
+double* g_noalloc_ptr[64] = {};
+
 constexpr int kRedBlocks = 304;  // 2 x 152 SMs
 constexpr int kRedThreads = 256;
 
@@ -329,6 +347,34 @@ int vibe_tridiagonal_solve_batched_f64_dev(const double* a, const double* b, con
   if (!work) { g_cerr = "scratch allocation failed"; return VIBE_C_ERR_DEVICE; }
   k_thomas_batched<<<(n_sys + 127) / 128, 128, 0, (cudaStream_t)stream>>>(a, b, c, d, n, n_sys, x, work, status);
   return device_ok(cudaGetLastError(), "thomas launch") ? VIBE_C_OK : VIBE_C_ERR_DEVICE;
+}
+
+int vibe_tridiagonal_solve_batched_f64_dev_noalloc(const double* a, const double* b, const double* c,
+                                                   const double* d, int n, int n_sys, double* x, int* status,
+                                                   vibe_stream_t stream) {
+  if (n <= 0 || n_sys < 0 || b == nullptr || d == nullptr || x == nullptr) return VIBE_C_ERR_BAD_ARG;
+  if ((size_t)n * (size_t)n_sys > kNoAllocThomasDoubles) {
+    g_cerr = "vibe_tridiagonal_solve_batched_f64_dev_noalloc: n * n_sys = " + std::to_string((size_t)n * n_sys) +
+             " exceeds the fixed workspace of " + std::to_string(kNoAllocThomasDoubles) + " doubles";
+    return VIBE_C_ERR_BAD_ARG;
+  }
+  if (n_sys == 0) return VIBE_C_OK;
+  const int dev = cur_dev();
+  if (dev < 0 || dev >= 64) { g_cerr = "device ordinal out of range"; return VIBE_C_ERR_DEVICE; }
+  double* work = nullptr;
+  {
+    // set-up on the first call per device: resolve the array's device address
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    if (!g_noalloc_ptr[dev]) {
+      void* p = nullptr;
+      if (!device_ok(cudaGetSymbolAddress(&p, g_noalloc_thomas_work), "cudaGetSymbolAddress")) return VIBE_C_ERR_DEVICE;
+      g_noalloc_ptr[dev] = (double*)p;
+    }
+    work = g_noalloc_ptr[dev];
+  }
+  // the workspace needs no clearing: every system writes cp[k] before it reads it
+  k_thomas_batched<<<(n_sys + 127) / 128, 128, 0, (cudaStream_t)stream>>>(a, b, c, d, n, n_sys, x, work, status);
+  return device_ok(cudaGetLastError(), "thomas (no-alloc) launch") ? VIBE_C_OK : VIBE_C_ERR_DEVICE;
 }
 
 int vibe_tridiagonal_solve_batched_f64(const double* a, const double* b, const double* c, const double* d, int n,
