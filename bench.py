@@ -219,6 +219,10 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--nx", type=int, default=NX, help="domain size (profiling runs use smaller cases)")
+    ap.add_argument("--ny", type=int, default=NY)
+    ap.add_argument("--only", choices=["all", "mixed"], default="all",
+                    help="mixed: time the mixed path only (no e2e, no FP64 leg)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -257,12 +261,13 @@ def main():
         return float(t.item())
 
     import vibe_gb300 as vg
-    setup = case_setup(vg.Setup)
-    cells = NX * NY * NZ
+    setup = case_setup(vg.Setup, args.nx, args.ny)
+    cells = args.nx * args.ny * NZ
 
     def make(prec):
         m = vg.Model(setup, prec)
-        th, pi = perturbed_state(setup, m.get(4), m.get(3), m.zeta(), seed=1 + rank)
+        th, pi = perturbed_state(setup, m.get(4), m.get(3), m.zeta(), seed=1 + rank,
+                                 nx_full=args.nx, ny_full=args.ny)
         m.set(4, th)
         m.set(5, pi)
         return m
@@ -289,6 +294,11 @@ def main():
     ms_mx = max_over_ranks(ms_mx)
     launches = mx.launches_per_step(NSUB) * args.steps
 
+    if args.only == "mixed":
+        mx.close()
+        print(json.dumps({"only": "mixed", "cells": cells, "ms_per_step": ms_mx / args.steps,
+                          "value": world * cells * args.steps / (ms_mx * 1e-3), "kernel_ms": ktimes}))
+        return
     # ---- end to end through the public API with host buffers ----
     pinned = [torch.empty(mx.size(sp), dtype=torch.float64, pin_memory=True) for sp in range(7)]
     ptrs = [p.data_ptr() for p in pinned]

@@ -74,62 +74,58 @@ __device__ __forceinline__ float gradc(float m3, float m2, float m1, float p1, f
   }
 }
 
-// scalar tendency of species q at cell (i,j,k); shift_theta: q is theta'
-__device__ float scalar_tend(const Dims& d, const Tab& t, const Flags& fl, const WS& win, int q, int i, int j, int k,
-                             bool is_theta) {
-  const float qc = WI(q, i, j, k);
-  const float* sh = t.t0d + 6 * k;  // theta0(clamp(k+m)) - theta0(k), m=-3..2
-  auto zq = [&](int m) {          // vertical stencil value shifted by theta0(k)
-    const float v = WC(q, i, j, k + m);
-    return is_theta ? v + sh[m + 3] : v;
-  };
-  const float u_w = WI(U, i, j, k), u_e = WI(U, i + 1, j, k);
-  const float v_s = WI(V, i, j, k), v_n = WI(V, i, j + 1, k);
-  const float w_b = WI(W, i, j, k), w_t = WI(W, i, j, k + 1);
-  const float idz = t.idza[k];
-  if (fl.weno_scalars) {
-    const float xm3 = WC(q, i - 3, j, k), xm2 = WC(q, i - 2, j, k), xm1 = WC(q, i - 1, j, k);
-    const float xp1 = WC(q, i + 1, j, k), xp2 = WC(q, i + 2, j, k);
-    const float ym3 = WC(q, i, j - 3, k), ym2 = WC(q, i, j - 2, k), ym1 = WC(q, i, j - 1, k);
-    const float yp1 = WC(q, i, j + 1, k), yp2 = WC(q, i, j + 2, k);
-    const float fe = weno_face_f(xm2, xm1, qc, xp1, xp2, u_e);
-    const float fw = weno_face_f(xm3, xm2, xm1, qc, xp1, u_w);
-    const float fn = weno_face_f(ym2, ym1, qc, yp1, yp2, v_n);
-    const float fs = weno_face_f(ym3, ym2, ym1, qc, yp1, v_s);
-    float ft = 0.f, fb = 0.f;
-    const bool vert = (k + 2 < d.nz || k >= 2);
-    const float zc = is_theta ? qc : qc;  // shift is 0 at m = 0
-    if (vert) {
-      const float zm3 = zq(-3), zm2 = zq(-2), zm1 = zq(-1), zp1 = zq(1), zp2 = zq(2);
-      ft = weno_face_f(zm2, zm1, zc, zp1, zp2, w_t);
-      fb = weno_face_f(zm3, zm2, zm1, zc, zp1, w_b);
-    }
-    float r = -(fe - fw) * t.dx_inv - (fn - fs) * t.dy_inv - (ft - fb) * idz;
-    float div = (u_e - u_w) * t.dx_inv + (v_n - v_s) * t.dy_inv;
-    if (vert) div += (w_t - w_b) * idz;
-    // flux form of (q'+c): -dF(q')/dx - c*div; advective form adds (q'+c)*div
-    if (fl.weno_advective) r += qc * div;
-    else if (is_theta) r -= t.t0c[k] * div;
-    return r;
+// ---- RK stage kernel: slow tendency + s = s0 + dt*R ------------------------
+// Block = 32 x 8 columns at one level k (grid z = k, faces k = 0..nz). Each
+// field's plane at the block's level is staged in shared memory with the
+// halo its stencils need (3 for the WENO / high-order scalar stencils, 1 for
+// the winds, pi', rho'), using the reference's clamps when loading, so a
+// stencil read is a shared-memory load at a fixed offset. Horizontal WENO
+// fluxes are computed once per face into shared memory and differenced;
+// vertical neighbours of a thread's own column come from L2 (the adjacent
+// planes were just read by the blocks of the neighbouring levels).
+constexpr int TX = 32, TY = 8;
+constexpr int W3 = TX + 6, H3 = TY + 6;  // halo-3 tile
+constexpr int W1 = TX + 2, H1 = TY + 2;  // halo-1 tile
+
+template <int H>
+__device__ __forceinline__ void load_tile(float* __restrict__ dst, const float* __restrict__ src, const Dims& d,
+                                          int i0, int j0, int k, int xmax, int ymax) {
+  constexpr int Wt = TX + 2 * H, Ht = TY + 2 * H;
+  const float* __restrict__ base = src + (size_t)k * d.plane;
+  for (int e = threadIdx.y * TX + threadIdx.x; e < Wt * Ht; e += TX * TY) {
+    const int tx = e % Wt, ty = e / Wt;
+    const int gi = iclamp(i0 - H + tx, 0, xmax), gj = iclamp(j0 - H + ty, 0, ymax);
+    dst[e] = base[(size_t)gj * d.P + gi];
   }
-  const float ua = 0.5f * (u_w + u_e), va = 0.5f * (v_s + v_n), wa = 0.5f * (w_b + w_t);
-  const float gx = gradc(WC(q, i - 3, j, k), WC(q, i - 2, j, k), WC(q, i - 1, j, k), WC(q, i + 1, j, k),
-                         WC(q, i + 2, j, k), WC(q, i + 3, j, k), t.dx_inv, fl.advection);
-  const float gy = gradc(WC(q, i, j - 3, k), WC(q, i, j - 2, k), WC(q, i, j - 1, k), WC(q, i, j + 1, k),
-                         WC(q, i, j + 2, k), WC(q, i, j + 3, k), t.dy_inv, fl.advection);
-  const float gz = (zq(1) - zq(-1)) * (0.5f * idz);
-  return -(ua * gx + va * gy + wa * gz);
 }
 
 template <bool kFP64Out>
-__global__ void __launch_bounds__(128) k_mx_stage(Dims d, Tab t, Flags fl, WS win, WS w0, WS wout, CS64 s0, MS64 ss,
+__global__ void __launch_bounds__(256) k_mx_stage(Dims d, Tab t, Flags fl, const __grid_constant__ WS win,
+                                                  const __grid_constant__ WS w0, const __grid_constant__ WS wout,
+                                                  const __grid_constant__ CS64 s0, const __grid_constant__ MS64 ss,
                                                   float dts, double dtd, unsigned* err) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  const int j = blockIdx.y * blockDim.y + threadIdx.y;
-  const int k = blockIdx.z;
-  if (i > d.nx || j > d.ny || k > d.nz) return;
+  __shared__ float sQ[H3 * W3];            // scalar (theta' or q) at level kc, halo 3
+  __shared__ float sU[H1 * W1], sV[H1 * W1], sWk[H1 * W1], sP[H1 * W1], sR[H1 * W1], sT[H3 * W3];
+  __shared__ float sFx[TY * (TX + 1)], sFy[(TY + 1) * TX];
   const int nx = d.nx, ny = d.ny, nz = d.nz;
-  const size_t c = IX(i, j, k);
+  const int i0 = blockIdx.x * TX, j0 = blockIdx.y * TY, k = blockIdx.z;
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  const int i = i0 + tx, j = j0 + ty;
+  const int kc = imin(k, nz - 1), km = imax(k - 1, 0);
+  const size_t P = d.P, pl = d.plane;
+  const bool cells_here = k < nz;
+  // stage the planes (clamp ranges: cells [0,nx-1]x[0,ny-1], u faces
+  // [0,nx]x[0,ny-1], v faces [0,nx-1]x[0,ny], rho' incl. its ghost line)
+  load_tile<3>(sT, win.f[THETA], d, i0, j0, kc, nx - 1, ny - 1);
+  load_tile<1>(sU, win.f[U], d, i0, j0, kc, nx, ny - 1);
+  load_tile<1>(sV, win.f[V], d, i0, j0, kc, nx - 1, ny);
+  load_tile<1>(sWk, win.f[W], d, i0, j0, k, nx - 1, ny - 1);
+  load_tile<1>(sP, win.f[PI], d, i0, j0, kc, nx - 1, ny - 1);
+  load_tile<1>(sR, win.f[RHO], d, i0, j0, kc, nx, ny);
+  __syncthreads();
+#define T3(a, gi, gj) a[((gj) - j0 + 3) * W3 + ((gi) - i0 + 3)]
+#define T1(a, gi, gj) a[((gj) - j0 + 1) * W1 + ((gi) - i0 + 1)]
+  const size_t c = (size_t)k * pl + (size_t)j * P + i;
   bool bad = false;
   auto emit = [&](int q, float r) {
     const float o = (w0.f[q] != nullptr) ? w0.f[q][c] + dts * r : r;  // no base: raw tendency
@@ -138,82 +134,167 @@ __global__ void __launch_bounds__(128) k_mx_stage(Dims d, Tab t, Flags fl, WS wi
     if (kFP64Out) ss.f[q][c] = s0.f[q][c] + dtd * (double)r;
   };
   const float cp = (float)kCp;
-  if (j < ny && k < nz) {  // u face
-    const int ip = imin(i, nx - 1), im = imax(i - 1, 0);
-    const int jp1 = imin(j + 1, ny - 1), jm1 = imax(j - 1, 0);
-    const float uc = 0.5f * (WI(U, im, j, k) + WI(U, ip, j, k));
-    const float ux = (WI(U, ip, j, k) - WI(U, im, j, k)) * t.dx_inv;
-    const float uy = (WI(U, ip, jp1, k) - WI(U, ip, jm1, k)) * (0.5f * t.dy_inv);
-    const float uz = (WI(U, ip, j, imin(k + 1, nz - 1)) - WI(U, ip, j, imax(k - 1, 0))) * (0.5f * t.idza[k]);
-    const float vc = 0.25f * (WI(V, im, jm1, k) + WI(V, ip, jm1, k) + WI(V, im, j, k) + WI(V, ip, j, k));
-    const float wc = 0.5f * (WI(W, ip, j, k) + WI(W, ip, j, imin(k + 1, nz - 1)));
-    float r = -(uc * ux + vc * uy + wc * uz);
-    if (fl.coriolis) r += (fl.coriolis == 2 ? t.f0 + t.beta * (((float)j + 0.5f) * t.dy - 0.5f * (float)ny * t.dy) : t.f0) * vc;
-    r -= cp * (0.5f * (WI(THETA, im, j, k) + WI(THETA, ip, j, k))) * (WI(PI, ip, j, k) - WI(PI, im, j, k)) * t.dx_inv;
-    emit(U, r);
-  }
-  if (i < nx && k < nz) {  // v face
-    const int jp = imin(j, ny - 1), jm = imax(j - 1, 0);
-    const int ip1 = imin(i + 1, nx - 1), im1 = imax(i - 1, 0);
-    const float vc = 0.5f * (WI(V, i, jm, k) + WI(V, i, jp, k));
-    const float vy = (WI(V, i, jp, k) - WI(V, i, jm, k)) * t.dy_inv;
-    const float vx = (WI(V, ip1, jp, k) - WI(V, im1, jp, k)) * (0.5f * t.dx_inv);
-    const float vz = (WI(V, i, jp, imin(k + 1, nz - 1)) - WI(V, i, jp, imax(k - 1, 0))) * (0.5f * t.idza[k]);
-    const float uc = 0.25f * (WI(U, im1, jm, k) + WI(U, i, jm, k) + WI(U, im1, jp, k) + WI(U, i, jp, k));
-    const float wc = 0.5f * (WI(W, i, jp, k) + WI(W, i, jp, imin(k + 1, nz - 1)));
-    float r = -(uc * vx + vc * vy + wc * vz);
-    if (fl.coriolis) r -= (fl.coriolis == 2 ? t.f0 + t.beta * (((float)j + 0.5f) * t.dy - 0.5f * (float)ny * t.dy) : t.f0) * uc;
-    r -= cp * (0.5f * (WI(THETA, i, jm, k) + WI(THETA, i, jp, k))) * (WI(PI, i, jp, k) - WI(PI, i, jm, k)) * t.dy_inv;
-    emit(V, r);
-  }
-  if (i < nx && j < ny) {  // w face
-    const int kc = imin(k, nz - 1), km = imax(k - 1, 0);
-    const int ip1 = imin(i + 1, nx - 1), im1 = imax(i - 1, 0);
-    const int jp1 = imin(j + 1, ny - 1), jm1 = imax(j - 1, 0);
-    const float wc = 0.5f * (WI(W, i, j, kc) + WI(W, i, j, k));
-    const float wz = (WI(W, i, j, k) - WI(W, i, j, km)) * t.idza[kc];
-    const float wx = (WI(W, ip1, j, k) - WI(W, im1, j, k)) * (0.5f * t.dx_inv);
-    const float wy = (WI(W, i, jp1, k) - WI(W, i, jm1, k)) * (0.5f * t.dy_inv);
-    const float uc = 0.5f * (WI(U, i, j, kc) + WI(U, i + 1, j, kc));
-    const float vc = 0.5f * (WI(V, i, j, kc) + WI(V, i, j + 1, kc));
-    float r = -(uc * wx + vc * wy + wc * wz);
-    r -= cp * (0.5f * (WI(THETA, i, j, km) + WI(THETA, i, j, kc))) * (WI(PI, i, j, kc) - WI(PI, i, j, km)) * t.idzw[k];
-    float qcond = 0.f;
-    if (fl.moist) qcond = WI(QC, i, j, kc) + WI(QR, i, j, kc) + WI(QI, i, j, kc) + WI(QS, i, j, kc) + WI(QG, i, j, kc);
-    r += (float)kG * (WI(THETA, i, j, kc) * t.th0inv[kc] + (float)kBuoyMoist * WI(QV, i, j, kc) - qcond);
-    emit(W, r);
-  }
-  if (i < nx && j < ny && k < nz) {  // cells
-    {
-      const float rc = WI(RHO, i, j, k);
-      const float fx = WI(U, i + 1, j, k) * 0.5f * (rc + WI(RHO, i + 1, j, k)) -
-                       WI(U, i, j, k) * 0.5f * (WI(RHO, imax(i - 1, 0), j, k) + rc);
-      const float fy = WI(V, i, j + 1, k) * 0.5f * (rc + WI(RHO, i, j + 1, k)) -
-                       WI(V, i, j, k) * 0.5f * (WI(RHO, i, imax(j - 1, 0), k) + rc);
-      const float fz = WI(W, i, j, k + 1) * 0.5f * (rc + WI(RHO, i, j, imin(k + 1, nz - 1))) -
-                       WI(W, i, j, k) * 0.5f * (WI(RHO, i, j, imax(k - 1, 0)) + rc);
-      emit(RHO, -(fx * t.dx_inv + fy * t.dy_inv + fz * t.idzc[k]));
+  const bool in_x = i <= nx, in_y = j <= ny;
+  if (in_x && in_y) {
+    if (cells_here && j < ny) {  // u face (i, j, k)
+      const int ip = imin(i, nx - 1), im = imax(i - 1, 0);
+      const int jp1 = imin(j + 1, ny - 1), jm1 = imax(j - 1, 0);
+      const float* __restrict__ ucol = win.f[U] + (size_t)j * P + ip;
+      const float uc = 0.5f * (T1(sU, im, j) + T1(sU, ip, j));
+      const float ux = (T1(sU, ip, j) - T1(sU, im, j)) * t.dx_inv;
+      const float uy = (T1(sU, ip, jp1) - T1(sU, ip, jm1)) * (0.5f * t.dy_inv);
+      const float uz = (ucol[(size_t)imin(k + 1, nz - 1) * pl] - ucol[(size_t)imax(k - 1, 0) * pl]) * (0.5f * t.idza[k]);
+      const float vc = 0.25f * (T1(sV, im, jm1) + T1(sV, ip, jm1) + T1(sV, im, j) + T1(sV, ip, j));
+      const float wc = 0.5f * (T1(sWk, ip, j) + win.f[W][(size_t)imin(k + 1, nz - 1) * pl + (size_t)j * P + ip]);
+      float r = -(uc * ux + vc * uy + wc * uz);
+      if (fl.coriolis) r += (fl.coriolis == 2 ? t.f0 + t.beta * (((float)j + 0.5f) * t.dy - 0.5f * (float)ny * t.dy) : t.f0) * vc;
+      r -= cp * (0.5f * (T3(sT, im, j) + T3(sT, ip, j))) * (T1(sP, ip, j) - T1(sP, im, j)) * t.dx_inv;
+      emit(U, r);
     }
-    {
+    if (cells_here && i < nx) {  // v face (i, j, k)
+      const int jp = imin(j, ny - 1), jm = imax(j - 1, 0);
+      const int ip1 = imin(i + 1, nx - 1), im1 = imax(i - 1, 0);
+      const float* __restrict__ vcol = win.f[V] + (size_t)jp * P + i;
+      const float vc = 0.5f * (T1(sV, i, jm) + T1(sV, i, jp));
+      const float vy = (T1(sV, i, jp) - T1(sV, i, jm)) * t.dy_inv;
+      const float vx = (T1(sV, ip1, jp) - T1(sV, im1, jp)) * (0.5f * t.dx_inv);
+      const float vz = (vcol[(size_t)imin(k + 1, nz - 1) * pl] - vcol[(size_t)imax(k - 1, 0) * pl]) * (0.5f * t.idza[k]);
+      const float uc = 0.25f * (T1(sU, im1, jm) + T1(sU, i, jm) + T1(sU, im1, jp) + T1(sU, i, jp));
+      const float wc = 0.5f * (T1(sWk, i, jp) + win.f[W][(size_t)imin(k + 1, nz - 1) * pl + (size_t)jp * P + i]);
+      float r = -(uc * vx + vc * vy + wc * vz);
+      if (fl.coriolis) r -= (fl.coriolis == 2 ? t.f0 + t.beta * (((float)j + 0.5f) * t.dy - 0.5f * (float)ny * t.dy) : t.f0) * uc;
+      r -= cp * (0.5f * (T3(sT, i, jm) + T3(sT, i, jp))) * (T1(sP, i, jp) - T1(sP, i, jm)) * t.dy_inv;
+      emit(V, r);
+    }
+    if (i < nx && j < ny) {  // w face (i, j, k), k = 0..nz
+      const size_t col = (size_t)j * P + i;
+      const float* __restrict__ wcol = win.f[W] + col;
+      const float wkc = wcol[(size_t)kc * pl], wk = T1(sWk, i, j), wkm = wcol[(size_t)km * pl];
+      const float wc = 0.5f * (wkc + wk);
+      const float wz = (wk - wkm) * t.idza[kc];
+      const float wx = (T1(sWk, imin(i + 1, nx - 1), j) - T1(sWk, imax(i - 1, 0), j)) * (0.5f * t.dx_inv);
+      const float wy = (T1(sWk, i, imin(j + 1, ny - 1)) - T1(sWk, i, imax(j - 1, 0))) * (0.5f * t.dy_inv);
+      const float uc = 0.5f * (T1(sU, i, j) + T1(sU, i + 1, j));
+      const float vc = 0.5f * (T1(sV, i, j) + T1(sV, i, j + 1));
+      float r = -(uc * wx + vc * wy + wc * wz);
+      const float thc = T3(sT, i, j), thm = win.f[THETA][(size_t)km * pl + col];
+      const float pic = T1(sP, i, j), pim = win.f[PI][(size_t)km * pl + col];
+      r -= cp * (0.5f * (thm + thc)) * (pic - pim) * t.idzw[k];
+      float qcond = 0.f;
+      const size_t ckc = (size_t)kc * pl + col;
+      if (fl.moist) qcond = win.f[QC][ckc] + win.f[QR][ckc] + win.f[QI][ckc] + win.f[QS][ckc] + win.f[QG][ckc];
+      r += (float)kG * (thc * t.th0inv[kc] + (float)kBuoyMoist * win.f[QV][ckc] - qcond);
+      emit(W, r);
+    }
+    if (cells_here && i < nx && j < ny) {  // mass
+      const float* __restrict__ rcol = win.f[RHO] + (size_t)j * P + i;
+      const float rc = T1(sR, i, j);
+      const float fx = T1(sU, i + 1, j) * 0.5f * (rc + T1(sR, i + 1, j)) -
+                       T1(sU, i, j) * 0.5f * (T1(sR, imax(i - 1, 0), j) + rc);
+      const float fy = T1(sV, i, j + 1) * 0.5f * (rc + T1(sR, i, j + 1)) -
+                       T1(sV, i, j) * 0.5f * (T1(sR, i, imax(j - 1, 0)) + rc);
+      const float fz = win.f[W][c + pl] * 0.5f * (rc + rcol[(size_t)imin(k + 1, nz - 1) * pl]) -
+                       T1(sWk, i, j) * 0.5f * (rcol[(size_t)imax(k - 1, 0) * pl] + rc);
+      emit(RHO, -(fx * t.dx_inv + fy * t.dy_inv + fz * t.idzc[k]));
       float r = 0.f;
       if (fl.div_damp > 0.0) {
-        const float pc = WI(PI, i, j, k);
-        const float lap = (WC(PI, i + 1, j, k) - 2.f * pc + WC(PI, i - 1, j, k)) * (t.dx_inv * t.dx_inv) +
-                          (WC(PI, i, j + 1, k) - 2.f * pc + WC(PI, i, j - 1, k)) * (t.dy_inv * t.dy_inv);
+        const float pc = T1(sP, i, j);
+        const float lap = (T1(sP, imin(i + 1, nx - 1), j) - 2.f * pc + T1(sP, imax(i - 1, 0), j)) * (t.dx_inv * t.dx_inv) +
+                          (T1(sP, i, imin(j + 1, ny - 1)) - 2.f * pc + T1(sP, i, imax(j - 1, 0))) * (t.dy_inv * t.dy_inv);
         r = -(float)fl.div_damp * lap;
       }
       emit(PI, r);
     }
-    // inactive moisture species (moist off) keep their values in every
-    // buffer: zero tendency, so they are neither read nor rewritten here
-    const int last = fl.moist ? QG : QV;
-    for (int q = THETA; q <= last; ++q) {
-      if (q == PI) continue;
-      float r = scalar_tend(d, t, fl, win, q, i, j, k, q == THETA);
-      if (q >= QV && WI(q, i, j, k) <= 0.f && r < 0.f) r = 0.f;
+  }
+  // ---- scalar species: theta' then the moisture species ----
+  if (!cells_here) {
+    if (bad) atomicOr(err, (unsigned)kErrNonFinite);
+    return;  // all threads of the block leave together (k is uniform)
+  }
+  const int last = fl.moist ? QG : QV;
+  const bool cell = i < nx && j < ny;
+  const size_t col = (size_t)j * P + i;
+  for (int q = THETA; q <= last; ++q) {
+    if (q == PI) continue;
+    const bool is_theta = (q == THETA);
+    float* Q = sT;
+    if (!is_theta) {
+      __syncthreads();  // previous species' tiles are no longer read
+      load_tile<3>(sQ, win.f[q], d, i0, j0, kc, nx - 1, ny - 1);
+      Q = sQ;
+      __syncthreads();
+    }
+    float r = 0.f;
+    if (fl.weno_scalars) {
+      // x faces f = i0..i0+TX of rows j0..j0+TY-1, y faces g = j0..j0+TY
+      for (int e = ty * TX + tx; e < TY * (TX + 1); e += TX * TY) {
+        const int f = i0 + e % (TX + 1), row = j0 + e / (TX + 1);
+        float F = 0.f;
+        if (f <= nx && row < ny) {
+          auto Qc = [&](int gi) { return T3(Q, iclamp(gi, 0, nx - 1), row); };
+          F = weno_face_f(Qc(f - 3), Qc(f - 2), Qc(f - 1), Qc(f), Qc(f + 1), T1(sU, f, row));
+        }
+        sFx[e] = F;
+      }
+      for (int e = ty * TX + tx; e < (TY + 1) * TX; e += TX * TY) {
+        const int g = j0 + e / TX, cl = i0 + e % TX;
+        float G = 0.f;
+        if (g <= ny && cl < nx) {
+          auto Qc = [&](int gj) { return T3(Q, cl, iclamp(gj, 0, ny - 1)); };
+          G = weno_face_f(Qc(g - 3), Qc(g - 2), Qc(g - 1), Qc(g), Qc(g + 1), T1(sV, cl, g));
+        }
+        sFy[e] = G;
+      }
+      __syncthreads();
+      if (cell) {
+        const float* __restrict__ qcol = win.f[q] + col;
+        const float* sh = t.t0d + 6 * k;
+        auto zq = [&](int m) {
+          const float v = qcol[(size_t)iclamp(k + m, 0, nz - 1) * pl];
+          return is_theta ? v + sh[m + 3] : v;
+        };
+        const float qc = T3(Q, i, j);
+        const float w_b = T1(sWk, i, j), w_t = win.f[W][c + pl];
+        const float idz = t.idza[k];
+        const bool vert = (k + 2 < nz || k >= 2);
+        float ft = 0.f, fb = 0.f;
+        if (vert) {
+          const float zm3 = zq(-3), zm2 = zq(-2), zm1 = zq(-1), zp1 = zq(1), zp2 = zq(2);
+          ft = weno_face_f(zm2, zm1, qc, zp1, zp2, w_t);
+          fb = weno_face_f(zm3, zm2, zm1, qc, zp1, w_b);
+        }
+        const float fe = sFx[ty * (TX + 1) + tx + 1], fw = sFx[ty * (TX + 1) + tx];
+        const float fn = sFy[(ty + 1) * TX + tx], fs = sFy[ty * TX + tx];
+        r = -(fe - fw) * t.dx_inv - (fn - fs) * t.dy_inv - (ft - fb) * idz;
+        float div = (T1(sU, i + 1, j) - T1(sU, i, j)) * t.dx_inv + (T1(sV, i, j + 1) - T1(sV, i, j)) * t.dy_inv;
+        if (vert) div += (w_t - w_b) * idz;
+        if (fl.weno_advective) r += qc * div;
+        else if (is_theta) r -= t.t0c[k] * div;
+      }
+      __syncthreads();  // sFx/sFy reused by the next species
+    } else if (cell) {
+      const float* __restrict__ qcol = win.f[q] + col;
+      const float* sh = t.t0d + 6 * k;
+      auto zq = [&](int m) {
+        const float v = qcol[(size_t)iclamp(k + m, 0, nz - 1) * pl];
+        return is_theta ? v + sh[m + 3] : v;
+      };
+      auto X = [&](int di) { return T3(Q, iclamp(i + di, 0, nx - 1), j); };
+      auto Y = [&](int dj) { return T3(Q, i, iclamp(j + dj, 0, ny - 1)); };
+      const float ua = 0.5f * (T1(sU, i, j) + T1(sU, i + 1, j)), va = 0.5f * (T1(sV, i, j) + T1(sV, i, j + 1));
+      const float wa = 0.5f * (T1(sWk, i, j) + win.f[W][c + pl]);
+      const float gx = gradc(X(-3), X(-2), X(-1), X(1), X(2), X(3), t.dx_inv, fl.advection);
+      const float gy = gradc(Y(-3), Y(-2), Y(-1), Y(1), Y(2), Y(3), t.dy_inv, fl.advection);
+      const float gz = (zq(1) - zq(-1)) * (0.5f * t.idza[k]);
+      r = -(ua * gx + va * gy + wa * gz);
+    }
+    if (cell) {
+      if (q >= QV && T3(Q, i, j) <= 0.f && r < 0.f) r = 0.f;
       emit(q, r);
     }
   }
+#undef T3
+#undef T1
   if (bad) atomicOr(err, (unsigned)kErrNonFinite);
 }
 
@@ -255,82 +336,107 @@ __global__ void k_mx_fb_mom(Dims d, Tab t, WS win, WS wout, float dtau, int do_w
 }
 
 // ---- consistent vertically implicit substep in FP32 ---------------------
-// One thread per column; the LU factors of the (column-independent)
-// tridiagonal matrix come in lu = [a(k), c'(k), 1/den(k)] x nz.
-// Per-thread scratch in shared memory: dp, S = Dh + (1-b) Dv_old, wt.
-__global__ void k_mx_hevi_col(Dims d, Tab t, Flags fl, WS win, WS wout, float dtau, const float* __restrict__ lu) {
-  extern __shared__ float sm[];
+// One thread per column, 32 x 4 columns per block. The tridiagonal matrix is
+// the same for every column, so its LU factors come precomputed in
+// lu = [a(k), c'(k), 1/den(k)] x nz. Only the forward-elimination values
+// dp(k) are kept on chip (one float per level and column in shared memory:
+// 40 KB per block at nz = 80, so 5 blocks -- 20 warps -- fit an SM); the
+// backward sweep re-derives the explicit terms from the same inputs, which
+// the forward sweep has just pulled through L2.
+__global__ void __launch_bounds__(128) k_mx_hevi_col(Dims d, Tab t, Flags fl, WS win, WS wout, float dtau,
+                                                      const float* __restrict__ lu) {
+  extern __shared__ float s_dp[];  // [nz][128]
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
   const int nz = d.nz;
-  const int tid = threadIdx.y * blockDim.x + threadIdx.x, nt = blockDim.x * blockDim.y;
-  float* s_dp = sm;                   // nz * nt
-  float* s_S = sm + (size_t)nz * nt;  // nz * nt
-  float* s_wt = s_S + (size_t)nz * nt; // (nz+1) * nt
+  const int tid = threadIdx.y * blockDim.x + threadIdx.x;
   if (i >= d.nx || j >= d.ny) return;
   const float b = (float)fl.hevi_beta, ob = 1.f - b;
-  const float cp = (float)kCp;
+  const float cpf = (float)kCp;
   const float* __restrict__ la = lu;
   const float* __restrict__ lc = lu + nz;
   const float* __restrict__ li = lu + 2 * nz;
-  // explicit part of w at face k: wt = w - dtau*(1-b)*cp*tf*G(pi'_old)
-  float p_k = WI(PI, i, j, 0);
-  float wt_k = WI(W, i, j, 0);  // face 0: no pressure gradient
-  s_wt[tid] = wt_k;
-  float w_k = wt_k;
+  const size_t col = (size_t)j * d.P + i;
+  const size_t pl = d.plane;
+  const float* __restrict__ U0 = win.f[U] + col;
+  const float* __restrict__ V0 = win.f[V] + col;
+  const float* __restrict__ W0 = win.f[W] + col;
+  const float* __restrict__ P0 = win.f[PI] + col;
+  const float* __restrict__ R0 = win.f[RHO] + col;
+  const size_t vn = d.P;  // v(j+1) offset
+  auto Dh_at = [&](int k) {
+    const size_t o = (size_t)k * pl;
+    return -(t.r0c[k] * ((U0[o + 1] - U0[o]) * t.dx_inv + (V0[o + vn] - V0[o]) * t.dy_inv));
+  };
+  // forward sweep: rhs(k) from the explicit part, dp(k) = (rhs - a dp(k-1)) / den
+  float p_k = P0[0];
+  float w_k = W0[0];
+  float wt_k = w_k;  // face 0: no pressure gradient
   float dp_prev = 0.f;
+#pragma unroll 4
   for (int k = 0; k < nz; ++k) {
-    const float w_k1 = WI(W, i, j, k + 1);
+    const size_t o1 = (size_t)(k + 1) * pl;
+    const float w_k1 = W0[o1];
     float wt_k1 = w_k1, p_k1 = 0.f;
     if (k + 1 < nz) {
-      p_k1 = WI(PI, i, j, k + 1);
-      wt_k1 = w_k1 - dtau * ob * cp * t.tfz[k + 1] * (p_k1 - p_k) * t.idzw[k + 1];
+      p_k1 = P0[o1];
+      wt_k1 = w_k1 - dtau * ob * cpf * t.tfz[k + 1] * (p_k1 - p_k) * t.idzw[k + 1];
     }
-    s_wt[(size_t)(k + 1) * nt + tid] = wt_k1;
-    const float r0 = t.r0c[k];
-    const float Dh = -(r0 * ((WI(U, i + 1, j, k) - WI(U, i, j, k)) * t.dx_inv + (WI(V, i, j + 1, k) - WI(V, i, j, k)) * t.dy_inv));
-    const float rk = t.rfz[k], rk1 = t.rfz[k + 1];
-    const float dv_old = -(rk1 * w_k1 - rk * w_k) * t.idzc[k];
-    const float dv_t = -(rk1 * wt_k1 - rk * wt_k) * t.idzc[k];
-    const float S = Dh + ob * dv_old;
+    const float rk = t.rfz[k], rk1 = t.rfz[k + 1], idz = t.idzc[k];
+    const float dv_old = -(rk1 * w_k1 - rk * w_k) * idz;
+    const float dv_t = -(rk1 * wt_k1 - rk * wt_k) * idz;
+    const float S = Dh_at(k) + ob * dv_old;
     const float rhs = p_k + dtau * t.kap[k] * (S + b * dv_t);
     const float dpk = (k == 0) ? rhs * li[0] : (rhs - la[k] * dp_prev) * li[k];
-    s_dp[(size_t)k * nt + tid] = dpk;
-    s_S[(size_t)k * nt + tid] = S;
+    s_dp[(size_t)k * 128 + tid] = dpk;
     dp_prev = dpk;
     w_k = w_k1;
     wt_k = wt_k1;
     p_k = p_k1;
   }
-  // back substitution with a one-level lag: x(k) = pi'_new(k);
-  // wn(k+1) needs x(k), x(k+1); rho'(k+1) needs wn(k+2), wn(k+1).
-  float x_up = s_dp[(size_t)(nz - 1) * nt + tid];  // x(nz-1)
-  float wn_up = s_wt[(size_t)nz * nt + tid];       // wn(nz) = wt(nz)
-  wout.f[W][IX(i, j, nz)] = wn_up;
+  // backward sweep: x(k) = dp(k) - c'(k) x(k+1); after x(k) is known, face
+  // k+1 (needs x(k), x(k+1)) and cell k+1 (needs faces k+1, k+2) are final.
+  float* __restrict__ Wo = wout.f[W] + col;
+  float* __restrict__ Po = wout.f[PI] + col;
+  float* __restrict__ Ro = wout.f[RHO] + col;
+  float x_up = s_dp[(size_t)(nz - 1) * 128 + tid];  // x(nz-1)
+  float w_up = W0[(size_t)nz * pl];                  // w_old(nz) = wn(nz)
+  float wn_up = w_up;
+  float p_up = P0[(size_t)(nz - 1) * pl];            // pi'_old(nz-1)
+  Wo[(size_t)nz * pl] = wn_up;
+#pragma unroll 4
   for (int k = nz - 2; k >= -1; --k) {
-    // x(k) (k >= 0), then finalise level k+1
-    float x_k = 0.f, wn_k1;
+    const int kk = k + 1;  // face kk and cell kk are finalised here
+    const size_t okk = (size_t)kk * pl;
+    const float w_kk = W0[okk];
+    float x_k = 0.f, wn_kk, p_k = 0.f;
     if (k >= 0) {
-      x_k = s_dp[(size_t)k * nt + tid] - lc[k] * x_up;
-      wn_k1 = s_wt[(size_t)(k + 1) * nt + tid] - dtau * b * cp * t.tfz[k + 1] * (x_up - x_k) * t.idzw[k + 1];
+      x_k = s_dp[(size_t)k * 128 + tid] - lc[k] * x_up;
+      p_k = P0[(size_t)k * pl];
+      const float wt_kk = w_kk - dtau * ob * cpf * t.tfz[kk] * (p_up - p_k) * t.idzw[kk];
+      wn_kk = wt_kk - dtau * b * cpf * t.tfz[kk] * (x_up - x_k) * t.idzw[kk];
     } else {
-      wn_k1 = s_wt[tid];  // face 0
+      wn_kk = w_kk;  // face 0
     }
-    const int kk = k + 1;  // finalise cell kk with faces kk, kk+1
-    const float dv_new = -(t.rfz[kk + 1] * wn_up - t.rfz[kk] * wn_k1) * t.idzc[kk];
-    const size_t ck = IX(i, j, kk);
-    wout.f[RHO][ck] = win.f[RHO][ck] + dtau * (s_S[(size_t)kk * nt + tid] + b * dv_new);
-    wout.f[PI][ck] = x_up;
-    wout.f[W][ck] = wn_k1;
+    const float rk = t.rfz[kk], rk1 = t.rfz[kk + 1], idz = t.idzc[kk];
+    const float dv_old = -(rk1 * w_up - rk * w_kk) * idz;
+    const float dv_new = -(rk1 * wn_up - rk * wn_kk) * idz;
+    const float S = Dh_at(kk) + ob * dv_old;
+    Ro[okk] = R0[okk] + dtau * (S + b * dv_new);
+    Po[okk] = x_up;
+    Wo[okk] = wn_kk;
     x_up = x_k;
-    wn_up = wn_k1;
+    wn_up = wn_kk;
+    w_up = w_kk;
+    p_up = p_k;
   }
 }
 
 // ---- finish: fold the last stage's acoustic increments into the FP64
 // state, apply the sponge (damping.cpp:76-140) in FP64 and to the FP32
 // working copy, which becomes the next step's s0 working copy.
-__global__ void k_mx_finish(Dims d, Tab t, Flags fl, WS wfin, WS wst, WS w0, MS64 ss, unsigned* err) {
+__global__ void k_mx_finish(Dims d, Tab t, Flags fl, const __grid_constant__ WS wfin, const __grid_constant__ WS wst,
+                            const __grid_constant__ WS w0, const __grid_constant__ MS64 ss, unsigned* err) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
   const int k = blockIdx.z;
@@ -388,7 +494,7 @@ __global__ void k_mx_unpack_f32(Dims d, int nsx, int nsy, int nsz, int ni, int n
 }
 
 // FP64 state -> FP32 working copy in perturbation form, incl. ghosts.
-__global__ void k_mx_to_working(Dims d, Tab t, CS64 s, WS w) {
+__global__ void k_mx_to_working(Dims d, Tab t, const __grid_constant__ CS64 s, const __grid_constant__ WS w) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
   const int k = blockIdx.z;
@@ -423,7 +529,7 @@ static MS64 ms64(double* const* f) {
 void mixed_stage(const Dims& d, const Tab& t, const Flags& fl, const WS& win, const WS& w0, const WS& wout,
                  double* const* s0, double* const* ss, double dt_stage, bool write_fp64, unsigned* err,
                  cudaStream_t stream) {
-  const dim3 b(32, 4);
+  const dim3 b(TX, TY);
   const dim3 g = g3(d.nx + 1, d.ny + 1, d.nz + 1, b);
   if (write_fp64)
     k_mx_stage<true><<<g, b, 0, stream>>>(d, t, fl, win, w0, wout, cs64(s0), ms64(ss), (float)dt_stage, dt_stage, err);
@@ -441,8 +547,8 @@ void mixed_fb_substep(const Dims& d, const Tab& t, const Flags& fl, const WS& wi
 
 void mixed_hevi_column(const Dims& d, const Tab& t, const Flags& fl, const WS& win, const WS& wout, float dtau,
                        const float* lu, cudaStream_t stream) {
-  const dim3 bc(32, 2);
-  const size_t smem = (size_t)(3 * d.nz + 1) * bc.x * bc.y * sizeof(float);
+  const dim3 bc(32, 4);
+  const size_t smem = (size_t)d.nz * bc.x * bc.y * sizeof(float);
   static size_t smem_set = 0;  // opt in above 48 KB once per size
   if (smem > 48 * 1024 && smem > smem_set) {
     cudaFuncSetAttribute(k_mx_hevi_col, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
