@@ -33,37 +33,43 @@ struct MS64 {
 #define WC(q, i, j, k) (win.f[q][IX(iclamp((i), 0, d.nx - 1), iclamp((j), 0, d.ny - 1), iclamp((k), 0, d.nz - 1))])
 
 // WENO5 face reconstruction + local Lax-Friedrichs flux in FP32
-// (advection.cpp:62-98,151-156), with the weights normalised by a single
-// division: a_k = d_k / s_k^2 -> numerator and denominator scaled by
-// (s0 s1 s2)^2.
-__device__ __forceinline__ float weno_face_f(float qm2, float qm1, float q0, float q1, float q2, float vel) {
-  const float eps = 1e-6f;
+// (advection.cpp:62-98,151-156), organised for FP32 throughput; the
+// arithmetic is the reference's up to rounding:
+//  * the right-biased reconstruction of (qm2..q2) is the left-biased one of
+//    the reversed stencil (q2..qm2), whose smoothness indicators are the same
+//    three values in reverse order -- they are computed once;
+//  * with alpha = max(|vel|, 1e-3) the flux 0.5*(vel*(ql+qr) - alpha*(qr-ql))
+//    is vel*ql for vel >= 1e-3 and vel*qr for vel <= -1e-3, so one
+//    reconstruction on the upwind-ordered stencil suffices there; only lanes
+//    with |vel| < 1e-3 evaluate the second one;
+//  * the weights a_k = d_k/s_k^2 are normalised with one division:
+//    numerator and denominator scaled by (s0 s1 s2)^2, all terms positive
+//    and far inside the FP32 range (s_k in [1e-6, ~1e4]).
+__device__ __forceinline__ float weno_left(float qm2, float qm1, float q0, float q1, float q2, float s0, float s1,
+                                           float s2) {
   const float v0 = (2.f * qm2 - 7.f * qm1 + 11.f * q0) * (1.f / 6.f);
   const float v1 = (-qm1 + 5.f * q0 + 2.f * q1) * (1.f / 6.f);
   const float v2 = (2.f * q0 + 5.f * q1 - q2) * (1.f / 6.f);
+  const float p01 = s0 * s1, p02 = s0 * s2, p12 = s1 * s2;
+  const float w0 = 0.1f * (p12 * p12), w1 = 0.6f * (p02 * p02), w2 = 0.3f * (p01 * p01);
+  return __fdividef(w0 * v0 + w1 * v1 + w2 * v2, w0 + w1 + w2);
+}
+__device__ __forceinline__ float weno_face_f(float qm2, float qm1, float q0, float q1, float q2, float vel) {
+  const float eps = 1e-6f;
   const float e0 = qm2 - 2.f * qm1 + q0, f0 = qm2 - 4.f * qm1 + 3.f * q0;
   const float e1 = qm1 - 2.f * q0 + q1, f1 = qm1 - q1;
   const float e2 = q0 - 2.f * q1 + q2, f2 = 3.f * q0 - 4.f * q1 + q2;
   const float s0 = eps + (13.f / 12.f) * (e0 * e0) + 0.25f * (f0 * f0);
   const float s1 = eps + (13.f / 12.f) * (e1 * e1) + 0.25f * (f1 * f1);
   const float s2 = eps + (13.f / 12.f) * (e2 * e2) + 0.25f * (f2 * f2);
-  const float p01 = s0 * s1, p02 = s0 * s2, p12 = s1 * s2;
-  const float w0 = 0.1f * (p12 * p12), w1 = 0.6f * (p02 * p02), w2 = 0.3f * (p01 * p01);
-  const float ql = (w0 * v0 + w1 * v1 + w2 * v2) / (w0 + w1 + w2);
-  const float u0 = (2.f * q2 - 7.f * q1 + 11.f * q0) * (1.f / 6.f);
-  const float u1 = (-q1 + 5.f * q0 + 2.f * qm1) * (1.f / 6.f);
-  const float u2 = (2.f * q0 + 5.f * qm1 - qm2) * (1.f / 6.f);
-  const float g0e = q2 - 2.f * q1 + q0, g0f = q2 - 4.f * q1 + 3.f * q0;
-  const float g1e = q1 - 2.f * q0 + qm1, g1f = q1 - qm1;
-  const float g2e = q0 - 2.f * qm1 + qm2, g2f = 3.f * q0 - 4.f * qm1 + qm2;
-  const float t0 = eps + (13.f / 12.f) * (g0e * g0e) + 0.25f * (g0f * g0f);
-  const float t1 = eps + (13.f / 12.f) * (g1e * g1e) + 0.25f * (g1f * g1f);
-  const float t2 = eps + (13.f / 12.f) * (g2e * g2e) + 0.25f * (g2f * g2f);
-  const float r01 = t0 * t1, r02 = t0 * t2, r12 = t1 * t2;
-  const float c0 = 0.1f * (r12 * r12), c1 = 0.6f * (r02 * r02), c2 = 0.3f * (r01 * r01);
-  const float qr = (c0 * u0 + c1 * u1 + c2 * u2) / (c0 + c1 + c2);
-  const float alpha = fmaxr(fabsf(vel), 1e-3f);
-  return 0.5f * (vel * (ql + qr) - alpha * (qr - ql));
+  const bool up = vel >= 0.f;  // upwind-ordered stencil (no divergence)
+  const float a0 = up ? qm2 : q2, a1 = up ? qm1 : q1, a3 = up ? q1 : qm1, a4 = up ? q2 : qm2;
+  const float t0 = up ? s0 : s2, t2 = up ? s2 : s0;
+  const float rec = weno_left(a0, a1, q0, a3, a4, t0, s1, t2);
+  if (fabsf(vel) >= 1e-3f) return vel * rec;
+  const float oth = weno_left(a4, a3, q0, a1, a0, t2, s1, t0);  // the other side
+  const float ql = up ? rec : oth, qr = up ? oth : rec;
+  return 0.5f * (vel * (ql + qr) - 1e-3f * (qr - ql));
 }
 
 __device__ __forceinline__ float gradc(float m3, float m2, float m1, float p1, float p2, float p3, float inv, int order) {
