@@ -16,6 +16,8 @@
 // Requires a horizontally uniform reference state on flat terrain (all
 // coefficients are per-level tables) and the stable composition
 // (pi' pressure gradient, fast terms integrated once by the substeps).
+#include <cmath>
+#include <cstdlib>
 #include "step_kernels.cuh"
 
 namespace vgb {
@@ -81,226 +83,268 @@ __device__ __forceinline__ float gradc(float m3, float m2, float m1, float p1, f
 }
 
 // ---- RK stage kernel: slow tendency + s = s0 + dt*R ------------------------
-// Block = 32 x 8 columns at one level k (grid z = k, faces k = 0..nz). Each
-// field's plane at the block's level is staged in shared memory with the
-// halo its stencils need (3 for the WENO / high-order scalar stencils, 1 for
-// the winds, pi', rho'), using the reference's clamps when loading, so a
-// stencil read is a shared-memory load at a fixed offset. Horizontal WENO
-// fluxes are computed once per face into shared memory and differenced;
-// vertical neighbours of a thread's own column come from L2 (the adjacent
-// planes were just read by the blocks of the neighbouring levels).
+// 2.5-D: a block owns 32 x 8 columns and marches up a chunk of levels
+// (grid z = chunk). At each level the fields' planes are staged in shared
+// memory with the halo their stencils need (3 for the scalar WENO /
+// high-order stencils, 1 for the winds, pi', rho'). The tiles are loaded
+// with the reference's clamps (clamp_at, field.hpp:91-96), so a tile read at
+// an unclamped offset returns the clamped value and most stencil reads need
+// no clamp of their own. Each thread keeps its own column's vertical
+// neighbours in registers: theta' and qv over k-3..k+3 for the vertical WENO,
+// whose flux through the top face of level k is carried to level k+1 as its
+// bottom flux (one WENO evaluation per vertical face), and w, pi', rho' at
+// k-1. Horizontal WENO fluxes are computed once per face into shared memory.
 constexpr int TX = 32, TY = 8;
 constexpr int W3 = TX + 6, H3 = TY + 6;  // halo-3 tile
 constexpr int W1 = TX + 2, H1 = TY + 2;  // halo-1 tile
+constexpr int NT = TX * TY;
 
 template <int H>
-__device__ __forceinline__ void load_tile(float* __restrict__ dst, const float* __restrict__ src, const Dims& d,
-                                          int i0, int j0, int k, int xmax, int ymax) {
+__device__ __forceinline__ void load_tile(float* __restrict__ dst, const float* __restrict__ plane, int P, int i0,
+                                          int j0, int xmax, int ymax) {
   constexpr int Wt = TX + 2 * H, Ht = TY + 2 * H;
-  const float* __restrict__ base = src + (size_t)k * d.plane;
-  for (int e = threadIdx.y * TX + threadIdx.x; e < Wt * Ht; e += TX * TY) {
-    const int tx = e % Wt, ty = e / Wt;
+  for (int e = threadIdx.y * TX + threadIdx.x; e < Wt * Ht; e += NT) {
+    const int ty = e / Wt, tx = e - ty * Wt;
     const int gi = iclamp(i0 - H + tx, 0, xmax), gj = iclamp(j0 - H + ty, 0, ymax);
-    dst[e] = base[(size_t)gj * d.P + gi];
+    dst[e] = plane[gj * P + gi];
   }
 }
 
 template <bool kFP64Out>
-__global__ void __launch_bounds__(256) k_mx_stage(Dims d, Tab t, Flags fl, const __grid_constant__ WS win,
-                                                  const __grid_constant__ WS w0, const __grid_constant__ WS wout,
-                                                  const __grid_constant__ CS64 s0, const __grid_constant__ MS64 ss,
-                                                  float dts, double dtd, unsigned* err) {
-  __shared__ float sQ[H3 * W3];            // scalar (theta' or q) at level kc, halo 3
-  __shared__ float sU[H1 * W1], sV[H1 * W1], sWk[H1 * W1], sP[H1 * W1], sR[H1 * W1], sT[H3 * W3];
+__global__ void __launch_bounds__(NT, 3) k_mx_stage(Dims d, Tab t, Flags fl, const __grid_constant__ WS win,
+                                                 const __grid_constant__ WS w0, const __grid_constant__ WS wout,
+                                                 const __grid_constant__ CS64 s0, const __grid_constant__ MS64 ss,
+                                                 float dts, double dtd, int kchunk, unsigned* err) {
+  __shared__ float sT[H3 * W3], sQ[H3 * W3];
+  __shared__ float sU[H1 * W1], sV[H1 * W1], sW[H1 * W1], sP[H1 * W1], sR[H1 * W1];
   __shared__ float sFx[TY * (TX + 1)], sFy[(TY + 1) * TX];
-  const int nx = d.nx, ny = d.ny, nz = d.nz;
-  const int i0 = blockIdx.x * TX, j0 = blockIdx.y * TY, k = blockIdx.z;
-  const int tx = threadIdx.x, ty = threadIdx.y;
+  const int nx = d.nx, ny = d.ny, nz = d.nz, P = d.P;
+  const size_t pl = d.plane;
+  const int i0 = blockIdx.x * TX, j0 = blockIdx.y * TY;
+  const int kb = blockIdx.z * kchunk;
+  const int klast = (kb + kchunk >= nz) ? nz : kb + kchunk - 1;  // the top chunk also owns face nz
+  const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * TX + tx;
   const int i = i0 + tx, j = j0 + ty;
-  const int kc = imin(k, nz - 1), km = imax(k - 1, 0);
-  const size_t P = d.P, pl = d.plane;
-  const bool cells_here = k < nz;
-  // stage the planes (clamp ranges: cells [0,nx-1]x[0,ny-1], u faces
-  // [0,nx]x[0,ny-1], v faces [0,nx-1]x[0,ny], rho' incl. its ghost line)
-  load_tile<3>(sT, win.f[THETA], d, i0, j0, kc, nx - 1, ny - 1);
-  load_tile<1>(sU, win.f[U], d, i0, j0, kc, nx, ny - 1);
-  load_tile<1>(sV, win.f[V], d, i0, j0, kc, nx - 1, ny);
-  load_tile<1>(sWk, win.f[W], d, i0, j0, k, nx - 1, ny - 1);
-  load_tile<1>(sP, win.f[PI], d, i0, j0, kc, nx - 1, ny - 1);
-  load_tile<1>(sR, win.f[RHO], d, i0, j0, kc, nx, ny);
-  __syncthreads();
-#define T3(a, gi, gj) a[((gj) - j0 + 3) * W3 + ((gi) - i0 + 3)]
-#define T1(a, gi, gj) a[((gj) - j0 + 1) * W1 + ((gi) - i0 + 1)]
-  const size_t c = (size_t)k * pl + (size_t)j * P + i;
-  bool bad = false;
-  auto emit = [&](int q, float r) {
-    const float o = (w0.f[q] != nullptr) ? w0.f[q][c] + dts * r : r;  // no base: raw tendency
-    wout.f[q][c] = o;
-    bad |= !isfinite(o);
-    if (kFP64Out) ss.f[q][c] = s0.f[q][c] + dtd * (double)r;
-  };
+  const bool in_box = i <= nx && j <= ny;
+  const bool cell = i < nx && j < ny;
   const float cp = (float)kCp;
-  const bool in_x = i <= nx, in_y = j <= ny;
-  if (in_x && in_y) {
-    if (cells_here && j < ny) {  // u face (i, j, k)
-      const int ip = imin(i, nx - 1), im = imax(i - 1, 0);
-      const int jp1 = imin(j + 1, ny - 1), jm1 = imax(j - 1, 0);
-      const float* __restrict__ ucol = win.f[U] + (size_t)j * P + ip;
-      const float uc = 0.5f * (T1(sU, im, j) + T1(sU, ip, j));
-      const float ux = (T1(sU, ip, j) - T1(sU, im, j)) * t.dx_inv;
-      const float uy = (T1(sU, ip, jp1) - T1(sU, ip, jm1)) * (0.5f * t.dy_inv);
-      const float uz = (ucol[(size_t)imin(k + 1, nz - 1) * pl] - ucol[(size_t)imax(k - 1, 0) * pl]) * (0.5f * t.idza[k]);
-      const float vc = 0.25f * (T1(sV, im, jm1) + T1(sV, ip, jm1) + T1(sV, im, j) + T1(sV, ip, j));
-      const float wc = 0.5f * (T1(sWk, ip, j) + win.f[W][(size_t)imin(k + 1, nz - 1) * pl + (size_t)j * P + ip]);
+  const int o1 = (ty + 1) * W1 + (tx + 1), o3 = (ty + 3) * W3 + (tx + 3);  // own point in the tiles
+  const int dim = (i > 0) ? -1 : 0;              // im - i, im = max(i-1, 0)
+  const int ipu = imin(i, nx - 1) - i;           // ip - i on u faces (-1 at i = nx)
+  const int jpv = imin(j, ny - 1) - j;           // jp - j on v faces (-1 at j = ny)
+  const int djm = (j > 0) ? -1 : 0;              // jm - j
+  const size_t colc = (size_t)imin(j, ny) * P + imin(i, nx);
+  const float* __restrict__ wcolp = win.f[W] + colc;
+  // vertical registers of the own column
+  float wT[7], wQ[7];
+  float wprev = 0.f, pprev = 0.f, rprev = 0.f;
+  if (cell) {
+#pragma unroll
+    for (int m = 0; m < 7; ++m) {
+      const size_t o = (size_t)iclamp(kb + m - 3, 0, nz - 1) * pl + colc;
+      wT[m] = win.f[THETA][o];
+      wQ[m] = win.f[QV][o];
+    }
+    const size_t o = (size_t)imax(kb - 1, 0) * pl + colc;
+    wprev = win.f[W][o];
+    pprev = win.f[PI][o];
+    rprev = win.f[RHO][o];
+  }
+  float fcT = 0.f, fcQ = 0.f;  // carried vertical WENO fluxes (top face of the level below)
+  bool bad = false;
+  for (int k = kb; k <= klast; ++k) {
+    const bool cells_here = k < nz;  // uniform across the block
+    const int kc = imin(k, nz - 1);
+    __syncthreads();  // the previous level's tiles are no longer read
+    if (cells_here) {
+      const size_t ok = (size_t)k * pl;
+      load_tile<3>(sT, win.f[THETA] + ok, P, i0, j0, nx - 1, ny - 1);
+      load_tile<3>(sQ, win.f[QV] + ok, P, i0, j0, nx - 1, ny - 1);
+      load_tile<1>(sU, win.f[U] + ok, P, i0, j0, nx, ny - 1);
+      load_tile<1>(sV, win.f[V] + ok, P, i0, j0, nx - 1, ny);
+      load_tile<1>(sP, win.f[PI] + ok, P, i0, j0, nx - 1, ny - 1);
+      load_tile<1>(sR, win.f[RHO] + ok, P, i0, j0, nx, ny);
+    }
+    load_tile<1>(sW, win.f[W] + (size_t)k * pl, P, i0, j0, nx - 1, ny - 1);
+    __syncthreads();
+    const size_t c = (size_t)k * pl + colc;
+    const int kp1 = imin(k + 1, nz - 1), km = imax(k - 1, 0);
+    auto emit = [&](int q, float r) {
+      const float o = (w0.f[q] != nullptr) ? w0.f[q][c] + dts * r : r;  // no base: raw tendency
+      wout.f[q][c] = o;
+      bad |= !isfinite(o);
+      if (kFP64Out) ss.f[q][c] = s0.f[q][c] + dtd * (double)r;
+    };
+    if (cells_here && in_box && j < ny) {  // u face (i, j, k)
+      const float ump = sU[o1 + ipu], umm = sU[o1 + dim];
+      const float uc = 0.5f * (umm + ump);
+      const float ux = (ump - umm) * t.dx_inv;
+      const float uy = (sU[o1 + ipu + W1] - sU[o1 + ipu - W1]) * (0.5f * t.dy_inv);
+      const float* __restrict__ ucol = win.f[U] + (size_t)j * P + (i + ipu);
+      const float uz = (ucol[(size_t)kp1 * pl] - ucol[(size_t)km * pl]) * (0.5f * t.idza[k]);
+      const float vc = 0.25f * (sV[o1 + dim - W1] + sV[o1 + ipu - W1] + sV[o1 + dim] + sV[o1 + ipu]);
+      const float wc = 0.5f * (sW[o1 + ipu] + win.f[W][(size_t)kp1 * pl + (size_t)j * P + (i + ipu)]);
       float r = -(uc * ux + vc * uy + wc * uz);
       if (fl.coriolis) r += (fl.coriolis == 2 ? t.f0 + t.beta * (((float)j + 0.5f) * t.dy - 0.5f * (float)ny * t.dy) : t.f0) * vc;
-      r -= cp * (0.5f * (T3(sT, im, j) + T3(sT, ip, j))) * (T1(sP, ip, j) - T1(sP, im, j)) * t.dx_inv;
+      r -= cp * (0.5f * (sT[o3 + dim] + sT[o3 + ipu])) * (sP[o1 + ipu] - sP[o1 + dim]) * t.dx_inv;
       emit(U, r);
     }
-    if (cells_here && i < nx) {  // v face (i, j, k)
-      const int jp = imin(j, ny - 1), jm = imax(j - 1, 0);
-      const int ip1 = imin(i + 1, nx - 1), im1 = imax(i - 1, 0);
-      const float* __restrict__ vcol = win.f[V] + (size_t)jp * P + i;
-      const float vc = 0.5f * (T1(sV, i, jm) + T1(sV, i, jp));
-      const float vy = (T1(sV, i, jp) - T1(sV, i, jm)) * t.dy_inv;
-      const float vx = (T1(sV, ip1, jp) - T1(sV, im1, jp)) * (0.5f * t.dx_inv);
-      const float vz = (vcol[(size_t)imin(k + 1, nz - 1) * pl] - vcol[(size_t)imax(k - 1, 0) * pl]) * (0.5f * t.idza[k]);
-      const float uc = 0.25f * (T1(sU, im1, jm) + T1(sU, i, jm) + T1(sU, im1, jp) + T1(sU, i, jp));
-      const float wc = 0.5f * (T1(sWk, i, jp) + win.f[W][(size_t)imin(k + 1, nz - 1) * pl + (size_t)jp * P + i]);
+    if (cells_here && in_box && i < nx) {  // v face (i, j, k)
+      const int dp1 = jpv * W1, dm1 = djm * W1;
+      const float vpp = sV[o1 + dp1], vmm = sV[o1 + dm1];
+      const float vc = 0.5f * (vmm + vpp);
+      const float vy = (vpp - vmm) * t.dy_inv;
+      const float vx = (sV[o1 + dp1 + 1] - sV[o1 + dp1 - 1]) * (0.5f * t.dx_inv);
+      const float* __restrict__ vcol = win.f[V] + (size_t)(j + jpv) * P + i;
+      const float vz = (vcol[(size_t)kp1 * pl] - vcol[(size_t)km * pl]) * (0.5f * t.idza[k]);
+      const float uc = 0.25f * (sU[o1 + dim + dm1] + sU[o1 + dm1] + sU[o1 + dim + dp1] + sU[o1 + dp1]);
+      const float wc = 0.5f * (sW[o1 + dp1] + win.f[W][(size_t)kp1 * pl + (size_t)(j + jpv) * P + i]);
       float r = -(uc * vx + vc * vy + wc * vz);
       if (fl.coriolis) r -= (fl.coriolis == 2 ? t.f0 + t.beta * (((float)j + 0.5f) * t.dy - 0.5f * (float)ny * t.dy) : t.f0) * uc;
-      r -= cp * (0.5f * (T3(sT, i, jm) + T3(sT, i, jp))) * (T1(sP, i, jp) - T1(sP, i, jm)) * t.dy_inv;
+      r -= cp * (0.5f * (sT[o3 + djm * W3] + sT[o3 + jpv * W3])) * (sP[o1 + dp1] - sP[o1 + dm1]) * t.dy_inv;
       emit(V, r);
     }
-    if (i < nx && j < ny) {  // w face (i, j, k), k = 0..nz
-      const size_t col = (size_t)j * P + i;
-      const float* __restrict__ wcol = win.f[W] + col;
-      const float wkc = wcol[(size_t)kc * pl], wk = T1(sWk, i, j), wkm = wcol[(size_t)km * pl];
+    // w face (i, j, k), k = 0..nz; at k = nz the tiles other than sW still
+    // hold level nz-1 = kc
+    const float wk = sW[o1];
+    if (cell) {
+      const float wkc = cells_here ? wk : wprev;
       const float wc = 0.5f * (wkc + wk);
-      const float wz = (wk - wkm) * t.idza[kc];
-      const float wx = (T1(sWk, imin(i + 1, nx - 1), j) - T1(sWk, imax(i - 1, 0), j)) * (0.5f * t.dx_inv);
-      const float wy = (T1(sWk, i, imin(j + 1, ny - 1)) - T1(sWk, i, imax(j - 1, 0))) * (0.5f * t.dy_inv);
-      const float uc = 0.5f * (T1(sU, i, j) + T1(sU, i + 1, j));
-      const float vc = 0.5f * (T1(sV, i, j) + T1(sV, i, j + 1));
+      const float wz = (wk - wprev) * t.idza[kc];
+      const float wx = (sW[o1 + 1] - sW[o1 - 1]) * (0.5f * t.dx_inv);
+      const float wy = (sW[o1 + W1] - sW[o1 - W1]) * (0.5f * t.dy_inv);
+      const float uc = 0.5f * (sU[o1] + sU[o1 + 1]);
+      const float vc = 0.5f * (sV[o1] + sV[o1 + W1]);
       float r = -(uc * wx + vc * wy + wc * wz);
-      const float thc = T3(sT, i, j), thm = win.f[THETA][(size_t)km * pl + col];
-      const float pic = T1(sP, i, j), pim = win.f[PI][(size_t)km * pl + col];
+      const float thc = sT[o3], pic = sP[o1];
+      const float thm = wT[2];  // theta'(max(k-1, 0))
+      const float pim = (k == 0) ? pic : pprev;
       r -= cp * (0.5f * (thm + thc)) * (pic - pim) * t.idzw[k];
-      float qcond = 0.f;
-      const size_t ckc = (size_t)kc * pl + col;
-      if (fl.moist) qcond = win.f[QC][ckc] + win.f[QR][ckc] + win.f[QI][ckc] + win.f[QS][ckc] + win.f[QG][ckc];
-      r += (float)kG * (thc * t.th0inv[kc] + (float)kBuoyMoist * win.f[QV][ckc] - qcond);
+      float qcond = 0.f, qvc = wQ[3];  // qv(kc)
+      if (fl.moist) {
+        const size_t ckc = (size_t)kc * pl + colc;
+        qcond = win.f[QC][ckc] + win.f[QR][ckc] + win.f[QI][ckc] + win.f[QS][ckc] + win.f[QG][ckc];
+      }
+      r += (float)kG * (thc * t.th0inv[kc] + (float)kBuoyMoist * qvc - qcond);
       emit(W, r);
     }
-    if (cells_here && i < nx && j < ny) {  // mass
-      const float* __restrict__ rcol = win.f[RHO] + (size_t)j * P + i;
-      const float rc = T1(sR, i, j);
-      const float fx = T1(sU, i + 1, j) * 0.5f * (rc + T1(sR, i + 1, j)) -
-                       T1(sU, i, j) * 0.5f * (T1(sR, imax(i - 1, 0), j) + rc);
-      const float fy = T1(sV, i, j + 1) * 0.5f * (rc + T1(sR, i, j + 1)) -
-                       T1(sV, i, j) * 0.5f * (T1(sR, i, imax(j - 1, 0)) + rc);
-      const float fz = win.f[W][c + pl] * 0.5f * (rc + rcol[(size_t)imin(k + 1, nz - 1) * pl]) -
-                       T1(sWk, i, j) * 0.5f * (rcol[(size_t)imax(k - 1, 0) * pl] + rc);
+    if (!cells_here) break;
+    const float wt = cell ? wcolp[(size_t)(k + 1) * pl] : 0.f;  // w at face k+1
+    if (cell) {  // mass and pi
+      const float rc = sR[o1];
+      const float fx = sU[o1 + 1] * 0.5f * (rc + sR[o1 + 1]) - sU[o1] * 0.5f * (sR[o1 - 1] + rc);
+      const float fy = sV[o1 + W1] * 0.5f * (rc + sR[o1 + W1]) - sV[o1] * 0.5f * (sR[o1 - W1] + rc);
+      const float rkp = win.f[RHO][(size_t)kp1 * pl + colc];
+      const float fz = wt * 0.5f * (rc + rkp) - wk * 0.5f * (rprev + rc);
       emit(RHO, -(fx * t.dx_inv + fy * t.dy_inv + fz * t.idzc[k]));
       float r = 0.f;
       if (fl.div_damp > 0.0) {
-        const float pc = T1(sP, i, j);
-        const float lap = (T1(sP, imin(i + 1, nx - 1), j) - 2.f * pc + T1(sP, imax(i - 1, 0), j)) * (t.dx_inv * t.dx_inv) +
-                          (T1(sP, i, imin(j + 1, ny - 1)) - 2.f * pc + T1(sP, i, imax(j - 1, 0))) * (t.dy_inv * t.dy_inv);
+        const float pc = sP[o1];
+        const float lap = (sP[o1 + 1] - 2.f * pc + sP[o1 - 1]) * (t.dx_inv * t.dx_inv) +
+                          (sP[o1 + W1] - 2.f * pc + sP[o1 - W1]) * (t.dy_inv * t.dy_inv);
         r = -(float)fl.div_damp * lap;
       }
       emit(PI, r);
     }
-  }
-  // ---- scalar species: theta' then the moisture species ----
-  if (!cells_here) {
-    if (bad) atomicOr(err, (unsigned)kErrNonFinite);
-    return;  // all threads of the block leave together (k is uniform)
-  }
-  const int last = fl.moist ? QG : QV;
-  const bool cell = i < nx && j < ny;
-  const size_t col = (size_t)j * P + i;
-  for (int q = THETA; q <= last; ++q) {
-    if (q == PI) continue;
-    const bool is_theta = (q == THETA);
-    float* Q = sT;
-    if (!is_theta) {
-      __syncthreads();  // previous species' tiles are no longer read
-      load_tile<3>(sQ, win.f[q], d, i0, j0, kc, nx - 1, ny - 1);
-      Q = sQ;
-      __syncthreads();
-    }
-    float r = 0.f;
-    if (fl.weno_scalars) {
-      // x faces f = i0..i0+TX of rows j0..j0+TY-1, y faces g = j0..j0+TY
-      for (int e = ty * TX + tx; e < TY * (TX + 1); e += TX * TY) {
-        const int f = i0 + e % (TX + 1), row = j0 + e / (TX + 1);
-        float F = 0.f;
-        if (f <= nx && row < ny) {
-          auto Qc = [&](int gi) { return T3(Q, iclamp(gi, 0, nx - 1), row); };
-          F = weno_face_f(Qc(f - 3), Qc(f - 2), Qc(f - 1), Qc(f), Qc(f + 1), T1(sU, f, row));
+    // ---- scalars ----
+    const float idz = t.idza[k];
+    const bool vert = (k + 2 < nz || k >= 2);
+    const float* sh = t.t0d + 6 * k;  // theta0(clamp(k+m)) - theta0(k), m = -3..2
+    const float divh = (sU[o1 + 1] - sU[o1]) * t.dx_inv + (sV[o1 + W1] - sV[o1]) * t.dy_inv;
+    // one species: Q = its tile at level k; z0..z5 = its column at k-3..k+2
+    // (z3 unused: the tile holds it); fc = carried flux, updated
+    auto scalar = [&](int q, const float* Q, float z0, float z1, float z2, float z4, float z5, float* fc,
+                      float fc_shift) {
+      float r = 0.f;
+      const float qc = Q[o3];
+      if (fl.weno_scalars) {
+#pragma unroll
+        for (int e = 0; e < 2; ++e) {
+          const int t_ = tid + e * NT;
+          if (t_ < TY * (TX + 1)) {
+            const int fr = t_ / (TX + 1), ff = t_ - fr * (TX + 1);
+            float F = 0.f;
+            if (i0 + ff <= nx && j0 + fr < ny) {
+              const float* qq = Q + (fr + 3) * W3 + ff + 3;  // cell i0+ff, the face's right cell
+              F = weno_face_f(qq[-3], qq[-2], qq[-1], qq[0], qq[1], sU[(fr + 1) * W1 + ff + 1]);
+            }
+            sFx[t_] = F;
+          }
+          if (t_ < (TY + 1) * TX) {
+            const int fg = t_ / TX, fcl = t_ - fg * TX;
+            float G = 0.f;
+            if (j0 + fg <= ny && i0 + fcl < nx) {
+              const float* qq = Q + (fg + 3) * W3 + fcl + 3;
+              G = weno_face_f(qq[-3 * W3], qq[-2 * W3], qq[-W3], qq[0], qq[W3], sV[(fg + 1) * W1 + fcl + 1]);
+            }
+            sFy[t_] = G;
+          }
         }
-        sFx[e] = F;
-      }
-      for (int e = ty * TX + tx; e < (TY + 1) * TX; e += TX * TY) {
-        const int g = j0 + e / TX, cl = i0 + e % TX;
-        float G = 0.f;
-        if (g <= ny && cl < nx) {
-          auto Qc = [&](int gj) { return T3(Q, cl, iclamp(gj, 0, ny - 1)); };
-          G = weno_face_f(Qc(g - 3), Qc(g - 2), Qc(g - 1), Qc(g), Qc(g + 1), T1(sV, cl, g));
+        __syncthreads();
+        if (cell) {
+          const float ft = weno_face_f(z1, z2, qc, z4, z5, wt);
+          const float fb = (fc != nullptr && k > kb) ? *fc + wk * fc_shift : weno_face_f(z0, z1, z2, qc, z4, wk);
+          if (fc != nullptr) *fc = ft;
+          const float fe = sFx[ty * (TX + 1) + tx + 1], fw = sFx[ty * (TX + 1) + tx];
+          const float fn = sFy[(ty + 1) * TX + tx], fs = sFy[ty * TX + tx];
+          r = -(fe - fw) * t.dx_inv - (fn - fs) * t.dy_inv;
+          float div = divh;
+          if (vert) {
+            r -= (ft - fb) * idz;
+            div += (wt - wk) * idz;
+          }
+          if (fl.weno_advective) r += qc * div;
+          else if (q == THETA) r -= t.t0c[k] * div;
         }
-        sFy[e] = G;
+        __syncthreads();  // sFx/sFy are reused by the next species
+      } else if (cell) {
+        const float ua = 0.5f * (sU[o1] + sU[o1 + 1]), va = 0.5f * (sV[o1] + sV[o1 + W1]);
+        const float wa = 0.5f * (wk + wt);
+        const float* qq = Q + o3;
+        const float gx = gradc(qq[-3], qq[-2], qq[-1], qq[1], qq[2], qq[3], t.dx_inv, fl.advection);
+        const float gy = gradc(qq[-3 * W3], qq[-2 * W3], qq[-W3], qq[W3], qq[2 * W3], qq[3 * W3], t.dy_inv, fl.advection);
+        r = -(ua * gx + va * gy + wa * (z4 - z2) * (0.5f * idz));
       }
-      __syncthreads();
       if (cell) {
-        const float* __restrict__ qcol = win.f[q] + col;
-        const float* sh = t.t0d + 6 * k;
-        auto zq = [&](int m) {
-          const float v = qcol[(size_t)iclamp(k + m, 0, nz - 1) * pl];
-          return is_theta ? v + sh[m + 3] : v;
-        };
-        const float qc = T3(Q, i, j);
-        const float w_b = T1(sWk, i, j), w_t = win.f[W][c + pl];
-        const float idz = t.idza[k];
-        const bool vert = (k + 2 < nz || k >= 2);
-        float ft = 0.f, fb = 0.f;
-        if (vert) {
-          const float zm3 = zq(-3), zm2 = zq(-2), zm1 = zq(-1), zp1 = zq(1), zp2 = zq(2);
-          ft = weno_face_f(zm2, zm1, qc, zp1, zp2, w_t);
-          fb = weno_face_f(zm3, zm2, zm1, qc, zp1, w_b);
-        }
-        const float fe = sFx[ty * (TX + 1) + tx + 1], fw = sFx[ty * (TX + 1) + tx];
-        const float fn = sFy[(ty + 1) * TX + tx], fs = sFy[ty * TX + tx];
-        r = -(fe - fw) * t.dx_inv - (fn - fs) * t.dy_inv - (ft - fb) * idz;
-        float div = (T1(sU, i + 1, j) - T1(sU, i, j)) * t.dx_inv + (T1(sV, i, j + 1) - T1(sV, i, j)) * t.dy_inv;
-        if (vert) div += (w_t - w_b) * idz;
-        if (fl.weno_advective) r += qc * div;
-        else if (is_theta) r -= t.t0c[k] * div;
+        if (q >= QV && qc <= 0.f && r < 0.f) r = 0.f;
+        emit(q, r);
       }
-      __syncthreads();  // sFx/sFy reused by the next species
-    } else if (cell) {
-      const float* __restrict__ qcol = win.f[q] + col;
-      const float* sh = t.t0d + 6 * k;
-      auto zq = [&](int m) {
-        const float v = qcol[(size_t)iclamp(k + m, 0, nz - 1) * pl];
-        return is_theta ? v + sh[m + 3] : v;
-      };
-      auto X = [&](int di) { return T3(Q, iclamp(i + di, 0, nx - 1), j); };
-      auto Y = [&](int dj) { return T3(Q, i, iclamp(j + dj, 0, ny - 1)); };
-      const float ua = 0.5f * (T1(sU, i, j) + T1(sU, i + 1, j)), va = 0.5f * (T1(sV, i, j) + T1(sV, i, j + 1));
-      const float wa = 0.5f * (T1(sWk, i, j) + win.f[W][c + pl]);
-      const float gx = gradc(X(-3), X(-2), X(-1), X(1), X(2), X(3), t.dx_inv, fl.advection);
-      const float gy = gradc(Y(-3), Y(-2), Y(-1), Y(1), Y(2), Y(3), t.dy_inv, fl.advection);
-      const float gz = (zq(1) - zq(-1)) * (0.5f * t.idza[k]);
-      r = -(ua * gx + va * gy + wa * gz);
+    };
+    // theta' is advected as theta - theta0(k): the carried flux of level
+    // k-1 was formed with theta0(k-1) subtracted, and a WENO flux of q + s
+    // is the flux of q plus w*s, so it is corrected by
+    // w*(theta0(k-1) - theta0(k)) = -w*(theta0(k) - theta0(k-1)).
+    const float tshift = (k > 0) ? -t.t0d[6 * (k - 1) + 4] : 0.f;
+    scalar(THETA, sT, wT[0] + sh[0], wT[1] + sh[1], wT[2] + sh[2], wT[4] + sh[4], wT[5] + sh[5], &fcT, tshift);
+    scalar(QV, sQ, wQ[0], wQ[1], wQ[2], wQ[4], wQ[5], &fcQ, 0.f);
+    if (fl.moist) {
+      for (int q = QC; q <= QG; ++q) {
+        __syncthreads();  // sQ is no longer read
+        load_tile<3>(sQ, win.f[q] + (size_t)k * pl, P, i0, j0, nx - 1, ny - 1);
+        __syncthreads();
+        float z[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+        if (cell) {
+#pragma unroll
+          for (int m = 0; m < 6; ++m) z[m] = win.f[q][(size_t)iclamp(k + m - 3, 0, nz - 1) * pl + colc];
+        }
+        scalar(q, sQ, z[0], z[1], z[2], z[4], z[5], nullptr, 0.f);
+      }
     }
+    // slide the column registers up one level
     if (cell) {
-      if (q >= QV && T3(Q, i, j) <= 0.f && r < 0.f) r = 0.f;
-      emit(q, r);
+#pragma unroll
+      for (int m = 0; m < 6; ++m) {
+        wT[m] = wT[m + 1];
+        wQ[m] = wQ[m + 1];
+      }
+      const size_t o = (size_t)imin(k + 4, nz - 1) * pl + colc;
+      wT[6] = win.f[THETA][o];
+      wQ[6] = win.f[QV][o];
+      wprev = wk;
+      pprev = sP[o1];
+      rprev = sR[o1];
     }
   }
-#undef T3
-#undef T1
   if (bad) atomicOr(err, (unsigned)kErrNonFinite);
 }
 
@@ -532,16 +576,55 @@ static MS64 ms64(double* const* f) {
   return s;
 }
 
+// Levels per block of the stage kernel: the columns' blocks times the level
+// chunks should fill whole waves of resident blocks (a block's chunk is long,
+// so a partial last wave idles the rest of the GPU). Chunks of at least 8
+// levels keep the per-chunk start-up (column registers, one extra vertical
+// flux per species) small.
+// VIBE_GB300_STAGE_LEVELS=<n> overrides the choice (levels per block).
+static int stage_kchunk(const Dims& d, bool fp64_out) {
+  if (const char* e = std::getenv("VIBE_GB300_STAGE_LEVELS")) {
+    const int v = std::atoi(e);
+    if (v > 0) return imin(v, d.nz);
+  }
+  static int resident[2] = {0, 0};
+  int& res = resident[fp64_out ? 1 : 0];
+  if (res == 0) {
+    int dev = 0, sms = 0, per_sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (fp64_out)
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_mx_stage<true>, NT, 0);
+    else
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_mx_stage<false>, NT, 0);
+    res = imax(1, sms * per_sm);
+  }
+  const long cols = (long)((d.nx + TX) / TX) * ((d.ny + TY) / TY);
+  int best = d.nz;
+  double best_eff = -1.0;
+  for (int nch = 1; nch <= 16; ++nch) {
+    const int kc = (d.nz + nch - 1) / nch;
+    if (kc < 8 && nch > 1) break;
+    const int n = (d.nz + kc - 1) / kc;
+    const double waves = (double)(cols * n) / res;
+    const double eff = waves / std::ceil(waves) - 0.004 * n;  // small cost per chunk
+    if (eff > best_eff) { best_eff = eff; best = kc; }
+  }
+  return best;
+}
+
 void mixed_stage(const Dims& d, const Tab& t, const Flags& fl, const WS& win, const WS& w0, const WS& wout,
                  double* const* s0, double* const* ss, double dt_stage, bool write_fp64, unsigned* err,
                  cudaStream_t stream) {
   const dim3 b(TX, TY);
-  const dim3 g = g3(d.nx + 1, d.ny + 1, d.nz + 1, b);
+  const int kchunk = stage_kchunk(d, write_fp64);
+  const dim3 g((d.nx + TX) / TX, (d.ny + TY) / TY, (d.nz + kchunk - 1) / kchunk);
   if (write_fp64)
-    k_mx_stage<true><<<g, b, 0, stream>>>(d, t, fl, win, w0, wout, cs64(s0), ms64(ss), (float)dt_stage, dt_stage, err);
+    k_mx_stage<true><<<g, b, 0, stream>>>(d, t, fl, win, w0, wout, cs64(s0), ms64(ss), (float)dt_stage, dt_stage,
+                                          kchunk, err);
   else
     k_mx_stage<false><<<g, b, 0, stream>>>(d, t, fl, win, w0, wout, cs64(nullptr), ms64(nullptr), (float)dt_stage,
-                                           dt_stage, err);
+                                           dt_stage, kchunk, err);
 }
 
 void mixed_fb_substep(const Dims& d, const Tab& t, const Flags& fl, const WS& win, const WS& wout, float dtau,
