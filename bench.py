@@ -146,14 +146,20 @@ def measured_peak():
         return HBM_FALLBACK, "fallback"
 
 
-def traffic_of(kernel):
-    """DRAM bytes per launch from the committed ncu summary, or None."""
-    p = os.path.join(ROOT, "profiles", "dram_traffic.json")
+def traffic_of(kernel, cells):
+    """DRAM bytes per launch of `kernel` scaled to `cells`, from the committed
+    ncu summary profiles/dram_traffic.md (rows "| kernel | cells | bytes per
+    launch |"), or None when the summary has no row for it."""
+    p = os.path.join(ROOT, "profiles", "dram_traffic.md")
     try:
         with open(p) as f:
-            return json.load(f).get(kernel)
+            for line in f:
+                cols = [c.strip() for c in line.strip().strip("|").split("|")]
+                if len(cols) >= 3 and cols[0] == kernel:
+                    return float(cols[2]) * cells / float(cols[1])
     except (OSError, ValueError):
         return None
+    return None
 
 
 # ---- CPU baseline / reference arm (oracle port on host cores) ---------------
@@ -333,7 +339,7 @@ def main():
 
     # roofline of the dominant kernel class (live CUDA-event times)
     peak, peak_kind = measured_peak()
-    per_cell = {0: (84.0 * 2 + 196.0) / 3.0, 1: 32.0, 2: 156.0, 3: 20.0}
+    per_cell = {0: (56.0 + 84.0 + 196.0) / 3.0, 1: 32.0, 2: 156.0, 3: 20.0}
     names = {0: "k_mx_stage", 1: "k_mx_hevi_col", 2: "k_mx_finish", 3: "k_mx_fb_mom(u,v)"}
     dom = max(ktimes, key=lambda c: ktimes[c][0])
     tot_ms, spans = ktimes[dom]
@@ -357,7 +363,7 @@ def main():
                 "note": "set_state (7 species, pinned host, FieldT layout) + step + get_state per step"},
         "roofline": {"bound": "hbm", "kernel": names[dom], "achieved": achieved, "peak": peak,
                      "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind,
-                     "traffic": traffic_of(names[dom]), "algorithmic_bytes_per_launch": bytes_launch,
+                     "traffic": traffic_of(names[dom], cells), "algorithmic_bytes_per_launch": bytes_launch,
                      "avg_launch_ms": avg_s * 1e3, "launches": spans, "time_share": share},
         "step_roofline": {"bytes_per_cell_update": 1944, "achieved": 1944.0 * value / world / 1e9,
                           "peak": peak, "unit": "GB/s", "frac": 1944.0 * value / world / 1e9 / peak},

@@ -115,16 +115,50 @@ def test_slow_tendency_fp64_exact(vg, oc, scheme):
             assert np.array_equal(vg.interior(s, sp, a), vg.interior(s, sp, b)), vg.SPECIES[sp]
 
 
-def test_slow_tendency_mixed(vg, oc):
-    s = small_setup(vg)
+MIXED_SCHEMES = [
+    dict(),
+    dict(advection=2, weno_scalars=0),
+    dict(advection=4, weno_scalars=0, coriolis=1),
+    dict(advection=6, weno_scalars=0, coriolis=2, moist=1, qv_surface=0.01),
+    dict(weno_advective=0, ref_kind=1, divergence_damping=50.0, divergence_order=2),
+    dict(moist=1, qv_surface=0.01, ref_kind=1, nz=26, z_top=6000.0, shear_u=0.004),
+]
+
+
+def assert_levels_close(vg, s, got, ref, tol, species, what, floors):
+    """Error of every level relative to that level's largest value (or the
+    species' floor): a wrong term confined to one level, e.g. the top or
+    bottom boundary, cannot hide behind a larger tendency elsewhere."""
+    for sp in species:
+        g = vg.interior(s, sp, got[sp])
+        r = vg.interior(s, sp, ref[sp])
+        for k in range(r.shape[0]):
+            scale = max(float(np.abs(r[k]).max()), floors[sp])
+            err = float(np.abs(g[k] - r[k]).max())
+            assert err <= tol * scale or (scale == 0.0 and err == 0.0), \
+                "%s: %s level %d error %.3e scale %.3e" % (what, vg.SPECIES[sp], k, err, scale)
+
+
+@pytest.mark.parametrize("scheme", range(len(MIXED_SCHEMES)))
+@pytest.mark.parametrize("levels", ["", "3"])
+def test_slow_tendency_mixed(vg, oc, scheme, levels, monkeypatch):
+    """Mixed-path slow tendency (FP32) against the oracle, level by level.
+    levels = "3" makes the stage kernel's blocks march 3 levels each, so the
+    chunk starts (fresh column registers and vertical fluxes) are exercised."""
+    monkeypatch.setenv("VIBE_GB300_STAGE_LEVELS", levels)
+    s = small_setup(vg, **MIXED_SCHEMES[scheme])
+    n = 12 if s.moist else 7
     with vg.Model(s, vg.MIXED) as m:
         o = oc.Model(oracle_setup(oc, s), "port")
-        floors = {sp: 1e-3 * np.abs(vg.interior(s, sp, o.get(sp))).max() for sp in range(7)}
+        ref = o.slow_tendency()
+        floors = {sp: 1e-3 * np.abs(vg.interior(s, sp, o.get(sp))).max() for sp in range(n)}
         vs = 1e-3 * velocity_scale(vg, s, o.state())
         for sp in (0, 1, 2):
             floors[sp] = max(floors[sp], vs)
-        assert_state_close(vg, s, m.slow_tendency(), o.slow_tendency(), TOLMX, range(7), "mixed slow tendency",
-                           floors, velocity=False)
+        got = m.slow_tendency()
+        assert_state_close(vg, s, got, ref, TOLMX, range(n), "mixed slow tendency", floors, velocity=False)
+        lf = {sp: 1e-2 * floors[sp] for sp in range(n)}
+        assert_levels_close(vg, s, got, ref, 1e-4, range(n), "mixed slow tendency per level", lf)
 
 
 @pytest.mark.parametrize("pgf", [0, 1])
