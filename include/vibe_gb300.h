@@ -54,9 +54,14 @@ enum vibe_gb300_species {
 };
 
 /* Case and numerics description. Field meaning as in config.hpp:26-68,
- * IcOptions (initial_conditions.hpp:49-74) and ReferenceState; the last
- * four fields select compositions the reference does not provide (see
- * the design doc). Plain C struct, no defaults: fill with
+ * IcOptions (initial_conditions.hpp:49-74) and ReferenceState. The last
+ * five fields select compositions the reference does not provide: the
+ * reference as written integrates the fast terms twice (once in the slow
+ * tendency, once in the substeps) and takes the pressure gradient of the
+ * total Exner function, and diverges within a few steps; pgf_perturbation,
+ * split_fast and weno_advective give the stable composition, acoustic_mode
+ * 2 a dimensionally consistent Crank-Nicolson HEVI with off-centring
+ * hevi_beta. Plain C struct, no defaults: fill with
  * vibe_gb300_setup_defaults() first. */
 typedef struct vibe_gb300_setup {
   int nx, ny, nz;
