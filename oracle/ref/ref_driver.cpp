@@ -13,6 +13,10 @@
 //     (runge_kutta.cpp:92 vs include/vibe/dyn/state.hpp:137-139); here that
 //     update is expanded field by field over the 12 species.
 //   * the acoustic substep follows runge_kutta.cpp:65-75 verbatim.
+//   * vref_si_step follows SemiImplicitIntegrator::step and assemble_rhs
+//     (src/time/semi_implicit.cpp:56-106,167-226), which do not compile
+//     (the same State::add_scaled(Real, Tendency) call, :182); the solve is
+//     the reference's own HelmholtzSolver from make_helmholtz_solver.
 //   * weno_scalars=1 replaces the non-conservative scalar advection of theta
 //     and the moisture species (src/dyn/equations.cpp:129-137) with
 //     Advection::scalar in WENO5 flux form (src/dyn/advection.cpp:144-187)
@@ -36,6 +40,7 @@
 #include "vibe/grid/decomposition.hpp"
 #include "vibe/grid/geometry.hpp"
 #include "vibe/time/acoustic_substep.hpp"
+#include "vibe/time/helmholtz.hpp"
 
 using namespace vibe;
 
@@ -258,6 +263,123 @@ void vref_hevi_substep(vref_model* m, double dtau) {
 
 void vref_sponge(vref_model* m, double dt) {
   m->eq->damping().apply_sponge(*m->state, *m->ref, dt);
+}
+
+namespace {
+grid::Field<Real> cell_field(const grid::Grid& g, const double* p, const char* name) {
+  grid::Field<Real> f(g, grid::Stagger::Cell, name);
+  if (p != nullptr) std::memcpy(f.storage().data(), p, f.storage().size() * sizeof(double));
+  return f;
+}
+int solve_with(vref_model* m, int kind, int max_iter, double tol, int refine, const grid::Field<Real>& a,
+               const grid::Field<Real>& b, const grid::Field<Real>& f, grid::Field<Real>& x, int* iterations,
+               double* residual) {
+  config::ModelConfig cfg = m->cfg;
+  cfg.numerics.helmholtz_max_iter = max_iter;
+  cfg.numerics.helmholtz_tol = tol;
+  auto solver = timeint::make_helmholtz_solver(static_cast<timeint::HelmholtzKind>(kind), *m->grid, cfg);
+  solver->set_iterative_refinement(refine != 0, gpu::Precision::FP64);
+  solver->set_coefficients(a, b);
+  try {
+    solver->solve(a, b, f, x);
+  } catch (const std::exception&) {
+    return 1;
+  }
+  if (iterations) *iterations = solver->iterations();
+  if (residual) *residual = solver->residual();
+  return 0;
+}
+}  // namespace
+
+void vref_helmholtz_apply_norm(vref_model* m, const double* a, const double* b, const double* f,
+                               const double* x, double* out) {
+  const grid::Grid& g = *m->grid;
+  *out = timeint::helmholtz_residual_l2(g, cell_field(g, a, "a"), cell_field(g, b, "b"), cell_field(g, f, "f"),
+                                        cell_field(g, x, "x"));
+}
+
+int vref_helmholtz_solve(vref_model* m, int kind, int max_iter, double tol, int refine, const double* a,
+                         const double* b, const double* f, double* x, int* iterations, double* residual) {
+  const grid::Grid& g = *m->grid;
+  grid::Field<Real> fx = cell_field(g, nullptr, "x");
+  const int rc = solve_with(m, kind, max_iter, tol, refine, cell_field(g, a, "a"), cell_field(g, b, "b"),
+                            cell_field(g, f, "f"), fx, iterations, residual);
+  std::memcpy(x, fx.storage().data(), fx.storage().size() * sizeof(double));
+  return rc;
+}
+
+void vref_multigrid_restrict(vref_model* m, const double* fine, double* coarse) {
+  const grid::Grid& g = *m->grid;
+  grid::Field<Real> c = cell_field(g, nullptr, "c");
+  timeint::multigrid_restrict(cell_field(g, fine, "f"), c);
+  std::memcpy(coarse, c.storage().data(), c.storage().size() * sizeof(double));
+}
+
+void vref_multigrid_prolong(vref_model* m, const double* coarse, double* fine) {
+  const grid::Grid& g = *m->grid;
+  grid::Field<Real> f = cell_field(g, nullptr, "f");
+  timeint::multigrid_prolong(cell_field(g, coarse, "c"), f);
+  std::memcpy(fine, f.storage().data(), f.storage().size() * sizeof(double));
+}
+
+int vref_si_step(vref_model* m, double dt, int kind, int max_iter, double tol, int* iterations,
+                 double* residual, double* pi_new, double* rhs_out, double* a_out) {
+  const grid::Grid& g = *m->grid;
+  const dyn::ReferenceState& ref = *m->ref;
+  dyn::State& s = *m->state;
+  dyn::Tendency& n = *m->slow;
+  slow_tendency(m, s, n);
+  const Int nx = g.nx(), ny = g.ny(), nz = g.nz();
+  const Real half_dt = Real(0.5) * dt;
+  grid::Field<Real> acoef = cell_field(g, nullptr, "a_coef"), bcoef = cell_field(g, nullptr, "b_coef");
+  grid::Field<Real> rhs = cell_field(g, nullptr, "rhs"), x = cell_field(g, nullptr, "pi_new");
+  for (Int k = 0; k < nz; ++k)
+    for (Int j = 0; j < ny; ++j)
+      for (Int i = 0; i < nx; ++i) {
+        acoef(i, j, k) = half_dt * half_dt * (kRd / kCv) * ref.pi0()(i, j, k) * kCp * ref.theta0()(i, j, k);
+        bcoef(i, j, k) = Real(1);
+      }
+  for (Int k = 0; k < nz; ++k)
+    for (Int j = 0; j < ny; ++j)
+      for (Int i = 0; i < nx; ++i) {
+        const Real dx = g.dx_at(i), dy = g.dy_at(j);
+        const Real scale = g.geom().z_top - g.terrain(i, j);
+        const Real dz = std::max(g.dzeta(k) * scale, Real(1));
+        const auto& r0 = ref.rho0();
+        auto flux_div = [&](const grid::Field<Real>& u, const grid::Field<Real>& v, const grid::Field<Real>& w) {
+          const Real fx = u(i + 1, j, k) * Real(0.5) * (r0(i, j, k) + r0(std::min(i + 1, nx - 1), j, k)) -
+                          u(i, j, k) * Real(0.5) * (r0(std::max(i - 1, Int(0)), j, k) + r0(i, j, k));
+          const Real fy = v(i, j + 1, k) * Real(0.5) * (r0(i, j, k) + r0(i, std::min(j + 1, ny - 1), k)) -
+                          v(i, j, k) * Real(0.5) * (r0(i, std::max(j - 1, Int(0)), k) + r0(i, j, k));
+          const Real fz = w(i, j, k + 1) * Real(0.5) * (r0(i, j, k) + r0(i, j, std::min(k + 1, nz - 1))) -
+                          w(i, j, k) * Real(0.5) * (r0(i, j, std::max(k - 1, Int(0))) + r0(i, j, k));
+          return fx / dx + fy / dy + fz / dz;
+        };
+        const Real G = flux_div(s.u(), s.v(), s.w()) + half_dt * flux_div(n.u(), n.v(), n.w());
+        const Real c = (kRd / kCv) * (ref.pi0()(i, j, k) / std::max(ref.rho0()(i, j, k), Real(1e-8)));
+        const Real a0 = acoef(i, j, k);
+        const auto& pi = s.pi();
+        const Real div_a_grad =
+            (a0 * (pi(std::min(i + 1, nx - 1), j, k) - pi(i, j, k)) -
+             a0 * (pi(i, j, k) - pi(std::max(i - 1, Int(0)), j, k))) / (dx * dx) +
+            (a0 * (pi(i, std::min(j + 1, ny - 1), k) - pi(i, j, k)) -
+             a0 * (pi(i, j, k) - pi(i, std::max(j - 1, Int(0)), k))) / (dy * dy);
+        rhs(i, j, k) = pi(i, j, k) - dt * c * G + div_a_grad;
+      }
+  const int rc = solve_with(m, kind, max_iter, tol, 1, acoef, bcoef, rhs, x, iterations, residual);
+  if (pi_new) std::memcpy(pi_new, x.storage().data(), x.storage().size() * sizeof(double));
+  if (rhs_out) std::memcpy(rhs_out, rhs.storage().data(), rhs.storage().size() * sizeof(double));
+  if (a_out) std::memcpy(a_out, acoef.storage().data(), acoef.storage().size() * sizeof(double));
+  if (rc) return 2;
+  s.theta().add_scaled(dt, n.theta());
+  s.qv().add_scaled(dt, n.qv());
+  s.rho().add_scaled(dt, n.rho());
+  for (int sp = static_cast<int>(dyn::Species::Qc); sp <= static_cast<int>(dyn::Species::Qg); ++sp) {
+    const auto species = static_cast<dyn::Species>(sp);
+    s.field(species).add_scaled(dt, n.field(species));
+  }
+  m->eq->damping().apply_sponge(s, ref, dt);
+  return s.has_nonfinite() ? 1 : 0;
 }
 
 }  // extern "C"

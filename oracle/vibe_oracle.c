@@ -1041,6 +1041,349 @@ int vo_rk3_step(vo_model *m, double dt, int n_sub_in) {
 }
 
 /* ------------------------------------------------------------------------ */
+/* Helmholtz family: src/time/helmholtz.cpp:126-495                          */
+/* ------------------------------------------------------------------------ */
+
+/* a cell field over caller storage (FieldT layout, halo 4) */
+static fld fld_view(const vo_model *m, const double *p) {
+  fld f;
+  f.nx = m->nx; f.ny = m->ny; f.nz = m->nz;
+  f.nsx = m->nx + 2 * VO_HALO; f.nsy = m->ny + 2 * VO_HALO; f.nsz = m->nz + 2 * VO_HALO;
+  f.d = (double *)p;
+  return f;
+}
+static fld fld_cell(const vo_model *m) {
+  fld f;
+  fld_alloc(&f, m->nx, m->ny, m->nz, 0);
+  return f;
+}
+static void fld_copy(fld *dst, const fld *src) { memcpy(dst->d, src->d, fld_size(src) * sizeof(double)); }
+
+/* apply_operator, helmholtz.cpp:173-201: y = -div(a grad x) + b x with
+ * arithmetic face means of a and clamped neighbours */
+static void h_apply(const vo_model *m, const fld *a, const fld *b, const fld *x, fld *y) {
+  const int nx = m->nx, ny = m->ny, nz = m->nz;
+  const double dx = m->s.dx, dy = m->s.dy;
+  fld_zero(y);
+  for (int k = 0; k < nz; ++k)
+    for (int j = 0; j < ny; ++j)
+      for (int i = 0; i < nx; ++i) {
+        const double scale = m->s.z_top - g_terrain(m, i, j);
+        const double dz = dmax(g_dzeta(m, k) * scale, 1.0);
+        const double ac = AT(*a, i, j, k);
+        const double ae = 0.5 * (ac + CL(a, i + 1, j, k));
+        const double aw = 0.5 * (ac + CL(a, i - 1, j, k));
+        const double an = 0.5 * (ac + CL(a, i, j + 1, k));
+        const double as = 0.5 * (ac + CL(a, i, j - 1, k));
+        const double at = 0.5 * (ac + CL(a, i, j, k + 1));
+        const double ab = 0.5 * (ac + CL(a, i, j, k - 1));
+        const double xc = AT(*x, i, j, k);
+        const double fx = (ae * (CL(x, i + 1, j, k) - xc) - aw * (xc - CL(x, i - 1, j, k))) / (dx * dx);
+        const double fy = (an * (CL(x, i, j + 1, k) - xc) - as * (xc - CL(x, i, j - 1, k))) / (dy * dy);
+        const double fz = (at * (CL(x, i, j, k + 1) - xc) - ab * (xc - CL(x, i, j, k - 1))) / (dz * dz);
+        AT(*y, i, j, k) = -fx - fy - fz + AT(*b, i, j, k) * xc;
+      }
+}
+
+/* dot_field, helmholtz.cpp:203-207: serial sum over the whole storage */
+static double h_dot(const fld *a, const fld *b) {
+  double s = 0.0;
+  const size_t n = fld_size(a);
+  for (size_t q = 0; q < n; ++q) s += a->d[q] * b->d[q];
+  return s;
+}
+
+/* helmholtz_residual_l2, helmholtz.cpp:211-227 */
+static double h_residual_l2(const vo_model *m, const fld *a, const fld *b, const fld *f, const fld *x) {
+  fld lx = fld_cell(m);
+  h_apply(m, a, b, x, &lx);
+  double s = 0.0;
+  for (int k = 0; k < m->nz; ++k)
+    for (int j = 0; j < m->ny; ++j)
+      for (int i = 0; i < m->nx; ++i) {
+        const double r = AT(lx, i, j, k) - AT(*f, i, j, k);
+        s += r * r;
+      }
+  free(lx.d);
+  return sqrt(s);
+}
+
+/* VerticalTridiagonalSolver::solve, helmholtz.cpp:241-274, with the Thomas
+ * solve of the documented C contract (the reference calls its own C Thomas,
+ * which does not solve the system, c_kernels.c:18-60) */
+static int h_solve_vertical(const vo_model *m, const fld *a, const fld *b, const fld *f, fld *x, int *iters,
+                            double *res) {
+  const int nx = m->nx, ny = m->ny, nz = m->nz;
+  double *sa = (double *)calloc((size_t)nz + 1, sizeof(double)), *sb = (double *)calloc((size_t)nz, sizeof(double));
+  double *sc = (double *)calloc((size_t)nz + 1, sizeof(double)), *sd = (double *)calloc((size_t)nz, sizeof(double));
+  double *sx = (double *)calloc((size_t)nz, sizeof(double)), *ws = (double *)calloc((size_t)nz, sizeof(double));
+  int rc = 0;
+  fld_zero(x);
+  for (int j = 0; j < ny && !rc; ++j)
+    for (int i = 0; i < nx && !rc; ++i) {
+      for (int k = 0; k < nz; ++k) {
+        const double scale = m->s.z_top - g_terrain(m, i, j);
+        const double dz = dmax(g_dzeta(m, k) * scale, 1.0);
+        const double az = 0.5 * (AT(*a, i, j, k) + CL(a, i, j, k + 1));
+        const double azm = 0.5 * (AT(*a, i, j, k) + CL(a, i, j, k - 1));
+        sb[k] = (az + azm) / (dz * dz) + AT(*b, i, j, k);
+        if (k > 0) sa[k - 1] = -azm / (dz * dz);
+        if (k < nz - 1) sc[k] = -az / (dz * dz);
+        sd[k] = AT(*f, i, j, k);
+      }
+      if (vo_tridiagonal_solve(sa, sb, sc, sd, nz, sx, ws) != 0) { rc = 1; break; }
+      for (int k = 0; k < nz; ++k) AT(*x, i, j, k) = sx[k];
+    }
+  free(sa); free(sb); free(sc); free(sd); free(sx); free(ws);
+  *iters = 1;
+  *res = 0.0;
+  return rc;
+}
+
+/* KrylovJacobiSolver::solve, helmholtz.cpp:296-366, operation for operation
+ * (including its residual recomputed from x at the top of each iteration and
+ * the update x += alpha p + omega s) */
+static void h_solve_krylov_jacobi(const vo_model *m, int max_iter, double tol, const fld *a, const fld *b,
+                                  const fld *f, fld *x, int *iters, double *res_out) {
+  const int nx = m->nx, ny = m->ny, nz = m->nz;
+  fld r = fld_cell(m), r0 = fld_cell(m), p = fld_cell(m), v = fld_cell(m), s = fld_cell(m), t = fld_cell(m);
+  fld prec = fld_cell(m), rhat = fld_cell(m), shat = fld_cell(m);
+  const size_t n = fld_size(&r);
+  for (int k = 0; k < nz; ++k)
+    for (int j = 0; j < ny; ++j)
+      for (int i = 0; i < nx; ++i) {
+        const double dx = m->s.dx, dy = m->s.dy;
+        const double scale = m->s.z_top - g_terrain(m, i, j);
+        const double dz = dmax(g_dzeta(m, k) * scale, 1.0);
+        const double ac = AT(*a, i, j, k);
+        const double diag = 2.0 * ac / (dx * dx) + 2.0 * ac / (dy * dy) + 2.0 * ac / (dz * dz) + AT(*b, i, j, k);
+        AT(prec, i, j, k) = 1.0 / dmax(diag, 1e-30);
+      }
+  fld_zero(x);
+  fld_copy(&r, f);
+  fld_copy(&r0, &r);
+  double rho = 1.0, alpha = 1.0, omega = 1.0, rho_prev = 1.0;
+  const double f_norm = sqrt(dmax(h_dot(f, f), 1e-300));
+  double res = 1.0;
+  int it = 0;
+  for (; it < max_iter; ++it) {
+    h_apply(m, a, b, x, &v);
+    for (size_t q = 0; q < n; ++q) r.d[q] = f->d[q] - v.d[q];
+    res = sqrt(h_dot(&r, &r)) / f_norm;
+    if (res < tol) break;
+    for (size_t q = 0; q < n; ++q) rhat.d[q] = prec.d[q] * r.d[q];
+    rho = h_dot(&rhat, &r0);
+    if (fabs(rho) < 1e-300) break;
+    const double beta = (rho / rho_prev) * (alpha / omega);
+    for (size_t q = 0; q < n; ++q) p.d[q] = rhat.d[q] + beta * (p.d[q] - omega * v.d[q]);
+    h_apply(m, a, b, &p, &v);
+    const double denom = h_dot(&r0, &v);
+    alpha = (fabs(denom) > 1e-300) ? rho / denom : 0.0;
+    for (size_t q = 0; q < n; ++q) s.d[q] = r.d[q] - alpha * v.d[q];
+    if (sqrt(h_dot(&s, &s)) / f_norm < tol) {
+      for (size_t q = 0; q < n; ++q) x->d[q] += alpha * p.d[q];
+      break;
+    }
+    for (size_t q = 0; q < n; ++q) shat.d[q] = prec.d[q] * s.d[q];
+    h_apply(m, a, b, &shat, &t);
+    const double tt = h_dot(&t, &t);
+    omega = (tt > 1e-300) ? h_dot(&t, &s) / tt : 0.0;
+    for (size_t q = 0; q < n; ++q) x->d[q] += alpha * p.d[q] + omega * s.d[q];
+    for (size_t q = 0; q < n; ++q) r.d[q] = s.d[q] - omega * t.d[q];
+    rho_prev = rho;
+    if (fabs(omega) < 1e-300) break;
+  }
+  *iters = it;
+  *res_out = res;
+  free(r.d); free(r0.d); free(p.d); free(v.d); free(s.d); free(t.d); free(prec.d); free(rhat.d); free(shat.d);
+}
+
+/* multigrid_restrict, helmholtz.cpp:130-145 (coarse has the fine field's
+ * shape; fine indices clamp at the edge) */
+static void h_restrict(const vo_model *m, const fld *fine, fld *coarse) {
+  for (int k = 0; k < m->nz; ++k)
+    for (int j = 0; j < m->ny; ++j)
+      for (int i = 0; i < m->nx; ++i) {
+        const int fi = 2 * i, fj = 2 * j;
+        double acc = 0.25 * CL(fine, fi, fj, k);
+        acc += 0.125 * (CL(fine, fi - 1, fj, k) + CL(fine, fi + 1, fj, k) + CL(fine, fi, fj - 1, k) +
+                        CL(fine, fi, fj + 1, k));
+        acc += 0.0625 * (CL(fine, fi - 1, fj - 1, k) + CL(fine, fi + 1, fj - 1, k) + CL(fine, fi - 1, fj + 1, k) +
+                         CL(fine, fi + 1, fj + 1, k));
+        AT(*coarse, i, j, k) = acc;
+      }
+}
+
+/* multigrid_prolong, helmholtz.cpp:147-164 */
+static void h_prolong(const vo_model *m, const fld *coarse, fld *fine) {
+  for (int k = 0; k < m->nz; ++k)
+    for (int j = 0; j < m->ny; ++j)
+      for (int i = 0; i < m->nx; ++i) {
+        const double xs = 0.5 * (double)i, ys = 0.5 * (double)j;
+        const int i0 = (int)floor(xs), j0 = (int)floor(ys);
+        const double wx = xs - (double)i0, wy = ys - (double)j0;
+        AT(*fine, i, j, k) = lerp(lerp(CL(coarse, i0, j0, k), CL(coarse, i0 + 1, j0, k), wx),
+                                  lerp(CL(coarse, i0, j0 + 1, k), CL(coarse, i0 + 1, j0 + 1, k), wx), wy);
+      }
+}
+
+/* KrylovMultigridSolver::solve, helmholtz.cpp:393-405. Its coarse solve
+ * (restrict f, solve, prolong into x) is discarded: the inner solver starts
+ * by zeroing x (:316). The result is the inner solve of f, restated so. */
+static void h_solve_krylov_mg(const vo_model *m, int max_iter, double tol, const fld *a, const fld *b,
+                              const fld *f, fld *x, int *iters, double *res) {
+  h_solve_krylov_jacobi(m, max_iter, tol, a, b, f, x, iters, res);
+}
+
+/* RefinementSolver::solve, helmholtz.cpp:433-462 (max_refine 3) */
+static void h_solve_refined(const vo_model *m, int max_iter, double tol, int refine, const fld *a, const fld *b,
+                            const fld *f, fld *x, int *iters, double *res) {
+  int it_in = 0;
+  double res_in = 1.0;
+  h_solve_krylov_mg(m, max_iter, tol, a, b, f, x, &it_in, &res_in);
+  if (!refine) { *iters = it_in; *res = res_in; return; }
+  fld r = fld_cell(m), lx = fld_cell(m), dxf = fld_cell(m);
+  const size_t n = fld_size(&r);
+  int total = it_in;
+  double residual = res_in;
+  for (int it = 0; it < 3; ++it) {
+    h_apply(m, a, b, x, &lx);
+    double rn = 0.0, fn = 0.0;
+    for (size_t q = 0; q < n; ++q) {
+      r.d[q] = f->d[q] - lx.d[q];
+      rn += r.d[q] * r.d[q];
+      fn += f->d[q] * f->d[q];
+    }
+    const double rel = sqrt(rn / dmax(fn, 1e-300));
+    residual = rel;
+    if (rel < tol) break;
+    fld_zero(&dxf);
+    h_solve_krylov_mg(m, max_iter, tol, a, b, &r, &dxf, &it_in, &res_in);
+    for (size_t q = 0; q < n; ++q) x->d[q] += dxf.d[q];
+    total += it_in;
+  }
+  *iters = total;
+  *res = residual;
+  free(r.d); free(lx.d); free(dxf.d);
+}
+
+static int h_solve(const vo_model *m, int kind, int max_iter, double tol, int refine, const fld *a, const fld *b,
+                   const fld *f, fld *x, int *iters, double *res) {
+  if (kind == VO_HZ_VERTICAL) return h_solve_vertical(m, a, b, f, x, iters, res);
+  if (kind == VO_HZ_KRYLOV_JACOBI) {
+    h_solve_krylov_jacobi(m, max_iter, tol, a, b, f, x, iters, res);
+    return 0;
+  }
+  h_solve_refined(m, max_iter, tol, refine, a, b, f, x, iters, res);
+  return 0;
+}
+
+void vo_helmholtz_apply(const vo_model *m, const double *a, const double *b, const double *x, double *y) {
+  const fld fa = fld_view(m, a), fb = fld_view(m, b), fx = fld_view(m, x);
+  fld fy = fld_view(m, y);
+  h_apply(m, &fa, &fb, &fx, &fy);
+}
+
+double vo_helmholtz_residual_l2(const vo_model *m, const double *a, const double *b, const double *f,
+                                const double *x) {
+  const fld fa = fld_view(m, a), fb = fld_view(m, b), ff = fld_view(m, f), fx = fld_view(m, x);
+  return h_residual_l2(m, &fa, &fb, &ff, &fx);
+}
+
+int vo_helmholtz_solve(const vo_model *m, int kind, int max_iter, double tol, int refine, const double *a,
+                       const double *b, const double *f, double *x, int *iterations, double *residual) {
+  const fld fa = fld_view(m, a), fb = fld_view(m, b), ff = fld_view(m, f);
+  fld fx = fld_view(m, x);
+  return h_solve(m, kind, max_iter, tol, refine, &fa, &fb, &ff, &fx, iterations, residual);
+}
+
+void vo_multigrid_restrict(const vo_model *m, const double *fine, double *coarse) {
+  const fld ff = fld_view(m, fine);
+  fld fc = fld_view(m, coarse);
+  h_restrict(m, &ff, &fc);
+}
+void vo_multigrid_prolong(const vo_model *m, const double *coarse, double *fine) {
+  const fld fc = fld_view(m, coarse);
+  fld ff = fld_view(m, fine);
+  h_prolong(m, &fc, &ff);
+}
+
+/* SemiImplicitIntegrator::assemble_rhs, semi_implicit.cpp:56-106: a =
+ * (dt/2)^2 (Rd/cv) pi0 cp theta0, b = 1, rhs = pi - dt c G + (horizontal)
+ * div(a0 grad pi), G = div(rho0 u^n) + dt/2 div(rho0 N_u) */
+static void si_assemble(const vo_model *m, const fld *st, const fld *n, double dt, fld *acoef, fld *bcoef,
+                        fld *rhs) {
+  const int nx = m->nx, ny = m->ny, nz = m->nz;
+  const double half_dt = 0.5 * dt;
+  const fld *pi0 = &m->ref[VO_PI0], *th0 = &m->ref[VO_THETA0], *r0 = &m->ref[VO_RHO0];
+  for (int k = 0; k < nz; ++k)
+    for (int j = 0; j < ny; ++j)
+      for (int i = 0; i < nx; ++i) {
+        AT(*acoef, i, j, k) = half_dt * half_dt * (K_RD / K_CV) * AT(*pi0, i, j, k) * K_CP * AT(*th0, i, j, k);
+        AT(*bcoef, i, j, k) = 1.0;
+      }
+  for (int k = 0; k < nz; ++k)
+    for (int j = 0; j < ny; ++j)
+      for (int i = 0; i < nx; ++i) {
+        const double dx = m->s.dx, dy = m->s.dy;
+        const double scale = m->s.z_top - g_terrain(m, i, j);
+        const double dz = dmax(g_dzeta(m, k) * scale, 1.0);
+        const fld *U[2] = {&st[VO_U], &n[VO_U]}, *V[2] = {&st[VO_V], &n[VO_V]}, *W[2] = {&st[VO_W], &n[VO_W]};
+        double dv[2];
+        for (int c = 0; c < 2; ++c) { /* flux_div lambda, :82-91 (unclamped i+1, j+1, k+1 face reads) */
+          const double fx = AT(*U[c], i + 1, j, k) * 0.5 * (AT(*r0, i, j, k) + AT(*r0, imin(i + 1, nx - 1), j, k)) -
+                            AT(*U[c], i, j, k) * 0.5 * (AT(*r0, imax(i - 1, 0), j, k) + AT(*r0, i, j, k));
+          const double fy = AT(*V[c], i, j + 1, k) * 0.5 * (AT(*r0, i, j, k) + AT(*r0, i, imin(j + 1, ny - 1), k)) -
+                            AT(*V[c], i, j, k) * 0.5 * (AT(*r0, i, imax(j - 1, 0), k) + AT(*r0, i, j, k));
+          const double fz = AT(*W[c], i, j, k + 1) * 0.5 * (AT(*r0, i, j, k) + AT(*r0, i, j, imin(k + 1, nz - 1))) -
+                            AT(*W[c], i, j, k) * 0.5 * (AT(*r0, i, j, imax(k - 1, 0)) + AT(*r0, i, j, k));
+          dv[c] = fx / dx + fy / dy + fz / dz;
+        }
+        const double G = dv[0] + half_dt * dv[1];
+        const double c = (K_RD / K_CV) * (AT(*pi0, i, j, k) / dmax(AT(*r0, i, j, k), 1e-8));
+        const double a0 = AT(*acoef, i, j, k);
+        const fld *pi = &st[VO_PI];
+        const double pc = AT(*pi, i, j, k);
+        const double div_a_grad =
+            (a0 * (AT(*pi, imin(i + 1, nx - 1), j, k) - pc) - a0 * (pc - AT(*pi, imax(i - 1, 0), j, k))) / (dx * dx) +
+            (a0 * (AT(*pi, i, imin(j + 1, ny - 1), k) - pc) - a0 * (pc - AT(*pi, i, imax(j - 1, 0), k))) / (dy * dy);
+        AT(*rhs, i, j, k) = pc - dt * c * G + div_a_grad;
+      }
+}
+
+/* SemiImplicitIntegrator::step, semi_implicit.cpp:167-226 (O-SI). The
+ * shipped step does not compile (State::add_scaled(Real, Tendency),
+ * :182); restated with that update expanded field by field. Observable
+ * effects kept: the Helmholtz solve (its solution and statistics), the
+ * explicit theta/qv/rho/moisture update, the sponge and the non-finite check.
+ * The shipped step writes the solved pressure only into its local copy
+ * s_explicit (update_from_pressure, :188), which it then drops, so u, v, w
+ * and pi of the state change only through the sponge; that copy is not
+ * formed here. No physics driver, RA filter off (its default). */
+int vo_si_step(vo_model *m, double dt, int kind, int max_iter, double tol, int *iterations, double *residual,
+               double *pi_new, double *rhs_out, double *a_out) {
+  fld acoef = fld_cell(m), bcoef = fld_cell(m), rhs = fld_cell(m), x = fld_cell(m);
+  slow_tendency_split(m, m->st, m->slow);
+  si_assemble(m, m->st, m->slow, dt, &acoef, &bcoef, &rhs);
+  int it = 0;
+  double res = 0.0;
+  int rc = h_solve(m, kind, max_iter, tol, 1, &acoef, &bcoef, &rhs, &x, &it, &res);
+  if (iterations) *iterations = it;
+  if (residual) *residual = res;
+  if (pi_new) memcpy(pi_new, x.d, fld_size(&x) * sizeof(double));
+  if (rhs_out) memcpy(rhs_out, rhs.d, fld_size(&rhs) * sizeof(double));
+  if (a_out) memcpy(a_out, acoef.d, fld_size(&acoef) * sizeof(double));
+  free(acoef.d); free(bcoef.d); free(rhs.d); free(x.d);
+  if (rc) return 2;
+  add_scaled(&m->st[VO_THETA], dt, &m->slow[VO_THETA]);
+  add_scaled(&m->st[VO_QV], dt, &m->slow[VO_QV]);
+  add_scaled(&m->st[VO_RHO], dt, &m->slow[VO_RHO]);
+  for (int sp = VO_QC; sp <= VO_QG; ++sp) add_scaled(&m->st[sp], dt, &m->slow[sp]);
+  sponge_apply(m, dt);
+  return has_nonfinite(m) ? 1 : 0;
+}
+
+/* ------------------------------------------------------------------------ */
 /* C-ABI kernels: src/common/c_kernels.c                                     */
 /* ------------------------------------------------------------------------ */
 int vo_tridiagonal_solve(const double *a, const double *b, const double *c, const double *d, int n,

@@ -115,6 +115,32 @@ void vo_acoustic_substep(vo_model *m, double dtau);
 void vo_hevi_substep(vo_model *m, double dtau);
 void vo_sponge(vo_model *m, double dt);
 
+/* Helmholtz family on the model's grid (src/time/helmholtz.cpp:126-495).
+ * a, b, f, x, y are cell FieldT storage arrays (vo_storage_size(m, VO_RHO)
+ * doubles, halo 4). apply: y = -div(a grad x) + b x (helmholtz.cpp:173-201);
+ * residual_l2: ||A x - f||_2 over the interior (:214-229). kind as
+ * HelmholtzKind (helmholtz.hpp:57): 0 vertical_tridiagonal, 1
+ * krylov_multigrid (the factory wraps it in the iterative-refinement solver,
+ * :486-488), 2 krylov_jacobi. Returns 0, or 1 where the reference throws
+ * (singular column). */
+enum vo_helmholtz_kind { VO_HZ_VERTICAL = 0, VO_HZ_KRYLOV_MG = 1, VO_HZ_KRYLOV_JACOBI = 2 };
+void vo_helmholtz_apply(const vo_model *m, const double *a, const double *b, const double *x, double *y);
+double vo_helmholtz_residual_l2(const vo_model *m, const double *a, const double *b, const double *f,
+                                const double *x);
+int vo_helmholtz_solve(const vo_model *m, int kind, int max_iter, double tol, int refine,
+                       const double *a, const double *b, const double *f, double *x, int *iterations,
+                       double *residual);
+/* multigrid_restrict / multigrid_prolong (helmholtz.cpp:130-164): same-size
+ * cell fields (the reference's coarse field lives on the fine grid). */
+void vo_multigrid_restrict(const vo_model *m, const double *fine, double *coarse);
+void vo_multigrid_prolong(const vo_model *m, const double *coarse, double *fine);
+/* One SemiImplicitIntegrator::step (semi_implicit.cpp:167-226, O-SI) with
+ * the Helmholtz solver of `kind`. pi_new (nullable) receives the solver's
+ * solution; rhs and a_coef (nullable) the assembled right-hand side and a.
+ * Returns 0, 1 on a non-finite state, 2 on a singular column. */
+int vo_si_step(vo_model *m, double dt, int kind, int max_iter, double tol, int *iterations, double *residual,
+               double *pi_new, double *rhs, double *a_coef);
+
 /* C-ABI kernels restated (src/common/c_kernels.c). vo_tridiagonal_solve
  * follows the documented contract (c_kernels.h:38-55) with the textbook
  * recurrence of thomas_solve (helmholtz.cpp:57-86): the shipped
@@ -151,6 +177,14 @@ void vref_slow_tendency(vref_model *m, double *const *out);
 void vref_acoustic_substep(vref_model *m, double dtau);
 void vref_hevi_substep(vref_model *m, double dtau);
 void vref_sponge(vref_model *m, double dt);
+void vref_helmholtz_apply_norm(vref_model *m, const double *a, const double *b, const double *f,
+                               const double *x, double *out);
+int vref_helmholtz_solve(vref_model *m, int kind, int max_iter, double tol, int refine, const double *a,
+                         const double *b, const double *f, double *x, int *iterations, double *residual);
+void vref_multigrid_restrict(vref_model *m, const double *fine, double *coarse);
+void vref_multigrid_prolong(vref_model *m, const double *coarse, double *fine);
+int vref_si_step(vref_model *m, double dt, int kind, int max_iter, double tol, int *iterations,
+                 double *residual, double *pi_new, double *rhs, double *a_coef);
 
 #ifdef __cplusplus
 }

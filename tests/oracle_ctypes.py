@@ -96,7 +96,16 @@ def _load(kind):
         "acoustic_substep": (None, [vp, _D]),
         "hevi_substep": (None, [vp, _D]),
         "sponge": (None, [vp, _D]),
+        "helmholtz_solve": (_I, [vp, _I, _I, _D, _I, vp, vp, vp, vp, ctypes.POINTER(_I), dp]),
+        "multigrid_restrict": (None, [vp, vp, vp]),
+        "multigrid_prolong": (None, [vp, vp, vp]),
+        "si_step": (_I, [vp, _D, _I, _I, _D, ctypes.POINTER(_I), dp, vp, vp, vp]),
     }
+    if kind == "port":
+        sig["helmholtz_apply"] = (None, [vp, vp, vp, vp, vp])
+        sig["helmholtz_residual_l2"] = (_D, [vp, vp, vp, vp, vp])
+    else:
+        sig["helmholtz_apply_norm"] = (None, [vp, vp, vp, vp, vp, dp])
     fns = {}
     for name, (res, args) in sig.items():
         f = getattr(lib, p + name)
@@ -215,3 +224,54 @@ class Model:
 
     def sponge(self, dt):
         self._f["sponge"](self.h, dt)
+
+    # ---- Helmholtz family and the semi-implicit step ----
+    def _cell(self, a):
+        a = np.ascontiguousarray(a, dtype=np.float64).ravel()
+        assert a.size == self.size(3)
+        return a
+
+    def helmholtz_apply(self, a, b, x):
+        a, b, x = self._cell(a), self._cell(b), self._cell(x)
+        y = np.zeros(self.size(3))
+        self._f["helmholtz_apply"](self.h, a.ctypes.data, b.ctypes.data, x.ctypes.data, y.ctypes.data)
+        return y
+
+    def helmholtz_residual_l2(self, a, b, f, x):
+        a, b, f, x = self._cell(a), self._cell(b), self._cell(f), self._cell(x)
+        if self.kind == "port":
+            return float(self._f["helmholtz_residual_l2"](self.h, a.ctypes.data, b.ctypes.data, f.ctypes.data,
+                                                          x.ctypes.data))
+        out = ctypes.c_double()
+        self._f["helmholtz_apply_norm"](self.h, a.ctypes.data, b.ctypes.data, f.ctypes.data, x.ctypes.data,
+                                        ctypes.byref(out))
+        return out.value
+
+    def helmholtz_solve(self, kind, max_iter, tol, a, b, f, refine=1):
+        """Returns (x, iterations, residual, rc)."""
+        a, b, f = self._cell(a), self._cell(b), self._cell(f)
+        x = np.zeros(self.size(3))
+        it, res = _I(), _D()
+        rc = self._f["helmholtz_solve"](self.h, kind, max_iter, tol, refine, a.ctypes.data, b.ctypes.data,
+                                        f.ctypes.data, x.ctypes.data, ctypes.byref(it), ctypes.byref(res))
+        return x, it.value, res.value, int(rc)
+
+    def multigrid_restrict(self, fine):
+        fine = self._cell(fine)
+        out = np.zeros(self.size(3))
+        self._f["multigrid_restrict"](self.h, fine.ctypes.data, out.ctypes.data)
+        return out
+
+    def multigrid_prolong(self, coarse):
+        coarse = self._cell(coarse)
+        out = np.zeros(self.size(3))
+        self._f["multigrid_prolong"](self.h, coarse.ctypes.data, out.ctypes.data)
+        return out
+
+    def si_step(self, dt, kind=1, max_iter=200, tol=1e-8):
+        """One O-SI step. Returns (rc, iterations, residual, pi_new, rhs, a_coef)."""
+        outs = [np.zeros(self.size(3)) for _ in range(3)]
+        it, res = _I(), _D()
+        rc = self._f["si_step"](self.h, dt, kind, max_iter, tol, ctypes.byref(it), ctypes.byref(res),
+                                *[o.ctypes.data for o in outs])
+        return int(rc), it.value, res.value, outs[0], outs[1], outs[2]

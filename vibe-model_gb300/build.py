@@ -21,7 +21,10 @@ SOURCES = [("step_fp64.cu", "step_fp64.o", []),
            ("step_fp64.cu", "step_fp64_exact.o", ["-DVGB_FP64_EXACT", "--fmad=false"]),
            ("step_mixed.cu", "step_mixed.o", []),
            ("model.cu", "model.o", []),
-           ("ckern.cu", "ckern.o", [])]
+           ("ckern.cu", "ckern.o", []),
+           ("helmholtz_ref.cu", "helmholtz_ref.o", ["--fmad=false"]),
+           ("helmholtz_mg.cu", "helmholtz_mg.o", []),
+           ("helmholtz_api.cu", "helmholtz_api.o", [])]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -1,0 +1,523 @@
+// vibe-model_gb300/csrc/helmholtz_mg.cu
+//
+// Right-preconditioned BiCGSTAB (van der Vorst 1992) with a geometric
+// multigrid V-cycle as preconditioner, for the reference's Helmholtz
+// operator y = -div(a grad x) + b x (src/time/helmholtz.cpp:173-201),
+// templated on the working precision (FP32 for the mixed solver, FP64).
+//
+// Operator in coupling form. For a cell, with W/E/S/N/B/T neighbours,
+//   (A x) = cD x + cE (x - xE) + cW (x - xW) + cN (x - xN) + cS (x - xS)
+//           + cT (x - xT) + cB (x - xB),
+// cE = (a + aE)/2 / dx^2 (0 on the east boundary: the reference's clamp
+// makes that flux vanish), cW(i) = cE(i-1), likewise N/S; cT = (a + aT)/2 /
+// dz^2 and cB = (a + aB)/2 / dz^2 with the cell's own dz (so A is not
+// symmetric on a stretched grid), cD = b.
+//
+// Multigrid. The vertical couplings dominate (dz << dx), so the smoother is
+// a vertical-line Gauss-Seidel: every column solves its tridiagonal system
+// exactly with the horizontal neighbours fixed, columns in red-black order
+// ((i + j) parity), one thread per column with coalesced loads along i; the
+// column LU factors are computed once per coefficient set. Coarse grids
+// halve nx and ny and keep nz (semi-coarsening); coarse couplings are the
+// 2x2 aggregates: cT, cB, cD averaged, the horizontal face couplings summed
+// over the two fine faces of the coarse face and divided by 8 (= the
+// rediscretised a/(2h)^2). Residuals are restricted by the 2x2 mean and
+// corrections prolonged piecewise constant. V(1,1) cycle, the coarsest grid
+// smoothed 8 times.
+#include <cmath>
+#include <cstdio>
+#include <vector>
+
+#include "helmholtz.cuh"
+
+namespace vgb {
+
+constexpr int kMgMaxLevels = 8;
+constexpr int kMT = 256;
+
+template <typename T>
+struct MgLevel {
+  int nx, ny, nz;
+  size_t n;
+  T *cE, *cN, *cT, *cB, *cD;  // couplings and mass term
+  T *lc, *li;                 // column LU: c'_k, 1/denom_k
+  T *x, *r, *t;               // correction, right-hand side, residual
+};
+
+template <typename T>
+struct MgSolver {
+  HGeo g;
+  int L = 0;
+  MgLevel<T> lv[kMgMaxLevels];
+  T *x, *r, *r0, *p, *v, *s, *t, *ph, *sh;  // Krylov vectors (fine level)
+  double* part = nullptr;                   // 2 x kRedBlocks partial sums
+  double* sc = nullptr;                     // device scalars
+  double* hsc = nullptr;                    // pinned host copy
+  std::vector<void*> allocs;
+};
+
+namespace {
+
+enum Sc { RHO_OLD = 0, ALPHA = 1, OMEGA = 2, RHO_NEW = 3, RV = 4, TS = 5, TT = 6, RR = 7, BREAK = 8, NSC = 16 };
+
+__device__ __forceinline__ void cell_of(size_t c, int nx, int ny, int& i, int& j, int& k) {
+  i = (int)(c % nx);
+  const size_t cj = c / nx;
+  j = (int)(cj % ny);
+  k = (int)(cj / ny);
+}
+
+// A x at cell c of level l (coupling form)
+template <typename T>
+__device__ __forceinline__ T apply_at(const MgLevel<T>& l, const T* __restrict__ x, size_t c, int i, int j, int k) {
+  const size_t pl = (size_t)l.nx * l.ny;
+  const T xc = x[c];
+  T y = l.cD[c] * xc;
+  const T ce = l.cE[c], cn = l.cN[c], ct = l.cT[c], cb = l.cB[c];
+  if (i + 1 < l.nx) y += ce * (xc - x[c + 1]);
+  if (i > 0) y += l.cE[c - 1] * (xc - x[c - 1]);
+  if (j + 1 < l.ny) y += cn * (xc - x[c + l.nx]);
+  if (j > 0) y += l.cN[c - l.nx] * (xc - x[c - l.nx]);
+  if (k + 1 < l.nz) y += ct * (xc - x[c + pl]);
+  if (k > 0) y += cb * (xc - x[c - pl]);
+  return y;
+}
+
+// ---- coefficient set-up ----
+template <typename T>
+__global__ void k_fine_coefs(HGeo g, const double* __restrict__ a, const double* __restrict__ b, MgLevel<T> l) {
+  const size_t n = g.n(), pl = (size_t)g.nx * g.ny;
+  for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < n; c += (size_t)gridDim.x * blockDim.x) {
+    int i, j, k;
+    cell_of(c, g.nx, g.ny, i, j, k);
+    const double dz = dmax(g.dzeta[k] * g.scale[(size_t)j * g.nx + i], 1.0);
+    const double ac = a[c], idx2 = 1.0 / (g.dx * g.dx), idy2 = 1.0 / (g.dy * g.dy), idz2 = 1.0 / (dz * dz);
+    l.cE[c] = (T)(i + 1 < g.nx ? 0.5 * (ac + a[c + 1]) * idx2 : 0.0);
+    l.cN[c] = (T)(j + 1 < g.ny ? 0.5 * (ac + a[c + g.nx]) * idy2 : 0.0);
+    l.cT[c] = (T)(k + 1 < g.nz ? 0.5 * (ac + a[c + pl]) * idz2 : 0.0);
+    l.cB[c] = (T)(k > 0 ? 0.5 * (ac + a[c - pl]) * idz2 : 0.0);
+    l.cD[c] = (T)b[c];
+  }
+}
+
+template <typename T>
+__global__ void k_coarse_coefs(MgLevel<T> f, MgLevel<T> cl) {
+  const size_t pf = (size_t)f.nx * f.ny;
+  for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < cl.n; c += (size_t)gridDim.x * blockDim.x) {
+    int I, J, k;
+    cell_of(c, cl.nx, cl.ny, I, J, k);
+    const size_t f00 = (size_t)k * pf + (size_t)(2 * J) * f.nx + 2 * I;
+    const size_t f10 = f00 + 1, f01 = f00 + f.nx, f11 = f01 + 1;
+    cl.cE[c] = (f.cE[f10] + f.cE[f11]) * (T)0.125;
+    cl.cN[c] = (f.cN[f01] + f.cN[f11]) * (T)0.125;
+    cl.cT[c] = (f.cT[f00] + f.cT[f10] + f.cT[f01] + f.cT[f11]) * (T)0.25;
+    cl.cB[c] = (f.cB[f00] + f.cB[f10] + f.cB[f01] + f.cB[f11]) * (T)0.25;
+    cl.cD[c] = (f.cD[f00] + f.cD[f10] + f.cD[f01] + f.cD[f11]) * (T)0.25;
+  }
+}
+
+template <typename T>
+__device__ __forceinline__ T diag_at(const MgLevel<T>& l, size_t c, int i, int j) {
+  T m = l.cD[c] + l.cE[c] + l.cN[c] + l.cT[c] + l.cB[c];
+  if (i > 0) m += l.cE[c - 1];
+  if (j > 0) m += l.cN[c - l.nx];
+  return m;
+}
+
+// column LU of (diag, -cB, -cT): denom_k = m_k + cB_k c'_{k-1}, c'_k = -cT_k / denom_k
+template <typename T>
+__global__ void k_column_lu(MgLevel<T> l) {
+  const int col = blockIdx.x * blockDim.x + threadIdx.x;
+  if (col >= l.nx * l.ny) return;
+  const int i = col % l.nx, j = col / l.nx;
+  const size_t pl = (size_t)l.nx * l.ny;
+  T cprev = 0;
+  for (int k = 0; k < l.nz; ++k) {
+    const size_t c = (size_t)k * pl + col;
+    const T den = diag_at(l, c, i, j) + (k > 0 ? l.cB[c] * cprev : (T)0);
+    const T inv = (T)1 / den;
+    cprev = -l.cT[c] * inv;
+    l.li[c] = inv;
+    l.lc[c] = cprev;
+  }
+}
+
+// ---- multigrid kernels ----
+// one red-black half sweep of vertical-line Gauss-Seidel on columns with
+// (i + j) % 2 == color; zero_nb: the horizontal neighbours are taken as 0
+// (first half sweep from a zero initial guess)
+template <typename T>
+__global__ void k_smooth(MgLevel<T> l, const T* __restrict__ rhs, T* __restrict__ x, int color, int zero_nb) {
+  const int col = blockIdx.x * blockDim.x + threadIdx.x;
+  if (col >= l.nx * l.ny) return;
+  const int i = col % l.nx, j = col / l.nx;
+  if (((i + j) & 1) != color) return;
+  const size_t pl = (size_t)l.nx * l.ny;
+  T dp = 0;
+  for (int k = 0; k < l.nz; ++k) {
+    const size_t c = (size_t)k * pl + col;
+    T d = rhs[c];
+    if (!zero_nb) {
+      if (i + 1 < l.nx) d += l.cE[c] * x[c + 1];
+      if (i > 0) d += l.cE[c - 1] * x[c - 1];
+      if (j + 1 < l.ny) d += l.cN[c] * x[c + l.nx];
+      if (j > 0) d += l.cN[c - l.nx] * x[c - l.nx];
+    }
+    dp = (d + (k > 0 ? l.cB[c] * dp : (T)0)) * l.li[c];
+    x[c] = dp;
+  }
+  T xn = dp;
+  for (int k = l.nz - 1; k-- > 0;) {
+    const size_t c = (size_t)k * pl + col;
+    xn = x[c] - l.lc[c] * xn;
+    x[c] = xn;
+  }
+}
+
+template <typename T>
+__global__ void k_resid(MgLevel<T> l, const T* __restrict__ rhs, const T* __restrict__ x, T* __restrict__ out) {
+  for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < l.n; c += (size_t)gridDim.x * blockDim.x) {
+    int i, j, k;
+    cell_of(c, l.nx, l.ny, i, j, k);
+    out[c] = rhs[c] - apply_at(l, x, c, i, j, k);
+  }
+}
+
+template <typename T>
+__global__ void k_restrict(MgLevel<T> f, const T* __restrict__ t, MgLevel<T> cl) {
+  const size_t pf = (size_t)f.nx * f.ny;
+  for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < cl.n; c += (size_t)gridDim.x * blockDim.x) {
+    int I, J, k;
+    cell_of(c, cl.nx, cl.ny, I, J, k);
+    const size_t f00 = (size_t)k * pf + (size_t)(2 * J) * f.nx + 2 * I;
+    cl.r[c] = (t[f00] + t[f00 + 1] + t[f00 + f.nx] + t[f00 + f.nx + 1]) * (T)0.25;
+  }
+}
+
+template <typename T>
+__global__ void k_prolong_add(MgLevel<T> f, T* __restrict__ x, MgLevel<T> cl) {
+  const size_t pc = (size_t)cl.nx * cl.ny;
+  for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < f.n; c += (size_t)gridDim.x * blockDim.x) {
+    int i, j, k;
+    cell_of(c, f.nx, f.ny, i, j, k);
+    x[c] += cl.x[(size_t)k * pc + (size_t)(j >> 1) * cl.nx + (i >> 1)];
+  }
+}
+
+// ---- Krylov kernels; dot products accumulate in FP64 ----
+__device__ __forceinline__ double block_sum(double v, double* sh) {
+  sh[threadIdx.x] = v;
+  __syncthreads();
+  for (int w = kMT / 2; w > 0; w >>= 1) {
+    if ((int)threadIdx.x < w) sh[threadIdx.x] += sh[threadIdx.x + w];
+    __syncthreads();
+  }
+  const double s = sh[0];
+  __syncthreads();
+  return s;
+}
+
+template <typename T>
+__global__ void k_init(const double* __restrict__ r64, double inv, size_t n, T* r, T* r0, T* x, T* p, T* v,
+                       double* part) {
+  __shared__ double sh[kMT];
+  double acc = 0.0;
+  for (size_t q = blockIdx.x * (size_t)kMT + threadIdx.x; q < n; q += (size_t)gridDim.x * kMT) {
+    const T rv = (T)(r64[q] * inv);
+    r[q] = rv;
+    r0[q] = rv;
+    x[q] = 0;
+    p[q] = 0;
+    v[q] = 0;
+    acc += (double)rv * (double)rv;
+  }
+  const double s = block_sum(acc, sh);
+  if (threadIdx.x == 0) part[blockIdx.x] = s;
+}
+
+// p = r + beta (p - omega v), beta = (rho_new / rho_old) (alpha / omega)
+template <typename T>
+__global__ void k_upd_p(const T* __restrict__ r, T* __restrict__ p, const T* __restrict__ v, size_t n,
+                        const double* __restrict__ sc) {
+  const double beta = (sc[RHO_NEW] / sc[RHO_OLD]) * (sc[ALPHA] / sc[OMEGA]);
+  const T b = (T)beta, om = (T)sc[OMEGA];
+  for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < n; q += (size_t)gridDim.x * blockDim.x)
+    p[q] = r[q] + b * (p[q] - om * v[q]);
+}
+
+// y = A xin, partials of (w1, y) [and (y, y) when two]
+template <typename T, bool kTwo>
+__global__ void k_apply_dot(MgLevel<T> l, const T* __restrict__ xin, T* __restrict__ y, const T* __restrict__ w1,
+                            double* part) {
+  __shared__ double sh[kMT];
+  double a1 = 0.0, a2 = 0.0;
+  for (size_t c = blockIdx.x * (size_t)kMT + threadIdx.x; c < l.n; c += (size_t)gridDim.x * kMT) {
+    int i, j, k;
+    cell_of(c, l.nx, l.ny, i, j, k);
+    const T yv = apply_at(l, xin, c, i, j, k);
+    y[c] = yv;
+    a1 += (double)w1[c] * (double)yv;
+    if (kTwo) a2 += (double)yv * (double)yv;
+  }
+  const double s1 = block_sum(a1, sh);
+  if (threadIdx.x == 0) part[blockIdx.x] = s1;
+  if (kTwo) {
+    const double s2 = block_sum(a2, sh);
+    if (threadIdx.x == 0) part[kRedBlocks + blockIdx.x] = s2;
+  }
+}
+
+// s = r - alpha v
+template <typename T>
+__global__ void k_upd_s(const T* __restrict__ r, const T* __restrict__ v, T* __restrict__ s, size_t n,
+                        const double* __restrict__ sc) {
+  const T al = (T)sc[ALPHA];
+  for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < n; q += (size_t)gridDim.x * blockDim.x)
+    s[q] = r[q] - al * v[q];
+}
+
+// x += alpha ph + omega sh; r = s - omega t; partials (r, r), (r0, r)
+template <typename T>
+__global__ void k_upd_xr(T* __restrict__ x, const T* __restrict__ ph, const T* __restrict__ shv,
+                         const T* __restrict__ s, const T* __restrict__ t, T* __restrict__ r,
+                         const T* __restrict__ r0, size_t n, const double* __restrict__ sc, double* part) {
+  __shared__ double sh[kMT];
+  const T al = (T)sc[ALPHA], om = (T)sc[OMEGA];
+  double a1 = 0.0, a2 = 0.0;
+  for (size_t q = blockIdx.x * (size_t)kMT + threadIdx.x; q < n; q += (size_t)gridDim.x * kMT) {
+    x[q] += al * ph[q] + om * shv[q];
+    const T rv = s[q] - om * t[q];
+    r[q] = rv;
+    a1 += (double)rv * (double)rv;
+    a2 += (double)r0[q] * (double)rv;
+  }
+  const double s1 = block_sum(a1, sh);
+  if (threadIdx.x == 0) part[blockIdx.x] = s1;
+  const double s2 = block_sum(a2, sh);
+  if (threadIdx.x == 0) part[kRedBlocks + blockIdx.x] = s2;
+}
+
+enum Op { OP_INIT = 0, OP_ALPHA = 1, OP_OMEGA = 2, OP_XR = 3 };
+
+__global__ void k_finish(const double* __restrict__ part, int nb, int op, double* sc) {
+  __shared__ double sh[kMT];
+  double a1 = 0.0, a2 = 0.0;
+  for (int q = threadIdx.x; q < nb; q += kMT) {
+    a1 += part[q];
+    a2 += part[kRedBlocks + q];
+  }
+  const double s1 = block_sum(a1, sh);
+  const double s2 = block_sum(a2, sh);
+  if (threadIdx.x != 0) return;
+  if (op == OP_INIT) {
+    sc[RR] = s1;
+    sc[RHO_NEW] = s1;
+    sc[RHO_OLD] = 1.0;
+    sc[ALPHA] = 1.0;
+    sc[OMEGA] = 1.0;
+    sc[BREAK] = 0.0;
+  } else if (op == OP_ALPHA) {
+    sc[RV] = s1;
+    if (s1 == 0.0 || !isfinite(s1)) {
+      sc[BREAK] = 1.0;
+      sc[ALPHA] = 0.0;
+    } else {
+      sc[ALPHA] = sc[RHO_NEW] / s1;
+    }
+  } else if (op == OP_OMEGA) {
+    sc[TS] = s1;
+    sc[TT] = s2;
+    if (!(s2 > 0.0) || !isfinite(s2)) {
+      sc[BREAK] = 1.0;
+      sc[OMEGA] = 0.0;
+    } else {
+      sc[OMEGA] = s1 / s2;
+      if (sc[OMEGA] == 0.0) sc[BREAK] = 1.0;
+    }
+  } else {  // OP_XR
+    sc[RR] = s1;
+    sc[RHO_OLD] = sc[RHO_NEW];
+    sc[RHO_NEW] = s2;
+    if (s2 == 0.0 || !isfinite(s1)) sc[BREAK] = 1.0;
+  }
+}
+
+template <typename T>
+__global__ void k_out(const T* __restrict__ x, double scale, double* __restrict__ d, size_t n) {
+  for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < n; q += (size_t)gridDim.x * blockDim.x)
+    d[q] = (double)x[q] * scale;
+}
+
+int cells_grid(size_t n) {
+  const size_t b = (n + kMT - 1) / kMT;
+  return (int)(b < 4096 ? (b > 0 ? b : 1) : 4096);
+}
+int red_grid(size_t n) {
+  const size_t b = (n + kMT - 1) / kMT;
+  return (int)(b < (size_t)kRedBlocks ? (b > 0 ? b : 1) : kRedBlocks);
+}
+int cols_grid(const int cols) { return (cols + 127) / 128; }
+
+template <typename T>
+void smooth(const MgLevel<T>& l, const T* rhs, T* x, int color, int zero_nb, cudaStream_t s) {
+  k_smooth<T><<<cols_grid(l.nx * l.ny), 128, 0, s>>>(l, rhs, x, color, zero_nb);
+}
+
+// x = V(rhs) on level li (zero initial guess)
+template <typename T>
+void vcycle(MgSolver<T>* m, int li, const T* rhs, T* x, cudaStream_t s) {
+  MgLevel<T>& l = m->lv[li];
+  if (li == m->L - 1) {
+    smooth(l, rhs, x, 0, 1, s);
+    smooth(l, rhs, x, 1, 0, s);
+    for (int it = 1; it < 8; ++it) {
+      smooth(l, rhs, x, 0, 0, s);
+      smooth(l, rhs, x, 1, 0, s);
+    }
+    return;
+  }
+  MgLevel<T>& cl = m->lv[li + 1];
+  smooth(l, rhs, x, 0, 1, s);
+  smooth(l, rhs, x, 1, 0, s);
+  k_resid<T><<<cells_grid(l.n), kMT, 0, s>>>(l, rhs, x, l.t);
+  k_restrict<T><<<cells_grid(cl.n), kMT, 0, s>>>(l, l.t, cl);
+  vcycle(m, li + 1, cl.r, cl.x, s);
+  k_prolong_add<T><<<cells_grid(l.n), kMT, 0, s>>>(l, x, cl);
+  smooth(l, rhs, x, 1, 0, s);
+  smooth(l, rhs, x, 0, 0, s);
+}
+
+template <typename T>
+T* dev_alloc(MgSolver<T>* m, size_t n) {
+  void* p = nullptr;
+  if (cudaMalloc(&p, n * sizeof(T)) != cudaSuccess) return nullptr;
+  m->allocs.push_back(p);
+  return (T*)p;
+}
+
+}  // namespace
+
+template <typename T>
+MgSolver<T>* mg_create(const HGeo& g, int max_levels) {
+  auto* m = new MgSolver<T>();
+  m->g = g;
+  int nx = g.nx, ny = g.ny;
+  const int cap = max_levels < 1 ? 1 : (max_levels > kMgMaxLevels ? kMgMaxLevels : max_levels);
+  bool ok = true;
+  for (int l = 0; l < cap; ++l) {
+    MgLevel<T>& L = m->lv[l];
+    L.nx = nx;
+    L.ny = ny;
+    L.nz = g.nz;
+    L.n = (size_t)nx * ny * g.nz;
+    T** arrs[] = {&L.cE, &L.cN, &L.cT, &L.cB, &L.cD, &L.lc, &L.li, &L.x, &L.r, &L.t};
+    for (T** a : arrs) {
+      *a = dev_alloc(m, L.n);
+      ok = ok && *a != nullptr;
+    }
+    m->L = l + 1;
+    if (nx % 2 || ny % 2 || nx / 2 < 4 || ny / 2 < 4) break;
+    nx /= 2;
+    ny /= 2;
+  }
+  const size_t n = g.n();
+  T** kv[] = {&m->x, &m->r, &m->r0, &m->p, &m->v, &m->s, &m->t, &m->ph, &m->sh};
+  for (T** a : kv) {
+    *a = dev_alloc(m, n);
+    ok = ok && *a != nullptr;
+  }
+  void* p = nullptr;
+  ok = ok && cudaMalloc(&p, 2 * kRedBlocks * sizeof(double)) == cudaSuccess;
+  if (p) m->allocs.push_back(p), m->part = (double*)p;
+  p = nullptr;
+  ok = ok && cudaMalloc(&p, NSC * sizeof(double)) == cudaSuccess;
+  if (p) m->allocs.push_back(p), m->sc = (double*)p;
+  ok = ok && cudaMallocHost(&m->hsc, NSC * sizeof(double)) == cudaSuccess;
+  if (!ok) {
+    mg_destroy(m);
+    return nullptr;
+  }
+  return m;
+}
+
+template <typename T>
+void mg_destroy(MgSolver<T>* m) {
+  if (!m) return;
+  for (void* p : m->allocs) cudaFree(p);
+  if (m->hsc) cudaFreeHost(m->hsc);
+  delete m;
+}
+
+template <typename T>
+int mg_levels(const MgSolver<T>* m) {
+  return m->L;
+}
+
+template <typename T>
+int mg_set_coefficients(MgSolver<T>* m, const double* a, const double* b, cudaStream_t s) {
+  k_fine_coefs<T><<<cells_grid(m->g.n()), kMT, 0, s>>>(m->g, a, b, m->lv[0]);
+  for (int l = 1; l < m->L; ++l)
+    k_coarse_coefs<T><<<cells_grid(m->lv[l].n), kMT, 0, s>>>(m->lv[l - 1], m->lv[l]);
+  for (int l = 0; l < m->L; ++l)
+    k_column_lu<T><<<cols_grid(m->lv[l].nx * m->lv[l].ny), 128, 0, s>>>(m->lv[l]);
+  return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+template <typename T>
+int mg_solve(MgSolver<T>* m, const double* r64, double* d64, double rtol, int max_iter, cudaStream_t s) {
+  const size_t n = m->g.n();
+  const int nb = red_grid(n), cg = cells_grid(n);
+  MgLevel<T>& f = m->lv[0];
+  // scale the right-hand side to unit norm (FP32 range), FP64 dot
+  dot64(r64, r64, n, m->part, m->sc + NSC - 1, s);
+  if (cudaMemcpyAsync(m->hsc, m->sc + NSC - 1, sizeof(double), cudaMemcpyDeviceToHost, s) != cudaSuccess) return -1;
+  if (cudaStreamSynchronize(s) != cudaSuccess) return -1;
+  const double rn = std::sqrt(m->hsc[0]);
+  if (!(rn > 0.0) || !std::isfinite(rn)) {
+    cudaMemsetAsync(d64, 0, n * sizeof(double), s);
+    return 0;
+  }
+  k_init<T><<<nb, kMT, 0, s>>>(r64, 1.0 / rn, n, m->r, m->r0, m->x, m->p, m->v, m->part);
+  k_finish<<<1, kMT, 0, s>>>(m->part, nb, OP_INIT, m->sc);
+  int it = 0;
+  bool broke = false;
+  for (; it < max_iter; ++it) {
+    k_upd_p<T><<<cg, kMT, 0, s>>>(m->r, m->p, m->v, n, m->sc);
+    vcycle(m, 0, m->p, m->ph, s);
+    k_apply_dot<T, false><<<nb, kMT, 0, s>>>(f, m->ph, m->v, m->r0, m->part);
+    k_finish<<<1, kMT, 0, s>>>(m->part, nb, OP_ALPHA, m->sc);
+    k_upd_s<T><<<cg, kMT, 0, s>>>(m->r, m->v, m->s, n, m->sc);
+    vcycle(m, 0, m->s, m->sh, s);
+    k_apply_dot<T, true><<<nb, kMT, 0, s>>>(f, m->sh, m->t, m->s, m->part);
+    k_finish<<<1, kMT, 0, s>>>(m->part, nb, OP_OMEGA, m->sc);
+    k_upd_xr<T><<<nb, kMT, 0, s>>>(m->x, m->ph, m->sh, m->s, m->t, m->r, m->r0, n, m->sc, m->part);
+    k_finish<<<1, kMT, 0, s>>>(m->part, nb, OP_XR, m->sc);
+    if (cudaMemcpyAsync(m->hsc, m->sc, NSC * sizeof(double), cudaMemcpyDeviceToHost, s) != cudaSuccess) return -1;
+    if (cudaStreamSynchronize(s) != cudaSuccess) return -1;
+    if (m->hsc[BREAK] != 0.0) {
+      broke = true;
+      ++it;
+      break;
+    }
+    if (std::sqrt(m->hsc[RR]) <= rtol) {
+      ++it;
+      break;
+    }
+  }
+  k_out<T><<<cg, kMT, 0, s>>>(m->x, rn, d64, n);
+  if (cudaGetLastError() != cudaSuccess) return -1;
+  return broke ? -it : it;
+}
+
+template MgSolver<float>* mg_create<float>(const HGeo&, int);
+template MgSolver<double>* mg_create<double>(const HGeo&, int);
+template void mg_destroy<float>(MgSolver<float>*);
+template void mg_destroy<double>(MgSolver<double>*);
+template int mg_levels<float>(const MgSolver<float>*);
+template int mg_levels<double>(const MgSolver<double>*);
+template int mg_set_coefficients<float>(MgSolver<float>*, const double*, const double*, cudaStream_t);
+template int mg_set_coefficients<double>(MgSolver<double>*, const double*, const double*, cudaStream_t);
+template int mg_solve<float>(MgSolver<float>*, const double*, double*, double, int, cudaStream_t);
+template int mg_solve<double>(MgSolver<double>*, const double*, double*, double, int, cudaStream_t);
+
+}  // namespace vgb

@@ -317,3 +317,117 @@ def advect_scalar_flux(q, rho, u, v, w, dzeta, zs, nx, ny, nz, dx, dy, z_top):
     out = np.full(nx * ny * nz, np.nan)
     lib.vibe_advect_scalar_flux_f64(*[_ptr(k) for k in keep], nx, ny, nz, dx, dy, z_top, out.ctypes.data)
     return out
+
+
+# ---- Helmholtz solvers (include/vibe_helmholtz.h) ---------------------------
+HZ_VERTICAL_TRIDIAGONAL, HZ_KRYLOV_MULTIGRID, HZ_KRYLOV_JACOBI, HZ_MG_BICGSTAB_FP64, HZ_MG_BICGSTAB_MIXED = range(5)
+_vp = ctypes.c_void_p
+for _name, _res, _args in (
+        ("vibe_helmholtz_create", _I, [_I, _I, _I, _I, _D, _D, _D, _vp, _vp, _I, _D, ctypes.POINTER(_vp)]),
+        ("vibe_helmholtz_destroy", None, [_vp]),
+        ("vibe_helmholtz_set_coefficients", _I, [_vp, _vp, _vp]),
+        ("vibe_helmholtz_solve", _I, [_vp, _vp, _vp, _vp, _vp]),
+        ("vibe_helmholtz_set_coefficients_dev", _I, [_vp, _vp, _vp, _vp]),
+        ("vibe_helmholtz_solve_dev", _I, [_vp, _vp, _vp, _vp]),
+        ("vibe_helmholtz_apply_dev", _I, [_vp, _vp, _vp, _vp]),
+        ("vibe_helmholtz_iterations", _I, [_vp]),
+        ("vibe_helmholtz_residual", _D, [_vp]),
+        ("vibe_helmholtz_name", ctypes.c_char_p, [_vp]),
+        ("vibe_helmholtz_set_iterative_refinement", _I, [_vp, _I, _I]),
+        ("vibe_helmholtz_levels", _I, [_vp]),
+        ("vibe_helmholtz_residual_l2", _D, [_vp, _vp, _vp]),
+        ("vibe_helmholtz_last_error", ctypes.c_char_p, [])):
+    _f = getattr(lib, _name)
+    _f.restype = _res
+    _f.argtypes = _args
+
+
+class HelmholtzError(RuntimeError):
+    def __init__(self, rc):
+        super().__init__("helmholtz rc=%d: %s" % (rc, lib.vibe_helmholtz_last_error().decode()))
+        self.rc = rc
+
+
+class Helmholtz:
+    """~ timeint::HelmholtzSolver from make_helmholtz_solver (helmholtz.hpp:63-98).
+    Fields are host arrays in FieldT cell storage (halo 4); the *_dev
+    methods take device addresses of nx*ny*nz doubles (i fastest)."""
+
+    def __init__(self, kind, nx, ny, nz, dx, dy, z_top, dzeta, zs=None, max_iter=200, tol=1e-8):
+        self.kind, self.shape = kind, (nz, ny, nx)
+        self.h = _vp()
+        dz = np.ascontiguousarray(dzeta, dtype=np.float64)
+        zz = None if zs is None else np.ascontiguousarray(zs, dtype=np.float64)
+        rc = lib.vibe_helmholtz_create(kind, nx, ny, nz, dx, dy, z_top, dz.ctypes.data,
+                                       None if zz is None else zz.ctypes.data, max_iter, tol, ctypes.byref(self.h))
+        if rc:
+            raise HelmholtzError(rc)
+
+    def close(self):
+        if self.h:
+            lib.vibe_helmholtz_destroy(self.h)
+            self.h = _vp()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_coefficients(self, a, b):
+        a, b = (np.ascontiguousarray(v, dtype=np.float64) for v in (a, b))
+        rc = lib.vibe_helmholtz_set_coefficients(self.h, a.ctypes.data, b.ctypes.data)
+        if rc:
+            raise HelmholtzError(rc)
+
+    def solve(self, a, b, f):
+        """Returns (rc, x): rc 0 or 1 (singular column), x in FieldT storage."""
+        f = np.ascontiguousarray(f, dtype=np.float64)
+        x = np.full(f.size, np.nan)
+        keep = [None if v is None else np.ascontiguousarray(v, dtype=np.float64) for v in (a, b)]
+        rc = lib.vibe_helmholtz_solve(self.h, *[None if v is None else v.ctypes.data for v in keep], f.ctypes.data,
+                                      x.ctypes.data)
+        if rc not in (0, 1):
+            raise HelmholtzError(rc)
+        return rc, x
+
+    def set_coefficients_dev(self, a_ptr, b_ptr, stream=0):
+        rc = lib.vibe_helmholtz_set_coefficients_dev(self.h, a_ptr, b_ptr, stream)
+        if rc:
+            raise HelmholtzError(rc)
+
+    def solve_dev(self, f_ptr, x_ptr, stream=0):
+        rc = lib.vibe_helmholtz_solve_dev(self.h, f_ptr, x_ptr, stream)
+        if rc not in (0, 1):
+            raise HelmholtzError(rc)
+        return rc
+
+    def apply_dev(self, x_ptr, y_ptr, stream=0):
+        rc = lib.vibe_helmholtz_apply_dev(self.h, x_ptr, y_ptr, stream)
+        if rc:
+            raise HelmholtzError(rc)
+
+    def iterations(self):
+        return int(lib.vibe_helmholtz_iterations(self.h))
+
+    def residual(self):
+        return float(lib.vibe_helmholtz_residual(self.h))
+
+    def name(self):
+        return lib.vibe_helmholtz_name(self.h).decode()
+
+    def levels(self):
+        return int(lib.vibe_helmholtz_levels(self.h))
+
+    def set_iterative_refinement(self, on, precision=3):
+        lib.vibe_helmholtz_set_iterative_refinement(self.h, 1 if on else 0, precision)
+
+    def residual_l2(self, f, x):
+        f, x = (np.ascontiguousarray(v, dtype=np.float64) for v in (f, x))
+        return float(lib.vibe_helmholtz_residual_l2(self.h, f.ctypes.data, x.ctypes.data))
