@@ -55,6 +55,52 @@ def case_setup(vg_setup_cls, nx=NX, ny=NY):
     return vg_setup_cls.defaults(nx=nx, ny=ny, **CASE)
 
 
+# Semi-implicit workload: 256 x 256 x 64, dx = 2 km, 20 km top (uniform
+# zeta), Gaussian hill h = 800 m with 10 km half-width, N = 0.01 profile,
+# u = 15 m/s, dt = 30 s; the reference's own composition (flags 0).
+SI_CASE = dict(nx=256, ny=256, nz=64, dx=2000.0, dy=2000.0, z_top=20000.0, zeta_first=1.0, zeta_stretch=1.0,
+               terrain_kind=1, hill_h=800.0, hill_a=10000.0, hill_xc=256000.0, hill_yc=256000.0,
+               ref_kind=1, theta0=300.0, bv_n=0.01, profile_dz=250.0, bubble_amplitude=0.0, qv_surface=0.0,
+               u_background=15.0, shear_u=0.0, advection=2, weno_scalars=0, weno_advective=0,
+               pgf_perturbation=0, split_fast=0, acoustic_mode=0)
+SI_DT, SI_TOL = 30.0, 1e-10
+
+
+def si_leg(vg, steps=3):
+    """Helmholtz solve of the semi-implicit step on the 256x256x64 hill case:
+    iterations and device time of the mixed solver (FP32 multigrid-BiCGSTAB
+    inside FP64 refinement to a relative residual of 1e-10), its error
+    against the FP64 solve of the same operator, and what the reference's
+    default solver (Jacobi-BiCGSTAB in the refinement wrapper) does on it."""
+    s = vg.Setup.defaults(**SI_CASE)
+    out = {"workload": "256x256x64 hill (h=800 m, a=10 km), dx=2 km, dt=30 s, N=0.01, u=15 m/s",
+           "cells": 256 * 256 * 64, "tol": SI_TOL}
+    with vg.Model(s, vg.FP64) as mx, vg.Model(s, vg.FP64) as m64:
+        ms, its = [], []
+        err_max = err_rms = 0.0
+        for step in range(steps + 1):
+            it4, res4, x4 = mx.si_step(SI_DT, kind=vg.HZ_MG_BICGSTAB_MIXED, tol=SI_TOL, want_pi=True)
+            ms4 = mx.si_stats()[2]
+            it3, res3, x3 = m64.si_step(SI_DT, kind=vg.HZ_MG_BICGSTAB_FP64, tol=SI_TOL, want_pi=True)
+            ms3 = m64.si_stats()[2]
+            if step == 0:
+                continue  # first call builds the solvers
+            ms.append(ms4)
+            its.append(it4)
+            d = x4 - x3
+            err_max = max(err_max, float(np.abs(d).max() / np.abs(x3).max()))
+            err_rms = max(err_rms, float(np.sqrt(np.mean(d * d)) / np.sqrt(np.mean(x3 * x3))))
+        out.update({"mixed_solve_ms": float(np.median(ms)), "mixed_iterations": int(np.median(its)),
+                    "mixed_residual": res4, "fp64_solve_ms": ms3, "fp64_iterations": it3, "fp64_residual": res3,
+                    "mixed_vs_fp64_max_rel_err": err_max, "mixed_vs_fp64_rms_rel_err": err_rms})
+    with vg.Model(s, vg.FP64) as mr:
+        itr, resr, _ = mr.si_step(SI_DT, kind=vg.HZ_KRYLOV_MULTIGRID)
+        out["reference_solver"] = {"kind": "krylov_multigrid (refinement wrapper), max_iter 200, tol 1e-8",
+                                   "iterations": itr, "residual": resr if np.isfinite(resr) else str(resr),
+                                   "solve_ms": mr.si_stats()[2]}
+    return out
+
+
 def perturbed_state(setup, theta, rho, zeta, seed=1, nx_full=NX, ny_full=NY, x_off=0, y_off=0):
     """theta/pi storage arrays with the seeded perturbations (numpy set-up)."""
     rng = np.random.default_rng(seed)
@@ -227,6 +273,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--nx", type=int, default=NX, help="domain size (profiling runs use smaller cases)")
     ap.add_argument("--ny", type=int, default=NY)
+    ap.add_argument("--no-si", action="store_true", help="skip the semi-implicit (Helmholtz) leg")
     ap.add_argument("--only", choices=["all", "mixed"], default="all",
                     help="mixed: time the mixed path only (no e2e, no FP64 leg)")
     args = ap.parse_args()
@@ -333,6 +380,8 @@ def main():
     ms_64 = max_over_ranks(timed_steps(f64, k64))
     f64.close()
 
+    si = si_leg(vg) if not args.no_si else None
+
     value = world * cells * args.steps / (ms_mx * 1e-3)
     value64 = world * cells * k64 / (ms_64 * 1e-3)
     e2e = world * cells * e2e_steps / (ms_e2e * 1e-3)
@@ -370,6 +419,8 @@ def main():
         "gpu_launches": launches,
         "clocks": clk.summary(),
     }
+    if si is not None:
+        line["semi_implicit"] = si
     if cpu is not None:
         line["cpu_baseline"] = cpu
     print(json.dumps(line))

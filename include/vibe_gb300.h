@@ -132,6 +132,24 @@ int vibe_gb300_acoustic_substep(vibe_gb300_model *m, double dtau);
 int vibe_gb300_hevi_substep(vibe_gb300_model *m, double dtau);
 int vibe_gb300_sponge(vibe_gb300_model *m, double dt);
 
+/* One semi-implicit step, replacing SemiImplicitIntegrator::step
+ * (src/time/semi_implicit.cpp:167-226) as the reference's code computes it
+ * (FP64 precisions only): slow tendency R; Helmholtz problem of
+ * assemble_rhs (:56-106: a = (dt/2)^2 (Rd/cv) pi0 cp theta0, b = 1); solve
+ * with the solver helmholtz_kind of include/vibe_helmholtz.h (the
+ * reference's default is krylov_multigrid, max_iter 200, tol 1e-8);
+ * theta, qv, rho and the moisture species += dt R; sponge; non-finite check.
+ * The shipped step writes the solved pressure only into a copy of the state
+ * that it then drops, so u, v, w and pi change only through the sponge.
+ * iterations, residual: the solver's statistics (nullable); pi_new
+ * (nullable): the solution, host FieldT cell storage. */
+int vibe_gb300_si_step(vibe_gb300_model *m, double dt, int helmholtz_kind, int max_iter, double tol,
+                       int *iterations, double *residual, double *pi_new);
+/* Statistics of the last semi-implicit step's solve (IntegratorStats::
+ * helmholtz_iterations / helmholtz_residual, integrator.hpp:53-59) and its
+ * device time in ms (coefficient set-up + solve, CUDA events). */
+int vibe_gb300_si_stats(const vibe_gb300_model *m, int *iterations, double *residual, double *solve_ms);
+
 /* Bulk forms of set/get_field over species 0..nspecies-1 (NULL entries are
  * skipped). Asynchronous on the model stream: host arrays must stay valid
  * until vibe_gb300_sync(); pinned host memory makes the copies overlap. */

@@ -13,6 +13,7 @@
 
 #include "step_kernels.cuh"
 #include "vibe_gb300.h"
+#include "vibe_helmholtz.h"
 
 using namespace vgb;
 
@@ -101,6 +102,15 @@ struct vibe_gb300_model {
   std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> ev_open;
   double class_ms[kClasses] = {};
   long class_n[kClasses] = {};
+  // semi-implicit step: Helmholtz solver and its problem (nx*ny*nz each)
+  vibe_helmholtz* hz = nullptr;
+  int hz_kind = -1, hz_max_iter = 0;
+  double hz_tol = 0.0;
+  double *hz_a = nullptr, *hz_b = nullptr, *hz_f = nullptr, *hz_x = nullptr;
+  int hz_iterations = 0;
+  double hz_residual = 0.0;
+  double hz_ms = 0.0;
+  cudaEvent_t hz_ev[2] = {nullptr, nullptr};
 };
 
 namespace {
@@ -765,6 +775,8 @@ int vibe_gb300_model_create(const vibe_gb300_setup* s, int precision, vibe_gb300
 }
 
 void vibe_gb300_model_destroy(vibe_gb300_model* m) {
+  if (m && m->hz) vibe_helmholtz_destroy(m->hz);
+  if (m && m->hz_ev[0]) { cudaEventDestroy(m->hz_ev[0]); cudaEventDestroy(m->hz_ev[1]); }
   if (!m) return;
   if (m->stream) cudaStreamSynchronize(m->stream);
   collect_timing(m);
@@ -943,6 +955,88 @@ int vibe_gb300_sponge(vibe_gb300_model* m, double dt) {
   if (int rc = sync_working(m)) return rc;
   CUDA_OK(cudaGetLastError());
   return read_status(m);
+}
+
+// SemiImplicitIntegrator::step (src/time/semi_implicit.cpp:167-226) as the
+// reference's code computes it (O-SI). The shipped step solves for pi' and
+// writes the solution with update_from_pressure into its local copy
+// s_explicit, which it then drops; that copy has no effect on the state and
+// is not formed here. No physics driver; the RA filter is off (default).
+int vibe_gb300_si_step(vibe_gb300_model* m, double dt, int kind, int max_iter, double tol, int* iterations,
+                       double* residual, double* pi_new) {
+  if (!m || !(dt > 0.0) || kind < 0 || kind > 4 || max_iter < 1) return fail(VIBE_GB300_EBADARG, "bad argument");
+  if (m->precision == VIBE_GB300_MIXED)
+    return fail(VIBE_GB300_EUNSUPPORTED, "the semi-implicit step runs on the FP64 precisions");
+  const Dims& d = m->d;
+  const size_t n = (size_t)d.nx * d.ny * d.nz;
+  if (!m->hz || m->hz_kind != kind || m->hz_max_iter != max_iter || m->hz_tol != tol) {
+    if (m->hz) vibe_helmholtz_destroy(m->hz);
+    m->hz = nullptr;
+    std::vector<double> dz(d.nz);
+    for (int k = 0; k < d.nz; ++k) dz[k] = m->hs.zeta[k + 1] - m->hs.zeta[k];
+    if (vibe_helmholtz_create(kind, d.nx, d.ny, d.nz, m->su.dx, m->su.dy, m->su.z_top, dz.data(), m->hs.zs.data(),
+                              max_iter, tol, &m->hz) != VIBE_C_OK)
+      return fail(VIBE_GB300_EDEVICE, std::string("helmholtz solver: ") + vibe_helmholtz_last_error());
+    m->hz_kind = kind;
+    m->hz_max_iter = max_iter;
+    m->hz_tol = tol;
+    if (!m->hz_a) {
+      int rc = dalloc(m, &m->hz_a, n);
+      rc = rc ? rc : dalloc(m, &m->hz_b, n);
+      rc = rc ? rc : dalloc(m, &m->hz_f, n);
+      rc = rc ? rc : dalloc(m, &m->hz_x, n);
+      if (rc) return rc;
+    }
+  }
+  double* const* st = m->S[m->cur];
+  m->f64->slow_tendency(d, m->met, m->fl, st, m->tend, m->scratch, m->stream);
+  si_assemble(d, m->met, st, m->tend, dt, m->hz_a, m->hz_b, m->hz_f, m->stream);
+  CUDA_OK(cudaGetLastError());
+  if (!m->hz_ev[0]) {
+    CUDA_OK(cudaEventCreate(&m->hz_ev[0]));
+    CUDA_OK(cudaEventCreate(&m->hz_ev[1]));
+  }
+  CUDA_OK(cudaEventRecord(m->hz_ev[0], m->stream));
+  if (vibe_helmholtz_set_coefficients_dev(m->hz, m->hz_a, m->hz_b, (vibe_stream_t)m->stream) != VIBE_C_OK)
+    return fail(VIBE_GB300_EDEVICE, std::string("helmholtz coefficients: ") + vibe_helmholtz_last_error());
+  const int hrc = vibe_helmholtz_solve_dev(m->hz, m->hz_f, m->hz_x, (vibe_stream_t)m->stream);
+  CUDA_OK(cudaEventRecord(m->hz_ev[1], m->stream));
+  CUDA_OK(cudaEventSynchronize(m->hz_ev[1]));
+  {
+    float ms = 0.f;
+    CUDA_OK(cudaEventElapsedTime(&ms, m->hz_ev[0], m->hz_ev[1]));
+    m->hz_ms = ms;
+  }
+  m->hz_iterations = vibe_helmholtz_iterations(m->hz);
+  m->hz_residual = vibe_helmholtz_residual(m->hz);
+  if (iterations) *iterations = m->hz_iterations;
+  if (residual) *residual = m->hz_residual;
+  if (hrc == VIBE_C_ERR_SINGULAR) return fail(VIBE_GB300_ESINGULAR, "singular Helmholtz column");
+  if (hrc != VIBE_C_OK) return fail(VIBE_GB300_EDEVICE, std::string("helmholtz solve: ") + vibe_helmholtz_last_error());
+  if (pi_new) {
+    si_to_cells(d, m->hz_x, m->tmp[PI], m->stream);
+    k_unpack<<<1024, 256, 0, m->stream>>>(d, m->nsx[RHO], m->nsy[RHO], m->nsz[RHO], d.nx, d.ny, d.nz, m->tmp[PI],
+                                          m->d_stage_in);
+    CUDA_OK(cudaMemcpyAsync(pi_new, m->d_stage_in, storage_count(m, RHO) * sizeof(double), cudaMemcpyDeviceToHost,
+                            m->stream));
+  }
+  const int upd[] = {THETA, QV, RHO, QC, QR, QI, QS, QG};
+  for (int q : upd) si_cells_add_scaled(d, st[q], m->tend[q], dt, m->stream);
+  int kmin = d.nz + 1;
+  for (int k = 0; k < d.nz; ++k)
+    if (m->hs.sponge[k] > 0.0) { kmin = k; break; }
+  m->f64->sponge(d, m->met, st, kmin, dt, m->stream);
+  m->f64->nonfinite(d, st, m->d_err, m->stream);
+  CUDA_OK(cudaGetLastError());
+  return read_status(m);
+}
+
+int vibe_gb300_si_stats(const vibe_gb300_model* m, int* iterations, double* residual, double* solve_ms) {
+  if (!m) return fail(VIBE_GB300_EBADARG, "bad argument");
+  if (iterations) *iterations = m->hz_iterations;
+  if (residual) *residual = m->hz_residual;
+  if (solve_ms) *solve_ms = m->hz_ms;
+  return 0;
 }
 
 int vibe_gb300_set_state(vibe_gb300_model* m, const double* const* host, int nspecies) {

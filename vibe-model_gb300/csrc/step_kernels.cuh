@@ -32,6 +32,13 @@ void fp64_cons_hevi_substep_exact(const Dims& d, const Metric& m, const Flags& f
 void fp64_sponge_exact(const Dims& d, const Metric& m, double* const* st, int kmin, double dt, cudaStream_t stream);
 void fp64_nonfinite_exact(const Dims& d, double* const* st, unsigned* err, cudaStream_t stream);
 
+// ---- semi-implicit step (si_step.cu, no FMA contraction) ----
+// a, b, f: nx*ny*nz (Helmholtz solver layout); st, tend: model layout
+void si_assemble(const Dims& d, const Metric& met, double* const* st, double* const* tend, double dt, double* a,
+                 double* b, double* f, cudaStream_t s);
+void si_cells_add_scaled(const Dims& d, double* x, const double* y, double a, cudaStream_t s);
+void si_to_cells(const Dims& d, const double* in, double* out, cudaStream_t s);
+
 // ---- mixed path (step_mixed.cu): FP64 state, FP32 working state ----
 // Horizontally uniform reference state on flat terrain: every coefficient
 // is a function of k only and lives in these FP32 tables (device).

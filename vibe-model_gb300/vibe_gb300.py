@@ -93,6 +93,8 @@ _sigs = {
     "vibe_gb300_stream": (_vp, [_vp]),
     "vibe_gb300_launches_per_step": (_I, [_vp, _I]),
     "vibe_gb300_last_error": (ctypes.c_char_p, []),
+    "vibe_gb300_si_step": (_I, [_vp, _D, _I, _I, _D, ctypes.POINTER(_I), _dp, _vp]),
+    "vibe_gb300_si_stats": (_I, [_vp, ctypes.POINTER(_I), _dp, _dp]),
     # C-ABI kernels (include/vibe_c_kernels.h)
     "vibe_tridiagonal_solve_f64": (_I, [_vp, _vp, _vp, _vp, _I, _vp, _vp]),
     "vibe_tridiagonal_solve_batched_f64": (_I, [_vp, _vp, _vp, _vp, _I, _I, _vp]),
@@ -256,6 +258,21 @@ class Model:
 
     def launches_per_step(self, n_sub):
         return int(lib.vibe_gb300_launches_per_step(self.h, n_sub))
+
+    def si_step(self, dt, kind=1, max_iter=200, tol=1e-8, want_pi=False):
+        """One semi-implicit step (SemiImplicitIntegrator::step). Returns
+        (iterations, residual, pi_new or None); pi_new in FieldT storage."""
+        it, res = ctypes.c_int(), ctypes.c_double()
+        pin = np.full(self.size(3), np.nan) if want_pi else None
+        _check(lib.vibe_gb300_si_step(self.h, dt, kind, max_iter, tol, ctypes.byref(it), ctypes.byref(res),
+                                      None if pin is None else pin.ctypes.data))
+        return it.value, res.value, pin
+
+    def si_stats(self):
+        """(iterations, residual, solve_ms) of the last semi-implicit step."""
+        it, res, ms = ctypes.c_int(), ctypes.c_double(), ctypes.c_double()
+        _check(lib.vibe_gb300_si_stats(self.h, ctypes.byref(it), ctypes.byref(res), ctypes.byref(ms)))
+        return it.value, res.value, ms.value
 
 
 # ---- C-ABI kernels (names as in the reference's c_kernels.h) ----------------
