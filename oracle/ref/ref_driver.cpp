@@ -41,6 +41,7 @@
 #include "vibe/grid/geometry.hpp"
 #include "vibe/time/acoustic_substep.hpp"
 #include "vibe/time/helmholtz.hpp"
+#include "vibe/grid/nest.hpp"
 
 using namespace vibe;
 
@@ -380,6 +381,97 @@ int vref_si_step(vref_model* m, double dt, int kind, int max_iter, double tol, i
   }
   m->eq->damping().apply_sponge(s, ref, dt);
   return s.has_nonfinite() ? 1 : 0;
+}
+
+
+namespace {
+grid::Grid plain_grid(int nx, int ny, int nz) {
+  grid::Geometry geo;
+  geo.nx = nx;
+  geo.ny = ny;
+  geo.nz = nz;
+  geo.dx = 1.0;
+  geo.dy = 1.0;
+  geo.z_top = 1.0;
+  geo.zeta = grid::make_stretched_zeta(nz, 1.0, 1.0);
+  geo.name = "nest";
+  return grid::Grid(geo, grid::Decomposition::make(nx, ny, nz, 1, 1, VO_HALO, false, false));
+}
+grid::Stagger stagger_of(int s) {
+  return s == 1 ? grid::Stagger::FaceX : s == 2 ? grid::Stagger::FaceY : s == 3 ? grid::Stagger::FaceZ
+                                                                               : grid::Stagger::Cell;
+}
+std::vector<grid::Field<Real>> fields_of(const grid::Grid& g, int nvars, const int* stagger, const double* const* p) {
+  std::vector<grid::Field<Real>> fs;
+  for (int v = 0; v < nvars; ++v) {
+    fs.emplace_back(g, stagger_of(stagger[v]), "f");
+    std::memcpy(fs.back().storage().data(), p[v], fs.back().storage().size() * sizeof(double));
+  }
+  return fs;
+}
+void copy_out(std::vector<grid::Field<Real>>& fs, double* const* p) {
+  for (size_t v = 0; v < fs.size(); ++v)
+    std::memcpy(p[v], fs[v].storage().data(), fs[v].storage().size() * sizeof(double));
+}
+std::vector<grid::Field<Real>*> ptrs(std::vector<grid::Field<Real>>& fs) {
+  std::vector<grid::Field<Real>*> out;
+  for (auto& f : fs) out.push_back(&f);
+  return out;
+}
+grid::NestPlacement placement_of(const vo_nest_placement* p) {
+  grid::NestPlacement q;
+  q.i0 = p->i0;
+  q.j0 = p->j0;
+  q.k0 = p->k0;
+  q.iext = p->iext;
+  q.jext = p->jext;
+  q.ratio = p->ratio;
+  q.boundary_zone = p->boundary_zone;
+  return q;
+}
+}  // namespace
+
+void vref_davies_profile(int n_zone, double alpha_max, double* out) {
+  const auto a = grid::davies_profile(n_zone, alpha_max);
+  std::memcpy(out, a.data(), a.size() * sizeof(double));
+}
+
+void vref_nest_interpolate_from_parent(const vo_nest_placement* p, int nvars, const int* stagger, int pnx, int pny,
+                                       int pnz, const double* const* parent, int cnx, int cny, int cnz,
+                                       double* const* child) {
+  grid::Grid pg = plain_grid(pnx, pny, pnz), cg = plain_grid(cnx, cny, cnz);
+  grid::Nest nest(cg, pg, placement_of(p));
+  auto pf = fields_of(pg, nvars, stagger, parent);
+  auto cf = fields_of(cg, nvars, stagger, child);
+  auto pp = ptrs(pf);
+  auto cp = ptrs(cf);
+  nest.interpolate_from_parent(pp, cp);
+  copy_out(cf, child);
+}
+
+void vref_nest_restrict_to_parent(const vo_nest_placement* p, int nvars, const int* stagger, int cnx, int cny,
+                                  int cnz, const double* const* child, int pnx, int pny, int pnz,
+                                  double* const* parent) {
+  grid::Grid pg = plain_grid(pnx, pny, pnz), cg = plain_grid(cnx, cny, cnz);
+  grid::Nest nest(cg, pg, placement_of(p));
+  auto pf = fields_of(pg, nvars, stagger, parent);
+  auto cf = fields_of(cg, nvars, stagger, child);
+  auto pp = ptrs(pf);
+  auto cp = ptrs(cf);
+  nest.restrict_to_parent(cp, pp);
+  copy_out(pf, parent);
+}
+
+void vref_nest_apply_lateral_boundary(const vo_nest_placement* p, int nvars, const int* stagger, int cnx, int cny,
+                                      int cnz, double* const* child, const double* const* parent_interp) {
+  grid::Grid cg = plain_grid(cnx, cny, cnz);
+  grid::Nest nest(cg, cg, placement_of(p));
+  auto cf = fields_of(cg, nvars, stagger, child);
+  auto pf = fields_of(cg, nvars, stagger, parent_interp);
+  auto cp = ptrs(cf);
+  auto pp = ptrs(pf);
+  nest.apply_lateral_boundary(cp, pp);
+  copy_out(cf, child);
 }
 
 }  // extern "C"

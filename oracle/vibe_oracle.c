@@ -1384,6 +1384,93 @@ int vo_si_step(vo_model *m, double dt, int kind, int max_iter, double tol, int *
 }
 
 /* ------------------------------------------------------------------------ */
+/* Nest transfers: src/grid/nest.cpp:34-124                                  */
+/* ------------------------------------------------------------------------ */
+static fld fld_of(int nx, int ny, int nz, int stagger, const double *p) {
+  fld f;
+  f.nx = nx; f.ny = ny; f.nz = nz;
+  f.nsx = nx + 2 * VO_HALO + (stagger == 1);
+  f.nsy = ny + 2 * VO_HALO + (stagger == 2);
+  f.nsz = nz + 2 * VO_HALO + (stagger == 3);
+  f.d = (double *)p;
+  return f;
+}
+
+/* davies_profile, nest.cpp:34-44 */
+void vo_davies_profile(int n_zone, double alpha_max, double *out) {
+  for (int n = 0; n < n_zone; ++n) {
+    const double arg = K_PI * (double)(n_zone - n) / (double)n_zone;
+    out[n] = alpha_max * 0.5 * (1.0 - cos(arg));
+  }
+}
+
+/* Nest::interpolate_from_parent, nest.cpp:58-84: child point (i, j) at
+ * parent coordinate ((i0 + i) + 0.5)/r - 0.5, bilinear with the parent's
+ * clamp; every stagger uses the cell-centre formula over the grid's nx x ny */
+void vo_nest_interpolate_from_parent(const vo_nest_placement *p, int nvars, const int *stagger, int pnx, int pny,
+                                     int pnz, const double *const *parent, int cnx, int cny, int cnz,
+                                     double *const *child) {
+  const double inv = 1.0 / (double)p->ratio;
+  for (int v = 0; v < nvars; ++v) {
+    const fld src = fld_of(pnx, pny, pnz, stagger[v], parent[v]);
+    fld dst = fld_of(cnx, cny, cnz, stagger[v], child[v]);
+    for (int k = 0; k < cnz; ++k)
+      for (int j = 0; j < cny; ++j)
+        for (int i = 0; i < cnx; ++i) {
+          const double xp = ((double)(p->i0 + i) + 0.5) * inv - 0.5;
+          const double yp = ((double)(p->j0 + j) + 0.5) * inv - 0.5;
+          const int ip = (int)floor(xp), jp = (int)floor(yp);
+          const double wx = xp - (double)ip, wy = yp - (double)jp;
+          AT(dst, i, j, k) = lerp(lerp(CL(&src, ip, jp, k), CL(&src, ip + 1, jp, k), wx),
+                                  lerp(CL(&src, ip, jp + 1, k), CL(&src, ip + 1, jp + 1, k), wx), wy);
+        }
+  }
+}
+
+/* Nest::restrict_to_parent, nest.cpp:86-105: parent (i0+i, j0+j, k) = mean of
+ * the child's r x r points (jj outer, ii inner), i < iext, j < jext, k < the
+ * parent's nz */
+void vo_nest_restrict_to_parent(const vo_nest_placement *p, int nvars, const int *stagger, int cnx, int cny,
+                                int cnz, const double *const *child, int pnx, int pny, int pnz,
+                                double *const *parent) {
+  const int r = p->ratio;
+  const double w = 1.0 / (double)(r * r);
+  for (int v = 0; v < nvars; ++v) {
+    const fld src = fld_of(cnx, cny, cnz, stagger[v], child[v]);
+    fld dst = fld_of(pnx, pny, pnz, stagger[v], parent[v]);
+    for (int j = 0; j < p->jext; ++j)
+      for (int i = 0; i < p->iext; ++i)
+        for (int k = 0; k < pnz; ++k) {
+          double acc = 0.0;
+          for (int jj = 0; jj < r; ++jj)
+            for (int ii = 0; ii < r; ++ii) acc += CL(&src, i * r + ii, j * r + jj, k);
+          AT(dst, p->i0 + i, p->j0 + j, k) = acc * w;
+        }
+  }
+}
+
+/* Nest::apply_lateral_boundary, nest.cpp:107-124 */
+void vo_nest_apply_lateral_boundary(const vo_nest_placement *p, int nvars, const int *stagger, int cnx, int cny,
+                                    int cnz, double *const *child, const double *const *parent_interp) {
+  const int nzone = p->boundary_zone > 0 ? p->boundary_zone : 0;
+  double *davies = (double *)calloc((size_t)nzone + 1, sizeof(double));
+  vo_davies_profile(nzone, 1.0, davies);
+  for (int v = 0; v < nvars; ++v) {
+    fld c = fld_of(cnx, cny, cnz, stagger[v], child[v]);
+    const fld pi = fld_of(cnx, cny, cnz, stagger[v], parent_interp[v]);
+    for (int k = 0; k < cnz; ++k)
+      for (int j = 0; j < cny; ++j)
+        for (int i = 0; i < cnx; ++i) {
+          const int d = imin(imin(i, cnx - 1 - i), imin(j, cny - 1 - j));
+          if (d >= nzone) continue;
+          const double alpha = davies[d];
+          AT(c, i, j, k) = (1.0 - alpha) * AT(c, i, j, k) + alpha * AT(pi, i, j, k);
+        }
+  }
+  free(davies);
+}
+
+/* ------------------------------------------------------------------------ */
 /* C-ABI kernels: src/common/c_kernels.c                                     */
 /* ------------------------------------------------------------------------ */
 int vo_tridiagonal_solve(const double *a, const double *b, const double *c, const double *d, int n,

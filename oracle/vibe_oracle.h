@@ -141,6 +141,21 @@ void vo_multigrid_prolong(const vo_model *m, const double *coarse, double *fine)
 int vo_si_step(vo_model *m, double dt, int kind, int max_iter, double tol, int *iterations, double *residual,
                double *pi_new, double *rhs, double *a_coef);
 
+/* Nest transfers (src/grid/nest.cpp:34-124) on FieldT storage arrays: nvars
+ * fields of the parent grid (pnx, pny, pnz) and of the child grid (cnx, cny,
+ * cnz); stagger[v] (0 cell, 1 x-face, 2 y-face, 3 z-face) sets each field's
+ * storage size. davies_profile: n_zone weights (nest.cpp:34-44). */
+typedef struct { int i0, j0, k0, iext, jext, ratio, boundary_zone; } vo_nest_placement;
+void vo_davies_profile(int n_zone, double alpha_max, double *out);
+void vo_nest_interpolate_from_parent(const vo_nest_placement *p, int nvars, const int *stagger, int pnx, int pny,
+                                     int pnz, const double *const *parent, int cnx, int cny, int cnz,
+                                     double *const *child);
+void vo_nest_restrict_to_parent(const vo_nest_placement *p, int nvars, const int *stagger, int cnx, int cny,
+                                int cnz, const double *const *child, int pnx, int pny, int pnz,
+                                double *const *parent);
+void vo_nest_apply_lateral_boundary(const vo_nest_placement *p, int nvars, const int *stagger, int cnx, int cny,
+                                    int cnz, double *const *child, const double *const *parent_interp);
+
 /* C-ABI kernels restated (src/common/c_kernels.c). vo_tridiagonal_solve
  * follows the documented contract (c_kernels.h:38-55) with the textbook
  * recurrence of thomas_solve (helmholtz.cpp:57-86): the shipped
@@ -185,6 +200,15 @@ void vref_multigrid_restrict(vref_model *m, const double *fine, double *coarse);
 void vref_multigrid_prolong(vref_model *m, const double *coarse, double *fine);
 int vref_si_step(vref_model *m, double dt, int kind, int max_iter, double tol, int *iterations,
                  double *residual, double *pi_new, double *rhs, double *a_coef);
+void vref_davies_profile(int n_zone, double alpha_max, double *out);
+void vref_nest_interpolate_from_parent(const vo_nest_placement *p, int nvars, const int *stagger, int pnx, int pny,
+                                       int pnz, const double *const *parent, int cnx, int cny, int cnz,
+                                       double *const *child);
+void vref_nest_restrict_to_parent(const vo_nest_placement *p, int nvars, const int *stagger, int cnx, int cny,
+                                  int cnz, const double *const *child, int pnx, int pny, int pnz,
+                                  double *const *parent);
+void vref_nest_apply_lateral_boundary(const vo_nest_placement *p, int nvars, const int *stagger, int cnx, int cny,
+                                      int cnz, double *const *child, const double *const *parent_interp);
 
 #ifdef __cplusplus
 }

@@ -275,3 +275,70 @@ class Model:
         rc = self._f["si_step"](self.h, dt, kind, max_iter, tol, ctypes.byref(it), ctypes.byref(res),
                                 *[o.ctypes.data for o in outs])
         return int(rc), it.value, res.value, outs[0], outs[1], outs[2]
+
+
+# ---- nest transfers (port: vo_*, reference-linked: vref_*) ----
+class NestPlacement(ctypes.Structure):
+    _fields_ = [("i0", _I), ("j0", _I), ("k0", _I), ("iext", _I), ("jext", _I), ("ratio", _I),
+                ("boundary_zone", _I)]
+
+
+def _nest_fns(kind):
+    lib = _load(kind)[0]
+    p = "vo_" if kind == "port" else "vref_"
+    vp = ctypes.c_void_p
+    f = {}
+    for name, args in (("nest_interpolate_from_parent", [vp, _I, vp, _I, _I, _I, vp, _I, _I, _I, vp]),
+                       ("nest_restrict_to_parent", [vp, _I, vp, _I, _I, _I, vp, _I, _I, _I, vp]),
+                       ("nest_apply_lateral_boundary", [vp, _I, vp, _I, _I, _I, vp, vp]),
+                       ("davies_profile", [_I, _D, vp])):
+        fn = getattr(lib, p + name)
+        fn.restype = None
+        fn.argtypes = args
+        f[name] = fn
+    return f
+
+
+def _arr(arrs):
+    return (ctypes.c_void_p * len(arrs))(*[a.ctypes.data for a in arrs])
+
+
+def _pl(pl):
+    q = NestPlacement()
+    for name, _ in NestPlacement._fields_:
+        setattr(q, name, int(pl.get(name, 0)))
+    return q
+
+
+def davies_profile(n_zone, alpha_max=1.0, kind="port"):
+    out = np.zeros(n_zone)
+    _nest_fns(kind)["davies_profile"](n_zone, alpha_max, out.ctypes.data)
+    return out
+
+
+def nest_interpolate_from_parent(pl, staggers, pdims, parent, cdims, child, kind="port"):
+    st = np.ascontiguousarray(staggers, dtype=np.int32)
+    q = _pl(pl)
+    _nest_fns(kind)["nest_interpolate_from_parent"](ctypes.byref(q), len(st), st.ctypes.data, *pdims, _arr(parent),
+                                                    *cdims, _arr(child))
+    return child
+
+
+def nest_restrict_to_parent(pl, staggers, cdims, child, pdims, parent, kind="port"):
+    st = np.ascontiguousarray(staggers, dtype=np.int32)
+    q = _pl(pl)
+    _nest_fns(kind)["nest_restrict_to_parent"](ctypes.byref(q), len(st), st.ctypes.data, *cdims, _arr(child),
+                                               *pdims, _arr(parent))
+    return parent
+
+
+def nest_apply_lateral_boundary(pl, staggers, cdims, child, parent_interp, kind="port"):
+    st = np.ascontiguousarray(staggers, dtype=np.int32)
+    q = _pl(pl)
+    _nest_fns(kind)["nest_apply_lateral_boundary"](ctypes.byref(q), len(st), st.ctypes.data, *cdims, _arr(child),
+                                                   _arr(parent_interp))
+    return child
+
+
+def fieldt_size(nx, ny, nz, stagger):
+    return (nx + 2 * HALO + (stagger == 1)) * (ny + 2 * HALO + (stagger == 2)) * (nz + 2 * HALO + (stagger == 3))

@@ -206,3 +206,26 @@ def test_semi_implicit_step_port_is_bit_exact_to_reference(oc):
         assert np.array_equal(op[4], orf[4]) and np.array_equal(op[5], orf[5])
         for sp in range(12):
             assert np.array_equal(p.get(sp), r.get(sp)), sp
+
+
+@need_ref
+@pytest.mark.parametrize("case", range(4))
+def test_nest_transfers_port_is_bit_exact_to_reference(oc, case):
+    import nest_cases as nc
+    pdims, cdims, pl = nc.CASES[case]
+    assert np.array_equal(oc.davies_profile(pl["boundary_zone"], 1.0, "port"),
+                          oc.davies_profile(pl["boundary_zone"], 1.0, "ref"))
+    parent = nc.fields(oc, pdims, 1)
+    out = {}
+    for kind in ("port", "ref"):
+        child = nc.fields(oc, cdims, 2)
+        oc.nest_interpolate_from_parent(pl, nc.STAGGERS, pdims, parent, cdims, child, kind)
+        interp = [c.copy() for c in child]
+        inner = nc.fields(oc, cdims, 3)
+        oc.nest_apply_lateral_boundary(pl, nc.STAGGERS, cdims, inner, interp, kind)
+        par = [p.copy() for p in parent]
+        oc.nest_restrict_to_parent(pl, nc.STAGGERS, cdims, inner, pdims, par, kind)
+        out[kind] = (interp, inner, par)
+    for a, b in zip(out["port"], out["ref"]):
+        for x, y in zip(a, b):
+            assert np.array_equal(x, y)

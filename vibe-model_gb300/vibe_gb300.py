@@ -448,3 +448,65 @@ class Helmholtz:
     def residual_l2(self, f, x):
         f, x = (np.ascontiguousarray(v, dtype=np.float64) for v in (f, x))
         return float(lib.vibe_helmholtz_residual_l2(self.h, f.ctypes.data, x.ctypes.data))
+
+
+# ---- nest transfers (include/vibe_nest.h) -----------------------------------
+class NestPlacement(ctypes.Structure):
+    """Mirror of vibe_nest_placement (NestPlacement, nest.hpp:41-48)."""
+    _fields_ = [("i0", _I), ("j0", _I), ("k0", _I), ("iext", _I), ("jext", _I), ("ratio", _I),
+                ("boundary_zone", _I), ("two_way", _I)]
+
+
+for _name, _args in (("vibe_nest_interpolate_from_parent", [_vp, _I, _vp, _I, _I, _I, _vp, _I, _I, _I, _vp]),
+                     ("vibe_nest_restrict_to_parent", [_vp, _I, _vp, _I, _I, _I, _vp, _I, _I, _I, _vp]),
+                     ("vibe_nest_apply_lateral_boundary", [_vp, _I, _vp, _I, _I, _I, _vp, _vp]),
+                     ("vibe_nest_interpolate_from_parent_dev", [_vp, _I, _vp, _I, _I, _I, _vp, _I, _I, _I, _vp, _vp]),
+                     ("vibe_nest_restrict_to_parent_dev", [_vp, _I, _vp, _I, _I, _I, _vp, _I, _I, _I, _vp, _vp]),
+                     ("vibe_nest_apply_lateral_boundary_dev", [_vp, _I, _vp, _I, _I, _I, _vp, _vp, _vp]),
+                     ("vibe_davies_profile", [_I, _D, _vp])):
+    _f = getattr(lib, _name)
+    _f.restype = _I
+    _f.argtypes = _args
+
+
+def _ptr_array(arrs):
+    return (_vp * len(arrs))(*[a.ctypes.data for a in arrs])
+
+
+def davies_profile(n_zone, alpha_max=1.0):
+    out = np.zeros(n_zone)
+    rc = lib.vibe_davies_profile(n_zone, alpha_max, out.ctypes.data)
+    if rc:
+        raise VibeError(-1)
+    return out
+
+
+def nest_interpolate_from_parent(pl, staggers, pdims, parent, cdims, child):
+    """child (list of FieldT arrays) updated in place and returned."""
+    st = np.ascontiguousarray(staggers, dtype=np.int32)
+    parent = [np.ascontiguousarray(a, dtype=np.float64) for a in parent]
+    rc = lib.vibe_nest_interpolate_from_parent(ctypes.byref(pl), len(st), st.ctypes.data, *pdims,
+                                               _ptr_array(parent), *cdims, _ptr_array(child))
+    if rc:
+        raise RuntimeError("nest interpolate rc=%d" % rc)
+    return child
+
+
+def nest_restrict_to_parent(pl, staggers, cdims, child, pdims, parent):
+    st = np.ascontiguousarray(staggers, dtype=np.int32)
+    child = [np.ascontiguousarray(a, dtype=np.float64) for a in child]
+    rc = lib.vibe_nest_restrict_to_parent(ctypes.byref(pl), len(st), st.ctypes.data, *cdims, _ptr_array(child),
+                                          *pdims, _ptr_array(parent))
+    if rc:
+        raise RuntimeError("nest restrict rc=%d" % rc)
+    return parent
+
+
+def nest_apply_lateral_boundary(pl, staggers, cdims, child, parent_interp):
+    st = np.ascontiguousarray(staggers, dtype=np.int32)
+    parent_interp = [np.ascontiguousarray(a, dtype=np.float64) for a in parent_interp]
+    rc = lib.vibe_nest_apply_lateral_boundary(ctypes.byref(pl), len(st), st.ctypes.data, *cdims, _ptr_array(child),
+                                              _ptr_array(parent_interp))
+    if rc:
+        raise RuntimeError("nest lateral rc=%d" % rc)
+    return child
