@@ -42,6 +42,7 @@
 #include "vibe/time/acoustic_substep.hpp"
 #include "vibe/time/helmholtz.hpp"
 #include "vibe/grid/nest.hpp"
+#include "vibe/da/tangent_linear.hpp"
 
 using namespace vibe;
 
@@ -472,6 +473,77 @@ void vref_nest_apply_lateral_boundary(const vo_nest_placement* p, int nvars, con
   auto pp = ptrs(pf);
   nest.apply_lateral_boundary(cp, pp);
   copy_out(cf, child);
+}
+
+
+namespace {
+void load_state(dyn::State& st, const double* const* p) {
+  for (int sp = 0; sp < dyn::kNumSpecies; ++sp) {
+    auto& f = st.field(static_cast<dyn::Species>(sp)).storage();
+    std::memcpy(f.data(), p[sp], f.size() * sizeof(double));
+  }
+}
+void store_state(const dyn::State& st, double* const* p) {
+  for (int sp = 0; sp < dyn::kNumSpecies; ++sp) {
+    const auto& f = st.field(static_cast<dyn::Species>(sp)).storage();
+    std::memcpy(p[sp], f.data(), f.size() * sizeof(double));
+  }
+}
+void store_tend(const dyn::Tendency& t, double* const* p) {
+  for (int sp = 0; sp < dyn::kNumSpecies; ++sp) {
+    const auto& f = t.field(static_cast<dyn::Species>(sp)).storage();
+    std::memcpy(p[sp], f.data(), f.size() * sizeof(double));
+  }
+}
+}  // namespace
+
+void vref_tl_step(vref_model* m, const double* const* xb, const double* const* dx, double dt, double* const* out) {
+  const grid::Grid& g = *m->grid;
+  config::DaConfig da;
+  da::TangentLinearModel tl(g, *m->ref, m->cfg, da);
+  dyn::State sxb(g), sdx(g), sout(g);
+  load_state(sxb, xb);
+  load_state(sdx, dx);
+  tl.step(sxb, sdx, dt, sout);
+  store_state(sout, out);
+}
+
+void vref_ad_step(vref_model* m, const double* const* xb, const double* const* bar_out, double dt,
+                  double* const* bar_in) {
+  const grid::Grid& g = *m->grid;
+  config::DaConfig da;
+  da::AdjointModel ad(g, *m->ref, m->cfg, da);
+  dyn::State sxb(g), sbo(g), sbi(g);
+  load_state(sxb, xb);
+  load_state(sbo, bar_out);
+  ad.step_adjoint(sxb, sbo, dt, sbi);
+  store_state(sbi, bar_in);
+}
+
+void vref_tl_propagate(vref_model* m, const double* const* xb, const double* const* dx0, double dt, int n_steps,
+                       double* const* out) {
+  const grid::Grid& g = *m->grid;
+  config::DaConfig da;
+  da::TangentLinearModel tl(g, *m->ref, m->cfg, da);
+  dyn::State sxb(g), sdx(g), sout(g);
+  load_state(sxb, xb);
+  load_state(sdx, dx0);
+  tl.propagate(sxb, sdx, dt, n_steps, sout);
+  store_state(sout, out);
+}
+
+void vref_ad_propagate(vref_model* m, const double* const* xb, const double* const* dy, double dt, int n_steps,
+                       double* const* out) {
+  const grid::Grid& g = *m->grid;
+  config::DaConfig da;
+  da::TangentLinearModel tl(g, *m->ref, m->cfg, da);
+  da::AdjointModel ad(g, *m->ref, m->cfg, da);
+  dyn::State sxb(g), sdy(g), sout(g), scratch(g);
+  load_state(sxb, xb);
+  load_state(sdy, dy);
+  tl.record_trajectory(sxb, dt, n_steps);
+  ad.propagate_with_trajectory(tl.trajectory(), sdy, sout);
+  store_state(sout, out);
 }
 
 }  // extern "C"

@@ -1384,6 +1384,373 @@ int vo_si_step(vo_model *m, double dt, int kind, int max_iter, double tol, int *
 }
 
 /* ------------------------------------------------------------------------ */
+/* TL/AD of the simplified collocated RK3: src/da/tangent_linear.cpp        */
+/* ------------------------------------------------------------------------ */
+/* Grid::inv_dz, geometry.cpp:265-270 (no 1 m floor here) */
+static double g_inv_dz(const vo_model *m, int i, int j, int k) {
+  const double dz = g_dzeta(m, k) * (m->s.z_top - g_terrain(m, i, j));
+  return dz > 0.0 ? 1.0 / dz : 0.0;
+}
+static fld sp_view(const vo_model *m, int sp, const double *p) { fld f = m->st[sp]; f.d = (double *)p; return f; }
+
+/* dop_x/y/z, tangent_linear.cpp:82-122: out += scale * c * (f(+1) - f(-1)) * inv, interior */
+static void dop(const vo_model *m, int dir, const fld *f, const fld *c, fld *out, double scale) {
+  const int nx = m->nx, ny = m->ny, nz = m->nz;
+  if (dir == 0) {
+    for (int k = 0; k < nz; ++k)
+      for (int j = 0; j < ny; ++j)
+        for (int i = 1; i + 1 < nx; ++i) {
+          const double inv = 0.5 / dmax(m->s.dx, 1e-6);
+          AT(*out, i, j, k) += scale * AT(*c, i, j, k) * (AT(*f, i + 1, j, k) - AT(*f, i - 1, j, k)) * inv;
+        }
+  } else if (dir == 1) {
+    for (int k = 0; k < nz; ++k)
+      for (int j = 1; j + 1 < ny; ++j) {
+        const double inv = 0.5 / dmax(m->s.dy, 1e-6);
+        for (int i = 0; i < nx; ++i)
+          AT(*out, i, j, k) += scale * AT(*c, i, j, k) * (AT(*f, i, j + 1, k) - AT(*f, i, j - 1, k)) * inv;
+      }
+  } else {
+    for (int k = 1; k + 1 < nz; ++k)
+      for (int j = 0; j < ny; ++j)
+        for (int i = 0; i < nx; ++i) {
+          const double inv = 0.5 * g_inv_dz(m, i, j, k);
+          AT(*out, i, j, k) += scale * AT(*c, i, j, k) * (AT(*f, i, j, k + 1) - AT(*f, i, j, k - 1)) * inv;
+        }
+  }
+}
+/* dop_*_ad_f, tangent_linear.cpp:124-205: transpose in the differentiated field */
+static void dop_ad_f(const vo_model *m, int dir, const fld *c, fld *bar_f, const fld *bar_out, double scale) {
+  const int nx = m->nx, ny = m->ny, nz = m->nz;
+  if (dir == 0) {
+    for (int k = 0; k < nz; ++k)
+      for (int j = 0; j < ny; ++j)
+        for (int i = 1; i + 1 < nx; ++i) {
+          const double inv = 0.5 / dmax(m->s.dx, 1e-6);
+          const double w = scale * AT(*c, i, j, k) * inv * AT(*bar_out, i, j, k);
+          AT(*bar_f, i + 1, j, k) += w;
+          AT(*bar_f, i - 1, j, k) -= w;
+        }
+  } else if (dir == 1) {
+    for (int k = 0; k < nz; ++k)
+      for (int j = 1; j + 1 < ny; ++j) {
+        const double inv = 0.5 / dmax(m->s.dy, 1e-6);
+        for (int i = 0; i < nx; ++i) {
+          const double w = scale * AT(*c, i, j, k) * inv * AT(*bar_out, i, j, k);
+          AT(*bar_f, i, j + 1, k) += w;
+          AT(*bar_f, i, j - 1, k) -= w;
+        }
+      }
+  } else {
+    for (int k = 1; k + 1 < nz; ++k)
+      for (int j = 0; j < ny; ++j)
+        for (int i = 0; i < nx; ++i) {
+          const double inv = 0.5 * g_inv_dz(m, i, j, k);
+          const double w = scale * AT(*c, i, j, k) * inv * AT(*bar_out, i, j, k);
+          AT(*bar_f, i, j, k + 1) += w;
+          AT(*bar_f, i, j, k - 1) -= w;
+        }
+  }
+}
+/* dop_*_ad_c: transpose in the (perturbed) coefficient */
+static void dop_ad_c(const vo_model *m, int dir, const fld *f, fld *bar_c, const fld *bar_out, double scale) {
+  const int nx = m->nx, ny = m->ny, nz = m->nz;
+  if (dir == 0) {
+    for (int k = 0; k < nz; ++k)
+      for (int j = 0; j < ny; ++j)
+        for (int i = 1; i + 1 < nx; ++i) {
+          const double inv = 0.5 / dmax(m->s.dx, 1e-6);
+          AT(*bar_c, i, j, k) += scale * AT(*bar_out, i, j, k) * (AT(*f, i + 1, j, k) - AT(*f, i - 1, j, k)) * inv;
+        }
+  } else if (dir == 1) {
+    for (int k = 0; k < nz; ++k)
+      for (int j = 1; j + 1 < ny; ++j) {
+        const double inv = 0.5 / dmax(m->s.dy, 1e-6);
+        for (int i = 0; i < nx; ++i)
+          AT(*bar_c, i, j, k) += scale * AT(*bar_out, i, j, k) * (AT(*f, i, j + 1, k) - AT(*f, i, j - 1, k)) * inv;
+      }
+  } else {
+    for (int k = 1; k + 1 < nz; ++k)
+      for (int j = 0; j < ny; ++j)
+        for (int i = 0; i < nx; ++i) {
+          const double inv = 0.5 * g_inv_dz(m, i, j, k);
+          AT(*bar_c, i, j, k) += scale * AT(*bar_out, i, j, k) * (AT(*f, i, j, k + 1) - AT(*f, i, j, k - 1)) * inv;
+        }
+  }
+}
+/* base_divergence (:207-235) and base_gradient (:237-266) */
+static void base_div(const vo_model *m, const fld *ub, const fld *vb, const fld *wb, fld *div) {
+  const int nx = m->nx, ny = m->ny, nz = m->nz;
+  fld_zero(div);
+  for (int k = 0; k < nz; ++k)
+    for (int j = 0; j < ny; ++j)
+      for (int i = 0; i < nx; ++i) {
+        double d = 0.0;
+        if (i >= 1 && i + 1 < nx) d += (AT(*ub, i + 1, j, k) - AT(*ub, i - 1, j, k)) * (0.5 / dmax(m->s.dx, 1e-6));
+        if (j >= 1 && j + 1 < ny) d += (AT(*vb, i, j + 1, k) - AT(*vb, i, j - 1, k)) * (0.5 / dmax(m->s.dy, 1e-6));
+        if (k >= 1 && k + 1 < nz) d += (AT(*wb, i, j, k + 1) - AT(*wb, i, j, k - 1)) * (0.5 * g_inv_dz(m, i, j, k));
+        AT(*div, i, j, k) = d;
+      }
+}
+static void base_grad(const vo_model *m, const fld *f, fld *gx, fld *gy, fld *gz) {
+  const int nx = m->nx, ny = m->ny, nz = m->nz;
+  fld_zero(gx); fld_zero(gy); fld_zero(gz);
+  for (int k = 0; k < nz; ++k)
+    for (int j = 0; j < ny; ++j)
+      for (int i = 0; i < nx; ++i) {
+        if (i >= 1 && i + 1 < nx) AT(*gx, i, j, k) = (AT(*f, i + 1, j, k) - AT(*f, i - 1, j, k)) * (0.5 / dmax(m->s.dx, 1e-6));
+        if (j >= 1 && j + 1 < ny) AT(*gy, i, j, k) = (AT(*f, i, j + 1, k) - AT(*f, i, j - 1, k)) * (0.5 / dmax(m->s.dy, 1e-6));
+        if (k >= 1 && k + 1 < nz) AT(*gz, i, j, k) = (AT(*f, i, j, k + 1) - AT(*f, i, j, k - 1)) * (0.5 * g_inv_dz(m, i, j, k));
+      }
+}
+static double tl_coriolis(void) { return 2.0 * K_OMEGA * sin(45.0 * (K_PI / 180.0)); } /* kCoriolis, :79 */
+static const int kTlScalars[7] = {VO_THETA, VO_QV, VO_QC, VO_QR, VO_QI, VO_QS, VO_QG};
+
+/* tendency_tl, tangent_linear.cpp:295-412 */
+static void tl_tendency(const vo_model *m, fld *xb, fld *dx, fld *d) {
+  const int nx = m->nx, ny = m->ny, nz = m->nz;
+  const double rdcv = K_RD / K_CV, fc = tl_coriolis();
+  for (int sp = 0; sp < VO_NSPECIES; ++sp) fld_zero(&d[sp]);
+  fld *ub = &xb[VO_U], *vb = &xb[VO_V], *wb = &xb[VO_W];
+  fld *rhob = &xb[VO_RHO], *thb = &xb[VO_THETA], *pib = &xb[VO_PI];
+  fld *du = &dx[VO_U], *dv = &dx[VO_V], *dw = &dx[VO_W], *drho = &dx[VO_RHO], *dth = &dx[VO_THETA], *dpi = &dx[VO_PI];
+  fld div = fld_cell(m);
+  base_div(m, ub, vb, wb, &div);
+  for (int si = 0; si < 7; ++si) {
+    const int sp = kTlScalars[si];
+    fld *sb = &xb[sp], *ds = &dx[sp], *out = &d[sp];
+    dop(m, 0, ds, ub, out, -1.0); dop(m, 1, ds, vb, out, -1.0); dop(m, 2, ds, wb, out, -1.0);
+    dop(m, 0, sb, du, out, -1.0); dop(m, 1, sb, dv, out, -1.0); dop(m, 2, sb, dw, out, -1.0);
+  }
+  {
+    fld *out = &d[VO_RHO];
+    dop(m, 0, du, rhob, out, -1.0); dop(m, 1, dv, rhob, out, -1.0); dop(m, 2, dw, rhob, out, -1.0);
+    dop(m, 0, drho, ub, out, -1.0); dop(m, 1, drho, vb, out, -1.0); dop(m, 2, drho, wb, out, -1.0);
+    for (int k = 0; k < nz; ++k)
+      for (int j = 0; j < ny; ++j)
+        for (int i = 0; i < nx; ++i) AT(*out, i, j, k) -= AT(div, i, j, k) * AT(*drho, i, j, k);
+    fld gx = fld_cell(m), gy = fld_cell(m), gz = fld_cell(m);
+    base_grad(m, rhob, &gx, &gy, &gz);
+    for (int k = 0; k < nz; ++k)
+      for (int j = 0; j < ny; ++j)
+        for (int i = 0; i < nx; ++i)
+          AT(*out, i, j, k) -= AT(*du, i, j, k) * AT(gx, i, j, k) + AT(*dv, i, j, k) * AT(gy, i, j, k) +
+                               AT(*dw, i, j, k) * AT(gz, i, j, k);
+    free(gx.d); free(gy.d); free(gz.d);
+  }
+  {
+    fld *out = &d[VO_PI];
+    dop(m, 0, dpi, ub, out, -1.0); dop(m, 1, dpi, vb, out, -1.0); dop(m, 2, dpi, wb, out, -1.0);
+    dop(m, 0, pib, du, out, -1.0); dop(m, 1, pib, dv, out, -1.0); dop(m, 2, pib, dw, out, -1.0);
+    dop(m, 0, du, pib, out, -rdcv); dop(m, 1, dv, pib, out, -rdcv); dop(m, 2, dw, pib, out, -rdcv);
+    for (int k = 0; k < nz; ++k)
+      for (int j = 0; j < ny; ++j)
+        for (int i = 0; i < nx; ++i) AT(*out, i, j, k) -= rdcv * AT(div, i, j, k) * AT(*dpi, i, j, k);
+  }
+  {
+    fld *out = &d[VO_U];
+    dop(m, 0, du, ub, out, -1.0); dop(m, 1, du, vb, out, -1.0); dop(m, 2, du, wb, out, -1.0);
+    dop(m, 0, ub, du, out, -1.0); dop(m, 1, ub, dv, out, -1.0); dop(m, 2, ub, dw, out, -1.0);
+    dop(m, 0, dpi, thb, out, -K_CP); dop(m, 0, pib, dth, out, -K_CP);
+    for (int k = 0; k < nz; ++k)
+      for (int j = 0; j < ny; ++j)
+        for (int i = 0; i < nx; ++i) AT(*out, i, j, k) += fc * AT(*dv, i, j, k);
+  }
+  {
+    fld *out = &d[VO_V];
+    dop(m, 0, dv, ub, out, -1.0); dop(m, 1, dv, vb, out, -1.0); dop(m, 2, dv, wb, out, -1.0);
+    dop(m, 0, vb, du, out, -1.0); dop(m, 1, vb, dv, out, -1.0); dop(m, 2, vb, dw, out, -1.0);
+    dop(m, 1, dpi, thb, out, -K_CP); dop(m, 1, pib, dth, out, -K_CP);
+    for (int k = 0; k < nz; ++k)
+      for (int j = 0; j < ny; ++j)
+        for (int i = 0; i < nx; ++i) AT(*out, i, j, k) -= fc * AT(*du, i, j, k);
+  }
+  {
+    fld *out = &d[VO_W];
+    dop(m, 0, dw, ub, out, -1.0); dop(m, 1, dw, vb, out, -1.0); dop(m, 2, dw, wb, out, -1.0);
+    dop(m, 0, wb, du, out, -1.0); dop(m, 1, wb, dv, out, -1.0); dop(m, 2, wb, dw, out, -1.0);
+    dop(m, 2, dpi, thb, out, -K_CP); dop(m, 2, pib, dth, out, -K_CP);
+    for (int k = 0; k < nz; ++k)
+      for (int j = 0; j < ny; ++j)
+        for (int i = 0; i < nx; ++i) {
+          const double th = dmax(AT(*thb, i, j, k), 1.0);
+          AT(*out, i, j, k) += K_GRAVITY * AT(*dth, i, j, k) / th;
+        }
+  }
+  free(div.d);
+}
+
+/* tendency_ad, tangent_linear.cpp:414-549: the statements of tendency_tl in
+ * reverse order, each replaced by its transpose; accumulates into bar_dx */
+static void ad_tendency(const vo_model *m, fld *xb, fld *bd, fld *bx) {
+  const int nx = m->nx, ny = m->ny, nz = m->nz;
+  const double rdcv = K_RD / K_CV, fc = tl_coriolis();
+  fld *ub = &xb[VO_U], *vb = &xb[VO_V], *wb = &xb[VO_W];
+  fld *rhob = &xb[VO_RHO], *thb = &xb[VO_THETA], *pib = &xb[VO_PI];
+  fld div = fld_cell(m);
+  base_div(m, ub, vb, wb, &div);
+  {
+    fld *bo = &bd[VO_W];
+    for (int k = 0; k < nz; ++k)
+      for (int j = 0; j < ny; ++j)
+        for (int i = 0; i < nx; ++i) {
+          const double th = dmax(AT(*thb, i, j, k), 1.0);
+          AT(bx[VO_THETA], i, j, k) += K_GRAVITY * AT(*bo, i, j, k) / th;
+        }
+    dop_ad_c(m, 2, pib, &bx[VO_THETA], bo, -K_CP);
+    dop_ad_f(m, 2, thb, &bx[VO_PI], bo, -K_CP);
+    dop_ad_c(m, 2, wb, &bx[VO_W], bo, -1.0);
+    dop_ad_c(m, 1, wb, &bx[VO_V], bo, -1.0);
+    dop_ad_c(m, 0, wb, &bx[VO_U], bo, -1.0);
+    dop_ad_f(m, 2, wb, &bx[VO_W], bo, -1.0);
+    dop_ad_f(m, 1, vb, &bx[VO_W], bo, -1.0);
+    dop_ad_f(m, 0, ub, &bx[VO_W], bo, -1.0);
+  }
+  {
+    fld *bo = &bd[VO_V];
+    for (int k = 0; k < nz; ++k)
+      for (int j = 0; j < ny; ++j)
+        for (int i = 0; i < nx; ++i) AT(bx[VO_U], i, j, k) -= fc * AT(*bo, i, j, k);
+    dop_ad_c(m, 1, pib, &bx[VO_THETA], bo, -K_CP);
+    dop_ad_f(m, 1, thb, &bx[VO_PI], bo, -K_CP);
+    dop_ad_c(m, 2, vb, &bx[VO_W], bo, -1.0);
+    dop_ad_c(m, 1, vb, &bx[VO_V], bo, -1.0);
+    dop_ad_c(m, 0, vb, &bx[VO_U], bo, -1.0);
+    dop_ad_f(m, 2, wb, &bx[VO_V], bo, -1.0);
+    dop_ad_f(m, 1, vb, &bx[VO_V], bo, -1.0);
+    dop_ad_f(m, 0, ub, &bx[VO_V], bo, -1.0);
+  }
+  {
+    fld *bo = &bd[VO_U];
+    for (int k = 0; k < nz; ++k)
+      for (int j = 0; j < ny; ++j)
+        for (int i = 0; i < nx; ++i) AT(bx[VO_V], i, j, k) += fc * AT(*bo, i, j, k);
+    dop_ad_c(m, 0, pib, &bx[VO_THETA], bo, -K_CP);
+    dop_ad_f(m, 0, thb, &bx[VO_PI], bo, -K_CP);
+    dop_ad_c(m, 2, ub, &bx[VO_W], bo, -1.0);
+    dop_ad_c(m, 1, ub, &bx[VO_V], bo, -1.0);
+    dop_ad_c(m, 0, ub, &bx[VO_U], bo, -1.0);
+    dop_ad_f(m, 2, wb, &bx[VO_U], bo, -1.0);
+    dop_ad_f(m, 1, vb, &bx[VO_U], bo, -1.0);
+    dop_ad_f(m, 0, ub, &bx[VO_U], bo, -1.0);
+  }
+  {
+    fld *bo = &bd[VO_PI];
+    for (int k = 0; k < nz; ++k)
+      for (int j = 0; j < ny; ++j)
+        for (int i = 0; i < nx; ++i) AT(bx[VO_PI], i, j, k) -= rdcv * AT(div, i, j, k) * AT(*bo, i, j, k);
+    dop_ad_f(m, 2, pib, &bx[VO_W], bo, -rdcv);
+    dop_ad_f(m, 1, pib, &bx[VO_V], bo, -rdcv);
+    dop_ad_f(m, 0, pib, &bx[VO_U], bo, -rdcv);
+    dop_ad_c(m, 2, pib, &bx[VO_W], bo, -1.0);
+    dop_ad_c(m, 1, pib, &bx[VO_V], bo, -1.0);
+    dop_ad_c(m, 0, pib, &bx[VO_U], bo, -1.0);
+    dop_ad_f(m, 2, wb, &bx[VO_PI], bo, -1.0);
+    dop_ad_f(m, 1, vb, &bx[VO_PI], bo, -1.0);
+    dop_ad_f(m, 0, ub, &bx[VO_PI], bo, -1.0);
+  }
+  {
+    fld *bo = &bd[VO_RHO];
+    fld gx = fld_cell(m), gy = fld_cell(m), gz = fld_cell(m);
+    base_grad(m, rhob, &gx, &gy, &gz);
+    for (int k = 0; k < nz; ++k)
+      for (int j = 0; j < ny; ++j)
+        for (int i = 0; i < nx; ++i) {
+          const double b = AT(*bo, i, j, k);
+          AT(bx[VO_U], i, j, k) -= AT(gx, i, j, k) * b;
+          AT(bx[VO_V], i, j, k) -= AT(gy, i, j, k) * b;
+          AT(bx[VO_W], i, j, k) -= AT(gz, i, j, k) * b;
+        }
+    free(gx.d); free(gy.d); free(gz.d);
+    for (int k = 0; k < nz; ++k)
+      for (int j = 0; j < ny; ++j)
+        for (int i = 0; i < nx; ++i) AT(bx[VO_RHO], i, j, k) -= AT(div, i, j, k) * AT(*bo, i, j, k);
+    dop_ad_f(m, 2, wb, &bx[VO_RHO], bo, -1.0);
+    dop_ad_f(m, 1, vb, &bx[VO_RHO], bo, -1.0);
+    dop_ad_f(m, 0, ub, &bx[VO_RHO], bo, -1.0);
+    dop_ad_f(m, 2, rhob, &bx[VO_W], bo, -1.0);
+    dop_ad_f(m, 1, rhob, &bx[VO_V], bo, -1.0);
+    dop_ad_f(m, 0, rhob, &bx[VO_U], bo, -1.0);
+  }
+  for (int si = 6; si >= 0; --si) {
+    const int sp = kTlScalars[si];
+    fld *sb = &xb[sp], *bs = &bx[sp], *bo = &bd[sp];
+    dop_ad_c(m, 2, sb, &bx[VO_W], bo, -1.0);
+    dop_ad_c(m, 1, sb, &bx[VO_V], bo, -1.0);
+    dop_ad_c(m, 0, sb, &bx[VO_U], bo, -1.0);
+    dop_ad_f(m, 2, wb, bs, bo, -1.0);
+    dop_ad_f(m, 1, vb, bs, bo, -1.0);
+    dop_ad_f(m, 0, ub, bs, bo, -1.0);
+  }
+  free(div.d);
+}
+
+static void views12(const vo_model *m, const double *const *p, fld *out) {
+  for (int sp = 0; sp < VO_NSPECIES; ++sp) out[sp] = sp_view(m, sp, p[sp]);
+}
+static void alloc12(const vo_model *m, fld *out) {
+  for (int sp = 0; sp < VO_NSPECIES; ++sp) fld_alloc(&out[sp], m->nx, m->ny, m->nz, stagger_of(sp));
+}
+static void free12(fld *f) { for (int sp = 0; sp < VO_NSPECIES; ++sp) free(f[sp].d); }
+
+void vo_tl_tendency(const vo_model *m, const double *const *xb, const double *const *dx, double *const *d) {
+  fld X[VO_NSPECIES], D[VO_NSPECIES], O[VO_NSPECIES];
+  views12(m, xb, X); views12(m, dx, D); views12(m, (const double *const *)d, O);
+  tl_tendency(m, X, D, O);
+}
+void vo_ad_tendency(const vo_model *m, const double *const *xb, const double *const *bar_d, double *const *bar_dx) {
+  fld X[VO_NSPECIES], B[VO_NSPECIES], O[VO_NSPECIES];
+  views12(m, xb, X); views12(m, bar_d, B); views12(m, (const double *const *)bar_dx, O);
+  ad_tendency(m, X, B, O);
+}
+
+/* rk3_tl, tangent_linear.cpp:559-572 (state_add_tendency over all storage) */
+void vo_tl_step(const vo_model *m, const double *const *xb, const double *const *dx, double dt, double *const *out) {
+  fld X[VO_NSPECIES], DX[VO_NSPECIES], OUT[VO_NSPECIES], d[VO_NSPECIES], s1[VO_NSPECIES];
+  views12(m, xb, X); views12(m, dx, DX); views12(m, (const double *const *)out, OUT);
+  alloc12(m, d); alloc12(m, s1);
+  const double a[3] = {dt / 3.0, dt / 2.0, dt};
+  fld *in = DX;
+  for (int st = 0; st < 3; ++st) {
+    tl_tendency(m, X, in, d);
+    fld *dst = (st == 2) ? OUT : s1;
+    for (int sp = 0; sp < VO_NSPECIES; ++sp) {
+      fld_copy(&dst[sp], &DX[sp]);
+      add_scaled(&dst[sp], a[st], &d[sp]);
+    }
+    in = s1;
+  }
+  free12(d); free12(s1);
+}
+
+/* rk3_ad, tangent_linear.cpp:574-603 */
+void vo_ad_step(const vo_model *m, const double *const *xb, const double *const *bar_out, double dt,
+                double *const *bar_in) {
+  fld X[VO_NSPECIES], BO[VO_NSPECIES], BI[VO_NSPECIES], bd[VO_NSPECIES], bx[VO_NSPECIES];
+  views12(m, xb, X); views12(m, bar_out, BO); views12(m, (const double *const *)bar_in, BI);
+  alloc12(m, bd); alloc12(m, bx);
+  for (int sp = 0; sp < VO_NSPECIES; ++sp) fld_copy(&BI[sp], &BO[sp]);
+  const double a[3] = {dt, dt / 2.0, dt / 3.0};
+  fld *src = BO;
+  fld prev[VO_NSPECIES];
+  alloc12(m, prev);
+  for (int st = 0; st < 3; ++st) {
+    for (int sp = 0; sp < VO_NSPECIES; ++sp) {
+      fld_zero(&bd[sp]);
+      add_scaled(&bd[sp], a[st], &src[sp]);
+      fld_zero(&bx[sp]);
+    }
+    ad_tendency(m, X, bd, bx);
+    for (int sp = 0; sp < VO_NSPECIES; ++sp) {
+      add_scaled(&BI[sp], 1.0, &bx[sp]);
+      fld_copy(&prev[sp], &bx[sp]);
+    }
+    src = prev;
+  }
+  free12(bd); free12(bx); free12(prev);
+}
+
+/* ------------------------------------------------------------------------ */
 /* Nest transfers: src/grid/nest.cpp:34-124                                  */
 /* ------------------------------------------------------------------------ */
 static fld fld_of(int nx, int ny, int nz, int stagger, const double *p) {

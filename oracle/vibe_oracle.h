@@ -156,6 +156,17 @@ void vo_nest_restrict_to_parent(const vo_nest_placement *p, int nvars, const int
 void vo_nest_apply_lateral_boundary(const vo_nest_placement *p, int nvars, const int *stagger, int cnx, int cny,
                                     int cnz, double *const *child, const double *const *parent_interp);
 
+/* Tangent-linear / adjoint of the simplified collocated RK3
+ * (src/da/tangent_linear.cpp:72-603) on the model's grid. xb, dx, d, ...:
+ * 12 FieldT storage arrays (species order). tendency_tl writes d (zeroed
+ * first); tendency_ad ACCUMULATES into bar_dx (tangent_linear.cpp:412: the
+ * caller zeroes it). tl_step = rk3_tl, ad_step = rk3_ad (:567-603). */
+void vo_tl_tendency(const vo_model *m, const double *const *xb, const double *const *dx, double *const *d);
+void vo_ad_tendency(const vo_model *m, const double *const *xb, const double *const *bar_d, double *const *bar_dx);
+void vo_tl_step(const vo_model *m, const double *const *xb, const double *const *dx, double dt, double *const *out);
+void vo_ad_step(const vo_model *m, const double *const *xb, const double *const *bar_out, double dt,
+                double *const *bar_in);
+
 /* C-ABI kernels restated (src/common/c_kernels.c). vo_tridiagonal_solve
  * follows the documented contract (c_kernels.h:38-55) with the textbook
  * recurrence of thomas_solve (helmholtz.cpp:57-86): the shipped
@@ -200,6 +211,17 @@ void vref_multigrid_restrict(vref_model *m, const double *fine, double *coarse);
 void vref_multigrid_prolong(vref_model *m, const double *coarse, double *fine);
 int vref_si_step(vref_model *m, double dt, int kind, int max_iter, double tol, int *iterations,
                  double *residual, double *pi_new, double *rhs, double *a_coef);
+/* tendency_tl/_ad are file-local in the reference (tangent_linear.cpp:295,
+ * 414); they are pinned through the public step and propagate calls. */
+void vref_tl_step(vref_model *m, const double *const *xb, const double *const *dx, double dt, double *const *out);
+void vref_ad_step(vref_model *m, const double *const *xb, const double *const *bar_out, double dt,
+                  double *const *bar_in);
+/* TangentLinearModel::propagate (frozen xb) and AdjointModel::
+ * propagate_with_trajectory over the trajectory it records */
+void vref_tl_propagate(vref_model *m, const double *const *xb, const double *const *dx0, double dt, int n_steps,
+                       double *const *out);
+void vref_ad_propagate(vref_model *m, const double *const *xb, const double *const *dy, double dt, int n_steps,
+                       double *const *out);
 void vref_davies_profile(int n_zone, double alpha_max, double *out);
 void vref_nest_interpolate_from_parent(const vo_nest_placement *p, int nvars, const int *stagger, int pnx, int pny,
                                        int pnz, const double *const *parent, int cnx, int cny, int cnz,

@@ -342,3 +342,79 @@ def nest_apply_lateral_boundary(pl, staggers, cdims, child, parent_interp, kind=
 
 def fieldt_size(nx, ny, nz, stagger):
     return (nx + 2 * HALO + (stagger == 1)) * (ny + 2 * HALO + (stagger == 2)) * (nz + 2 * HALO + (stagger == 3))
+
+
+# ---- TL/AD (port: vo_*, reference-linked: vref_*) ----
+def _tlad_fns(kind):
+    lib = _load(kind)[0]
+    p = "vo_" if kind == "port" else "vref_"
+    vp = ctypes.c_void_p
+    f = {}
+    names = [("tl_step", [vp, vp, vp, _D, vp]), ("ad_step", [vp, vp, vp, _D, vp])]
+    if kind == "port":
+        names += [("tl_tendency", [vp, vp, vp, vp]), ("ad_tendency", [vp, vp, vp, vp])]
+    else:
+        names += [("tl_propagate", [vp, vp, vp, _D, _I, vp]), ("ad_propagate", [vp, vp, vp, _D, _I, vp])]
+    for name, args in names:
+        fn = getattr(lib, p + name)
+        fn.restype = None
+        fn.argtypes = args
+        f[name] = fn
+    return f
+
+
+def _arr12(arrs):
+    return (ctypes.c_void_p * 12)(*[a.ctypes.data for a in arrs])
+
+
+def _tl_call(model, name, *args):
+    return _tlad_fns(model.kind)[name](model.h, *args)
+
+
+def tl_tendency(model, xb, dx):
+    d = [np.zeros(model.size(sp)) for sp in range(12)]
+    _tl_call(model, "tl_tendency", _arr12(xb), _arr12(dx), _arr12(d))
+    return d
+
+
+def ad_tendency(model, xb, bar_d):
+    bx = [np.zeros(model.size(sp)) for sp in range(12)]
+    _tl_call(model, "ad_tendency", _arr12(xb), _arr12(bar_d), _arr12(bx))
+    return bx
+
+
+def tl_step(model, xb, dx, dt):
+    out = [np.zeros(model.size(sp)) for sp in range(12)]
+    _tl_call(model, "tl_step", _arr12(xb), _arr12(dx), dt, _arr12(out))
+    return out
+
+
+def ad_step(model, xb, bar_out, dt):
+    out = [np.zeros(model.size(sp)) for sp in range(12)]
+    _tl_call(model, "ad_step", _arr12(xb), _arr12(bar_out), dt, _arr12(out))
+    return out
+
+
+def tl_propagate(model, xb, dx0, dt, n):
+    """Port: n frozen-base TL steps; reference: TangentLinearModel::propagate."""
+    if model.kind == "ref":
+        out = [np.zeros(model.size(sp)) for sp in range(12)]
+        _tl_call(model, "tl_propagate", _arr12(xb), _arr12(dx0), dt, n, _arr12(out))
+        return out
+    cur = [a.copy() for a in dx0]
+    for _ in range(n):
+        cur = tl_step(model, xb, cur, dt)
+    return cur
+
+
+def ad_propagate(model, xb, dy, dt, n):
+    """Port: n frozen-base AD steps; reference: propagate_with_trajectory over
+    the trajectory record_trajectory stores."""
+    if model.kind == "ref":
+        out = [np.zeros(model.size(sp)) for sp in range(12)]
+        _tl_call(model, "ad_propagate", _arr12(xb), _arr12(dy), dt, n, _arr12(out))
+        return out
+    cur = [a.copy() for a in dy]
+    for _ in range(n):
+        cur = ad_step(model, xb, cur, dt)
+    return cur

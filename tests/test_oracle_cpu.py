@@ -229,3 +229,34 @@ def test_nest_transfers_port_is_bit_exact_to_reference(oc, case):
     for a, b in zip(out["port"], out["ref"]):
         for x, y in zip(a, b):
             assert np.array_equal(x, y)
+
+
+@need_ref
+def test_tlad_port_is_bit_exact_to_reference(oc):
+    """TangentLinearModel::step / propagate and AdjointModel::step_adjoint /
+    propagate_with_trajectory (src/da/tangent_linear.cpp) against the port."""
+    import tlad_cases as tc
+    s = tc.tl_setup(oc)
+    p, r = oc.Model(s, "port"), oc.Model(s, "ref")
+    xb = tc.base_state(oc, p)
+    dx, dy = tc.perturbation(oc, p, 1), tc.perturbation(oc, p, 2)
+    for a, b in zip(oc.tl_step(p, xb, dx, 15.0), oc.tl_step(r, xb, dx, 15.0)):
+        assert np.array_equal(a, b)
+    for a, b in zip(oc.ad_step(p, xb, dy, 15.0), oc.ad_step(r, xb, dy, 15.0)):
+        assert np.array_equal(a, b)
+    for a, b in zip(oc.tl_propagate(p, xb, dx, 15.0, 3), oc.tl_propagate(r, xb, dx, 15.0, 3)):
+        assert np.array_equal(a, b)
+    for a, b in zip(oc.ad_propagate(p, xb, dy, 15.0, 3), oc.ad_propagate(r, xb, dy, 15.0, 3)):
+        assert np.array_equal(a, b)
+
+
+def test_tlad_port_dot_product(oc):
+    """The port's AD is the transpose of its TL (the reference's check_adjoint)."""
+    import tlad_cases as tc
+    s = tc.tl_setup(oc)
+    p = oc.Model(s, "port")
+    xb = tc.base_state(oc, p)
+    dx, dy = tc.perturbation(oc, p, 1), tc.perturbation(oc, p, 2)
+    lhs = tc.dot(oc, s, oc.tl_propagate(p, xb, dx, 15.0, 2), dy)
+    rhs = tc.dot(oc, s, dx, oc.ad_propagate(p, xb, dy, 15.0, 2))
+    assert abs(lhs - rhs) <= 1e-12 * max(abs(lhs), abs(rhs))

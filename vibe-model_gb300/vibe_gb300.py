@@ -510,3 +510,93 @@ def nest_apply_lateral_boundary(pl, staggers, cdims, child, parent_interp):
     if rc:
         raise RuntimeError("nest lateral rc=%d" % rc)
     return child
+
+
+# ---- tangent-linear / adjoint (include/vibe_tlad.h) -------------------------
+for _name, _args in (("vibe_tlad_create", [_I, _I, _I, _D, _D, _D, _vp, _vp, _I, ctypes.POINTER(_vp)]),
+                     ("vibe_tlad_set_base", [_vp, _vp]),
+                     ("vibe_tl_tendency", [_vp, _vp, _vp]),
+                     ("vibe_ad_tendency", [_vp, _vp, _vp]),
+                     ("vibe_tl_step", [_vp, _D, _vp, _vp]),
+                     ("vibe_tl_propagate", [_vp, _D, _I, _vp, _vp]),
+                     ("vibe_ad_step", [_vp, _D, _vp, _vp]),
+                     ("vibe_ad_propagate", [_vp, _D, _I, _vp, _vp])):
+    _f = getattr(lib, _name)
+    _f.restype = _I
+    _f.argtypes = _args
+lib.vibe_tlad_destroy.restype = None
+lib.vibe_tlad_destroy.argtypes = [_vp]
+lib.vibe_tlad_last_error.restype = ctypes.c_char_p
+lib.vibe_tlad_last_error.argtypes = []
+
+
+class TLAD:
+    """~ da::TangentLinearModel + da::AdjointModel (tangent_linear.hpp:80-150).
+    States: lists of 12 FieldT storage arrays (species order)."""
+
+    def __init__(self, nx, ny, nz, dx, dy, z_top, dzeta, zs=None, precision=0):
+        self.h = _vp()
+        self.sizes = None
+        dz = np.ascontiguousarray(dzeta, dtype=np.float64)
+        zz = None if zs is None else np.ascontiguousarray(zs, dtype=np.float64)
+        rc = lib.vibe_tlad_create(nx, ny, nz, dx, dy, z_top, dz.ctypes.data, None if zz is None else zz.ctypes.data,
+                                  precision, ctypes.byref(self.h))
+        self._rc(rc)
+
+    @staticmethod
+    def _rc(rc):
+        if rc:
+            raise RuntimeError("tlad rc=%d: %s" % (rc, lib.vibe_tlad_last_error().decode()))
+
+    def close(self):
+        if self.h:
+            lib.vibe_tlad_destroy(self.h)
+            self.h = _vp()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    @staticmethod
+    def _arr(states):
+        return (_vp * 12)(*[s.ctypes.data for s in states])
+
+    def _prep(self, states):
+        return [np.ascontiguousarray(s, dtype=np.float64) for s in states]
+
+    def set_base(self, xb):
+        xb = self._prep(xb)
+        self.sizes = [a.size for a in xb]
+        self._rc(lib.vibe_tlad_set_base(self.h, self._arr(xb)))
+
+    def _out(self):
+        return [np.zeros(n) for n in self.sizes]
+
+    def tl_tendency(self, dx):
+        dx, d = self._prep(dx), self._out()
+        self._rc(lib.vibe_tl_tendency(self.h, self._arr(dx), self._arr(d)))
+        return d
+
+    def ad_tendency(self, bar_d, bar_dx=None):
+        bar_d = self._prep(bar_d)
+        out = self._out() if bar_dx is None else [a.copy() for a in self._prep(bar_dx)]
+        self._rc(lib.vibe_ad_tendency(self.h, self._arr(bar_d), self._arr(out)))
+        return out
+
+    def tl_propagate(self, dt, n, dx0):
+        dx0, out = self._prep(dx0), self._out()
+        self._rc(lib.vibe_tl_propagate(self.h, dt, n, self._arr(dx0), self._arr(out)))
+        return out
+
+    def ad_propagate(self, dt, n, dy):
+        dy, out = self._prep(dy), self._out()
+        self._rc(lib.vibe_ad_propagate(self.h, dt, n, self._arr(dy), self._arr(out)))
+        return out
+
+    def tl_step(self, dt, dx):
+        return self.tl_propagate(dt, 1, dx)
+
+    def ad_step(self, dt, dy):
+        return self.ad_propagate(dt, 1, dy)
