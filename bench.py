@@ -338,19 +338,23 @@ def main():
 
     # ---- mixed path (the headline) ----
     mx = make(vg.MIXED)
-    mx.step(DT, NSUB, args.warmup)
-    mx.set_kernel_timing(True)
+    mx.step(DT, NSUB, args.warmup)  # the first step runs eagerly, the next capture the step graphs
     with ClockSampler(local) as clk:
-        ms_mx = timed_steps(mx, args.steps)
+        ms_mx = timed_steps(mx, args.steps)  # graph replay
+    ms_mx = max_over_ranks(ms_mx)
+    # per-kernel-class device times (event spans; eager launches) for the roofline
+    mx.set_kernel_timing(True)
+    kt_steps = max(2, min(5, args.steps))
+    ms_kt = timed_steps(mx, kt_steps)
     ktimes = mx.kernel_times()
     mx.set_kernel_timing(False)
-    ms_mx = max_over_ranks(ms_mx)
     launches = mx.launches_per_step(NSUB) * args.steps
 
     if args.only == "mixed":
         mx.close()
         print(json.dumps({"only": "mixed", "cells": cells, "ms_per_step": ms_mx / args.steps,
-                          "value": world * cells * args.steps / (ms_mx * 1e-3), "kernel_ms": ktimes}))
+                          "value": world * cells * args.steps / (ms_mx * 1e-3), "kernel_ms": ktimes,
+                          "eager_ms_per_step": ms_kt / kt_steps}))
         return
     # ---- end to end through the public API with host buffers ----
     pinned = [torch.empty(mx.size(sp), dtype=torch.float64, pin_memory=True) for sp in range(7)]

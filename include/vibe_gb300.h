@@ -126,6 +126,11 @@ int vibe_gb300_step(vibe_gb300_model *m, double dt, int n_sub, int n_steps);
 int vibe_gb300_step_async(vibe_gb300_model *m, double dt, int n_sub, int n_steps);
 int vibe_gb300_sync(vibe_gb300_model *m);
 
+/* Mixed path: replay each step as a CUDA graph (default on; the first step
+ * after a dt/n_sub change runs eagerly, the next ones capture and replay;
+ * off while kernel timing is on). */
+int vibe_gb300_set_graph(vibe_gb300_model *m, int enable);
+
 /* Kernel-level entry points (FP64 path only for the tendency). */
 int vibe_gb300_slow_tendency(vibe_gb300_model *m, double *const *host_out);
 int vibe_gb300_acoustic_substep(vibe_gb300_model *m, double dtau);

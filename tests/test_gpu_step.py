@@ -320,3 +320,18 @@ def test_terrain_fp64_step(vg, oc):
         m.step(2.0, 3, 1)
         assert o.rk3_step(2.0, 3) == 0
         assert_state_close(vg, s, m.state(), o.state(), TOL64, range(7), "terrain step")
+
+
+def test_mixed_graph_replay_is_bitwise_identical(vg):
+    """The CUDA-graph replay of the mixed step gives the eager launches' bits."""
+    s = small_setup(vg, acoustic_mode=2, ref_kind=1)
+    with vg.Model(s, vg.MIXED) as a, vg.Model(s, vg.MIXED) as b:
+        b.set_graph(False)
+        a.step(2.0, 6, 5)
+        b.step(2.0, 6, 5)
+        a.step(2.0, 6, 2)  # same dt: graphs reused
+        b.step(2.0, 6, 2)
+        a.step(1.0, 4, 3)  # new dt: eager step, new graphs
+        b.step(1.0, 4, 3)
+        for sp in range(7):
+            assert np.array_equal(a.get(sp), b.get(sp)), vg.SPECIES[sp]

@@ -111,6 +111,11 @@ struct vibe_gb300_model {
   double hz_residual = 0.0;
   double hz_ms = 0.0;
   cudaEvent_t hz_ev[2] = {nullptr, nullptr};
+  // CUDA graphs of one mixed step, per state parity
+  bool use_graph = true, graph_warm = false;
+  cudaGraphExec_t gexec[2] = {nullptr, nullptr};
+  double graph_dt = -1.0;
+  int graph_nsub = -1;
 };
 
 namespace {
@@ -546,12 +551,11 @@ void collect_timing(vibe_gb300_model* m) {  // after a stream sync
   m->ev_open.clear();
 }
 
-int enqueue_steps(vibe_gb300_model* m, double dt, int n_sub_in, int n_steps) {
-  const int n_sub = n_sub_in > 1 ? n_sub_in : 1;
-  if (int rc = configure_dt(m, dt, n_sub)) return rc;
+// One step's launches on the model stream (the state ping-pong m->cur flips).
+int enqueue_one_step(vibe_gb300_model* m, double dt, int n_sub) {
   const double dts[3] = {dt / 3.0, dt / 2.0, dt};
   const Dims& d = m->d;
-  for (int step = 0; step < n_steps; ++step) {
+  {
     double** S0 = m->S[m->cur];
     double** S1 = m->S[1 - m->cur];
     if (m->precision == VIBE_GB300_FP64) {
@@ -611,6 +615,58 @@ int enqueue_steps(vibe_gb300_model* m, double dt, int n_sub_in, int n_steps) {
       Span sp(m, 2);
       mixed_finish(d, m->tab, m->fl, ws_of(final_sub), ws_of(m->WSt[0]), w0, S1, dt, m->kmin, m->d_err, m->stream);
     }
+    m->cur = 1 - m->cur;
+  }
+  CUDA_OK(cudaGetLastError());
+  return 0;
+}
+
+void drop_graphs(vibe_gb300_model* m) {
+  for (int p = 0; p < 2; ++p) {
+    if (m->gexec[p]) cudaGraphExecDestroy(m->gexec[p]);
+    m->gexec[p] = nullptr;
+  }
+  m->graph_dt = -1.0;
+  m->graph_nsub = -1;
+}
+
+// The mixed step as a CUDA graph: one graph per state parity (the step reads
+// S[cur] and writes S[1-cur]), captured from the same launches the eager
+// path enqueues, after one eager step with the same dt/n_sub has set every
+// kernel attribute. Replayed with one cudaGraphLaunch per step.
+int enqueue_steps(vibe_gb300_model* m, double dt, int n_sub_in, int n_steps) {
+  const int n_sub = n_sub_in > 1 ? n_sub_in : 1;
+  if (int rc = configure_dt(m, dt, n_sub)) return rc;
+  const bool graph = m->use_graph && !m->timing && m->precision == VIBE_GB300_MIXED;
+  if (graph && (m->graph_dt != dt || m->graph_nsub != n_sub)) {
+    drop_graphs(m);
+    m->graph_dt = dt;
+    m->graph_nsub = n_sub;
+    m->graph_warm = false;
+  }
+  for (int step = 0; step < n_steps; ++step) {
+    if (!graph || !m->graph_warm) {
+      if (int rc = enqueue_one_step(m, dt, n_sub)) return rc;
+      m->graph_warm = true;
+      continue;
+    }
+    const int parity = m->cur;
+    if (!m->gexec[parity]) {
+      cudaGraph_t g = nullptr;
+      CUDA_OK(cudaStreamBeginCapture(m->stream, cudaStreamCaptureModeThreadLocal));
+      const int rc = enqueue_one_step(m, dt, n_sub);
+      const cudaError_t e = cudaStreamEndCapture(m->stream, &g);
+      m->cur = parity;  // capture enqueues nothing: undo the flip
+      if (rc) {
+        if (g) cudaGraphDestroy(g);
+        return rc;
+      }
+      CUDA_OK(e);
+      const cudaError_t ei = cudaGraphInstantiate(&m->gexec[parity], g, 0);
+      cudaGraphDestroy(g);
+      CUDA_OK(ei);
+    }
+    CUDA_OK(cudaGraphLaunch(m->gexec[parity], m->stream));
     m->cur = 1 - m->cur;
   }
   CUDA_OK(cudaGetLastError());
@@ -777,6 +833,7 @@ int vibe_gb300_model_create(const vibe_gb300_setup* s, int precision, vibe_gb300
 void vibe_gb300_model_destroy(vibe_gb300_model* m) {
   if (m && m->hz) vibe_helmholtz_destroy(m->hz);
   if (m && m->hz_ev[0]) { cudaEventDestroy(m->hz_ev[0]); cudaEventDestroy(m->hz_ev[1]); }
+  if (m) drop_graphs(m);
   if (!m) return;
   if (m->stream) cudaStreamSynchronize(m->stream);
   collect_timing(m);
@@ -1029,6 +1086,14 @@ int vibe_gb300_si_step(vibe_gb300_model* m, double dt, int kind, int max_iter, d
   m->f64->nonfinite(d, st, m->d_err, m->stream);
   CUDA_OK(cudaGetLastError());
   return read_status(m);
+}
+
+int vibe_gb300_set_graph(vibe_gb300_model* m, int enable) {
+  if (!m) return fail(VIBE_GB300_EBADARG, "bad argument");
+  if (m->stream) cudaStreamSynchronize(m->stream);
+  drop_graphs(m);
+  m->use_graph = enable != 0;
+  return 0;
 }
 
 int vibe_gb300_si_stats(const vibe_gb300_model* m, int* iterations, double* residual, double* solve_ms) {

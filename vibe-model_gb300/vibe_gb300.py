@@ -95,6 +95,7 @@ _sigs = {
     "vibe_gb300_last_error": (ctypes.c_char_p, []),
     "vibe_gb300_si_step": (_I, [_vp, _D, _I, _I, _D, ctypes.POINTER(_I), _dp, _vp]),
     "vibe_gb300_si_stats": (_I, [_vp, ctypes.POINTER(_I), _dp, _dp]),
+    "vibe_gb300_set_graph": (_I, [_vp, _I]),
     # C-ABI kernels (include/vibe_c_kernels.h)
     "vibe_tridiagonal_solve_f64": (_I, [_vp, _vp, _vp, _vp, _I, _vp, _vp]),
     "vibe_tridiagonal_solve_batched_f64": (_I, [_vp, _vp, _vp, _vp, _I, _I, _vp]),
@@ -267,6 +268,9 @@ class Model:
         _check(lib.vibe_gb300_si_step(self.h, dt, kind, max_iter, tol, ctypes.byref(it), ctypes.byref(res),
                                       None if pin is None else pin.ctypes.data))
         return it.value, res.value, pin
+
+    def set_graph(self, on):
+        _check(lib.vibe_gb300_set_graph(self.h, 1 if on else 0))
 
     def si_stats(self):
         """(iterations, residual, solve_ms) of the last semi-implicit step."""
