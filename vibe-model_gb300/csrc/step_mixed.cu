@@ -393,19 +393,44 @@ __global__ void k_mx_fb_mom(Dims d, Tab t, WS win, WS wout, float dtau, int do_w
 // 40 KB per block at nz = 80, so 5 blocks -- 20 warps -- fit an SM); the
 // backward sweep re-derives the explicit terms from the same inputs, which
 // the forward sweep has just pulled through L2.
-__global__ void __launch_bounds__(128) k_mx_hevi_col(Dims d, Tab t, Flags fl, WS win, WS wout, float dtau,
-                                                      const float* __restrict__ lu) {
-  extern __shared__ float s_dp[];  // [nz][128]
+template <int kPF>
+__global__ void __launch_bounds__(128, 6) k_mx_hevi_col(Dims d, Tab t, Flags fl, WS win, WS wout, float dtau,
+                                                         const float* __restrict__ lu) {
+  // per-level tables in shared memory; the forward sweep parks its per-level
+  // results in the thread's own column of the output arrays (wt on the w
+  // faces, dp on pi', the explicit source S on rho'), where the backward
+  // sweep reads them back (from L2) and overwrites them with the final values
+  extern __shared__ float s_tab[];
+  const int nz = d.nz;
+  float* s_tfz = s_tab;                    // nz+1
+  float* s_idzw = s_tfz + (nz + 1);        // nz+1
+  float* s_rfz = s_idzw + (nz + 1);        // nz+1
+  float* s_idzc = s_rfz + (nz + 1);        // nz
+  float* s_kap = s_idzc + nz;              // nz
+  float* s_la = s_kap + nz;                // nz
+  float* s_lc = s_la + nz;                 // nz
+  float* s_li = s_lc + nz;                 // nz
+  float* s_r0 = s_li + nz;                 // nz
+  const int tid = threadIdx.y * blockDim.x + threadIdx.x;
+  for (int e = tid; e <= nz; e += 128) {
+    s_tfz[e] = t.tfz[e];
+    s_idzw[e] = t.idzw[e];
+    s_rfz[e] = t.rfz[e];
+    if (e < nz) {
+      s_idzc[e] = t.idzc[e];
+      s_kap[e] = t.kap[e];
+      s_la[e] = lu[e];
+      s_lc[e] = lu[nz + e];
+      s_li[e] = lu[2 * nz + e];
+      s_r0[e] = t.r0c[e];
+    }
+  }
+  __syncthreads();
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
-  const int nz = d.nz;
-  const int tid = threadIdx.y * blockDim.x + threadIdx.x;
   if (i >= d.nx || j >= d.ny) return;
   const float b = (float)fl.hevi_beta, ob = 1.f - b;
   const float cpf = (float)kCp;
-  const float* __restrict__ la = lu;
-  const float* __restrict__ lc = lu + nz;
-  const float* __restrict__ li = lu + 2 * nz;
   const size_t col = (size_t)j * d.P + i;
   const size_t pl = d.plane;
   const float* __restrict__ U0 = win.f[U] + col;
@@ -413,72 +438,98 @@ __global__ void __launch_bounds__(128) k_mx_hevi_col(Dims d, Tab t, Flags fl, WS
   const float* __restrict__ W0 = win.f[W] + col;
   const float* __restrict__ P0 = win.f[PI] + col;
   const float* __restrict__ R0 = win.f[RHO] + col;
-  const size_t vn = d.P;  // v(j+1) offset
-  auto Dh_at = [&](int k) {
-    const size_t o = (size_t)k * pl;
-    return -(t.r0c[k] * ((U0[o + 1] - U0[o]) * t.dx_inv + (V0[o + vn] - V0[o]) * t.dy_inv));
-  };
-  // forward sweep: rhs(k) from the explicit part, dp(k) = (rhs - a dp(k-1)) / den
-  float p_k = P0[0];
-  float w_k = W0[0];
-  float wt_k = w_k;  // face 0: no pressure gradient
-  float dp_prev = 0.f;
-#pragma unroll 4
-  for (int k = 0; k < nz; ++k) {
-    const size_t o1 = (size_t)(k + 1) * pl;
-    const float w_k1 = W0[o1];
-    float wt_k1 = w_k1, p_k1 = 0.f;
-    if (k + 1 < nz) {
-      p_k1 = P0[o1];
-      wt_k1 = w_k1 - dtau * ob * cpf * t.tfz[k + 1] * (p_k1 - p_k) * t.idzw[k + 1];
-    }
-    const float rk = t.rfz[k], rk1 = t.rfz[k + 1], idz = t.idzc[k];
-    const float dv_old = -(rk1 * w_k1 - rk * w_k) * idz;
-    const float dv_t = -(rk1 * wt_k1 - rk * wt_k) * idz;
-    const float S = Dh_at(k) + ob * dv_old;
-    const float rhs = p_k + dtau * t.kap[k] * (S + b * dv_t);
-    const float dpk = (k == 0) ? rhs * li[0] : (rhs - la[k] * dp_prev) * li[k];
-    s_dp[(size_t)k * 128 + tid] = dpk;
-    dp_prev = dpk;
-    w_k = w_k1;
-    wt_k = wt_k1;
-    p_k = p_k1;
-  }
-  // backward sweep: x(k) = dp(k) - c'(k) x(k+1); after x(k) is known, face
-  // k+1 (needs x(k), x(k+1)) and cell k+1 (needs faces k+1, k+2) are final.
   float* __restrict__ Wo = wout.f[W] + col;
   float* __restrict__ Po = wout.f[PI] + col;
   float* __restrict__ Ro = wout.f[RHO] + col;
-  float x_up = s_dp[(size_t)(nz - 1) * 128 + tid];  // x(nz-1)
-  float w_up = W0[(size_t)nz * pl];                  // w_old(nz) = wn(nz)
-  float wn_up = w_up;
-  float p_up = P0[(size_t)(nz - 1) * pl];            // pi'_old(nz-1)
-  Wo[(size_t)nz * pl] = wn_up;
-#pragma unroll 4
-  for (int k = nz - 2; k >= -1; --k) {
-    const int kk = k + 1;  // face kk and cell kk are finalised here
-    const size_t okk = (size_t)kk * pl;
-    const float w_kk = W0[okk];
-    float x_k = 0.f, wn_kk, p_k = 0.f;
-    if (k >= 0) {
-      x_k = s_dp[(size_t)k * 128 + tid] - lc[k] * x_up;
-      p_k = P0[(size_t)k * pl];
-      const float wt_kk = w_kk - dtau * ob * cpf * t.tfz[kk] * (p_up - p_k) * t.idzw[kk];
-      wn_kk = wt_kk - dtau * b * cpf * t.tfz[kk] * (x_up - x_k) * t.idzw[kk];
-    } else {
-      wn_kk = w_kk;  // face 0
+  const size_t vn = d.P;  // v(j+1) offset
+  const float dxi = t.dx_inv, dyi = t.dy_inv;
+  // Loads run kPF levels ahead of their use (register ring, static slots).
+  // ---- forward sweep: wt, S and dp = (rhs - a dp(k-1)) / den per level
+  float fw[kPF], fp[kPF], fu0[kPF], fu1[kPF], fv0[kPF], fv1[kPF];
+  auto loadF = [&](int L, int q) {
+    const size_t o = (size_t)L * pl, o1 = o + pl;
+    fw[q] = W0[o1];
+    fp[q] = (L + 1 < nz) ? P0[o1] : 0.f;
+    fu0[q] = U0[o];
+    fu1[q] = U0[o + 1];
+    fv0[q] = V0[o];
+    fv1[q] = V0[o + vn];
+  };
+#pragma unroll
+  for (int q = 0; q < kPF; ++q)
+    if (q < nz) loadF(q, q);
+  float p_k = P0[0];
+  float w_k = W0[0];
+  float wt_k = w_k;  // face 0: no pressure gradient
+  Wo[0] = w_k;
+  float dp_prev = 0.f;
+  for (int k0 = 0; k0 < nz; k0 += kPF) {
+#pragma unroll
+    for (int q = 0; q < kPF; ++q) {
+      const int k = k0 + q;
+      if (k < nz) {
+        const float w_k1 = fw[q];
+        float wt_k1 = w_k1, p_k1 = 0.f;
+        if (k + 1 < nz) {
+          p_k1 = fp[q];
+          wt_k1 = w_k1 - dtau * ob * cpf * s_tfz[k + 1] * (p_k1 - p_k) * s_idzw[k + 1];
+        }
+        const float Dh = -(s_r0[k] * ((fu1[q] - fu0[q]) * dxi + (fv1[q] - fv0[q]) * dyi));
+        if (k + kPF < nz) loadF(k + kPF, q);
+        const float rk = s_rfz[k], rk1 = s_rfz[k + 1], idz = s_idzc[k];
+        const float dv_old = -(rk1 * w_k1 - rk * w_k) * idz;
+        const float dv_t = -(rk1 * wt_k1 - rk * wt_k) * idz;
+        const float S = Dh + ob * dv_old;
+        const float rhs = p_k + dtau * s_kap[k] * (S + b * dv_t);
+        const float dpk = (k == 0) ? rhs * s_li[0] : (rhs - s_la[k] * dp_prev) * s_li[k];
+        const size_t o = (size_t)k * pl;
+        Po[o] = dpk;
+        Ro[o] = S;
+        Wo[o + pl] = wt_k1;  // face k+1 (face nz: w_old(nz), already final)
+        dp_prev = dpk;
+        w_k = w_k1;
+        wt_k = wt_k1;
+        p_k = p_k1;
+      }
     }
-    const float rk = t.rfz[kk], rk1 = t.rfz[kk + 1], idz = t.idzc[kk];
-    const float dv_old = -(rk1 * w_up - rk * w_kk) * idz;
-    const float dv_new = -(rk1 * wn_up - rk * wn_kk) * idz;
-    const float S = Dh_at(kk) + ob * dv_old;
-    Ro[okk] = R0[okk] + dtau * (S + b * dv_new);
-    Po[okk] = x_up;
-    Wo[okk] = wn_kk;
-    x_up = x_k;
-    wn_up = wn_kk;
-    w_up = w_kk;
-    p_up = p_k;
+  }
+  // ---- backward sweep: x(k) = dp(k) - c'(k) x(k+1); after x(k) is known, face
+  // k+1 (needs x(k), x(k+1)) and cell k+1 (needs faces k+1, k+2) are final.
+  float bdp[kPF], bwt[kPF], bS[kPF], br[kPF];
+  auto loadB = [&](int kk, int q) {  // inputs of step kk (cell/face kk)
+    const size_t o = (size_t)kk * pl;
+    bdp[q] = (kk >= 1) ? Po[o - pl] : 0.f;  // dp(kk-1)
+    bwt[q] = Wo[o];                          // wt(kk)
+    bS[q] = Ro[o];                           // S(kk)
+    br[q] = R0[o];                           // rho'_old(kk)
+  };
+#pragma unroll
+  for (int q = 0; q < kPF; ++q)
+    if (nz - 1 - q >= 0) loadB(nz - 1 - q, q);
+  float x_up = dp_prev;  // x(nz-1) = dp(nz-1)
+  float wn_up = Wo[(size_t)nz * pl];
+  for (int kk0 = nz - 1; kk0 >= 0; kk0 -= kPF) {
+#pragma unroll
+    for (int q = 0; q < kPF; ++q) {
+      const int kk = kk0 - q;  // face kk and cell kk are finalised here
+      if (kk >= 0) {
+        const int k = kk - 1;
+        const size_t okk = (size_t)kk * pl;
+        float x_k = 0.f, wn_kk = bwt[q];
+        if (k >= 0) {
+          x_k = bdp[q] - s_lc[k] * x_up;
+          wn_kk = bwt[q] - dtau * b * cpf * s_tfz[kk] * (x_up - x_k) * s_idzw[kk];
+        }
+        const float dv_new = -(s_rfz[kk + 1] * wn_up - s_rfz[kk] * wn_kk) * s_idzc[kk];
+        const float rnew = br[q] + dtau * (bS[q] + b * dv_new);
+        if (kk - kPF >= 0) loadB(kk - kPF, q);
+        Ro[okk] = rnew;
+        Po[okk] = x_up;
+        Wo[okk] = wn_kk;
+        x_up = x_k;
+        wn_up = wn_kk;
+      }
+    }
   }
 }
 
@@ -634,17 +685,31 @@ void mixed_fb_substep(const Dims& d, const Tab& t, const Flags& fl, const WS& wi
   k_mx_fb_mom<<<g3(d.nx + 1, d.ny + 1, d.nz + 1, b), b, 0, stream>>>(d, t, win, wout, dtau, 1);
 }
 
+// Prefetch depth of the HEVI column kernel (levels of loads in flight per
+// thread); VIBE_GB300_HEVI_PF=2|4|6|8 overrides the built-in choice.
+static int hevi_pf() {
+  static int pf = 0;
+  if (pf == 0) {
+    pf = 2;  // measured best at 512x512x80: 2 < 4 < 6 < 8 (0.237 / 0.267 / 0.273 / 0.310 ms)
+    if (const char* e = std::getenv("VIBE_GB300_HEVI_PF")) {
+      const int v = std::atoi(e);
+      if (v == 2 || v == 4 || v == 6 || v == 8) pf = v;
+    }
+  }
+  return pf;
+}
+
 void mixed_hevi_column(const Dims& d, const Tab& t, const Flags& fl, const WS& win, const WS& wout, float dtau,
                        const float* lu, cudaStream_t stream) {
   const dim3 bc(32, 4);
-  const size_t smem = (size_t)d.nz * bc.x * bc.y * sizeof(float);
-  static size_t smem_set = 0;  // opt in above 48 KB once per size
-  if (smem > 48 * 1024 && smem > smem_set) {
-    cudaFuncSetAttribute(k_mx_hevi_col, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    smem_set = smem;
+  const size_t smem = 9 * (size_t)(d.nz + 1) * sizeof(float);
+  const dim3 g((d.nx + bc.x - 1) / bc.x, (d.ny + bc.y - 1) / bc.y);
+  switch (hevi_pf()) {
+    case 6: k_mx_hevi_col<6><<<g, bc, smem, stream>>>(d, t, fl, win, wout, dtau, lu); break;
+    case 8: k_mx_hevi_col<8><<<g, bc, smem, stream>>>(d, t, fl, win, wout, dtau, lu); break;
+    case 4: k_mx_hevi_col<4><<<g, bc, smem, stream>>>(d, t, fl, win, wout, dtau, lu); break;
+    default: k_mx_hevi_col<2><<<g, bc, smem, stream>>>(d, t, fl, win, wout, dtau, lu); break;
   }
-  k_mx_hevi_col<<<dim3((d.nx + bc.x - 1) / bc.x, (d.ny + bc.y - 1) / bc.y), bc, smem, stream>>>(d, t, fl, win, wout,
-                                                                                               dtau, lu);
 }
 
 void mixed_uv_backward(const Dims& d, const Tab& t, const WS& win, const WS& wout, float dtau, cudaStream_t stream) {
