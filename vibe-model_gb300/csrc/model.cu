@@ -590,7 +590,9 @@ int enqueue_one_step(vibe_gb300_model* m, double dt, int n_sub) {
         const WS win = (stage == 0) ? w0 : ws_compose(final_sub, m->WSt[(stage - 1) & 1]);
         {
           Span sp(m, 0);
-          mixed_stage(d, m->tab, m->fl, win, w0, ws_of(st_out), S0, S1, dts[stage], stage == 2, m->d_err, m->stream);
+          if (mixed_stage(d, m->tab, m->fl, win, w0, ws_of(st_out), S0, S1, dts[stage], stage == 2, m->d_err,
+                          m->stream))
+            return fail(VIBE_GB300_EDEVICE, "TMA descriptor creation failed (cuTensorMapEncodeTiled)");
         }
         const float dtau = (float)(dts[stage] / (double)n_sub);
         float** in = st_out;
@@ -679,6 +681,7 @@ int read_status(vibe_gb300_model* m) {
   collect_timing(m);
   const unsigned e = *m->h_err;
   CUDA_OK(cudaMemsetAsync(m->d_err, 0, sizeof(unsigned), m->stream));
+  if (e & kErrWaitTimeout) return fail(VIBE_GB300_EDEVICE, "a TMA box of the stage kernel did not arrive (bounded wait)");
   if (e & kErrSingular) return fail(VIBE_GB300_ESINGULAR, "tridiagonal pivot below 1e-300");
   if (e & kErrNonFinite) return fail(VIBE_GB300_ENONFINITE, "non-finite value in the state");
   return 0;
@@ -925,8 +928,9 @@ int vibe_gb300_slow_tendency(vibe_gb300_model* m, double* const* host_out) {
     if (int rc = sync_working(m)) return rc;
     WS none;
     for (int q = 0; q < NSPECIES; ++q) none.f[q] = nullptr;
-    mixed_stage(m->d, m->tab, m->fl, ws_of(m->W0), none, ws_of(m->WSt[1]), nullptr, nullptr, 1.0, false, m->d_err,
-                 m->stream);
+    if (mixed_stage(m->d, m->tab, m->fl, ws_of(m->W0), none, ws_of(m->WSt[1]), nullptr, nullptr, 1.0, false,
+                    m->d_err, m->stream))
+      return fail(VIBE_GB300_EDEVICE, "TMA descriptor creation failed (cuTensorMapEncodeTiled)");
     for (int q = 0; q < NSPECIES; ++q) {
       int ni = m->d.nx + (q == U), nj = m->d.ny + (q == V), nk = m->d.nz + (q == W);
       const bool active = q <= QV || m->fl.moist;

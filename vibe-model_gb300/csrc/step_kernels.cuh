@@ -66,7 +66,7 @@ struct WS {          // FP32 working state (perturbation form)
   float* f[NSPECIES]; // u v w rho' theta' pi' qv qc..qg
 };
 
-void mixed_stage(const Dims& d, const Tab& t, const Flags& fl, const WS& win, const WS& w0, const WS& wout,
+int mixed_stage(const Dims& d, const Tab& t, const Flags& fl, const WS& win, const WS& w0, const WS& wout,
                  double* const* s0, double* const* ss, double dt_stage, bool write_fp64, unsigned* err,
                  cudaStream_t stream);
 void mixed_fb_substep(const Dims& d, const Tab& t, const Flags& fl, const WS& win, const WS& wout, float dtau,

@@ -18,6 +18,12 @@
 // (pi' pressure gradient, fast terms integrated once by the substeps).
 #include <cmath>
 #include <cstdlib>
+#include <map>
+#include <mutex>
+#include <tuple>
+
+#include <cuda.h>
+#include <cudaTypedefs.h>
 #include "step_kernels.cuh"
 
 namespace vgb {
@@ -84,40 +90,123 @@ __device__ __forceinline__ float gradc(float m3, float m2, float m1, float p1, f
 
 // ---- RK stage kernel: slow tendency + s = s0 + dt*R ------------------------
 // 2.5-D: a block owns 32 x 8 columns and marches up a chunk of levels
-// (grid z = chunk). At each level the fields' planes are staged in shared
-// memory with the halo their stencils need (3 for the scalar WENO /
-// high-order stencils, 1 for the winds, pi', rho'). The tiles are loaded
-// with the reference's clamps (clamp_at, field.hpp:91-96), so a tile read at
-// an unclamped offset returns the clamped value and most stencil reads need
-// no clamp of their own. Each thread keeps its own column's vertical
-// neighbours in registers: theta' and qv over k-3..k+3 for the vertical WENO,
-// whose flux through the top face of level k is carried to level k+1 as its
-// bottom flux (one WENO evaluation per vertical face), and w, pi', rho' at
-// k-1. Horizontal WENO fluxes are computed once per face into shared memory.
+// (grid z = chunk). Each level's planes of theta', qv, u, v, w, pi', rho' are
+// brought into shared memory by TMA (cp.async.bulk.tensor, one box per field
+// with the halo its stencils need: 3 rows for the scalar WENO / high-order
+// stencils, 1 row for the others; every box is 40 columns wide starting 4
+// columns left of the block, keeping the TMA x coordinate 16-byte aligned),
+// double-buffered: the next level's boxes are in flight, tracked by an
+// mbarrier, while the current level computes. Elements outside a field's
+// index range arrive as zeros; blocks at the domain edge then overwrite them
+// with the reference's clamped values (clamp_at, field.hpp:91-96), so a tile
+// read at an unclamped offset returns the clamped value. Each thread keeps
+// its own column's vertical neighbours in registers: theta' and qv over
+// k-3..k+3 for the vertical WENO, whose flux through the top face of level k
+// is carried to level k+1 as its bottom flux (one WENO evaluation per
+// vertical face), and w, pi', rho' at k-1. Horizontal WENO fluxes are
+// computed once per face into shared memory.
 constexpr int TX = 32, TY = 8;
-constexpr int W3 = TX + 6, H3 = TY + 6;  // halo-3 tile
-constexpr int W1 = TX + 2, H1 = TY + 2;  // halo-1 tile
 constexpr int NT = TX * TY;
+constexpr int TW = 40;                   // box width (floats), all fields
+constexpr int XO = 4;                    // local column of global i0
+constexpr int R3 = TY + 6, R1 = TY + 2;  // box rows: halo 3 / halo 1
+constexpr int SZ3 = 576, SZ1 = 416;      // box sizes padded to 128 B
+constexpr int kBuf = 2 * SZ3 + 5 * SZ1;  // floats per level buffer
+enum StageTile { TT = 0, TQ, TU, TV, TWF, TP, TR, NTILE };
+__host__ __device__ constexpr int tile_off(int b) { return b < 2 ? b * SZ3 : 2 * SZ3 + (b - 2) * SZ1; }
+constexpr unsigned kLevelBytes = (2 * R3 * TW + 5 * R1 * TW) * 4;
+constexpr long long kSpinLimit = 1ll << 24;  // bounded mbarrier waits
 
-template <int H>
-__device__ __forceinline__ void load_tile(float* __restrict__ dst, const float* __restrict__ plane, int P, int i0,
+struct StageMaps {
+  CUtensorMap m[NTILE];
+  int xmax[NTILE], ymax[NTILE];
+};
+
+// plain loader with the TMA box geometry (moisture species beyond qv)
+__device__ __forceinline__ void load_box3(float* __restrict__ dst, const float* __restrict__ plane, int P, int i0,
                                           int j0, int xmax, int ymax) {
-  constexpr int Wt = TX + 2 * H, Ht = TY + 2 * H;
-  for (int e = threadIdx.y * TX + threadIdx.x; e < Wt * Ht; e += NT) {
-    const int ty = e / Wt, tx = e - ty * Wt;
-    const int gi = iclamp(i0 - H + tx, 0, xmax), gj = iclamp(j0 - H + ty, 0, ymax);
+  for (int e = threadIdx.y * TX + threadIdx.x; e < R3 * TW; e += NT) {
+    const int ty = e / TW, tx = e - ty * TW;
+    const int gi = iclamp(i0 - XO + tx, 0, xmax), gj = iclamp(j0 - 3 + ty, 0, ymax);
     dst[e] = plane[gj * P + gi];
   }
 }
 
+__device__ __forceinline__ unsigned smem_u32(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbar_init(unsigned long long* b, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(b)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(unsigned long long* b, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(b)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(unsigned long long* b, unsigned parity) {
+  unsigned ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_u32(b)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+__device__ __forceinline__ bool mbar_wait_bounded(unsigned long long* b, unsigned parity) {
+  for (long long it = 0; it < kSpinLimit; ++it)
+    if (mbar_try_wait(b, parity)) return true;
+  return false;
+}
+__device__ __forceinline__ void tma_load_3d(float* dst, const CUtensorMap* map, int x, int y, int z,
+                                            unsigned long long* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];"
+      ::"r"(smem_u32(dst)), "l"(map), "r"(x), "r"(y), "r"(z), "r"(smem_u32(bar))
+      : "memory");
+}
+
+// one level's seven boxes into buffer `buf` (called by one thread)
+__device__ __forceinline__ void issue_level(const StageMaps& M, float* buf, unsigned long long* bar, int i0, int j0,
+                                            int k, int nz) {
+  const int kc = imin(k, nz - 1);
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  mbar_expect_tx(bar, kLevelBytes);
+  tma_load_3d(buf + tile_off(TT), &M.m[TT], i0 - XO, j0 - 3, kc, bar);
+  tma_load_3d(buf + tile_off(TQ), &M.m[TQ], i0 - XO, j0 - 3, kc, bar);
+  tma_load_3d(buf + tile_off(TU), &M.m[TU], i0 - XO, j0 - 1, kc, bar);
+  tma_load_3d(buf + tile_off(TV), &M.m[TV], i0 - XO, j0 - 1, kc, bar);
+  tma_load_3d(buf + tile_off(TWF), &M.m[TWF], i0 - XO, j0 - 1, k, bar);
+  tma_load_3d(buf + tile_off(TP), &M.m[TP], i0 - XO, j0 - 1, kc, bar);
+  tma_load_3d(buf + tile_off(TR), &M.m[TR], i0 - XO, j0 - 1, kc, bar);
+}
+
+// replace out-of-range box elements by the clamped ones: columns first, then
+// whole rows (so corners get clamp(x) and clamp(y))
+__device__ void fix_box(float* t, int rows, int halo, int i0, int j0, int xmax, int ymax, int tid) {
+  const int x0 = i0 - XO, y0 = j0 - halo;
+  const int lxlo = imax(-x0, 0), lxhi = imin(xmax - x0, TW - 1);
+  const int lylo = imax(-y0, 0), lyhi = imin(ymax - y0, rows - 1);
+  if (lxlo > 0 || lxhi < TW - 1)
+    for (int e = tid; e < rows * TW; e += NT) {
+      const int r = e / TW, c = e - r * TW;
+      if (c < lxlo) t[e] = t[r * TW + lxlo];
+      else if (c > lxhi) t[e] = t[r * TW + lxhi];
+    }
+  __syncthreads();
+  if (lylo > 0 || lyhi < rows - 1)
+    for (int e = tid; e < rows * TW; e += NT) {
+      const int r = e / TW, c = e - r * TW;
+      if (r < lylo) t[e] = t[lylo * TW + c];
+      else if (r > lyhi) t[e] = t[lyhi * TW + c];
+    }
+}
+
 template <bool kFP64Out>
-__global__ void __launch_bounds__(NT, 3) k_mx_stage(Dims d, Tab t, Flags fl, const __grid_constant__ WS win,
-                                                 const __grid_constant__ WS w0, const __grid_constant__ WS wout,
-                                                 const __grid_constant__ CS64 s0, const __grid_constant__ MS64 ss,
-                                                 float dts, double dtd, int kchunk, unsigned* err) {
-  __shared__ float sT[H3 * W3], sQ[H3 * W3];
-  __shared__ float sU[H1 * W1], sV[H1 * W1], sW[H1 * W1], sP[H1 * W1], sR[H1 * W1];
+__global__ void __launch_bounds__(NT, 3) k_mx_stage(Dims d, Tab t, Flags fl, const __grid_constant__ StageMaps M,
+                                                    const __grid_constant__ WS win, const __grid_constant__ WS w0,
+                                                    const __grid_constant__ WS wout, const __grid_constant__ CS64 s0,
+                                                    const __grid_constant__ MS64 ss, float dts, double dtd,
+                                                    int kchunk, unsigned* err) {
+  __shared__ __align__(128) float sbuf[2][kBuf];
+  __shared__ __align__(128) float sQm[R3 * TW];  // moisture species beyond qv (plain loads)
   __shared__ float sFx[TY * (TX + 1)], sFy[(TY + 1) * TX];
+  __shared__ __align__(8) unsigned long long sbar[2];
   const int nx = d.nx, ny = d.ny, nz = d.nz, P = d.P;
   const size_t pl = d.plane;
   const int i0 = blockIdx.x * TX, j0 = blockIdx.y * TY;
@@ -128,13 +217,20 @@ __global__ void __launch_bounds__(NT, 3) k_mx_stage(Dims d, Tab t, Flags fl, con
   const bool in_box = i <= nx && j <= ny;
   const bool cell = i < nx && j < ny;
   const float cp = (float)kCp;
-  const int o1 = (ty + 1) * W1 + (tx + 1), o3 = (ty + 3) * W3 + (tx + 3);  // own point in the tiles
-  const int dim = (i > 0) ? -1 : 0;              // im - i, im = max(i-1, 0)
-  const int ipu = imin(i, nx - 1) - i;           // ip - i on u faces (-1 at i = nx)
-  const int jpv = imin(j, ny - 1) - j;           // jp - j on v faces (-1 at j = ny)
-  const int djm = (j > 0) ? -1 : 0;              // jm - j
+  const int o1 = (ty + 1) * TW + (tx + XO), o3 = (ty + 3) * TW + (tx + XO);  // own point in the boxes
+  const int dim = (i > 0) ? -1 : 0;     // im - i, im = max(i-1, 0)
+  const int ipu = imin(i, nx - 1) - i;  // ip - i on u faces (-1 at i = nx)
+  const int jpv = imin(j, ny - 1) - j;  // jp - j on v faces (-1 at j = ny)
+  const int djm = (j > 0) ? -1 : 0;     // jm - j
   const size_t colc = (size_t)imin(j, ny) * P + imin(i, nx);
   const float* __restrict__ wcolp = win.f[W] + colc;
+  const bool edge = (i0 - XO < 0) || (j0 - 3 < 0) || (i0 - XO + TW > nx - 1) || (j0 + TY + 3 > ny - 1);
+  if (tid == 0) {
+    mbar_init(&sbar[0], 1);
+    mbar_init(&sbar[1], 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    issue_level(M, sbuf[0], &sbar[0], i0, j0, kb, nz);
+  }
   // vertical registers of the own column
   float wT[7], wQ[7];
   float wprev = 0.f, pprev = 0.f, rprev = 0.f;
@@ -153,20 +249,35 @@ __global__ void __launch_bounds__(NT, 3) k_mx_stage(Dims d, Tab t, Flags fl, con
   float fcT = 0.f, fcQ = 0.f;  // carried vertical WENO fluxes (top face of the level below)
   bool bad = false;
   for (int k = kb; k <= klast; ++k) {
+    const int lev = k - kb, cur = lev & 1;
     const bool cells_here = k < nz;  // uniform across the block
     const int kc = imin(k, nz - 1);
-    __syncthreads();  // the previous level's tiles are no longer read
-    if (cells_here) {
-      const size_t ok = (size_t)k * pl;
-      load_tile<3>(sT, win.f[THETA] + ok, P, i0, j0, nx - 1, ny - 1);
-      load_tile<3>(sQ, win.f[QV] + ok, P, i0, j0, nx - 1, ny - 1);
-      load_tile<1>(sU, win.f[U] + ok, P, i0, j0, nx, ny - 1);
-      load_tile<1>(sV, win.f[V] + ok, P, i0, j0, nx - 1, ny);
-      load_tile<1>(sP, win.f[PI] + ok, P, i0, j0, nx - 1, ny - 1);
-      load_tile<1>(sR, win.f[RHO] + ok, P, i0, j0, nx, ny);
+    __syncthreads();  // every thread is done with the other buffer (level k-1)
+    if (tid == 0 && k + 1 <= klast) issue_level(M, sbuf[cur ^ 1], &sbar[cur ^ 1], i0, j0, k + 1, nz);
+    const bool arrived = mbar_wait_bounded(&sbar[cur], (lev >> 1) & 1);
+    if (__syncthreads_or(!arrived)) {
+      // a box did not arrive: report, and leave none in flight before exiting
+      if (tid == 0) {
+        atomicOr(err, (unsigned)kErrWaitTimeout);
+        mbar_wait_bounded(&sbar[cur], (lev >> 1) & 1);
+        if (k + 1 <= klast) mbar_wait_bounded(&sbar[cur ^ 1], ((lev + 1) >> 1) & 1);
+      }
+      break;
     }
-    load_tile<1>(sW, win.f[W] + (size_t)k * pl, P, i0, j0, nx - 1, ny - 1);
-    __syncthreads();
+    float* const buf = sbuf[cur];
+    const float* const sT = buf + tile_off(TT);
+    const float* const sQ = buf + tile_off(TQ);
+    const float* const sU = buf + tile_off(TU);
+    const float* const sV = buf + tile_off(TV);
+    const float* const sW = buf + tile_off(TWF);
+    const float* const sP = buf + tile_off(TP);
+    const float* const sR = buf + tile_off(TR);
+    if (edge) {
+      fix_box(buf + tile_off(TT), R3, 3, i0, j0, M.xmax[TT], M.ymax[TT], tid);
+      fix_box(buf + tile_off(TQ), R3, 3, i0, j0, M.xmax[TQ], M.ymax[TQ], tid);
+      for (int b = TU; b < NTILE; ++b) fix_box(buf + tile_off(b), R1, 1, i0, j0, M.xmax[b], M.ymax[b], tid);
+      __syncthreads();
+    }
     const size_t c = (size_t)k * pl + colc;
     const int kp1 = imin(k + 1, nz - 1), km = imax(k - 1, 0);
     auto emit = [&](int q, float r) {
@@ -179,10 +290,10 @@ __global__ void __launch_bounds__(NT, 3) k_mx_stage(Dims d, Tab t, Flags fl, con
       const float ump = sU[o1 + ipu], umm = sU[o1 + dim];
       const float uc = 0.5f * (umm + ump);
       const float ux = (ump - umm) * t.dx_inv;
-      const float uy = (sU[o1 + ipu + W1] - sU[o1 + ipu - W1]) * (0.5f * t.dy_inv);
+      const float uy = (sU[o1 + ipu + TW] - sU[o1 + ipu - TW]) * (0.5f * t.dy_inv);
       const float* __restrict__ ucol = win.f[U] + (size_t)j * P + (i + ipu);
       const float uz = (ucol[(size_t)kp1 * pl] - ucol[(size_t)km * pl]) * (0.5f * t.idza[k]);
-      const float vc = 0.25f * (sV[o1 + dim - W1] + sV[o1 + ipu - W1] + sV[o1 + dim] + sV[o1 + ipu]);
+      const float vc = 0.25f * (sV[o1 + dim - TW] + sV[o1 + ipu - TW] + sV[o1 + dim] + sV[o1 + ipu]);
       const float wc = 0.5f * (sW[o1 + ipu] + win.f[W][(size_t)kp1 * pl + (size_t)j * P + (i + ipu)]);
       float r = -(uc * ux + vc * uy + wc * uz);
       if (fl.coriolis) r += (fl.coriolis == 2 ? t.f0 + t.beta * (((float)j + 0.5f) * t.dy - 0.5f * (float)ny * t.dy) : t.f0) * vc;
@@ -190,7 +301,7 @@ __global__ void __launch_bounds__(NT, 3) k_mx_stage(Dims d, Tab t, Flags fl, con
       emit(U, r);
     }
     if (cells_here && in_box && i < nx) {  // v face (i, j, k)
-      const int dp1 = jpv * W1, dm1 = djm * W1;
+      const int dp1 = jpv * TW, dm1 = djm * TW;
       const float vpp = sV[o1 + dp1], vmm = sV[o1 + dm1];
       const float vc = 0.5f * (vmm + vpp);
       const float vy = (vpp - vmm) * t.dy_inv;
@@ -201,20 +312,19 @@ __global__ void __launch_bounds__(NT, 3) k_mx_stage(Dims d, Tab t, Flags fl, con
       const float wc = 0.5f * (sW[o1 + dp1] + win.f[W][(size_t)kp1 * pl + (size_t)(j + jpv) * P + i]);
       float r = -(uc * vx + vc * vy + wc * vz);
       if (fl.coriolis) r -= (fl.coriolis == 2 ? t.f0 + t.beta * (((float)j + 0.5f) * t.dy - 0.5f * (float)ny * t.dy) : t.f0) * uc;
-      r -= cp * (0.5f * (sT[o3 + djm * W3] + sT[o3 + jpv * W3])) * (sP[o1 + dp1] - sP[o1 + dm1]) * t.dy_inv;
+      r -= cp * (0.5f * (sT[o3 + djm * TW] + sT[o3 + jpv * TW])) * (sP[o1 + dp1] - sP[o1 + dm1]) * t.dy_inv;
       emit(V, r);
     }
-    // w face (i, j, k), k = 0..nz; at k = nz the tiles other than sW still
-    // hold level nz-1 = kc
+    // w face (i, j, k), k = 0..nz; at k = nz the boxes other than w hold level nz-1 = kc
     const float wk = sW[o1];
     if (cell) {
       const float wkc = cells_here ? wk : wprev;
       const float wc = 0.5f * (wkc + wk);
       const float wz = (wk - wprev) * t.idza[kc];
       const float wx = (sW[o1 + 1] - sW[o1 - 1]) * (0.5f * t.dx_inv);
-      const float wy = (sW[o1 + W1] - sW[o1 - W1]) * (0.5f * t.dy_inv);
+      const float wy = (sW[o1 + TW] - sW[o1 - TW]) * (0.5f * t.dy_inv);
       const float uc = 0.5f * (sU[o1] + sU[o1 + 1]);
-      const float vc = 0.5f * (sV[o1] + sV[o1 + W1]);
+      const float vc = 0.5f * (sV[o1] + sV[o1 + TW]);
       float r = -(uc * wx + vc * wy + wc * wz);
       const float thc = sT[o3], pic = sP[o1];
       const float thm = wT[2];  // theta'(max(k-1, 0))
@@ -233,7 +343,7 @@ __global__ void __launch_bounds__(NT, 3) k_mx_stage(Dims d, Tab t, Flags fl, con
     if (cell) {  // mass and pi
       const float rc = sR[o1];
       const float fx = sU[o1 + 1] * 0.5f * (rc + sR[o1 + 1]) - sU[o1] * 0.5f * (sR[o1 - 1] + rc);
-      const float fy = sV[o1 + W1] * 0.5f * (rc + sR[o1 + W1]) - sV[o1] * 0.5f * (sR[o1 - W1] + rc);
+      const float fy = sV[o1 + TW] * 0.5f * (rc + sR[o1 + TW]) - sV[o1] * 0.5f * (sR[o1 - TW] + rc);
       const float rkp = win.f[RHO][(size_t)kp1 * pl + colc];
       const float fz = wt * 0.5f * (rc + rkp) - wk * 0.5f * (rprev + rc);
       emit(RHO, -(fx * t.dx_inv + fy * t.dy_inv + fz * t.idzc[k]));
@@ -241,7 +351,7 @@ __global__ void __launch_bounds__(NT, 3) k_mx_stage(Dims d, Tab t, Flags fl, con
       if (fl.div_damp > 0.0) {
         const float pc = sP[o1];
         const float lap = (sP[o1 + 1] - 2.f * pc + sP[o1 - 1]) * (t.dx_inv * t.dx_inv) +
-                          (sP[o1 + W1] - 2.f * pc + sP[o1 - W1]) * (t.dy_inv * t.dy_inv);
+                          (sP[o1 + TW] - 2.f * pc + sP[o1 - TW]) * (t.dy_inv * t.dy_inv);
         r = -(float)fl.div_damp * lap;
       }
       emit(PI, r);
@@ -250,9 +360,9 @@ __global__ void __launch_bounds__(NT, 3) k_mx_stage(Dims d, Tab t, Flags fl, con
     const float idz = t.idza[k];
     const bool vert = (k + 2 < nz || k >= 2);
     const float* sh = t.t0d + 6 * k;  // theta0(clamp(k+m)) - theta0(k), m = -3..2
-    const float divh = (sU[o1 + 1] - sU[o1]) * t.dx_inv + (sV[o1 + W1] - sV[o1]) * t.dy_inv;
-    // one species: Q = its tile at level k; z0..z5 = its column at k-3..k+2
-    // (z3 unused: the tile holds it); fc = carried flux, updated
+    const float divh = (sU[o1 + 1] - sU[o1]) * t.dx_inv + (sV[o1 + TW] - sV[o1]) * t.dy_inv;
+    // one species: Q = its box at level k; z0..z5 = its column at k-3..k+2
+    // (z3 unused: the box holds it); fc = carried flux, updated
     auto scalar = [&](int q, const float* Q, float z0, float z1, float z2, float z4, float z5, float* fc,
                       float fc_shift) {
       float r = 0.f;
@@ -265,8 +375,8 @@ __global__ void __launch_bounds__(NT, 3) k_mx_stage(Dims d, Tab t, Flags fl, con
             const int fr = t_ / (TX + 1), ff = t_ - fr * (TX + 1);
             float F = 0.f;
             if (i0 + ff <= nx && j0 + fr < ny) {
-              const float* qq = Q + (fr + 3) * W3 + ff + 3;  // cell i0+ff, the face's right cell
-              F = weno_face_f(qq[-3], qq[-2], qq[-1], qq[0], qq[1], sU[(fr + 1) * W1 + ff + 1]);
+              const float* qq = Q + (fr + 3) * TW + ff + XO;  // cell i0+ff, the face's right cell
+              F = weno_face_f(qq[-3], qq[-2], qq[-1], qq[0], qq[1], sU[(fr + 1) * TW + ff + XO]);
             }
             sFx[t_] = F;
           }
@@ -274,8 +384,8 @@ __global__ void __launch_bounds__(NT, 3) k_mx_stage(Dims d, Tab t, Flags fl, con
             const int fg = t_ / TX, fcl = t_ - fg * TX;
             float G = 0.f;
             if (j0 + fg <= ny && i0 + fcl < nx) {
-              const float* qq = Q + (fg + 3) * W3 + fcl + 3;
-              G = weno_face_f(qq[-3 * W3], qq[-2 * W3], qq[-W3], qq[0], qq[W3], sV[(fg + 1) * W1 + fcl + 1]);
+              const float* qq = Q + (fg + 3) * TW + fcl + XO;
+              G = weno_face_f(qq[-3 * TW], qq[-2 * TW], qq[-TW], qq[0], qq[TW], sV[(fg + 1) * TW + fcl + XO]);
             }
             sFy[t_] = G;
           }
@@ -298,11 +408,11 @@ __global__ void __launch_bounds__(NT, 3) k_mx_stage(Dims d, Tab t, Flags fl, con
         }
         __syncthreads();  // sFx/sFy are reused by the next species
       } else if (cell) {
-        const float ua = 0.5f * (sU[o1] + sU[o1 + 1]), va = 0.5f * (sV[o1] + sV[o1 + W1]);
+        const float ua = 0.5f * (sU[o1] + sU[o1 + 1]), va = 0.5f * (sV[o1] + sV[o1 + TW]);
         const float wa = 0.5f * (wk + wt);
         const float* qq = Q + o3;
         const float gx = gradc(qq[-3], qq[-2], qq[-1], qq[1], qq[2], qq[3], t.dx_inv, fl.advection);
-        const float gy = gradc(qq[-3 * W3], qq[-2 * W3], qq[-W3], qq[W3], qq[2 * W3], qq[3 * W3], t.dy_inv, fl.advection);
+        const float gy = gradc(qq[-3 * TW], qq[-2 * TW], qq[-TW], qq[TW], qq[2 * TW], qq[3 * TW], t.dy_inv, fl.advection);
         r = -(ua * gx + va * gy + wa * (z4 - z2) * (0.5f * idz));
       }
       if (cell) {
@@ -319,15 +429,15 @@ __global__ void __launch_bounds__(NT, 3) k_mx_stage(Dims d, Tab t, Flags fl, con
     scalar(QV, sQ, wQ[0], wQ[1], wQ[2], wQ[4], wQ[5], &fcQ, 0.f);
     if (fl.moist) {
       for (int q = QC; q <= QG; ++q) {
-        __syncthreads();  // sQ is no longer read
-        load_tile<3>(sQ, win.f[q] + (size_t)k * pl, P, i0, j0, nx - 1, ny - 1);
+        __syncthreads();  // sQm is no longer read
+        load_box3(sQm, win.f[q] + (size_t)k * pl, P, i0, j0, nx - 1, ny - 1);
         __syncthreads();
         float z[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
         if (cell) {
 #pragma unroll
           for (int m = 0; m < 6; ++m) z[m] = win.f[q][(size_t)iclamp(k + m - 3, 0, nz - 1) * pl + colc];
         }
-        scalar(q, sQ, z[0], z[1], z[2], z[4], z[5], nullptr, 0.f);
+        scalar(q, sQm, z[0], z[1], z[2], z[4], z[5], nullptr, 0.f);
       }
     }
     // slide the column registers up one level
@@ -664,18 +774,79 @@ static int stage_kchunk(const Dims& d, bool fp64_out) {
   return best;
 }
 
-void mixed_stage(const Dims& d, const Tab& t, const Flags& fl, const WS& win, const WS& w0, const WS& wout,
-                 double* const* s0, double* const* ss, double dt_stage, bool write_fp64, unsigned* err,
-                 cudaStream_t stream) {
+// TMA descriptors of the stage kernel's boxes, one per (field, box shape),
+// cached for the life of the process (buffers live as long as their model;
+// the key includes the shape, so a reused address with other sizes gets its
+// own descriptor).
+namespace {
+PFN_cuTensorMapEncodeTiled_v12000 g_encode = nullptr;
+std::mutex g_map_mu;
+std::map<std::tuple<const void*, int, int, int, int, size_t, int>, CUtensorMap> g_maps;
+
+bool encode_fn() {
+  if (g_encode) return true;
+  void* fn = nullptr;
+  cudaDriverEntryPointQueryResult q{};
+  if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+      q != cudaDriverEntryPointSuccess || !fn)
+    return false;
+  g_encode = (PFN_cuTensorMapEncodeTiled_v12000)fn;
+  return true;
+}
+
+bool box_map(const float* base, int xext, int yext, int zext, int P, size_t plane, int rows, CUtensorMap* out) {
+  const auto key = std::make_tuple((const void*)base, xext, yext, zext, P, plane, rows);
+  std::lock_guard<std::mutex> lk(g_map_mu);
+  auto it = g_maps.find(key);
+  if (it != g_maps.end()) {
+    *out = it->second;
+    return true;
+  }
+  if (!encode_fn()) return false;
+  CUtensorMap m;
+  const cuuint64_t dims[3] = {(cuuint64_t)xext, (cuuint64_t)yext, (cuuint64_t)zext};
+  const cuuint64_t strides[2] = {(cuuint64_t)P * sizeof(float), (cuuint64_t)plane * sizeof(float)};
+  const cuuint32_t box[3] = {(cuuint32_t)TW, (cuuint32_t)rows, 1};
+  const cuuint32_t es[3] = {1, 1, 1};
+  if (g_encode(&m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, (void*)base, dims, strides, box, es,
+               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+    return false;
+  g_maps.emplace(key, m);
+  *out = m;
+  return true;
+}
+
+bool stage_maps(const Dims& d, const WS& win, StageMaps& M) {
+  struct Spec { int q, xe, ye, ze, rows; };
+  const Spec sp[NTILE] = {{THETA, d.nx, d.ny, d.nz, R3},     {QV, d.nx, d.ny, d.nz, R3},
+                          {U, d.nx + 1, d.ny, d.nz, R1},     {V, d.nx, d.ny + 1, d.nz, R1},
+                          {W, d.nx, d.ny, d.nz + 1, R1},     {PI, d.nx, d.ny, d.nz, R1},
+                          {RHO, d.nx + 1, d.ny + 1, d.nz, R1}};
+  for (int b = 0; b < NTILE; ++b) {
+    if (!box_map(win.f[sp[b].q], sp[b].xe, sp[b].ye, sp[b].ze, d.P, d.plane, sp[b].rows, &M.m[b])) return false;
+    M.xmax[b] = sp[b].xe - 1;
+    M.ymax[b] = sp[b].ye - 1;
+  }
+  return true;
+}
+}  // namespace
+
+int mixed_stage(const Dims& d, const Tab& t, const Flags& fl, const WS& win, const WS& w0, const WS& wout,
+                double* const* s0, double* const* ss, double dt_stage, bool write_fp64, unsigned* err,
+                cudaStream_t stream) {
+  StageMaps M;
+  if (!stage_maps(d, win, M)) return -1;
   const dim3 b(TX, TY);
   const int kchunk = stage_kchunk(d, write_fp64);
   const dim3 g((d.nx + TX) / TX, (d.ny + TY) / TY, (d.nz + kchunk - 1) / kchunk);
   if (write_fp64)
-    k_mx_stage<true><<<g, b, 0, stream>>>(d, t, fl, win, w0, wout, cs64(s0), ms64(ss), (float)dt_stage, dt_stage,
+    k_mx_stage<true><<<g, b, 0, stream>>>(d, t, fl, M, win, w0, wout, cs64(s0), ms64(ss), (float)dt_stage, dt_stage,
                                           kchunk, err);
   else
-    k_mx_stage<false><<<g, b, 0, stream>>>(d, t, fl, win, w0, wout, cs64(nullptr), ms64(nullptr), (float)dt_stage,
+    k_mx_stage<false><<<g, b, 0, stream>>>(d, t, fl, M, win, w0, wout, cs64(nullptr), ms64(nullptr), (float)dt_stage,
                                            dt_stage, kchunk, err);
+  return 0;
 }
 
 void mixed_fb_substep(const Dims& d, const Tab& t, const Flags& fl, const WS& win, const WS& wout, float dtau,
