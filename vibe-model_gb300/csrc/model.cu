@@ -599,18 +599,19 @@ int enqueue_one_step(vibe_gb300_model* m, double dt, int n_sub) {
         for (int n = 0; n < n_sub; ++n) {
           float** out = (n & 1) ? m->WB : m->WA;
           if (m->fl.acoustic_mode == 2) {
-            {
-              Span sp(m, 1);
-              mixed_hevi_column(d, m->tab, m->fl, ws_of(in), ws_of(out), dtau, m->d_lu + (size_t)stage * 3 * d.nz,
-                                m->stream);
-            }
-            Span sp(m, 3);
-            mixed_uv_backward(d, m->tab, ws_of(in), ws_of(out), dtau, m->stream);
+            // the u/v update of substep n-1 is applied inside substep n's column kernel
+            Span sp(m, 1);
+            mixed_hevi_column(d, m->tab, m->fl, ws_of(in), ws_of(out), dtau, m->d_lu + (size_t)stage * 3 * d.nz,
+                              n > 0, m->stream);
           } else {
             Span sp(m, 1);
             mixed_fb_substep(d, m->tab, m->fl, ws_of(in), ws_of(out), dtau, m->stream);
           }
           in = out;
+        }
+        if (m->fl.acoustic_mode == 2) {  // the last substep's u/v update, in place
+          Span sp(m, 3);
+          mixed_uv_backward(d, m->tab, ws_of(in), ws_of(in), dtau, m->stream);
         }
         final_sub = in;
       }
@@ -1177,7 +1178,8 @@ vibe_stream_t vibe_gb300_stream(vibe_gb300_model* m) { return m ? (vibe_stream_t
 int vibe_gb300_launches_per_step(const vibe_gb300_model* m, int n_sub) {
   if (!m) return 0;
   n_sub = n_sub > 1 ? n_sub : 1;
-  if (m->precision == VIBE_GB300_MIXED) return 3 * (1 + 2 * n_sub) + 1;
+  if (m->precision == VIBE_GB300_MIXED)
+    return (m->fl.acoustic_mode == 2) ? 3 * (1 + n_sub + 1) + 1 : 3 * (1 + 2 * n_sub) + 1;
   const int tend = 4 + ((m->fl.div_damp > 0.0 && m->fl.div_order > 2) ? 1 : 0);
   const int sub = (m->fl.acoustic_mode == 0) ? 2 : (m->fl.acoustic_mode == 1 ? 4 : 2);
   return 3 * (tend + NSPECIES + n_sub * sub + 1) + 1;

@@ -74,7 +74,7 @@ void mixed_fb_substep(const Dims& d, const Tab& t, const Flags& fl, const WS& wi
 void mixed_hevi_substep(const Dims& d, const Tab& t, const Flags& fl, const WS& win, const WS& wout, float dtau,
                         const float* lu /* 3*nz: a, cprime, inv_denom */, unsigned* err, cudaStream_t stream);
 void mixed_hevi_column(const Dims& d, const Tab& t, const Flags& fl, const WS& win, const WS& wout, float dtau,
-                       const float* lu, cudaStream_t stream);
+                       const float* lu, bool apply_uv, cudaStream_t stream);
 void mixed_uv_backward(const Dims& d, const Tab& t, const WS& win, const WS& wout, float dtau, cudaStream_t stream);
 void mixed_finish(const Dims& d, const Tab& t, const Flags& fl, const WS& wfin, const WS& wst, const WS& w0,
                   double* const* ss, double dt, int kmin, unsigned* err, cudaStream_t stream);

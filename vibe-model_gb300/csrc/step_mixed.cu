@@ -503,9 +503,17 @@ __global__ void k_mx_fb_mom(Dims d, Tab t, WS win, WS wout, float dtau, int do_w
 // 40 KB per block at nz = 80, so 5 blocks -- 20 warps -- fit an SM); the
 // backward sweep re-derives the explicit terms from the same inputs, which
 // the forward sweep has just pulled through L2.
+// apply_uv: the u/v backward update of the previous substep is applied here,
+// on the fly, from this substep's input pi' (the previous substep's result):
+// u(i) += dtau (-cp theta0(k) (pi'(ip) - pi'(im)) / dx) with the clamped
+// neighbours ip = min(i, nx-1), im = max(i-1, 0) (runge_kutta.cpp:65-75
+// backward half); the updated u, v enter this substep's divergence and are
+// written to the output. After the last substep of a stage one u/v kernel
+// applies the final update in place. cdx = -cp dtau / dx, cdy likewise.
 template <int kPF>
 __global__ void __launch_bounds__(128, 6) k_mx_hevi_col(Dims d, Tab t, Flags fl, WS win, WS wout, float dtau,
-                                                         const float* __restrict__ lu) {
+                                                         const float* __restrict__ lu, int apply_uv, float cdx,
+                                                         float cdy) {
   // per-level tables in shared memory; the forward sweep parks its per-level
   // results in the thread's own column of the output arrays (wt on the w
   // faces, dp on pi', the explicit source S on rho'), where the backward
@@ -521,6 +529,7 @@ __global__ void __launch_bounds__(128, 6) k_mx_hevi_col(Dims d, Tab t, Flags fl,
   float* s_lc = s_la + nz;                 // nz
   float* s_li = s_lc + nz;                 // nz
   float* s_r0 = s_li + nz;                 // nz
+  float* s_t0 = s_r0 + nz;                 // nz
   const int tid = threadIdx.y * blockDim.x + threadIdx.x;
   for (int e = tid; e <= nz; e += 128) {
     s_tfz[e] = t.tfz[e];
@@ -533,6 +542,7 @@ __global__ void __launch_bounds__(128, 6) k_mx_hevi_col(Dims d, Tab t, Flags fl,
       s_lc[e] = lu[nz + e];
       s_li[e] = lu[2 * nz + e];
       s_r0[e] = t.r0c[e];
+      s_t0[e] = t.t0c[e];
     }
   }
   __syncthreads();
@@ -551,11 +561,18 @@ __global__ void __launch_bounds__(128, 6) k_mx_hevi_col(Dims d, Tab t, Flags fl,
   float* __restrict__ Wo = wout.f[W] + col;
   float* __restrict__ Po = wout.f[PI] + col;
   float* __restrict__ Ro = wout.f[RHO] + col;
+  float* __restrict__ Uo = wout.f[U] + col;
+  float* __restrict__ Vo = wout.f[V] + col;
   const size_t vn = d.P;  // v(j+1) offset
   const float dxi = t.dx_inv, dyi = t.dy_inv;
+  // clamped neighbour offsets of pi' (0 where the clamp lands on the column)
+  const int ow = (i > 0) ? -1 : 0, oe = (i + 1 < d.nx) ? 1 : 0;
+  const long long os = (j > 0) ? -(long long)vn : 0, on = (j + 1 < d.ny) ? (long long)vn : 0;
+  const bool last_i = (i == d.nx - 1), last_j = (j == d.ny - 1);
   // Loads run kPF levels ahead of their use (register ring, static slots).
   // ---- forward sweep: wt, S and dp = (rhs - a dp(k-1)) / den per level
   float fw[kPF], fp[kPF], fu0[kPF], fu1[kPF], fv0[kPF], fv1[kPF];
+  float fpw[kPF], fpe[kPF], fps[kPF], fpn[kPF];
   auto loadF = [&](int L, int q) {
     const size_t o = (size_t)L * pl, o1 = o + pl;
     fw[q] = W0[o1];
@@ -564,6 +581,12 @@ __global__ void __launch_bounds__(128, 6) k_mx_hevi_col(Dims d, Tab t, Flags fl,
     fu1[q] = U0[o + 1];
     fv0[q] = V0[o];
     fv1[q] = V0[o + vn];
+    if (apply_uv) {
+      fpw[q] = P0[o + ow];
+      fpe[q] = P0[o + oe];
+      fps[q] = P0[o + os];
+      fpn[q] = P0[o + on];
+    }
   };
 #pragma unroll
   for (int q = 0; q < kPF; ++q)
@@ -584,8 +607,23 @@ __global__ void __launch_bounds__(128, 6) k_mx_hevi_col(Dims d, Tab t, Flags fl,
           p_k1 = fp[q];
           wt_k1 = w_k1 - dtau * ob * cpf * s_tfz[k + 1] * (p_k1 - p_k) * s_idzw[k + 1];
         }
-        const float Dh = -(s_r0[k] * ((fu1[q] - fu0[q]) * dxi + (fv1[q] - fv0[q]) * dyi));
+        float u0 = fu0[q], u1 = fu1[q], v0 = fv0[q], v1 = fv1[q];
+        if (apply_uv) {
+          const float tx_ = s_t0[k] * cdx, ty_ = s_t0[k] * cdy;
+          u0 += tx_ * (p_k - fpw[q]);
+          u1 += tx_ * (fpe[q] - p_k);
+          v0 += ty_ * (p_k - fps[q]);
+          v1 += ty_ * (fpn[q] - p_k);
+        }
+        const float Dh = -(s_r0[k] * ((u1 - u0) * dxi + (v1 - v0) * dyi));
         if (k + kPF < nz) loadF(k + kPF, q);
+        {
+          const size_t o = (size_t)k * pl;
+          Uo[o] = u0;
+          Vo[o] = v0;
+          if (last_i) Uo[o + 1] = u1;  // face nx (zero clamped gradient)
+          if (last_j) Vo[o + vn] = v1;
+        }
         const float rk = s_rfz[k], rk1 = s_rfz[k + 1], idz = s_idzc[k];
         const float dv_old = -(rk1 * w_k1 - rk * w_k) * idz;
         const float dv_t = -(rk1 * wt_k1 - rk * wt_k) * idz;
@@ -871,15 +909,17 @@ static int hevi_pf() {
 }
 
 void mixed_hevi_column(const Dims& d, const Tab& t, const Flags& fl, const WS& win, const WS& wout, float dtau,
-                       const float* lu, cudaStream_t stream) {
+                       const float* lu, bool apply_uv, cudaStream_t stream) {
   const dim3 bc(32, 4);
-  const size_t smem = 9 * (size_t)(d.nz + 1) * sizeof(float);
+  const size_t smem = 10 * (size_t)(d.nz + 1) * sizeof(float);
   const dim3 g((d.nx + bc.x - 1) / bc.x, (d.ny + bc.y - 1) / bc.y);
+  const float cdx = -(float)kCp * dtau * t.dx_inv, cdy = -(float)kCp * dtau * t.dy_inv;
+  const int au = apply_uv ? 1 : 0;
   switch (hevi_pf()) {
-    case 6: k_mx_hevi_col<6><<<g, bc, smem, stream>>>(d, t, fl, win, wout, dtau, lu); break;
-    case 8: k_mx_hevi_col<8><<<g, bc, smem, stream>>>(d, t, fl, win, wout, dtau, lu); break;
-    case 4: k_mx_hevi_col<4><<<g, bc, smem, stream>>>(d, t, fl, win, wout, dtau, lu); break;
-    default: k_mx_hevi_col<2><<<g, bc, smem, stream>>>(d, t, fl, win, wout, dtau, lu); break;
+    case 6: k_mx_hevi_col<6><<<g, bc, smem, stream>>>(d, t, fl, win, wout, dtau, lu, au, cdx, cdy); break;
+    case 8: k_mx_hevi_col<8><<<g, bc, smem, stream>>>(d, t, fl, win, wout, dtau, lu, au, cdx, cdy); break;
+    case 4: k_mx_hevi_col<4><<<g, bc, smem, stream>>>(d, t, fl, win, wout, dtau, lu, au, cdx, cdy); break;
+    default: k_mx_hevi_col<2><<<g, bc, smem, stream>>>(d, t, fl, win, wout, dtau, lu, au, cdx, cdy); break;
   }
 }
 
@@ -891,8 +931,8 @@ void mixed_uv_backward(const Dims& d, const Tab& t, const WS& win, const WS& wou
 void mixed_hevi_substep(const Dims& d, const Tab& t, const Flags& fl, const WS& win, const WS& wout, float dtau,
                         const float* lu, unsigned* err, cudaStream_t stream) {
   (void)err;
-  mixed_hevi_column(d, t, fl, win, wout, dtau, lu, stream);
-  mixed_uv_backward(d, t, win, wout, dtau, stream);
+  mixed_hevi_column(d, t, fl, win, wout, dtau, lu, false, stream);
+  mixed_uv_backward(d, t, wout, wout, dtau, stream);  // in place: u, v were copied by the column kernel
 }
 
 void mixed_finish(const Dims& d, const Tab& t, const Flags& fl, const WS& wfin, const WS& wst, const WS& w0,
