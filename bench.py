@@ -392,7 +392,11 @@ def main():
 
     # roofline of the dominant kernel class (live CUDA-event times)
     peak, peak_kind = measured_peak()
-    per_cell = {0: (56.0 + 84.0 + 196.0) / 3.0, 1: 32.0, 2: 156.0, 3: 20.0}
+    # algorithmic bytes per cell of one launch of each kernel class (FP32 fields 4 B, FP64 8 B):
+    # stage: 56 (stage 1: win = w0), 84 (stage 2), 112 (stage 3, + its tendency);
+    # column: read u v w rho pi, write w rho pi u v; finish: read S0, R3, 5 substep
+    # fields, 7 stage fields, write S1, W0; u/v in place: read u v pi, write u v
+    per_cell = {0: (56.0 + 84.0 + 112.0) / 3.0, 1: 40.0, 2: 216.0, 3: 20.0}
     names = {0: "k_mx_stage", 1: "k_mx_hevi_col", 2: "k_mx_finish", 3: "k_mx_fb_mom(u,v)"}
     dom = max(ktimes, key=lambda c: ktimes[c][0])
     tot_ms, spans = ktimes[dom]

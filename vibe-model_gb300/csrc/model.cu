@@ -81,6 +81,7 @@ struct vibe_gb300_model {
   float* WSt[2][NSPECIES] = {};
   float* WA[NSPECIES] = {};
   float* WB[NSPECIES] = {};
+  float* WR[NSPECIES] = {};       // last stage's FP32 tendency
   float* d_ftab = nullptr;        // FP32 tables
   double* d_dtab = nullptr;       // FP64 tables
   float* d_lu = nullptr;          // 3 stages x 3*nz
@@ -590,8 +591,9 @@ int enqueue_one_step(vibe_gb300_model* m, double dt, int n_sub) {
         const WS win = (stage == 0) ? w0 : ws_compose(final_sub, m->WSt[(stage - 1) & 1]);
         {
           Span sp(m, 0);
-          if (mixed_stage(d, m->tab, m->fl, win, w0, ws_of(st_out), S0, S1, dts[stage], stage == 2, m->d_err,
-                          m->stream))
+          const WS wr = ws_of(m->WR);
+          if (mixed_stage(d, m->tab, m->fl, win, w0, ws_of(st_out), stage == 2 ? &wr : nullptr, dts[stage],
+                          m->d_err, m->stream))
             return fail(VIBE_GB300_EDEVICE, "TMA descriptor creation failed (cuTensorMapEncodeTiled)");
         }
         const float dtau = (float)(dts[stage] / (double)n_sub);
@@ -616,7 +618,8 @@ int enqueue_one_step(vibe_gb300_model* m, double dt, int n_sub) {
         final_sub = in;
       }
       Span sp(m, 2);
-      mixed_finish(d, m->tab, m->fl, ws_of(final_sub), ws_of(m->WSt[0]), w0, S1, dt, m->kmin, m->d_err, m->stream);
+      const WS wr = ws_of(m->WR);
+      mixed_finish(d, m->tab, m->fl, ws_of(final_sub), ws_of(m->WSt[0]), w0, &wr, dt, S0, S1, m->d_err, m->stream);
     }
     m->cur = 1 - m->cur;
   }
@@ -798,6 +801,7 @@ int vibe_gb300_model_create(const vibe_gb300_setup* s, int precision, vibe_gb300
       for (int q = 0; q < NSPECIES && !rc; ++q) rc = dalloc(m, &m->WSt[b][q], nfield);
     for (int q = 0; q < NSPECIES && !rc; ++q) rc = acoustic_field(q) ? dalloc(m, &m->WA[q], nfield) : 0;
     for (int q = 0; q < NSPECIES && !rc; ++q) rc = acoustic_field(q) ? dalloc(m, &m->WB[q], nfield) : 0;
+    for (int q = 0; q < NSPECIES && !rc; ++q) rc = dalloc(m, &m->WR[q], nfield);
     rc = rc ? rc : dalloc(m, &m->d_lu, 9 * (size_t)nz);
   }
   if (rc) return bail(rc);
@@ -929,8 +933,7 @@ int vibe_gb300_slow_tendency(vibe_gb300_model* m, double* const* host_out) {
     if (int rc = sync_working(m)) return rc;
     WS none;
     for (int q = 0; q < NSPECIES; ++q) none.f[q] = nullptr;
-    if (mixed_stage(m->d, m->tab, m->fl, ws_of(m->W0), none, ws_of(m->WSt[1]), nullptr, nullptr, 1.0, false,
-                    m->d_err, m->stream))
+    if (mixed_stage(m->d, m->tab, m->fl, ws_of(m->W0), none, ws_of(m->WSt[1]), nullptr, 1.0, m->d_err, m->stream))
       return fail(VIBE_GB300_EDEVICE, "TMA descriptor creation failed (cuTensorMapEncodeTiled)");
     for (int q = 0; q < NSPECIES; ++q) {
       int ni = m->d.nx + (q == U), nj = m->d.ny + (q == V), nk = m->d.nz + (q == W);
@@ -973,8 +976,8 @@ int vibe_gb300_acoustic_substep(vibe_gb300_model* m, double dtau) {
     mixed_fb_substep(m->d, m->tab, m->fl, ws_of(m->W0), ws_of(m->WA), (float)dtau, m->stream);
     Tab id = m->tab;
     id.spwd = m->d_spid; id.spdt = m->d_spid + (m->d.nz + 1); id.spw = m->d_spif;
-    mixed_finish(m->d, id, m->fl, ws_compose(m->WA, m->W0), ws_of(m->W0), ws_of(m->WSt[1]), m->S[m->cur], 0.0, 0,
-                 m->d_err, m->stream);
+    mixed_finish(m->d, id, m->fl, ws_compose(m->WA, m->W0), ws_of(m->W0), ws_of(m->WSt[1]), nullptr, 0.0,
+                 m->S[m->cur], m->S[m->cur], m->d_err, m->stream);
   }
   CUDA_OK(cudaGetLastError());
   return read_status(m);
@@ -1000,8 +1003,8 @@ int vibe_gb300_hevi_substep(vibe_gb300_model* m, double dtau) {
     mixed_hevi_substep(m->d, m->tab, m->fl, ws_of(m->W0), ws_of(m->WA), (float)dtau, m->d_lu, m->d_err, m->stream);
     Tab id = m->tab;
     id.spwd = m->d_spid; id.spdt = m->d_spid + (m->d.nz + 1); id.spw = m->d_spif;
-    mixed_finish(m->d, id, m->fl, ws_compose(m->WA, m->W0), ws_of(m->W0), ws_of(m->WSt[1]), m->S[m->cur], 0.0, 0,
-                 m->d_err, m->stream);
+    mixed_finish(m->d, id, m->fl, ws_compose(m->WA, m->W0), ws_of(m->W0), ws_of(m->WSt[1]), nullptr, 0.0,
+                 m->S[m->cur], m->S[m->cur], m->d_err, m->stream);
     m->cfg_dt = -1.0;
   }
   CUDA_OK(cudaGetLastError());

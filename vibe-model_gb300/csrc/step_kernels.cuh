@@ -66,9 +66,9 @@ struct WS {          // FP32 working state (perturbation form)
   float* f[NSPECIES]; // u v w rho' theta' pi' qv qc..qg
 };
 
+// rout: when given, the tendency R is also written there (FP32)
 int mixed_stage(const Dims& d, const Tab& t, const Flags& fl, const WS& win, const WS& w0, const WS& wout,
-                 double* const* s0, double* const* ss, double dt_stage, bool write_fp64, unsigned* err,
-                 cudaStream_t stream);
+                const WS* rout, double dt_stage, unsigned* err, cudaStream_t stream);
 void mixed_fb_substep(const Dims& d, const Tab& t, const Flags& fl, const WS& win, const WS& wout, float dtau,
                       cudaStream_t stream);
 void mixed_hevi_substep(const Dims& d, const Tab& t, const Flags& fl, const WS& win, const WS& wout, float dtau,
@@ -77,7 +77,8 @@ void mixed_hevi_column(const Dims& d, const Tab& t, const Flags& fl, const WS& w
                        const float* lu, bool apply_uv, cudaStream_t stream);
 void mixed_uv_backward(const Dims& d, const Tab& t, const WS& win, const WS& wout, float dtau, cudaStream_t stream);
 void mixed_finish(const Dims& d, const Tab& t, const Flags& fl, const WS& wfin, const WS& wst, const WS& w0,
-                  double* const* ss, double dt, int kmin, unsigned* err, cudaStream_t stream);
+                  const WS* rin, double dt, double* const* s0, double* const* s1, unsigned* err,
+                  cudaStream_t stream);
 void mixed_unpack_f32(const Dims& d, int nsx, int nsy, int nsz, int ni, int nj, int nk, const float* src, double* dst,
                       cudaStream_t stream);
 void mixed_to_working(const Dims& d, const Tab& t, double* const* s, const WS& w, cudaStream_t stream);

@@ -197,12 +197,13 @@ __device__ void fix_box(float* t, int rows, int halo, int i0, int j0, int xmax, 
     }
 }
 
-template <bool kFP64Out>
+// kRaw: also write the tendency R itself (the last stage: the finish kernel
+// forms the FP64 state from it)
+template <bool kRaw>
 __global__ void __launch_bounds__(NT, 3) k_mx_stage(Dims d, Tab t, Flags fl, const __grid_constant__ StageMaps M,
                                                     const __grid_constant__ WS win, const __grid_constant__ WS w0,
-                                                    const __grid_constant__ WS wout, const __grid_constant__ CS64 s0,
-                                                    const __grid_constant__ MS64 ss, float dts, double dtd,
-                                                    int kchunk, unsigned* err) {
+                                                    const __grid_constant__ WS wout, const __grid_constant__ WS rout,
+                                                    float dts, int kchunk, unsigned* err) {
   __shared__ __align__(128) float sbuf[2][kBuf];
   __shared__ __align__(128) float sQm[R3 * TW];  // moisture species beyond qv (plain loads)
   __shared__ float sFx[TY * (TX + 1)], sFy[(TY + 1) * TX];
@@ -284,7 +285,7 @@ __global__ void __launch_bounds__(NT, 3) k_mx_stage(Dims d, Tab t, Flags fl, con
       const float o = (w0.f[q] != nullptr) ? w0.f[q][c] + dts * r : r;  // no base: raw tendency
       wout.f[q][c] = o;
       bad |= !isfinite(o);
-      if (kFP64Out) ss.f[q][c] = s0.f[q][c] + dtd * (double)r;
+      if (kRaw) rout.f[q][c] = r;
     };
     if (cells_here && in_box && j < ny) {  // u face (i, j, k)
       const float ump = sU[o1 + ipu], umm = sU[o1 + dim];
@@ -684,8 +685,15 @@ __global__ void __launch_bounds__(128, 6) k_mx_hevi_col(Dims d, Tab t, Flags fl,
 // ---- finish: fold the last stage's acoustic increments into the FP64
 // state, apply the sponge (damping.cpp:76-140) in FP64 and to the FP32
 // working copy, which becomes the next step's s0 working copy.
+// S1 = sponge(S0 + (double)(dt R3 + (W_final - W_stage3))) for the acoustic
+// fields, S0 + (double)(dt R3) for theta and q (sponge on theta): the stage-3
+// tendency and the acoustic increment of its substeps are summed in FP32 and
+// added to the FP64 state with one conversion and one FP64 add per field.
+// rin == nullptr: no tendency (single-substep entry points, S1 == S0).
+// Also writes the next step's FP32 working copy W0.
 __global__ void k_mx_finish(Dims d, Tab t, Flags fl, const __grid_constant__ WS wfin, const __grid_constant__ WS wst,
-                            const __grid_constant__ WS w0, const __grid_constant__ MS64 ss, unsigned* err) {
+                            const __grid_constant__ WS w0, const __grid_constant__ WS rin, float dtf,
+                            const __grid_constant__ CS64 s0, const __grid_constant__ MS64 s1, unsigned* err) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
   const int k = blockIdx.z;
@@ -695,10 +703,12 @@ __global__ void k_mx_finish(Dims d, Tab t, Flags fl, const __grid_constant__ WS 
   const double wd = t.spwd[k];
   const float wf = t.spw[k];
   bool bad = false;
+  auto incr = [&](int q) { return rin.f[q] ? dtf * rin.f[q][c] : 0.f; };
   auto face = [&](int q) {
-    const double v = wd * (ss.f[q][c] + (double)(wfin.f[q][c] - wst.f[q][c]));
-    ss.f[q][c] = v;
-    w0.f[q][c] = wf * wfin.f[q][c];
+    const float wv = wfin.f[q][c];
+    const double v = wd * (s0.f[q][c] + (double)(incr(q) + (wv - wst.f[q][c])));
+    s1.f[q][c] = v;
+    w0.f[q][c] = wf * wv;
     bad |= !isfinite(v);
   };
   if (j < d.ny && k < d.nz) face(U);
@@ -707,24 +717,32 @@ __global__ void k_mx_finish(Dims d, Tab t, Flags fl, const __grid_constant__ WS 
   if (i < d.nx && j < d.ny && k < d.nz) {
     const double sdt = t.spdt[k];
     {
-      const double v = wd * ((ss.f[RHO][c] + (double)(wfin.f[RHO][c] - wst.f[RHO][c])) + sdt * t.r0d[kc]);
-      ss.f[RHO][c] = v;
-      w0.f[RHO][c] = wf * wfin.f[RHO][c];
+      const float wv = wfin.f[RHO][c];
+      const double v = wd * ((s0.f[RHO][c] + (double)(incr(RHO) + (wv - wst.f[RHO][c]))) + sdt * t.r0d[kc]);
+      s1.f[RHO][c] = v;
+      w0.f[RHO][c] = wf * wv;
       bad |= !isfinite(v);
     }
     {
-      const double v = wd * ((ss.f[PI][c] + (double)(wfin.f[PI][c] - wst.f[PI][c])) + sdt * t.p0d[kc]);
-      ss.f[PI][c] = v;
-      w0.f[PI][c] = wf * wfin.f[PI][c];
+      const float wv = wfin.f[PI][c];
+      const double v = wd * ((s0.f[PI][c] + (double)(incr(PI) + (wv - wst.f[PI][c]))) + sdt * t.p0d[kc]);
+      s1.f[PI][c] = v;
+      w0.f[PI][c] = wf * wv;
       bad |= !isfinite(v);
     }
-    if (wd != 1.0) ss.f[THETA][c] = wd * (ss.f[THETA][c] + sdt * t.t0dd[kc]);
-    w0.f[THETA][c] = wf * wst.f[THETA][c];
-    bad |= !isfinite(ss.f[THETA][c]);
+    {
+      double v = s0.f[THETA][c] + (double)incr(THETA);
+      if (wd != 1.0) v = wd * (v + sdt * t.t0dd[kc]);
+      s1.f[THETA][c] = v;
+      w0.f[THETA][c] = wf * wst.f[THETA][c];
+      bad |= !isfinite(v);
+    }
     const int last = fl.moist ? QG : QV;
     for (int q = QV; q <= last; ++q) {
+      const double v = s0.f[q][c] + (double)incr(q);
+      s1.f[q][c] = v;
       w0.f[q][c] = wst.f[q][c];
-      bad |= !isfinite(ss.f[q][c]);
+      bad |= !isfinite(v);
     }
   }
   if (bad) atomicOr(err, (unsigned)kErrNonFinite);
@@ -871,19 +889,17 @@ bool stage_maps(const Dims& d, const WS& win, StageMaps& M) {
 }  // namespace
 
 int mixed_stage(const Dims& d, const Tab& t, const Flags& fl, const WS& win, const WS& w0, const WS& wout,
-                double* const* s0, double* const* ss, double dt_stage, bool write_fp64, unsigned* err,
-                cudaStream_t stream) {
+                const WS* rout, double dt_stage, unsigned* err, cudaStream_t stream) {
   StageMaps M;
   if (!stage_maps(d, win, M)) return -1;
   const dim3 b(TX, TY);
-  const int kchunk = stage_kchunk(d, write_fp64);
+  const bool raw = rout != nullptr;
+  const int kchunk = stage_kchunk(d, raw);
   const dim3 g((d.nx + TX) / TX, (d.ny + TY) / TY, (d.nz + kchunk - 1) / kchunk);
-  if (write_fp64)
-    k_mx_stage<true><<<g, b, 0, stream>>>(d, t, fl, M, win, w0, wout, cs64(s0), ms64(ss), (float)dt_stage, dt_stage,
-                                          kchunk, err);
+  if (raw)
+    k_mx_stage<true><<<g, b, 0, stream>>>(d, t, fl, M, win, w0, wout, *rout, (float)dt_stage, kchunk, err);
   else
-    k_mx_stage<false><<<g, b, 0, stream>>>(d, t, fl, M, win, w0, wout, cs64(nullptr), ms64(nullptr), (float)dt_stage,
-                                           dt_stage, kchunk, err);
+    k_mx_stage<false><<<g, b, 0, stream>>>(d, t, fl, M, win, w0, wout, wout, (float)dt_stage, kchunk, err);
   return 0;
 }
 
@@ -936,10 +952,13 @@ void mixed_hevi_substep(const Dims& d, const Tab& t, const Flags& fl, const WS& 
 }
 
 void mixed_finish(const Dims& d, const Tab& t, const Flags& fl, const WS& wfin, const WS& wst, const WS& w0,
-                  double* const* ss, double dt, int kmin, unsigned* err, cudaStream_t stream) {
-  (void)dt; (void)kmin;
+                  const WS* rin, double dt, double* const* s0, double* const* s1, unsigned* err,
+                  cudaStream_t stream) {
   const dim3 b(32, 4);
-  k_mx_finish<<<g3(d.nx + 1, d.ny + 1, d.nz + 1, b), b, 0, stream>>>(d, t, fl, wfin, wst, w0, ms64(ss), err);
+  WS none;
+  for (int q = 0; q < NSPECIES; ++q) none.f[q] = nullptr;
+  k_mx_finish<<<g3(d.nx + 1, d.ny + 1, d.nz + 1, b), b, 0, stream>>>(d, t, fl, wfin, wst, w0, rin ? *rin : none,
+                                                                     (float)dt, cs64(s0), ms64(s1), err);
 }
 
 void mixed_unpack_f32(const Dims& d, int nsx, int nsy, int nsz, int ni, int nj, int nk, const float* src, double* dst,
