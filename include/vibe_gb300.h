@@ -126,6 +126,16 @@ int vibe_gb300_step(vibe_gb300_model *m, double dt, int n_sub, int n_steps);
 int vibe_gb300_step_async(vibe_gb300_model *m, double dt, int n_sub, int n_steps);
 int vibe_gb300_sync(vibe_gb300_model *m);
 
+/* Time-step diagnostics of the current state (FP64, exact maxima):
+ * adv_cfl = Advection::cfl_number(s, dt) (advection.cpp:325-340),
+ * max_sound_speed = Equations::max_sound_speed(s) (equations.cpp:238-249),
+ * acoustic_cfl = AcousticSubstepper::acoustic_cfl(s, dtau)
+ * (acoustic_substep.cpp:151-168). Outputs nullable. */
+int vibe_gb300_cfl(vibe_gb300_model *m, double dt, double dtau, double *adv_cfl, double *max_sound_speed,
+                   double *acoustic_cfl);
+/* RungeKutta3Integrator::max_stable_dt (runge_kutta.cpp:121-140). */
+int vibe_gb300_max_stable_dt(vibe_gb300_model *m, double *dt_out);
+
 /* Mixed path: replay each step as a CUDA graph (default on; the first step
  * after a dt/n_sub change runs eagerly, the next ones capture and replay;
  * off while kernel timing is on). */

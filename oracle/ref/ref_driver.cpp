@@ -546,4 +546,37 @@ void vref_ad_propagate(vref_model* m, const double* const* xb, const double* con
   store_state(sout, out);
 }
 
+
+void vref_cfl(vref_model* m, double dt, double dtau, double* adv_cfl, double* max_sound_speed,
+              double* acoustic_cfl) {
+  const dyn::State& s = *m->state;
+  if (adv_cfl) *adv_cfl = m->eq->advection().cfl_number(s, dt);
+  if (max_sound_speed) *max_sound_speed = m->eq->max_sound_speed(s);
+  if (acoustic_cfl) {
+    timeint::AcousticOptions opt;
+    timeint::AcousticSubstepper sub(*m->grid, opt);
+    *acoustic_cfl = sub.acoustic_cfl(s, dtau);
+  }
+}
+
+// RungeKutta3Integrator::max_stable_dt (runge_kutta.cpp:121-140) restated: the
+// translation unit does not compile (see vref_rk3_step)
+double vref_max_stable_dt(vref_model* m) {
+  const grid::Grid& g = *m->grid;
+  const dyn::State& s = *m->state;
+  const Real adv_cfl = m->eq->advection().cfl_number(s, Real(1));
+  const Real cs = m->eq->max_sound_speed(s);
+  Real acoustic_rate = Real(0);
+  for (Int k = 0; k < g.nz(); ++k)
+    for (Int j = 0; j < g.ny(); ++j)
+      for (Int i = 0; i < g.nx(); ++i) {
+        const Real scale = g.geom().z_top - g.terrain(i, j);
+        const Real dz = std::max(g.dzeta(k) * scale, Real(1));
+        acoustic_rate = std::max(acoustic_rate, cs * (Real(1) / g.dx_at(i) + Real(1) / g.dy_at(j) + Real(1) / dz));
+      }
+  const Real dt_adv = (adv_cfl > Real(0)) ? Real(0.8) / adv_cfl : Real(1e9);
+  const Real dt_ac = (acoustic_rate > Real(0)) ? Real(2) / acoustic_rate : Real(1e9);
+  return std::min(dt_adv, dt_ac);
+}
+
 }  // extern "C"

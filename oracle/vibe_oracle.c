@@ -1751,6 +1751,53 @@ void vo_ad_step(const vo_model *m, const double *const *xb, const double *const 
 }
 
 /* ------------------------------------------------------------------------ */
+/* Time-step diagnostics                                                     */
+/* ------------------------------------------------------------------------ */
+void vo_cfl(const vo_model *m, double dt, double dtau, double *adv_cfl, double *max_sound_speed,
+            double *acoustic_cfl) {
+  const fld *u = &m->st[VO_U], *v = &m->st[VO_V], *w = &m->st[VO_W], *th = &m->st[VO_THETA], *pi = &m->st[VO_PI];
+  double worst = 0.0, best = 0.0, ac = 0.0;
+  for (int k = 0; k < m->nz; ++k)
+    for (int j = 0; j < m->ny; ++j)
+      for (int i = 0; i < m->nx; ++i) {
+        const double dx = m->s.dx, dy = m->s.dy;
+        const double scale = m->s.z_top - g_terrain(m, i, j);
+        const double dz = dmax(g_dzeta(m, k) * scale, 1.0);
+        const double uu = 0.5 * (AT(*u, i, j, k) + AT(*u, i + 1, j, k));
+        const double vv = 0.5 * (AT(*v, i, j, k) + AT(*v, i, j + 1, k));
+        const double ww = 0.5 * (AT(*w, i, j, k) + AT(*w, i, j, k + 1));
+        /* cfl_number, advection.cpp:325-340 */
+        worst = dmax(worst, dt * (fabs(uu) / dx + fabs(vv) / dy + fabs(ww) / dz));
+        /* max_sound_speed, equations.cpp:238-249 */
+        const double t = AT(*th, i, j, k) * AT(*pi, i, j, k);
+        const double cs = sqrt((K_CP / K_CV) * K_RD * dmax(t, 1.0));
+        best = dmax(best, cs);
+        /* acoustic_cfl, acoustic_substep.cpp:151-168 */
+        ac = dmax(ac, dtau * ((cs + fabs(uu)) / dx + (cs + fabs(vv)) / dy + (cs + fabs(ww)) / dz));
+      }
+  if (adv_cfl) *adv_cfl = worst;
+  if (max_sound_speed) *max_sound_speed = best;
+  if (acoustic_cfl) *acoustic_cfl = ac;
+}
+
+/* RungeKutta3Integrator::max_stable_dt, runge_kutta.cpp:121-140 */
+double vo_max_stable_dt(const vo_model *m) {
+  double adv = 0.0, cs = 0.0;
+  vo_cfl(m, 1.0, 1.0, &adv, &cs, NULL);
+  double rate = 0.0;
+  for (int k = 0; k < m->nz; ++k)
+    for (int j = 0; j < m->ny; ++j)
+      for (int i = 0; i < m->nx; ++i) {
+        const double scale = m->s.z_top - g_terrain(m, i, j);
+        const double dz = dmax(g_dzeta(m, k) * scale, 1.0);
+        rate = dmax(rate, cs * (1.0 / m->s.dx + 1.0 / m->s.dy + 1.0 / dz));
+      }
+  const double dt_adv = (adv > 0.0) ? 0.8 / adv : 1e9;
+  const double dt_ac = (rate > 0.0) ? 2.0 / rate : 1e9;
+  return dmin(dt_adv, dt_ac);
+}
+
+/* ------------------------------------------------------------------------ */
 /* Nest transfers: src/grid/nest.cpp:34-124                                  */
 /* ------------------------------------------------------------------------ */
 static fld fld_of(int nx, int ny, int nz, int stagger, const double *p) {

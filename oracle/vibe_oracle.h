@@ -167,6 +167,14 @@ void vo_tl_step(const vo_model *m, const double *const *xb, const double *const 
 void vo_ad_step(const vo_model *m, const double *const *xb, const double *const *bar_out, double dt,
                 double *const *bar_in);
 
+/* Time-step diagnostics: Advection::cfl_number (advection.cpp:325-340),
+ * Equations::max_sound_speed (equations.cpp:238-249), AcousticSubstepper::
+ * acoustic_cfl (acoustic_substep.cpp:151-168) and RungeKutta3Integrator::
+ * max_stable_dt (runge_kutta.cpp:121-140). */
+void vo_cfl(const vo_model *m, double dt, double dtau, double *adv_cfl, double *max_sound_speed,
+            double *acoustic_cfl);
+double vo_max_stable_dt(const vo_model *m);
+
 /* C-ABI kernels restated (src/common/c_kernels.c). vo_tridiagonal_solve
  * follows the documented contract (c_kernels.h:38-55) with the textbook
  * recurrence of thomas_solve (helmholtz.cpp:57-86): the shipped
@@ -222,6 +230,9 @@ void vref_tl_propagate(vref_model *m, const double *const *xb, const double *con
                        double *const *out);
 void vref_ad_propagate(vref_model *m, const double *const *xb, const double *const *dy, double dt, int n_steps,
                        double *const *out);
+void vref_cfl(vref_model *m, double dt, double dtau, double *adv_cfl, double *max_sound_speed,
+              double *acoustic_cfl);
+double vref_max_stable_dt(vref_model *m);
 void vref_davies_profile(int n_zone, double alpha_max, double *out);
 void vref_nest_interpolate_from_parent(const vo_nest_placement *p, int nvars, const int *stagger, int pnx, int pny,
                                        int pnz, const double *const *parent, int cnx, int cny, int cnz,

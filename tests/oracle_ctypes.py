@@ -418,3 +418,22 @@ def ad_propagate(model, xb, dy, dt, n):
     for _ in range(n):
         cur = ad_step(model, xb, cur, dt)
     return cur
+
+
+def cfl(model, dt, dtau):
+    """(cfl_number, max_sound_speed, acoustic_cfl) of the model's state."""
+    lib = _load(model.kind)[0]
+    f = getattr(lib, ("vo_" if model.kind == "port" else "vref_") + "cfl")
+    f.restype = None
+    f.argtypes = [ctypes.c_void_p, _D, _D, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
+    out = [ctypes.c_double() for _ in range(3)]
+    f(model.h, dt, dtau, *[ctypes.byref(o) for o in out])
+    return tuple(o.value for o in out)
+
+
+def max_stable_dt(model):
+    lib = _load(model.kind)[0]
+    f = getattr(lib, ("vo_" if model.kind == "port" else "vref_") + "max_stable_dt")
+    f.restype = _D
+    f.argtypes = [ctypes.c_void_p]
+    return f(model.h)

@@ -335,3 +335,15 @@ def test_mixed_graph_replay_is_bitwise_identical(vg):
         b.step(1.0, 4, 3)
         for sp in range(7):
             assert np.array_equal(a.get(sp), b.get(sp)), vg.SPECIES[sp]
+
+
+@pytest.mark.parametrize("prec", ["FP64", "MIXED"])
+def test_cfl_diagnostics_bit_exact(vg, oc, prec):
+    """cfl_number / max_sound_speed / acoustic_cfl / max_stable_dt of the
+    device state equal the oracle's serial loops bit for bit (maxima)."""
+    s = small_setup(vg, **STEP_CASES[0]) if prec == "FP64" else small_setup(vg)
+    with vg.Model(s, getattr(vg, prec)) as m:
+        o = oc.Model(oracle_setup(oc, s), "port")
+        o.set_state(m.state())  # same state on both sides
+        assert m.cfl(2.0, 0.3) == oc.cfl(o, 2.0, 0.3)
+        assert m.max_stable_dt() == oc.max_stable_dt(o)

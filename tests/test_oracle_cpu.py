@@ -260,3 +260,13 @@ def test_tlad_port_dot_product(oc):
     lhs = tc.dot(oc, s, oc.tl_propagate(p, xb, dx, 15.0, 2), dy)
     rhs = tc.dot(oc, s, dx, oc.ad_propagate(p, xb, dy, 15.0, 2))
     assert abs(lhs - rhs) <= 1e-12 * max(abs(lhs), abs(rhs))
+
+
+@need_ref
+@pytest.mark.parametrize("case", [0, 3])
+def test_cfl_diagnostics_port_is_bit_exact_to_reference(oc, case):
+    s = small(oc, **REF_CASES[case])
+    p, r = oc.Model(s, "port"), oc.Model(s, "ref")
+    assert p.rk3_step(1.0, 2) == r.rk3_step(1.0, 2) == 0
+    assert oc.cfl(p, 2.0, 0.3) == oc.cfl(r, 2.0, 0.3)
+    assert oc.max_stable_dt(p) == oc.max_stable_dt(r)

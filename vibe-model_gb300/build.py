@@ -27,7 +27,8 @@ SOURCES = [("step_fp64.cu", "step_fp64.o", []),
            ("helmholtz_api.cu", "helmholtz_api.o", []),
            ("si_step.cu", "si_step.o", ["--fmad=false"]),
            ("nest.cu", "nest.o", ["--fmad=false"]),
-           ("tlad.cu", "tlad.o", [])]
+           ("tlad.cu", "tlad.o", []),
+           ("diag.cu", "diag.o", ["--fmad=false"])]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

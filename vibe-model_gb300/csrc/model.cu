@@ -111,6 +111,7 @@ struct vibe_gb300_model {
   int hz_iterations = 0;
   double hz_residual = 0.0;
   double hz_ms = 0.0;
+  double cfl_rate = 0.0;  // max over cells of 1/dx + 1/dy + 1/dz
   cudaEvent_t hz_ev[2] = {nullptr, nullptr};
   // CUDA graphs of one mixed step, per state parity
   bool use_graph = true, graph_warm = false;
@@ -1101,6 +1102,38 @@ int vibe_gb300_set_graph(vibe_gb300_model* m, int enable) {
   if (m->stream) cudaStreamSynchronize(m->stream);
   drop_graphs(m);
   m->use_graph = enable != 0;
+  return 0;
+}
+
+int vibe_gb300_cfl(vibe_gb300_model* m, double dt, double dtau, double* adv_cfl, double* max_sound_speed,
+                   double* acoustic_cfl) {
+  if (!m) return fail(VIBE_GB300_EBADARG, "bad argument");
+  unsigned long long* dv = nullptr;
+  CUDA_OK(cudaMallocAsync((void**)&dv, 4 * sizeof(unsigned long long), m->stream));
+  diag_cfl(m->d, m->met, m->S[m->cur], dt, dtau, dv, m->stream);
+  unsigned long long hv[4] = {0, 0, 0, 0};
+  CUDA_OK(cudaMemcpyAsync(hv, dv, sizeof(hv), cudaMemcpyDeviceToHost, m->stream));
+  CUDA_OK(cudaFreeAsync(dv, m->stream));
+  CUDA_OK(cudaStreamSynchronize(m->stream));
+  double r[4];
+  for (int q = 0; q < 4; ++q) std::memcpy(&r[q], &hv[q], sizeof(double));
+  if (adv_cfl) *adv_cfl = r[0];
+  if (max_sound_speed) *max_sound_speed = r[1];
+  if (acoustic_cfl) *acoustic_cfl = r[2];
+  m->cfl_rate = r[3];
+  return 0;
+}
+
+// RungeKutta3Integrator::max_stable_dt (runge_kutta.cpp:121-140):
+// min(0.8 / cfl_number(s, 1), 2 / (max sound speed * max(1/dx + 1/dy + 1/dz)))
+int vibe_gb300_max_stable_dt(vibe_gb300_model* m, double* dt_out) {
+  if (!m || !dt_out) return fail(VIBE_GB300_EBADARG, "bad argument");
+  double adv = 0.0, cs = 0.0;
+  if (int rc = vibe_gb300_cfl(m, 1.0, 1.0, &adv, &cs, nullptr)) return rc;
+  const double rate = cs * m->cfl_rate;
+  const double dt_adv = (adv > 0.0) ? 0.8 / adv : 1e9;
+  const double dt_ac = (rate > 0.0) ? 2.0 / rate : 1e9;
+  *dt_out = std::min(dt_adv, dt_ac);
   return 0;
 }
 

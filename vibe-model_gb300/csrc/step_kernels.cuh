@@ -39,6 +39,11 @@ void si_assemble(const Dims& d, const Metric& met, double* const* st, double* co
 void si_cells_add_scaled(const Dims& d, double* x, const double* y, double a, cudaStream_t s);
 void si_to_cells(const Dims& d, const double* in, double* out, cudaStream_t s);
 
+// ---- time-step diagnostics (diag.cu): out[0..3] = advective CFL at dt,
+// max sound speed, acoustic CFL at dtau, max(1/dx + 1/dy + 1/dz), as IEEE bits ----
+void diag_cfl(const Dims& d, const Metric& met, double* const* st, double dt, double dtau, unsigned long long* out,
+              cudaStream_t s);
+
 // ---- mixed path (step_mixed.cu): FP64 state, FP32 working state ----
 // Horizontally uniform reference state on flat terrain: every coefficient
 // is a function of k only and lives in these FP32 tables (device).

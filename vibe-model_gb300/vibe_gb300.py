@@ -96,6 +96,8 @@ _sigs = {
     "vibe_gb300_si_step": (_I, [_vp, _D, _I, _I, _D, ctypes.POINTER(_I), _dp, _vp]),
     "vibe_gb300_si_stats": (_I, [_vp, ctypes.POINTER(_I), _dp, _dp]),
     "vibe_gb300_set_graph": (_I, [_vp, _I]),
+    "vibe_gb300_cfl": (_I, [_vp, _D, _D, _dp, _dp, _dp]),
+    "vibe_gb300_max_stable_dt": (_I, [_vp, _dp]),
     # C-ABI kernels (include/vibe_c_kernels.h)
     "vibe_tridiagonal_solve_f64": (_I, [_vp, _vp, _vp, _vp, _I, _vp, _vp]),
     "vibe_tridiagonal_solve_batched_f64": (_I, [_vp, _vp, _vp, _vp, _I, _I, _vp]),
@@ -268,6 +270,17 @@ class Model:
         _check(lib.vibe_gb300_si_step(self.h, dt, kind, max_iter, tol, ctypes.byref(it), ctypes.byref(res),
                                       None if pin is None else pin.ctypes.data))
         return it.value, res.value, pin
+
+    def cfl(self, dt, dtau):
+        """(cfl_number(s, dt), max_sound_speed(s), acoustic_cfl(s, dtau))."""
+        out = [ctypes.c_double() for _ in range(3)]
+        _check(lib.vibe_gb300_cfl(self.h, dt, dtau, *[ctypes.byref(o) for o in out]))
+        return tuple(o.value for o in out)
+
+    def max_stable_dt(self):
+        out = ctypes.c_double()
+        _check(lib.vibe_gb300_max_stable_dt(self.h, ctypes.byref(out)))
+        return out.value
 
     def set_graph(self, on):
         _check(lib.vibe_gb300_set_graph(self.h, 1 if on else 0))
