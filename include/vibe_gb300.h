@@ -141,6 +141,20 @@ int vibe_gb300_max_stable_dt(vibe_gb300_model *m, double *dt_out);
  * off while kernel timing is on). */
 int vibe_gb300_set_graph(vibe_gb300_model *m, int enable);
 
+/* Groups: several mixed-precision models (acoustic_mode 2, equal nz and
+ * numerics flags, any nx/ny; members of an ensemble, or the parents, or the
+ * nests of a nested set) advanced together with one launch per kernel for
+ * all of them (a work-list over every domain's blocks) and each step
+ * replayed as a CUDA graph. The models keep their state; the group does not
+ * own them (destroy the group first). group_step blocks until done and
+ * returns the first failure of any member (VIBE_GB300_ENONFINITE, ...). */
+typedef struct vibe_gb300_group vibe_gb300_group;
+int vibe_gb300_group_create(vibe_gb300_model *const *models, int n, vibe_gb300_group **out);
+void vibe_gb300_group_destroy(vibe_gb300_group *g);
+int vibe_gb300_group_step(vibe_gb300_group *g, double dt, int n_sub, int n_steps);
+int vibe_gb300_group_launches_per_step(const vibe_gb300_group *g);
+vibe_stream_t vibe_gb300_group_stream(vibe_gb300_group *g);
+
 /* Kernel-level entry points (FP64 path only for the tendency). */
 int vibe_gb300_slow_tendency(vibe_gb300_model *m, double *const *host_out);
 int vibe_gb300_acoustic_substep(vibe_gb300_model *m, double dtau);

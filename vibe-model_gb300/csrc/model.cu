@@ -1145,6 +1145,134 @@ int vibe_gb300_si_stats(const vibe_gb300_model* m, int* iterations, double* resi
   return 0;
 }
 
+// ---- groups: several mixed models advanced together, one launch per kernel
+// for all of them (work-list over the domains' blocks), each step replayed as
+// a CUDA graph per state parity.
+}  // extern "C"
+
+struct vibe_gb300_group {
+  std::vector<vibe_gb300_model*> ms;
+  cudaStream_t stream = nullptr;
+  unsigned *d_err = nullptr, *h_err = nullptr;
+  MixedBatch* batch[2] = {nullptr, nullptr};
+  cudaGraphExec_t g[2] = {nullptr, nullptr};
+  double dt = -1.0;
+  int nsub = -1;
+};
+
+namespace {
+void group_drop(vibe_gb300_group* g) {
+  for (int p = 0; p < 2; ++p) {
+    if (g->g[p]) cudaGraphExecDestroy(g->g[p]);
+    g->g[p] = nullptr;
+    mixed_batch_destroy(g->batch[p]);
+    g->batch[p] = nullptr;
+  }
+}
+}  // namespace
+
+extern "C" {
+
+int vibe_gb300_group_create(vibe_gb300_model* const* models, int n, vibe_gb300_group** out) {
+  if (!models || n < 1 || !out) return fail(VIBE_GB300_EBADARG, "bad argument");
+  for (int q = 0; q < n; ++q) {
+    vibe_gb300_model* m = models[q];
+    if (!m || m->precision != VIBE_GB300_MIXED || m->fl.acoustic_mode != 2)
+      return fail(VIBE_GB300_EUNSUPPORTED, "a group holds mixed-precision models with acoustic_mode 2");
+    if (m->d.nz != models[0]->d.nz || m->fl.moist != models[0]->fl.moist ||
+        m->fl.weno_scalars != models[0]->fl.weno_scalars || m->fl.advection != models[0]->fl.advection ||
+        m->fl.weno_advective != models[0]->fl.weno_advective || m->fl.coriolis != models[0]->fl.coriolis ||
+        m->fl.div_damp != models[0]->fl.div_damp || m->fl.hevi_beta != models[0]->fl.hevi_beta)
+      return fail(VIBE_GB300_EUNSUPPORTED, "group members need the same nz and numerics flags");
+  }
+  auto* g = new vibe_gb300_group();
+  g->ms.assign(models, models + n);
+  if (cudaStreamCreateWithFlags(&g->stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaMalloc(&g->d_err, sizeof(unsigned)) != cudaSuccess || cudaMallocHost(&g->h_err, sizeof(unsigned)) != cudaSuccess ||
+      cudaMemset(g->d_err, 0, sizeof(unsigned)) != cudaSuccess) {
+    vibe_gb300_group_destroy(g);
+    return fail(VIBE_GB300_EDEVICE, "group allocation failed");
+  }
+  *out = g;
+  return 0;
+}
+
+void vibe_gb300_group_destroy(vibe_gb300_group* g) {
+  if (!g) return;
+  if (g->stream) cudaStreamSynchronize(g->stream);
+  group_drop(g);
+  cudaFree(g->d_err);
+  if (g->h_err) cudaFreeHost(g->h_err);
+  if (g->stream) cudaStreamDestroy(g->stream);
+  delete g;
+}
+
+int vibe_gb300_group_step(vibe_gb300_group* g, double dt, int n_sub_in, int n_steps) {
+  if (!g || !(dt > 0.0) || n_steps < 0) return fail(VIBE_GB300_EBADARG, "bad argument");
+  const int n_sub = n_sub_in > 1 ? n_sub_in : 1;
+  const int parity0 = g->ms[0]->cur;
+  for (auto* m : g->ms) {
+    if (m->cur != parity0) return fail(VIBE_GB300_EUNSUPPORTED, "group members must share the state parity");
+    CUDA_OK(cudaStreamSynchronize(m->stream));  // nothing of theirs in flight
+  }
+  if (g->dt != dt || g->nsub != n_sub) {
+    CUDA_OK(cudaStreamSynchronize(g->stream));
+    group_drop(g);
+    for (auto* m : g->ms)
+      if (int rc = configure_dt(m, dt, n_sub)) return rc;
+    for (int p = 0; p < 2; ++p) {
+      std::vector<MixedDomain> doms;
+      for (auto* m : g->ms) {
+        MixedDomain md;
+        md.d = m->d;
+        md.t = m->tab;
+        md.lu = m->d_lu;
+        md.W0 = m->W0;
+        md.WSt0 = m->WSt[0];
+        md.WSt1 = m->WSt[1];
+        md.WA = m->WA;
+        md.WB = m->WB;
+        md.WR = m->WR;
+        md.S0 = m->S[p];
+        md.S1 = m->S[1 - p];
+        doms.push_back(md);
+      }
+      g->batch[p] = mixed_batch_build(doms, g->ms[0]->fl, dt, n_sub, g->d_err);
+      if (!g->batch[p]) return fail(VIBE_GB300_EDEVICE, "group launch set-up failed");
+    }
+    g->dt = dt;
+    g->nsub = n_sub;
+  }
+  for (int step = 0; step < n_steps; ++step) {
+    const int p = g->ms[0]->cur;
+    if (!g->g[p]) {
+      cudaGraph_t gr = nullptr;
+      CUDA_OK(cudaStreamBeginCapture(g->stream, cudaStreamCaptureModeThreadLocal));
+      mixed_batch_enqueue(g->batch[p], g->stream);
+      const cudaError_t e = cudaStreamEndCapture(g->stream, &gr);
+      CUDA_OK(e);
+      const cudaError_t ei = cudaGraphInstantiate(&g->g[p], gr, 0);
+      cudaGraphDestroy(gr);
+      CUDA_OK(ei);
+    }
+    CUDA_OK(cudaGraphLaunch(g->g[p], g->stream));
+    for (auto* m : g->ms) m->cur = 1 - m->cur;
+  }
+  CUDA_OK(cudaMemcpyAsync(g->h_err, g->d_err, sizeof(unsigned), cudaMemcpyDeviceToHost, g->stream));
+  CUDA_OK(cudaStreamSynchronize(g->stream));
+  const unsigned e = *g->h_err;
+  CUDA_OK(cudaMemsetAsync(g->d_err, 0, sizeof(unsigned), g->stream));
+  if (e & kErrWaitTimeout) return fail(VIBE_GB300_EDEVICE, "a TMA box of the stage kernel did not arrive (bounded wait)");
+  if (e & kErrNonFinite) return fail(VIBE_GB300_ENONFINITE, "non-finite value in a group member's state");
+  return 0;
+}
+
+int vibe_gb300_group_launches_per_step(const vibe_gb300_group* g) {
+  return (g && g->batch[0]) ? mixed_batch_launches(g->batch[0]) : 0;
+}
+
+vibe_stream_t vibe_gb300_group_stream(vibe_gb300_group* g) { return g ? (vibe_stream_t)g->stream : nullptr; }
+
 int vibe_gb300_set_state(vibe_gb300_model* m, const double* const* host, int nspecies) {
   if (!m || !host || nspecies < 1 || nspecies > NSPECIES) return fail(VIBE_GB300_EBADARG, "bad argument");
   for (int q = 0; q < nspecies; ++q) {

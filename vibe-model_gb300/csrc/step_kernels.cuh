@@ -1,5 +1,7 @@
 // vibe-model_gb300/csrc/step_kernels.cuh -- launchers of the step kernels.
 #pragma once
+#include <vector>
+
 #include "vibe_internal.cuh"
 
 namespace vgb {
@@ -84,6 +86,29 @@ void mixed_uv_backward(const Dims& d, const Tab& t, const WS& win, const WS& wou
 void mixed_finish(const Dims& d, const Tab& t, const Flags& fl, const WS& wfin, const WS& wst, const WS& w0,
                   const WS* rin, double dt, double* const* s0, double* const* s1, unsigned* err,
                   cudaStream_t stream);
+// ---- several domains per launch (work-list), mixed path, HEVI mode ----
+struct MixedDomain {
+  Dims d;
+  Tab t;
+  const float* lu;  // 3 stages x 3*nz LU factors (configured for the step's dt, n_sub)
+  float* const* W0;
+  float* const* WSt0;
+  float* const* WSt1;
+  float* const* WA;
+  float* const* WB;
+  float* const* WR;
+  double* const* S0;  // state read by the step
+  double* const* S1;  // state written by the step
+};
+struct MixedBatch;
+// the launches of one full step of every domain (all with nz equal, the
+// same flags, acoustic_mode 2); nullptr on failure
+MixedBatch* mixed_batch_build(const std::vector<MixedDomain>& doms, const Flags& fl, double dt, int n_sub,
+                              unsigned* err);
+void mixed_batch_enqueue(const MixedBatch* b, cudaStream_t s);
+int mixed_batch_launches(const MixedBatch* b);
+void mixed_batch_destroy(MixedBatch* b);
+
 void mixed_unpack_f32(const Dims& d, int nsx, int nsy, int nsz, int ni, int nj, int nk, const float* src, double* dst,
                       cudaStream_t stream);
 void mixed_to_working(const Dims& d, const Tab& t, double* const* s, const WS& w, cudaStream_t stream);

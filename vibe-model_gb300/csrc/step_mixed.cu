@@ -200,18 +200,17 @@ __device__ void fix_box(float* t, int rows, int halo, int i0, int j0, int xmax, 
 // kRaw: also write the tendency R itself (the last stage: the finish kernel
 // forms the FP64 state from it)
 template <bool kRaw>
-__global__ void __launch_bounds__(NT, 3) k_mx_stage(Dims d, Tab t, Flags fl, const __grid_constant__ StageMaps M,
-                                                    const __grid_constant__ WS win, const __grid_constant__ WS w0,
-                                                    const __grid_constant__ WS wout, const __grid_constant__ WS rout,
-                                                    float dts, int kchunk, unsigned* err) {
+__device__ __forceinline__ void stage_body(const Dims& d, const Tab& t, const Flags& fl, const StageMaps& M,
+                                           const WS& win, const WS& w0, const WS& wout, const WS& rout, float dts,
+                                           int kchunk, unsigned* err, int bx, int by, int bz) {
   __shared__ __align__(128) float sbuf[2][kBuf];
   __shared__ __align__(128) float sQm[R3 * TW];  // moisture species beyond qv (plain loads)
   __shared__ float sFx[TY * (TX + 1)], sFy[(TY + 1) * TX];
   __shared__ __align__(8) unsigned long long sbar[2];
   const int nx = d.nx, ny = d.ny, nz = d.nz, P = d.P;
   const size_t pl = d.plane;
-  const int i0 = blockIdx.x * TX, j0 = blockIdx.y * TY;
-  const int kb = blockIdx.z * kchunk;
+  const int i0 = bx * TX, j0 = by * TY;
+  const int kb = bz * kchunk;
   const int klast = (kb + kchunk >= nz) ? nz : kb + kchunk - 1;  // the top chunk also owns face nz
   const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * TX + tx;
   const int i = i0 + tx, j = j0 + ty;
@@ -459,6 +458,16 @@ __global__ void __launch_bounds__(NT, 3) k_mx_stage(Dims d, Tab t, Flags fl, con
   if (bad) atomicOr(err, (unsigned)kErrNonFinite);
 }
 
+template <bool kRaw>
+__global__ void __launch_bounds__(NT, 3) k_mx_stage(const __grid_constant__ Dims d, const __grid_constant__ Tab t,
+                                                    const __grid_constant__ Flags fl,
+                                                    const __grid_constant__ StageMaps M,
+                                                    const __grid_constant__ WS win, const __grid_constant__ WS w0,
+                                                    const __grid_constant__ WS wout, const __grid_constant__ WS rout,
+                                                    float dts, int kchunk, unsigned* err) {
+  stage_body<kRaw>(d, t, fl, M, win, w0, wout, rout, dts, kchunk, err, blockIdx.x, blockIdx.y, blockIdx.z);
+}
+
 // ---- explicit forward-backward substep in FP32 (runge_kutta.cpp:65-75) --
 __global__ void k_mx_fb_mass(Dims d, Tab t, WS win, WS wout, float dtau) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -474,10 +483,11 @@ __global__ void k_mx_fb_mass(Dims d, Tab t, WS win, WS wout, float dtau) {
   wout.f[PI][c] = win.f[PI][c] + dtau * (t.kap[k] * drho);
 }
 // momentum backward with the new pi' (read from wout)
-__global__ void k_mx_fb_mom(Dims d, Tab t, WS win, WS wout, float dtau, int do_w) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  const int j = blockIdx.y * blockDim.y + threadIdx.y;
-  const int k = blockIdx.z;
+__device__ __forceinline__ void fb_mom_body(const Dims& d, const Tab& t, const WS& win, const WS& wout, float dtau,
+                                            int do_w, int bx, int by, int bz) {
+  const int i = bx * blockDim.x + threadIdx.x;
+  const int j = by * blockDim.y + threadIdx.y;
+  const int k = bz;
   if (i > d.nx || j > d.ny || k > d.nz) return;
   const size_t c = IX(i, j, k);
   const float* __restrict__ pn = wout.f[PI];
@@ -504,6 +514,11 @@ __global__ void k_mx_fb_mom(Dims d, Tab t, WS win, WS wout, float dtau, int do_w
 // 40 KB per block at nz = 80, so 5 blocks -- 20 warps -- fit an SM); the
 // backward sweep re-derives the explicit terms from the same inputs, which
 // the forward sweep has just pulled through L2.
+__global__ void k_mx_fb_mom(const __grid_constant__ Dims d, const __grid_constant__ Tab t,
+                            const __grid_constant__ WS win, const __grid_constant__ WS wout, float dtau, int do_w) {
+  fb_mom_body(d, t, win, wout, dtau, do_w, blockIdx.x, blockIdx.y, blockIdx.z);
+}
+
 // apply_uv: the u/v backward update of the previous substep is applied here,
 // on the fly, from this substep's input pi' (the previous substep's result):
 // u(i) += dtau (-cp theta0(k) (pi'(ip) - pi'(im)) / dx) with the clamped
@@ -512,9 +527,9 @@ __global__ void k_mx_fb_mom(Dims d, Tab t, WS win, WS wout, float dtau, int do_w
 // written to the output. After the last substep of a stage one u/v kernel
 // applies the final update in place. cdx = -cp dtau / dx, cdy likewise.
 template <int kPF>
-__global__ void __launch_bounds__(128, 6) k_mx_hevi_col(Dims d, Tab t, Flags fl, WS win, WS wout, float dtau,
-                                                         const float* __restrict__ lu, int apply_uv, float cdx,
-                                                         float cdy) {
+__device__ __forceinline__ void hevi_body(const Dims& d, const Tab& t, const Flags& fl, const WS& win, const WS& wout,
+                                          float dtau, const float* __restrict__ lu, int apply_uv, float cdx,
+                                          float cdy, int bx, int by) {
   // per-level tables in shared memory; the forward sweep parks its per-level
   // results in the thread's own column of the output arrays (wt on the w
   // faces, dp on pi', the explicit source S on rho'), where the backward
@@ -547,8 +562,8 @@ __global__ void __launch_bounds__(128, 6) k_mx_hevi_col(Dims d, Tab t, Flags fl,
     }
   }
   __syncthreads();
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  const int j = blockIdx.y * blockDim.y + threadIdx.y;
+  const int i = bx * blockDim.x + threadIdx.x;
+  const int j = by * blockDim.y + threadIdx.y;
   if (i >= d.nx || j >= d.ny) return;
   const float b = (float)fl.hevi_beta, ob = 1.f - b;
   const float cpf = (float)kCp;
@@ -691,12 +706,12 @@ __global__ void __launch_bounds__(128, 6) k_mx_hevi_col(Dims d, Tab t, Flags fl,
 // added to the FP64 state with one conversion and one FP64 add per field.
 // rin == nullptr: no tendency (single-substep entry points, S1 == S0).
 // Also writes the next step's FP32 working copy W0.
-__global__ void k_mx_finish(Dims d, Tab t, Flags fl, const __grid_constant__ WS wfin, const __grid_constant__ WS wst,
-                            const __grid_constant__ WS w0, const __grid_constant__ WS rin, float dtf,
-                            const __grid_constant__ CS64 s0, const __grid_constant__ MS64 s1, unsigned* err) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  const int j = blockIdx.y * blockDim.y + threadIdx.y;
-  const int k = blockIdx.z;
+__device__ __forceinline__ void finish_body(const Dims& d, const Tab& t, const Flags& fl, const WS& wfin,
+                                            const WS& wst, const WS& w0, const WS& rin, float dtf, const CS64& s0,
+                                            const MS64& s1, unsigned* err, int bx, int by, int bz) {
+  const int i = bx * blockDim.x + threadIdx.x;
+  const int j = by * blockDim.y + threadIdx.y;
+  const int k = bz;
   if (i > d.nx || j > d.ny || k > d.nz) return;
   const size_t c = IX(i, j, k);
   const int kc = imin(k, d.nz - 1);
@@ -749,6 +764,14 @@ __global__ void k_mx_finish(Dims d, Tab t, Flags fl, const __grid_constant__ WS 
 }
 
 // FP32 field (device layout) -> FP64 FieldT storage (zeros outside the box)
+__global__ void k_mx_finish(const __grid_constant__ Dims d, const __grid_constant__ Tab t,
+                            const __grid_constant__ Flags fl, const __grid_constant__ WS wfin,
+                            const __grid_constant__ WS wst, const __grid_constant__ WS w0,
+                            const __grid_constant__ WS rin, float dtf, const __grid_constant__ CS64 s0,
+                            const __grid_constant__ MS64 s1, unsigned* err) {
+  finish_body(d, t, fl, wfin, wst, w0, rin, dtf, s0, s1, err, blockIdx.x, blockIdx.y, blockIdx.z);
+}
+
 __global__ void k_mx_unpack_f32(Dims d, int nsx, int nsy, int nsz, int ni, int nj, int nk, const float* __restrict__ src,
                                 double* __restrict__ dst) {
   const size_t n = (size_t)nsx * nsy * nsz;
@@ -761,10 +784,11 @@ __global__ void k_mx_unpack_f32(Dims d, int nsx, int nsy, int nsz, int ni, int n
 }
 
 // FP64 state -> FP32 working copy in perturbation form, incl. ghosts.
-__global__ void k_mx_to_working(Dims d, Tab t, const __grid_constant__ CS64 s, const __grid_constant__ WS w) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  const int j = blockIdx.y * blockDim.y + threadIdx.y;
-  const int k = blockIdx.z;
+__device__ __forceinline__ void to_working_body(const Dims& d, const Tab& t, const CS64& s, const WS& w, int bx,
+                                                int by, int bz) {
+  const int i = bx * blockDim.x + threadIdx.x;
+  const int j = by * blockDim.y + threadIdx.y;
+  const int k = bz;
   if (i > d.nx || j > d.ny || k > d.nz) return;
   const size_t c = IX(i, j, k);
   if (j < d.ny && k < d.nz) w.f[U][c] = (float)s.f[U][c];
@@ -776,6 +800,10 @@ __global__ void k_mx_to_working(Dims d, Tab t, const __grid_constant__ CS64 s, c
     w.f[PI][c] = (float)(s.f[PI][c] - t.p0d[k]);
     for (int q = QV; q < NSPECIES; ++q) w.f[q][c] = (float)s.f[q][c];
   }
+}
+__global__ void k_mx_to_working(const __grid_constant__ Dims d, const __grid_constant__ Tab t,
+                                const __grid_constant__ CS64 s, const __grid_constant__ WS w) {
+  to_working_body(d, t, s, w, blockIdx.x, blockIdx.y, blockIdx.z);
 }
 
 }  // namespace
@@ -910,6 +938,16 @@ void mixed_fb_substep(const Dims& d, const Tab& t, const Flags& fl, const WS& wi
   k_mx_fb_mom<<<g3(d.nx + 1, d.ny + 1, d.nz + 1, b), b, 0, stream>>>(d, t, win, wout, dtau, 1);
 }
 
+template <int kPF>
+__global__ void __launch_bounds__(128, 6) k_mx_hevi_col(const __grid_constant__ Dims d, const __grid_constant__ Tab t,
+                                                         const __grid_constant__ Flags fl,
+                                                         const __grid_constant__ WS win,
+                                                         const __grid_constant__ WS wout, float dtau,
+                                                         const float* __restrict__ lu, int apply_uv, float cdx,
+                                                         float cdy) {
+  hevi_body<kPF>(d, t, fl, win, wout, dtau, lu, apply_uv, cdx, cdy, blockIdx.x, blockIdx.y);
+}
+
 // Prefetch depth of the HEVI column kernel (levels of loads in flight per
 // thread); VIBE_GB300_HEVI_PF=2|4|6|8 overrides the built-in choice.
 static int hevi_pf() {
@@ -969,6 +1007,282 @@ void mixed_unpack_f32(const Dims& d, int nsx, int nsy, int nsz, int ni, int nj, 
 void mixed_to_working(const Dims& d, const Tab& t, double* const* s, const WS& w, cudaStream_t stream) {
   const dim3 b(32, 4);
   k_mx_to_working<<<g3(d.nx + 1, d.ny + 1, d.nz + 1, b), b, 0, stream>>>(d, t, cs64(s), w);
+}
+
+
+// ===========================================================================
+// Several domains in one launch per kernel: a work-list of blocks over all
+// domains (start[d] = first block of domain d); each block finds its domain
+// and runs the single-domain body with that domain's arguments, read from
+// device memory (TMA descriptors included, 64-byte aligned).
+// ===========================================================================
+namespace {
+struct StageArgs {  // 64-byte aligned through its CUtensorMap members
+  StageMaps M;
+  Dims d;
+  Tab t;
+  Flags fl;
+  WS win, w0, wout, rout;
+  float dts;
+  int kchunk, gx, gy, gz;
+};
+struct HeviArgs {
+  Dims d;
+  Tab t;
+  Flags fl;
+  WS win, wout;
+  float dtau, cdx, cdy;
+  const float* lu;
+  int apply_uv, gx, gy;
+};
+struct UvArgs {
+  Dims d;
+  Tab t;
+  WS win, wout;
+  float dtau;
+  int gx, gy, gz;
+};
+struct FinishArgs {
+  Dims d;
+  Tab t;
+  Flags fl;
+  WS wfin, wst, w0, rin;
+  float dtf;
+  CS64 s0;
+  MS64 s1;
+  int gx, gy, gz;
+};
+
+__device__ __forceinline__ int find_domain(const int* __restrict__ start, int nd) {
+  int dom = 0;
+  while (dom + 1 < nd && (int)blockIdx.x >= start[dom + 1]) ++dom;
+  return dom;
+}
+
+template <bool kRaw>
+__global__ void __launch_bounds__(NT, 3) k_b_stage(const StageArgs* __restrict__ A, const int* __restrict__ start,
+                                                   int nd, unsigned* err) {
+  const int dom = find_domain(start, nd);
+  const StageArgs& a = A[dom];
+  const int l = (int)blockIdx.x - start[dom];
+  stage_body<kRaw>(a.d, a.t, a.fl, a.M, a.win, a.w0, a.wout, a.rout, a.dts, a.kchunk, err, l % a.gx,
+                   (l / a.gx) % a.gy, l / (a.gx * a.gy));
+}
+
+__global__ void __launch_bounds__(128, 6) k_b_hevi(const HeviArgs* __restrict__ A, const int* __restrict__ start,
+                                                   int nd) {
+  const int dom = find_domain(start, nd);
+  const HeviArgs& a = A[dom];
+  const int l = (int)blockIdx.x - start[dom];
+  hevi_body<2>(a.d, a.t, a.fl, a.win, a.wout, a.dtau, a.lu, a.apply_uv, a.cdx, a.cdy, l % a.gx, l / a.gx);
+}
+
+__global__ void k_b_uv(const UvArgs* __restrict__ A, const int* __restrict__ start, int nd) {
+  const int dom = find_domain(start, nd);
+  const UvArgs& a = A[dom];
+  const int l = (int)blockIdx.x - start[dom];
+  fb_mom_body(a.d, a.t, a.win, a.wout, a.dtau, 0, l % a.gx, (l / a.gx) % a.gy, l / (a.gx * a.gy));
+}
+
+__global__ void k_b_finish(const FinishArgs* __restrict__ A, const int* __restrict__ start, int nd, unsigned* err) {
+  const int dom = find_domain(start, nd);
+  const FinishArgs& a = A[dom];
+  const int l = (int)blockIdx.x - start[dom];
+  finish_body(a.d, a.t, a.fl, a.wfin, a.wst, a.w0, a.rin, a.dtf, a.s0, a.s1, err, l % a.gx, (l / a.gx) % a.gy,
+              l / (a.gx * a.gy));
+}
+
+WS ws_from(float* const* a) {
+  WS w;
+  for (int q = 0; q < NSPECIES; ++q) w.f[q] = a ? a[q] : nullptr;
+  return w;
+}
+WS ws_mix(float* const* sub, float* const* stage) {  // acoustic fields from sub, the rest from stage
+  WS w;
+  for (int q = 0; q < NSPECIES; ++q)
+    w.f[q] = (q == U || q == V || q == W || q == RHO || q == PI) ? sub[q] : stage[q];
+  return w;
+}
+}  // namespace
+
+struct MixedBatch {
+  struct Launch {
+    int kind = 0;  // 0 stage, 1 column, 2 u/v, 3 finish
+    int raw = 0, nd = 0, blocks = 0;
+    void* args = nullptr;
+    int* start = nullptr;
+  };
+  std::vector<Launch> seq;
+  std::vector<void*> allocs;
+  size_t hevi_smem = 0;
+  unsigned* err = nullptr;
+};
+
+namespace {
+template <class A>
+bool upload_launch(MixedBatch* b, int kind, int raw, const std::vector<A>& args, const std::vector<int>& start,
+                   int blocks) {
+  MixedBatch::Launch L;
+  L.kind = kind;
+  L.raw = raw;
+  L.nd = (int)args.size();
+  L.blocks = blocks;
+  if (cudaMalloc(&L.args, args.size() * sizeof(A)) != cudaSuccess) return false;
+  b->allocs.push_back(L.args);
+  if (cudaMalloc((void**)&L.start, start.size() * sizeof(int)) != cudaSuccess) return false;
+  b->allocs.push_back(L.start);
+  if (cudaMemcpy(L.args, args.data(), args.size() * sizeof(A), cudaMemcpyHostToDevice) != cudaSuccess ||
+      cudaMemcpy(L.start, start.data(), start.size() * sizeof(int), cudaMemcpyHostToDevice) != cudaSuccess)
+    return false;
+  b->seq.push_back(L);
+  return true;
+}
+int ceil_div(int a, int b) { return (a + b - 1) / b; }
+}  // namespace
+
+MixedBatch* mixed_batch_build(const std::vector<MixedDomain>& doms, const Flags& fl, double dt, int n_sub,
+                              unsigned* err) {
+  if (doms.empty() || fl.acoustic_mode != 2) return nullptr;
+  const int nz = doms[0].d.nz;
+  for (const auto& m : doms)
+    if (m.d.nz != nz) return nullptr;
+  auto* b = new MixedBatch();
+  b->err = err;
+  b->hevi_smem = 10 * (size_t)(nz + 1) * sizeof(float);
+  const double dts[3] = {dt / 3.0, dt / 2.0, dt};
+  const int nd = (int)doms.size();
+  auto sub_out = [&](const MixedDomain& m, int n) { return (n & 1) ? m.WB : m.WA; };
+  bool ok = true;
+  for (int stage = 0; stage < 3 && ok; ++stage) {
+    std::vector<StageArgs> sa(nd);
+    std::vector<int> start(nd);
+    int blocks = 0;
+    const bool raw = stage == 2;
+    for (int q = 0; q < nd && ok; ++q) {
+      const MixedDomain& m = doms[q];
+      float* const* st_out = stage & 1 ? m.WSt1 : m.WSt0;
+      const WS win = (stage == 0) ? ws_from(m.W0) : ws_mix(sub_out(m, n_sub - 1), (stage - 1) & 1 ? m.WSt1 : m.WSt0);
+      StageArgs& a = sa[q];
+      ok = stage_maps(m.d, win, a.M);
+      a.d = m.d;
+      a.t = m.t;
+      a.fl = fl;
+      a.win = win;
+      a.w0 = ws_from(m.W0);
+      a.wout = ws_from(st_out);
+      a.rout = raw ? ws_from(m.WR) : a.wout;
+      a.dts = (float)dts[stage];
+      a.kchunk = stage_kchunk(m.d, raw);
+      a.gx = (m.d.nx + TX) / TX;
+      a.gy = (m.d.ny + TY) / TY;
+      a.gz = ceil_div(m.d.nz, a.kchunk);
+      start[q] = blocks;
+      blocks += a.gx * a.gy * a.gz;
+    }
+    ok = ok && upload_launch(b, 0, raw ? 1 : 0, sa, start, blocks);
+    const float dtau = (float)(dts[stage] / (double)n_sub);
+    for (int n = 0; n < n_sub && ok; ++n) {
+      std::vector<HeviArgs> ha(nd);
+      int hb = 0;
+      for (int q = 0; q < nd; ++q) {
+        const MixedDomain& m = doms[q];
+        float* const* in = (n == 0) ? (stage & 1 ? m.WSt1 : m.WSt0) : sub_out(m, n - 1);
+        HeviArgs& a = ha[q];
+        a.d = m.d;
+        a.t = m.t;
+        a.fl = fl;
+        a.win = ws_from(in);
+        a.wout = ws_from(sub_out(m, n));
+        a.dtau = dtau;
+        a.cdx = -(float)kCp * dtau * m.t.dx_inv;
+        a.cdy = -(float)kCp * dtau * m.t.dy_inv;
+        a.lu = m.lu + (size_t)stage * 3 * nz;
+        a.apply_uv = n > 0;
+        a.gx = ceil_div(m.d.nx, 32);
+        a.gy = ceil_div(m.d.ny, 4);
+        start[q] = hb;
+        hb += a.gx * a.gy;
+      }
+      ok = upload_launch(b, 1, 0, ha, start, hb);
+    }
+    std::vector<UvArgs> ua(nd);
+    int ub = 0;
+    for (int q = 0; q < nd; ++q) {
+      const MixedDomain& m = doms[q];
+      UvArgs& a = ua[q];
+      a.d = m.d;
+      a.t = m.t;
+      a.win = ws_from(sub_out(m, n_sub - 1));
+      a.wout = a.win;
+      a.dtau = dtau;
+      a.gx = ceil_div(m.d.nx + 1, 32);
+      a.gy = ceil_div(m.d.ny + 1, 4);
+      a.gz = m.d.nz;
+      start[q] = ub;
+      ub += a.gx * a.gy * a.gz;
+    }
+    ok = ok && upload_launch(b, 2, 0, ua, start, ub);
+  }
+  if (ok) {
+    std::vector<FinishArgs> fa(nd);
+    std::vector<int> start(nd);
+    int fb = 0;
+    for (int q = 0; q < nd; ++q) {
+      const MixedDomain& m = doms[q];
+      FinishArgs& a = fa[q];
+      a.d = m.d;
+      a.t = m.t;
+      a.fl = fl;
+      a.wfin = ws_from(sub_out(m, n_sub - 1));
+      a.wst = ws_from(m.WSt0);
+      a.w0 = ws_from(m.W0);
+      a.rin = ws_from(m.WR);
+      a.dtf = (float)dt;
+      a.s0 = cs64(m.S0);
+      a.s1 = ms64(m.S1);
+      a.gx = ceil_div(m.d.nx + 1, 32);
+      a.gy = ceil_div(m.d.ny + 1, 4);
+      a.gz = m.d.nz + 1;
+      start[q] = fb;
+      fb += a.gx * a.gy * a.gz;
+    }
+    ok = upload_launch(b, 3, 0, fa, start, fb);
+  }
+  if (!ok) {
+    mixed_batch_destroy(b);
+    return nullptr;
+  }
+  return b;
+}
+
+void mixed_batch_enqueue(const MixedBatch* b, cudaStream_t s) {
+  for (const auto& L : b->seq) {
+    switch (L.kind) {
+      case 0:
+        if (L.raw)
+          k_b_stage<true><<<L.blocks, dim3(TX, TY), 0, s>>>((const StageArgs*)L.args, L.start, L.nd, b->err);
+        else
+          k_b_stage<false><<<L.blocks, dim3(TX, TY), 0, s>>>((const StageArgs*)L.args, L.start, L.nd, b->err);
+        break;
+      case 1:
+        k_b_hevi<<<L.blocks, dim3(32, 4), b->hevi_smem, s>>>((const HeviArgs*)L.args, L.start, L.nd);
+        break;
+      case 2:
+        k_b_uv<<<L.blocks, dim3(32, 4), 0, s>>>((const UvArgs*)L.args, L.start, L.nd);
+        break;
+      default:
+        k_b_finish<<<L.blocks, dim3(32, 4), 0, s>>>((const FinishArgs*)L.args, L.start, L.nd, b->err);
+        break;
+    }
+  }
+}
+
+int mixed_batch_launches(const MixedBatch* b) { return (int)b->seq.size(); }
+
+void mixed_batch_destroy(MixedBatch* b) {
+  if (!b) return;
+  for (void* p : b->allocs) cudaFree(p);
+  delete b;
 }
 
 }  // namespace vgb

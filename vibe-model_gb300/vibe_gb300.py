@@ -617,3 +617,45 @@ class TLAD:
 
     def ad_step(self, dt, dy):
         return self.ad_propagate(dt, 1, dy)
+
+
+# ---- groups of models advanced together (include/vibe_gb300.h) --------------
+for _name, _res, _args in (("vibe_gb300_group_create", _I, [ctypes.POINTER(_vp), _I, ctypes.POINTER(_vp)]),
+                           ("vibe_gb300_group_destroy", None, [_vp]),
+                           ("vibe_gb300_group_step", _I, [_vp, _D, _I, _I]),
+                           ("vibe_gb300_group_launches_per_step", _I, [_vp]),
+                           ("vibe_gb300_group_stream", _vp, [_vp])):
+    _f = getattr(lib, _name)
+    _f.restype = _res
+    _f.argtypes = _args
+
+
+class Group:
+    """Several mixed-precision models stepped with one launch per kernel for
+    all of them (the batched ensemble / nest step)."""
+
+    def __init__(self, models):
+        self.models = list(models)
+        arr = (_vp * len(self.models))(*[m.h for m in self.models])
+        self.h = _vp()
+        _check(lib.vibe_gb300_group_create(arr, len(self.models), ctypes.byref(self.h)))
+
+    def step(self, dt, n_sub, n_steps=1):
+        _check(lib.vibe_gb300_group_step(self.h, dt, n_sub, n_steps))
+
+    def launches_per_step(self):
+        return int(lib.vibe_gb300_group_launches_per_step(self.h))
+
+    def stream(self):
+        return lib.vibe_gb300_group_stream(self.h)
+
+    def close(self):
+        if self.h:
+            lib.vibe_gb300_group_destroy(self.h)
+            self.h = _vp()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
