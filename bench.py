@@ -101,6 +101,86 @@ def si_leg(vg, steps=3):
     return out
 
 
+# Batched nests: 8 members, each a 384 x 384 x 60 parent at 3 km with two
+# r = 3 two-way nests at 1 km (193 x 193 x 60 and 130 x 241 x 60), Davies
+# zone 5 points; 60 levels stretched from a 50 m first layer to the 20 km top
+# (ratio 1.0530384502435775); the single-domain base state (theta0 = 300 K,
+# N = 0.01 1/s, u = 10 m/s); members differ by seeded theta' ~ N(0, 0.3 K)
+# and u' ~ N(0, 0.5 m/s). Parent dt = 18 s, nest dt = 6 s, 6 substeps per stage.
+NEST_NZ, NEST_STRETCH, NEST_DT, NEST_MEMBERS = 60, 1.0530384502435775, 18.0, 8
+NEST_PARENT = (384, 384, 3000.0)
+NEST_CHILDREN = [  # (nx, ny, interp (i0, j0) in nest points, restrict box (i0, j0, iext, jext) in parent points)
+    (193, 193, (180, 180), (60, 60, 64, 64)),
+    (130, 241, (660, 600), (220, 200, 43, 80)),
+]
+
+
+def nest_leg(vg, torch, steps, warmup):
+    """One parent step of all 8 members with their nests = one CUDA graph
+    (parents of all members in one work-list launch per kernel, nests of all
+    members in another, transfers between)."""
+    case = dict(CASE, nz=NEST_NZ, zeta_stretch=NEST_STRETCH)
+    base = {k: v for k, v in case.items() if k not in ("dx", "dy")}
+    ps = vg.Setup.defaults(nx=NEST_PARENT[0], ny=NEST_PARENT[1], dx=NEST_PARENT[2], dy=NEST_PARENT[2], **base)
+    cs = [vg.Setup.defaults(nx=nx, ny=ny, dx=1000.0, dy=1000.0, **base) for nx, ny, _, _ in NEST_CHILDREN]
+    pl_i, pl_r = [], []
+    for nx, ny, (ii, jj), (ri, rj, re, rf) in NEST_CHILDREN:
+        a, b = vg.NestPlacement(), vg.NestPlacement()
+        a.i0, a.j0, a.ratio, a.boundary_zone, a.two_way = ii, jj, 3, 5, 1
+        b.i0, b.j0, b.iext, b.jext, b.ratio, b.boundary_zone, b.two_way = ri, rj, re, rf, 3, 5, 1
+        pl_i.append(a)
+        pl_r.append(b)
+    parents, children, parent_of, ip, rp = [], [], [], [], []
+    staggers = [1, 2, 3, 0, 0, 0, 0]
+    for mbr in range(NEST_MEMBERS):
+        rng = np.random.default_rng(100 + mbr)
+        p = vg.Model(ps, vg.MIXED)
+        th, u, rho = p.get(4), p.get(0), p.get(3)
+        th = th + np.where(th != 0.0, rng.normal(0.0, 0.3, th.size), 0.0)
+        u = u + np.where(u != 0.0, rng.normal(0.0, 0.5, u.size), 0.0)
+        # pi from the equation of state (dry), as the single-domain set-up
+        pi = np.where(rho != 0.0, np.power(np.maximum(rho * 287.05 * th / 100000.0, 0.0), 287.05 / 717.63), 0.0)
+        p.set(4, th)
+        p.set(0, u)
+        p.set(5, pi)
+        parents.append(p)
+        pst = [p.get(q) for q in range(7)]
+        for c, s in enumerate(cs):
+            m = vg.Model(s, vg.MIXED)
+            cst = [m.get(q) for q in range(7)]
+            vg.nest_interpolate_from_parent(pl_i[c], staggers, (ps.nx, ps.ny, ps.nz), pst, (s.nx, s.ny, s.nz),
+                                            cst)
+            for q in range(7):
+                m.set(q, cst[q])
+            children.append(m)
+            parent_of.append(mbr)
+            ip.append(pl_i[c])
+            rp.append(pl_r[c])
+    cells = NEST_MEMBERS * (ps.nx * ps.ny * NEST_NZ + 3 * sum(s.nx * s.ny * NEST_NZ for s in cs))
+    n = vg.Nested(parents, children, parent_of, ip, rp)
+    try:
+        n.step(NEST_DT, NSUB, warmup)
+        ext = torch.cuda.ExternalStream(n.stream())
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(ext)
+        n.step_async(NEST_DT, NSUB, steps)
+        e1.record(ext)
+        n.wait()
+        ms = e0.elapsed_time(e1)
+        launches = n.launches_per_step()
+    finally:
+        n.close()
+        for m in parents + children:
+            m.close()
+    return {"workload": "8 members x (384x384x60 parent at 3 km + r=3 two-way nests 193x193x60 and 130x241x60 at "
+                        "1 km, Davies zone 5), theta'~N(0,0.3 K), u'~N(0,0.5 m/s); parent dt=18 s, nest dt=6 s, "
+                        "6 HEVI substeps per stage; one CUDA graph per parent step",
+            "cell_updates_per_parent_step": cells, "parent_steps": steps, "ms_per_parent_step": ms / steps,
+            "value": cells * steps / (ms * 1e-3), "unit": UNIT, "gpu_launches_per_parent_step": launches,
+            "hevi_columns_per_parent_launch": NEST_MEMBERS * ps.nx * ps.ny}
+
+
 def perturbed_state(setup, theta, rho, zeta, seed=1, nx_full=NX, ny_full=NY, x_off=0, y_off=0):
     """theta/pi storage arrays with the seeded perturbations (numpy set-up)."""
     rng = np.random.default_rng(seed)
@@ -274,6 +354,7 @@ def main():
     ap.add_argument("--nx", type=int, default=NX, help="domain size (profiling runs use smaller cases)")
     ap.add_argument("--ny", type=int, default=NY)
     ap.add_argument("--no-si", action="store_true", help="skip the semi-implicit (Helmholtz) leg")
+    ap.add_argument("--no-nest", action="store_true", help="skip the batched nests leg")
     ap.add_argument("--only", choices=["all", "mixed"], default="all",
                     help="mixed: time the mixed path only (no e2e, no FP64 leg)")
     args = ap.parse_args()
@@ -385,6 +466,7 @@ def main():
     f64.close()
 
     si = si_leg(vg) if not args.no_si else None
+    nest = nest_leg(vg, torch, max(2, args.steps // 4), args.warmup) if not args.no_nest else None
 
     value = world * cells * args.steps / (ms_mx * 1e-3)
     value64 = world * cells * k64 / (ms_64 * 1e-3)
@@ -429,6 +511,8 @@ def main():
     }
     if si is not None:
         line["semi_implicit"] = si
+    if nest is not None:
+        line["batched_nests"] = nest
     if cpu is not None:
         line["cpu_baseline"] = cpu
     print(json.dumps(line))

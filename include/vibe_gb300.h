@@ -155,6 +155,34 @@ int vibe_gb300_group_step(vibe_gb300_group *g, double dt, int n_sub, int n_steps
 int vibe_gb300_group_launches_per_step(const vibe_gb300_group *g);
 vibe_stream_t vibe_gb300_group_stream(vibe_gb300_group *g);
 
+/* Nested sets (two-way nests with time sub-cycling, O-NEST): the parents
+ * step with dt as one group, then every nest gets its parent's state
+ * interpolated into a boundary buffer (Nest::interpolate_from_parent,
+ * nest.cpp:58-84, with interp_pl[c]), the nests take r = ratio sub-steps of
+ * dt/r as one group, each followed by the Davies relaxation towards that
+ * buffer (apply_lateral_boundary, nest.cpp:107-124), and finally each nest
+ * is restricted onto its parent (restrict_to_parent, nest.cpp:86-105, with
+ * restrict_pl[c]). The reference's interpolation takes the nest offset in
+ * child points and its restriction in parent points, hence two placements.
+ * Fields transferred: u v w rho theta pi qv (+ the moisture species when
+ * moist). Models are not owned. */
+struct vibe_nest_placement;
+typedef struct vibe_gb300_nested vibe_gb300_nested;
+int vibe_gb300_nested_create(vibe_gb300_model *const *parents, int n_parents, vibe_gb300_model *const *children,
+                             int n_children, const int *parent_of, const struct vibe_nest_placement *interp_pl,
+                             const struct vibe_nest_placement *restrict_pl, vibe_gb300_nested **out);
+void vibe_gb300_nested_destroy(vibe_gb300_nested *n);
+/* One parent step is one CUDA graph on the set's stream (captured once per
+ * pair of state parities). nested_step = nested_launch (enqueue, returns at
+ * once) + nested_wait (synchronise, then report a non-finite state or a
+ * device wait that gave up). */
+int vibe_gb300_nested_step(vibe_gb300_nested *n, double dt, int n_sub, int n_steps);
+int vibe_gb300_nested_launch(vibe_gb300_nested *n, double dt, int n_sub, int n_steps);
+int vibe_gb300_nested_wait(vibe_gb300_nested *n);
+/* kernel launches of one parent step (after the first launch) */
+int vibe_gb300_nested_launches_per_step(const vibe_gb300_nested *n);
+vibe_stream_t vibe_gb300_nested_stream(vibe_gb300_nested *n);
+
 /* Kernel-level entry points (FP64 path only for the tendency). */
 int vibe_gb300_slow_tendency(vibe_gb300_model *m, double *const *host_out);
 int vibe_gb300_acoustic_substep(vibe_gb300_model *m, double dtau);

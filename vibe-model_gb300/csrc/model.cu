@@ -14,6 +14,7 @@
 #include "step_kernels.cuh"
 #include "vibe_gb300.h"
 #include "vibe_helmholtz.h"
+#include "vibe_nest.h"
 
 using namespace vgb;
 
@@ -1207,42 +1208,65 @@ void vibe_gb300_group_destroy(vibe_gb300_group* g) {
   delete g;
 }
 
-int vibe_gb300_group_step(vibe_gb300_group* g, double dt, int n_sub_in, int n_steps) {
-  if (!g || !(dt > 0.0) || n_steps < 0) return fail(VIBE_GB300_EBADARG, "bad argument");
-  const int n_sub = n_sub_in > 1 ? n_sub_in : 1;
+}  // extern "C"
+
+namespace {
+// (re)build the work lists of a group for (dt, n_sub); members idle
+int group_prepare(vibe_gb300_group* g, double dt, int n_sub) {
   const int parity0 = g->ms[0]->cur;
   for (auto* m : g->ms) {
     if (m->cur != parity0) return fail(VIBE_GB300_EUNSUPPORTED, "group members must share the state parity");
     CUDA_OK(cudaStreamSynchronize(m->stream));  // nothing of theirs in flight
   }
-  if (g->dt != dt || g->nsub != n_sub) {
-    CUDA_OK(cudaStreamSynchronize(g->stream));
-    group_drop(g);
-    for (auto* m : g->ms)
-      if (int rc = configure_dt(m, dt, n_sub)) return rc;
-    for (int p = 0; p < 2; ++p) {
-      std::vector<MixedDomain> doms;
-      for (auto* m : g->ms) {
-        MixedDomain md;
-        md.d = m->d;
-        md.t = m->tab;
-        md.lu = m->d_lu;
-        md.W0 = m->W0;
-        md.WSt0 = m->WSt[0];
-        md.WSt1 = m->WSt[1];
-        md.WA = m->WA;
-        md.WB = m->WB;
-        md.WR = m->WR;
-        md.S0 = m->S[p];
-        md.S1 = m->S[1 - p];
-        doms.push_back(md);
-      }
-      g->batch[p] = mixed_batch_build(doms, g->ms[0]->fl, dt, n_sub, g->d_err);
-      if (!g->batch[p]) return fail(VIBE_GB300_EDEVICE, "group launch set-up failed");
+  if (g->dt == dt && g->nsub == n_sub) return 0;
+  CUDA_OK(cudaStreamSynchronize(g->stream));
+  group_drop(g);
+  for (auto* m : g->ms)
+    if (int rc = configure_dt(m, dt, n_sub)) return rc;
+  for (int p = 0; p < 2; ++p) {
+    std::vector<MixedDomain> doms;
+    for (auto* m : g->ms) {
+      MixedDomain md;
+      md.d = m->d;
+      md.t = m->tab;
+      md.lu = m->d_lu;
+      md.W0 = m->W0;
+      md.WSt0 = m->WSt[0];
+      md.WSt1 = m->WSt[1];
+      md.WA = m->WA;
+      md.WB = m->WB;
+      md.WR = m->WR;
+      md.S0 = m->S[p];
+      md.S1 = m->S[1 - p];
+      doms.push_back(md);
     }
-    g->dt = dt;
-    g->nsub = n_sub;
+    g->batch[p] = mixed_batch_build(doms, g->ms[0]->fl, dt, n_sub, g->d_err);
+    if (!g->batch[p]) return fail(VIBE_GB300_EDEVICE, "group launch set-up failed");
   }
+  g->dt = dt;
+  g->nsub = n_sub;
+  return 0;
+}
+
+// wait for the group's stream, then read and clear its error word
+int group_check(vibe_gb300_group* g) {
+  CUDA_OK(cudaMemcpyAsync(g->h_err, g->d_err, sizeof(unsigned), cudaMemcpyDeviceToHost, g->stream));
+  CUDA_OK(cudaStreamSynchronize(g->stream));
+  const unsigned e = *g->h_err;
+  CUDA_OK(cudaMemsetAsync(g->d_err, 0, sizeof(unsigned), g->stream));
+  CUDA_OK(cudaStreamSynchronize(g->stream));
+  if (e & kErrWaitTimeout) return fail(VIBE_GB300_EDEVICE, "a TMA box of the stage kernel did not arrive (bounded wait)");
+  if (e & kErrNonFinite) return fail(VIBE_GB300_ENONFINITE, "non-finite value in a group member's state");
+  return 0;
+}
+}  // namespace
+
+extern "C" {
+
+int vibe_gb300_group_step(vibe_gb300_group* g, double dt, int n_sub_in, int n_steps) {
+  if (!g || !(dt > 0.0) || n_steps < 0) return fail(VIBE_GB300_EBADARG, "bad argument");
+  const int n_sub = n_sub_in > 1 ? n_sub_in : 1;
+  if (int rc = group_prepare(g, dt, n_sub)) return rc;
   for (int step = 0; step < n_steps; ++step) {
     const int p = g->ms[0]->cur;
     if (!g->g[p]) {
@@ -1258,13 +1282,7 @@ int vibe_gb300_group_step(vibe_gb300_group* g, double dt, int n_sub_in, int n_st
     CUDA_OK(cudaGraphLaunch(g->g[p], g->stream));
     for (auto* m : g->ms) m->cur = 1 - m->cur;
   }
-  CUDA_OK(cudaMemcpyAsync(g->h_err, g->d_err, sizeof(unsigned), cudaMemcpyDeviceToHost, g->stream));
-  CUDA_OK(cudaStreamSynchronize(g->stream));
-  const unsigned e = *g->h_err;
-  CUDA_OK(cudaMemsetAsync(g->d_err, 0, sizeof(unsigned), g->stream));
-  if (e & kErrWaitTimeout) return fail(VIBE_GB300_EDEVICE, "a TMA box of the stage kernel did not arrive (bounded wait)");
-  if (e & kErrNonFinite) return fail(VIBE_GB300_ENONFINITE, "non-finite value in a group member's state");
-  return 0;
+  return group_check(g);
 }
 
 int vibe_gb300_group_launches_per_step(const vibe_gb300_group* g) {
@@ -1272,6 +1290,215 @@ int vibe_gb300_group_launches_per_step(const vibe_gb300_group* g) {
 }
 
 vibe_stream_t vibe_gb300_group_stream(vibe_gb300_group* g) { return g ? (vibe_stream_t)g->stream : nullptr; }
+
+// ---- nested sets: parents advanced by one group with dt, their two-way
+// nests by another group with r sub-steps of dt/r (the parent step; the
+// parent state interpolated into a boundary buffer of every nest
+// (Nest::interpolate_from_parent); r nest sub-steps, each followed by the
+// Davies relaxation towards that buffer (apply_lateral_boundary); the nests
+// restricted back onto their parents (restrict_to_parent, two-way)). One
+// parent step is one CUDA graph, captured once per pair of state parities.
+}  // extern "C"
+
+struct vibe_gb300_nested {
+  std::vector<vibe_gb300_model*> parents, children;
+  std::vector<int> parent_of;
+  std::vector<vibe_nest_placement> pl_interp, pl_restrict;
+  vibe_gb300_group* gp = nullptr;
+  vibe_gb300_group* gc = nullptr;
+  std::vector<std::vector<double*>> buf;  // per nest: boundary buffer (FP64, model layout)
+  std::vector<void*> allocs;
+  cudaStream_t stream = nullptr;
+  cudaGraphExec_t graph[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};  // [parent parity][nest parity]
+  int nvars = 7;
+  int launches = 0;
+};
+
+namespace {
+// op 0: parent S[pp] -> boundary buffer; 1: nest S[cp] -> parent S[pp];
+// 2: Davies blend of nest S[cp] with the buffer
+int nested_transfer(vibe_gb300_nested* n, int op, int c, int pp, int cp) {
+  vibe_gb300_model* ch = n->children[c];
+  vibe_gb300_model* pa = n->parents[n->parent_of[c]];
+  const vibe_nest_placement* pl = (op == 1) ? &n->pl_restrict[c] : &n->pl_interp[c];
+  const double* pin[NSPECIES];
+  double* pout[NSPECIES];
+  const double* cin[NSPECIES];
+  double* cout[NSPECIES];
+  for (int q = 0; q < n->nvars; ++q) {
+    pin[q] = pa->S[pp][q];
+    pout[q] = pa->S[pp][q];
+    cin[q] = (op == 2) ? n->buf[c][q] : ch->S[cp][q];
+    cout[q] = (op == 0) ? n->buf[c][q] : ch->S[cp][q];
+  }
+  const int rc = nest_model_layout(op, pl, n->nvars, pa->d.nx, pa->d.ny, pa->d.nz, pin, pa->d.P, pa->d.plane,
+                                   ch->d.nx, ch->d.ny, ch->d.nz, cin, op == 1 ? pout : cout, ch->d.P, ch->d.plane,
+                                   n->stream);
+  ++n->launches;
+  return rc == VIBE_C_OK ? 0 : fail(VIBE_GB300_EDEVICE, "nest transfer failed");
+}
+
+void to_working_on(vibe_gb300_nested* n, vibe_gb300_model* m, int parity) {
+  mixed_to_working(m->d, m->tab, m->S[parity], ws_of(m->W0), n->stream);
+  ++n->launches;
+}
+
+// one parent step from parities (pp, cp), enqueued on the nested stream
+int nested_enqueue(vibe_gb300_nested* n, int pp, int cp, int r) {
+  n->launches = mixed_batch_launches(n->gp->batch[pp]) + r * mixed_batch_launches(n->gc->batch[0]);
+  mixed_batch_enqueue(n->gp->batch[pp], n->stream);
+  const int pn = 1 - pp;
+  const int nc = (int)n->children.size();
+  for (int c = 0; c < nc; ++c)
+    if (int rc = nested_transfer(n, 0, c, pn, cp)) return rc;
+  int cc = cp;
+  for (int sub = 0; sub < r; ++sub) {
+    mixed_batch_enqueue(n->gc->batch[cc], n->stream);
+    cc = 1 - cc;
+    for (int c = 0; c < nc; ++c) {
+      if (int rc = nested_transfer(n, 2, c, pn, cc)) return rc;
+      to_working_on(n, n->children[c], cc);
+    }
+  }
+  for (int c = 0; c < nc; ++c)
+    if (int rc = nested_transfer(n, 1, c, pn, cc)) return rc;
+  for (auto* p : n->parents) to_working_on(n, p, pn);
+  return 0;
+}
+
+void nested_drop(vibe_gb300_nested* n) {
+  for (auto& row : n->graph)
+    for (auto& g : row) {
+      if (g) cudaGraphExecDestroy(g);
+      g = nullptr;
+    }
+}
+}  // namespace
+
+extern "C" {
+
+int vibe_gb300_nested_create(vibe_gb300_model* const* parents, int np, vibe_gb300_model* const* children, int nc,
+                             const int* parent_of, const vibe_nest_placement* interp_pl,
+                             const vibe_nest_placement* restrict_pl, vibe_gb300_nested** out) {
+  if (!parents || np < 1 || !children || nc < 1 || !parent_of || !interp_pl || !restrict_pl || !out)
+    return fail(VIBE_GB300_EBADARG, "bad argument");
+  for (int c = 0; c < nc; ++c) {
+    if (parent_of[c] < 0 || parent_of[c] >= np) return fail(VIBE_GB300_EBADARG, "parent index out of range");
+    if (interp_pl[c].ratio != interp_pl[0].ratio || restrict_pl[c].ratio != interp_pl[0].ratio || interp_pl[0].ratio < 2)
+      return fail(VIBE_GB300_EBADARG, "every nest needs the same ratio r >= 2 (time sub-cycling)");
+    const vibe_gb300_model* pa = parents[parent_of[c]];
+    if (children[c]->d.nz != pa->d.nz) return fail(VIBE_GB300_EBADARG, "nests share their parent's levels");
+    const vibe_nest_placement& q = restrict_pl[c];
+    if (q.i0 < 0 || q.j0 < 0 || q.iext < 0 || q.jext < 0 || q.i0 + q.iext > pa->d.nx + 1 ||
+        q.j0 + q.jext > pa->d.ny + 1)
+      return fail(VIBE_GB300_EBADARG, "restriction box outside the parent");
+    if (interp_pl[c].boundary_zone < 1 || interp_pl[c].boundary_zone > 64)
+      return fail(VIBE_GB300_EBADARG, "boundary zone must be 1..64 points");
+    if (children[c]->precision != VIBE_GB300_MIXED || pa->precision != VIBE_GB300_MIXED)
+      return fail(VIBE_GB300_EBADARG, "nested sets step mixed-precision models");
+  }
+  auto* n = new vibe_gb300_nested();
+  n->parents.assign(parents, parents + np);
+  n->children.assign(children, children + nc);
+  n->parent_of.assign(parent_of, parent_of + nc);
+  n->pl_interp.assign(interp_pl, interp_pl + nc);
+  n->pl_restrict.assign(restrict_pl, restrict_pl + nc);
+  n->nvars = parents[0]->fl.moist ? NSPECIES : QV + 1;
+  int rc = vibe_gb300_group_create(parents, np, &n->gp);
+  rc = rc ? rc : vibe_gb300_group_create(children, nc, &n->gc);
+  if (!rc && cudaStreamCreateWithFlags(&n->stream, cudaStreamNonBlocking) != cudaSuccess)
+    rc = fail(VIBE_GB300_EDEVICE, "stream");
+  for (int c = 0; c < nc && !rc; ++c) {
+    std::vector<double*> b(NSPECIES, nullptr);
+    const size_t cnt = children[c]->d.plane * (size_t)(children[c]->d.nz + 1);
+    for (int q = 0; q < n->nvars && !rc; ++q) {
+      void* p = nullptr;
+      if (cudaMalloc(&p, cnt * sizeof(double)) != cudaSuccess) {
+        rc = fail(VIBE_GB300_EDEVICE, "buffer allocation");
+      } else {
+        n->allocs.push_back(p);
+        b[q] = (double*)p;
+        if (cudaMemset(p, 0, cnt * sizeof(double)) != cudaSuccess) rc = fail(VIBE_GB300_EDEVICE, "memset");
+      }
+    }
+    n->buf.push_back(b);
+  }
+  if (rc) {
+    vibe_gb300_nested_destroy(n);
+    return rc;
+  }
+  *out = n;
+  return 0;
+}
+
+void vibe_gb300_nested_destroy(vibe_gb300_nested* n) {
+  if (!n) return;
+  if (n->stream) cudaStreamSynchronize(n->stream);
+  nested_drop(n);
+  vibe_gb300_group_destroy(n->gp);
+  vibe_gb300_group_destroy(n->gc);
+  for (void* p : n->allocs) cudaFree(p);
+  if (n->stream) cudaStreamDestroy(n->stream);
+  delete n;
+}
+
+int vibe_gb300_nested_launch(vibe_gb300_nested* n, double dt, int n_sub_in, int n_steps) {
+  if (!n || !(dt > 0.0) || n_steps < 0) return fail(VIBE_GB300_EBADARG, "bad argument");
+  const int n_sub = n_sub_in > 1 ? n_sub_in : 1;
+  const int r = n->pl_interp[0].ratio;
+  const double dtc = dt / r;
+  const bool rebuild = n->gp->dt != dt || n->gp->nsub != n_sub || n->gc->dt != dtc || n->gc->nsub != n_sub;
+  if (rebuild) {
+    CUDA_OK(cudaStreamSynchronize(n->stream));
+    nested_drop(n);
+  }
+  if (int rc = group_prepare(n->gp, dt, n_sub)) return rc;
+  if (int rc = group_prepare(n->gc, dtc, n_sub)) return rc;
+  for (int step = 0; step < n_steps; ++step) {
+    const int pp = n->parents[0]->cur, cp = n->children[0]->cur;
+    for (auto* m : n->parents)
+      if (m->cur != pp) return fail(VIBE_GB300_EUNSUPPORTED, "parents must share the state parity");
+    for (auto* m : n->children)
+      if (m->cur != cp) return fail(VIBE_GB300_EUNSUPPORTED, "nests must share the state parity");
+    if (!n->graph[pp][cp]) {
+      cudaGraph_t gr = nullptr;
+      CUDA_OK(cudaStreamBeginCapture(n->stream, cudaStreamCaptureModeThreadLocal));
+      const int erc = nested_enqueue(n, pp, cp, r);
+      const cudaError_t e = cudaStreamEndCapture(n->stream, &gr);
+      if (erc) {
+        if (gr) cudaGraphDestroy(gr);
+        return erc;
+      }
+      CUDA_OK(e);
+      const cudaError_t ei = cudaGraphInstantiate(&n->graph[pp][cp], gr, 0);
+      cudaGraphDestroy(gr);
+      CUDA_OK(ei);
+    }
+    CUDA_OK(cudaGraphLaunch(n->graph[pp][cp], n->stream));
+    for (auto* m : n->parents) m->cur = 1 - m->cur;
+    for (auto* m : n->children)
+      if (r & 1) m->cur = 1 - m->cur;
+  }
+  CUDA_OK(cudaGetLastError());
+  return 0;
+}
+
+int vibe_gb300_nested_wait(vibe_gb300_nested* n) {
+  if (!n) return fail(VIBE_GB300_EBADARG, "bad argument");
+  CUDA_OK(cudaStreamSynchronize(n->stream));
+  const int rp = group_check(n->gp);
+  const int rc = group_check(n->gc);
+  return rp ? rp : rc;
+}
+
+int vibe_gb300_nested_step(vibe_gb300_nested* n, double dt, int n_sub, int n_steps) {
+  if (int rc = vibe_gb300_nested_launch(n, dt, n_sub, n_steps)) return rc;
+  return vibe_gb300_nested_wait(n);
+}
+
+int vibe_gb300_nested_launches_per_step(const vibe_gb300_nested* n) { return n ? n->launches : 0; }
+
+vibe_stream_t vibe_gb300_nested_stream(vibe_gb300_nested* n) { return n ? (vibe_stream_t)n->stream : nullptr; }
 
 int vibe_gb300_set_state(vibe_gb300_model* m, const double* const* host, int nspecies) {
   if (!m || !host || nspecies < 1 || nspecies > NSPECIES) return fail(VIBE_GB300_EBADARG, "bad argument");

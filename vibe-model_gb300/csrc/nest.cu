@@ -238,6 +238,57 @@ int run_host(Op op, const vibe_nest_placement* p, int nvars, const int* stagger,
 }
 
 }  // namespace
+
+// The same transfers on fields in the model's device layout (element (i,j,k)
+// at k*plane + j*pitch + i, no halo): op 0 interpolate parent -> child,
+// 1 restrict child -> parent, 2 Davies blend of child with child_in. The
+// restriction box must lie inside the parent's interior plus its extra face.
+int nest_model_layout(int op, const vibe_nest_placement* p, int nvars, int pnx, int pny, int pnz,
+                      const double* const* parent, size_t p_pitch, size_t p_plane, int cnx, int cny, int cnz,
+                      const double* const* child_in, double* const* out, size_t c_pitch, size_t c_plane,
+                      cudaStream_t s) {
+  if (!check_placement(p)) return VIBE_C_ERR_BAD_ARG;
+  if (op == 1 && (p->i0 < 0 || p->j0 < 0 || p->i0 + p->iext > pnx + 1 || p->j0 + p->jext > pny + 1)) {
+    g_nerr = "restriction box outside the parent";
+    return VIBE_C_ERR_BAD_ARG;
+  }
+  NestArgs a = args_of(p, pnx, pny, pnz, cnx, cny, cnz);
+  auto view = [](NestViews& v, int q, const double* ptr, size_t pitch, size_t plane) {
+    v.p[q] = const_cast<double*>(ptr);
+    v.sj[q] = (int)pitch;
+    v.sk[q] = (long long)plane;
+    v.off[q] = 0;
+  };
+  for (int v0 = 0; v0 < nvars; v0 += kNestVars) {
+    NestViews A{}, B{};
+    const int nv = imin(kNestVars, nvars - v0);
+    a.nvars = nv;
+    for (int q = 0; q < nv; ++q) {
+      if (op == 0) {
+        view(A, q, parent[v0 + q], p_pitch, p_plane);
+        view(B, q, out[v0 + q], c_pitch, c_plane);
+      } else if (op == 1) {
+        view(A, q, child_in[v0 + q], c_pitch, c_plane);
+        view(B, q, out[v0 + q], p_pitch, p_plane);
+      } else {
+        view(A, q, out[v0 + q], c_pitch, c_plane);
+        view(B, q, child_in[v0 + q], c_pitch, c_plane);
+      }
+    }
+    const dim3 b(32, 8);
+    if (op == 0)
+      k_interp<<<dim3((cnx + 31) / 32, (cny + 7) / 8, cnz), b, 0, s>>>(a, A, B);
+    else if (op == 1) {
+      if (p->iext > 0 && p->jext > 0)
+        k_restrict<<<dim3((p->iext + 31) / 32, (p->jext + 7) / 8, pnz), b, 0, s>>>(a, A, B);
+    } else
+      k_lateral<<<dim3((cnx + 31) / 32, (cny + 7) / 8, cnz), b, 0, s>>>(a, A, B);
+  }
+  return cudaGetLastError() == cudaSuccess ? VIBE_C_OK : VIBE_C_ERR_DEVICE;
+}
+
+namespace {
+}  // namespace
 }  // namespace vgb
 
 using namespace vgb;

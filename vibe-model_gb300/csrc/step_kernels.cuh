@@ -46,6 +46,16 @@ void si_to_cells(const Dims& d, const double* in, double* out, cudaStream_t s);
 void diag_cfl(const Dims& d, const Metric& met, double* const* st, double dt, double dtau, unsigned long long* out,
               cudaStream_t s);
 
+// ---- nest transfers on model-layout fields (nest.cu): op 0 interpolate,
+// 1 restrict, 2 Davies blend (see include/vibe_nest.h) ----
+}  // namespace vgb
+struct vibe_nest_placement;
+namespace vgb {
+int nest_model_layout(int op, const vibe_nest_placement* p, int nvars, int pnx, int pny, int pnz,
+                      const double* const* parent, size_t p_pitch, size_t p_plane, int cnx, int cny, int cnz,
+                      const double* const* child_in, double* const* out, size_t c_pitch, size_t c_plane,
+                      cudaStream_t s);
+
 // ---- mixed path (step_mixed.cu): FP64 state, FP32 working state ----
 // Horizontally uniform reference state on flat terrain: every coefficient
 // is a function of k only and lives in these FP32 tables (device).

@@ -659,3 +659,62 @@ class Group:
 
     def __exit__(self, *a):
         self.close()
+
+
+# ---- nested sets: parents with two-way nests (include/vibe_gb300.h) ---------
+for _name, _res, _args in (("vibe_gb300_nested_create", _I, [ctypes.POINTER(_vp), _I, ctypes.POINTER(_vp), _I,
+                                                              ctypes.POINTER(_I), ctypes.POINTER(NestPlacement),
+                                                              ctypes.POINTER(NestPlacement), ctypes.POINTER(_vp)]),
+                           ("vibe_gb300_nested_destroy", None, [_vp]),
+                           ("vibe_gb300_nested_step", _I, [_vp, _D, _I, _I]),
+                           ("vibe_gb300_nested_launch", _I, [_vp, _D, _I, _I]),
+                           ("vibe_gb300_nested_wait", _I, [_vp]),
+                           ("vibe_gb300_nested_launches_per_step", _I, [_vp]),
+                           ("vibe_gb300_nested_stream", _vp, [_vp])):
+    _f = getattr(lib, _name)
+    _f.restype = _res
+    _f.argtypes = _args
+
+
+class Nested:
+    """Parents stepped with dt and their two-way nests with ratio sub-steps
+    of dt/ratio, coupled by interpolation, Davies relaxation and
+    restriction. interp_pl / restrict_pl: one NestPlacement per nest, the
+    first with its offset in nest points, the second in parent points."""
+
+    def __init__(self, parents, children, parent_of, interp_pl, restrict_pl):
+        self.parents, self.children = list(parents), list(children)
+        pa = (_vp * len(self.parents))(*[m.h for m in self.parents])
+        ch = (_vp * len(self.children))(*[m.h for m in self.children])
+        po = (_I * len(self.children))(*parent_of)
+        ip = (NestPlacement * len(self.children))(*interp_pl)
+        rp = (NestPlacement * len(self.children))(*restrict_pl)
+        self.h = _vp()
+        _check(lib.vibe_gb300_nested_create(pa, len(self.parents), ch, len(self.children), po, ip, rp,
+                                            ctypes.byref(self.h)))
+
+    def step(self, dt, n_sub, n_steps=1):
+        _check(lib.vibe_gb300_nested_step(self.h, dt, n_sub, n_steps))
+
+    def step_async(self, dt, n_sub, n_steps=1):
+        _check(lib.vibe_gb300_nested_launch(self.h, dt, n_sub, n_steps))
+
+    def wait(self):
+        _check(lib.vibe_gb300_nested_wait(self.h))
+
+    def launches_per_step(self):
+        return int(lib.vibe_gb300_nested_launches_per_step(self.h))
+
+    def stream(self):
+        return lib.vibe_gb300_nested_stream(self.h)
+
+    def close(self):
+        if self.h:
+            lib.vibe_gb300_nested_destroy(self.h)
+            self.h = _vp()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
