@@ -187,6 +187,12 @@ vibe_stream_t vibe_gb300_nested_stream(vibe_gb300_nested *n);
 int vibe_gb300_slow_tendency(vibe_gb300_model *m, double *const *host_out);
 int vibe_gb300_acoustic_substep(vibe_gb300_model *m, double dtau);
 int vibe_gb300_hevi_substep(vibe_gb300_model *m, double dtau);
+/* Device-side copy of the prognostic state: op 0 saves the current state
+ * (all species, model layout) into a snapshot held by the model, op 1 puts
+ * it back (and refreshes the FP32 working copy). Asynchronous on the model's
+ * stream; no host memory is touched. Used for restarts of a run from a
+ * checkpoint and for trajectory checkpoints. */
+int vibe_gb300_snapshot(vibe_gb300_model *m, int op);
 int vibe_gb300_sponge(vibe_gb300_model *m, double dt);
 
 /* One semi-implicit step, replacing SemiImplicitIntegrator::step

@@ -347,3 +347,19 @@ def test_cfl_diagnostics_bit_exact(vg, oc, prec):
         o.set_state(m.state())  # same state on both sides
         assert m.cfl(2.0, 0.3) == oc.cfl(o, 2.0, 0.3)
         assert m.max_stable_dt() == oc.max_stable_dt(o)
+
+
+def test_snapshot_restart_is_bitwise(vg):
+    """A run restarted from the device snapshot repeats itself bit for bit."""
+    s = small_setup(vg, acoustic_mode=2, ref_kind=1, pgf_perturbation=1, split_fast=1)
+    for prec in (vg.MIXED, vg.FP64):
+        with vg.Model(s, prec) as m:
+            m.save_snapshot()
+            m.step(2.0, 4, 3)
+            first = m.state()
+            m.restore_snapshot()
+            m.step(2.0, 4, 3)
+            for sp, (a, b) in enumerate(zip(first, m.state())):
+                assert np.array_equal(a, b), vg.SPECIES[sp]
+        with vg.Model(s, prec) as m, pytest.raises(vg.VibeError):
+            m.restore_snapshot()

@@ -119,6 +119,9 @@ struct vibe_gb300_model {
   cudaGraphExec_t gexec[2] = {nullptr, nullptr};
   double graph_dt = -1.0;
   int graph_nsub = -1;
+  // device copy of the prognostic state (vibe_gb300_snapshot), made on first save
+  double* snap[NSPECIES] = {};
+  bool has_snap = false;
 };
 
 namespace {
@@ -1011,6 +1014,24 @@ int vibe_gb300_hevi_substep(vibe_gb300_model* m, double dtau) {
   }
   CUDA_OK(cudaGetLastError());
   return read_status(m);
+}
+
+int vibe_gb300_snapshot(vibe_gb300_model* m, int op) {
+  if (!m || op < 0 || op > 1) return fail(VIBE_GB300_EBADARG, "bad argument");
+  const size_t n = m->d.plane * (size_t)(m->d.nz + 1);
+  if (op == 0) {
+    if (!m->snap[0])
+      for (int q = 0; q < NSPECIES; ++q)
+        if (int rc = dalloc(m, &m->snap[q], n)) return rc;
+    for (int q = 0; q < NSPECIES; ++q)
+      CUDA_OK(cudaMemcpyAsync(m->snap[q], m->S[m->cur][q], n * sizeof(double), cudaMemcpyDeviceToDevice, m->stream));
+    m->has_snap = true;
+    return 0;
+  }
+  if (!m->has_snap) return fail(VIBE_GB300_EBADARG, "no snapshot saved");
+  for (int q = 0; q < NSPECIES; ++q)
+    CUDA_OK(cudaMemcpyAsync(m->S[m->cur][q], m->snap[q], n * sizeof(double), cudaMemcpyDeviceToDevice, m->stream));
+  return sync_working(m);
 }
 
 int vibe_gb300_sponge(vibe_gb300_model* m, double dt) {

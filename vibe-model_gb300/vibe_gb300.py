@@ -85,6 +85,7 @@ _sigs = {
     "vibe_gb300_acoustic_substep": (_I, [_vp, _D]),
     "vibe_gb300_hevi_substep": (_I, [_vp, _D]),
     "vibe_gb300_sponge": (_I, [_vp, _D]),
+    "vibe_gb300_snapshot": (_I, [_vp, _I]),
     "vibe_gb300_device_field": (_I, [_vp, _I, ctypes.POINTER(_dp), ctypes.POINTER(_I)]),
     "vibe_gb300_set_state": (_I, [_vp, ctypes.POINTER(_dp), _I]),
     "vibe_gb300_get_state": (_I, [_vp, ctypes.POINTER(_dp), _I]),
@@ -233,6 +234,13 @@ class Model:
 
     def hevi_substep(self, dtau):
         _check(lib.vibe_gb300_hevi_substep(self.h, dtau))
+
+    def save_snapshot(self):
+        """Device copy of the current state (asynchronous)."""
+        _check(lib.vibe_gb300_snapshot(self.h, 0))
+
+    def restore_snapshot(self):
+        _check(lib.vibe_gb300_snapshot(self.h, 1))
 
     def sponge(self, dt):
         _check(lib.vibe_gb300_sponge(self.h, dt))
