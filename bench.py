@@ -188,6 +188,85 @@ def nest_leg(vg, torch, warmup, steps=4):
             "hevi_columns_per_parent_launch": NEST_MEMBERS * ps.nx * ps.ny}
 
 
+# Assimilation window: 192 x 192 x 50, dx = 3 km, 50 uniform 400 m levels to
+# 20 km, the single-domain base state (theta0 = 300 K, N = 0.01 1/s,
+# u = 10 m/s) plus seeded theta' ~ N(0, 0.3 K), u' ~ N(0, 0.5 m/s); 120 model
+# steps of dt = 15 s (6 HEVI substeps per stage), checkpoints every 10 steps.
+# The TL/AD (the reference's collocated RK3 with explicit acoustics) is
+# stable only below ~1.4 s on this grid, so it takes 12 steps of 1.25 s per
+# model step. TL input dx ~ N(0, 1) scaled: u, v 1 m/s, w 0.1 m/s, theta
+# 0.5 K, pi' from a 50 Pa pressure perturbation (pi' = kappa pi0 p'/p0(z)).
+WIN = dict(nx=192, ny=192, nz=50, dx=3000.0, dt=15.0, n_steps=120, every=10, tl_sub=12)
+
+
+def window_leg(vg, torch):
+    case = {k: v for k, v in CASE.items() if k not in ("dx", "dy", "nz", "zeta_stretch")}
+    s = vg.Setup.defaults(nx=WIN["nx"], ny=WIN["ny"], nz=WIN["nz"], dx=WIN["dx"], dy=WIN["dx"], zeta_stretch=1.0,
+                          **case)
+    out = {"workload": "192x192x50 (dx=3 km, 400 m levels), dt=15 s x 120 steps, checkpoints every 10 steps, "
+                       "TL/AD 12 x 1.25 s per step; theta'~N(0,0.3 K), u'~N(0,0.5 m/s) on the base state",
+           "tl_substeps": WIN["tl_sub"], "tl_dt_s": WIN["dt"] / WIN["tl_sub"]}
+    kappa = 287.05 / 1004.5
+    for name, prec, tprec, tol in (("fp64", vg.FP64, 0, 1e-10), ("mixed", vg.MIXED, 1, 1e-5)):
+        m = vg.Model(s, prec)
+        rng = np.random.default_rng(7)
+        th, u, rho = m.get(4), m.get(0), m.get(3)
+        th = th + np.where(th != 0.0, rng.normal(0.0, 0.3, th.size), 0.0)
+        u = u + np.where(u != 0.0, rng.normal(0.0, 0.5, u.size), 0.0)
+        pi = np.where(rho != 0.0, np.power(np.maximum(rho * 287.05 * th / 100000.0, 0.0), 287.05 / 717.63), 0.0)
+        m.set(4, th)
+        m.set(0, u)
+        m.set(5, pi)
+        t = vg.TLAD(s.nx, s.ny, s.nz, s.dx, s.dy, s.z_top, np.diff(m.zeta()), m.terrain(), tprec)
+        pi0 = vg.interior(s, 5, m.reffield(1))  # reference Exner function and pressure
+        vecs = []
+        for seed in (11, 12):
+            r = np.random.default_rng(seed)
+            v = [np.zeros(m.size(sp)) for sp in range(12)]
+            for sp, amp in ((0, 1.0), (1, 1.0), (2, 0.1), (4, 0.5)):
+                vg.interior(s, sp, v[sp])[...] = amp * r.standard_normal(vg.interior(s, sp, v[sp]).shape)
+            p0 = vg.interior(s, 5, m.reffield(3))
+            vg.interior(s, 5, v[5])[...] = kappa * pi0 * 50.0 * r.standard_normal(pi0.shape) / p0
+            vecs.append(v)
+        dx, dy = vecs
+        w = vg.Window(m, t, WIN["dt"], NSUB, WIN["n_steps"], WIN["every"], WIN["tl_sub"])
+        try:
+            ldx = w.tl(dx)
+            tl_ms = w.stats()[0]
+            ady = w.ad(dy)
+            ad_ms, ck, sg = w.stats()
+        finally:
+            w.close()
+        lhs = sum(float(np.sum(vg.interior(s, sp, ldx[sp]) * vg.interior(s, sp, dy[sp]))) for sp in range(12))
+        rhs = sum(float(np.sum(vg.interior(s, sp, dx[sp]) * vg.interior(s, sp, ady[sp]))) for sp in range(12))
+        cells = s.nx * s.ny * s.nz
+        tl_steps = WIN["n_steps"] * WIN["tl_sub"]
+        res = {"tl_window_ms": tl_ms, "ad_window_ms": ad_ms, "dot_lhs": lhs, "dot_rhs": rhs,
+               "dot_rel_err": abs(lhs - rhs) / max(abs(lhs), abs(rhs)), "dot_tol": tol,
+               "tl_cell_steps_per_s": cells * tl_steps / (tl_ms * 1e-3),
+               "ad_cell_steps_per_s": cells * tl_steps / (ad_ms * 1e-3),
+               "checkpoint_bytes": ck, "segment_bytes": sg,
+               "model_steps": {"tl": WIN["n_steps"] - 1, "ad": 2 * WIN["n_steps"] - WIN["n_steps"] // WIN["every"]}}
+        if name == "fp64":
+            # finite differences of the nonlinear collocated tendency against the TL tendency
+            x0 = m.state()
+            t.set_base(x0)
+            f = t.tl_tendency(dx)
+            n0 = t.nl_tendency(x0)
+            nf = np.sqrt(sum(float(np.sum(a * a)) for a in f))
+            fd = {}
+            for k in range(3, 9):
+                e = 10.0 ** -k
+                n1 = t.nl_tendency([a + e * b for a, b in zip(x0, dx)])
+                d = sum(float(np.sum(((a - b) / e - c) ** 2)) for a, b, c in zip(n1, n0, f))
+                fd["%.0e" % e] = np.sqrt(d) / nf
+            res["fd_tendency_rel_err"] = fd
+        out[name] = res
+        t.close()
+        m.close()
+    return out
+
+
 def field_errors(vg, setup, got, ref):
     """Per-field max and RMS error of got against ref over the interior,
     relative to the field's max |ref| (u, v, w: the common velocity scale)."""
@@ -379,6 +458,7 @@ def main():
     ap.add_argument("--ny", type=int, default=NY)
     ap.add_argument("--no-si", action="store_true", help="skip the semi-implicit (Helmholtz) leg")
     ap.add_argument("--no-nest", action="store_true", help="skip the batched nests leg")
+    ap.add_argument("--no-window", action="store_true", help="skip the TL/AD assimilation-window leg")
     ap.add_argument("--only", choices=["all", "mixed"], default="all",
                     help="mixed: time the mixed path only (no e2e, no FP64 leg)")
     args = ap.parse_args()
@@ -512,6 +592,7 @@ def main():
 
     si = si_leg(vg) if not args.no_si else None
     nest = nest_leg(vg, torch, args.warmup) if not args.no_nest else None
+    window = window_leg(vg, torch) if not args.no_window else None
 
     value = world * cells * args.steps / (ms_mx * 1e-3)
     value64 = world * cells * k64 / (ms_64 * 1e-3)
@@ -564,6 +645,8 @@ def main():
         line["semi_implicit"] = si
     if nest is not None:
         line["batched_nests"] = nest
+    if window is not None:
+        line["assimilation_window"] = window
     if cpu is not None:
         line["cpu_baseline"] = cpu
     print(json.dumps(line))

@@ -183,6 +183,29 @@ int vibe_gb300_nested_wait(vibe_gb300_nested *n);
 int vibe_gb300_nested_launches_per_step(const vibe_gb300_nested *n);
 vibe_stream_t vibe_gb300_nested_stream(vibe_gb300_nested *n);
 
+/* Assimilation windows (Config-5 style): the TL/AD model of a vibe_tlad
+ * object (include/vibe_tlad.h, same grid) linearised about this model's own
+ * trajectory over n_steps steps of dt (n_sub acoustic substeps), the TL/AD
+ * taking tl_substeps steps of dt/tl_substeps per model step (its explicit
+ * acoustics need the shorter step). The state at model step n is the
+ * linearisation point of TL/AD step n (TangentLinearModel::propagate with a
+ * recorded trajectory, tangent_linear.cpp:679-716; AdjointModel::
+ * propagate_with_trajectory, :749-765). States are copied to device
+ * checkpoints every `every` steps; the adjoint recomputes each segment from
+ * its checkpoint (CheckpointStrategy::Recompute, tangent_linear.hpp:56-61).
+ * Both sweeps start from the model's current state and leave it there.
+ * Perturbations: 12 FieldT host arrays (species order), halos pass through.
+ * window_stats: device time of the last sweep, checkpoint and segment memory. */
+struct vibe_tlad;
+typedef struct vibe_gb300_window vibe_gb300_window;
+int vibe_gb300_window_create(vibe_gb300_model *m, struct vibe_tlad *t, double dt, int n_sub, int n_steps, int every,
+                             int tl_substeps, vibe_gb300_window **out);
+void vibe_gb300_window_destroy(vibe_gb300_window *w);
+int vibe_gb300_window_tl(vibe_gb300_window *w, const double *const *dx0, double *const *dx_out);
+int vibe_gb300_window_ad(vibe_gb300_window *w, const double *const *dy, double *const *dx0_adjoint);
+int vibe_gb300_window_stats(const vibe_gb300_window *w, double *last_ms, size_t *checkpoint_bytes,
+                            size_t *segment_bytes);
+
 /* Kernel-level entry points (FP64 path only for the tendency). */
 int vibe_gb300_slow_tendency(vibe_gb300_model *m, double *const *host_out);
 int vibe_gb300_acoustic_substep(vibe_gb300_model *m, double dtau);

@@ -46,6 +46,14 @@ int vibe_tl_step(vibe_tlad *t, double dt, const double *const *dx, double *const
 int vibe_tl_propagate(vibe_tlad *t, double dt, int n_steps, const double *const *dx0, double *const *dx_out);
 int vibe_ad_step(vibe_tlad *t, double dt, const double *const *dx_next, double *const *dx_prev);
 int vibe_ad_propagate(vibe_tlad *t, double dt, int n_steps, const double *const *dy, double *const *dx0_adjoint);
+/* The nonlinear collocated RK3 whose tangent-linear model is the one above
+ * (nl_rk3 / nl_tendency of the reference's TL/AD test, tests/unit/
+ * test_tl_ad.cpp:100-199; the buoyancy uses the set base's theta): the
+ * model of the finite-difference check of the TL (check_tangent,
+ * tangent_linear.cpp:832-880). */
+int vibe_nl_propagate(vibe_tlad *t, double dt, int n_steps, const double *const *x0, double *const *x_out);
+/* its tendency N(x): vibe_tl_tendency is the exact derivative of N at the base */
+int vibe_nl_tendency(vibe_tlad *t, const double *const *x, double *const *d);
 
 /* Message of the last failure seen by this thread ("" if none). */
 const char *vibe_tlad_last_error(void);

@@ -1704,6 +1704,83 @@ void vo_ad_tendency(const vo_model *m, const double *const *xb, const double *co
   ad_tendency(m, X, B, O);
 }
 
+/* nl_tendency of the reference's TL/AD test (tests/unit/test_tl_ad.cpp:100-180):
+ * the nonlinear collocated tendency whose Jacobian at xb is tl_tendency; the
+ * buoyancy g (theta/max(theta_b, 1) - 1) takes theta_b from the base xb. */
+static void nl_tendency(const vo_model *m, fld *xb, fld *x, fld *d) {
+  const int nx = m->nx, ny = m->ny, nz = m->nz;
+  const double rdcv = K_RD / K_CV, fc = tl_coriolis();
+  for (int sp = 0; sp < VO_NSPECIES; ++sp) fld_zero(&d[sp]);
+  fld *u = &x[VO_U], *v = &x[VO_V], *w = &x[VO_W], *rho = &x[VO_RHO], *th = &x[VO_THETA], *pi = &x[VO_PI];
+  for (int si = 0; si < 7; ++si) {
+    const int sp = kTlScalars[si];
+    fld *q = &x[sp], *out = &d[sp];
+    dop(m, 0, q, u, out, -1.0); dop(m, 1, q, v, out, -1.0); dop(m, 2, q, w, out, -1.0);
+  }
+  {
+    fld *out = &d[VO_RHO];
+    dop(m, 0, u, rho, out, -1.0); dop(m, 1, v, rho, out, -1.0); dop(m, 2, w, rho, out, -1.0);
+    dop(m, 0, rho, u, out, -1.0); dop(m, 1, rho, v, out, -1.0); dop(m, 2, rho, w, out, -1.0);
+  }
+  {
+    fld *out = &d[VO_PI];
+    dop(m, 0, pi, u, out, -1.0); dop(m, 1, pi, v, out, -1.0); dop(m, 2, pi, w, out, -1.0);
+    dop(m, 0, u, pi, out, -rdcv); dop(m, 1, v, pi, out, -rdcv); dop(m, 2, w, pi, out, -rdcv);
+  }
+  {
+    fld *out = &d[VO_U];
+    dop(m, 0, u, u, out, -1.0); dop(m, 1, u, v, out, -1.0); dop(m, 2, u, w, out, -1.0);
+    dop(m, 0, pi, th, out, -K_CP);
+    for (int k = 0; k < nz; ++k)
+      for (int j = 0; j < ny; ++j)
+        for (int i = 0; i < nx; ++i) AT(*out, i, j, k) += fc * AT(*v, i, j, k);
+  }
+  {
+    fld *out = &d[VO_V];
+    dop(m, 0, v, u, out, -1.0); dop(m, 1, v, v, out, -1.0); dop(m, 2, v, w, out, -1.0);
+    dop(m, 1, pi, th, out, -K_CP);
+    for (int k = 0; k < nz; ++k)
+      for (int j = 0; j < ny; ++j)
+        for (int i = 0; i < nx; ++i) AT(*out, i, j, k) -= fc * AT(*u, i, j, k);
+  }
+  {
+    fld *out = &d[VO_W];
+    dop(m, 0, w, u, out, -1.0); dop(m, 1, w, v, out, -1.0); dop(m, 2, w, w, out, -1.0);
+    dop(m, 2, pi, th, out, -K_CP);
+    for (int k = 0; k < nz; ++k)
+      for (int j = 0; j < ny; ++j)
+        for (int i = 0; i < nx; ++i) {
+          const double tb = dmax(AT(xb[VO_THETA], i, j, k), 1.0);
+          AT(*out, i, j, k) += K_GRAVITY * (AT(*th, i, j, k) / tb - 1.0);
+        }
+  }
+}
+
+void vo_nl_tendency(const vo_model *m, const double *const *xb, const double *const *x, double *const *d) {
+  fld X[VO_NSPECIES], XN[VO_NSPECIES], D[VO_NSPECIES];
+  views12(m, xb, X); views12(m, x, XN); views12(m, (const double *const *)d, D);
+  nl_tendency(m, X, XN, D);
+}
+
+/* nl_rk3 of the same test (test_tl_ad.cpp:186-199): one step */
+void vo_nl_step(const vo_model *m, const double *const *xb, const double *const *x, double dt, double *const *out) {
+  fld X[VO_NSPECIES], XN[VO_NSPECIES], OUT[VO_NSPECIES], d[VO_NSPECIES], s1[VO_NSPECIES];
+  views12(m, xb, X); views12(m, x, XN); views12(m, (const double *const *)out, OUT);
+  alloc12(m, d); alloc12(m, s1);
+  const double a[3] = {dt / 3.0, dt / 2.0, dt};
+  fld *in = XN;
+  for (int st = 0; st < 3; ++st) {
+    nl_tendency(m, X, in, d);
+    fld *dst = (st == 2) ? OUT : s1;
+    for (int sp = 0; sp < VO_NSPECIES; ++sp) {
+      fld_copy(&dst[sp], &XN[sp]);
+      add_scaled(&dst[sp], a[st], &d[sp]);
+    }
+    in = s1;
+  }
+  free12(d); free12(s1);
+}
+
 /* rk3_tl, tangent_linear.cpp:559-572 (state_add_tendency over all storage) */
 void vo_tl_step(const vo_model *m, const double *const *xb, const double *const *dx, double dt, double *const *out) {
   fld X[VO_NSPECIES], DX[VO_NSPECIES], OUT[VO_NSPECIES], d[VO_NSPECIES], s1[VO_NSPECIES];

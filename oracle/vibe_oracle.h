@@ -164,6 +164,10 @@ void vo_nest_apply_lateral_boundary(const vo_nest_placement *p, int nvars, const
 void vo_tl_tendency(const vo_model *m, const double *const *xb, const double *const *dx, double *const *d);
 void vo_ad_tendency(const vo_model *m, const double *const *xb, const double *const *bar_d, double *const *bar_dx);
 void vo_tl_step(const vo_model *m, const double *const *xb, const double *const *dx, double dt, double *const *out);
+/* the nonlinear collocated RK3 whose TL is vo_tl_step (nl_rk3 of the
+ * reference's tests/unit/test_tl_ad.cpp:100-199); theta_b from xb */
+void vo_nl_step(const vo_model *m, const double *const *xb, const double *const *x, double dt, double *const *out);
+void vo_nl_tendency(const vo_model *m, const double *const *xb, const double *const *x, double *const *d);
 void vo_ad_step(const vo_model *m, const double *const *xb, const double *const *bar_out, double dt,
                 double *const *bar_in);
 

@@ -352,7 +352,8 @@ def _tlad_fns(kind):
     f = {}
     names = [("tl_step", [vp, vp, vp, _D, vp]), ("ad_step", [vp, vp, vp, _D, vp])]
     if kind == "port":
-        names += [("tl_tendency", [vp, vp, vp, vp]), ("ad_tendency", [vp, vp, vp, vp])]
+        names += [("tl_tendency", [vp, vp, vp, vp]), ("ad_tendency", [vp, vp, vp, vp]),
+                  ("nl_step", [vp, vp, vp, _D, vp]), ("nl_tendency", [vp, vp, vp, vp])]
     else:
         names += [("tl_propagate", [vp, vp, vp, _D, _I, vp]), ("ad_propagate", [vp, vp, vp, _D, _I, vp])]
     for name, args in names:
@@ -386,6 +387,18 @@ def ad_tendency(model, xb, bar_d):
 def tl_step(model, xb, dx, dt):
     out = [np.zeros(model.size(sp)) for sp in range(12)]
     _tl_call(model, "tl_step", _arr12(xb), _arr12(dx), dt, _arr12(out))
+    return out
+
+
+def nl_tendency(model, xb, x):
+    d = [np.zeros(model.size(sp)) for sp in range(12)]
+    _tl_call(model, "nl_tendency", _arr12(xb), _arr12(x), _arr12(d))
+    return d
+
+
+def nl_step(model, xb, x, dt):
+    out = [np.zeros(model.size(sp)) for sp in range(12)]
+    _tl_call(model, "nl_step", _arr12(xb), _arr12(x), dt, _arr12(out))
     return out
 
 

@@ -270,3 +270,34 @@ def test_cfl_diagnostics_port_is_bit_exact_to_reference(oc, case):
     assert p.rk3_step(1.0, 2) == r.rk3_step(1.0, 2) == 0
     assert oc.cfl(p, 2.0, 0.3) == oc.cfl(r, 2.0, 0.3)
     assert oc.max_stable_dt(p) == oc.max_stable_dt(r)
+
+
+def fd_curve(oc, s, port, xb, dx, eps):
+    """Relative error of (N(xb + e dx) - N(xb)) / e against F(xb, dx)."""
+    t = oc.tl_tendency(port, xb, dx)
+    f0 = oc.nl_tendency(port, xb, xb)
+    nt = np.sqrt(sum(np.sum(a * a) for a in t))
+    out = []
+    for e in eps:
+        f1 = oc.nl_tendency(port, xb, [a + e * b for a, b in zip(xb, dx)])
+        fd = [(a - b) / e for a, b in zip(f1, f0)]
+        num = np.sqrt(sum(np.sum((a - b) ** 2) for a, b in zip(fd, t)))
+        out.append(num / max(nt, np.sqrt(sum(np.sum(a * a) for a in fd)), 1e-30))
+    return out
+
+
+def test_tl_tendency_is_the_derivative_of_the_nonlinear_tendency(oc):
+    """check_tangent's finite-difference criterion (tangent_linear.cpp:832-880;
+    the U-shaped curve of test_tl_ad.cpp:420-460) at the tendency level:
+    truncation error O(e) for large e, rounding O(1/e) for small e, and a
+    small interior minimum."""
+    import tlad_cases as tc
+    s = tc.tl_setup(oc)
+    p = oc.Model(s, "port")
+    xb = tc.base_state(oc, p)
+    dx = tc.perturbation(oc, p, 41)
+    eps = [10.0 ** -k for k in range(1, 11)]
+    errs = fd_curve(oc, s, p, xb, dx, eps)
+    k = int(np.argmin(errs))
+    assert 0 < k < len(eps) - 1 and errs[0] > errs[k] and errs[-1] > errs[k], errs
+    assert errs[k] < 1e-6, errs

@@ -15,6 +15,9 @@
 #include "vibe_gb300.h"
 #include "vibe_helmholtz.h"
 #include "vibe_nest.h"
+#include "vibe_tlad.h"
+#include "tlad_internal.cuh"
+#include <array>
 
 using namespace vgb;
 
@@ -1520,6 +1523,215 @@ int vibe_gb300_nested_step(vibe_gb300_nested* n, double dt, int n_sub, int n_ste
 int vibe_gb300_nested_launches_per_step(const vibe_gb300_nested* n) { return n ? n->launches : 0; }
 
 vibe_stream_t vibe_gb300_nested_stream(vibe_gb300_nested* n) { return n ? (vibe_stream_t)n->stream : nullptr; }
+
+// ---- assimilation windows: the TL/AD model linearised about the model's own
+// trajectory, with checkpoints and recomputation (TangentLinearModel::
+// propagate / record_trajectory, tangent_linear.cpp:679-716;
+// AdjointModel::propagate_with_trajectory, :749-765; the Recompute
+// checkpoint strategy, tangent_linear.hpp:56-61). The model state at step n
+// is the linearisation point of TL/AD step n, read in place from the
+// model's device buffers (same layout); every `every` steps the state is
+// copied to a checkpoint; the adjoint sweep recomputes each segment's states
+// from its checkpoint (double-buffered, so the recomputation of one segment
+// overlaps the adjoint of the next).
+}  // extern "C"
+
+struct vibe_gb300_window {
+  vibe_gb300_model* m = nullptr;
+  vibe_tlad* t = nullptr;
+  double dt = 0.0;
+  int n_sub = 1, n_steps = 0, every = 10, tl_sub = 1;
+  std::vector<std::array<double*, NSPECIES>> ckpt;
+  std::vector<std::array<double*, NSPECIES>> seg[2];
+  std::vector<void*> allocs;
+  cudaEvent_t ev_model = nullptr, ev_seg[2] = {nullptr, nullptr}, e0 = nullptr, e1 = nullptr;
+  double last_ms = 0.0;
+};
+
+namespace {
+size_t state_count(const vibe_gb300_model* m) { return m->d.plane * (size_t)(m->d.nz + 1); }
+
+int copy_state(vibe_gb300_model* m, double* const* dst, double* const* src) {
+  for (int q = 0; q < NSPECIES; ++q)
+    CUDA_OK(cudaMemcpyAsync(dst[q], src[q], state_count(m) * sizeof(double), cudaMemcpyDeviceToDevice, m->stream));
+  return 0;
+}
+
+// checkpoint the current state; the FP32 working copy is rebuilt from it as a
+// restart from the checkpoint will, so that recomputed states repeat the bits
+int window_checkpoint(vibe_gb300_window* w, int c) {
+  if (int rc = copy_state(w->m, w->ckpt[c].data(), w->m->S[w->m->cur])) return rc;
+  return sync_working(w->m);
+}
+int window_restart(vibe_gb300_window* w, int c) {
+  if (int rc = copy_state(w->m, w->m->S[w->m->cur], w->ckpt[c].data())) return rc;
+  return sync_working(w->m);
+}
+int window_begin(vibe_gb300_window* w) {
+  CUDA_OK(cudaEventRecord(w->e0, w->m->stream));
+  return 0;
+}
+int window_end(vibe_gb300_window* w, cudaStream_t ts) {
+  CUDA_OK(cudaEventRecord(w->ev_model, w->m->stream));
+  CUDA_OK(cudaStreamWaitEvent(ts, w->ev_model, 0));
+  CUDA_OK(cudaEventRecord(w->e1, ts));
+  CUDA_OK(cudaStreamSynchronize(ts));
+  float ms = 0.f;
+  CUDA_OK(cudaEventElapsedTime(&ms, w->e0, w->e1));
+  w->last_ms = ms;
+  vgb::tlad_use_base(w->t, nullptr);
+  return 0;
+}
+}  // namespace
+
+extern "C" {
+
+int vibe_gb300_window_create(vibe_gb300_model* m, vibe_tlad* t, double dt, int n_sub, int n_steps, int every,
+                             int tl_substeps, vibe_gb300_window** out) {
+  if (!m || !t || !out || !(dt > 0.0) || n_steps < 1 || every < 1 || tl_substeps < 1)
+    return fail(VIBE_GB300_EBADARG, "bad argument");
+  int nx, ny, nz;
+  vgb::tlad_grid(t, &nx, &ny, &nz);
+  if (nx != m->d.nx || ny != m->d.ny || nz != m->d.nz)
+    return fail(VIBE_GB300_EBADARG, "the TL/AD grid differs from the model's");
+  auto* w = new vibe_gb300_window();
+  w->m = m;
+  w->t = t;
+  w->dt = dt;
+  w->n_sub = n_sub;
+  w->n_steps = n_steps;
+  w->every = every;
+  w->tl_sub = tl_substeps;
+  const int nck = (n_steps + every - 1) / every, seg_len = std::min(every, n_steps);
+  const size_t n = state_count(m);
+  int rc = 0;
+  auto alloc_state = [&](std::array<double*, NSPECIES>& a) {
+    for (int q = 0; q < NSPECIES && !rc; ++q) {
+      void* p = nullptr;
+      if (cudaMalloc(&p, n * sizeof(double)) != cudaSuccess) {
+        rc = fail(VIBE_GB300_EDEVICE, "window buffer allocation");
+      } else {
+        w->allocs.push_back(p);
+        a[q] = (double*)p;
+      }
+    }
+  };
+  w->ckpt.resize(nck);
+  for (auto& a : w->ckpt) alloc_state(a);
+  for (int b = 0; b < 2; ++b) {
+    w->seg[b].resize(seg_len);
+    for (auto& a : w->seg[b]) alloc_state(a);
+  }
+  if (!rc && (cudaEventCreateWithFlags(&w->ev_model, cudaEventDisableTiming) != cudaSuccess ||
+              cudaEventCreateWithFlags(&w->ev_seg[0], cudaEventDisableTiming) != cudaSuccess ||
+              cudaEventCreateWithFlags(&w->ev_seg[1], cudaEventDisableTiming) != cudaSuccess ||
+              cudaEventCreate(&w->e0) != cudaSuccess || cudaEventCreate(&w->e1) != cudaSuccess))
+    rc = fail(VIBE_GB300_EDEVICE, "events");
+  if (rc) {
+    vibe_gb300_window_destroy(w);
+    return rc;
+  }
+  *out = w;
+  return 0;
+}
+
+void vibe_gb300_window_destroy(vibe_gb300_window* w) {
+  if (!w) return;
+  if (w->m) cudaStreamSynchronize(w->m->stream);
+  if (w->t) cudaStreamSynchronize(vgb::tlad_stream(w->t));
+  for (cudaEvent_t e : {w->ev_model, w->ev_seg[0], w->ev_seg[1], w->e0, w->e1})
+    if (e) cudaEventDestroy(e);
+  for (void* p : w->allocs) cudaFree(p);
+  delete w;
+}
+
+int vibe_gb300_window_tl(vibe_gb300_window* w, const double* const* dx0, double* const* dx_out) {
+  if (!w || !dx0 || !dx_out) return fail(VIBE_GB300_EBADARG, "bad argument");
+  vibe_gb300_model* m = w->m;
+  vibe_tlad* t = w->t;
+  cudaStream_t ts = vgb::tlad_stream(t);
+  CUDA_OK(cudaStreamSynchronize(m->stream));
+  double* const* v[2] = {vgb::tlad_work(t, 0), vgb::tlad_work(t, 1)};
+  if (!vgb::tlad_upload(t, dx0, v[0])) return fail(VIBE_GB300_EBADARG, vibe_tlad_last_error());
+  if (int rc = window_begin(w)) return rc;
+  const double dtl = w->dt / w->tl_sub;
+  int c = 0;
+  for (int n = 0; n < w->n_steps; ++n) {
+    if (n % w->every == 0)
+      if (int rc = window_checkpoint(w, n / w->every)) return rc;
+    CUDA_OK(cudaEventRecord(w->ev_model, m->stream));  // x_n is ready
+    CUDA_OK(cudaStreamWaitEvent(ts, w->ev_model, 0));
+    vgb::tlad_use_base(t, m->S[m->cur]);
+    for (int j = 0; j < w->tl_sub; ++j, c = 1 - c) vgb::tlad_tl_step(t, v[c], v[1 - c], dtl);
+    CUDA_OK(cudaEventRecord(w->ev_seg[0], ts));
+    if (n + 1 < w->n_steps) {
+      // step n reads x_n and writes the other buffer (overlaps the TL step);
+      // step n + 1 overwrites x_n, so it waits for the TL step
+      if (int rc = enqueue_steps(m, w->dt, w->n_sub, 1)) return rc;
+      CUDA_OK(cudaStreamWaitEvent(m->stream, w->ev_seg[0], 0));
+    }
+  }
+  if (int rc = window_end(w, ts)) return rc;
+  if (!vgb::tlad_download(t, v[c], dx0, dx_out)) return fail(VIBE_GB300_EDEVICE, vibe_tlad_last_error());
+  if (int rc = read_status(m)) return rc;
+  if (int rc = window_restart(w, 0)) return rc;  // back to the window's initial state
+  return read_status(m);
+}
+
+int vibe_gb300_window_ad(vibe_gb300_window* w, const double* const* dy, double* const* dx0_adjoint) {
+  if (!w || !dy || !dx0_adjoint) return fail(VIBE_GB300_EBADARG, "bad argument");
+  vibe_gb300_model* m = w->m;
+  vibe_tlad* t = w->t;
+  cudaStream_t ts = vgb::tlad_stream(t);
+  CUDA_OK(cudaStreamSynchronize(m->stream));
+  double* const* v[2] = {vgb::tlad_work(t, 0), vgb::tlad_work(t, 1)};
+  if (!vgb::tlad_upload(t, dy, v[0])) return fail(VIBE_GB300_EBADARG, vibe_tlad_last_error());
+  if (int rc = window_begin(w)) return rc;
+  // forward sweep: checkpoints only
+  const int nck = (int)w->ckpt.size();
+  const int last_ck = (nck - 1) * w->every;
+  for (int n = 0; n <= last_ck; ++n) {
+    if (n % w->every == 0)
+      if (int rc = window_checkpoint(w, n / w->every)) return rc;
+    if (n < last_ck)
+      if (int rc = enqueue_steps(m, w->dt, w->n_sub, 1)) return rc;
+  }
+  // backward sweep over the segments, recomputing each from its checkpoint
+  const double dtl = w->dt / w->tl_sub;
+  int c = 0;
+  for (int sgm = nck - 1; sgm >= 0; --sgm) {
+    const int b = sgm & 1, first = sgm * w->every, last = std::min(w->n_steps, first + w->every);
+    if (sgm <= nck - 3) CUDA_OK(cudaStreamWaitEvent(m->stream, w->ev_seg[b], 0));  // its buffers are free again
+    if (int rc = window_restart(w, sgm)) return rc;
+    for (int n = first; n < last; ++n) {
+      if (int rc = copy_state(m, w->seg[b][n - first].data(), m->S[m->cur])) return rc;
+      if (n + 1 < last)
+        if (int rc = enqueue_steps(m, w->dt, w->n_sub, 1)) return rc;
+    }
+    CUDA_OK(cudaEventRecord(w->ev_model, m->stream));
+    CUDA_OK(cudaStreamWaitEvent(ts, w->ev_model, 0));
+    for (int n = last - 1; n >= first; --n) {
+      vgb::tlad_use_base(t, w->seg[b][n - first].data());
+      for (int j = 0; j < w->tl_sub; ++j, c = 1 - c) vgb::tlad_ad_step(t, v[c], v[1 - c], dtl);
+    }
+    CUDA_OK(cudaEventRecord(w->ev_seg[b], ts));
+  }
+  if (int rc = window_end(w, ts)) return rc;
+  if (!vgb::tlad_download(t, v[c], dy, dx0_adjoint)) return fail(VIBE_GB300_EDEVICE, vibe_tlad_last_error());
+  if (int rc = read_status(m)) return rc;
+  if (int rc = window_restart(w, 0)) return rc;
+  return read_status(m);
+}
+
+int vibe_gb300_window_stats(const vibe_gb300_window* w, double* last_ms, size_t* checkpoint_bytes,
+                            size_t* segment_bytes) {
+  if (!w) return fail(VIBE_GB300_EBADARG, "bad argument");
+  const size_t st = state_count(w->m) * NSPECIES * sizeof(double);
+  if (last_ms) *last_ms = w->last_ms;
+  if (checkpoint_bytes) *checkpoint_bytes = st * w->ckpt.size();
+  if (segment_bytes) *segment_bytes = st * (w->seg[0].size() + w->seg[1].size());
+  return 0;
+}
 
 int vibe_gb300_set_state(vibe_gb300_model* m, const double* const* host, int nspecies) {
   if (!m || !host || nspecies < 1 || nspecies > NSPECIES) return fail(VIBE_GB300_EBADARG, "bad argument");

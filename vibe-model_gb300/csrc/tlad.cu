@@ -111,6 +111,39 @@ __global__ void k_tl(TlGeo g, const __grid_constant__ F12 xb, const __grid_const
   for (int q = 0; q < kSp; ++q) out.f[q][c] = in.f[q][c] + a * (double)r[q];
 }
 
+// out = in + a * N(x): the nonlinear collocated tendency whose Jacobian at
+// xb is F(xb, .) (nl_tendency of the reference's TL/AD test,
+// tests/unit/test_tl_ad.cpp:100-180): -u.D(s) for the scalars,
+// -rho div(u) - u.D(rho), -u.D(pi) - (Rd/cv) pi div(u), momentum
+// -u.D(u) - cp theta D(pi) +- f (v, u), and buoyancy g (theta/max(thb,1) - 1)
+// with thb the base state's theta.
+template <typename T>
+__global__ void k_nl(TlGeo g, const __grid_constant__ F12 xb, const __grid_constant__ F12 x,
+                     const __grid_constant__ F12 in, const __grid_constant__ M12 out, double a) {
+  const Dims& d = g.d;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y, k = blockIdx.z;
+  if (i > d.nx || j > d.ny) return;
+  const size_t c = d.idx(i, j, k);
+  if (i >= d.nx || j >= d.ny || k >= d.nz) {
+    for (int q = 0; q < kSp; ++q) out.f[q][c] = in.f[q][c];
+    return;
+  }
+  const Pt<T> p(g, i, j, k);
+  const T u = p.v(x.f[U], c), v = p.v(x.f[V], c), w = p.v(x.f[W], c);
+  const T div = p.Dx(x.f[U]) + p.Dy(x.f[V]) + p.Dz(x.f[W]);
+  const T cp = (T)g.cp, rdcv = (T)g.rdcv, fc = (T)g.fcor;
+  auto adv = [&](const double* f) { return -(u * p.Dx(f) + v * p.Dy(f) + w * p.Dz(f)); };
+  T r[kSp];
+  for (int s = 0; s < 7; ++s) r[kScal[s]] = adv(x.f[kScal[s]]);
+  r[RHO] = -p.v(x.f[RHO], c) * div + adv(x.f[RHO]);
+  r[PI] = adv(x.f[PI]) - rdcv * p.v(x.f[PI], c) * div;
+  const T th = p.v(x.f[THETA], c), thb = p.v(xb.f[THETA], c);
+  r[U] = adv(x.f[U]) - cp * th * p.Dx(x.f[PI]) + fc * v;
+  r[V] = adv(x.f[V]) - cp * th * p.Dy(x.f[PI]) - fc * u;
+  r[W] = adv(x.f[W]) - cp * th * p.Dz(x.f[PI]) + (T)g.g * (th / (thb < (T)1 ? (T)1 : thb) - (T)1);
+  for (int q = 0; q < kSp; ++q) out.f[q][c] = in.f[q][c] + a * (double)r[q];
+}
+
 // Adjoint of F at one point: bar_x(q) = sum of the transposed TL terms.
 // b = the adjoint input field (bar of the tendency), scaled by `a`.
 template <typename T>
@@ -229,6 +262,7 @@ struct vibe_tlad {
   cudaStream_t stream = nullptr;
   std::vector<void*> allocs;
   double* xb[kSp] = {};
+  double* const* base = nullptr;  // linearisation point in use (xb, or a trajectory state)
   double* w[6][kSp] = {};  // work states
   double* izh = nullptr;
   std::vector<double> host;  // staging
@@ -309,18 +343,36 @@ M12 mf(double* const* a) {
 void launch_tl(vibe_tlad* t, double* const* x, double* const* in, double* const* out, double a) {
   const dim3 b(32, 4), gr((t->d.nx + 1 + 31) / 32, (t->d.ny + 1 + 3) / 4, t->d.nz + 1);
   if (t->precision == 1)
-    k_tl<float><<<gr, b, 0, t->stream>>>(t->g, cf(t->xb), cf(x), cf(in), mf(out), a);
+    k_tl<float><<<gr, b, 0, t->stream>>>(t->g, cf(t->base), cf(x), cf(in), mf(out), a);
   else
-    k_tl<double><<<gr, b, 0, t->stream>>>(t->g, cf(t->xb), cf(x), cf(in), mf(out), a);
+    k_tl<double><<<gr, b, 0, t->stream>>>(t->g, cf(t->base), cf(x), cf(in), mf(out), a);
 }
 // out = base + add1 + add2 + a * F^T(b)
 void launch_ad(vibe_tlad* t, double* const* b, double* const* base, double* const* add1, double* const* add2,
                double* const* out, double a) {
   const dim3 bl(32, 4), gr((t->d.nx + 1 + 31) / 32, (t->d.ny + 1 + 3) / 4, t->d.nz + 1);
   if (t->precision == 1)
-    k_ad<float><<<gr, bl, 0, t->stream>>>(t->g, cf(t->xb), cf(b), cf(base), cf(add1), cf(add2), mf(out), a);
+    k_ad<float><<<gr, bl, 0, t->stream>>>(t->g, cf(t->base), cf(b), cf(base), cf(add1), cf(add2), mf(out), a);
   else
-    k_ad<double><<<gr, bl, 0, t->stream>>>(t->g, cf(t->xb), cf(b), cf(base), cf(add1), cf(add2), mf(out), a);
+    k_ad<double><<<gr, bl, 0, t->stream>>>(t->g, cf(t->base), cf(b), cf(base), cf(add1), cf(add2), mf(out), a);
+}
+
+void launch_nl(vibe_tlad* t, double* const* x, double* const* in, double* const* out, double a) {
+  const dim3 b(32, 4), gr((t->d.nx + 1 + 31) / 32, (t->d.ny + 1 + 3) / 4, t->d.nz + 1);
+  if (t->precision == 1)
+    k_nl<float><<<gr, b, 0, t->stream>>>(t->g, cf(t->xb), cf(x), cf(in), mf(out), a);
+  else
+    k_nl<double><<<gr, b, 0, t->stream>>>(t->g, cf(t->xb), cf(x), cf(in), mf(out), a);
+}
+
+// nl_rk3 (tests/unit/test_tl_ad.cpp:186-199) on device: in -> out; uses w[4]
+void nl_step_dev(vibe_tlad* t, double* const* in, double* const* out, double dt) {
+  double* const* s1 = t->w[4];
+  launch_nl(t, in, in, s1, dt / 3.0);
+  launch_nl(t, s1, in, out, dt / 2.0);
+  launch_nl(t, out, in, s1, dt);
+  for (int q = 0; q < kSp; ++q)
+    cudaMemcpyAsync(out[q], s1[q], field_count(t) * sizeof(double), cudaMemcpyDeviceToDevice, t->stream);
 }
 
 // rk3_tl on device: in -> out (out distinct from in); uses w[4]
@@ -389,6 +441,7 @@ int vibe_tlad_create(int nx, int ny, int nz, double dx, double dy, double z_top,
   t->g.rdcv = kRd / kCv;
   t->g.cp = kCp;
   t->g.g = kG;
+  t->base = t->xb;
   *out = t;
   return VIBE_C_OK;
 }
@@ -455,4 +508,44 @@ int vibe_ad_step(vibe_tlad* t, double dt, const double* const* dx_next, double* 
   return vibe_ad_propagate(t, dt, 1, dx_next, dx_prev);
 }
 
+int vibe_nl_tendency(vibe_tlad* t, const double* const* x, double* const* d) {
+  if (!t || !x || !d) return VIBE_C_ERR_BAD_ARG;
+  if (!upload12(t, x, t->w[0])) return VIBE_C_ERR_DEVICE;
+  for (int q = 0; q < kSp; ++q) cudaMemsetAsync(t->w[1][q], 0, field_count(t) * sizeof(double), t->stream);
+  launch_nl(t, t->w[0], t->w[1], t->w[2], 1.0);  // 0 + 1*N
+  if (!ok(cudaStreamSynchronize(t->stream), "nl tendency")) return VIBE_C_ERR_DEVICE;
+  return download12(t, t->w[2], nullptr, d) ? VIBE_C_OK : VIBE_C_ERR_DEVICE;
+}
+
+int vibe_nl_propagate(vibe_tlad* t, double dt, int n_steps, const double* const* x0, double* const* x_out) {
+  if (!t || !x0 || !x_out || n_steps < 0) return VIBE_C_ERR_BAD_ARG;
+  if (!upload12(t, x0, t->w[0])) return VIBE_C_ERR_DEVICE;
+  int cur = 0;
+  for (int s = 0; s < n_steps; ++s) {
+    nl_step_dev(t, t->w[cur], t->w[1 - cur], dt);
+    cur = 1 - cur;
+  }
+  if (!ok(cudaStreamSynchronize(t->stream), "nl propagate")) return VIBE_C_ERR_DEVICE;
+  return download12(t, t->w[cur], x0, x_out) ? VIBE_C_OK : VIBE_C_ERR_DEVICE;
+}
+
 }  // extern "C"
+
+// ---- device-side access for trajectory runs (tlad_internal.cuh) ----
+namespace vgb {
+void tlad_grid(const vibe_tlad* t, int* nx, int* ny, int* nz) {
+  *nx = t->d.nx;
+  *ny = t->d.ny;
+  *nz = t->d.nz;
+}
+cudaStream_t tlad_stream(vibe_tlad* t) { return t->stream; }
+double* const* tlad_work(vibe_tlad* t, int s) { return t->w[s]; }
+void tlad_use_base(vibe_tlad* t, double* const* base) { t->base = base ? base : t->xb; }
+void tlad_tl_step(vibe_tlad* t, double* const* in, double* const* out, double dt) { tl_step_dev(t, in, out, dt); }
+void tlad_ad_step(vibe_tlad* t, double* const* bo, double* const* bi, double dt) { ad_step_dev(t, bo, bi, dt); }
+bool tlad_upload(vibe_tlad* t, const double* const* host, double* const* dst) { return upload12(t, host, dst); }
+bool tlad_download(vibe_tlad* t, double* const* src, const double* const* keep, double* const* host) {
+  return download12(t, src, keep, host);
+}
+void tlad_set_error(const char* msg) { g_terr = msg; }
+}  // namespace vgb

@@ -545,7 +545,9 @@ for _name, _args in (("vibe_tlad_create", [_I, _I, _I, _D, _D, _D, _vp, _vp, _I,
                      ("vibe_tl_step", [_vp, _D, _vp, _vp]),
                      ("vibe_tl_propagate", [_vp, _D, _I, _vp, _vp]),
                      ("vibe_ad_step", [_vp, _D, _vp, _vp]),
-                     ("vibe_ad_propagate", [_vp, _D, _I, _vp, _vp])):
+                     ("vibe_ad_propagate", [_vp, _D, _I, _vp, _vp]),
+                     ("vibe_nl_propagate", [_vp, _D, _I, _vp, _vp]),
+                     ("vibe_nl_tendency", [_vp, _vp, _vp])):
     _f = getattr(lib, _name)
     _f.restype = _I
     _f.argtypes = _args
@@ -618,6 +620,17 @@ class TLAD:
     def ad_propagate(self, dt, n, dy):
         dy, out = self._prep(dy), self._out()
         self._rc(lib.vibe_ad_propagate(self.h, dt, n, self._arr(dy), self._arr(out)))
+        return out
+
+    def nl_tendency(self, x):
+        x, d = self._prep(x), self._out()
+        self._rc(lib.vibe_nl_tendency(self.h, self._arr(x), self._arr(d)))
+        return d
+
+    def nl_propagate(self, dt, n, x0):
+        """The nonlinear collocated RK3 whose TL this is (FD checks)."""
+        x0, out = self._prep(x0), self._out()
+        self._rc(lib.vibe_nl_propagate(self.h, dt, n, self._arr(x0), self._arr(out)))
         return out
 
     def tl_step(self, dt, dx):
@@ -719,6 +732,63 @@ class Nested:
     def close(self):
         if self.h:
             lib.vibe_gb300_nested_destroy(self.h)
+            self.h = _vp()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+
+# ---- assimilation windows: TL/AD about the model trajectory (vibe_gb300.h) --
+for _name, _res, _args in (("vibe_gb300_window_create", _I, [_vp, _vp, _D, _I, _I, _I, _I, ctypes.POINTER(_vp)]),
+                           ("vibe_gb300_window_destroy", None, [_vp]),
+                           ("vibe_gb300_window_tl", _I, [_vp, _vp, _vp]),
+                           ("vibe_gb300_window_ad", _I, [_vp, _vp, _vp]),
+                           ("vibe_gb300_window_stats", _I, [_vp, ctypes.POINTER(_D), ctypes.POINTER(ctypes.c_size_t),
+                                                            ctypes.POINTER(ctypes.c_size_t)])):
+    _f = getattr(lib, _name)
+    _f.restype = _res
+    _f.argtypes = _args
+
+
+class Window:
+    """TL/AD (a TLAD object) linearised about the trajectory of a Model over
+    n_steps steps of dt, checkpointed every `every` steps and recomputed in
+    the adjoint sweep; the TL/AD takes tl_substeps steps per model step.
+    Perturbations are lists of 12 FieldT arrays."""
+
+    def __init__(self, model, tlad, dt, n_sub, n_steps, every=10, tl_substeps=1):
+        self.model, self.tlad = model, tlad
+        self.h = _vp()
+        _check(lib.vibe_gb300_window_create(model.h, tlad.h, dt, n_sub, n_steps, every, tl_substeps,
+                                            ctypes.byref(self.h)))
+
+    def _io(self, states):
+        ins = [np.ascontiguousarray(a, dtype=np.float64) for a in states]
+        outs = [np.zeros(a.size) for a in ins]
+        return ins, outs
+
+    def tl(self, dx0):
+        ins, outs = self._io(dx0)
+        _check(lib.vibe_gb300_window_tl(self.h, TLAD._arr(ins), TLAD._arr(outs)))
+        return outs
+
+    def ad(self, dy):
+        ins, outs = self._io(dy)
+        _check(lib.vibe_gb300_window_ad(self.h, TLAD._arr(ins), TLAD._arr(outs)))
+        return outs
+
+    def stats(self):
+        """(device ms of the last sweep, checkpoint bytes, segment bytes)"""
+        ms, ck, sg = _D(), ctypes.c_size_t(), ctypes.c_size_t()
+        _check(lib.vibe_gb300_window_stats(self.h, ctypes.byref(ms), ctypes.byref(ck), ctypes.byref(sg)))
+        return ms.value, ck.value, sg.value
+
+    def close(self):
+        if self.h:
+            lib.vibe_gb300_window_destroy(self.h)
             self.h = _vp()
 
     def __enter__(self):
