@@ -88,6 +88,7 @@ typedef struct vibe_gb300_setup {
   double hevi_beta;
   int split_fast;                   /* fast terms integrated only by the substeps */
   int weno_advective;               /* WENO5 flux form + q div(u) */
+  int w_rigid;                      /* 1: w = 0 on the ground and lid faces after every step */
 } vibe_gb300_setup;
 
 typedef struct vibe_gb300_model vibe_gb300_model;

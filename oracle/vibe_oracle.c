@@ -1037,6 +1037,12 @@ int vo_rk3_step(vo_model *m, double dt, int n_sub_in) {
     if (has_nonfinite(m)) return 1;
   }
   sponge_apply(m, dt);
+  if (m->s.w_rigid)
+    for (int j = 0; j < m->ny; ++j)
+      for (int i = 0; i < m->nx; ++i) {
+        AT(m->st[VO_W], i, j, 0) = 0.0;
+        AT(m->st[VO_W], i, j, m->nz) = 0.0;
+      }
   return 0;
 }
 

@@ -93,6 +93,12 @@ typedef struct vo_setup {
    *   dq/dt = -u.grad(q) that equations.cpp:8-11 documents; a constant field
    *   then has zero tendency even where the flow is divergent. */
   int weno_advective;
+  /* w_rigid: 1 = rigid ground and lid: after every RK3 step (after the
+   *   sponge) w is set to zero on the k = 0 and k = nz faces. 0 = the
+   *   reference, whose tendencies move every w face (equations.cpp:91-110
+   *   over k in [0, nz]), so a buoyant or unbalanced column pushes mass
+   *   through the ground. */
+  int w_rigid;
 } vo_setup;
 
 /* Fill *s with the Config-1 warm-bubble case on an nx x ny x nz grid. */

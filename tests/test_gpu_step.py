@@ -208,6 +208,7 @@ STEP_CASES = [
     dict(),                                                                                  # stable, FB
     dict(acoustic_mode=2, ref_kind=1),                                                        # stable, HEVI
     dict(acoustic_mode=1, pgf_perturbation=0, split_fast=0),                                  # O-HEVI
+    dict(acoustic_mode=2, ref_kind=1, w_rigid=1, hevi_beta=0.6),                              # rigid ground/lid
 ]
 
 
@@ -236,7 +237,7 @@ def test_rk3_step_fp64_exact(vg, oc, case):
             assert np.array_equal(vg.interior(s, sp, m.get(sp)), vg.interior(s, sp, o.get(sp))), vg.SPECIES[sp]
 
 
-@pytest.mark.parametrize("case", [2, 3])
+@pytest.mark.parametrize("case", [2, 3, 5])
 def test_rk3_step_mixed(vg, oc, case):
     s = small_setup(vg, **STEP_CASES[case])
     with vg.Model(s, vg.MIXED) as m:
@@ -363,3 +364,16 @@ def test_snapshot_restart_is_bitwise(vg):
                 assert np.array_equal(a, b), vg.SPECIES[sp]
         with vg.Model(s, prec) as m, pytest.raises(vg.VibeError):
             m.restore_snapshot()
+
+
+def test_rigid_ground_and_lid(vg):
+    """w_rigid: w is zero on the k = 0 and k = nz faces after every step (the
+    reference moves them: a bubble touching the ground pushes mass through it)."""
+    for prec in (vg.FP64, vg.MIXED):
+        for rigid in (0, 1):
+            s = small_setup(vg, acoustic_mode=2, ref_kind=1, w_rigid=rigid, bubble_zc=300.0)
+            with vg.Model(s, prec) as m:
+                m.step(2.0, 4, 2)
+                w = vg.interior(s, 2, m.get(2))
+                edge = max(np.abs(w[0]).max(), np.abs(w[-1]).max())
+                assert (edge == 0.0) == bool(rigid), (prec, rigid, edge)

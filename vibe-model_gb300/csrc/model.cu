@@ -323,6 +323,14 @@ __global__ void k_unpack(Dims d, int nsx, int nsy, int nsz, int ni, int nj, int 
   }
 }
 
+// rigid ground and lid (w_rigid): w = 0 on the k = 0 and k = nz faces
+__global__ void k_rigid_w(Dims d, double* __restrict__ w) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
+  if (i >= d.nx || j >= d.ny) return;
+  w[d.idx(i, j, 0)] = 0.0;
+  w[d.idx(i, j, d.nz)] = 0.0;
+}
+
 void box_of(const vibe_gb300_model* m, int q, int& ni, int& nj, int& nk) {
   ni = m->d.nx + 1;
   nj = m->d.ny + 1;
@@ -591,6 +599,10 @@ int enqueue_one_step(vibe_gb300_model* m, double dt, int n_sub) {
       }
       Span sp(m, 2);
       m->f64->sponge(d, m->met, S1, m->kmin, dt, m->stream);
+      if (m->fl.w_rigid) {
+        const dim3 b(32, 8);
+        k_rigid_w<<<dim3((d.nx + 31) / 32, (d.ny + 7) / 8), b, 0, m->stream>>>(d, S1[W]);
+      }
     } else {
       const WS w0 = ws_of(m->W0);
       float** final_sub = nullptr;
@@ -758,6 +770,7 @@ int vibe_gb300_model_create(const vibe_gb300_setup* s, int precision, vibe_gb300
   fl.advection = s->advection; fl.weno_scalars = s->weno_scalars; fl.weno_advective = s->weno_advective;
   fl.moist = s->moist; fl.coriolis = s->coriolis; fl.div_damp = s->divergence_damping;
   fl.div_order = s->divergence_order; fl.pgf_pert = s->pgf_perturbation; fl.split_fast = s->split_fast;
+  fl.w_rigid = s->w_rigid;
   fl.acoustic_mode = s->acoustic_mode; fl.hevi_beta = s->hevi_beta;
   host_setup(m);
   // horizontally uniform reference state on flat terrain?

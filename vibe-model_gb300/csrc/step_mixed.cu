@@ -728,7 +728,14 @@ __device__ __forceinline__ void finish_body(const Dims& d, const Tab& t, const F
   };
   if (j < d.ny && k < d.nz) face(U);
   if (i < d.nx && k < d.nz) face(V);
-  if (i < d.nx && j < d.ny) face(W);
+  if (i < d.nx && j < d.ny) {
+    if (fl.w_rigid && (k == 0 || k == d.nz)) {
+      s1.f[W][c] = 0.0;
+      w0.f[W][c] = 0.f;
+    } else {
+      face(W);
+    }
+  }
   if (i < d.nx && j < d.ny && k < d.nz) {
     const double sdt = t.spdt[k];
     {

@@ -68,6 +68,7 @@ struct Flags {
   int split_fast;
   int acoustic_mode;     // 0 explicit FB, 1 reference HEVI, 2 consistent HEVI
   double hevi_beta;
+  int w_rigid;           // w = 0 on the ground and lid faces after every step
 };
 
 __host__ __device__ inline int iclamp(int v, int lo, int hi) { return v < lo ? lo : (v > hi ? hi : v); }

@@ -48,7 +48,7 @@ class Setup(ctypes.Structure):
         ("sponge_alpha", _D), ("sponge_start_fraction", _D),
         ("divergence_damping", _D), ("divergence_order", _I),
         ("pgf_perturbation", _I), ("acoustic_mode", _I), ("hevi_beta", _D),
-        ("split_fast", _I), ("weno_advective", _I),
+        ("split_fast", _I), ("weno_advective", _I), ("w_rigid", _I),
     ]
 
     @classmethod
