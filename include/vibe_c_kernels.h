@@ -8,7 +8,8 @@
  * through device memory on an internal stream; the *_dev entry points take
  * device pointers and a stream and never copy.
  *
- * Conventions kept from c_kernels.h:13-19: all scalars double; errors are
+ * Conventions kept from c_kernels.h:13-19: scalars double (float in the
+ * *_f32 twins, h:15-16); errors are
  * return codes, never errno; no global state visible to the caller.
  * Differences, each deliberate:
  *   - vibe_tridiagonal_solve_f64 solves the system its contract documents
@@ -126,6 +127,48 @@ int vibe_advect_scalar_flux_f64_dev(const double *q, const double *rho,
                                     const double *zs, int nx, int ny, int nz,
                                     double dx, double dy, double z_top,
                                     double *dqdt, vibe_stream_t stream);
+
+/* ---- FP32 twins: the *_f32 names c_kernels.h:15-16 reserves for the
+ * single-precision build (the reference declares none). Same contracts as
+ * the FP64 functions above, arithmetic and storage in float. ---- */
+int vibe_tridiagonal_solve_f32(const float *a, const float *b, const float *c,
+                               const float *d, int n, float *x, float *ws);
+void vibe_weno5_reconstruct_f32(float qm2, float qm1, float q0, float q1,
+                                float q2, float *q_left, float *q_right);
+float vibe_bilinear_f32(const float *f, int halo, int nsx, int nsy, int nz,
+                        float xi, float yj, int k);
+float vibe_cfl_scan_f32(const float *u, const float *v, const float *w,
+                        const float *dzeta, const float *zs, int nx, int ny,
+                        int nz, float dx, float dy, float z_top, float dt,
+                        float *max_wind_out, float *min_dz_out);
+float vibe_neumaier_sum_f32(const float *x, size_t n);
+void vibe_advect_scalar_flux_f32(const float *q, const float *rho,
+                                 const float *u, const float *v, const float *w,
+                                 const float *dzeta, const float *zs, int nx,
+                                 int ny, int nz, float dx, float dy,
+                                 float z_top, float *dqdt);
+int vibe_tridiagonal_solve_batched_f32(const float *a, const float *b,
+                                       const float *c, const float *d, int n,
+                                       int n_sys, float *x);
+int vibe_tridiagonal_solve_batched_f32_dev(const float *a, const float *b,
+                                           const float *c, const float *d,
+                                           int n, int n_sys, float *x,
+                                           int *status, vibe_stream_t stream);
+int vibe_weno5_reconstruct_batched_f32_dev(const float *q, size_t n,
+                                           float *q_left, float *q_right,
+                                           vibe_stream_t stream);
+int vibe_cfl_scan_f32_dev(const float *u, const float *v, const float *w,
+                          const float *dzeta, const float *zs, int nx, int ny,
+                          int nz, float dx, float dy, float z_top, float dt,
+                          float *out3, vibe_stream_t stream);
+int vibe_neumaier_sum_f32_dev(const float *x, size_t n, float *out,
+                              vibe_stream_t stream);
+int vibe_advect_scalar_flux_f32_dev(const float *q, const float *rho,
+                                    const float *u, const float *v,
+                                    const float *w, const float *dzeta,
+                                    const float *zs, int nx, int ny, int nz,
+                                    float dx, float dy, float z_top,
+                                    float *dqdt, vibe_stream_t stream);
 
 /* Message of the last device failure seen by this thread ("" if none). */
 const char *vibe_c_last_error(void);

@@ -179,3 +179,95 @@ def test_flux_advection_matches_oracle(vg, oc):
                                         dzeta.ctypes.data, zs.ctypes.data, nx, ny, nz, 900.0, 1100.0, 15000.0,
                                         out.ctypes.data)
     assert np.abs(dq - out).max() <= 1e-12 * np.abs(out).max()
+
+
+# ---- FP32 twins (the *_f32 names of c_kernels.h:15-16) -----------------------
+_F = ctypes.c_float
+_fp = ctypes.POINTER(ctypes.c_float)
+
+
+def f32(a):
+    return np.ascontiguousarray(a, dtype=np.float32)
+
+
+def _sig(vg, name, res, args):
+    fn = getattr(vg.lib, name)
+    fn.restype = res
+    fn.argtypes = args
+    return fn
+
+
+def test_f32_thomas(vg):
+    """diag(1,-4,1) known answer and variable coefficients at float precision;
+    singular and bad-argument codes as the FP64 form."""
+    fn = _sig(vg, "vibe_tridiagonal_solve_f32", ctypes.c_int, [ctypes.c_void_p] * 4 + [ctypes.c_int] +
+              [ctypes.c_void_p] * 2)
+    n = 24
+    j = np.arange(n)
+    for a, b, c, d in ((np.ones(n - 1), np.full(n, -4.0), np.ones(n - 1), np.ones(n)),
+                       (np.full(n - 1, -1.0), 4.0 + 0.1 * j, np.full(n - 1, -1.2), np.sin(0.3 * j))):
+        a32, b32, c32, d32 = f32(a), f32(b), f32(c), f32(d)
+        x, ws = np.zeros(n, np.float32), np.zeros(n, np.float32)
+        assert fn(a32.ctypes.data, b32.ctypes.data, c32.ctypes.data, d32.ctypes.data, n, x.ctypes.data,
+                  ws.ctypes.data) == 0
+        A = np.diag(b) + np.diag(a, -1) + np.diag(c, 1)
+        ref = np.linalg.solve(A, d)
+        assert np.abs(x - ref).max() <= 1e-5 * np.abs(ref).max()
+    z, one, x, ws = np.zeros(2, np.float32), np.ones(2, np.float32), np.zeros(2, np.float32), np.zeros(2, np.float32)
+    assert fn(None, z.ctypes.data, None, one.ctypes.data, 2, x.ctypes.data, ws.ctypes.data) == 1
+    assert fn(None, None, None, None, 2, x.ctypes.data, ws.ctypes.data) == 2
+
+
+def test_f32_weno_bilinear_cfl_neumaier_flux(vg, oc):
+    """Each twin against the FP64 entry point on the same (float-representable)
+    inputs: relative differences at float rounding."""
+    weno = _sig(vg, "vibe_weno5_reconstruct_f32", None, [_F] * 5 + [_fp, _fp])
+    rng = np.random.default_rng(9)
+    for _ in range(20):
+        q = f32(rng.standard_normal(5)).astype(np.float64)
+        l32, r32 = _F(), _F()
+        weno(*[float(v) for v in q], ctypes.byref(l32), ctypes.byref(r32))
+        l64, r64 = vg.weno5_reconstruct(*q)
+        assert abs(l32.value - l64) <= 2e-5 * max(1.0, abs(l64)) and abs(r32.value - r64) <= 2e-5 * max(1.0, abs(r64))
+
+    bil = _sig(vg, "vibe_bilinear_f32", _F, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                               ctypes.c_int, _F, _F, ctypes.c_int])
+    halo, nx, ny, nz = 2, 7, 5, 3
+    nsx, nsy = nx + 2 * halo, ny + 2 * halo
+    f = f32(rng.standard_normal(nsx * nsy * (nz + 2 * halo)))
+    for xi, yj, k in ((2.25, 1.5, 1), (-3.0, 9.0, 0), (5.75, 3.125, 2)):
+        got = bil(f.ctypes.data, halo, nsx, nsy, nz, xi, yj, k)
+        ref = vg.bilinear(f.astype(np.float64), halo, nsx, nsy, nz, xi, yj, k)
+        assert abs(got - ref) <= 1e-5 * max(1.0, abs(ref))
+
+    cfl = _sig(vg, "vibe_cfl_scan_f32", _F, [ctypes.c_void_p] * 5 + [ctypes.c_int] * 3 + [_F] * 4 + [_fp, _fp])
+    nx, ny, nz = 37, 23, 19
+    n = nx * ny * nz
+    u, v, w = (f32(rng.standard_normal(n) * s) for s in (15.0, 10.0, 2.0))
+    dzeta, zs = f32(rng.random(nz) * 0.1 + 1e-3), f32(rng.random(nx * ny) * 500.0)
+    mw, mdz = _F(), _F()
+    got = cfl(u.ctypes.data, v.ctypes.data, w.ctypes.data, dzeta.ctypes.data, zs.ctypes.data, nx, ny, nz, 1000.0,
+              800.0, 20000.0, 6.0, ctypes.byref(mw), ctypes.byref(mdz))
+    r, m64, d64 = vg.cfl_scan(*(a.astype(np.float64) for a in (u, v, w, dzeta, zs)), nx, ny, nz, 1000.0, 800.0,
+                              20000.0, 6.0)
+    assert abs(got - r) <= 1e-5 * r and abs(mw.value - m64) <= 1e-5 * m64 and abs(mdz.value - d64) <= 1e-5 * d64
+
+    neu = _sig(vg, "vibe_neumaier_sum_f32", _F, [ctypes.c_void_p, ctypes.c_size_t])
+    x = np.ones(10000, np.float32)
+    x[0], x[-1] = 1e8, -1e8
+    assert neu(x.ctypes.data, x.size) == 9998.0  # compensation recovers what a plain float sum loses
+    y = f32(rng.standard_normal(1_000_003))
+    assert abs(neu(y.ctypes.data, y.size) - y.astype(np.float64).sum()) <= 1e-6 * np.abs(y).sum()
+
+    flux = _sig(vg, "vibe_advect_scalar_flux_f32", None, [ctypes.c_void_p] * 7 + [ctypes.c_int] * 3 + [_F] * 3 +
+                [ctypes.c_void_p])
+    nx, ny, nz = 33, 17, 9
+    n = nx * ny * nz
+    q, rho = f32(rng.random(n)), f32(1.0 + 0.1 * rng.random(n))
+    u, v, w = (f32(rng.standard_normal(n)) for _ in range(3))
+    dzeta, zs = f32(rng.random(nz) * 0.1 + 0.01), f32(rng.random(nx * ny) * 300.0)
+    out = np.zeros(n, np.float32)
+    flux(*(a.ctypes.data for a in (q, rho, u, v, w, dzeta, zs)), nx, ny, nz, 900.0, 1100.0, 15000.0, out.ctypes.data)
+    ref = vg.advect_scalar_flux(*(a.astype(np.float64) for a in (q, rho, u, v, w, dzeta, zs)), nx, ny, nz, 900.0,
+                                1100.0, 15000.0)
+    assert np.abs(out - ref).max() <= 1e-4 * np.abs(ref).max()

@@ -78,34 +78,35 @@ struct DBuf {
 // recurrence of thomas_solve (src/time/helmholtz.cpp:71-85); NULL a/c read
 // as 0; exact-zero pivots give VIBE_C_ERR_SINGULAR as c_kernels.c:26,34,40.
 // cp (the modified super-diagonal) lives in `work` (n per system).
-__global__ void k_thomas_batched(const double* __restrict__ a, const double* __restrict__ b,
-                                 const double* __restrict__ c, const double* __restrict__ d, int n, int n_sys,
-                                 double* __restrict__ x, double* __restrict__ work, int* __restrict__ status) {
+template <typename T>
+__global__ void k_thomas_batched(const T* __restrict__ a, const T* __restrict__ b, const T* __restrict__ c,
+                                 const T* __restrict__ d, int n, int n_sys, T* __restrict__ x, T* __restrict__ work,
+                                 int* __restrict__ status) {
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= n_sys) return;
-  const double* as = a ? a + (size_t)s * (n - 1) : nullptr;
-  const double* bs = b + (size_t)s * n;
-  const double* cs = c ? c + (size_t)s * (n - 1) : nullptr;
-  const double* ds = d + (size_t)s * n;
-  double* xs = x + (size_t)s * n;
-  double* cp = work + (size_t)s * n;
+  const T* as = a ? a + (size_t)s * (n - 1) : nullptr;
+  const T* bs = b + (size_t)s * n;
+  const T* cs = c ? c + (size_t)s * (n - 1) : nullptr;
+  const T* ds = d + (size_t)s * n;
+  T* xs = x + (size_t)s * n;
+  T* cp = work + (size_t)s * n;
   int rc = VIBE_C_OK;
   if (n == 1) {
-    if (bs[0] == 0.0) rc = VIBE_C_ERR_SINGULAR;
+    if (bs[0] == (T)0) rc = VIBE_C_ERR_SINGULAR;
     else xs[0] = ds[0] / bs[0];
   } else {
-    double denom = bs[0];
-    if (denom == 0.0) {
+    T denom = bs[0];
+    if (denom == (T)0) {
       rc = VIBE_C_ERR_SINGULAR;
     } else {
-      cp[0] = (cs ? cs[0] : 0.0) / denom;
+      cp[0] = (cs ? cs[0] : (T)0) / denom;
       xs[0] = ds[0] / denom;
       for (int k = 1; k < n; ++k) {
-        const double am = as ? as[k - 1] : 0.0;
+        const T am = as ? as[k - 1] : (T)0;
         denom = bs[k] - am * cp[k - 1];
-        if (denom == 0.0) { rc = VIBE_C_ERR_SINGULAR; break; }
+        if (denom == (T)0) { rc = VIBE_C_ERR_SINGULAR; break; }
         xs[k] = (ds[k] - am * xs[k - 1]) / denom;
-        if (k < n - 1) cp[k] = (cs ? cs[k] : 0.0) / denom;
+        if (k < n - 1) cp[k] = (cs ? cs[k] : (T)0) / denom;
       }
       if (rc == VIBE_C_OK)
         for (int k = n - 1; k-- > 0;) xs[k] = xs[k] - cp[k] * xs[k + 1];
@@ -115,70 +116,77 @@ __global__ void k_thomas_batched(const double* __restrict__ a, const double* __r
 }
 
 // WENO5 (c_kernels.c:64-104), one thread per stencil
-__device__ void weno5_d(double qm2, double qm1, double q0, double q1, double q2, double* ql, double* qr) {
-  const double eps = 1e-6, d0 = 0.1, d1 = 0.6, d2 = 0.3;
-  const double v0 = (2.0 * qm2 - 7.0 * qm1 + 11.0 * q0) / 6.0;
-  const double v1 = (-qm1 + 5.0 * q0 + 2.0 * q1) / 6.0;
-  const double v2 = (2.0 * q0 + 5.0 * q1 - q2) / 6.0;
-  const double b0 = (13.0 / 12.0) * (qm2 - 2.0 * qm1 + q0) * (qm2 - 2.0 * qm1 + q0) +
-                    0.25 * (qm2 - 4.0 * qm1 + 3.0 * q0) * (qm2 - 4.0 * qm1 + 3.0 * q0);
-  const double b1 = (13.0 / 12.0) * (qm1 - 2.0 * q0 + q1) * (qm1 - 2.0 * q0 + q1) + 0.25 * (qm1 - q1) * (qm1 - q1);
-  const double b2 = (13.0 / 12.0) * (q0 - 2.0 * q1 + q2) * (q0 - 2.0 * q1 + q2) +
-                    0.25 * (3.0 * q0 - 4.0 * q1 + q2) * (3.0 * q0 - 4.0 * q1 + q2);
-  const double a0 = d0 / ((eps + b0) * (eps + b0)), a1 = d1 / ((eps + b1) * (eps + b1)),
+template <typename T>
+__device__ void weno5_d(T qm2, T qm1, T q0, T q1, T q2, T* ql, T* qr) {
+  const T eps = (T)1e-6, d0 = (T)0.1, d1 = (T)0.6, d2 = (T)0.3;
+  const T t12 = (T)13 / (T)12, q4 = (T)0.25;
+  const T v0 = ((T)2.0 * qm2 - (T)7.0 * qm1 + (T)11.0 * q0) / (T)6;
+  const T v1 = (-qm1 + (T)5.0 * q0 + (T)2.0 * q1) / (T)6;
+  const T v2 = ((T)2.0 * q0 + (T)5.0 * q1 - q2) / (T)6;
+  const T b0 = t12 * (qm2 - (T)2.0 * qm1 + q0) * (qm2 - (T)2.0 * qm1 + q0) +
+                    q4 * (qm2 - (T)4.0 * qm1 + (T)3.0 * q0) * (qm2 - (T)4.0 * qm1 + (T)3.0 * q0);
+  const T b1 = t12 * (qm1 - (T)2.0 * q0 + q1) * (qm1 - (T)2.0 * q0 + q1) + q4 * (qm1 - q1) * (qm1 - q1);
+  const T b2 = t12 * (q0 - (T)2.0 * q1 + q2) * (q0 - (T)2.0 * q1 + q2) +
+                    q4 * ((T)3.0 * q0 - (T)4.0 * q1 + q2) * ((T)3.0 * q0 - (T)4.0 * q1 + q2);
+  const T a0 = d0 / ((eps + b0) * (eps + b0)), a1 = d1 / ((eps + b1) * (eps + b1)),
                a2 = d2 / ((eps + b2) * (eps + b2));
   *ql = (a0 * v0 + a1 * v1 + a2 * v2) / (a0 + a1 + a2);
-  const double u0 = (2.0 * q2 - 7.0 * q1 + 11.0 * q0) / 6.0;
-  const double u1 = (-q1 + 5.0 * q0 + 2.0 * qm1) / 6.0;
-  const double u2 = (2.0 * q0 + 5.0 * qm1 - qm2) / 6.0;
-  const double g0 = (13.0 / 12.0) * (q2 - 2.0 * q1 + q0) * (q2 - 2.0 * q1 + q0) +
-                    0.25 * (q2 - 4.0 * q1 + 3.0 * q0) * (q2 - 4.0 * q1 + 3.0 * q0);
-  const double g1 = (13.0 / 12.0) * (q1 - 2.0 * q0 + qm1) * (q1 - 2.0 * q0 + qm1) + 0.25 * (q1 - qm1) * (q1 - qm1);
-  const double g2 = (13.0 / 12.0) * (q0 - 2.0 * qm1 + qm2) * (q0 - 2.0 * qm1 + qm2) +
-                    0.25 * (3.0 * q0 - 4.0 * qm1 + qm2) * (3.0 * q0 - 4.0 * qm1 + qm2);
-  const double c0 = d0 / ((eps + g0) * (eps + g0)), c1 = d1 / ((eps + g1) * (eps + g1)),
+  const T u0 = ((T)2.0 * q2 - (T)7.0 * q1 + (T)11.0 * q0) / (T)6;
+  const T u1 = (-q1 + (T)5.0 * q0 + (T)2.0 * qm1) / (T)6;
+  const T u2 = ((T)2.0 * q0 + (T)5.0 * qm1 - qm2) / (T)6;
+  const T g0 = t12 * (q2 - (T)2.0 * q1 + q0) * (q2 - (T)2.0 * q1 + q0) +
+                    q4 * (q2 - (T)4.0 * q1 + (T)3.0 * q0) * (q2 - (T)4.0 * q1 + (T)3.0 * q0);
+  const T g1 = t12 * (q1 - (T)2.0 * q0 + qm1) * (q1 - (T)2.0 * q0 + qm1) + q4 * (q1 - qm1) * (q1 - qm1);
+  const T g2 = t12 * (q0 - (T)2.0 * qm1 + qm2) * (q0 - (T)2.0 * qm1 + qm2) +
+                    q4 * ((T)3.0 * q0 - (T)4.0 * qm1 + qm2) * ((T)3.0 * q0 - (T)4.0 * qm1 + qm2);
+  const T c0 = d0 / ((eps + g0) * (eps + g0)), c1 = d1 / ((eps + g1) * (eps + g1)),
                c2 = d2 / ((eps + g2) * (eps + g2));
   *qr = (c0 * u0 + c1 * u1 + c2 * u2) / (c0 + c1 + c2);
 }
-__global__ void k_weno_batched(const double* __restrict__ q, size_t n, double* __restrict__ ql, double* __restrict__ qr) {
+template <typename T>
+__global__ void k_weno_batched(const T* __restrict__ q, size_t n, T* __restrict__ ql, T* __restrict__ qr) {
   for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x)
     weno5_d(q[5 * e], q[5 * e + 1], q[5 * e + 2], q[5 * e + 3], q[5 * e + 4], ql + e, qr + e);
 }
 
 // bilinear (c_kernels.c:108-144) on one level plane held in `plane`
-__global__ void k_bilinear(const double* __restrict__ plane, int halo, int nsx, int nsy, double xi, double yj,
-                           double* out) {
+template <typename T>
+__global__ void k_bilinear(const T* __restrict__ plane, int halo, int nsx, int nsy, T xi, T yj, T* out) {
   const int nxi = nsx - 2 * halo, nyi = nsy - 2 * halo;
   const int i0 = (int)floor(xi), j0 = (int)floor(yj);
-  const double wx = xi - (double)i0, wy = yj - (double)j0;
+  const T wx = xi - (T)i0, wy = yj - (T)j0;
   const int ia = vgb::iclamp(i0, 0, nxi - 1), ib = vgb::iclamp(i0 + 1, 0, nxi - 1);
   const int ja = vgb::iclamp(j0, 0, nyi - 1), jb = vgb::iclamp(j0 + 1, 0, nyi - 1);
   auto at = [&](int i, int j) { return plane[(size_t)(j + halo) * nsx + (size_t)(i + halo)]; };
-  const double q00 = at(ia, ja), q10 = at(ib, ja), q01 = at(ia, jb), q11 = at(ib, jb);
+  const T q00 = at(ia, ja), q10 = at(ib, ja), q01 = at(ia, jb), q11 = at(ib, jb);
   *out = (q00 + wx * (q10 - q00)) + wy * ((q01 + wx * (q11 - q01)) - (q00 + wx * (q10 - q00)));
 }
 
 // ---- reductions ----------------------------------------------------------
+template <typename T>
 struct Neu {
-  double s, c;
+  T s, c;
 };
 // Neumaier add of one value (c_kernels.c:195-203)
-__device__ __forceinline__ void neu_add(Neu& a, double x) {
-  const double t = a.s + x;
+template <typename T>
+__device__ __forceinline__ void neu_add(Neu<T>& a, T x) {
+  const T t = a.s + x;
   if (fabs(a.s) >= fabs(x)) a.c += (a.s - t) + x;
   else a.c += (x - t) + a.s;
   a.s = t;
 }
 // merge of two compensated partial sums: add b.s with compensation, then b.c
-__device__ __forceinline__ Neu neu_merge(Neu a, Neu b) {
+template <typename T>
+__device__ __forceinline__ Neu<T> neu_merge(Neu<T> a, Neu<T> b) {
   neu_add(a, b.s);
   a.c += b.c;
   return a;
 }
-__device__ Neu neu_block(Neu v) {
-  __shared__ double sh_s[32], sh_c[32];
+template <typename T>
+__device__ Neu<T> neu_block(Neu<T> v) {
+  __shared__ T sh_s[32], sh_c[32];
   for (int off = 16; off > 0; off >>= 1) {
-    Neu o;
+    Neu<T> o;
     o.s = __shfl_down_sync(0xffffffffu, v.s, off);
     o.c = __shfl_down_sync(0xffffffffu, v.c, off);
     v = neu_merge(v, o);
@@ -188,10 +196,10 @@ __device__ Neu neu_block(Neu v) {
   __syncthreads();
   const int nw = (blockDim.x + 31) >> 5;
   if (warp == 0) {
-    v.s = lane < nw ? sh_s[lane] : 0.0;
-    v.c = lane < nw ? sh_c[lane] : 0.0;
+    v.s = lane < nw ? sh_s[lane] : (T)0;
+    v.c = lane < nw ? sh_c[lane] : (T)0;
     for (int off = 16; off > 0; off >>= 1) {
-      Neu o;
+      Neu<T> o;
       o.s = __shfl_down_sync(0xffffffffu, v.s, off);
       o.c = __shfl_down_sync(0xffffffffu, v.c, off);
       v = neu_merge(v, o);
@@ -200,16 +208,18 @@ __device__ Neu neu_block(Neu v) {
   return v;
 }
 // each block sums a contiguous chunk; partials[2*block] = (s, c)
-__global__ void k_neu_partial(const double* __restrict__ x, size_t n, size_t chunk, double* __restrict__ partials) {
+template <typename T>
+__global__ void k_neu_partial(const T* __restrict__ x, size_t n, size_t chunk, T* __restrict__ partials) {
   const size_t lo = (size_t)blockIdx.x * chunk, hi = lo + chunk < n ? lo + chunk : n;
-  Neu v{0.0, 0.0};
+  Neu<T> v{(T)0, (T)0};
   for (size_t e = lo + threadIdx.x; e < hi; e += blockDim.x) neu_add(v, x[e]);
   v = neu_block(v);
   if (threadIdx.x == 0) { partials[2 * blockIdx.x] = v.s; partials[2 * blockIdx.x + 1] = v.c; }
 }
-__global__ void k_neu_final(const double* __restrict__ partials, int nb, double* __restrict__ out) {
-  Neu v{0.0, 0.0};
-  for (int b = threadIdx.x; b < nb; b += blockDim.x) v = neu_merge(v, Neu{partials[2 * b], partials[2 * b + 1]});
+template <typename T>
+__global__ void k_neu_final(const T* __restrict__ partials, int nb, T* __restrict__ out) {
+  Neu<T> v{(T)0, (T)0};
+  for (int b = threadIdx.x; b < nb; b += blockDim.x) v = neu_merge(v, Neu<T>{partials[2 * b], partials[2 * b + 1]});
   v = neu_block(v);
   if (threadIdx.x == 0) *out = v.s + v.c;
 }
@@ -217,8 +227,9 @@ __global__ void k_neu_final(const double* __restrict__ partials, int nb, double*
 // CFL scan (c_kernels.c:148-186): per cell dz = max(dzeta[k]*scale, 1),
 // speed = sqrt(u^2+v^2+w^2), cfl = dt*(|u|/dx + |v|/dy + |w|/dz); block maxima
 // of (cfl, speed) and min of dz, then one block merges.
-__device__ __forceinline__ void max3_block(double& a, double& b, double& c) {  // max, max, min
-  __shared__ double s1[32], s2[32], s3[32];
+template <typename T>
+__device__ __forceinline__ void max3_block(T& a, T& b, T& c) {  // max, max, min
+  __shared__ T s1[32], s2[32], s3[32];
   for (int off = 16; off > 0; off >>= 1) {
     a = fmax(a, __shfl_down_sync(0xffffffffu, a, off));
     b = fmax(b, __shfl_down_sync(0xffffffffu, b, off));
@@ -228,9 +239,9 @@ __device__ __forceinline__ void max3_block(double& a, double& b, double& c) {  /
   if (lane == 0) { s1[warp] = a; s2[warp] = b; s3[warp] = c; }
   __syncthreads();
   if (warp == 0) {
-    a = lane < nw ? s1[lane] : 0.0;
-    b = lane < nw ? s2[lane] : 0.0;
-    c = lane < nw ? s3[lane] : 1e30;
+    a = lane < nw ? s1[lane] : (T)0;
+    b = lane < nw ? s2[lane] : (T)0;
+    c = lane < nw ? s3[lane] : (T)1e30;
     for (int off = 16; off > 0; off >>= 1) {
       a = fmax(a, __shfl_down_sync(0xffffffffu, a, off));
       b = fmax(b, __shfl_down_sync(0xffffffffu, b, off));
@@ -238,18 +249,19 @@ __device__ __forceinline__ void max3_block(double& a, double& b, double& c) {  /
     }
   }
 }
-__global__ void k_cfl_partial(const double* __restrict__ u, const double* __restrict__ v, const double* __restrict__ w,
-                              const double* __restrict__ dzeta, const double* __restrict__ zs, int nx, int ny, int nz,
-                              double dx, double dy, double z_top, double dt, double* __restrict__ partials) {
+template <typename T>
+__global__ void k_cfl_partial(const T* __restrict__ u, const T* __restrict__ v, const T* __restrict__ w,
+                              const T* __restrict__ dzeta, const T* __restrict__ zs, int nx, int ny, int nz, T dx, T dy,
+                              T z_top, T dt, T* __restrict__ partials) {
   const size_t n = (size_t)nx * ny * nz, nxy = (size_t)nx * ny;
-  double worst = 0.0, mw = 0.0, mdz = 1e30;
+  T worst = 0, mw = 0, mdz = (T)1e30;
   for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x) {
     const int k = (int)(e / nxy);
     const size_t col = e % nxy;
-    const double uu = u[e], vv = v[e], ww = w[e];
-    const double scale = zs ? (z_top - zs[col]) : z_top;
-    double dz = dzeta[k] * scale;
-    if (dz < 1.0) dz = 1.0;
+    const T uu = u[e], vv = v[e], ww = w[e];
+    const T scale = zs ? (z_top - zs[col]) : z_top;
+    T dz = dzeta[k] * scale;
+    if (dz < (T)1) dz = (T)1;
     mdz = fmin(mdz, dz);
     mw = fmax(mw, sqrt(uu * uu + vv * vv + ww * ww));
     worst = fmax(worst, dt * (fabs(uu) / dx + fabs(vv) / dy + fabs(ww) / dz));
@@ -261,8 +273,9 @@ __global__ void k_cfl_partial(const double* __restrict__ u, const double* __rest
     partials[3 * blockIdx.x + 2] = mdz;
   }
 }
-__global__ void k_cfl_final(const double* __restrict__ partials, int nb, double* __restrict__ out3) {
-  double a = 0.0, b = 0.0, c = 1e30;
+template <typename T>
+__global__ void k_cfl_final(const T* __restrict__ partials, int nb, T* __restrict__ out3) {
+  T a = 0, b = 0, c = (T)1e30;
   for (int e = threadIdx.x; e < nb; e += blockDim.x) {
     a = fmax(a, partials[3 * e]);
     b = fmax(b, partials[3 * e + 1]);
@@ -272,42 +285,42 @@ __global__ void k_cfl_final(const double* __restrict__ partials, int nb, double*
   if (threadIdx.x == 0) {
     out3[0] = a;
     out3[1] = b;
-    out3[2] = (c > 1e29) ? 0.0 : c;
+    out3[2] = (c > (T)1e29) ? (T)0 : c;
   }
 }
 
 // flux advection (c_kernels.c:209-286), one thread per cell
-__global__ void k_flux_adv(const double* __restrict__ q, const double* __restrict__ rho, const double* __restrict__ u,
-                           const double* __restrict__ v, const double* __restrict__ w, const double* __restrict__ dzeta,
-                           const double* __restrict__ zs, int nx, int ny, int nz, double dx, double dy, double z_top,
-                           double* __restrict__ dqdt) {
+template <typename T>
+__global__ void k_flux_adv(const T* __restrict__ q, const T* __restrict__ rho, const T* __restrict__ u,
+                           const T* __restrict__ v, const T* __restrict__ w, const T* __restrict__ dzeta,
+                           const T* __restrict__ zs, int nx, int ny, int nz, T dx, T dy, T z_top, T* __restrict__ dqdt) {
   const size_t nxy = (size_t)nx * ny, n = nxy * nz;
-  const double inv_dx = 1.0 / dx, inv_dy = 1.0 / dy;
+  const T inv_dx = (T)1 / dx, inv_dy = (T)1 / dy, hf = (T)0.5;
   for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < n; idx += (size_t)gridDim.x * blockDim.x) {
     const int k = (int)(idx / nxy);
     const int j = (int)((idx / nx) % ny);
     const int i = (int)(idx % nx);
     const size_t base_k = (size_t)k * nxy;
-    const double scale = zs ? (z_top - zs[(size_t)j * nx + i]) : z_top;
-    double dz = dzeta[k] * scale;
-    if (dz < 1.0) dz = 1.0;
+    const T scale = zs ? (z_top - zs[(size_t)j * nx + i]) : z_top;
+    T dz = dzeta[k] * scale;
+    if (dz < (T)1) dz = (T)1;
     const size_t c = idx;
     const size_t e = base_k + (size_t)j * nx + (size_t)((i + 1) % nx);
     const size_t ws = base_k + (size_t)j * nx + (size_t)((i + nx - 1) % nx);
-    const double fxE = u[e] * (0.5 * (rho[c] + rho[e])) * (0.5 * (q[c] + q[e]));
-    const double fxW = u[c] * (0.5 * (rho[ws] + rho[c])) * (0.5 * (q[ws] + q[c]));
+    const T fxE = u[e] * (hf * (rho[c] + rho[e])) * (hf * (q[c] + q[e]));
+    const T fxW = u[c] * (hf * (rho[ws] + rho[c])) * (hf * (q[ws] + q[c]));
     const size_t nn = base_k + (size_t)((j + 1) % ny) * nx + (size_t)i;
     const size_t ss = base_k + (size_t)((j + ny - 1) % ny) * nx + (size_t)i;
-    const double fyN = v[nn] * (0.5 * (rho[c] + rho[nn])) * (0.5 * (q[c] + q[nn]));
-    const double fyS = v[c] * (0.5 * (rho[ss] + rho[c])) * (0.5 * (q[ss] + q[c]));
-    double fzT = 0.0, fzB = 0.0;
+    const T fyN = v[nn] * (hf * (rho[c] + rho[nn])) * (hf * (q[c] + q[nn]));
+    const T fyS = v[c] * (hf * (rho[ss] + rho[c])) * (hf * (q[ss] + q[c]));
+    T fzT = 0, fzB = 0;
     if (k > 0 && k + 1 < nz) {
       const size_t t = c + nxy, b = c - nxy;
-      fzT = w[t] * (0.5 * (rho[c] + rho[t])) * (0.5 * (q[c] + q[t]));
-      fzB = w[c] * (0.5 * (rho[b] + rho[c])) * (0.5 * (q[b] + q[c]));
+      fzT = w[t] * (hf * (rho[c] + rho[t])) * (hf * (q[c] + q[t]));
+      fzB = w[c] * (hf * (rho[b] + rho[c])) * (hf * (q[b] + q[c]));
     }
-    const double div = (fxE - fxW) * inv_dx + (fyN - fyS) * inv_dy + (fzT - fzB) / dz;
-    const double rr = (rho[idx] > 1e-12) ? rho[idx] : 1e-12;
+    const T div = (fxE - fxW) * inv_dx + (fyN - fyS) * inv_dy + (fzT - fzB) / dz;
+    const T rr = (rho[idx] > (T)1e-12) ? rho[idx] : (T)1e-12;
     dqdt[idx] = -div / rr;
   }
 }
@@ -333,20 +346,210 @@ double* g_noalloc_ptr[64] = {};
 constexpr int kRedBlocks = 304;  // 2 x 152 SMs
 constexpr int kRedThreads = 256;
 
+// ---- entry points, one template per ABI function: T = double (the
+// reference's *_f64 names) or float (the *_f32 twins its header reserves,
+// c_kernels.h:15-16) ----
+template <typename T>
+int thomas_batched_dev(const T* a, const T* b, const T* c, const T* d, int n, int n_sys, T* x, int* status,
+                       vibe_stream_t stream) {
+  if (n <= 0 || n_sys < 0 || b == nullptr || d == nullptr || x == nullptr) return VIBE_C_ERR_BAD_ARG;
+  if (n_sys == 0) return VIBE_C_OK;
+  T* work = (T*)scratch((size_t)n * n_sys * sizeof(T));
+  if (!work) { g_cerr = "scratch allocation failed"; return VIBE_C_ERR_DEVICE; }
+  k_thomas_batched<T><<<(n_sys + 127) / 128, 128, 0, (cudaStream_t)stream>>>(a, b, c, d, n, n_sys, x, work, status);
+  return device_ok(cudaGetLastError(), "thomas launch") ? VIBE_C_OK : VIBE_C_ERR_DEVICE;
+}
+
+template <typename T>
+int thomas_batched_host(const T* a, const T* b, const T* c, const T* d, int n, int n_sys, T* x) {
+  if (n <= 0 || n_sys < 0 || b == nullptr || d == nullptr || x == nullptr) return VIBE_C_ERR_BAD_ARG;
+  if (n_sys == 0) return VIBE_C_OK;
+  const size_t e = sizeof(T), nn = (size_t)n * n_sys, no = (size_t)(n - 1) * n_sys;
+  DBuf da(a ? no * e + e : 0), db(nn * e), dc(c ? no * e + e : 0), dd(nn * e), dx(nn * e), ds((size_t)n_sys * 4);
+  if (!db.p || !dd.p || !dx.p || !ds.p || (a && !da.p) || (c && !dc.p)) { g_cerr = "cudaMalloc failed"; return VIBE_C_ERR_DEVICE; }
+  cudaStream_t st = own_stream();
+  bool ok = true;
+  if (a && no) ok &= device_ok(cudaMemcpyAsync(da.p, a, no * e, cudaMemcpyHostToDevice, st), "H2D a");
+  if (c && no) ok &= device_ok(cudaMemcpyAsync(dc.p, c, no * e, cudaMemcpyHostToDevice, st), "H2D c");
+  ok &= device_ok(cudaMemcpyAsync(db.p, b, nn * e, cudaMemcpyHostToDevice, st), "H2D b");
+  ok &= device_ok(cudaMemcpyAsync(dd.p, d, nn * e, cudaMemcpyHostToDevice, st), "H2D d");
+  if (!ok) return VIBE_C_ERR_DEVICE;
+  int rc = thomas_batched_dev<T>(a ? da.as<T>() : nullptr, db.as<T>(), c ? dc.as<T>() : nullptr, dd.as<T>(), n, n_sys,
+                                 dx.as<T>(), ds.as<int>(), (vibe_stream_t)st);
+  if (rc) return rc;
+  std::string st_host((size_t)n_sys * 4, '\0');
+  ok &= device_ok(cudaMemcpyAsync(x, dx.p, nn * e, cudaMemcpyDeviceToHost, st), "D2H x");
+  ok &= device_ok(cudaMemcpyAsync(&st_host[0], ds.p, (size_t)n_sys * 4, cudaMemcpyDeviceToHost, st), "D2H status");
+  ok &= device_ok(cudaStreamSynchronize(st), "sync");
+  if (!ok) return VIBE_C_ERR_DEVICE;
+  const int* sv = (const int*)st_host.data();
+  for (int s = 0; s < n_sys; ++s)
+    if (sv[s] != VIBE_C_OK) return sv[s];
+  return VIBE_C_OK;
+}
+
+template <typename T>
+int weno_batched_dev(const T* q, size_t n, T* q_left, T* q_right, vibe_stream_t stream) {
+  if (!q || !q_left || !q_right) return VIBE_C_ERR_BAD_ARG;
+  if (n == 0) return VIBE_C_OK;
+  const int blocks = (int)((n + 255) / 256 < 65535 ? (n + 255) / 256 : 65535);
+  k_weno_batched<T><<<blocks, 256, 0, (cudaStream_t)stream>>>(q, n, q_left, q_right);
+  return device_ok(cudaGetLastError(), "weno launch") ? VIBE_C_OK : VIBE_C_ERR_DEVICE;
+}
+
+template <typename T>
+void weno_host(T qm2, T qm1, T q0, T q1, T q2, T* q_left, T* q_right) {
+  if (q_left == nullptr || q_right == nullptr) return;
+  const size_t e = sizeof(T);
+  DBuf dq(5 * e), dl(e), dr(e);
+  if (!dq.p || !dl.p || !dr.p) { g_cerr = "cudaMalloc failed"; *q_left = *q_right = (T)NAN; return; }
+  const T q[5] = {qm2, qm1, q0, q1, q2};
+  cudaStream_t st = own_stream();
+  bool ok = device_ok(cudaMemcpyAsync(dq.p, q, 5 * e, cudaMemcpyHostToDevice, st), "H2D");
+  ok = ok && weno_batched_dev<T>(dq.as<T>(), 1, dl.as<T>(), dr.as<T>(), (vibe_stream_t)st) == VIBE_C_OK;
+  ok = ok && device_ok(cudaMemcpyAsync(q_left, dl.p, e, cudaMemcpyDeviceToHost, st), "D2H");
+  ok = ok && device_ok(cudaMemcpyAsync(q_right, dr.p, e, cudaMemcpyDeviceToHost, st), "D2H");
+  ok = ok && device_ok(cudaStreamSynchronize(st), "sync");
+  if (!ok) *q_left = *q_right = (T)NAN;
+}
+
+template <typename T>
+T bilinear_host(const T* f, int halo, int nsx, int nsy, int nz, T xi, T yj, int k) {
+  if (f == nullptr || nz <= 0) return (T)0;
+  if (k < 0) k = 0;
+  if (k >= nz) k = nz - 1;
+  const size_t plane = (size_t)nsx * nsy, e = sizeof(T);
+  DBuf dp(plane * e), dout(e);
+  if (!dp.p || !dout.p) { g_cerr = "cudaMalloc failed"; return (T)NAN; }
+  cudaStream_t st = own_stream();
+  T r = (T)NAN;
+  bool ok = device_ok(cudaMemcpyAsync(dp.p, f + (size_t)(k + halo) * plane, plane * e, cudaMemcpyHostToDevice, st), "H2D");
+  if (ok) {
+    k_bilinear<T><<<1, 1, 0, st>>>(dp.as<T>(), halo, nsx, nsy, xi, yj, dout.as<T>());
+    ok = device_ok(cudaGetLastError(), "bilinear launch");
+  }
+  ok = ok && device_ok(cudaMemcpyAsync(&r, dout.p, e, cudaMemcpyDeviceToHost, st), "D2H");
+  ok = ok && device_ok(cudaStreamSynchronize(st), "sync");
+  return ok ? r : (T)NAN;
+}
+
+template <typename T>
+int cfl_dev(const T* u, const T* v, const T* w, const T* dzeta, const T* zs, int nx, int ny, int nz, T dx, T dy,
+            T z_top, T dt, T* out3, vibe_stream_t stream) {
+  if (!u || !v || !w || !dzeta || !out3 || nx < 0 || ny < 0 || nz < 0) return VIBE_C_ERR_BAD_ARG;
+  T* part = (T*)scratch((size_t)3 * kRedBlocks * sizeof(T));
+  if (!part) { g_cerr = "scratch allocation failed"; return VIBE_C_ERR_DEVICE; }
+  cudaStream_t st = (cudaStream_t)stream;
+  k_cfl_partial<T><<<kRedBlocks, kRedThreads, 0, st>>>(u, v, w, dzeta, zs, nx, ny, nz, dx, dy, z_top, dt, part);
+  k_cfl_final<T><<<1, kRedThreads, 0, st>>>(part, kRedBlocks, out3);
+  return device_ok(cudaGetLastError(), "cfl launch") ? VIBE_C_OK : VIBE_C_ERR_DEVICE;
+}
+
+template <typename T>
+T cfl_host(const T* u, const T* v, const T* w, const T* dzeta, const T* zs, int nx, int ny, int nz, T dx, T dy, T z_top,
+           T dt, T* max_wind_out, T* min_dz_out) {
+  if (u == nullptr || v == nullptr || w == nullptr || dzeta == nullptr) return (T)0;
+  const size_t e = sizeof(T);
+  const size_t n = (size_t)(nx > 0 ? nx : 0) * (ny > 0 ? ny : 0) * (nz > 0 ? nz : 0);
+  const size_t nzp = (size_t)(nz > 0 ? nz : 0);
+  DBuf du(n * e + e), dv(n * e + e), dw(n * e + e), dz(nzp * e + e), dzs(zs ? (size_t)nx * ny * e + e : 0), dout(3 * e);
+  if (!du.p || !dv.p || !dw.p || !dz.p || !dout.p || (zs && !dzs.p)) { g_cerr = "cudaMalloc failed"; return (T)NAN; }
+  cudaStream_t st = own_stream();
+  bool ok = true;
+  ok &= device_ok(cudaMemcpyAsync(du.p, u, n * e, cudaMemcpyHostToDevice, st), "H2D");
+  ok &= device_ok(cudaMemcpyAsync(dv.p, v, n * e, cudaMemcpyHostToDevice, st), "H2D");
+  ok &= device_ok(cudaMemcpyAsync(dw.p, w, n * e, cudaMemcpyHostToDevice, st), "H2D");
+  ok &= device_ok(cudaMemcpyAsync(dz.p, dzeta, nzp * e, cudaMemcpyHostToDevice, st), "H2D");
+  if (zs) ok &= device_ok(cudaMemcpyAsync(dzs.p, zs, (size_t)nx * ny * e, cudaMemcpyHostToDevice, st), "H2D");
+  if (!ok) return (T)NAN;
+  if (cfl_dev<T>(du.as<T>(), dv.as<T>(), dw.as<T>(), dz.as<T>(), zs ? dzs.as<T>() : nullptr, nx, ny, nz, dx, dy, z_top,
+                 dt, dout.as<T>(), (vibe_stream_t)st) != VIBE_C_OK)
+    return (T)NAN;
+  T r[3];
+  ok &= device_ok(cudaMemcpyAsync(r, dout.p, 3 * e, cudaMemcpyDeviceToHost, st), "D2H");
+  ok &= device_ok(cudaStreamSynchronize(st), "sync");
+  if (!ok) return (T)NAN;
+  if (max_wind_out) *max_wind_out = r[1];
+  if (min_dz_out) *min_dz_out = r[2];
+  return r[0];
+}
+
+template <typename T>
+int neu_dev(const T* x, size_t n, T* out, vibe_stream_t stream) {
+  if (!x || !out) return VIBE_C_ERR_BAD_ARG;
+  T* part = (T*)scratch((size_t)2 * kRedBlocks * sizeof(T));
+  if (!part) { g_cerr = "scratch allocation failed"; return VIBE_C_ERR_DEVICE; }
+  cudaStream_t st = (cudaStream_t)stream;
+  const size_t chunk = (n + kRedBlocks - 1) / kRedBlocks;
+  k_neu_partial<T><<<kRedBlocks, kRedThreads, 0, st>>>(x, n, chunk > 0 ? chunk : 1, part);
+  k_neu_final<T><<<1, kRedThreads, 0, st>>>(part, kRedBlocks, out);
+  return device_ok(cudaGetLastError(), "neumaier launch") ? VIBE_C_OK : VIBE_C_ERR_DEVICE;
+}
+
+template <typename T>
+T neu_host(const T* x, size_t n) {
+  if (x == nullptr) return (T)0;
+  const size_t e = sizeof(T);
+  DBuf dx(n * e + e), dout(e);
+  if (!dx.p || !dout.p) { g_cerr = "cudaMalloc failed"; return (T)NAN; }
+  cudaStream_t st = own_stream();
+  bool ok = device_ok(cudaMemcpyAsync(dx.p, x, n * e, cudaMemcpyHostToDevice, st), "H2D");
+  ok = ok && neu_dev<T>(dx.as<T>(), n, dout.as<T>(), (vibe_stream_t)st) == VIBE_C_OK;
+  T r = (T)NAN;
+  ok = ok && device_ok(cudaMemcpyAsync(&r, dout.p, e, cudaMemcpyDeviceToHost, st), "D2H");
+  ok = ok && device_ok(cudaStreamSynchronize(st), "sync");
+  return ok ? r : (T)NAN;
+}
+
+template <typename T>
+int flux_dev(const T* q, const T* rho, const T* u, const T* v, const T* w, const T* dzeta, const T* zs, int nx, int ny,
+             int nz, T dx, T dy, T z_top, T* dqdt, vibe_stream_t stream) {
+  if (!q || !rho || !u || !v || !w || !dzeta || !dqdt) return VIBE_C_ERR_BAD_ARG;
+  const size_t n = (size_t)nx * ny * nz;
+  if (n == 0) return VIBE_C_OK;
+  const int blocks = (int)((n + 255) / 256 < 65535 ? (n + 255) / 256 : 65535);
+  k_flux_adv<T><<<blocks, 256, 0, (cudaStream_t)stream>>>(q, rho, u, v, w, dzeta, zs, nx, ny, nz, dx, dy, z_top, dqdt);
+  return device_ok(cudaGetLastError(), "flux advection launch") ? VIBE_C_OK : VIBE_C_ERR_DEVICE;
+}
+
+template <typename T>
+void flux_host(const T* q, const T* rho, const T* u, const T* v, const T* w, const T* dzeta, const T* zs, int nx, int ny,
+               int nz, T dx, T dy, T z_top, T* dqdt) {
+  if (q == nullptr || rho == nullptr || u == nullptr || v == nullptr || w == nullptr || dzeta == nullptr ||
+      dqdt == nullptr)
+    return;
+  const size_t n = (size_t)nx * ny * nz, e = sizeof(T);
+  if (n == 0) return;
+  DBuf dq(n * e), dr(n * e), du(n * e), dv(n * e), dw(n * e), dz((size_t)nz * e), dzs(zs ? (size_t)nx * ny * e : 0),
+      dout(n * e);
+  if (!dq.p || !dr.p || !du.p || !dv.p || !dw.p || !dz.p || !dout.p || (zs && !dzs.p)) { g_cerr = "cudaMalloc failed"; return; }
+  cudaStream_t st = own_stream();
+  bool ok = true;
+  ok &= device_ok(cudaMemcpyAsync(dq.p, q, n * e, cudaMemcpyHostToDevice, st), "H2D");
+  ok &= device_ok(cudaMemcpyAsync(dr.p, rho, n * e, cudaMemcpyHostToDevice, st), "H2D");
+  ok &= device_ok(cudaMemcpyAsync(du.p, u, n * e, cudaMemcpyHostToDevice, st), "H2D");
+  ok &= device_ok(cudaMemcpyAsync(dv.p, v, n * e, cudaMemcpyHostToDevice, st), "H2D");
+  ok &= device_ok(cudaMemcpyAsync(dw.p, w, n * e, cudaMemcpyHostToDevice, st), "H2D");
+  ok &= device_ok(cudaMemcpyAsync(dz.p, dzeta, (size_t)nz * e, cudaMemcpyHostToDevice, st), "H2D");
+  if (zs) ok &= device_ok(cudaMemcpyAsync(dzs.p, zs, (size_t)nx * ny * e, cudaMemcpyHostToDevice, st), "H2D");
+  if (!ok) return;
+  if (flux_dev<T>(dq.as<T>(), dr.as<T>(), du.as<T>(), dv.as<T>(), dw.as<T>(), dz.as<T>(), zs ? dzs.as<T>() : nullptr,
+                  nx, ny, nz, dx, dy, z_top, dout.as<T>(), (vibe_stream_t)st) != VIBE_C_OK)
+    return;
+  device_ok(cudaMemcpyAsync(dqdt, dout.p, n * e, cudaMemcpyDeviceToHost, st), "D2H");
+  device_ok(cudaStreamSynchronize(st), "sync");
+}
+
 }  // namespace
 
 extern "C" {
 
 const char* vibe_c_last_error(void) { return g_cerr.c_str(); }
 
+// ---- FP64: the reference's names ----
 int vibe_tridiagonal_solve_batched_f64_dev(const double* a, const double* b, const double* c, const double* d, int n,
                                            int n_sys, double* x, int* status, vibe_stream_t stream) {
-  if (n <= 0 || n_sys < 0 || b == nullptr || d == nullptr || x == nullptr) return VIBE_C_ERR_BAD_ARG;
-  if (n_sys == 0) return VIBE_C_OK;
-  double* work = (double*)scratch((size_t)n * n_sys * sizeof(double));
-  if (!work) { g_cerr = "scratch allocation failed"; return VIBE_C_ERR_DEVICE; }
-  k_thomas_batched<<<(n_sys + 127) / 128, 128, 0, (cudaStream_t)stream>>>(a, b, c, d, n, n_sys, x, work, status);
-  return device_ok(cudaGetLastError(), "thomas launch") ? VIBE_C_OK : VIBE_C_ERR_DEVICE;
+  return thomas_batched_dev<double>(a, b, c, d, n, n_sys, x, status, stream);
 }
 
 int vibe_tridiagonal_solve_batched_f64_dev_noalloc(const double* a, const double* b, const double* c,
@@ -373,192 +576,112 @@ int vibe_tridiagonal_solve_batched_f64_dev_noalloc(const double* a, const double
     work = g_noalloc_ptr[dev];
   }
   // the workspace needs no clearing: every system writes cp[k] before it reads it
-  k_thomas_batched<<<(n_sys + 127) / 128, 128, 0, (cudaStream_t)stream>>>(a, b, c, d, n, n_sys, x, work, status);
+  k_thomas_batched<double><<<(n_sys + 127) / 128, 128, 0, (cudaStream_t)stream>>>(a, b, c, d, n, n_sys, x, work,
+                                                                                 status);
   return device_ok(cudaGetLastError(), "thomas (no-alloc) launch") ? VIBE_C_OK : VIBE_C_ERR_DEVICE;
 }
 
 int vibe_tridiagonal_solve_batched_f64(const double* a, const double* b, const double* c, const double* d, int n,
                                        int n_sys, double* x) {
-  if (n <= 0 || n_sys < 0 || b == nullptr || d == nullptr || x == nullptr) return VIBE_C_ERR_BAD_ARG;
-  if (n_sys == 0) return VIBE_C_OK;
-  const size_t nn = (size_t)n * n_sys, no = (size_t)(n - 1) * n_sys;
-  DBuf da(a ? no * 8 + 8 : 0), db(nn * 8), dc(c ? no * 8 + 8 : 0), dd(nn * 8), dx(nn * 8), ds((size_t)n_sys * 4);
-  if (!db.p || !dd.p || !dx.p || !ds.p || (a && !da.p) || (c && !dc.p)) { g_cerr = "cudaMalloc failed"; return VIBE_C_ERR_DEVICE; }
-  cudaStream_t st = own_stream();
-  bool ok = true;
-  if (a && no) ok &= device_ok(cudaMemcpyAsync(da.p, a, no * 8, cudaMemcpyHostToDevice, st), "H2D a");
-  if (c && no) ok &= device_ok(cudaMemcpyAsync(dc.p, c, no * 8, cudaMemcpyHostToDevice, st), "H2D c");
-  ok &= device_ok(cudaMemcpyAsync(db.p, b, nn * 8, cudaMemcpyHostToDevice, st), "H2D b");
-  ok &= device_ok(cudaMemcpyAsync(dd.p, d, nn * 8, cudaMemcpyHostToDevice, st), "H2D d");
-  if (!ok) return VIBE_C_ERR_DEVICE;
-  int rc = vibe_tridiagonal_solve_batched_f64_dev(a ? da.as<double>() : nullptr, db.as<double>(),
-                                                  c ? dc.as<double>() : nullptr, dd.as<double>(), n, n_sys,
-                                                  dx.as<double>(), ds.as<int>(), (vibe_stream_t)st);
-  if (rc) return rc;
-  std::string st_host((size_t)n_sys * 4, '\0');
-  ok &= device_ok(cudaMemcpyAsync(x, dx.p, nn * 8, cudaMemcpyDeviceToHost, st), "D2H x");
-  ok &= device_ok(cudaMemcpyAsync(&st_host[0], ds.p, (size_t)n_sys * 4, cudaMemcpyDeviceToHost, st), "D2H status");
-  ok &= device_ok(cudaStreamSynchronize(st), "sync");
-  if (!ok) return VIBE_C_ERR_DEVICE;
-  const int* sv = (const int*)st_host.data();
-  for (int s = 0; s < n_sys; ++s)
-    if (sv[s] != VIBE_C_OK) return sv[s];
-  return VIBE_C_OK;
+  return thomas_batched_host<double>(a, b, c, d, n, n_sys, x);
 }
 
 int vibe_tridiagonal_solve_f64(const double* a, const double* b, const double* c, const double* d, int n, double* x,
                                double* ws) {
   if (n <= 0 || b == nullptr || d == nullptr || x == nullptr || ws == nullptr) return VIBE_C_ERR_BAD_ARG;
-  return vibe_tridiagonal_solve_batched_f64(a, b, c, d, n, 1, x);
+  return thomas_batched_host<double>(a, b, c, d, n, 1, x);
 }
 
 int vibe_weno5_reconstruct_batched_f64_dev(const double* q, size_t n, double* q_left, double* q_right,
                                            vibe_stream_t stream) {
-  if (!q || !q_left || !q_right) return VIBE_C_ERR_BAD_ARG;
-  if (n == 0) return VIBE_C_OK;
-  const int blocks = (int)((n + 255) / 256 < 65535 ? (n + 255) / 256 : 65535);
-  k_weno_batched<<<blocks, 256, 0, (cudaStream_t)stream>>>(q, n, q_left, q_right);
-  return device_ok(cudaGetLastError(), "weno launch") ? VIBE_C_OK : VIBE_C_ERR_DEVICE;
+  return weno_batched_dev<double>(q, n, q_left, q_right, stream);
 }
 
 void vibe_weno5_reconstruct_f64(double qm2, double qm1, double q0, double q1, double q2, double* q_left,
                                 double* q_right) {
-  if (q_left == nullptr || q_right == nullptr) return;
-  DBuf dq(5 * 8), dl(8), dr(8);
-  if (!dq.p || !dl.p || !dr.p) { g_cerr = "cudaMalloc failed"; *q_left = *q_right = NAN; return; }
-  const double q[5] = {qm2, qm1, q0, q1, q2};
-  cudaStream_t st = own_stream();
-  bool ok = device_ok(cudaMemcpyAsync(dq.p, q, 40, cudaMemcpyHostToDevice, st), "H2D");
-  ok = ok && vibe_weno5_reconstruct_batched_f64_dev(dq.as<double>(), 1, dl.as<double>(), dr.as<double>(),
-                                                    (vibe_stream_t)st) == VIBE_C_OK;
-  ok = ok && device_ok(cudaMemcpyAsync(q_left, dl.p, 8, cudaMemcpyDeviceToHost, st), "D2H");
-  ok = ok && device_ok(cudaMemcpyAsync(q_right, dr.p, 8, cudaMemcpyDeviceToHost, st), "D2H");
-  ok = ok && device_ok(cudaStreamSynchronize(st), "sync");
-  if (!ok) *q_left = *q_right = NAN;
+  weno_host<double>(qm2, qm1, q0, q1, q2, q_left, q_right);
 }
 
 double vibe_bilinear_f64(const double* f, int halo, int nsx, int nsy, int nz, double xi, double yj, int k) {
-  if (f == nullptr || nz <= 0) return 0.0;
-  if (k < 0) k = 0;
-  if (k >= nz) k = nz - 1;
-  const size_t plane = (size_t)nsx * nsy;
-  DBuf dp(plane * 8), dout(8);
-  if (!dp.p || !dout.p) { g_cerr = "cudaMalloc failed"; return NAN; }
-  cudaStream_t st = own_stream();
-  double r = NAN;
-  bool ok = device_ok(cudaMemcpyAsync(dp.p, f + (size_t)(k + halo) * plane, plane * 8, cudaMemcpyHostToDevice, st), "H2D");
-  if (ok) {
-    k_bilinear<<<1, 1, 0, st>>>(dp.as<double>(), halo, nsx, nsy, xi, yj, dout.as<double>());
-    ok = device_ok(cudaGetLastError(), "bilinear launch");
-  }
-  ok = ok && device_ok(cudaMemcpyAsync(&r, dout.p, 8, cudaMemcpyDeviceToHost, st), "D2H");
-  ok = ok && device_ok(cudaStreamSynchronize(st), "sync");
-  return ok ? r : NAN;
+  return bilinear_host<double>(f, halo, nsx, nsy, nz, xi, yj, k);
 }
 
 int vibe_cfl_scan_f64_dev(const double* u, const double* v, const double* w, const double* dzeta, const double* zs,
                           int nx, int ny, int nz, double dx, double dy, double z_top, double dt, double* out3,
                           vibe_stream_t stream) {
-  if (!u || !v || !w || !dzeta || !out3 || nx < 0 || ny < 0 || nz < 0) return VIBE_C_ERR_BAD_ARG;
-  double* part = (double*)scratch((size_t)3 * kRedBlocks * sizeof(double));
-  if (!part) { g_cerr = "scratch allocation failed"; return VIBE_C_ERR_DEVICE; }
-  cudaStream_t st = (cudaStream_t)stream;
-  k_cfl_partial<<<kRedBlocks, kRedThreads, 0, st>>>(u, v, w, dzeta, zs, nx, ny, nz, dx, dy, z_top, dt, part);
-  k_cfl_final<<<1, kRedThreads, 0, st>>>(part, kRedBlocks, out3);
-  return device_ok(cudaGetLastError(), "cfl launch") ? VIBE_C_OK : VIBE_C_ERR_DEVICE;
+  return cfl_dev<double>(u, v, w, dzeta, zs, nx, ny, nz, dx, dy, z_top, dt, out3, stream);
 }
 
 double vibe_cfl_scan_f64(const double* u, const double* v, const double* w, const double* dzeta, const double* zs,
                          int nx, int ny, int nz, double dx, double dy, double z_top, double dt, double* max_wind_out,
                          double* min_dz_out) {
-  if (u == nullptr || v == nullptr || w == nullptr || dzeta == nullptr) return 0.0;
-  const size_t n = (size_t)(nx > 0 ? nx : 0) * (ny > 0 ? ny : 0) * (nz > 0 ? nz : 0);
-  DBuf du(n * 8 + 8), dv(n * 8 + 8), dw(n * 8 + 8), dz((size_t)(nz > 0 ? nz : 0) * 8 + 8),
-      dzs(zs ? (size_t)nx * ny * 8 + 8 : 0), dout(3 * 8);
-  if (!du.p || !dv.p || !dw.p || !dz.p || !dout.p || (zs && !dzs.p)) { g_cerr = "cudaMalloc failed"; return NAN; }
-  cudaStream_t st = own_stream();
-  bool ok = true;
-  ok &= device_ok(cudaMemcpyAsync(du.p, u, n * 8, cudaMemcpyHostToDevice, st), "H2D");
-  ok &= device_ok(cudaMemcpyAsync(dv.p, v, n * 8, cudaMemcpyHostToDevice, st), "H2D");
-  ok &= device_ok(cudaMemcpyAsync(dw.p, w, n * 8, cudaMemcpyHostToDevice, st), "H2D");
-  ok &= device_ok(cudaMemcpyAsync(dz.p, dzeta, (size_t)(nz > 0 ? nz : 0) * 8, cudaMemcpyHostToDevice, st), "H2D");
-  if (zs) ok &= device_ok(cudaMemcpyAsync(dzs.p, zs, (size_t)nx * ny * 8, cudaMemcpyHostToDevice, st), "H2D");
-  if (!ok) return NAN;
-  if (vibe_cfl_scan_f64_dev(du.as<double>(), dv.as<double>(), dw.as<double>(), dz.as<double>(),
-                            zs ? dzs.as<double>() : nullptr, nx, ny, nz, dx, dy, z_top, dt, dout.as<double>(),
-                            (vibe_stream_t)st) != VIBE_C_OK)
-    return NAN;
-  double r[3];
-  ok &= device_ok(cudaMemcpyAsync(r, dout.p, 24, cudaMemcpyDeviceToHost, st), "D2H");
-  ok &= device_ok(cudaStreamSynchronize(st), "sync");
-  if (!ok) return NAN;
-  if (max_wind_out) *max_wind_out = r[1];
-  if (min_dz_out) *min_dz_out = r[2];
-  return r[0];
+  return cfl_host<double>(u, v, w, dzeta, zs, nx, ny, nz, dx, dy, z_top, dt, max_wind_out, min_dz_out);
 }
 
 int vibe_neumaier_sum_f64_dev(const double* x, size_t n, double* out, vibe_stream_t stream) {
-  if (!x || !out) return VIBE_C_ERR_BAD_ARG;
-  double* part = (double*)scratch((size_t)2 * kRedBlocks * sizeof(double));
-  if (!part) { g_cerr = "scratch allocation failed"; return VIBE_C_ERR_DEVICE; }
-  cudaStream_t st = (cudaStream_t)stream;
-  const size_t chunk = (n + kRedBlocks - 1) / kRedBlocks;
-  k_neu_partial<<<kRedBlocks, kRedThreads, 0, st>>>(x, n, chunk > 0 ? chunk : 1, part);
-  k_neu_final<<<1, kRedThreads, 0, st>>>(part, kRedBlocks, out);
-  return device_ok(cudaGetLastError(), "neumaier launch") ? VIBE_C_OK : VIBE_C_ERR_DEVICE;
+  return neu_dev<double>(x, n, out, stream);
 }
 
-double vibe_neumaier_sum_f64(const double* x, size_t n) {
-  if (x == nullptr) return 0.0;
-  DBuf dx(n * 8 + 8), dout(8);
-  if (!dx.p || !dout.p) { g_cerr = "cudaMalloc failed"; return NAN; }
-  cudaStream_t st = own_stream();
-  bool ok = device_ok(cudaMemcpyAsync(dx.p, x, n * 8, cudaMemcpyHostToDevice, st), "H2D");
-  ok = ok && vibe_neumaier_sum_f64_dev(dx.as<double>(), n, dout.as<double>(), (vibe_stream_t)st) == VIBE_C_OK;
-  double r = NAN;
-  ok = ok && device_ok(cudaMemcpyAsync(&r, dout.p, 8, cudaMemcpyDeviceToHost, st), "D2H");
-  ok = ok && device_ok(cudaStreamSynchronize(st), "sync");
-  return ok ? r : NAN;
-}
+double vibe_neumaier_sum_f64(const double* x, size_t n) { return neu_host<double>(x, n); }
 
 int vibe_advect_scalar_flux_f64_dev(const double* q, const double* rho, const double* u, const double* v,
                                     const double* w, const double* dzeta, const double* zs, int nx, int ny, int nz,
                                     double dx, double dy, double z_top, double* dqdt, vibe_stream_t stream) {
-  if (!q || !rho || !u || !v || !w || !dzeta || !dqdt) return VIBE_C_ERR_BAD_ARG;
-  const size_t n = (size_t)nx * ny * nz;
-  if (n == 0) return VIBE_C_OK;
-  const int blocks = (int)((n + 255) / 256 < 65535 ? (n + 255) / 256 : 65535);
-  k_flux_adv<<<blocks, 256, 0, (cudaStream_t)stream>>>(q, rho, u, v, w, dzeta, zs, nx, ny, nz, dx, dy, z_top, dqdt);
-  return device_ok(cudaGetLastError(), "flux advection launch") ? VIBE_C_OK : VIBE_C_ERR_DEVICE;
+  return flux_dev<double>(q, rho, u, v, w, dzeta, zs, nx, ny, nz, dx, dy, z_top, dqdt, stream);
 }
 
 void vibe_advect_scalar_flux_f64(const double* q, const double* rho, const double* u, const double* v, const double* w,
                                  const double* dzeta, const double* zs, int nx, int ny, int nz, double dx, double dy,
                                  double z_top, double* dqdt) {
-  if (q == nullptr || rho == nullptr || u == nullptr || v == nullptr || w == nullptr || dzeta == nullptr ||
-      dqdt == nullptr)
-    return;
-  const size_t n = (size_t)nx * ny * nz;
-  if (n == 0) return;
-  DBuf dq(n * 8), dr(n * 8), du(n * 8), dv(n * 8), dw(n * 8), dz((size_t)nz * 8), dzs(zs ? (size_t)nx * ny * 8 : 0),
-      dout(n * 8);
-  if (!dq.p || !dr.p || !du.p || !dv.p || !dw.p || !dz.p || !dout.p || (zs && !dzs.p)) { g_cerr = "cudaMalloc failed"; return; }
-  cudaStream_t st = own_stream();
-  bool ok = true;
-  ok &= device_ok(cudaMemcpyAsync(dq.p, q, n * 8, cudaMemcpyHostToDevice, st), "H2D");
-  ok &= device_ok(cudaMemcpyAsync(dr.p, rho, n * 8, cudaMemcpyHostToDevice, st), "H2D");
-  ok &= device_ok(cudaMemcpyAsync(du.p, u, n * 8, cudaMemcpyHostToDevice, st), "H2D");
-  ok &= device_ok(cudaMemcpyAsync(dv.p, v, n * 8, cudaMemcpyHostToDevice, st), "H2D");
-  ok &= device_ok(cudaMemcpyAsync(dw.p, w, n * 8, cudaMemcpyHostToDevice, st), "H2D");
-  ok &= device_ok(cudaMemcpyAsync(dz.p, dzeta, (size_t)nz * 8, cudaMemcpyHostToDevice, st), "H2D");
-  if (zs) ok &= device_ok(cudaMemcpyAsync(dzs.p, zs, (size_t)nx * ny * 8, cudaMemcpyHostToDevice, st), "H2D");
-  if (!ok) return;
-  if (vibe_advect_scalar_flux_f64_dev(dq.as<double>(), dr.as<double>(), du.as<double>(), dv.as<double>(),
-                                      dw.as<double>(), dz.as<double>(), zs ? dzs.as<double>() : nullptr, nx, ny, nz, dx,
-                                      dy, z_top, dout.as<double>(), (vibe_stream_t)st) != VIBE_C_OK)
-    return;
-  device_ok(cudaMemcpyAsync(dqdt, dout.p, n * 8, cudaMemcpyDeviceToHost, st), "D2H");
-  device_ok(cudaStreamSynchronize(st), "sync");
+  flux_host<double>(q, rho, u, v, w, dzeta, zs, nx, ny, nz, dx, dy, z_top, dqdt);
+}
+
+// ---- FP32 twins ----
+int vibe_tridiagonal_solve_f32(const float* a, const float* b, const float* c, const float* d, int n, float* x,
+                               float* ws) {
+  if (n <= 0 || b == nullptr || d == nullptr || x == nullptr || ws == nullptr) return VIBE_C_ERR_BAD_ARG;
+  return thomas_batched_host<float>(a, b, c, d, n, 1, x);
+}
+int vibe_tridiagonal_solve_batched_f32(const float* a, const float* b, const float* c, const float* d, int n,
+                                       int n_sys, float* x) {
+  return thomas_batched_host<float>(a, b, c, d, n, n_sys, x);
+}
+int vibe_tridiagonal_solve_batched_f32_dev(const float* a, const float* b, const float* c, const float* d, int n,
+                                           int n_sys, float* x, int* status, vibe_stream_t stream) {
+  return thomas_batched_dev<float>(a, b, c, d, n, n_sys, x, status, stream);
+}
+void vibe_weno5_reconstruct_f32(float qm2, float qm1, float q0, float q1, float q2, float* q_left, float* q_right) {
+  weno_host<float>(qm2, qm1, q0, q1, q2, q_left, q_right);
+}
+int vibe_weno5_reconstruct_batched_f32_dev(const float* q, size_t n, float* q_left, float* q_right,
+                                           vibe_stream_t stream) {
+  return weno_batched_dev<float>(q, n, q_left, q_right, stream);
+}
+float vibe_bilinear_f32(const float* f, int halo, int nsx, int nsy, int nz, float xi, float yj, int k) {
+  return bilinear_host<float>(f, halo, nsx, nsy, nz, xi, yj, k);
+}
+float vibe_cfl_scan_f32(const float* u, const float* v, const float* w, const float* dzeta, const float* zs, int nx,
+                        int ny, int nz, float dx, float dy, float z_top, float dt, float* max_wind_out,
+                        float* min_dz_out) {
+  return cfl_host<float>(u, v, w, dzeta, zs, nx, ny, nz, dx, dy, z_top, dt, max_wind_out, min_dz_out);
+}
+int vibe_cfl_scan_f32_dev(const float* u, const float* v, const float* w, const float* dzeta, const float* zs, int nx,
+                          int ny, int nz, float dx, float dy, float z_top, float dt, float* out3, vibe_stream_t stream) {
+  return cfl_dev<float>(u, v, w, dzeta, zs, nx, ny, nz, dx, dy, z_top, dt, out3, stream);
+}
+float vibe_neumaier_sum_f32(const float* x, size_t n) { return neu_host<float>(x, n); }
+int vibe_neumaier_sum_f32_dev(const float* x, size_t n, float* out, vibe_stream_t stream) {
+  return neu_dev<float>(x, n, out, stream);
+}
+void vibe_advect_scalar_flux_f32(const float* q, const float* rho, const float* u, const float* v, const float* w,
+                                 const float* dzeta, const float* zs, int nx, int ny, int nz, float dx, float dy,
+                                 float z_top, float* dqdt) {
+  flux_host<float>(q, rho, u, v, w, dzeta, zs, nx, ny, nz, dx, dy, z_top, dqdt);
+}
+int vibe_advect_scalar_flux_f32_dev(const float* q, const float* rho, const float* u, const float* v, const float* w,
+                                    const float* dzeta, const float* zs, int nx, int ny, int nz, float dx, float dy,
+                                    float z_top, float* dqdt, vibe_stream_t stream) {
+  return flux_dev<float>(q, rho, u, v, w, dzeta, zs, nx, ny, nz, dx, dy, z_top, dqdt, stream);
 }
 
 }  // extern "C"
