@@ -526,7 +526,19 @@ __global__ void k_mx_fb_mom(const __grid_constant__ Dims d, const __grid_constan
 // backward half); the updated u, v enter this substep's divergence and are
 // written to the output. After the last substep of a stage one u/v kernel
 // applies the final update in place. cdx = -cp dtau / dx, cdy likewise.
-template <int kPF>
+constexpr int kDefaultHeviRing = 0;  // single-domain column kernel: 0 = register ring
+constexpr int kBatchRing = 0;        // work-list column kernel of groups
+
+// 4-byte asynchronous global -> shared copies (sm_80+ cp.async), grouped
+__device__ __forceinline__ void cp_async4(float* smem, const float* gmem) {
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(sa), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
+
+template <int kPF, int kRing>
 __device__ __forceinline__ void hevi_body(const Dims& d, const Tab& t, const Flags& fl, const WS& win, const WS& wout,
                                           float dtau, const float* __restrict__ lu, int apply_uv, float cdx,
                                           float cdy, int bx, int by) {
@@ -585,10 +597,32 @@ __device__ __forceinline__ void hevi_body(const Dims& d, const Tab& t, const Fla
   const int ow = (i > 0) ? -1 : 0, oe = (i + 1 < d.nx) ? 1 : 0;
   const long long os = (j > 0) ? -(long long)vn : 0, on = (j + 1 < d.ny) ? (long long)vn : 0;
   const bool last_i = (i == d.nx - 1), last_j = (j == d.ny - 1);
-  // Loads run kPF levels ahead of their use (register ring, static slots).
-  // ---- forward sweep: wt, S and dp = (rhs - a dp(k-1)) / den per level
+  // Forward-sweep loads run ahead of their use: with kRing > 0 as 4-byte
+  // cp.async copies into a per-thread shared-memory ring kRing levels deep
+  // (no registers held, one commit group per level, wait_group kRing-1 before
+  // a level is read; each thread reads only its own slots), else in a
+  // register ring kPF levels deep.
   float fw[kPF], fp[kPF], fu0[kPF], fu1[kPF], fv0[kPF], fv1[kPF];
   float fpw[kPF], fpe[kPF], fps[kPF], fpn[kPF];
+  float* ring = s_t0 + nz;  // kRing x 10 x 128 floats after the tables
+  auto rs = [&](int slot, int f) -> float* { return ring + ((size_t)slot * 10 + f) * 128 + tid; };
+  auto issueF = [&](int L) {  // level L -> slot L % kRing
+    const int slot = L % (kRing > 0 ? kRing : 1);
+    const size_t o = (size_t)L * pl, o1 = o + pl;
+    cp_async4(rs(slot, 0), W0 + o1);
+    if (L + 1 < nz) cp_async4(rs(slot, 1), P0 + o1);
+    else *rs(slot, 1) = 0.f;
+    cp_async4(rs(slot, 2), U0 + o);
+    cp_async4(rs(slot, 3), U0 + o + 1);
+    cp_async4(rs(slot, 4), V0 + o);
+    cp_async4(rs(slot, 5), V0 + o + vn);
+    if (apply_uv) {
+      cp_async4(rs(slot, 6), P0 + o + ow);
+      cp_async4(rs(slot, 7), P0 + o + oe);
+      cp_async4(rs(slot, 8), P0 + o + os);
+      cp_async4(rs(slot, 9), P0 + o + on);
+    }
+  };
   auto loadF = [&](int L, int q) {
     const size_t o = (size_t)L * pl, o1 = o + pl;
     fw[q] = W0[o1];
@@ -604,9 +638,16 @@ __device__ __forceinline__ void hevi_body(const Dims& d, const Tab& t, const Fla
       fpn[q] = P0[o + on];
     }
   };
+  if (kRing > 0) {
+    for (int L = 0; L < kRing; ++L) {
+      if (L < nz) issueF(L);
+      cp_async_commit();
+    }
+  } else {
 #pragma unroll
-  for (int q = 0; q < kPF; ++q)
-    if (q < nz) loadF(q, q);
+    for (int q = 0; q < kPF; ++q)
+      if (q < nz) loadF(q, q);
+  }
   float p_k = P0[0];
   float w_k = W0[0];
   float wt_k = w_k;  // face 0: no pressure gradient
@@ -617,22 +658,50 @@ __device__ __forceinline__ void hevi_body(const Dims& d, const Tab& t, const Fla
     for (int q = 0; q < kPF; ++q) {
       const int k = k0 + q;
       if (k < nz) {
-        const float w_k1 = fw[q];
+        float w_k1, pf1, u0, u1, v0, v1, pw_ = 0.f, pe_ = 0.f, ps_ = 0.f, pn_ = 0.f;
+        if (kRing > 0) {
+          cp_async_wait<(kRing > 0 ? kRing - 1 : 0)>();
+          const int slot = k % (kRing > 0 ? kRing : 1);
+          w_k1 = *rs(slot, 0);
+          pf1 = *rs(slot, 1);
+          u0 = *rs(slot, 2);
+          u1 = *rs(slot, 3);
+          v0 = *rs(slot, 4);
+          v1 = *rs(slot, 5);
+          if (apply_uv) {
+            pw_ = *rs(slot, 6);
+            pe_ = *rs(slot, 7);
+            ps_ = *rs(slot, 8);
+            pn_ = *rs(slot, 9);
+          }
+        } else {
+          w_k1 = fw[q];
+          pf1 = fp[q];
+          u0 = fu0[q];
+          u1 = fu1[q];
+          v0 = fv0[q];
+          v1 = fv1[q];
+          if (apply_uv) {
+            pw_ = fpw[q];
+            pe_ = fpe[q];
+            ps_ = fps[q];
+            pn_ = fpn[q];
+          }
+        }
         float wt_k1 = w_k1, p_k1 = 0.f;
         if (k + 1 < nz) {
-          p_k1 = fp[q];
+          p_k1 = pf1;
           wt_k1 = w_k1 - dtau * ob * cpf * s_tfz[k + 1] * (p_k1 - p_k) * s_idzw[k + 1];
         }
-        float u0 = fu0[q], u1 = fu1[q], v0 = fv0[q], v1 = fv1[q];
         if (apply_uv) {
           const float tx_ = s_t0[k] * cdx, ty_ = s_t0[k] * cdy;
-          u0 += tx_ * (p_k - fpw[q]);
-          u1 += tx_ * (fpe[q] - p_k);
-          v0 += ty_ * (p_k - fps[q]);
-          v1 += ty_ * (fpn[q] - p_k);
+          u0 += tx_ * (p_k - pw_);
+          u1 += tx_ * (pe_ - p_k);
+          v0 += ty_ * (p_k - ps_);
+          v1 += ty_ * (pn_ - p_k);
         }
         const float Dh = -(s_r0[k] * ((u1 - u0) * dxi + (v1 - v0) * dyi));
-        if (k + kPF < nz) loadF(k + kPF, q);
+        if (kRing == 0 && k + kPF < nz) loadF(k + kPF, q);
         {
           const size_t o = (size_t)k * pl;
           Uo[o] = u0;
@@ -650,6 +719,11 @@ __device__ __forceinline__ void hevi_body(const Dims& d, const Tab& t, const Fla
         Po[o] = dpk;
         Ro[o] = S;
         Wo[o + pl] = wt_k1;  // face k+1 (face nz: w_old(nz), already final)
+        if (kRing > 0) {
+          // refill the slot only now that every value read from it has been used
+          if (k + kRing < nz) issueF(k + kRing);
+          cp_async_commit();
+        }
         dp_prev = dpk;
         w_k = w_k1;
         wt_k = wt_k1;
@@ -659,6 +733,7 @@ __device__ __forceinline__ void hevi_body(const Dims& d, const Tab& t, const Fla
   }
   // ---- backward sweep: x(k) = dp(k) - c'(k) x(k+1); after x(k) is known, face
   // k+1 (needs x(k), x(k+1)) and cell k+1 (needs faces k+1, k+2) are final.
+  if (kRing > 0) cp_async_wait<0>();
   float bdp[kPF], bwt[kPF], bS[kPF], br[kPF];
   auto loadB = [&](int kk, int q) {  // inputs of step kk (cell/face kk)
     const size_t o = (size_t)kk * pl;
@@ -945,14 +1020,14 @@ void mixed_fb_substep(const Dims& d, const Tab& t, const Flags& fl, const WS& wi
   k_mx_fb_mom<<<g3(d.nx + 1, d.ny + 1, d.nz + 1, b), b, 0, stream>>>(d, t, win, wout, dtau, 1);
 }
 
-template <int kPF>
+template <int kPF, int kRing>
 __global__ void __launch_bounds__(128, 6) k_mx_hevi_col(const __grid_constant__ Dims d, const __grid_constant__ Tab t,
                                                          const __grid_constant__ Flags fl,
                                                          const __grid_constant__ WS win,
                                                          const __grid_constant__ WS wout, float dtau,
                                                          const float* __restrict__ lu, int apply_uv, float cdx,
                                                          float cdy) {
-  hevi_body<kPF>(d, t, fl, win, wout, dtau, lu, apply_uv, cdx, cdy, blockIdx.x, blockIdx.y);
+  hevi_body<kPF, kRing>(d, t, fl, win, wout, dtau, lu, apply_uv, cdx, cdy, blockIdx.x, blockIdx.y);
 }
 
 // Prefetch depth of the HEVI column kernel (levels of loads in flight per
@@ -969,18 +1044,45 @@ static int hevi_pf() {
   return pf;
 }
 
+// Depth of the shared-memory cp.async ring of the column kernel's forward
+// sweep (0 = the register ring of hevi_pf()); VIBE_GB300_HEVI_RING=0|4|6|8.
+int hevi_ring() {
+  static int r = -1;
+  if (r < 0) {
+    r = kDefaultHeviRing;
+    if (const char* e = std::getenv("VIBE_GB300_HEVI_RING")) {
+      const int v = std::atoi(e);
+      if (v == 0 || v == 4 || v == 6 || v == 8) r = v;
+    }
+  }
+  return r;
+}
+
+size_t hevi_smem_bytes(int nz, int ring) {
+  return (10 * (size_t)(nz + 1) + (size_t)ring * 10 * 128) * sizeof(float);
+}
+
 void mixed_hevi_column(const Dims& d, const Tab& t, const Flags& fl, const WS& win, const WS& wout, float dtau,
                        const float* lu, bool apply_uv, cudaStream_t stream) {
   const dim3 bc(32, 4);
-  const size_t smem = 10 * (size_t)(d.nz + 1) * sizeof(float);
+  const int ring = hevi_ring();
+  const size_t smem = hevi_smem_bytes(d.nz, ring);
   const dim3 g((d.nx + bc.x - 1) / bc.x, (d.ny + bc.y - 1) / bc.y);
   const float cdx = -(float)kCp * dtau * t.dx_inv, cdy = -(float)kCp * dtau * t.dy_inv;
   const int au = apply_uv ? 1 : 0;
-  switch (hevi_pf()) {
-    case 6: k_mx_hevi_col<6><<<g, bc, smem, stream>>>(d, t, fl, win, wout, dtau, lu, au, cdx, cdy); break;
-    case 8: k_mx_hevi_col<8><<<g, bc, smem, stream>>>(d, t, fl, win, wout, dtau, lu, au, cdx, cdy); break;
-    case 4: k_mx_hevi_col<4><<<g, bc, smem, stream>>>(d, t, fl, win, wout, dtau, lu, au, cdx, cdy); break;
-    default: k_mx_hevi_col<2><<<g, bc, smem, stream>>>(d, t, fl, win, wout, dtau, lu, au, cdx, cdy); break;
+  if (ring == 8) {
+    k_mx_hevi_col<2, 8><<<g, bc, smem, stream>>>(d, t, fl, win, wout, dtau, lu, au, cdx, cdy);
+  } else if (ring == 6) {
+    k_mx_hevi_col<2, 6><<<g, bc, smem, stream>>>(d, t, fl, win, wout, dtau, lu, au, cdx, cdy);
+  } else if (ring == 4) {
+    k_mx_hevi_col<2, 4><<<g, bc, smem, stream>>>(d, t, fl, win, wout, dtau, lu, au, cdx, cdy);
+  } else {
+    switch (hevi_pf()) {
+      case 6: k_mx_hevi_col<6, 0><<<g, bc, smem, stream>>>(d, t, fl, win, wout, dtau, lu, au, cdx, cdy); break;
+      case 8: k_mx_hevi_col<8, 0><<<g, bc, smem, stream>>>(d, t, fl, win, wout, dtau, lu, au, cdx, cdy); break;
+      case 4: k_mx_hevi_col<4, 0><<<g, bc, smem, stream>>>(d, t, fl, win, wout, dtau, lu, au, cdx, cdy); break;
+      default: k_mx_hevi_col<2, 0><<<g, bc, smem, stream>>>(d, t, fl, win, wout, dtau, lu, au, cdx, cdy); break;
+    }
   }
 }
 
@@ -1081,7 +1183,7 @@ __global__ void __launch_bounds__(128, 6) k_b_hevi(const HeviArgs* __restrict__ 
   const int dom = find_domain(start, nd);
   const HeviArgs& a = A[dom];
   const int l = (int)blockIdx.x - start[dom];
-  hevi_body<2>(a.d, a.t, a.fl, a.win, a.wout, a.dtau, a.lu, a.apply_uv, a.cdx, a.cdy, l % a.gx, l / a.gx);
+  hevi_body<2, kBatchRing>(a.d, a.t, a.fl, a.win, a.wout, a.dtau, a.lu, a.apply_uv, a.cdx, a.cdy, l % a.gx, l / a.gx);
 }
 
 __global__ void k_b_uv(const UvArgs* __restrict__ A, const int* __restrict__ start, int nd) {
@@ -1155,7 +1257,7 @@ MixedBatch* mixed_batch_build(const std::vector<MixedDomain>& doms, const Flags&
     if (m.d.nz != nz) return nullptr;
   auto* b = new MixedBatch();
   b->err = err;
-  b->hevi_smem = 10 * (size_t)(nz + 1) * sizeof(float);
+  b->hevi_smem = (10 * (size_t)(nz + 1) + (size_t)kBatchRing * 10 * 128) * sizeof(float);
   const double dts[3] = {dt / 3.0, dt / 2.0, dt};
   const int nd = (int)doms.size();
   auto sub_out = [&](const MixedDomain& m, int n) { return (n & 1) ? m.WB : m.WA; };
