@@ -526,7 +526,8 @@ __global__ void k_mx_fb_mom(const __grid_constant__ Dims d, const __grid_constan
 // backward half); the updated u, v enter this substep's divergence and are
 // written to the output. After the last substep of a stage one u/v kernel
 // applies the final update in place. cdx = -cp dtau / dx, cdy likewise.
-constexpr int kDefaultHeviRing = 0;  // single-domain column kernel: 0 = register ring
+constexpr int kDefaultHeviRing = 4;  // single-domain column kernel: 0 = register ring
+constexpr int kDefaultHeviPar = 0;   // levels per thread of the level-split column kernel (0 = off)
 constexpr int kBatchRing = 0;        // work-list column kernel of groups
 
 // 4-byte asynchronous global -> shared copies (sm_80+ cp.async), grouped
@@ -603,9 +604,9 @@ __device__ __forceinline__ void hevi_body(const Dims& d, const Tab& t, const Fla
   // a level is read; each thread reads only its own slots), else in a
   // register ring kPF levels deep.
   float fw[kPF], fp[kPF], fu0[kPF], fu1[kPF], fv0[kPF], fv1[kPF];
-  float fpw[kPF], fpe[kPF], fps[kPF], fpn[kPF];
-  float* ring = s_t0 + nz;  // kRing x 10 x 128 floats after the tables
-  auto rs = [&](int slot, int f) -> float* { return ring + ((size_t)slot * 10 + f) * 128 + tid; };
+  float fpw[kPF], fpe[kPF], fps[kPF], fpn[kPF], fr[kPF];
+  float* ring = s_t0 + nz;  // kRing x 11 x 128 floats after the tables
+  auto rs = [&](int slot, int f) -> float* { return ring + ((size_t)slot * 11 + f) * 128 + tid; };
   auto issueF = [&](int L) {  // level L -> slot L % kRing
     const int slot = L % (kRing > 0 ? kRing : 1);
     const size_t o = (size_t)L * pl, o1 = o + pl;
@@ -616,6 +617,7 @@ __device__ __forceinline__ void hevi_body(const Dims& d, const Tab& t, const Fla
     cp_async4(rs(slot, 3), U0 + o + 1);
     cp_async4(rs(slot, 4), V0 + o);
     cp_async4(rs(slot, 5), V0 + o + vn);
+    cp_async4(rs(slot, 10), R0 + o);
     if (apply_uv) {
       cp_async4(rs(slot, 6), P0 + o + ow);
       cp_async4(rs(slot, 7), P0 + o + oe);
@@ -631,6 +633,7 @@ __device__ __forceinline__ void hevi_body(const Dims& d, const Tab& t, const Fla
     fu1[q] = U0[o + 1];
     fv0[q] = V0[o];
     fv1[q] = V0[o + vn];
+    fr[q] = R0[o];
     if (apply_uv) {
       fpw[q] = P0[o + ow];
       fpe[q] = P0[o + oe];
@@ -658,7 +661,7 @@ __device__ __forceinline__ void hevi_body(const Dims& d, const Tab& t, const Fla
     for (int q = 0; q < kPF; ++q) {
       const int k = k0 + q;
       if (k < nz) {
-        float w_k1, pf1, u0, u1, v0, v1, pw_ = 0.f, pe_ = 0.f, ps_ = 0.f, pn_ = 0.f;
+        float w_k1, pf1, u0, u1, v0, v1, r0_, pw_ = 0.f, pe_ = 0.f, ps_ = 0.f, pn_ = 0.f;
         if (kRing > 0) {
           cp_async_wait<(kRing > 0 ? kRing - 1 : 0)>();
           const int slot = k % (kRing > 0 ? kRing : 1);
@@ -668,6 +671,7 @@ __device__ __forceinline__ void hevi_body(const Dims& d, const Tab& t, const Fla
           u1 = *rs(slot, 3);
           v0 = *rs(slot, 4);
           v1 = *rs(slot, 5);
+          r0_ = *rs(slot, 10);
           if (apply_uv) {
             pw_ = *rs(slot, 6);
             pe_ = *rs(slot, 7);
@@ -681,6 +685,7 @@ __device__ __forceinline__ void hevi_body(const Dims& d, const Tab& t, const Fla
           u1 = fu1[q];
           v0 = fv0[q];
           v1 = fv1[q];
+          r0_ = fr[q];
           if (apply_uv) {
             pw_ = fpw[q];
             pe_ = fpe[q];
@@ -717,7 +722,7 @@ __device__ __forceinline__ void hevi_body(const Dims& d, const Tab& t, const Fla
         const float dpk = (k == 0) ? rhs * s_li[0] : (rhs - s_la[k] * dp_prev) * s_li[k];
         const size_t o = (size_t)k * pl;
         Po[o] = dpk;
-        Ro[o] = S;
+        Ro[o] = r0_ + dtau * S;  // rho' less the implicit part, added in the backward sweep
         Wo[o + pl] = wt_k1;  // face k+1 (face nz: w_old(nz), already final)
         if (kRing > 0) {
           // refill the slot only now that every value read from it has been used
@@ -734,22 +739,22 @@ __device__ __forceinline__ void hevi_body(const Dims& d, const Tab& t, const Fla
   // ---- backward sweep: x(k) = dp(k) - c'(k) x(k+1); after x(k) is known, face
   // k+1 (needs x(k), x(k+1)) and cell k+1 (needs faces k+1, k+2) are final.
   if (kRing > 0) cp_async_wait<0>();
-  float bdp[kPF], bwt[kPF], bS[kPF], br[kPF];
-  auto loadB = [&](int kk, int q) {  // inputs of step kk (cell/face kk)
+  constexpr int kB = kRing > 0 ? 4 : kPF;  // backward loads in flight (L2 hits)
+  float bdp[kB], bwt[kB], bS[kB];
+  auto loadB = [&](int kk, int q) {  // inputs of step kk (cell/face kk), parked by the forward sweep
     const size_t o = (size_t)kk * pl;
     bdp[q] = (kk >= 1) ? Po[o - pl] : 0.f;  // dp(kk-1)
     bwt[q] = Wo[o];                          // wt(kk)
-    bS[q] = Ro[o];                           // S(kk)
-    br[q] = R0[o];                           // rho'_old(kk)
+    bS[q] = Ro[o];                           // rho'_old(kk) + dtau S(kk)
   };
 #pragma unroll
-  for (int q = 0; q < kPF; ++q)
+  for (int q = 0; q < kB; ++q)
     if (nz - 1 - q >= 0) loadB(nz - 1 - q, q);
   float x_up = dp_prev;  // x(nz-1) = dp(nz-1)
   float wn_up = Wo[(size_t)nz * pl];
-  for (int kk0 = nz - 1; kk0 >= 0; kk0 -= kPF) {
+  for (int kk0 = nz - 1; kk0 >= 0; kk0 -= kB) {
 #pragma unroll
-    for (int q = 0; q < kPF; ++q) {
+    for (int q = 0; q < kB; ++q) {
       const int kk = kk0 - q;  // face kk and cell kk are finalised here
       if (kk >= 0) {
         const int k = kk - 1;
@@ -760,8 +765,8 @@ __device__ __forceinline__ void hevi_body(const Dims& d, const Tab& t, const Fla
           wn_kk = bwt[q] - dtau * b * cpf * s_tfz[kk] * (x_up - x_k) * s_idzw[kk];
         }
         const float dv_new = -(s_rfz[kk + 1] * wn_up - s_rfz[kk] * wn_kk) * s_idzc[kk];
-        const float rnew = br[q] + dtau * (bS[q] + b * dv_new);
-        if (kk - kPF >= 0) loadB(kk - kPF, q);
+        const float rnew = bS[q] + dtau * b * dv_new;
+        if (kk - kB >= 0) loadB(kk - kB, q);
         Ro[okk] = rnew;
         Po[okk] = x_up;
         Wo[okk] = wn_kk;
@@ -1020,6 +1025,230 @@ void mixed_fb_substep(const Dims& d, const Tab& t, const Flags& fl, const WS& wi
   k_mx_fb_mom<<<g3(d.nx + 1, d.ny + 1, d.nz + 1, b), b, 0, stream>>>(d, t, win, wout, dtau, 1);
 }
 
+// ---- the same HEVI column update with the levels split over threads ------
+// The column system's LU factors (la, lc, li) depend on the level only, so
+// both recurrences, dp(k) = (rhs(k) - la(k) dp(k-1)) li(k) and
+// x(k) = dp(k) - lc(k) x(k+1), split into chunks of kM levels: each thread
+// solves its chunk with a zero carry and the chunks are joined by a scan of
+// the carries, dp(k) = dpl(k) + G(k) dp(k0-1) with G(k) = prod_{l=k0..k}
+// (-la(l) li(l)), and x(k) = xl(k) + H(k) x(k0+kM) with H(k) = prod_{l=k..
+// k0+kM-1} (-lc(l)). A block is 32 consecutive columns (one warp per chunk,
+// so every level's load is one 128-byte row) by C = ceil(nz/kM) chunks; every
+// thread issues all the loads of its chunk at once and nothing is parked
+// between sweeps. Same arithmetic per level as hevi_body; the carries change
+// the rounding of the tridiagonal solve only.
+template <int kM>
+__device__ __forceinline__ void hevi_par_body(const Dims& d, const Tab& t, const Flags& fl, const WS& win,
+                                              const WS& wout, float dtau, const float* __restrict__ lu,
+                                              int apply_uv, float cdx, float cdy, int bx, int by) {
+  extern __shared__ float s_tab[];
+  const int nz = d.nz;
+  const int C = blockDim.y;
+  float* s_tfz = s_tab;                    // nz+1
+  float* s_idzw = s_tfz + (nz + 1);        // nz+1
+  float* s_rfz = s_idzw + (nz + 1);        // nz+1
+  float* s_idzc = s_rfz + (nz + 1);        // nz
+  float* s_kap = s_idzc + nz;              // nz
+  float* s_la = s_kap + nz;                // nz
+  float* s_lc = s_la + nz;                 // nz
+  float* s_li = s_lc + nz;                 // nz
+  float* s_r0 = s_li + nz;                 // nz
+  float* s_t0 = s_r0 + nz;                 // nz
+  float* s_a = s_t0 + nz;                  // C x 32: chunk result with zero carry
+  float* s_g = s_a + C * 32;               // C x 32: its carry coefficient
+  float* s_e = s_g + C * 32;               // (C+1) x 32: scanned carries
+  float* s_x = s_e + (C + 1) * 32;         // C x 32: x at each chunk's top level
+  const int tx = threadIdx.x, c = threadIdx.y;
+  const int tid = c * 32 + tx, nthr = 32 * C;
+  for (int e = tid; e <= nz; e += nthr) {
+    s_tfz[e] = t.tfz[e];
+    s_idzw[e] = t.idzw[e];
+    s_rfz[e] = t.rfz[e];
+    if (e < nz) {
+      s_idzc[e] = t.idzc[e];
+      s_kap[e] = t.kap[e];
+      s_la[e] = lu[e];
+      s_lc[e] = lu[nz + e];
+      s_li[e] = lu[2 * nz + e];
+      s_r0[e] = t.r0c[e];
+      s_t0[e] = t.t0c[e];
+    }
+  }
+  __syncthreads();
+  const int i = bx * 32 + tx;
+  const int j = by;
+  const bool active = i < d.nx && j < d.ny;
+  const int k0 = c * kM;
+  const int kn = imin(kM, nz - k0);  // >= 1: C = ceil(nz / kM)
+  const float b = (float)fl.hevi_beta, ob = 1.f - b;
+  const float cpf = (float)kCp;
+  const size_t pl = d.plane;
+  const size_t col = active ? (size_t)j * d.P + i : 0;
+  const float* __restrict__ U0 = win.f[U] + col;
+  const float* __restrict__ V0 = win.f[V] + col;
+  const float* __restrict__ W0 = win.f[W] + col;
+  const float* __restrict__ P0 = win.f[PI] + col;
+  const float* __restrict__ R0 = win.f[RHO] + col;
+  float* __restrict__ Wo = wout.f[W] + col;
+  float* __restrict__ Po = wout.f[PI] + col;
+  float* __restrict__ Ro = wout.f[RHO] + col;
+  float* __restrict__ Uo = wout.f[U] + col;
+  float* __restrict__ Vo = wout.f[V] + col;
+  const size_t vn = d.P;
+  const float dxi = t.dx_inv, dyi = t.dy_inv;
+  const int ow = (i > 0) ? -1 : 0, oe = (i + 1 < d.nx) ? 1 : 0;
+  const long long os = (j > 0) ? -(long long)vn : 0, on = (j + 1 < d.ny) ? (long long)vn : 0;
+  const bool last_i = (i == d.nx - 1), last_j = (j == d.ny - 1);
+
+  float pv[kM + 2];  // p'(k0-1+q), 0 outside [0, nz)
+  float wv[kM + 1];  // w(face k0+q)
+  float wt[kM + 1];  // w with the explicit pressure gradient, faces k0..k0+kM
+  float rhs[kM], rs[kM], dp[kM], gq[kM];
+#pragma unroll
+  for (int q = 0; q < kM + 2; ++q) {
+    const int kk = k0 - 1 + q;
+    pv[q] = (active && kk >= 0 && kk < nz && q <= kn + 1) ? P0[(size_t)kk * pl] : 0.f;
+  }
+#pragma unroll
+  for (int q = 0; q < kM + 1; ++q) {
+    const int f = k0 + q;
+    wv[q] = (active && q <= kn && f <= nz) ? W0[(size_t)f * pl] : 0.f;
+  }
+#pragma unroll
+  for (int q = 0; q < kM + 1; ++q) {
+    const int f = k0 + q;
+    wt[q] = wv[q];
+    if (q <= kn && f >= 1 && f < nz)
+      wt[q] = wv[q] - dtau * ob * cpf * s_tfz[f] * (pv[q + 1] - pv[q]) * s_idzw[f];
+  }
+  float w_top = 0.f;  // w(face k0+kn)
+#pragma unroll
+  for (int q = 0; q < kM + 1; ++q)
+    if (q == kn) w_top = wv[q];
+  float prev = 0.f, g = 1.f, d_last = 0.f, g_last = 1.f;
+#pragma unroll
+  for (int q = 0; q < kM; ++q) {
+    rhs[q] = rs[q] = dp[q] = 0.f;
+    gq[q] = 1.f;
+    if (q < kn) {
+      const int k = k0 + q;
+      if (active) {
+        const size_t o = (size_t)k * pl;
+        const float p_k = pv[q + 1];
+        float u0 = U0[o], u1 = U0[o + 1], v0 = V0[o], v1 = V0[o + vn];
+        if (apply_uv) {
+          const float tx_ = s_t0[k] * cdx, ty_ = s_t0[k] * cdy;
+          u0 += tx_ * (p_k - P0[o + ow]);
+          u1 += tx_ * (P0[o + oe] - p_k);
+          v0 += ty_ * (p_k - P0[o + os]);
+          v1 += ty_ * (P0[o + on] - p_k);
+        }
+        const float Dh = -(s_r0[k] * ((u1 - u0) * dxi + (v1 - v0) * dyi));
+        Uo[o] = u0;
+        Vo[o] = v0;
+        if (last_i) Uo[o + 1] = u1;
+        if (last_j) Vo[o + vn] = v1;
+        const float rk = s_rfz[k], rk1 = s_rfz[k + 1], idz = s_idzc[k];
+        const float dv_old = -(rk1 * wv[q + 1] - rk * wv[q]) * idz;
+        const float dv_t = -(rk1 * wt[q + 1] - rk * wt[q]) * idz;
+        const float S = Dh + ob * dv_old;
+        rhs[q] = p_k + dtau * s_kap[k] * (S + b * dv_t);
+        rs[q] = R0[o] + dtau * S;
+      }
+      dp[q] = (rhs[q] - s_la[k] * prev) * s_li[k];
+      prev = dp[q];
+      g *= -s_la[k] * s_li[k];
+      gq[q] = g;
+      d_last = dp[q];
+      g_last = g;
+    }
+  }
+  s_a[tid] = d_last;
+  s_g[tid] = g_last;
+  __syncthreads();
+  if (c == 0) {  // forward carries: s_e[cc] = dp(last level of chunk cc-1)
+    float e = 0.f;
+    s_e[tx] = 0.f;
+    for (int cc = 0; cc < C; ++cc) {
+      e = s_a[cc * 32 + tx] + s_g[cc * 32 + tx] * e;
+      s_e[(cc + 1) * 32 + tx] = e;
+    }
+  }
+  __syncthreads();
+  const float ein = s_e[tid];
+  float hq[kM];
+#pragma unroll
+  for (int q = 0; q < kM; ++q) dp[q] += gq[q] * ein;
+  float nxt = 0.f, h = 1.f;
+#pragma unroll
+  for (int q = kM - 1; q >= 0; --q) {
+    hq[q] = 1.f;
+    if (q < kn) {
+      const int k = k0 + q;
+      dp[q] = dp[q] - s_lc[k] * nxt;  // local x with zero carry from above
+      nxt = dp[q];
+      h *= -s_lc[k];
+      hq[q] = h;
+    }
+  }
+  s_a[tid] = dp[0];
+  s_g[tid] = hq[0];
+  __syncthreads();
+  if (c == 0) {  // backward carries: s_e[cc] = x(first level of chunk cc), s_e[C] = 0
+    float x = 0.f;
+    s_e[C * 32 + tx] = 0.f;
+    for (int cc = C - 1; cc >= 0; --cc) {
+      x = s_a[cc * 32 + tx] + s_g[cc * 32 + tx] * x;
+      s_e[cc * 32 + tx] = x;
+    }
+  }
+  __syncthreads();
+  const float xin = s_e[(c + 1) * 32 + tx];  // x(k0 + kn), 0 above the top
+  float x_last = 0.f;
+#pragma unroll
+  for (int q = 0; q < kM; ++q) {
+    dp[q] += hq[q] * xin;  // dp now holds x
+    if (q == kn - 1) x_last = dp[q];
+  }
+  s_x[tid] = x_last;
+  __syncthreads();
+  if (!active) return;
+  const float xprev = (c > 0) ? s_x[tid - 32] : 0.f;
+  // final w on faces k0..k0+kn, then rho' and the outputs
+  float wn[kM + 1];
+#pragma unroll
+  for (int q = 0; q < kM + 1; ++q) {
+    const int f = k0 + q;
+    wn[q] = wt[q];
+    if (q <= kn && f >= 1 && f < nz) {
+      const float xf = (q < kn) ? dp[q] : xin;
+      const float xb = (q == 0) ? xprev : dp[q - 1];
+      wn[q] = wt[q] - dtau * b * cpf * s_tfz[f] * (xf - xb) * s_idzw[f];
+    }
+  }
+#pragma unroll
+  for (int q = 0; q < kM; ++q) {
+    if (q < kn) {
+      const int k = k0 + q;
+      const size_t o = (size_t)k * pl;
+      const float dv_new = -(s_rfz[k + 1] * wn[q + 1] - s_rfz[k] * wn[q]) * s_idzc[k];
+      Ro[o] = rs[q] + dtau * b * dv_new;
+      Po[o] = dp[q];
+      Wo[o] = wn[q];
+    }
+  }
+  if (k0 + kn == nz) Wo[(size_t)nz * pl] = w_top;
+}
+
+template <int kM>
+__global__ void __launch_bounds__(640, 2) k_mx_hevi_par(const __grid_constant__ Dims d, const __grid_constant__ Tab t,
+                                                      const __grid_constant__ Flags fl, const __grid_constant__ WS win,
+                                                      const __grid_constant__ WS wout, float dtau,
+                                                      const float* __restrict__ lu, int apply_uv, float cdx,
+                                                      float cdy) {
+  hevi_par_body<kM>(d, t, fl, win, wout, dtau, lu, apply_uv, cdx, cdy, blockIdx.x, blockIdx.y);
+}
+
 template <int kPF, int kRing>
 __global__ void __launch_bounds__(128, 6) k_mx_hevi_col(const __grid_constant__ Dims d, const __grid_constant__ Tab t,
                                                          const __grid_constant__ Flags fl,
@@ -1059,11 +1288,44 @@ int hevi_ring() {
 }
 
 size_t hevi_smem_bytes(int nz, int ring) {
-  return (10 * (size_t)(nz + 1) + (size_t)ring * 10 * 128) * sizeof(float);
+  return (10 * (size_t)(nz + 1) + (size_t)ring * 11 * 128) * sizeof(float);
+}
+
+// Levels per thread of the level-split column kernel (0 = one thread per
+// column, hevi_body); VIBE_GB300_HEVI_PAR=0|4|8 overrides the built-in choice.
+int hevi_par_levels(int nz) {
+  static int v = -1;
+  if (v < 0) {
+    v = kDefaultHeviPar;
+    if (const char* e = std::getenv("VIBE_GB300_HEVI_PAR")) {
+      const int x = std::atoi(e);
+      if (x == 0 || x == 4 || x == 8) v = x;
+    }
+  }
+  if (v == 0) return 0;
+  int m = v;
+  if ((nz + m - 1) / m > 20) m = 8;       // at most 20 chunks (640 threads)
+  return ((nz + m - 1) / m > 20) ? 0 : m;  // taller columns: one thread per column
+}
+
+size_t hevi_par_smem_bytes(int nz, int m) {
+  const int C = (nz + m - 1) / m;
+  return (10 * (size_t)(nz + 1) + (size_t)32 * (4 * C + 1)) * sizeof(float);
 }
 
 void mixed_hevi_column(const Dims& d, const Tab& t, const Flags& fl, const WS& win, const WS& wout, float dtau,
                        const float* lu, bool apply_uv, cudaStream_t stream) {
+  if (const int m = hevi_par_levels(d.nz)) {
+    const dim3 bp(32, (d.nz + m - 1) / m);
+    const dim3 gp((d.nx + 31) / 32, d.ny);
+    const float cdx = -(float)kCp * dtau * t.dx_inv, cdy = -(float)kCp * dtau * t.dy_inv;
+    const size_t sm = hevi_par_smem_bytes(d.nz, m);
+    if (m == 4)
+      k_mx_hevi_par<4><<<gp, bp, sm, stream>>>(d, t, fl, win, wout, dtau, lu, apply_uv ? 1 : 0, cdx, cdy);
+    else
+      k_mx_hevi_par<8><<<gp, bp, sm, stream>>>(d, t, fl, win, wout, dtau, lu, apply_uv ? 1 : 0, cdx, cdy);
+    return;
+  }
   const dim3 bc(32, 4);
   const int ring = hevi_ring();
   const size_t smem = hevi_smem_bytes(d.nz, ring);
@@ -1257,7 +1519,7 @@ MixedBatch* mixed_batch_build(const std::vector<MixedDomain>& doms, const Flags&
     if (m.d.nz != nz) return nullptr;
   auto* b = new MixedBatch();
   b->err = err;
-  b->hevi_smem = (10 * (size_t)(nz + 1) + (size_t)kBatchRing * 10 * 128) * sizeof(float);
+  b->hevi_smem = (10 * (size_t)(nz + 1) + (size_t)kBatchRing * 11 * 128) * sizeof(float);
   const double dts[3] = {dt / 3.0, dt / 2.0, dt};
   const int nd = (int)doms.size();
   auto sub_out = [&](const MixedDomain& m, int n) { return (n & 1) ? m.WB : m.WA; };
