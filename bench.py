@@ -444,6 +444,54 @@ def reference_arm(args):
     print(json.dumps(line))
 
 
+# ---- ranks: one process per GPU, each advancing its own replica -------------
+class Ranks:
+    """Replica ranks under torchrun (weak scaling: every rank advances its own
+    ensemble member). The data path has no collective; the only ones are the
+    timing barrier and the max over ranks of the timed region."""
+
+    def __init__(self, world, rank, backend="nccl", device=None):
+        import torch
+        self.torch = torch
+        self.world, self.rank, self.device = world, rank, device
+        self.dist = None
+        if world > 1:
+            import torch.distributed as dist
+            if backend == "nccl":
+                dist.init_process_group("nccl", device_id=device)
+            else:
+                dist.init_process_group(backend)
+            self.dist = dist
+
+    def barrier(self):
+        if self.dist is not None:
+            self.dist.barrier()
+        if self.device is not None and self.device.type == "cuda":
+            self.torch.cuda.synchronize()
+
+    def max(self, x):
+        if self.dist is None:
+            return x
+        t = self.torch.tensor([x], dtype=self.torch.float64, device=self.device or "cpu")
+        self.dist.all_reduce(t, op=self.dist.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self):
+        if self.dist is not None:
+            self.dist.destroy_process_group()
+            self.dist = None
+
+
+def member_seed(rank):
+    """Seed of the perturbations of the replica a rank advances."""
+    return 1 + rank
+
+
+def whole_job_rate(world, cells, steps, ms_max):
+    """Cell-updates/s of all ranks together over the slowest rank's time."""
+    return world * cells * steps / (ms_max * 1e-3)
+
+
 # ---- GPU arm -----------------------------------------------------------------
 def main():
     ap = argparse.ArgumentParser()
@@ -479,22 +527,8 @@ def main():
 
     import torch
     torch.cuda.set_device(local)
-    dist = None
-    if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
-
-    def barrier():
-        if dist is not None:
-            dist.barrier()
-        torch.cuda.synchronize()
-
-    def max_over_ranks(x):
-        if dist is None:
-            return x
-        t = torch.tensor([x], dtype=torch.float64, device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        return float(t.item())
+    ranks = Ranks(world, rank, "nccl", torch.device("cuda", local))
+    barrier, max_over_ranks = ranks.barrier, ranks.max
 
     import vibe_gb300 as vg
     setup = case_setup(vg.Setup, args.nx, args.ny)
@@ -502,7 +536,7 @@ def main():
 
     def make(prec):
         m = vg.Model(setup, prec)
-        th, pi = perturbed_state(setup, m.get(4), m.get(3), m.zeta(), seed=1 + rank,
+        th, pi = perturbed_state(setup, m.get(4), m.get(3), m.zeta(), seed=member_seed(rank),
                                  nx_full=args.nx, ny_full=args.ny)
         m.set(4, th)
         m.set(5, pi)
@@ -592,9 +626,9 @@ def main():
     nest = nest_leg(vg, torch, args.warmup) if not args.no_nest else None
     window = window_leg(vg, torch) if not args.no_window else None
 
-    value = world * cells * args.steps / (ms_mx * 1e-3)
-    value64 = world * cells * k64 / (ms_64 * 1e-3)
-    e2e = world * cells * e2e_steps / (ms_e2e * 1e-3)
+    value = whole_job_rate(world, cells, args.steps, ms_mx)
+    value64 = whole_job_rate(world, cells, k64, ms_64)
+    e2e = whole_job_rate(world, cells, e2e_steps, ms_e2e)
 
     # roofline of the dominant kernel class (live CUDA-event times)
     peak, peak_kind = measured_peak()
@@ -612,6 +646,7 @@ def main():
     share = {names[c]: round(ktimes[c][0] / max(sum(v[0] for v in ktimes.values()), 1e-9), 4) for c in ktimes}
 
     if rank != 0:
+        ranks.close()
         return
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -648,8 +683,7 @@ def main():
     if cpu is not None:
         line["cpu_baseline"] = cpu
     print(json.dumps(line))
-    if dist is not None:
-        dist.destroy_process_group()
+    ranks.close()
 
 
 if __name__ == "__main__":

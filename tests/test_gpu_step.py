@@ -377,3 +377,17 @@ def test_rigid_ground_and_lid(vg):
                 w = vg.interior(s, 2, m.get(2))
                 edge = max(np.abs(w[0]).max(), np.abs(w[-1]).max())
                 assert (edge == 0.0) == bool(rigid), (prec, rigid, edge)
+
+
+@pytest.mark.parametrize("dims", [(13, 7, 5), (9, 11, 3), (1, 6, 4), (2, 3, 6)])
+def test_mixed_hevi_ragged_grids(vg, oc, dims):
+    """The HEVI column kernels on odd and tiny horizontal sizes (a thread's
+    second column falls on the ghost line when nx is odd)."""
+    nx, ny, nz = dims
+    t = small_setup(vg, nx=nx, ny=ny, nz=nz, bubble_xc=nx * 125.0, bubble_yc=ny * 125.0, bubble_zc=500.0,
+                    **STEP_CASES[3])
+    with vg.Model(t, vg.MIXED) as m:
+        o = oc.Model(oracle_setup(oc, t), "port")
+        m.step(1.0, 3, 2)
+        assert o.rk3_step(1.0, 3) == 0 and o.rk3_step(1.0, 3) == 0
+        assert_state_close(vg, t, m.state(), o.state(), 2 * TOLMX, range(7), "mixed HEVI grid %s" % (dims,))

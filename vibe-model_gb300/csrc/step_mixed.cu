@@ -528,6 +528,7 @@ __global__ void k_mx_fb_mom(const __grid_constant__ Dims d, const __grid_constan
 // applies the final update in place. cdx = -cp dtau / dx, cdy likewise.
 constexpr int kDefaultHeviRing = 4;  // single-domain column kernel: 0 = register ring
 constexpr int kDefaultHeviPar = 0;   // levels per thread of the level-split column kernel (0 = off)
+constexpr int kDefaultHeviTwo = 0;   // ring depth of the two-columns-per-thread kernel (0 = off)
 constexpr int kBatchRing = 0;        // work-list column kernel of groups
 
 // 4-byte asynchronous global -> shared copies (sm_80+ cp.async), grouped
@@ -1025,6 +1026,260 @@ void mixed_fb_substep(const Dims& d, const Tab& t, const Flags& fl, const WS& wi
   k_mx_fb_mom<<<g3(d.nx + 1, d.ny + 1, d.nz + 1, b), b, 0, stream>>>(d, t, win, wout, dtau, 1);
 }
 
+__device__ __forceinline__ void cp_async8(float* smem, const float* gmem) {
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(sa), "l"(gmem) : "memory");
+}
+
+// ---- the HEVI column update for two adjacent columns per thread ----------
+// Same arithmetic per column and level as hevi_body; a thread owns columns i
+// and i+1 (i even, so every row access is one aligned 8-byte load or store of
+// both columns) and carries two independent recurrences. Forward loads go
+// through a kRing-deep cp.async ring (8-byte copies for the row pairs, 4-byte
+// for the three single neighbours); the backward sweep reads the parked data
+// (L2) four levels ahead in registers. With nx odd, the last thread of a row
+// computes a second, ghost column (i + 1 = nx) from in-bounds ghost-line data
+// and stores nothing of it.
+template <int kRing>
+__device__ __forceinline__ void hevi2_body(const Dims& d, const Tab& t, const Flags& fl, const WS& win,
+                                           const WS& wout, float dtau, const float* __restrict__ lu, int apply_uv,
+                                           float cdx, float cdy, int bx, int by) {
+  extern __shared__ float s_tab[];
+  const int nz = d.nz;
+  float* s_tfz = s_tab;                    // nz+1
+  float* s_idzw = s_tfz + (nz + 1);        // nz+1
+  float* s_rfz = s_idzw + (nz + 1);        // nz+1
+  float* s_idzc = s_rfz + (nz + 1);        // nz
+  float* s_kap = s_idzc + nz;              // nz
+  float* s_la = s_kap + nz;                // nz
+  float* s_lc = s_la + nz;                 // nz
+  float* s_li = s_lc + nz;                 // nz
+  float* s_r0 = s_li + nz;                 // nz
+  float* s_t0 = s_r0 + nz;                 // nz
+  const int tid = threadIdx.y * blockDim.x + threadIdx.x;
+  for (int e = tid; e <= nz; e += 128) {
+    s_tfz[e] = t.tfz[e];
+    s_idzw[e] = t.idzw[e];
+    s_rfz[e] = t.rfz[e];
+    if (e < nz) {
+      s_idzc[e] = t.idzc[e];
+      s_kap[e] = t.kap[e];
+      s_la[e] = lu[e];
+      s_lc[e] = lu[nz + e];
+      s_li[e] = lu[2 * nz + e];
+      s_r0[e] = t.r0c[e];
+      s_t0[e] = t.t0c[e];
+    }
+  }
+  __syncthreads();
+  const int i = 2 * (bx * blockDim.x + threadIdx.x);
+  const int j = by * blockDim.y + threadIdx.y;
+  if (i >= d.nx || j >= d.ny) return;
+  const bool two = i + 1 < d.nx;
+  const float b = (float)fl.hevi_beta, ob = 1.f - b;
+  const float cpf = (float)kCp;
+  const size_t col = (size_t)j * d.P + i;
+  const size_t pl = d.plane;
+  const float* __restrict__ U0 = win.f[U] + col;
+  const float* __restrict__ V0 = win.f[V] + col;
+  const float* __restrict__ W0 = win.f[W] + col;
+  const float* __restrict__ P0 = win.f[PI] + col;
+  const float* __restrict__ R0 = win.f[RHO] + col;
+  float* __restrict__ Wo = wout.f[W] + col;
+  float* __restrict__ Po = wout.f[PI] + col;
+  float* __restrict__ Ro = wout.f[RHO] + col;
+  float* __restrict__ Uo = wout.f[U] + col;
+  float* __restrict__ Vo = wout.f[V] + col;
+  const size_t vn = d.P;
+  const float dxi = t.dx_inv, dyi = t.dy_inv;
+  // single neighbours: u(i+2) (u(i+1) when i+1 is the last face), pi'(i-1)
+  // (clamped to i), pi'(i+2) (clamped to the last column); row pairs j-1, j+1
+  // clamped to j
+  const int ou2 = two ? 2 : 1;
+  const int opw = (i > 0) ? -1 : 0;
+  const int ope = (i + 2 < d.nx) ? 2 : (two ? 1 : 0);
+  const long long os = (j > 0) ? -(long long)vn : 0, on = (j + 1 < d.ny) ? (long long)vn : 0;
+  const bool last_j = (j == d.ny - 1);
+  auto st2 = [&](float* p, float a, float c) {
+    if (two) *reinterpret_cast<float2*>(p) = make_float2(a, c);
+    else *p = a;
+  };
+  // ring: per slot 8 float2 fields (w, pi', u(i..i+1), v(j), v(j+1), rho',
+  // pi'(j-1), pi'(j+1)) then 3 float fields (u(i+2), pi'(i-1), pi'(i+2))
+  float* ring = s_tab + ((10 * (size_t)(nz + 1) + 3) & ~(size_t)3);
+  auto r2 = [&](int slot, int f) -> float* { return ring + ((size_t)slot * 19 * 128) + ((size_t)f * 128 + tid) * 2; };
+  auto r1 = [&](int slot, int f) -> float* {
+    return ring + ((size_t)slot * 19 * 128) + 16 * 128 + (size_t)f * 128 + tid;
+  };
+  auto issue = [&](int L) {
+    const int slot = L % kRing;
+    const size_t o = (size_t)L * pl, o1 = o + pl;
+    cp_async8(r2(slot, 0), W0 + o1);
+    if (L + 1 < nz) cp_async8(r2(slot, 1), P0 + o1);
+    else { r2(slot, 1)[0] = 0.f; r2(slot, 1)[1] = 0.f; }
+    cp_async8(r2(slot, 2), U0 + o);
+    cp_async8(r2(slot, 3), V0 + o);
+    cp_async8(r2(slot, 4), V0 + o + vn);
+    cp_async8(r2(slot, 5), R0 + o);
+    cp_async4(r1(slot, 0), U0 + o + ou2);
+    if (apply_uv) {
+      cp_async8(r2(slot, 6), P0 + o + os);
+      cp_async8(r2(slot, 7), P0 + o + on);
+      cp_async4(r1(slot, 1), P0 + o + opw);
+      cp_async4(r1(slot, 2), P0 + o + ope);
+    }
+  };
+  for (int L = 0; L < kRing; ++L) {
+    if (L < nz) issue(L);
+    cp_async_commit();
+  }
+  float pk[2], wk[2], wtk[2], dpp[2] = {0.f, 0.f};
+  {
+    const float2 p0 = *reinterpret_cast<const float2*>(P0);
+    const float2 w0 = *reinterpret_cast<const float2*>(W0);
+    pk[0] = p0.x; pk[1] = p0.y;
+    wk[0] = w0.x; wk[1] = w0.y;
+    wtk[0] = wk[0]; wtk[1] = wk[1];  // face 0: no pressure gradient
+    st2(Wo, wk[0], wk[1]);
+  }
+  for (int k = 0; k < nz; ++k) {
+    cp_async_wait<kRing - 1>();
+    const int slot = k % kRing;
+    const float2 fw = *reinterpret_cast<const float2*>(r2(slot, 0));
+    const float2 fp = *reinterpret_cast<const float2*>(r2(slot, 1));
+    const float2 fu = *reinterpret_cast<const float2*>(r2(slot, 2));
+    const float2 fv0 = *reinterpret_cast<const float2*>(r2(slot, 3));
+    const float2 fv1 = *reinterpret_cast<const float2*>(r2(slot, 4));
+    const float2 fr = *reinterpret_cast<const float2*>(r2(slot, 5));
+    const float fu2 = *r1(slot, 0);
+    float u0[2] = {fu.x, fu.y}, u1[2] = {fu.y, fu2};
+    float v0[2] = {fv0.x, fv0.y}, v1[2] = {fv1.x, fv1.y};
+    if (apply_uv) {
+      const float2 fs = *reinterpret_cast<const float2*>(r2(slot, 6));
+      const float2 fn = *reinterpret_cast<const float2*>(r2(slot, 7));
+      const float fpw = *r1(slot, 1), fpe = *r1(slot, 2);
+      const float tx_ = s_t0[k] * cdx, ty_ = s_t0[k] * cdy;
+      // column i: west pi'(i-1), east pi'(i+1) (itself at the last column);
+      // column i+1: west pi'(i), east pi'(i+2)
+      const float peA = two ? pk[1] : pk[0];
+      u0[0] += tx_ * (pk[0] - fpw);
+      u1[0] += tx_ * (peA - pk[0]);
+      u0[1] += tx_ * (pk[1] - pk[0]);
+      u1[1] += tx_ * (fpe - pk[1]);
+      v0[0] += ty_ * (pk[0] - fs.x);
+      v1[0] += ty_ * (fn.x - pk[0]);
+      v0[1] += ty_ * (pk[1] - fs.y);
+      v1[1] += ty_ * (fn.y - pk[1]);
+    }
+    const size_t o = (size_t)k * pl;
+    st2(Uo + o, u0[0], u0[1]);
+    st2(Vo + o, v0[0], v0[1]);
+    if (two) {
+      if (i + 1 == d.nx - 1) Uo[o + 2] = u1[1];  // face nx
+    } else {
+      Uo[o + 1] = u1[0];
+    }
+    if (last_j) st2(Vo + o + vn, v1[0], v1[1]);
+    const float wk1[2] = {fw.x, fw.y}, pk1in[2] = {fp.x, fp.y}, r0v[2] = {fr.x, fr.y};
+    const float rk = s_rfz[k], rk1 = s_rfz[k + 1], idz = s_idzc[k];
+    float dpk[2], rsv[2], wtk1[2], pk1[2];
+#pragma unroll
+    for (int c = 0; c < 2; ++c) {
+      wtk1[c] = wk1[c];
+      pk1[c] = 0.f;
+      if (k + 1 < nz) {
+        pk1[c] = pk1in[c];
+        wtk1[c] = wk1[c] - dtau * ob * cpf * s_tfz[k + 1] * (pk1[c] - pk[c]) * s_idzw[k + 1];
+      }
+      const float Dh = -(s_r0[k] * ((u1[c] - u0[c]) * dxi + (v1[c] - v0[c]) * dyi));
+      const float dv_old = -(rk1 * wk1[c] - rk * wk[c]) * idz;
+      const float dv_t = -(rk1 * wtk1[c] - rk * wtk[c]) * idz;
+      const float S = Dh + ob * dv_old;
+      const float rhs = pk[c] + dtau * s_kap[k] * (S + b * dv_t);
+      dpk[c] = (k == 0) ? rhs * s_li[0] : (rhs - s_la[k] * dpp[c]) * s_li[k];
+      rsv[c] = r0v[c] + dtau * S;
+    }
+    st2(Po + o, dpk[0], dpk[1]);
+    st2(Ro + o, rsv[0], rsv[1]);
+    st2(Wo + o + pl, wtk1[0], wtk1[1]);
+    if (k + kRing < nz) issue(k + kRing);
+    cp_async_commit();
+#pragma unroll
+    for (int c = 0; c < 2; ++c) {
+      dpp[c] = dpk[c];
+      wk[c] = wk1[c];
+      wtk[c] = wtk1[c];
+      pk[c] = pk1[c];
+    }
+  }
+  cp_async_wait<0>();
+  // backward sweep (as hevi_body), both columns
+  constexpr int kB = 4;
+  float2 bdp[kB], bwt[kB], bS[kB];
+  auto ld2 = [&](const float* p) -> float2 {
+    if (two) return *reinterpret_cast<const float2*>(p);
+    return make_float2(*p, 0.f);
+  };
+  auto loadB = [&](int kk, int q) {
+    const size_t o = (size_t)kk * pl;
+    bdp[q] = (kk >= 1) ? ld2(Po + o - pl) : make_float2(0.f, 0.f);
+    bwt[q] = ld2(Wo + o);
+    bS[q] = ld2(Ro + o);
+  };
+#pragma unroll
+  for (int q = 0; q < kB; ++q)
+    if (nz - 1 - q >= 0) loadB(nz - 1 - q, q);
+  float xu[2] = {dpp[0], dpp[1]};
+  float wu[2];
+  {
+    const float2 t2 = ld2(Wo + (size_t)nz * pl);
+    wu[0] = t2.x;
+    wu[1] = t2.y;
+  }
+  for (int kk0 = nz - 1; kk0 >= 0; kk0 -= kB) {
+#pragma unroll
+    for (int q = 0; q < kB; ++q) {
+      const int kk = kk0 - q;
+      if (kk >= 0) {
+        const int k = kk - 1;
+        const size_t okk = (size_t)kk * pl;
+        const float bd[2] = {bdp[q].x, bdp[q].y}, bw[2] = {bwt[q].x, bwt[q].y}, bs[2] = {bS[q].x, bS[q].y};
+        float xk[2], wkk[2], rn[2];
+#pragma unroll
+        for (int c = 0; c < 2; ++c) {
+          xk[c] = 0.f;
+          wkk[c] = bw[c];
+          if (k >= 0) {
+            xk[c] = bd[c] - s_lc[k] * xu[c];
+            wkk[c] = bw[c] - dtau * b * cpf * s_tfz[kk] * (xu[c] - xk[c]) * s_idzw[kk];
+          }
+          const float dv_new = -(s_rfz[kk + 1] * wu[c] - s_rfz[kk] * wkk[c]) * s_idzc[kk];
+          rn[c] = bs[c] + dtau * b * dv_new;
+        }
+        if (kk - kB >= 0) loadB(kk - kB, q);
+        st2(Ro + okk, rn[0], rn[1]);
+        st2(Po + okk, xu[0], xu[1]);
+        st2(Wo + okk, wkk[0], wkk[1]);
+#pragma unroll
+        for (int c = 0; c < 2; ++c) {
+          xu[c] = xk[c];
+          wu[c] = wkk[c];
+        }
+      }
+    }
+  }
+}
+
+template <int kRing>
+__global__ void __launch_bounds__(128, 4) k_mx_hevi_col2(const __grid_constant__ Dims d, const __grid_constant__ Tab t,
+                                                          const __grid_constant__ Flags fl,
+                                                          const __grid_constant__ WS win,
+                                                          const __grid_constant__ WS wout, float dtau,
+                                                          const float* __restrict__ lu, int apply_uv, float cdx,
+                                                          float cdy) {
+  hevi2_body<kRing>(d, t, fl, win, wout, dtau, lu, apply_uv, cdx, cdy, blockIdx.x, blockIdx.y);
+}
+
 // ---- the same HEVI column update with the levels split over threads ------
 // The column system's LU factors (la, lc, li) depend on the level only, so
 // both recurrences, dp(k) = (rhs(k) - la(k) dp(k-1)) li(k) and
@@ -1313,8 +1568,37 @@ size_t hevi_par_smem_bytes(int nz, int m) {
   return (10 * (size_t)(nz + 1) + (size_t)32 * (4 * C + 1)) * sizeof(float);
 }
 
+// Ring depth of the two-columns-per-thread kernel (0 = off);
+// VIBE_GB300_HEVI_TWO=0|2|3|4 overrides the built-in choice.
+int hevi_two_ring() {
+  static int v = -1;
+  if (v < 0) {
+    v = kDefaultHeviTwo;
+    if (const char* e = std::getenv("VIBE_GB300_HEVI_TWO")) {
+      const int x = std::atoi(e);
+      if (x == 0 || x == 2 || x == 3 || x == 4) v = x;
+    }
+  }
+  return v;
+}
+
+size_t hevi2_smem_bytes(int nz, int ring) {
+  return ((((size_t)10 * (nz + 1) + 3) & ~(size_t)3) + (size_t)ring * 19 * 128) * sizeof(float);
+}
+
 void mixed_hevi_column(const Dims& d, const Tab& t, const Flags& fl, const WS& win, const WS& wout, float dtau,
                        const float* lu, bool apply_uv, cudaStream_t stream) {
+  if (const int r2 = hevi_two_ring()) {
+    const dim3 bc(32, 4);
+    const dim3 g((d.nx + 63) / 64, (d.ny + 3) / 4);
+    const float cdx = -(float)kCp * dtau * t.dx_inv, cdy = -(float)kCp * dtau * t.dy_inv;
+    const size_t sm = hevi2_smem_bytes(d.nz, r2);
+    const int au = apply_uv ? 1 : 0;
+    if (r2 == 4) k_mx_hevi_col2<4><<<g, bc, sm, stream>>>(d, t, fl, win, wout, dtau, lu, au, cdx, cdy);
+    else if (r2 == 3) k_mx_hevi_col2<3><<<g, bc, sm, stream>>>(d, t, fl, win, wout, dtau, lu, au, cdx, cdy);
+    else k_mx_hevi_col2<2><<<g, bc, sm, stream>>>(d, t, fl, win, wout, dtau, lu, au, cdx, cdy);
+    return;
+  }
   if (const int m = hevi_par_levels(d.nz)) {
     const dim3 bp(32, (d.nz + m - 1) / m);
     const dim3 gp((d.nx + 31) / 32, d.ny);
