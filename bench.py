@@ -566,6 +566,7 @@ def main():
 
     # ---- mixed path (the headline) ----
     mx = make(vg.MIXED)
+    tuning = mx.autotune(DT, NSUB)  # launch shapes for this grid (same update, FP32 rounding aside)
     mx.step(DT, NSUB, args.warmup)  # the first step runs eagerly, the next capture the step graphs
     with ClockSampler(local) as clk:
         ms_mx, restarts = timed_steps(mx, args.steps)  # graph replay
@@ -672,6 +673,7 @@ def main():
         "step_roofline": {"bytes_per_cell_update": 1944, "achieved": 1944.0 * value / world / 1e9,
                           "peak": peak, "unit": "GB/s", "frac": 1944.0 * value / world / 1e9 / peak},
         "gpu_launches": launches,
+        "tuning": tuning,
         "clocks": clk.summary(),
     }
     if si is not None:

@@ -211,6 +211,22 @@ int vibe_gb300_window_stats(const vibe_gb300_window *w, double *last_ms, size_t 
 int vibe_gb300_slow_tendency(vibe_gb300_model *m, double *const *host_out);
 int vibe_gb300_acoustic_substep(vibe_gb300_model *m, double dtau);
 int vibe_gb300_hevi_substep(vibe_gb300_model *m, double dtau);
+/* Autotuner of the mixed step: times, on this model's grid, the launch shapes
+ * of the same update -- the HEVI column kernel variant (0 register ring,
+ * 1 cp.async ring, 2/3 two columns per thread; -1 = the built-in choice) and
+ * the stage kernel's levels per block -- and keeps the fastest for every
+ * single model of this grid in the process (groups keep the built-in column
+ * kernel). Variants differ only by FP32 rounding (FMA contraction, vertical
+ * fluxes recomputed at level-chunk starts). The model's state is left as it
+ * was. Returns the choice, its time per step and the built-in one's. */
+typedef struct {
+  int stage_levels;
+  int column_kernel;
+  double ms_per_step;
+  double default_ms_per_step;
+  int candidates;
+} vibe_gb300_tuning;
+int vibe_gb300_autotune(vibe_gb300_model *m, double dt, int n_sub, vibe_gb300_tuning *out);
 /* Device-side copy of the prognostic state: op 0 saves the current state
  * (all species, model layout) into a snapshot held by the model, op 1 puts
  * it back (and refreshes the FP32 working copy). Asynchronous on the model's

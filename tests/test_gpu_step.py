@@ -391,3 +391,20 @@ def test_mixed_hevi_ragged_grids(vg, oc, dims):
         m.step(1.0, 3, 2)
         assert o.rk3_step(1.0, 3) == 0 and o.rk3_step(1.0, 3) == 0
         assert_state_close(vg, t, m.state(), o.state(), 2 * TOLMX, range(7), "mixed HEVI grid %s" % (dims,))
+
+
+def test_autotune_keeps_the_update(vg):
+    """The autotuner only chooses among launch shapes of the same update: a run
+    after tuning matches the run before it to FP32 rounding (1e-6 of each
+    field's scale), and tuning leaves the model's state as it was."""
+    s = small_setup(vg, acoustic_mode=2, ref_kind=1, nx=45, ny=22, nz=24)
+    with vg.Model(s, vg.MIXED) as a:
+        a.save_snapshot()
+        a.step(2.0, 4, 3)
+        before = a.state()
+        a.restore_snapshot()
+        t = a.autotune(2.0, 4)
+        assert t["column_kernel"] in (-1, 0, 1, 2, 3) and 1 <= t["stage_levels"] <= s.nz
+        assert t["ms_per_step"] > 0.0 and t["ms_per_step"] <= t["default_ms_per_step"] and t["candidates"] >= 5
+        a.step(2.0, 4, 3)
+        assert_state_close(vg, s, a.state(), before, 1e-6, range(7), "tuned vs built-in launch shapes")

@@ -1032,6 +1032,88 @@ int vibe_gb300_hevi_substep(vibe_gb300_model* m, double dtau) {
   return read_status(m);
 }
 
+// ---- autotuner: time the launch shapes of the mixed step that give the
+// same bits (column kernel variant, then the stage kernel's levels per
+// block) on this model's grid and keep the fastest for the process.
+int vibe_gb300_autotune(vibe_gb300_model* m, double dt, int n_sub, vibe_gb300_tuning* out) {
+  if (!m || !(dt > 0.0) || !out) return fail(VIBE_GB300_EBADARG, "bad argument");
+  if (m->precision != VIBE_GB300_MIXED) return fail(VIBE_GB300_EUNSUPPORTED, "the autotuner tunes the mixed path");
+  CUDA_OK(cudaStreamSynchronize(m->stream));
+  const size_t n = m->d.plane * (size_t)(m->d.nz + 1);
+  std::vector<void*> keep(NSPECIES, nullptr);
+  auto release = [&]() {
+    for (void* p : keep)
+      if (p) cudaFree(p);
+  };
+  for (int q = 0; q < NSPECIES; ++q) {
+    if (cudaMalloc(&keep[q], n * sizeof(double)) != cudaSuccess) {
+      release();
+      return fail(VIBE_GB300_EDEVICE, "autotune state copy");
+    }
+    CUDA_OK(cudaMemcpyAsync(keep[q], m->S[m->cur][q], n * sizeof(double), cudaMemcpyDeviceToDevice, m->stream));
+  }
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  const int kSteps = 3;
+  auto trial = [&](const MixedTune& tn, double* ms) -> int {
+    mixed_set_tune(m->d, tn);
+    drop_graphs(m);
+    for (int q = 0; q < NSPECIES; ++q)
+      CUDA_OK(cudaMemcpyAsync(m->S[m->cur][q], keep[q], n * sizeof(double), cudaMemcpyDeviceToDevice, m->stream));
+    if (int rc = sync_working(m)) return rc;
+    if (int rc = enqueue_steps(m, dt, n_sub, 2)) return rc;  // eager step + graph capture
+    CUDA_OK(cudaEventRecord(e0, m->stream));
+    if (int rc = enqueue_steps(m, dt, n_sub, kSteps)) return rc;
+    CUDA_OK(cudaEventRecord(e1, m->stream));
+    if (int rc = read_status(m)) return rc;
+    float t = 0.f;
+    CUDA_OK(cudaEventElapsedTime(&t, e0, e1));
+    *ms = t / kSteps;
+    return 0;
+  };
+  MixedTune best, cur;
+  double best_ms = 0.0, default_ms = 0.0, ms = 0.0;
+  int rc = trial(MixedTune{}, &default_ms), tried = 1;
+  best_ms = default_ms;
+  // column kernel: 0 register ring, 1 cp.async ring, 2/3 two columns per thread
+  for (int c = 0; c <= 3 && !rc; ++c) {
+    cur = MixedTune{};
+    cur.column = c;
+    rc = trial(cur, &ms);
+    ++tried;
+    if (!rc && ms < best_ms) { best_ms = ms; best = cur; }
+  }
+  // stage levels per block around the built-in choice
+  const int base = mixed_stage_levels(m->d);
+  const int cand[] = {m->d.nz, (m->d.nz + 1) / 2, (m->d.nz + 2) / 3, (m->d.nz + 3) / 4, base / 2, base * 2};
+  for (int v : cand) {
+    if (rc || v < 4 || v > m->d.nz || v == base) continue;
+    cur = best;
+    cur.stage_levels = v;
+    rc = trial(cur, &ms);
+    ++tried;
+    if (!rc && ms < best_ms) { best_ms = ms; best = cur; }
+  }
+  mixed_set_tune(m->d, rc ? MixedTune{} : best);
+  drop_graphs(m);
+  for (int q = 0; q < NSPECIES; ++q)
+    cudaMemcpyAsync(m->S[m->cur][q], keep[q], n * sizeof(double), cudaMemcpyDeviceToDevice, m->stream);
+  const int rs = sync_working(m);
+  cudaStreamSynchronize(m->stream);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  release();
+  if (rc) return rc;
+  if (rs) return rs;
+  out->stage_levels = best.stage_levels > 0 ? best.stage_levels : base;
+  out->column_kernel = best.column;
+  out->ms_per_step = best_ms;
+  out->default_ms_per_step = default_ms;
+  out->candidates = tried;
+  return 0;
+}
+
 int vibe_gb300_snapshot(vibe_gb300_model* m, int op) {
   if (!m || op < 0 || op > 1) return fail(VIBE_GB300_EBADARG, "bad argument");
   const size_t n = m->d.plane * (size_t)(m->d.nz + 1);

@@ -51,6 +51,16 @@ void diag_cfl(const Dims& d, const Metric& met, double* const* st, double dt, do
 }  // namespace vgb
 struct vibe_nest_placement;
 namespace vgb {
+// Launch choices of the mixed step per grid (stage levels per block, 0 =
+// built-in choice; column kernel 0 register ring, 1 cp.async ring, 2/3 two
+// columns per thread, -1 = built-in), as the autotuner sets them.
+struct MixedTune {
+  int stage_levels = 0;
+  int column = -1;
+};
+void mixed_set_tune(const Dims& d, const MixedTune& t);
+int mixed_stage_levels(const Dims& d);
+
 int nest_model_layout(int op, const vibe_nest_placement* p, int nvars, int pnx, int pny, int pnz,
                       const double* const* parent, size_t p_pitch, size_t p_plane, int cnx, int cny, int cnz,
                       const double* const* child_in, double* const* out, size_t c_pitch, size_t c_plane,

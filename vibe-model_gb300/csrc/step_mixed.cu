@@ -526,10 +526,32 @@ __global__ void k_mx_fb_mom(const __grid_constant__ Dims d, const __grid_constan
 // backward half); the updated u, v enter this substep's divergence and are
 // written to the output. After the last substep of a stage one u/v kernel
 // applies the final update in place. cdx = -cp dtau / dx, cdy likewise.
+// Per-grid launch choices set by the autotuner (vibe_gb300_autotune): the
+// stage kernel's levels per block and the column kernel variant. Every
+// variant computes the same update; results differ only by FP32 rounding
+// (each variant's own FMA contraction, the stage kernel's recomputed
+// vertical fluxes at level-chunk starts).
+struct TuneKey {
+  int nx, ny, nz;
+  bool operator<(const TuneKey& o) const {
+    return nx != o.nx ? nx < o.nx : (ny != o.ny ? ny < o.ny : nz < o.nz);
+  }
+};
+std::mutex g_tune_mu;
+std::map<TuneKey, MixedTune> g_tune;
+
+bool tune_of(const Dims& d, MixedTune* t) {
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  auto it = g_tune.find(TuneKey{d.nx, d.ny, d.nz});
+  if (it == g_tune.end()) return false;
+  *t = it->second;
+  return true;
+}
+
 constexpr int kDefaultHeviRing = 4;  // single-domain column kernel: 0 = register ring
 constexpr int kDefaultHeviPar = 0;   // levels per thread of the level-split column kernel (0 = off)
 constexpr int kDefaultHeviTwo = 0;   // ring depth of the two-columns-per-thread kernel (0 = off)
-constexpr int kBatchRing = 0;        // work-list column kernel of groups
+constexpr int kBatchRing = 4;        // work-list column kernel of groups (= the single-domain default)
 
 // 4-byte asynchronous global -> shared copies (sm_80+ cp.async), grouped
 __device__ __forceinline__ void cp_async4(float* smem, const float* gmem) {
@@ -916,6 +938,8 @@ static MS64 ms64(double* const* f) {
 // flux per species) small.
 // VIBE_GB300_STAGE_LEVELS=<n> overrides the choice (levels per block).
 static int stage_kchunk(const Dims& d, bool fp64_out) {
+  MixedTune tn;
+  if (tune_of(d, &tn) && tn.stage_levels > 0) return imin(tn.stage_levels, d.nz);
   if (const char* e = std::getenv("VIBE_GB300_STAGE_LEVELS")) {
     const int v = std::atoi(e);
     if (v > 0) return imin(v, d.nz);
@@ -1588,7 +1612,14 @@ size_t hevi2_smem_bytes(int nz, int ring) {
 
 void mixed_hevi_column(const Dims& d, const Tab& t, const Flags& fl, const WS& win, const WS& wout, float dtau,
                        const float* lu, bool apply_uv, cudaStream_t stream) {
-  if (const int r2 = hevi_two_ring()) {
+  MixedTune tn;
+  const bool tuned = tune_of(d, &tn) && tn.column >= 0;
+  int r2 = hevi_two_ring(), ring = hevi_ring();
+  if (tuned) {  // 0: register ring, 1: cp.async ring 4, 2/3: two columns per thread with ring 2/3
+    r2 = (tn.column == 2) ? 2 : (tn.column == 3 ? 3 : 0);
+    ring = (tn.column == 1) ? 4 : 0;
+  }
+  if (r2) {
     const dim3 bc(32, 4);
     const dim3 g((d.nx + 63) / 64, (d.ny + 3) / 4);
     const float cdx = -(float)kCp * dtau * t.dx_inv, cdy = -(float)kCp * dtau * t.dy_inv;
@@ -1599,7 +1630,7 @@ void mixed_hevi_column(const Dims& d, const Tab& t, const Flags& fl, const WS& w
     else k_mx_hevi_col2<2><<<g, bc, sm, stream>>>(d, t, fl, win, wout, dtau, lu, au, cdx, cdy);
     return;
   }
-  if (const int m = hevi_par_levels(d.nz)) {
+  if (const int m = tuned ? 0 : hevi_par_levels(d.nz)) {
     const dim3 bp(32, (d.nz + m - 1) / m);
     const dim3 gp((d.nx + 31) / 32, d.ny);
     const float cdx = -(float)kCp * dtau * t.dx_inv, cdy = -(float)kCp * dtau * t.dy_inv;
@@ -1611,7 +1642,6 @@ void mixed_hevi_column(const Dims& d, const Tab& t, const Flags& fl, const WS& w
     return;
   }
   const dim3 bc(32, 4);
-  const int ring = hevi_ring();
   const size_t smem = hevi_smem_bytes(d.nz, ring);
   const dim3 g((d.nx + bc.x - 1) / bc.x, (d.ny + bc.y - 1) / bc.y);
   const float cdx = -(float)kCp * dtau * t.dx_inv, cdy = -(float)kCp * dtau * t.dy_inv;
@@ -1940,4 +1970,13 @@ void mixed_batch_destroy(MixedBatch* b) {
   delete b;
 }
 
+}  // namespace vgb
+
+namespace vgb {
+void mixed_set_tune(const Dims& d, const MixedTune& t) {
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  if (t.stage_levels <= 0 && t.column < 0) g_tune.erase(TuneKey{d.nx, d.ny, d.nz});
+  else g_tune[TuneKey{d.nx, d.ny, d.nz}] = t;
+}
+int mixed_stage_levels(const Dims& d) { return stage_kchunk(d, false); }
 }  // namespace vgb

@@ -146,6 +146,16 @@ def interior(setup, species, arr):
              HALO:HALO + setup.nx + (species == 0)]
 
 
+class Tuning(ctypes.Structure):
+    """Mirror of vibe_gb300_tuning."""
+    _fields_ = [("stage_levels", _I), ("column_kernel", _I), ("ms_per_step", _D), ("default_ms_per_step", _D),
+                ("candidates", _I)]
+
+
+lib.vibe_gb300_autotune.restype = _I
+lib.vibe_gb300_autotune.argtypes = [_vp, _D, _I, ctypes.POINTER(Tuning)]
+
+
 class Model:
     """A device-resident state plus its RK3 integrator."""
 
@@ -234,6 +244,12 @@ class Model:
 
     def hevi_substep(self, dtau):
         _check(lib.vibe_gb300_hevi_substep(self.h, dtau))
+
+    def autotune(self, dt, n_sub):
+        """Pick the fastest bit-identical launch shapes for this grid (mixed path)."""
+        t = Tuning()
+        _check(lib.vibe_gb300_autotune(self.h, dt, n_sub, ctypes.byref(t)))
+        return {name: getattr(t, name) for name, _ in Tuning._fields_}
 
     def save_snapshot(self):
         """Device copy of the current state (asynchronous)."""
