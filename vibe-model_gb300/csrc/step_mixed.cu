@@ -254,6 +254,42 @@ __device__ __forceinline__ void stage_body(const Dims& d, const Tab& t, const Fl
     const int kc = imin(k, nz - 1);
     __syncthreads();  // every thread is done with the other buffer (level k-1)
     if (tid == 0 && k + 1 <= klast) issue_level(M, sbuf[cur ^ 1], &sbar[cur ^ 1], i0, j0, k + 1, nz);
+    // This level's global loads (the own columns' vertical neighbours and the
+    // base state the stage adds its tendency to), all issued before the wait
+    // for the boxes so that their latencies overlap it and one another.
+    const size_t c = (size_t)k * pl + colc;
+    const int kp1 = imin(k + 1, nz - 1), km = imax(k - 1, 0);
+    const bool do_u = cells_here && in_box && j < ny, do_v = cells_here && in_box && i < nx;
+    const bool has_base = w0.f[U] != nullptr;
+    float gu_p = 0.f, gu_m = 0.f, gw_u = 0.f, gv_p = 0.f, gv_m = 0.f, gw_v = 0.f, g_wt = 0.f, g_rk = 0.f;
+    float bU = 0.f, bV = 0.f, bW = 0.f, bR = 0.f, bP = 0.f, bT = 0.f, bQ = 0.f;
+    if (do_u) {
+      const float* __restrict__ ucol = win.f[U] + (size_t)j * P + (i + ipu);
+      gu_p = ucol[(size_t)kp1 * pl];
+      gu_m = ucol[(size_t)km * pl];
+      gw_u = win.f[W][(size_t)kp1 * pl + (size_t)j * P + (i + ipu)];
+      if (has_base) bU = w0.f[U][c];
+    }
+    if (do_v) {
+      const float* __restrict__ vcol = win.f[V] + (size_t)(j + jpv) * P + i;
+      gv_p = vcol[(size_t)kp1 * pl];
+      gv_m = vcol[(size_t)km * pl];
+      gw_v = win.f[W][(size_t)kp1 * pl + (size_t)(j + jpv) * P + i];
+      if (has_base) bV = w0.f[V][c];
+    }
+    if (cell) {
+      if (has_base) bW = w0.f[W][c];
+      if (cells_here) {
+        g_wt = wcolp[(size_t)(k + 1) * pl];
+        g_rk = win.f[RHO][(size_t)kp1 * pl + colc];
+        if (has_base) {
+          bR = w0.f[RHO][c];
+          bP = w0.f[PI][c];
+          bT = w0.f[THETA][c];
+          bQ = w0.f[QV][c];
+        }
+      }
+    }
     const bool arrived = mbar_wait_bounded(&sbar[cur], (lev >> 1) & 1);
     if (__syncthreads_or(!arrived)) {
       // a box did not arrive: report, and leave none in flight before exiting
@@ -278,38 +314,47 @@ __device__ __forceinline__ void stage_body(const Dims& d, const Tab& t, const Fl
       for (int b = TU; b < NTILE; ++b) fix_box(buf + tile_off(b), R1, 1, i0, j0, M.xmax[b], M.ymax[b], tid);
       __syncthreads();
     }
-    const size_t c = (size_t)k * pl + colc;
-    const int kp1 = imin(k + 1, nz - 1), km = imax(k - 1, 0);
+    // base value of q at this point: preloaded for the dynamic fields
+    auto base_of = [&](int q) -> float {
+      switch (q) {
+        case U: return bU;
+        case V: return bV;
+        case W: return bW;
+        case RHO: return bR;
+        case PI: return bP;
+        case THETA: return bT;
+        case QV: return bQ;
+        default: return w0.f[q][c];
+      }
+    };
     auto emit = [&](int q, float r) {
-      const float o = (w0.f[q] != nullptr) ? w0.f[q][c] + dts * r : r;  // no base: raw tendency
+      const float o = has_base ? base_of(q) + dts * r : r;  // no base: raw tendency
       wout.f[q][c] = o;
       bad |= !isfinite(o);
       if (kRaw) rout.f[q][c] = r;
     };
-    if (cells_here && in_box && j < ny) {  // u face (i, j, k)
+    if (do_u) {  // u face (i, j, k)
       const float ump = sU[o1 + ipu], umm = sU[o1 + dim];
       const float uc = 0.5f * (umm + ump);
       const float ux = (ump - umm) * t.dx_inv;
       const float uy = (sU[o1 + ipu + TW] - sU[o1 + ipu - TW]) * (0.5f * t.dy_inv);
-      const float* __restrict__ ucol = win.f[U] + (size_t)j * P + (i + ipu);
-      const float uz = (ucol[(size_t)kp1 * pl] - ucol[(size_t)km * pl]) * (0.5f * t.idza[k]);
+      const float uz = (gu_p - gu_m) * (0.5f * t.idza[k]);
       const float vc = 0.25f * (sV[o1 + dim - TW] + sV[o1 + ipu - TW] + sV[o1 + dim] + sV[o1 + ipu]);
-      const float wc = 0.5f * (sW[o1 + ipu] + win.f[W][(size_t)kp1 * pl + (size_t)j * P + (i + ipu)]);
+      const float wc = 0.5f * (sW[o1 + ipu] + gw_u);
       float r = -(uc * ux + vc * uy + wc * uz);
       if (fl.coriolis) r += (fl.coriolis == 2 ? t.f0 + t.beta * (((float)j + 0.5f) * t.dy - 0.5f * (float)ny * t.dy) : t.f0) * vc;
       r -= cp * (0.5f * (sT[o3 + dim] + sT[o3 + ipu])) * (sP[o1 + ipu] - sP[o1 + dim]) * t.dx_inv;
       emit(U, r);
     }
-    if (cells_here && in_box && i < nx) {  // v face (i, j, k)
+    if (do_v) {  // v face (i, j, k)
       const int dp1 = jpv * TW, dm1 = djm * TW;
       const float vpp = sV[o1 + dp1], vmm = sV[o1 + dm1];
       const float vc = 0.5f * (vmm + vpp);
       const float vy = (vpp - vmm) * t.dy_inv;
       const float vx = (sV[o1 + dp1 + 1] - sV[o1 + dp1 - 1]) * (0.5f * t.dx_inv);
-      const float* __restrict__ vcol = win.f[V] + (size_t)(j + jpv) * P + i;
-      const float vz = (vcol[(size_t)kp1 * pl] - vcol[(size_t)km * pl]) * (0.5f * t.idza[k]);
+      const float vz = (gv_p - gv_m) * (0.5f * t.idza[k]);
       const float uc = 0.25f * (sU[o1 + dim + dm1] + sU[o1 + dm1] + sU[o1 + dim + dp1] + sU[o1 + dp1]);
-      const float wc = 0.5f * (sW[o1 + dp1] + win.f[W][(size_t)kp1 * pl + (size_t)(j + jpv) * P + i]);
+      const float wc = 0.5f * (sW[o1 + dp1] + gw_v);
       float r = -(uc * vx + vc * vy + wc * vz);
       if (fl.coriolis) r -= (fl.coriolis == 2 ? t.f0 + t.beta * (((float)j + 0.5f) * t.dy - 0.5f * (float)ny * t.dy) : t.f0) * uc;
       r -= cp * (0.5f * (sT[o3 + djm * TW] + sT[o3 + jpv * TW])) * (sP[o1 + dp1] - sP[o1 + dm1]) * t.dy_inv;
@@ -339,12 +384,12 @@ __device__ __forceinline__ void stage_body(const Dims& d, const Tab& t, const Fl
       emit(W, r);
     }
     if (!cells_here) break;
-    const float wt = cell ? wcolp[(size_t)(k + 1) * pl] : 0.f;  // w at face k+1
+    const float wt = g_wt;  // w at face k+1
     if (cell) {  // mass and pi
       const float rc = sR[o1];
       const float fx = sU[o1 + 1] * 0.5f * (rc + sR[o1 + 1]) - sU[o1] * 0.5f * (sR[o1 - 1] + rc);
       const float fy = sV[o1 + TW] * 0.5f * (rc + sR[o1 + TW]) - sV[o1] * 0.5f * (sR[o1 - TW] + rc);
-      const float rkp = win.f[RHO][(size_t)kp1 * pl + colc];
+      const float rkp = g_rk;
       const float fz = wt * 0.5f * (rc + rkp) - wk * 0.5f * (rprev + rc);
       emit(RHO, -(fx * t.dx_inv + fy * t.dy_inv + fz * t.idzc[k]));
       float r = 0.f;
