@@ -205,7 +205,7 @@ __device__ __forceinline__ void stage_body(const Dims& d, const Tab& t, const Fl
                                            int kchunk, unsigned* err, int bx, int by, int bz) {
   __shared__ __align__(128) float sbuf[2][kBuf];
   __shared__ __align__(128) float sQm[R3 * TW];  // moisture species beyond qv (plain loads)
-  __shared__ float sFx[TY * (TX + 1)], sFy[(TY + 1) * TX];
+  __shared__ float sFx[2][TY * (TX + 1)], sFy[2][(TY + 1) * TX];  // theta' / qv (or one moisture species)
   __shared__ __align__(8) unsigned long long sbar[2];
   const int nx = d.nx, ny = d.ny, nz = d.nz, P = d.P;
   const size_t pl = d.plane;
@@ -407,41 +407,45 @@ __device__ __forceinline__ void stage_body(const Dims& d, const Tab& t, const Fl
     const float* sh = t.t0d + 6 * k;  // theta0(clamp(k+m)) - theta0(k), m = -3..2
     const float divh = (sU[o1 + 1] - sU[o1]) * t.dx_inv + (sV[o1 + TW] - sV[o1]) * t.dy_inv;
     // one species: Q = its box at level k; z0..z5 = its column at k-3..k+2
-    // (z3 unused: the box holds it); fc = carried flux, updated
-    auto scalar = [&](int q, const float* Q, float z0, float z1, float z2, float z4, float z5, float* fc,
+    // (z3 unused: the box holds it); fc = carried flux, updated. With WENO,
+    // the horizontal face fluxes of a species are first computed into
+    // sFx[slot] / sFy[slot] by hflux (all threads), and after one barrier
+    // scalar reads them; theta' and qv share that barrier pair.
+    auto hflux = [&](const float* Q, int slot) {
+#pragma unroll
+      for (int e = 0; e < 2; ++e) {
+        const int t_ = tid + e * NT;
+        if (t_ < TY * (TX + 1)) {
+          const int fr = t_ / (TX + 1), ff = t_ - fr * (TX + 1);
+          float F = 0.f;
+          if (i0 + ff <= nx && j0 + fr < ny) {
+            const float* qq = Q + (fr + 3) * TW + ff + XO;  // cell i0+ff, the face's right cell
+            F = weno_face_f(qq[-3], qq[-2], qq[-1], qq[0], qq[1], sU[(fr + 1) * TW + ff + XO]);
+          }
+          sFx[slot][t_] = F;
+        }
+        if (t_ < (TY + 1) * TX) {
+          const int fg = t_ / TX, fcl = t_ - fg * TX;
+          float G = 0.f;
+          if (j0 + fg <= ny && i0 + fcl < nx) {
+            const float* qq = Q + (fg + 3) * TW + fcl + XO;
+            G = weno_face_f(qq[-3 * TW], qq[-2 * TW], qq[-TW], qq[0], qq[TW], sV[(fg + 1) * TW + fcl + XO]);
+          }
+          sFy[slot][t_] = G;
+        }
+      }
+    };
+    auto scalar = [&](int q, const float* Q, int slot, float z0, float z1, float z2, float z4, float z5, float* fc,
                       float fc_shift) {
       float r = 0.f;
       const float qc = Q[o3];
       if (fl.weno_scalars) {
-#pragma unroll
-        for (int e = 0; e < 2; ++e) {
-          const int t_ = tid + e * NT;
-          if (t_ < TY * (TX + 1)) {
-            const int fr = t_ / (TX + 1), ff = t_ - fr * (TX + 1);
-            float F = 0.f;
-            if (i0 + ff <= nx && j0 + fr < ny) {
-              const float* qq = Q + (fr + 3) * TW + ff + XO;  // cell i0+ff, the face's right cell
-              F = weno_face_f(qq[-3], qq[-2], qq[-1], qq[0], qq[1], sU[(fr + 1) * TW + ff + XO]);
-            }
-            sFx[t_] = F;
-          }
-          if (t_ < (TY + 1) * TX) {
-            const int fg = t_ / TX, fcl = t_ - fg * TX;
-            float G = 0.f;
-            if (j0 + fg <= ny && i0 + fcl < nx) {
-              const float* qq = Q + (fg + 3) * TW + fcl + XO;
-              G = weno_face_f(qq[-3 * TW], qq[-2 * TW], qq[-TW], qq[0], qq[TW], sV[(fg + 1) * TW + fcl + XO]);
-            }
-            sFy[t_] = G;
-          }
-        }
-        __syncthreads();
         if (cell) {
           const float ft = weno_face_f(z1, z2, qc, z4, z5, wt);
           const float fb = (fc != nullptr && k > kb) ? *fc + wk * fc_shift : weno_face_f(z0, z1, z2, qc, z4, wk);
           if (fc != nullptr) *fc = ft;
-          const float fe = sFx[ty * (TX + 1) + tx + 1], fw = sFx[ty * (TX + 1) + tx];
-          const float fn = sFy[(ty + 1) * TX + tx], fs = sFy[ty * TX + tx];
+          const float fe = sFx[slot][ty * (TX + 1) + tx + 1], fw = sFx[slot][ty * (TX + 1) + tx];
+          const float fn = sFy[slot][(ty + 1) * TX + tx], fs = sFy[slot][ty * TX + tx];
           r = -(fe - fw) * t.dx_inv - (fn - fs) * t.dy_inv;
           float div = divh;
           if (vert) {
@@ -451,7 +455,6 @@ __device__ __forceinline__ void stage_body(const Dims& d, const Tab& t, const Fl
           if (fl.weno_advective) r += qc * div;
           else if (q == THETA) r -= t.t0c[k] * div;
         }
-        __syncthreads();  // sFx/sFy are reused by the next species
       } else if (cell) {
         const float ua = 0.5f * (sU[o1] + sU[o1 + 1]), va = 0.5f * (sV[o1] + sV[o1 + TW]);
         const float wa = 0.5f * (wk + wt);
@@ -470,19 +473,28 @@ __device__ __forceinline__ void stage_body(const Dims& d, const Tab& t, const Fl
     // is the flux of q plus w*s, so it is corrected by
     // w*(theta0(k-1) - theta0(k)) = -w*(theta0(k) - theta0(k-1)).
     const float tshift = (k > 0) ? -t.t0d[6 * (k - 1) + 4] : 0.f;
-    scalar(THETA, sT, wT[0] + sh[0], wT[1] + sh[1], wT[2] + sh[2], wT[4] + sh[4], wT[5] + sh[5], &fcT, tshift);
-    scalar(QV, sQ, wQ[0], wQ[1], wQ[2], wQ[4], wQ[5], &fcQ, 0.f);
+    if (fl.weno_scalars) {
+      hflux(sT, 0);
+      hflux(sQ, 1);
+      __syncthreads();
+    }
+    scalar(THETA, sT, 0, wT[0] + sh[0], wT[1] + sh[1], wT[2] + sh[2], wT[4] + sh[4], wT[5] + sh[5], &fcT, tshift);
+    scalar(QV, sQ, 1, wQ[0], wQ[1], wQ[2], wQ[4], wQ[5], &fcQ, 0.f);
     if (fl.moist) {
       for (int q = QC; q <= QG; ++q) {
-        __syncthreads();  // sQm is no longer read
+        __syncthreads();  // sQm and the flux slots are no longer read
         load_box3(sQm, win.f[q] + (size_t)k * pl, P, i0, j0, nx - 1, ny - 1);
         __syncthreads();
+        if (fl.weno_scalars) {
+          hflux(sQm, 0);
+          __syncthreads();
+        }
         float z[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
         if (cell) {
 #pragma unroll
           for (int m = 0; m < 6; ++m) z[m] = win.f[q][(size_t)iclamp(k + m - 3, 0, nz - 1) * pl + colc];
         }
-        scalar(q, sQm, z[0], z[1], z[2], z[4], z[5], nullptr, 0.f);
+        scalar(q, sQm, 0, z[0], z[1], z[2], z[4], z[5], nullptr, 0.f);
       }
     }
     // slide the column registers up one level
