@@ -516,7 +516,7 @@ __device__ __forceinline__ void stage_body(const Dims& d, const Tab& t, const Fl
 }
 
 template <bool kRaw>
-__global__ void __launch_bounds__(NT, 3) k_mx_stage(const __grid_constant__ Dims d, const __grid_constant__ Tab t,
+__global__ void __launch_bounds__(NT, 4) k_mx_stage(const __grid_constant__ Dims d, const __grid_constant__ Tab t,
                                                     const __grid_constant__ Flags fl,
                                                     const __grid_constant__ StageMaps M,
                                                     const __grid_constant__ WS win, const __grid_constant__ WS w0,
