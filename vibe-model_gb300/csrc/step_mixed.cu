@@ -1352,7 +1352,7 @@ __device__ __forceinline__ void hevi2_body(const Dims& d, const Tab& t, const Fl
 }
 
 template <int kRing>
-__global__ void __launch_bounds__(128, 4) k_mx_hevi_col2(const __grid_constant__ Dims d, const __grid_constant__ Tab t,
+__global__ void __launch_bounds__(128, 5) k_mx_hevi_col2(const __grid_constant__ Dims d, const __grid_constant__ Tab t,
                                                           const __grid_constant__ Flags fl,
                                                           const __grid_constant__ WS win,
                                                           const __grid_constant__ WS wout, float dtau,
@@ -1586,7 +1586,7 @@ __global__ void __launch_bounds__(640, 2) k_mx_hevi_par(const __grid_constant__ 
 }
 
 template <int kPF, int kRing>
-__global__ void __launch_bounds__(128, 6) k_mx_hevi_col(const __grid_constant__ Dims d, const __grid_constant__ Tab t,
+__global__ void __launch_bounds__(128, 8) k_mx_hevi_col(const __grid_constant__ Dims d, const __grid_constant__ Tab t,
                                                          const __grid_constant__ Flags fl,
                                                          const __grid_constant__ WS win,
                                                          const __grid_constant__ WS wout, float dtau,
