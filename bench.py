@@ -505,6 +505,7 @@ def main():
     ap.add_argument("--no-si", action="store_true", help="skip the semi-implicit (Helmholtz) leg")
     ap.add_argument("--no-nest", action="store_true", help="skip the batched nests leg")
     ap.add_argument("--no-window", action="store_true", help="skip the TL/AD assimilation-window leg")
+    ap.add_argument("--no-tune", action="store_true", help="skip the autotuner (built-in launch shapes)")
     ap.add_argument("--only", choices=["all", "mixed"], default="all",
                     help="mixed: time the mixed path only (no e2e, no FP64 leg)")
     args = ap.parse_args()
@@ -566,7 +567,8 @@ def main():
 
     # ---- mixed path (the headline) ----
     mx = make(vg.MIXED)
-    tuning = mx.autotune(DT, NSUB)  # launch shapes for this grid (same update, FP32 rounding aside)
+    # launch shapes for this grid (same update, FP32 rounding aside)
+    tuning = None if args.no_tune else mx.autotune(DT, NSUB)
     mx.step(DT, NSUB, args.warmup)  # the first step runs eagerly, the next capture the step graphs
     with ClockSampler(local) as clk:
         ms_mx, restarts = timed_steps(mx, args.steps)  # graph replay

@@ -857,6 +857,10 @@ __device__ __forceinline__ void hevi_body(const Dims& d, const Tab& t, const Fla
   }
 }
 
+// Finite test of an FP64 value on its exponent bits (integer pipe; the FP64
+// pipe, which bounds the finish kernel, is left to the arithmetic).
+__device__ __forceinline__ bool finite64(double v) { return (__double2hiint(v) & 0x7ff00000) != 0x7ff00000; }
+
 // ---- finish: fold the last stage's acoustic increments into the FP64
 // state, apply the sponge (damping.cpp:76-140) in FP64 and to the FP32
 // working copy, which becomes the next step's s0 working copy.
@@ -884,7 +888,7 @@ __device__ __forceinline__ void finish_body(const Dims& d, const Tab& t, const F
     const double v = wd * (s0.f[q][c] + (double)(incr(q) + (wv - wst.f[q][c])));
     s1.f[q][c] = v;
     w0.f[q][c] = wf * wv;
-    bad |= !isfinite(v);
+    bad |= !finite64(v);
   };
   if (j < d.ny && k < d.nz) face(U);
   if (i < d.nx && k < d.nz) face(V);
@@ -903,28 +907,28 @@ __device__ __forceinline__ void finish_body(const Dims& d, const Tab& t, const F
       const double v = wd * ((s0.f[RHO][c] + (double)(incr(RHO) + (wv - wst.f[RHO][c]))) + sdt * t.r0d[kc]);
       s1.f[RHO][c] = v;
       w0.f[RHO][c] = wf * wv;
-      bad |= !isfinite(v);
+      bad |= !finite64(v);
     }
     {
       const float wv = wfin.f[PI][c];
       const double v = wd * ((s0.f[PI][c] + (double)(incr(PI) + (wv - wst.f[PI][c]))) + sdt * t.p0d[kc]);
       s1.f[PI][c] = v;
       w0.f[PI][c] = wf * wv;
-      bad |= !isfinite(v);
+      bad |= !finite64(v);
     }
     {
       double v = s0.f[THETA][c] + (double)incr(THETA);
       if (wd != 1.0) v = wd * (v + sdt * t.t0dd[kc]);
       s1.f[THETA][c] = v;
       w0.f[THETA][c] = wf * wst.f[THETA][c];
-      bad |= !isfinite(v);
+      bad |= !finite64(v);
     }
     const int last = fl.moist ? QG : QV;
     for (int q = QV; q <= last; ++q) {
       const double v = s0.f[q][c] + (double)incr(q);
       s1.f[q][c] = v;
       w0.f[q][c] = wst.f[q][c];
-      bad |= !isfinite(v);
+      bad |= !finite64(v);
     }
   }
   if (bad) atomicOr(err, (unsigned)kErrNonFinite);
