@@ -1,10 +1,24 @@
 """Groups (vibe_gb300_group_*): several mixed models of different sizes
-advanced with one launch per kernel for all of them give the bits of the same
-models stepped one by one."""
+advanced with one launch per kernel for all of them match the same models
+stepped one by one. The work-list kernels run the single-domain kernel bodies
+compiled in another kernel, whose FMA contraction may differ: the bound is
+FP32 rounding, 1e-6 of each field's scale (velocities: the common velocity
+scale) after five steps."""
 import numpy as np
 import pytest
 
 pytestmark = pytest.mark.gpu
+TOL_GROUP = 1e-6
+
+
+def assert_rounding_close(vg, s, got, ref, tol=TOL_GROUP, what=""):
+    """got, ref: lists of 7 FieldT arrays (u v w rho theta pi qv)."""
+    ins = [vg.interior(s, q, ref[q]) for q in range(7)]
+    vs = max(float(np.abs(ins[q]).max()) for q in range(3))
+    for q in range(7):
+        scale = vs if q < 3 else float(np.abs(ins[q]).max())
+        err = float(np.abs(vg.interior(s, q, got[q]) - ins[q]).max())
+        assert err <= tol * max(scale, 1e-30) or err == 0.0, (what, vg.SPECIES[q], err, scale)
 
 
 def member(vg, nx, ny, seed):
@@ -27,9 +41,9 @@ def test_group_step_equals_individual_steps(vg, sizes):
             g.step(2.0, 6, 2)
         for m in single:
             m.step(2.0, 6, 5)
-        for a, b in zip(grouped, single):
-            for sp in range(7):
-                assert np.array_equal(a.get(sp), b.get(sp)), vg.SPECIES[sp]
+        for a, b, s in zip(grouped, single, setups):
+            assert_rounding_close(vg, s, [a.get(sp) for sp in range(7)], [b.get(sp) for sp in range(7)],
+                                  what="group vs single")
     finally:
         for m in grouped + single:
             m.close()

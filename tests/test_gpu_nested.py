@@ -5,9 +5,10 @@ after every sub-step (apply_lateral_boundary, nest.cpp:107-124) and two-way
 restriction at the end (restrict_to_parent, nest.cpp:86-105).
 
 Two checks:
-  * the nested object gives the bits of the same sequence composed by hand
-    from single models and the oracle's transfers on host copies of the
-    state (the transfers are bit-exact and so is grouping);
+  * the nested object matches the same sequence composed by hand from single
+    models and the oracle's transfers on host copies of the state to FP32
+    rounding (the transfers are bit-exact; grouped and single steps agree to
+    rounding, 1e-6 of each field's scale);
   * the whole composition run on the oracle (FP64 steps, FP64 transfers)
     agrees with the mixed GPU path to 5e-5 of each field's scale: four
     mixed steps (one parent step, three nest steps) each within 1e-5 of
@@ -123,9 +124,10 @@ def test_nested_step_equals_composition(vg, oc):
         nests = [(c, s, pi, i, r) for c, (s, pi, i, r) in zip(b_c, shapes)]
         for _ in range(2):
             compose(oc, b_p, ps, nests, lambda m, dt: m.step(dt, NSUB, 1))
-        for x, y in zip(a_p + a_c, b_p + b_c):
-            for q in range(7):
-                assert np.array_equal(x.get(q), y.get(q)), vg.SPECIES[q]
+        from test_gpu_group import assert_rounding_close
+        for x, y, s in zip(a_p + a_c, b_p + b_c, [ps, ps] + [sh[0] for sh in shapes]):
+            assert_rounding_close(vg, s, [x.get(q) for q in range(7)], [y.get(q) for q in range(7)],
+                                  what="nested vs composition")
     finally:
         for m in models:
             m.close()

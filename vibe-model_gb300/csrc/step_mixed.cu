@@ -607,8 +607,8 @@ bool tune_of(const Dims& d, MixedTune* t) {
 
 constexpr int kDefaultHeviRing = 4;  // single-domain column kernel: 0 = register ring
 constexpr int kDefaultHeviPar = 0;   // levels per thread of the level-split column kernel (0 = off)
-constexpr int kDefaultHeviTwo = 0;   // ring depth of the two-columns-per-thread kernel (0 = off)
-constexpr int kBatchRing = 4;        // work-list column kernel of groups (= the single-domain default)
+constexpr int kDefaultHeviTwo = 2;   // ring depth of the two-columns-per-thread kernel (0 = off)
+constexpr int kBatchTwoRing = 2;     // work-list column kernel of groups: the single-domain default
 
 // 4-byte asynchronous global -> shared copies (sm_80+ cp.async), grouped
 __device__ __forceinline__ void cp_async4(float* smem, const float* gmem) {
@@ -1356,7 +1356,7 @@ __device__ __forceinline__ void hevi2_body(const Dims& d, const Tab& t, const Fl
 }
 
 template <int kRing>
-__global__ void __launch_bounds__(128, 5) k_mx_hevi_col2(const __grid_constant__ Dims d, const __grid_constant__ Tab t,
+__global__ void __launch_bounds__(128, 7) k_mx_hevi_col2(const __grid_constant__ Dims d, const __grid_constant__ Tab t,
                                                           const __grid_constant__ Flags fl,
                                                           const __grid_constant__ WS win,
                                                           const __grid_constant__ WS wout, float dtau,
@@ -1815,12 +1815,13 @@ __global__ void __launch_bounds__(NT, 3) k_b_stage(const StageArgs* __restrict__
                    (l / a.gx) % a.gy, l / (a.gx * a.gy));
 }
 
-__global__ void __launch_bounds__(128, 6) k_b_hevi(const HeviArgs* __restrict__ A, const int* __restrict__ start,
+__global__ void __launch_bounds__(128, 7) k_b_hevi(const HeviArgs* __restrict__ A, const int* __restrict__ start,
                                                    int nd) {
   const int dom = find_domain(start, nd);
   const HeviArgs& a = A[dom];
   const int l = (int)blockIdx.x - start[dom];
-  hevi_body<2, kBatchRing>(a.d, a.t, a.fl, a.win, a.wout, a.dtau, a.lu, a.apply_uv, a.cdx, a.cdy, l % a.gx, l / a.gx);
+  hevi2_body<kBatchTwoRing>(a.d, a.t, a.fl, a.win, a.wout, a.dtau, a.lu, a.apply_uv, a.cdx, a.cdy, l % a.gx,
+                            l / a.gx);
 }
 
 __global__ void k_b_uv(const UvArgs* __restrict__ A, const int* __restrict__ start, int nd) {
@@ -1894,7 +1895,7 @@ MixedBatch* mixed_batch_build(const std::vector<MixedDomain>& doms, const Flags&
     if (m.d.nz != nz) return nullptr;
   auto* b = new MixedBatch();
   b->err = err;
-  b->hevi_smem = (10 * (size_t)(nz + 1) + (size_t)kBatchRing * 11 * 128) * sizeof(float);
+  b->hevi_smem = hevi2_smem_bytes(nz, kBatchTwoRing);
   const double dts[3] = {dt / 3.0, dt / 2.0, dt};
   const int nd = (int)doms.size();
   auto sub_out = [&](const MixedDomain& m, int n) { return (n & 1) ? m.WB : m.WA; };
@@ -1944,7 +1945,7 @@ MixedBatch* mixed_batch_build(const std::vector<MixedDomain>& doms, const Flags&
         a.cdy = -(float)kCp * dtau * m.t.dy_inv;
         a.lu = m.lu + (size_t)stage * 3 * nz;
         a.apply_uv = n > 0;
-        a.gx = ceil_div(m.d.nx, 32);
+        a.gx = ceil_div(m.d.nx, 64);  // two columns per thread
         a.gy = ceil_div(m.d.ny, 4);
         start[q] = hb;
         hb += a.gx * a.gy;
