@@ -227,6 +227,19 @@ typedef struct {
   int candidates;
 } vibe_gb300_tuning;
 int vibe_gb300_autotune(vibe_gb300_model *m, double dt, int n_sub, vibe_gb300_tuning *out);
+/* One step with host input and output (FieldT storage, pinned host memory
+ * for full speed), asynchronous and pipelined across calls: the call
+ * enqueues the input's host -> device copies on a copy stream, the step on
+ * the model's stream and the result's device -> host copies on a second copy
+ * stream, with two device staging buffers each way, so that step n's
+ * download and step n+2's upload overlap step n+1. host_in[q] / host_out[q]
+ * may be NULL (species not uploaded / not read); n_in, n_out <= 12. The host
+ * buffers must stay untouched until vibe_gb300_sync (which also reports
+ * errors) returns. vibe_gb300_io_join makes the model's stream wait for all
+ * copies (a CUDA event recorded on it afterwards covers the whole pipeline). */
+int vibe_gb300_step_io(vibe_gb300_model *m, const double *const *host_in, int n_in, double *const *host_out,
+                       int n_out, double dt, int n_sub);
+int vibe_gb300_io_join(vibe_gb300_model *m);
 /* Device-side copy of the prognostic state: op 0 saves the current state
  * (all species, model layout) into a snapshot held by the model, op 1 puts
  * it back (and refreshes the FP32 working copy). Asynchronous on the model's

@@ -408,3 +408,36 @@ def test_autotune_keeps_the_update(vg):
         assert t["ms_per_step"] > 0.0 and t["ms_per_step"] <= t["default_ms_per_step"] and t["candidates"] >= 5
         a.step(2.0, 4, 3)
         assert_state_close(vg, s, a.state(), before, 1e-6, range(7), "tuned vs built-in launch shapes")
+
+
+def test_step_io_pipeline_matches_synchronous_steps(vg):
+    """vibe_gb300_step_io: five pipelined calls (inputs A, B, A, C, B; the
+    staging buffers are reused every other call) give the bits of the same
+    steps done one at a time with set_state / step / get_state; a species
+    passed as NULL is neither uploaded nor read back."""
+    torch = pytest.importorskip("torch")
+    s = small_setup(vg, acoustic_mode=2, ref_kind=1)
+    with vg.Model(s, vg.MIXED) as m, vg.Model(s, vg.MIXED) as ref:
+        base = m.state()
+        rng = np.random.default_rng(4)
+        inputs = []
+        for _ in range(3):
+            st = [a.copy() for a in base[:7]]
+            th = st[4]
+            th += 0.2 * rng.standard_normal(th.size) * (th != 0.0)
+            inputs.append([torch.from_numpy(a).pin_memory() for a in st])
+        order = [0, 1, 0, 2, 1]
+        outs = [[torch.zeros(m.size(q), dtype=torch.float64).pin_memory() for q in range(7)] for _ in order]
+        for n, which in enumerate(order):
+            in_ptrs = [t.data_ptr() for t in inputs[which]]
+            out_ptrs = [t.data_ptr() for t in outs[n]]
+            out_ptrs[6] = None  # qv not read back
+            m.step_io(in_ptrs, out_ptrs, 2.0, 4)
+        m.sync()
+        for n, which in enumerate(order):
+            for q in range(7):
+                ref.set(q, inputs[which][q].numpy())
+            ref.step(2.0, 4, 1)
+            for q in range(6):
+                assert np.array_equal(outs[n][q].numpy(), ref.get(q)), (n, vg.SPECIES[q])
+            assert not outs[n][6].numpy().any()

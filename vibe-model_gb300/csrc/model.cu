@@ -125,7 +125,22 @@ struct vibe_gb300_model {
   // device copy of the prognostic state (vibe_gb300_snapshot), made on first save
   double* snap[NSPECIES] = {};
   bool has_snap = false;
+  // pipelined host I/O (vibe_gb300_step_io): copy streams, double-buffered
+  // FieldT staging on the device, events ordering the three streams
+  struct IoPipe {
+    cudaStream_t sin = nullptr, sout = nullptr;
+    double* in[2][NSPECIES] = {};
+    double* out[2][NSPECIES] = {};
+    cudaEvent_t start = nullptr, in_done[2] = {}, packed[2] = {}, unpacked[2] = {}, out_done[2] = {};
+    long n = 0;
+    bool idle = true;  // no call since the last join: the next uploads start after the model's stream
+  };
+  IoPipe* io = nullptr;
 };
+
+namespace {
+void io_release(vibe_gb300_model* m);
+}  // namespace
 
 namespace {
 
@@ -865,6 +880,7 @@ void vibe_gb300_model_destroy(vibe_gb300_model* m) {
   if (m) drop_graphs(m);
   if (!m) return;
   if (m->stream) cudaStreamSynchronize(m->stream);
+  io_release(m);
   collect_timing(m);
   for (cudaEvent_t e : m->ev_pool) cudaEventDestroy(e);
   for (void* p : m->allocs) cudaFree(p);
@@ -939,6 +955,7 @@ int vibe_gb300_step_async(vibe_gb300_model* m, double dt, int n_sub, int n_steps
 
 int vibe_gb300_sync(vibe_gb300_model* m) {
   if (!m) return fail(VIBE_GB300_EBADARG, "bad argument");
+  if (int rc = vibe_gb300_io_join(m)) return rc;
   return read_status(m);
 }
 
@@ -1828,28 +1845,154 @@ int vibe_gb300_window_stats(const vibe_gb300_window* w, double* last_ms, size_t*
   return 0;
 }
 
+}  // extern "C"
+
+namespace {
+// after new FP64 state values of the species in `given` (others untouched):
+// the FP32 working copy, and the ghost line of rho' and the inactive species
+// in every FP32 buffer
+int after_upload(vibe_gb300_model* m, const bool* given, int nspecies) {
+  if (m->precision != VIBE_GB300_MIXED) return 0;
+  if (int rc = sync_working(m)) return rc;
+  const size_t n = m->d.plane * (size_t)(m->d.nz + 1) * sizeof(float);
+  const int last = m->fl.moist ? QG : QV;
+  for (int q = 0; q < nspecies; ++q) {
+    if (!given[q] || !(q == RHO || q > last)) continue;
+    for (int b = 0; b < 2; ++b) CUDA_OK(cudaMemcpyAsync(m->WSt[b][q], m->W0[q], n, cudaMemcpyDeviceToDevice, m->stream));
+    if (acoustic_field(q)) {
+      CUDA_OK(cudaMemcpyAsync(m->WA[q], m->W0[q], n, cudaMemcpyDeviceToDevice, m->stream));
+      CUDA_OK(cudaMemcpyAsync(m->WB[q], m->W0[q], n, cudaMemcpyDeviceToDevice, m->stream));
+    }
+  }
+  return 0;
+}
+
+void pack_both(vibe_gb300_model* m, int q, const double* src) {
+  int ni, nj, nk;
+  box_of(m, q, ni, nj, nk);
+  const dim3 b(32, 4);
+  for (int t = 0; t < 2; ++t)
+    k_pack<<<dim3((ni + 31) / 32, (nj + 3) / 4, nk), b, 0, m->stream>>>(m->d, m->nsx[q], m->nsy[q], ni, nj, nk, src,
+                                                                         m->S[t][q]);
+}
+
+int io_setup(vibe_gb300_model* m) {
+  auto* io = new vibe_gb300_model::IoPipe();
+  m->io = io;
+  CUDA_OK(cudaStreamCreateWithFlags(&io->sin, cudaStreamNonBlocking));
+  CUDA_OK(cudaStreamCreateWithFlags(&io->sout, cudaStreamNonBlocking));
+  CUDA_OK(cudaEventCreateWithFlags(&io->start, cudaEventDisableTiming));
+  for (int b = 0; b < 2; ++b) {
+    for (cudaEvent_t* e : {&io->in_done[b], &io->packed[b], &io->unpacked[b], &io->out_done[b]})
+      CUDA_OK(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
+    for (int q = 0; q < NSPECIES; ++q) {
+      if (int rc = dalloc(m, &io->in[b][q], storage_count(m, q))) return rc;
+      if (int rc = dalloc(m, &io->out[b][q], storage_count(m, q))) return rc;
+    }
+  }
+  CUDA_OK(cudaStreamSynchronize(m->stream));
+  return 0;
+}
+
+void io_release(vibe_gb300_model* m) {
+  auto* io = m->io;
+  if (!io) return;
+  if (io->sin) cudaStreamSynchronize(io->sin);
+  if (io->sout) cudaStreamSynchronize(io->sout);
+  for (cudaEvent_t e : {io->start, io->in_done[0], io->in_done[1], io->packed[0], io->packed[1], io->unpacked[0],
+                        io->unpacked[1], io->out_done[0], io->out_done[1]})
+    if (e) cudaEventDestroy(e);
+  if (io->sin) cudaStreamDestroy(io->sin);
+  if (io->sout) cudaStreamDestroy(io->sout);
+  delete io;  // staging buffers are in m->allocs
+  m->io = nullptr;
+}
+}  // namespace
+
+extern "C" {
+
 int vibe_gb300_set_state(vibe_gb300_model* m, const double* const* host, int nspecies) {
   if (!m || !host || nspecies < 1 || nspecies > NSPECIES) return fail(VIBE_GB300_EBADARG, "bad argument");
+  bool given[NSPECIES] = {};
   for (int q = 0; q < nspecies; ++q) {
     if (!host[q]) continue;
+    given[q] = true;
     double* dst[2] = {m->S[0][q], m->S[1][q]};
     if (int rc = upload_storage(m, q, host[q], dst, 2)) return rc;
   }
-  if (m->precision == VIBE_GB300_MIXED) {
-    if (int rc = sync_working(m)) return rc;
-    // the ghost line of rho' and inactive species live in every FP32 buffer
-    const size_t n = m->d.plane * (size_t)(m->d.nz + 1) * sizeof(float);
-    const int last = m->fl.moist ? QG : QV;
-    for (int q = 0; q < nspecies; ++q) {
-      if (!host[q] || !(q == RHO || q > last)) continue;
-      for (int b = 0; b < 2; ++b) CUDA_OK(cudaMemcpyAsync(m->WSt[b][q], m->W0[q], n, cudaMemcpyDeviceToDevice, m->stream));
-      if (acoustic_field(q)) {
-        CUDA_OK(cudaMemcpyAsync(m->WA[q], m->W0[q], n, cudaMemcpyDeviceToDevice, m->stream));
-        CUDA_OK(cudaMemcpyAsync(m->WB[q], m->W0[q], n, cudaMemcpyDeviceToDevice, m->stream));
-      }
-    }
-  }
+  if (int rc = after_upload(m, given, nspecies)) return rc;
   CUDA_OK(cudaGetLastError());
+  return 0;
+}
+
+// One step with host input and output, pipelined across calls: the input's
+// host -> device copies run on one copy stream, the step on the model's
+// stream, the result's device -> host copies on another; with two staging
+// buffers each way, step n's download and step n+2's upload overlap step
+// n+1's compute.
+int vibe_gb300_step_io(vibe_gb300_model* m, const double* const* host_in, int n_in, double* const* host_out,
+                       int n_out, double dt, int n_sub) {
+  if (!m || n_in < 0 || n_in > NSPECIES || n_out < 0 || n_out > NSPECIES || (n_in && !host_in) ||
+      (n_out && !host_out) || !(dt > 0.0))
+    return fail(VIBE_GB300_EBADARG, "bad argument");
+  if (!m->io)
+    if (int rc = io_setup(m)) return rc;
+  auto* io = m->io;
+  const int b = (int)(io->n & 1);
+  // the first call after a join starts its uploads after whatever is on the
+  // model's stream (so an event recorded there before it brackets the
+  // pipeline); later uploads only wait until their staging buffer was packed,
+  // and so overlap the previous step
+  if (io->idle) {
+    CUDA_OK(cudaEventRecord(io->start, m->stream));
+    CUDA_OK(cudaStreamWaitEvent(io->sin, io->start, 0));
+    io->idle = false;
+  }
+  CUDA_OK(cudaStreamWaitEvent(io->sin, io->packed[b], 0));
+  bool given[NSPECIES] = {};
+  for (int q = 0; q < n_in; ++q) {
+    if (!host_in[q]) continue;
+    given[q] = true;
+    CUDA_OK(cudaMemcpyAsync(io->in[b][q], host_in[q], storage_count(m, q) * sizeof(double), cudaMemcpyHostToDevice,
+                            io->sin));
+  }
+  CUDA_OK(cudaEventRecord(io->in_done[b], io->sin));
+  CUDA_OK(cudaStreamWaitEvent(m->stream, io->in_done[b], 0));
+  for (int q = 0; q < n_in; ++q)
+    if (given[q]) pack_both(m, q, io->in[b][q]);
+  if (int rc = after_upload(m, given, n_in)) return rc;
+  CUDA_OK(cudaEventRecord(io->packed[b], m->stream));
+  if (int rc = enqueue_steps(m, dt, n_sub, 1)) return rc;
+  CUDA_OK(cudaStreamWaitEvent(m->stream, io->out_done[b], 0));  // the staging buffer was read out
+  for (int q = 0; q < n_out; ++q) {
+    if (!host_out[q]) continue;
+    int ni, nj, nk;
+    box_of(m, q, ni, nj, nk);
+    k_unpack<<<1024, 256, 0, m->stream>>>(m->d, m->nsx[q], m->nsy[q], m->nsz[q], ni, nj, nk, m->S[m->cur][q],
+                                          io->out[b][q]);
+  }
+  CUDA_OK(cudaEventRecord(io->unpacked[b], m->stream));
+  CUDA_OK(cudaStreamWaitEvent(io->sout, io->unpacked[b], 0));
+  for (int q = 0; q < n_out; ++q)
+    if (host_out[q])
+      CUDA_OK(cudaMemcpyAsync(host_out[q], io->out[b][q], storage_count(m, q) * sizeof(double),
+                              cudaMemcpyDeviceToHost, io->sout));
+  CUDA_OK(cudaEventRecord(io->out_done[b], io->sout));
+  ++io->n;
+  CUDA_OK(cudaGetLastError());
+  return 0;
+}
+
+// make the model's stream wait for every copy of the host-I/O pipeline (an
+// event recorded on the model's stream after this covers all of it)
+int vibe_gb300_io_join(vibe_gb300_model* m) {
+  if (!m) return fail(VIBE_GB300_EBADARG, "bad argument");
+  if (!m->io) return 0;
+  for (int b = 0; b < 2; ++b) {
+    CUDA_OK(cudaStreamWaitEvent(m->stream, m->io->in_done[b], 0));
+    CUDA_OK(cudaStreamWaitEvent(m->stream, m->io->out_done[b], 0));
+  }
+  m->io->idle = true;
   return 0;
 }
 

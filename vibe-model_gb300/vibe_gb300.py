@@ -86,6 +86,8 @@ _sigs = {
     "vibe_gb300_hevi_substep": (_I, [_vp, _D]),
     "vibe_gb300_sponge": (_I, [_vp, _D]),
     "vibe_gb300_snapshot": (_I, [_vp, _I]),
+    "vibe_gb300_step_io": (_I, [_vp, ctypes.POINTER(_dp), _I, ctypes.POINTER(_dp), _I, _D, _I]),
+    "vibe_gb300_io_join": (_I, [_vp]),
     "vibe_gb300_device_field": (_I, [_vp, _I, ctypes.POINTER(_dp), ctypes.POINTER(_I)]),
     "vibe_gb300_set_state": (_I, [_vp, ctypes.POINTER(_dp), _I]),
     "vibe_gb300_get_state": (_I, [_vp, ctypes.POINTER(_dp), _I]),
@@ -250,6 +252,16 @@ class Model:
         t = Tuning()
         _check(lib.vibe_gb300_autotune(self.h, dt, n_sub, ctypes.byref(t)))
         return {name: getattr(t, name) for name, _ in Tuning._fields_}
+
+    def step_io(self, in_ptrs, out_ptrs, dt, n_sub):
+        """One asynchronous, pipelined step from host input to host output
+        (lists of host addresses, None skips a species); finish with sync()."""
+        a = (_dp * len(in_ptrs))(*[ctypes.cast(p, _dp) if p else None for p in in_ptrs])
+        b = (_dp * len(out_ptrs))(*[ctypes.cast(p, _dp) if p else None for p in out_ptrs])
+        _check(lib.vibe_gb300_step_io(self.h, a, len(in_ptrs), b, len(out_ptrs), dt, n_sub))
+
+    def io_join(self):
+        _check(lib.vibe_gb300_io_join(self.h))
 
     def save_snapshot(self):
         """Device copy of the current state (asynchronous)."""
