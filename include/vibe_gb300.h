@@ -240,6 +240,14 @@ int vibe_gb300_autotune(vibe_gb300_model *m, double dt, int n_sub, vibe_gb300_tu
 int vibe_gb300_step_io(vibe_gb300_model *m, const double *const *host_in, int n_in, double *const *host_out,
                        int n_out, double dt, int n_sub);
 int vibe_gb300_io_join(vibe_gb300_model *m);
+/* Restart files of the device state in the reference's .vibebin format
+ * (io::write_restart / read_restart, src/io/field_io.cpp:207-250; layout
+ * src/io/binary_writer.cpp:1-20): the 12 species over their stagger's
+ * points plus "__restart_info__" = [time, step]; files are interchangeable
+ * with the reference's. Reading keeps the points the file does not hold
+ * (halo, ghost lines, absent species) and refreshes the FP32 working copy. */
+int vibe_gb300_write_restart(vibe_gb300_model *m, const char *path, double time, int step);
+int vibe_gb300_read_restart(vibe_gb300_model *m, const char *path, double *time, int *step);
 /* Device-side copy of the prognostic state: op 0 saves the current state
  * (all species, model layout) into a snapshot held by the model, op 1 puts
  * it back (and refreshes the FP32 working copy). Asynchronous on the model's

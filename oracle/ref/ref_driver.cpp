@@ -36,6 +36,7 @@
 #include "vibe/dyn/equations.hpp"
 #include "vibe/dyn/reference_state.hpp"
 #include "vibe/dyn/state.hpp"
+#include "vibe/io/field_io.hpp"
 #include "vibe/dyn/tendency.hpp"
 #include "vibe/grid/decomposition.hpp"
 #include "vibe/grid/geometry.hpp"
@@ -577,6 +578,33 @@ double vref_max_stable_dt(vref_model* m) {
   const Real dt_adv = (adv_cfl > Real(0)) ? Real(0.8) / adv_cfl : Real(1e9);
   const Real dt_ac = (acoustic_rate > Real(0)) ? Real(2) / acoustic_rate : Real(1e9);
   return std::min(dt_adv, dt_ac);
+}
+
+
+// io::write_restart / io::read_restart (src/io/field_io.cpp:207-250): the
+// .vibebin restart file of the model's state (header time = state time).
+int vref_write_restart(vref_model* m, const char* path, double time, int step) {
+  try {
+    m->state->time = time;
+    io::RestartInfo info;
+    info.time = time;
+    info.step = step;
+    io::write_restart(path, *m->state, info);
+  } catch (...) {
+    return 1;
+  }
+  return 0;
+}
+
+int vref_read_restart(vref_model* m, const char* path, double* time, int* step) {
+  try {
+    const io::RestartInfo info = io::read_restart(path, *m->state);
+    if (time) *time = info.time;
+    if (step) *step = info.step;
+  } catch (...) {
+    return 1;
+  }
+  return 0;
 }
 
 }  // extern "C"

@@ -12,6 +12,7 @@
 #include "vibe_oracle.h"
 
 #include <math.h>
+#include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
 
@@ -2102,4 +2103,118 @@ void vo_advect_scalar_flux(const double *q, const double *rho, const double *u, 
         dqdt[idx] = -div / rr;
       }
   }
+}
+
+
+/* ---- .vibebin restart files (io::write_restart / read_restart,
+ * src/io/field_io.cpp:175-250; byte layout src/io/binary_writer.cpp:1-20,
+ * 271-320): header "VIBEBIN1", int32 nx ny nz real_kind(0), float64 time,
+ * int32 nvars nlevels(=nz), then per variable char name[32] and its
+ * float64 values over the stagger's points (u: nx+1 in i, v: ny+1 in j,
+ * w: nz+1 in k; "__restart_info__" = [time, step]), i fastest; all
+ * little-endian, assembled byte by byte. ---- */
+static const char *const kSpeciesName[VO_NSPECIES] = {"u", "v", "w", "rho", "theta", "pi",
+                                                      "qv", "qc", "qr", "qi", "qs", "qg"};
+static void put_i32(FILE *f, int v) {
+  const unsigned u = (unsigned)v;
+  unsigned char b[4] = {(unsigned char)(u & 0xFFu), (unsigned char)((u >> 8) & 0xFFu),
+                        (unsigned char)((u >> 16) & 0xFFu), (unsigned char)((u >> 24) & 0xFFu)};
+  fwrite(b, 1, 4, f);
+}
+static void put_f64(FILE *f, double v) {
+  unsigned long long u;
+  unsigned char b[8];
+  memcpy(&u, &v, 8);
+  for (int i = 0; i < 8; ++i) b[i] = (unsigned char)((u >> (8 * i)) & 0xFFu);
+  fwrite(b, 1, 8, f);
+}
+static int get_i32(FILE *f, int *v) {
+  unsigned char b[4];
+  if (fread(b, 1, 4, f) != 4) return 0;
+  *v = (int)((unsigned)b[0] | ((unsigned)b[1] << 8) | ((unsigned)b[2] << 16) | ((unsigned)b[3] << 24));
+  return 1;
+}
+static int get_f64(FILE *f, double *v) {
+  unsigned char b[8];
+  unsigned long long u = 0;
+  if (fread(b, 1, 8, f) != 8) return 0;
+  for (int i = 0; i < 8; ++i) u |= (unsigned long long)b[i] << (8 * i);
+  memcpy(v, &u, 8);
+  return 1;
+}
+static void shape_of(int sp, int nx, int ny, int nz, int *ni, int *nj, int *nk) {
+  *ni = nx + (sp == VO_U);
+  *nj = ny + (sp == VO_V);
+  *nk = nz + (sp == VO_W);
+}
+
+int vo_write_restart(const vo_model *m, const char *path, double time, int step) {
+  FILE *f = fopen(path, "wb");
+  if (!f) return 1;
+  fwrite("VIBEBIN1", 1, 8, f);
+  put_i32(f, m->nx);
+  put_i32(f, m->ny);
+  put_i32(f, m->nz);
+  put_i32(f, 0);
+  put_f64(f, time);
+  put_i32(f, 1 + VO_NSPECIES);
+  put_i32(f, m->nz);
+  char name[32];
+  memset(name, 0, sizeof name);
+  strcpy(name, "__restart_info__");
+  fwrite(name, 1, 32, f);
+  put_f64(f, time);
+  put_f64(f, (double)step);
+  for (int sp = 0; sp < VO_NSPECIES; ++sp) {
+    memset(name, 0, sizeof name);
+    strcpy(name, kSpeciesName[sp]);
+    fwrite(name, 1, 32, f);
+    int ni, nj, nk;
+    shape_of(sp, m->nx, m->ny, m->nz, &ni, &nj, &nk);
+    for (int k = 0; k < nk; ++k)
+      for (int j = 0; j < nj; ++j)
+        for (int i = 0; i < ni; ++i) put_f64(f, AT(m->st[sp], i, j, k));
+  }
+  return fclose(f) == 0 ? 0 : 1;
+}
+
+int vo_read_restart(vo_model *m, const char *path, double *time, int *step) {
+  FILE *f = fopen(path, "rb");
+  if (!f) return 1;
+  char magic[8];
+  int nx, ny, nz, kind, nvars, nlev;
+  double t;
+  int ok = fread(magic, 1, 8, f) == 8 && memcmp(magic, "VIBEBIN1", 8) == 0 && get_i32(f, &nx) && get_i32(f, &ny) &&
+           get_i32(f, &nz) && get_i32(f, &kind) && get_f64(f, &t) && get_i32(f, &nvars) && get_i32(f, &nlev);
+  ok = ok && nx == m->nx && ny == m->ny && nz == m->nz;
+  double info[2] = {0.0, 0.0};
+  for (int v = 0; ok && v < nvars; ++v) {
+    char name[33];
+    name[32] = 0;
+    if (fread(name, 1, 32, f) != 32) { ok = 0; break; }
+    if (strcmp(name, "__restart_info__") == 0) {
+      ok = get_f64(f, &info[0]) && get_f64(f, &info[1]);
+      continue;
+    }
+    int sp = -1;
+    for (int q = 0; q < VO_NSPECIES; ++q)
+      if (strcmp(name, kSpeciesName[q]) == 0) sp = q;
+    /* the shape follows from the name (binary_writer.cpp:100-118) */
+    const int st = (strcmp(name, "u") == 0 || strcmp(name, "u_facex") == 0) ? 1
+                   : (strcmp(name, "v") == 0 || strcmp(name, "v_facey") == 0) ? 2
+                   : (strcmp(name, "w") == 0 || strcmp(name, "zeta") == 0 || strcmp(name, "w_facez") == 0) ? 3 : 0;
+    const int ni = nx + (st == 1), nj = ny + (st == 2), nk = nz + (st == 3);
+    for (int k = 0; ok && k < nk; ++k)
+      for (int j = 0; ok && j < nj; ++j)
+        for (int i = 0; ok && i < ni; ++i) {
+          double x;
+          ok = get_f64(f, &x);
+          if (ok && sp >= 0) AT(m->st[sp], i, j, k) = x;
+        }
+  }
+  fclose(f);
+  if (!ok) return 1;
+  if (time) *time = info[0];
+  if (step) *step = (int)llround(info[1]);
+  return 0;
 }

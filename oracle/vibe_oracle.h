@@ -174,6 +174,12 @@ void vo_tl_step(const vo_model *m, const double *const *xb, const double *const 
  * reference's tests/unit/test_tl_ad.cpp:100-199); theta_b from xb */
 void vo_nl_step(const vo_model *m, const double *const *xb, const double *const *x, double dt, double *const *out);
 void vo_nl_tendency(const vo_model *m, const double *const *xb, const double *const *x, double *const *d);
+/* .vibebin restart file of the state (io::write_restart / read_restart,
+ * src/io/field_io.cpp:207-250, format src/io/binary_writer.cpp:1-20);
+ * 0 on success. */
+int vo_write_restart(const vo_model *m, const char *path, double time, int step);
+int vo_read_restart(vo_model *m, const char *path, double *time, int *step);
+
 void vo_ad_step(const vo_model *m, const double *const *xb, const double *const *bar_out, double dt,
                 double *const *bar_in);
 
@@ -208,6 +214,8 @@ void vo_advect_scalar_flux(const double *q, const double *rho, const double *u,
 /* ---- reference-linked driver (oracle/ref/ref_driver.cpp) ---- */
 typedef struct vref_model vref_model;
 vref_model *vref_create(const vo_setup *s);
+int vref_write_restart(vref_model *m, const char *path, double time, int step);
+int vref_read_restart(vref_model *m, const char *path, double *time, int *step);
 void vref_destroy(vref_model *m);
 size_t vref_storage_size(const vref_model *m, int species);
 void vref_get_field(const vref_model *m, int species, double *out);

@@ -7,6 +7,8 @@ Outputs (interior points of u v w rho theta pi qv, float64):
                    schemes (RungeKutta3Integrator::step restated over the
                    reference's Equations/Advection/Damping objects)
   ref_kernels.npz  Equations::tendencies and AcousticSubstepper::step (HEVI)
+  ref_restart.vibebin  io::write_restart of the small case after one RK3
+                   step (dt 1, 2 substeps), time 12.5, step 3
 """
 import os
 import sys
@@ -51,6 +53,9 @@ def main():
     for sp in range(7):
         kern["hevi_sp%d" % sp] = oc.interior(s, sp, m.get(sp)).copy()
     np.savez_compressed(os.path.join(HERE, "ref_kernels.npz"), **kern)
+    m = oc.Model(small(oc), "ref")
+    assert m.rk3_step(1.0, 2) == 0
+    assert oc.write_restart(m, os.path.join(HERE, "ref_restart.vibebin"), 12.5, 3) == 0
     print("wrote", os.listdir(HERE))
 
 

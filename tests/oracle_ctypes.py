@@ -100,6 +100,8 @@ def _load(kind):
         "multigrid_restrict": (None, [vp, vp, vp]),
         "multigrid_prolong": (None, [vp, vp, vp]),
         "si_step": (_I, [vp, _D, _I, _I, _D, ctypes.POINTER(_I), dp, vp, vp, vp]),
+        "write_restart": (_I, [vp, ctypes.c_char_p, _D, _I]),
+        "read_restart": (_I, [vp, ctypes.c_char_p, dp, ctypes.POINTER(_I)]),
     }
     if kind == "port":
         sig["helmholtz_apply"] = (None, [vp, vp, vp, vp, vp])
@@ -450,3 +452,14 @@ def max_stable_dt(model):
     f.restype = _D
     f.argtypes = [ctypes.c_void_p]
     return f(model.h)
+
+
+# ---- .vibebin restart files (io::write_restart / read_restart) ----
+def write_restart(model, path, time=0.0, step=0):
+    return model._f["write_restart"](model.h, os.fsencode(path), time, step)
+
+
+def read_restart(model, path):
+    t, n = ctypes.c_double(), ctypes.c_int()
+    rc = model._f["read_restart"](model.h, os.fsencode(path), ctypes.byref(t), ctypes.byref(n))
+    return rc, t.value, n.value

@@ -441,3 +441,29 @@ def test_step_io_pipeline_matches_synchronous_steps(vg):
             for q in range(6):
                 assert np.array_equal(outs[n][q].numpy(), ref.get(q)), (n, vg.SPECIES[q])
             assert not outs[n][6].numpy().any()
+
+
+def test_restart_files_match_the_reference_format(vg, oc, tmp_path):
+    """Restart files of the device state are the bytes the reference's
+    io::write_restart writes for the same state (committed golden file), and
+    reading one restores the state, its time and step."""
+    import os
+    golden = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "ref_restart.vibebin")
+    import test_oracle_cpu as tc
+    s = tc.small(oc)
+    t = vg.Setup.defaults()
+    for name, _ in vg.Setup._fields_:
+        setattr(t, name, getattr(s, name))
+    with vg.Model(t, vg.FP64_EXACT) as m, vg.Model(t, vg.FP64_EXACT) as fresh:
+        m.step(1.0, 2, 1)
+        path = str(tmp_path / "gpu.vibebin")
+        m.write_restart(path, 12.5, 3)
+        assert open(path, "rb").read() == open(golden, "rb").read()
+        assert fresh.read_restart(golden) == (12.5, 3)
+        for sp in range(12):
+            assert np.array_equal(fresh.get(sp), m.get(sp)), vg.SPECIES[sp]
+    t.pgf_perturbation, t.split_fast, t.weno_advective = 1, 1, 1  # the mixed path's composition
+    with vg.Model(t, vg.MIXED) as mx:
+        mx.read_restart(golden)
+        mx.step(1.0, 2, 1)  # the FP32 working copy follows the loaded state
+        assert np.isfinite(mx.get(4)).all()

@@ -301,3 +301,34 @@ def test_tl_tendency_is_the_derivative_of_the_nonlinear_tendency(oc):
     k = int(np.argmin(errs))
     assert 0 < k < len(eps) - 1 and errs[0] > errs[k] and errs[-1] > errs[k], errs
     assert errs[k] < 1e-6, errs
+
+
+def test_restart_port_matches_golden_and_reads_back(oc, tmp_path):
+    """.vibebin restart (io::write_restart, field_io.cpp:207-227): the port
+    writes the bytes of the reference-written golden file for the same state,
+    and reading it back restores the state, time and step."""
+    golden = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "ref_restart.vibebin")
+    s = small(oc)
+    p = oc.Model(s, "port")
+    assert p.rk3_step(1.0, 2) == 0
+    path = str(tmp_path / "port.vibebin")
+    assert oc.write_restart(p, path, 12.5, 3) == 0
+    assert open(path, "rb").read() == open(golden, "rb").read()
+    q = oc.Model(s, "port")
+    assert oc.read_restart(q, golden) == (0, 12.5, 3)
+    for sp in range(12):
+        assert np.array_equal(q.get(sp), p.get(sp))
+
+
+@need_ref
+def test_restart_port_is_bit_exact_to_reference(oc, tmp_path):
+    s = small(oc, advection=5, weno_scalars=1, moist=1, qv_surface=0.01)
+    p, r = oc.Model(s, "port"), oc.Model(s, "ref")
+    assert p.rk3_step(1.0, 2) == 0 and r.rk3_step(1.0, 2) == 0
+    a, b = str(tmp_path / "a.vibebin"), str(tmp_path / "b.vibebin")
+    assert oc.write_restart(p, a, 7.0, 11) == 0 and oc.write_restart(r, b, 7.0, 11) == 0
+    assert open(a, "rb").read() == open(b, "rb").read()
+    q = oc.Model(s, "ref")
+    assert oc.read_restart(q, a) == (0, 7.0, 11)
+    for sp in range(12):
+        assert np.array_equal(q.get(sp), r.get(sp))

@@ -6,6 +6,7 @@
 // both precisions, and the C ABI declared in include/vibe_gb300.h.
 // Nothing here computes the step on the CPU: every state update is a kernel.
 #include <cmath>
+#include <cstdint>
 #include <cstdio>
 #include <cstring>
 #include <string>
@@ -1128,6 +1129,143 @@ int vibe_gb300_autotune(vibe_gb300_model* m, double dt, int n_sub, vibe_gb300_tu
   out->ms_per_step = best_ms;
   out->default_ms_per_step = default_ms;
   out->candidates = tried;
+  return 0;
+}
+
+// ---- restart files of the device state in the reference's .vibebin
+// format (io::write_restart / read_restart, src/io/field_io.cpp:207-250;
+// byte layout src/io/binary_writer.cpp:1-20 and 271-320): "VIBEBIN1",
+// int32 nx ny nz, int32 real_kind (0), float64 time, int32 nvars, int32
+// nlevels (= nz); then per variable char name[32] and float64 values over
+// the stagger's points, i fastest; "__restart_info__" holds [time, step].
+// Integers and doubles little-endian, assembled byte by byte.
+}  // extern "C"
+
+namespace {
+const char* const kVbName[NSPECIES] = {"u", "v", "w", "rho", "theta", "pi", "qv", "qc", "qr", "qi", "qs", "qg"};
+
+void vb_i32(std::vector<unsigned char>& b, int v) {
+  const uint32_t u = (uint32_t)v;
+  for (int s = 0; s < 32; s += 8) b.push_back((unsigned char)((u >> s) & 0xFFu));
+}
+void vb_f64(std::vector<unsigned char>& b, double v) {
+  uint64_t u;
+  std::memcpy(&u, &v, 8);
+  for (int s = 0; s < 64; s += 8) b.push_back((unsigned char)((u >> s) & 0xFFu));
+}
+void vb_name(std::vector<unsigned char>& b, const char* name) {
+  char n[32] = {};
+  std::strncpy(n, name, 31);
+  b.insert(b.end(), n, n + 32);
+}
+uint32_t rd_u32(const unsigned char* p) {
+  return (uint32_t)p[0] | ((uint32_t)p[1] << 8) | ((uint32_t)p[2] << 16) | ((uint32_t)p[3] << 24);
+}
+double rd_f64(const unsigned char* p) {
+  uint64_t u = 0;
+  for (int i = 0; i < 8; ++i) u |= (uint64_t)p[i] << (8 * i);
+  double v;
+  std::memcpy(&v, &u, 8);
+  return v;
+}
+// stagger implied by a variable name (binary_writer.cpp:100-118): 1 x-face, 2 y-face, 3 z-face, 0 cell
+int vb_stagger(const std::string& n) {
+  if (n == "u" || n == "u_facex") return 1;
+  if (n == "v" || n == "v_facey") return 2;
+  if (n == "w" || n == "zeta" || n == "w_facez") return 3;
+  return 0;
+}
+}  // namespace
+
+extern "C" {
+
+int vibe_gb300_write_restart(vibe_gb300_model* m, const char* path, double time, int step) {
+  if (!m || !path) return fail(VIBE_GB300_EBADARG, "bad argument");
+  const int nx = m->d.nx, ny = m->d.ny, nz = m->d.nz;
+  std::vector<unsigned char> b;
+  b.insert(b.end(), {'V', 'I', 'B', 'E', 'B', 'I', 'N', '1'});
+  vb_i32(b, nx);
+  vb_i32(b, ny);
+  vb_i32(b, nz);
+  vb_i32(b, 0);
+  vb_f64(b, time);
+  vb_i32(b, 1 + NSPECIES);
+  vb_i32(b, nz);
+  vb_name(b, "__restart_info__");
+  vb_f64(b, time);
+  vb_f64(b, (double)step);
+  std::vector<double> h;
+  for (int q = 0; q < NSPECIES; ++q) {
+    h.resize(storage_count(m, q));
+    if (int rc = vibe_gb300_get_field(m, q, h.data())) return rc;
+    vb_name(b, kVbName[q]);
+    const int ni = nx + (q == U), nj = ny + (q == V), nk = nz + (q == W);
+    for (int k = 0; k < nk; ++k)
+      for (int j = 0; j < nj; ++j)
+        for (int i = 0; i < ni; ++i) vb_f64(b, h[soff(m->nsx[q], m->nsy[q], i, j, k)]);
+  }
+  std::FILE* f = std::fopen(path, "wb");
+  if (!f) return fail(VIBE_GB300_EBADARG, std::string("cannot write ") + path);
+  const bool ok = std::fwrite(b.data(), 1, b.size(), f) == b.size();
+  if (std::fclose(f) != 0 || !ok) return fail(VIBE_GB300_EDEVICE, std::string("write failed: ") + path);
+  return 0;
+}
+
+int vibe_gb300_read_restart(vibe_gb300_model* m, const char* path, double* time, int* step) {
+  if (!m || !path) return fail(VIBE_GB300_EBADARG, "bad argument");
+  std::FILE* f = std::fopen(path, "rb");
+  if (!f) return fail(VIBE_GB300_EBADARG, std::string("cannot read ") + path);
+  std::vector<unsigned char> b;
+  unsigned char chunk[1 << 16];
+  size_t got;
+  while ((got = std::fread(chunk, 1, sizeof chunk, f)) > 0) b.insert(b.end(), chunk, chunk + got);
+  std::fclose(f);
+  if (b.size() < 40 || std::memcmp(b.data(), "VIBEBIN1", 8) != 0) return fail(VIBE_GB300_EBADARG, "not a .vibebin file");
+  const int nx = (int)rd_u32(&b[8]), ny = (int)rd_u32(&b[12]), nz = (int)rd_u32(&b[16]);
+  const int nvars = (int)rd_u32(&b[32]);
+  if (nx != m->d.nx || ny != m->d.ny || nz != m->d.nz)
+    return fail(VIBE_GB300_EBADARG, "restart grid differs from the model's");
+  // start from the current state so points the file does not hold (halo,
+  // ghost lines, species not in the file) keep their values
+  std::vector<std::vector<double>> st(NSPECIES);
+  const double* ptrs[NSPECIES] = {};
+  double rinfo[2] = {0.0, 0.0};
+  size_t at = 40;
+  for (int v = 0; v < nvars; ++v) {
+    if (at + 32 > b.size()) return fail(VIBE_GB300_EBADARG, "truncated .vibebin file");
+    char nm[33] = {};
+    std::memcpy(nm, &b[at], 32);
+    at += 32;
+    const std::string name(nm);
+    if (name == "__restart_info__") {
+      if (at + 16 > b.size()) return fail(VIBE_GB300_EBADARG, "truncated .vibebin file");
+      rinfo[0] = rd_f64(&b[at]);
+      rinfo[1] = rd_f64(&b[at + 8]);
+      at += 16;
+      continue;
+    }
+    const int sg = vb_stagger(name);
+    const int ni = nx + (sg == 1), nj = ny + (sg == 2), nk = nz + (sg == 3);
+    const size_t cnt = (size_t)ni * nj * nk;
+    if (at + 8 * cnt > b.size()) return fail(VIBE_GB300_EBADARG, "truncated .vibebin file");
+    int q = -1;
+    for (int s = 0; s < NSPECIES; ++s)
+      if (name == kVbName[s]) q = s;
+    if (q >= 0) {
+      st[q].resize(storage_count(m, q));
+      if (int rc = vibe_gb300_get_field(m, q, st[q].data())) return rc;
+      size_t e = at;
+      for (int k = 0; k < nk; ++k)
+        for (int j = 0; j < nj; ++j)
+          for (int i = 0; i < ni; ++i, e += 8) st[q][soff(m->nsx[q], m->nsy[q], i, j, k)] = rd_f64(&b[e]);
+      ptrs[q] = st[q].data();
+    }
+    at += 8 * cnt;
+  }
+  if (int rc = vibe_gb300_set_state(m, ptrs, NSPECIES)) return rc;
+  CUDA_OK(cudaStreamSynchronize(m->stream));
+  if (time) *time = rinfo[0];
+  if (step) *step = (int)std::llround(rinfo[1]);
   return 0;
 }
 

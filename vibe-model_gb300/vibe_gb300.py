@@ -88,6 +88,8 @@ _sigs = {
     "vibe_gb300_snapshot": (_I, [_vp, _I]),
     "vibe_gb300_step_io": (_I, [_vp, ctypes.POINTER(_dp), _I, ctypes.POINTER(_dp), _I, _D, _I]),
     "vibe_gb300_io_join": (_I, [_vp]),
+    "vibe_gb300_write_restart": (_I, [_vp, ctypes.c_char_p, _D, _I]),
+    "vibe_gb300_read_restart": (_I, [_vp, ctypes.c_char_p, ctypes.POINTER(_D), ctypes.POINTER(_I)]),
     "vibe_gb300_device_field": (_I, [_vp, _I, ctypes.POINTER(_dp), ctypes.POINTER(_I)]),
     "vibe_gb300_set_state": (_I, [_vp, ctypes.POINTER(_dp), _I]),
     "vibe_gb300_get_state": (_I, [_vp, ctypes.POINTER(_dp), _I]),
@@ -262,6 +264,16 @@ class Model:
 
     def io_join(self):
         _check(lib.vibe_gb300_io_join(self.h))
+
+    def write_restart(self, path, time=0.0, step=0):
+        """.vibebin restart file of the state (the reference's format)."""
+        _check(lib.vibe_gb300_write_restart(self.h, os.fsencode(path), time, step))
+
+    def read_restart(self, path):
+        """Load a .vibebin restart file; returns (time, step)."""
+        t, n = _D(), _I()
+        _check(lib.vibe_gb300_read_restart(self.h, os.fsencode(path), ctypes.byref(t), ctypes.byref(n)))
+        return t.value, n.value
 
     def save_snapshot(self):
         """Device copy of the current state (asynchronous)."""
