@@ -1806,7 +1806,7 @@ __device__ __forceinline__ int find_domain(const int* __restrict__ start, int nd
 }
 
 template <bool kRaw>
-__global__ void __launch_bounds__(NT, 3) k_b_stage(const StageArgs* __restrict__ A, const int* __restrict__ start,
+__global__ void __launch_bounds__(NT, 4) k_b_stage(const StageArgs* __restrict__ A, const int* __restrict__ start,
                                                    int nd, unsigned* err) {
   const int dom = find_domain(start, nd);
   const StageArgs& a = A[dom];
