@@ -614,8 +614,10 @@ def main():
     h2d = sum(mx.size(sp) for sp in range(7)) * 8
     # ---- accuracy: mixed vs plain FP64 after ERR_STEPS steps from the same state
     mx.restore_snapshot()
+    budget0 = mx.energy_budget()
     mx.step(DT, NSUB, ERR_STEPS)
     st_mx = [mx.get(sp) for sp in range(7)]
+    budget_mx = mx.energy_budget()
     mx.close()
 
     # ---- plain FP64 path (timed over the same ERR_STEPS steps) ----
@@ -625,6 +627,7 @@ def main():
     ms_64 = max_over_ranks(ms_64)
     k64 = ERR_STEPS
     st_64 = [f64.get(sp) for sp in range(7)]
+    budget_64 = f64.energy_budget()
     f64.close()
     accuracy = field_errors(vg, setup, st_mx, st_64)
 
@@ -664,6 +667,14 @@ def main():
                    "l2": "inputs (1.7 GB state) >> 129 MB L2; no flush", "parallelism": "replica per GPU"},
         "fp64_value": value64, "fp64_ms_per_step": ms_64 / k64, "mixed_over_fp64": value / value64,
         "mixed_vs_fp64_error": {"steps": ERR_STEPS, "fields": accuracy},
+        "conservation": {
+            "steps": ERR_STEPS, "note": "FP64 global sums on the device (dyn::energy_budget); the lateral "
+                                        "boundaries are open (clamped), so mass and energy also cross them",
+            "mass_rel_change": {"mixed": budget_mx["mass"] / budget0["mass"] - 1.0,
+                                "fp64": budget_64["mass"] / budget0["mass"] - 1.0},
+            "total_energy_rel_change": {"mixed": budget_mx["total"] / budget0["total"] - 1.0,
+                                        "fp64": budget_64["total"] / budget0["total"] - 1.0},
+            "mixed_vs_fp64_mass": budget_mx["mass"] / budget_64["mass"] - 1.0},
         "restarts": {"every_steps": RESTART, "in_timed_region": restarts,
                      "why": "superadiabatic theta noise in 50 m layers grows convectively (e-fold ~40 s) and the "
                             "state blows up after ~25-30 steps in the FP64 path as well; the timed run puts the "

@@ -240,6 +240,11 @@ int vibe_gb300_autotune(vibe_gb300_model *m, double dt, int n_sub, vibe_gb300_tu
 int vibe_gb300_step_io(vibe_gb300_model *m, const double *const *host_in, int n_in, double *const *host_out,
                        int n_out, double dt, int n_sub);
 int vibe_gb300_io_join(vibe_gb300_model *m);
+/* Global energy and mass budget of the current state in FP64 (dyn::
+ * energy_budget, src/dyn/diagnostics.cpp:255-277): out6 = {kinetic,
+ * internal, potential, latent, total, mass} in J and kg, summed on the
+ * device with compensated (Neumaier) FP64 accumulation, deterministic. */
+int vibe_gb300_energy_budget(vibe_gb300_model *m, double *out6);
 /* Restart files of the device state in the reference's .vibebin format
  * (io::write_restart / read_restart, src/io/field_io.cpp:207-250; layout
  * src/io/binary_writer.cpp:1-20): the 12 species over their stagger's

@@ -33,6 +33,7 @@
 #include "vibe/config/config.hpp"
 #include "vibe/driver/initial_conditions.hpp"
 #include "vibe/dyn/advection.hpp"
+#include "vibe/dyn/diagnostics.hpp"
 #include "vibe/dyn/equations.hpp"
 #include "vibe/dyn/reference_state.hpp"
 #include "vibe/dyn/state.hpp"
@@ -605,6 +606,18 @@ int vref_read_restart(vref_model* m, const char* path, double* time, int* step) 
     return 1;
   }
   return 0;
+}
+
+
+// dyn::energy_budget (src/dyn/diagnostics.cpp:255-277)
+void vref_energy_budget(vref_model* m, double* out6) {
+  const dyn::EnergyBudget e = dyn::energy_budget(*m->state, *m->ref);
+  out6[0] = e.kinetic;
+  out6[1] = e.internal;
+  out6[2] = e.potential;
+  out6[3] = e.latent;
+  out6[4] = e.total;
+  out6[5] = e.mass;
 }
 
 }  // extern "C"

@@ -2218,3 +2218,33 @@ int vo_read_restart(vo_model *m, const char *path, double *time, int *step) {
   if (step) *step = (int)llround(info[1]);
   return 0;
 }
+
+
+/* dyn::energy_budget (src/dyn/diagnostics.cpp:255-277), serial FP64 sums in
+ * the reference's loop order; out6 = {kinetic, internal, potential, latent,
+ * total, mass}. cell_volume = dx dy jacobian dzeta z_top (geometry.hpp:
+ * 145-147), z_center = height(k + 1/2) (geometry.hpp:135-137). */
+void vo_energy_budget(const vo_model *m, double *out6) {
+  const int nx = m->nx, ny = m->ny, nz = m->nz;
+  const double H = m->s.z_top, Lv = 2.501e6;
+  double ke = 0, ie = 0, pe = 0, le = 0, mass = 0;
+  for (int k = 0; k < nz; ++k)
+    for (int j = 0; j < ny; ++j)
+      for (int i = 0; i < nx; ++i) {
+        const double zs = m->zs[(size_t)j * nx + i];
+        const double dzeta = m->zeta[k + 1] - m->zeta[k];
+        const double dv = m->s.dx * m->s.dy * ((H - zs) / H) * dzeta * H;
+        const double rho = AT(m->st[VO_RHO], i, j, k);
+        const double uc = 0.5 * (AT(m->st[VO_U], i, j, k) + AT(m->st[VO_U], i + 1, j, k));
+        const double vc = 0.5 * (AT(m->st[VO_V], i, j, k) + AT(m->st[VO_V], i, j + 1, k));
+        const double wc = 0.5 * (AT(m->st[VO_W], i, j, k) + AT(m->st[VO_W], i, j, k + 1));
+        const double T = AT(m->st[VO_THETA], i, j, k) * AT(m->st[VO_PI], i, j, k);
+        const double z = zs + 0.5 * (m->zeta[k] + m->zeta[k + 1]) * (H - zs);
+        mass += rho * dv;
+        ke += 0.5 * rho * (uc * uc + vc * vc + wc * wc) * dv;
+        ie += rho * K_CV * T * dv;
+        pe += rho * K_GRAVITY * z * dv;
+        le += rho * Lv * dmax(AT(m->st[VO_QV], i, j, k), 0.0) * dv;
+      }
+  out6[0] = ke; out6[1] = ie; out6[2] = pe; out6[3] = le; out6[4] = ke + ie + pe + le; out6[5] = mass;
+}

@@ -178,6 +178,9 @@ void vo_nl_tendency(const vo_model *m, const double *const *xb, const double *co
  * src/io/field_io.cpp:207-250, format src/io/binary_writer.cpp:1-20);
  * 0 on success. */
 int vo_write_restart(const vo_model *m, const char *path, double time, int step);
+/* dyn::energy_budget (src/dyn/diagnostics.cpp:255-277): {kinetic, internal,
+ * potential, latent, total, mass} */
+void vo_energy_budget(const vo_model *m, double *out6);
 int vo_read_restart(vo_model *m, const char *path, double *time, int *step);
 
 void vo_ad_step(const vo_model *m, const double *const *xb, const double *const *bar_out, double dt,
@@ -215,6 +218,7 @@ void vo_advect_scalar_flux(const double *q, const double *rho, const double *u,
 typedef struct vref_model vref_model;
 vref_model *vref_create(const vo_setup *s);
 int vref_write_restart(vref_model *m, const char *path, double time, int step);
+void vref_energy_budget(vref_model *m, double *out6);
 int vref_read_restart(vref_model *m, const char *path, double *time, int *step);
 void vref_destroy(vref_model *m);
 size_t vref_storage_size(const vref_model *m, int species);

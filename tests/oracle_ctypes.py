@@ -102,6 +102,7 @@ def _load(kind):
         "si_step": (_I, [vp, _D, _I, _I, _D, ctypes.POINTER(_I), dp, vp, vp, vp]),
         "write_restart": (_I, [vp, ctypes.c_char_p, _D, _I]),
         "read_restart": (_I, [vp, ctypes.c_char_p, dp, ctypes.POINTER(_I)]),
+        "energy_budget": (None, [vp, dp]),
     }
     if kind == "port":
         sig["helmholtz_apply"] = (None, [vp, vp, vp, vp, vp])
@@ -463,3 +464,10 @@ def read_restart(model, path):
     t, n = ctypes.c_double(), ctypes.c_int()
     rc = model._f["read_restart"](model.h, os.fsencode(path), ctypes.byref(t), ctypes.byref(n))
     return rc, t.value, n.value
+
+
+def energy_budget(model):
+    """{kinetic, internal, potential, latent, total, mass} (dyn::energy_budget)."""
+    out = (ctypes.c_double * 6)()
+    model._f["energy_budget"](model.h, out)
+    return dict(zip(("kinetic", "internal", "potential", "latent", "total", "mass"), out))

@@ -467,3 +467,24 @@ def test_restart_files_match_the_reference_format(vg, oc, tmp_path):
         mx.read_restart(golden)
         mx.step(1.0, 2, 1)  # the FP32 working copy follows the loaded state
         assert np.isfinite(mx.get(4)).all()
+
+
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+def test_energy_budget_matches_oracle(vg, oc, prec):
+    """Global FP64 sums of the state (dyn::energy_budget) on the device against
+    the oracle's serial sums (pinned to the reference), with terrain and
+    moisture: 1e-12 relative per component (summation order and FMA
+    contraction aside the terms are the same)."""
+    kw = dict(terrain_kind=1, hill_h=300.0, hill_a=1500.0, hill_xc=2500.0, hill_yc=2000.0, moist=1,
+              qv_surface=0.01, ref_kind=1)
+    if prec == "mixed":
+        kw.update(acoustic_mode=2)
+    s = small_setup(vg, **kw)
+    with vg.Model(s, vg.FP64 if prec == "fp64" else vg.MIXED) as m:
+        m.step(1.0, 2, 1)
+        o = oc.Model(oracle_setup(oc, s), "port")
+        for sp in range(12):
+            o.set(sp, m.get(sp))
+        got, ref = m.energy_budget(), oc.energy_budget(o)
+        for key in ref:
+            assert abs(got[key] - ref[key]) <= 1e-12 * abs(ref[key]) + 1e-300, (key, got[key], ref[key])

@@ -332,3 +332,15 @@ def test_restart_port_is_bit_exact_to_reference(oc, tmp_path):
     assert oc.read_restart(q, a) == (0, 7.0, 11)
     for sp in range(12):
         assert np.array_equal(q.get(sp), r.get(sp))
+
+
+@need_ref
+@pytest.mark.parametrize("case", [0, 3])
+def test_energy_budget_port_is_bit_exact_to_reference(oc, case):
+    """dyn::energy_budget (diagnostics.cpp:255-277) with terrain and moisture."""
+    kw = dict(REF_CASES[case], terrain_kind=1, hill_h=300.0, hill_a=1500.0, hill_xc=2500.0, hill_yc=2000.0,
+              moist=1, qv_surface=0.01)
+    s = small(oc, **kw)
+    p, r = oc.Model(s, "port"), oc.Model(s, "ref")
+    assert p.rk3_step(1.0, 2) == 0 and r.rk3_step(1.0, 2) == 0
+    assert oc.energy_budget(p) == oc.energy_budget(r)

@@ -1269,6 +1269,133 @@ int vibe_gb300_read_restart(vibe_gb300_model* m, const char* path, double* time,
   return 0;
 }
 
+// ---- global energy and mass budget (dyn::energy_budget,
+// src/dyn/diagnostics.cpp:255-277) in FP64 on the device: per cell with
+// dv = dx dy ((H - zs)/H) dzeta(k) H and z = zs + zeta(k + 1/2) (H - zs),
+// mass += rho dv, kinetic += 0.5 rho |u_c|^2 dv (face averages), internal +=
+// rho cv theta pi dv, potential += rho g z dv, latent += rho Lv max(qv, 0) dv.
+// Each thread sums with Neumaier compensation, blocks merge their partials in
+// shared memory and one block merges the blocks in order (deterministic).
+}  // extern "C"
+
+namespace {
+constexpr int kBudgetBlocks = 304, kBudgetThreads = 256;
+struct StatePtrs {
+  const double* f[NSPECIES];
+};
+constexpr double kLatentVap = 2.501e6;  // constants.hpp:29
+
+struct Comp {
+  double s = 0.0, c = 0.0;
+  __device__ void add(double x) {
+    const double t = s + x;
+    if (fabs(s) >= fabs(x)) c += (s - t) + x;
+    else c += (x - t) + s;
+    s = t;
+  }
+  __device__ void merge(const Comp& o) {
+    add(o.s);
+    c += o.c;
+  }
+};
+
+__device__ void budget_block_merge(Comp (&v)[5], double* out) {
+  __shared__ double sh[kBudgetThreads][10];
+  for (int q = 0; q < 5; ++q) {
+    sh[threadIdx.x][2 * q] = v[q].s;
+    sh[threadIdx.x][2 * q + 1] = v[q].c;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    Comp r[5];
+    for (int t = 0; t < (int)blockDim.x; ++t)
+      for (int q = 0; q < 5; ++q) {
+        Comp o;
+        o.s = sh[t][2 * q];
+        o.c = sh[t][2 * q + 1];
+        r[q].merge(o);
+      }
+    for (int q = 0; q < 5; ++q) {
+      out[2 * q] = r[q].s;
+      out[2 * q + 1] = r[q].c;
+    }
+  }
+}
+
+__global__ void k_budget(Dims d, double dx, double dy, double ztop, const double* __restrict__ scale,
+                         const double* __restrict__ dzeta, const double* __restrict__ zc, StatePtrs s,
+                         double* __restrict__ part) {
+  Comp v[5];  // mass, kinetic, internal, potential, latent
+  const size_t ncol = (size_t)d.nx * d.ny, n = ncol * d.nz;
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x) {
+    const int k = (int)(e / ncol);
+    const size_t col = e % ncol;
+    const int j = (int)(col / d.nx), i = (int)(col % d.nx);
+    const size_t c = d.idx(i, j, k);
+    const double sc = scale[col], zs = ztop - sc;
+    const double dv = dx * dy * (sc / ztop) * dzeta[k] * ztop;
+    const double rho = s.f[RHO][c];
+    const double uc = 0.5 * (s.f[U][c] + s.f[U][c + 1]);
+    const double vc = 0.5 * (s.f[V][c] + s.f[V][c + d.P]);
+    const double wc = 0.5 * (s.f[W][c] + s.f[W][c + d.plane]);
+    const double T = s.f[THETA][c] * s.f[PI][c];
+    const double z = zs + zc[k] * sc;
+    v[0].add(rho * dv);
+    v[1].add(0.5 * rho * (uc * uc + vc * vc + wc * wc) * dv);
+    v[2].add(rho * kCv * T * dv);
+    v[3].add(rho * kG * z * dv);
+    v[4].add(rho * kLatentVap * fmax(s.f[QV][c], 0.0) * dv);
+  }
+  budget_block_merge(v, part + (size_t)blockIdx.x * 10);
+}
+
+__global__ void k_budget_final(const double* __restrict__ part, int nb, double* __restrict__ out) {
+  Comp v[5];
+  for (int b = threadIdx.x; b < nb; b += blockDim.x)
+    for (int q = 0; q < 5; ++q) {
+      Comp o;
+      o.s = part[(size_t)b * 10 + 2 * q];
+      o.c = part[(size_t)b * 10 + 2 * q + 1];
+      v[q].merge(o);
+    }
+  budget_block_merge(v, out);
+}
+}  // namespace
+
+extern "C" {
+
+int vibe_gb300_energy_budget(vibe_gb300_model* m, double* out6) {
+  if (!m || !out6) return fail(VIBE_GB300_EBADARG, "bad argument");
+  const int nz = m->d.nz;
+  // zeta at the level centres (Grid::z_center, geometry.hpp:135-137, with
+  // zeta_at's half-level branch, geometry.cpp:20-31)
+  std::vector<double> zc(nz);
+  for (int k = 0; k < nz; ++k) zc[k] = 0.5 * (m->hs.zeta[k] + m->hs.zeta[k + 1]);
+  double* buf = nullptr;
+  CUDA_OK(cudaMallocAsync((void**)&buf, ((size_t)nz + (size_t)kBudgetBlocks * 10 + 10) * sizeof(double), m->stream));
+  double* dzc = buf;
+  double* part = buf + nz;
+  double* dout = part + (size_t)kBudgetBlocks * 10;
+  CUDA_OK(cudaMemcpyAsync(dzc, zc.data(), nz * sizeof(double), cudaMemcpyHostToDevice, m->stream));
+  StatePtrs sp;
+  for (int q = 0; q < NSPECIES; ++q) sp.f[q] = m->S[m->cur][q];
+  k_budget<<<kBudgetBlocks, kBudgetThreads, 0, m->stream>>>(m->d, m->met.dx, m->met.dy, m->met.z_top, m->met.scale,
+                                                             m->met.dzeta, dzc, sp, part);
+  k_budget_final<<<1, kBudgetThreads, 0, m->stream>>>(part, kBudgetBlocks, dout);
+  double r[10];
+  CUDA_OK(cudaMemcpyAsync(r, dout, sizeof r, cudaMemcpyDeviceToHost, m->stream));
+  CUDA_OK(cudaFreeAsync(buf, m->stream));
+  CUDA_OK(cudaStreamSynchronize(m->stream));
+  const double mass = r[0] + r[1], ke = r[2] + r[3], ie = r[4] + r[5], pe = r[6] + r[7], le = r[8] + r[9];
+  out6[0] = ke;
+  out6[1] = ie;
+  out6[2] = pe;
+  out6[3] = le;
+  out6[4] = ke + ie + pe + le;
+  out6[5] = mass;
+  return 0;
+}
+
 int vibe_gb300_snapshot(vibe_gb300_model* m, int op) {
   if (!m || op < 0 || op > 1) return fail(VIBE_GB300_EBADARG, "bad argument");
   const size_t n = m->d.plane * (size_t)(m->d.nz + 1);

@@ -88,6 +88,7 @@ _sigs = {
     "vibe_gb300_snapshot": (_I, [_vp, _I]),
     "vibe_gb300_step_io": (_I, [_vp, ctypes.POINTER(_dp), _I, ctypes.POINTER(_dp), _I, _D, _I]),
     "vibe_gb300_io_join": (_I, [_vp]),
+    "vibe_gb300_energy_budget": (_I, [_vp, _dp]),
     "vibe_gb300_write_restart": (_I, [_vp, ctypes.c_char_p, _D, _I]),
     "vibe_gb300_read_restart": (_I, [_vp, ctypes.c_char_p, ctypes.POINTER(_D), ctypes.POINTER(_I)]),
     "vibe_gb300_device_field": (_I, [_vp, _I, ctypes.POINTER(_dp), ctypes.POINTER(_I)]),
@@ -264,6 +265,12 @@ class Model:
 
     def io_join(self):
         _check(lib.vibe_gb300_io_join(self.h))
+
+    def energy_budget(self):
+        """{kinetic, internal, potential, latent, total, mass} of the state (FP64)."""
+        out = (_D * 6)()
+        _check(lib.vibe_gb300_energy_budget(self.h, out))
+        return dict(zip(("kinetic", "internal", "potential", "latent", "total", "mass"), out))
 
     def write_restart(self, path, time=0.0, step=0):
         """.vibebin restart file of the state (the reference's format)."""
