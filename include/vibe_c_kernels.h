@@ -170,6 +170,43 @@ int vibe_advect_scalar_flux_f32_dev(const float *q, const float *rho,
                                     float dx, float dy, float z_top,
                                     float *dqdt, vibe_stream_t stream);
 
+/* ---- tangent-linear and adjoint of the flux advection (no reference
+ * counterpart; for the incremental 4D-Var built on this ABI) ----
+ * TL: d_dqdt = the derivative of vibe_advect_scalar_flux_f64's dqdt at
+ * (q, rho, u, v, w) applied to (dq, drho, du, dv, dw): every face flux
+ * vel*Rbar*Qbar differentiated in all three factors, and the density
+ * divisor where rho > 1e-12 (the 1e-12 floor is constant). AD: its
+ * transpose applied to bar_dqdt, ADDED to bar_q, bar_rho, bar_u, bar_v,
+ * bar_w (as the reference's adjoint kernels accumulate, tangent_linear.cpp:
+ * 426-546). Arrays as in the forward function; returns VIBE_C_OK,
+ * VIBE_C_ERR_BAD_ARG or VIBE_C_ERR_DEVICE. */
+int vibe_advect_scalar_flux_tl_f64(const double *q, const double *rho, const double *u, const double *v,
+                                   const double *w, const double *dq, const double *drho, const double *du,
+                                   const double *dv, const double *dw, const double *dzeta, const double *zs, int nx,
+                                   int ny, int nz, double dx, double dy, double z_top, double *d_dqdt);
+int vibe_advect_scalar_flux_ad_f64(const double *q, const double *rho, const double *u, const double *v,
+                                   const double *w, const double *bar_dqdt, const double *dzeta, const double *zs,
+                                   int nx, int ny, int nz, double dx, double dy, double z_top, double *bar_q,
+                                   double *bar_rho, double *bar_u, double *bar_v, double *bar_w);
+int vibe_advect_scalar_flux_tl_f64_dev(const double *q, const double *rho, const double *u, const double *v,
+                                       const double *w, const double *dq, const double *drho, const double *du,
+                                       const double *dv, const double *dw, const double *dzeta, const double *zs,
+                                       int nx, int ny, int nz, double dx, double dy, double z_top, double *d_dqdt,
+                                       vibe_stream_t stream);
+int vibe_advect_scalar_flux_ad_f64_dev(const double *q, const double *rho, const double *u, const double *v,
+                                       const double *w, const double *bar_dqdt, const double *dzeta, const double *zs,
+                                       int nx, int ny, int nz, double dx, double dy, double z_top, double *bar_q,
+                                       double *bar_rho, double *bar_u, double *bar_v, double *bar_w,
+                                       vibe_stream_t stream);
+int vibe_advect_scalar_flux_tl_f32(const float *q, const float *rho, const float *u, const float *v, const float *w,
+                                   const float *dq, const float *drho, const float *du, const float *dv,
+                                   const float *dw, const float *dzeta, const float *zs, int nx, int ny, int nz,
+                                   float dx, float dy, float z_top, float *d_dqdt);
+int vibe_advect_scalar_flux_ad_f32(const float *q, const float *rho, const float *u, const float *v, const float *w,
+                                   const float *bar_dqdt, const float *dzeta, const float *zs, int nx, int ny, int nz,
+                                   float dx, float dy, float z_top, float *bar_q, float *bar_rho, float *bar_u,
+                                   float *bar_v, float *bar_w);
+
 /* Message of the last device failure seen by this thread ("" if none). */
 const char *vibe_c_last_error(void);
 

@@ -271,3 +271,92 @@ def test_f32_weno_bilinear_cfl_neumaier_flux(vg, oc):
     ref = vg.advect_scalar_flux(*(a.astype(np.float64) for a in (q, rho, u, v, w, dzeta, zs)), nx, ny, nz, 900.0,
                                 1100.0, 15000.0)
     assert np.abs(out - ref).max() <= 1e-4 * np.abs(ref).max()
+
+
+# ---- TL / AD of the flux advection ------------------------------------------
+def _adv_case(seed, nx=23, ny=17, nz=9, dtype=np.float64):
+    rng = np.random.default_rng(seed)
+    n = nx * ny * nz
+    x = {"q": 0.5 + rng.random(n), "rho": 1.0 + 0.1 * rng.random(n), "u": rng.standard_normal(n),
+         "v": rng.standard_normal(n), "w": 0.3 * rng.standard_normal(n)}
+    d = {k: rng.standard_normal(n) * (0.1 if k == "rho" else 1.0) for k in x}
+    dzeta = rng.random(nz) * 0.1 + 0.01
+    zs = rng.random(nx * ny) * 300.0
+    cast = lambda a: np.ascontiguousarray(a, dtype=dtype)
+    return ({k: cast(a) for k, a in x.items()}, {k: cast(a) for k, a in d.items()}, cast(dzeta), cast(zs),
+            (nx, ny, nz))
+
+
+ADV = ("q", "rho", "u", "v", "w")
+GEO = (900.0, 1100.0, 15000.0)
+
+
+def _tl(vg, x, d, dzeta, zs, dims, f32=False):
+    nx, ny, nz = dims
+    out = np.zeros(nx * ny * nz, dtype=np.float32 if f32 else np.float64)
+    fn = vg.lib.vibe_advect_scalar_flux_tl_f32 if f32 else vg.lib.vibe_advect_scalar_flux_tl_f64
+    fn.restype = ctypes.c_int
+    F = ctypes.c_float if f32 else ctypes.c_double
+    fn.argtypes = [ctypes.c_void_p] * 12 + [ctypes.c_int] * 3 + [F] * 3 + [ctypes.c_void_p]
+    rc = fn(*[x[k].ctypes.data for k in ADV], *[d[k].ctypes.data for k in ADV], dzeta.ctypes.data, zs.ctypes.data,
+            nx, ny, nz, *GEO, out.ctypes.data)
+    assert rc == 0
+    return out
+
+
+def _ad(vg, x, bd, dzeta, zs, dims, acc=None, f32=False):
+    nx, ny, nz = dims
+    n = nx * ny * nz
+    dt = np.float32 if f32 else np.float64
+    outs = {k: (acc[k].copy() if acc else np.zeros(n, dtype=dt)) for k in ADV}
+    fn = vg.lib.vibe_advect_scalar_flux_ad_f32 if f32 else vg.lib.vibe_advect_scalar_flux_ad_f64
+    fn.restype = ctypes.c_int
+    F = ctypes.c_float if f32 else ctypes.c_double
+    fn.argtypes = [ctypes.c_void_p] * 8 + [ctypes.c_int] * 3 + [F] * 3 + [ctypes.c_void_p] * 5
+    rc = fn(*[x[k].ctypes.data for k in ADV], bd.ctypes.data, dzeta.ctypes.data, zs.ctypes.data, nx, ny, nz, *GEO,
+            *[outs[k].ctypes.data for k in ADV])
+    assert rc == 0
+    return outs
+
+
+def test_flux_advection_tl_matches_finite_differences(vg):
+    """Central differences of the FP64 forward kernel (which matches the
+    oracle) converge to the TL: error O(eps^2) down to rounding."""
+    x, d, dzeta, zs, dims = _adv_case(1)
+    nx, ny, nz = dims
+    fwd = lambda xx: vg.advect_scalar_flux(*[xx[k] for k in ADV], dzeta, zs, nx, ny, nz, *GEO)
+    tl = _tl(vg, x, d, dzeta, zs, dims)
+    errs = []
+    for eps in (1e-2, 1e-3, 1e-4):
+        xp = {k: x[k] + eps * d[k] for k in ADV}
+        xm = {k: x[k] - eps * d[k] for k in ADV}
+        fd = (fwd(xp) - fwd(xm)) / (2 * eps)
+        errs.append(np.abs(fd - tl).max() / np.abs(tl).max())
+    # second order (x100 per decade of eps) until rounding takes over
+    assert errs[1] <= 0.02 * errs[0] or errs[1] < 1e-9, errs
+    assert min(errs) < 1e-7, errs
+
+
+@pytest.mark.parametrize("dims", [(23, 17, 9), (1, 5, 4), (2, 1, 3)])
+def test_flux_advection_adjoint_dot_product(vg, dims):
+    """<TL dx, y> = <dx, AD y> over all five inputs (1e-12 in FP64), on
+    regular, one-column-wide and two-wide periodic grids; AD accumulates."""
+    x, d, dzeta, zs, dims = _adv_case(2, *dims)
+    rng = np.random.default_rng(3)
+    y = rng.standard_normal(x["q"].size)
+    lhs = float(np.dot(_tl(vg, x, d, dzeta, zs, dims), y))
+    bar = _ad(vg, x, y, dzeta, zs, dims)
+    rhs = float(sum(np.dot(d[k], bar[k]) for k in ADV))
+    assert abs(lhs - rhs) <= 1e-12 * max(abs(lhs), abs(rhs)), (lhs, rhs)
+    twice = _ad(vg, x, y, dzeta, zs, dims, acc=bar)
+    for k in ADV:
+        assert np.allclose(twice[k], 2 * bar[k], rtol=1e-14, atol=0)
+
+
+def test_flux_advection_adjoint_dot_product_f32(vg):
+    x, d, dzeta, zs, dims = _adv_case(4, dtype=np.float32)
+    y = np.random.default_rng(5).standard_normal(x["q"].size).astype(np.float32)
+    lhs = float(np.dot(_tl(vg, x, d, dzeta, zs, dims, f32=True).astype(np.float64), y))
+    bar = _ad(vg, x, y, dzeta, zs, dims, f32=True)
+    rhs = float(sum(np.dot(d[k].astype(np.float64), bar[k]) for k in ADV))
+    assert abs(lhs - rhs) <= 1e-5 * max(abs(lhs), abs(rhs)), (lhs, rhs)

@@ -28,6 +28,7 @@ SOURCES = [("step_fp64.cu", "step_fp64.o", []),
            ("si_step.cu", "si_step.o", ["--fmad=false"]),
            ("nest.cu", "nest.o", ["--fmad=false"]),
            ("tlad.cu", "tlad.o", []),
+           ("advect_tlad.cu", "advect_tlad.o", []),
            ("diag.cu", "diag.o", ["--fmad=false"])]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
