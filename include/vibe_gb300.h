@@ -210,6 +210,18 @@ int vibe_gb300_window_stats(const vibe_gb300_window *w, double *last_ms, size_t 
 /* Kernel-level entry points (FP64 path only for the tendency). */
 int vibe_gb300_slow_tendency(vibe_gb300_model *m, double *const *host_out);
 int vibe_gb300_acoustic_substep(vibe_gb300_model *m, double dtau);
+
+/* Tangent-linear and adjoint of the explicit forward-backward substep
+ * (RungeKutta3Integrator::acoustic_substep, runge_kutta.cpp:65-75, with
+ * Equations::acoustic_tendencies, equations.cpp:152-209, taking the pressure
+ * gradient of pi itself so that the substep is linear in the perturbation):
+ * n_sub substeps of dtau about the model's reference state, in FP64 for
+ * either precision. in / out: FieldT storage of the perturbations of u, v, w,
+ * rho and pi, in that order (out may alias in). The adjoint runs the
+ * transposed phases in reverse. Points outside each field's staggered box
+ * pass through unchanged. */
+int vibe_gb300_acoustic_tl(vibe_gb300_model *m, double dtau, int n_sub, const double *const *in, double *const *out);
+int vibe_gb300_acoustic_ad(vibe_gb300_model *m, double dtau, int n_sub, const double *const *in, double *const *out);
 int vibe_gb300_hevi_substep(vibe_gb300_model *m, double dtau);
 /* Autotuner of the mixed step: times, on this model's grid, the launch shapes
  * of the same update -- the HEVI column kernel variant (0 register ring,

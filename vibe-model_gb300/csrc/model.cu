@@ -52,12 +52,13 @@ struct Fp64Ops {
   decltype(&fp64_cons_hevi_substep) cons_hevi_substep;
   decltype(&fp64_sponge) sponge;
   decltype(&fp64_nonfinite) nonfinite;
+  decltype(&fp64_fb_substep_ad) fb_substep_ad;
 };
 static const Fp64Ops kFp64Fast = {fp64_slow_tendency, fp64_stage_update, fp64_fb_substep, fp64_ref_hevi_substep,
-                                  fp64_cons_hevi_substep, fp64_sponge, fp64_nonfinite};
+                                  fp64_cons_hevi_substep, fp64_sponge, fp64_nonfinite, fp64_fb_substep_ad};
 static const Fp64Ops kFp64Exact = {fp64_slow_tendency_exact, fp64_stage_update_exact, fp64_fb_substep_exact,
                                    fp64_ref_hevi_substep_exact, fp64_cons_hevi_substep_exact, fp64_sponge_exact,
-                                   fp64_nonfinite_exact};
+                                   fp64_nonfinite_exact, fp64_fb_substep_ad_exact};
 
 struct vibe_gb300_model {
   vibe_gb300_setup su{};
@@ -77,6 +78,7 @@ struct vibe_gb300_model {
   int cur = 0;
   double* tend[NSPECIES] = {};
   double* tmp[NSPECIES] = {};
+  double* lin[5] = {};  // u, v, w, rho, pi perturbations of the acoustic TL/AD (allocated on first use)
   double* scratch = nullptr;
   double *d_dzeta = nullptr, *d_scale = nullptr, *d_sponge = nullptr;
   double *d_th0 = nullptr, *d_pi0 = nullptr, *d_rho0 = nullptr;
@@ -1020,6 +1022,65 @@ int vibe_gb300_acoustic_substep(vibe_gb300_model* m, double dtau) {
   }
   CUDA_OK(cudaGetLastError());
   return read_status(m);
+}
+
+// FieldT storage -> device layout over the staggered box (inverse of k_pack);
+// points outside the box keep what dst holds
+__global__ void k_scatter(Dims d, int nsx, int nsy, int ni, int nj, int nk, const double* __restrict__ src,
+                          double* __restrict__ dst) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y, k = blockIdx.z;
+  if (i >= ni || j >= nj || k >= nk) return;
+  dst[soff(nsx, nsy, i, j, k)] = src[d.idx(i, j, k)];
+}
+
+namespace {
+constexpr int kLinField[5] = {U, V, W, RHO, PI};
+
+int acoustic_linear(vibe_gb300_model* m, double dtau, int n_sub, const double* const* in, double* const* out,
+                    bool adjoint) {
+  if (!m || !in || !out || n_sub < 0) return fail(VIBE_GB300_EBADARG, "bad argument");
+  for (int f = 0; f < 5; ++f)
+    if (!in[f] || !out[f]) return fail(VIBE_GB300_EBADARG, "bad argument");
+  if (!m->lin[0]) {
+    const size_t nfield = m->d.plane * (size_t)(m->d.nz + 1);
+    for (int f = 0; f < 5; ++f)
+      if (int rc = dalloc(m, &m->lin[f], nfield)) return rc;
+  }
+  double* st[NSPECIES] = {};  // the substep kernels see the perturbation as their state
+  for (int f = 0; f < 5; ++f) {
+    st[kLinField[f]] = m->lin[f];
+    if (int rc = upload_storage(m, kLinField[f], in[f], &m->lin[f], 1)) return rc;
+  }
+  Flags lf = m->fl;
+  lf.pgf_pert = 0;  // gradient of pi' itself: the substep is linear
+  for (int n = 0; n < n_sub; ++n) {
+    if (adjoint) m->f64->fb_substep_ad(m->d, m->met, st, dtau, m->stream);
+    else m->f64->fb_substep(m->d, m->met, lf, st, dtau, m->stream);
+  }
+  CUDA_OK(cudaGetLastError());
+  const dim3 b(32, 4);
+  for (int f = 0; f < 5; ++f) {
+    const int q = kLinField[f];
+    int ni, nj, nk;
+    box_of(m, q, ni, nj, nk);
+    const size_t n = storage_count(m, q);
+    CUDA_OK(cudaMemcpyAsync(m->d_stage_in, in[f], n * sizeof(double), cudaMemcpyHostToDevice, m->stream));
+    k_scatter<<<dim3((ni + 31) / 32, (nj + 3) / 4, nk), b, 0, m->stream>>>(m->d, m->nsx[q], m->nsy[q], ni, nj, nk,
+                                                                            m->lin[f], m->d_stage_in);
+    CUDA_OK(cudaGetLastError());
+    CUDA_OK(cudaMemcpyAsync(out[f], m->d_stage_in, n * sizeof(double), cudaMemcpyDeviceToHost, m->stream));
+    CUDA_OK(cudaStreamSynchronize(m->stream));
+  }
+  return 0;
+}
+}  // namespace
+
+int vibe_gb300_acoustic_tl(vibe_gb300_model* m, double dtau, int n_sub, const double* const* in, double* const* out) {
+  return acoustic_linear(m, dtau, n_sub, in, out, false);
+}
+
+int vibe_gb300_acoustic_ad(vibe_gb300_model* m, double dtau, int n_sub, const double* const* in, double* const* out) {
+  return acoustic_linear(m, dtau, n_sub, in, out, true);
 }
 
 int vibe_gb300_hevi_substep(vibe_gb300_model* m, double dtau) {

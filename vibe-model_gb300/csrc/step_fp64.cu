@@ -606,6 +606,100 @@ __global__ void k_nonfinite(Dims d, CS s, unsigned* err) {
   if (bad) atomicOr(err, (unsigned)kErrNonFinite);
 }
 
+// ---- adjoint of the explicit forward-backward substep ---------------------
+// The substep (runge_kutta.cpp:65-75 with Equations::acoustic_tendencies,
+// equations.cpp:152-209) is linear in (u, v, w, rho, pi) with coefficients
+// from the reference state when the gradient is taken of pi itself: phase 1
+// adds dtau D(u,v,w) to rho and dtau kappa D to pi (D = mass_div0, kappa =
+// (Rd/cv) pi0/max(rho0, 1e-8)); phase 2 adds dtau G(pi) to u, v, w (ac_u,
+// ac_v, ac_w). Its tangent-linear is the substep itself on the perturbation;
+// its adjoint runs the transposed phases in reverse, each as a gather:
+//   bar_pi(c) += dtau sum_faces a_f (+1 if c is the face's upper point, -1 if
+//                its lower point) bar_vel(f),   a_f = -cp theta0_f / h_f
+//   bar_vel(f) += dtau sum_cells dD(c)/dvel(f) (bar_rho(c) + kappa(c) bar_pi(c))
+__device__ inline double ac_coef_u(const Metric& m, const Dims& d, int i, int j, int k) {
+  const int ip = imin(i, d.nx - 1), im = imax(i - 1, 0);
+  return -kCp * (0.5 * (R3(m.th0, d, im, j, k) + R3(m.th0, d, ip, j, k))) / m.dx;
+}
+__device__ inline double ac_coef_v(const Metric& m, const Dims& d, int i, int j, int k) {
+  const int jp = imin(j, d.ny - 1), jm = imax(j - 1, 0);
+  return -kCp * (0.5 * (R3(m.th0, d, i, jm, k) + R3(m.th0, d, i, jp, k))) / m.dy;
+}
+__device__ inline double ac_coef_w(const Metric& m, const Dims& d, int i, int j, int k) {
+  const int kc = imin(imax(k, 0), d.nz - 1), km = imax(k - 1, 0);
+  const double dz = dmax(dzeta(m, d, kc) * scale_at(m, d, i, j), 1.0);
+  return -kCp * (0.5 * (R3(m.th0, d, i, j, km) + R3(m.th0, d, i, j, kc))) / dz;
+}
+
+// phase 2 transposed: cells
+__global__ void k_fbad_pi(Dims d, Metric m, const double* __restrict__ bu, const double* __restrict__ bv,
+                          const double* __restrict__ bw, double* __restrict__ bpi, double dtau) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y;
+  const int k = blockIdx.z;
+  if (i >= d.nx || j >= d.ny || k >= d.nz) return;
+  double acc = 0.0;
+  // x faces f with ip(f) == i: f = i, and f = nx when i = nx-1; with im(f) == i: f = i+1, and f = 0 when i = 0
+  acc += ac_coef_u(m, d, i, j, k) * bu[IDX(i, j, k)];
+  if (i == d.nx - 1) acc += ac_coef_u(m, d, d.nx, j, k) * bu[IDX(d.nx, j, k)];
+  acc -= ac_coef_u(m, d, i + 1, j, k) * bu[IDX(i + 1, j, k)];
+  if (i == 0) acc -= ac_coef_u(m, d, 0, j, k) * bu[IDX(0, j, k)];
+  acc += ac_coef_v(m, d, i, j, k) * bv[IDX(i, j, k)];
+  if (j == d.ny - 1) acc += ac_coef_v(m, d, i, d.ny, k) * bv[IDX(i, d.ny, k)];
+  acc -= ac_coef_v(m, d, i, j + 1, k) * bv[IDX(i, j + 1, k)];
+  if (j == 0) acc -= ac_coef_v(m, d, i, 0, k) * bv[IDX(i, 0, k)];
+  acc += ac_coef_w(m, d, i, j, k) * bw[IDX(i, j, k)];
+  if (k == d.nz - 1) acc += ac_coef_w(m, d, i, j, d.nz) * bw[IDX(i, j, d.nz)];
+  acc -= ac_coef_w(m, d, i, j, k + 1) * bw[IDX(i, j, k + 1)];
+  if (k == 0) acc -= ac_coef_w(m, d, i, j, 0) * bw[IDX(i, j, 0)];
+  bpi[IDX(i, j, k)] += dtau * acc;
+}
+
+// phase 1 transposed: faces
+__global__ void k_fbad_vel(Dims d, Metric m, const double* __restrict__ brho, const double* __restrict__ bpi,
+                           double* __restrict__ bu, double* __restrict__ bv, double* __restrict__ bw, double dtau) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y;
+  const int k = blockIdx.z;
+  if (i > d.nx || j > d.ny || k > d.nz) return;
+  const double* r0 = m.rho0;
+  auto Z = [&](int ci, int cj, int ck) {
+    const size_t c = IDX(ci, cj, ck);
+    return brho[c] + (kRd / kCv) * (m.pi0[c] / dmax(m.rho0[c], 1e-8)) * bpi[c];
+  };
+  if (j < d.ny && k < d.nz) {  // u face i: east face of cell i-1, west face of cell i
+    double acc = 0.0;
+    if (i >= 1) {
+      const int c = i - 1;
+      acc -= 0.5 * (R3(r0, d, c, j, k) + R3(r0, d, imin(c + 1, d.nx - 1), j, k)) / m.dx * Z(c, j, k);
+    }
+    if (i < d.nx) acc += 0.5 * (R3(r0, d, imax(i - 1, 0), j, k) + R3(r0, d, i, j, k)) / m.dx * Z(i, j, k);
+    bu[IDX(i, j, k)] += dtau * acc;
+  }
+  if (i < d.nx && k < d.nz) {  // v face j
+    double acc = 0.0;
+    if (j >= 1) {
+      const int c = j - 1;
+      acc -= 0.5 * (R3(r0, d, i, c, k) + R3(r0, d, i, imin(c + 1, d.ny - 1), k)) / m.dy * Z(i, c, k);
+    }
+    if (j < d.ny) acc += 0.5 * (R3(r0, d, i, imax(j - 1, 0), k) + R3(r0, d, i, j, k)) / m.dy * Z(i, j, k);
+    bv[IDX(i, j, k)] += dtau * acc;
+  }
+  if (i < d.nx && j < d.ny) {  // w face k: top face of cell k-1, bottom face of cell k
+    double acc = 0.0;
+    if (k >= 1) {
+      const int c = k - 1;
+      const double dz = dmax(dzeta(m, d, c) * scale_at(m, d, i, j), 1.0);
+      acc -= 0.5 * (R3(r0, d, i, j, c) + R3(r0, d, i, j, imin(c + 1, d.nz - 1))) / dz * Z(i, j, c);
+    }
+    if (k < d.nz) {
+      const double dz = dmax(dzeta(m, d, k) * scale_at(m, d, i, j), 1.0);
+      acc += 0.5 * (R3(r0, d, i, j, imax(k - 1, 0)) + R3(r0, d, i, j, k)) / dz * Z(i, j, k);
+    }
+    bw[IDX(i, j, k)] += dtau * acc;
+  }
+}
+
 }  // namespace
 
 // ---------------------------------------------------------------------------
@@ -647,6 +741,12 @@ void FP64_FN(fp64_stage_update)(const Dims& d, double* const* s0, double* const*
     const int ni = d.nx + (q == U), nj = d.ny + (q == V), nk = d.nz + (q == W);
     k_axpy_field<<<grid3(d, ni, nj, nk, kBlk), kBlk, 0, stream>>>(d, ni, nj, nk, s0[q], tend[q], a, out[q]);
   }
+}
+
+void FP64_FN(fp64_fb_substep_ad)(const Dims& d, const Metric& m, double* const* bar, double dtau, cudaStream_t stream) {
+  k_fbad_pi<<<grid3(d, d.nx, d.ny, d.nz, kBlk), kBlk, 0, stream>>>(d, m, bar[U], bar[V], bar[W], bar[PI], dtau);
+  k_fbad_vel<<<grid3(d, d.nx + 1, d.ny + 1, d.nz + 1, kBlk), kBlk, 0, stream>>>(d, m, bar[RHO], bar[PI], bar[U], bar[V],
+                                                                               bar[W], dtau);
 }
 
 void FP64_FN(fp64_fb_substep)(const Dims& d, const Metric& m, const Flags& fl, double* const* st, double dtau,

@@ -83,6 +83,8 @@ _sigs = {
     "vibe_gb300_sync": (_I, [_vp]),
     "vibe_gb300_slow_tendency": (_I, [_vp, ctypes.POINTER(_dp)]),
     "vibe_gb300_acoustic_substep": (_I, [_vp, _D]),
+    "vibe_gb300_acoustic_tl": (_I, [_vp, _D, _I, ctypes.POINTER(_dp), ctypes.POINTER(_dp)]),
+    "vibe_gb300_acoustic_ad": (_I, [_vp, _D, _I, ctypes.POINTER(_dp), ctypes.POINTER(_dp)]),
     "vibe_gb300_hevi_substep": (_I, [_vp, _D]),
     "vibe_gb300_sponge": (_I, [_vp, _D]),
     "vibe_gb300_snapshot": (_I, [_vp, _I]),
@@ -250,8 +252,32 @@ class Model:
     def hevi_substep(self, dtau):
         _check(lib.vibe_gb300_hevi_substep(self.h, dtau))
 
+    ACOUSTIC_FIELDS = (0, 1, 2, 3, 5)  # species of u, v, w, rho, pi
+
+    def _acoustic_linear(self, fn, dtau, n_sub, fields):
+        ins = [np.ascontiguousarray(fields[f], dtype=np.float64) for f in range(5)]
+        for f, a in enumerate(ins):
+            sp = self.ACOUSTIC_FIELDS[f]
+            if a.size != self.size(sp):
+                raise ValueError("%s has %d points, expected %d" % (SPECIES[sp], a.size, self.size(sp)))
+        outs = [np.empty_like(a) for a in ins]
+        pin = (_dp * 5)(*[a.ctypes.data_as(_dp) for a in ins])
+        pout = (_dp * 5)(*[o.ctypes.data_as(_dp) for o in outs])
+        _check(fn(self.h, dtau, n_sub, pin, pout))
+        return outs
+
+    def acoustic_tl(self, dtau, n_sub, fields):
+        """Tangent-linear of n_sub explicit forward-backward substeps on the
+        perturbations [u, v, w, rho, pi] (FieldT storage)."""
+        return self._acoustic_linear(lib.vibe_gb300_acoustic_tl, dtau, n_sub, fields)
+
+    def acoustic_ad(self, dtau, n_sub, fields):
+        """Adjoint of acoustic_tl: <acoustic_tl(x), y> = <x, acoustic_ad(y)>."""
+        return self._acoustic_linear(lib.vibe_gb300_acoustic_ad, dtau, n_sub, fields)
+
     def autotune(self, dt, n_sub):
-        """Pick the fastest bit-identical launch shapes for this grid (mixed path)."""
+        """Pick the fastest launch shapes for this grid (mixed path); the
+        candidates compute the same update up to FP32 rounding."""
         t = Tuning()
         _check(lib.vibe_gb300_autotune(self.h, dt, n_sub, ctypes.byref(t)))
         return {name: getattr(t, name) for name, _ in Tuning._fields_}
