@@ -225,7 +225,8 @@ int vibe_gb300_acoustic_ad(vibe_gb300_model *m, double dtau, int n_sub, const do
 int vibe_gb300_hevi_substep(vibe_gb300_model *m, double dtau);
 /* Autotuner of the mixed step: times, on this model's grid, the launch shapes
  * of the same update -- the HEVI column kernel variant (0 register ring,
- * 1 cp.async ring, 2/3 two columns per thread; -1 = the built-in choice) and
+ * 1 cp.async ring, 2/3 two columns per thread, 4 two columns per thread fed
+ * by TMA boxes; -1 = the built-in choice) and
  * the stage kernel's levels per block -- and keeps the fastest for every
  * single model of this grid in the process (groups keep the built-in column
  * kernel). Variants differ only by FP32 rounding (FMA contraction, vertical
@@ -239,6 +240,10 @@ typedef struct {
   int candidates;
 } vibe_gb300_tuning;
 int vibe_gb300_autotune(vibe_gb300_model *m, double dt, int n_sub, vibe_gb300_tuning *out);
+/* Pin a tuning (stage_levels 0 = built-in, column_kernel -1 = built-in) for
+ * this model's grid, e.g. one found by an earlier autotune run; the other
+ * fields of t are ignored. */
+int vibe_gb300_set_tuning(vibe_gb300_model *m, const vibe_gb300_tuning *t);
 /* One step with host input and output (FieldT storage, pinned host memory
  * for full speed), asynchronous and pipelined across calls: the call
  * enqueues the input's host -> device copies on a copy stream, the step on

@@ -379,18 +379,42 @@ def test_rigid_ground_and_lid(vg):
                 assert (edge == 0.0) == bool(rigid), (prec, rigid, edge)
 
 
-@pytest.mark.parametrize("dims", [(13, 7, 5), (9, 11, 3), (1, 6, 4), (2, 3, 6)])
-def test_mixed_hevi_ragged_grids(vg, oc, dims):
-    """The HEVI column kernels on odd and tiny horizontal sizes (a thread's
-    second column falls on the ghost line when nx is odd)."""
+@pytest.mark.parametrize("column", [-1, 4])
+@pytest.mark.parametrize("dims", [(13, 7, 5), (9, 11, 3), (1, 6, 4), (2, 3, 6), (67, 9, 7)])
+def test_mixed_hevi_ragged_grids(vg, oc, dims, column):
+    """The HEVI column kernels (built-in and TMA-fed) on odd and tiny
+    horizontal sizes (a thread's second column falls on the ghost line when nx
+    is odd; 67 columns leave a second block with three)."""
     nx, ny, nz = dims
     t = small_setup(vg, nx=nx, ny=ny, nz=nz, bubble_xc=nx * 125.0, bubble_yc=ny * 125.0, bubble_zc=500.0,
                     **STEP_CASES[3])
     with vg.Model(t, vg.MIXED) as m:
-        o = oc.Model(oracle_setup(oc, t), "port")
-        m.step(1.0, 3, 2)
-        assert o.rk3_step(1.0, 3) == 0 and o.rk3_step(1.0, 3) == 0
-        assert_state_close(vg, t, m.state(), o.state(), 2 * TOLMX, range(7), "mixed HEVI grid %s" % (dims,))
+        m.set_tuning(column_kernel=column)
+        try:
+            o = oc.Model(oracle_setup(oc, t), "port")
+            m.step(1.0, 3, 2)
+            assert o.rk3_step(1.0, 3) == 0 and o.rk3_step(1.0, 3) == 0
+            assert_state_close(vg, t, m.state(), o.state(), 2 * TOLMX, range(7), "mixed HEVI grid %s" % (dims,))
+        finally:
+            m.set_tuning()
+
+
+def test_column_kernel_variants_agree(vg):
+    """Every HEVI column kernel variant computes the built-in one's update to
+    FP32 rounding (1e-6 of each field's scale) over 3 steps."""
+    s = small_setup(vg, acoustic_mode=2, ref_kind=1, nx=45, ny=22, nz=24)
+    with vg.Model(s, vg.MIXED) as m:
+        m.save_snapshot()
+        m.step(2.0, 4, 3)
+        ref = m.state()
+        try:
+            for column in range(5):
+                m.restore_snapshot()
+                m.set_tuning(column_kernel=column)
+                m.step(2.0, 4, 3)
+                assert_state_close(vg, s, m.state(), ref, 1e-6, range(7), "column kernel %d" % column)
+        finally:
+            m.set_tuning()
 
 
 def test_autotune_keeps_the_update(vg):
@@ -404,10 +428,11 @@ def test_autotune_keeps_the_update(vg):
         before = a.state()
         a.restore_snapshot()
         t = a.autotune(2.0, 4)
-        assert t["column_kernel"] in (-1, 0, 1, 2, 3) and 1 <= t["stage_levels"] <= s.nz
+        assert t["column_kernel"] in (-1, 0, 1, 2, 3, 4) and 1 <= t["stage_levels"] <= s.nz
         assert t["ms_per_step"] > 0.0 and t["ms_per_step"] <= t["default_ms_per_step"] and t["candidates"] >= 5
         a.step(2.0, 4, 3)
         assert_state_close(vg, s, a.state(), before, 1e-6, range(7), "tuned vs built-in launch shapes")
+        a.set_tuning()
 
 
 def test_step_io_pipeline_matches_synchronous_steps(vg):

@@ -641,8 +641,9 @@ int enqueue_one_step(vibe_gb300_model* m, double dt, int n_sub) {
           if (m->fl.acoustic_mode == 2) {
             // the u/v update of substep n-1 is applied inside substep n's column kernel
             Span sp(m, 1);
-            mixed_hevi_column(d, m->tab, m->fl, ws_of(in), ws_of(out), dtau, m->d_lu + (size_t)stage * 3 * d.nz,
-                              n > 0, m->stream);
+            if (mixed_hevi_column(d, m->tab, m->fl, ws_of(in), ws_of(out), dtau, m->d_lu + (size_t)stage * 3 * d.nz,
+                                  n > 0, m->d_err, m->stream))
+              return fail(VIBE_GB300_EDEVICE, "TMA descriptor creation failed (cuTensorMapEncodeTiled)");
           } else {
             Span sp(m, 1);
             mixed_fb_substep(d, m->tab, m->fl, ws_of(in), ws_of(out), dtau, m->stream);
@@ -1100,7 +1101,8 @@ int vibe_gb300_hevi_substep(vibe_gb300_model* m, double dtau) {
     m->cfg_dt = -1.0;
     if (int rc = configure_dt(m, dt_equiv, 1)) return rc;
     if (int rc = sync_working(m)) return rc;
-    mixed_hevi_substep(m->d, m->tab, m->fl, ws_of(m->W0), ws_of(m->WA), (float)dtau, m->d_lu, m->d_err, m->stream);
+    if (mixed_hevi_substep(m->d, m->tab, m->fl, ws_of(m->W0), ws_of(m->WA), (float)dtau, m->d_lu, m->d_err, m->stream))
+      return fail(VIBE_GB300_EDEVICE, "TMA descriptor creation failed (cuTensorMapEncodeTiled)");
     Tab id = m->tab;
     id.spwd = m->d_spid; id.spdt = m->d_spid + (m->d.nz + 1); id.spw = m->d_spif;
     mixed_finish(m->d, id, m->fl, ws_compose(m->WA, m->W0), ws_of(m->W0), ws_of(m->WSt[1]), nullptr, 0.0,
@@ -1155,8 +1157,8 @@ int vibe_gb300_autotune(vibe_gb300_model* m, double dt, int n_sub, vibe_gb300_tu
   double best_ms = 0.0, default_ms = 0.0, ms = 0.0;
   int rc = trial(MixedTune{}, &default_ms), tried = 1;
   best_ms = default_ms;
-  // column kernel: 0 register ring, 1 cp.async ring, 2/3 two columns per thread
-  for (int c = 0; c <= 3 && !rc; ++c) {
+  // column kernel: 0 register ring, 1 cp.async ring, 2/3 two columns per thread, 4 TMA-fed two columns
+  for (int c = 0; c <= 4 && !rc; ++c) {
     cur = MixedTune{};
     cur.column = c;
     rc = trial(cur, &ms);
@@ -1190,6 +1192,17 @@ int vibe_gb300_autotune(vibe_gb300_model* m, double dt, int n_sub, vibe_gb300_tu
   out->ms_per_step = best_ms;
   out->default_ms_per_step = default_ms;
   out->candidates = tried;
+  return 0;
+}
+
+int vibe_gb300_set_tuning(vibe_gb300_model* m, const vibe_gb300_tuning* t) {
+  if (!m || !t || t->stage_levels < 0 || t->stage_levels > m->d.nz || t->column_kernel < -1 || t->column_kernel > 4)
+    return fail(VIBE_GB300_EBADARG, "bad argument");
+  MixedTune tn;
+  tn.stage_levels = t->stage_levels;
+  tn.column = t->column_kernel;
+  mixed_set_tune(m->d, tn);
+  drop_graphs(m);
   return 0;
 }
 

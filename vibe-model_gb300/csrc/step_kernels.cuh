@@ -100,10 +100,11 @@ int mixed_stage(const Dims& d, const Tab& t, const Flags& fl, const WS& win, con
                 const WS* rout, double dt_stage, unsigned* err, cudaStream_t stream);
 void mixed_fb_substep(const Dims& d, const Tab& t, const Flags& fl, const WS& win, const WS& wout, float dtau,
                       cudaStream_t stream);
-void mixed_hevi_substep(const Dims& d, const Tab& t, const Flags& fl, const WS& win, const WS& wout, float dtau,
-                        const float* lu /* 3*nz: a, cprime, inv_denom */, unsigned* err, cudaStream_t stream);
-void mixed_hevi_column(const Dims& d, const Tab& t, const Flags& fl, const WS& win, const WS& wout, float dtau,
-                       const float* lu, bool apply_uv, cudaStream_t stream);
+int mixed_hevi_substep(const Dims& d, const Tab& t, const Flags& fl, const WS& win, const WS& wout, float dtau,
+                       const float* lu /* 3*nz: a, cprime, inv_denom */, unsigned* err, cudaStream_t stream);
+// returns nonzero when a TMA descriptor cannot be made
+int mixed_hevi_column(const Dims& d, const Tab& t, const Flags& fl, const WS& win, const WS& wout, float dtau,
+                      const float* lu, bool apply_uv, unsigned* err, cudaStream_t stream);
 void mixed_uv_backward(const Dims& d, const Tab& t, const WS& win, const WS& wout, float dtau, cudaStream_t stream);
 void mixed_finish(const Dims& d, const Tab& t, const Flags& fl, const WS& wfin, const WS& wst, const WS& w0,
                   const WS* rin, double dt, double* const* s0, double* const* s1, unsigned* err,

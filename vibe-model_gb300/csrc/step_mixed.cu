@@ -122,6 +122,27 @@ struct StageMaps {
   int xmax[NTILE], ymax[NTILE];
 };
 
+// TMA-fed column kernel: a block owns 64 x 4 columns (two per thread); per
+// level one box per field, 72 floats wide from i0-4 (16-byte aligned x):
+// w, u, rho rows j0..j0+3, v rows j0..j0+4, pi' rows j0-1..j0+4
+constexpr int CW = 72, CX = 4;
+constexpr int kColBoxes = 5;  // w, pi', u, v, rho'
+constexpr int kColRows[kColBoxes] = {4, 6, 4, 5, 4};
+// box offsets in a level slot (floats, 128-byte aligned)
+constexpr int kOffW = 0, kOffP = 288, kOffU = 736, kOffV = 1024, kOffR = 1408;
+constexpr int kColSlot = 1696;                                  // floats per level slot (6784 B)
+constexpr unsigned kColLevelBytes = (4 + 6 + 4 + 5 + 4) * CW * 4;
+constexpr int kColRing = 4;
+// backward sweep: per level the parked w, rho' and pi' (one level lower) of
+// the block's own 64 x 4 columns, 64-float boxes at i0
+constexpr int kBackBoxes = 3, BW = 64;
+constexpr int kBOffW = 0, kBOffR = 256, kBOffP = 512;
+constexpr unsigned kBackLevelBytes = 3 * BW * 4 * 4;
+struct ColumnMaps {
+  CUtensorMap m[kColBoxes];
+  CUtensorMap back[kBackBoxes];  // w, rho', pi' of the output
+};
+
 // plain loader with the TMA box geometry (moisture species beyond qv)
 __device__ __forceinline__ void load_box3(float* __restrict__ dst, const float* __restrict__ plane, int P, int i0,
                                           int j0, int xmax, int ymax) {
@@ -608,6 +629,7 @@ bool tune_of(const Dims& d, MixedTune* t) {
 constexpr int kDefaultHeviRing = 4;  // single-domain column kernel: 0 = register ring
 constexpr int kDefaultHeviPar = 0;   // levels per thread of the level-split column kernel (0 = off)
 constexpr int kDefaultHeviTwo = 2;   // ring depth of the two-columns-per-thread kernel (0 = off)
+constexpr bool kDefaultHeviTma = true;  // TMA-fed two-column kernel (VIBE_GB300_HEVI_TMA=0 turns it off; candidate 4)
 constexpr int kBatchTwoRing = 2;     // work-list column kernel of groups: the single-domain default
 
 // 4-byte asynchronous global -> shared copies (sm_80+ cp.async), grouped
@@ -1051,8 +1073,9 @@ bool encode_fn() {
   return true;
 }
 
-bool box_map(const float* base, int xext, int yext, int zext, int P, size_t plane, int rows, CUtensorMap* out) {
-  const auto key = std::make_tuple((const void*)base, xext, yext, zext, P, plane, rows);
+bool box_map(const float* base, int xext, int yext, int zext, int P, size_t plane, int rows, CUtensorMap* out,
+             int width = TW) {
+  const auto key = std::make_tuple((const void*)base, xext, yext, zext, P, plane, rows * 1024 + width);
   std::lock_guard<std::mutex> lk(g_map_mu);
   auto it = g_maps.find(key);
   if (it != g_maps.end()) {
@@ -1063,7 +1086,7 @@ bool box_map(const float* base, int xext, int yext, int zext, int P, size_t plan
   CUtensorMap m;
   const cuuint64_t dims[3] = {(cuuint64_t)xext, (cuuint64_t)yext, (cuuint64_t)zext};
   const cuuint64_t strides[2] = {(cuuint64_t)P * sizeof(float), (cuuint64_t)plane * sizeof(float)};
-  const cuuint32_t box[3] = {(cuuint32_t)TW, (cuuint32_t)rows, 1};
+  const cuuint32_t box[3] = {(cuuint32_t)width, (cuuint32_t)rows, 1};
   const cuuint32_t es[3] = {1, 1, 1};
   if (g_encode(&m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, (void*)base, dims, strides, box, es,
                CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
@@ -1085,6 +1108,19 @@ bool stage_maps(const Dims& d, const WS& win, StageMaps& M) {
     M.xmax[b] = sp[b].xe - 1;
     M.ymax[b] = sp[b].ye - 1;
   }
+  return true;
+}
+
+// boxes of the TMA-fed column kernel: every field over the whole padded
+// allocation (P x (ny+1) x (nz+1)), so only the left edge and the rows outside
+// 0..ny arrive as zeros (the kernel never uses them)
+bool column_maps(const Dims& d, const WS& win, const WS& wout, ColumnMaps& C) {
+  const int q[kColBoxes] = {W, PI, U, V, RHO};
+  for (int b = 0; b < kColBoxes; ++b)
+    if (!box_map(win.f[q[b]], d.P, d.ny + 1, d.nz + 1, d.P, d.plane, kColRows[b], &C.m[b], CW)) return false;
+  const int qb[kBackBoxes] = {W, RHO, PI};
+  for (int b = 0; b < kBackBoxes; ++b)
+    if (!box_map(wout.f[qb[b]], d.P, d.ny + 1, d.nz + 1, d.P, d.plane, 4, &C.back[b], BW)) return false;
   return true;
 }
 }  // namespace
@@ -1363,6 +1399,279 @@ __global__ void __launch_bounds__(128, 7) k_mx_hevi_col2(const __grid_constant__
                                                           const float* __restrict__ lu, int apply_uv, float cdx,
                                                           float cdy) {
   hevi2_body<kRing>(d, t, fl, win, wout, dtau, lu, apply_uv, cdx, cdy, blockIdx.x, blockIdx.y);
+}
+
+// ---- the two-column HEVI update fed by TMA -------------------------------
+// Same arithmetic per column and level as hevi2_body. The forward sweep's
+// loads of a level (w and pi' of the level above, u, v, rho' and the pi'
+// neighbours of the level) are five TMA boxes per block issued by one thread
+// into a kColRing-deep ring of level slots tracked by mbarriers, instead of
+// eleven per-thread cp.async copies; threads read their points from the
+// boxes. At iteration k a thread needs the slots of levels k and k+1; after
+// the block barrier of iteration k the slot of level k-1 is free and receives
+// level k-1+kColRing. Neighbours outside the domain are never read: the
+// clamped neighbour offsets of hevi2_body select in-range box points. Waits
+// are bounded; a box that does not arrive sets kErrWaitTimeout, and the block
+// waits (bounded) for its copies in flight before it returns.
+__global__ void __launch_bounds__(128, 7) k_mx_hevi_tma(const __grid_constant__ Dims d, const __grid_constant__ Tab t,
+                                                         const __grid_constant__ Flags fl,
+                                                         const __grid_constant__ ColumnMaps C,
+                                                         const __grid_constant__ WS win,
+                                                         const __grid_constant__ WS wout, float dtau,
+                                                         const float* __restrict__ lu, int apply_uv, float cdx,
+                                                         float cdy, unsigned* err) {
+  extern __shared__ float s_dyn[];
+  __shared__ __align__(8) unsigned long long bar[kColRing], bbar[kColRing];
+  const int nz = d.nz;
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(s_dyn);
+  float* ring = s_dyn + ((((sa + 127u) & ~127u) - sa) >> 2);
+  float* s_tfz = ring + (size_t)kColRing * kColSlot;  // nz+1
+  float* s_idzw = s_tfz + (nz + 1);                   // nz+1
+  float* s_rfz = s_idzw + (nz + 1);                   // nz+1
+  float* s_idzc = s_rfz + (nz + 1);                   // nz
+  float* s_kap = s_idzc + nz;                         // nz
+  float* s_la = s_kap + nz;                           // nz
+  float* s_lc = s_la + nz;                            // nz
+  float* s_li = s_lc + nz;                            // nz
+  float* s_r0 = s_li + nz;                            // nz
+  float* s_t0 = s_r0 + nz;                            // nz
+  const int tid = threadIdx.y * blockDim.x + threadIdx.x;
+  const int i0 = blockIdx.x * 64, j0 = blockIdx.y * 4;
+  auto issue = [&](int L) {  // one thread: level L (0..nz) into its slot
+    float* s = ring + (size_t)(L % kColRing) * kColSlot;
+    unsigned long long* b = &bar[L % kColRing];
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    mbar_expect_tx(b, kColLevelBytes);
+    tma_load_3d(s + kOffW, &C.m[0], i0 - CX, j0, L, b);
+    tma_load_3d(s + kOffP, &C.m[1], i0 - CX, j0 - 1, L, b);
+    tma_load_3d(s + kOffU, &C.m[2], i0 - CX, j0, L, b);
+    tma_load_3d(s + kOffV, &C.m[3], i0 - CX, j0, L, b);
+    tma_load_3d(s + kOffR, &C.m[4], i0 - CX, j0, L, b);
+  };
+  if (tid == 0) {
+    for (int s = 0; s < kColRing; ++s) {
+      mbar_init(&bar[s], 1);
+      mbar_init(&bbar[s], 1);
+    }
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    for (int L = 0; L < kColRing && L <= nz; ++L) issue(L);
+  }
+  for (int e = tid; e <= nz; e += 128) {
+    s_tfz[e] = t.tfz[e];
+    s_idzw[e] = t.idzw[e];
+    s_rfz[e] = t.rfz[e];
+    if (e < nz) {
+      s_idzc[e] = t.idzc[e];
+      s_kap[e] = t.kap[e];
+      s_la[e] = lu[e];
+      s_lc[e] = lu[nz + e];
+      s_li[e] = lu[2 * nz + e];
+      s_r0[e] = t.r0c[e];
+      s_t0[e] = t.t0c[e];
+    }
+  }
+  __syncthreads();
+  // bounded wait for level L by every thread; on a timeout thread 0 drains
+  // the copies still in flight (levels L..hi) and the block returns
+  int hi = imin(kColRing - 1, nz);  // highest level issued
+  auto level_ready = [&](int L) -> bool {
+    const bool ok = mbar_wait_bounded(&bar[L % kColRing], (unsigned)(L / kColRing) & 1u);
+    if (__syncthreads_or(!ok)) {
+      if (tid == 0) {
+        atomicOr(err, (unsigned)kErrWaitTimeout);
+        for (int l = L; l <= hi; ++l) mbar_wait_bounded(&bar[l % kColRing], (unsigned)(l / kColRing) & 1u);
+      }
+      return false;
+    }
+    return true;
+  };
+  const int i = i0 + 2 * threadIdx.x;
+  const int j = j0 + threadIdx.y;
+  const bool active = i < d.nx && j < d.ny;
+  const bool two = i + 1 < d.nx;
+  const float b = (float)fl.hevi_beta, ob = 1.f - b;
+  const float cpf = (float)kCp;
+  const size_t col = (size_t)imin(j, d.ny - 1) * d.P + imin(i, d.nx - 1);
+  const size_t pl = d.plane;
+  float* __restrict__ Wo = wout.f[W] + col;
+  float* __restrict__ Po = wout.f[PI] + col;
+  float* __restrict__ Ro = wout.f[RHO] + col;
+  float* __restrict__ Uo = wout.f[U] + col;
+  float* __restrict__ Vo = wout.f[V] + col;
+  const size_t vn = d.P;
+  const float dxi = t.dx_inv, dyi = t.dy_inv;
+  // box-local offsets of the own points (row r, column c = CX + 2 tx)
+  const int c0 = CX + 2 * threadIdx.x, r = threadIdx.y;
+  const int oW = kOffW + r * CW + c0, oU = kOffU + r * CW + c0, oV = kOffV + r * CW + c0;
+  const int oR = kOffR + r * CW + c0, oP = kOffP + (r + 1) * CW + c0;
+  const int ou2 = two ? 2 : 1;
+  const int opw = (i > 0) ? -1 : 0;
+  const int ope = (i + 2 < d.nx) ? 2 : (two ? 1 : 0);
+  const int ops = (j > 0) ? -CW : 0, opn = (j + 1 < d.ny) ? CW : 0;
+  const bool last_j = (j == d.ny - 1);
+  auto st2 = [&](float* p, float a, float c) {
+    if (two) *reinterpret_cast<float2*>(p) = make_float2(a, c);
+    else *p = a;
+  };
+  if (!level_ready(0)) return;
+  float pk[2], wk[2], wtk[2], dpp[2] = {0.f, 0.f};
+  {
+    const float2 p0 = *reinterpret_cast<const float2*>(ring + oP);
+    const float2 w0 = *reinterpret_cast<const float2*>(ring + oW);
+    pk[0] = p0.x; pk[1] = p0.y;
+    wk[0] = w0.x; wk[1] = w0.y;
+    wtk[0] = wk[0]; wtk[1] = wk[1];  // face 0: no pressure gradient
+    if (active) st2(Wo, wk[0], wk[1]);
+  }
+  for (int k = 0; k < nz; ++k) {
+    if (!level_ready(k + 1)) return;  // also: every thread is done with level k-1's slot
+    if (tid == 0 && k >= 1 && k - 1 + kColRing <= nz) {
+      issue(k - 1 + kColRing);
+      hi = k - 1 + kColRing;
+    }
+    const float* s0 = ring + (size_t)(k % kColRing) * kColSlot;
+    const float* s1 = ring + (size_t)((k + 1) % kColRing) * kColSlot;
+    const float2 fw = *reinterpret_cast<const float2*>(s1 + oW);
+    const float2 fp = *reinterpret_cast<const float2*>(s1 + oP);
+    const float2 fu = *reinterpret_cast<const float2*>(s0 + oU);
+    const float2 fv0 = *reinterpret_cast<const float2*>(s0 + oV);
+    const float2 fv1 = *reinterpret_cast<const float2*>(s0 + oV + CW);
+    const float2 fr = *reinterpret_cast<const float2*>(s0 + oR);
+    const float fu2 = s0[oU + ou2];
+    float u0[2] = {fu.x, fu.y}, u1[2] = {fu.y, fu2};
+    float v0[2] = {fv0.x, fv0.y}, v1[2] = {fv1.x, fv1.y};
+    if (apply_uv) {
+      const float2 fs = *reinterpret_cast<const float2*>(s0 + oP + ops);
+      const float2 fn = *reinterpret_cast<const float2*>(s0 + oP + opn);
+      const float fpw = s0[oP + opw], fpe = s0[oP + ope];
+      const float tx_ = s_t0[k] * cdx, ty_ = s_t0[k] * cdy;
+      const float peA = two ? pk[1] : pk[0];
+      u0[0] += tx_ * (pk[0] - fpw);
+      u1[0] += tx_ * (peA - pk[0]);
+      u0[1] += tx_ * (pk[1] - pk[0]);
+      u1[1] += tx_ * (fpe - pk[1]);
+      v0[0] += ty_ * (pk[0] - fs.x);
+      v1[0] += ty_ * (fn.x - pk[0]);
+      v0[1] += ty_ * (pk[1] - fs.y);
+      v1[1] += ty_ * (fn.y - pk[1]);
+    }
+    const size_t o = (size_t)k * pl;
+    const float wk1[2] = {fw.x, fw.y}, pk1in[2] = {fp.x, fp.y}, r0v[2] = {fr.x, fr.y};
+    const float rk = s_rfz[k], rk1 = s_rfz[k + 1], idz = s_idzc[k];
+    float dpk[2], rsv[2], wtk1[2], pk1[2];
+#pragma unroll
+    for (int c = 0; c < 2; ++c) {
+      wtk1[c] = wk1[c];
+      pk1[c] = 0.f;
+      if (k + 1 < nz) {
+        pk1[c] = pk1in[c];
+        wtk1[c] = wk1[c] - dtau * ob * cpf * s_tfz[k + 1] * (pk1[c] - pk[c]) * s_idzw[k + 1];
+      }
+      const float Dh = -(s_r0[k] * ((u1[c] - u0[c]) * dxi + (v1[c] - v0[c]) * dyi));
+      const float dv_old = -(rk1 * wk1[c] - rk * wk[c]) * idz;
+      const float dv_t = -(rk1 * wtk1[c] - rk * wtk[c]) * idz;
+      const float S = Dh + ob * dv_old;
+      const float rhs = pk[c] + dtau * s_kap[k] * (S + b * dv_t);
+      dpk[c] = (k == 0) ? rhs * s_li[0] : (rhs - s_la[k] * dpp[c]) * s_li[k];
+      rsv[c] = r0v[c] + dtau * S;
+    }
+    if (active) {
+      st2(Uo + o, u0[0], u0[1]);
+      st2(Vo + o, v0[0], v0[1]);
+      if (two) {
+        if (i + 1 == d.nx - 1) Uo[o + 2] = u1[1];  // face nx
+      } else {
+        Uo[o + 1] = u1[0];
+      }
+      if (last_j) st2(Vo + o + vn, v1[0], v1[1]);
+      st2(Po + o, dpk[0], dpk[1]);
+      st2(Ro + o, rsv[0], rsv[1]);
+      st2(Wo + o + pl, wtk1[0], wtk1[1]);
+    }
+#pragma unroll
+    for (int c = 0; c < 2; ++c) {
+      dpp[c] = dpk[c];
+      wk[c] = wk1[c];
+      wtk[c] = wtk1[c];
+      pk[c] = pk1[c];
+    }
+  }
+  // backward sweep (as hevi2_body), the parked data of the block's columns
+  // brought back by TMA: every thread's forward stores are made visible to
+  // the async proxy before thread 0 issues the first box
+  asm volatile("fence.proxy.async.global;" ::: "memory");
+  __syncthreads();
+  auto issue_b = [&](int n) {  // backward level n: face kk = nz-1-n (w, rho') and pi'(kk-1)
+    const int kk = nz - 1 - n;
+    float* s = ring + (size_t)(n % kColRing) * kColSlot;
+    unsigned long long* bb = &bbar[n % kColRing];
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    mbar_expect_tx(bb, kBackLevelBytes);
+    tma_load_3d(s + kBOffW, &C.back[0], i0, j0, kk, bb);
+    tma_load_3d(s + kBOffR, &C.back[1], i0, j0, kk, bb);
+    tma_load_3d(s + kBOffP, &C.back[2], i0, j0, imax(kk - 1, 0), bb);
+  };
+  int bhi = imin(kColRing, nz) - 1;
+  if (tid == 0)
+    for (int n = 0; n <= bhi; ++n) issue_b(n);
+  auto back_ready = [&](int n) -> bool {
+    const bool ok = mbar_wait_bounded(&bbar[n % kColRing], (unsigned)(n / kColRing) & 1u);
+    if (__syncthreads_or(!ok)) {
+      if (tid == 0) {
+        atomicOr(err, (unsigned)kErrWaitTimeout);
+        for (int l = n; l <= bhi; ++l) mbar_wait_bounded(&bbar[l % kColRing], (unsigned)(l / kColRing) & 1u);
+      }
+      return false;
+    }
+    return true;
+  };
+  const int obk = threadIdx.y * BW + 2 * threadIdx.x;
+  float xu[2] = {dpp[0], dpp[1]};
+  float wu[2] = {0.f, 0.f};
+  if (active) {
+    wu[0] = Wo[(size_t)nz * pl];
+    if (two) wu[1] = Wo[(size_t)nz * pl + 1];
+  }
+  for (int n = 0; n < nz; ++n) {
+    if (!back_ready(n)) return;  // also: every thread is done with level n-1's slot
+    if (tid == 0 && n >= 1 && n - 1 + kColRing < nz) {
+      issue_b(n - 1 + kColRing);
+      bhi = n - 1 + kColRing;
+    }
+    const float* sb = ring + (size_t)(n % kColRing) * kColSlot;
+    const int kk = nz - 1 - n, k = kk - 1;
+    const float2 fd = *reinterpret_cast<const float2*>(sb + kBOffP + obk);
+    const float2 fw = *reinterpret_cast<const float2*>(sb + kBOffW + obk);
+    const float2 fs = *reinterpret_cast<const float2*>(sb + kBOffR + obk);
+    const float bd[2] = {fd.x, fd.y}, bw[2] = {fw.x, fw.y}, bs[2] = {fs.x, fs.y};
+    float xk[2], wkk[2], rn[2];
+#pragma unroll
+    for (int c = 0; c < 2; ++c) {
+      xk[c] = 0.f;
+      wkk[c] = bw[c];
+      if (k >= 0) {
+        xk[c] = bd[c] - s_lc[k] * xu[c];
+        wkk[c] = bw[c] - dtau * b * cpf * s_tfz[kk] * (xu[c] - xk[c]) * s_idzw[kk];
+      }
+      const float dv_new = -(s_rfz[kk + 1] * wu[c] - s_rfz[kk] * wkk[c]) * s_idzc[kk];
+      rn[c] = bs[c] + dtau * b * dv_new;
+    }
+    if (active) {
+      const size_t okk = (size_t)kk * pl;
+      st2(Ro + okk, rn[0], rn[1]);
+      st2(Po + okk, xu[0], xu[1]);
+      st2(Wo + okk, wkk[0], wkk[1]);
+    }
+#pragma unroll
+    for (int c = 0; c < 2; ++c) {
+      xu[c] = xk[c];
+      wu[c] = wkk[c];
+    }
+  }
+}
+
+size_t hevi_tma_smem_bytes(int nz) {
+  return 128 + ((size_t)kColRing * kColSlot + 10 * (size_t)(nz + 1)) * sizeof(float);
 }
 
 // ---- the same HEVI column update with the levels split over threads ------
@@ -1667,18 +1976,39 @@ int hevi_two_ring() {
   return v;
 }
 
+bool hevi_tma() {
+  static int v = -1;
+  if (v < 0) {
+    v = kDefaultHeviTma ? 1 : 0;
+    if (const char* e = std::getenv("VIBE_GB300_HEVI_TMA")) v = std::atoi(e) != 0;
+  }
+  return v != 0;
+}
+
 size_t hevi2_smem_bytes(int nz, int ring) {
   return ((((size_t)10 * (nz + 1) + 3) & ~(size_t)3) + (size_t)ring * 19 * 128) * sizeof(float);
 }
 
-void mixed_hevi_column(const Dims& d, const Tab& t, const Flags& fl, const WS& win, const WS& wout, float dtau,
-                       const float* lu, bool apply_uv, cudaStream_t stream) {
+int mixed_hevi_column(const Dims& d, const Tab& t, const Flags& fl, const WS& win, const WS& wout, float dtau,
+                      const float* lu, bool apply_uv, unsigned* err, cudaStream_t stream) {
   MixedTune tn;
   const bool tuned = tune_of(d, &tn) && tn.column >= 0;
   int r2 = hevi_two_ring(), ring = hevi_ring();
-  if (tuned) {  // 0: register ring, 1: cp.async ring 4, 2/3: two columns per thread with ring 2/3
+  bool tma = hevi_tma();
+  if (tuned) {  // 0: register ring, 1: cp.async ring 4, 2/3: two columns per thread with ring 2/3, 4: TMA-fed
     r2 = (tn.column == 2) ? 2 : (tn.column == 3 ? 3 : 0);
     ring = (tn.column == 1) ? 4 : 0;
+    tma = tn.column == 4;
+  }
+  if (tma && hevi_tma_smem_bytes(d.nz) <= 48 * 1024) {
+    ColumnMaps C;
+    if (!column_maps(d, win, wout, C)) return -1;
+    const dim3 bc(32, 4);
+    const dim3 g((d.nx + 63) / 64, (d.ny + 3) / 4);
+    const float cdx = -(float)kCp * dtau * t.dx_inv, cdy = -(float)kCp * dtau * t.dy_inv;
+    k_mx_hevi_tma<<<g, bc, hevi_tma_smem_bytes(d.nz), stream>>>(d, t, fl, C, win, wout, dtau, lu, apply_uv ? 1 : 0,
+                                                                  cdx, cdy, err);
+    return 0;
   }
   if (r2) {
     const dim3 bc(32, 4);
@@ -1689,7 +2019,7 @@ void mixed_hevi_column(const Dims& d, const Tab& t, const Flags& fl, const WS& w
     if (r2 == 4) k_mx_hevi_col2<4><<<g, bc, sm, stream>>>(d, t, fl, win, wout, dtau, lu, au, cdx, cdy);
     else if (r2 == 3) k_mx_hevi_col2<3><<<g, bc, sm, stream>>>(d, t, fl, win, wout, dtau, lu, au, cdx, cdy);
     else k_mx_hevi_col2<2><<<g, bc, sm, stream>>>(d, t, fl, win, wout, dtau, lu, au, cdx, cdy);
-    return;
+    return 0;
   }
   if (const int m = tuned ? 0 : hevi_par_levels(d.nz)) {
     const dim3 bp(32, (d.nz + m - 1) / m);
@@ -1700,7 +2030,7 @@ void mixed_hevi_column(const Dims& d, const Tab& t, const Flags& fl, const WS& w
       k_mx_hevi_par<4><<<gp, bp, sm, stream>>>(d, t, fl, win, wout, dtau, lu, apply_uv ? 1 : 0, cdx, cdy);
     else
       k_mx_hevi_par<8><<<gp, bp, sm, stream>>>(d, t, fl, win, wout, dtau, lu, apply_uv ? 1 : 0, cdx, cdy);
-    return;
+    return 0;
   }
   const dim3 bc(32, 4);
   const size_t smem = hevi_smem_bytes(d.nz, ring);
@@ -1721,6 +2051,7 @@ void mixed_hevi_column(const Dims& d, const Tab& t, const Flags& fl, const WS& w
       default: k_mx_hevi_col<2, 0><<<g, bc, smem, stream>>>(d, t, fl, win, wout, dtau, lu, au, cdx, cdy); break;
     }
   }
+  return 0;
 }
 
 void mixed_uv_backward(const Dims& d, const Tab& t, const WS& win, const WS& wout, float dtau, cudaStream_t stream) {
@@ -1728,11 +2059,11 @@ void mixed_uv_backward(const Dims& d, const Tab& t, const WS& win, const WS& wou
   k_mx_fb_mom<<<g3(d.nx + 1, d.ny + 1, d.nz, b), b, 0, stream>>>(d, t, win, wout, dtau, 0);
 }
 
-void mixed_hevi_substep(const Dims& d, const Tab& t, const Flags& fl, const WS& win, const WS& wout, float dtau,
-                        const float* lu, unsigned* err, cudaStream_t stream) {
-  (void)err;
-  mixed_hevi_column(d, t, fl, win, wout, dtau, lu, false, stream);
+int mixed_hevi_substep(const Dims& d, const Tab& t, const Flags& fl, const WS& win, const WS& wout, float dtau,
+                       const float* lu, unsigned* err, cudaStream_t stream) {
+  if (mixed_hevi_column(d, t, fl, win, wout, dtau, lu, false, err, stream)) return -1;
   mixed_uv_backward(d, t, wout, wout, dtau, stream);  // in place: u, v were copied by the column kernel
+  return 0;
 }
 
 void mixed_finish(const Dims& d, const Tab& t, const Flags& fl, const WS& wfin, const WS& wst, const WS& w0,

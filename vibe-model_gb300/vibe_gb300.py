@@ -161,6 +161,8 @@ class Tuning(ctypes.Structure):
 
 lib.vibe_gb300_autotune.restype = _I
 lib.vibe_gb300_autotune.argtypes = [_vp, _D, _I, ctypes.POINTER(Tuning)]
+lib.vibe_gb300_set_tuning.restype = _I
+lib.vibe_gb300_set_tuning.argtypes = [_vp, ctypes.POINTER(Tuning)]
 
 
 class Model:
@@ -281,6 +283,11 @@ class Model:
         t = Tuning()
         _check(lib.vibe_gb300_autotune(self.h, dt, n_sub, ctypes.byref(t)))
         return {name: getattr(t, name) for name, _ in Tuning._fields_}
+
+    def set_tuning(self, stage_levels=0, column_kernel=-1):
+        """Pin launch shapes for this grid (0 / -1: the built-in choice)."""
+        t = Tuning(stage_levels=stage_levels, column_kernel=column_kernel)
+        _check(lib.vibe_gb300_set_tuning(self.h, ctypes.byref(t)))
 
     def step_io(self, in_ptrs, out_ptrs, dt, n_sub):
         """One asynchronous, pipelined step from host input to host output
