@@ -883,6 +883,30 @@ __device__ __forceinline__ void hevi_body(const Dims& d, const Tab& t, const Fla
 // pipe, which bounds the finish kernel, is left to the arithmetic).
 __device__ __forceinline__ bool finite64(double v) { return (__double2hiint(v) & 0x7ff00000) != 0x7ff00000; }
 
+// Exact FP32 -> FP64 widening on the integer pipe (IEEE 754 binary32 ->
+// binary64: rebias the exponent by 1023 - 127 = 896 and move the 23 fraction
+// bits to the top of the 52; a subnormal m * 2^-149 with leading bit p becomes
+// the normal 2^(p-149) (1 + frac), exponent field p + 874; zeros keep their
+// sign; inf and NaN keep exponent 0x7ff and their fraction). GB300's FP64
+// pipe, where the hardware conversion issues, runs at 1/64 of the FP32 rate;
+// these integer operations run at full rate.
+__device__ __forceinline__ double widen(float f) {
+  const unsigned u = __float_as_uint(f);
+  const unsigned s = u & 0x80000000u, e = (u >> 23) & 0xffu;
+  unsigned m = u & 0x7fffffu, ex = e + 896u;
+  if (e == 0xffu) ex = 0x7ffu;
+  if (e == 0u) {
+    if (m == 0u) {
+      ex = 0u;
+    } else {
+      const int p = 31 - __clz((int)m);  // 0..22
+      ex = (unsigned)(p + 874);
+      m = (m << (23 - p)) & 0x7fffffu;
+    }
+  }
+  return __hiloint2double((int)(s | (ex << 20) | (m >> 3)), (int)(m << 29));
+}
+
 // ---- finish: fold the last stage's acoustic increments into the FP64
 // state, apply the sponge (damping.cpp:76-140) in FP64 and to the FP32
 // working copy, which becomes the next step's s0 working copy.
@@ -903,11 +927,17 @@ __device__ __forceinline__ void finish_body(const Dims& d, const Tab& t, const F
   const int kc = imin(k, d.nz - 1);
   const double wd = t.spwd[k];
   const float wf = t.spw[k];
+  const double sdt = (k < d.nz) ? t.spdt[k] : 0.0;
+  // below the sponge layers (weight exactly 1, relaxation exactly 0; uniform
+  // over the block, whose level is blockIdx.z) the sponge leaves every value
+  // unchanged, so only the FP64 additions remain
+  const bool plain = __double_as_longlong(wd) == 0x3ff0000000000000ll && __double_as_longlong(sdt) == 0ll;
   bool bad = false;
   auto incr = [&](int q) { return rin.f[q] ? dtf * rin.f[q][c] : 0.f; };
   auto face = [&](int q) {
     const float wv = wfin.f[q][c];
-    const double v = wd * (s0.f[q][c] + (double)(incr(q) + (wv - wst.f[q][c])));
+    const double a = s0.f[q][c] + widen(incr(q) + (wv - wst.f[q][c]));
+    const double v = plain ? a : wd * a;
     s1.f[q][c] = v;
     w0.f[q][c] = wf * wv;
     bad |= !finite64(v);
@@ -923,31 +953,32 @@ __device__ __forceinline__ void finish_body(const Dims& d, const Tab& t, const F
     }
   }
   if (i < d.nx && j < d.ny && k < d.nz) {
-    const double sdt = t.spdt[k];
     {
       const float wv = wfin.f[RHO][c];
-      const double v = wd * ((s0.f[RHO][c] + (double)(incr(RHO) + (wv - wst.f[RHO][c]))) + sdt * t.r0d[kc]);
+      const double a = s0.f[RHO][c] + widen(incr(RHO) + (wv - wst.f[RHO][c]));
+      const double v = plain ? a : wd * (a + sdt * t.r0d[kc]);
       s1.f[RHO][c] = v;
       w0.f[RHO][c] = wf * wv;
       bad |= !finite64(v);
     }
     {
       const float wv = wfin.f[PI][c];
-      const double v = wd * ((s0.f[PI][c] + (double)(incr(PI) + (wv - wst.f[PI][c]))) + sdt * t.p0d[kc]);
+      const double a = s0.f[PI][c] + widen(incr(PI) + (wv - wst.f[PI][c]));
+      const double v = plain ? a : wd * (a + sdt * t.p0d[kc]);
       s1.f[PI][c] = v;
       w0.f[PI][c] = wf * wv;
       bad |= !finite64(v);
     }
     {
-      double v = s0.f[THETA][c] + (double)incr(THETA);
-      if (wd != 1.0) v = wd * (v + sdt * t.t0dd[kc]);
+      double v = s0.f[THETA][c] + widen(incr(THETA));
+      if (!plain) v = wd * (v + sdt * t.t0dd[kc]);
       s1.f[THETA][c] = v;
       w0.f[THETA][c] = wf * wst.f[THETA][c];
       bad |= !finite64(v);
     }
     const int last = fl.moist ? QG : QV;
     for (int q = QV; q <= last; ++q) {
-      const double v = s0.f[q][c] + (double)incr(q);
+      const double v = s0.f[q][c] + widen(incr(q));
       s1.f[q][c] = v;
       w0.f[q][c] = wst.f[q][c];
       bad |= !finite64(v);
