@@ -646,7 +646,7 @@ def main():
     # column: read u v w rho pi, write w rho pi u v; finish: read S0, R3, 5 substep
     # fields, 7 stage fields, write S1, W0; u/v in place: read u v pi, write u v
     per_cell = {0: (56.0 + 84.0 + 112.0) / 3.0, 1: 40.0, 2: 216.0, 3: 20.0}
-    names = {0: "k_mx_stage", 1: "k_mx_hevi_col", 2: "k_mx_finish", 3: "k_mx_fb_mom(u,v)"}
+    names = {0: "k_mx_stage", 1: "k_mx_hevi_tma", 2: "k_mx_finish", 3: "k_mx_fb_mom(u,v)"}
     dom = max(ktimes, key=lambda c: ktimes[c][0])
     tot_ms, spans = ktimes[dom]
     avg_s = tot_ms / max(spans, 1) * 1e-3
