@@ -42,6 +42,7 @@
 #include "vibe/grid/decomposition.hpp"
 #include "vibe/grid/geometry.hpp"
 #include "vibe/time/acoustic_substep.hpp"
+#include "vibe/physics/microphysics.hpp"
 #include "vibe/time/helmholtz.hpp"
 #include "vibe/grid/nest.hpp"
 #include "vibe/da/tangent_linear.hpp"
@@ -618,6 +619,47 @@ void vref_energy_budget(vref_model* m, double* out6) {
   out6[3] = e.latent;
   out6[4] = e.total;
   out6[5] = e.mass;
+}
+
+// KesslerMicrophysics::step_column (src/physics/microphysics_kessler.cpp:269-331)
+// on a column built like state_to_column leaves it (dz from
+// PhysicsColumn::diagnose_layer_depth; qi, qs, qg zero). PhysicsDriver itself
+// does not build in the reference tree (pbl_myj.cpp / pbl_ysu.cpp declare
+// diagnose_height with another exception specifier, surface_layer.cpp names
+// an option PhysicsOptions does not have), so the column step is pinned here
+// and state_to_column is restated in the oracle.
+double vref_kessler_column(const vo_kessler* k, int n, double dt, const double* z, const double* p,
+                           const double* rho, double* theta, double* qv, double* qc, double* qr) {
+  physics::PhysicsOptions opt;
+  opt.kessler_qc0 = k->qc0;
+  opt.kessler_k1 = k->k1;
+  opt.kessler_k2 = k->k2;
+  opt.kessler_evap_coef = k->evap_coef;
+  opt.kessler_rain_a = k->rain_a;
+  opt.kessler_rain_b = k->rain_b;
+  opt.positive_definite = k->positive_definite != 0;
+  physics::KesslerMicrophysics mp(opt);
+  physics::PhysicsColumn col;
+  col.resize(n);
+  for (int s = 0; s < n; ++s) {
+    col.z[s] = z[s];
+    col.p[s] = p[s];
+    col.rho[s] = rho[s];
+    col.theta[s] = theta[s];
+    col.qv[s] = qv[s];
+    col.qc[s] = qc[s];
+    col.qr[s] = qr[s];
+  }
+  col.diagnose_layer_depth();
+  physics::PhysicsDiagnostics diag;
+  const double precip = mp.step_column(col, dt, diag);
+  for (int s = 0; s < n; ++s) {
+    theta[s] = col.theta[s];
+    qv[s] = col.qv[s];
+    qc[s] = col.qc[s];
+    qr[s] = col.qr[s];
+  }
+  return precip;
 }
 
 }  // extern "C"

@@ -78,6 +78,8 @@ struct vo_model {
   fld scr[VO_NSPECIES];
   fld ref[5];     /* theta0, pi0, rho0, p0, qv0 */
   double f0, beta;
+  int physics;            /* 1: Kessler coupled into vo_rk3_step */
+  vo_kessler kessler;
 };
 
 /* ------------------------------------------------------------------------ */
@@ -1017,6 +1019,265 @@ void vo_slow_tendency(vo_model *m, double *const *out) {
     memcpy(out[sp], m->slow[sp].d, fld_size(&m->slow[sp]) * sizeof(double));
 }
 
+/* ------------------------------------------------------------------------ */
+/* Kessler warm rain: src/physics/microphysics_kessler.cpp, helpers from      */
+/* src/physics/physics_types.cpp and include/vibe/physics/physics_types.hpp  */
+/* ------------------------------------------------------------------------ */
+static fld fld_view(const vo_model *m, const double *p);
+#define KP_RV 461.51
+#define KP_KAPPA 0.28571
+#define KP_T0 273.15
+#define KP_RHO_WATER 1000.0
+#define KP_DV_WATER 2.21e-5
+#define KP_THERM_COND_AIR 2.40e-2
+#define KP_DYN_VISC_AIR 1.8e-5 /* microphysics_kessler.cpp:23 */
+#define KP_SCHMIDT 0.6         /* :24 */
+#define KP_RAIN_N0 8.0e6       /* microphysics.hpp:192 */
+#define KP_RAIN_B 3.0          /* microphysics.hpp:195 */
+
+static double kp_max(double a, double b) { return a > b ? a : b; } /* std::max: a < b ? b : a */
+static double kp_min(double a, double b) { return b < a ? b : a; } /* std::min */
+static double kp_clamp(double v, double lo, double hi) { return v < lo ? lo : (hi < v ? hi : v); }
+
+void vo_kessler_defaults(vo_kessler *k) { /* PhysicsOptions, physics_types.hpp:420-429 */
+  k->qc0 = 1.0e-3;
+  k->k1 = 1.0e-3;
+  k->k2 = 2.2;
+  k->evap_coef = 1.0;
+  k->rain_a = 36.34;
+  k->rain_b = 0.1364;
+  k->positive_definite = 1;
+  k->exner_offset = 1;
+}
+
+static double kp_exner(double p) { return pow(p / K_P0, KP_KAPPA); }            /* physics_types.hpp:136-138 */
+static double kp_lv(double t) { return (2.501 - 0.00237 * (t - KP_T0)) * 1.0e6; } /* :159-161 */
+static double kp_es(double t) {                                                 /* physics_types.cpp:143-146 */
+  const double tc = kp_max(t - KP_T0, -80.0);
+  return 611.2 * exp(17.67 * tc / (tc + 243.5));
+}
+static double kp_qs(double p, double t) { /* saturation_mixing_ratio, physics_types.cpp:163-167 (liquid) */
+  const double es = kp_es(t);
+  const double den = kp_max(p - es, 1.0);
+  return K_EPS_VAP * es / den;
+}
+static double kp_fall_speed(const vo_kessler *o, double rho, double qr) { /* microphysics_kessler.cpp:188-191 */
+  const double load = kp_max(rho * kp_max(qr, 0.0), 0.0);
+  return o->rain_a * pow(load, o->rain_b);
+}
+
+/* saturation_adjust_point (liquid), microphysics_kessler.cpp:100-144 */
+static void kp_adjust(double *qv_io, double *qc_io, double *theta_io, double p) {
+  double qv = kp_max(*qv_io, 0.0), qc = kp_max(*qc_io, 0.0), theta = *theta_io;
+  const double pi = kp_exner(p);
+  double t = kp_max(theta * pi, 150.0);
+  double qs = kp_qs(p, t);
+  double l = kp_lv(t);
+  const double denom0 = 1.0 + l * l * qs / (K_CP * KP_RV * t * t);
+  double delta = kp_clamp((qv - qs) / denom0, -qc, qv);
+  if (fabs(delta) < 1.0e-16) {
+    *qv_io = qv;
+    *qc_io = qc;
+    return;
+  }
+  for (int it = 1; it <= 10; ++it) {
+    t = theta * pi + (l / K_CP) * delta;
+    t = kp_max(t, 150.0);
+    qs = kp_qs(p, t);
+    l = kp_lv(t);
+    const double f = qv - delta - qs;
+    const double dqsdT = l * qs / (KP_RV * t * t);
+    const double df = -1.0 - (l / K_CP) * dqsdT;
+    const double residual = fabs(f) / kp_max(qs, 1.0e-12);
+    if (residual <= 1.0e-10) break;
+    const double step = -f / df;
+    const double trial = kp_clamp(delta + kp_clamp(step, -1.0, 1.0), -qc, qv);
+    if (trial == delta) break;
+    delta = trial;
+  }
+  qv -= delta;
+  qc += delta;
+  theta += l * delta / (K_CP * pi);
+  *qv_io = kp_max(qv, 0.0);
+  *qc_io = kp_max(qc, 0.0);
+  *theta_io = theta;
+}
+
+/* rain_evaporation_rate, microphysics_kessler.cpp:213-227, with
+ * slope_parameter, number_concentration, ventilation_factor and
+ * particle_mass_rate (:38-76) */
+static double kp_evap_rate(const vo_kessler *o, double p, double t, double rho, double qv, double qs, double qr) {
+  (void)p;
+  if (!(qr > 0.0) || !(rho > 0.0)) return 0.0;
+  const double a = K_PI / 6.0 * KP_RHO_WATER;
+  const double qq = kp_max(qr, 1.0e-14);
+  const double num = a * KP_RAIN_N0 * tgamma(1.0 + KP_RAIN_B);
+  const double den = kp_max(rho * qq, 1.0e-20);
+  const double lambda = pow(num / den, 1.0 / KP_RAIN_B);
+  const double nr = KP_RAIN_N0 / kp_max(lambda, 1.0e-8);
+  const double r_mean = 0.5 / kp_max(lambda, 1.0e-8);
+  const double vt = kp_fall_speed(o, rho, qr);
+  double fv = 1.0;
+  if (r_mean > 0.0) {
+    const double re = 2.0 * r_mean * kp_max(vt, 0.0) * rho / KP_DYN_VISC_AIR;
+    fv = kp_max(0.78 + 0.308 * cbrt(KP_SCHMIDT) * sqrt(kp_max(re, 0.0)), 1.0);
+  }
+  double dm = 0.0;
+  if (r_mean > 0.0 && rho > 0.0 && t > 0.0) {
+    const double rho_v = qv * rho, rho_vs = qs * rho;
+    const double l = kp_lv(t);
+    const double dnm = 1.0 + l * l * KP_DV_WATER * rho_vs / (KP_THERM_COND_AIR * KP_RV * t * t);
+    dm = 4.0 * K_PI * r_mean * fv * (rho_v - rho_vs) / dnm;
+  }
+  const double rate = (-dm) * nr / rho;
+  return kp_max(o->evap_coef * rate, 0.0);
+}
+
+/* KesslerMicrophysics::step_column, microphysics_kessler.cpp:269-331, with
+ * PhysicsColumn::diagnose_layer_depth (physics_types.cpp:257-284) for dz */
+double vo_kessler_column(const vo_kessler *o, int n, double dt, const double *z, const double *p,
+                         const double *rho, double *theta, double *qv, double *qc, double *qr) {
+  if (!(dt > 0.0) || n <= 0) return 0.0;
+  double *dz = (double *)malloc(sizeof(double) * (size_t)n);
+  double *zf = (double *)malloc(sizeof(double) * (size_t)(n + 1));
+  if (n == 1) {
+    zf[0] = z[0] - 0.5 * 100.0;
+    zf[1] = z[0] + 0.5 * 100.0;
+  } else {
+    zf[0] = z[0] - 0.5 * (z[1] - z[0]);
+    for (int k = 1; k < n; ++k) zf[k] = 0.5 * (z[k - 1] + z[k]);
+    zf[n] = z[n - 1] + 0.5 * (z[n - 1] - z[n - 2]);
+  }
+  for (int k = 0; k < n; ++k) dz[k] = kp_max(zf[k + 1] - zf[k], 1.0e-6);
+  /* 1. saturation adjustment */
+  for (int k = 0; k < n; ++k) kp_adjust(&qv[k], &qc[k], &theta[k], p[k]);
+  /* 2. autoconversion + accretion */
+  for (int k = 0; k < n; ++k) {
+    const double c = kp_max(qc[k], 0.0), r = kp_max(qr[k], 0.0);
+    const double rate = o->k1 * kp_max(c - o->qc0, 0.0) + o->k2 * kp_max(c, 0.0) * kp_max(r, 0.0);
+    const double dq = kp_min(rate * dt, c);
+    qc[k] = c - dq;
+    qr[k] = r + dq;
+  }
+  /* 3. sedimentation (sediment_rain, :240-262) */
+  double flux_in = 0.0;
+  for (int k = n - 1; k >= 0; --k) {
+    const double rh = kp_max(rho[k], 1.0e-6), d = kp_max(dz[k], 1.0e-6), r = kp_max(qr[k], 0.0);
+    const double mass = rh * r * d;
+    const double vt = kp_fall_speed(o, rh, r);
+    const double available = mass + flux_in * dt;
+    const double out = kp_min(rh * r * vt * dt, kp_max(available, 0.0));
+    qr[k] = kp_max(available - out, 0.0) / (rh * d);
+    flux_in = out / dt;
+  }
+  const double precip = flux_in * dt;
+  /* 4. rain evaporation */
+  for (int k = 0; k < n; ++k) {
+    const double r = kp_max(qr[k], 0.0);
+    if (r <= 0.0) continue;
+    const double pk = kp_exner(p[k]);
+    const double t = theta[k] * pk;
+    const double qs = kp_qs(p[k], t);
+    const double v = kp_max(qv[k], 0.0);
+    if (v >= qs) continue;
+    double evap = kp_evap_rate(o, p[k], t, rho[k], v, qs, r) * dt;
+    evap = kp_min(evap, r);
+    const double lv = kp_lv(t);
+    const double cap = (qs - v) / (1.0 + lv * lv * qs / (K_CP * KP_RV * t * t));
+    evap = kp_min(evap, kp_max(cap, 0.0));
+    if (!(evap > 0.0)) continue;
+    qr[k] = r - evap;
+    qv[k] = v + evap;
+    theta[k] = theta[k] - lv * evap / (K_CP * pk);
+  }
+  /* 5. positive definite */
+  if (o->positive_definite)
+    for (int k = 0; k < n; ++k) {
+      qv[k] = kp_max(qv[k], 0.0);
+      qc[k] = kp_max(qc[k], 0.0);
+      qr[k] = kp_max(qr[k], 0.0);
+    }
+  free(dz);
+  free(zf);
+  return precip / dt;
+}
+
+/* PhysicsDriver microphysics step for the current state: state_to_column
+ * (physics_driver.cpp:95-128; qi, qs, qg enter only the virtual temperature
+ * used where rho <= 0), step_column, td = (after - before) / dt (:271-288),
+ * scattered into cell fields (:369-383). pt[0..3]: theta, qv, qc, qr. */
+static void kessler_tendency(const vo_model *m, const vo_kessler *o, double dt, fld *pt) {
+  const int nz = m->nz;
+  double *z = (double *)malloc(sizeof(double) * (size_t)nz * 10);
+  double *p = z + nz, *rho = p + nz, *th = rho + nz, *qv = th + nz, *qc = qv + nz, *qr = qc + nz;
+  double *th0 = qr + nz, *qv0 = th0 + nz, *qc0 = qv0 + nz;
+  double *qr0 = (double *)malloc(sizeof(double) * (size_t)nz);
+  for (int j = 0; j < m->ny; ++j)
+    for (int i = 0; i < m->nx; ++i) {
+      for (int k = 0; k < nz; ++k) {
+        z[k] = g_zc(m, i, j, k);
+        const double pi0 = AT(m->ref[1], i, j, k);
+        const double pis = AT(m->st[VO_PI], i, j, k);
+        const double pi = o->exner_offset ? pi0 + pis : pis;
+        p[k] = K_P0 * pow(kp_max(pi, 1.0e-3), 1.0 / KP_KAPPA);
+        th[k] = AT(m->st[VO_THETA], i, j, k);
+        qv[k] = kp_max(AT(m->st[VO_QV], i, j, k), 0.0);
+        qc[k] = kp_max(AT(m->st[VO_QC], i, j, k), 0.0);
+        qr[k] = kp_max(AT(m->st[VO_QR], i, j, k), 0.0);
+        const double rs = AT(m->st[VO_RHO], i, j, k);
+        if (rs > 0.0) {
+          rho[k] = rs;
+        } else {
+          const double qi = kp_max(AT(m->st[VO_QI], i, j, k), 0.0), qsn = kp_max(AT(m->st[VO_QS], i, j, k), 0.0),
+                       qg = kp_max(AT(m->st[VO_QG], i, j, k), 0.0);
+          const double tv = th[k] * kp_exner(p[k]) * (1.0 + 0.608 * qv[k] - qc[k] - qi - qsn - qg);
+          rho[k] = p[k] / (K_RD * tv);
+        }
+        th0[k] = th[k]; qv0[k] = qv[k]; qc0[k] = qc[k]; qr0[k] = qr[k];
+      }
+      vo_kessler_column(o, nz, dt, z, p, rho, th, qv, qc, qr);
+      for (int k = 0; k < nz; ++k) {
+        AT(pt[0], i, j, k) = 0.0 + (th[k] - th0[k]) / dt;
+        AT(pt[1], i, j, k) = 0.0 + (qv[k] - qv0[k]) / dt;
+        AT(pt[2], i, j, k) = 0.0 + (qc[k] - qc0[k]) / dt;
+        AT(pt[3], i, j, k) = 0.0 + (qr[k] - qr0[k]) / dt;
+      }
+    }
+  free(z);
+  free(qr0);
+}
+
+void vo_kessler_tendency(const vo_model *m, const vo_kessler *k, double dt, double *const *out) {
+  fld pt[4];
+  for (int q = 0; q < 4; ++q) {
+    pt[q] = fld_view(m, out[q]);
+    memset(out[q], 0, fld_size(&pt[q]) * sizeof(double));
+  }
+  kessler_tendency(m, k, dt, pt);
+}
+
+void vo_set_physics_kessler(vo_model *m, const vo_kessler *k) {
+  m->physics = k != NULL;
+  if (k) m->kessler = *k;
+}
+
+/* RungeKutta3Integrator::slow_tendency with physics (runge_kutta.cpp:46-63):
+ * d += pt for theta, qv, qc, qr (the other PhysicsTendency fields stay zero
+ * under this scheme) */
+static void physics_into(vo_model *m, double dt) {
+  fld pt[4];
+  for (int q = 0; q < 4; ++q) {
+    fld_alloc(&pt[q], m->nx, m->ny, m->nz, 0);
+    fld_zero(&pt[q]);
+  }
+  kessler_tendency(m, &m->kessler, dt, pt);
+  const int sp[4] = {VO_THETA, VO_QV, VO_QC, VO_QR};
+  for (int q = 0; q < 4; ++q) {
+    add_scaled(&m->slow[sp[q]], 1.0, &pt[q]);
+    free(pt[q].d);
+  }
+}
+
 /* RungeKutta3Integrator::step, runge_kutta.cpp:77-119, with
  * State::add_scaled(Real, Tendency) expanded field by field */
 int vo_rk3_step(vo_model *m, double dt, int n_sub_in) {
@@ -1026,6 +1287,7 @@ int vo_rk3_step(vo_model *m, double dt, int n_sub_in) {
   const double dt_stage[3] = {dt / 3.0, dt / 2.0, dt};
   for (int stage = 0; stage < 3; ++stage) {
     slow_tendency_split(m, m->st, m->slow);
+    if (m->physics) physics_into(m, dt);
     for (int sp = 0; sp < VO_NSPECIES; ++sp) {
       memcpy(m->st[sp].d, m->s0[sp].d, fld_size(&m->st[sp]) * sizeof(double));
       add_scaled(&m->st[sp], dt_stage[stage], &m->slow[sp]);

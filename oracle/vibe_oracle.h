@@ -214,6 +214,30 @@ void vo_advect_scalar_flux(const double *q, const double *rho, const double *u,
                            const double *zs, int nx, int ny, int nz, double dx,
                            double dy, double z_top, double *dqdt);
 
+/* Kessler warm-rain microphysics (src/physics/microphysics_kessler.cpp) and
+ * its coupling through PhysicsDriver's microphysics step
+ * (physics_driver.cpp:95-128 state_to_column, :271-288 tendencies) and
+ * RungeKutta3Integrator::slow_tendency (runge_kutta.cpp:46-63). The option
+ * defaults are PhysicsOptions' (physics_types.hpp:417-430). exner_offset = 1
+ * builds the column pressure from pi0 + pi as state_to_column does (the
+ * state's pi being the total Exner function, this doubles it); 0 uses pi. */
+typedef struct {
+  double qc0, k1, k2, evap_coef, rain_a, rain_b;
+  int positive_definite, exner_offset;
+} vo_kessler;
+void vo_kessler_defaults(vo_kessler *k);
+/* KesslerMicrophysics::step_column on one column of n levels (k = 0 at the
+ * bottom): z (level heights), p, rho given; theta, qv, qc, qr updated in
+ * place (qi, qs, qg zero). Returns the surface precipitation rate. */
+double vo_kessler_column(const vo_kessler *k, int n, double dt, const double *z, const double *p,
+                         const double *rho, double *theta, double *qv, double *qc, double *qr);
+/* The PhysicsTendency the microphysics step adds to the slow tendency for
+ * the model's current state: out[0..3] = theta, qv, qc, qr rates (cell
+ * FieldT storage, zero outside the interior). */
+void vo_kessler_tendency(const vo_model *m, const vo_kessler *k, double dt, double *const *out);
+/* Couple the scheme into vo_rk3_step (NULL: off). */
+void vo_set_physics_kessler(vo_model *m, const vo_kessler *k);
+
 /* ---- reference-linked driver (oracle/ref/ref_driver.cpp) ---- */
 typedef struct vref_model vref_model;
 vref_model *vref_create(const vo_setup *s);
@@ -221,6 +245,10 @@ int vref_write_restart(vref_model *m, const char *path, double time, int step);
 void vref_energy_budget(vref_model *m, double *out6);
 int vref_read_restart(vref_model *m, const char *path, double *time, int *step);
 void vref_destroy(vref_model *m);
+/* KesslerMicrophysics::step_column of the compiled reference on the same
+ * column as vo_kessler_column. */
+double vref_kessler_column(const vo_kessler *k, int n, double dt, const double *z, const double *p,
+                           const double *rho, double *theta, double *qv, double *qc, double *qr);
 size_t vref_storage_size(const vref_model *m, int species);
 void vref_get_field(const vref_model *m, int species, double *out);
 void vref_set_field(vref_model *m, int species, const double *in);

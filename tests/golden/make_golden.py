@@ -9,6 +9,9 @@ Outputs (interior points of u v w rho theta pi qv, float64):
   ref_kernels.npz  Equations::tendencies and AcousticSubstepper::step (HEVI)
   ref_restart.vibebin  io::write_restart of the small case after one RK3
                    step (dt 1, 2 substeps), time 12.5, step 3
+  ref_kessler.npz  KesslerMicrophysics::step_column on the seeded columns of
+                   tests/kessler_cases.py (theta, qv, qc, qr after the step and
+                   the surface precipitation rate)
 """
 import os
 import sys
@@ -56,6 +59,14 @@ def main():
     m = oc.Model(small(oc), "ref")
     assert m.rk3_step(1.0, 2) == 0
     assert oc.write_restart(m, os.path.join(HERE, "ref_restart.vibebin"), 12.5, 3) == 0
+    from test_oracle_cpu import _kessler_runs
+    runs = _kessler_runs(oc, "ref")
+    kes = {"nruns": len(runs)}
+    for r, run in enumerate(runs):
+        for f, name in enumerate(("theta", "qv", "qc", "qr")):
+            kes["run%d_%s" % (r, name)] = run[f]
+        kes["run%d_precip" % r] = run[4]
+    np.savez_compressed(os.path.join(HERE, "ref_kessler.npz"), **kes)
     print("wrote", os.listdir(HERE))
 
 

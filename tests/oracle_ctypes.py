@@ -471,3 +471,52 @@ def energy_budget(model):
     out = (ctypes.c_double * 6)()
     model._f["energy_budget"](model.h, out)
     return dict(zip(("kinetic", "internal", "potential", "latent", "total", "mass"), out))
+
+
+# ---- Kessler warm rain (KesslerMicrophysics::step_column, PhysicsDriver's microphysics step) ----
+class Kessler(ctypes.Structure):
+    """Mirror of vo_kessler (PhysicsOptions' Kessler fields)."""
+    _fields_ = [("qc0", _D), ("k1", _D), ("k2", _D), ("evap_coef", _D), ("rain_a", _D), ("rain_b", _D),
+                ("positive_definite", _I), ("exner_offset", _I)]
+
+    @classmethod
+    def defaults(cls, **kw):
+        k = cls()
+        lib = port_lib()
+        lib.vo_kessler_defaults.argtypes = [ctypes.POINTER(Kessler)]
+        lib.vo_kessler_defaults.restype = None
+        lib.vo_kessler_defaults(ctypes.byref(k))
+        for name, v in kw.items():
+            setattr(k, name, v)
+        return k
+
+
+def kessler_column(k, dt, z, p, rho, theta, qv, qc, qr, kind="port"):
+    """One column step; returns (theta, qv, qc, qr, precipitation rate)."""
+    lib = _load(kind)[0]
+    f = getattr(lib, "vo_kessler_column" if kind == "port" else "vref_kessler_column")
+    vp = ctypes.c_void_p
+    f.argtypes = [ctypes.POINTER(Kessler), _I, _D] + [vp] * 7
+    f.restype = _D
+    arrs = [np.ascontiguousarray(a, dtype=np.float64).copy() for a in (z, p, rho, theta, qv, qc, qr)]
+    pr = f(ctypes.byref(k), len(arrs[0]), dt, *[a.ctypes.data for a in arrs])
+    return arrs[3], arrs[4], arrs[5], arrs[6], pr
+
+
+def kessler_tendency(model, k, dt):
+    """PhysicsTendency of the microphysics step: [theta, qv, qc, qr] rates (cell FieldT storage)."""
+    lib = model._lib
+    dp = ctypes.POINTER(ctypes.c_double)
+    lib.vo_kessler_tendency.argtypes = [ctypes.c_void_p, ctypes.POINTER(Kessler), _D, ctypes.POINTER(dp)]
+    lib.vo_kessler_tendency.restype = None
+    outs = [np.zeros(model.size(3)) for _ in range(4)]
+    arr = (dp * 4)(*[o.ctypes.data_as(dp) for o in outs])
+    lib.vo_kessler_tendency(model.h, ctypes.byref(k), dt, arr)
+    return outs
+
+
+def set_physics_kessler(model, k):
+    lib = model._lib
+    lib.vo_set_physics_kessler.argtypes = [ctypes.c_void_p, ctypes.POINTER(Kessler)]
+    lib.vo_set_physics_kessler.restype = None
+    lib.vo_set_physics_kessler(model.h, ctypes.byref(k) if k is not None else None)

@@ -344,3 +344,63 @@ def test_energy_budget_port_is_bit_exact_to_reference(oc, case):
     p, r = oc.Model(s, "port"), oc.Model(s, "ref")
     assert p.rk3_step(1.0, 2) == 0 and r.rk3_step(1.0, 2) == 0
     assert oc.energy_budget(p) == oc.energy_budget(r)
+
+
+# ---- Kessler warm rain (src/physics/microphysics_kessler.cpp) ----
+def _kessler_runs(oc, kind):
+    import kessler_cases as kc
+    out = []
+    for c in kc.cases():
+        for dt in kc.DTS:
+            for offset in (1,):
+                k = oc.Kessler.defaults(exner_offset=offset)
+                out.append(oc.kessler_column(k, dt, c["z"], c["p"], c["rho"], c["theta"], c["qv"], c["qc"], c["qr"],
+                                             kind=kind))
+    return out
+
+
+@need_ref
+def test_kessler_column_port_is_bit_exact_to_reference(oc):
+    """The restated column step against KesslerMicrophysics::step_column of
+    the compiled reference: saturation adjustment, autoconversion and
+    accretion, sedimentation, rain evaporation, positivity."""
+    for a, b in zip(_kessler_runs(oc, "port"), _kessler_runs(oc, "ref")):
+        for x, y in zip(a[:4], b[:4]):
+            assert np.array_equal(x, y)
+        assert a[4] == b[4]
+
+
+def test_kessler_column_port_matches_golden(oc):
+    path = os.path.join(GOLDEN, "ref_kessler.npz")
+    if not os.path.exists(path):
+        pytest.skip("golden fixture ref_kessler.npz missing")
+    g = np.load(path)
+    runs = _kessler_runs(oc, "port")
+    assert int(g["nruns"]) == len(runs)
+    for r, run in enumerate(runs):
+        for f, name in enumerate(("theta", "qv", "qc", "qr")):
+            assert np.array_equal(run[f], g["run%d_%s" % (r, name)]), (r, name)
+        assert run[4] == float(g["run%d_precip" % r])
+    # every process acted somewhere in the cases
+    import kessler_cases as kc
+    cs = kc.cases()
+    assert np.any(runs[0][2] > 0)                         # condensation (case 0, no cloud before)
+    assert np.all(runs[2][2] <= cs[1]["qc"])              # cloud evaporates or converts in subsaturated air
+    assert runs[4][4] > 0.0                                # rain reaches the ground
+    assert np.any(runs[4][1] > cs[2]["qv"])                # rain evaporation moistens the dry layer
+
+
+def test_kessler_coupling_in_rk3_step(oc):
+    """vo_rk3_step with the scheme coupled: a moist case condenses (qc
+    appears), with physics off it does not; the tendency of a state without
+    water is zero."""
+    s = small(oc, moist=1, qv_surface=0.018, qv_decay_height=2500.0)
+    k = oc.Kessler.defaults(exner_offset=0)
+    a, b = oc.Model(s, "port"), oc.Model(s, "port")
+    oc.set_physics_kessler(a, k)
+    assert a.rk3_step(1.0, 2) == 0 and b.rk3_step(1.0, 2) == 0
+    qc_a, qc_b = oc.interior(s, 7, a.get(7)), oc.interior(s, 7, b.get(7))
+    assert qc_a.max() > 0.0 and qc_b.max() == 0.0
+    dry = oc.Model(small(oc, qv_surface=0.0), "port")
+    for t in oc.kessler_tendency(dry, k, 1.0):
+        assert not np.any(t)
