@@ -244,6 +244,62 @@ int vibe_gb300_autotune(vibe_gb300_model *m, double dt, int n_sub, vibe_gb300_tu
  * this model's grid, e.g. one found by an earlier autotune run; the other
  * fields of t are ignored. */
 int vibe_gb300_set_tuning(vibe_gb300_model *m, const vibe_gb300_tuning *t);
+
+/* ---- physics coupling (Integrator::set_physics, integrator.hpp:74;
+ * RungeKutta3Integrator::slow_tendency, runge_kutta.cpp:46-63) ----
+ * A physics package is a function that the step calls once per RK stage,
+ * while the stage's launches are enqueued, with the stage's input state and
+ * zeroed tendency accumulators; it enqueues its work on `stream` (work on
+ * that stream is captured into the step's CUDA graph, so the function must
+ * not synchronise) and returns 0, or nonzero to fail the step. The step then
+ * adds the accumulated local rates of theta, qv..qg, u and v to the slow
+ * tendency (d += pt) before the stage update, as the reference does with its
+ * PhysicsTendency. Device layout of every field: element (i, j, k) at
+ * (k*(ny+1) + j)*pitch + i. */
+typedef struct {
+  int precision;          /* VIBE_GB300_FP64 (double fields) or VIBE_GB300_MIXED (float fields) */
+  int stage;              /* RK stage 0, 1, 2 */
+  double dt;              /* the step's dt (what PhysicsDriver::step receives) */
+  int nx, ny, nz, pitch;
+  int moist;              /* 1: qc..qg are prognostic (setup.moist) */
+  /* stage input per species (device). FP64: the totals. MIXED: u, v, w and
+   * the moisture species as totals, rho, theta, pi as departures from the
+   * reference state below. */
+  const void *state[12];
+  /* zeroed device accumulators (local rates) for u, v, theta, qv..qg; the
+   * other species' entries are NULL */
+  void *tend[12];
+  const double *ref_theta, *ref_pi, *ref_rho; /* device, reference state (device layout, FP64) */
+  const double *zeta_mid;                     /* device, nz: normalised height of the level centres */
+  const double *terrain;                      /* device, nx*ny row-major: terrain height */
+  const double *depth;                        /* device, nx*ny: z_top - terrain height */
+  void *stream;                               /* cudaStream_t */
+} vibe_gb300_physics_args;
+typedef int (*vibe_gb300_physics_fn)(void *user, const vibe_gb300_physics_args *args);
+/* Install (fn != NULL) or remove the package; drops the step graphs. */
+int vibe_gb300_set_physics(vibe_gb300_model *m, vibe_gb300_physics_fn fn, void *user);
+/* The installed package's tendency for the current state (one call as at
+ * stage 0 with this dt), downloaded as FieldT storage: out[0..8] = u, v,
+ * theta, qv, qc, qr, qi, qs, qg (entries may be NULL). */
+int vibe_gb300_physics_tendency(vibe_gb300_model *m, double dt, double *const *out);
+
+/* Built-in package: Kessler warm rain (KesslerMicrophysics::step_column,
+ * src/physics/microphysics_kessler.cpp:269-331) as PhysicsDriver's
+ * microphysics step applies it (state_to_column, physics_driver.cpp:95-128;
+ * tendencies (after - before)/dt, :271-288), radiation, surface, boundary
+ * layer, cumulus and subgrid momentum off. One thread per column; FP64
+ * arithmetic for FP64 models, FP32 for mixed ones. Needs moisture species
+ * (setup.moist = 1). user = const vibe_gb300_kessler* (kept by the caller). */
+typedef struct {
+  double qc0, k1, k2, evap_coef, rain_a, rain_b; /* PhysicsOptions::kessler_* (physics_types.hpp:424-429) */
+  int positive_definite;                         /* PhysicsOptions::positive_definite */
+  /* 1: column pressure from ref_pi + pi, as state_to_column builds it (the
+   * state's pi is the total Exner function there, so this doubles it);
+   * 0: from pi alone */
+  int exner_offset;
+} vibe_gb300_kessler;
+void vibe_gb300_kessler_defaults(vibe_gb300_kessler *k);
+int vibe_gb300_physics_kessler(void *user, const vibe_gb300_physics_args *args);
 /* One step with host input and output (FieldT storage, pinned host memory
  * for full speed), asynchronous and pipelined across calls: the call
  * enqueues the input's host -> device copies on a copy stream, the step on

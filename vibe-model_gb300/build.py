@@ -29,6 +29,7 @@ SOURCES = [("step_fp64.cu", "step_fp64.o", []),
            ("nest.cu", "nest.o", ["--fmad=false"]),
            ("tlad.cu", "tlad.o", []),
            ("advect_tlad.cu", "advect_tlad.o", []),
+           ("physics.cu", "physics.o", ["--fmad=false"]),
            ("diag.cu", "diag.o", ["--fmad=false"])]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 

@@ -79,6 +79,12 @@ struct vibe_gb300_model {
   double* tend[NSPECIES] = {};
   double* tmp[NSPECIES] = {};
   double* lin[5] = {};  // u, v, w, rho, pi perturbations of the acoustic TL/AD (allocated on first use)
+  // physics package (vibe_gb300_set_physics) and its tendency accumulators
+  vibe_gb300_physics_fn phys_fn = nullptr;
+  void* phys_user = nullptr;
+  void* pt[NSPECIES] = {};  // u, v, theta, qv..qg: double (FP64) or float (mixed)
+  double* d_zmid = nullptr;
+  double* d_zs = nullptr;
   double* scratch = nullptr;
   double *d_dzeta = nullptr, *d_scale = nullptr, *d_sponge = nullptr;
   double *d_th0 = nullptr, *d_pi0 = nullptr, *d_rho0 = nullptr;
@@ -586,6 +592,55 @@ void collect_timing(vibe_gb300_model* m) {  // after a stream sync
   m->ev_open.clear();
 }
 
+// ---- physics coupling (runge_kutta.cpp:46-63) -------------------------------
+constexpr int kPhysFields[9] = {U, V, THETA, QV, QC, QR, QI, QS, QG};
+
+// d += pt over whole buffers (FP64 path): State's add_scaled(1, pt) per field
+__global__ void k_add_pt64(size_t n, const double* __restrict__ pt, double* __restrict__ d) {
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x)
+    d[e] = d[e] + pt[e];
+}
+// mixed path: the stage kernel has written s = s0 + dt_s R; add dt_s pt, and
+// pt to the stage-3 tendency R the finish kernel folds into the FP64 state
+__global__ void k_add_pt32(size_t n, const float* __restrict__ pt, float* __restrict__ s, float dts,
+                           float* __restrict__ r) {
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x) {
+    const float p = pt[e];
+    s[e] = s[e] + dts * p;
+    if (r) r[e] = r[e] + p;
+  }
+}
+
+// zero the accumulators and let the package enqueue its work for this stage
+int physics_stage(vibe_gb300_model* m, int stage, double dt, const void* const* state) {
+  const bool mixed = m->precision == VIBE_GB300_MIXED;
+  const size_t n = m->d.plane * (size_t)(m->d.nz + 1), es = mixed ? sizeof(float) : sizeof(double);
+  vibe_gb300_physics_args a{};
+  a.precision = mixed ? VIBE_GB300_MIXED : VIBE_GB300_FP64;
+  a.stage = stage;
+  a.dt = dt;
+  a.nx = m->d.nx;
+  a.ny = m->d.ny;
+  a.nz = m->d.nz;
+  a.pitch = m->d.P;
+  a.moist = m->fl.moist ? 1 : 0;
+  for (int q = 0; q < NSPECIES; ++q) a.state[q] = state[q];
+  for (int q : kPhysFields) {
+    CUDA_OK(cudaMemsetAsync(m->pt[q], 0, n * es, m->stream));
+    a.tend[q] = m->pt[q];
+  }
+  a.ref_theta = m->d_th0;
+  a.ref_pi = m->d_pi0;
+  a.ref_rho = m->d_rho0;
+  a.zeta_mid = m->d_zmid;
+  a.terrain = m->d_zs;
+  a.depth = m->d_scale;
+  a.stream = m->stream;
+  if (int rc = m->phys_fn(m->phys_user, &a)) return fail(rc < 0 ? rc : VIBE_GB300_EDEVICE, "physics package failed");
+  CUDA_OK(cudaGetLastError());
+  return 0;
+}
+
 // One step's launches on the model stream (the state ping-pong m->cur flips).
 int enqueue_one_step(vibe_gb300_model* m, double dt, int n_sub) {
   const double dts[3] = {dt / 3.0, dt / 2.0, dt};
@@ -599,6 +654,12 @@ int enqueue_one_step(vibe_gb300_model* m, double dt, int n_sub) {
         {
           Span sp(m, 0);
           m->f64->slow_tendency(d, m->met, m->fl, src, m->tend, m->scratch, m->stream);
+          if (m->phys_fn) {
+            if (int rc = physics_stage(m, stage, dt, (const void* const*)src)) return rc;
+            const size_t n = d.plane * (size_t)(d.nz + 1);
+            for (int q : kPhysFields)
+              k_add_pt64<<<1024, 256, 0, m->stream>>>(n, (const double*)m->pt[q], m->tend[q]);
+          }
           m->f64->stage_update(d, S0, m->tend, dts[stage], S1, m->stream);
         }
         const double dtau = dts[stage] / (double)n_sub;
@@ -630,9 +691,20 @@ int enqueue_one_step(vibe_gb300_model* m, double dt, int n_sub) {
         {
           Span sp(m, 0);
           const WS wr = ws_of(m->WR);
+          if (m->phys_fn) {  // on the stage input, before the stage kernel overwrites nothing it reads
+            const void* st[NSPECIES];
+            for (int q = 0; q < NSPECIES; ++q) st[q] = win.f[q];
+            if (int rc = physics_stage(m, stage, dt, st)) return rc;
+          }
           if (mixed_stage(d, m->tab, m->fl, win, w0, ws_of(st_out), stage == 2 ? &wr : nullptr, dts[stage],
                           m->d_err, m->stream))
             return fail(VIBE_GB300_EDEVICE, "TMA descriptor creation failed (cuTensorMapEncodeTiled)");
+          if (m->phys_fn) {
+            const size_t n = d.plane * (size_t)(d.nz + 1);
+            for (int q : kPhysFields)
+              k_add_pt32<<<1024, 256, 0, m->stream>>>(n, (const float*)m->pt[q], st_out[q], (float)dts[stage],
+                                                      stage == 2 ? m->WR[q] : nullptr);
+          }
         }
         const float dtau = (float)(dts[stage] / (double)n_sub);
         float** in = st_out;
@@ -1193,6 +1265,76 @@ int vibe_gb300_autotune(vibe_gb300_model* m, double dt, int n_sub, vibe_gb300_tu
   out->default_ms_per_step = default_ms;
   out->candidates = tried;
   return 0;
+}
+
+int vibe_gb300_set_physics(vibe_gb300_model* m, vibe_gb300_physics_fn fn, void* user) {
+  if (!m) return fail(VIBE_GB300_EBADARG, "bad argument");
+  if (fn && !m->pt[THETA]) {
+    const size_t n = m->d.plane * (size_t)(m->d.nz + 1);
+    for (int q : kPhysFields) {
+      int rc = 0;
+      if (m->precision == VIBE_GB300_MIXED) rc = dalloc(m, (float**)&m->pt[q], n);
+      else rc = dalloc(m, (double**)&m->pt[q], n);
+      if (rc) return rc;
+    }
+    const int nz = m->d.nz;
+    std::vector<double> zmid(nz);
+    for (int k = 0; k < nz; ++k) zmid[k] = 0.5 * (m->hs.zeta[k] + m->hs.zeta[k + 1]);  // geometry.cpp:20-31 at k + 1/2
+    if (int rc = dalloc(m, &m->d_zmid, (size_t)nz)) return rc;
+    if (int rc = dalloc(m, &m->d_zs, m->hs.zs.size())) return rc;
+    CUDA_OK(cudaMemcpyAsync(m->d_zmid, zmid.data(), nz * sizeof(double), cudaMemcpyHostToDevice, m->stream));
+    CUDA_OK(cudaMemcpyAsync(m->d_zs, m->hs.zs.data(), m->hs.zs.size() * sizeof(double), cudaMemcpyHostToDevice,
+                            m->stream));
+    CUDA_OK(cudaStreamSynchronize(m->stream));
+  }
+  m->phys_fn = fn;
+  m->phys_user = user;
+  drop_graphs(m);
+  return 0;
+}
+
+// FP32 device layout -> FP64 FieldT storage (zeros outside the box)
+__global__ void k_unpack_f32(Dims d, int nsx, int nsy, int nsz, int ni, int nj, int nk, const float* __restrict__ src,
+                             double* __restrict__ dst) {
+  const size_t n = (size_t)nsx * nsy * nsz;
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x) {
+    const int ii = (int)(e % nsx) - H;
+    const int jj = (int)((e / nsx) % nsy) - H;
+    const int kk = (int)(e / ((size_t)nsx * nsy)) - H;
+    double v = 0.0;
+    if (ii >= 0 && ii < ni && jj >= 0 && jj < nj && kk >= 0 && kk < nk) v = (double)src[d.idx(ii, jj, kk)];
+    dst[e] = v;
+  }
+}
+
+int vibe_gb300_physics_tendency(vibe_gb300_model* m, double dt, double* const* out) {
+  if (!m || !out) return fail(VIBE_GB300_EBADARG, "bad argument");
+  if (!m->phys_fn) return fail(VIBE_GB300_EBADARG, "no physics package installed");
+  const void* st[NSPECIES];
+  if (m->precision == VIBE_GB300_MIXED) {
+    if (int rc = sync_working(m)) return rc;
+    for (int q = 0; q < NSPECIES; ++q) st[q] = m->W0[q];
+  } else {
+    for (int q = 0; q < NSPECIES; ++q) st[q] = m->S[m->cur][q];
+  }
+  if (int rc = physics_stage(m, 0, dt, st)) return rc;
+  for (int f = 0; f < 9; ++f) {
+    const int q = kPhysFields[f];
+    if (!out[f]) continue;
+    int ni, nj, nk;
+    box_of(m, q, ni, nj, nk);
+    if (m->precision == VIBE_GB300_MIXED)
+      k_unpack_f32<<<1024, 256, 0, m->stream>>>(m->d, m->nsx[q], m->nsy[q], m->nsz[q], ni, nj, nk,
+                                                (const float*)m->pt[q], m->d_stage_in);
+    else
+      k_unpack<<<1024, 256, 0, m->stream>>>(m->d, m->nsx[q], m->nsy[q], m->nsz[q], ni, nj, nk,
+                                            (const double*)m->pt[q], m->d_stage_in);
+    CUDA_OK(cudaGetLastError());
+    CUDA_OK(cudaMemcpyAsync(out[f], m->d_stage_in, storage_count(m, q) * sizeof(double), cudaMemcpyDeviceToHost,
+                            m->stream));
+    CUDA_OK(cudaStreamSynchronize(m->stream));
+  }
+  return read_status(m);
 }
 
 int vibe_gb300_set_tuning(vibe_gb300_model* m, const vibe_gb300_tuning* t) {

@@ -165,6 +165,31 @@ lib.vibe_gb300_set_tuning.restype = _I
 lib.vibe_gb300_set_tuning.argtypes = [_vp, ctypes.POINTER(Tuning)]
 
 
+class Kessler(ctypes.Structure):
+    """Mirror of vibe_gb300_kessler (PhysicsOptions' Kessler fields)."""
+    _fields_ = [("qc0", _D), ("k1", _D), ("k2", _D), ("evap_coef", _D), ("rain_a", _D), ("rain_b", _D),
+                ("positive_definite", _I), ("exner_offset", _I)]
+
+    @classmethod
+    def defaults(cls, **kw):
+        k = cls()
+        lib.vibe_gb300_kessler_defaults(ctypes.byref(k))
+        for name, v in kw.items():
+            if not hasattr(k, name):
+                raise AttributeError(name)
+            setattr(k, name, v)
+        return k
+
+
+lib.vibe_gb300_kessler_defaults.restype = None
+lib.vibe_gb300_kessler_defaults.argtypes = [ctypes.POINTER(Kessler)]
+lib.vibe_gb300_set_physics.restype = _I
+lib.vibe_gb300_set_physics.argtypes = [_vp, _vp, _vp]
+lib.vibe_gb300_physics_tendency.restype = _I
+lib.vibe_gb300_physics_tendency.argtypes = [_vp, _D, ctypes.POINTER(ctypes.POINTER(_D))]
+PHYSICS_FIELDS = (0, 1, 4, 6, 7, 8, 9, 10, 11)  # u, v, theta, qv..qg
+
+
 class Model:
     """A device-resident state plus its RK3 integrator."""
 
@@ -283,6 +308,26 @@ class Model:
         t = Tuning()
         _check(lib.vibe_gb300_autotune(self.h, dt, n_sub, ctypes.byref(t)))
         return {name: getattr(t, name) for name, _ in Tuning._fields_}
+
+    def set_physics_kessler(self, kessler=None):
+        """Couple the built-in Kessler warm-rain package into every RK stage
+        (None: no physics). The options are kept alive by the model."""
+        if kessler is None:
+            _check(lib.vibe_gb300_set_physics(self.h, None, None))
+            self._kessler = None
+            return
+        self._kessler = Kessler()
+        ctypes.memmove(ctypes.addressof(self._kessler), ctypes.addressof(kessler), ctypes.sizeof(Kessler))
+        fn = ctypes.cast(lib.vibe_gb300_physics_kessler, _vp)
+        _check(lib.vibe_gb300_set_physics(self.h, fn, ctypes.addressof(self._kessler)))
+
+    def physics_tendency(self, dt):
+        """The installed package's tendency of the current state: dict species -> FieldT array."""
+        outs = [np.zeros(self.size(sp)) for sp in PHYSICS_FIELDS]
+        dp = ctypes.POINTER(_D)
+        arr = (dp * 9)(*[o.ctypes.data_as(dp) for o in outs])
+        _check(lib.vibe_gb300_physics_tendency(self.h, dt, arr))
+        return dict(zip(PHYSICS_FIELDS, outs))
 
     def set_tuning(self, stage_levels=0, column_kernel=-1):
         """Pin launch shapes for this grid (0 / -1: the built-in choice)."""
