@@ -103,6 +103,41 @@ def si_leg(vg, steps=3):
     return out
 
 
+# Physics coupling: the single-domain workload with the moisture species
+# prognostic (qv from 0.025 at the ground, decaying over 2.5 km: saturated
+# near the ground, so the saturation adjustment condenses from the first step)
+# and the built-in Kessler warm-rain package at every RK stage (column
+# pressure from the total Exner function); mixed path, 10 steps each way.
+def physics_leg(vg, torch, steps=10, warmup=3):
+    s = vg.Setup.defaults(nx=NX, ny=NY, **dict(CASE, moist=1, qv_surface=0.025, qv_decay_height=2500.0))
+    k = vg.Kessler.defaults(exner_offset=0)
+    out = {"workload": "%dx%dx%d, moist (qv_surface 0.025, 2.5 km decay), Kessler warm rain at every RK stage, "
+                       "mixed path, dt=%g s, %d substeps" % (NX, NY, NZ, DT, NSUB), "steps": steps}
+    with vg.Model(s, vg.MIXED) as m:
+        m.save_snapshot()
+        ext = torch.cuda.ExternalStream(m.stream())
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ms = {}
+        for phys in (False, True):
+            m.set_physics_kessler(k if phys else None)
+            m.restore_snapshot()
+            m.step(DT, NSUB, warmup)  # eager step + graph capture
+            m.restore_snapshot()
+            m.sync()
+            e0.record(ext)
+            m.step_async(DT, NSUB, steps)
+            e1.record(ext)
+            m.sync()
+            ms[phys] = e0.elapsed_time(e1) / steps
+        qc = vg.interior(s, 7, m.get(7))
+        m.set_physics_kessler(None)
+    cells = NX * NY * NZ
+    out.update({"ms_per_step_dynamics_only": ms[False], "ms_per_step_with_kessler": ms[True],
+                "kessler_ms_per_stage": (ms[True] - ms[False]) / 3.0,
+                "value": cells / (ms[True] * 1e-3), "unit": "cell-updates/s", "max_qc_after": float(qc.max())})
+    return out
+
+
 # Batched nests: 8 members, each a 384 x 384 x 60 parent at 3 km with two
 # r = 3 two-way nests at 1 km (193 x 193 x 60 and 130 x 241 x 60), Davies
 # zone 5 points; 60 levels stretched from a 50 m first layer to the 20 km top
@@ -506,8 +541,9 @@ def main():
     ap.add_argument("--no-nest", action="store_true", help="skip the batched nests leg")
     ap.add_argument("--no-window", action="store_true", help="skip the TL/AD assimilation-window leg")
     ap.add_argument("--no-tune", action="store_true", help="skip the autotuner (built-in launch shapes)")
-    ap.add_argument("--only", choices=["all", "mixed"], default="all",
-                    help="mixed: time the mixed path only (no e2e, no FP64 leg)")
+    ap.add_argument("--no-physics", action="store_true", help="skip the Kessler physics-coupling leg")
+    ap.add_argument("--only", choices=["all", "mixed", "physics"], default="all",
+                    help="mixed: time the mixed path only (no e2e, no FP64 leg); physics: the physics leg only")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -532,6 +568,10 @@ def main():
     barrier, max_over_ranks = ranks.barrier, ranks.max
 
     import vibe_gb300 as vg
+    if args.only == "physics":
+        print(json.dumps({"only": "physics", "physics_coupling": physics_leg(vg, torch)}))
+        ranks.close()
+        return
     setup = case_setup(vg.Setup, args.nx, args.ny)
     cells = args.nx * args.ny * NZ
 
@@ -634,6 +674,7 @@ def main():
     si = si_leg(vg) if not args.no_si else None
     nest = nest_leg(vg, torch, args.warmup) if not args.no_nest else None
     window = window_leg(vg, torch) if not args.no_window else None
+    physics = physics_leg(vg, torch) if not args.no_physics else None
 
     value = whole_job_rate(world, cells, args.steps, ms_mx)
     value64 = whole_job_rate(world, cells, k64, ms_64)
@@ -699,6 +740,8 @@ def main():
         line["batched_nests"] = nest
     if window is not None:
         line["assimilation_window"] = window
+    if physics is not None:
+        line["physics_coupling"] = physics
     if cpu is not None:
         line["cpu_baseline"] = cpu
     print(json.dumps(line))

@@ -150,22 +150,27 @@ __global__ void k_kessler(const vibe_gb300_physics_args a, KesslerParams<R> o) {
   T* t_qc = (T*)a.tend[QC];
   T* t_qr = (T*)a.tend[QR];
   const bool mixed = sizeof(T) == sizeof(float);
-  const double zs = a.terrain[(size_t)j * a.nx + i], depth = a.depth[(size_t)j * a.nx + i];
-  auto zc = [&](int k) { return (R)(zs + a.zeta_mid[k] * depth); };  // Grid::z_center
+  const R zs = (R)a.terrain[(size_t)j * a.nx + i], depth = (R)a.depth[(size_t)j * a.nx + i];
+  auto zc = [&](int k) { return zs + (R)a.zeta_mid[k] * depth; };  // Grid::z_center
   R flux_in = (R)0;
+  // level heights around the current level, carried down the column
+  R z_up = (R)0, z_here = zc(nz - 1), z_dn = (nz > 1) ? zc(nz - 2) : (R)0;
   for (int k = nz - 1; k >= 0; --k) {
     const size_t c = (size_t)k * plane + col;
     // layer depth (diagnose_layer_depth): interfaces halfway between centres,
     // extrapolated at the bottom and top; 100 m for a single level
     R dz;
     if (nz == 1) {
-      dz = rmax((zc(0) + (R)0.5 * (R)100) - (zc(0) - (R)0.5 * (R)100), (R)1.0e-6);
+      dz = rmax((z_here + (R)0.5 * (R)100) - (z_here - (R)0.5 * (R)100), (R)1.0e-6);
     } else {
-      const R z = zc(k);
-      const R zlo = (k == 0) ? z - (R)0.5 * (zc(1) - z) : (R)0.5 * (zc(k - 1) + z);
-      const R zhi = (k == nz - 1) ? z + (R)0.5 * (z - zc(nz - 2)) : (R)0.5 * (z + zc(k + 1));
+      const R z = z_here;
+      const R zlo = (k == 0) ? z - (R)0.5 * (z_up - z) : (R)0.5 * (z_dn + z);
+      const R zhi = (k == nz - 1) ? z + (R)0.5 * (z - z_dn) : (R)0.5 * (z + z_up);
       dz = rmax(zhi - zlo, (R)1.0e-6);
     }
+    z_up = z_here;
+    z_here = z_dn;
+    if (k >= 2) z_dn = zc(k - 2);
     // state_to_column
     const R pi0 = (R)a.ref_pi[c];
     const R pis = mixed ? tot<R>(pi_s, a.ref_pi, c) : (R)pi_s[c];
