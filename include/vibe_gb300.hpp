@@ -111,8 +111,18 @@ class State {
   std::unique_ptr<vibe_gb300_model, Del> m_;
 };
 
-// timeint::Integrator (integrator.hpp:62-82); physics coupling is not part of
-// this library (PhysicsDriver stays on the host side of the caller).
+// A device physics package for Integrator::set_physics: the built-in Kessler
+// warm-rain scheme with PhysicsOptions' defaults (vibe_gb300_physics_kessler).
+struct KesslerPhysics {
+  vibe_gb300_kessler options{};
+  KesslerPhysics() { vibe_gb300_kessler_defaults(&options); }
+  vibe_gb300_physics_fn fn() const { return vibe_gb300_physics_kessler; }
+  void* user() { return &options; }
+};
+
+// timeint::Integrator (integrator.hpp:62-82). set_physics takes a device
+// package (vibe_gb300_set_physics) in place of a host PhysicsDriver*; it is
+// installed on the state's model at the next step.
 class Integrator {
  public:
   using BoundaryCallback = std::function<void(State&, const StepContext&)>;
@@ -127,10 +137,29 @@ class Integrator {
     return dt;
   }
   virtual void set_boundary_callback(BoundaryCallback cb) { boundary_ = std::move(cb); }
+  virtual void set_physics(vibe_gb300_physics_fn fn, void* user) {
+    phys_fn_ = fn;
+    phys_user_ = user;
+    phys_dirty_ = true;
+    phys_ever_ = phys_ever_ || fn != nullptr;
+  }
 
  protected:
+  // the package goes onto a model once per change (installing drops the
+  // step graphs); a removed package is taken off the next state stepped
+  void install_physics(State& s) {
+    if (!phys_dirty_ && phys_model_ == s.model()) return;
+    if (!phys_ever_) return;
+    check(vibe_gb300_set_physics(s.model(), phys_fn_, phys_user_));
+    phys_model_ = s.model();
+    phys_dirty_ = false;
+  }
   IntegratorStats stats_{};
   BoundaryCallback boundary_;
+  vibe_gb300_physics_fn phys_fn_ = nullptr;
+  void* phys_user_ = nullptr;
+  vibe_gb300_model* phys_model_ = nullptr;
+  bool phys_dirty_ = false, phys_ever_ = false;
 };
 
 // RungeKutta3Integrator: SSP-RK3 with n_sub acoustic substeps per stage and
@@ -138,6 +167,7 @@ class Integrator {
 class Rk3Integrator final : public Integrator {
  public:
   void step(State& s, const StepContext& ctx) override {
+    install_physics(s);
     const int rc = vibe_gb300_step(s.model(), ctx.dt, ctx.acoustic_substeps, 1);
     if (rc == VIBE_GB300_ENONFINITE) stats_.diverged = true;
     check(rc);

@@ -2,8 +2,10 @@
 // interfaces of include/vibe_gb300.hpp, the way the reference's own driver
 // uses timeint::Integrator (src/driver/driver.cpp:127-138,288): build a
 // state, step it with the RK3 integrator and the semi-implicit integrator,
-// solve a Helmholtz problem and run the TL/AD dot-product test. It writes the
-// fields it produced to the file named by argv[1] for the test to compare.
+// solve a Helmholtz problem, step a moist state with the Kessler physics
+// package installed through Integrator::set_physics, and run the TL/AD
+// dot-product test. It writes the fields it produced to the file named by
+// argv[1] for the test to compare.
 #include <cstdio>
 #include <cstring>
 #include <vector>
@@ -50,6 +52,16 @@ int main(int argc, char** argv) {
     hz->solve(a, b, f, x);
     dump(x);
     std::printf("helmholtz %s: %d iterations, residual %.3e\n", hz->name(), hz->iterations(), hz->residual());
+
+    vibe_gb300_setup mo = su;
+    mo.moist = 1; mo.qv_surface = 0.025; mo.qv_decay_height = 2500.0;
+    State wet(mo, Precision::FP64);
+    KesslerPhysics kessler;
+    kessler.options.exner_offset = 0;
+    Rk3Integrator rk3w;
+    rk3w.set_physics(kessler.fn(), kessler.user());
+    for (int n = 0; n < 2; ++n) rk3w.step(wet, StepContext::make(dt, 4, wet.time));
+    for (int q : {VIBE_THETA, VIBE_QV, VIBE_QC, VIBE_QR}) dump(wet.field(q));
 
     AcousticSubstepper sub;
     std::printf("acoustic cfl %.6f, substeps for dt=4: %d\n", sub.acoustic_cfl(s, 0.25), sub.required_substeps(s, 4.0));

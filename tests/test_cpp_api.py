@@ -31,4 +31,14 @@ def test_cpp_api_runs_and_matches_python(vg, tmp_path):
         si.si_step(2.0, kind=vg.HZ_VERTICAL_TRIDIAGONAL)
         ref = np.concatenate([m.get(q) for q in range(7)] + [si.get(q) for q in range(7)])
     assert np.array_equal(data[:ref.size], ref)
+    # the moist state stepped with the Kessler package through Integrator::set_physics
+    mo = vg.Setup.defaults(**dict(s.as_dict(), moist=1, qv_surface=0.025, qv_decay_height=2500.0))
+    with vg.Model(mo, vg.FP64) as w:
+        w.set_physics_kessler(vg.Kessler.defaults(exner_offset=0))
+        w.step(1.0, 4, 2)
+        wet = np.concatenate([w.get(q) for q in (4, 6, 7, 8)])
+    ncell = (s.nx + 8) * (s.ny + 8) * (s.nz + 8)  # the Helmholtz solution written before them
+    tail = data[ref.size + ncell:ref.size + ncell + wet.size]
+    assert np.array_equal(tail, wet)
+    assert vg.interior(mo, 7, wet[2 * ncell:3 * ncell]).max() > 0.0  # the scheme condensed
     assert "dot test" in r.stdout
