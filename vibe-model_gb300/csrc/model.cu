@@ -802,9 +802,18 @@ int read_status(vibe_gb300_model* m) {
   return 0;
 }
 
+// the FP32 working copy's targets: moisture species beyond qv only when they
+// are prognostic (no kernel of a dry model reads them)
+WS working_targets(const vibe_gb300_model* m, float* const* w) {
+  WS t = ws_of(w);
+  if (!m->fl.moist)
+    for (int q = QV + 1; q < NSPECIES; ++q) t.f[q] = nullptr;
+  return t;
+}
+
 int sync_working(vibe_gb300_model* m) {
   if (m->precision != VIBE_GB300_MIXED) return 0;
-  mixed_to_working(m->d, m->tab, m->S[m->cur], ws_of(m->W0), m->stream);
+  mixed_to_working(m->d, m->tab, m->S[m->cur], working_targets(m, m->W0), m->stream);
   CUDA_OK(cudaGetLastError());
   return 0;
 }
@@ -1956,7 +1965,7 @@ int nested_transfer(vibe_gb300_nested* n, int op, int c, int pp, int cp) {
 }
 
 void to_working_on(vibe_gb300_nested* n, vibe_gb300_model* m, int parity) {
-  mixed_to_working(m->d, m->tab, m->S[parity], ws_of(m->W0), n->stream);
+  mixed_to_working(m->d, m->tab, m->S[parity], working_targets(m, m->W0), n->stream);
   ++n->launches;
 }
 
@@ -2348,6 +2357,54 @@ int after_upload(vibe_gb300_model* m, const bool* given, int nspecies) {
   return 0;
 }
 
+// mixed models: one pass from the FieldT staging into both FP64 state
+// buffers and the FP32 working copy (the conversion of to_working_body), plus
+// the working copies that hold the species' unwritten points (rho's ghost
+// line and the non-prognostic species: stage outputs and substep buffers)
+__global__ void k_pack_mixed(Dims d, int q, int nsx, int nsy, int ni, int nj, int nk, const double* __restrict__ ref,
+                             const double* __restrict__ src, double* __restrict__ s0, double* __restrict__ s1,
+                             float* __restrict__ w0, float* __restrict__ c0, float* __restrict__ c1,
+                             float* __restrict__ c2, float* __restrict__ c3) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y, k = blockIdx.z;
+  if (i >= ni || j >= nj || k >= nk) return;
+  const size_t c = d.idx(i, j, k);
+  const double v = src[soff(nsx, nsy, i, j, k)];
+  s0[c] = v;
+  s1[c] = v;
+  if (!w0) return;
+  bool put;  // the points to_working_body converts
+  if (q == U) put = j < d.ny && k < d.nz;
+  else if (q == V) put = i < d.nx && k < d.nz;
+  else if (q == W) put = i < d.nx && j < d.ny;
+  else put = k < d.nz;
+  if (!put) return;
+  const float wv = ref ? (float)(v - ref[k]) : (float)v;
+  w0[c] = wv;
+  if (c0) c0[c] = wv;
+  if (c1) c1[c] = wv;
+  if (c2) c2[c] = wv;
+  if (c3) c3[c] = wv;
+}
+
+void pack_mixed(vibe_gb300_model* m, int q, const double* src) {
+  int ni, nj, nk;
+  box_of(m, q, ni, nj, nk);
+  const int last = m->fl.moist ? QG : QV;
+  const double* ref = (q == RHO) ? m->tab.r0d : (q == THETA) ? m->tab.t0dd : (q == PI) ? m->tab.p0d : nullptr;
+  float* w0 = (q > last) ? nullptr : m->W0[q];
+  float *c0 = nullptr, *c1 = nullptr, *c2 = nullptr, *c3 = nullptr;
+  if (q == RHO) {  // after_upload's copies of the working value
+    c0 = m->WSt[0][q];
+    c1 = m->WSt[1][q];
+    c2 = m->WA[q];
+    c3 = m->WB[q];
+  }
+  const dim3 b(32, 4);
+  k_pack_mixed<<<dim3((ni + 31) / 32, (nj + 3) / 4, nk), b, 0, m->stream>>>(m->d, q, m->nsx[q], m->nsy[q], ni, nj, nk,
+                                                                            ref, src, m->S[0][q], m->S[1][q], w0, c0,
+                                                                            c1, c2, c3);
+}
+
 void pack_both(vibe_gb300_model* m, int q, const double* src) {
   int ni, nj, nk;
   box_of(m, q, ni, nj, nk);
@@ -2439,9 +2496,13 @@ int vibe_gb300_step_io(vibe_gb300_model* m, const double* const* host_in, int n_
   }
   CUDA_OK(cudaEventRecord(io->in_done[b], io->sin));
   CUDA_OK(cudaStreamWaitEvent(m->stream, io->in_done[b], 0));
-  for (int q = 0; q < n_in; ++q)
-    if (given[q]) pack_both(m, q, io->in[b][q]);
-  if (int rc = after_upload(m, given, n_in)) return rc;
+  if (m->precision == VIBE_GB300_MIXED) {  // state and working copy in one pass per field
+    for (int q = 0; q < n_in; ++q)
+      if (given[q]) pack_mixed(m, q, io->in[b][q]);
+  } else {
+    for (int q = 0; q < n_in; ++q)
+      if (given[q]) pack_both(m, q, io->in[b][q]);
+  }
   CUDA_OK(cudaEventRecord(io->packed[b], m->stream));
   if (int rc = enqueue_steps(m, dt, n_sub, 1)) return rc;
   CUDA_OK(cudaStreamWaitEvent(m->stream, io->out_done[b], 0));  // the staging buffer was read out

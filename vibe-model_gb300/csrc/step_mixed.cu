@@ -1022,7 +1022,8 @@ __device__ __forceinline__ void to_working_body(const Dims& d, const Tab& t, con
     w.f[RHO][c] = (float)(s.f[RHO][c] - t.r0d[k]);
     w.f[THETA][c] = (float)(s.f[THETA][c] - t.t0dd[k]);
     w.f[PI][c] = (float)(s.f[PI][c] - t.p0d[k]);
-    for (int q = QV; q < NSPECIES; ++q) w.f[q][c] = (float)s.f[q][c];
+    for (int q = QV; q < NSPECIES; ++q)
+      if (w.f[q]) w.f[q][c] = (float)s.f[q][c];  // species without a target are not prognostic
   }
 }
 __global__ void k_mx_to_working(const __grid_constant__ Dims d, const __grid_constant__ Tab t,
