@@ -685,6 +685,7 @@ int enqueue_one_step(vibe_gb300_model* m, double dt, int n_sub) {
     } else {
       const WS w0 = ws_of(m->W0);
       float** final_sub = nullptr;
+      float last_dtau = 0.f;
       for (int stage = 0; stage < 3; ++stage) {
         float** st_out = m->WSt[stage & 1];
         const WS win = (stage == 0) ? w0 : ws_compose(final_sub, m->WSt[(stage - 1) & 1]);
@@ -722,15 +723,18 @@ int enqueue_one_step(vibe_gb300_model* m, double dt, int n_sub) {
           }
           in = out;
         }
-        if (m->fl.acoustic_mode == 2) {  // the last substep's u/v update, in place
+        if (m->fl.acoustic_mode == 2 && stage < 2) {  // the last substep's u/v update, in place
           Span sp(m, 3);
           mixed_uv_backward(d, m->tab, ws_of(in), ws_of(in), dtau, m->stream);
         }
         final_sub = in;
+        last_dtau = dtau;
       }
       Span sp(m, 2);
       const WS wr = ws_of(m->WR);
-      mixed_finish(d, m->tab, m->fl, ws_of(final_sub), ws_of(m->WSt[0]), w0, &wr, dt, S0, S1, m->d_err, m->stream);
+      // stage 3's last u/v update is folded into the finish kernel
+      mixed_finish(d, m->tab, m->fl, ws_of(final_sub), ws_of(m->WSt[0]), w0, &wr, dt, S0, S1, m->d_err, m->stream,
+                   m->fl.acoustic_mode == 2 ? last_dtau : 0.f);
     }
     m->cur = 1 - m->cur;
   }
@@ -2583,7 +2587,7 @@ int vibe_gb300_launches_per_step(const vibe_gb300_model* m, int n_sub) {
   if (!m) return 0;
   n_sub = n_sub > 1 ? n_sub : 1;
   if (m->precision == VIBE_GB300_MIXED)
-    return (m->fl.acoustic_mode == 2) ? 3 * (1 + n_sub + 1) + 1 : 3 * (1 + 2 * n_sub) + 1;
+    return (m->fl.acoustic_mode == 2) ? 3 * (1 + n_sub) + 2 + 1 : 3 * (1 + 2 * n_sub) + 1;  // stage 3's u/v in finish
   const int tend = 4 + ((m->fl.div_damp > 0.0 && m->fl.div_order > 2) ? 1 : 0);
   const int sub = (m->fl.acoustic_mode == 0) ? 2 : (m->fl.acoustic_mode == 1 ? 4 : 2);
   return 3 * (tend + NSPECIES + n_sub * sub + 1) + 1;

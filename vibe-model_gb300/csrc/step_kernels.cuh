@@ -106,9 +106,11 @@ int mixed_hevi_substep(const Dims& d, const Tab& t, const Flags& fl, const WS& w
 int mixed_hevi_column(const Dims& d, const Tab& t, const Flags& fl, const WS& win, const WS& wout, float dtau,
                       const float* lu, bool apply_uv, unsigned* err, cudaStream_t stream);
 void mixed_uv_backward(const Dims& d, const Tab& t, const WS& win, const WS& wout, float dtau, cudaStream_t stream);
+// uv_dtau != 0: also applies the last substep's u/v backward update (the
+// in-place mixed_uv_backward launch is then left out)
 void mixed_finish(const Dims& d, const Tab& t, const Flags& fl, const WS& wfin, const WS& wst, const WS& w0,
                   const WS* rin, double dt, double* const* s0, double* const* s1, unsigned* err,
-                  cudaStream_t stream);
+                  cudaStream_t stream, float uv_dtau = 0.f);
 // ---- several domains per launch (work-list), mixed path, HEVI mode ----
 struct MixedDomain {
   Dims d;

@@ -916,9 +916,12 @@ __device__ __forceinline__ double widen(float f) {
 // added to the FP64 state with one conversion and one FP64 add per field.
 // rin == nullptr: no tendency (single-substep entry points, S1 == S0).
 // Also writes the next step's FP32 working copy W0.
+// uv_dtau != 0: the last substep's u/v backward update (fb_mom_body, u and
+// v) is applied here on the fly instead of by its own in-place launch
 __device__ __forceinline__ void finish_body(const Dims& d, const Tab& t, const Flags& fl, const WS& wfin,
                                             const WS& wst, const WS& w0, const WS& rin, float dtf, const CS64& s0,
-                                            const MS64& s1, unsigned* err, int bx, int by, int bz) {
+                                            const MS64& s1, unsigned* err, int bx, int by, int bz,
+                                            float uv_dtau = 0.f) {
   const int i = bx * blockDim.x + threadIdx.x;
   const int j = by * blockDim.y + threadIdx.y;
   const int k = bz;
@@ -935,7 +938,18 @@ __device__ __forceinline__ void finish_body(const Dims& d, const Tab& t, const F
   bool bad = false;
   auto incr = [&](int q) { return rin.f[q] ? dtf * rin.f[q][c] : 0.f; };
   auto face = [&](int q) {
-    const float wv = wfin.f[q][c];
+    float wv = wfin.f[q][c];
+    if (uv_dtau != 0.f && q != W) {  // as fb_mom_body: k < nz and the face's clamped pi' neighbours
+      const float* __restrict__ pn = wfin.f[PI];
+      const float cp = (float)kCp;
+      if (q == U) {
+        const int ip = imin(i, d.nx - 1), im = imax(i - 1, 0);
+        wv = wv + uv_dtau * (-cp * t.t0c[k] * (pn[IX(ip, j, k)] - pn[IX(im, j, k)]) * t.dx_inv);
+      } else {
+        const int jp = imin(j, d.ny - 1), jm = imax(j - 1, 0);
+        wv = wv + uv_dtau * (-cp * t.t0c[k] * (pn[IX(i, jp, k)] - pn[IX(i, jm, k)]) * t.dy_inv);
+      }
+    }
     const double a = s0.f[q][c] + widen(incr(q) + (wv - wst.f[q][c]));
     const double v = plain ? a : wd * a;
     s1.f[q][c] = v;
@@ -992,8 +1006,8 @@ __global__ void k_mx_finish(const __grid_constant__ Dims d, const __grid_constan
                             const __grid_constant__ Flags fl, const __grid_constant__ WS wfin,
                             const __grid_constant__ WS wst, const __grid_constant__ WS w0,
                             const __grid_constant__ WS rin, float dtf, const __grid_constant__ CS64 s0,
-                            const __grid_constant__ MS64 s1, unsigned* err) {
-  finish_body(d, t, fl, wfin, wst, w0, rin, dtf, s0, s1, err, blockIdx.x, blockIdx.y, blockIdx.z);
+                            const __grid_constant__ MS64 s1, unsigned* err, float uv_dtau) {
+  finish_body(d, t, fl, wfin, wst, w0, rin, dtf, s0, s1, err, blockIdx.x, blockIdx.y, blockIdx.z, uv_dtau);
 }
 
 __global__ void k_mx_unpack_f32(Dims d, int nsx, int nsy, int nsz, int ni, int nj, int nk, const float* __restrict__ src,
@@ -2100,12 +2114,12 @@ int mixed_hevi_substep(const Dims& d, const Tab& t, const Flags& fl, const WS& w
 
 void mixed_finish(const Dims& d, const Tab& t, const Flags& fl, const WS& wfin, const WS& wst, const WS& w0,
                   const WS* rin, double dt, double* const* s0, double* const* s1, unsigned* err,
-                  cudaStream_t stream) {
+                  cudaStream_t stream, float uv_dtau) {
   const dim3 b(32, 4);
   WS none;
   for (int q = 0; q < NSPECIES; ++q) none.f[q] = nullptr;
   k_mx_finish<<<g3(d.nx + 1, d.ny + 1, d.nz + 1, b), b, 0, stream>>>(d, t, fl, wfin, wst, w0, rin ? *rin : none,
-                                                                     (float)dt, cs64(s0), ms64(s1), err);
+                                                                     (float)dt, cs64(s0), ms64(s1), err, uv_dtau);
 }
 
 void mixed_unpack_f32(const Dims& d, int nsx, int nsy, int nsz, int ni, int nj, int nk, const float* src, double* dst,
