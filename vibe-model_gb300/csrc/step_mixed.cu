@@ -1459,13 +1459,9 @@ __global__ void __launch_bounds__(128, 7) k_mx_hevi_col2(const __grid_constant__
 // clamped neighbour offsets of hevi2_body select in-range box points. Waits
 // are bounded; a box that does not arrive sets kErrWaitTimeout, and the block
 // waits (bounded) for its copies in flight before it returns.
-__global__ void __launch_bounds__(128, 7) k_mx_hevi_tma(const __grid_constant__ Dims d, const __grid_constant__ Tab t,
-                                                         const __grid_constant__ Flags fl,
-                                                         const __grid_constant__ ColumnMaps C,
-                                                         const __grid_constant__ WS win,
-                                                         const __grid_constant__ WS wout, float dtau,
-                                                         const float* __restrict__ lu, int apply_uv, float cdx,
-                                                         float cdy, unsigned* err) {
+__device__ __forceinline__ void hevi_tma_body(const Dims& d, const Tab& t, const Flags& fl, const ColumnMaps& C,
+                                              const WS& win, const WS& wout, float dtau, const float* __restrict__ lu,
+                                              int apply_uv, float cdx, float cdy, unsigned* err, int bx, int by) {
   extern __shared__ float s_dyn[];
   __shared__ __align__(8) unsigned long long bar[kColRing], bbar[kColRing];
   const int nz = d.nz;
@@ -1482,7 +1478,7 @@ __global__ void __launch_bounds__(128, 7) k_mx_hevi_tma(const __grid_constant__ 
   float* s_r0 = s_li + nz;                            // nz
   float* s_t0 = s_r0 + nz;                            // nz
   const int tid = threadIdx.y * blockDim.x + threadIdx.x;
-  const int i0 = blockIdx.x * 64, j0 = blockIdx.y * 4;
+  const int i0 = bx * 64, j0 = by * 4;
   auto issue = [&](int L) {  // one thread: level L (0..nz) into its slot
     float* s = ring + (size_t)(L % kColRing) * kColSlot;
     unsigned long long* b = &bar[L % kColRing];
@@ -1714,6 +1710,16 @@ __global__ void __launch_bounds__(128, 7) k_mx_hevi_tma(const __grid_constant__ 
       wu[c] = wkk[c];
     }
   }
+}
+
+__global__ void __launch_bounds__(128, 7) k_mx_hevi_tma(const __grid_constant__ Dims d, const __grid_constant__ Tab t,
+                                                         const __grid_constant__ Flags fl,
+                                                         const __grid_constant__ ColumnMaps C,
+                                                         const __grid_constant__ WS win,
+                                                         const __grid_constant__ WS wout, float dtau,
+                                                         const float* __restrict__ lu, int apply_uv, float cdx,
+                                                         float cdy, unsigned* err) {
+  hevi_tma_body(d, t, fl, C, win, wout, dtau, lu, apply_uv, cdx, cdy, err, blockIdx.x, blockIdx.y);
 }
 
 size_t hevi_tma_smem_bytes(int nz) {
@@ -2149,7 +2155,8 @@ struct StageArgs {  // 64-byte aligned through its CUtensorMap members
   float dts;
   int kchunk, gx, gy, gz;
 };
-struct HeviArgs {
+struct HeviArgs {  // 64-byte aligned through its CUtensorMap members
+  ColumnMaps C;     // boxes of the TMA-fed body (unused by the cp.async body)
   Dims d;
   Tab t;
   Flags fl;
@@ -2201,6 +2208,15 @@ __global__ void __launch_bounds__(128, 7) k_b_hevi(const HeviArgs* __restrict__ 
                             l / a.gx);
 }
 
+__global__ void __launch_bounds__(128, 7) k_b_hevi_tma(const HeviArgs* __restrict__ A, const int* __restrict__ start,
+                                                       int nd, unsigned* err) {
+  const int dom = find_domain(start, nd);
+  const HeviArgs& a = A[dom];
+  const int l = (int)blockIdx.x - start[dom];
+  hevi_tma_body(a.d, a.t, a.fl, a.C, a.win, a.wout, a.dtau, a.lu, a.apply_uv, a.cdx, a.cdy, err, l % a.gx,
+                l / a.gx);
+}
+
 __global__ void k_b_uv(const UvArgs* __restrict__ A, const int* __restrict__ start, int nd) {
   const int dom = find_domain(start, nd);
   const UvArgs& a = A[dom];
@@ -2239,6 +2255,7 @@ struct MixedBatch {
   std::vector<Launch> seq;
   std::vector<void*> allocs;
   size_t hevi_smem = 0;
+  bool hevi_tma = false;  // TMA-fed column body (else the cp.async two-column body)
   unsigned* err = nullptr;
 };
 
@@ -2272,7 +2289,8 @@ MixedBatch* mixed_batch_build(const std::vector<MixedDomain>& doms, const Flags&
     if (m.d.nz != nz) return nullptr;
   auto* b = new MixedBatch();
   b->err = err;
-  b->hevi_smem = hevi2_smem_bytes(nz, kBatchTwoRing);
+  b->hevi_tma = hevi_tma() && hevi_tma_smem_bytes(nz) <= 48 * 1024;
+  b->hevi_smem = b->hevi_tma ? hevi_tma_smem_bytes(nz) : hevi2_smem_bytes(nz, kBatchTwoRing);
   const double dts[3] = {dt / 3.0, dt / 2.0, dt};
   const int nd = (int)doms.size();
   auto sub_out = [&](const MixedDomain& m, int n) { return (n & 1) ? m.WB : m.WA; };
@@ -2322,12 +2340,13 @@ MixedBatch* mixed_batch_build(const std::vector<MixedDomain>& doms, const Flags&
         a.cdy = -(float)kCp * dtau * m.t.dy_inv;
         a.lu = m.lu + (size_t)stage * 3 * nz;
         a.apply_uv = n > 0;
+        if (b->hevi_tma && !column_maps(m.d, a.win, a.wout, a.C)) ok = false;
         a.gx = ceil_div(m.d.nx, 64);  // two columns per thread
         a.gy = ceil_div(m.d.ny, 4);
         start[q] = hb;
         hb += a.gx * a.gy;
       }
-      ok = upload_launch(b, 1, 0, ha, start, hb);
+      ok = ok && upload_launch(b, 1, 0, ha, start, hb);
     }
     std::vector<UvArgs> ua(nd);
     int ub = 0;
@@ -2389,7 +2408,10 @@ void mixed_batch_enqueue(const MixedBatch* b, cudaStream_t s) {
           k_b_stage<false><<<L.blocks, dim3(TX, TY), 0, s>>>((const StageArgs*)L.args, L.start, L.nd, b->err);
         break;
       case 1:
-        k_b_hevi<<<L.blocks, dim3(32, 4), b->hevi_smem, s>>>((const HeviArgs*)L.args, L.start, L.nd);
+        if (b->hevi_tma)
+          k_b_hevi_tma<<<L.blocks, dim3(32, 4), b->hevi_smem, s>>>((const HeviArgs*)L.args, L.start, L.nd, b->err);
+        else
+          k_b_hevi<<<L.blocks, dim3(32, 4), b->hevi_smem, s>>>((const HeviArgs*)L.args, L.start, L.nd);
         break;
       case 2:
         k_b_uv<<<L.blocks, dim3(32, 4), 0, s>>>((const UvArgs*)L.args, L.start, L.nd);
