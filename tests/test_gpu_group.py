@@ -37,7 +37,7 @@ def test_group_step_equals_individual_steps(vg, sizes):
     try:
         with vg.Group(grouped) as g:
             g.step(2.0, 6, 3)
-            assert g.launches_per_step() == 3 * (1 + 6 + 1) + 1
+            assert g.launches_per_step() == 3 * (1 + 6) + 2 + 1  # stage 3's u/v update is in the finish
             g.step(2.0, 6, 2)
         for m in single:
             m.step(2.0, 6, 5)

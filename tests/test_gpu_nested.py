@@ -119,7 +119,7 @@ def test_nested_step_equals_composition(vg, oc):
             n.step_async(DT, NSUB, 1)
             n.wait()
             per_nest = 1 + 2 * R + 1
-            group = 3 * (1 + NSUB + 1) + 1
+            group = 3 * (1 + NSUB) + 2 + 1  # stage 3's u/v update is in the finish
             assert n.launches_per_step() == group + R * group + len(shapes) * per_nest + 2
         nests = [(c, s, pi, i, r) for c, (s, pi, i, r) in zip(b_c, shapes)]
         for _ in range(2):

@@ -2177,7 +2177,7 @@ struct FinishArgs {
   Tab t;
   Flags fl;
   WS wfin, wst, w0, rin;
-  float dtf;
+  float dtf, uv_dtau;  // uv_dtau: stage 3's last u/v update, applied in the finish
   CS64 s0;
   MS64 s1;
   int gx, gy, gz;
@@ -2229,7 +2229,7 @@ __global__ void k_b_finish(const FinishArgs* __restrict__ A, const int* __restri
   const FinishArgs& a = A[dom];
   const int l = (int)blockIdx.x - start[dom];
   finish_body(a.d, a.t, a.fl, a.wfin, a.wst, a.w0, a.rin, a.dtf, a.s0, a.s1, err, l % a.gx, (l / a.gx) % a.gy,
-              l / (a.gx * a.gy));
+              l / (a.gx * a.gy), a.uv_dtau);
 }
 
 WS ws_from(float* const* a) {
@@ -2348,6 +2348,7 @@ MixedBatch* mixed_batch_build(const std::vector<MixedDomain>& doms, const Flags&
       }
       ok = ok && upload_launch(b, 1, 0, ha, start, hb);
     }
+    if (stage == 2) break;  // stage 3's last u/v update happens in the finish
     std::vector<UvArgs> ua(nd);
     int ub = 0;
     for (int q = 0; q < nd; ++q) {
@@ -2381,6 +2382,7 @@ MixedBatch* mixed_batch_build(const std::vector<MixedDomain>& doms, const Flags&
       a.w0 = ws_from(m.W0);
       a.rin = ws_from(m.WR);
       a.dtf = (float)dt;
+      a.uv_dtau = (float)(dt / (double)n_sub);
       a.s0 = cs64(m.S0);
       a.s1 = ms64(m.S1);
       a.gx = ceil_div(m.d.nx + 1, 32);
