@@ -51,3 +51,36 @@ def test_config1_100_steps(vg, oc):
             err = errors(vg, s, m.state(), ref)
             print("config 1, precision %d, max/rms relative error after %d steps: %s" % (prec, STEPS, err))
             assert all(e[0] <= tol for e in err.values()), err
+
+
+def test_config1_reference_composition_until_it_diverges(vg, oc):
+    """O-RK3 as the reference writes it (every composition flag 0, 2nd-order
+    advection, explicit substeps) on the same case: it stays finite for 6
+    steps and is non-finite at the 7th, as the reference is. All 12 fields:
+    the FMA-free build bit for bit after 5 steps; the FP64 path within 1e-11
+    after 2 steps (the growing mode amplifies FMA rounding differences after
+    that)."""
+    s = config1(vg)
+    for name, v in dict(advection=2, weno_scalars=0, weno_advective=0, pgf_perturbation=0, split_fast=0).items():
+        setattr(s, name, v)
+    t = oc.Setup()
+    for name, _ in oc.Setup._fields_:
+        setattr(t, name, getattr(s, name))
+    o = oc.Model(t, "port")
+    for _ in range(2):
+        assert o.rk3_step(2.0, 6) == 0
+    ref2 = [o.get(q) for q in range(12)]
+    for _ in range(3):
+        assert o.rk3_step(2.0, 6) == 0
+    ref = [o.get(q) for q in range(12)]
+    with vg.Model(s, vg.FP64_EXACT) as m:
+        m.step(2.0, 6, 5)
+        for q, a in enumerate(m.state()):
+            assert np.array_equal(vg.interior(s, q, a), vg.interior(s, q, ref[q])), vg.SPECIES[q]
+    with vg.Model(s, vg.FP64) as m:
+        m.step(2.0, 6, 2)
+        got = m.state()
+        for q in range(12):
+            r = vg.interior(s, q, ref2[q])
+            scale = max(float(np.abs(r).max()), 1e-300)
+            assert np.abs(vg.interior(s, q, got[q]) - r).max() <= 1e-11 * scale, vg.SPECIES[q]
