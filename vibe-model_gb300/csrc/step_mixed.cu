@@ -311,7 +311,10 @@ __device__ __forceinline__ void stage_body(const Dims& d, const Tab& t, const Fl
         }
       }
     }
-    const bool arrived = mbar_wait_bounded(&sbar[cur], (lev >> 1) & 1);
+    // one thread polls the level's mbarrier; the block barrier below then
+    // orders the boxes' contents for every thread (the others wait there
+    // without issuing)
+    const bool arrived = (tid != 0) || mbar_wait_bounded(&sbar[cur], (lev >> 1) & 1);
     if (__syncthreads_or(!arrived)) {
       // a box did not arrive: report, and leave none in flight before exiting
       if (tid == 0) {
@@ -1517,7 +1520,7 @@ __device__ __forceinline__ void hevi_tma_body(const Dims& d, const Tab& t, const
   // the copies still in flight (levels L..hi) and the block returns
   int hi = imin(kColRing - 1, nz);  // highest level issued
   auto level_ready = [&](int L) -> bool {
-    const bool ok = mbar_wait_bounded(&bar[L % kColRing], (unsigned)(L / kColRing) & 1u);
+    const bool ok = (tid != 0) || mbar_wait_bounded(&bar[L % kColRing], (unsigned)(L / kColRing) & 1u);
     if (__syncthreads_or(!ok)) {
       if (tid == 0) {
         atomicOr(err, (unsigned)kErrWaitTimeout);
@@ -1657,7 +1660,7 @@ __device__ __forceinline__ void hevi_tma_body(const Dims& d, const Tab& t, const
   if (tid == 0)
     for (int n = 0; n <= bhi; ++n) issue_b(n);
   auto back_ready = [&](int n) -> bool {
-    const bool ok = mbar_wait_bounded(&bbar[n % kColRing], (unsigned)(n / kColRing) & 1u);
+    const bool ok = (tid != 0) || mbar_wait_bounded(&bbar[n % kColRing], (unsigned)(n / kColRing) & 1u);
     if (__syncthreads_or(!ok)) {
       if (tid == 0) {
         atomicOr(err, (unsigned)kErrWaitTimeout);
