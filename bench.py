@@ -453,6 +453,28 @@ def cpu_sample_run(args):
     return nx * ny * NZ * steps, time.perf_counter() - t0
 
 
+# The CPU-runnable warm-bubble case (64 x 64 x 40, dx = dy = dz = 250 m,
+# +2 K bubble of 2 km radius at (8, 8, 2) km, WENO5 scalars, dt = 2 s, 6
+# substeps): its single-core oracle rate is reported beside the bench line.
+CONFIG1 = dict(nx=64, ny=64, nz=40, dx=250.0, dy=250.0, z_top=10000.0, zeta_first=1.0, zeta_stretch=1.0,
+               ref_kind=0, theta0=300.0, p_surf=100000.0, bubble_amplitude=2.0, bubble_radius_x=2000.0,
+               bubble_radius_z=2000.0, bubble_xc=8000.0, bubble_yc=8000.0, bubble_zc=2000.0, qv_surface=0.0,
+               advection=5, weno_scalars=1, weno_advective=1, pgf_perturbation=1, split_fast=1, acoustic_mode=0,
+               u_background=0.0, shear_u=0.0)
+
+
+def cpu_config1_run(steps=3):
+    oc = _oracle()
+    s = oc.defaults()
+    for k, v in CONFIG1.items():
+        setattr(s, k, v)
+    m = oc.Model(s, "port")
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        m.rk3_step(2.0, 6)
+    return 64 * 64 * 40 * steps, time.perf_counter() - t0
+
+
 def reference_arm(args):
     import multiprocessing as mp
     cores = os.cpu_count() or 1
@@ -561,6 +583,9 @@ def main():
         cells, secs = cpu_sample_run((128, 128, 2, 0, 1))
         cpu = {"value": cells / secs, "unit": UNIT, "cores": 1, "kind": "port",
                "sample": "128x128x80 horizontal sample of the workload, 2 RK3 steps, single thread (%.1f s)" % secs}
+        c1, s1 = cpu_config1_run()
+        cpu["warm_bubble_64x64x40"] = {"value": c1 / s1, "unit": UNIT, "cores": 1,
+                                       "sample": "3 RK3 steps (dt 2 s, 6 substeps), single thread (%.1f s)" % s1}
 
     import torch
     torch.cuda.set_device(local)
