@@ -274,8 +274,13 @@ typedef struct {
   const double *terrain;                      /* device, nx*ny row-major: terrain height */
   const double *depth;                        /* device, nx*ny: z_top - terrain height */
   void *stream;                               /* cudaStream_t */
+  /* in/out: bit q set = the package may write tend[q]. It comes in with all
+   * nine accumulators; a package that writes fewer clears the others' bits,
+   * and only those accumulators are zeroed before its next call and added to
+   * the tendency (the rest stay zero). */
+  unsigned written;
 } vibe_gb300_physics_args;
-typedef int (*vibe_gb300_physics_fn)(void *user, const vibe_gb300_physics_args *args);
+typedef int (*vibe_gb300_physics_fn)(void *user, vibe_gb300_physics_args *args);
 /* Install (fn != NULL) or remove the package; drops the step graphs. */
 int vibe_gb300_set_physics(vibe_gb300_model *m, vibe_gb300_physics_fn fn, void *user);
 /* The installed package's tendency for the current state (one call as at
@@ -299,7 +304,7 @@ typedef struct {
   int exner_offset;
 } vibe_gb300_kessler;
 void vibe_gb300_kessler_defaults(vibe_gb300_kessler *k);
-int vibe_gb300_physics_kessler(void *user, const vibe_gb300_physics_args *args);
+int vibe_gb300_physics_kessler(void *user, vibe_gb300_physics_args *args);
 /* One step with host input and output (FieldT storage, pinned host memory
  * for full speed), asynchronous and pipelined across calls: the call
  * enqueues the input's host -> device copies on a copy stream, the step on

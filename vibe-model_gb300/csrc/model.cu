@@ -82,6 +82,7 @@ struct vibe_gb300_model {
   // physics package (vibe_gb300_set_physics) and its tendency accumulators
   vibe_gb300_physics_fn phys_fn = nullptr;
   void* phys_user = nullptr;
+  unsigned phys_written = 0;  // accumulators the package wrote in its last call (they need zeroing)
   void* pt[NSPECIES] = {};  // u, v, theta, qv..qg: double (FP64) or float (mixed)
   double* d_zmid = nullptr;
   double* d_zs = nullptr;
@@ -625,10 +626,13 @@ int physics_stage(vibe_gb300_model* m, int stage, double dt, const void* const* 
   a.pitch = m->d.P;
   a.moist = m->fl.moist ? 1 : 0;
   for (int q = 0; q < NSPECIES; ++q) a.state[q] = state[q];
+  unsigned all = 0;
   for (int q : kPhysFields) {
-    CUDA_OK(cudaMemsetAsync(m->pt[q], 0, n * es, m->stream));
+    all |= 1u << q;
+    if (m->phys_written & (1u << q)) CUDA_OK(cudaMemsetAsync(m->pt[q], 0, n * es, m->stream));
     a.tend[q] = m->pt[q];
   }
+  a.written = all;
   a.ref_theta = m->d_th0;
   a.ref_pi = m->d_pi0;
   a.ref_rho = m->d_rho0;
@@ -638,6 +642,7 @@ int physics_stage(vibe_gb300_model* m, int stage, double dt, const void* const* 
   a.stream = m->stream;
   if (int rc = m->phys_fn(m->phys_user, &a)) return fail(rc < 0 ? rc : VIBE_GB300_EDEVICE, "physics package failed");
   CUDA_OK(cudaGetLastError());
+  m->phys_written = a.written & all;
   return 0;
 }
 
@@ -658,7 +663,8 @@ int enqueue_one_step(vibe_gb300_model* m, double dt, int n_sub) {
             if (int rc = physics_stage(m, stage, dt, (const void* const*)src)) return rc;
             const size_t n = d.plane * (size_t)(d.nz + 1);
             for (int q : kPhysFields)
-              k_add_pt64<<<1024, 256, 0, m->stream>>>(n, (const double*)m->pt[q], m->tend[q]);
+              if (m->phys_written & (1u << q))
+                k_add_pt64<<<1024, 256, 0, m->stream>>>(n, (const double*)m->pt[q], m->tend[q]);
           }
           m->f64->stage_update(d, S0, m->tend, dts[stage], S1, m->stream);
         }
@@ -703,8 +709,9 @@ int enqueue_one_step(vibe_gb300_model* m, double dt, int n_sub) {
           if (m->phys_fn) {
             const size_t n = d.plane * (size_t)(d.nz + 1);
             for (int q : kPhysFields)
-              k_add_pt32<<<1024, 256, 0, m->stream>>>(n, (const float*)m->pt[q], st_out[q], (float)dts[stage],
-                                                      stage == 2 ? m->WR[q] : nullptr);
+              if (m->phys_written & (1u << q))
+                k_add_pt32<<<1024, 256, 0, m->stream>>>(n, (const float*)m->pt[q], st_out[q], (float)dts[stage],
+                                                        stage == 2 ? m->WR[q] : nullptr);
           }
         }
         const float dtau = (float)(dts[stage] / (double)n_sub);
@@ -1300,8 +1307,17 @@ int vibe_gb300_set_physics(vibe_gb300_model* m, vibe_gb300_physics_fn fn, void* 
                             m->stream));
     CUDA_OK(cudaStreamSynchronize(m->stream));
   }
+  // accumulators a package may have written are zero again before the next one's first call
+  if (m->pt[THETA] && m->phys_written) {
+    const size_t n = m->d.plane * (size_t)(m->d.nz + 1);
+    const size_t es = m->precision == VIBE_GB300_MIXED ? sizeof(float) : sizeof(double);
+    for (int q : kPhysFields)
+      if (m->phys_written & (1u << q)) CUDA_OK(cudaMemsetAsync(m->pt[q], 0, n * es, m->stream));
+    CUDA_OK(cudaStreamSynchronize(m->stream));
+  }
   m->phys_fn = fn;
   m->phys_user = user;
+  m->phys_written = 0;
   drop_graphs(m);
   return 0;
 }

@@ -42,12 +42,16 @@ struct KesslerParams {
 template <class R> __device__ __forceinline__ R rmax(R a, R b) { return a < b ? b : a; }  // std::max
 template <class R> __device__ __forceinline__ R rmin(R a, R b) { return b < a ? b : a; }  // std::min
 template <class R> __device__ __forceinline__ R rclamp(R v, R lo, R hi) { return v < lo ? lo : (hi < v ? hi : v); }
+// FP64 models: the library functions (the reference's libm calls to an ulp
+// or two). Mixed models: the FP32 hardware approximations, whose relative
+// error (a few 1e-6 for these arguments) is far inside the FP32 path's
+// tolerance against the FP64 scheme.
 __device__ __forceinline__ double rpow(double a, double b) { return pow(a, b); }
-__device__ __forceinline__ float rpow(float a, float b) { return powf(a, b); }
+__device__ __forceinline__ float rpow(float a, float b) { return __powf(a, b); }
 __device__ __forceinline__ double rexp(double a) { return exp(a); }
 __device__ __forceinline__ double rabs(double a) { return fabs(a); }
 __device__ __forceinline__ float rabs(float a) { return fabsf(a); }
-__device__ __forceinline__ float rexp(float a) { return expf(a); }
+__device__ __forceinline__ float rexp(float a) { return __expf(a); }
 
 template <class R> __device__ __forceinline__ R exner_of(R p) { return rpow(p / (R)kP0, (R)kKappaPhys); }
 template <class R> __device__ __forceinline__ R latent_v(R t) { return ((R)2.501 - (R)0.00237 * (t - (R)kT0)) * (R)1.0e6; }
@@ -277,7 +281,7 @@ void vibe_gb300_kessler_defaults(vibe_gb300_kessler* k) {  // PhysicsOptions, ph
   k->exner_offset = 1;
 }
 
-int vibe_gb300_physics_kessler(void* user, const vibe_gb300_physics_args* a) {
+int vibe_gb300_physics_kessler(void* user, vibe_gb300_physics_args* a) {
   if (!user || !a || a->nx <= 0 || a->ny <= 0 || a->nz <= 0) return VIBE_GB300_EBADARG;
   if (!a->moist) return VIBE_GB300_EUNSUPPORTED;  // qc and qr must be prognostic
   for (int q : {THETA, PI, RHO, QV, QC, QR, QI, QS, QG})
@@ -287,6 +291,7 @@ int vibe_gb300_physics_kessler(void* user, const vibe_gb300_physics_args* a) {
   const vibe_gb300_kessler& k = *static_cast<const vibe_gb300_kessler*>(user);
   const dim3 b(32, 4), g((a->nx + 31) / 32, (a->ny + 3) / 4);
   cudaStream_t s = static_cast<cudaStream_t>(a->stream);
+  a->written = (1u << THETA) | (1u << QV) | (1u << QC) | (1u << QR);
   if (a->precision == VIBE_GB300_MIXED) k_kessler<float, float><<<g, b, 0, s>>>(*a, params_of<float>(k));
   else k_kessler<double, double><<<g, b, 0, s>>>(*a, params_of<double>(k));
   return cudaGetLastError() == cudaSuccess ? 0 : VIBE_GB300_EDEVICE;
