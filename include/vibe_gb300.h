@@ -222,6 +222,14 @@ int vibe_gb300_acoustic_substep(vibe_gb300_model *m, double dtau);
  * pass through unchanged. */
 int vibe_gb300_acoustic_tl(vibe_gb300_model *m, double dtau, int n_sub, const double *const *in, double *const *out);
 int vibe_gb300_acoustic_ad(vibe_gb300_model *m, double dtau, int n_sub, const double *const *in, double *const *out);
+/* The same pair for the dimensionally consistent HEVI substep (the
+ * vertically implicit Crank-Nicolson substep with the model's hevi_beta and
+ * the horizontal u/v backward update), also linear about the reference state
+ * with the gradient of pi itself; the adjoint transposes the column system.
+ * As the model's own substep does, it sets the ghost column i = nx and row
+ * j = ny of w, rho and pi to zero. */
+int vibe_gb300_hevi_tl(vibe_gb300_model *m, double dtau, int n_sub, const double *const *in, double *const *out);
+int vibe_gb300_hevi_ad(vibe_gb300_model *m, double dtau, int n_sub, const double *const *in, double *const *out);
 int vibe_gb300_hevi_substep(vibe_gb300_model *m, double dtau);
 /* Autotuner of the mixed step: times, on this model's grid, the launch shapes
  * of the same update -- the HEVI column kernel variant (0 register ring,

@@ -155,3 +155,71 @@ def test_bad_arguments(vg):
             m.acoustic_tl(0.5, 1, [f[0][:-1]] + f[1:])
         with pytest.raises(RuntimeError):
             m.acoustic_tl(0.5, -1, f)
+
+
+# ---- the consistent HEVI substep (vibe_gb300_hevi_tl / _ad) ----------------
+def test_hevi_tl_is_the_substep_on_the_perturbation(vg):
+    """With pgf_perturbation=0 the model's own consistent HEVI substep (column
+    solve + u/v update) is linear: on the perturbation it gives the TL's
+    bits."""
+    s = setup(vg, pgf_perturbation=0, acoustic_mode=2, hevi_beta=0.6)
+    with vg.Model(s, vg.FP64) as m:
+        dx = random_fields(vg, m, 21)
+        got = m.hevi_tl(0.8, 3, dx)
+        st = m.state()
+        for f, sp in enumerate(FIELDS):
+            st[sp] = dx[f]
+        m.set_state(st)
+        for _ in range(3):
+            m.hevi_substep(0.8)
+        ref = m.state()
+        for f, sp in enumerate(FIELDS):
+            assert np.array_equal(vg.interior(s, sp, got[f]), vg.interior(s, sp, ref[sp])), vg.SPECIES[sp]
+
+
+@pytest.mark.parametrize("prec", ["FP64", "MIXED"])
+def test_hevi_dot_product(vg, prec):
+    """<TL dx, dy> = <dx, AD dy> over 4 HEVI substeps to 1e-12, with terrain
+    (FP64 model) and on the mixed model's flat grid; points outside the boxes
+    pass through."""
+    kw = dict(terrain_kind=0, ref_kind=0) if prec == "MIXED" else {}
+    s = setup(vg, acoustic_mode=2, hevi_beta=0.6, **kw)
+    with vg.Model(s, getattr(vg, prec)) as m:
+        for seed in (23, 24):
+            dx, dy = random_fields(vg, m, seed), random_fields(vg, m, seed + 10)
+            tdx = m.hevi_tl(1.5, 4, dx)
+            ady = m.hevi_ad(1.5, 4, dy)
+            lhs, rhs = dot(tdx, dy), dot(dx, ady)
+            assert abs(lhs - rhs) <= 1e-12 * max(abs(lhs), abs(rhs)), (lhs, rhs)
+            for f, sp in enumerate(FIELDS):
+                keep = np.ones(m.size(sp), bool)
+                box(vg, s, sp, keep)[...] = False
+                assert np.array_equal(tdx[f][keep], dx[f][keep])
+                assert np.array_equal(ady[f][keep], dy[f][keep])
+
+
+def test_hevi_adjoint_is_the_transposed_matrix(vg):
+    """3 x 2 x 3 grid with terrain: the HEVI AD of each unit vector is the
+    corresponding row of the HEVI TL matrix (to 1e-13 of the largest entry)."""
+    s = setup(vg, nx=3, ny=2, nz=3, dx=500.0, dy=500.0, hill_xc=700.0, hill_yc=500.0, hill_a=600.0,
+              bubble_xc=700.0, bubble_yc=500.0, bubble_radius_x=600.0, acoustic_mode=2, hevi_beta=0.6)
+    with vg.Model(s, vg.FP64) as m:
+        pts = []
+        for f, sp in enumerate(FIELDS):
+            idx = np.arange(m.size(sp))
+            pts += [(f, int(e)) for e in box(vg, s, sp, idx).ravel()]
+        zero = [np.zeros(m.size(sp)) for sp in FIELDS]
+
+        def unit(p):
+            u = [a.copy() for a in zero]
+            u[p[0]][p[1]] = 1.0
+            return u
+
+        def row(fields):
+            return np.array([fields[f][e] for f, e in pts])
+
+        tl = np.array([row(m.hevi_tl(2.0, 2, unit(p))) for p in pts]).T
+        ad = np.array([row(m.hevi_ad(2.0, 2, unit(p))) for p in pts]).T
+        scale = np.abs(tl).max()
+        assert np.abs(ad - tl.T).max() <= 1e-13 * scale, np.abs(ad - tl.T).max() / scale
+        assert np.count_nonzero(tl - np.eye(len(pts))) > len(pts)

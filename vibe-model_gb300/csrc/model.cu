@@ -53,12 +53,14 @@ struct Fp64Ops {
   decltype(&fp64_sponge) sponge;
   decltype(&fp64_nonfinite) nonfinite;
   decltype(&fp64_fb_substep_ad) fb_substep_ad;
+  decltype(&fp64_hevi_substep_ad) hevi_substep_ad;
 };
 static const Fp64Ops kFp64Fast = {fp64_slow_tendency, fp64_stage_update, fp64_fb_substep, fp64_ref_hevi_substep,
-                                  fp64_cons_hevi_substep, fp64_sponge, fp64_nonfinite, fp64_fb_substep_ad};
+                                  fp64_cons_hevi_substep, fp64_sponge, fp64_nonfinite, fp64_fb_substep_ad,
+                                  fp64_hevi_substep_ad};
 static const Fp64Ops kFp64Exact = {fp64_slow_tendency_exact, fp64_stage_update_exact, fp64_fb_substep_exact,
                                    fp64_ref_hevi_substep_exact, fp64_cons_hevi_substep_exact, fp64_sponge_exact,
-                                   fp64_nonfinite_exact, fp64_fb_substep_ad_exact};
+                                   fp64_nonfinite_exact, fp64_fb_substep_ad_exact, fp64_hevi_substep_ad_exact};
 
 struct vibe_gb300_model {
   vibe_gb300_setup su{};
@@ -79,6 +81,9 @@ struct vibe_gb300_model {
   double* tend[NSPECIES] = {};
   double* tmp[NSPECIES] = {};
   double* lin[5] = {};  // u, v, w, rho, pi perturbations of the acoustic TL/AD (allocated on first use)
+  double* lin_tmp[3] = {};         // HEVI TL: the column solve's w, rho, pi outputs
+  double* lin_scr = nullptr;       // HEVI TL/AD: per-column work
+  double* lin_dh = nullptr;        // HEVI AD: bar of the horizontal divergence
   // physics package (vibe_gb300_set_physics) and its tendency accumulators
   vibe_gb300_physics_fn phys_fn = nullptr;
   void* phys_user = nullptr;
@@ -1129,15 +1134,23 @@ __global__ void k_scatter(Dims d, int nsx, int nsy, int ni, int nj, int nk, cons
 namespace {
 constexpr int kLinField[5] = {U, V, W, RHO, PI};
 
+// hevi: the consistent HEVI substep (k_chevi_column + k_uv_backward) instead
+// of the explicit forward-backward one
 int acoustic_linear(vibe_gb300_model* m, double dtau, int n_sub, const double* const* in, double* const* out,
-                    bool adjoint) {
+                    bool adjoint, bool hevi = false) {
   if (!m || !in || !out || n_sub < 0) return fail(VIBE_GB300_EBADARG, "bad argument");
   for (int f = 0; f < 5; ++f)
     if (!in[f] || !out[f]) return fail(VIBE_GB300_EBADARG, "bad argument");
+  const size_t nfield = m->d.plane * (size_t)(m->d.nz + 1);
   if (!m->lin[0]) {
-    const size_t nfield = m->d.plane * (size_t)(m->d.nz + 1);
     for (int f = 0; f < 5; ++f)
       if (int rc = dalloc(m, &m->lin[f], nfield)) return rc;
+  }
+  if (hevi && !m->lin_scr) {
+    for (int f = 0; f < 3; ++f)
+      if (int rc = dalloc(m, &m->lin_tmp[f], nfield)) return rc;
+    if (int rc = dalloc(m, &m->lin_dh, nfield)) return rc;
+    if (int rc = dalloc(m, &m->lin_scr, (size_t)m->d.nx * m->d.ny * (5 * (size_t)m->d.nz + 2))) return rc;
   }
   double* st[NSPECIES] = {};  // the substep kernels see the perturbation as their state
   for (int f = 0; f < 5; ++f) {
@@ -1146,9 +1159,18 @@ int acoustic_linear(vibe_gb300_model* m, double dtau, int n_sub, const double* c
   }
   Flags lf = m->fl;
   lf.pgf_pert = 0;  // gradient of pi' itself: the substep is linear
+  double* tmp[NSPECIES] = {};
+  tmp[W] = m->lin_tmp[0];
+  tmp[RHO] = m->lin_tmp[1];
+  tmp[PI] = m->lin_tmp[2];
   for (int n = 0; n < n_sub; ++n) {
-    if (adjoint) m->f64->fb_substep_ad(m->d, m->met, st, dtau, m->stream);
-    else m->f64->fb_substep(m->d, m->met, lf, st, dtau, m->stream);
+    if (hevi) {
+      if (adjoint) m->f64->hevi_substep_ad(m->d, m->met, lf, st, m->lin_dh, m->lin_scr, dtau, m->d_err, m->stream);
+      else m->f64->cons_hevi_substep(m->d, m->met, lf, st, tmp, m->lin_scr, dtau, m->d_err, m->stream);
+    } else {
+      if (adjoint) m->f64->fb_substep_ad(m->d, m->met, st, dtau, m->stream);
+      else m->f64->fb_substep(m->d, m->met, lf, st, dtau, m->stream);
+    }
   }
   CUDA_OK(cudaGetLastError());
   const dim3 b(32, 4);
@@ -1164,7 +1186,7 @@ int acoustic_linear(vibe_gb300_model* m, double dtau, int n_sub, const double* c
     CUDA_OK(cudaMemcpyAsync(out[f], m->d_stage_in, n * sizeof(double), cudaMemcpyDeviceToHost, m->stream));
     CUDA_OK(cudaStreamSynchronize(m->stream));
   }
-  return 0;
+  return read_status(m);
 }
 }  // namespace
 
@@ -1174,6 +1196,14 @@ int vibe_gb300_acoustic_tl(vibe_gb300_model* m, double dtau, int n_sub, const do
 
 int vibe_gb300_acoustic_ad(vibe_gb300_model* m, double dtau, int n_sub, const double* const* in, double* const* out) {
   return acoustic_linear(m, dtau, n_sub, in, out, true);
+}
+
+int vibe_gb300_hevi_tl(vibe_gb300_model* m, double dtau, int n_sub, const double* const* in, double* const* out) {
+  return acoustic_linear(m, dtau, n_sub, in, out, false, true);
+}
+
+int vibe_gb300_hevi_ad(vibe_gb300_model* m, double dtau, int n_sub, const double* const* in, double* const* out) {
+  return acoustic_linear(m, dtau, n_sub, in, out, true, true);
 }
 
 int vibe_gb300_hevi_substep(vibe_gb300_model* m, double dtau) {

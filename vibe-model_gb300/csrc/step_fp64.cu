@@ -633,7 +633,7 @@ __device__ inline double ac_coef_w(const Metric& m, const Dims& d, int i, int j,
 
 // phase 2 transposed: cells
 __global__ void k_fbad_pi(Dims d, Metric m, const double* __restrict__ bu, const double* __restrict__ bv,
-                          const double* __restrict__ bw, double* __restrict__ bpi, double dtau) {
+                          const double* __restrict__ bw, double* __restrict__ bpi, double dtau, int with_w) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
   const int k = blockIdx.z;
@@ -648,10 +648,12 @@ __global__ void k_fbad_pi(Dims d, Metric m, const double* __restrict__ bu, const
   if (j == d.ny - 1) acc += ac_coef_v(m, d, i, d.ny, k) * bv[IDX(i, d.ny, k)];
   acc -= ac_coef_v(m, d, i, j + 1, k) * bv[IDX(i, j + 1, k)];
   if (j == 0) acc -= ac_coef_v(m, d, i, 0, k) * bv[IDX(i, 0, k)];
-  acc += ac_coef_w(m, d, i, j, k) * bw[IDX(i, j, k)];
-  if (k == d.nz - 1) acc += ac_coef_w(m, d, i, j, d.nz) * bw[IDX(i, j, d.nz)];
-  acc -= ac_coef_w(m, d, i, j, k + 1) * bw[IDX(i, j, k + 1)];
-  if (k == 0) acc -= ac_coef_w(m, d, i, j, 0) * bw[IDX(i, j, 0)];
+  if (with_w) {
+    acc += ac_coef_w(m, d, i, j, k) * bw[IDX(i, j, k)];
+    if (k == d.nz - 1) acc += ac_coef_w(m, d, i, j, d.nz) * bw[IDX(i, j, d.nz)];
+    acc -= ac_coef_w(m, d, i, j, k + 1) * bw[IDX(i, j, k + 1)];
+    if (k == 0) acc -= ac_coef_w(m, d, i, j, 0) * bw[IDX(i, j, 0)];
+  }
   bpi[IDX(i, j, k)] += dtau * acc;
 }
 
@@ -700,6 +702,156 @@ __global__ void k_fbad_vel(Dims d, Metric m, const double* __restrict__ brho, co
   }
 }
 
+
+// ---- adjoint of the consistent HEVI substep (k_chevi_column + k_uv_backward)
+// With the gradient taken of pi itself (pgf_perturbation = 0) the substep is
+// linear in (u, v, w, rho, pi): wt = w - dtau (1-b) cp theta0_f d(pi)/dz on
+// interior faces; per cell pstar = pi + dtau kappa (Dh + (1-b) dv(w) + b dv(wt))
+// and the column system A x = pstar (A from the reference state only);
+// wn = wt - dtau b cp theta0_f dx/dz; rho += dtau (Dh + (1-b) dv(w) + b dv(wn));
+// pi = x; w = wn; then u, v take the horizontal gradient of the new pi. The
+// adjoint runs these in reverse: the horizontal gradient transposed (cells
+// gather from their faces, k_fbad_pi without w), one thread per column for the
+// vertical part (the column system transposed: A^T y = bar_x by the Thomas
+// recurrence on the swapped off-diagonals), and the horizontal divergence
+// Dh transposed (faces gather from their two cells).
+__global__ void k_hevi_ad_column(Dims d, Metric m, Flags fl, double* __restrict__ bw, const double* __restrict__ brho,
+                                 double* __restrict__ bpi, double* __restrict__ bdh, double* __restrict__ scratch,
+                                 double dtau, unsigned* err) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y;
+  if (i >= d.nx || j >= d.ny) return;
+  const int nz = d.nz;
+  const double b = fl.hevi_beta, ob = 1.0 - b;
+  const size_t col = (size_t)j * d.nx + i;
+  double* ya = scratch + col * (5 * (size_t)nz + 2);  // nz: bar_x, then y
+  double* cpr = ya + nz;                              // nz: Thomas c'
+  double* bwn = cpr + nz;                             // nz+1: bar_wn, then bar_wt
+  double* dvo = bwn + nz + 1;                         // nz: bar_dv_old
+  const double sc = m.scale[col];
+  auto rf = [&](int k) { return 0.5 * (R3(m.rho0, d, i, j, imax(k - 1, 0)) + R3(m.rho0, d, i, j, imin(k, nz - 1))); };
+  auto tf = [&](int k) { return 0.5 * (R3(m.th0, d, i, j, imax(k - 1, 0)) + R3(m.th0, d, i, j, imin(k, nz - 1))); };
+  auto dzf = [&](int k) { return dmax(m.dzeta[imin(k, nz - 1)] * sc, 1.0); };
+  auto dzc = [&](int k) { return dmax(m.dzeta[k] * sc, 1.0); };
+  auto kap = [&](int k) { return (kRd / kCv) * (R3(m.pi0, d, i, j, k) / dmax(R3(m.rho0, d, i, j, k), 1e-8)); };
+  // the column matrix of k_chevi_column: row k = (a_k, bb_k, c_k)
+  auto row = [&](int k, double& a, double& bb, double& c) {
+    const double ck = (dtau * b) * (dtau * b) * kap(k) / dzc(k);
+    const double Tk = (k == 0) ? 0.0 : rf(k) * kCp * tf(k) / dzf(k);
+    const double Tk1 = (k + 1 == nz) ? 0.0 : rf(k + 1) * kCp * tf(k + 1) / dzf(k + 1);
+    a = -ck * Tk;
+    c = -ck * Tk1;
+    bb = 1.0 + ck * (Tk + Tk1);
+  };
+  // rho = rho + dtau (Dh + ob dv_old + b dv_new): bar_dv_new = dtau b bar_rho
+  // wn feeds dv_new of the cells below and above each face, and w_out
+  for (int k = 0; k <= nz; ++k) {
+    double g = bw[IDX(i, j, k)];
+    if (k < nz) g += rf(k) / dzc(k) * (dtau * b * brho[IDX(i, j, k)]);
+    if (k >= 1) g -= rf(k) / dzc(k - 1) * (dtau * b * brho[IDX(i, j, k - 1)]);
+    bwn[k] = g;
+  }
+  // wn = wt - cb_k (x_k - x_{k-1}) on interior faces; x = pi_out
+  for (int k = 0; k < nz; ++k) ya[k] = bpi[IDX(i, j, k)];
+  for (int k = 1; k < nz; ++k) {
+    const double cb = dtau * b * kCp * tf(k) / dzf(k);
+    ya[k] -= cb * bwn[k];
+    ya[k - 1] += cb * bwn[k];
+  }
+  // A^T y = bar_x: row k of A^T has (c_{k-1}, bb_k, a_{k+1})
+  double yprev = 0.0, cprev = 0.0;
+  for (int k = 0; k < nz; ++k) {
+    double a, bb, c, a1 = 0.0, bb1, c1;
+    row(k, a, bb, c);
+    double cm = 0.0;
+    if (k > 0) {
+      double a0, bb0, c0;
+      row(k - 1, a0, bb0, c0);
+      cm = c0;  // A^T sub-diagonal
+    }
+    if (k + 1 < nz) row(k + 1, a1, bb1, c1);
+    const double denom = (k == 0) ? bb : bb - cm * cprev;
+    if (fabs(denom) < 1e-300) { atomicOr(err, (unsigned)kErrSingular); return; }
+    yprev = (k == 0) ? ya[k] / denom : (ya[k] - cm * yprev) / denom;
+    cprev = (k + 1 < nz) ? a1 / denom : 0.0;
+    cpr[k] = cprev;
+    ya[k] = yprev;
+  }
+  for (int k = nz - 1; k-- > 0;) ya[k] -= cpr[k] * ya[k + 1];
+  // pstar = pi + dtau kappa (Dh + ob dv_old + b dv_t)
+  for (int k = 0; k < nz; ++k) {
+    const double y = ya[k], kp = dtau * kap(k) * y;
+    bdh[IDX(i, j, k)] = dtau * brho[IDX(i, j, k)] + kp;
+    dvo[k] = dtau * ob * brho[IDX(i, j, k)] + ob * kp;
+    cpr[k] = b * kp;  // bar_dv_t
+  }
+  // bar_wt: from wn (identity) and dv_t
+  for (int k = 0; k <= nz; ++k) {
+    double g = bwn[k];
+    if (k < nz) g += rf(k) / dzc(k) * cpr[k];
+    if (k >= 1) g -= rf(k) / dzc(k - 1) * cpr[k - 1];
+    bwn[k] = g;
+  }
+  // bar_w: from wt (identity) and dv_old
+  for (int k = 0; k <= nz; ++k) {
+    double g = bwn[k];
+    if (k < nz) g += rf(k) / dzc(k) * dvo[k];
+    if (k >= 1) g -= rf(k) / dzc(k - 1) * dvo[k - 1];
+    bw[IDX(i, j, k)] = g;
+  }
+  // bar_pi of the input: pstar's pi (y) and wt's gradient, wt(k) = w - ce_k (pi_k - pi_{k-1});
+  // the output pi is x itself, whose bar went into y
+  for (int k = 0; k < nz; ++k) {
+    double g = ya[k];
+    if (k >= 1) g -= dtau * ob * kCp * tf(k) / dzf(k) * bwn[k];
+    if (k + 1 < nz) g += dtau * ob * kCp * tf(k + 1) / dzf(k + 1) * bwn[k + 1];
+    bpi[IDX(i, j, k)] = g;
+  }
+}
+
+// The forward substep copies the column solve's whole w, rho, pi outputs back,
+// whose ghost column i = nx and ghost row j = ny it never writes (zeros): those
+// outputs do not depend on the input, so their bars do not reach it
+__global__ void k_hevi_ad_ghost(Dims d, double* __restrict__ bw, double* __restrict__ brho, double* __restrict__ bpi) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y;
+  const int k = blockIdx.z;
+  if (i > d.nx || j > d.ny || k > d.nz || (i < d.nx && j < d.ny)) return;
+  const size_t c = IDX(i, j, k);
+  bw[c] = 0.0;
+  if (k < d.nz) {
+    brho[c] = 0.0;
+    bpi[c] = 0.0;
+  }
+}
+
+// Dh = -(fx/dx + fy/dy) transposed: each u / v face gathers from its two cells
+__global__ void k_dh_ad(Dims d, Metric m, const double* __restrict__ bdh, double* __restrict__ bu,
+                        double* __restrict__ bv) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y;
+  const int k = blockIdx.z;
+  if (i > d.nx || j > d.ny || k >= d.nz) return;
+  const double* r0 = m.rho0;
+  if (j < d.ny) {
+    double acc = 0.0;
+    if (i >= 1) {
+      const int c = i - 1;
+      acc -= 0.5 * (R3(r0, d, c, j, k) + R3(r0, d, imin(c + 1, d.nx - 1), j, k)) / m.dx * bdh[IDX(c, j, k)];
+    }
+    if (i < d.nx) acc += 0.5 * (R3(r0, d, imax(i - 1, 0), j, k) + R3(r0, d, i, j, k)) / m.dx * bdh[IDX(i, j, k)];
+    bu[IDX(i, j, k)] += acc;
+  }
+  if (i < d.nx) {
+    double acc = 0.0;
+    if (j >= 1) {
+      const int c = j - 1;
+      acc -= 0.5 * (R3(r0, d, i, c, k) + R3(r0, d, i, imin(c + 1, d.ny - 1), k)) / m.dy * bdh[IDX(i, c, k)];
+    }
+    if (j < d.ny) acc += 0.5 * (R3(r0, d, i, imax(j - 1, 0), k) + R3(r0, d, i, j, k)) / m.dy * bdh[IDX(i, j, k)];
+    bv[IDX(i, j, k)] += acc;
+  }
+}
 }  // namespace
 
 // ---------------------------------------------------------------------------
@@ -744,9 +896,19 @@ void FP64_FN(fp64_stage_update)(const Dims& d, double* const* s0, double* const*
 }
 
 void FP64_FN(fp64_fb_substep_ad)(const Dims& d, const Metric& m, double* const* bar, double dtau, cudaStream_t stream) {
-  k_fbad_pi<<<grid3(d, d.nx, d.ny, d.nz, kBlk), kBlk, 0, stream>>>(d, m, bar[U], bar[V], bar[W], bar[PI], dtau);
+  k_fbad_pi<<<grid3(d, d.nx, d.ny, d.nz, kBlk), kBlk, 0, stream>>>(d, m, bar[U], bar[V], bar[W], bar[PI], dtau, 1);
   k_fbad_vel<<<grid3(d, d.nx + 1, d.ny + 1, d.nz + 1, kBlk), kBlk, 0, stream>>>(d, m, bar[RHO], bar[PI], bar[U], bar[V],
                                                                                bar[W], dtau);
+}
+
+void FP64_FN(fp64_hevi_substep_ad)(const Dims& d, const Metric& m, const Flags& fl, double* const* bar, double* bdh,
+                                   double* scratch, double dtau, unsigned* err, cudaStream_t stream) {
+  k_fbad_pi<<<grid3(d, d.nx, d.ny, d.nz, kBlk), kBlk, 0, stream>>>(d, m, bar[U], bar[V], bar[W], bar[PI], dtau, 0);
+  k_hevi_ad_column<<<dim3((d.nx + 31) / 32, (d.ny + 3) / 4), dim3(32, 4), 0, stream>>>(d, m, fl, bar[W], bar[RHO],
+                                                                                      bar[PI], bdh, scratch, dtau,
+                                                                                      err);
+  k_dh_ad<<<grid3(d, d.nx + 1, d.ny + 1, d.nz, kBlk), kBlk, 0, stream>>>(d, m, bdh, bar[U], bar[V]);
+  k_hevi_ad_ghost<<<grid3(d, d.nx + 1, d.ny + 1, d.nz + 1, kBlk), kBlk, 0, stream>>>(d, bar[W], bar[RHO], bar[PI]);
 }
 
 void FP64_FN(fp64_fb_substep)(const Dims& d, const Metric& m, const Flags& fl, double* const* st, double dtau,

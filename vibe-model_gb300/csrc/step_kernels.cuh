@@ -14,6 +14,8 @@ void fp64_stage_update(const Dims& d, double* const* s0, double* const* tend, do
 void fp64_fb_substep(const Dims& d, const Metric& m, const Flags& fl, double* const* st, double dtau,
                      cudaStream_t stream);
 void fp64_fb_substep_ad(const Dims& d, const Metric& m, double* const* bar, double dtau, cudaStream_t stream);
+void fp64_hevi_substep_ad(const Dims& d, const Metric& m, const Flags& fl, double* const* bar, double* bdh,
+                          double* scratch, double dtau, unsigned* err, cudaStream_t stream);
 void fp64_ref_hevi_substep(const Dims& d, const Metric& m, double* const* st, double dtau, const double* ta,
                            const double* tb, const double* tc, double* scratch, unsigned* err, cudaStream_t stream);
 void fp64_cons_hevi_substep(const Dims& d, const Metric& m, const Flags& fl, double* const* st, double* const* tmp,
@@ -29,6 +31,8 @@ void fp64_stage_update_exact(const Dims& d, double* const* s0, double* const* te
 void fp64_fb_substep_exact(const Dims& d, const Metric& m, const Flags& fl, double* const* st, double dtau,
                      cudaStream_t stream);
 void fp64_fb_substep_ad_exact(const Dims& d, const Metric& m, double* const* bar, double dtau, cudaStream_t stream);
+void fp64_hevi_substep_ad_exact(const Dims& d, const Metric& m, const Flags& fl, double* const* bar, double* bdh,
+                                double* scratch, double dtau, unsigned* err, cudaStream_t stream);
 void fp64_ref_hevi_substep_exact(const Dims& d, const Metric& m, double* const* st, double dtau, const double* ta,
                            const double* tb, const double* tc, double* scratch, unsigned* err, cudaStream_t stream);
 void fp64_cons_hevi_substep_exact(const Dims& d, const Metric& m, const Flags& fl, double* const* st, double* const* tmp,

@@ -85,6 +85,8 @@ _sigs = {
     "vibe_gb300_acoustic_substep": (_I, [_vp, _D]),
     "vibe_gb300_acoustic_tl": (_I, [_vp, _D, _I, ctypes.POINTER(_dp), ctypes.POINTER(_dp)]),
     "vibe_gb300_acoustic_ad": (_I, [_vp, _D, _I, ctypes.POINTER(_dp), ctypes.POINTER(_dp)]),
+    "vibe_gb300_hevi_tl": (_I, [_vp, _D, _I, ctypes.POINTER(_dp), ctypes.POINTER(_dp)]),
+    "vibe_gb300_hevi_ad": (_I, [_vp, _D, _I, ctypes.POINTER(_dp), ctypes.POINTER(_dp)]),
     "vibe_gb300_hevi_substep": (_I, [_vp, _D]),
     "vibe_gb300_sponge": (_I, [_vp, _D]),
     "vibe_gb300_snapshot": (_I, [_vp, _I]),
@@ -301,6 +303,14 @@ class Model:
     def acoustic_ad(self, dtau, n_sub, fields):
         """Adjoint of acoustic_tl: <acoustic_tl(x), y> = <x, acoustic_ad(y)>."""
         return self._acoustic_linear(lib.vibe_gb300_acoustic_ad, dtau, n_sub, fields)
+
+    def hevi_tl(self, dtau, n_sub, fields):
+        """Tangent-linear of n_sub consistent HEVI substeps on [u, v, w, rho, pi]."""
+        return self._acoustic_linear(lib.vibe_gb300_hevi_tl, dtau, n_sub, fields)
+
+    def hevi_ad(self, dtau, n_sub, fields):
+        """Adjoint of hevi_tl."""
+        return self._acoustic_linear(lib.vibe_gb300_hevi_ad, dtau, n_sub, fields)
 
     def autotune(self, dt, n_sub):
         """Pick the fastest launch shapes for this grid (mixed path); the
