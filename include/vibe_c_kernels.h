@@ -82,7 +82,11 @@ void vibe_advect_scalar_flux_f64(const double *q, const double *rho,
  * arithmetic as the host entry points above) ---- */
 
 /* n_sys independent systems of size n, each stored contiguously
- * (system s uses a + s*(n-1), b + s*n, ...). One thread per system.
+ * (system s uses a + s*(n-1), b + s*n, ...). One thread per system for
+ * n <= 128; above, one warp per system (each lane eliminates a chunk of rows,
+ * the chunks' end unknowns are joined by a 2x2 block-tridiagonal solve), whose
+ * results agree with the single sweep to rounding and whose pivots are the
+ * chunks' (a zero one is VIBE_C_ERR_SINGULAR).
  * status (device, n_sys ints) receives the per-system return code; may be
  * NULL. Returns VIBE_C_OK or VIBE_C_ERR_BAD_ARG/VIBE_C_ERR_DEVICE (launch). */
 int vibe_tridiagonal_solve_batched_f64_dev(const double *a, const double *b,

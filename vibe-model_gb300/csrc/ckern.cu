@@ -115,6 +115,133 @@ __global__ void k_thomas_batched(const T* __restrict__ a, const T* __restrict__ 
   if (status) status[s] = rc;
 }
 
+// ---------------------------------------------------------------------------
+// Tall systems (n > kTallN): one warp per system. The n rows split into 32
+// contiguous chunks, one per lane; each lane factors its chunk once (the
+// recurrence above) and solves it for three right-hand sides: the chunk's d
+// (y), its coupling to the unknown left of the chunk (v, from a at the first
+// row) and to the unknown right of it (w, from c at the last row), so that
+// x_i = y_i - v_i x_left - w_i x_right on the chunk. The chunks' first and
+// last unknowns z_j = (F_j, E_j) then satisfy a 2x2 block-tridiagonal system,
+// z_j + [vF; vE]_j E_{j-1} + [wF; wE]_j F_{j+1} = [yF; yE]_j, which lane 0
+// solves by block elimination (32 blocks); every lane then reads its two
+// neighbours' interface values from shared memory and finishes its chunk.
+// A zero pivot of a chunk or a singular 2x2 block gives VIBE_C_ERR_SINGULAR.
+// The elimination order differs from one sequential sweep, so results agree
+// with it to rounding. Scratch: 3n per system (c', v, w).
+constexpr int kTallN = 128;
+constexpr int kTallWarps = 4;  // systems per block
+
+template <typename T>
+__global__ void __launch_bounds__(32 * kTallWarps) k_thomas_tall(const T* __restrict__ a, const T* __restrict__ b,
+                                                                 const T* __restrict__ c, const T* __restrict__ d,
+                                                                 int n, int n_sys, T* __restrict__ x,
+                                                                 T* __restrict__ work, int* __restrict__ status) {
+  __shared__ T sh[kTallWarps][32][6];  // per lane: yF, yE, vF, vE, wF, wE
+  __shared__ T zs[kTallWarps][32][2];  // interface solution F_j, E_j
+  __shared__ int bad[kTallWarps];
+  const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int s = blockIdx.x * kTallWarps + wid;
+  const bool live = s < n_sys;
+  const int m = (n + 31) / 32;                   // rows per chunk
+  const int r0 = min(lane * m, n), r1 = min(r0 + m, n), L = r1 - r0;
+  const int nch = (n + m - 1) / m;               // chunks with rows (lanes >= nch hold none)
+  if (lane == 0) bad[wid] = 0;
+  __syncwarp();
+  const T* as = (live && a) ? a + (size_t)s * (n - 1) : nullptr;
+  const T* bs = live ? b + (size_t)s * n : nullptr;
+  const T* cs = (live && c) ? c + (size_t)s * (n - 1) : nullptr;
+  const T* ds = live ? d + (size_t)s * n : nullptr;
+  T* xs = live ? x + (size_t)s * n : nullptr;
+  T* cp = live ? work + (size_t)s * 3 * n : nullptr;
+  T* vv = cp ? cp + n : nullptr;
+  T* ww = cp ? cp + 2 * n : nullptr;
+  bool ok = true;
+  if (live && L > 0) {
+    // forward elimination of the chunk with the three right-hand sides
+    T den = bs[r0];
+    if (den == (T)0) ok = false;
+    if (ok) {
+      const T a0 = (r0 > 0 && as) ? as[r0 - 1] : (T)0;   // coupling to x_{r0-1}
+      const T cl = (r1 < n && cs) ? cs[r1 - 1] : (T)0;   // coupling to x_{r1}
+      cp[r0] = (r0 + 1 < r1) ? ((cs ? cs[r0] : (T)0) / den) : (T)0;
+      xs[r0] = ds[r0] / den;
+      vv[r0] = a0 / den;
+      ww[r0] = (L == 1) ? cl / den : (T)0;
+      for (int k = r0 + 1; k < r1 && ok; ++k) {
+        const T am = as ? as[k - 1] : (T)0;
+        den = bs[k] - am * cp[k - 1];
+        if (den == (T)0) { ok = false; break; }
+        xs[k] = (ds[k] - am * xs[k - 1]) / den;
+        vv[k] = (-am * vv[k - 1]) / den;
+        ww[k] = ((k == r1 - 1 ? cl : (T)0) - am * ww[k - 1]) / den;
+        if (k < r1 - 1) cp[k] = (cs ? cs[k] : (T)0) / den;
+      }
+      if (ok)
+        for (int k = r1 - 1; k-- > r0;) {
+          xs[k] -= cp[k] * xs[k + 1];
+          vv[k] -= cp[k] * vv[k + 1];
+          ww[k] -= cp[k] * ww[k + 1];
+        }
+    }
+    if (ok) {
+      sh[wid][lane][0] = xs[r0];
+      sh[wid][lane][1] = xs[r1 - 1];
+      sh[wid][lane][2] = vv[r0];
+      sh[wid][lane][3] = vv[r1 - 1];
+      sh[wid][lane][4] = ww[r0];
+      sh[wid][lane][5] = ww[r1 - 1];
+    }
+  }
+  if (!ok) bad[wid] = 1;
+  __syncwarp();
+  // the interface system, block elimination by lane 0: z_j + Lj z_{j-1} + Uj z_{j+1} = Yj,
+  // Lj = [[0, vF], [0, vE]] and Uj = [[wF, 0], [wE, 0]]
+  if (live && lane == 0 && !bad[wid]) {
+    T C[32][2][2], Y[32][2];
+    for (int j = 0; j < nch; ++j) {
+      const T* q = sh[wid][j];
+      T D00 = 1, D01 = 0, D10 = 0, D11 = 1, r0v = q[0], r1v = q[1];
+      if (j > 0) {  // D = I - Lj C_{j-1}, rhs = Yj - Lj Y_{j-1}; Lj picks row 1 (E) of the previous block
+        D00 -= q[2] * C[j - 1][1][0];
+        D01 -= q[2] * C[j - 1][1][1];
+        D10 -= q[3] * C[j - 1][1][0];
+        D11 -= q[3] * C[j - 1][1][1];
+        r0v -= q[2] * Y[j - 1][1];
+        r1v -= q[3] * Y[j - 1][1];
+      }
+      const T det = D00 * D11 - D01 * D10;
+      if (det == (T)0) { bad[wid] = 1; break; }
+      const T i00 = D11 / det, i01 = -D01 / det, i10 = -D10 / det, i11 = D00 / det;
+      // C_j = D^-1 Uj (Uj acts on F_{j+1}: column 0), Y_j = D^-1 rhs
+      const T u0 = (j + 1 < nch) ? q[4] : (T)0, u1 = (j + 1 < nch) ? q[5] : (T)0;
+      C[j][0][0] = i00 * u0 + i01 * u1;
+      C[j][1][0] = i10 * u0 + i11 * u1;
+      C[j][0][1] = 0;
+      C[j][1][1] = 0;
+      Y[j][0] = i00 * r0v + i01 * r1v;
+      Y[j][1] = i10 * r0v + i11 * r1v;
+    }
+    if (!bad[wid])
+      for (int j = nch - 1; j >= 0; --j) {
+        T f = Y[j][0], e = Y[j][1];
+        if (j + 1 < nch) {  // z_j = Y_j - C_j z_{j+1}, C_j acting on F_{j+1}
+          f -= C[j][0][0] * zs[wid][j + 1][0];
+          e -= C[j][1][0] * zs[wid][j + 1][0];
+        }
+        zs[wid][j][0] = f;
+        zs[wid][j][1] = e;
+      }
+  }
+  __syncwarp();
+  if (live && L > 0 && !bad[wid]) {
+    const T xl = (lane > 0) ? zs[wid][lane - 1][1] : (T)0;        // E of the chunk to the left
+    const T xr = (lane + 1 < nch) ? zs[wid][lane + 1][0] : (T)0;  // F of the chunk to the right
+    for (int k = r0; k < r1; ++k) xs[k] = xs[k] - vv[k] * xl - ww[k] * xr;
+  }
+  if (live && lane == 0 && status) status[s] = bad[wid] ? VIBE_C_ERR_SINGULAR : VIBE_C_OK;
+}
+
 // WENO5 (c_kernels.c:64-104), one thread per stencil
 template <typename T>
 __device__ void weno5_d(T qm2, T qm1, T q0, T q1, T q2, T* ql, T* qr) {
@@ -354,9 +481,15 @@ int thomas_batched_dev(const T* a, const T* b, const T* c, const T* d, int n, in
                        vibe_stream_t stream) {
   if (n <= 0 || n_sys < 0 || b == nullptr || d == nullptr || x == nullptr) return VIBE_C_ERR_BAD_ARG;
   if (n_sys == 0) return VIBE_C_OK;
-  T* work = (T*)scratch((size_t)n * n_sys * sizeof(T));
+  const bool tall = n > kTallN;
+  T* work = (T*)scratch((size_t)n * n_sys * sizeof(T) * (tall ? 3 : 1));
   if (!work) { g_cerr = "scratch allocation failed"; return VIBE_C_ERR_DEVICE; }
-  k_thomas_batched<T><<<(n_sys + 127) / 128, 128, 0, (cudaStream_t)stream>>>(a, b, c, d, n, n_sys, x, work, status);
+  if (tall)
+    k_thomas_tall<T><<<(n_sys + kTallWarps - 1) / kTallWarps, 32 * kTallWarps, 0, (cudaStream_t)stream>>>(
+        a, b, c, d, n, n_sys, x, work, status);
+  else
+    k_thomas_batched<T><<<(n_sys + 127) / 128, 128, 0, (cudaStream_t)stream>>>(a, b, c, d, n, n_sys, x, work,
+                                                                              status);
   return device_ok(cudaGetLastError(), "thomas launch") ? VIBE_C_OK : VIBE_C_ERR_DEVICE;
 }
 
