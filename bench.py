@@ -108,11 +108,11 @@ def si_leg(vg, steps=3):
 # near the ground, so the saturation adjustment condenses from the first step)
 # and the built-in Kessler warm-rain package at every RK stage (column
 # pressure from the total Exner function); mixed path, 10 steps each way.
-def physics_leg(vg, torch, steps=10, warmup=3):
-    s = vg.Setup.defaults(nx=NX, ny=NY, **dict(CASE, moist=1, qv_surface=0.025, qv_decay_height=2500.0))
+def physics_leg(vg, torch, steps=10, warmup=3, nx=NX, ny=NY):
+    s = vg.Setup.defaults(nx=nx, ny=ny, **dict(CASE, moist=1, qv_surface=0.025, qv_decay_height=2500.0))
     k = vg.Kessler.defaults(exner_offset=0)
     out = {"workload": "%dx%dx%d, moist (qv_surface 0.025, 2.5 km decay), Kessler warm rain at every RK stage, "
-                       "mixed path, dt=%g s, %d substeps" % (NX, NY, NZ, DT, NSUB), "steps": steps}
+                       "mixed path, dt=%g s, %d substeps" % (nx, ny, NZ, DT, NSUB), "steps": steps}
     with vg.Model(s, vg.MIXED) as m:
         m.save_snapshot()
         ext = torch.cuda.ExternalStream(m.stream())
@@ -131,7 +131,7 @@ def physics_leg(vg, torch, steps=10, warmup=3):
             ms[phys] = e0.elapsed_time(e1) / steps
         qc = vg.interior(s, 7, m.get(7))
         m.set_physics_kessler(None)
-    cells = NX * NY * NZ
+    cells = nx * ny * NZ
     out.update({"ms_per_step_dynamics_only": ms[False], "ms_per_step_with_kessler": ms[True],
                 "kessler_ms_per_stage": (ms[True] - ms[False]) / 3.0,
                 "value": cells / (ms[True] * 1e-3), "unit": "cell-updates/s", "max_qc_after": float(qc.max())})
@@ -594,7 +594,7 @@ def main():
 
     import vibe_gb300 as vg
     if args.only == "physics":
-        print(json.dumps({"only": "physics", "physics_coupling": physics_leg(vg, torch)}))
+        print(json.dumps({"only": "physics", "physics_coupling": physics_leg(vg, torch, nx=args.nx, ny=args.ny)}))
         ranks.close()
         return
     setup = case_setup(vg.Setup, args.nx, args.ny)
