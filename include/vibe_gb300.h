@@ -289,7 +289,10 @@ typedef struct {
   unsigned written;
 } vibe_gb300_physics_args;
 typedef int (*vibe_gb300_physics_fn)(void *user, vibe_gb300_physics_args *args);
-/* Install (fn != NULL) or remove the package; drops the step graphs. */
+/* Install (fn != NULL) or remove the package; drops the step graphs. Groups
+ * and nested sets step their members without physics: creating one from a
+ * model with a package installed fails (VIBE_GB300_EUNSUPPORTED), and a
+ * package installed on a member afterwards does not enter the group's steps. */
 int vibe_gb300_set_physics(vibe_gb300_model *m, vibe_gb300_physics_fn fn, void *user);
 /* The installed package's tendency for the current state (one call as at
  * stage 0 with this dt), downloaded as FieldT storage: out[0..8] = u, v,

@@ -142,3 +142,16 @@ def test_kessler_needs_moisture(vg):
         m.set_physics_kessler(vg.Kessler.defaults())
         with pytest.raises(vg.VibeError):
             m.step(2.0, 4, 1)
+
+
+def test_groups_refuse_models_with_physics(vg):
+    """The work-list launches of a group have no physics call: a member with a
+    package installed is refused rather than stepped without it."""
+    s = setup(vg, terrain_kind=0, ref_kind=0)
+    with vg.Model(s, vg.MIXED) as a, vg.Model(s, vg.MIXED) as b:
+        a.set_physics_kessler(vg.Kessler.defaults())
+        with pytest.raises(vg.VibeError):
+            vg.Group([a, b])
+        a.set_physics_kessler(None)
+        with vg.Group([a, b]) as g:
+            g.step(2.0, 4, 1)

@@ -1856,6 +1856,8 @@ int vibe_gb300_group_create(vibe_gb300_model* const* models, int n, vibe_gb300_g
     vibe_gb300_model* m = models[q];
     if (!m || m->precision != VIBE_GB300_MIXED || m->fl.acoustic_mode != 2)
       return fail(VIBE_GB300_EUNSUPPORTED, "a group holds mixed-precision models with acoustic_mode 2");
+    if (m->phys_fn)  // the work-list launches have no physics call
+      return fail(VIBE_GB300_EUNSUPPORTED, "group members cannot have a physics package installed");
     if (m->d.nz != models[0]->d.nz || m->fl.moist != models[0]->fl.moist ||
         m->fl.weno_scalars != models[0]->fl.weno_scalars || m->fl.advection != models[0]->fl.advection ||
         m->fl.weno_advective != models[0]->fl.weno_advective || m->fl.coriolis != models[0]->fl.coriolis ||
