@@ -229,6 +229,13 @@ int vibe_gb300_acoustic_ad(vibe_gb300_model *m, double dtau, int n_sub, const do
  * As the model's own substep does, it sets the ghost column i = nx and row
  * j = ny of w, rho and pi to zero. */
 int vibe_gb300_hevi_tl(vibe_gb300_model *m, double dtau, int n_sub, const double *const *in, double *const *out);
+/* FP32 forms for mixed models: the model's own FP32 forward-backward substep
+ * (per-level reference tables) on perturbations of u, v, w, rho' = rho - rho0
+ * and pi' = pi - pi0 (FieldT storage in and out, as above), and its adjoint. */
+int vibe_gb300_acoustic_tl_f32(vibe_gb300_model *m, double dtau, int n_sub, const double *const *in,
+                               double *const *out);
+int vibe_gb300_acoustic_ad_f32(vibe_gb300_model *m, double dtau, int n_sub, const double *const *in,
+                               double *const *out);
 int vibe_gb300_hevi_ad(vibe_gb300_model *m, double dtau, int n_sub, const double *const *in, double *const *out);
 int vibe_gb300_hevi_substep(vibe_gb300_model *m, double dtau);
 /* Autotuner of the mixed step: times, on this model's grid, the launch shapes

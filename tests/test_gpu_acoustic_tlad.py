@@ -223,3 +223,25 @@ def test_hevi_adjoint_is_the_transposed_matrix(vg):
         scale = np.abs(tl).max()
         assert np.abs(ad - tl.T).max() <= 1e-13 * scale, np.abs(ad - tl.T).max() / scale
         assert np.count_nonzero(tl - np.eye(len(pts))) > len(pts)
+
+
+# ---- the FP32 form on mixed models (vibe_gb300_acoustic_tl_f32 / _ad_f32) ----
+def test_fp32_acoustic_tl_ad(vg):
+    """The mixed model's own FP32 forward-backward substep as a linear map of
+    (u, v, w, rho', pi'): it tracks the FP64 tangent-linear to 1e-5 of each
+    field's scale over 4 substeps, and its adjoint passes the dot-product test
+    to 1e-5."""
+    s = setup(vg, terrain_kind=0, ref_kind=0)
+    with vg.Model(s, vg.MIXED) as m:
+        dx, dy = random_fields(vg, m, 31), random_fields(vg, m, 32)
+        t32 = m.acoustic_tl_f32(0.5, 4, dx)
+        t64 = m.acoustic_tl(0.5, 4, dx)
+        for f, sp in enumerate(FIELDS):
+            g, r = vg.interior(s, sp, t32[f]), vg.interior(s, sp, t64[f])
+            assert np.abs(g - r).max() <= 1e-5 * np.abs(r).max(), (vg.SPECIES[sp], np.abs(g - r).max())
+        a32 = m.acoustic_ad_f32(0.5, 4, dy)
+        lhs, rhs = dot(t32, dy), dot(dx, a32)
+        assert abs(lhs - rhs) <= 1e-5 * max(abs(lhs), abs(rhs)), (lhs, rhs)
+    with vg.Model(s, vg.FP64) as f64:
+        with pytest.raises(vg.VibeError):
+            f64.acoustic_tl_f32(0.5, 1, random_fields(vg, f64, 33))

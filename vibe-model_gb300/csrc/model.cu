@@ -81,6 +81,7 @@ struct vibe_gb300_model {
   double* tend[NSPECIES] = {};
   double* tmp[NSPECIES] = {};
   double* lin[5] = {};  // u, v, w, rho, pi perturbations of the acoustic TL/AD (allocated on first use)
+  float* lin32[2][5] = {};         // FP32 acoustic TL/AD (mixed models): ping-pong perturbations
   double* lin_tmp[3] = {};         // HEVI TL: the column solve's w, rho, pi outputs
   double* lin_scr = nullptr;       // HEVI TL/AD: per-column work
   double* lin_dh = nullptr;        // HEVI AD: bar of the horizontal divergence
@@ -1189,6 +1190,88 @@ int acoustic_linear(vibe_gb300_model* m, double dtau, int n_sub, const double* c
   return read_status(m);
 }
 }  // namespace
+
+// FieldT storage (double) <-> FP32 device layout over the staggered box
+__global__ void k_pack_to_f32(Dims d, int nsx, int nsy, int ni, int nj, int nk, const double* __restrict__ src,
+                              float* __restrict__ dst) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y, k = blockIdx.z;
+  if (i >= ni || j >= nj || k >= nk) return;
+  dst[d.idx(i, j, k)] = (float)src[soff(nsx, nsy, i, j, k)];
+}
+__global__ void k_scatter_from_f32(Dims d, int nsx, int nsy, int ni, int nj, int nk, const float* __restrict__ src,
+                                   double* __restrict__ dst) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y, k = blockIdx.z;
+  if (i >= ni || j >= nj || k >= nk) return;
+  dst[soff(nsx, nsy, i, j, k)] = (double)src[d.idx(i, j, k)];
+}
+
+namespace {
+// the mixed model's own FP32 forward-backward substep (mixed_fb_substep) on
+// perturbations of (u, v, w, rho', pi'), and its adjoint
+int acoustic_linear_f32(vibe_gb300_model* m, double dtau, int n_sub, const double* const* in, double* const* out,
+                        bool adjoint) {
+  if (!m || !in || !out || n_sub < 0) return fail(VIBE_GB300_EBADARG, "bad argument");
+  if (m->precision != VIBE_GB300_MIXED) return fail(VIBE_GB300_EUNSUPPORTED, "the FP32 form needs a mixed model");
+  for (int f = 0; f < 5; ++f)
+    if (!in[f] || !out[f]) return fail(VIBE_GB300_EBADARG, "bad argument");
+  const size_t nfield = m->d.plane * (size_t)(m->d.nz + 1);
+  if (!m->lin32[0][0])
+    for (int b = 0; b < 2; ++b)
+      for (int f = 0; f < 5; ++f)
+        if (int rc = dalloc(m, &m->lin32[b][f], nfield)) return rc;
+  const dim3 bl(32, 4);
+  auto ws_lin = [&](int b) {
+    WS w;
+    for (int q = 0; q < NSPECIES; ++q) w.f[q] = nullptr;
+    for (int f = 0; f < 5; ++f) w.f[kLinField[f]] = m->lin32[b][f];
+    return w;
+  };
+  for (int f = 0; f < 5; ++f) {
+    const int q = kLinField[f];
+    int ni, nj, nk;
+    box_of(m, q, ni, nj, nk);
+    CUDA_OK(cudaMemcpyAsync(m->d_stage_in, in[f], storage_count(m, q) * sizeof(double), cudaMemcpyHostToDevice,
+                            m->stream));
+    k_pack_to_f32<<<dim3((ni + 31) / 32, (nj + 3) / 4, nk), bl, 0, m->stream>>>(m->d, m->nsx[q], m->nsy[q], ni, nj,
+                                                                                nk, m->d_stage_in, m->lin32[0][f]);
+    CUDA_OK(cudaMemcpyAsync(m->lin32[1][f], m->lin32[0][f], nfield * sizeof(float), cudaMemcpyDeviceToDevice,
+                            m->stream));
+  }
+  int cur = 0;
+  for (int n = 0; n < n_sub; ++n) {
+    if (adjoint) {
+      mixed_fb_substep_ad(m->d, m->tab, ws_lin(0), (float)dtau, m->stream);
+    } else {
+      mixed_fb_substep(m->d, m->tab, m->fl, ws_lin(cur), ws_lin(1 - cur), (float)dtau, m->stream);
+      cur = 1 - cur;
+    }
+  }
+  CUDA_OK(cudaGetLastError());
+  for (int f = 0; f < 5; ++f) {
+    const int q = kLinField[f];
+    int ni, nj, nk;
+    box_of(m, q, ni, nj, nk);
+    const size_t n = storage_count(m, q);
+    CUDA_OK(cudaMemcpyAsync(m->d_stage_in, in[f], n * sizeof(double), cudaMemcpyHostToDevice, m->stream));
+    k_scatter_from_f32<<<dim3((ni + 31) / 32, (nj + 3) / 4, nk), bl, 0, m->stream>>>(
+        m->d, m->nsx[q], m->nsy[q], ni, nj, nk, m->lin32[cur][f], m->d_stage_in);
+    CUDA_OK(cudaGetLastError());
+    CUDA_OK(cudaMemcpyAsync(out[f], m->d_stage_in, n * sizeof(double), cudaMemcpyDeviceToHost, m->stream));
+    CUDA_OK(cudaStreamSynchronize(m->stream));
+  }
+  return read_status(m);
+}
+}  // namespace
+
+int vibe_gb300_acoustic_tl_f32(vibe_gb300_model* m, double dtau, int n_sub, const double* const* in,
+                               double* const* out) {
+  return acoustic_linear_f32(m, dtau, n_sub, in, out, false);
+}
+
+int vibe_gb300_acoustic_ad_f32(vibe_gb300_model* m, double dtau, int n_sub, const double* const* in,
+                               double* const* out) {
+  return acoustic_linear_f32(m, dtau, n_sub, in, out, true);
+}
 
 int vibe_gb300_acoustic_tl(vibe_gb300_model* m, double dtau, int n_sub, const double* const* in, double* const* out) {
   return acoustic_linear(m, dtau, n_sub, in, out, false);

@@ -1189,6 +1189,72 @@ int mixed_stage(const Dims& d, const Tab& t, const Flags& fl, const WS& win, con
   return 0;
 }
 
+// ---- adjoint of the FP32 forward-backward substep (k_mx_fb_mass, then
+// fb_mom_body with w): the transposed momentum phase (each cell gathers the
+// pressure-gradient coefficients of its faces, uniform per level) and then
+// the transposed mass phase (each face gathers the divergence of its two
+// cells, with Z = bar_rho' + kappa bar_pi'); in place on the bars.
+__global__ void k_mxad_pi(Dims d, Tab t, WS bar, float dtau) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y;
+  const int k = blockIdx.z;
+  if (i >= d.nx || j >= d.ny || k >= d.nz) return;
+  const float cp = (float)kCp;
+  const float* bu = bar.f[U];
+  const float* bv = bar.f[V];
+  const float* bw = bar.f[W];
+  const float cu = -cp * t.t0c[k] * t.dx_inv, cv = -cp * t.t0c[k] * t.dy_inv;
+  float acc = cu * (bu[IX(i, j, k)] - bu[IX(i + 1, j, k)]);
+  if (i == d.nx - 1) acc += cu * bu[IX(d.nx, j, k)];
+  if (i == 0) acc -= cu * bu[IX(0, j, k)];
+  acc += cv * (bv[IX(i, j, k)] - bv[IX(i, j + 1, k)]);
+  if (j == d.ny - 1) acc += cv * bv[IX(i, d.ny, k)];
+  if (j == 0) acc -= cv * bv[IX(i, 0, k)];
+  // w faces: face f uses pi'(min(f, nz-1)) - pi'(max(f-1, 0)) with -cp tfz(f) idzw(f)
+  auto cw = [&](int f) { return -cp * t.tfz[f] * t.idzw[f]; };
+  acc += cw(k) * bw[IX(i, j, k)] - cw(k + 1) * bw[IX(i, j, k + 1)];
+  if (k == d.nz - 1) acc += cw(d.nz) * bw[IX(i, j, d.nz)];
+  if (k == 0) acc -= cw(0) * bw[IX(i, j, 0)];
+  bar.f[PI][IX(i, j, k)] += dtau * acc;
+}
+
+__global__ void k_mxad_vel(Dims d, Tab t, WS bar, float dtau) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y;
+  const int k = blockIdx.z;
+  if (i > d.nx || j > d.ny || k > d.nz) return;
+  auto Z = [&](int ci, int cj, int ck) {
+    const size_t c = IX(ci, cj, ck);
+    return bar.f[RHO][c] + t.kap[ck] * bar.f[PI][c];
+  };
+  if (j < d.ny && k < d.nz) {
+    const float r = t.r0c[k] * t.dx_inv;
+    float acc = 0.f;
+    if (i >= 1) acc -= r * Z(i - 1, j, k);
+    if (i < d.nx) acc += r * Z(i, j, k);
+    bar.f[U][IX(i, j, k)] += dtau * acc;
+  }
+  if (i < d.nx && k < d.nz) {
+    const float r = t.r0c[k] * t.dy_inv;
+    float acc = 0.f;
+    if (j >= 1) acc -= r * Z(i, j - 1, k);
+    if (j < d.ny) acc += r * Z(i, j, k);
+    bar.f[V][IX(i, j, k)] += dtau * acc;
+  }
+  if (i < d.nx && j < d.ny) {
+    float acc = 0.f;
+    if (k >= 1) acc -= t.rfz[k] * t.idzc[k - 1] * Z(i, j, k - 1);
+    if (k < d.nz) acc += t.rfz[k] * t.idzc[k] * Z(i, j, k);
+    bar.f[W][IX(i, j, k)] += dtau * acc;
+  }
+}
+
+void mixed_fb_substep_ad(const Dims& d, const Tab& t, const WS& bar, float dtau, cudaStream_t stream) {
+  const dim3 b(32, 4);
+  k_mxad_pi<<<g3(d.nx, d.ny, d.nz, b), b, 0, stream>>>(d, t, bar, dtau);
+  k_mxad_vel<<<g3(d.nx + 1, d.ny + 1, d.nz + 1, b), b, 0, stream>>>(d, t, bar, dtau);
+}
+
 void mixed_fb_substep(const Dims& d, const Tab& t, const Flags& fl, const WS& win, const WS& wout, float dtau,
                       cudaStream_t stream) {
   const dim3 b(32, 4);
