@@ -155,3 +155,23 @@ def test_groups_refuse_models_with_physics(vg):
         a.set_physics_kessler(None)
         with vg.Group([a, b]) as g:
             g.step(2.0, 4, 1)
+
+
+def test_fp64_physics_graph_replay_and_errors(vg):
+    """FP64 model: graph replay with the package equals eager steps bit for
+    bit; asking for a tendency without a package is an error."""
+    s = setup(vg)
+    kg = vg.Kessler.defaults(exner_offset=0)
+    with vg.Model(s, vg.FP64) as a, vg.Model(s, vg.FP64) as b:
+        with pytest.raises(vg.VibeError):
+            a.physics_tendency(1.0)
+        st = with_clouds(vg, s, a.state())
+        a.set_state(st)
+        b.set_state(st)
+        a.set_physics_kessler(kg)
+        b.set_physics_kessler(kg)
+        b.set_graph(0)
+        a.step(2.0, 4, 3)
+        b.step(2.0, 4, 3)
+        for x, y in zip(a.state(), b.state()):
+            assert np.array_equal(x, y)
