@@ -5,6 +5,7 @@
 // reference's formulas), device buffers, the per-step kernel schedule for
 // both precisions, and the C ABI declared in include/vibe_gb300.h.
 // Nothing here computes the step on the CPU: every state update is a kernel.
+#include <algorithm>
 #include <cmath>
 #include <cstdint>
 #include <cstdio>
@@ -1372,9 +1373,14 @@ int vibe_gb300_autotune(vibe_gb300_model* m, double dt, int n_sub, vibe_gb300_tu
   }
   // stage levels per block around the built-in choice
   const int base = mixed_stage_levels(m->d);
-  const int cand[] = {m->d.nz, (m->d.nz + 1) / 2, (m->d.nz + 2) / 3, (m->d.nz + 3) / 4, base / 2, base * 2};
+  // the chunk sizes that split the column evenly, the built-in one halved and
+  // doubled, and the short chunks around it (wave quantisation of the grid)
+  const int cand[] = {m->d.nz, (m->d.nz + 1) / 2, (m->d.nz + 2) / 3, (m->d.nz + 3) / 4, base / 2, base * 2,
+                      base - 2, base - 1, base + 1, base + 2, base + 3};
+  std::vector<int> seen;
   for (int v : cand) {
-    if (rc || v < 4 || v > m->d.nz || v == base) continue;
+    if (rc || v < 4 || v > m->d.nz || v == base || std::find(seen.begin(), seen.end(), v) != seen.end()) continue;
+    seen.push_back(v);
     cur = best;
     cur.stage_levels = v;
     rc = trial(cur, &ms);
