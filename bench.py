@@ -564,8 +564,8 @@ def main():
     ap.add_argument("--no-window", action="store_true", help="skip the TL/AD assimilation-window leg")
     ap.add_argument("--no-tune", action="store_true", help="skip the autotuner (built-in launch shapes)")
     ap.add_argument("--no-physics", action="store_true", help="skip the Kessler physics-coupling leg")
-    ap.add_argument("--only", choices=["all", "mixed", "physics"], default="all",
-                    help="mixed: time the mixed path only (no e2e, no FP64 leg); physics: the physics leg only")
+    ap.add_argument("--only", choices=["all", "mixed", "physics", "nest"], default="all",
+                    help="mixed: time the mixed path only (no e2e, no FP64 leg); physics / nest: that leg only")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -595,6 +595,10 @@ def main():
     import vibe_gb300 as vg
     if args.only == "physics":
         print(json.dumps({"only": "physics", "physics_coupling": physics_leg(vg, torch, nx=args.nx, ny=args.ny)}))
+        ranks.close()
+        return
+    if args.only == "nest":
+        print(json.dumps({"only": "nest", "batched_nests": nest_leg(vg, torch, args.warmup)}))
         ranks.close()
         return
     setup = case_setup(vg.Setup, args.nx, args.ny)

@@ -1326,6 +1326,7 @@ int vibe_gb300_autotune(vibe_gb300_model* m, double dt, int n_sub, vibe_gb300_tu
   if (!m || !(dt > 0.0) || !out) return fail(VIBE_GB300_EBADARG, "bad argument");
   if (m->precision != VIBE_GB300_MIXED) return fail(VIBE_GB300_EUNSUPPORTED, "the autotuner tunes the mixed path");
   CUDA_OK(cudaStreamSynchronize(m->stream));
+  const int cur0 = m->cur;  // the trials' steps flip the state parity; it is put back with the state
   const size_t n = m->d.plane * (size_t)(m->d.nz + 1);
   std::vector<void*> keep(NSPECIES, nullptr);
   auto release = [&]() {
@@ -1389,6 +1390,7 @@ int vibe_gb300_autotune(vibe_gb300_model* m, double dt, int n_sub, vibe_gb300_tu
   }
   mixed_set_tune(m->d, rc ? MixedTune{} : best);
   drop_graphs(m);
+  m->cur = cur0;
   for (int q = 0; q < NSPECIES; ++q)
     cudaMemcpyAsync(m->S[m->cur][q], keep[q], n * sizeof(double), cudaMemcpyDeviceToDevice, m->stream);
   const int rs = sync_working(m);
