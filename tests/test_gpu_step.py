@@ -433,6 +433,12 @@ def test_autotune_keeps_the_update(vg):
         a.step(2.0, 4, 3)
         assert_state_close(vg, s, a.state(), before, 1e-6, range(7), "tuned vs built-in launch shapes")
         a.set_tuning()
+        # tuning leaves the state parity too: a fresh model joins it in a group
+        a.restore_snapshot()
+        a.autotune(2.0, 4)
+        a.set_tuning()
+        with vg.Model(s, vg.MIXED) as b, vg.Group([a, b]) as g:
+            g.step(2.0, 4, 1)
 
 
 def test_step_io_pipeline_matches_synchronous_steps(vg):
