@@ -194,6 +194,9 @@ vibe_stream_t vibe_gb300_nested_stream(vibe_gb300_nested *n);
  * propagate_with_trajectory, :749-765). States are copied to device
  * checkpoints every `every` steps; the adjoint recomputes each segment from
  * its checkpoint (CheckpointStrategy::Recompute, tangent_linear.hpp:56-61).
+ * every = 0 chooses by free device memory: every step stored when the whole
+ * trajectory fits (StoreAll), else checkpoints every ceil(sqrt(n_steps/2))
+ * steps with recomputation; window_stats reports the choice.
  * Both sweeps start from the model's current state and leave it there.
  * Perturbations: 12 FieldT host arrays (species order), halos pass through.
  * window_stats: device time of the last sweep, checkpoint and segment memory. */

@@ -163,3 +163,20 @@ def test_window_dot_product(vg, mixed, tol):
             ms, ck, sg = w.stats()
             assert ck == 3 * sg // 6 and ms > 0.0
         assert abs(lhs - rhs) <= tol * max(abs(lhs), abs(rhs)), (lhs, rhs)
+
+
+def test_window_automatic_checkpointing(vg):
+    """every = 0: the small window fits in device memory, so every step is
+    stored (no recomputation); TL and AD are the bits of the checkpointed and
+    recomputed window."""
+    s, m, t = window_case(vg, vg.FP64, 0)
+    with m, t:
+        dx, dy = perturb(vg, s, m, 5), perturb(vg, s, m, 6)
+        with vg.Window(m, t, DT_W, NSUB_W, 7, every=0, tl_substeps=TLSUB) as w:
+            tl0, ad0 = w.tl(dx), w.ad(dy)
+            _, ck, sg = w.stats()
+            assert ck == 7 * sg // 2  # 7 checkpoints, a one-step segment double-buffered
+        with vg.Window(m, t, DT_W, NSUB_W, 7, every=3, tl_substeps=TLSUB) as w:
+            tl3, ad3 = w.tl(dx), w.ad(dy)
+        for a, b in zip(tl0 + ad0, tl3 + ad3):
+            assert np.array_equal(a, b)

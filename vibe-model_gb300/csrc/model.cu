@@ -2333,12 +2333,30 @@ extern "C" {
 
 int vibe_gb300_window_create(vibe_gb300_model* m, vibe_tlad* t, double dt, int n_sub, int n_steps, int every,
                              int tl_substeps, vibe_gb300_window** out) {
-  if (!m || !t || !out || !(dt > 0.0) || n_steps < 1 || every < 1 || tl_substeps < 1)
+  if (!m || !t || !out || !(dt > 0.0) || n_steps < 1 || every < 0 || tl_substeps < 1)
     return fail(VIBE_GB300_EBADARG, "bad argument");
   int nx, ny, nz;
   vgb::tlad_grid(t, &nx, &ny, &nz);
   if (nx != m->d.nx || ny != m->d.ny || nz != m->d.nz)
     return fail(VIBE_GB300_EBADARG, "the TL/AD grid differs from the model's");
+  if (every == 0) {
+    // automatic: store every step when the whole trajectory (n_steps
+    // checkpoints and a two-state segment) fits in 80 % of the free device
+    // memory; otherwise checkpoint every ceil(sqrt(n_steps / 2)) steps, which
+    // minimises checkpoints + double-buffered segment, and recompute
+    size_t free_b = 0, total_b = 0;
+    CUDA_OK(cudaMemGetInfo(&free_b, &total_b));
+    const double state_b = (double)state_count(m) * sizeof(double) * NSPECIES;
+    const double budget = 0.8 * (double)free_b;
+    if ((n_steps + 2.0) * state_b <= budget) {
+      every = 1;
+    } else {
+      every = std::max(1, (int)std::ceil(std::sqrt(n_steps / 2.0)));
+      const int nck = (n_steps + every - 1) / every;
+      if ((nck + 2.0 * every) * state_b > budget)
+        return fail(VIBE_GB300_EDEVICE, "the window's checkpoints do not fit in device memory");
+    }
+  }
   auto* w = new vibe_gb300_window();
   w->m = m;
   w->t = t;
