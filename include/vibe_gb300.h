@@ -239,6 +239,11 @@ int vibe_gb300_acoustic_tl_f32(vibe_gb300_model *m, double dtau, int n_sub, cons
                                double *const *out);
 int vibe_gb300_acoustic_ad_f32(vibe_gb300_model *m, double dtau, int n_sub, const double *const *in,
                                double *const *out);
+/* The FP32 pair for the mixed model's own consistent HEVI substep (column
+ * kernel + u/v update, hevi_beta of the model); the adjoint transposes the
+ * column system through its LU factors. */
+int vibe_gb300_hevi_tl_f32(vibe_gb300_model *m, double dtau, int n_sub, const double *const *in, double *const *out);
+int vibe_gb300_hevi_ad_f32(vibe_gb300_model *m, double dtau, int n_sub, const double *const *in, double *const *out);
 int vibe_gb300_hevi_ad(vibe_gb300_model *m, double dtau, int n_sub, const double *const *in, double *const *out);
 int vibe_gb300_hevi_substep(vibe_gb300_model *m, double dtau);
 /* Autotuner of the mixed step: times, on this model's grid, the launch shapes

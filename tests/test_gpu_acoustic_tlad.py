@@ -245,3 +245,27 @@ def test_fp32_acoustic_tl_ad(vg):
     with vg.Model(s, vg.FP64) as f64:
         with pytest.raises(vg.VibeError):
             f64.acoustic_tl_f32(0.5, 1, random_fields(vg, f64, 33))
+
+
+def test_fp32_hevi_tl_ad(vg):
+    """The mixed model's own FP32 HEVI substep (TMA column kernel + u/v
+    update) as a linear map: it tracks the FP64 HEVI tangent-linear to 1e-5
+    of each field's scale over 3 substeps, and its adjoint (the column system
+    transposed through its LU factors) passes the dot-product test to 1e-5;
+    a step afterwards still matches a model that never ran it (the column
+    factors are put back for the step's own dt)."""
+    s = setup(vg, terrain_kind=0, ref_kind=0, acoustic_mode=2, hevi_beta=0.6)
+    with vg.Model(s, vg.MIXED) as m, vg.Model(s, vg.MIXED) as ref:
+        dx, dy = random_fields(vg, m, 41), random_fields(vg, m, 42)
+        t32 = m.hevi_tl_f32(1.5, 3, dx)
+        t64 = m.hevi_tl(1.5, 3, dx)
+        for f, sp in enumerate(FIELDS):
+            g, r = vg.interior(s, sp, t32[f]), vg.interior(s, sp, t64[f])
+            assert np.abs(g - r).max() <= 1e-5 * np.abs(r).max(), (vg.SPECIES[sp], np.abs(g - r).max())
+        a32 = m.hevi_ad_f32(1.5, 3, dy)
+        lhs, rhs = dot(t32, dy), dot(dx, a32)
+        assert abs(lhs - rhs) <= 1e-5 * max(abs(lhs), abs(rhs)), (lhs, rhs)
+        m.step(2.0, 4, 2)
+        ref.step(2.0, 4, 2)
+        for a, b in zip(m.state(), ref.state()):
+            assert np.array_equal(a, b)

@@ -83,6 +83,8 @@ struct vibe_gb300_model {
   double* tmp[NSPECIES] = {};
   double* lin[5] = {};  // u, v, w, rho, pi perturbations of the acoustic TL/AD (allocated on first use)
   float* lin32[2][5] = {};         // FP32 acoustic TL/AD (mixed models): ping-pong perturbations
+  float* lin32_dh = nullptr;       // FP32 HEVI AD: bar of the horizontal divergence
+  float* lin32_scr = nullptr;      // FP32 HEVI AD: per-column work
   double* lin_tmp[3] = {};         // HEVI TL: the column solve's w, rho, pi outputs
   double* lin_scr = nullptr;       // HEVI TL/AD: per-column work
   double* lin_dh = nullptr;        // HEVI AD: bar of the horizontal divergence
@@ -1210,7 +1212,7 @@ namespace {
 // the mixed model's own FP32 forward-backward substep (mixed_fb_substep) on
 // perturbations of (u, v, w, rho', pi'), and its adjoint
 int acoustic_linear_f32(vibe_gb300_model* m, double dtau, int n_sub, const double* const* in, double* const* out,
-                        bool adjoint) {
+                        bool adjoint, bool hevi = false) {
   if (!m || !in || !out || n_sub < 0) return fail(VIBE_GB300_EBADARG, "bad argument");
   if (m->precision != VIBE_GB300_MIXED) return fail(VIBE_GB300_EUNSUPPORTED, "the FP32 form needs a mixed model");
   for (int f = 0; f < 5; ++f)
@@ -1220,6 +1222,14 @@ int acoustic_linear_f32(vibe_gb300_model* m, double dtau, int n_sub, const doubl
     for (int b = 0; b < 2; ++b)
       for (int f = 0; f < 5; ++f)
         if (int rc = dalloc(m, &m->lin32[b][f], nfield)) return rc;
+  if (hevi && !m->lin32_dh) {
+    if (int rc = dalloc(m, &m->lin32_dh, nfield)) return rc;
+    if (int rc = dalloc(m, &m->lin32_scr, (size_t)m->d.nx * m->d.ny * (4 * (size_t)m->d.nz + 2))) return rc;
+  }
+  if (hevi) {  // the column factors for this dtau in stage slot 0, as vibe_gb300_hevi_substep sets them
+    m->cfg_dt = -1.0;
+    if (int rc = configure_dt(m, 3.0 * dtau, 1)) return rc;
+  }
   const dim3 bl(32, 4);
   auto ws_lin = [&](int b) {
     WS w;
@@ -1240,7 +1250,17 @@ int acoustic_linear_f32(vibe_gb300_model* m, double dtau, int n_sub, const doubl
   }
   int cur = 0;
   for (int n = 0; n < n_sub; ++n) {
-    if (adjoint) {
+    if (hevi) {
+      if (adjoint) {
+        mixed_hevi_substep_ad(m->d, m->tab, m->fl, ws_lin(0), m->d_lu, m->lin32_dh, m->lin32_scr, (float)dtau,
+                              m->stream);
+      } else {
+        if (mixed_hevi_substep(m->d, m->tab, m->fl, ws_lin(cur), ws_lin(1 - cur), (float)dtau, m->d_lu, m->d_err,
+                               m->stream))
+          return fail(VIBE_GB300_EDEVICE, "TMA descriptor creation failed (cuTensorMapEncodeTiled)");
+        cur = 1 - cur;
+      }
+    } else if (adjoint) {
       mixed_fb_substep_ad(m->d, m->tab, ws_lin(0), (float)dtau, m->stream);
     } else {
       mixed_fb_substep(m->d, m->tab, m->fl, ws_lin(cur), ws_lin(1 - cur), (float)dtau, m->stream);
@@ -1272,6 +1292,14 @@ int vibe_gb300_acoustic_tl_f32(vibe_gb300_model* m, double dtau, int n_sub, cons
 int vibe_gb300_acoustic_ad_f32(vibe_gb300_model* m, double dtau, int n_sub, const double* const* in,
                                double* const* out) {
   return acoustic_linear_f32(m, dtau, n_sub, in, out, true);
+}
+
+int vibe_gb300_hevi_tl_f32(vibe_gb300_model* m, double dtau, int n_sub, const double* const* in, double* const* out) {
+  return acoustic_linear_f32(m, dtau, n_sub, in, out, false, true);
+}
+
+int vibe_gb300_hevi_ad_f32(vibe_gb300_model* m, double dtau, int n_sub, const double* const* in, double* const* out) {
+  return acoustic_linear_f32(m, dtau, n_sub, in, out, true, true);
 }
 
 int vibe_gb300_acoustic_tl(vibe_gb300_model* m, double dtau, int n_sub, const double* const* in, double* const* out) {

@@ -112,6 +112,10 @@ int mixed_hevi_column(const Dims& d, const Tab& t, const Flags& fl, const WS& wi
 void mixed_uv_backward(const Dims& d, const Tab& t, const WS& win, const WS& wout, float dtau, cudaStream_t stream);
 // adjoint of mixed_fb_substep, in place on bars of (u, v, w, rho', pi')
 void mixed_fb_substep_ad(const Dims& d, const Tab& t, const WS& bar, float dtau, cudaStream_t stream);
+// adjoint of mixed_hevi_substep (lu: the column factors for dtau), in place;
+// bdh: nfield floats, scratch: nx*ny*(4nz+2) floats
+void mixed_hevi_substep_ad(const Dims& d, const Tab& t, const Flags& fl, const WS& bar, const float* lu, float* bdh,
+                           float* scratch, float dtau, cudaStream_t stream);
 // uv_dtau != 0: also applies the last substep's u/v backward update (the
 // in-place mixed_uv_backward launch is then left out)
 void mixed_finish(const Dims& d, const Tab& t, const Flags& fl, const WS& wfin, const WS& wst, const WS& w0,

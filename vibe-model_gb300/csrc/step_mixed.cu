@@ -1194,7 +1194,7 @@ int mixed_stage(const Dims& d, const Tab& t, const Flags& fl, const WS& win, con
 // pressure-gradient coefficients of its faces, uniform per level) and then
 // the transposed mass phase (each face gathers the divergence of its two
 // cells, with Z = bar_rho' + kappa bar_pi'); in place on the bars.
-__global__ void k_mxad_pi(Dims d, Tab t, WS bar, float dtau) {
+__global__ void k_mxad_pi(Dims d, Tab t, WS bar, float dtau, int with_w) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
   const int k = blockIdx.z;
@@ -1212,9 +1212,11 @@ __global__ void k_mxad_pi(Dims d, Tab t, WS bar, float dtau) {
   if (j == 0) acc -= cv * bv[IX(i, 0, k)];
   // w faces: face f uses pi'(min(f, nz-1)) - pi'(max(f-1, 0)) with -cp tfz(f) idzw(f)
   auto cw = [&](int f) { return -cp * t.tfz[f] * t.idzw[f]; };
-  acc += cw(k) * bw[IX(i, j, k)] - cw(k + 1) * bw[IX(i, j, k + 1)];
-  if (k == d.nz - 1) acc += cw(d.nz) * bw[IX(i, j, d.nz)];
-  if (k == 0) acc -= cw(0) * bw[IX(i, j, 0)];
+  if (with_w) {
+    acc += cw(k) * bw[IX(i, j, k)] - cw(k + 1) * bw[IX(i, j, k + 1)];
+    if (k == d.nz - 1) acc += cw(d.nz) * bw[IX(i, j, d.nz)];
+    if (k == 0) acc -= cw(0) * bw[IX(i, j, 0)];
+  }
   bar.f[PI][IX(i, j, k)] += dtau * acc;
 }
 
@@ -1249,9 +1251,105 @@ __global__ void k_mxad_vel(Dims d, Tab t, WS bar, float dtau) {
   }
 }
 
+// adjoint of one standalone FP32 HEVI substep (the column kernel without a
+// pending u/v update, then the in-place u/v update): the u/v gradient
+// transposed, the column transposed (the steps of hevi2_body in reverse; the
+// column system A = L U, with L = (la sub, 1/li diagonal) and U = (1, lc
+// super), transposed as U^T z = bar_x forward and L^T y = z backward), and the
+// horizontal divergence transposed
+__global__ void k_mxad_hevi_column(Dims d, Tab t, Flags fl, const float* __restrict__ lu, WS bar,
+                                   float* __restrict__ bdh, float* __restrict__ scratch, float dtau) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y;
+  if (i >= d.nx || j >= d.ny) return;
+  const int nz = d.nz;
+  const float b = (float)fl.hevi_beta, ob = 1.f - b, cp = (float)kCp;
+  const float* la = lu;
+  const float* lc = lu + nz;
+  const float* li = lu + 2 * nz;
+  float* bw = bar.f[W];
+  const float* brho = bar.f[RHO];
+  float* bpi = bar.f[PI];
+  const size_t col = (size_t)j * d.nx + i;
+  float* ya = scratch + col * (4 * (size_t)nz + 2);  // nz
+  float* bwn = ya + nz;                              // nz+1
+  float* dvo = bwn + nz + 1;                         // nz
+  float* dvt = dvo + nz;                             // nz
+  auto rho_bar = [&](int k) { return brho[IX(i, j, k)]; };
+  for (int k = 0; k <= nz; ++k) {  // wn: w_out and dv_new of the cells around face k
+    float g = bw[IX(i, j, k)];
+    if (k < nz) g += t.rfz[k] * t.idzc[k] * (dtau * b * rho_bar(k));
+    if (k >= 1) g -= t.rfz[k] * t.idzc[k - 1] * (dtau * b * rho_bar(k - 1));
+    bwn[k] = g;
+  }
+  for (int k = 0; k < nz; ++k) ya[k] = bpi[IX(i, j, k)];  // pi_out = x
+  for (int k = 1; k < nz; ++k) {  // wn = wt - cb_k (x_k - x_{k-1})
+    const float cb = dtau * b * cp * t.tfz[k] * t.idzw[k];
+    ya[k] -= cb * bwn[k];
+    ya[k - 1] += cb * bwn[k];
+  }
+  for (int k = 1; k < nz; ++k) ya[k] -= lc[k - 1] * ya[k - 1];           // U^T z = bar_x
+  ya[nz - 1] *= li[nz - 1];                                              // L^T y = z
+  for (int k = nz - 2; k >= 0; --k) ya[k] = (ya[k] - la[k + 1] * ya[k + 1]) * li[k];
+  for (int k = 0; k < nz; ++k) {  // rhs = pi + dtau kappa (Dh + ob dv_old + b dv_t); rho += dtau (Dh + ob dv_old)
+    const float kp = dtau * t.kap[k] * ya[k];
+    bdh[IX(i, j, k)] = dtau * rho_bar(k) + kp;
+    dvo[k] = dtau * ob * rho_bar(k) + ob * kp;
+    dvt[k] = b * kp;
+  }
+  for (int k = 0; k <= nz; ++k) {  // bar_wt
+    float g = bwn[k];
+    if (k < nz) g += t.rfz[k] * t.idzc[k] * dvt[k];
+    if (k >= 1) g -= t.rfz[k] * t.idzc[k - 1] * dvt[k - 1];
+    bwn[k] = g;
+  }
+  for (int k = 0; k <= nz; ++k) {  // bar_w: wt's identity and dv_old
+    float g = bwn[k];
+    if (k < nz) g += t.rfz[k] * t.idzc[k] * dvo[k];
+    if (k >= 1) g -= t.rfz[k] * t.idzc[k - 1] * dvo[k - 1];
+    bw[IX(i, j, k)] = g;
+  }
+  for (int k = 0; k < nz; ++k) {  // bar_pi: rhs's pi and wt's gradient
+    float g = ya[k];
+    if (k >= 1) g -= dtau * ob * cp * t.tfz[k] * t.idzw[k] * bwn[k];
+    if (k + 1 < nz) g += dtau * ob * cp * t.tfz[k + 1] * t.idzw[k + 1] * bwn[k + 1];
+    bpi[IX(i, j, k)] = g;
+  }
+}
+
+__global__ void k_mxad_dh(Dims d, Tab t, const float* __restrict__ bdh, WS bar) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y;
+  const int k = blockIdx.z;
+  if (i > d.nx || j > d.ny || k >= d.nz) return;
+  if (j < d.ny) {
+    const float r = t.r0c[k] * t.dx_inv;
+    float acc = 0.f;
+    if (i >= 1) acc -= r * bdh[IX(i - 1, j, k)];
+    if (i < d.nx) acc += r * bdh[IX(i, j, k)];
+    bar.f[U][IX(i, j, k)] += acc;
+  }
+  if (i < d.nx) {
+    const float r = t.r0c[k] * t.dy_inv;
+    float acc = 0.f;
+    if (j >= 1) acc -= r * bdh[IX(i, j - 1, k)];
+    if (j < d.ny) acc += r * bdh[IX(i, j, k)];
+    bar.f[V][IX(i, j, k)] += acc;
+  }
+}
+
+void mixed_hevi_substep_ad(const Dims& d, const Tab& t, const Flags& fl, const WS& bar, const float* lu, float* bdh,
+                           float* scratch, float dtau, cudaStream_t stream) {
+  const dim3 b(32, 4);
+  k_mxad_pi<<<g3(d.nx, d.ny, d.nz, b), b, 0, stream>>>(d, t, bar, dtau, 0);
+  k_mxad_hevi_column<<<dim3((d.nx + 31) / 32, (d.ny + 3) / 4), b, 0, stream>>>(d, t, fl, lu, bar, bdh, scratch,
+                                                                                dtau);
+  k_mxad_dh<<<g3(d.nx + 1, d.ny + 1, d.nz, b), b, 0, stream>>>(d, t, bdh, bar);
+}
+
 void mixed_fb_substep_ad(const Dims& d, const Tab& t, const WS& bar, float dtau, cudaStream_t stream) {
   const dim3 b(32, 4);
-  k_mxad_pi<<<g3(d.nx, d.ny, d.nz, b), b, 0, stream>>>(d, t, bar, dtau);
+  k_mxad_pi<<<g3(d.nx, d.ny, d.nz, b), b, 0, stream>>>(d, t, bar, dtau, 1);
   k_mxad_vel<<<g3(d.nx + 1, d.ny + 1, d.nz + 1, b), b, 0, stream>>>(d, t, bar, dtau);
 }
 

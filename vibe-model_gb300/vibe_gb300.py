@@ -88,6 +88,8 @@ _sigs = {
     "vibe_gb300_hevi_tl": (_I, [_vp, _D, _I, ctypes.POINTER(_dp), ctypes.POINTER(_dp)]),
     "vibe_gb300_acoustic_tl_f32": (_I, [_vp, _D, _I, ctypes.POINTER(_dp), ctypes.POINTER(_dp)]),
     "vibe_gb300_acoustic_ad_f32": (_I, [_vp, _D, _I, ctypes.POINTER(_dp), ctypes.POINTER(_dp)]),
+    "vibe_gb300_hevi_tl_f32": (_I, [_vp, _D, _I, ctypes.POINTER(_dp), ctypes.POINTER(_dp)]),
+    "vibe_gb300_hevi_ad_f32": (_I, [_vp, _D, _I, ctypes.POINTER(_dp), ctypes.POINTER(_dp)]),
     "vibe_gb300_hevi_ad": (_I, [_vp, _D, _I, ctypes.POINTER(_dp), ctypes.POINTER(_dp)]),
     "vibe_gb300_hevi_substep": (_I, [_vp, _D]),
     "vibe_gb300_sponge": (_I, [_vp, _D]),
@@ -313,6 +315,14 @@ class Model:
     def acoustic_ad_f32(self, dtau, n_sub, fields):
         """Adjoint of acoustic_tl_f32."""
         return self._acoustic_linear(lib.vibe_gb300_acoustic_ad_f32, dtau, n_sub, fields)
+
+    def hevi_tl_f32(self, dtau, n_sub, fields):
+        """FP32 tangent-linear of the mixed model's HEVI substep."""
+        return self._acoustic_linear(lib.vibe_gb300_hevi_tl_f32, dtau, n_sub, fields)
+
+    def hevi_ad_f32(self, dtau, n_sub, fields):
+        """Adjoint of hevi_tl_f32."""
+        return self._acoustic_linear(lib.vibe_gb300_hevi_ad_f32, dtau, n_sub, fields)
 
     def hevi_tl(self, dtau, n_sub, fields):
         """Tangent-linear of n_sub consistent HEVI substeps on [u, v, w, rho, pi]."""
