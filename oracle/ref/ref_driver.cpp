@@ -21,6 +21,13 @@
 //     and the moisture species (src/dyn/equations.cpp:129-137) with
 //     Advection::scalar in WENO5 flux form (src/dyn/advection.cpp:144-187)
 //     and re-applies the positivity clip (equations.cpp:139-149).
+//   * the composition flags of vo_setup (pgf_perturbation, split_fast,
+//     weno_advective, acoustic_mode 0/1/2, hevi_beta, w_rigid) are composed
+//     from the reference's own operators (Equations::tendencies,
+//     Equations::acoustic_tendencies, Advection::scalar,
+//     AcousticSubstepper::step, timeint::thomas_solve): see slow_tendency,
+//     acoustic_substep and consistent_hevi_substep below. This is an
+//     independent second statement of the flags the plain-C oracle restates.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -81,37 +88,209 @@ const grid::Field<Real>& reffield(const vref_model* m, int which) {
   }
 }
 
-void slow_tendency(vref_model* m, dyn::State& s, dyn::Tendency& d) {
-  m->eq->tendencies(s, d);
-  if (!m->setup.weno_scalars) return;
-  const grid::Grid& g = *m->grid;
-  m->weno->scalar(s.theta(), s.u(), s.v(), s.w(), s.rho(), d.theta());
-  const int last = m->setup.moist ? static_cast<int>(dyn::Species::Qg)
-                                  : static_cast<int>(dyn::Species::Qv);
-  for (int sp = static_cast<int>(dyn::Species::Qv); sp <= last; ++sp) {
-    const auto species = static_cast<dyn::Species>(sp);
-    m->weno->scalar(s.field(species), s.u(), s.v(), s.w(), s.rho(), d.field(species));
+// The state the pressure-gradient terms see: with pgf_perturbation = 1 a
+// copy whose Exner field holds pi' = pi - pi0 (every other field as given),
+// so Equations::tendencies / acoustic_tendencies (equations.cpp:70-110,
+// 157-185) difference pi' instead of the total Exner function.
+dyn::State pgf_view(const vref_model* m, const dyn::State& s) {
+  dyn::State v = s.clone();
+  if (m->setup.pgf_perturbation) {
+    auto& p = v.pi().storage();
+    const auto& p0 = m->ref->pi0().storage();
+    for (Size e = 0; e < p.size(); ++e) p[e] = p[e] - p0[e];
   }
-  for (int sp = static_cast<int>(dyn::Species::Qv); sp <= static_cast<int>(dyn::Species::Qg); ++sp) {
-    const auto species = static_cast<dyn::Species>(sp);
-    const grid::Field<Real>& q = s.field(species);
-    grid::Field<Real>& dq = d.field(species);
-    for (Int k = 0; k < g.nz(); ++k)
-      for (Int j = 0; j < g.ny(); ++j)
-        for (Int i = 0; i < g.nx(); ++i)
-          if (q(i, j, k) <= Real(0) && dq(i, j, k) < Real(0)) dq(i, j, k) = Real(0);
+  return v;
+}
+
+// Slow tendency of the composition the setup selects, built from the
+// reference's own operators only:
+//   * Equations::tendencies (equations.cpp:60-150) on pgf_view(s); the
+//     divergence damping of pi (damping.cpp:43-74, the only writer of the pi
+//     tendency there) keeps acting on the total Exner function;
+//   * weno_scalars: Advection::scalar in WENO5 flux form (advection.cpp:144-187)
+//     for theta and the moisture species, then the positivity clip again
+//     (equations.cpp:139-149);
+//   * weno_advective: + q div(u). Advection::scalar of a field of ones is
+//     exactly -div(u) with the same face winds, spacings and vertical-flux
+//     condition (every WENO5 candidate of a constant is the constant, so the
+//     face flux is the face wind), so q div(u) = q * (-scalar(1));
+//   * split_fast: minus Equations::acoustic_tendencies (equations.cpp:152-209)
+//     of the same state for u, v, w and rho.
+void slow_tendency(vref_model* m, dyn::State& s, dyn::Tendency& d) {
+  const grid::Grid& g = *m->grid;
+  const dyn::State v = pgf_view(m, s);
+  m->eq->tendencies(v, d);
+  if (m->setup.pgf_perturbation && m->setup.divergence_damping > 0.0) {
+    m->eq->tendencies(s, *m->scratch);
+    d.pi().storage() = m->scratch->pi().storage();
+  }
+  if (m->setup.weno_scalars) {
+    grid::Field<Real> negdiv(g, grid::Stagger::Cell, "negdiv");
+    if (m->setup.weno_advective) {
+      grid::Field<Real> ones(g, grid::Stagger::Cell, "ones");
+      ones.fill(Real(1));
+      m->weno->scalar(ones, s.u(), s.v(), s.w(), s.rho(), negdiv);
+    }
+    const int last = m->setup.moist ? static_cast<int>(dyn::Species::Qg)
+                                    : static_cast<int>(dyn::Species::Qv);
+    for (int sp = static_cast<int>(dyn::Species::Theta); sp <= last; ++sp) {
+      if (sp == static_cast<int>(dyn::Species::Pi)) continue;
+      const auto species = static_cast<dyn::Species>(sp);
+      const grid::Field<Real>& q = s.field(species);
+      grid::Field<Real>& dq = d.field(species);
+      m->weno->scalar(q, s.u(), s.v(), s.w(), s.rho(), dq);
+      if (!m->setup.weno_advective) continue;
+      for (Int k = 0; k < g.nz(); ++k)
+        for (Int j = 0; j < g.ny(); ++j)
+          for (Int i = 0; i < g.nx(); ++i) dq(i, j, k) += q(i, j, k) * -negdiv(i, j, k);
+    }
+    for (int sp = static_cast<int>(dyn::Species::Qv); sp <= static_cast<int>(dyn::Species::Qg); ++sp) {
+      const auto species = static_cast<dyn::Species>(sp);
+      const grid::Field<Real>& q = s.field(species);
+      grid::Field<Real>& dq = d.field(species);
+      for (Int k = 0; k < g.nz(); ++k)
+        for (Int j = 0; j < g.ny(); ++j)
+          for (Int i = 0; i < g.nx(); ++i)
+            if (q(i, j, k) <= Real(0) && dq(i, j, k) < Real(0)) dq(i, j, k) = Real(0);
+    }
+  }
+  if (m->setup.split_fast) {
+    m->eq->acoustic_tendencies(v, *m->scratch);
+    const dyn::Species fast[4] = {dyn::Species::U, dyn::Species::V, dyn::Species::W, dyn::Species::Rho};
+    for (const auto sp : fast) {
+      auto& t = d.field(sp).storage();
+      const auto& f = m->scratch->field(sp).storage();
+      for (Size e = 0; e < t.size(); ++e) t[e] -= f[e];
+    }
   }
 }
 
+// RungeKutta3Integrator::acoustic_substep (runge_kutta.cpp:65-75): forward
+// rho/pi, then u/v/w from the updated pressure (through pgf_view).
 void acoustic_substep(vref_model* m, dyn::State& s, Real dtau) {
   dyn::Tendency& sc = *m->scratch;
-  m->eq->acoustic_tendencies(s, sc);
+  m->eq->acoustic_tendencies(pgf_view(m, s), sc);
   s.rho().add_scaled(dtau, sc.rho());
   s.pi().add_scaled(dtau, sc.pi());
-  m->eq->acoustic_tendencies(s, sc);
+  m->eq->acoustic_tendencies(pgf_view(m, s), sc);
   s.u().add_scaled(dtau, sc.u());
   s.v().add_scaled(dtau, sc.v());
   s.w().add_scaled(dtau, sc.w());
+}
+
+// The vertically implicit substep of docs/design/04_time_integration.md
+// sec. 2.4 (Crank-Nicolson weight b = hevi_beta on the vertical acoustic
+// terms, explicit horizontal terms), assembled from the reference's linear
+// acoustic operator alone. With A(u, v, w, x) = Equations::acoustic_tendencies
+// of a state with winds (u, v, w) and Exner field x (pi', or total pi when
+// pgf_perturbation = 0):
+//   W(x)  = A(0, 0, 0, x).w          vertical pressure gradient on w faces
+//   R(..) = A(.., .., .., 0).rho     mass divergence, P(..) = A(..).pi its pi rate
+//   w~    = w + dtau (1-b) W(x_old)
+//   pi*   = pi + dtau [P(u,v,0) + (1-b) P(0,0,w) + b P(0,0,w~)]
+//   (I - (dtau b)^2 L) x = pi* - pi0 (or pi*),  L x = P(0, 0, W(x))
+//   w_new = w~ + dtau b W(x),  rho_new = rho + dtau [R(u,v,0) + (1-b) R(0,0,w) + b R(0,0,w_new)]
+//   pi_new = x + pi0 (or x),   u, v += dtau A(., ., ., x).u/.v
+// L is read off the reference operator itself: it couples levels of one
+// column only and is tridiagonal, so three probes (x = 1 on the levels
+// k = r mod 3) give every column's three diagonals. Each column is solved
+// with timeint::thomas_solve (helmholtz.cpp:57-86).
+void consistent_hevi_substep(vref_model* m, dyn::State& s, Real dtau) {
+  const grid::Grid& g = *m->grid;
+  const Int nx = g.nx(), ny = g.ny(), nz = g.nz();
+  const Real b = m->setup.hevi_beta, ob = Real(1) - b;
+  const bool pert = m->setup.pgf_perturbation != 0;
+  const auto& pi0 = m->ref->pi0();
+  dyn::State a(g);
+  a.set_reference(m->ref.get());
+  dyn::Tendency t(g);
+  auto zero_winds = [&]() {
+    a.u().fill(Real(0));
+    a.v().fill(Real(0));
+    a.w().fill(Real(0));
+  };
+  // x_old and W(x_old)
+  grid::Field<Real> x(g, grid::Stagger::Cell, "x");
+  for (Size e = 0; e < x.storage().size(); ++e)
+    x.storage()[e] = s.pi().storage()[e] - (pert ? pi0.storage()[e] : Real(0));
+  zero_winds();
+  a.pi() = x;
+  m->eq->acoustic_tendencies(a, t);
+  grid::Field<Real> wt = s.w();
+  wt.add_scaled(dtau * ob, t.w());
+  // horizontal and vertical mass divergences and their pi rates
+  a.pi().fill(Real(0));
+  a.u() = s.u();
+  a.v() = s.v();
+  m->eq->acoustic_tendencies(a, t);
+  const grid::Field<Real> rh = t.rho(), ph = t.pi();
+  zero_winds();
+  a.w() = s.w();
+  m->eq->acoustic_tendencies(a, t);
+  const grid::Field<Real> rv_old = t.rho(), pv_old = t.pi();
+  a.w() = wt;
+  m->eq->acoustic_tendencies(a, t);
+  const grid::Field<Real> pv_t = t.pi();
+  // L = P(0, 0, W(.)) probed per level colour
+  std::vector<grid::Field<Real>> probe;
+  for (int r = 0; r < 3; ++r) {
+    zero_winds();
+    a.pi().fill(Real(0));
+    for (Int k = r; k < nz; k += 3)
+      for (Int j = 0; j < ny; ++j)
+        for (Int i = 0; i < nx; ++i) a.pi()(i, j, k) = Real(1);
+    m->eq->acoustic_tendencies(a, t);
+    a.w() = t.w();
+    a.pi().fill(Real(0));
+    m->eq->acoustic_tendencies(a, t);
+    probe.push_back(t.pi());
+  }
+  const Real c2 = (dtau * b) * (dtau * b);
+  std::vector<Real> ta(static_cast<Size>(nz > 1 ? nz - 1 : 0)), tb(static_cast<Size>(nz)),
+      tc(static_cast<Size>(nz > 1 ? nz - 1 : 0)), rhs(static_cast<Size>(nz)), sol;
+  for (Int j = 0; j < ny; ++j)
+    for (Int i = 0; i < nx; ++i) {
+      for (Int k = 0; k < nz; ++k) {
+        tb[k] = Real(1) - c2 * probe[k % 3](i, j, k);
+        if (k > 0) ta[k - 1] = -c2 * probe[(k - 1) % 3](i, j, k);
+        if (k + 1 < nz) tc[k] = -c2 * probe[(k + 1) % 3](i, j, k);
+        const Real pstar = s.pi()(i, j, k) + dtau * (ph(i, j, k) + ob * pv_old(i, j, k) + b * pv_t(i, j, k));
+        rhs[k] = pstar - (pert ? pi0(i, j, k) : Real(0));
+      }
+      timeint::thomas_solve(ta, tb, tc, rhs, sol);
+      for (Int k = 0; k < nz; ++k) x(i, j, k) = sol[k];
+    }
+  // w_new = w~ + dtau b W(x); the mass update with it
+  zero_winds();
+  a.pi() = x;
+  m->eq->acoustic_tendencies(a, t);
+  const grid::Field<Real> ux = t.u(), vx = t.v();
+  grid::Field<Real> wn = wt;
+  wn.add_scaled(dtau * b, t.w());
+  a.pi().fill(Real(0));
+  a.w() = wn;
+  m->eq->acoustic_tendencies(a, t);
+  for (Int k = 0; k < nz; ++k)
+    for (Int j = 0; j < ny; ++j)
+      for (Int i = 0; i < nx; ++i) {
+        s.rho()(i, j, k) += dtau * (rh(i, j, k) + ob * rv_old(i, j, k) + b * t.rho()(i, j, k));
+        s.pi()(i, j, k) = x(i, j, k) + (pert ? pi0(i, j, k) : Real(0));
+      }
+  s.w() = wn;
+  // horizontal momentum, backward with the new pressure
+  s.u().add_scaled(dtau, ux);
+  s.v().add_scaled(dtau, vx);
+}
+
+void hevi_substep(vref_model* m, dyn::State& s, Real dtau) {
+  if (m->setup.acoustic_mode == 1) {
+    timeint::AcousticOptions opt;
+    opt.vertical_implicit = true;
+    timeint::AcousticSubstepper sub(*m->grid, opt);
+    sub.step(s, dtau, *m->ref);
+  } else {
+    consistent_hevi_substep(m, s, dtau);
+  }
 }
 
 }  // namespace
@@ -241,10 +420,23 @@ int vref_rk3_step(vref_model* m, double dt, int n_sub_in) {
       s.field(species).add_scaled(dt_stage[stage], m->slow->field(species));
     }
     const Real dtau_stage = dt_stage[stage] / static_cast<Real>(n_sub);
-    for (int n = 0; n < n_sub; ++n) acoustic_substep(m, s, dtau_stage);
+    for (int n = 0; n < n_sub; ++n) {
+      if (m->setup.acoustic_mode == 0)
+        acoustic_substep(m, s, dtau_stage);
+      else
+        hevi_substep(m, s, dtau_stage);
+    }
     if (s.has_nonfinite()) return 1;
   }
   m->eq->damping().apply_sponge(s, *m->ref, dt);
+  if (m->setup.w_rigid) {
+    const grid::Grid& g = *m->grid;
+    for (Int j = 0; j < g.ny(); ++j)
+      for (Int i = 0; i < g.nx(); ++i) {
+        s.w()(i, j, 0) = Real(0);
+        s.w()(i, j, g.nz()) = Real(0);
+      }
+  }
   s.step += 1;
   return 0;
 }
@@ -259,12 +451,7 @@ void vref_slow_tendency(vref_model* m, double* const* out) {
 
 void vref_acoustic_substep(vref_model* m, double dtau) { acoustic_substep(m, *m->state, dtau); }
 
-void vref_hevi_substep(vref_model* m, double dtau) {
-  timeint::AcousticOptions opt;
-  opt.vertical_implicit = true;
-  timeint::AcousticSubstepper sub(*m->grid, opt);
-  sub.step(*m->state, dtau, *m->ref);
-}
+void vref_hevi_substep(vref_model* m, double dtau) { hevi_substep(m, *m->state, dtau); }
 
 void vref_sponge(vref_model* m, double dt) {
   m->eq->damping().apply_sponge(*m->state, *m->ref, dt);

@@ -64,7 +64,9 @@ typedef struct vo_setup {
   double sponge_alpha, sponge_start_fraction;
   double divergence_damping;
   int divergence_order;
-  /* --- compositions the reference does not provide (not read by vref_*) ---
+  /* --- compositions the reference does not provide: the port restates them
+   * in C, the reference-linked driver composes them from the reference's
+   * own operators (oracle/ref/ref_driver.cpp) ---
    * pgf_perturbation: 0 = pressure-gradient terms act on the total Exner
    *   function, as src/dyn/equations.cpp:79,88,101,164,173,183 compute;
    *   1 = they act on pi' = pi - pi0, the form the reference documents

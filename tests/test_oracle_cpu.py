@@ -113,6 +113,165 @@ def test_reference_composition_diverges_and_documented_one_does_not(oc):
     assert np.abs(w).max() < 5.0
 
 
+# ---- the composition flags against the reference's own operators ----------
+# oracle/ref/ref_driver.cpp composes pgf_perturbation, split_fast,
+# weno_advective and w_rigid from Equations::tendencies / acoustic_tendencies
+# and Advection::scalar, and the consistent HEVI (acoustic_mode = 2) from
+# acoustic_tendencies (its column matrix probed from that operator) and
+# timeint::thomas_solve; the port restates the same flags in plain C.
+HEADLINE_FLAGS = dict(advection=5, weno_scalars=1, weno_advective=1, pgf_perturbation=1, split_fast=1, ref_kind=1)
+FLAG_CASES = [dict(HEADLINE_FLAGS, acoustic_mode=0),
+              dict(HEADLINE_FLAGS, acoustic_mode=0, moist=1, qv_surface=0.01, w_rigid=1),
+              dict(advection=4, weno_scalars=0, pgf_perturbation=1, split_fast=1, acoustic_mode=0,
+                   divergence_damping=50.0, moist=1, qv_surface=0.01, coriolis=1),
+              dict(HEADLINE_FLAGS, acoustic_mode=0, split_fast=0, terrain_kind=1, hill_h=300.0, hill_a=1500.0,
+                   hill_xc=2500.0, hill_yc=2000.0)]
+HEVI_CASES = [dict(HEADLINE_FLAGS, acoustic_mode=2, hevi_beta=0.5),
+              dict(HEADLINE_FLAGS, acoustic_mode=2, hevi_beta=0.6, w_rigid=1),
+              dict(HEADLINE_FLAGS, acoustic_mode=2, hevi_beta=0.7, pgf_perturbation=0, ref_kind=0, terrain_kind=1,
+                   hill_h=300.0, hill_a=1500.0, hill_xc=2500.0, hill_yc=2000.0)]
+
+
+def _need_ref():
+    if not os.path.exists(os.path.join(os.path.dirname(GOLDEN), "..", "oracle", "_ref", "libvibe_ref.so")):
+        pytest.skip("reference-linked oracle not built (reference tree absent)")
+
+
+@pytest.mark.parametrize("case", range(len(FLAG_CASES)))
+def test_composition_flags_port_is_bit_exact_to_reference_operators(oc, case):
+    """pgf_perturbation, split_fast, weno_advective and w_rigid with the
+    explicit substep: slow tendency and two RK3 steps bit for bit."""
+    _need_ref()
+    s = small(oc, **FLAG_CASES[case])
+    a, b = oc.Model(s, "port"), oc.Model(s, "ref")
+    for x, y in zip(a.slow_tendency(), b.slow_tendency()):
+        assert np.array_equal(x, y)
+    for _ in range(2):
+        assert a.rk3_step(2.0, 3) == b.rk3_step(2.0, 3) == 0
+    for sp in range(12):
+        assert np.array_equal(a.get(sp), b.get(sp)), oc.SPECIES[sp]
+
+
+@pytest.mark.parametrize("case", range(len(HEVI_CASES)))
+def test_consistent_hevi_port_matches_reference_operators(oc, case):
+    """The consistent HEVI substep of the port against the one assembled from
+    the reference's acoustic operator and thomas_solve: from the same state,
+    every field's change agrees to 1e-11 of its size (the two differ only in
+    operation order; pi' = pi - pi0 carries ~1e-16 of pi into u and v), and
+    two full RK3 steps of the headline composition agree to 1e-9 of each
+    field's size. A sign, weight or staggering error would differ at O(1)."""
+    _need_ref()
+    s = small(oc, **HEVI_CASES[case])
+    a, b = oc.Model(s, "port"), oc.Model(s, "ref")
+    for x, y in zip(a.slow_tendency(), b.slow_tendency()):
+        assert np.array_equal(x, y)
+    assert a.rk3_step(2.0, 3) == 0
+    b.set_state(a.state())
+    x0 = a.state()
+    a.hevi_substep(0.7)
+    b.hevi_substep(0.7)
+    for sp in (0, 1, 2, 3, 5):
+        x, y, z = (oc.interior(s, sp, f) for f in (a.get(sp), b.get(sp), x0[sp]))
+        change = np.abs(x - z).max()
+        assert change > 0
+        assert np.abs(x - y).max() <= 1e-11 * change, oc.SPECIES[sp]
+    for _ in range(2):
+        assert a.rk3_step(2.0, 3) == b.rk3_step(2.0, 3) == 0
+    for sp in range(7):
+        x, y = oc.interior(s, sp, a.get(sp)), oc.interior(s, sp, b.get(sp))
+        assert np.abs(x - y).max() <= 1e-9 * max(np.abs(x).max(), 1e-30), oc.SPECIES[sp]
+
+
+K_RD, K_CP, K_CV = 287.05, 1004.64, 717.63
+
+
+def _column_case(oc, beta, nz=16):
+    """One column (nx = ny = 1, so the horizontal terms vanish) of the N =
+    0.01 profile on stretched levels, with random pi' and interior w."""
+    s = small(oc, nx=1, ny=1, nz=nz, dx=250.0, dy=250.0, z_top=4000.0, zeta_first=1.0, zeta_stretch=1.06,
+              ref_kind=1, bubble_amplitude=0.0, u_background=0.0, shear_u=0.0, qv_surface=0.0,
+              acoustic_mode=2, hevi_beta=beta, pgf_perturbation=1, split_fast=1)
+    m = oc.Model(s, "port")
+    rng = np.random.default_rng(7)
+    for sp in (0, 1):
+        m.set(sp, np.zeros(m.size(sp)))
+    w = np.zeros(m.size(2))
+    oc.interior(s, 2, w)[1:nz, 0, 0] = rng.uniform(-1.0, 1.0, nz - 1)
+    m.set(2, w)
+    pi = m.reffield(1).copy()
+    oc.interior(s, 5, pi)[:, 0, 0] += rng.uniform(-1e-3, 1e-3, nz)
+    m.set(5, pi)
+    return s, m
+
+
+def _acoustic_energy(oc, s, m):
+    """E = 1/2 sum_k (dz_k / kappa_k) pi'_k^2 + 1/2 sum_f (r_f dzf_f / (cp t_f)) w_f^2:
+    the quadratic form in which the linear column operator (w rate
+    -cp t_f d(pi')/dz on interior faces, pi' rate kappa_k * (-d(r_f w)/dz))
+    is skew-adjoint, so Crank-Nicolson at beta = 1/2 keeps it exactly."""
+    nz = s.nz
+    zeta = m.zeta()
+    dzc = np.maximum(np.diff(zeta) * s.z_top, 1.0)
+    th0 = oc.interior(s, 4, m.reffield(0))[:, 0, 0]
+    pi0 = oc.interior(s, 5, m.reffield(1))[:, 0, 0]
+    r0 = oc.interior(s, 3, m.reffield(2))[:, 0, 0]
+    kap = (K_RD / K_CV) * pi0 / np.maximum(r0, 1e-8)
+    f = np.arange(1, nz)
+    rf = 0.5 * (r0[f - 1] + r0[f])
+    tf = 0.5 * (th0[f - 1] + th0[f])
+    dzf = dzc[f]
+    pip = oc.interior(s, 5, m.get(5))[:, 0, 0] - pi0
+    w = oc.interior(s, 2, m.get(2))[1:nz, 0, 0]
+    return 0.5 * np.sum(dzc / kap * pip ** 2) + 0.5 * np.sum(rf * dzf / (K_CP * tf) * w ** 2)
+
+
+def test_consistent_hevi_conserves_linear_acoustic_energy(oc):
+    """Property of the consistent HEVI (no reference routine exists for it):
+    at beta = 1/2 it is the trapezoidal rule of the linear column acoustics,
+    so the column's acoustic energy is kept to rounding over 200 substeps
+    at a vertical Courant number far above 1; off-centred (beta = 0.6) it
+    decays monotonically; the ground and lid faces stay at rest."""
+    s, m = _column_case(oc, 0.5)
+    e0 = _acoustic_energy(oc, s, m)
+    for _ in range(200):
+        m.hevi_substep(2.0)
+    assert abs(_acoustic_energy(oc, s, m) - e0) <= 1e-10 * e0
+    w = oc.interior(s, 2, m.get(2))[:, 0, 0]
+    assert w[0] == 0.0 and w[-1] == 0.0
+    s, m = _column_case(oc, 0.6)
+    es = [_acoustic_energy(oc, s, m)]
+    for _ in range(20):
+        m.hevi_substep(2.0)
+        es.append(_acoustic_energy(oc, s, m))
+    assert all(b < a for a, b in zip(es, es[1:])) and es[-1] < 0.9 * es[0]
+
+
+def test_consistent_hevi_tends_to_forward_backward_as_dtau_shrinks(oc):
+    """One off-centred HEVI substep and one explicit forward-backward
+    substep from the same state integrate the same linear acoustics; their
+    difference, relative to the substep's change, shrinks in proportion to
+    dtau (first order), on the full 3-D state with terrain."""
+    base = dict(HEADLINE_FLAGS, terrain_kind=1, hill_h=300.0, hill_a=1500.0, hill_xc=2500.0, hill_yc=2000.0)
+    hs, fs = small(oc, acoustic_mode=2, hevi_beta=0.6, **base), small(oc, acoustic_mode=0, **base)
+    start = oc.Model(hs, "port")
+    assert start.rk3_step(1.0, 4) == 0
+    x0 = start.state()
+    ratios = []
+    for dtau in (0.08, 0.04, 0.02, 0.01):
+        h, f = oc.Model(hs, "port"), oc.Model(fs, "port")
+        h.set_state(x0)
+        f.set_state(x0)
+        h.hevi_substep(dtau)
+        f.acoustic_substep(dtau)
+        num = sum(np.linalg.norm(oc.interior(hs, sp, h.get(sp)) - oc.interior(hs, sp, f.get(sp)))
+                  / max(np.linalg.norm(oc.interior(hs, sp, x0[sp])), 1e-30) for sp in (0, 1, 2, 3, 5))
+        den = sum(np.linalg.norm(oc.interior(hs, sp, f.get(sp)) - oc.interior(hs, sp, x0[sp]))
+                  / max(np.linalg.norm(oc.interior(hs, sp, x0[sp])), 1e-30) for sp in (0, 1, 2, 3, 5))
+        ratios.append(num / den)
+    for a, b in zip(ratios, ratios[1:]):
+        assert 0.4 <= b / a <= 0.6, ratios
+
+
 # ---- C-ABI known answers on the oracle (test_common.cpp:163-266) -------------
 def test_oracle_c_abi_known_answers(oc):
     L = oc.port_lib()
