@@ -17,6 +17,16 @@
  *     reference's own test matrix diag(1,-4,1) it leaves a residual of 9e-2.
  *   - device failures return VIBE_C_ERR_DEVICE (new code 3); void/double
  *     functions report them through vibe_c_last_error().
+ * No allocation per call and reentrancy (c_kernels.h:17-18): every host
+ * thread owns, per device, a stream and staging buffers (pinned host,
+ * device) that grow on demand and are reused; a host-pointer call packs its
+ * inputs into the pinned buffer, makes one host-to-device copy, runs, makes
+ * one copy back and waits for its own stream only. After a thread's first
+ * calls of a given size its calls allocate nothing (vibe_c_allocations()
+ * counts every allocation this layer makes). A host-pointer call costs a
+ * launch and two copies (tens of microseconds), so callers with many small
+ * systems use the batched or _dev forms. The caller's ws is accepted as the
+ * reference requires and left unused: the device workspace is the thread's.
  */
 #ifndef VIBE_GB300_C_KERNELS_H
 #define VIBE_GB300_C_KERNELS_H
@@ -84,11 +94,20 @@ void vibe_advect_scalar_flux_f64(const double *q, const double *rho,
 /* n_sys independent systems of size n, each stored contiguously
  * (system s uses a + s*(n-1), b + s*n, ...). One thread per system for
  * n <= 128; above, one warp per system (each lane eliminates a chunk of rows,
- * the chunks' end unknowns are joined by a 2x2 block-tridiagonal solve), whose
- * results agree with the single sweep to rounding and whose pivots are the
- * chunks' (a zero one is VIBE_C_ERR_SINGULAR).
+ * the chunks' end unknowns are joined by a 2x2 block-tridiagonal solve),
+ * whose results agree with the single sweep to rounding. A system whose chunk
+ * pivots or interface blocks are zero or tiny (b[r0] = 0 at a chunk start,
+ * non-dominant diagonals) is solved again with the single sweep, so the error
+ * contract stays the reference's: VIBE_C_ERR_SINGULAR only on an exactly zero
+ * sweep pivot (c_kernels.c:26,34,40).
  * status (device, n_sys ints) receives the per-system return code; may be
- * NULL. Returns VIBE_C_OK or VIBE_C_ERR_BAD_ARG/VIBE_C_ERR_DEVICE (launch). */
+ * NULL. Returns VIBE_C_OK or VIBE_C_ERR_BAD_ARG/VIBE_C_ERR_DEVICE (launch).
+ * Scratch (n*n_sys doubles, 3x for n > 128) comes from a buffer owned by
+ * the calling host thread: after its first calls of a size it allocates
+ * nothing, and calls of one thread on different streams are ordered through
+ * it (the later waits for the earlier), so they never share it while one
+ * runs. Under stream capture the scratch is a stream-ordered allocation of
+ * the graph instead. */
 int vibe_tridiagonal_solve_batched_f64_dev(const double *a, const double *b,
                                            const double *c, const double *d,
                                            int n, int n_sys, double *x,
@@ -102,8 +121,12 @@ int vibe_tridiagonal_solve_batched_f64_dev(const double *a, const double *b,
  * n * n_sys must not exceed 262144 (larger requests return
  * VIBE_C_ERR_BAD_ARG; vibe_c_last_error() says why). Inputs and outputs are
  * device pointers as in the _dev form. The first call on each device
- * resolves the array's device address (cudaGetSymbolAddress); make that
- * first call before any stream capture. All calls share the one array:
+ * resolves the array's device address (cudaGetSymbolAddress) and keeps it for
+ * the life of the process; make that first call before any stream capture,
+ * and do not call this form on a device after cudaDeviceReset of it. It runs
+ * the one-thread-per-system sweep for every n, so for n > 128 it agrees with
+ * the _dev form to rounding (and reports VIBE_C_ERR_SINGULAR on the sweep's
+ * exact-zero pivot only). All calls share the one array:
  * calls whose kernels can overlap on the GPU (different streams, no
  * ordering between them) race on it. */
 int vibe_tridiagonal_solve_batched_f64_dev_noalloc(const double *a, const double *b,
@@ -213,6 +236,13 @@ int vibe_advect_scalar_flux_ad_f32(const float *q, const float *rho, const float
 
 /* Message of the last device failure seen by this thread ("" if none). */
 const char *vibe_c_last_error(void);
+
+/* Number of device and pinned-host allocations (cudaMalloc, cudaMallocHost)
+ * the C-ABI layer has made in this process, over all threads and devices; it
+ * stops growing once every calling thread's buffers fit its calls. No
+ * reference counterpart: it makes the no-allocation convention of
+ * c_kernels.h:17 checkable. */
+unsigned long long vibe_c_allocations(void);
 
 #ifdef __cplusplus
 }

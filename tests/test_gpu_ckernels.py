@@ -114,6 +114,188 @@ def test_thomas_tall_systems_warp_cooperative(vg, oc, n, n_sys):
     assert rcz == 1
 
 
+def _residual(a, b, c, d, x):
+    """max |Ax - d| / max(|A||x| + |d|) of one tridiagonal system."""
+    r = b * x - d
+    r[1:] += a * x[:-1]
+    r[:-1] += c * x[1:]
+    scale = np.abs(b * x) + np.abs(d)
+    scale[1:] += np.abs(a * x[:-1])
+    scale[:-1] += np.abs(c * x[1:])
+    return float(np.abs(r).max() / scale.max())
+
+
+def _oracle_solve(oc, a, b, c, d):
+    n = b.size
+    xo, ws = np.zeros(n), np.zeros(n)
+    aa, bb, cc, dd = (np.ascontiguousarray(v) for v in (a, b, c, d))
+    rc = oc.port_lib().vo_tridiagonal_solve(aa.ctypes.data, bb.ctypes.data, cc.ctypes.data, dd.ctypes.data, n,
+                                            xo.ctypes.data, ws.ctypes.data)
+    return rc, xo
+
+
+@pytest.mark.parametrize("n", [300, 1000])
+def test_thomas_tall_zero_chunk_pivot_falls_back_to_the_sweep(vg, oc, n):
+    """A nonsingular system whose diagonal is 0 at the first row of a warp
+    chunk (rows per chunk m = ceil(n/32)): the chunked elimination has a zero
+    pivot there, the single sweep does not. The reference's contract
+    (c_kernels.c:26,34,40) reports singular only on a zero sweep pivot, so
+    the solver must solve it, as the oracle's sweep does."""
+    m = (n + 31) // 32
+    rng = np.random.default_rng(n + 5)
+    n_sys = 6
+    b = 4.0 + rng.random((n_sys, n))
+    a = -rng.random((n_sys, n - 1))
+    c = -rng.random((n_sys, n - 1))
+    d = rng.standard_normal((n_sys, n))
+    for s in range(n_sys):  # a zero at the start of chunk s+1 (every system a different chunk)
+        b[s, (s + 1) * m] = 0.0
+    rc, x = vg.tridiagonal_solve_batched(a, b, c, d)
+    assert rc == 0
+    for s in range(n_sys):
+        rco, xo = _oracle_solve(oc, a[s], b[s], c[s], d[s])
+        assert rco == 0
+        assert np.abs(x[s] - xo).max() <= 1e-12 * np.abs(xo).max()
+        assert _residual(a[s], b[s], c[s], d[s], x[s]) <= 1e-13
+
+
+def test_thomas_tall_non_dominant_diagonals(vg, oc):
+    """Diagonals of either sign and no dominance (|b| ~ |a| + |c|): every
+    system is solved to the sweep's accuracy (residual 1e-10 of the row
+    scale, the sweep's own residual within a factor 100), and the return code
+    is the sweep's."""
+    rng = np.random.default_rng(11)
+    n, n_sys = 513, 40
+    b = rng.uniform(-2.0, 2.0, (n_sys, n))
+    a = rng.uniform(-1.0, 1.0, (n_sys, n - 1))
+    c = rng.uniform(-1.0, 1.0, (n_sys, n - 1))
+    d = rng.standard_normal((n_sys, n))
+    _, x = vg.tridiagonal_solve_batched(a, b, c, d)
+    for s in range(n_sys):
+        rco, xo = _oracle_solve(oc, a[s], b[s], c[s], d[s])
+        assert rco == 0
+        r_gpu, r_seq = _residual(a[s], b[s], c[s], d[s], x[s]), _residual(a[s], b[s], c[s], d[s], xo)
+        assert r_gpu <= max(1e-10, 100.0 * r_seq), (s, r_gpu, r_seq)
+        rc1, x1 = vg.tridiagonal_solve(a[s], b[s], c[s], d[s])
+        assert rc1 == rco
+
+
+def test_host_entry_points_reentrant_and_allocation_free(vg, oc):
+    """c_kernels.h:17-18: reentrant, OpenMP-thread-safe, no allocation per
+    call. Eight host threads call vibe_tridiagonal_solve_f64 and
+    vibe_neumaier_sum_f64 concurrently on their own inputs (ctypes releases
+    the interpreter lock during the call); every result matches the oracle.
+    After each thread's first calls, further calls of the same sizes make no
+    allocation (vibe_c_allocations() stays put). Prints the latency of one
+    n = 80 solve."""
+    import threading
+    import time
+    lib = vg.lib
+    lib.vibe_c_allocations.restype = ctypes.c_ulonglong
+    lib.vibe_neumaier_sum_f64.restype = ctypes.c_double
+    lib.vibe_neumaier_sum_f64.argtypes = [ctypes.c_void_p, ctypes.c_size_t]
+    L = oc.port_lib()
+    nthreads, calls, n = 8, 40, 80
+    cases = []
+    for t in range(nthreads):
+        rng = np.random.default_rng(100 + t)
+        sys_ = []
+        for q in range(calls):
+            b = 4.0 + rng.random(n)
+            a, c = -rng.random(n - 1), -rng.random(n - 1)
+            d = rng.standard_normal(n)
+            xs = rng.standard_normal(5000) * 10.0 ** rng.integers(-8, 8, 5000)
+            _, xo = _oracle_solve(oc, a, b, c, d)
+            so = L.vo_neumaier_sum(xs.ctypes.data, xs.size)
+            sys_.append((a, b, c, d, xo, xs, so))
+        cases.append(sys_)
+    errors = []
+    warm, go, done = threading.Barrier(nthreads + 1), threading.Barrier(nthreads + 1), threading.Barrier(nthreads + 1)
+
+    def worker(t):
+        try:
+            x, ws = np.zeros(n), np.zeros(n)
+
+            def run_all():
+                for a, b, c, d, xo, xs, so in cases[t]:
+                    rc = lib.vibe_tridiagonal_solve_f64(a.ctypes.data, b.ctypes.data, c.ctypes.data, d.ctypes.data,
+                                                        n, x.ctypes.data, ws.ctypes.data)
+                    if rc != 0 or np.abs(x - xo).max() > 1e-12 * np.abs(xo).max():
+                        errors.append(("thomas", t, rc))
+                    sv = lib.vibe_neumaier_sum_f64(xs.ctypes.data, xs.size)
+                    if abs(sv - so) > 1e-13 * np.abs(xs).sum():
+                        errors.append(("neumaier", t, sv, so))
+            run_all()
+            warm.wait()
+            go.wait()
+            run_all()
+            done.wait()
+        except Exception as e:  # noqa: BLE001 - reported below
+            errors.append(("exception", t, repr(e)))
+            for bar in (warm, go, done):
+                bar.abort()
+
+    threads = [threading.Thread(target=worker, args=(t,)) for t in range(nthreads)]
+    for th in threads:
+        th.start()
+    warm.wait()
+    before = lib.vibe_c_allocations()
+    go.wait()
+    done.wait()
+    after = lib.vibe_c_allocations()
+    for th in threads:
+        th.join()
+    assert not errors, errors[:5]
+    assert after == before, (before, after)
+    a, b, c, d, xo, _, _ = cases[0][0]
+    x, ws = np.zeros(n), np.zeros(n)
+    for _ in range(20):
+        lib.vibe_tridiagonal_solve_f64(a.ctypes.data, b.ctypes.data, c.ctypes.data, d.ctypes.data, n, x.ctypes.data,
+                                       ws.ctypes.data)
+    t0 = time.perf_counter()
+    for _ in range(500):
+        lib.vibe_tridiagonal_solve_f64(a.ctypes.data, b.ctypes.data, c.ctypes.data, d.ctypes.data, n, x.ctypes.data,
+                                       ws.ctypes.data)
+    print("host vibe_tridiagonal_solve_f64, n = 80: %.1f us per call" % ((time.perf_counter() - t0) / 500 * 1e6))
+
+
+def test_dev_entry_points_share_no_scratch_across_streams(vg, oc):
+    """The _dev forms take their scratch from the calling thread's buffer and
+    order a call on one stream after the previous call on another: solves
+    queued back to back on two streams, the second needing a larger scratch
+    than the first (the buffer is replaced only after its last user), with a
+    Neumaier sum after each, all come out right."""
+    torch = pytest.importorskip("torch")
+    dev = torch.device("cuda", 0)
+    vp, i = ctypes.c_void_p, ctypes.c_int
+    f = vg.lib.vibe_tridiagonal_solve_batched_f64_dev
+    f.restype, f.argtypes = i, [vp, vp, vp, vp, i, i, vp, vp, vp]
+    g = vg.lib.vibe_neumaier_sum_f64_dev
+    g.restype, g.argtypes = i, [vp, ctypes.c_size_t, vp, vp]
+    s1, s2 = torch.cuda.Stream(dev), torch.cuda.Stream(dev)
+    outs = []
+    for q, (n, n_sys, st) in enumerate(((60, 2000, s1), (300, 2000, s2), (60, 20000, s1))):
+        rng = np.random.default_rng(q)
+        arrs = [4.0 + rng.random((n_sys, n)), -rng.random((n_sys, n - 1)), -rng.random((n_sys, n - 1)),
+                rng.standard_normal((n_sys, n))]
+        b, a, c, d = (torch.tensor(v, device=dev) for v in arrs)
+        x = torch.zeros((n_sys, n), dtype=torch.float64, device=dev)
+        assert f(a.data_ptr(), b.data_ptr(), c.data_ptr(), d.data_ptr(), n, n_sys, x.data_ptr(), None,
+                 st.cuda_stream) == 0
+        xs = torch.tensor(rng.standard_normal(100000), device=dev)
+        out = torch.zeros(1, dtype=torch.float64, device=dev)
+        assert g(xs.data_ptr(), xs.numel(), out.data_ptr(), s1.cuda_stream) == 0
+        outs.append((arrs, x, xs, out))
+    torch.cuda.synchronize(dev)
+    for arrs, x, xs, out in outs:
+        b, a, c, d = arrs
+        xg = x.cpu().numpy()
+        for s in (0, b.shape[0] - 1):
+            _, xo = _oracle_solve(oc, a[s], b[s], c[s], d[s])
+            assert np.abs(xg[s] - xo).max() <= 1e-12 * np.abs(xo).max()
+        assert abs(float(out.item()) - float(np.sum(xs.cpu().numpy()))) <= 1e-10 * float(xs.abs().sum())
+
+
 def test_weno5_known_answers(vg, oc):
     """test_common.cpp:188-205: exact on constants, bounded on monotone data."""
     ql, qr = vg.weno5_reconstruct(3.5, 3.5, 3.5, 3.5, 3.5)

@@ -56,3 +56,31 @@ def test_group_rejects_unsupported_members(vg):
         for bad in ([a, b], [a, c]):
             with pytest.raises(vg.VibeError):
                 vg.Group(bad)
+
+
+def test_group_after_members_reconfigured_for_another_dt(vg):
+    """A member stepped alone with another dt, and a member's FP32 HEVI
+    tangent-linear (which builds its column factors for 3*dtau), rewrite
+    that member's per-model dt tables in place; the group's next step must
+    put them back for its own dt, or its cached graph replays with the
+    wrong HEVI factors and sponge weights."""
+    setups = [member(vg, 40, 24, 0), member(vg, 17, 33, 1)]
+    grouped = [vg.Model(s, vg.MIXED) for s in setups]
+    single = [vg.Model(s, vg.MIXED) for s in setups]
+    try:
+        pert = [np.random.default_rng(3).standard_normal(grouped[1].size(sp)) for sp in (0, 1, 2, 3, 5)]
+        with vg.Group(grouped) as g:
+            g.step(2.0, 6, 2)
+            grouped[0].step(1.0, 6, 2)       # stepped alone with another dt (parity kept)
+            grouped[1].hevi_tl_f32(0.7, 2, pert)
+            g.step(2.0, 6, 2)
+        single[0].step(2.0, 6, 2)
+        single[0].step(1.0, 6, 2)
+        single[0].step(2.0, 6, 2)
+        single[1].step(2.0, 6, 4)
+        for a, b, s in zip(grouped, single, setups):
+            assert_rounding_close(vg, s, [a.get(sp) for sp in range(7)], [b.get(sp) for sp in range(7)],
+                                  what="group after reconfiguration vs single")
+    finally:
+        for m in grouped + single:
+            m.close()

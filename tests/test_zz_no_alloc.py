@@ -65,3 +65,33 @@ def test_noalloc_rejects_requests_beyond_its_workspace(vg):
     rc = noalloc(p, p, p, p, n, n_sys, p, None, torch.cuda.current_stream(dev).cuda_stream)
     assert rc == 2
     assert b"exceeds the fixed workspace" in vg.lib.vibe_c_last_error()
+
+
+def test_noalloc_tall_systems_and_null_status(vg):
+    """n > 128: this form runs the one-thread sweep where the allocating form
+    runs the warp-per-system solver, so the two agree to rounding; a call
+    without a status array (status = NULL) solves the same."""
+    torch = pytest.importorskip("torch")
+    noalloc, alloc = _bind(vg)
+    dev = torch.device("cuda", 0)
+    stream = torch.cuda.current_stream(dev).cuda_stream
+    n, n_sys = 300, 800
+    assert n * n_sys <= LIMIT
+    rng = np.random.default_rng(3)
+    b = torch.tensor(4.0 + rng.random((n_sys, n)), device=dev)
+    a = torch.tensor(-rng.random((n_sys, n - 1)), device=dev)
+    c = torch.tensor(-rng.random((n_sys, n - 1)), device=dev)
+    d = torch.tensor(rng.standard_normal((n_sys, n)), device=dev)
+    args = [t.data_ptr() for t in (a, b, c, d)]
+    x_ref = torch.full((n_sys, n), float("nan"), dtype=torch.float64, device=dev)
+    x_na = torch.full((n_sys, n), float("nan"), dtype=torch.float64, device=dev)
+    x_nul = torch.full((n_sys, n), float("nan"), dtype=torch.float64, device=dev)
+    st = torch.full((n_sys,), -1, dtype=torch.int32, device=dev)
+    assert alloc(*args, n, n_sys, x_ref.data_ptr(), None, stream) == 0
+    assert noalloc(*args, n, n_sys, x_na.data_ptr(), st.data_ptr(), stream) == 0
+    assert noalloc(*args, n, n_sys, x_nul.data_ptr(), None, stream) == 0
+    torch.cuda.synchronize(dev)
+    assert int(st.abs().sum()) == 0
+    scale = float(x_ref.abs().max())
+    assert float((x_na - x_ref).abs().max()) <= 1e-12 * scale
+    assert torch.equal(x_na, x_nul)

@@ -16,12 +16,11 @@
 #include <cmath>
 #include <string>
 
+#include "cabi_host.cuh"
 #include "vibe_c_kernels.h"
 #include "vibe_internal.cuh"
 
 namespace {
-
-thread_local std::string g_aerr;
 
 struct Grid3 {
   int nx, ny, nz;
@@ -145,9 +144,10 @@ __global__ void k_flux_ad(const T* __restrict__ q, const T* __restrict__ rho, co
   }
 }
 
+// device failures go to the thread's C-ABI error message (vibe_c_last_error)
 bool ok(cudaError_t e, const char* what) {
   if (e == cudaSuccess) return true;
-  g_aerr = std::string(what) + ": " + cudaGetErrorString(e);
+  vgb_cabi::set_error(what, e);
   return false;
 }
 
@@ -177,20 +177,8 @@ int ad_dev(const T* q, const T* rho, const T* u, const T* v, const T* w, const T
   return ok(cudaGetLastError(), "flux AD launch") ? VIBE_C_OK : VIBE_C_ERR_DEVICE;
 }
 
-// host forms: stage every array through device memory on a private stream
-template <typename T>
-struct Staged {
-  T* p = nullptr;
-  Staged(const T* h, size_t n, cudaStream_t s, bool& good) {
-    if (!good) return;
-    good = cudaMalloc(&p, n * sizeof(T) + 16) == cudaSuccess;
-    if (good && h) good = cudaMemcpyAsync(p, h, n * sizeof(T), cudaMemcpyHostToDevice, s) == cudaSuccess;
-  }
-  ~Staged() {
-    if (p) cudaFree(p);
-  }
-};
-
+// host forms: every array staged through the calling thread's buffers in
+// one copy each way (cabi_host.cuh), no allocation once they fit
 template <typename T>
 int tl_host(const T* q, const T* rho, const T* u, const T* v, const T* w, const T* dq, const T* drho, const T* du,
             const T* dv, const T* dw, const T* dzeta, const T* zs, int nx, int ny, int nz, T dx, T dy, T z_top,
@@ -198,23 +186,21 @@ int tl_host(const T* q, const T* rho, const T* u, const T* v, const T* w, const 
   if (!q || !rho || !u || !v || !w || !dq || !drho || !du || !dv || !dw || !dzeta || !out || nx < 1 || ny < 1 ||
       nz < 1)
     return VIBE_C_ERR_BAD_ARG;
-  cudaStream_t s = nullptr;
-  if (!ok(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking), "stream")) return VIBE_C_ERR_DEVICE;
-  const size_t n = (size_t)nx * ny * nz;
-  bool good = true;
-  int rc = VIBE_C_ERR_DEVICE;
-  {
-    Staged<T> a(q, n, s, good), b(rho, n, s, good), c(u, n, s, good), d(v, n, s, good), e(w, n, s, good),
-        f(dq, n, s, good), g2(drho, n, s, good), h(du, n, s, good), i2(dv, n, s, good), j2(dw, n, s, good),
-        z(dzeta, nz, s, good), zz(zs, zs ? (size_t)nx * ny : 0, s, good), o(nullptr, n, s, good);
-    if (good)
-      rc = tl_dev<T>(a.p, b.p, c.p, d.p, e.p, f.p, g2.p, h.p, i2.p, j2.p, z.p, zs ? zz.p : nullptr, nx, ny, nz, dx,
-                     dy, z_top, o.p, s);
-    if (rc == VIBE_C_OK && !ok(cudaMemcpyAsync(out, o.p, n * sizeof(T), cudaMemcpyDeviceToHost, s), "D2H"))
-      rc = VIBE_C_ERR_DEVICE;
-    if (!ok(cudaStreamSynchronize(s), "sync")) rc = VIBE_C_ERR_DEVICE;
-  }
-  cudaStreamDestroy(s);
+  using vgb_cabi::HostCall;
+  const size_t n = (size_t)nx * ny * nz, e = sizeof(T);
+  HostCall hc;
+  const T* ins[10] = {q, rho, u, v, w, dq, drho, du, dv, dw};
+  int id[10];
+  for (int t = 0; t < 10; ++t) id[t] = hc.add(ins[t], n * e, HostCall::kIn);
+  const int iz = hc.add(dzeta, (size_t)nz * e, HostCall::kIn);
+  const int izs = hc.add(zs, zs ? (size_t)nx * ny * e : 0, HostCall::kIn);
+  const int io = hc.add(out, n * e, HostCall::kOut);
+  int rc = hc.commit() ? VIBE_C_OK : VIBE_C_ERR_DEVICE;
+  if (rc == VIBE_C_OK)
+    rc = tl_dev<T>(hc.dev<T>(id[0]), hc.dev<T>(id[1]), hc.dev<T>(id[2]), hc.dev<T>(id[3]), hc.dev<T>(id[4]),
+                   hc.dev<T>(id[5]), hc.dev<T>(id[6]), hc.dev<T>(id[7]), hc.dev<T>(id[8]), hc.dev<T>(id[9]),
+                   hc.dev<T>(iz), hc.dev<T>(izs), nx, ny, nz, dx, dy, z_top, hc.dev<T>(io), hc.stream());
+  if (!hc.finish() && rc == VIBE_C_OK) rc = VIBE_C_ERR_DEVICE;
   return rc;
 }
 
@@ -223,26 +209,24 @@ int ad_host(const T* q, const T* rho, const T* u, const T* v, const T* w, const 
             int nx, int ny, int nz, T dx, T dy, T z_top, T* bq, T* brho, T* bu, T* bv, T* bw) {
   if (!q || !rho || !u || !v || !w || !bd || !dzeta || !bq || !brho || !bu || !bv || !bw || nx < 1 || ny < 1 || nz < 1)
     return VIBE_C_ERR_BAD_ARG;
-  cudaStream_t s = nullptr;
-  if (!ok(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking), "stream")) return VIBE_C_ERR_DEVICE;
-  const size_t n = (size_t)nx * ny * nz;
-  bool good = true;
-  int rc = VIBE_C_ERR_DEVICE;
-  {
-    // the outputs accumulate: their current values travel to the device too
-    Staged<T> a(q, n, s, good), b(rho, n, s, good), c(u, n, s, good), d(v, n, s, good), e(w, n, s, good),
-        f(bd, n, s, good), z(dzeta, nz, s, good), zz(zs, zs ? (size_t)nx * ny : 0, s, good), oq(bq, n, s, good),
-        orho(brho, n, s, good), ou(bu, n, s, good), ov(bv, n, s, good), ow(bw, n, s, good);
-    if (good)
-      rc = ad_dev<T>(a.p, b.p, c.p, d.p, e.p, f.p, z.p, zs ? zz.p : nullptr, nx, ny, nz, dx, dy, z_top, oq.p, orho.p,
-                     ou.p, ov.p, ow.p, s);
-    T* outs[5] = {bq, brho, bu, bv, bw};
-    T* devs[5] = {oq.p, orho.p, ou.p, ov.p, ow.p};
-    for (int t = 0; t < 5 && rc == VIBE_C_OK; ++t)
-      if (!ok(cudaMemcpyAsync(outs[t], devs[t], n * sizeof(T), cudaMemcpyDeviceToHost, s), "D2H")) rc = VIBE_C_ERR_DEVICE;
-    if (!ok(cudaStreamSynchronize(s), "sync")) rc = VIBE_C_ERR_DEVICE;
-  }
-  cudaStreamDestroy(s);
+  using vgb_cabi::HostCall;
+  const size_t n = (size_t)nx * ny * nz, e = sizeof(T);
+  HostCall hc;
+  const T* ins[6] = {q, rho, u, v, w, bd};
+  int id[6];
+  for (int t = 0; t < 6; ++t) id[t] = hc.add(ins[t], n * e, HostCall::kIn);
+  const int iz = hc.add(dzeta, (size_t)nz * e, HostCall::kIn);
+  const int izs = hc.add(zs, zs ? (size_t)nx * ny * e : 0, HostCall::kIn);
+  // the outputs accumulate: their current values travel to the device and back
+  T* outs[5] = {bq, brho, bu, bv, bw};
+  int io[5];
+  for (int t = 0; t < 5; ++t) io[t] = hc.add(outs[t], n * e, HostCall::kInOut);
+  int rc = hc.commit() ? VIBE_C_OK : VIBE_C_ERR_DEVICE;
+  if (rc == VIBE_C_OK)
+    rc = ad_dev<T>(hc.dev<T>(id[0]), hc.dev<T>(id[1]), hc.dev<T>(id[2]), hc.dev<T>(id[3]), hc.dev<T>(id[4]),
+                   hc.dev<T>(id[5]), hc.dev<T>(iz), hc.dev<T>(izs), nx, ny, nz, dx, dy, z_top, hc.dev<T>(io[0]),
+                   hc.dev<T>(io[1]), hc.dev<T>(io[2]), hc.dev<T>(io[3]), hc.dev<T>(io[4]), hc.stream());
+  if (!hc.finish() && rc == VIBE_C_OK) rc = VIBE_C_ERR_DEVICE;
   return rc;
 }
 

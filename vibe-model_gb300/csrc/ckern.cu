@@ -8,24 +8,19 @@
 // warp shuffles inside a block, one partial per block in device scratch, and
 // a single-block pass that merges the partials in block order, so results are
 // deterministic run to run.
+#include <atomic>
 #include <cmath>
 #include <cstring>
 #include <mutex>
 #include <string>
 
+#include "cabi_host.cuh"
 #include "vibe_c_kernels.h"
 #include "vibe_internal.cuh"
 
 namespace {
 
 thread_local std::string g_cerr;
-
-// Per-device scratch for block partials and per-system workspace. Grows on
-// demand, never shrinks; guarded by a mutex (the ABI promises reentrancy).
-std::mutex g_scr_mu;
-void* g_scr[64] = {};
-size_t g_scr_n[64] = {};
-cudaStream_t g_stream[64] = {};
 
 bool device_ok(cudaError_t e, const char* what) {
   if (e == cudaSuccess) return true;
@@ -39,39 +34,68 @@ int cur_dev() {
   return d;
 }
 
-void* scratch(size_t bytes) {
-  const int dev = cur_dev();
-  if (dev < 0 || dev >= 64) return nullptr;
-  std::lock_guard<std::mutex> lk(g_scr_mu);
-  if (g_scr_n[dev] < bytes) {
-    if (g_scr[dev]) cudaFree(g_scr[dev]);
-    g_scr[dev] = nullptr;
-    g_scr_n[dev] = 0;
-    if (cudaMalloc(&g_scr[dev], bytes) != cudaSuccess) return nullptr;
-    g_scr_n[dev] = bytes;
-  }
-  return g_scr[dev];
-}
+// ---- per-thread call contexts (cabi_host.cuh) ----------------------------
+constexpr int kMaxDev = 64;
+std::atomic<unsigned long long> g_allocs{0};
 
-cudaStream_t own_stream() {
-  const int dev = cur_dev();
-  std::lock_guard<std::mutex> lk(g_scr_mu);
-  if (!g_stream[dev]) cudaStreamCreateWithFlags(&g_stream[dev], cudaStreamNonBlocking);
-  return g_stream[dev];
-}
-
-// RAII device buffer for the host-pointer entry points
-struct DBuf {
-  void* p = nullptr;
-  explicit DBuf(size_t bytes) {
-    if (bytes && cudaMalloc(&p, bytes) != cudaSuccess) p = nullptr;
-  }
-  ~DBuf() {
-    if (p) cudaFree(p);
-  }
-  template <class T>
-  T* as() const { return (T*)p; }
+struct Ctx {
+  cudaStream_t st = nullptr;
+  cudaEvent_t last = nullptr;  // recorded after the last launch that used scr
+  bool has_last = false;
+  char* pin = nullptr;         // pinned host staging
+  size_t pin_n = 0;
+  char* dbuf = nullptr;        // device staging of host-pointer calls
+  size_t dbuf_n = 0;
+  char* scr = nullptr;         // scratch of _dev calls
+  size_t scr_n = 0;
 };
+
+// One context per (host thread, device); freed when the thread exits (the
+// main thread's at process exit, before the CUDA runtime's own teardown).
+struct Holder {
+  Ctx* c[kMaxDev] = {};
+  ~Holder() {
+    for (auto*& x : c) {
+      if (!x) continue;
+      if (x->st) cudaStreamSynchronize(x->st);
+      if (x->has_last) cudaEventSynchronize(x->last);
+      if (x->pin) cudaFreeHost(x->pin);
+      if (x->dbuf) cudaFree(x->dbuf);
+      if (x->scr) cudaFree(x->scr);
+      if (x->last) cudaEventDestroy(x->last);
+      if (x->st) cudaStreamDestroy(x->st);
+      delete x;
+      x = nullptr;
+    }
+  }
+};
+thread_local Holder t_hold;
+
+Ctx* ctx() {
+  int d = -1;
+  if (!device_ok(cudaGetDevice(&d), "cudaGetDevice")) return nullptr;
+  if (d < 0 || d >= kMaxDev) { g_cerr = "device ordinal out of range"; return nullptr; }
+  Ctx*& c = t_hold.c[d];
+  if (!c) {
+    Ctx* n = new Ctx();
+    if (!device_ok(cudaStreamCreateWithFlags(&n->st, cudaStreamNonBlocking), "cudaStreamCreate") ||
+        !device_ok(cudaEventCreateWithFlags(&n->last, cudaEventDisableTiming), "cudaEventCreate")) {
+      if (n->st) cudaStreamDestroy(n->st);
+      delete n;
+      return nullptr;
+    }
+    c = n;
+  }
+  return c;
+}
+
+size_t grown(size_t have, size_t need) {
+  size_t n = have ? have : (size_t)4096;
+  while (n < need) n *= 2;
+  return n;
+}
+
+inline size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 
 // ---------------------------------------------------------------------------
 // Thomas: one thread per system. Contract c_kernels.h:38-55 with the
@@ -79,39 +103,37 @@ struct DBuf {
 // as 0; exact-zero pivots give VIBE_C_ERR_SINGULAR as c_kernels.c:26,34,40.
 // cp (the modified super-diagonal) lives in `work` (n per system).
 template <typename T>
+__device__ int thomas_seq(const T* __restrict__ as, const T* __restrict__ bs, const T* __restrict__ cs,
+                          const T* __restrict__ ds, int n, T* __restrict__ xs, T* __restrict__ cp) {
+  if (n == 1) {
+    if (bs[0] == (T)0) return VIBE_C_ERR_SINGULAR;
+    xs[0] = ds[0] / bs[0];
+    return VIBE_C_OK;
+  }
+  T denom = bs[0];
+  if (denom == (T)0) return VIBE_C_ERR_SINGULAR;
+  cp[0] = (cs ? cs[0] : (T)0) / denom;
+  xs[0] = ds[0] / denom;
+  for (int k = 1; k < n; ++k) {
+    const T am = as ? as[k - 1] : (T)0;
+    denom = bs[k] - am * cp[k - 1];
+    if (denom == (T)0) return VIBE_C_ERR_SINGULAR;
+    xs[k] = (ds[k] - am * xs[k - 1]) / denom;
+    if (k < n - 1) cp[k] = (cs ? cs[k] : (T)0) / denom;
+  }
+  for (int k = n - 1; k-- > 0;) xs[k] = xs[k] - cp[k] * xs[k + 1];
+  return VIBE_C_OK;
+}
+
+template <typename T>
 __global__ void k_thomas_batched(const T* __restrict__ a, const T* __restrict__ b, const T* __restrict__ c,
                                  const T* __restrict__ d, int n, int n_sys, T* __restrict__ x, T* __restrict__ work,
                                  int* __restrict__ status) {
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= n_sys) return;
-  const T* as = a ? a + (size_t)s * (n - 1) : nullptr;
-  const T* bs = b + (size_t)s * n;
-  const T* cs = c ? c + (size_t)s * (n - 1) : nullptr;
-  const T* ds = d + (size_t)s * n;
-  T* xs = x + (size_t)s * n;
-  T* cp = work + (size_t)s * n;
-  int rc = VIBE_C_OK;
-  if (n == 1) {
-    if (bs[0] == (T)0) rc = VIBE_C_ERR_SINGULAR;
-    else xs[0] = ds[0] / bs[0];
-  } else {
-    T denom = bs[0];
-    if (denom == (T)0) {
-      rc = VIBE_C_ERR_SINGULAR;
-    } else {
-      cp[0] = (cs ? cs[0] : (T)0) / denom;
-      xs[0] = ds[0] / denom;
-      for (int k = 1; k < n; ++k) {
-        const T am = as ? as[k - 1] : (T)0;
-        denom = bs[k] - am * cp[k - 1];
-        if (denom == (T)0) { rc = VIBE_C_ERR_SINGULAR; break; }
-        xs[k] = (ds[k] - am * xs[k - 1]) / denom;
-        if (k < n - 1) cp[k] = (cs ? cs[k] : (T)0) / denom;
-      }
-      if (rc == VIBE_C_OK)
-        for (int k = n - 1; k-- > 0;) xs[k] = xs[k] - cp[k] * xs[k + 1];
-    }
-  }
+  const int rc = thomas_seq<T>(a ? a + (size_t)s * (n - 1) : nullptr, b + (size_t)s * n,
+                               c ? c + (size_t)s * (n - 1) : nullptr, d + (size_t)s * n, n, x + (size_t)s * n,
+                               work + (size_t)s * n);
   if (status) status[s] = rc;
 }
 
@@ -126,11 +148,23 @@ __global__ void k_thomas_batched(const T* __restrict__ a, const T* __restrict__ 
 // z_j + [vF; vE]_j E_{j-1} + [wF; wE]_j F_{j+1} = [yF; yE]_j, which lane 0
 // solves by block elimination (32 blocks); every lane then reads its two
 // neighbours' interface values from shared memory and finishes its chunk.
-// A zero pivot of a chunk or a singular 2x2 block gives VIBE_C_ERR_SINGULAR.
 // The elimination order differs from one sequential sweep, so results agree
-// with it to rounding. Scratch: 3n per system (c', v, w).
+// with it to rounding. A chunk starts from its raw diagonal b[r0], so its
+// pivots are not the sweep's: a nonsingular system can have a zero or a
+// tiny chunk pivot (b[r0] = 0, non-dominant diagonals) or a near-singular
+// 2x2 interface block. Whenever a chunk pivot is at most tall_rel (1e-8 in
+// FP64, 1e-3 in FP32) of its row's |a| + |b| + |c|, or a block determinant at
+// most tall_rel of its terms, lane 0 solves that system again with the single sequential sweep, whose
+// contract is the reference's (c_kernels.c:26,34,40): VIBE_C_ERR_SINGULAR
+// only on an exactly zero sweep pivot. Scratch: 3n per system (c', v, w).
 constexpr int kTallN = 128;
 constexpr int kTallWarps = 4;  // systems per block
+template <typename T>
+__device__ __forceinline__ T tall_rel();
+template <>
+__device__ __forceinline__ double tall_rel<double>() { return 1e-8; }
+template <>
+__device__ __forceinline__ float tall_rel<float>() { return 1e-3f; }
 
 template <typename T>
 __global__ void __launch_bounds__(32 * kTallWarps) k_thomas_tall(const T* __restrict__ a, const T* __restrict__ b,
@@ -139,15 +173,16 @@ __global__ void __launch_bounds__(32 * kTallWarps) k_thomas_tall(const T* __rest
                                                                  T* __restrict__ work, int* __restrict__ status) {
   __shared__ T sh[kTallWarps][32][6];  // per lane: yF, yE, vF, vE, wF, wE
   __shared__ T zs[kTallWarps][32][2];  // interface solution F_j, E_j
-  __shared__ int bad[kTallWarps];
+  __shared__ int seq[kTallWarps];  // 1: this system falls back to the sequential sweep
   const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int s = blockIdx.x * kTallWarps + wid;
   const bool live = s < n_sys;
   const int m = (n + 31) / 32;                   // rows per chunk
   const int r0 = min(lane * m, n), r1 = min(r0 + m, n), L = r1 - r0;
   const int nch = (n + m - 1) / m;               // chunks with rows (lanes >= nch hold none)
-  if (lane == 0) bad[wid] = 0;
+  if (lane == 0) seq[wid] = 0;
   __syncwarp();
+  const T rel = tall_rel<T>();
   const T* as = (live && a) ? a + (size_t)s * (n - 1) : nullptr;
   const T* bs = live ? b + (size_t)s * n : nullptr;
   const T* cs = (live && c) ? c + (size_t)s * (n - 1) : nullptr;
@@ -160,18 +195,20 @@ __global__ void __launch_bounds__(32 * kTallWarps) k_thomas_tall(const T* __rest
   if (live && L > 0) {
     // forward elimination of the chunk with the three right-hand sides
     T den = bs[r0];
-    if (den == (T)0) ok = false;
+    const T a0 = (r0 > 0 && as) ? as[r0 - 1] : (T)0;   // coupling to x_{r0-1}
+    const T cl = (r1 < n && cs) ? cs[r1 - 1] : (T)0;   // coupling to x_{r1}
+    const T c0 = (r0 + 1 < n && cs) ? cs[r0] : (T)0;
+    if (!(fabs(den) > rel * (fabs(a0) + fabs(den) + fabs(c0)))) ok = false;
     if (ok) {
-      const T a0 = (r0 > 0 && as) ? as[r0 - 1] : (T)0;   // coupling to x_{r0-1}
-      const T cl = (r1 < n && cs) ? cs[r1 - 1] : (T)0;   // coupling to x_{r1}
       cp[r0] = (r0 + 1 < r1) ? ((cs ? cs[r0] : (T)0) / den) : (T)0;
       xs[r0] = ds[r0] / den;
       vv[r0] = a0 / den;
       ww[r0] = (L == 1) ? cl / den : (T)0;
       for (int k = r0 + 1; k < r1 && ok; ++k) {
         const T am = as ? as[k - 1] : (T)0;
+        const T ck = (k + 1 < n && cs) ? cs[k] : (T)0;
         den = bs[k] - am * cp[k - 1];
-        if (den == (T)0) { ok = false; break; }
+        if (!(fabs(den) > rel * (fabs(am) + fabs(bs[k]) + fabs(ck)))) { ok = false; break; }
         xs[k] = (ds[k] - am * xs[k - 1]) / den;
         vv[k] = (-am * vv[k - 1]) / den;
         ww[k] = ((k == r1 - 1 ? cl : (T)0) - am * ww[k - 1]) / den;
@@ -193,11 +230,11 @@ __global__ void __launch_bounds__(32 * kTallWarps) k_thomas_tall(const T* __rest
       sh[wid][lane][5] = ww[r1 - 1];
     }
   }
-  if (!ok) bad[wid] = 1;
+  if (!ok) seq[wid] = 1;
   __syncwarp();
   // the interface system, block elimination by lane 0: z_j + Lj z_{j-1} + Uj z_{j+1} = Yj,
   // Lj = [[0, vF], [0, vE]] and Uj = [[wF, 0], [wE, 0]]
-  if (live && lane == 0 && !bad[wid]) {
+  if (live && lane == 0 && !seq[wid]) {
     T C[32][2][2], Y[32][2];
     for (int j = 0; j < nch; ++j) {
       const T* q = sh[wid][j];
@@ -211,7 +248,7 @@ __global__ void __launch_bounds__(32 * kTallWarps) k_thomas_tall(const T* __rest
         r1v -= q[3] * Y[j - 1][1];
       }
       const T det = D00 * D11 - D01 * D10;
-      if (det == (T)0) { bad[wid] = 1; break; }
+      if (!(fabs(det) > rel * (fabs(D00 * D11) + fabs(D01 * D10)))) { seq[wid] = 1; break; }
       const T i00 = D11 / det, i01 = -D01 / det, i10 = -D10 / det, i11 = D00 / det;
       // C_j = D^-1 Uj (Uj acts on F_{j+1}: column 0), Y_j = D^-1 rhs
       const T u0 = (j + 1 < nch) ? q[4] : (T)0, u1 = (j + 1 < nch) ? q[5] : (T)0;
@@ -222,7 +259,7 @@ __global__ void __launch_bounds__(32 * kTallWarps) k_thomas_tall(const T* __rest
       Y[j][0] = i00 * r0v + i01 * r1v;
       Y[j][1] = i10 * r0v + i11 * r1v;
     }
-    if (!bad[wid])
+    if (!seq[wid])
       for (int j = nch - 1; j >= 0; --j) {
         T f = Y[j][0], e = Y[j][1];
         if (j + 1 < nch) {  // z_j = Y_j - C_j z_{j+1}, C_j acting on F_{j+1}
@@ -234,12 +271,19 @@ __global__ void __launch_bounds__(32 * kTallWarps) k_thomas_tall(const T* __rest
       }
   }
   __syncwarp();
-  if (live && L > 0 && !bad[wid]) {
+  if (seq[wid]) {  // the sequential sweep over the whole system, on lane 0
+    if (live && lane == 0) {
+      const int rc = thomas_seq<T>(as, bs, cs, ds, n, xs, cp);
+      if (status) status[s] = rc;
+    }
+    return;
+  }
+  if (live && L > 0) {
     const T xl = (lane > 0) ? zs[wid][lane - 1][1] : (T)0;        // E of the chunk to the left
     const T xr = (lane + 1 < nch) ? zs[wid][lane + 1][0] : (T)0;  // F of the chunk to the right
     for (int k = r0; k < r1; ++k) xs[k] = xs[k] - vv[k] * xl - ww[k] * xr;
   }
-  if (live && lane == 0 && status) status[s] = bad[wid] ? VIBE_C_ERR_SINGULAR : VIBE_C_OK;
+  if (live && lane == 0 && status) status[s] = VIBE_C_OK;
 }
 
 // WENO5 (c_kernels.c:64-104), one thread per stencil
@@ -461,12 +505,18 @@ __global__ void k_flux_adv(const T* __restrict__ q, const T* __restrict__ rho, c
 // workspace (the modified super-diagonal, n doubles per system) in this
 // fixed device array instead of the allocated scratch buffer. The array is
 // sized here, once, and every GPU that loads the library holds it until the
-// process exits.
+// process exits. It always runs the one-thread-per-system sweep
+// (k_thomas_batched), also for n > 128 where the allocating _dev form runs
+// the warp-per-system solver: there the two agree to rounding, and this
+// form's singular test is the sweep's exact-zero pivot.
 constexpr size_t kNoAllocThomasDoubles = (size_t)1 << 18;  // 2 MiB: n * n_sys <= 262144
 static __device__ __align__(256) double g_noalloc_thomas_work[kNoAllocThomasDoubles];
 // Device address of that array per device. Host code only sees a host-side
 // stand-in for the symbol; the address a kernel may use comes from
-// cudaGetSymbolAddress, called with the device current.
+// cudaGetSymbolAddress, called with the device current, on the first call per
+// device, and is kept for the life of the process: a process that resets a
+// device (cudaDeviceReset) loads the module into a new context there, and
+// must not call this entry point on that device afterwards.
 std::mutex g_noalloc_mu;
 double* g_noalloc_ptr[64] = {};
 
@@ -475,22 +525,36 @@ constexpr int kRedThreads = 256;
 
 // ---- entry points, one template per ABI function: T = double (the
 // reference's *_f64 names) or float (the *_f32 twins its header reserves,
-// c_kernels.h:15-16) ----
+// c_kernels.h:15-16). The _dev forms take their scratch from the calling
+// thread's DevScratch; the host forms stage everything through one HostCall
+// (cabi_host.cuh) and allocate nothing once the thread's buffers are large
+// enough. ----
+using vgb_cabi::DevScratch;
+using vgb_cabi::HostCall;
+
+size_t thomas_work(int n, int n_sys) { return (size_t)n * (size_t)n_sys * (n > kTallN ? 3 : 1); }
+
+template <typename T>
+int thomas_launch(const T* a, const T* b, const T* c, const T* d, int n, int n_sys, T* x, T* work, int* status,
+                  cudaStream_t st) {
+  if (n > kTallN)
+    k_thomas_tall<T><<<(n_sys + kTallWarps - 1) / kTallWarps, 32 * kTallWarps, 0, st>>>(a, b, c, d, n, n_sys, x,
+                                                                                       work, status);
+  else
+    k_thomas_batched<T><<<(n_sys + 127) / 128, 128, 0, st>>>(a, b, c, d, n, n_sys, x, work, status);
+  return device_ok(cudaGetLastError(), "thomas launch") ? VIBE_C_OK : VIBE_C_ERR_DEVICE;
+}
+
 template <typename T>
 int thomas_batched_dev(const T* a, const T* b, const T* c, const T* d, int n, int n_sys, T* x, int* status,
                        vibe_stream_t stream) {
   if (n <= 0 || n_sys < 0 || b == nullptr || d == nullptr || x == nullptr) return VIBE_C_ERR_BAD_ARG;
   if (n_sys == 0) return VIBE_C_OK;
-  const bool tall = n > kTallN;
-  T* work = (T*)scratch((size_t)n * n_sys * sizeof(T) * (tall ? 3 : 1));
-  if (!work) { g_cerr = "scratch allocation failed"; return VIBE_C_ERR_DEVICE; }
-  if (tall)
-    k_thomas_tall<T><<<(n_sys + kTallWarps - 1) / kTallWarps, 32 * kTallWarps, 0, (cudaStream_t)stream>>>(
-        a, b, c, d, n, n_sys, x, work, status);
-  else
-    k_thomas_batched<T><<<(n_sys + 127) / 128, 128, 0, (cudaStream_t)stream>>>(a, b, c, d, n, n_sys, x, work,
-                                                                              status);
-  return device_ok(cudaGetLastError(), "thomas launch") ? VIBE_C_OK : VIBE_C_ERR_DEVICE;
+  DevScratch w(thomas_work(n, n_sys) * sizeof(T), (cudaStream_t)stream);
+  if (!w.get()) return VIBE_C_ERR_DEVICE;
+  int rc = thomas_launch<T>(a, b, c, d, n, n_sys, x, (T*)w.get(), status, (cudaStream_t)stream);
+  if (!w.release() && rc == VIBE_C_OK) rc = VIBE_C_ERR_DEVICE;
+  return rc;
 }
 
 template <typename T>
@@ -498,26 +562,19 @@ int thomas_batched_host(const T* a, const T* b, const T* c, const T* d, int n, i
   if (n <= 0 || n_sys < 0 || b == nullptr || d == nullptr || x == nullptr) return VIBE_C_ERR_BAD_ARG;
   if (n_sys == 0) return VIBE_C_OK;
   const size_t e = sizeof(T), nn = (size_t)n * n_sys, no = (size_t)(n - 1) * n_sys;
-  DBuf da(a ? no * e + e : 0), db(nn * e), dc(c ? no * e + e : 0), dd(nn * e), dx(nn * e), ds((size_t)n_sys * 4);
-  if (!db.p || !dd.p || !dx.p || !ds.p || (a && !da.p) || (c && !dc.p)) { g_cerr = "cudaMalloc failed"; return VIBE_C_ERR_DEVICE; }
-  cudaStream_t st = own_stream();
-  bool ok = true;
-  if (a && no) ok &= device_ok(cudaMemcpyAsync(da.p, a, no * e, cudaMemcpyHostToDevice, st), "H2D a");
-  if (c && no) ok &= device_ok(cudaMemcpyAsync(dc.p, c, no * e, cudaMemcpyHostToDevice, st), "H2D c");
-  ok &= device_ok(cudaMemcpyAsync(db.p, b, nn * e, cudaMemcpyHostToDevice, st), "H2D b");
-  ok &= device_ok(cudaMemcpyAsync(dd.p, d, nn * e, cudaMemcpyHostToDevice, st), "H2D d");
-  if (!ok) return VIBE_C_ERR_DEVICE;
-  int rc = thomas_batched_dev<T>(a ? da.as<T>() : nullptr, db.as<T>(), c ? dc.as<T>() : nullptr, dd.as<T>(), n, n_sys,
-                                 dx.as<T>(), ds.as<int>(), (vibe_stream_t)st);
+  HostCall hc;
+  const int ia = hc.add(a, no * e, HostCall::kIn), ib = hc.add(b, nn * e, HostCall::kIn);
+  const int ic = hc.add(c, no * e, HostCall::kIn), id = hc.add(d, nn * e, HostCall::kIn);
+  const int ix = hc.add(x, nn * e, HostCall::kOut), is = hc.add(nullptr, (size_t)n_sys * sizeof(int), HostCall::kOut);
+  const int iw = hc.add(nullptr, thomas_work(n, n_sys) * e, HostCall::kScratch);
+  if (!hc.commit()) return VIBE_C_ERR_DEVICE;
+  int rc = thomas_launch<T>(hc.dev<T>(ia), hc.dev<T>(ib), hc.dev<T>(ic), hc.dev<T>(id), n, n_sys, hc.dev<T>(ix),
+                            hc.dev<T>(iw), hc.dev<int>(is), hc.stream());
+  if (!hc.finish()) return VIBE_C_ERR_DEVICE;
   if (rc) return rc;
-  std::string st_host((size_t)n_sys * 4, '\0');
-  ok &= device_ok(cudaMemcpyAsync(x, dx.p, nn * e, cudaMemcpyDeviceToHost, st), "D2H x");
-  ok &= device_ok(cudaMemcpyAsync(&st_host[0], ds.p, (size_t)n_sys * 4, cudaMemcpyDeviceToHost, st), "D2H status");
-  ok &= device_ok(cudaStreamSynchronize(st), "sync");
-  if (!ok) return VIBE_C_ERR_DEVICE;
-  const int* sv = (const int*)st_host.data();
-  for (int s = 0; s < n_sys; ++s)
-    if (sv[s] != VIBE_C_OK) return sv[s];
+  const int* sv = (const int*)hc.host(is);
+  for (int q = 0; q < n_sys; ++q)
+    if (sv[q] != VIBE_C_OK) return sv[q];
   return VIBE_C_OK;
 }
 
@@ -533,16 +590,15 @@ int weno_batched_dev(const T* q, size_t n, T* q_left, T* q_right, vibe_stream_t 
 template <typename T>
 void weno_host(T qm2, T qm1, T q0, T q1, T q2, T* q_left, T* q_right) {
   if (q_left == nullptr || q_right == nullptr) return;
-  const size_t e = sizeof(T);
-  DBuf dq(5 * e), dl(e), dr(e);
-  if (!dq.p || !dl.p || !dr.p) { g_cerr = "cudaMalloc failed"; *q_left = *q_right = (T)NAN; return; }
   const T q[5] = {qm2, qm1, q0, q1, q2};
-  cudaStream_t st = own_stream();
-  bool ok = device_ok(cudaMemcpyAsync(dq.p, q, 5 * e, cudaMemcpyHostToDevice, st), "H2D");
-  ok = ok && weno_batched_dev<T>(dq.as<T>(), 1, dl.as<T>(), dr.as<T>(), (vibe_stream_t)st) == VIBE_C_OK;
-  ok = ok && device_ok(cudaMemcpyAsync(q_left, dl.p, e, cudaMemcpyDeviceToHost, st), "D2H");
-  ok = ok && device_ok(cudaMemcpyAsync(q_right, dr.p, e, cudaMemcpyDeviceToHost, st), "D2H");
-  ok = ok && device_ok(cudaStreamSynchronize(st), "sync");
+  const size_t e = sizeof(T);
+  HostCall hc;
+  const int iq = hc.add(q, 5 * e, HostCall::kIn), il = hc.add(q_left, e, HostCall::kOut),
+            ir = hc.add(q_right, e, HostCall::kOut);
+  bool ok = hc.commit();
+  ok = ok && weno_batched_dev<T>(hc.dev<T>(iq), 1, hc.dev<T>(il), hc.dev<T>(ir), (vibe_stream_t)hc.stream()) ==
+                 VIBE_C_OK;
+  ok = hc.finish() && ok;
   if (!ok) *q_left = *q_right = (T)NAN;
 }
 
@@ -552,30 +608,36 @@ T bilinear_host(const T* f, int halo, int nsx, int nsy, int nz, T xi, T yj, int 
   if (k < 0) k = 0;
   if (k >= nz) k = nz - 1;
   const size_t plane = (size_t)nsx * nsy, e = sizeof(T);
-  DBuf dp(plane * e), dout(e);
-  if (!dp.p || !dout.p) { g_cerr = "cudaMalloc failed"; return (T)NAN; }
-  cudaStream_t st = own_stream();
   T r = (T)NAN;
-  bool ok = device_ok(cudaMemcpyAsync(dp.p, f + (size_t)(k + halo) * plane, plane * e, cudaMemcpyHostToDevice, st), "H2D");
+  HostCall hc;
+  const int ip = hc.add(f + (size_t)(k + halo) * plane, plane * e, HostCall::kIn), io = hc.add(&r, e, HostCall::kOut);
+  bool ok = hc.commit();
   if (ok) {
-    k_bilinear<T><<<1, 1, 0, st>>>(dp.as<T>(), halo, nsx, nsy, xi, yj, dout.as<T>());
+    k_bilinear<T><<<1, 1, 0, hc.stream()>>>(hc.dev<T>(ip), halo, nsx, nsy, xi, yj, hc.dev<T>(io));
     ok = device_ok(cudaGetLastError(), "bilinear launch");
   }
-  ok = ok && device_ok(cudaMemcpyAsync(&r, dout.p, e, cudaMemcpyDeviceToHost, st), "D2H");
-  ok = ok && device_ok(cudaStreamSynchronize(st), "sync");
+  ok = hc.finish() && ok;
   return ok ? r : (T)NAN;
+}
+
+template <typename T>
+int cfl_launch(const T* u, const T* v, const T* w, const T* dzeta, const T* zs, int nx, int ny, int nz, T dx, T dy,
+               T z_top, T dt, T* out3, T* part, cudaStream_t st) {
+  k_cfl_partial<T><<<kRedBlocks, kRedThreads, 0, st>>>(u, v, w, dzeta, zs, nx, ny, nz, dx, dy, z_top, dt, part);
+  k_cfl_final<T><<<1, kRedThreads, 0, st>>>(part, kRedBlocks, out3);
+  return device_ok(cudaGetLastError(), "cfl launch") ? VIBE_C_OK : VIBE_C_ERR_DEVICE;
 }
 
 template <typename T>
 int cfl_dev(const T* u, const T* v, const T* w, const T* dzeta, const T* zs, int nx, int ny, int nz, T dx, T dy,
             T z_top, T dt, T* out3, vibe_stream_t stream) {
   if (!u || !v || !w || !dzeta || !out3 || nx < 0 || ny < 0 || nz < 0) return VIBE_C_ERR_BAD_ARG;
-  T* part = (T*)scratch((size_t)3 * kRedBlocks * sizeof(T));
-  if (!part) { g_cerr = "scratch allocation failed"; return VIBE_C_ERR_DEVICE; }
-  cudaStream_t st = (cudaStream_t)stream;
-  k_cfl_partial<T><<<kRedBlocks, kRedThreads, 0, st>>>(u, v, w, dzeta, zs, nx, ny, nz, dx, dy, z_top, dt, part);
-  k_cfl_final<T><<<1, kRedThreads, 0, st>>>(part, kRedBlocks, out3);
-  return device_ok(cudaGetLastError(), "cfl launch") ? VIBE_C_OK : VIBE_C_ERR_DEVICE;
+  DevScratch part((size_t)3 * kRedBlocks * sizeof(T), (cudaStream_t)stream);
+  if (!part.get()) return VIBE_C_ERR_DEVICE;
+  int rc = cfl_launch<T>(u, v, w, dzeta, zs, nx, ny, nz, dx, dy, z_top, dt, out3, (T*)part.get(),
+                         (cudaStream_t)stream);
+  if (!part.release() && rc == VIBE_C_OK) rc = VIBE_C_ERR_DEVICE;
+  return rc;
 }
 
 template <typename T>
@@ -584,23 +646,17 @@ T cfl_host(const T* u, const T* v, const T* w, const T* dzeta, const T* zs, int 
   if (u == nullptr || v == nullptr || w == nullptr || dzeta == nullptr) return (T)0;
   const size_t e = sizeof(T);
   const size_t n = (size_t)(nx > 0 ? nx : 0) * (ny > 0 ? ny : 0) * (nz > 0 ? nz : 0);
-  const size_t nzp = (size_t)(nz > 0 ? nz : 0);
-  DBuf du(n * e + e), dv(n * e + e), dw(n * e + e), dz(nzp * e + e), dzs(zs ? (size_t)nx * ny * e + e : 0), dout(3 * e);
-  if (!du.p || !dv.p || !dw.p || !dz.p || !dout.p || (zs && !dzs.p)) { g_cerr = "cudaMalloc failed"; return (T)NAN; }
-  cudaStream_t st = own_stream();
-  bool ok = true;
-  ok &= device_ok(cudaMemcpyAsync(du.p, u, n * e, cudaMemcpyHostToDevice, st), "H2D");
-  ok &= device_ok(cudaMemcpyAsync(dv.p, v, n * e, cudaMemcpyHostToDevice, st), "H2D");
-  ok &= device_ok(cudaMemcpyAsync(dw.p, w, n * e, cudaMemcpyHostToDevice, st), "H2D");
-  ok &= device_ok(cudaMemcpyAsync(dz.p, dzeta, nzp * e, cudaMemcpyHostToDevice, st), "H2D");
-  if (zs) ok &= device_ok(cudaMemcpyAsync(dzs.p, zs, (size_t)nx * ny * e, cudaMemcpyHostToDevice, st), "H2D");
-  if (!ok) return (T)NAN;
-  if (cfl_dev<T>(du.as<T>(), dv.as<T>(), dw.as<T>(), dz.as<T>(), zs ? dzs.as<T>() : nullptr, nx, ny, nz, dx, dy, z_top,
-                 dt, dout.as<T>(), (vibe_stream_t)st) != VIBE_C_OK)
-    return (T)NAN;
-  T r[3];
-  ok &= device_ok(cudaMemcpyAsync(r, dout.p, 3 * e, cudaMemcpyDeviceToHost, st), "D2H");
-  ok &= device_ok(cudaStreamSynchronize(st), "sync");
+  const size_t nzp = (size_t)(nz > 0 ? nz : 0), nxy = (size_t)(nx > 0 ? nx : 0) * (ny > 0 ? ny : 0);
+  T r[3] = {(T)NAN, (T)NAN, (T)NAN};
+  HostCall hc;
+  const int iu = hc.add(u, n * e, HostCall::kIn), iv = hc.add(v, n * e, HostCall::kIn),
+            iw = hc.add(w, n * e, HostCall::kIn), iz = hc.add(dzeta, nzp * e, HostCall::kIn),
+            izs = hc.add(zs, zs ? nxy * e : 0, HostCall::kIn), io = hc.add(r, 3 * e, HostCall::kOut),
+            ip = hc.add(nullptr, (size_t)3 * kRedBlocks * e, HostCall::kScratch);
+  bool ok = hc.commit();
+  ok = ok && cfl_launch<T>(hc.dev<T>(iu), hc.dev<T>(iv), hc.dev<T>(iw), hc.dev<T>(iz), hc.dev<T>(izs), nx, ny, nz, dx,
+                           dy, z_top, dt, hc.dev<T>(io), hc.dev<T>(ip), hc.stream()) == VIBE_C_OK;
+  ok = hc.finish() && ok;
   if (!ok) return (T)NAN;
   if (max_wind_out) *max_wind_out = r[1];
   if (min_dz_out) *min_dz_out = r[2];
@@ -608,11 +664,7 @@ T cfl_host(const T* u, const T* v, const T* w, const T* dzeta, const T* zs, int 
 }
 
 template <typename T>
-int neu_dev(const T* x, size_t n, T* out, vibe_stream_t stream) {
-  if (!x || !out) return VIBE_C_ERR_BAD_ARG;
-  T* part = (T*)scratch((size_t)2 * kRedBlocks * sizeof(T));
-  if (!part) { g_cerr = "scratch allocation failed"; return VIBE_C_ERR_DEVICE; }
-  cudaStream_t st = (cudaStream_t)stream;
+int neu_launch(const T* x, size_t n, T* out, T* part, cudaStream_t st) {
   const size_t chunk = (n + kRedBlocks - 1) / kRedBlocks;
   k_neu_partial<T><<<kRedBlocks, kRedThreads, 0, st>>>(x, n, chunk > 0 ? chunk : 1, part);
   k_neu_final<T><<<1, kRedThreads, 0, st>>>(part, kRedBlocks, out);
@@ -620,17 +672,26 @@ int neu_dev(const T* x, size_t n, T* out, vibe_stream_t stream) {
 }
 
 template <typename T>
+int neu_dev(const T* x, size_t n, T* out, vibe_stream_t stream) {
+  if (!x || !out) return VIBE_C_ERR_BAD_ARG;
+  DevScratch part((size_t)2 * kRedBlocks * sizeof(T), (cudaStream_t)stream);
+  if (!part.get()) return VIBE_C_ERR_DEVICE;
+  int rc = neu_launch<T>(x, n, out, (T*)part.get(), (cudaStream_t)stream);
+  if (!part.release() && rc == VIBE_C_OK) rc = VIBE_C_ERR_DEVICE;
+  return rc;
+}
+
+template <typename T>
 T neu_host(const T* x, size_t n) {
   if (x == nullptr) return (T)0;
   const size_t e = sizeof(T);
-  DBuf dx(n * e + e), dout(e);
-  if (!dx.p || !dout.p) { g_cerr = "cudaMalloc failed"; return (T)NAN; }
-  cudaStream_t st = own_stream();
-  bool ok = device_ok(cudaMemcpyAsync(dx.p, x, n * e, cudaMemcpyHostToDevice, st), "H2D");
-  ok = ok && neu_dev<T>(dx.as<T>(), n, dout.as<T>(), (vibe_stream_t)st) == VIBE_C_OK;
   T r = (T)NAN;
-  ok = ok && device_ok(cudaMemcpyAsync(&r, dout.p, e, cudaMemcpyDeviceToHost, st), "D2H");
-  ok = ok && device_ok(cudaStreamSynchronize(st), "sync");
+  HostCall hc;
+  const int ix = hc.add(x, n * e, HostCall::kIn), io = hc.add(&r, e, HostCall::kOut),
+            ip = hc.add(nullptr, (size_t)2 * kRedBlocks * e, HostCall::kScratch);
+  bool ok = hc.commit();
+  ok = ok && neu_launch<T>(hc.dev<T>(ix), n, hc.dev<T>(io), hc.dev<T>(ip), hc.stream()) == VIBE_C_OK;
+  ok = hc.finish() && ok;
   return ok ? r : (T)NAN;
 }
 
@@ -653,31 +714,155 @@ void flux_host(const T* q, const T* rho, const T* u, const T* v, const T* w, con
     return;
   const size_t n = (size_t)nx * ny * nz, e = sizeof(T);
   if (n == 0) return;
-  DBuf dq(n * e), dr(n * e), du(n * e), dv(n * e), dw(n * e), dz((size_t)nz * e), dzs(zs ? (size_t)nx * ny * e : 0),
-      dout(n * e);
-  if (!dq.p || !dr.p || !du.p || !dv.p || !dw.p || !dz.p || !dout.p || (zs && !dzs.p)) { g_cerr = "cudaMalloc failed"; return; }
-  cudaStream_t st = own_stream();
-  bool ok = true;
-  ok &= device_ok(cudaMemcpyAsync(dq.p, q, n * e, cudaMemcpyHostToDevice, st), "H2D");
-  ok &= device_ok(cudaMemcpyAsync(dr.p, rho, n * e, cudaMemcpyHostToDevice, st), "H2D");
-  ok &= device_ok(cudaMemcpyAsync(du.p, u, n * e, cudaMemcpyHostToDevice, st), "H2D");
-  ok &= device_ok(cudaMemcpyAsync(dv.p, v, n * e, cudaMemcpyHostToDevice, st), "H2D");
-  ok &= device_ok(cudaMemcpyAsync(dw.p, w, n * e, cudaMemcpyHostToDevice, st), "H2D");
-  ok &= device_ok(cudaMemcpyAsync(dz.p, dzeta, (size_t)nz * e, cudaMemcpyHostToDevice, st), "H2D");
-  if (zs) ok &= device_ok(cudaMemcpyAsync(dzs.p, zs, (size_t)nx * ny * e, cudaMemcpyHostToDevice, st), "H2D");
-  if (!ok) return;
-  if (flux_dev<T>(dq.as<T>(), dr.as<T>(), du.as<T>(), dv.as<T>(), dw.as<T>(), dz.as<T>(), zs ? dzs.as<T>() : nullptr,
-                  nx, ny, nz, dx, dy, z_top, dout.as<T>(), (vibe_stream_t)st) != VIBE_C_OK)
-    return;
-  device_ok(cudaMemcpyAsync(dqdt, dout.p, n * e, cudaMemcpyDeviceToHost, st), "D2H");
-  device_ok(cudaStreamSynchronize(st), "sync");
+  HostCall hc;
+  const int iq = hc.add(q, n * e, HostCall::kIn), ir = hc.add(rho, n * e, HostCall::kIn),
+            iu = hc.add(u, n * e, HostCall::kIn), iv = hc.add(v, n * e, HostCall::kIn),
+            iw = hc.add(w, n * e, HostCall::kIn), iz = hc.add(dzeta, (size_t)nz * e, HostCall::kIn),
+            izs = hc.add(zs, zs ? (size_t)nx * ny * e : 0, HostCall::kIn), io = hc.add(dqdt, n * e, HostCall::kOut);
+  bool ok = hc.commit();
+  ok = ok && flux_dev<T>(hc.dev<T>(iq), hc.dev<T>(ir), hc.dev<T>(iu), hc.dev<T>(iv), hc.dev<T>(iw), hc.dev<T>(iz),
+                         hc.dev<T>(izs), nx, ny, nz, dx, dy, z_top, hc.dev<T>(io), (vibe_stream_t)hc.stream()) ==
+                 VIBE_C_OK;
+  hc.finish();
 }
 
 }  // namespace
 
+// ---- vgb_cabi: the call machinery declared in cabi_host.cuh ----
+namespace vgb_cabi {
+
+void set_error(const char* what, cudaError_t e) { device_ok(e, what); }
+unsigned long long allocations() { return g_allocs.load(); }
+
+HostCall::HostCall() {
+  Ctx* c = ctx();
+  ctx_ = c;
+  ok_ = c != nullptr;
+}
+
+int HostCall::add(const void* h, size_t bytes, Kind kind) {
+  Arg a{h, bytes, 0, kind, (kind == kIn || kind == kInOut) && h == nullptr};
+  args_.push_back(a);
+  return (int)args_.size() - 1;
+}
+
+cudaStream_t HostCall::stream() const { return ctx_ ? static_cast<Ctx*>(ctx_)->st : nullptr; }
+
+// Layout in the device buffer: [inputs | in-outs | outputs | scratch]; the
+// pinned buffer mirrors the first three regions. One copy moves
+// [0, end of in-outs) to the device, one copy moves [in-outs, outputs) back.
+bool HostCall::commit() {
+  if (!ok_) return false;
+  Ctx* c = static_cast<Ctx*>(ctx_);
+  size_t off = 0;
+  for (int k = kIn; k <= kScratch; ++k) {
+    if (k == kInOut) d2h_beg_ = off;
+    for (auto& a : args_)
+      if (a.kind == k && !a.absent) {
+        a.off = off;
+        off = align256(off + a.bytes);
+      }
+    if (k == kInOut) h2d_end_ = off;
+    if (k == kOut) d2h_end_ = off;
+  }
+  const size_t total = off > 0 ? off : 256;
+  if (c->dbuf_n < total) {
+    if (c->dbuf) cudaFree(c->dbuf);
+    c->dbuf = nullptr;
+    const size_t n = grown(c->dbuf_n, total);
+    c->dbuf_n = 0;
+    ++g_allocs;
+    if (!device_ok(cudaMalloc(&c->dbuf, n), "cudaMalloc (staging)")) return ok_ = false;
+    c->dbuf_n = n;
+  }
+  if (c->pin_n < d2h_end_) {
+    if (c->pin) cudaFreeHost(c->pin);
+    c->pin = nullptr;
+    const size_t n = grown(c->pin_n, d2h_end_);
+    c->pin_n = 0;
+    ++g_allocs;
+    if (!device_ok(cudaMallocHost(&c->pin, n), "cudaMallocHost (staging)")) return ok_ = false;
+    c->pin_n = n;
+  }
+  base_ = c->dbuf;
+  for (const auto& a : args_)
+    if ((a.kind == kIn || a.kind == kInOut) && !a.absent && a.bytes) std::memcpy(c->pin + a.off, a.h, a.bytes);
+  if (h2d_end_ && !device_ok(cudaMemcpyAsync(c->dbuf, c->pin, h2d_end_, cudaMemcpyHostToDevice, c->st), "H2D"))
+    return ok_ = false;
+  return true;
+}
+
+bool HostCall::finish() {
+  if (!ctx_) return false;
+  Ctx* c = static_cast<Ctx*>(ctx_);
+  bool good = ok_;
+  if (good && d2h_end_ > d2h_beg_)
+    good = device_ok(cudaMemcpyAsync(c->pin + d2h_beg_, c->dbuf + d2h_beg_, d2h_end_ - d2h_beg_,
+                                     cudaMemcpyDeviceToHost, c->st),
+                     "D2H");
+  // always wait: the staging buffers must be idle before the thread's next call
+  good = device_ok(cudaStreamSynchronize(c->st), "sync") && good;
+  if (good)
+    for (const auto& a : args_)
+      if ((a.kind == kInOut || a.kind == kOut) && a.h && a.bytes)
+        std::memcpy(const_cast<void*>(a.h), c->pin + a.off, a.bytes);
+  return ok_ = good;
+}
+
+const void* HostCall::host(int id) const {
+  return ctx_ ? static_cast<Ctx*>(ctx_)->pin + args_[id].off : nullptr;
+}
+
+DevScratch::DevScratch(size_t bytes, cudaStream_t stream) : s_(stream) {
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  if (!device_ok(cudaStreamIsCapturing(stream, &cs), "cudaStreamIsCapturing")) return;
+  if (cs != cudaStreamCaptureStatusNone) {  // inside a capture: graph-owned, stream-ordered memory
+    graph_ = true;
+    if (!device_ok(cudaMallocAsync(&p_, bytes > 0 ? bytes : 256, stream), "cudaMallocAsync (captured scratch)"))
+      p_ = nullptr;
+    return;
+  }
+  Ctx* c = ctx();
+  if (!c) return;
+  if (c->scr_n < bytes) {
+    // the old buffer goes once its last user has finished
+    if (c->has_last && !device_ok(cudaEventSynchronize(c->last), "scratch wait")) return;
+    if (c->scr) cudaFree(c->scr);
+    c->scr = nullptr;
+    const size_t n = grown(c->scr_n, bytes);
+    c->scr_n = 0;
+    ++g_allocs;
+    if (!device_ok(cudaMalloc(&c->scr, n), "cudaMalloc (scratch)")) return;
+    c->scr_n = n;
+  }
+  // after the previous user of this thread's scratch, whatever its stream
+  if (c->has_last && !device_ok(cudaStreamWaitEvent(stream, c->last, 0), "scratch order")) return;
+  p_ = c->scr;
+}
+
+bool DevScratch::release() {
+  if (released_) return p_ != nullptr;
+  released_ = true;
+  if (!p_) return false;
+  if (graph_) return device_ok(cudaFreeAsync(p_, s_), "cudaFreeAsync (captured scratch)");
+  Ctx* c = ctx();
+  if (!c) return false;
+  if (!device_ok(cudaEventRecord(c->last, s_), "scratch record")) return false;
+  c->has_last = true;
+  return true;
+}
+
+DevScratch::~DevScratch() {
+  if (!released_) release();
+}
+
+}  // namespace vgb_cabi
+
 extern "C" {
 
 const char* vibe_c_last_error(void) { return g_cerr.c_str(); }
+
+unsigned long long vibe_c_allocations(void) { return vgb_cabi::allocations(); }
 
 // ---- FP64: the reference's names ----
 int vibe_tridiagonal_solve_batched_f64_dev(const double* a, const double* b, const double* c, const double* d, int n,

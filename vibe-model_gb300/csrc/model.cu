@@ -2015,11 +2015,17 @@ int group_prepare(vibe_gb300_group* g, double dt, int n_sub) {
     if (m->cur != parity0) return fail(VIBE_GB300_EUNSUPPORTED, "group members must share the state parity");
     CUDA_OK(cudaStreamSynchronize(m->stream));  // nothing of theirs in flight
   }
-  if (g->dt == dt && g->nsub == n_sub) return 0;
+  // A member stepped alone, or run through a substep / TL-AD entry point, may
+  // have rebuilt its per-model dt tables (HEVI LU factors, sponge weights)
+  // for another dt since the group last ran: put them back for the group's
+  // (dt, n_sub) on every call. The tables are rewritten in place (same device
+  // pointers), so the work lists and captured graphs below stay valid; the
+  // call is free when a member's tables already match.
   CUDA_OK(cudaStreamSynchronize(g->stream));
-  group_drop(g);
   for (auto* m : g->ms)
     if (int rc = configure_dt(m, dt, n_sub)) return rc;
+  if (g->dt == dt && g->nsub == n_sub) return 0;
+  group_drop(g);
   for (int p = 0; p < 2; ++p) {
     std::vector<MixedDomain> doms;
     for (auto* m : g->ms) {
