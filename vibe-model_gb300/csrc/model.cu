@@ -96,6 +96,7 @@ struct vibe_gb300_model {
   double* d_zmid = nullptr;
   double* d_zs = nullptr;
   double* scratch = nullptr;
+  double* wface = nullptr;  // FP64 path: WENO face fluxes of one scalar
   double *d_dzeta = nullptr, *d_scale = nullptr, *d_sponge = nullptr;
   double *d_th0 = nullptr, *d_pi0 = nullptr, *d_rho0 = nullptr;
   double* d_stage_in = nullptr;   // staging for FieldT <-> device layout
@@ -667,7 +668,7 @@ int enqueue_one_step(vibe_gb300_model* m, double dt, int n_sub) {
         double** src = (stage == 0) ? S0 : S1;
         {
           Span sp(m, 0);
-          m->f64->slow_tendency(d, m->met, m->fl, src, m->tend, m->scratch, m->stream);
+          m->f64->slow_tendency(d, m->met, m->fl, src, m->tend, m->scratch, m->wface, m->stream);
           if (m->phys_fn) {
             if (int rc = physics_stage(m, stage, dt, (const void* const*)src)) return rc;
             const size_t n = d.plane * (size_t)(d.nz + 1);
@@ -933,8 +934,9 @@ int vibe_gb300_model_create(const vibe_gb300_setup* s, int precision, vibe_gb300
   if (!rc && precision == VIBE_GB300_FP64) {
     for (int q = 0; q < NSPECIES && !rc; ++q) rc = dalloc(m, &m->tend[q], nfield);
     for (int q = 0; q < NSPECIES && !rc; ++q) rc = (q == W || q == RHO || q == PI) ? dalloc(m, &m->tmp[q], nfield) : 0;
-    const size_t scr = std::max(m->d.plane * (size_t)nz + (size_t)nx * ny * 2 * nz, (size_t)nx * ny * (5 * (size_t)nz + 2));
+    const size_t scr = std::max(m->d.plane * (size_t)nz + (size_t)nx * ny * 2 * nz, (size_t)nx * ny * (6 * (size_t)nz + 6));
     rc = rc ? rc : dalloc(m, &m->scratch, std::max(scr, nfield));
+    rc = rc ? rc : dalloc(m, &m->wface, 3 * nfield);  // WENO face fluxes of one scalar (x, y, z faces)
   }
   if (!rc && precision == VIBE_GB300_MIXED) {
     for (int q = 0; q < NSPECIES && !rc; ++q) rc = dalloc(m, &m->W0[q], nfield);
@@ -957,6 +959,7 @@ int vibe_gb300_model_create(const vibe_gb300_setup* s, int precision, vibe_gb300
       cudaMemcpy(m->d_sponge, m->hs.sponge.data(), nz * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess)
     return bail(fail(VIBE_GB300_EDEVICE, "metric upload failed"));
   m->met.dx = s->dx; m->met.dy = s->dy; m->met.z_top = s->z_top;
+  m->met.inv_dx = 1.0 / s->dx; m->met.inv_dy = 1.0 / s->dy;
   m->met.dzeta = m->d_dzeta; m->met.scale = m->d_scale; m->met.sponge = m->d_sponge;
   m->met.th0 = m->d_th0; m->met.pi0 = m->d_pi0; m->met.rho0 = m->d_rho0;
   {
@@ -1093,7 +1096,7 @@ int vibe_gb300_slow_tendency(vibe_gb300_model* m, double* const* host_out) {
     CUDA_OK(cudaStreamSynchronize(m->stream));
     return read_status(m);
   }
-  m->f64->slow_tendency(m->d, m->met, m->fl, m->S[m->cur], m->tend, m->scratch, m->stream);
+  m->f64->slow_tendency(m->d, m->met, m->fl, m->S[m->cur], m->tend, m->scratch, m->wface, m->stream);
   for (int q = 0; q < NSPECIES; ++q) {
     int ni, nj, nk;
     box_of(m, q, ni, nj, nk);
@@ -1154,7 +1157,7 @@ int acoustic_linear(vibe_gb300_model* m, double dtau, int n_sub, const double* c
     for (int f = 0; f < 3; ++f)
       if (int rc = dalloc(m, &m->lin_tmp[f], nfield)) return rc;
     if (int rc = dalloc(m, &m->lin_dh, nfield)) return rc;
-    if (int rc = dalloc(m, &m->lin_scr, (size_t)m->d.nx * m->d.ny * (5 * (size_t)m->d.nz + 2))) return rc;
+    if (int rc = dalloc(m, &m->lin_scr, (size_t)m->d.nx * m->d.ny * (6 * (size_t)m->d.nz + 6))) return rc;
   }
   double* st[NSPECIES] = {};  // the substep kernels see the perturbation as their state
   for (int f = 0; f < 5; ++f) {
@@ -1851,7 +1854,7 @@ int vibe_gb300_si_step(vibe_gb300_model* m, double dt, int kind, int max_iter, d
     }
   }
   double* const* st = m->S[m->cur];
-  m->f64->slow_tendency(d, m->met, m->fl, st, m->tend, m->scratch, m->stream);
+  m->f64->slow_tendency(d, m->met, m->fl, st, m->tend, m->scratch, m->wface, m->stream);
   si_assemble(d, m->met, st, m->tend, dt, m->hz_a, m->hz_b, m->hz_f, m->stream);
   CUDA_OK(cudaGetLastError());
   if (!m->hz_ev[0]) {

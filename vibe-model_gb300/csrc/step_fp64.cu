@@ -18,6 +18,15 @@
 #define FP64_FN(name) name
 #endif
 
+// a / b as the reference writes it (bit-exact build), or a * rb with the
+// reciprocal rb = 1/b computed once (fast build: an FP64 division costs a
+// dozen FP64 operations on this GPU, which has few of them)
+#ifdef VGB_FP64_EXACT
+#define DIVR(a, b, rb) ((a) / (b))
+#else
+#define DIVR(a, b, rb) ((a) * (rb))
+#endif
+
 namespace vgb {
 namespace {
 
@@ -76,12 +85,50 @@ __device__ inline void weno5(double qm2, double qm1, double q0, double q1, doubl
   const double c2 = d2 / ((eps + g2) * (eps + g2));
   qr = (c0 * u0 + c1 * u1 + c2 * u2) / (c0 + c1 + c2);
 }
+#ifdef VGB_FP64_EXACT
 __device__ inline double weno_face(double qm2, double qm1, double q0, double q1, double q2, double vel) {
   double ql, qr;
   weno5(qm2, qm1, q0, q1, q2, ql, qr);
   const double alpha = dmax(fabs(vel), 1e-3);
   return 0.5 * (vel * (ql + qr) - alpha * (qr - ql));
 }
+#else
+// The same face flux with the arithmetic arranged for the FP64 pipe: the
+// right-biased reconstruction is the left-biased one of the reversed
+// stencil (same three smoothness indicators, reversed), the weights
+// a_k = d_k / s_k^2 (s_k = eps + beta_k) are normalised with one division
+// by scaling numerator and denominator with (s0 s1 s2)^2, the 1/6 is a
+// multiplication, and for |vel| >= 1e-3 the Lax-Friedrichs flux
+// 0.5*(vel*(ql+qr) - |vel|*(qr-ql)) is vel times the upwind reconstruction
+// alone. Equal to the reference's to rounding.
+__device__ inline double weno_left_d(double qm2, double qm1, double q0, double q1, double q2, double s0, double s1,
+                                     double s2) {
+  const double sixth = 1.0 / 6.0;
+  const double v0 = (2.0 * qm2 - 7.0 * qm1 + 11.0 * q0) * sixth;
+  const double v1 = (-qm1 + 5.0 * q0 + 2.0 * q1) * sixth;
+  const double v2 = (2.0 * q0 + 5.0 * q1 - q2) * sixth;
+  const double p01 = s0 * s1, p02 = s0 * s2, p12 = s1 * s2;
+  const double w0 = 0.1 * (p12 * p12), w1 = 0.6 * (p02 * p02), w2 = 0.3 * (p01 * p01);
+  return (w0 * v0 + w1 * v1 + w2 * v2) / (w0 + w1 + w2);
+}
+__device__ inline double weno_face(double qm2, double qm1, double q0, double q1, double q2, double vel) {
+  const double eps = 1e-6;
+  const double e0 = qm2 - 2.0 * qm1 + q0, f0 = qm2 - 4.0 * qm1 + 3.0 * q0;
+  const double e1 = qm1 - 2.0 * q0 + q1, f1 = qm1 - q1;
+  const double e2 = q0 - 2.0 * q1 + q2, f2 = 3.0 * q0 - 4.0 * q1 + q2;
+  const double s0 = eps + (13.0 / 12.0) * (e0 * e0) + 0.25 * (f0 * f0);
+  const double s1 = eps + (13.0 / 12.0) * (e1 * e1) + 0.25 * (f1 * f1);
+  const double s2 = eps + (13.0 / 12.0) * (e2 * e2) + 0.25 * (f2 * f2);
+  const bool up = vel >= 0.0;
+  const double a0 = up ? qm2 : q2, a1 = up ? qm1 : q1, a3 = up ? q1 : qm1, a4 = up ? q2 : qm2;
+  const double t0 = up ? s0 : s2, t2 = up ? s2 : s0;
+  const double rec = weno_left_d(a0, a1, q0, a3, a4, t0, s1, t2);
+  if (fabs(vel) >= 1e-3) return vel * rec;
+  const double oth = weno_left_d(a4, a3, q0, a1, a0, t2, s1, t0);
+  const double ql = up ? rec : oth, qr = up ? oth : rec;
+  return 0.5 * (vel * (ql + qr) - 1e-3 * (qr - ql));
+}
+#endif
 
 // grad_x / grad_y, advection.cpp:106-136 (q = species index)
 __device__ inline double grad_x(const CS& s, const Dims& d, int q, int i, int j, int k, double inv_dx, int order) {
@@ -128,19 +175,19 @@ __device__ inline double mass_div0(const CS& s, const Metric& m, const Dims& d, 
                     SF(V, i, j, k) * 0.5 * (R3(r0, d, i, imax(j - 1, 0), k) + R3(r0, d, i, j, k));
   const double fz = SF(W, i, j, k + 1) * 0.5 * (R3(r0, d, i, j, k) + R3(r0, d, i, j, imin(k + 1, d.nz - 1))) -
                     SF(W, i, j, k) * 0.5 * (R3(r0, d, i, j, imax(k - 1, 0)) + R3(r0, d, i, j, k));
-  return -(fx / m.dx + fy / m.dy + fz / dz);
+  return -(DIVR(fx, m.dx, m.inv_dx) + DIVR(fy, m.dy, m.inv_dy) + DIVR(fz, dz, 1.0 / dz));
 }
 
 // acoustic pressure-gradient tendencies, equations.cpp:157-184
 __device__ inline double ac_u(const CS& s, const Metric& m, const Dims& d, const Flags& fl, int i, int j, int k) {
   const int ip = imin(i, d.nx - 1), im = imax(i - 1, 0);
   const double t0 = 0.5 * (R3(m.th0, d, im, j, k) + R3(m.th0, d, ip, j, k));
-  return -kCp * t0 * dpi(s, m, d, fl, ip, j, k, im, j, k) / m.dx;
+  return DIVR(-kCp * t0 * dpi(s, m, d, fl, ip, j, k, im, j, k), m.dx, m.inv_dx);
 }
 __device__ inline double ac_v(const CS& s, const Metric& m, const Dims& d, const Flags& fl, int i, int j, int k) {
   const int jp = imin(j, d.ny - 1), jm = imax(j - 1, 0);
   const double t0 = 0.5 * (R3(m.th0, d, i, jm, k) + R3(m.th0, d, i, jp, k));
-  return -kCp * t0 * dpi(s, m, d, fl, i, jp, k, i, jm, k) / m.dy;
+  return DIVR(-kCp * t0 * dpi(s, m, d, fl, i, jp, k, i, jm, k), m.dy, m.inv_dy);
 }
 __device__ inline double ac_w(const CS& s, const Metric& m, const Dims& d, const Flags& fl, int i, int j, int k) {
   const int kc = imin(imax(k, 0), d.nz - 1), km = imax(k - 1, 0);
@@ -164,8 +211,8 @@ __global__ void k_tend_u(Dims d, Metric m, Flags fl, CS s, double* __restrict__ 
   {
     const double dz = dzeta(m, d, imin(k, nz - 1)) * scale_at(m, d, ip, j);
     const double uc = 0.5 * (SF(U, imax(i - 1, 0), j, k) + SF(U, ip, j, k));
-    const double ux = (SF(U, ip, j, k) - SF(U, imax(i - 1, 0), j, k)) / m.dx;
-    const double uy = (SF(U, ip, imin(j + 1, ny - 1), k) - SF(U, ip, imax(j - 1, 0), k)) / (2.0 * m.dy);
+    const double ux = DIVR(SF(U, ip, j, k) - SF(U, imax(i - 1, 0), j, k), m.dx, m.inv_dx);
+    const double uy = DIVR(SF(U, ip, imin(j + 1, ny - 1), k) - SF(U, ip, imax(j - 1, 0), k), 2.0 * m.dy, 0.5 * m.inv_dy);
     const double uz = (SF(U, ip, j, imin(k + 1, nz - 1)) - SF(U, ip, j, imax(k - 1, 0))) / (2.0 * dz);
     const double vc = 0.25 * (SF(V, imax(i - 1, 0), imax(j - 1, 0), k) + SF(V, ip, imax(j - 1, 0), k) +
                               SF(V, imax(i - 1, 0), j, k) + SF(V, ip, j, k));
@@ -180,7 +227,7 @@ __global__ void k_tend_u(Dims d, Metric m, Flags fl, CS s, double* __restrict__ 
   {
     const int im = imax(i - 1, 0);
     const double th = 0.5 * (SF(THETA, im, j, k) + SF(THETA, ip, j, k));
-    acc -= kCp * th * dpi(s, m, d, fl, ip, j, k, im, j, k) / m.dx;
+    acc -= DIVR(kCp * th * dpi(s, m, d, fl, ip, j, k, im, j, k), m.dx, m.inv_dx);
   }
   if (fl.split_fast) acc -= ac_u(s, m, d, fl, i, j, k);
   out[IDX(i, j, k)] = acc;
@@ -197,8 +244,8 @@ __global__ void k_tend_v(Dims d, Metric m, Flags fl, CS s, double* __restrict__ 
   {
     const double dz = dzeta(m, d, imin(k, nz - 1)) * scale_at(m, d, i, jp);
     const double vc = 0.5 * (SF(V, i, imax(j - 1, 0), k) + SF(V, i, jp, k));
-    const double vy = (SF(V, i, jp, k) - SF(V, i, imax(j - 1, 0), k)) / m.dy;
-    const double vx = (SF(V, imin(i + 1, nx - 1), jp, k) - SF(V, imax(i - 1, 0), jp, k)) / (2.0 * m.dx);
+    const double vy = DIVR(SF(V, i, jp, k) - SF(V, i, imax(j - 1, 0), k), m.dy, m.inv_dy);
+    const double vx = DIVR(SF(V, imin(i + 1, nx - 1), jp, k) - SF(V, imax(i - 1, 0), jp, k), 2.0 * m.dx, 0.5 * m.inv_dx);
     const double vz = (SF(V, i, jp, imin(k + 1, nz - 1)) - SF(V, i, jp, imax(k - 1, 0))) / (2.0 * dz);
     const double uc = 0.25 * (SF(U, imax(i - 1, 0), imax(j - 1, 0), k) + SF(U, i, imax(j - 1, 0), k) +
                               SF(U, imax(i - 1, 0), jp, k) + SF(U, i, jp, k));
@@ -213,7 +260,7 @@ __global__ void k_tend_v(Dims d, Metric m, Flags fl, CS s, double* __restrict__ 
   {
     const int jm = imax(j - 1, 0);
     const double th = 0.5 * (SF(THETA, i, jm, k) + SF(THETA, i, jp, k));
-    acc -= kCp * th * dpi(s, m, d, fl, i, jp, k, i, jm, k) / m.dy;
+    acc -= DIVR(kCp * th * dpi(s, m, d, fl, i, jp, k, i, jm, k), m.dy, m.inv_dy);
   }
   if (fl.split_fast) acc -= ac_v(s, m, d, fl, i, j, k);
   out[IDX(i, j, k)] = acc;
@@ -231,8 +278,10 @@ __global__ void k_tend_w(Dims d, Metric m, Flags fl, CS s, double* __restrict__ 
     const double dz = dzeta(m, d, kc) * scale_at(m, d, i, j);
     const double wc = 0.5 * (SF(W, i, j, kc) + SF(W, i, j, imin(k, nz)));
     const double wz = (SF(W, i, j, imin(k, nz)) - SF(W, i, j, imax(k - 1, 0))) / dz;
-    const double wx = (SF(W, imin(i + 1, nx - 1), j, imin(k, nz)) - SF(W, imax(i - 1, 0), j, imin(k, nz))) / (2.0 * m.dx);
-    const double wy = (SF(W, i, imin(j + 1, ny - 1), imin(k, nz)) - SF(W, i, imax(j - 1, 0), imin(k, nz))) / (2.0 * m.dy);
+    const double wx = DIVR(SF(W, imin(i + 1, nx - 1), j, imin(k, nz)) - SF(W, imax(i - 1, 0), j, imin(k, nz)), 2.0 * m.dx,
+                           0.5 * m.inv_dx);
+    const double wy = DIVR(SF(W, i, imin(j + 1, ny - 1), imin(k, nz)) - SF(W, i, imax(j - 1, 0), imin(k, nz)), 2.0 * m.dy,
+                           0.5 * m.inv_dy);
     const double uc = 0.5 * (SF(U, i, j, kc) + SF(U, i + 1, j, kc));
     const double vc = 0.5 * (SF(V, i, j, kc) + SF(V, i, j + 1, kc));
     acc -= uc * wx + vc * wy + wc * wz;
@@ -262,34 +311,60 @@ __device__ double adv_nc(const CS& s, const Metric& m, const Dims& d, const Flag
            wa * (CLP(q, i, j, k + 1) - CLP(q, i, j, k - 1)) * (0.5 / dz));
 }
 
-// Advection::scalar WENO5 branch, advection.cpp:144-187 (+ q div(u) when
-// weno_advective)
-__device__ double adv_weno(const CS& s, const Metric& m, const Dims& d, const Flags& fl, int q, int i, int j, int k) {
+// Advection::scalar WENO5 branch, advection.cpp:144-187, face fluxes.
+// Each cell's east flux and its east neighbour's west flux are the same
+// number: the clamped stencil of a face is the same seen from either side
+// (at i = nx the clamps make the east flux of cell nx-1 the stencil centred
+// on face nx). So every face flux is computed once, face f of a direction
+// from CL(f-3..f+1) and the normal wind at f:
+//   fx(f, j, k), f = 0..nx; fy(i, f, k), f = 0..ny; fz(i, j, f), f = 0..nz.
+__global__ void k_weno_faces(Dims d, CS s, int q, double* __restrict__ fx, double* __restrict__ fy,
+                             double* __restrict__ fz) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y;
+  const int k = blockIdx.z;
+  if (i > d.nx || j > d.ny || k > d.nz) return;
+  const size_t c = IDX(i, j, k);
+  if (j < d.ny && k < d.nz)
+    fx[c] = weno_face(CLP(q, i - 3, j, k), CLP(q, i - 2, j, k), CLP(q, i - 1, j, k), CLP(q, i, j, k),
+                      CLP(q, i + 1, j, k), SF(U, i, j, k));
+  if (i < d.nx && k < d.nz)
+    fy[c] = weno_face(CLP(q, i, j - 3, k), CLP(q, i, j - 2, k), CLP(q, i, j - 1, k), CLP(q, i, j, k),
+                      CLP(q, i, j + 1, k), SF(V, i, j, k));
+  if (i < d.nx && j < d.ny)
+    fz[c] = weno_face(CLP(q, i, j, k - 3), CLP(q, i, j, k - 2), CLP(q, i, j, k - 1), CLP(q, i, j, k),
+                      CLP(q, i, j, k + 1), SF(W, i, j, k));
+}
+
+// The cell tendency from the face fluxes (+ q div(u) when weno_advective),
+// with the positivity clip of the moisture species (equations.cpp:139-149).
+__global__ void k_weno_cells(Dims d, Metric m, Flags fl, CS s, int q, const double* __restrict__ fx,
+                             const double* __restrict__ fy, const double* __restrict__ fz, double* __restrict__ out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y;
+  const int k = blockIdx.z;
+  if (i >= d.nx || j >= d.ny || k >= d.nz) return;
+  const size_t c = IDX(i, j, k);
   const double dz = dzeta(m, d, k) * scale_at(m, d, i, j);
+  const double idz = 1.0 / dz;
   const double qc = SF(q, i, j, k);
-  const double fe = weno_face(CLP(q, i - 2, j, k), CLP(q, i - 1, j, k), qc, CLP(q, i + 1, j, k), CLP(q, i + 2, j, k),
-                              SF(U, i + 1, j, k));
-  const double fw = weno_face(CLP(q, i - 3, j, k), CLP(q, i - 2, j, k), CLP(q, i - 1, j, k), qc, CLP(q, i + 1, j, k),
-                              SF(U, i, j, k));
-  const double fn = weno_face(CLP(q, i, j - 2, k), CLP(q, i, j - 1, k), qc, CLP(q, i, j + 1, k), CLP(q, i, j + 2, k),
-                              SF(V, i, j + 1, k));
-  const double fs = weno_face(CLP(q, i, j - 3, k), CLP(q, i, j - 2, k), CLP(q, i, j - 1, k), qc, CLP(q, i, j + 1, k),
-                              SF(V, i, j, k));
+  const double fe = fx[IDX(i + 1, j, k)], fw = fx[c];
+  const double fn = fy[IDX(i, j + 1, k)], fs = fy[c];
   double ft = 0.0, fb = 0.0;
   const bool vert = (k + 2 < d.nz || k >= 2);
   if (vert) {
-    ft = weno_face(CLP(q, i, j, k - 2), CLP(q, i, j, k - 1), qc, CLP(q, i, j, k + 1), CLP(q, i, j, k + 2),
-                   SF(W, i, j, k + 1));
-    fb = weno_face(CLP(q, i, j, k - 3), CLP(q, i, j, k - 2), CLP(q, i, j, k - 1), qc, CLP(q, i, j, k + 1),
-                   SF(W, i, j, k));
+    ft = fz[IDX(i, j, k + 1)];
+    fb = fz[c];
   }
-  double r = -(fe - fw) / m.dx - (fn - fs) / m.dy - (ft - fb) / dz;
+  double r = DIVR(-(fe - fw), m.dx, m.inv_dx) - DIVR(fn - fs, m.dy, m.inv_dy) - DIVR(ft - fb, dz, idz);
   if (fl.weno_advective) {
-    double div = (SF(U, i + 1, j, k) - SF(U, i, j, k)) / m.dx + (SF(V, i, j + 1, k) - SF(V, i, j, k)) / m.dy;
-    if (vert) div += (SF(W, i, j, k + 1) - SF(W, i, j, k)) / dz;
+    double div = DIVR(SF(U, i + 1, j, k) - SF(U, i, j, k), m.dx, m.inv_dx) +
+                 DIVR(SF(V, i, j + 1, k) - SF(V, i, j, k), m.dy, m.inv_dy);
+    if (vert) div += DIVR(SF(W, i, j, k + 1) - SF(W, i, j, k), dz, idz);
     r += qc * div;
   }
-  return r;
+  if (q >= QV && qc <= 0.0 && r < 0.0) r = 0.0;
+  out[c] = r;
 }
 
 // Damping::tendencies laplacian, damping.cpp:48-53
@@ -328,7 +403,7 @@ __global__ void k_tend_cells(Dims d, Metric m, Flags fl, CS s, MS out, const dou
                       SF(V, i, j, k) * 0.5 * (SF(RHO, i, imax(j - 1, 0), k) + SF(RHO, i, j, k));
     const double fz = SF(W, i, j, k + 1) * 0.5 * (SF(RHO, i, j, k) + SF(RHO, i, j, imin(k + 1, nz - 1))) -
                       SF(W, i, j, k) * 0.5 * (SF(RHO, i, j, imax(k - 1, 0)) + SF(RHO, i, j, k));
-    double r = -(fx / m.dx + fy / m.dy + fz / dz);
+    double r = -(DIVR(fx, m.dx, m.inv_dx) + DIVR(fy, m.dy, m.inv_dy) + DIVR(fz, dz, 1.0 / dz));
     if (fl.split_fast) r -= mass_div0(s, m, d, i, j, k);
     out.f[RHO][c] = r;
   }
@@ -340,11 +415,13 @@ __global__ void k_tend_cells(Dims d, Metric m, Flags fl, CS s, MS out, const dou
     }
     out.f[PI][c] = r;
   }
+  // the advected scalars' tendencies; with WENO5 they come from
+  // k_weno_faces / k_weno_cells, launched after this kernel
   const int last = fl.moist ? QG : QV;
   for (int q = THETA; q <= QG; ++q) {
-    if (q == PI) continue;
+    if (q == PI || (fl.weno_scalars && q <= last)) continue;
     double r = 0.0;
-    if (q <= last) r = fl.weno_scalars ? adv_weno(s, m, d, fl, q, i, j, k) : adv_nc(s, m, d, fl, q, i, j, k);
+    if (q <= last) r = adv_nc(s, m, d, fl, q, i, j, k);
     if (q >= QV && SF(q, i, j, k) <= 0.0 && r < 0.0) r = 0.0;
     out.f[q][c] = r;
   }
@@ -481,6 +558,11 @@ __global__ void k_rhevi_mom(Dims d, Metric m, CS s, double* __restrict__ u, doub
 //     c_k = (dtau b)^2 kappa_k / dz_k, T_f = r_f cp t_f / dzf_f, x = new pi'
 //   w_new = w~ - dtau b cp t_f G(x), rho += dtau (Dh + (1-b) Dv(w) + b Dv(w_new))
 // One thread per column; horizontal momentum afterwards (k_uv_backward).
+// Scratch is level-major (row r, level k of column col at
+// ((r*(nz+1) + k)*ncol + col)), so a warp's 32 columns touch one contiguous
+// run per access: rows cp, dp, Dh, w~, w_new and, in the fast build, the
+// reciprocal spacings 1/dz of the column (dzf(k) = dzc(min(k, nz-1)), so one
+// row serves both).
 __global__ void k_chevi_column(Dims d, Metric m, Flags fl, CS s, double* __restrict__ w_out,
                                double* __restrict__ rho_out, double* __restrict__ pi_out,
                                double* __restrict__ scratch, double dtau, unsigned* err) {
@@ -490,72 +572,78 @@ __global__ void k_chevi_column(Dims d, Metric m, Flags fl, CS s, double* __restr
   const int nz = d.nz, nx = d.nx, ny = d.ny;
   const double b = fl.hevi_beta, ob = 1.0 - b;
   const int pert = fl.pgf_pert;
-  const size_t col = (size_t)j * nx + i;
-  // scratch per column: cp, dp, Dh, wt (nz+1), wn (nz+1)
-  double* cp = scratch + col * (5 * (size_t)nz + 2);
-  double* dp = cp + nz;
-  double* Dh = dp + nz;
-  double* wt = Dh + nz;
-  double* wn = wt + nz + 1;
+  const size_t ncol = (size_t)nx * ny, col = (size_t)j * nx + i;
+  auto S = [&](int r, int k) -> double& { return scratch[((size_t)r * (nz + 1) + k) * ncol + col]; };
+  enum { CP = 0, DP, DH, WT, WN, IDZ };
   const double sc = m.scale[col];
   auto rf = [&](int k) { return 0.5 * (R3(m.rho0, d, i, j, imax(k - 1, 0)) + R3(m.rho0, d, i, j, imin(k, nz - 1))); };
   auto tf = [&](int k) { return 0.5 * (R3(m.th0, d, i, j, imax(k - 1, 0)) + R3(m.th0, d, i, j, imin(k, nz - 1))); };
-  auto dzf = [&](int k) { return dmax(m.dzeta[imin(k, nz - 1)] * sc, 1.0); };
+  auto dzc = [&](int k) { return dmax(m.dzeta[k] * sc, 1.0); };
+  auto dzf = [&](int k) { return dzc(imin(k, nz - 1)); };
+#ifndef VGB_FP64_EXACT
+  for (int k = 0; k < nz; ++k) S(IDZ, k) = 1.0 / dzc(k);
+#endif
+  auto idzc = [&](int k) { return S(IDZ, k); };
+  auto idzf = [&](int k) { return S(IDZ, imin(k, nz - 1)); };
   auto pp = [&](int k) { return SF(PI, i, j, k) - (pert ? R3(m.pi0, d, i, j, k) : 0.0); };
   for (int k = 0; k <= nz; ++k) {
     double G = 0.0;
-    if (k > 0 && k < nz) G = (pp(k) - pp(k - 1)) / dzf(k);
-    wt[k] = SF(W, i, j, k) - dtau * ob * kCp * tf(k) * G;
+    if (k > 0 && k < nz) G = DIVR(pp(k) - pp(k - 1), dzf(k), idzf(k));
+    S(WT, k) = SF(W, i, j, k) - dtau * ob * kCp * tf(k) * G;
   }
   // forward elimination (Thomas, helmholtz.cpp:71-83 recurrence)
   double cprev = 0.0, dprev = 0.0;
   for (int k = 0; k < nz; ++k) {
-    const double dzc = dmax(m.dzeta[k] * sc, 1.0);
     const double r0 = R3(m.rho0, d, i, j, k);
     const double kap = (kRd / kCv) * (R3(m.pi0, d, i, j, k) / dmax(r0, 1e-8));
     const double fx = SF(U, i + 1, j, k) * 0.5 * (r0 + R3(m.rho0, d, imin(i + 1, nx - 1), j, k)) -
                       SF(U, i, j, k) * 0.5 * (R3(m.rho0, d, imax(i - 1, 0), j, k) + r0);
     const double fy = SF(V, i, j + 1, k) * 0.5 * (r0 + R3(m.rho0, d, i, imin(j + 1, ny - 1), k)) -
                       SF(V, i, j, k) * 0.5 * (R3(m.rho0, d, i, imax(j - 1, 0), k) + r0);
-    Dh[k] = -(fx / m.dx + fy / m.dy);
+    const double dh = -(DIVR(fx, m.dx, m.inv_dx) + DIVR(fy, m.dy, m.inv_dy));
+    S(DH, k) = dh;
     const double rk = rf(k), rk1 = rf(k + 1);
-    const double dv_old = -(rk1 * SF(W, i, j, k + 1) - rk * SF(W, i, j, k)) / dzc;
-    const double dv_t = -(rk1 * wt[k + 1] - rk * wt[k]) / dzc;
-    const double pstar = SF(PI, i, j, k) + dtau * kap * (Dh[k] + ob * dv_old + b * dv_t);
-    const double ck = (dtau * b) * (dtau * b) * kap / dzc;
-    const double Tk = (k == 0) ? 0.0 : rk * kCp * tf(k) / dzf(k);
-    const double Tk1 = (k + 1 == nz) ? 0.0 : rk1 * kCp * tf(k + 1) / dzf(k + 1);
+    const double dv_old = DIVR(-(rk1 * SF(W, i, j, k + 1) - rk * SF(W, i, j, k)), dzc(k), idzc(k));
+    const double dv_t = DIVR(-(rk1 * S(WT, k + 1) - rk * S(WT, k)), dzc(k), idzc(k));
+    const double pstar = SF(PI, i, j, k) + dtau * kap * (dh + ob * dv_old + b * dv_t);
+    const double ck = DIVR((dtau * b) * (dtau * b) * kap, dzc(k), idzc(k));
+    const double Tk = (k == 0) ? 0.0 : DIVR(rk * kCp * tf(k), dzf(k), idzf(k));
+    const double Tk1 = (k + 1 == nz) ? 0.0 : DIVR(rk1 * kCp * tf(k + 1), dzf(k + 1), idzf(k + 1));
     const double a = -ck * Tk, c = -ck * Tk1, bb = 1.0 + ck * (Tk + Tk1);
     const double rhs = pstar - (pert ? R3(m.pi0, d, i, j, k) : 0.0);
     const double denom = (k == 0) ? bb : bb - a * cprev;
     if (fabs(denom) < 1e-300) { atomicOr(err, (unsigned)kErrSingular); return; }
+#ifdef VGB_FP64_EXACT
     dprev = (k == 0) ? rhs / denom : (rhs - a * dprev) / denom;
     cprev = (k < nz - 1) ? c / denom : 0.0;
-    cp[k] = cprev;
-    dp[k] = dprev;
+#else
+    const double rden = 1.0 / denom;
+    dprev = (k == 0) ? rhs * rden : (rhs - a * dprev) * rden;
+    cprev = (k < nz - 1) ? c * rden : 0.0;
+#endif
+    S(CP, k) = cprev;
+    S(DP, k) = dprev;
   }
   // back substitution; x_k = pi'_new
-  double xk1 = dp[nz - 1];
-  dp[nz - 1] = xk1;
+  double xk1 = S(DP, nz - 1);
   for (int k = nz - 1; k-- > 0;) {
-    xk1 = dp[k] - cp[k] * xk1;
-    dp[k] = xk1;
+    xk1 = S(DP, k) - S(CP, k) * xk1;
+    S(DP, k) = xk1;
   }
   for (int k = 0; k <= nz; ++k) {
     double g = 0.0;
-    if (k > 0 && k < nz) g = (dp[k] - dp[k - 1]) / dzf(k);
-    wn[k] = wt[k] - dtau * b * kCp * tf(k) * g;
+    if (k > 0 && k < nz) g = DIVR(S(DP, k) - S(DP, k - 1), dzf(k), idzf(k));
+    S(WN, k) = S(WT, k) - dtau * b * kCp * tf(k) * g;
   }
   for (int k = 0; k < nz; ++k) {
-    const double dzc = dmax(m.dzeta[k] * sc, 1.0);
     const double rk = rf(k), rk1 = rf(k + 1);
-    const double dv_old = -(rk1 * SF(W, i, j, k + 1) - rk * SF(W, i, j, k)) / dzc;
-    const double dv_new = -(rk1 * wn[k + 1] - rk * wn[k]) / dzc;
+    const double dv_old = DIVR(-(rk1 * SF(W, i, j, k + 1) - rk * SF(W, i, j, k)), dzc(k), idzc(k));
+    const double dv_new = DIVR(-(rk1 * S(WN, k + 1) - rk * S(WN, k)), dzc(k), idzc(k));
     const size_t c = IDX(i, j, k);
-    rho_out[c] = SF(RHO, i, j, k) + dtau * (Dh[k] + ob * dv_old + b * dv_new);
-    pi_out[c] = dp[k] + (pert ? R3(m.pi0, d, i, j, k) : 0.0);
+    rho_out[c] = SF(RHO, i, j, k) + dtau * (S(DH, k) + ob * dv_old + b * dv_new);
+    pi_out[c] = S(DP, k) + (pert ? R3(m.pi0, d, i, j, k) : 0.0);
   }
-  for (int k = 0; k <= nz; ++k) w_out[IDX(i, j, k)] = wn[k];
+  for (int k = 0; k <= nz; ++k) w_out[IDX(i, j, k)] = S(WN, k);
 }
 
 __global__ void k_uv_backward(Dims d, Metric m, Flags fl, CS s, double* __restrict__ u, double* __restrict__ v,
@@ -874,7 +962,7 @@ static MS to_ms(double* const* f) {
 }
 
 void FP64_FN(fp64_slow_tendency)(const Dims& d, const Metric& m, const Flags& fl, double* const* st, double* const* tend,
-                        double* lap_scratch, cudaStream_t stream) {
+                        double* lap_scratch, double* face_scratch, cudaStream_t stream) {
   const CS s = to_cs(st);
   k_tend_u<<<grid3(d, d.nx + 1, d.ny, d.nz, kBlk), kBlk, 0, stream>>>(d, m, fl, s, tend[U]);
   k_tend_v<<<grid3(d, d.nx, d.ny + 1, d.nz, kBlk), kBlk, 0, stream>>>(d, m, fl, s, tend[V]);
@@ -885,6 +973,18 @@ void FP64_FN(fp64_slow_tendency)(const Dims& d, const Metric& m, const Flags& fl
     lapf = lap_scratch;
   }
   k_tend_cells<<<grid3(d, d.nx, d.ny, d.nz, kBlk), kBlk, 0, stream>>>(d, m, fl, s, to_ms(tend), lapf);
+  if (fl.weno_scalars) {
+    const size_t nf = d.plane * (size_t)(d.nz + 1);
+    double* fx = face_scratch;
+    double* fy = fx + nf;
+    double* fz = fy + nf;
+    const int last = fl.moist ? QG : QV;
+    for (int q = THETA; q <= last; ++q) {
+      if (q == PI) continue;
+      k_weno_faces<<<grid3(d, d.nx + 1, d.ny + 1, d.nz + 1, kBlk), kBlk, 0, stream>>>(d, s, q, fx, fy, fz);
+      k_weno_cells<<<grid3(d, d.nx, d.ny, d.nz, kBlk), kBlk, 0, stream>>>(d, m, fl, s, q, fx, fy, fz, tend[q]);
+    }
+  }
 }
 
 void FP64_FN(fp64_stage_update)(const Dims& d, double* const* s0, double* const* tend, double a, double* const* out,

@@ -8,7 +8,7 @@ namespace vgb {
 
 // ---- FP64 path (step_fp64.cu) ----
 void fp64_slow_tendency(const Dims& d, const Metric& m, const Flags& fl, double* const* st, double* const* tend,
-                        double* lap_scratch, cudaStream_t stream);
+                        double* lap_scratch, double* face_scratch, cudaStream_t stream);
 void fp64_stage_update(const Dims& d, double* const* s0, double* const* tend, double a, double* const* out,
                        cudaStream_t stream);
 void fp64_fb_substep(const Dims& d, const Metric& m, const Flags& fl, double* const* st, double dtau,
@@ -25,7 +25,7 @@ void fp64_nonfinite(const Dims& d, double* const* st, unsigned* err, cudaStream_
 
 // ---- bit-exact FP64 path (step_fp64.cu built with --fmad=false) ----
 void fp64_slow_tendency_exact(const Dims& d, const Metric& m, const Flags& fl, double* const* st, double* const* tend,
-                        double* lap_scratch, cudaStream_t stream);
+                        double* lap_scratch, double* face_scratch, cudaStream_t stream);
 void fp64_stage_update_exact(const Dims& d, double* const* s0, double* const* tend, double a, double* const* out,
                        cudaStream_t stream);
 void fp64_fb_substep_exact(const Dims& d, const Metric& m, const Flags& fl, double* const* st, double dtau,

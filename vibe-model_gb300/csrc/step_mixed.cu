@@ -99,12 +99,19 @@ __device__ __forceinline__ float gradc(float m3, float m2, float m1, float p1, f
 // mbarrier, while the current level computes. Elements outside a field's
 // index range arrive as zeros; blocks at the domain edge then overwrite them
 // with the reference's clamped values (clamp_at, field.hpp:91-96), so a tile
-// read at an unclamped offset returns the clamped value. Each thread keeps
-// its own column's vertical neighbours in registers: theta' and qv over
-// k-3..k+3 for the vertical WENO, whose flux through the top face of level k
-// is carried to level k+1 as its bottom flux (one WENO evaluation per
-// vertical face), and w, pi', rho' at k-1. Horizontal WENO fluxes are
-// computed once per face into shared memory.
+// read at an unclamped offset returns the clamped value. The level boxes
+// form a ring of three slots: while level k is computed, the boxes of level
+// k+1 are resident too (the u, v, w, rho' values one level up that the
+// vertical differences and the vertical mass flux need come from there) and
+// those of level k+2 are in flight. Each thread keeps its own column's
+// vertical neighbours in registers: theta' and qv over k-3..k+3 for the
+// vertical WENO, whose flux through the top face of level k is carried to
+// level k+1 as its bottom flux (one WENO evaluation per vertical face), and
+// u, v, w, pi', rho' at k-1. Horizontal WENO fluxes are computed once per
+// face into shared memory. When the stage's base state is its input (the
+// first stage) the base values are read from the boxes too.
+// kSpec: the composition the bench times (WENO5 scalars in advective form,
+// dry, no Coriolis, no divergence damping) compiled with those flags fixed.
 constexpr int TX = 32, TY = 8;
 constexpr int NT = TX * TY;
 constexpr int TW = 40;                   // box width (floats), all fields
@@ -220,14 +227,20 @@ __device__ void fix_box(float* t, int rows, int halo, int i0, int j0, int xmax, 
 
 // kRaw: also write the tendency R itself (the last stage: the finish kernel
 // forms the FP64 state from it)
-template <bool kRaw>
+constexpr int kStageRing = 3;  // level slots: k, k+1 resident, k+2 in flight
+
+template <bool kRaw, bool kSpec>
 __device__ __forceinline__ void stage_body(const Dims& d, const Tab& t, const Flags& fl, const StageMaps& M,
                                            const WS& win, const WS& w0, const WS& wout, const WS& rout, float dts,
                                            int kchunk, unsigned* err, int bx, int by, int bz) {
-  __shared__ __align__(128) float sbuf[2][kBuf];
+  __shared__ __align__(128) float sbuf[kStageRing][kBuf];
   __shared__ __align__(128) float sQm[R3 * TW];  // moisture species beyond qv (plain loads)
   __shared__ float sFx[2][TY * (TX + 1)], sFy[2][(TY + 1) * TX];  // theta' / qv (or one moisture species)
-  __shared__ __align__(8) unsigned long long sbar[2];
+  __shared__ __align__(8) unsigned long long sbar[kStageRing];
+  // the flags, fixed at compile time for the kSpec composition
+  const bool f_weno = kSpec || fl.weno_scalars, f_adv = kSpec || fl.weno_advective;
+  const bool f_moist = !kSpec && fl.moist, f_dd = !kSpec && fl.div_damp > 0.0;
+  const int f_cor = kSpec ? 0 : fl.coriolis;
   const int nx = d.nx, ny = d.ny, nz = d.nz, P = d.P;
   const size_t pl = d.plane;
   const int i0 = bx * TX, j0 = by * TY;
@@ -244,17 +257,43 @@ __device__ __forceinline__ void stage_body(const Dims& d, const Tab& t, const Fl
   const int jpv = imin(j, ny - 1) - j;  // jp - j on v faces (-1 at j = ny)
   const int djm = (j > 0) ? -1 : 0;     // jm - j
   const size_t colc = (size_t)imin(j, ny) * P + imin(i, nx);
-  const float* __restrict__ wcolp = win.f[W] + colc;
   const bool edge = (i0 - XO < 0) || (j0 - 3 < 0) || (i0 - XO + TW > nx - 1) || (j0 + TY + 3 > ny - 1);
+  // levels kb..ktop are read: every level of the chunk, and the one above
+  // its last cell level (capped at the top face nz); level L sits in slot
+  // (L - kb) % kStageRing, whose mbarrier phase is ((L - kb) / kStageRing) & 1
+  const int ktop = (klast < nz) ? klast + 1 : nz;
+  int hi = imin(kb + 1, ktop);  // highest level issued
   if (tid == 0) {
-    mbar_init(&sbar[0], 1);
-    mbar_init(&sbar[1], 1);
+    for (int sl = 0; sl < kStageRing; ++sl) mbar_init(&sbar[sl], 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-    issue_level(M, sbuf[0], &sbar[0], i0, j0, kb, nz);
+    for (int L = kb; L <= hi; ++L) issue_level(M, sbuf[L - kb], &sbar[L - kb], i0, j0, L, nz);
   }
+  // bounded wait for level L by one thread, released to the block by the
+  // barrier; on a timeout thread 0 drains every copy still in flight
+  auto level_ready = [&](int L) -> bool {
+    const int lev = L - kb;
+    const bool arrived =
+        (tid != 0) || mbar_wait_bounded(&sbar[lev % kStageRing], (unsigned)(lev / kStageRing) & 1u);
+    if (__syncthreads_or(!arrived)) {
+      if (tid == 0) {
+        atomicOr(err, (unsigned)kErrWaitTimeout);
+        for (int l = L; l <= hi; ++l)
+          mbar_wait_bounded(&sbar[(l - kb) % kStageRing], (unsigned)((l - kb) / kStageRing) & 1u);
+      }
+      return false;
+    }
+    return true;
+  };
+  // edge blocks: out-of-range box elements become the clamped ones
+  auto fix_level = [&](float* buf) {
+    fix_box(buf + tile_off(TT), R3, 3, i0, j0, M.xmax[TT], M.ymax[TT], tid);
+    fix_box(buf + tile_off(TQ), R3, 3, i0, j0, M.xmax[TQ], M.ymax[TQ], tid);
+    for (int b = TU; b < NTILE; ++b) fix_box(buf + tile_off(b), R1, 1, i0, j0, M.xmax[b], M.ymax[b], tid);
+    __syncthreads();
+  };
   // vertical registers of the own column
   float wT[7], wQ[7];
-  float wprev = 0.f, pprev = 0.f, rprev = 0.f;
+  float wprev = 0.f, pprev = 0.f, rprev = 0.f, uprev = 0.f, vprev = 0.f;
   if (cell) {
 #pragma unroll
     for (int m = 0; m < 7; ++m) {
@@ -267,43 +306,38 @@ __device__ __forceinline__ void stage_body(const Dims& d, const Tab& t, const Fl
     pprev = win.f[PI][o];
     rprev = win.f[RHO][o];
   }
+  // u, v of the level below the chunk at the own faces (k = 0: the level itself)
+  if (kb > 0 && in_box) {
+    const size_t o = (size_t)(kb - 1) * pl;
+    if (j < ny) uprev = win.f[U][o + (size_t)j * P + (i + ipu)];
+    if (i < nx) vprev = win.f[V][o + (size_t)(j + jpv) * P + i];
+  }
+  const bool has_base = w0.f[U] != nullptr;
+  const bool base_in = has_base && w0.f[U] == win.f[U];  // first stage: the base state is the input
   float fcT = 0.f, fcQ = 0.f;  // carried vertical WENO fluxes (top face of the level below)
   bool bad = false;
+  if (!level_ready(kb)) return;
+  if (edge) fix_level(sbuf[0]);
   for (int k = kb; k <= klast; ++k) {
-    const int lev = k - kb, cur = lev & 1;
+    const int lev = k - kb, cur = lev % kStageRing, nxt = (lev + 1) % kStageRing;
     const bool cells_here = k < nz;  // uniform across the block
     const int kc = imin(k, nz - 1);
-    __syncthreads();  // every thread is done with the other buffer (level k-1)
-    if (tid == 0 && k + 1 <= klast) issue_level(M, sbuf[cur ^ 1], &sbar[cur ^ 1], i0, j0, k + 1, nz);
-    // This level's global loads (the own columns' vertical neighbours and the
-    // base state the stage adds its tendency to), all issued before the wait
-    // for the boxes so that their latencies overlap it and one another.
+    __syncthreads();  // every thread is done with the slot of level k-1 (it takes level k+2)
+    if (tid == 0 && k + 2 <= ktop)
+      issue_level(M, sbuf[(lev + 2) % kStageRing], &sbar[(lev + 2) % kStageRing], i0, j0, k + 2, nz);
+    if (k + 2 <= ktop) hi = k + 2;
+    // This level's global loads (the base state the stage adds its tendency
+    // to, when it is not the input), issued before the wait for the next
+    // level's boxes so that their latencies overlap it and one another.
     const size_t c = (size_t)k * pl + colc;
-    const int kp1 = imin(k + 1, nz - 1), km = imax(k - 1, 0);
     const bool do_u = cells_here && in_box && j < ny, do_v = cells_here && in_box && i < nx;
-    const bool has_base = w0.f[U] != nullptr;
-    float gu_p = 0.f, gu_m = 0.f, gw_u = 0.f, gv_p = 0.f, gv_m = 0.f, gw_v = 0.f, g_wt = 0.f, g_rk = 0.f;
     float bU = 0.f, bV = 0.f, bW = 0.f, bR = 0.f, bP = 0.f, bT = 0.f, bQ = 0.f;
-    if (do_u) {
-      const float* __restrict__ ucol = win.f[U] + (size_t)j * P + (i + ipu);
-      gu_p = ucol[(size_t)kp1 * pl];
-      gu_m = ucol[(size_t)km * pl];
-      gw_u = win.f[W][(size_t)kp1 * pl + (size_t)j * P + (i + ipu)];
-      if (has_base) bU = w0.f[U][c];
-    }
-    if (do_v) {
-      const float* __restrict__ vcol = win.f[V] + (size_t)(j + jpv) * P + i;
-      gv_p = vcol[(size_t)kp1 * pl];
-      gv_m = vcol[(size_t)km * pl];
-      gw_v = win.f[W][(size_t)kp1 * pl + (size_t)(j + jpv) * P + i];
-      if (has_base) bV = w0.f[V][c];
-    }
-    if (cell) {
-      if (has_base) bW = w0.f[W][c];
-      if (cells_here) {
-        g_wt = wcolp[(size_t)(k + 1) * pl];
-        g_rk = win.f[RHO][(size_t)kp1 * pl + colc];
-        if (has_base) {
+    if (has_base && !base_in) {
+      if (do_u) bU = w0.f[U][c];
+      if (do_v) bV = w0.f[V][c];
+      if (cell) {
+        bW = w0.f[W][c];
+        if (cells_here) {
           bR = w0.f[RHO][c];
           bP = w0.f[PI][c];
           bT = w0.f[THETA][c];
@@ -311,18 +345,9 @@ __device__ __forceinline__ void stage_body(const Dims& d, const Tab& t, const Fl
         }
       }
     }
-    // one thread polls the level's mbarrier; the block barrier below then
-    // orders the boxes' contents for every thread (the others wait there
-    // without issuing)
-    const bool arrived = (tid != 0) || mbar_wait_bounded(&sbar[cur], (lev >> 1) & 1);
-    if (__syncthreads_or(!arrived)) {
-      // a box did not arrive: report, and leave none in flight before exiting
-      if (tid == 0) {
-        atomicOr(err, (unsigned)kErrWaitTimeout);
-        mbar_wait_bounded(&sbar[cur], (lev >> 1) & 1);
-        if (k + 1 <= klast) mbar_wait_bounded(&sbar[cur ^ 1], ((lev + 1) >> 1) & 1);
-      }
-      break;
+    if (k + 1 <= ktop) {
+      if (!level_ready(k + 1)) break;
+      if (edge) fix_level(sbuf[nxt]);
     }
     float* const buf = sbuf[cur];
     const float* const sT = buf + tile_off(TT);
@@ -332,11 +357,28 @@ __device__ __forceinline__ void stage_body(const Dims& d, const Tab& t, const Fl
     const float* const sW = buf + tile_off(TWF);
     const float* const sP = buf + tile_off(TP);
     const float* const sR = buf + tile_off(TR);
-    if (edge) {
-      fix_box(buf + tile_off(TT), R3, 3, i0, j0, M.xmax[TT], M.ymax[TT], tid);
-      fix_box(buf + tile_off(TQ), R3, 3, i0, j0, M.xmax[TQ], M.ymax[TQ], tid);
-      for (int b = TU; b < NTILE; ++b) fix_box(buf + tile_off(b), R1, 1, i0, j0, M.xmax[b], M.ymax[b], tid);
-      __syncthreads();
+    const float* const nb = sbuf[nxt];  // level k+1 (k < nz)
+    const float* const nU = nb + tile_off(TU);
+    const float* const nV = nb + tile_off(TV);
+    const float* const nW = nb + tile_off(TWF);
+    const float* const nR = nb + tile_off(TR);
+    // the level's vertical neighbours: u, v at kp1 = min(k+1, nz-1) and at
+    // km = max(k-1, 0), w at face kp1 beside the u / v faces, w at face k+1
+    // and rho' at kp1 in the own column
+    const float* const wkp1 = (k + 1 < nz) ? nW : sW;  // face kp1
+    const float gu_p = nU[o1 + ipu], gu_m = (k > 0) ? uprev : sU[o1 + ipu];
+    const float gw_u = wkp1[o1 + ipu];
+    const float gv_p = nV[o1 + jpv * TW], gv_m = (k > 0) ? vprev : sV[o1 + jpv * TW];
+    const float gw_v = wkp1[o1 + jpv * TW];
+    const float g_wt = nW[o1], g_rk = nR[o1];
+    if (base_in) {
+      bU = sU[o1];
+      bV = sV[o1];
+      bW = sW[o1];
+      bR = sR[o1];
+      bP = sP[o1];
+      bT = sT[o3];
+      bQ = sQ[o3];
     }
     // base value of q at this point: preloaded for the dynamic fields
     auto base_of = [&](int q) -> float {
@@ -366,7 +408,7 @@ __device__ __forceinline__ void stage_body(const Dims& d, const Tab& t, const Fl
       const float vc = 0.25f * (sV[o1 + dim - TW] + sV[o1 + ipu - TW] + sV[o1 + dim] + sV[o1 + ipu]);
       const float wc = 0.5f * (sW[o1 + ipu] + gw_u);
       float r = -(uc * ux + vc * uy + wc * uz);
-      if (fl.coriolis) r += (fl.coriolis == 2 ? t.f0 + t.beta * (((float)j + 0.5f) * t.dy - 0.5f * (float)ny * t.dy) : t.f0) * vc;
+      if (f_cor) r += (f_cor == 2 ? t.f0 + t.beta * (((float)j + 0.5f) * t.dy - 0.5f * (float)ny * t.dy) : t.f0) * vc;
       r -= cp * (0.5f * (sT[o3 + dim] + sT[o3 + ipu])) * (sP[o1 + ipu] - sP[o1 + dim]) * t.dx_inv;
       emit(U, r);
     }
@@ -380,7 +422,7 @@ __device__ __forceinline__ void stage_body(const Dims& d, const Tab& t, const Fl
       const float uc = 0.25f * (sU[o1 + dim + dm1] + sU[o1 + dm1] + sU[o1 + dim + dp1] + sU[o1 + dp1]);
       const float wc = 0.5f * (sW[o1 + dp1] + gw_v);
       float r = -(uc * vx + vc * vy + wc * vz);
-      if (fl.coriolis) r -= (fl.coriolis == 2 ? t.f0 + t.beta * (((float)j + 0.5f) * t.dy - 0.5f * (float)ny * t.dy) : t.f0) * uc;
+      if (f_cor) r -= (f_cor == 2 ? t.f0 + t.beta * (((float)j + 0.5f) * t.dy - 0.5f * (float)ny * t.dy) : t.f0) * uc;
       r -= cp * (0.5f * (sT[o3 + djm * TW] + sT[o3 + jpv * TW])) * (sP[o1 + dp1] - sP[o1 + dm1]) * t.dy_inv;
       emit(V, r);
     }
@@ -400,7 +442,7 @@ __device__ __forceinline__ void stage_body(const Dims& d, const Tab& t, const Fl
       const float pim = (k == 0) ? pic : pprev;
       r -= cp * (0.5f * (thm + thc)) * (pic - pim) * t.idzw[k];
       float qcond = 0.f, qvc = wQ[3];  // qv(kc)
-      if (fl.moist) {
+      if (f_moist) {
         const size_t ckc = (size_t)kc * pl + colc;
         qcond = win.f[QC][ckc] + win.f[QR][ckc] + win.f[QI][ckc] + win.f[QS][ckc] + win.f[QG][ckc];
       }
@@ -417,7 +459,7 @@ __device__ __forceinline__ void stage_body(const Dims& d, const Tab& t, const Fl
       const float fz = wt * 0.5f * (rc + rkp) - wk * 0.5f * (rprev + rc);
       emit(RHO, -(fx * t.dx_inv + fy * t.dy_inv + fz * t.idzc[k]));
       float r = 0.f;
-      if (fl.div_damp > 0.0) {
+      if (f_dd) {
         const float pc = sP[o1];
         const float lap = (sP[o1 + 1] - 2.f * pc + sP[o1 - 1]) * (t.dx_inv * t.dx_inv) +
                           (sP[o1 + TW] - 2.f * pc + sP[o1 - TW]) * (t.dy_inv * t.dy_inv);
@@ -463,7 +505,7 @@ __device__ __forceinline__ void stage_body(const Dims& d, const Tab& t, const Fl
                       float fc_shift) {
       float r = 0.f;
       const float qc = Q[o3];
-      if (fl.weno_scalars) {
+      if (f_weno) {
         if (cell) {
           const float ft = weno_face_f(z1, z2, qc, z4, z5, wt);
           const float fb = (fc != nullptr && k > kb) ? *fc + wk * fc_shift : weno_face_f(z0, z1, z2, qc, z4, wk);
@@ -476,7 +518,7 @@ __device__ __forceinline__ void stage_body(const Dims& d, const Tab& t, const Fl
             r -= (ft - fb) * idz;
             div += (wt - wk) * idz;
           }
-          if (fl.weno_advective) r += qc * div;
+          if (f_adv) r += qc * div;
           else if (q == THETA) r -= t.t0c[k] * div;
         }
       } else if (cell) {
@@ -497,19 +539,19 @@ __device__ __forceinline__ void stage_body(const Dims& d, const Tab& t, const Fl
     // is the flux of q plus w*s, so it is corrected by
     // w*(theta0(k-1) - theta0(k)) = -w*(theta0(k) - theta0(k-1)).
     const float tshift = (k > 0) ? -t.t0d[6 * (k - 1) + 4] : 0.f;
-    if (fl.weno_scalars) {
+    if (f_weno) {
       hflux(sT, 0);
       hflux(sQ, 1);
       __syncthreads();
     }
     scalar(THETA, sT, 0, wT[0] + sh[0], wT[1] + sh[1], wT[2] + sh[2], wT[4] + sh[4], wT[5] + sh[5], &fcT, tshift);
     scalar(QV, sQ, 1, wQ[0], wQ[1], wQ[2], wQ[4], wQ[5], &fcQ, 0.f);
-    if (fl.moist) {
+    if (f_moist) {
       for (int q = QC; q <= QG; ++q) {
         __syncthreads();  // sQm and the flux slots are no longer read
         load_box3(sQm, win.f[q] + (size_t)k * pl, P, i0, j0, nx - 1, ny - 1);
         __syncthreads();
-        if (fl.weno_scalars) {
+        if (f_weno) {
           hflux(sQm, 0);
           __syncthreads();
         }
@@ -535,18 +577,26 @@ __device__ __forceinline__ void stage_body(const Dims& d, const Tab& t, const Fl
       pprev = sP[o1];
       rprev = sR[o1];
     }
+    uprev = sU[o1 + ipu];
+    vprev = sV[o1 + jpv * TW];
   }
   if (bad) atomicOr(err, (unsigned)kErrNonFinite);
 }
 
-template <bool kRaw>
+template <bool kRaw, bool kSpec>
 __global__ void __launch_bounds__(NT, 4) k_mx_stage(const __grid_constant__ Dims d, const __grid_constant__ Tab t,
                                                     const __grid_constant__ Flags fl,
                                                     const __grid_constant__ StageMaps M,
                                                     const __grid_constant__ WS win, const __grid_constant__ WS w0,
                                                     const __grid_constant__ WS wout, const __grid_constant__ WS rout,
                                                     float dts, int kchunk, unsigned* err) {
-  stage_body<kRaw>(d, t, fl, M, win, w0, wout, rout, dts, kchunk, err, blockIdx.x, blockIdx.y, blockIdx.z);
+  stage_body<kRaw, kSpec>(d, t, fl, M, win, w0, wout, rout, dts, kchunk, err, blockIdx.x, blockIdx.y, blockIdx.z);
+}
+
+// the flag set kSpec compiles in: WENO5 scalars in advective form, dry, no
+// Coriolis, no divergence damping
+bool stage_spec(const Flags& fl) {
+  return fl.weno_scalars && fl.weno_advective && !fl.moist && fl.coriolis == 0 && !(fl.div_damp > 0.0);
 }
 
 // ---- explicit forward-backward substep in FP32 (runge_kutta.cpp:65-75) --
@@ -1083,9 +1133,9 @@ static int stage_kchunk(const Dims& d, bool fp64_out) {
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     if (fp64_out)
-      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_mx_stage<true>, NT, 0);
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_mx_stage<true, false>, NT, 0);
     else
-      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_mx_stage<false>, NT, 0);
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_mx_stage<false, false>, NT, 0);
     res = imax(1, sms * per_sm);
   }
   const long cols = (long)((d.nx + TX) / TX) * ((d.ny + TY) / TY);
@@ -1182,10 +1232,15 @@ int mixed_stage(const Dims& d, const Tab& t, const Flags& fl, const WS& win, con
   const bool raw = rout != nullptr;
   const int kchunk = stage_kchunk(d, raw);
   const dim3 g((d.nx + TX) / TX, (d.ny + TY) / TY, (d.nz + kchunk - 1) / kchunk);
-  if (raw)
-    k_mx_stage<true><<<g, b, 0, stream>>>(d, t, fl, M, win, w0, wout, *rout, (float)dt_stage, kchunk, err);
+  const bool spec = stage_spec(fl);
+  if (raw && spec)
+    k_mx_stage<true, true><<<g, b, 0, stream>>>(d, t, fl, M, win, w0, wout, *rout, (float)dt_stage, kchunk, err);
+  else if (raw)
+    k_mx_stage<true, false><<<g, b, 0, stream>>>(d, t, fl, M, win, w0, wout, *rout, (float)dt_stage, kchunk, err);
+  else if (spec)
+    k_mx_stage<false, true><<<g, b, 0, stream>>>(d, t, fl, M, win, w0, wout, wout, (float)dt_stage, kchunk, err);
   else
-    k_mx_stage<false><<<g, b, 0, stream>>>(d, t, fl, M, win, w0, wout, wout, (float)dt_stage, kchunk, err);
+    k_mx_stage<false, false><<<g, b, 0, stream>>>(d, t, fl, M, win, w0, wout, wout, (float)dt_stage, kchunk, err);
   return 0;
 }
 
@@ -2362,7 +2417,7 @@ __global__ void __launch_bounds__(NT, 4) k_b_stage(const StageArgs* __restrict__
   const int dom = find_domain(start, nd);
   const StageArgs& a = A[dom];
   const int l = (int)blockIdx.x - start[dom];
-  stage_body<kRaw>(a.d, a.t, a.fl, a.M, a.win, a.w0, a.wout, a.rout, a.dts, a.kchunk, err, l % a.gx,
+  stage_body<kRaw, false>(a.d, a.t, a.fl, a.M, a.win, a.w0, a.wout, a.rout, a.dts, a.kchunk, err, l % a.gx,
                    (l / a.gx) % a.gy, l / (a.gx * a.gy));
 }
 

@@ -53,6 +53,7 @@ struct Metric {
   const double* pi0;
   const double* rho0;
   double f0, beta;       // Coriolis (coriolis.cpp:25-41)
+  double inv_dx, inv_dy; // 1/dx, 1/dy (the fast FP64 build multiplies by them)
 };
 
 // Composition switches (same meaning as the setup struct in vibe_gb300.h).
