@@ -564,8 +564,8 @@ def main():
     ap.add_argument("--no-window", action="store_true", help="skip the TL/AD assimilation-window leg")
     ap.add_argument("--no-tune", action="store_true", help="skip the autotuner (built-in launch shapes)")
     ap.add_argument("--no-physics", action="store_true", help="skip the Kessler physics-coupling leg")
-    ap.add_argument("--only", choices=["all", "mixed", "physics", "nest"], default="all",
-                    help="mixed: time the mixed path only (no e2e, no FP64 leg); physics / nest: that leg only")
+    ap.add_argument("--only", choices=["all", "mixed", "fp64", "physics", "nest"], default="all",
+                    help="mixed / fp64: time that path only (no e2e, no other legs); physics / nest: that leg only")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -633,6 +633,20 @@ def main():
         m.sync()
         barrier()
         return e0.elapsed_time(e1), (k - 1) // RESTART
+
+    if args.only == "fp64":  # the plain FP64 path alone (profiling runs)
+        f64 = make(vg.FP64)
+        f64.step(DT, NSUB, 1)
+        ms_64, _ = timed_steps(f64, args.steps)
+        f64.set_kernel_timing(True)
+        ms_kt, _ = timed_steps(f64, 2)
+        ktimes = f64.kernel_times()
+        f64.close()
+        print(json.dumps({"only": "fp64", "cells": cells, "ms_per_step": ms_64 / args.steps,
+                          "value": world * cells * args.steps / (ms_64 * 1e-3), "kernel_ms": ktimes,
+                          "eager_ms_per_step": ms_kt / 2}))
+        ranks.close()
+        return
 
     # ---- mixed path (the headline) ----
     mx = make(vg.MIXED)
