@@ -199,9 +199,22 @@ vibe_stream_t vibe_gb300_nested_stream(vibe_gb300_nested *n);
  * steps with recomputation; window_stats reports the choice.
  * Both sweeps start from the model's current state and leave it there.
  * Perturbations: 12 FieldT host arrays (species order), halos pass through.
- * window_stats: device time of the last sweep, checkpoint and segment memory. */
+ * window_stats: device time of the last sweep, checkpoint and segment memory.
+ * t = NULL selects the tangent-linear and adjoint of the model's own step
+ * instead (vibe_gb300_step_tl / _ad below: the configured slow tendency, its
+ * acoustic substeps and the sponge, runge_kutta.cpp:77-119), linearised about
+ * the model's trajectory, one TL/AD step per model step (tl_substeps must be
+ * 1); its segments hold each step's three stage inputs, recomputed from the
+ * checkpoints.
+ * window_plan: the automatic choice of `every` (every = 0) as a pure
+ * function: store every step when n_steps + seg_states states fit in 80 % of
+ * free_bytes, else every = ceil(sqrt(n_steps / seg_states)) if the
+ * checkpoints and one segment (seg_states states per step) fit, else
+ * VIBE_GB300_EDEVICE. seg_states: 2 with a vibe_tlad object (double-buffered
+ * segments), 3 for the model's own step. */
 struct vibe_tlad;
 typedef struct vibe_gb300_window vibe_gb300_window;
+int vibe_gb300_window_plan(size_t free_bytes, size_t state_bytes, int n_steps, int seg_states, int *every);
 int vibe_gb300_window_create(vibe_gb300_model *m, struct vibe_tlad *t, double dt, int n_sub, int n_steps, int every,
                              int tl_substeps, vibe_gb300_window **out);
 void vibe_gb300_window_destroy(vibe_gb300_window *w);
@@ -209,6 +222,32 @@ int vibe_gb300_window_tl(vibe_gb300_window *w, const double *const *dx0, double 
 int vibe_gb300_window_ad(vibe_gb300_window *w, const double *const *dy, double *const *dx0_adjoint);
 int vibe_gb300_window_stats(const vibe_gb300_window *w, double *last_ms, size_t *checkpoint_bytes,
                             size_t *segment_bytes);
+
+/* Tangent-linear and adjoint of the model's own slow tendency and step,
+ * linearised about the model's current state (which they leave as it is);
+ * no counterpart in the reference, whose TL/AD (tangent_linear.cpp:295-603)
+ * is of a collocated step without acoustic substeps. The step is the one
+ * vibe_gb300_step takes (runge_kutta.cpp:77-119 with the configured
+ * composition): x1 = A^n (x0 + dt/3 R(x0)), x2 = A^n (x0 + dt/2 R(x1)),
+ * x3 = A^n (x0 + dt R(x2)), then the sponge and the rigid ground/lid; R the
+ * slow tendency (Equations::tendencies, equations.cpp:60-150, with the WENO5
+ * or central scalar scheme), A one acoustic substep (explicit or consistent
+ * HEVI). The TL of R differentiates the WENO5 weights and the
+ * Lax-Friedrichs switch exactly (the positivity clip contributes zero where
+ * it holds); the adjoint is its exact transpose. FP64 models compute in FP64;
+ * mixed models in FP32 (the slow tendency's TL/AD and the model's own FP32
+ * substeps and their adjoints), with FP64 storage.
+ * Arrays: 12 FieldT host arrays (species order). tendency_tl writes the
+ * tendency's staggered boxes (zero elsewhere); tendency_ad takes the bar of
+ * those boxes and returns the bar of every input point (the boxes with the
+ * ghost column and row); step_tl / step_ad keep the points no step writes
+ * from their input. Not supported (VIBE_GB300_EUNSUPPORTED): a physics
+ * package, acoustic_mode 1 (the reference HEVI), fourth-order divergence
+ * damping. */
+int vibe_gb300_tendency_tl(vibe_gb300_model *m, const double *const *dx, double *const *out);
+int vibe_gb300_tendency_ad(vibe_gb300_model *m, const double *const *bar_r, double *const *bar_x);
+int vibe_gb300_step_tl(vibe_gb300_model *m, double dt, int n_sub, const double *const *dx, double *const *out);
+int vibe_gb300_step_ad(vibe_gb300_model *m, double dt, int n_sub, const double *const *dy, double *const *out);
 
 /* Kernel-level entry points (FP64 path only for the tendency). */
 int vibe_gb300_slow_tendency(vibe_gb300_model *m, double *const *host_out);

@@ -28,6 +28,7 @@ SOURCES = [("step_fp64.cu", "step_fp64.o", []),
            ("si_step.cu", "si_step.o", ["--fmad=false"]),
            ("nest.cu", "nest.o", ["--fmad=false"]),
            ("tlad.cu", "tlad.o", []),
+           ("step_tlad.cu", "step_tlad.o", []),
            ("advect_tlad.cu", "advect_tlad.o", []),
            ("physics.cu", "physics.o", ["--fmad=false"]),
            ("diag.cu", "diag.o", ["--fmad=false"])]

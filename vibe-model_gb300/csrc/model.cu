@@ -88,6 +88,15 @@ struct vibe_gb300_model {
   double* lin_tmp[3] = {};         // HEVI TL: the column solve's w, rho, pi outputs
   double* lin_scr = nullptr;       // HEVI TL/AD: per-column work
   double* lin_dh = nullptr;        // HEVI AD: bar of the horizontal divergence
+  // TL/AD of the model's own step (allocated on first use): six perturbation
+  // states of 12 fields, the WENO face fluxes (6 fields), one cell field and
+  // a zero field (the reference of the sponge's linear part)
+  double* stl[6][NSPECIES] = {};
+  double* stl_face = nullptr;
+  double* stl_cell = nullptr;
+  double* stl_zero = nullptr;
+  // while set, a step copies its second and third stages' input states here
+  double* const* rec_stage[2] = {nullptr, nullptr};
   // physics package (vibe_gb300_set_physics) and its tendency accumulators
   vibe_gb300_physics_fn phys_fn = nullptr;
   void* phys_user = nullptr;
@@ -364,6 +373,17 @@ __global__ void k_rigid_w(Dims d, double* __restrict__ w) {
   if (i >= d.nx || j >= d.ny) return;
   w[d.idx(i, j, 0)] = 0.0;
   w[d.idx(i, j, d.nz)] = 0.0;
+}
+
+// zero every point of a field outside the box i < ni, j < nj, k < nk
+__global__ void k_keep_box(Dims d, int ni, int nj, int nk, double* __restrict__ f) {
+  const size_t n = d.plane * (size_t)(d.nz + 1);
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x) {
+    const int k = (int)(e / d.plane);
+    const size_t r = e - (size_t)k * d.plane;
+    const int j = (int)(r / d.P), i = (int)(r - (size_t)j * d.P);
+    if (i >= ni || j >= nj || k >= nk) f[e] = 0.0;
+  }
 }
 
 void box_of(const vibe_gb300_model* m, int q, int& ni, int& nj, int& nk) {
@@ -691,6 +711,10 @@ int enqueue_one_step(vibe_gb300_model* m, double dt, int n_sub) {
         }
         Span sp(m, 2);
         m->f64->nonfinite(d, S1, m->d_err, m->stream);
+        if (stage < 2 && m->rec_stage[stage])
+          for (int q = 0; q < NSPECIES; ++q)
+            CUDA_OK(cudaMemcpyAsync(m->rec_stage[stage][q], S1[q], d.plane * (size_t)(d.nz + 1) * sizeof(double),
+                                    cudaMemcpyDeviceToDevice, m->stream));
       }
       Span sp(m, 2);
       m->f64->sponge(d, m->met, S1, m->kmin, dt, m->stream);
@@ -746,6 +770,17 @@ int enqueue_one_step(vibe_gb300_model* m, double dt, int n_sub) {
         }
         final_sub = in;
         last_dtau = dtau;
+        if (stage < 2 && m->rec_stage[stage]) {
+          // the next stage's input as FP64 totals; what the working copy does
+          // not hold (inactive species, points off the boxes) from the step's start
+          for (int q = 0; q < NSPECIES; ++q)
+            CUDA_OK(cudaMemcpyAsync(m->rec_stage[stage][q], S0[q], d.plane * (size_t)(d.nz + 1) * sizeof(double),
+                                    cudaMemcpyDeviceToDevice, m->stream));
+          WS next = ws_compose(in, m->WSt[stage & 1]);
+          if (!m->fl.moist)
+            for (int q = QV + 1; q < NSPECIES; ++q) next.f[q] = nullptr;
+          working_to_f64(d, m->tab, next, m->rec_stage[stage], m->stream);
+        }
       }
       Span sp(m, 2);
       const WS wr = ws_of(m->WR);
@@ -2361,38 +2396,258 @@ int window_end(vibe_gb300_window* w, cudaStream_t ts) {
   float ms = 0.f;
   CUDA_OK(cudaEventElapsedTime(&ms, w->e0, w->e1));
   w->last_ms = ms;
-  vgb::tlad_use_base(w->t, nullptr);
+  if (w->t) vgb::tlad_use_base(w->t, nullptr);
+  return 0;
+}
+
+// ---- tangent-linear and adjoint of the model's own step ----------------------
+// The step (runge_kutta.cpp:77-119 as this model composes it) is
+//   x1 = A^n (x0 + dt/3 R(x0)),  x2 = A^n (x0 + dt/2 R(x1)),
+//   x3 = A^n (x0 + dt R(x2)),     x_new = rigid(sponge(x3)),
+// R the slow tendency, A one acoustic substep of the stage's dtau. A is
+// affine in the state (its linear part is the substep applied to a
+// perturbation with the gradient of pi itself), the sponge is affine (its
+// linear part: the sponge toward a zero reference) and the rigid ground/lid
+// is linear. The TL of a step needs the step's three stage inputs x0, x1,
+// x2, which a step records when rec_stage is set. FP64 models: FP64 TL/AD;
+// mixed models: the slow tendency's TL/AD in FP32 arithmetic and the model's
+// own FP32 substep and its adjoint (perturbations stored in FP64).
+int stl_supported(const vibe_gb300_model* m) {
+  if (m->phys_fn) return fail(VIBE_GB300_EUNSUPPORTED, "the step's TL/AD has no physics package");
+  if (m->fl.acoustic_mode == 1)
+    return fail(VIBE_GB300_EUNSUPPORTED, "the reference HEVI substep (acoustic_mode 1) has no adjoint here");
+  if (m->fl.div_damp > 0.0 && m->fl.div_order > 2)
+    return fail(VIBE_GB300_EUNSUPPORTED, "fourth-order divergence damping has no TL/AD here");
+  return 0;
+}
+
+int stl_ensure(vibe_gb300_model* m) {
+  if (m->stl_zero) return 0;
+  const size_t n = state_count(m);
+  for (auto& st : m->stl)
+    for (int q = 0; q < NSPECIES; ++q)
+      if (int rc = dalloc(m, &st[q], n)) return rc;
+  if (int rc = dalloc(m, &m->stl_face, 6 * n)) return rc;
+  if (int rc = dalloc(m, &m->stl_cell, n)) return rc;
+  if (m->precision == VIBE_GB300_FP64) {
+    if (!m->lin_scr) {  // as the substep TL/AD entry points allocate them
+      for (int f = 0; f < 3; ++f)
+        if (int rc = dalloc(m, &m->lin_tmp[f], n)) return rc;
+      if (int rc = dalloc(m, &m->lin_dh, n)) return rc;
+      if (int rc = dalloc(m, &m->lin_scr, (size_t)m->d.nx * m->d.ny * (6 * (size_t)m->d.nz + 6))) return rc;
+    }
+  } else {
+    if (!m->lin32[0][0])
+      for (int b = 0; b < 2; ++b)
+        for (int f = 0; f < 5; ++f)
+          if (int rc = dalloc(m, &m->lin32[b][f], n)) return rc;
+    if (!m->lin32_dh) {
+      if (int rc = dalloc(m, &m->lin32_dh, n)) return rc;
+      if (int rc = dalloc(m, &m->lin32_scr, (size_t)m->d.nx * m->d.ny * (4 * (size_t)m->d.nz + 2))) return rc;
+    }
+  }
+  return dalloc(m, &m->stl_zero, n);  // last: it marks the set as allocated
+}
+
+// n_sub substeps of stage `stage` (or their adjoint) on the acoustic fields of x
+int stl_substeps(vibe_gb300_model* m, int stage, double dtau, int n_sub, double* const* x, bool adjoint) {
+  const Dims& d = m->d;
+  const bool hevi = m->fl.acoustic_mode == 2;
+  if (m->precision == VIBE_GB300_FP64) {
+    Flags lf = m->fl;
+    lf.pgf_pert = 0;  // the linear part: the gradient of the perturbation of pi
+    double* tmp[NSPECIES] = {};
+    tmp[W] = m->lin_tmp[0];
+    tmp[RHO] = m->lin_tmp[1];
+    tmp[PI] = m->lin_tmp[2];
+    for (int n = 0; n < n_sub; ++n) {
+      if (adjoint) {
+        if (hevi) m->f64->hevi_substep_ad(d, m->met, lf, x, m->lin_dh, m->lin_scr, dtau, m->d_err, m->stream);
+        else m->f64->fb_substep_ad(d, m->met, x, dtau, m->stream);
+      } else {
+        if (hevi) m->f64->cons_hevi_substep(d, m->met, lf, x, tmp, m->lin_scr, dtau, m->d_err, m->stream);
+        else m->f64->fb_substep(d, m->met, lf, x, dtau, m->stream);
+      }
+    }
+    CUDA_OK(cudaGetLastError());
+    return 0;
+  }
+  const size_t n = state_count(m);
+  for (int f = 0; f < 5; ++f) {
+    lin_to_f32(n, x[kLinField[f]], m->lin32[0][f], m->stream);
+    CUDA_OK(cudaMemcpyAsync(m->lin32[1][f], m->lin32[0][f], n * sizeof(float), cudaMemcpyDeviceToDevice, m->stream));
+  }
+  auto ws_lin = [&](int b) {
+    WS w;
+    for (int q = 0; q < NSPECIES; ++q) w.f[q] = nullptr;
+    for (int f = 0; f < 5; ++f) w.f[kLinField[f]] = m->lin32[b][f];
+    return w;
+  };
+  const float* lu = m->d_lu + (size_t)stage * 3 * d.nz;
+  int cur = 0;
+  for (int k = 0; k < n_sub; ++k) {
+    if (hevi) {
+      if (adjoint) {
+        mixed_hevi_substep_ad(d, m->tab, m->fl, ws_lin(0), lu, m->lin32_dh, m->lin32_scr, (float)dtau, m->stream);
+      } else {
+        if (mixed_hevi_substep(d, m->tab, m->fl, ws_lin(cur), ws_lin(1 - cur), (float)dtau, lu, m->d_err, m->stream))
+          return fail(VIBE_GB300_EDEVICE, "TMA descriptor creation failed (cuTensorMapEncodeTiled)");
+        cur = 1 - cur;
+      }
+    } else if (adjoint) {
+      mixed_fb_substep_ad(d, m->tab, ws_lin(0), (float)dtau, m->stream);
+    } else {
+      mixed_fb_substep(d, m->tab, m->fl, ws_lin(cur), ws_lin(1 - cur), (float)dtau, m->stream);
+      cur = 1 - cur;
+    }
+  }
+  for (int f = 0; f < 5; ++f) lin_to_f64(n, m->lin32[cur][f], x[kLinField[f]], m->stream);
+  CUDA_OK(cudaGetLastError());
+  return 0;
+}
+
+// the linear parts of the sponge and of the rigid ground and lid (both
+// diagonal, so each is its own adjoint)
+int stl_sponge_rigid(vibe_gb300_model* m, double dt, double* const* x) {
+  Metric mz = m->met;
+  mz.th0 = mz.pi0 = mz.rho0 = m->stl_zero;
+  m->f64->sponge(m->d, mz, x, m->kmin, dt, m->stream);
+  if (m->fl.w_rigid)
+    k_rigid_w<<<dim3((m->d.nx + 31) / 32, (m->d.ny + 7) / 8), dim3(32, 8), 0, m->stream>>>(m->d, x[W]);
+  CUDA_OK(cudaGetLastError());
+  return 0;
+}
+
+// x: the perturbation of the step's input in, of its output out;
+// base[s]: the input state of stage s of the trajectory step
+int stl_step_tl(vibe_gb300_model* m, double dt, int n_sub, double* const* const* base, double* const* x) {
+  const size_t n = state_count(m);
+  const bool f32 = m->precision == VIBE_GB300_MIXED;
+  double* const* x0 = m->stl[0];
+  double* const* r = m->stl[2];
+  if (int rc = copy_state(m, x0, x)) return rc;
+  const double dts[3] = {dt / 3.0, dt / 2.0, dt};
+  for (int st = 0; st < 3; ++st) {
+    tend_tl(m->d, m->met, m->fl, base[st], st == 0 ? x0 : x, r, m->stl_face, f32, m->stream);
+    for (int q = 0; q < NSPECIES; ++q) lin_axpy(n, x0[q], r[q], dts[st], x[q], m->stream);
+    if (int rc = stl_substeps(m, st, dts[st] / n_sub, n_sub, x, false)) return rc;
+  }
+  return stl_sponge_rigid(m, dt, x);
+}
+
+// x: the bar of the step's output in, of its input out
+int stl_step_ad(vibe_gb300_model* m, double dt, int n_sub, double* const* const* base, double* const* x) {
+  const size_t n = state_count(m);
+  const bool f32 = m->precision == VIBE_GB300_MIXED;
+  double* const* acc = m->stl[0];
+  double* const* r = m->stl[2];
+  double* const* prev = m->stl[5];
+  if (int rc = stl_sponge_rigid(m, dt, x)) return rc;
+  for (int q = 0; q < NSPECIES; ++q) CUDA_OK(cudaMemsetAsync(acc[q], 0, n * sizeof(double), m->stream));
+  const double dts[3] = {dt / 3.0, dt / 2.0, dt};
+  for (int st = 2; st >= 0; --st) {
+    if (int rc = stl_substeps(m, st, dts[st] / n_sub, n_sub, x, true)) return rc;
+    for (int q = 0; q < NSPECIES; ++q) {
+      lin_scale_add(n, x[q], 1.0, acc[q], m->stream);           // through x0 directly
+      lin_axpy(n, m->stl_zero, x[q], dts[st], r[q], m->stream);  // bar of R = dt_stage * bar
+      CUDA_OK(cudaMemsetAsync(prev[q], 0, n * sizeof(double), m->stream));
+    }
+    tend_ad(m->d, m->met, m->fl, base[st], r, prev, m->stl_face, m->stl_cell, f32, m->stream);
+    if (st == 0) {
+      for (int q = 0; q < NSPECIES; ++q) lin_scale_add(n, prev[q], 1.0, acc[q], m->stream);
+    } else if (int rc = copy_state(m, x, prev)) {
+      return rc;
+    }
+  }
+  return copy_state(m, x, acc);
+}
+
+// one step from the model's current state that records its stage inputs;
+// base[0] is the step's input (the model's buffer, intact until the next step)
+int stl_record_step(vibe_gb300_model* m, double dt, int n_sub, double* const* rec1, double* const* rec2,
+                    double* const** base) {
+  base[0] = m->S[m->cur];
+  base[1] = rec1;
+  base[2] = rec2;
+  m->rec_stage[0] = rec1;
+  m->rec_stage[1] = rec2;
+  const int rc = enqueue_one_step(m, dt, n_sub);
+  m->rec_stage[0] = m->rec_stage[1] = nullptr;
+  return rc;
+}
+
+// 12 FieldT host arrays -> device perturbation fields (zero off the boxes)
+int stl_upload(vibe_gb300_model* m, const double* const* host, double* const* dev) {
+  for (int q = 0; q < NSPECIES; ++q) {
+    if (!host[q]) return fail(VIBE_GB300_EBADARG, "bad argument");
+    CUDA_OK(cudaMemsetAsync(dev[q], 0, state_count(m) * sizeof(double), m->stream));
+    if (int rc = upload_storage(m, q, host[q], &dev[q], 1)) return rc;
+  }
+  return 0;
+}
+// device -> FieldT: the boxes from dev, every other point from keep
+int stl_download(vibe_gb300_model* m, double* const* dev, const double* const* keep, double* const* host) {
+  const dim3 b(32, 4);
+  for (int q = 0; q < NSPECIES; ++q) {
+    if (!host[q]) return fail(VIBE_GB300_EBADARG, "bad argument");
+    int ni, nj, nk;
+    box_of(m, q, ni, nj, nk);
+    const size_t n = storage_count(m, q);
+    CUDA_OK(cudaMemcpyAsync(m->d_stage_in, keep[q], n * sizeof(double), cudaMemcpyHostToDevice, m->stream));
+    k_scatter<<<dim3((ni + 31) / 32, (nj + 3) / 4, nk), b, 0, m->stream>>>(m->d, m->nsx[q], m->nsy[q], ni, nj, nk,
+                                                                            dev[q], m->d_stage_in);
+    CUDA_OK(cudaGetLastError());
+    CUDA_OK(cudaMemcpyAsync(host[q], m->d_stage_in, n * sizeof(double), cudaMemcpyDeviceToHost, m->stream));
+    CUDA_OK(cudaStreamSynchronize(m->stream));
+  }
   return 0;
 }
 }  // namespace
 
 extern "C" {
 
+int vibe_gb300_window_plan(size_t free_bytes, size_t state_bytes, int n_steps, int seg_states, int* every) {
+  if (!every || n_steps < 1 || seg_states < 1 || state_bytes == 0) return fail(VIBE_GB300_EBADARG, "bad argument");
+  // store every step when n_steps checkpoints and a one-step segment fit in
+  // 80 % of the free device memory; otherwise checkpoint every
+  // ceil(sqrt(n_steps / seg_states)) steps, which minimises checkpoints +
+  // segment states, and recompute each segment from its checkpoint
+  const double st = (double)state_bytes, budget = 0.8 * (double)free_bytes;
+  if ((n_steps + (double)seg_states) * st <= budget) {
+    *every = 1;
+    return 0;
+  }
+  const int e = std::max(1, (int)std::ceil(std::sqrt((double)n_steps / seg_states)));
+  const int nck = (n_steps + e - 1) / e;
+  if ((nck + (double)seg_states * e) * st > budget)
+    return fail(VIBE_GB300_EDEVICE, "the window's checkpoints do not fit in device memory");
+  *every = e;
+  return 0;
+}
+
 int vibe_gb300_window_create(vibe_gb300_model* m, vibe_tlad* t, double dt, int n_sub, int n_steps, int every,
                              int tl_substeps, vibe_gb300_window** out) {
-  if (!m || !t || !out || !(dt > 0.0) || n_steps < 1 || every < 0 || tl_substeps < 1)
+  if (!m || !out || !(dt > 0.0) || n_steps < 1 || every < 0 || tl_substeps < 1)
     return fail(VIBE_GB300_EBADARG, "bad argument");
-  int nx, ny, nz;
-  vgb::tlad_grid(t, &nx, &ny, &nz);
-  if (nx != m->d.nx || ny != m->d.ny || nz != m->d.nz)
-    return fail(VIBE_GB300_EBADARG, "the TL/AD grid differs from the model's");
+  // t == NULL: the TL/AD of the model's own step; a segment then holds three
+  // states per step (its input and its second and third stages' inputs)
+  const bool own = (t == nullptr);
+  if (own) {
+    if (tl_substeps != 1) return fail(VIBE_GB300_EBADARG, "the model's own step TL/AD takes tl_substeps = 1");
+    if (int rc = stl_supported(m)) return rc;
+    if (int rc = stl_ensure(m)) return rc;
+  } else {
+    int nx, ny, nz;
+    vgb::tlad_grid(t, &nx, &ny, &nz);
+    if (nx != m->d.nx || ny != m->d.ny || nz != m->d.nz)
+      return fail(VIBE_GB300_EBADARG, "the TL/AD grid differs from the model's");
+  }
+  const int seg_states = own ? 3 : 2;
   if (every == 0) {
-    // automatic: store every step when the whole trajectory (n_steps
-    // checkpoints and a two-state segment) fits in 80 % of the free device
-    // memory; otherwise checkpoint every ceil(sqrt(n_steps / 2)) steps, which
-    // minimises checkpoints + double-buffered segment, and recompute
     size_t free_b = 0, total_b = 0;
     CUDA_OK(cudaMemGetInfo(&free_b, &total_b));
-    const double state_b = (double)state_count(m) * sizeof(double) * NSPECIES;
-    const double budget = 0.8 * (double)free_b;
-    if ((n_steps + 2.0) * state_b <= budget) {
-      every = 1;
-    } else {
-      every = std::max(1, (int)std::ceil(std::sqrt(n_steps / 2.0)));
-      const int nck = (n_steps + every - 1) / every;
-      if ((nck + 2.0 * every) * state_b > budget)
-        return fail(VIBE_GB300_EDEVICE, "the window's checkpoints do not fit in device memory");
-    }
+    const size_t state_b = state_count(m) * sizeof(double) * NSPECIES;
+    if (int rc = vibe_gb300_window_plan(free_b, state_b, n_steps, seg_states, &every)) return rc;
   }
   auto* w = new vibe_gb300_window();
   w->m = m;
@@ -2418,9 +2673,14 @@ int vibe_gb300_window_create(vibe_gb300_model* m, vibe_tlad* t, double dt, int n
   };
   w->ckpt.resize(nck);
   for (auto& a : w->ckpt) alloc_state(a);
-  for (int b = 0; b < 2; ++b) {
-    w->seg[b].resize(seg_len);
-    for (auto& a : w->seg[b]) alloc_state(a);
+  if (own) {
+    w->seg[0].resize(3 * (size_t)seg_len);
+    for (auto& a : w->seg[0]) alloc_state(a);
+  } else {
+    for (int b = 0; b < 2; ++b) {
+      w->seg[b].resize(seg_len);
+      for (auto& a : w->seg[b]) alloc_state(a);
+    }
   }
   if (!rc && (cudaEventCreateWithFlags(&w->ev_model, cudaEventDisableTiming) != cudaSuccess ||
               cudaEventCreateWithFlags(&w->ev_seg[0], cudaEventDisableTiming) != cudaSuccess ||
@@ -2445,8 +2705,92 @@ void vibe_gb300_window_destroy(vibe_gb300_window* w) {
   delete w;
 }
 
+}  // extern "C"
+
+namespace {
+// the model's own step TL/AD over the window (t == NULL), on the model stream
+int own_window_tl(vibe_gb300_window* w, const double* const* dx0, double* const* dx_out) {
+  vibe_gb300_model* m = w->m;
+  const int n_sub = std::max(w->n_sub, 1);
+  if (int rc = configure_dt(m, w->dt, n_sub)) return rc;
+  if (int rc = stl_upload(m, dx0, m->stl[1])) return rc;
+  if (int rc = window_begin(w)) return rc;
+  for (int n = 0; n < w->n_steps; ++n) {
+    if (n % w->every == 0)
+      if (int rc = window_checkpoint(w, n / w->every)) return rc;
+    double* const* base[3];
+    if (int rc = stl_record_step(m, w->dt, n_sub, m->stl[3], m->stl[4], base)) return rc;
+    if (int rc = stl_step_tl(m, w->dt, n_sub, base, m->stl[1])) return rc;
+  }
+  if (int rc = window_end(w, m->stream)) return rc;
+  if (int rc = stl_download(m, m->stl[1], dx0, dx_out)) return rc;
+  if (int rc = read_status(m)) return rc;
+  if (int rc = window_restart(w, 0)) return rc;
+  return read_status(m);
+}
+
+int own_window_ad(vibe_gb300_window* w, const double* const* dy, double* const* dx0_adjoint) {
+  vibe_gb300_model* m = w->m;
+  const int n_sub = std::max(w->n_sub, 1);
+  if (int rc = configure_dt(m, w->dt, n_sub)) return rc;
+  if (int rc = stl_upload(m, dy, m->stl[1])) return rc;
+  if (int rc = window_begin(w)) return rc;
+  const int nck = (int)w->ckpt.size();
+  const int last_ck = (nck - 1) * w->every;
+  for (int n = 0; n <= last_ck; ++n) {  // forward sweep: checkpoints only
+    if (n % w->every == 0)
+      if (int rc = window_checkpoint(w, n / w->every)) return rc;
+    if (n < last_ck)
+      if (int rc = enqueue_one_step(m, w->dt, n_sub)) return rc;
+  }
+  auto& seg = w->seg[0];
+  for (int sgm = nck - 1; sgm >= 0; --sgm) {  // backward over the segments
+    const int first = sgm * w->every, last = std::min(w->n_steps, first + w->every);
+    if (int rc = window_restart(w, sgm)) return rc;
+    for (int n = first; n < last; ++n) {  // recompute: each step's three stage inputs
+      const size_t o = 3 * (size_t)(n - first);
+      if (int rc = copy_state(m, seg[o].data(), m->S[m->cur])) return rc;
+      double* const* base[3];
+      if (int rc = stl_record_step(m, w->dt, n_sub, seg[o + 1].data(), seg[o + 2].data(), base)) return rc;
+    }
+    for (int n = last - 1; n >= first; --n) {
+      const size_t o = 3 * (size_t)(n - first);
+      double* const* base[3] = {seg[o].data(), seg[o + 1].data(), seg[o + 2].data()};
+      if (int rc = stl_step_ad(m, w->dt, n_sub, base, m->stl[1])) return rc;
+    }
+  }
+  if (int rc = window_end(w, m->stream)) return rc;
+  if (int rc = stl_download(m, m->stl[1], dy, dx0_adjoint)) return rc;
+  if (int rc = read_status(m)) return rc;
+  if (int rc = window_restart(w, 0)) return rc;
+  return read_status(m);
+}
+
+int own_step_linear(vibe_gb300_model* m, double dt, int n_sub_in, const double* const* in, double* const* out,
+                    bool adjoint) {
+  if (!m || !in || !out || !(dt > 0.0)) return fail(VIBE_GB300_EBADARG, "bad argument");
+  if (int rc = stl_supported(m)) return rc;
+  if (int rc = stl_ensure(m)) return rc;
+  const int n_sub = std::max(n_sub_in, 1);
+  if (int rc = configure_dt(m, dt, n_sub)) return rc;
+  if (int rc = stl_upload(m, in, m->stl[1])) return rc;
+  const int c0 = m->cur;
+  double* const* base[3];
+  if (int rc = stl_record_step(m, dt, n_sub, m->stl[3], m->stl[4], base)) return rc;
+  const int rc = adjoint ? stl_step_ad(m, dt, n_sub, base, m->stl[1]) : stl_step_tl(m, dt, n_sub, base, m->stl[1]);
+  m->cur = c0;  // the linearisation point stays the model's state
+  if (rc) return rc;
+  if (int rc2 = sync_working(m)) return rc2;
+  if (int rc2 = stl_download(m, m->stl[1], in, out)) return rc2;
+  return read_status(m);
+}
+}  // namespace
+
+extern "C" {
+
 int vibe_gb300_window_tl(vibe_gb300_window* w, const double* const* dx0, double* const* dx_out) {
   if (!w || !dx0 || !dx_out) return fail(VIBE_GB300_EBADARG, "bad argument");
+  if (!w->t) return own_window_tl(w, dx0, dx_out);
   vibe_gb300_model* m = w->m;
   vibe_tlad* t = w->t;
   cudaStream_t ts = vgb::tlad_stream(t);
@@ -2480,6 +2824,7 @@ int vibe_gb300_window_tl(vibe_gb300_window* w, const double* const* dx0, double*
 
 int vibe_gb300_window_ad(vibe_gb300_window* w, const double* const* dy, double* const* dx0_adjoint) {
   if (!w || !dy || !dx0_adjoint) return fail(VIBE_GB300_EBADARG, "bad argument");
+  if (!w->t) return own_window_ad(w, dy, dx0_adjoint);
   vibe_gb300_model* m = w->m;
   vibe_tlad* t = w->t;
   cudaStream_t ts = vgb::tlad_stream(t);
@@ -2521,6 +2866,58 @@ int vibe_gb300_window_ad(vibe_gb300_window* w, const double* const* dy, double* 
   if (int rc = read_status(m)) return rc;
   if (int rc = window_restart(w, 0)) return rc;
   return read_status(m);
+}
+
+int vibe_gb300_tendency_tl(vibe_gb300_model* m, const double* const* dx, double* const* out) {
+  if (!m || !dx || !out) return fail(VIBE_GB300_EBADARG, "bad argument");
+  if (int rc = stl_supported(m)) return rc;
+  if (int rc = stl_ensure(m)) return rc;
+  if (int rc = stl_upload(m, dx, m->stl[1])) return rc;
+  tend_tl(m->d, m->met, m->fl, m->S[m->cur], m->stl[1], m->stl[2], m->stl_face, m->precision == VIBE_GB300_MIXED,
+          m->stream);
+  CUDA_OK(cudaGetLastError());
+  for (int q = 0; q < NSPECIES; ++q) {  // the tendency's boxes; zero elsewhere
+    const int ni = m->d.nx + (q == U), nj = m->d.ny + (q == V), nk = m->d.nz + (q == W);
+    k_unpack<<<1024, 256, 0, m->stream>>>(m->d, m->nsx[q], m->nsy[q], m->nsz[q], ni, nj, nk, m->stl[2][q],
+                                          m->d_stage_in);
+    CUDA_OK(cudaMemcpyAsync(out[q], m->d_stage_in, storage_count(m, q) * sizeof(double), cudaMemcpyDeviceToHost,
+                            m->stream));
+    CUDA_OK(cudaStreamSynchronize(m->stream));
+  }
+  return read_status(m);
+}
+
+int vibe_gb300_tendency_ad(vibe_gb300_model* m, const double* const* bar_r, double* const* bar_x) {
+  if (!m || !bar_r || !bar_x) return fail(VIBE_GB300_EBADARG, "bad argument");
+  if (int rc = stl_supported(m)) return rc;
+  if (int rc = stl_ensure(m)) return rc;
+  if (int rc = stl_upload(m, bar_r, m->stl[2])) return rc;
+  for (int q = 0; q < NSPECIES; ++q)  // only the tendency's boxes are its outputs
+    k_keep_box<<<1024, 256, 0, m->stream>>>(m->d, m->d.nx + (q == U), m->d.ny + (q == V), m->d.nz + (q == W),
+                                            m->stl[2][q]);
+  for (int q = 0; q < NSPECIES; ++q)
+    CUDA_OK(cudaMemsetAsync(m->stl[5][q], 0, state_count(m) * sizeof(double), m->stream));
+  tend_ad(m->d, m->met, m->fl, m->S[m->cur], m->stl[2], m->stl[5], m->stl_face, m->stl_cell,
+          m->precision == VIBE_GB300_MIXED, m->stream);
+  CUDA_OK(cudaGetLastError());
+  for (int q = 0; q < NSPECIES; ++q) {  // every uploaded point (the boxes incl. ghosts)
+    int ni, nj, nk;
+    box_of(m, q, ni, nj, nk);
+    k_unpack<<<1024, 256, 0, m->stream>>>(m->d, m->nsx[q], m->nsy[q], m->nsz[q], ni, nj, nk, m->stl[5][q],
+                                          m->d_stage_in);
+    CUDA_OK(cudaMemcpyAsync(bar_x[q], m->d_stage_in, storage_count(m, q) * sizeof(double), cudaMemcpyDeviceToHost,
+                            m->stream));
+    CUDA_OK(cudaStreamSynchronize(m->stream));
+  }
+  return read_status(m);
+}
+
+int vibe_gb300_step_tl(vibe_gb300_model* m, double dt, int n_sub, const double* const* dx, double* const* out) {
+  return own_step_linear(m, dt, n_sub, dx, out, false);
+}
+
+int vibe_gb300_step_ad(vibe_gb300_model* m, double dt, int n_sub, const double* const* dy, double* const* out) {
+  return own_step_linear(m, dt, n_sub, dy, out, true);
 }
 
 int vibe_gb300_window_stats(const vibe_gb300_window* w, double* last_ms, size_t* checkpoint_bytes,

@@ -148,4 +148,23 @@ void mixed_unpack_f32(const Dims& d, int nsx, int nsy, int nsz, int ni, int nj, 
                       cudaStream_t stream);
 void mixed_to_working(const Dims& d, const Tab& t, double* const* s, const WS& w, cudaStream_t stream);
 
+// ---- tangent-linear and adjoint of the slow tendency (step_tlad.cu) ----
+// base, pert, out, bar_*: 12 fields each, model layout (plane * (nz+1)
+// doubles); face: 6 * plane * (nz+1) doubles; cell_scr: plane * (nz+1).
+// f32: FP32 arithmetic (mixed models), else FP64.
+// out = J(base) pert, every point of every field written (0 off the boxes)
+void tend_tl(const Dims& d, const Metric& m, const Flags& fl, double* const* base, double* const* pert,
+             double* const* out, double* face, bool f32, cudaStream_t s);
+// bar_in += J(base)^T bar_out (atomic adds)
+void tend_ad(const Dims& d, const Metric& m, const Flags& fl, double* const* base, double* const* bar_out,
+             double* const* bar_in, double* face, double* cell_scr, bool f32, cudaStream_t s);
+// whole-array helpers: out = x0 + a r; acc += a x; conversions
+void lin_axpy(size_t n, const double* x0, const double* r, double a, double* out, cudaStream_t s);
+void lin_scale_add(size_t n, const double* x, double a, double* acc, cudaStream_t s);
+void lin_to_f32(size_t n, const double* x, float* y, cudaStream_t s);
+void lin_to_f64(size_t n, const float* x, double* y, cudaStream_t s);
+// FP32 working state (perturbation form) -> FP64 total fields (species with a
+// null working pointer are left as they are)
+void working_to_f64(const Dims& d, const Tab& t, const WS& w, double* const* out, cudaStream_t s);
+
 }  // namespace vgb

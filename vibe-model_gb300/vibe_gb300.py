@@ -92,6 +92,11 @@ _sigs = {
     "vibe_gb300_hevi_ad_f32": (_I, [_vp, _D, _I, ctypes.POINTER(_dp), ctypes.POINTER(_dp)]),
     "vibe_gb300_hevi_ad": (_I, [_vp, _D, _I, ctypes.POINTER(_dp), ctypes.POINTER(_dp)]),
     "vibe_gb300_hevi_substep": (_I, [_vp, _D]),
+    "vibe_gb300_tendency_tl": (_I, [_vp, ctypes.POINTER(_dp), ctypes.POINTER(_dp)]),
+    "vibe_gb300_tendency_ad": (_I, [_vp, ctypes.POINTER(_dp), ctypes.POINTER(_dp)]),
+    "vibe_gb300_step_tl": (_I, [_vp, _D, _I, ctypes.POINTER(_dp), ctypes.POINTER(_dp)]),
+    "vibe_gb300_step_ad": (_I, [_vp, _D, _I, ctypes.POINTER(_dp), ctypes.POINTER(_dp)]),
+    "vibe_gb300_window_plan": (_I, [ctypes.c_size_t, ctypes.c_size_t, _I, _I, ctypes.POINTER(_I)]),
     "vibe_gb300_sponge": (_I, [_vp, _D]),
     "vibe_gb300_snapshot": (_I, [_vp, _I]),
     "vibe_gb300_step_io": (_I, [_vp, ctypes.POINTER(_dp), _I, ctypes.POINTER(_dp), _I, _D, _I]),
@@ -331,6 +336,33 @@ class Model:
     def hevi_ad(self, dtau, n_sub, fields):
         """Adjoint of hevi_tl."""
         return self._acoustic_linear(lib.vibe_gb300_hevi_ad, dtau, n_sub, fields)
+
+    def _own_linear(self, fn, args, states):
+        ins = [np.ascontiguousarray(a, dtype=np.float64) for a in states]
+        assert len(ins) == NSPECIES
+        outs = [np.zeros(a.size) for a in ins]
+        pin = (_dp * NSPECIES)(*[a.ctypes.data_as(_dp) for a in ins])
+        pout = (_dp * NSPECIES)(*[a.ctypes.data_as(_dp) for a in outs])
+        _check(fn(self.h, *args, pin, pout))
+        return outs
+
+    def tendency_tl(self, dx):
+        """Tangent-linear of the slow tendency about the current state: 12
+        FieldT perturbations in, the tendency's perturbation out."""
+        return self._own_linear(lib.vibe_gb300_tendency_tl, (), dx)
+
+    def tendency_ad(self, bar_r):
+        """Adjoint of tendency_tl."""
+        return self._own_linear(lib.vibe_gb300_tendency_ad, (), bar_r)
+
+    def step_tl(self, dt, n_sub, dx):
+        """Tangent-linear of one model step (slow tendency, acoustic substeps,
+        sponge) about the current state, which it leaves as it is."""
+        return self._own_linear(lib.vibe_gb300_step_tl, (dt, n_sub), dx)
+
+    def step_ad(self, dt, n_sub, dy):
+        """Adjoint of step_tl."""
+        return self._own_linear(lib.vibe_gb300_step_ad, (dt, n_sub), dy)
 
     def autotune(self, dt, n_sub):
         """Pick the fastest launch shapes for this grid (mixed path); the
@@ -908,17 +940,27 @@ for _name, _res, _args in (("vibe_gb300_window_create", _I, [_vp, _vp, _D, _I, _
     _f.argtypes = _args
 
 
+def window_plan(free_bytes, state_bytes, n_steps, seg_states):
+    """The window's automatic checkpoint spacing (every = 0) for a given free
+    device memory: 1 (store every step) or ceil(sqrt(n_steps / seg_states));
+    raises VibeError when the checkpoints do not fit."""
+    every = _I()
+    _check(lib.vibe_gb300_window_plan(free_bytes, state_bytes, n_steps, seg_states, ctypes.byref(every)))
+    return every.value
+
+
 class Window:
-    """TL/AD (a TLAD object) linearised about the trajectory of a Model over
-    n_steps steps of dt, checkpointed every `every` steps and recomputed in
-    the adjoint sweep; the TL/AD takes tl_substeps steps per model step.
+    """TL/AD linearised about the trajectory of a Model over n_steps steps of
+    dt, checkpointed every `every` steps and recomputed in the adjoint sweep.
+    tlad = a TLAD object (the reference's collocated TL/AD, tl_substeps steps
+    per model step) or None (the TL/AD of the model's own step).
     Perturbations are lists of 12 FieldT arrays."""
 
     def __init__(self, model, tlad, dt, n_sub, n_steps, every=10, tl_substeps=1):
         self.model, self.tlad = model, tlad
         self.h = _vp()
-        _check(lib.vibe_gb300_window_create(model.h, tlad.h, dt, n_sub, n_steps, every, tl_substeps,
-                                            ctypes.byref(self.h)))
+        _check(lib.vibe_gb300_window_create(model.h, tlad.h if tlad is not None else None, dt, n_sub, n_steps,
+                                            every, tl_substeps, ctypes.byref(self.h)))
 
     def _io(self, states):
         ins = [np.ascontiguousarray(a, dtype=np.float64) for a in states]
