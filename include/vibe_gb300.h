@@ -288,7 +288,10 @@ int vibe_gb300_hevi_substep(vibe_gb300_model *m, double dtau);
 /* Autotuner of the mixed step: times, on this model's grid, the launch shapes
  * of the same update -- the HEVI column kernel variant (0 register ring,
  * 1 cp.async ring, 2/3 two columns per thread, 4 two columns per thread fed
- * by TMA boxes; -1 = the built-in choice) and
+ * by TMA boxes, 5 the same with the w/rho' corrections of the implicit
+ * sweep applied by the next reader of those fields, which cuts the
+ * backward sweep's traffic to pi' alone -- the built-in choice; -1 = the
+ * built-in choice) and
  * the stage kernel's levels per block -- and keeps the fastest for every
  * single model of this grid in the process (groups keep the built-in column
  * kernel). Variants differ only by FP32 rounding (FMA contraction, vertical

@@ -89,7 +89,7 @@ struct vibe_gb300_model {
   double* lin_scr = nullptr;       // HEVI TL/AD: per-column work
   double* lin_dh = nullptr;        // HEVI AD: bar of the horizontal divergence
   // TL/AD of the model's own step (allocated on first use): six perturbation
-  // states of 12 fields, the WENO face fluxes (6 fields), one cell field and
+  // states of 12 fields, the WENO face fluxes (9 fields), one cell field and
   // a zero field (the reference of the sponge's linear part)
   double* stl[6][NSPECIES] = {};
   double* stl_face = nullptr;
@@ -766,7 +766,8 @@ int enqueue_one_step(vibe_gb300_model* m, double dt, int n_sub) {
         }
         if (m->fl.acoustic_mode == 2 && stage < 2) {  // the last substep's u/v update, in place
           Span sp(m, 3);
-          mixed_uv_backward(d, m->tab, ws_of(in), ws_of(in), dtau, m->stream);
+          if (mixed_hevi_defers(d)) mixed_uv_fix(d, m->tab, m->fl, ws_of(in), dtau, m->stream);
+          else mixed_uv_backward(d, m->tab, ws_of(in), ws_of(in), dtau, m->stream);
         }
         final_sub = in;
         last_dtau = dtau;
@@ -786,7 +787,7 @@ int enqueue_one_step(vibe_gb300_model* m, double dt, int n_sub) {
       const WS wr = ws_of(m->WR);
       // stage 3's last u/v update is folded into the finish kernel
       mixed_finish(d, m->tab, m->fl, ws_of(final_sub), ws_of(m->WSt[0]), w0, &wr, dt, S0, S1, m->d_err, m->stream,
-                   m->fl.acoustic_mode == 2 ? last_dtau : 0.f);
+                   m->fl.acoustic_mode == 2 ? last_dtau : 0.f, m->fl.acoustic_mode == 2 && mixed_hevi_defers(d));
     }
     m->cur = 1 - m->cur;
   }
@@ -1430,8 +1431,9 @@ int vibe_gb300_autotune(vibe_gb300_model* m, double dt, int n_sub, vibe_gb300_tu
   double best_ms = 0.0, default_ms = 0.0, ms = 0.0;
   int rc = trial(MixedTune{}, &default_ms), tried = 1;
   best_ms = default_ms;
-  // column kernel: 0 register ring, 1 cp.async ring, 2/3 two columns per thread, 4 TMA-fed two columns
-  for (int c = 0; c <= 4 && !rc; ++c) {
+  // column kernel: 0 register ring, 1 cp.async ring, 2/3 two columns per thread, 4 TMA-fed two columns,
+  // 5 the same with the w/rho' corrections deferred to the reader
+  for (int c = 0; c <= 5 && !rc; ++c) {
     cur = MixedTune{};
     cur.column = c;
     rc = trial(cur, &ms);
@@ -1554,7 +1556,7 @@ int vibe_gb300_physics_tendency(vibe_gb300_model* m, double dt, double* const* o
 }
 
 int vibe_gb300_set_tuning(vibe_gb300_model* m, const vibe_gb300_tuning* t) {
-  if (!m || !t || t->stage_levels < 0 || t->stage_levels > m->d.nz || t->column_kernel < -1 || t->column_kernel > 4)
+  if (!m || !t || t->stage_levels < 0 || t->stage_levels > m->d.nz || t->column_kernel < -1 || t->column_kernel > 5)
     return fail(VIBE_GB300_EBADARG, "bad argument");
   MixedTune tn;
   tn.stage_levels = t->stage_levels;
@@ -2427,7 +2429,7 @@ int stl_ensure(vibe_gb300_model* m) {
   for (auto& st : m->stl)
     for (int q = 0; q < NSPECIES; ++q)
       if (int rc = dalloc(m, &st[q], n)) return rc;
-  if (int rc = dalloc(m, &m->stl_face, 6 * n)) return rc;
+  if (int rc = dalloc(m, &m->stl_face, 9 * n)) return rc;
   if (int rc = dalloc(m, &m->stl_cell, n)) return rc;
   if (m->precision == VIBE_GB300_FP64) {
     if (!m->lin_scr) {  // as the substep TL/AD entry points allocate them

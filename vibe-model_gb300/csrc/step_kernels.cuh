@@ -110,6 +110,12 @@ int mixed_hevi_substep(const Dims& d, const Tab& t, const Flags& fl, const WS& w
 int mixed_hevi_column(const Dims& d, const Tab& t, const Flags& fl, const WS& win, const WS& wout, float dtau,
                       const float* lu, bool apply_uv, unsigned* err, cudaStream_t stream);
 void mixed_uv_backward(const Dims& d, const Tab& t, const WS& win, const WS& wout, float dtau, cudaStream_t stream);
+// whether the column kernel chosen for this grid defers its w/rho'
+// corrections to the reader (then the last substep of a stage is finished
+// by mixed_uv_fix instead of mixed_uv_backward, and mixed_finish gets defer)
+bool mixed_hevi_defers(const Dims& d);
+// u/v backward update and the deferred w/rho' corrections, in place
+void mixed_uv_fix(const Dims& d, const Tab& t, const Flags& fl, const WS& s, float dtau, cudaStream_t stream);
 // adjoint of mixed_fb_substep, in place on bars of (u, v, w, rho', pi')
 void mixed_fb_substep_ad(const Dims& d, const Tab& t, const WS& bar, float dtau, cudaStream_t stream);
 // adjoint of mixed_hevi_substep (lu: the column factors for dtau), in place;
@@ -120,7 +126,7 @@ void mixed_hevi_substep_ad(const Dims& d, const Tab& t, const Flags& fl, const W
 // in-place mixed_uv_backward launch is then left out)
 void mixed_finish(const Dims& d, const Tab& t, const Flags& fl, const WS& wfin, const WS& wst, const WS& w0,
                   const WS* rin, double dt, double* const* s0, double* const* s1, unsigned* err,
-                  cudaStream_t stream, float uv_dtau = 0.f);
+                  cudaStream_t stream, float uv_dtau = 0.f, bool defer = false);
 // ---- several domains per launch (work-list), mixed path, HEVI mode ----
 struct MixedDomain {
   Dims d;
@@ -150,7 +156,7 @@ void mixed_to_working(const Dims& d, const Tab& t, double* const* s, const WS& w
 
 // ---- tangent-linear and adjoint of the slow tendency (step_tlad.cu) ----
 // base, pert, out, bar_*: 12 fields each, model layout (plane * (nz+1)
-// doubles); face: 6 * plane * (nz+1) doubles; cell_scr: plane * (nz+1).
+// doubles); face: 9 * plane * (nz+1) doubles; cell_scr: plane * (nz+1).
 // f32: FP32 arithmetic (mixed models), else FP64.
 // out = J(base) pert, every point of every field written (0 off the boxes)
 void tend_tl(const Dims& d, const Metric& m, const Flags& fl, double* const* base, double* const* pert,

@@ -683,6 +683,7 @@ constexpr int kDefaultHeviRing = 4;  // single-domain column kernel: 0 = registe
 constexpr int kDefaultHeviPar = 0;   // levels per thread of the level-split column kernel (0 = off)
 constexpr int kDefaultHeviTwo = 2;   // ring depth of the two-columns-per-thread kernel (0 = off)
 constexpr bool kDefaultHeviTma = true;  // TMA-fed two-column kernel (VIBE_GB300_HEVI_TMA=0 turns it off; candidate 4)
+constexpr bool kDefaultHeviDefer = true;  // ... with the w/rho' corrections deferred to the reader (candidate 5)
 constexpr int kBatchTwoRing = 2;     // work-list column kernel of groups: the single-domain default
 
 // 4-byte asynchronous global -> shared copies (sm_80+ cp.async), grouped
@@ -971,10 +972,24 @@ __device__ __forceinline__ double widen(float f) {
 // Also writes the next step's FP32 working copy W0.
 // uv_dtau != 0: the last substep's u/v backward update (fb_mom_body, u and
 // v) is applied here on the fly instead of by its own in-place launch
+// The deferred corrections of a kDefer column kernel's w and rho' (see
+// hevi_tma_body below), for 1 <= k <= nz-1 with cb = dtau beta cp:
+//   w(k) = w~(k) - cb tfz(k) (pi'(k) - pi'(k-1)) idzw(k)   (faces 0, nz: w = w~)
+// and with db = dtau beta, from the corrected w(k), w(k+1):
+//   rho'(k) = rho~(k) - db (rfz(k+1) w(k+1) - rfz(k) w(k)) idzc(k)
+__device__ __forceinline__ float defer_fix_w(const Tab& t, int nz, float cb, float wt, float pk, float pkm, int k) {
+  return (k >= 1 && k < nz) ? wt - cb * t.tfz[k] * (pk - pkm) * t.idzw[k] : wt;
+}
+__device__ __forceinline__ float defer_fix_rho(const Tab& t, float db, float rt, float wk, float wk1, int k) {
+  return rt + db * (-(t.rfz[k + 1] * wk1 - t.rfz[k] * wk) * t.idzc[k]);
+}
+
+// defer: wfin is a kDefer column kernel's output; its w and rho' get their
+// corrections (with dtau = uv_dtau) on the fly
 __device__ __forceinline__ void finish_body(const Dims& d, const Tab& t, const Flags& fl, const WS& wfin,
                                             const WS& wst, const WS& w0, const WS& rin, float dtf, const CS64& s0,
                                             const MS64& s1, unsigned* err, int bx, int by, int bz,
-                                            float uv_dtau = 0.f) {
+                                            float uv_dtau = 0.f, bool defer = false) {
   const int i = bx * blockDim.x + threadIdx.x;
   const int j = by * blockDim.y + threadIdx.y;
   const int k = bz;
@@ -990,8 +1005,14 @@ __device__ __forceinline__ void finish_body(const Dims& d, const Tab& t, const F
   const bool plain = __double_as_longlong(wd) == 0x3ff0000000000000ll && __double_as_longlong(sdt) == 0ll;
   bool bad = false;
   auto incr = [&](int q) { return rin.f[q] ? dtf * rin.f[q][c] : 0.f; };
+  const float cb = uv_dtau * (float)fl.hevi_beta * (float)kCp, db = uv_dtau * (float)fl.hevi_beta;
+  auto w_at = [&](int kf) {  // w at face kf of this column, corrected when deferred
+    const float wt = wfin.f[W][IX(i, j, kf)];
+    if (!defer || kf < 1 || kf >= d.nz) return wt;
+    return defer_fix_w(t, d.nz, cb, wt, wfin.f[PI][IX(i, j, kf)], wfin.f[PI][IX(i, j, kf - 1)], kf);
+  };
   auto face = [&](int q) {
-    float wv = wfin.f[q][c];
+    float wv = (q == W) ? w_at(k) : wfin.f[q][c];
     if (uv_dtau != 0.f && q != W) {  // as fb_mom_body: k < nz and the face's clamped pi' neighbours
       const float* __restrict__ pn = wfin.f[PI];
       const float cp = (float)kCp;
@@ -1021,7 +1042,8 @@ __device__ __forceinline__ void finish_body(const Dims& d, const Tab& t, const F
   }
   if (i < d.nx && j < d.ny && k < d.nz) {
     {
-      const float wv = wfin.f[RHO][c];
+      float wv = wfin.f[RHO][c];
+      if (defer) wv = defer_fix_rho(t, db, wv, w_at(k), w_at(k + 1), k);
       const double a = s0.f[RHO][c] + widen(incr(RHO) + (wv - wst.f[RHO][c]));
       const double v = plain ? a : wd * (a + sdt * t.r0d[kc]);
       s1.f[RHO][c] = v;
@@ -1059,8 +1081,9 @@ __global__ void k_mx_finish(const __grid_constant__ Dims d, const __grid_constan
                             const __grid_constant__ Flags fl, const __grid_constant__ WS wfin,
                             const __grid_constant__ WS wst, const __grid_constant__ WS w0,
                             const __grid_constant__ WS rin, float dtf, const __grid_constant__ CS64 s0,
-                            const __grid_constant__ MS64 s1, unsigned* err, float uv_dtau) {
-  finish_body(d, t, fl, wfin, wst, w0, rin, dtf, s0, s1, err, blockIdx.x, blockIdx.y, blockIdx.z, uv_dtau);
+                            const __grid_constant__ MS64 s1, unsigned* err, float uv_dtau, int defer) {
+  finish_body(d, t, fl, wfin, wst, w0, rin, dtf, s0, s1, err, blockIdx.x, blockIdx.y, blockIdx.z, uv_dtau,
+              defer != 0);
 }
 
 __global__ void k_mx_unpack_f32(Dims d, int nsx, int nsy, int nsz, int ni, int nj, int nk, const float* __restrict__ src,
@@ -1681,6 +1704,16 @@ __global__ void __launch_bounds__(128, 7) k_mx_hevi_col2(const __grid_constant__
 // clamped neighbour offsets of hevi2_body select in-range box points. Waits
 // are bounded; a box that does not arrive sets kErrWaitTimeout, and the block
 // waits (bounded) for its copies in flight before it returns.
+// kDefer: the HEVI backward sweep updates pi' alone. w and rho' leave the
+// kernel as their explicit parts w~ (= wt) and rho~ (= rho' + dtau S), and
+// every reader applies the implicit corrections from the final pi' itself
+// (defer_fix_w / defer_fix_rho). This kernel applies them to its own input
+// when apply_uv is set (its input is then a deferred substep's output); the
+// u/v kernel after a stage's last substep (k_mx_fix_col) and the finish
+// kernel apply them to the last one. The parked sweep data shrinks from
+// w~, rho~ and the eliminated pi' to the eliminated pi' alone: 48 instead of
+// 64 bytes of traffic per cell and substep.
+template <bool kDefer>
 __device__ __forceinline__ void hevi_tma_body(const Dims& d, const Tab& t, const Flags& fl, const ColumnMaps& C,
                                               const WS& win, const WS& wout, float dtau, const float* __restrict__ lu,
                                               int apply_uv, float cdx, float cdy, unsigned* err, int bx, int by) {
@@ -1820,8 +1853,16 @@ __device__ __forceinline__ void hevi_tma_body(const Dims& d, const Tab& t, const
       v1[1] += ty_ * (fn.y - pk[1]);
     }
     const size_t o = (size_t)k * pl;
-    const float wk1[2] = {fw.x, fw.y}, pk1in[2] = {fp.x, fp.y}, r0v[2] = {fr.x, fr.y};
+    float wk1[2] = {fw.x, fw.y}, r0v[2] = {fr.x, fr.y};
+    const float pk1in[2] = {fp.x, fp.y};
     const float rk = s_rfz[k], rk1 = s_rfz[k + 1], idz = s_idzc[k];
+    if (kDefer && apply_uv) {  // the input's deferred corrections (wk: corrected last iteration)
+#pragma unroll
+      for (int c = 0; c < 2; ++c) {
+        if (k + 1 < nz) wk1[c] = wk1[c] - dtau * b * cpf * s_tfz[k + 1] * (pk1in[c] - pk[c]) * s_idzw[k + 1];
+        r0v[c] = r0v[c] + dtau * b * (-(rk1 * wk1[c] - rk * wk[c]) * idz);
+      }
+    }
     float dpk[2], rsv[2], wtk1[2], pk1[2];
 #pragma unroll
     for (int c = 0; c < 2; ++c) {
@@ -1870,9 +1911,11 @@ __device__ __forceinline__ void hevi_tma_body(const Dims& d, const Tab& t, const
     float* s = ring + (size_t)(n % kColRing) * kColSlot;
     unsigned long long* bb = &bbar[n % kColRing];
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-    mbar_expect_tx(bb, kBackLevelBytes);
-    tma_load_3d(s + kBOffW, &C.back[0], i0, j0, kk, bb);
-    tma_load_3d(s + kBOffR, &C.back[1], i0, j0, kk, bb);
+    mbar_expect_tx(bb, kDefer ? kBackLevelBytes / 3 : kBackLevelBytes);
+    if (!kDefer) {
+      tma_load_3d(s + kBOffW, &C.back[0], i0, j0, kk, bb);
+      tma_load_3d(s + kBOffR, &C.back[1], i0, j0, kk, bb);
+    }
     tma_load_3d(s + kBOffP, &C.back[2], i0, j0, imax(kk - 1, 0), bb);
   };
   int bhi = imin(kColRing, nz) - 1;
@@ -1892,7 +1935,7 @@ __device__ __forceinline__ void hevi_tma_body(const Dims& d, const Tab& t, const
   const int obk = threadIdx.y * BW + 2 * threadIdx.x;
   float xu[2] = {dpp[0], dpp[1]};
   float wu[2] = {0.f, 0.f};
-  if (active) {
+  if (!kDefer && active) {
     wu[0] = Wo[(size_t)nz * pl];
     if (two) wu[1] = Wo[(size_t)nz * pl + 1];
   }
@@ -1905,6 +1948,15 @@ __device__ __forceinline__ void hevi_tma_body(const Dims& d, const Tab& t, const
     const float* sb = ring + (size_t)(n % kColRing) * kColSlot;
     const int kk = nz - 1 - n, k = kk - 1;
     const float2 fd = *reinterpret_cast<const float2*>(sb + kBOffP + obk);
+    if (kDefer) {
+      float xk[2];
+#pragma unroll
+      for (int c = 0; c < 2; ++c) xk[c] = (k >= 0) ? (c == 0 ? fd.x : fd.y) - s_lc[k] * xu[c] : 0.f;
+      if (active) st2(Po + (size_t)kk * pl, xu[0], xu[1]);
+      xu[0] = xk[0];
+      xu[1] = xk[1];
+      continue;
+    }
     const float2 fw = *reinterpret_cast<const float2*>(sb + kBOffW + obk);
     const float2 fs = *reinterpret_cast<const float2*>(sb + kBOffR + obk);
     const float bd[2] = {fd.x, fd.y}, bw[2] = {fw.x, fw.y}, bs[2] = {fs.x, fs.y};
@@ -1941,7 +1993,57 @@ __global__ void __launch_bounds__(128, 7) k_mx_hevi_tma(const __grid_constant__ 
                                                          const __grid_constant__ WS wout, float dtau,
                                                          const float* __restrict__ lu, int apply_uv, float cdx,
                                                          float cdy, unsigned* err) {
-  hevi_tma_body(d, t, fl, C, win, wout, dtau, lu, apply_uv, cdx, cdy, err, blockIdx.x, blockIdx.y);
+  hevi_tma_body<false>(d, t, fl, C, win, wout, dtau, lu, apply_uv, cdx, cdy, err, blockIdx.x, blockIdx.y);
+}
+__global__ void __launch_bounds__(128, 7) k_mx_hevi_tmad(const __grid_constant__ Dims d, const __grid_constant__ Tab t,
+                                                          const __grid_constant__ Flags fl,
+                                                          const __grid_constant__ ColumnMaps C,
+                                                          const __grid_constant__ WS win,
+                                                          const __grid_constant__ WS wout, float dtau,
+                                                          const float* __restrict__ lu, int apply_uv, float cdx,
+                                                          float cdy, unsigned* err) {
+  hevi_tma_body<true>(d, t, fl, C, win, wout, dtau, lu, apply_uv, cdx, cdy, err, blockIdx.x, blockIdx.y);
+}
+
+// After a stage's last substep of the kDefer column kernel: its u/v backward
+// update (as fb_mom_body) and the w/rho' corrections, in place; one thread per
+// column walks the levels upward, so every value is read before it is replaced.
+__global__ void k_mx_fix_col(const __grid_constant__ Dims d, const __grid_constant__ Tab t,
+                             const __grid_constant__ Flags fl, const __grid_constant__ WS s, float dtau) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y;
+  if (i > d.nx || j > d.ny) return;
+  const float* __restrict__ pn = s.f[PI];
+  const float cp = (float)kCp;
+  const int nz = d.nz;
+  const bool col = i < d.nx && j < d.ny;
+  const float b = (float)fl.hevi_beta;
+  const float cb = dtau * b * cp, db = dtau * b;
+  float wprev = 0.f, pprev = 0.f;
+  if (col) {
+    wprev = s.f[W][IX(i, j, 0)];  // face 0 is final
+    pprev = pn[IX(i, j, 0)];
+  }
+  for (int k = 0; k < nz; ++k) {
+    const size_t c = IX(i, j, k);
+    if (j < d.ny) {
+      const int ip = imin(i, d.nx - 1), im = imax(i - 1, 0);
+      s.f[U][c] = s.f[U][c] + dtau * (-cp * t.t0c[k] * (pn[IX(ip, j, k)] - pn[IX(im, j, k)]) * t.dx_inv);
+    }
+    if (i < d.nx) {
+      const int jp = imin(j, d.ny - 1), jm = imax(j - 1, 0);
+      s.f[V][c] = s.f[V][c] + dtau * (-cp * t.t0c[k] * (pn[IX(i, jp, k)] - pn[IX(i, jm, k)]) * t.dy_inv);
+    }
+    if (col) {
+      const size_t c1 = IX(i, j, k + 1);
+      const float pk1 = (k + 1 < nz) ? pn[c1] : 0.f;
+      const float w1 = defer_fix_w(t, nz, cb, s.f[W][c1], pk1, pprev, k + 1);
+      s.f[RHO][c] = defer_fix_rho(t, db, s.f[RHO][c], wprev, w1, k);
+      if (k + 1 < nz) s.f[W][c1] = w1;
+      wprev = w1;
+      pprev = pk1;
+    }
+  }
 }
 
 size_t hevi_tma_smem_bytes(int nz) {
@@ -2259,6 +2361,30 @@ bool hevi_tma() {
   return v != 0;
 }
 
+// the TMA column kernel defers the w/rho' corrections (kDefer);
+// VIBE_GB300_HEVI_DEFER=0 keeps both sweeps on all three fields
+bool hevi_defer() {
+  static int v = -1;
+  if (v < 0) {
+    v = kDefaultHeviDefer ? 1 : 0;
+    if (const char* e = std::getenv("VIBE_GB300_HEVI_DEFER")) v = std::atoi(e) != 0;
+  }
+  return v != 0;
+}
+
+// the column kernel variant for this grid among the TMA ones: 4 TMA,
+// 5 TMA with deferred corrections, -1 neither
+int hevi_tma_variant(const Dims& d) {
+  MixedTune tn;
+  bool tma = hevi_tma(), defer = hevi_defer();
+  if (tune_of(d, &tn) && tn.column >= 0) {
+    tma = tn.column == 4 || tn.column == 5;
+    defer = tn.column == 5;
+  }
+  if (!tma || hevi_tma_smem_bytes(d.nz) > 48 * 1024) return -1;
+  return defer ? 5 : 4;
+}
+
 size_t hevi2_smem_bytes(int nz, int ring) {
   return ((((size_t)10 * (nz + 1) + 3) & ~(size_t)3) + (size_t)ring * 19 * 128) * sizeof(float);
 }
@@ -2268,20 +2394,22 @@ int mixed_hevi_column(const Dims& d, const Tab& t, const Flags& fl, const WS& wi
   MixedTune tn;
   const bool tuned = tune_of(d, &tn) && tn.column >= 0;
   int r2 = hevi_two_ring(), ring = hevi_ring();
-  bool tma = hevi_tma();
-  if (tuned) {  // 0: register ring, 1: cp.async ring 4, 2/3: two columns per thread with ring 2/3, 4: TMA-fed
+  if (tuned) {  // 0: register ring, 1: cp.async ring 4, 2/3: two columns per thread with ring 2/3, 4/5: TMA-fed
     r2 = (tn.column == 2) ? 2 : (tn.column == 3 ? 3 : 0);
     ring = (tn.column == 1) ? 4 : 0;
-    tma = tn.column == 4;
   }
-  if (tma && hevi_tma_smem_bytes(d.nz) <= 48 * 1024) {
+  if (const int v = hevi_tma_variant(d); v >= 0) {
     ColumnMaps C;
     if (!column_maps(d, win, wout, C)) return -1;
     const dim3 bc(32, 4);
     const dim3 g((d.nx + 63) / 64, (d.ny + 3) / 4);
     const float cdx = -(float)kCp * dtau * t.dx_inv, cdy = -(float)kCp * dtau * t.dy_inv;
-    k_mx_hevi_tma<<<g, bc, hevi_tma_smem_bytes(d.nz), stream>>>(d, t, fl, C, win, wout, dtau, lu, apply_uv ? 1 : 0,
-                                                                  cdx, cdy, err);
+    if (v == 5)
+      k_mx_hevi_tmad<<<g, bc, hevi_tma_smem_bytes(d.nz), stream>>>(d, t, fl, C, win, wout, dtau, lu,
+                                                                     apply_uv ? 1 : 0, cdx, cdy, err);
+    else
+      k_mx_hevi_tma<<<g, bc, hevi_tma_smem_bytes(d.nz), stream>>>(d, t, fl, C, win, wout, dtau, lu,
+                                                                    apply_uv ? 1 : 0, cdx, cdy, err);
     return 0;
   }
   if (r2) {
@@ -2333,21 +2461,31 @@ void mixed_uv_backward(const Dims& d, const Tab& t, const WS& win, const WS& wou
   k_mx_fb_mom<<<g3(d.nx + 1, d.ny + 1, d.nz, b), b, 0, stream>>>(d, t, win, wout, dtau, 0);
 }
 
+bool mixed_hevi_defers(const Dims& d) { return hevi_tma_variant(d) == 5; }
+
+void mixed_uv_fix(const Dims& d, const Tab& t, const Flags& fl, const WS& s, float dtau, cudaStream_t stream) {
+  const dim3 b(32, 4);
+  k_mx_fix_col<<<dim3((d.nx + 32) / 32, (d.ny + 4) / 4), b, 0, stream>>>(d, t, fl, s, dtau);
+}
+
 int mixed_hevi_substep(const Dims& d, const Tab& t, const Flags& fl, const WS& win, const WS& wout, float dtau,
                        const float* lu, unsigned* err, cudaStream_t stream) {
   if (mixed_hevi_column(d, t, fl, win, wout, dtau, lu, false, err, stream)) return -1;
-  mixed_uv_backward(d, t, wout, wout, dtau, stream);  // in place: u, v were copied by the column kernel
+  // in place: u, v were copied by the column kernel
+  if (mixed_hevi_defers(d)) mixed_uv_fix(d, t, fl, wout, dtau, stream);
+  else mixed_uv_backward(d, t, wout, wout, dtau, stream);
   return 0;
 }
 
 void mixed_finish(const Dims& d, const Tab& t, const Flags& fl, const WS& wfin, const WS& wst, const WS& w0,
                   const WS* rin, double dt, double* const* s0, double* const* s1, unsigned* err,
-                  cudaStream_t stream, float uv_dtau) {
+                  cudaStream_t stream, float uv_dtau, bool defer) {
   const dim3 b(32, 4);
   WS none;
   for (int q = 0; q < NSPECIES; ++q) none.f[q] = nullptr;
   k_mx_finish<<<g3(d.nx + 1, d.ny + 1, d.nz + 1, b), b, 0, stream>>>(d, t, fl, wfin, wst, w0, rin ? *rin : none,
-                                                                     (float)dt, cs64(s0), ms64(s1), err, uv_dtau);
+                                                                     (float)dt, cs64(s0), ms64(s1), err, uv_dtau,
+                                                                     defer ? 1 : 0);
 }
 
 void mixed_unpack_f32(const Dims& d, int nsx, int nsy, int nsz, int ni, int nj, int nk, const float* src, double* dst,
@@ -2435,7 +2573,7 @@ __global__ void __launch_bounds__(128, 7) k_b_hevi_tma(const HeviArgs* __restric
   const int dom = find_domain(start, nd);
   const HeviArgs& a = A[dom];
   const int l = (int)blockIdx.x - start[dom];
-  hevi_tma_body(a.d, a.t, a.fl, a.C, a.win, a.wout, a.dtau, a.lu, a.apply_uv, a.cdx, a.cdy, err, l % a.gx,
+  hevi_tma_body<false>(a.d, a.t, a.fl, a.C, a.win, a.wout, a.dtau, a.lu, a.apply_uv, a.cdx, a.cdy, err, l % a.gx,
                 l / a.gx);
 }
 

@@ -24,6 +24,10 @@
 //   * A WENO5 face flux is shared by the two cells beside the face, so its
 //     adjoint runs per face: bar_F is gathered from the two cells' bars (zero
 //     where the clip is active) and then scattered to the face's six loads.
+//     Face fluxes are carried as F(q - c) with c = q at the stencil centre,
+//     and the cells add the c u parts back as (q - c) u, so that the large
+//     products q u of the flux and advective forms never cancel (this keeps
+//     FP32 tangents and adjoints consistent to ~1e-7).
 // The pressure-gradient and mass-flux terms that split_fast moves to the
 // acoustic substeps are folded into the slow ones they cancel (theta -
 // theta0, rho - rho0 beside each wind), so no two loads carry large
@@ -305,8 +309,10 @@ __device__ __forceinline__ Jet<R> weno_left_(Jet<R> qm2, Jet<R> qm1, Jet<R> q0, 
   const T s0 = (13.0 / 12.0) * (e0 * e0) + 0.25 * (f0 * f0) + 1e-6;
   const T s1 = (13.0 / 12.0) * (e1 * e1) + 0.25 * (f1 * f1) + 1e-6;
   const T s2 = (13.0 / 12.0) * (e2 * e2) + 0.25 * (f2 * f2) + 1e-6;
-  const T one{(R)1, (R)0};
-  const T a0 = 0.1 * (one / (s0 * s0)), a1 = 0.6 * (one / (s1 * s1)), a2 = 0.3 * (one / (s2 * s2));
+  // the weights d_k / s_k^2 scaled by (s0 s1 s2)^2: no 1/s^2 of s ~ 1e-6, so
+  // the derivatives of the normalisation do not cancel large numbers
+  const T p12 = s1 * s2, p02 = s0 * s2, p01 = s0 * s1;
+  const T a0 = 0.1 * (p12 * p12), a1 = 0.6 * (p02 * p02), a2 = 0.3 * (p01 * p01);
   return (a0 * v0 + a1 * v1 + a2 * v2) / (a0 + a1 + a2);
 }
 // Lax-Friedrichs face flux 0.5 (u (qL + qR) - max(|u|, 1e-3) (qR - qL)),
@@ -320,18 +326,30 @@ __device__ __forceinline__ Jet<R> weno_flux_(Jet<R> qm2, Jet<R> qm1, Jet<R> q0, 
   else if (vel.v <= (R)-1e-3) alpha = -vel;
   return 0.5 * (vel * (ql + qr) - alpha * (qr - ql));
 }
-// the face flux of direction dir (0 x, 1 y, 2 z) at face index (i, j, k):
-// k_weno_faces' stencil CL(f-3..f+1) and the normal wind at the face
+// The face flux of direction dir (0 x, 1 y, 2 z) at face index (i, j, k)
+// (k_weno_faces' stencil CL(f-3..f+1) and the normal wind at the face), as
+// G = F(q - c) = F(q) - c u: the reconstruction is translation invariant, so
+// shifting the stencil by c = q at its centre point (a value, without
+// derivative) changes only the c u part. The small shifted values keep FP32
+// accurate; a cell combines G with c and its own q without cancelling the
+// large c u terms of its faces (pt_wcell).
 template <class R, class Ld>
-__device__ __forceinline__ Jet<R> pt_wface(const Dims& d, Ld& L, int q, int dir, int i, int j, int k) {
-  if (dir == 0)
-    return weno_flux_<R>(LDC(q, i - 3, j, k), LDC(q, i - 2, j, k), LDC(q, i - 1, j, k), LDC(q, i, j, k),
-                         LDC(q, i + 1, j, k), LD(U, i, j, k));
-  if (dir == 1)
-    return weno_flux_<R>(LDC(q, i, j - 3, k), LDC(q, i, j - 2, k), LDC(q, i, j - 1, k), LDC(q, i, j, k),
-                         LDC(q, i, j + 1, k), LD(V, i, j, k));
-  return weno_flux_<R>(LDC(q, i, j, k - 3), LDC(q, i, j, k - 2), LDC(q, i, j, k - 1), LDC(q, i, j, k),
-                       LDC(q, i, j, k + 1), LD(W, i, j, k));
+__device__ __forceinline__ Jet<R> pt_wface(const Dims& d, Ld& L, int q, int dir, int i, int j, int k, R c) {
+  Jet<R> z[5];
+  int di = 0, dj = 0, dk = 0;
+  if (dir == 0) di = 1;
+  else if (dir == 1) dj = 1;
+  else dk = 1;
+#pragma unroll
+  for (int m = 0; m < 5; ++m) z[m] = LDC(q, i + (m - 3) * di, j + (m - 3) * dj, k + (m - 3) * dk) - (double)c;
+  const Jet<R> vel = LD(dir == 0 ? U : (dir == 1 ? V : W), i, j, k);
+  return weno_flux_<R>(z[0], z[1], z[2], z[3], z[4], vel);
+}
+// c of the face at index (i, j, k): q at the stencil's centre (the cell at
+// the face's index, clamped)
+template <class R>
+__device__ __forceinline__ R wface_shift(const Dims& d, const double* q, int i, int j, int k) {
+  return (R)q[d.idx(iclamp(i, 0, d.nx - 1), iclamp(j, 0, d.ny - 1), iclamp(k, 0, d.nz - 1))];
 }
 
 // faces that exist for direction dir at index (i, j, k)
@@ -345,29 +363,44 @@ __device__ __forceinline__ bool face_exists(const Dims& d, int dir, int i, int j
 // derivative of each face, loaded by `face`), the advective-form term and
 // the clip
 struct FaceArr {
-  double* v[3];  // fx, fy, fz values
+  double* v[3];  // G of the x, y, z faces (values)
   double* t[3];  // their tangents (TL only)
+  double* c[3];  // their shifts c
 };
+// With F = G + c u and div = sum_f s_f u_f / D_f (s_f = +1 on the east,
+// north and top faces, -1 on the others), the cell's
+//   r = -sum_f s_f F_f / D_f (+ q div with weno_advective)
+// is evaluated as
+//   r = -sum_f s_f G_f / D_f + sum_f s_f (q - c_f) u_f / D_f   (advective)
+//   r = -sum_f s_f (G_f + c_f u_f) / D_f                        (flux form)
+// where q - c_f is a difference of two nearby values.
 template <class R, class Ld>
 __device__ __forceinline__ Jet<R> pt_wcell(const Dims& d, const Metric& m, const Flags& fl, Ld& L, const FaceArr& F,
-                                           bool with_t, int q, int i, int j, int k) {
+                                           bool with_t, int q, int i, int j, int k, bool clip = true) {
   using T = Jet<R>;
-  auto f = [&](int dir, int a, int b, int c) -> T {
-    const size_t o = d.idx(a, b, c);
-    return {(R)F.v[dir][o], with_t ? (R)F.t[dir][o] : (R)0};
-  };
   const double dz = dzeta_(m, d, k) * scale_(m, d, i, j);
   const double idz = 1.0 / dz;
   const T qc = LD(q, i, j, k);
   const bool vert = (k + 2 < d.nz || k >= 2);
-  T r = -((f(0, i + 1, j, k) - f(0, i, j, k)) * m.inv_dx) - (f(1, i, j + 1, k) - f(1, i, j, k)) * m.inv_dy;
-  if (vert) r = r - (f(2, i, j, k + 1) - f(2, i, j, k)) * idz;
-  if (fl.weno_advective) {
-    T div = (LD(U, i + 1, j, k) - LD(U, i, j, k)) * m.inv_dx + (LD(V, i, j + 1, k) - LD(V, i, j, k)) * m.inv_dy;
-    if (vert) div = div + (LD(W, i, j, k + 1) - LD(W, i, j, k)) * idz;
-    r = r + qc * div;
+  const bool adv = fl.weno_advective;
+  T r{(R)0, (R)0};
+  auto face = [&](int dir, int a, int b, int c, double sgn, double inv) {
+    const size_t o = d.idx(a, b, c);
+    const T G{(R)F.v[dir][o], with_t ? (R)F.t[dir][o] : (R)0};
+    const R cf = (R)F.c[dir][o];
+    const T u = L(dir == 0 ? U : (dir == 1 ? V : W), o);
+    if (adv) r = r + (-sgn * inv) * G + (sgn * inv) * ((qc - (double)cf) * u);
+    else r = r + (-sgn * inv) * (G + u * (double)cf);
+  };
+  face(0, i + 1, j, k, 1.0, m.inv_dx);
+  face(0, i, j, k, -1.0, m.inv_dx);
+  face(1, i, j + 1, k, 1.0, m.inv_dy);
+  face(1, i, j, k, -1.0, m.inv_dy);
+  if (vert) {
+    face(2, i, j, k + 1, 1.0, idz);
+    face(2, i, j, k, -1.0, idz);
   }
-  if (q >= QV && qc.v <= (R)0 && r.v < (R)0) r = T{(R)0, (R)0};
+  if (clip && q >= QV && qc.v <= (R)0 && r.v < (R)0) r = T{(R)0, (R)0};
   return r;
 }
 
@@ -413,18 +446,20 @@ __global__ void k_tl_wface(Dims d, const __grid_constant__ F12 b, const __grid_c
   const int k = blockIdx.z;
   if (i > d.nx || j > d.ny || k > d.nz) return;
   const size_t c = d.idx(i, j, k);
+  const R sh = wface_shift<R>(d, b.f[q], i, j, k);
   for (int dir = 0; dir < 3; ++dir) {
     if (!face_exists(d, dir, i, j, k)) continue;
     Jet<R> f;
     if (with_t) {
       TlLoad<R> L{&b, &p};
-      f = pt_wface<R>(d, L, q, dir, i, j, k);
+      f = pt_wface<R>(d, L, q, dir, i, j, k, sh);
       F.t[dir][c] = (double)f.d;
     } else {
       ValLoad<R> L{&b};
-      f = pt_wface<R>(d, L, q, dir, i, j, k);
+      f = pt_wface<R>(d, L, q, dir, i, j, k, sh);
     }
     F.v[dir][c] = (double)f.v;
+    F.c[dir][c] = (double)sh;
   }
 }
 
@@ -504,39 +539,78 @@ __global__ void k_ad_wcell(Dims d, Metric m, Flags fl, const __grid_constant__ F
   double lam = bo[c];
   if (lam != 0.0 && q >= QV) {
     ValLoad<R> VL{&b};
-    const Jet<R> r = pt_wcell<R>(d, m, fl, VL, F, false, q, i, j, k);
-    if (r.v == (R)0 && VL(q, c).v <= (R)0) lam = 0.0;  // the clip holds R at zero
+    const Jet<R> r = pt_wcell<R>(d, m, fl, VL, F, false, q, i, j, k, false);
+    if (VL(q, c).v <= (R)0 && r.v < (R)0) lam = 0.0;  // the clip holds R at zero
   }
   ebar[c] = lam;
   if (lam == 0.0 || !fl.weno_advective) return;
-  // r += qc * div: the face fluxes enter through ebar; here the loads of
-  // qc * div alone (the face values carry no derivative in this pass)
-  ad_scatter<R>(b, bi, lam, [&](AdLoad<R>& L) { return pt_wcell<R>(d, m, fl, L, F, false, q, i, j, k); });
+  // the cell's own q enters r (beyond its faces' G) through (q - c_f) u_f:
+  // dr/dq = div; the winds' part is scattered per face (k_ad_wface)
+  const double dz = dzeta_(m, d, k) * scale_(m, d, i, j);
+  const bool vert = (k + 2 < d.nz || k >= 2);
+  R div = ((R)b.f[U][d.idx(i + 1, j, k)] - (R)b.f[U][c]) * (R)m.inv_dx +
+          ((R)b.f[V][d.idx(i, j + 1, k)] - (R)b.f[V][c]) * (R)m.inv_dy;
+  if (vert) div += ((R)b.f[W][d.idx(i, j, k + 1)] - (R)b.f[W][c]) * (R)(1.0 / dz);
+  atomicAdd(&bi.f[q][c], (double)div * lam);
 }
 
 // WENO faces: bar_F from the two cells beside each face, then the face's loads
+// Face at index (i, j, k) of direction dir: cell R = the cell at that index
+// (the face is its west / south / bottom face), cell L the one before it.
+// aR = bar(R) / D_R and aL = bar(L) / D_L where the cell exists and uses the
+// face (vertical faces only where the cell's vertical terms are on); then
+// bar_G = aR - aL, and the face's wind also carries the cells' (q - c) u and
+// c u parts (pt_wcell).
 template <class R>
-__global__ void k_ad_wface(Dims d, Metric m, const __grid_constant__ F12 b, int q, const double* __restrict__ ebar,
-                           const __grid_constant__ B12 bi) {
+__global__ void k_ad_wface(Dims d, Metric m, Flags fl, const __grid_constant__ F12 b, int q,
+                           const double* __restrict__ ebar, const __grid_constant__ B12 bi) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
   const int k = blockIdx.z;
   if (i > d.nx || j > d.ny || k > d.nz) return;
+  const R sh = wface_shift<R>(d, b.f[q], i, j, k);
   for (int dir = 0; dir < 3; ++dir) {
     if (!face_exists(d, dir, i, j, k)) continue;
-    double lam = 0.0;
+    const int li = i - (dir == 0), lj = j - (dir == 1), lk = k - (dir == 2);
+    bool hasR, hasL;
+    double invR, invL;
     if (dir == 0) {
-      if (i < d.nx) lam += ebar[d.idx(i, j, k)] * m.inv_dx;    // west face of cell i
-      if (i >= 1) lam -= ebar[d.idx(i - 1, j, k)] * m.inv_dx;  // east face of cell i-1
+      hasR = i < d.nx;
+      hasL = i >= 1;
+      invR = invL = m.inv_dx;
     } else if (dir == 1) {
-      if (j < d.ny) lam += ebar[d.idx(i, j, k)] * m.inv_dy;
-      if (j >= 1) lam -= ebar[d.idx(i, j - 1, k)] * m.inv_dy;
+      hasR = j < d.ny;
+      hasL = j >= 1;
+      invR = invL = m.inv_dy;
     } else {
-      if (k < d.nz && (k + 2 < d.nz || k >= 2)) lam += ebar[d.idx(i, j, k)] / (dzeta_(m, d, k) * scale_(m, d, i, j));
-      if (k >= 1 && (k + 1 < d.nz || k - 1 >= 2))
-        lam -= ebar[d.idx(i, j, k - 1)] / (dzeta_(m, d, k - 1) * scale_(m, d, i, j));
+      hasR = k < d.nz && (k + 2 < d.nz || k >= 2);
+      hasL = k >= 1 && (lk + 2 < d.nz || lk >= 2);
+      invR = hasR ? 1.0 / (dzeta_(m, d, k) * scale_(m, d, i, j)) : 0.0;
+      invL = hasL ? 1.0 / (dzeta_(m, d, lk) * scale_(m, d, i, j)) : 0.0;
     }
-    if (lam != 0.0) ad_scatter<R>(b, bi, lam, [&](AdLoad<R>& L) { return pt_wface<R>(d, L, q, dir, i, j, k); });
+    const double aR = hasR ? ebar[d.idx(i, j, k)] * invR : 0.0;
+    const double aL = hasL ? ebar[d.idx(li, lj, lk)] * invL : 0.0;
+    const double lamG = aR - aL;
+    if (aR == 0.0 && aL == 0.0) continue;
+    double extra;  // the wind's part beyond G
+    if (fl.weno_advective) {
+      const R qR = hasR ? (R)b.f[q][d.idx(i, j, k)] : sh, qL = hasL ? (R)b.f[q][d.idx(li, lj, lk)] : sh;
+      extra = -(double)(qR - sh) * aR + (double)(qL - sh) * aL;
+    } else {
+      extra = (double)sh * lamG;
+    }
+    const int vq = dir == 0 ? U : (dir == 1 ? V : W);
+    AdLoad<R> L{&b, 0, 0, -1, 0};
+    for (int seed = 0; seed < kMaxLoads; ++seed) {
+      L.seed = seed;
+      L.n = 0;
+      L.hq = -1;
+      const Jet<R> g = pt_wface<R>(d, L, q, dir, i, j, k, sh);
+      if (L.hq < 0) break;
+      double v = (double)g.d * lamG;
+      if (L.hq == vq) v += extra;
+      if (v != 0.0) atomicAdd(&bi.f[L.hq][L.hc], v);
+    }
   }
 }
 
@@ -599,6 +673,7 @@ FaceArr face_arr(const Dims& d, double* face) {
   for (int a = 0; a < 3; ++a) {
     F.v[a] = face + a * nf;
     F.t[a] = face + (3 + a) * nf;
+    F.c[a] = face + (6 + a) * nf;
   }
   return F;
 }
@@ -636,7 +711,7 @@ void tend_ad_t(const Dims& d, const Metric& m, const Flags& fl, double* const* b
       if (q == PI) continue;
       k_tl_wface<R><<<grid3_(d, d.nx + 1, d.ny + 1, d.nz + 1, kB), kB, 0, s>>>(d, b, b, q, F, 0);
       k_ad_wcell<R><<<grid3_(d, d.nx, d.ny, d.nz, kB), kB, 0, s>>>(d, m, fl, b, q, F, bar_out[q], cell_scr, bi);
-      k_ad_wface<R><<<grid3_(d, d.nx + 1, d.ny + 1, d.nz + 1, kB), kB, 0, s>>>(d, m, b, q, cell_scr, bi);
+      k_ad_wface<R><<<grid3_(d, d.nx + 1, d.ny + 1, d.nz + 1, kB), kB, 0, s>>>(d, m, fl, b, q, cell_scr, bi);
     }
   }
 }
