@@ -238,18 +238,19 @@ def window_leg(vg, torch):
     case = {k: v for k, v in CASE.items() if k not in ("dx", "dy", "nz", "zeta_stretch", "hevi_beta")}
     s = vg.Setup.defaults(nx=WIN["nx"], ny=WIN["ny"], nz=WIN["nz"], dx=WIN["dx"], dy=WIN["dx"], zeta_stretch=1.0,
                           w_rigid=1, hevi_beta=0.6, **case)
-    out = {"workload": "192x192x50 (dx=3 km, 400 m levels), dt=15 s x 120 steps, checkpoints every 10 steps, "
-                       "TL/AD 12 x 1.25 s per step; trajectory from the base state plus the single-domain case's "
-                       "seeded perturbations (20 bubbles, theta' noise below 1 km), rigid ground and lid, "
-                       "HEVI off-centred (beta 0.6)",
+    out = {"workload": "192x192x50 (dx=3 km, 400 m levels), dt=15 s x 120 steps, checkpoints every 10 steps; "
+                       "trajectory from the base state plus the single-domain case's seeded perturbations "
+                       "(20 bubbles, theta' noise below 1 km), rigid ground and lid, HEVI off-centred (beta 0.6); "
+                       "model_step: the TL/AD of the model's own step, one per model step; the rest: the "
+                       "reference's collocated TL/AD at 12 x 1.25 s per step",
            "tl_substeps": WIN["tl_sub"], "tl_dt_s": WIN["dt"] / WIN["tl_sub"]}
     kappa = 287.05 / 1004.5
-    for name, prec, tprec, tol in (("fp64", vg.FP64, 0, 1e-10), ("mixed", vg.MIXED, 1, 1e-5)):
+
+    def model_and_vectors(prec):
         m = vg.Model(s, prec)
         th, pi = perturbed_state(s, m.get(4), m.get(3), m.zeta(), seed=5, nx_full=s.nx, ny_full=s.ny)
         m.set(4, th)
         m.set(5, pi)
-        t = vg.TLAD(s.nx, s.ny, s.nz, s.dx, s.dy, s.z_top, np.diff(m.zeta()), m.terrain(), tprec)
         pi0 = vg.interior(s, 5, m.reffield(1))  # reference Exner function and pressure
         vecs = []
         for seed in (11, 12):
@@ -260,7 +261,56 @@ def window_leg(vg, torch):
             p0 = vg.interior(s, 5, m.reffield(3))
             vg.interior(s, 5, v[5])[...] = kappa * pi0 * 50.0 * r.standard_normal(pi0.shape) / p0
             vecs.append(v)
-        dx, dy = vecs
+        return m, vecs[0], vecs[1]
+
+    def vdot(a, b):
+        return sum(float(np.sum(vg.interior(s, sp, a[sp]) * vg.interior(s, sp, b[sp]))) for sp in range(12))
+
+    cells = s.nx * s.ny * s.nz
+    # the model's own step (slow tendency, HEVI substeps, sponge): one TL/AD
+    # step per 15 s model step, checkpoints with recomputation
+    own = {"what": "TL/AD of the model's own step (vibe_gb300_step_tl/_ad composed over the window, "
+                   "vibe_gb300_window_* with tlad = NULL): WENO5 advective-form scalars with exact weight "
+                   "derivatives, momentum, buoyancy, pi' pressure gradient, consistent HEVI substeps, sponge; "
+                   "one TL/AD step per model step (no sub-stepping)"}
+    for name, prec, tol in (("fp64", vg.FP64, 1e-10), ("mixed", vg.MIXED, 1e-5)):
+        m, dx, dy = model_and_vectors(prec)
+        try:
+            with vg.Window(m, None, WIN["dt"], NSUB, WIN["n_steps"], WIN["every"]) as w:
+                ldx = w.tl(dx)
+                tl_ms = w.stats()[0]
+                ady = w.ad(dy)
+                ad_ms, ck, sg = w.stats()
+            lhs, rhs = vdot(ldx, dy), vdot(dx, ady)
+            res = {"tl_window_ms": tl_ms, "ad_window_ms": ad_ms, "dot_lhs": lhs, "dot_rhs": rhs,
+                   "dot_rel_err": abs(lhs - rhs) / max(abs(lhs), abs(rhs)), "dot_tol": tol,
+                   "tl_cell_steps_per_s": cells * WIN["n_steps"] / (tl_ms * 1e-3),
+                   "ad_cell_steps_per_s": cells * WIN["n_steps"] / (ad_ms * 1e-3),
+                   "checkpoint_bytes": ck, "segment_bytes": sg}
+            if name == "fp64":
+                # (M(x + e dx) - M(x)) / e against the window TL, M = the 120 nonlinear steps
+                x0 = m.state()
+                m.step(WIN["dt"], NSUB, WIN["n_steps"])
+                mx = m.state()
+                nl = np.sqrt(vdot(ldx, ldx))
+                fd = {}
+                for k in range(2, 8):
+                    e = 10.0 ** -k
+                    m.set_state([a + e * b for a, b in zip(x0, dx)])
+                    m.step(WIN["dt"], NSUB, WIN["n_steps"])
+                    d = [(a - b) / e - c for a, b, c in zip(m.state(), mx, ldx)]
+                    fd["%.0e" % e] = np.sqrt(vdot(d, d)) / nl
+                m.set_state(x0)
+                res["fd_window_rel_err"] = fd
+            own[name] = res
+        finally:
+            m.close()
+    out["model_step"] = own
+    out["collocated_reference_check"] = "the reference's own TL/AD (tangent_linear.cpp: collocated RK3 " \
+                                        "without acoustic substeps) over the same trajectory: fp64 / mixed below"
+    for name, prec, tprec, tol in (("fp64", vg.FP64, 0, 1e-10), ("mixed", vg.MIXED, 1, 1e-5)):
+        m, dx, dy = model_and_vectors(prec)
+        t = vg.TLAD(s.nx, s.ny, s.nz, s.dx, s.dy, s.z_top, np.diff(m.zeta()), m.terrain(), tprec)
         w = vg.Window(m, t, WIN["dt"], NSUB, WIN["n_steps"], WIN["every"], WIN["tl_sub"])
         try:
             ldx = w.tl(dx)
@@ -269,9 +319,7 @@ def window_leg(vg, torch):
             ad_ms, ck, sg = w.stats()
         finally:
             w.close()
-        lhs = sum(float(np.sum(vg.interior(s, sp, ldx[sp]) * vg.interior(s, sp, dy[sp]))) for sp in range(12))
-        rhs = sum(float(np.sum(vg.interior(s, sp, dx[sp]) * vg.interior(s, sp, ady[sp]))) for sp in range(12))
-        cells = s.nx * s.ny * s.nz
+        lhs, rhs = vdot(ldx, dy), vdot(dx, ady)
         tl_steps = WIN["n_steps"] * WIN["tl_sub"]
         res = {"tl_window_ms": tl_ms, "ad_window_ms": ad_ms, "dot_lhs": lhs, "dot_rhs": rhs,
                "dot_rel_err": abs(lhs - rhs) / max(abs(lhs), abs(rhs)), "dot_tol": tol,

@@ -1709,7 +1709,7 @@ __global__ void __launch_bounds__(128, 7) k_mx_hevi_col2(const __grid_constant__
 // every reader applies the implicit corrections from the final pi' itself
 // (defer_fix_w / defer_fix_rho). This kernel applies them to its own input
 // when apply_uv is set (its input is then a deferred substep's output); the
-// u/v kernel after a stage's last substep (k_mx_fix_col) and the finish
+// u/v kernel after a stage's last substep (k_mx_fix_a/_b) and the finish
 // kernel apply them to the last one. The parked sweep data shrinks from
 // w~, rho~ and the eliminated pi' to the eliminated pi' alone: 48 instead of
 // 64 bytes of traffic per cell and substep.
@@ -2006,44 +2006,44 @@ __global__ void __launch_bounds__(128, 7) k_mx_hevi_tmad(const __grid_constant__
 }
 
 // After a stage's last substep of the kDefer column kernel: its u/v backward
-// update (as fb_mom_body) and the w/rho' corrections, in place; one thread per
-// column walks the levels upward, so every value is read before it is replaced.
-__global__ void k_mx_fix_col(const __grid_constant__ Dims d, const __grid_constant__ Tab t,
-                             const __grid_constant__ Flags fl, const __grid_constant__ WS s, float dtau) {
+// update (as fb_mom_body) and the w/rho' corrections, in place, as two
+// launches: k_mx_fix_a updates u, v and rho' (reading w~ as the column
+// kernel left it), then k_mx_fix_b replaces w~ by w.
+__global__ void k_mx_fix_a(const __grid_constant__ Dims d, const __grid_constant__ Tab t,
+                           const __grid_constant__ Flags fl, const __grid_constant__ WS s, float dtau) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
-  if (i > d.nx || j > d.ny) return;
+  const int k = blockIdx.z;
+  if (i > d.nx || j > d.ny || k >= d.nz) return;
   const float* __restrict__ pn = s.f[PI];
   const float cp = (float)kCp;
-  const int nz = d.nz;
-  const bool col = i < d.nx && j < d.ny;
-  const float b = (float)fl.hevi_beta;
-  const float cb = dtau * b * cp, db = dtau * b;
-  float wprev = 0.f, pprev = 0.f;
-  if (col) {
-    wprev = s.f[W][IX(i, j, 0)];  // face 0 is final
-    pprev = pn[IX(i, j, 0)];
+  const size_t c = IX(i, j, k);
+  if (j < d.ny) {
+    const int ip = imin(i, d.nx - 1), im = imax(i - 1, 0);
+    s.f[U][c] = s.f[U][c] + dtau * (-cp * t.t0c[k] * (pn[IX(ip, j, k)] - pn[IX(im, j, k)]) * t.dx_inv);
   }
-  for (int k = 0; k < nz; ++k) {
-    const size_t c = IX(i, j, k);
-    if (j < d.ny) {
-      const int ip = imin(i, d.nx - 1), im = imax(i - 1, 0);
-      s.f[U][c] = s.f[U][c] + dtau * (-cp * t.t0c[k] * (pn[IX(ip, j, k)] - pn[IX(im, j, k)]) * t.dx_inv);
-    }
-    if (i < d.nx) {
-      const int jp = imin(j, d.ny - 1), jm = imax(j - 1, 0);
-      s.f[V][c] = s.f[V][c] + dtau * (-cp * t.t0c[k] * (pn[IX(i, jp, k)] - pn[IX(i, jm, k)]) * t.dy_inv);
-    }
-    if (col) {
-      const size_t c1 = IX(i, j, k + 1);
-      const float pk1 = (k + 1 < nz) ? pn[c1] : 0.f;
-      const float w1 = defer_fix_w(t, nz, cb, s.f[W][c1], pk1, pprev, k + 1);
-      s.f[RHO][c] = defer_fix_rho(t, db, s.f[RHO][c], wprev, w1, k);
-      if (k + 1 < nz) s.f[W][c1] = w1;
-      wprev = w1;
-      pprev = pk1;
-    }
+  if (i < d.nx) {
+    const int jp = imin(j, d.ny - 1), jm = imax(j - 1, 0);
+    s.f[V][c] = s.f[V][c] + dtau * (-cp * t.t0c[k] * (pn[IX(i, jp, k)] - pn[IX(i, jm, k)]) * t.dy_inv);
   }
+  if (i < d.nx && j < d.ny) {
+    const float b = (float)fl.hevi_beta, cb = dtau * b * cp, db = dtau * b;
+    const int nz = d.nz;
+    const float pk = pn[c], pkm = (k > 0) ? pn[IX(i, j, k - 1)] : 0.f, pk1 = (k + 1 < nz) ? pn[IX(i, j, k + 1)] : 0.f;
+    const float wk = defer_fix_w(t, nz, cb, s.f[W][c], pk, pkm, k);
+    const float wk1 = defer_fix_w(t, nz, cb, s.f[W][IX(i, j, k + 1)], pk1, pk, k + 1);
+    s.f[RHO][c] = defer_fix_rho(t, db, s.f[RHO][c], wk, wk1, k);
+  }
+}
+__global__ void k_mx_fix_b(const __grid_constant__ Dims d, const __grid_constant__ Tab t,
+                           const __grid_constant__ Flags fl, const __grid_constant__ WS s, float dtau) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y;
+  const int k = blockIdx.z + 1;  // faces 1 .. nz-1
+  if (i >= d.nx || j >= d.ny || k >= d.nz) return;
+  const size_t c = IX(i, j, k);
+  const float cb = dtau * (float)fl.hevi_beta * (float)kCp;
+  s.f[W][c] = defer_fix_w(t, d.nz, cb, s.f[W][c], s.f[PI][c], s.f[PI][IX(i, j, k - 1)], k);
 }
 
 size_t hevi_tma_smem_bytes(int nz) {
@@ -2465,7 +2465,8 @@ bool mixed_hevi_defers(const Dims& d) { return hevi_tma_variant(d) == 5; }
 
 void mixed_uv_fix(const Dims& d, const Tab& t, const Flags& fl, const WS& s, float dtau, cudaStream_t stream) {
   const dim3 b(32, 4);
-  k_mx_fix_col<<<dim3((d.nx + 32) / 32, (d.ny + 4) / 4), b, 0, stream>>>(d, t, fl, s, dtau);
+  k_mx_fix_a<<<g3(d.nx + 1, d.ny + 1, d.nz, b), b, 0, stream>>>(d, t, fl, s, dtau);
+  if (d.nz > 1) k_mx_fix_b<<<g3(d.nx, d.ny, d.nz - 1, b), b, 0, stream>>>(d, t, fl, s, dtau);
 }
 
 int mixed_hevi_substep(const Dims& d, const Tab& t, const Flags& fl, const WS& win, const WS& wout, float dtau,

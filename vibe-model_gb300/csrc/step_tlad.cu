@@ -91,11 +91,16 @@ struct B12 {  // writable fields: tangents out, or bars accumulated
 };
 
 // Loads. Tangent-linear: the derivative is the perturbation at the point.
+// Every loader also offers operator()(q, c, ref): the value minus a
+// reference, the difference taken in FP64 before the conversion, so FP32
+// arithmetic sees theta - theta0 (~1 K), not theta (~300 K).
 template <class R>
 struct TlLoad {
   const F12* s;
   const F12* p;
-  __device__ __forceinline__ Jet<R> operator()(int q, size_t c) { return {(R)s->f[q][c], (R)p->f[q][c]}; }
+  __device__ __forceinline__ Jet<R> operator()(int q, size_t c, double ref = 0.0) {
+    return {(R)(s->f[q][c] - ref), (R)p->f[q][c]};
+  }
 };
 // Adjoint pass: a unit derivative on load number `seed` only; remembers
 // which point that load read.
@@ -104,8 +109,8 @@ struct AdLoad {
   const F12* s;
   int seed, n, hq;
   size_t hc;
-  __device__ __forceinline__ Jet<R> operator()(int q, size_t c) {
-    Jet<R> r{(R)s->f[q][c], (R)0};
+  __device__ __forceinline__ Jet<R> operator()(int q, size_t c, double ref = 0.0) {
+    Jet<R> r{(R)(s->f[q][c] - ref), (R)0};
     if (n == seed) {
       r.d = (R)1;
       hq = q;
@@ -119,12 +124,15 @@ struct AdLoad {
 template <class R>
 struct ValLoad {
   const F12* s;
-  __device__ __forceinline__ Jet<R> operator()(int q, size_t c) { return {(R)s->f[q][c], (R)0}; }
+  __device__ __forceinline__ Jet<R> operator()(int q, size_t c, double ref = 0.0) {
+    return {(R)(s->f[q][c] - ref), (R)0};
+  }
 };
 
 constexpr int kMaxLoads = 48;  // more than any point function below reads
 
 #define LD(q, i, j, k) L((q), d.idx((i), (j), (k)))
+#define LDS(q, i, j, k, ref) L((q), d.idx((i), (j), (k)), (ref))
 #define LDC(q, i, j, k) L((q), d.idx(iclamp((i), 0, d.nx - 1), iclamp((j), 0, d.ny - 1), iclamp((k), 0, d.nz - 1)))
 
 __device__ __forceinline__ double dzeta_(const Metric& m, const Dims& d, int k) {
@@ -146,9 +154,8 @@ __device__ __forceinline__ double corf_(const Metric& m, const Flags& fl, const 
 template <class R, class Ld>
 __device__ __forceinline__ Jet<R> dpi_(const Dims& d, const Metric& m, const Flags& fl, Ld& L, int ia, int ja, int ka,
                                        int ib, int jb, int kb) {
-  const Jet<R> a = LD(PI, ia, ja, ka), b = LD(PI, ib, jb, kb);
-  if (!fl.pgf_pert) return a - b;
-  return (a - ref_(m.pi0, d, ia, ja, ka)) - (b - ref_(m.pi0, d, ib, jb, kb));
+  if (!fl.pgf_pert) return LD(PI, ia, ja, ka) - LD(PI, ib, jb, kb);
+  return LDS(PI, ia, ja, ka, ref_(m.pi0, d, ia, ja, ka)) - LDS(PI, ib, jb, kb, ref_(m.pi0, d, ib, jb, kb));
 }
 
 // u face (i, j, k), i = 0..nx: k_tend_u
@@ -167,8 +174,9 @@ __device__ __forceinline__ Jet<R> pt_u(const Dims& d, const Metric& m, const Fla
   const T wc = 0.5 * (LD(W, ip, j, k) + LD(W, ip, j, imin(k + 1, nz - 1)));
   T acc = -(uc * ux + vc * uy + wc * uz);
   if (fl.coriolis) acc = acc + corf_(m, fl, d, j) * vc;  // v at the u face: the same four points
-  const double t0 = fl.split_fast ? 0.5 * (ref_(m.th0, d, im, j, k) + ref_(m.th0, d, ip, j, k)) : 0.0;
-  const T th = 0.5 * (LD(THETA, im, j, k) + LD(THETA, ip, j, k)) - t0;
+  const bool sp = fl.split_fast;  // the slow part takes theta - theta0
+  const T th = 0.5 * (LDS(THETA, im, j, k, sp ? ref_(m.th0, d, im, j, k) : 0.0) +
+                      LDS(THETA, ip, j, k, sp ? ref_(m.th0, d, ip, j, k) : 0.0));
   return acc - kCp * (th * dpi_<R>(d, m, fl, L, ip, j, k, im, j, k)) * m.inv_dx;
 }
 
@@ -189,8 +197,9 @@ __device__ __forceinline__ Jet<R> pt_v(const Dims& d, const Metric& m, const Fla
   const T wc = 0.5 * (LD(W, i, jp, k) + LD(W, i, jp, imin(k + 1, nz - 1)));
   T acc = -(uc * vx + vc * vy + wc * vz);
   if (fl.coriolis) acc = acc - corf_(m, fl, d, j) * uc;
-  const double t0 = fl.split_fast ? 0.5 * (ref_(m.th0, d, i, jm, k) + ref_(m.th0, d, i, jp, k)) : 0.0;
-  const T th = 0.5 * (LD(THETA, i, jm, k) + LD(THETA, i, jp, k)) - t0;
+  const bool sp = fl.split_fast;
+  const T th = 0.5 * (LDS(THETA, i, jm, k, sp ? ref_(m.th0, d, i, jm, k) : 0.0) +
+                      LDS(THETA, i, jp, k, sp ? ref_(m.th0, d, i, jp, k) : 0.0));
   return acc - kCp * (th * dpi_<R>(d, m, fl, L, i, jp, k, i, jm, k)) * m.inv_dy;
 }
 
@@ -210,11 +219,12 @@ __device__ __forceinline__ Jet<R> pt_w(const Dims& d, const Metric& m, const Fla
   const T vc = 0.5 * (LD(V, i, j, kc) + LD(V, i, j + 1, kc));
   T acc = -(uc * wx + vc * wy + wc * wz);
   const double dz1 = dmax(dz, 1.0);
-  const double t0 = fl.split_fast ? 0.5 * (ref_(m.th0, d, i, j, km) + ref_(m.th0, d, i, j, kc)) : 0.0;
-  const T th = 0.5 * (LD(THETA, i, j, km) + LD(THETA, i, j, kc)) - t0;
+  const bool sp = fl.split_fast;
+  const T th = 0.5 * (LDS(THETA, i, j, km, sp ? ref_(m.th0, d, i, j, km) : 0.0) +
+                      LDS(THETA, i, j, kc, sp ? ref_(m.th0, d, i, j, kc) : 0.0));
   acc = acc - kCp * (th * dpi_<R>(d, m, fl, L, i, j, kc, i, j, km)) * (1.0 / dz1);
   const double th0 = ref_(m.th0, d, i, j, kc);
-  const T thp = LD(THETA, i, j, kc) - th0;
+  const T thp = LDS(THETA, i, j, kc, th0);
   const T qcond = LD(QC, i, j, kc) + LD(QR, i, j, kc) + LD(QI, i, j, kc) + LD(QS, i, j, kc) + LD(QG, i, j, kc);
   return acc + kG * (thp * (1.0 / dmax(th0, 1.0)) + kBuoyMoist * LD(QV, i, j, kc) - qcond);
 }
@@ -229,18 +239,21 @@ __device__ __forceinline__ Jet<R> pt_rho(const Dims& d, const Metric& m, const F
   const bool sp = fl.split_fast;
   const double* r0 = m.rho0;
   const double dz = dmax(dzeta_(m, d, k) * scale_(m, d, i, j), 1.0);
-  const T rc = LD(RHO, i, j, k);
-  auto lin = [&](int a0, int b0, int c0, int a1, int b1, int c1) {  // 0.5 (rho0(p0) + rho0(p1)) when split
-    return sp ? 0.5 * (ref_(r0, d, a0, b0, c0) + ref_(r0, d, a1, b1, c1)) : 0.0;
+  // rho at point p minus (with split) rho0 at point p0 (mass_div0 reads rho0
+  // at clamped neighbours where the flux reads rho's ghost line)
+  auto rr = [&](int a, int b, int c, int a0, int b0, int c0) {
+    return LDS(RHO, a, b, c, sp ? ref_(r0, d, a0, b0, c0) : 0.0);
   };
-  const T ex = 0.5 * (rc + LD(RHO, i + 1, j, k)) - lin(i, j, k, imin(i + 1, nx - 1), j, k);
-  const T wx = 0.5 * (LD(RHO, imax(i - 1, 0), j, k) + rc) - lin(imax(i - 1, 0), j, k, i, j, k);
+  const T rc = rr(i, j, k, i, j, k);
+  const T ex = 0.5 * (rc + rr(i + 1, j, k, imin(i + 1, nx - 1), j, k));
+  const T wx = 0.5 * (rr(imax(i - 1, 0), j, k, imax(i - 1, 0), j, k) + rc);
   const T fx = LD(U, i + 1, j, k) * ex - LD(U, i, j, k) * wx;
-  const T ny_ = 0.5 * (rc + LD(RHO, i, j + 1, k)) - lin(i, j, k, i, imin(j + 1, ny - 1), k);
-  const T sy = 0.5 * (LD(RHO, i, imax(j - 1, 0), k) + rc) - lin(i, imax(j - 1, 0), k, i, j, k);
+  const T ny_ = 0.5 * (rc + rr(i, j + 1, k, i, imin(j + 1, ny - 1), k));
+  const T sy = 0.5 * (rr(i, imax(j - 1, 0), k, i, imax(j - 1, 0), k) + rc);
   const T fy = LD(V, i, j + 1, k) * ny_ - LD(V, i, j, k) * sy;
-  const T tz = 0.5 * (rc + LD(RHO, i, j, imin(k + 1, nz - 1))) - lin(i, j, k, i, j, imin(k + 1, nz - 1));
-  const T bz = 0.5 * (LD(RHO, i, j, imax(k - 1, 0)) + rc) - lin(i, j, imax(k - 1, 0), i, j, k);
+  const int kp = imin(k + 1, nz - 1), km = imax(k - 1, 0);
+  const T tz = 0.5 * (rc + rr(i, j, kp, i, j, kp));
+  const T bz = 0.5 * (rr(i, j, km, i, j, km) + rc);
   const T fz = LD(W, i, j, k + 1) * tz - LD(W, i, j, k) * bz;
   return -(fx * m.inv_dx + fy * m.inv_dy + fz * (1.0 / dz));
 }
@@ -334,22 +347,24 @@ __device__ __forceinline__ Jet<R> weno_flux_(Jet<R> qm2, Jet<R> qm1, Jet<R> q0, 
 // accurate; a cell combines G with c and its own q without cancelling the
 // large c u terms of its faces (pt_wcell).
 template <class R, class Ld>
-__device__ __forceinline__ Jet<R> pt_wface(const Dims& d, Ld& L, int q, int dir, int i, int j, int k, R c) {
+__device__ __forceinline__ Jet<R> pt_wface(const Dims& d, Ld& L, int q, int dir, int i, int j, int k, double c) {
   Jet<R> z[5];
   int di = 0, dj = 0, dk = 0;
   if (dir == 0) di = 1;
   else if (dir == 1) dj = 1;
   else dk = 1;
 #pragma unroll
-  for (int m = 0; m < 5; ++m) z[m] = LDC(q, i + (m - 3) * di, j + (m - 3) * dj, k + (m - 3) * dk) - (double)c;
+  for (int m = 0; m < 5; ++m) {
+    const int a = iclamp(i + (m - 3) * di, 0, d.nx - 1), b = iclamp(j + (m - 3) * dj, 0, d.ny - 1);
+    z[m] = L(q, d.idx(a, b, iclamp(k + (m - 3) * dk, 0, d.nz - 1)), c);
+  }
   const Jet<R> vel = LD(dir == 0 ? U : (dir == 1 ? V : W), i, j, k);
   return weno_flux_<R>(z[0], z[1], z[2], z[3], z[4], vel);
 }
 // c of the face at index (i, j, k): q at the stencil's centre (the cell at
 // the face's index, clamped)
-template <class R>
-__device__ __forceinline__ R wface_shift(const Dims& d, const double* q, int i, int j, int k) {
-  return (R)q[d.idx(iclamp(i, 0, d.nx - 1), iclamp(j, 0, d.ny - 1), iclamp(k, 0, d.nz - 1))];
+__device__ __forceinline__ double wface_shift(const Dims& d, const double* q, int i, int j, int k) {
+  return q[d.idx(iclamp(i, 0, d.nx - 1), iclamp(j, 0, d.ny - 1), iclamp(k, 0, d.nz - 1))];
 }
 
 // faces that exist for direction dir at index (i, j, k)
@@ -384,13 +399,14 @@ __device__ __forceinline__ Jet<R> pt_wcell(const Dims& d, const Metric& m, const
   const bool vert = (k + 2 < d.nz || k >= 2);
   const bool adv = fl.weno_advective;
   T r{(R)0, (R)0};
+  const size_t oc = d.idx(i, j, k);
   auto face = [&](int dir, int a, int b, int c, double sgn, double inv) {
     const size_t o = d.idx(a, b, c);
     const T G{(R)F.v[dir][o], with_t ? (R)F.t[dir][o] : (R)0};
-    const R cf = (R)F.c[dir][o];
+    const double cf = F.c[dir][o];
     const T u = L(dir == 0 ? U : (dir == 1 ? V : W), o);
-    if (adv) r = r + (-sgn * inv) * G + (sgn * inv) * ((qc - (double)cf) * u);
-    else r = r + (-sgn * inv) * (G + u * (double)cf);
+    if (adv) r = r + (-sgn * inv) * G + (sgn * inv) * (L(q, oc, cf) * u);  // (q - c_f) u
+    else r = r + (-sgn * inv) * (G + u * cf);
   };
   face(0, i + 1, j, k, 1.0, m.inv_dx);
   face(0, i, j, k, -1.0, m.inv_dx);
@@ -446,7 +462,7 @@ __global__ void k_tl_wface(Dims d, const __grid_constant__ F12 b, const __grid_c
   const int k = blockIdx.z;
   if (i > d.nx || j > d.ny || k > d.nz) return;
   const size_t c = d.idx(i, j, k);
-  const R sh = wface_shift<R>(d, b.f[q], i, j, k);
+  const double sh = wface_shift(d, b.f[q], i, j, k);
   for (int dir = 0; dir < 3; ++dir) {
     if (!face_exists(d, dir, i, j, k)) continue;
     Jet<R> f;
@@ -459,7 +475,7 @@ __global__ void k_tl_wface(Dims d, const __grid_constant__ F12 b, const __grid_c
       f = pt_wface<R>(d, L, q, dir, i, j, k, sh);
     }
     F.v[dir][c] = (double)f.v;
-    F.c[dir][c] = (double)sh;
+    F.c[dir][c] = sh;
   }
 }
 
@@ -568,7 +584,7 @@ __global__ void k_ad_wface(Dims d, Metric m, Flags fl, const __grid_constant__ F
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
   const int k = blockIdx.z;
   if (i > d.nx || j > d.ny || k > d.nz) return;
-  const R sh = wface_shift<R>(d, b.f[q], i, j, k);
+  const double sh = wface_shift(d, b.f[q], i, j, k);
   for (int dir = 0; dir < 3; ++dir) {
     if (!face_exists(d, dir, i, j, k)) continue;
     const int li = i - (dir == 0), lj = j - (dir == 1), lk = k - (dir == 2);
@@ -594,10 +610,11 @@ __global__ void k_ad_wface(Dims d, Metric m, Flags fl, const __grid_constant__ F
     if (aR == 0.0 && aL == 0.0) continue;
     double extra;  // the wind's part beyond G
     if (fl.weno_advective) {
-      const R qR = hasR ? (R)b.f[q][d.idx(i, j, k)] : sh, qL = hasL ? (R)b.f[q][d.idx(li, lj, lk)] : sh;
-      extra = -(double)(qR - sh) * aR + (double)(qL - sh) * aL;
+      const R dR = hasR ? (R)(b.f[q][d.idx(i, j, k)] - sh) : (R)0;
+      const R dL = hasL ? (R)(b.f[q][d.idx(li, lj, lk)] - sh) : (R)0;
+      extra = -(double)dR * aR + (double)dL * aL;
     } else {
-      extra = (double)sh * lamG;
+      extra = sh * lamG;
     }
     const int vq = dir == 0 ? U : (dir == 1 ? V : W);
     AdLoad<R> L{&b, 0, 0, -1, 0};
