@@ -612,8 +612,9 @@ def main():
     ap.add_argument("--no-window", action="store_true", help="skip the TL/AD assimilation-window leg")
     ap.add_argument("--no-tune", action="store_true", help="skip the autotuner (built-in launch shapes)")
     ap.add_argument("--no-physics", action="store_true", help="skip the Kessler physics-coupling leg")
-    ap.add_argument("--only", choices=["all", "mixed", "fp64", "physics", "nest"], default="all",
-                    help="mixed / fp64: time that path only (no e2e, no other legs); physics / nest: that leg only")
+    ap.add_argument("--only", choices=["all", "mixed", "fp64", "physics", "nest", "si", "window"], default="all",
+                    help="mixed / fp64: time that path only (no e2e, no other legs); physics / nest / si / "
+                         "window: that leg only")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -647,6 +648,14 @@ def main():
         return
     if args.only == "nest":
         print(json.dumps({"only": "nest", "batched_nests": nest_leg(vg, torch, args.warmup)}))
+        ranks.close()
+        return
+    if args.only == "si":
+        print(json.dumps({"only": "si", "semi_implicit": si_leg(vg)}))
+        ranks.close()
+        return
+    if args.only == "window":
+        print(json.dumps({"only": "window", "assimilation_window": window_leg(vg, torch)}))
         ranks.close()
         return
     setup = case_setup(vg.Setup, args.nx, args.ny)
