@@ -294,7 +294,7 @@ def window_leg(vg, torch):
                 mx = m.state()
                 nl = np.sqrt(vdot(ldx, ldx))
                 fd = {}
-                for k in range(2, 8):
+                for k in range(2, 12):
                     e = 10.0 ** -k
                     m.set_state([a + e * b for a, b in zip(x0, dx)])
                     m.step(WIN["dt"], NSUB, WIN["n_steps"])
