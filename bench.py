@@ -785,9 +785,15 @@ def main():
     # algorithmic bytes per cell of one launch of each kernel class (FP32 fields 4 B, FP64 8 B):
     # stage: 56 (stage 1: win = w0), 84 (stage 2), 112 (stage 3, + its tendency);
     # column: read u v w rho pi, write w rho pi u v; finish: read S0, R3, 5 substep
-    # fields, 7 stage fields, write S1, W0; u/v in place: read u v pi, write u v
-    per_cell = {0: (56.0 + 84.0 + 112.0) / 3.0, 1: 40.0, 2: 216.0, 3: 20.0}
-    names = {0: "k_mx_stage", 1: "k_mx_hevi_tma", 2: "k_mx_finish", 3: "k_mx_fb_mom(u,v)"}
+    # fields, 7 stage fields, write S1, W0; after a stage's last substep, in
+    # place: u/v update (read u v pi, write u v) and, when the column kernel
+    # defers its w/rho' corrections (variant 5, the built-in one), those
+    # corrections too (+ read rho w, write rho; read w pi, write w)
+    col = tuning.get("column_kernel", -1) if isinstance(tuning, dict) else -1
+    defer = col in (-1, 5)
+    per_cell = {0: (56.0 + 84.0 + 112.0) / 3.0, 1: 40.0, 2: 216.0, 3: 44.0 if defer else 20.0}
+    names = {0: "k_mx_stage", 1: "k_mx_hevi_tmad" if defer else "k_mx_hevi_tma", 2: "k_mx_finish",
+             3: "k_mx_fix_a+k_mx_fix_b" if defer else "k_mx_fb_mom(u,v)"}
     dom = max(ktimes, key=lambda c: ktimes[c][0])
     tot_ms, spans = ktimes[dom]
     avg_s = tot_ms / max(spans, 1) * 1e-3

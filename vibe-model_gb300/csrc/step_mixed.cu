@@ -322,10 +322,6 @@ __device__ __forceinline__ void stage_body(const Dims& d, const Tab& t, const Fl
     const int lev = k - kb, cur = lev % kStageRing, nxt = (lev + 1) % kStageRing;
     const bool cells_here = k < nz;  // uniform across the block
     const int kc = imin(k, nz - 1);
-    __syncthreads();  // every thread is done with the slot of level k-1 (it takes level k+2)
-    if (tid == 0 && k + 2 <= ktop)
-      issue_level(M, sbuf[(lev + 2) % kStageRing], &sbar[(lev + 2) % kStageRing], i0, j0, k + 2, nz);
-    if (k + 2 <= ktop) hi = k + 2;
     // This level's global loads (the base state the stage adds its tendency
     // to, when it is not the input), issued before the wait for the next
     // level's boxes so that their latencies overlap it and one another.
@@ -349,6 +345,11 @@ __device__ __forceinline__ void stage_body(const Dims& d, const Tab& t, const Fl
       if (!level_ready(k + 1)) break;
       if (edge) fix_level(sbuf[nxt]);
     }
+    // past that barrier every thread is done with level k-1 (its values of
+    // the level below live in registers), so its slot takes level k+2
+    if (tid == 0 && k + 2 <= ktop)
+      issue_level(M, sbuf[(lev + 2) % kStageRing], &sbar[(lev + 2) % kStageRing], i0, j0, k + 2, nz);
+    if (k + 2 <= ktop) hi = k + 2;
     float* const buf = sbuf[cur];
     const float* const sT = buf + tile_off(TT);
     const float* const sQ = buf + tile_off(TQ);
@@ -501,6 +502,42 @@ __device__ __forceinline__ void stage_body(const Dims& d, const Tab& t, const Fl
         }
       }
     };
+    // theta' and qv together: the 2 x (TY (TX+1) + (TY+1) TX) faces of both
+    // species are dealt out evenly over the block's threads (4 or 5 each;
+    // per species, TY (TX+1) and (TY+1) TX exceed NT by 8 and 32 faces, so
+    // one warp would do twice the others' work before the barrier), and x
+    // and y faces share one WENO evaluation with the stencil stride chosen
+    // per face, so a warp holding both kinds does not diverge around it.
+    // Same face values as hflux.
+    auto hflux2 = [&](const float* Q0, const float* Q1) {
+      constexpr int NXF = TY * (TX + 1), NF = NXF + (TY + 1) * TX;
+      for (int e = tid; e < 2 * NF; e += NT) {
+        const int slot = e >= NF ? 1 : 0;
+        const int r = e - slot * NF;
+        int off, st;
+        float vel;
+        bool valid;
+        float* dst;
+        if (r < NXF) {
+          const int fr = r / (TX + 1), ff = r - fr * (TX + 1);
+          off = (fr + 3) * TW + ff + XO;  // cell i0+ff, the face's right cell
+          st = 1;
+          vel = sU[(fr + 1) * TW + ff + XO];
+          valid = i0 + ff <= nx && j0 + fr < ny;
+          dst = &sFx[slot][r];
+        } else {
+          const int r2 = r - NXF, fg = r2 / TX, fcl = r2 - fg * TX;
+          off = (fg + 3) * TW + fcl + XO;
+          st = TW;
+          vel = sV[(fg + 1) * TW + fcl + XO];
+          valid = j0 + fg <= ny && i0 + fcl < nx;
+          dst = &sFy[slot][r2];
+        }
+        const float* qq = (slot ? Q1 : Q0) + off;  // in the box for every face of the tile
+        const float F = weno_face_f(qq[-3 * st], qq[-2 * st], qq[-st], qq[0], qq[st], vel);
+        *dst = valid ? F : 0.f;
+      }
+    };
     auto scalar = [&](int q, const float* Q, int slot, float z0, float z1, float z2, float z4, float z5, float* fc,
                       float fc_shift) {
       float r = 0.f;
@@ -540,8 +577,7 @@ __device__ __forceinline__ void stage_body(const Dims& d, const Tab& t, const Fl
     // w*(theta0(k-1) - theta0(k)) = -w*(theta0(k) - theta0(k-1)).
     const float tshift = (k > 0) ? -t.t0d[6 * (k - 1) + 4] : 0.f;
     if (f_weno) {
-      hflux(sT, 0);
-      hflux(sQ, 1);
+      hflux2(sT, sQ);
       __syncthreads();
     }
     scalar(THETA, sT, 0, wT[0] + sh[0], wT[1] + sh[1], wT[2] + sh[2], wT[4] + sh[4], wT[5] + sh[5], &fcT, tshift);
