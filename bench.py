@@ -737,7 +737,10 @@ def main():
     p_in, p_out = [p.data_ptr() for p in pin_in], [p.data_ptr() for p in pin_out]
     mx.get_state_ptrs(p_in)
     mx.sync()
-    e2e_steps = max(6, args.steps // 2)
+    # every step starts from the same host input, so the run can be long
+    # enough that the pipeline's fill (the first upload) and drain (the last
+    # download) do not dominate
+    e2e_steps = max(6, 2 * args.steps)
     ext = torch.cuda.ExternalStream(mx.stream())
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     mx.step_io(p_in, p_out, DT, NSUB)  # sets up the pipeline's streams and staging buffers

@@ -2045,11 +2045,11 @@ __global__ void __launch_bounds__(128, 7) k_mx_hevi_tmad(const __grid_constant__
 // update (as fb_mom_body) and the w/rho' corrections, in place, as two
 // launches: k_mx_fix_a updates u, v and rho' (reading w~ as the column
 // kernel left it), then k_mx_fix_b replaces w~ by w.
-__global__ void k_mx_fix_a(const __grid_constant__ Dims d, const __grid_constant__ Tab t,
-                           const __grid_constant__ Flags fl, const __grid_constant__ WS s, float dtau) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  const int j = blockIdx.y * blockDim.y + threadIdx.y;
-  const int k = blockIdx.z;
+__device__ __forceinline__ void fix_a_body(const Dims& d, const Tab& t, const Flags& fl, const WS& s, float dtau,
+                                           int bx, int by, int bz) {
+  const int i = bx * blockDim.x + threadIdx.x;
+  const int j = by * blockDim.y + threadIdx.y;
+  const int k = bz;
   if (i > d.nx || j > d.ny || k >= d.nz) return;
   const float* __restrict__ pn = s.f[PI];
   const float cp = (float)kCp;
@@ -2071,15 +2071,23 @@ __global__ void k_mx_fix_a(const __grid_constant__ Dims d, const __grid_constant
     s.f[RHO][c] = defer_fix_rho(t, db, s.f[RHO][c], wk, wk1, k);
   }
 }
-__global__ void k_mx_fix_b(const __grid_constant__ Dims d, const __grid_constant__ Tab t,
-                           const __grid_constant__ Flags fl, const __grid_constant__ WS s, float dtau) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  const int j = blockIdx.y * blockDim.y + threadIdx.y;
-  const int k = blockIdx.z + 1;  // faces 1 .. nz-1
+__device__ __forceinline__ void fix_b_body(const Dims& d, const Tab& t, const Flags& fl, const WS& s, float dtau,
+                                           int bx, int by, int bz) {
+  const int i = bx * blockDim.x + threadIdx.x;
+  const int j = by * blockDim.y + threadIdx.y;
+  const int k = bz + 1;  // faces 1 .. nz-1
   if (i >= d.nx || j >= d.ny || k >= d.nz) return;
   const size_t c = IX(i, j, k);
   const float cb = dtau * (float)fl.hevi_beta * (float)kCp;
   s.f[W][c] = defer_fix_w(t, d.nz, cb, s.f[W][c], s.f[PI][c], s.f[PI][IX(i, j, k - 1)], k);
+}
+__global__ void k_mx_fix_a(const __grid_constant__ Dims d, const __grid_constant__ Tab t,
+                           const __grid_constant__ Flags fl, const __grid_constant__ WS s, float dtau) {
+  fix_a_body(d, t, fl, s, dtau, blockIdx.x, blockIdx.y, blockIdx.z);
+}
+__global__ void k_mx_fix_b(const __grid_constant__ Dims d, const __grid_constant__ Tab t,
+                           const __grid_constant__ Flags fl, const __grid_constant__ WS s, float dtau) {
+  fix_b_body(d, t, fl, s, dtau, blockIdx.x, blockIdx.y, blockIdx.z);
 }
 
 size_t hevi_tma_smem_bytes(int nz) {
@@ -2565,6 +2573,7 @@ struct HeviArgs {  // 64-byte aligned through its CUtensorMap members
 struct UvArgs {
   Dims d;
   Tab t;
+  Flags fl;
   WS win, wout;
   float dtau;
   int gx, gy, gz;
@@ -2577,7 +2586,7 @@ struct FinishArgs {
   float dtf, uv_dtau;  // uv_dtau: stage 3's last u/v update, applied in the finish
   CS64 s0;
   MS64 s1;
-  int gx, gy, gz;
+  int gx, gy, gz, defer;
 };
 
 __device__ __forceinline__ int find_domain(const int* __restrict__ start, int nd) {
@@ -2614,11 +2623,32 @@ __global__ void __launch_bounds__(128, 7) k_b_hevi_tma(const HeviArgs* __restric
                 l / a.gx);
 }
 
+__global__ void __launch_bounds__(128, 7) k_b_hevi_tmad(const HeviArgs* __restrict__ A,
+                                                        const int* __restrict__ start, int nd, unsigned* err) {
+  const int dom = find_domain(start, nd);
+  const HeviArgs& a = A[dom];
+  const int l = (int)blockIdx.x - start[dom];
+  hevi_tma_body<true>(a.d, a.t, a.fl, a.C, a.win, a.wout, a.dtau, a.lu, a.apply_uv, a.cdx, a.cdy, err, l % a.gx,
+                      l / a.gx);
+}
+
 __global__ void k_b_uv(const UvArgs* __restrict__ A, const int* __restrict__ start, int nd) {
   const int dom = find_domain(start, nd);
   const UvArgs& a = A[dom];
   const int l = (int)blockIdx.x - start[dom];
   fb_mom_body(a.d, a.t, a.win, a.wout, a.dtau, 0, l % a.gx, (l / a.gx) % a.gy, l / (a.gx * a.gy));
+}
+__global__ void k_b_fix_a(const UvArgs* __restrict__ A, const int* __restrict__ start, int nd) {
+  const int dom = find_domain(start, nd);
+  const UvArgs& a = A[dom];
+  const int l = (int)blockIdx.x - start[dom];
+  fix_a_body(a.d, a.t, a.fl, a.wout, a.dtau, l % a.gx, (l / a.gx) % a.gy, l / (a.gx * a.gy));
+}
+__global__ void k_b_fix_b(const UvArgs* __restrict__ A, const int* __restrict__ start, int nd) {
+  const int dom = find_domain(start, nd);
+  const UvArgs& a = A[dom];
+  const int l = (int)blockIdx.x - start[dom];
+  fix_b_body(a.d, a.t, a.fl, a.wout, a.dtau, l % a.gx, (l / a.gx) % a.gy, l / (a.gx * a.gy));
 }
 
 __global__ void k_b_finish(const FinishArgs* __restrict__ A, const int* __restrict__ start, int nd, unsigned* err) {
@@ -2626,7 +2656,7 @@ __global__ void k_b_finish(const FinishArgs* __restrict__ A, const int* __restri
   const FinishArgs& a = A[dom];
   const int l = (int)blockIdx.x - start[dom];
   finish_body(a.d, a.t, a.fl, a.wfin, a.wst, a.w0, a.rin, a.dtf, a.s0, a.s1, err, l % a.gx, (l / a.gx) % a.gy,
-              l / (a.gx * a.gy), a.uv_dtau);
+              l / (a.gx * a.gy), a.uv_dtau, a.defer != 0);
 }
 
 WS ws_from(float* const* a) {
@@ -2644,7 +2674,7 @@ WS ws_mix(float* const* sub, float* const* stage) {  // acoustic fields from sub
 
 struct MixedBatch {
   struct Launch {
-    int kind = 0;  // 0 stage, 1 column, 2 u/v, 3 finish
+    int kind = 0;  // 0 stage, 1 column, 2 u/v (with deferral: u/v/rho' fix-up), 3 finish, 4 w fix-up
     int raw = 0, nd = 0, blocks = 0;
     void* args = nullptr;
     int* start = nullptr;
@@ -2653,6 +2683,7 @@ struct MixedBatch {
   std::vector<void*> allocs;
   size_t hevi_smem = 0;
   bool hevi_tma = false;  // TMA-fed column body (else the cp.async two-column body)
+  bool defer = false;     // the TMA body defers its w/rho' corrections (u/v launches become fix-ups)
   unsigned* err = nullptr;
 };
 
@@ -2687,6 +2718,7 @@ MixedBatch* mixed_batch_build(const std::vector<MixedDomain>& doms, const Flags&
   auto* b = new MixedBatch();
   b->err = err;
   b->hevi_tma = hevi_tma() && hevi_tma_smem_bytes(nz) <= 48 * 1024;
+  b->defer = b->hevi_tma && hevi_defer();
   b->hevi_smem = b->hevi_tma ? hevi_tma_smem_bytes(nz) : hevi2_smem_bytes(nz, kBatchTwoRing);
   const double dts[3] = {dt / 3.0, dt / 2.0, dt};
   const int nd = (int)doms.size();
@@ -2753,6 +2785,7 @@ MixedBatch* mixed_batch_build(const std::vector<MixedDomain>& doms, const Flags&
       UvArgs& a = ua[q];
       a.d = m.d;
       a.t = m.t;
+      a.fl = fl;
       a.win = ws_from(sub_out(m, n_sub - 1));
       a.wout = a.win;
       a.dtau = dtau;
@@ -2763,6 +2796,18 @@ MixedBatch* mixed_batch_build(const std::vector<MixedDomain>& doms, const Flags&
       ub += a.gx * a.gy * a.gz;
     }
     ok = ok && upload_launch(b, 2, 0, ua, start, ub);
+    if (b->defer && nz > 1) {  // the w corrections, after the u/v/rho' launch
+      int wb = 0;
+      for (int q = 0; q < nd; ++q) {
+        UvArgs& a = ua[q];
+        a.gx = ceil_div(a.d.nx, 32);
+        a.gy = ceil_div(a.d.ny, 4);
+        a.gz = a.d.nz - 1;
+        start[q] = wb;
+        wb += a.gx * a.gy * a.gz;
+      }
+      ok = ok && upload_launch(b, 4, 0, ua, start, wb);
+    }
   }
   if (ok) {
     std::vector<FinishArgs> fa(nd);
@@ -2782,6 +2827,7 @@ MixedBatch* mixed_batch_build(const std::vector<MixedDomain>& doms, const Flags&
       a.uv_dtau = (float)(dt / (double)n_sub);
       a.s0 = cs64(m.S0);
       a.s1 = ms64(m.S1);
+      a.defer = b->defer ? 1 : 0;
       a.gx = ceil_div(m.d.nx + 1, 32);
       a.gy = ceil_div(m.d.ny + 1, 4);
       a.gz = m.d.nz + 1;
@@ -2807,13 +2853,19 @@ void mixed_batch_enqueue(const MixedBatch* b, cudaStream_t s) {
           k_b_stage<false><<<L.blocks, dim3(TX, TY), 0, s>>>((const StageArgs*)L.args, L.start, L.nd, b->err);
         break;
       case 1:
-        if (b->hevi_tma)
+        if (b->defer)
+          k_b_hevi_tmad<<<L.blocks, dim3(32, 4), b->hevi_smem, s>>>((const HeviArgs*)L.args, L.start, L.nd, b->err);
+        else if (b->hevi_tma)
           k_b_hevi_tma<<<L.blocks, dim3(32, 4), b->hevi_smem, s>>>((const HeviArgs*)L.args, L.start, L.nd, b->err);
         else
           k_b_hevi<<<L.blocks, dim3(32, 4), b->hevi_smem, s>>>((const HeviArgs*)L.args, L.start, L.nd);
         break;
       case 2:
-        k_b_uv<<<L.blocks, dim3(32, 4), 0, s>>>((const UvArgs*)L.args, L.start, L.nd);
+        if (b->defer) k_b_fix_a<<<L.blocks, dim3(32, 4), 0, s>>>((const UvArgs*)L.args, L.start, L.nd);
+        else k_b_uv<<<L.blocks, dim3(32, 4), 0, s>>>((const UvArgs*)L.args, L.start, L.nd);
+        break;
+      case 4:
+        k_b_fix_b<<<L.blocks, dim3(32, 4), 0, s>>>((const UvArgs*)L.args, L.start, L.nd);
         break;
       default:
         k_b_finish<<<L.blocks, dim3(32, 4), 0, s>>>((const FinishArgs*)L.args, L.start, L.nd, b->err);
