@@ -59,8 +59,10 @@ template <typename T>
 int mg_set_coefficients(MgSolver<T>* m, const double* a, const double* b, cudaStream_t s);
 // approximately solves A d = r64 / scale (FP64 in, FP64 out scaled back):
 // BiCGSTAB in T to relative tolerance rtol or max_iter iterations.
+// r_norm2: (r64, r64) when the caller has it, else negative (computed here).
 // Returns the iterations done (negative on breakdown).
 template <typename T>
-int mg_solve(MgSolver<T>* m, const double* r64, double* d64, double rtol, int max_iter, cudaStream_t s);
+int mg_solve(MgSolver<T>* m, const double* r64, double* d64, double rtol, int max_iter, cudaStream_t s,
+             double r_norm2 = -1.0);
 
 }  // namespace vgb

@@ -203,7 +203,8 @@ int mg_refined(vibe_helmholtz* h, const double* f, double* x, cudaStream_t s) {
     if (!hdot(h, r, r, s, rn)) return VIBE_C_ERR_DEVICE;
     rel = (fnorm > 0.0) ? std::sqrt(rn) / fnorm : std::sqrt(rn);
     if (!(rel >= h->tol) || pass == kMaxRefinements) break;  // converged, or NaN
-    const int it = fp32 ? mg_solve(h->mg32, r, dx, rtol, h->max_iter, s) : mg_solve(h->mg64, r, dx, rtol, h->max_iter, s);
+    const int it = fp32 ? mg_solve(h->mg32, r, dx, rtol, h->max_iter, s, rn)
+                        : mg_solve(h->mg64, r, dx, rtol, h->max_iter, s, rn);
     if (it == -1 && cudaGetLastError() != cudaSuccess) return VIBE_C_ERR_DEVICE;
     total += it < 0 ? -it : it;
     vop_add(x, dx, n, s);
