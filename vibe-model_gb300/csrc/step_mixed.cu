@@ -80,6 +80,89 @@ __device__ __forceinline__ float weno_face_f(float qm2, float qm1, float q0, flo
   return 0.5f * (vel * (ql + qr) - 1e-3f * (qr - ql));
 }
 
+// ---- theta' and qv side by side: packed FP32 pairs ----
+// The stage kernel reconstructs theta' and qv at the same faces with the
+// same velocity, so their WENO5 arithmetic runs on f32x2 pairs (low:
+// theta', high: qv): one add/mul/fma.rn.f32x2 does both species' operation,
+// each lane IEEE-rounded as the scalar instruction would be.
+struct F2 {
+  unsigned long long r;
+};
+__device__ __forceinline__ F2 mk2(float a, float b) {
+  F2 o;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(o.r) : "f"(a), "f"(b));
+  return o;
+}
+__device__ __forceinline__ F2 dup2(float a) { return mk2(a, a); }
+__device__ __forceinline__ void un2(F2 x, float& a, float& b) { asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(x.r)); }
+__device__ __forceinline__ F2 add2(F2 a, F2 b) {
+  F2 o;
+  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(o.r) : "l"(a.r), "l"(b.r));
+  return o;
+}
+__device__ __forceinline__ F2 sub2(F2 a, F2 b) {
+  F2 o;
+  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(o.r) : "l"(a.r), "l"(b.r));
+  return o;
+}
+__device__ __forceinline__ F2 mul2(F2 a, F2 b) {
+  F2 o;
+  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(o.r) : "l"(a.r), "l"(b.r));
+  return o;
+}
+__device__ __forceinline__ F2 fma2(F2 a, F2 b, F2 c) {
+  F2 o;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(o.r) : "l"(a.r), "l"(b.r), "l"(c.r));
+  return o;
+}
+__device__ __forceinline__ F2 sel2(bool p, F2 a, F2 b) { return p ? a : b; }
+
+// WENO5 left-biased reconstruction of the stencil a0..a4 (centre a2) with
+// smoothness indicators s0..s2, as weno_left; the candidates are formed at
+// 6x and the 1/6 folded into the normalisation
+__device__ __forceinline__ F2 weno_left2(F2 a0, F2 a1, F2 a2, F2 a3, F2 a4, F2 s0, F2 s1, F2 s2) {
+  const F2 V0 = fma2(dup2(11.f), a2, fma2(dup2(-7.f), a1, add2(a0, a0)));
+  const F2 V1 = fma2(dup2(5.f), a2, sub2(add2(a3, a3), a1));
+  const F2 V2 = sub2(fma2(dup2(5.f), a3, add2(a2, a2)), a4);
+  const F2 p01 = mul2(s0, s1), p02 = mul2(s0, s2), p12 = mul2(s1, s2);
+  const F2 w0 = mul2(dup2(0.1f), mul2(p12, p12)), w1 = mul2(dup2(0.6f), mul2(p02, p02));
+  const F2 w2 = mul2(dup2(0.3f), mul2(p01, p01));
+  const F2 num = fma2(w2, V2, fma2(w1, V1, mul2(w0, V0)));
+  float d0, d1;
+  un2(mul2(dup2(6.f), add2(add2(w0, w1), w2)), d0, d1);
+  float i0, i1;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(i0) : "f"(d0));
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(i1) : "f"(d1));
+  return mul2(num, mk2(i0, i1));
+}
+// WENO5 face flux of a pair (local Lax-Friedrichs, as weno_face_f) from the
+// stencil in upwind order: qm2 qm1 q0 q1 q2 for vel >= 0, its mirror image
+// q2 q1 q0 qm1 qm2 for vel < 0 (centre q0 either way). The smoothness
+// indicators of the mirrored stencil are the original ones in reverse
+// order, so the caller's choice of load addresses replaces the selects.
+__device__ __forceinline__ F2 weno_flux2(F2 a0, F2 a1, F2 a2, F2 a3, F2 a4, float vel) {
+  const F2 eps = dup2(1e-6f), c1312 = dup2(13.f / 12.f), q25 = dup2(0.25f), m2 = dup2(-2.f), m4 = dup2(-4.f),
+           c3 = dup2(3.f);
+  const F2 e0 = add2(fma2(m2, a1, a0), a2), f0 = fma2(c3, a2, fma2(m4, a1, a0));
+  const F2 e1 = add2(fma2(m2, a2, a1), a3), f1 = sub2(a1, a3);
+  const F2 e2 = add2(fma2(m2, a3, a2), a4), f2 = fma2(m4, a3, fma2(c3, a2, a4));
+  const F2 s0 = fma2(q25, mul2(f0, f0), fma2(c1312, mul2(e0, e0), eps));
+  const F2 s1 = fma2(q25, mul2(f1, f1), fma2(c1312, mul2(e1, e1), eps));
+  const F2 s2 = fma2(q25, mul2(f2, f2), fma2(c1312, mul2(e2, e2), eps));
+  const F2 rec = weno_left2(a0, a1, a2, a3, a4, s0, s1, s2);
+  if (fabsf(vel) >= 1e-3f) return mul2(dup2(vel), rec);
+  const F2 oth = weno_left2(a4, a3, a2, a1, a0, s2, s1, s0);  // the other side
+  const bool up = vel >= 0.f;
+  const F2 ql = sel2(up, rec, oth), qr = sel2(up, oth, rec);
+  return mul2(dup2(0.5f), sub2(mul2(dup2(vel), add2(ql, qr)), mul2(dup2(1e-3f), sub2(qr, ql))));
+}
+// the pair's flux through a vertical face from the column's values
+// qm2..q2 in bottom-to-top order (the face between q0 and q1)
+__device__ __forceinline__ F2 weno_vflux2(F2 qm2, F2 qm1, F2 q0, F2 q1, F2 q2, float vel) {
+  const bool up = vel >= 0.f;
+  return weno_flux2(sel2(up, qm2, q2), sel2(up, qm1, q1), q0, sel2(up, q1, qm1), sel2(up, q2, qm2), vel);
+}
+
 __device__ __forceinline__ float gradc(float m3, float m2, float m1, float p1, float p2, float p3, float inv, int order) {
   switch (order) {
     case 4: return (m2 - 8.f * m1 + 8.f * p1 - p2) * (inv * (1.f / 12.f));
@@ -502,51 +585,57 @@ __device__ __forceinline__ void stage_body(const Dims& d, const Tab& t, const Fl
         }
       }
     };
-    // theta' and qv together: the 2 x (TY (TX+1) + (TY+1) TX) faces of both
-    // species are dealt out evenly over the block's threads (4 or 5 each;
-    // per species, TY (TX+1) and (TY+1) TX exceed NT by 8 and 32 faces, so
-    // one warp would do twice the others' work before the barrier), and x
-    // and y faces share one WENO evaluation with the stencil stride chosen
-    // per face, so a warp holding both kinds does not diverge around it.
-    // Same face values as hflux.
-    auto hflux2 = [&](const float* Q0, const float* Q1) {
+    // theta' and qv together: every face of the tile, TY (TX+1) x faces and
+    // (TY+1) TX y faces, reconstructs both species as one f32x2 pair (same
+    // face velocity, same stencil addresses in the two boxes), the stencil
+    // loaded in upwind order by choosing the addresses; x and y faces share
+    // one code path with the stencil stride chosen per face. Same face values
+    // as hflux up to rounding.
+    auto hflux_pair = [&]() {
       constexpr int NXF = TY * (TX + 1), NF = NXF + (TY + 1) * TX;
-      for (int e = tid; e < 2 * NF; e += NT) {
-        const int slot = e >= NF ? 1 : 0;
-        const int r = e - slot * NF;
-        int off, st;
+      for (int e = tid; e < NF; e += NT) {
+        int off, st, dst;
         float vel;
         bool valid;
-        float* dst;
-        if (r < NXF) {
-          const int fr = r / (TX + 1), ff = r - fr * (TX + 1);
-          off = (fr + 3) * TW + ff + XO;  // cell i0+ff, the face's right cell
+        if (e < NXF) {
+          const int fr = e / (TX + 1), ff = e - fr * (TX + 1);
+          off = (fr + 3) * TW + ff + XO - 1;  // cell i0+ff-1, left of the face
           st = 1;
           vel = sU[(fr + 1) * TW + ff + XO];
           valid = i0 + ff <= nx && j0 + fr < ny;
-          dst = &sFx[slot][r];
+          dst = e;
         } else {
-          const int r2 = r - NXF, fg = r2 / TX, fcl = r2 - fg * TX;
-          off = (fg + 3) * TW + fcl + XO;
+          const int r2 = e - NXF, fg = r2 / TX, fcl = r2 - fg * TX;
+          off = (fg + 2) * TW + fcl + XO;  // cell j0+fg-1, below the face
           st = TW;
           vel = sV[(fg + 1) * TW + fcl + XO];
           valid = j0 + fg <= ny && i0 + fcl < nx;
-          dst = &sFy[slot][r2];
+          dst = r2;
         }
-        const float* qq = (slot ? Q1 : Q0) + off;  // in the box for every face of the tile
-        const float F = weno_face_f(qq[-3 * st], qq[-2 * st], qq[-st], qq[0], qq[st], vel);
-        *dst = valid ? F : 0.f;
+        const int sp = vel >= 0.f ? st : -st;  // upwind order
+        const F2 a0 = mk2(sT[off - 2 * sp], sQ[off - 2 * sp]), a1 = mk2(sT[off - sp], sQ[off - sp]);
+        const F2 a2 = mk2(sT[off], sQ[off]), a3 = mk2(sT[off + sp], sQ[off + sp]);
+        const F2 a4 = mk2(sT[off + 2 * sp], sQ[off + 2 * sp]);
+        float Ft, Fq;
+        un2(weno_flux2(a0, a1, a2, a3, a4, vel), Ft, Fq);
+        if (!valid) Ft = Fq = 0.f;
+        if (e < NXF) {
+          sFx[0][dst] = Ft;
+          sFx[1][dst] = Fq;
+        } else {
+          sFy[0][dst] = Ft;
+          sFy[1][dst] = Fq;
+        }
       }
     };
-    auto scalar = [&](int q, const float* Q, int slot, float z0, float z1, float z2, float z4, float z5, float* fc,
-                      float fc_shift) {
+    // species q's tendency from its horizontal face fluxes (slot) and its
+    // vertical ones: ft through the top face, fb through the bottom face
+    // (WENO), or the column values z2 = q(k-1), z4 = q(k+1) (central)
+    auto scalar = [&](int q, const float* Q, int slot, float ft, float fb, float z2, float z4) {
       float r = 0.f;
       const float qc = Q[o3];
       if (f_weno) {
         if (cell) {
-          const float ft = weno_face_f(z1, z2, qc, z4, z5, wt);
-          const float fb = (fc != nullptr && k > kb) ? *fc + wk * fc_shift : weno_face_f(z0, z1, z2, qc, z4, wk);
-          if (fc != nullptr) *fc = ft;
           const float fe = sFx[slot][ty * (TX + 1) + tx + 1], fw = sFx[slot][ty * (TX + 1) + tx];
           const float fn = sFy[slot][(ty + 1) * TX + tx], fs = sFy[slot][ty * TX + tx];
           r = -(fe - fw) * t.dx_inv - (fn - fs) * t.dy_inv;
@@ -576,12 +665,27 @@ __device__ __forceinline__ void stage_body(const Dims& d, const Tab& t, const Fl
     // is the flux of q plus w*s, so it is corrected by
     // w*(theta0(k-1) - theta0(k)) = -w*(theta0(k) - theta0(k-1)).
     const float tshift = (k > 0) ? -t.t0d[6 * (k - 1) + 4] : 0.f;
+    float ftT = 0.f, fbT = 0.f, ftQ = 0.f, fbQ = 0.f;  // vertical face fluxes of theta' and qv
     if (f_weno) {
-      hflux2(sT, sQ);
+      hflux_pair();
+      if (cell) {  // the top face's pair, carried up as the next level's bottom face
+        const F2 z1 = mk2(wT[1] + sh[1], wQ[1]), z2 = mk2(wT[2] + sh[2], wQ[2]);
+        const F2 z4 = mk2(wT[4] + sh[4], wQ[4]), z5 = mk2(wT[5] + sh[5], wQ[5]);
+        const F2 qc = mk2(sT[o3], sQ[o3]);
+        un2(weno_vflux2(z1, z2, qc, z4, z5, wt), ftT, ftQ);
+        if (k > kb) {
+          fbT = fcT + wk * tshift;
+          fbQ = fcQ;
+        } else {
+          un2(weno_vflux2(mk2(wT[0] + sh[0], wQ[0]), z1, z2, qc, z4, wk), fbT, fbQ);
+        }
+        fcT = ftT;
+        fcQ = ftQ;
+      }
       __syncthreads();
     }
-    scalar(THETA, sT, 0, wT[0] + sh[0], wT[1] + sh[1], wT[2] + sh[2], wT[4] + sh[4], wT[5] + sh[5], &fcT, tshift);
-    scalar(QV, sQ, 1, wQ[0], wQ[1], wQ[2], wQ[4], wQ[5], &fcQ, 0.f);
+    scalar(THETA, sT, 0, ftT, fbT, wT[2] + sh[2], wT[4] + sh[4]);
+    scalar(QV, sQ, 1, ftQ, fbQ, wQ[2], wQ[4]);
     if (f_moist) {
       for (int q = QC; q <= QG; ++q) {
         __syncthreads();  // sQm and the flux slots are no longer read
@@ -592,11 +696,17 @@ __device__ __forceinline__ void stage_body(const Dims& d, const Tab& t, const Fl
           __syncthreads();
         }
         float z[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+        float ft = 0.f, fb = 0.f;
         if (cell) {
 #pragma unroll
           for (int m = 0; m < 6; ++m) z[m] = win.f[q][(size_t)iclamp(k + m - 3, 0, nz - 1) * pl + colc];
+          if (f_weno) {
+            const float qc = sQm[o3];
+            ft = weno_face_f(z[1], z[2], qc, z[4], z[5], wt);
+            fb = weno_face_f(z[0], z[1], z[2], qc, z[4], wk);
+          }
         }
-        scalar(q, sQm, 0, z[0], z[1], z[2], z[4], z[5], nullptr, 0.f);
+        scalar(q, sQm, 0, ft, fb, z[2], z[4]);
       }
     }
     // slide the column registers up one level
