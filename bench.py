@@ -791,12 +791,12 @@ def main():
     # fields, 7 stage fields, write S1, W0; after a stage's last substep, in
     # place: u/v update (read u v pi, write u v) and, when the column kernel
     # defers its w/rho' corrections (variant 5, the built-in one), those
-    # corrections too (+ read rho w, write rho; read w pi, write w)
+    # corrections too in the same column march (+ read w rho, write w rho)
     col = tuning.get("column_kernel", -1) if isinstance(tuning, dict) else -1
     defer = col in (-1, 5)
-    per_cell = {0: (56.0 + 84.0 + 112.0) / 3.0, 1: 40.0, 2: 216.0, 3: 44.0 if defer else 20.0}
+    per_cell = {0: (56.0 + 84.0 + 112.0) / 3.0, 1: 40.0, 2: 216.0, 3: 36.0 if defer else 20.0}
     names = {0: "k_mx_stage", 1: "k_mx_hevi_tmad" if defer else "k_mx_hevi_tma", 2: "k_mx_finish",
-             3: "k_mx_fix_a+k_mx_fix_b" if defer else "k_mx_fb_mom(u,v)"}
+             3: "k_mx_fix" if defer else "k_mx_fb_mom(u,v)"}
     dom = max(ktimes, key=lambda c: ktimes[c][0])
     tot_ms, spans = ktimes[dom]
     avg_s = tot_ms / max(spans, 1) * 1e-3

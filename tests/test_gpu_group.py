@@ -38,9 +38,9 @@ def test_group_step_equals_individual_steps(vg, sizes):
         with vg.Group(grouped) as g:
             g.step(2.0, 6, 3)
             # per stage 1 stage + 6 column launches; after stages 1 and 2 the
-            # u/v/rho' and the w fix-ups of the deferred column kernel; stage
-            # 3's are in the finish
-            assert g.launches_per_step() == 3 * (1 + 6) + 2 * 2 + 1
+            # fix-up of the deferred column kernel (u/v update, w/rho'
+            # corrections); stage 3's is in the finish
+            assert g.launches_per_step() == 3 * (1 + 6) + 2 + 1
             g.step(2.0, 6, 2)
         for m in single:
             m.step(2.0, 6, 5)

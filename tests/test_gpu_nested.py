@@ -119,9 +119,9 @@ def test_nested_step_equals_composition(vg, oc):
             n.step_async(DT, NSUB, 1)
             n.wait()
             per_nest = 1 + 2 * R + 1
-            # per stage 1 stage + NSUB column launches; the u/v/rho' and w
-            # fix-ups after stages 1 and 2; stage 3's are in the finish
-            group = 3 * (1 + NSUB) + 2 * 2 + 1
+            # per stage 1 stage + NSUB column launches; the fix-up after
+            # stages 1 and 2; stage 3's is in the finish
+            group = 3 * (1 + NSUB) + 2 + 1
             assert n.launches_per_step() == group + R * group + len(shapes) * per_nest + 2
         nests = [(c, s, pi, i, r) for c, (s, pi, i, r) in zip(b_c, shapes)]
         for _ in range(2):

@@ -947,6 +947,10 @@ int vibe_gb300_model_create(const vibe_gb300_setup* s, int precision, vibe_gb300
     if (s->acoustic_mode == 1) return bail(fail(VIBE_GB300_EUNSUPPORTED, "mixed path supports acoustic_mode 0 and 2"));
     if (s->divergence_damping > 0.0 && s->divergence_order > 2)
       return bail(fail(VIBE_GB300_EUNSUPPORTED, "mixed path supports 2nd-order divergence damping only"));
+    // the mixed kernels index a field with 32-bit offsets (any grid whose
+    // state fits in device memory is far below this)
+    if (m->d.plane * (size_t)(nz + 1) >= ((size_t)1 << 32))
+      return bail(fail(VIBE_GB300_EUNSUPPORTED, "mixed path needs fewer than 2^32 elements per field"));
   }
   m->met.f0 = 2.0 * kOmega * std::sin(s->latitude * (kPi / 180.0));
   m->met.beta = 2.0 * kOmega * std::cos(s->latitude * (kPi / 180.0)) / kEarthRadius;

@@ -325,7 +325,7 @@ __device__ __forceinline__ void stage_body(const Dims& d, const Tab& t, const Fl
   const bool f_moist = !kSpec && fl.moist, f_dd = !kSpec && fl.div_damp > 0.0;
   const int f_cor = kSpec ? 0 : fl.coriolis;
   const int nx = d.nx, ny = d.ny, nz = d.nz, P = d.P;
-  const size_t pl = d.plane;
+  const unsigned pl = (unsigned)d.plane;  // a field has < 2^32 elements (checked when the model is made)
   const int i0 = bx * TX, j0 = by * TY;
   const int kb = bz * kchunk;
   const int klast = (kb + kchunk >= nz) ? nz : kb + kchunk - 1;  // the top chunk also owns face nz
@@ -339,7 +339,7 @@ __device__ __forceinline__ void stage_body(const Dims& d, const Tab& t, const Fl
   const int ipu = imin(i, nx - 1) - i;  // ip - i on u faces (-1 at i = nx)
   const int jpv = imin(j, ny - 1) - j;  // jp - j on v faces (-1 at j = ny)
   const int djm = (j > 0) ? -1 : 0;     // jm - j
-  const size_t colc = (size_t)imin(j, ny) * P + imin(i, nx);
+  const unsigned colc = (unsigned)(imin(j, ny) * P + imin(i, nx));
   const bool edge = (i0 - XO < 0) || (j0 - 3 < 0) || (i0 - XO + TW > nx - 1) || (j0 + TY + 3 > ny - 1);
   // levels kb..ktop are read: every level of the chunk, and the one above
   // its last cell level (capped at the top face nz); level L sits in slot
@@ -380,20 +380,20 @@ __device__ __forceinline__ void stage_body(const Dims& d, const Tab& t, const Fl
   if (cell) {
 #pragma unroll
     for (int m = 0; m < 7; ++m) {
-      const size_t o = (size_t)iclamp(kb + m - 3, 0, nz - 1) * pl + colc;
+      const unsigned o = (unsigned)iclamp(kb + m - 3, 0, nz - 1) * pl + colc;
       wT[m] = win.f[THETA][o];
       wQ[m] = win.f[QV][o];
     }
-    const size_t o = (size_t)imax(kb - 1, 0) * pl + colc;
+    const unsigned o = (unsigned)imax(kb - 1, 0) * pl + colc;
     wprev = win.f[W][o];
     pprev = win.f[PI][o];
     rprev = win.f[RHO][o];
   }
   // u, v of the level below the chunk at the own faces (k = 0: the level itself)
   if (kb > 0 && in_box) {
-    const size_t o = (size_t)(kb - 1) * pl;
-    if (j < ny) uprev = win.f[U][o + (size_t)j * P + (i + ipu)];
-    if (i < nx) vprev = win.f[V][o + (size_t)(j + jpv) * P + i];
+    const unsigned o = (unsigned)(kb - 1) * pl;
+    if (j < ny) uprev = win.f[U][o + (unsigned)(j * P + (i + ipu))];
+    if (i < nx) vprev = win.f[V][o + (unsigned)((j + jpv) * P + i)];
   }
   const bool has_base = w0.f[U] != nullptr;
   const bool base_in = has_base && w0.f[U] == win.f[U];  // first stage: the base state is the input
@@ -408,7 +408,7 @@ __device__ __forceinline__ void stage_body(const Dims& d, const Tab& t, const Fl
     // This level's global loads (the base state the stage adds its tendency
     // to, when it is not the input), issued before the wait for the next
     // level's boxes so that their latencies overlap it and one another.
-    const size_t c = (size_t)k * pl + colc;
+    const unsigned c = (unsigned)k * pl + colc;
     const bool do_u = cells_here && in_box && j < ny, do_v = cells_here && in_box && i < nx;
     float bU = 0.f, bV = 0.f, bW = 0.f, bR = 0.f, bP = 0.f, bT = 0.f, bQ = 0.f;
     if (has_base && !base_in) {
@@ -527,7 +527,7 @@ __device__ __forceinline__ void stage_body(const Dims& d, const Tab& t, const Fl
       r -= cp * (0.5f * (thm + thc)) * (pic - pim) * t.idzw[k];
       float qcond = 0.f, qvc = wQ[3];  // qv(kc)
       if (f_moist) {
-        const size_t ckc = (size_t)kc * pl + colc;
+        const unsigned ckc = (unsigned)kc * pl + colc;
         qcond = win.f[QC][ckc] + win.f[QR][ckc] + win.f[QI][ckc] + win.f[QS][ckc] + win.f[QG][ckc];
       }
       r += (float)kG * (thc * t.th0inv[kc] + (float)kBuoyMoist * qvc - qcond);
@@ -592,40 +592,31 @@ __device__ __forceinline__ void stage_body(const Dims& d, const Tab& t, const Fl
     // one code path with the stencil stride chosen per face. Same face values
     // as hflux up to rounding.
     auto hflux_pair = [&]() {
-      constexpr int NXF = TY * (TX + 1), NF = NXF + (TY + 1) * TX;
-      for (int e = tid; e < NF; e += NT) {
-        int off, st, dst;
-        float vel;
-        bool valid;
-        if (e < NXF) {
-          const int fr = e / (TX + 1), ff = e - fr * (TX + 1);
-          off = (fr + 3) * TW + ff + XO - 1;  // cell i0+ff-1, left of the face
-          st = 1;
-          vel = sU[(fr + 1) * TW + ff + XO];
-          valid = i0 + ff <= nx && j0 + fr < ny;
-          dst = e;
-        } else {
-          const int r2 = e - NXF, fg = r2 / TX, fcl = r2 - fg * TX;
-          off = (fg + 2) * TW + fcl + XO;  // cell j0+fg-1, below the face
-          st = TW;
-          vel = sV[(fg + 1) * TW + fcl + XO];
-          valid = j0 + fg <= ny && i0 + fcl < nx;
-          dst = r2;
-        }
+      // one x and one y face pair per thread: its cell's left and lower
+      // faces; the top row's y faces go to warp 0 and the right column's x
+      // faces to lanes 0..7 of warp 1 as a third (no warp diverges on it)
+      auto face = [&](int off, int st, float vel, bool valid, float* d0, float* d1) {
         const int sp = vel >= 0.f ? st : -st;  // upwind order
         const F2 a0 = mk2(sT[off - 2 * sp], sQ[off - 2 * sp]), a1 = mk2(sT[off - sp], sQ[off - sp]);
         const F2 a2 = mk2(sT[off], sQ[off]), a3 = mk2(sT[off + sp], sQ[off + sp]);
         const F2 a4 = mk2(sT[off + 2 * sp], sQ[off + 2 * sp]);
         float Ft, Fq;
         un2(weno_flux2(a0, a1, a2, a3, a4, vel), Ft, Fq);
-        if (!valid) Ft = Fq = 0.f;
-        if (e < NXF) {
-          sFx[0][dst] = Ft;
-          sFx[1][dst] = Fq;
-        } else {
-          sFy[0][dst] = Ft;
-          sFy[1][dst] = Fq;
-        }
+        *d0 = valid ? Ft : 0.f;
+        *d1 = valid ? Fq : 0.f;
+      };
+      // x face (i0+tx, j0+ty): cells i-1 (centre) .. in row ty
+      face(o3 - 1, 1, sU[o1], i <= nx && j < ny, &sFx[0][ty * (TX + 1) + tx], &sFx[1][ty * (TX + 1) + tx]);
+      // y face (i0+tx, j0+ty): cells j-1 (centre) .. in column tx
+      face(o3 - TW, TW, sV[o1], j <= ny && i < nx, &sFy[0][ty * TX + tx], &sFy[1][ty * TX + tx]);
+      if (tid < TX) {  // y face (i0+c, j0+TY)
+        const int c = tid, bo = (TY + 3) * TW + c + XO;
+        face(bo - TW, TW, sV[(TY + 1) * TW + c + XO], j0 + TY <= ny && i0 + c < nx, &sFy[0][TY * TX + c],
+             &sFy[1][TY * TX + c]);
+      } else if (tid < TX + TY) {  // x face (i0+TX, j0+f)
+        const int f = tid - TX, bo = (f + 3) * TW + TX + XO;
+        face(bo - 1, 1, sU[(f + 1) * TW + TX + XO], i0 + TX <= nx && j0 + f < ny, &sFx[0][f * (TX + 1) + TX],
+             &sFx[1][f * (TX + 1) + TX]);
       }
     };
     // species q's tendency from its horizontal face fluxes (slot) and its
@@ -689,7 +680,7 @@ __device__ __forceinline__ void stage_body(const Dims& d, const Tab& t, const Fl
     if (f_moist) {
       for (int q = QC; q <= QG; ++q) {
         __syncthreads();  // sQm and the flux slots are no longer read
-        load_box3(sQm, win.f[q] + (size_t)k * pl, P, i0, j0, nx - 1, ny - 1);
+        load_box3(sQm, win.f[q] + (unsigned)k * pl, P, i0, j0, nx - 1, ny - 1);
         __syncthreads();
         if (f_weno) {
           hflux(sQm, 0);
@@ -699,7 +690,7 @@ __device__ __forceinline__ void stage_body(const Dims& d, const Tab& t, const Fl
         float ft = 0.f, fb = 0.f;
         if (cell) {
 #pragma unroll
-          for (int m = 0; m < 6; ++m) z[m] = win.f[q][(size_t)iclamp(k + m - 3, 0, nz - 1) * pl + colc];
+          for (int m = 0; m < 6; ++m) z[m] = win.f[q][(unsigned)iclamp(k + m - 3, 0, nz - 1) * pl + colc];
           if (f_weno) {
             const float qc = sQm[o3];
             ft = weno_face_f(z[1], z[2], qc, z[4], z[5], wt);
@@ -716,7 +707,7 @@ __device__ __forceinline__ void stage_body(const Dims& d, const Tab& t, const Fl
         wT[m] = wT[m + 1];
         wQ[m] = wQ[m + 1];
       }
-      const size_t o = (size_t)imin(k + 4, nz - 1) * pl + colc;
+      const unsigned o = (unsigned)imin(k + 4, nz - 1) * pl + colc;
       wT[6] = win.f[THETA][o];
       wQ[6] = win.f[QV][o];
       wprev = wk;
@@ -1855,7 +1846,7 @@ __global__ void __launch_bounds__(128, 7) k_mx_hevi_col2(const __grid_constant__
 // every reader applies the implicit corrections from the final pi' itself
 // (defer_fix_w / defer_fix_rho). This kernel applies them to its own input
 // when apply_uv is set (its input is then a deferred substep's output); the
-// u/v kernel after a stage's last substep (k_mx_fix_a/_b) and the finish
+// fix-up kernel after a stage's last substep (k_mx_fix) and the finish
 // kernel apply them to the last one. The parked sweep data shrinks from
 // w~, rho~ and the eliminated pi' to the eliminated pi' alone: 48 instead of
 // 64 bytes of traffic per cell and substep.
@@ -2152,52 +2143,51 @@ __global__ void __launch_bounds__(128, 7) k_mx_hevi_tmad(const __grid_constant__
 }
 
 // After a stage's last substep of the kDefer column kernel: its u/v backward
-// update (as fb_mom_body) and the w/rho' corrections, in place, as two
-// launches: k_mx_fix_a updates u, v and rho' (reading w~ as the column
-// kernel left it), then k_mx_fix_b replaces w~ by w.
-__device__ __forceinline__ void fix_a_body(const Dims& d, const Tab& t, const Flags& fl, const WS& s, float dtau,
-                                           int bx, int by, int bz) {
+// update (as fb_mom_body) and the w/rho' corrections, in place, in one
+// launch: a thread owns a column position of the (nx+1) x (ny+1) face grid
+// and marches up the levels, reading w~(k+1) (and correcting it) before it
+// writes w(k+1), so no other thread's read races a write (pi' itself is not
+// changed; the u/v updates read it across columns).
+__device__ __forceinline__ void fix_body(const Dims& d, const Tab& t, const Flags& fl, const WS& s, float dtau,
+                                         int bx, int by) {
   const int i = bx * blockDim.x + threadIdx.x;
   const int j = by * blockDim.y + threadIdx.y;
-  const int k = bz;
-  if (i > d.nx || j > d.ny || k >= d.nz) return;
+  if (i > d.nx || j > d.ny) return;
+  const int nz = d.nz;
   const float* __restrict__ pn = s.f[PI];
-  const float cp = (float)kCp;
-  const size_t c = IX(i, j, k);
-  if (j < d.ny) {
-    const int ip = imin(i, d.nx - 1), im = imax(i - 1, 0);
-    s.f[U][c] = s.f[U][c] + dtau * (-cp * t.t0c[k] * (pn[IX(ip, j, k)] - pn[IX(im, j, k)]) * t.dx_inv);
-  }
-  if (i < d.nx) {
-    const int jp = imin(j, d.ny - 1), jm = imax(j - 1, 0);
-    s.f[V][c] = s.f[V][c] + dtau * (-cp * t.t0c[k] * (pn[IX(i, jp, k)] - pn[IX(i, jm, k)]) * t.dy_inv);
-  }
-  if (i < d.nx && j < d.ny) {
-    const float b = (float)fl.hevi_beta, cb = dtau * b * cp, db = dtau * b;
-    const int nz = d.nz;
-    const float pk = pn[c], pkm = (k > 0) ? pn[IX(i, j, k - 1)] : 0.f, pk1 = (k + 1 < nz) ? pn[IX(i, j, k + 1)] : 0.f;
-    const float wk = defer_fix_w(t, nz, cb, s.f[W][c], pk, pkm, k);
-    const float wk1 = defer_fix_w(t, nz, cb, s.f[W][IX(i, j, k + 1)], pk1, pk, k + 1);
-    s.f[RHO][c] = defer_fix_rho(t, db, s.f[RHO][c], wk, wk1, k);
+  float* __restrict__ su = s.f[U];
+  float* __restrict__ sv = s.f[V];
+  float* __restrict__ sw = s.f[W];
+  float* __restrict__ sr = s.f[RHO];
+  const float cp = (float)kCp, b = (float)fl.hevi_beta, cb = dtau * b * cp, db = dtau * b;
+  const bool du = j < d.ny, dv = i < d.nx, cell = du && dv;
+  // (indices clamped into the grid; each is used only where it is in range)
+  const int ic = imin(i, d.nx - 1), jc = imin(j, d.ny - 1);
+  const int ip = ic, im = imax(i - 1, 0), jp = jc, jm = imax(j - 1, 0);
+  const size_t pl = d.plane;
+  const size_t cf = IX(i, j, 0);                                  // u face (j < ny), v face (i < nx)
+  const size_t ue = IX(ip, jc, 0), uw = IX(im, jc, 0);            // pi' beside the u face
+  const size_t vn = IX(ic, jp, 0), vs = IX(ic, jm, 0);            // pi' beside the v face
+  const size_t cc = IX(ic, jc, 0);                                // the cell (i, j) when cell
+  float pk = cell ? pn[cc] : 0.f, wk = cell ? sw[cc] : 0.f;  // pi'(k), w(k) (w(0) = w~(0))
+  for (int k = 0; k < nz; ++k) {
+    const size_t o = (size_t)k * pl;
+    if (du) su[cf + o] = su[cf + o] + dtau * (-cp * t.t0c[k] * (pn[ue + o] - pn[uw + o]) * t.dx_inv);
+    if (dv) sv[cf + o] = sv[cf + o] + dtau * (-cp * t.t0c[k] * (pn[vn + o] - pn[vs + o]) * t.dy_inv);
+    if (cell) {
+      const size_t c = cc + o;
+      const float pk1 = (k + 1 < nz) ? pn[c + pl] : 0.f;
+      const float wk1 = defer_fix_w(t, nz, cb, sw[c + pl], pk1, pk, k + 1);
+      sr[c] = defer_fix_rho(t, db, sr[c], wk, wk1, k);
+      if (k >= 1) sw[c] = wk;  // faces 1 .. nz-1 (w(0) and w(nz) keep w~)
+      wk = wk1;
+      pk = pk1;
+    }
   }
 }
-__device__ __forceinline__ void fix_b_body(const Dims& d, const Tab& t, const Flags& fl, const WS& s, float dtau,
-                                           int bx, int by, int bz) {
-  const int i = bx * blockDim.x + threadIdx.x;
-  const int j = by * blockDim.y + threadIdx.y;
-  const int k = bz + 1;  // faces 1 .. nz-1
-  if (i >= d.nx || j >= d.ny || k >= d.nz) return;
-  const size_t c = IX(i, j, k);
-  const float cb = dtau * (float)fl.hevi_beta * (float)kCp;
-  s.f[W][c] = defer_fix_w(t, d.nz, cb, s.f[W][c], s.f[PI][c], s.f[PI][IX(i, j, k - 1)], k);
-}
-__global__ void k_mx_fix_a(const __grid_constant__ Dims d, const __grid_constant__ Tab t,
-                           const __grid_constant__ Flags fl, const __grid_constant__ WS s, float dtau) {
-  fix_a_body(d, t, fl, s, dtau, blockIdx.x, blockIdx.y, blockIdx.z);
-}
-__global__ void k_mx_fix_b(const __grid_constant__ Dims d, const __grid_constant__ Tab t,
-                           const __grid_constant__ Flags fl, const __grid_constant__ WS s, float dtau) {
-  fix_b_body(d, t, fl, s, dtau, blockIdx.x, blockIdx.y, blockIdx.z);
+__global__ void k_mx_fix(const __grid_constant__ Dims d, const __grid_constant__ Tab t,
+                         const __grid_constant__ Flags fl, const __grid_constant__ WS s, float dtau) {
+  fix_body(d, t, fl, s, dtau, blockIdx.x, blockIdx.y);
 }
 
 size_t hevi_tma_smem_bytes(int nz) {
@@ -2619,8 +2609,7 @@ bool mixed_hevi_defers(const Dims& d) { return hevi_tma_variant(d) == 5; }
 
 void mixed_uv_fix(const Dims& d, const Tab& t, const Flags& fl, const WS& s, float dtau, cudaStream_t stream) {
   const dim3 b(32, 4);
-  k_mx_fix_a<<<g3(d.nx + 1, d.ny + 1, d.nz, b), b, 0, stream>>>(d, t, fl, s, dtau);
-  if (d.nz > 1) k_mx_fix_b<<<g3(d.nx, d.ny, d.nz - 1, b), b, 0, stream>>>(d, t, fl, s, dtau);
+  k_mx_fix<<<g3(d.nx + 1, d.ny + 1, 1, b), b, 0, stream>>>(d, t, fl, s, dtau);
 }
 
 int mixed_hevi_substep(const Dims& d, const Tab& t, const Flags& fl, const WS& win, const WS& wout, float dtau,
@@ -2748,17 +2737,11 @@ __global__ void k_b_uv(const UvArgs* __restrict__ A, const int* __restrict__ sta
   const int l = (int)blockIdx.x - start[dom];
   fb_mom_body(a.d, a.t, a.win, a.wout, a.dtau, 0, l % a.gx, (l / a.gx) % a.gy, l / (a.gx * a.gy));
 }
-__global__ void k_b_fix_a(const UvArgs* __restrict__ A, const int* __restrict__ start, int nd) {
+__global__ void k_b_fix(const UvArgs* __restrict__ A, const int* __restrict__ start, int nd) {
   const int dom = find_domain(start, nd);
   const UvArgs& a = A[dom];
   const int l = (int)blockIdx.x - start[dom];
-  fix_a_body(a.d, a.t, a.fl, a.wout, a.dtau, l % a.gx, (l / a.gx) % a.gy, l / (a.gx * a.gy));
-}
-__global__ void k_b_fix_b(const UvArgs* __restrict__ A, const int* __restrict__ start, int nd) {
-  const int dom = find_domain(start, nd);
-  const UvArgs& a = A[dom];
-  const int l = (int)blockIdx.x - start[dom];
-  fix_b_body(a.d, a.t, a.fl, a.wout, a.dtau, l % a.gx, (l / a.gx) % a.gy, l / (a.gx * a.gy));
+  fix_body(a.d, a.t, a.fl, a.wout, a.dtau, l % a.gx, l / a.gx);
 }
 
 __global__ void k_b_finish(const FinishArgs* __restrict__ A, const int* __restrict__ start, int nd, unsigned* err) {
@@ -2784,7 +2767,7 @@ WS ws_mix(float* const* sub, float* const* stage) {  // acoustic fields from sub
 
 struct MixedBatch {
   struct Launch {
-    int kind = 0;  // 0 stage, 1 column, 2 u/v (with deferral: u/v/rho' fix-up), 3 finish, 4 w fix-up
+    int kind = 0;  // 0 stage, 1 column, 2 u/v (with deferral: the u/v/w/rho' fix-up), 3 finish
     int raw = 0, nd = 0, blocks = 0;
     void* args = nullptr;
     int* start = nullptr;
@@ -2901,23 +2884,11 @@ MixedBatch* mixed_batch_build(const std::vector<MixedDomain>& doms, const Flags&
       a.dtau = dtau;
       a.gx = ceil_div(m.d.nx + 1, 32);
       a.gy = ceil_div(m.d.ny + 1, 4);
-      a.gz = m.d.nz;
+      a.gz = b->defer ? 1 : m.d.nz;  // the deferred fix-up marches the levels
       start[q] = ub;
       ub += a.gx * a.gy * a.gz;
     }
     ok = ok && upload_launch(b, 2, 0, ua, start, ub);
-    if (b->defer && nz > 1) {  // the w corrections, after the u/v/rho' launch
-      int wb = 0;
-      for (int q = 0; q < nd; ++q) {
-        UvArgs& a = ua[q];
-        a.gx = ceil_div(a.d.nx, 32);
-        a.gy = ceil_div(a.d.ny, 4);
-        a.gz = a.d.nz - 1;
-        start[q] = wb;
-        wb += a.gx * a.gy * a.gz;
-      }
-      ok = ok && upload_launch(b, 4, 0, ua, start, wb);
-    }
   }
   if (ok) {
     std::vector<FinishArgs> fa(nd);
@@ -2971,11 +2942,8 @@ void mixed_batch_enqueue(const MixedBatch* b, cudaStream_t s) {
           k_b_hevi<<<L.blocks, dim3(32, 4), b->hevi_smem, s>>>((const HeviArgs*)L.args, L.start, L.nd);
         break;
       case 2:
-        if (b->defer) k_b_fix_a<<<L.blocks, dim3(32, 4), 0, s>>>((const UvArgs*)L.args, L.start, L.nd);
+        if (b->defer) k_b_fix<<<L.blocks, dim3(32, 4), 0, s>>>((const UvArgs*)L.args, L.start, L.nd);
         else k_b_uv<<<L.blocks, dim3(32, 4), 0, s>>>((const UvArgs*)L.args, L.start, L.nd);
-        break;
-      case 4:
-        k_b_fix_b<<<L.blocks, dim3(32, 4), 0, s>>>((const UvArgs*)L.args, L.start, L.nd);
         break;
       default:
         k_b_finish<<<L.blocks, dim3(32, 4), 0, s>>>((const FinishArgs*)L.args, L.start, L.nd, b->err);
