@@ -721,7 +721,7 @@ __device__ __forceinline__ void stage_body(const Dims& d, const Tab& t, const Fl
 }
 
 template <bool kRaw, bool kSpec>
-__global__ void __launch_bounds__(NT, 4) k_mx_stage(const __grid_constant__ Dims d, const __grid_constant__ Tab t,
+__global__ void __launch_bounds__(NT, 3) k_mx_stage(const __grid_constant__ Dims d, const __grid_constant__ Tab t,
                                                     const __grid_constant__ Flags fl,
                                                     const __grid_constant__ StageMaps M,
                                                     const __grid_constant__ WS win, const __grid_constant__ WS w0,
@@ -2161,28 +2161,57 @@ __device__ __forceinline__ void fix_body(const Dims& d, const Tab& t, const Flag
   float* __restrict__ sr = s.f[RHO];
   const float cp = (float)kCp, b = (float)fl.hevi_beta, cb = dtau * b * cp, db = dtau * b;
   const bool du = j < d.ny, dv = i < d.nx, cell = du && dv;
-  // (indices clamped into the grid; each is used only where it is in range)
+  // (indices clamped into the grid; each is used only where it is in range;
+  // 32-bit offsets: a field has < 2^32 elements, checked when the model is made)
   const int ic = imin(i, d.nx - 1), jc = imin(j, d.ny - 1);
   const int ip = ic, im = imax(i - 1, 0), jp = jc, jm = imax(j - 1, 0);
-  const size_t pl = d.plane;
-  const size_t cf = IX(i, j, 0);                                  // u face (j < ny), v face (i < nx)
-  const size_t ue = IX(ip, jc, 0), uw = IX(im, jc, 0);            // pi' beside the u face
-  const size_t vn = IX(ic, jp, 0), vs = IX(ic, jm, 0);            // pi' beside the v face
-  const size_t cc = IX(ic, jc, 0);                                // the cell (i, j) when cell
-  float pk = cell ? pn[cc] : 0.f, wk = cell ? sw[cc] : 0.f;  // pi'(k), w(k) (w(0) = w~(0))
-  for (int k = 0; k < nz; ++k) {
-    const size_t o = (size_t)k * pl;
-    if (du) su[cf + o] = su[cf + o] + dtau * (-cp * t.t0c[k] * (pn[ue + o] - pn[uw + o]) * t.dx_inv);
-    if (dv) sv[cf + o] = sv[cf + o] + dtau * (-cp * t.t0c[k] * (pn[vn + o] - pn[vs + o]) * t.dy_inv);
+  const unsigned pl = (unsigned)d.plane, P = (unsigned)d.P;
+  const unsigned cf = j * P + i;                    // u face (j < ny), v face (i < nx)
+  const unsigned ue = jc * P + ip, uw = jc * P + im;  // pi' beside the u face
+  const unsigned vn = jp * P + ic, vs = jm * P + ic;  // pi' beside the v face
+  const unsigned cc = jc * P + ic;                  // the cell (i, j) when cell
+  // a level's inputs, loaded one level ahead so that their latency overlaps
+  // the level below's arithmetic and stores
+  struct Lv {
+    float uc, ue, uw, vc, vn, vs, rc, wn, pn;
+  };
+  auto load = [&](int k) {
+    const unsigned o = (unsigned)k * pl;
+    Lv L = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    if (du) {
+      L.uc = su[cf + o];
+      L.ue = pn[ue + o];
+      L.uw = pn[uw + o];
+    }
+    if (dv) {
+      L.vc = sv[cf + o];
+      L.vn = pn[vn + o];
+      L.vs = pn[vs + o];
+    }
     if (cell) {
-      const size_t c = cc + o;
-      const float pk1 = (k + 1 < nz) ? pn[c + pl] : 0.f;
-      const float wk1 = defer_fix_w(t, nz, cb, sw[c + pl], pk1, pk, k + 1);
-      sr[c] = defer_fix_rho(t, db, sr[c], wk, wk1, k);
+      L.rc = sr[cc + o];
+      L.wn = sw[cc + o + pl];                       // w~(k+1) (w has nz+1 faces)
+      if (k + 1 < nz) L.pn = pn[cc + o + pl];       // pi'(k+1)
+    }
+    return L;
+  };
+  float pk = cell ? pn[cc] : 0.f, wk = cell ? sw[cc] : 0.f;  // pi'(k), w(k) (w(0) = w~(0))
+  Lv cur = load(0);
+  for (int k = 0; k < nz; ++k) {
+    const Lv nxt = (k + 1 < nz) ? load(k + 1) : cur;
+    const unsigned o = (unsigned)k * pl;
+    if (du) su[cf + o] = cur.uc + dtau * (-cp * t.t0c[k] * (cur.ue - cur.uw) * t.dx_inv);
+    if (dv) sv[cf + o] = cur.vc + dtau * (-cp * t.t0c[k] * (cur.vn - cur.vs) * t.dy_inv);
+    if (cell) {
+      const unsigned c = cc + o;
+      const float pk1 = cur.pn;
+      const float wk1 = defer_fix_w(t, nz, cb, cur.wn, pk1, pk, k + 1);
+      sr[c] = defer_fix_rho(t, db, cur.rc, wk, wk1, k);
       if (k >= 1) sw[c] = wk;  // faces 1 .. nz-1 (w(0) and w(nz) keep w~)
       wk = wk1;
       pk = pk1;
     }
+    cur = nxt;
   }
 }
 __global__ void k_mx_fix(const __grid_constant__ Dims d, const __grid_constant__ Tab t,
@@ -2695,7 +2724,7 @@ __device__ __forceinline__ int find_domain(const int* __restrict__ start, int nd
 }
 
 template <bool kRaw>
-__global__ void __launch_bounds__(NT, 4) k_b_stage(const StageArgs* __restrict__ A, const int* __restrict__ start,
+__global__ void __launch_bounds__(NT, 3) k_b_stage(const StageArgs* __restrict__ A, const int* __restrict__ start,
                                                    int nd, unsigned* err) {
   const int dom = find_domain(start, nd);
   const StageArgs& a = A[dom];
