@@ -398,11 +398,14 @@ __device__ __forceinline__ void stage_body(const Dims& d, const Tab& t, const Fl
   const bool has_base = w0.f[U] != nullptr;
   const bool base_in = has_base && w0.f[U] == win.f[U];  // first stage: the base state is the input
   float fcT = 0.f, fcQ = 0.f;  // carried vertical WENO fluxes (top face of the level below)
-  bool bad = false;
+  // the sum of every value written: non-finite iff one of them is (the
+  // values are perturbations, far from overflowing a sum)
+  float fsum = 0.f;
   if (!level_ready(kb)) return;
   if (edge) fix_level(sbuf[0]);
+  int cur = 0;  // ring slot of level k (k - kb mod kStageRing, rotated)
   for (int k = kb; k <= klast; ++k) {
-    const int lev = k - kb, cur = lev % kStageRing, nxt = (lev + 1) % kStageRing;
+    const int nxt = (cur + 1 == kStageRing) ? 0 : cur + 1, nn = (nxt + 1 == kStageRing) ? 0 : nxt + 1;
     const bool cells_here = k < nz;  // uniform across the block
     const int kc = imin(k, nz - 1);
     // This level's global loads (the base state the stage adds its tendency
@@ -431,7 +434,7 @@ __device__ __forceinline__ void stage_body(const Dims& d, const Tab& t, const Fl
     // past that barrier every thread is done with level k-1 (its values of
     // the level below live in registers), so its slot takes level k+2
     if (tid == 0 && k + 2 <= ktop)
-      issue_level(M, sbuf[(lev + 2) % kStageRing], &sbar[(lev + 2) % kStageRing], i0, j0, k + 2, nz);
+      issue_level(M, sbuf[nn], &sbar[nn], i0, j0, k + 2, nz);
     if (k + 2 <= ktop) hi = k + 2;
     float* const buf = sbuf[cur];
     const float* const sT = buf + tile_off(TT);
@@ -480,7 +483,7 @@ __device__ __forceinline__ void stage_body(const Dims& d, const Tab& t, const Fl
     auto emit = [&](int q, float r) {
       const float o = has_base ? base_of(q) + dts * r : r;  // no base: raw tendency
       wout.f[q][c] = o;
-      bad |= !isfinite(o);
+      fsum += o;
       if (kRaw) rout.f[q][c] = r;
     };
     if (do_u) {  // u face (i, j, k)
@@ -716,8 +719,9 @@ __device__ __forceinline__ void stage_body(const Dims& d, const Tab& t, const Fl
     }
     uprev = sU[o1 + ipu];
     vprev = sV[o1 + jpv * TW];
+    cur = nxt;
   }
-  if (bad) atomicOr(err, (unsigned)kErrNonFinite);
+  if (!isfinite(fsum)) atomicOr(err, (unsigned)kErrNonFinite);
 }
 
 template <bool kRaw, bool kSpec>
