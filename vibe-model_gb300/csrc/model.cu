@@ -354,17 +354,23 @@ __global__ void k_pack(Dims d, int nsx, int nsy, int ni, int nj, int nk, const d
   if (i >= ni || j >= nj || k >= nk) return;
   dst[d.idx(i, j, k)] = src[soff(nsx, nsy, i, j, k)];
 }
-__global__ void k_unpack(Dims d, int nsx, int nsy, int nsz, int ni, int nj, int nk, const double* __restrict__ src,
-                         double* __restrict__ dst) {
-  const size_t n = (size_t)nsx * nsy * nsz;
-  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x) {
-    const int ii = (int)(e % nsx) - H;
-    const int jj = (int)((e / nsx) % nsy) - H;
-    const int kk = (int)(e / ((size_t)nsx * nsy)) - H;
-    double v = 0.0;
-    if (ii >= 0 && ii < ni && jj >= 0 && jj < nj && kk >= 0 && kk < nk) v = src[d.idx(ii, jj, kk)];
-    dst[e] = v;
-  }
+// device layout (FP64 or FP32) -> FP64 FieldT storage, zeros outside the
+// box i < ni, j < nj, k < nk: one thread per storage point of a 3-D grid
+// (no index divisions), coalesced along i on both sides
+template <class T>
+__global__ void k_unpack_t(Dims d, int nsx, int nsy, int ni, int nj, int nk, const T* __restrict__ src,
+                           double* __restrict__ dst) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y, z = blockIdx.z;
+  if (x >= nsx || y >= nsy) return;
+  const int ii = x - H, jj = y - H, kk = z - H;
+  double v = 0.0;
+  if (ii >= 0 && ii < ni && jj >= 0 && jj < nj && kk >= 0 && kk < nk) v = (double)src[d.idx(ii, jj, kk)];
+  dst[((size_t)z * nsy + y) * nsx + x] = v;
+}
+template <class T>
+void unpack(const Dims& d, int nsx, int nsy, int nsz, int ni, int nj, int nk, const T* src, double* dst,
+            cudaStream_t s) {
+  k_unpack_t<T><<<dim3((nsx + 31) / 32, (nsy + 7) / 8, nsz), dim3(32, 8), 0, s>>>(d, nsx, nsy, ni, nj, nk, src, dst);
 }
 
 // rigid ground and lid (w_rigid): w = 0 on the k = 0 and k = nz faces
@@ -1067,8 +1073,8 @@ int vibe_gb300_get_field(vibe_gb300_model* m, int q, double* host) {
   const size_t n = storage_count(m, q);
   int ni, nj, nk;
   box_of(m, q, ni, nj, nk);
-  k_unpack<<<1024, 256, 0, m->stream>>>(m->d, m->nsx[q], m->nsy[q], m->nsz[q], ni, nj, nk, m->S[m->cur][q],
-                                        m->d_stage_in);
+  unpack<double>(m->d, m->nsx[q], m->nsy[q], m->nsz[q], ni, nj, nk, m->S[m->cur][q],
+                                        m->d_stage_in, m->stream);
   CUDA_OK(cudaGetLastError());
   CUDA_OK(cudaMemcpyAsync(host, m->d_stage_in, n * sizeof(double), cudaMemcpyDeviceToHost, m->stream));
   CUDA_OK(cudaStreamSynchronize(m->stream));
@@ -1144,7 +1150,7 @@ int vibe_gb300_slow_tendency(vibe_gb300_model* m, double* const* host_out) {
     else if (q == V) ni = m->d.nx;
     else if (q == W) { ni = m->d.nx; nj = m->d.ny; }
     else { ni = m->d.nx; nj = m->d.ny; }
-    k_unpack<<<1024, 256, 0, m->stream>>>(m->d, m->nsx[q], m->nsy[q], m->nsz[q], ni, nj, nk, m->tend[q], m->d_stage_in);
+    unpack<double>(m->d, m->nsx[q], m->nsy[q], m->nsz[q], ni, nj, nk, m->tend[q], m->d_stage_in, m->stream);
     CUDA_OK(cudaMemcpyAsync(host_out[q], m->d_stage_in, storage_count(m, q) * sizeof(double), cudaMemcpyDeviceToHost,
                             m->stream));
     CUDA_OK(cudaStreamSynchronize(m->stream));
@@ -1515,20 +1521,6 @@ int vibe_gb300_set_physics(vibe_gb300_model* m, vibe_gb300_physics_fn fn, void* 
   return 0;
 }
 
-// FP32 device layout -> FP64 FieldT storage (zeros outside the box)
-__global__ void k_unpack_f32(Dims d, int nsx, int nsy, int nsz, int ni, int nj, int nk, const float* __restrict__ src,
-                             double* __restrict__ dst) {
-  const size_t n = (size_t)nsx * nsy * nsz;
-  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x) {
-    const int ii = (int)(e % nsx) - H;
-    const int jj = (int)((e / nsx) % nsy) - H;
-    const int kk = (int)(e / ((size_t)nsx * nsy)) - H;
-    double v = 0.0;
-    if (ii >= 0 && ii < ni && jj >= 0 && jj < nj && kk >= 0 && kk < nk) v = (double)src[d.idx(ii, jj, kk)];
-    dst[e] = v;
-  }
-}
-
 int vibe_gb300_physics_tendency(vibe_gb300_model* m, double dt, double* const* out) {
   if (!m || !out) return fail(VIBE_GB300_EBADARG, "bad argument");
   if (!m->phys_fn) return fail(VIBE_GB300_EBADARG, "no physics package installed");
@@ -1546,11 +1538,11 @@ int vibe_gb300_physics_tendency(vibe_gb300_model* m, double dt, double* const* o
     int ni, nj, nk;
     box_of(m, q, ni, nj, nk);
     if (m->precision == VIBE_GB300_MIXED)
-      k_unpack_f32<<<1024, 256, 0, m->stream>>>(m->d, m->nsx[q], m->nsy[q], m->nsz[q], ni, nj, nk,
-                                                (const float*)m->pt[q], m->d_stage_in);
+      unpack<float>(m->d, m->nsx[q], m->nsy[q], m->nsz[q], ni, nj, nk,
+                                                (const float*)m->pt[q], m->d_stage_in, m->stream);
     else
-      k_unpack<<<1024, 256, 0, m->stream>>>(m->d, m->nsx[q], m->nsy[q], m->nsz[q], ni, nj, nk,
-                                            (const double*)m->pt[q], m->d_stage_in);
+      unpack<double>(m->d, m->nsx[q], m->nsy[q], m->nsz[q], ni, nj, nk,
+                                            (const double*)m->pt[q], m->d_stage_in, m->stream);
     CUDA_OK(cudaGetLastError());
     CUDA_OK(cudaMemcpyAsync(out[f], m->d_stage_in, storage_count(m, q) * sizeof(double), cudaMemcpyDeviceToHost,
                             m->stream));
@@ -1921,8 +1913,8 @@ int vibe_gb300_si_step(vibe_gb300_model* m, double dt, int kind, int max_iter, d
   if (hrc != VIBE_C_OK) return fail(VIBE_GB300_EDEVICE, std::string("helmholtz solve: ") + vibe_helmholtz_last_error());
   if (pi_new) {
     si_to_cells(d, m->hz_x, m->tmp[PI], m->stream);
-    k_unpack<<<1024, 256, 0, m->stream>>>(d, m->nsx[RHO], m->nsy[RHO], m->nsz[RHO], d.nx, d.ny, d.nz, m->tmp[PI],
-                                          m->d_stage_in);
+    unpack<double>(d, m->nsx[RHO], m->nsy[RHO], m->nsz[RHO], d.nx, d.ny, d.nz, m->tmp[PI],
+                                          m->d_stage_in, m->stream);
     CUDA_OK(cudaMemcpyAsync(pi_new, m->d_stage_in, storage_count(m, RHO) * sizeof(double), cudaMemcpyDeviceToHost,
                             m->stream));
   }
@@ -2884,8 +2876,8 @@ int vibe_gb300_tendency_tl(vibe_gb300_model* m, const double* const* dx, double*
   CUDA_OK(cudaGetLastError());
   for (int q = 0; q < NSPECIES; ++q) {  // the tendency's boxes; zero elsewhere
     const int ni = m->d.nx + (q == U), nj = m->d.ny + (q == V), nk = m->d.nz + (q == W);
-    k_unpack<<<1024, 256, 0, m->stream>>>(m->d, m->nsx[q], m->nsy[q], m->nsz[q], ni, nj, nk, m->stl[2][q],
-                                          m->d_stage_in);
+    unpack<double>(m->d, m->nsx[q], m->nsy[q], m->nsz[q], ni, nj, nk, m->stl[2][q],
+                                          m->d_stage_in, m->stream);
     CUDA_OK(cudaMemcpyAsync(out[q], m->d_stage_in, storage_count(m, q) * sizeof(double), cudaMemcpyDeviceToHost,
                             m->stream));
     CUDA_OK(cudaStreamSynchronize(m->stream));
@@ -2909,8 +2901,8 @@ int vibe_gb300_tendency_ad(vibe_gb300_model* m, const double* const* bar_r, doub
   for (int q = 0; q < NSPECIES; ++q) {  // every uploaded point (the boxes incl. ghosts)
     int ni, nj, nk;
     box_of(m, q, ni, nj, nk);
-    k_unpack<<<1024, 256, 0, m->stream>>>(m->d, m->nsx[q], m->nsy[q], m->nsz[q], ni, nj, nk, m->stl[5][q],
-                                          m->d_stage_in);
+    unpack<double>(m->d, m->nsx[q], m->nsy[q], m->nsz[q], ni, nj, nk, m->stl[5][q],
+                                          m->d_stage_in, m->stream);
     CUDA_OK(cudaMemcpyAsync(bar_x[q], m->d_stage_in, storage_count(m, q) * sizeof(double), cudaMemcpyDeviceToHost,
                             m->stream));
     CUDA_OK(cudaStreamSynchronize(m->stream));
@@ -2958,20 +2950,24 @@ int after_upload(vibe_gb300_model* m, const bool* given, int nspecies) {
   return 0;
 }
 
-// mixed models: one pass from the FieldT staging into both FP64 state
-// buffers and the FP32 working copy (the conversion of to_working_body), plus
-// the working copies that hold the species' unwritten points (rho's ghost
-// line and the non-prognostic species: stage outputs and substep buffers)
-__global__ void k_pack_mixed(Dims d, int q, int nsx, int nsy, int ni, int nj, int nk, const double* __restrict__ ref,
-                             const double* __restrict__ src, double* __restrict__ s0, double* __restrict__ s1,
-                             float* __restrict__ w0, float* __restrict__ c0, float* __restrict__ c1,
-                             float* __restrict__ c2, float* __restrict__ c3) {
+// mixed models: one pass from the FieldT staging into the FP64 state (the
+// buffer of the current parity) and the FP32 working copy (the conversion of
+// to_working_body), plus the points that the step about to run does not
+// write but reads later: in the other state buffer the ghost lines (i = nx for cell fields and w, j = ny for u,
+// i = nx for v; the finish writes every other point of the next state) and
+// all of a species it does not carry (beyond `last`); in rho's other working
+// copies (stage outputs and substep buffers) its ghost lines
+__global__ void k_pack_mixed(Dims d, int q, int last, int nsx, int nsy, int ni, int nj, int nk,
+                             const double* __restrict__ ref, const double* __restrict__ src, double* __restrict__ s0,
+                             double* __restrict__ s1, float* __restrict__ w0, float* __restrict__ c0,
+                             float* __restrict__ c1, float* __restrict__ c2, float* __restrict__ c3) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y, k = blockIdx.z;
   if (i >= ni || j >= nj || k >= nk) return;
   const size_t c = d.idx(i, j, k);
   const double v = src[soff(nsx, nsy, i, j, k)];
+  const bool ghost = (q == U) ? j == d.ny : (q == V) ? i == d.nx : (i == d.nx || j == d.ny);
   s0[c] = v;
-  s1[c] = v;
+  if (ghost || q > last) s1[c] = v;
   if (!w0) return;
   bool put;  // the points to_working_body converts
   if (q == U) put = j < d.ny && k < d.nz;
@@ -2981,10 +2977,12 @@ __global__ void k_pack_mixed(Dims d, int q, int nsx, int nsy, int ni, int nj, in
   if (!put) return;
   const float wv = ref ? (float)(v - ref[k]) : (float)v;
   w0[c] = wv;
-  if (c0) c0[c] = wv;
-  if (c1) c1[c] = wv;
-  if (c2) c2[c] = wv;
-  if (c3) c3[c] = wv;
+  if (c0 && ghost) {
+    c0[c] = wv;
+    c1[c] = wv;
+    c2[c] = wv;
+    c3[c] = wv;
+  }
 }
 
 void pack_mixed(vibe_gb300_model* m, int q, const double* src) {
@@ -3001,9 +2999,9 @@ void pack_mixed(vibe_gb300_model* m, int q, const double* src) {
     c3 = m->WB[q];
   }
   const dim3 b(32, 4);
-  k_pack_mixed<<<dim3((ni + 31) / 32, (nj + 3) / 4, nk), b, 0, m->stream>>>(m->d, q, m->nsx[q], m->nsy[q], ni, nj, nk,
-                                                                            ref, src, m->S[0][q], m->S[1][q], w0, c0,
-                                                                            c1, c2, c3);
+  k_pack_mixed<<<dim3((ni + 31) / 32, (nj + 3) / 4, nk), b, 0, m->stream>>>(m->d, q, last, m->nsx[q], m->nsy[q], ni,
+                                                                            nj, nk, ref, src, m->S[m->cur][q],
+                                                                            m->S[1 - m->cur][q], w0, c0, c1, c2, c3);
 }
 
 void pack_both(vibe_gb300_model* m, int q, const double* src) {
@@ -3111,8 +3109,8 @@ int vibe_gb300_step_io(vibe_gb300_model* m, const double* const* host_in, int n_
     if (!host_out[q]) continue;
     int ni, nj, nk;
     box_of(m, q, ni, nj, nk);
-    k_unpack<<<1024, 256, 0, m->stream>>>(m->d, m->nsx[q], m->nsy[q], m->nsz[q], ni, nj, nk, m->S[m->cur][q],
-                                          io->out[b][q]);
+    unpack<double>(m->d, m->nsx[q], m->nsy[q], m->nsz[q], ni, nj, nk, m->S[m->cur][q],
+                                          io->out[b][q], m->stream);
   }
   CUDA_OK(cudaEventRecord(io->unpacked[b], m->stream));
   CUDA_OK(cudaStreamWaitEvent(io->sout, io->unpacked[b], 0));
@@ -3145,8 +3143,8 @@ int vibe_gb300_get_state(vibe_gb300_model* m, double* const* host, int nspecies)
     if (!host[q]) continue;
     int ni, nj, nk;
     box_of(m, q, ni, nj, nk);
-    k_unpack<<<1024, 256, 0, m->stream>>>(m->d, m->nsx[q], m->nsy[q], m->nsz[q], ni, nj, nk, m->S[m->cur][q],
-                                          m->d_stage_in);
+    unpack<double>(m->d, m->nsx[q], m->nsy[q], m->nsz[q], ni, nj, nk, m->S[m->cur][q],
+                                          m->d_stage_in, m->stream);
     CUDA_OK(cudaMemcpyAsync(host[q], m->d_stage_in, storage_count(m, q) * sizeof(double), cudaMemcpyDeviceToHost,
                             m->stream));
   }
