@@ -481,9 +481,11 @@ def _oracle():
     return oc
 
 
-def cpu_sample_run(args):
+def cpu_sample_run(args, record=None):
     """One worker: steps a horizontal sample of the workload on the oracle
-    port (the reference's serial FP64 algorithm). Returns (cells, seconds)."""
+    port (the reference's serial FP64 algorithm). Returns (cells, seconds).
+    record: a dict that receives the sample's state before and after the
+    first timed step (the checker for mixed_vs_oracle_error)."""
     nx, ny, steps, warmup, seed = args
     oc = _oracle()
     s = oc.defaults()
@@ -495,10 +497,45 @@ def cpu_sample_run(args):
     m.set(5, pi)
     for _i in range(warmup):
         m.rk3_step(DT, NSUB)
-    t0 = time.perf_counter()
-    for _i in range(steps):
+    secs = 0.0
+    for i in range(steps):
+        if record is not None and i == 0:
+            record["x0"] = [m.get(q) for q in range(7)]
+        t0 = time.perf_counter()
         m.rk3_step(DT, NSUB)
-    return nx * ny * NZ * steps, time.perf_counter() - t0
+        secs += time.perf_counter() - t0
+        if record is not None and i == 0:
+            record["x1"] = [m.get(q) for q in range(7)]
+    return nx * ny * NZ * steps, secs
+
+
+def oracle_errors(vg, nx, ny, record):
+    """Per-field max / RMS relative error of one GPU step (mixed and FP64)
+    from the oracle's state, against the oracle's next state, on the CPU
+    baseline's sample of the workload (each field over its own scale,
+    velocities over the common velocity scale; qv, zero in the dry case,
+    absolutely)."""
+    s = case_setup(vg.Setup, nx, ny)
+    x0, x1 = record["x0"], record["x1"]
+    ins = [vg.interior(s, q, x1[q]) for q in range(7)]
+    vs = max(float(np.abs(ins[q]).max()) for q in range(3))
+    out = {"sample": "%dx%dx%d horizontal sample of the workload (the CPU baseline's), one step from the "
+                     "oracle's state" % (nx, ny, NZ)}
+    for prec, name in ((vg.MIXED, "mixed"), (vg.FP64, "fp64")):
+        with vg.Model(s, prec) as m:
+            for q in range(7):
+                m.set(q, x0[q])
+            m.step(DT, NSUB, 1)
+            got = m.state()[:7]
+        fields = {}
+        for q in range(7):
+            scale = vs if q < 3 else float(np.abs(ins[q]).max())
+            scale = scale if scale > 0.0 else 1.0
+            d = vg.interior(s, q, got[q]) - ins[q]
+            fields[vg.SPECIES[q]] = {"max_rel": float(np.abs(d).max()) / scale,
+                                     "rms_rel": float(np.sqrt(np.mean(d * d))) / scale}
+        out[name] = {"max_rel": max(f["max_rel"] for f in fields.values()), "fields": fields}
+    return out
 
 
 # The CPU-runnable warm-bubble case (64 x 64 x 40, dx = dy = dz = 250 m,
@@ -629,7 +666,8 @@ def main():
     # CPU baseline first (rank 0 at N=1 only), before any CUDA work
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        cells, secs = cpu_sample_run((128, 128, 2, 0, 1))
+        oracle_record = {}
+        cells, secs = cpu_sample_run((128, 128, 2, 0, 1), oracle_record)
         cpu = {"value": cells / secs, "unit": UNIT, "cores": 1, "kind": "port",
                "sample": "128x128x80 horizontal sample of the workload, 2 RK3 steps, single thread (%.1f s)" % secs}
         c1, s1 = cpu_config1_run()
@@ -853,6 +891,7 @@ def main():
         line["physics_coupling"] = physics
     if cpu is not None:
         line["cpu_baseline"] = cpu
+        line["mixed_vs_oracle_error"] = oracle_errors(vg, 128, 128, oracle_record)
     print(json.dumps(line))
     ranks.close()
 
