@@ -118,11 +118,13 @@ def test_nested_step_equals_composition(vg, oc):
             n.step(DT, NSUB, 1)
             n.step_async(DT, NSUB, 1)
             n.wait()
-            per_nest = 1 + 2 * R + 1
+            # interpolation, R x (relaxation + the frame's working copy),
+            # restriction + the parent box's working copy
+            per_nest = 1 + 2 * R + 2
             # per stage 1 stage + NSUB column launches; the fix-up after
             # stages 1 and 2; stage 3's is in the finish
             group = 3 * (1 + NSUB) + 2 + 1
-            assert n.launches_per_step() == group + R * group + len(shapes) * per_nest + 2
+            assert n.launches_per_step() == group + R * group + len(shapes) * per_nest
         nests = [(c, s, pi, i, r) for c, (s, pi, i, r) in zip(b_c, shapes)]
         for _ in range(2):
             compose(oc, b_p, ps, nests, lambda m, dt: m.step(dt, NSUB, 1))

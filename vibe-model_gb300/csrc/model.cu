@@ -2170,15 +2170,29 @@ int nested_transfer(vibe_gb300_nested* n, int op, int c, int pp, int cp) {
     cin[q] = (op == 2) ? n->buf[c][q] : ch->S[cp][q];
     cout[q] = (op == 0) ? n->buf[c][q] : ch->S[cp][q];
   }
+  // (the boundary buffer is read only in the Davies zone: op 0 fills just that)
   const int rc = nest_model_layout(op, pl, n->nvars, pa->d.nx, pa->d.ny, pa->d.nz, pin, pa->d.P, pa->d.plane,
                                    ch->d.nx, ch->d.ny, ch->d.nz, cin, op == 1 ? pout : cout, ch->d.P, ch->d.plane,
-                                   n->stream);
+                                   n->stream, op == 0);
   ++n->launches;
   return rc == VIBE_C_OK ? 0 : fail(VIBE_GB300_EDEVICE, "nest transfer failed");
 }
 
-void to_working_on(vibe_gb300_nested* n, vibe_gb300_model* m, int parity) {
-  mixed_to_working(m->d, m->tab, m->S[parity], working_targets(m, m->W0), n->stream);
+// The FP32 working copy after a transfer changed the FP64 state, on the
+// points it changed: a nest's Davies frame after the relaxation, the
+// restriction box of a parent after the feedback. Elsewhere the working copy
+// the finish kernel wrote stands, as after any step.
+void to_working_frame(vibe_gb300_nested* n, int c, int parity) {
+  vibe_gb300_model* m = n->children[c];
+  mixed_to_working_region(m->d, m->tab, m->S[parity], working_targets(m, m->W0), 0, 0, m->d.nx + 1, m->d.ny + 1,
+                          n->pl_interp[c].boundary_zone, n->stream);
+  ++n->launches;
+}
+void to_working_box(vibe_gb300_nested* n, int c, int parity) {
+  vibe_gb300_model* m = n->parents[n->parent_of[c]];
+  const vibe_nest_placement& q = n->pl_restrict[c];
+  mixed_to_working_region(m->d, m->tab, m->S[parity], working_targets(m, m->W0), q.i0, q.j0, q.iext, q.jext, 0,
+                          n->stream);
   ++n->launches;
 }
 
@@ -2196,12 +2210,12 @@ int nested_enqueue(vibe_gb300_nested* n, int pp, int cp, int r) {
     cc = 1 - cc;
     for (int c = 0; c < nc; ++c) {
       if (int rc = nested_transfer(n, 2, c, pn, cc)) return rc;
-      to_working_on(n, n->children[c], cc);
+      to_working_frame(n, c, cc);
     }
   }
   for (int c = 0; c < nc; ++c)
     if (int rc = nested_transfer(n, 1, c, pn, cc)) return rc;
-  for (auto* p : n->parents) to_working_on(n, p, pn);
+  for (int c = 0; c < nc; ++c) to_working_box(n, c, pn);
   return 0;
 }
 

@@ -40,10 +40,12 @@ __device__ __forceinline__ double& at(const NestViews& v, int q, int i, int j, i
 }
 __device__ __forceinline__ double lerpd(double a, double b, double w) { return a + w * (b - a); }
 
+// zone_only: only the points of the Davies zone (what k_lateral reads)
 __global__ void k_interp(const __grid_constant__ NestArgs a, const __grid_constant__ NestViews P,
-                         const __grid_constant__ NestViews C) {
+                         const __grid_constant__ NestViews C, int zone_only) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y, k = blockIdx.z;
   if (i >= a.cnx || j >= a.cny) return;
+  if (zone_only && imin(imin(i, a.cnx - 1 - i), imin(j, a.cny - 1 - j)) >= a.nzone) return;
   const double xp = ((double)(a.i0 + i) + 0.5) * a.inv - 0.5;
   const double yp = ((double)(a.j0 + j) + 0.5) * a.inv - 0.5;
   const int ip = (int)floor(xp), jp = (int)floor(yp);
@@ -165,7 +167,7 @@ int run_dev(Op op, const vibe_nest_placement* p, int nvars, const int* stagger, 
     }
     const dim3 b(32, 8);
     if (op == INTERP)
-      k_interp<<<dim3((cnx + 31) / 32, (cny + 7) / 8, cnz), b, 0, s>>>(a, A, B);
+      k_interp<<<dim3((cnx + 31) / 32, (cny + 7) / 8, cnz), b, 0, s>>>(a, A, B, 0);
     else if (op == RESTRICT) {
       if (p->iext > 0 && p->jext > 0)
         k_restrict<<<dim3((p->iext + 31) / 32, (p->jext + 7) / 8, pnz), b, 0, s>>>(a, A, B);
@@ -246,7 +248,7 @@ int run_host(Op op, const vibe_nest_placement* p, int nvars, const int* stagger,
 int nest_model_layout(int op, const vibe_nest_placement* p, int nvars, int pnx, int pny, int pnz,
                       const double* const* parent, size_t p_pitch, size_t p_plane, int cnx, int cny, int cnz,
                       const double* const* child_in, double* const* out, size_t c_pitch, size_t c_plane,
-                      cudaStream_t s) {
+                      cudaStream_t s, bool zone_only) {
   if (!check_placement(p)) return VIBE_C_ERR_BAD_ARG;
   if (op == 1 && (p->i0 < 0 || p->j0 < 0 || p->i0 + p->iext > pnx + 1 || p->j0 + p->jext > pny + 1)) {
     g_nerr = "restriction box outside the parent";
@@ -277,7 +279,7 @@ int nest_model_layout(int op, const vibe_nest_placement* p, int nvars, int pnx, 
     }
     const dim3 b(32, 8);
     if (op == 0)
-      k_interp<<<dim3((cnx + 31) / 32, (cny + 7) / 8, cnz), b, 0, s>>>(a, A, B);
+      k_interp<<<dim3((cnx + 31) / 32, (cny + 7) / 8, cnz), b, 0, s>>>(a, A, B, zone_only ? 1 : 0);
     else if (op == 1) {
       if (p->iext > 0 && p->jext > 0)
         k_restrict<<<dim3((p->iext + 31) / 32, (p->jext + 7) / 8, pnz), b, 0, s>>>(a, A, B);

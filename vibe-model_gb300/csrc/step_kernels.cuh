@@ -67,10 +67,12 @@ struct MixedTune {
 void mixed_set_tune(const Dims& d, const MixedTune& t);
 int mixed_stage_levels(const Dims& d);
 
+// zone_only (op 0): interpolate only the points of the Davies zone, the
+// only ones op 2 reads (for a boundary buffer)
 int nest_model_layout(int op, const vibe_nest_placement* p, int nvars, int pnx, int pny, int pnz,
                       const double* const* parent, size_t p_pitch, size_t p_plane, int cnx, int cny, int cnz,
                       const double* const* child_in, double* const* out, size_t c_pitch, size_t c_plane,
-                      cudaStream_t s);
+                      cudaStream_t s, bool zone_only = false);
 
 // ---- mixed path (step_mixed.cu): FP64 state, FP32 working state ----
 // Horizontally uniform reference state on flat terrain: every coefficient
@@ -153,6 +155,11 @@ void mixed_batch_destroy(MixedBatch* b);
 void mixed_unpack_f32(const Dims& d, int nsx, int nsy, int nsz, int ni, int nj, int nk, const float* src, double* dst,
                       cudaStream_t stream);
 void mixed_to_working(const Dims& d, const Tab& t, double* const* s, const WS& w, cudaStream_t stream);
+// the same conversion on the columns of the box [ia, ia + ni) x [ja, ja + nj)
+// (clipped to the grid), and there, when frame > 0, only on the columns
+// within frame points of the lateral edge (min(i, nx-1-i, j, ny-1-j) < frame)
+void mixed_to_working_region(const Dims& d, const Tab& t, double* const* s, const WS& w, int ia, int ja, int ni,
+                             int nj, int frame, cudaStream_t stream);
 
 // ---- tangent-linear and adjoint of the slow tendency (step_tlad.cu) ----
 // base, pert, out, bar_*: 12 fields each, model layout (plane * (nz+1)

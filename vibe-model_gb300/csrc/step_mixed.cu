@@ -1239,12 +1239,8 @@ __global__ void k_mx_unpack_f32(Dims d, int nsx, int nsy, int nsz, int ni, int n
 }
 
 // FP64 state -> FP32 working copy in perturbation form, incl. ghosts.
-__device__ __forceinline__ void to_working_body(const Dims& d, const Tab& t, const CS64& s, const WS& w, int bx,
-                                                int by, int bz) {
-  const int i = bx * blockDim.x + threadIdx.x;
-  const int j = by * blockDim.y + threadIdx.y;
-  const int k = bz;
-  if (i > d.nx || j > d.ny || k > d.nz) return;
+__device__ __forceinline__ void to_working_point(const Dims& d, const Tab& t, const CS64& s, const WS& w, int i,
+                                                 int j, int k) {
   const size_t c = IX(i, j, k);
   if (j < d.ny && k < d.nz) w.f[U][c] = (float)s.f[U][c];
   if (i < d.nx && k < d.nz) w.f[V][c] = (float)s.f[V][c];
@@ -1257,9 +1253,28 @@ __device__ __forceinline__ void to_working_body(const Dims& d, const Tab& t, con
       if (w.f[q]) w.f[q][c] = (float)s.f[q][c];  // species without a target are not prognostic
   }
 }
+__device__ __forceinline__ void to_working_body(const Dims& d, const Tab& t, const CS64& s, const WS& w, int bx,
+                                                int by, int bz) {
+  const int i = bx * blockDim.x + threadIdx.x;
+  const int j = by * blockDim.y + threadIdx.y;
+  const int k = bz;
+  if (i > d.nx || j > d.ny || k > d.nz) return;
+  to_working_point(d, t, s, w, i, j, k);
+}
 __global__ void k_mx_to_working(const __grid_constant__ Dims d, const __grid_constant__ Tab t,
                                 const __grid_constant__ CS64 s, const __grid_constant__ WS w) {
   to_working_body(d, t, s, w, blockIdx.x, blockIdx.y, blockIdx.z);
+}
+// the columns of a box, or of the lateral frame within it (frame > 0)
+__global__ void k_mx_to_working_region(const __grid_constant__ Dims d, const __grid_constant__ Tab t,
+                                       const __grid_constant__ CS64 s, const __grid_constant__ WS w, int ia, int ja,
+                                       int ib, int jb, int frame) {
+  const int i = ia + blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = ja + blockIdx.y * blockDim.y + threadIdx.y;
+  const int k = blockIdx.z;
+  if (i >= ib || j >= jb || k > d.nz) return;
+  if (frame > 0 && imin(imin(i, d.nx - 1 - i), imin(j, d.ny - 1 - j)) >= frame) return;
+  to_working_point(d, t, s, w, i, j, k);
 }
 
 }  // namespace
@@ -2668,6 +2683,16 @@ void mixed_finish(const Dims& d, const Tab& t, const Flags& fl, const WS& wfin, 
 void mixed_unpack_f32(const Dims& d, int nsx, int nsy, int nsz, int ni, int nj, int nk, const float* src, double* dst,
                       cudaStream_t stream) {
   k_mx_unpack_f32<<<1024, 256, 0, stream>>>(d, nsx, nsy, nsz, ni, nj, nk, src, dst);
+}
+
+void mixed_to_working_region(const Dims& d, const Tab& t, double* const* s, const WS& w, int ia, int ja, int ni,
+                             int nj, int frame, cudaStream_t stream) {
+  const int a0 = imax(ia, 0), b0 = imax(ja, 0);
+  const int a1 = imin(ia + ni, d.nx + 1), b1 = imin(ja + nj, d.ny + 1);
+  if (a1 <= a0 || b1 <= b0) return;
+  const dim3 b(32, 4);
+  k_mx_to_working_region<<<g3(a1 - a0, b1 - b0, d.nz + 1, b), b, 0, stream>>>(d, t, cs64(s), w, a0, b0, a1, b1,
+                                                                              frame);
 }
 
 void mixed_to_working(const Dims& d, const Tab& t, double* const* s, const WS& w, cudaStream_t stream) {
