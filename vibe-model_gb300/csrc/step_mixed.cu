@@ -2752,14 +2752,16 @@ __device__ __forceinline__ int find_domain(const int* __restrict__ start, int nd
   return dom;
 }
 
-template <bool kRaw>
+// kSpec: every domain runs the composition the single-domain kSpec kernel
+// fixes at compile time (the flags are common to a batch)
+template <bool kRaw, bool kSpec>
 __global__ void __launch_bounds__(NT, 3) k_b_stage(const StageArgs* __restrict__ A, const int* __restrict__ start,
                                                    int nd, unsigned* err) {
   const int dom = find_domain(start, nd);
   const StageArgs& a = A[dom];
   const int l = (int)blockIdx.x - start[dom];
-  stage_body<kRaw, false>(a.d, a.t, a.fl, a.M, a.win, a.w0, a.wout, a.rout, a.dts, a.kchunk, err, l % a.gx,
-                   (l / a.gx) % a.gy, l / (a.gx * a.gy));
+  stage_body<kRaw, kSpec>(a.d, a.t, a.fl, a.M, a.win, a.w0, a.wout, a.rout, a.dts, a.kchunk, err, l % a.gx,
+                          (l / a.gx) % a.gy, l / (a.gx * a.gy));
 }
 
 __global__ void __launch_bounds__(128, 7) k_b_hevi(const HeviArgs* __restrict__ A, const int* __restrict__ start,
@@ -2835,6 +2837,7 @@ struct MixedBatch {
   size_t hevi_smem = 0;
   bool hevi_tma = false;  // TMA-fed column body (else the cp.async two-column body)
   bool defer = false;     // the TMA body defers its w/rho' corrections (u/v launches become fix-ups)
+  bool spec = false;      // the stage body with the flags of the kSpec composition fixed
   unsigned* err = nullptr;
 };
 
@@ -2870,6 +2873,7 @@ MixedBatch* mixed_batch_build(const std::vector<MixedDomain>& doms, const Flags&
   b->err = err;
   b->hevi_tma = hevi_tma() && hevi_tma_smem_bytes(nz) <= 48 * 1024;
   b->defer = b->hevi_tma && hevi_defer();
+  b->spec = stage_spec(fl);
   b->hevi_smem = b->hevi_tma ? hevi_tma_smem_bytes(nz) : hevi2_smem_bytes(nz, kBatchTwoRing);
   const double dts[3] = {dt / 3.0, dt / 2.0, dt};
   const int nd = (int)doms.size();
@@ -2986,10 +2990,14 @@ void mixed_batch_enqueue(const MixedBatch* b, cudaStream_t s) {
   for (const auto& L : b->seq) {
     switch (L.kind) {
       case 0:
-        if (L.raw)
-          k_b_stage<true><<<L.blocks, dim3(TX, TY), 0, s>>>((const StageArgs*)L.args, L.start, L.nd, b->err);
+        if (L.raw && b->spec)
+          k_b_stage<true, true><<<L.blocks, dim3(TX, TY), 0, s>>>((const StageArgs*)L.args, L.start, L.nd, b->err);
+        else if (L.raw)
+          k_b_stage<true, false><<<L.blocks, dim3(TX, TY), 0, s>>>((const StageArgs*)L.args, L.start, L.nd, b->err);
+        else if (b->spec)
+          k_b_stage<false, true><<<L.blocks, dim3(TX, TY), 0, s>>>((const StageArgs*)L.args, L.start, L.nd, b->err);
         else
-          k_b_stage<false><<<L.blocks, dim3(TX, TY), 0, s>>>((const StageArgs*)L.args, L.start, L.nd, b->err);
+          k_b_stage<false, false><<<L.blocks, dim3(TX, TY), 0, s>>>((const StageArgs*)L.args, L.start, L.nd, b->err);
         break;
       case 1:
         if (b->defer)
