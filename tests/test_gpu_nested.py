@@ -118,9 +118,9 @@ def test_nested_step_equals_composition(vg, oc):
             n.step(DT, NSUB, 1)
             n.step_async(DT, NSUB, 1)
             n.wait()
-            # interpolation, R x (relaxation + the frame's working copy),
-            # restriction + the parent box's working copy
-            per_nest = 1 + 2 * R + 2
+            # interpolation, R relaxations (each with its frame's working
+            # copy), restriction + the parent box's working copy
+            per_nest = 1 + R + 2
             # per stage 1 stage + NSUB column launches; the fix-up after
             # stages 1 and 2; stage 3's is in the finish
             group = 3 * (1 + NSUB) + 2 + 1

@@ -2146,6 +2146,7 @@ struct vibe_gb300_nested {
   vibe_gb300_group* gp = nullptr;
   vibe_gb300_group* gc = nullptr;
   std::vector<std::vector<double*>> buf;  // per nest: boundary buffer (FP64, model layout)
+  std::vector<std::vector<double>> davies;  // per nest: the Davies weights of its zone
   std::vector<void*> allocs;
   cudaStream_t stream = nullptr;
   cudaGraphExec_t graph[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};  // [parent parity][nest parity]
@@ -2179,14 +2180,16 @@ int nested_transfer(vibe_gb300_nested* n, int op, int c, int pp, int cp) {
 }
 
 // The FP32 working copy after a transfer changed the FP64 state, on the
-// points it changed: a nest's Davies frame after the relaxation, the
-// restriction box of a parent after the feedback. Elsewhere the working copy
-// the finish kernel wrote stands, as after any step.
-void to_working_frame(vibe_gb300_nested* n, int c, int parity) {
+// points it changed: a nest's Davies frame (in the relaxation's own launch),
+// the restriction box of a parent after the feedback. Elsewhere the working
+// copy the finish kernel wrote stands, as after any step.
+int relax_nest(vibe_gb300_nested* n, int c, int parity) {
   vibe_gb300_model* m = n->children[c];
-  mixed_to_working_region(m->d, m->tab, m->S[parity], working_targets(m, m->W0), 0, 0, m->d.nx + 1, m->d.ny + 1,
-                          n->pl_interp[c].boundary_zone, n->stream);
   ++n->launches;
+  if (mixed_nest_relax(m->d, m->tab, m->S[parity], n->buf[c].data(), n->nvars, n->davies[c].data(),
+                       n->pl_interp[c].boundary_zone, working_targets(m, m->W0), n->stream))
+    return fail(VIBE_GB300_EBADARG, "bad Davies zone");
+  return 0;
 }
 void to_working_box(vibe_gb300_nested* n, int c, int parity) {
   vibe_gb300_model* m = n->parents[n->parent_of[c]];
@@ -2208,10 +2211,8 @@ int nested_enqueue(vibe_gb300_nested* n, int pp, int cp, int r) {
   for (int sub = 0; sub < r; ++sub) {
     mixed_batch_enqueue(n->gc->batch[cc], n->stream);
     cc = 1 - cc;
-    for (int c = 0; c < nc; ++c) {
-      if (int rc = nested_transfer(n, 2, c, pn, cc)) return rc;
-      to_working_frame(n, c, cc);
-    }
+    for (int c = 0; c < nc; ++c)
+      if (int rc = relax_nest(n, c, cc)) return rc;
   }
   for (int c = 0; c < nc; ++c)
     if (int rc = nested_transfer(n, 1, c, pn, cc)) return rc;
@@ -2275,6 +2276,10 @@ int vibe_gb300_nested_create(vibe_gb300_model* const* parents, int np, vibe_gb30
       }
     }
     n->buf.push_back(b);
+    std::vector<double> dw(64, 0.0);
+    if (!rc && vibe_davies_profile(interp_pl[c].boundary_zone, 1.0, dw.data()) != 0)
+      rc = fail(VIBE_GB300_EBADARG, "Davies profile");
+    n->davies.push_back(dw);
   }
   if (rc) {
     vibe_gb300_nested_destroy(n);

@@ -40,12 +40,8 @@ __device__ __forceinline__ double& at(const NestViews& v, int q, int i, int j, i
 }
 __device__ __forceinline__ double lerpd(double a, double b, double w) { return a + w * (b - a); }
 
-// zone_only: only the points of the Davies zone (what k_lateral reads)
-__global__ void k_interp(const __grid_constant__ NestArgs a, const __grid_constant__ NestViews P,
-                         const __grid_constant__ NestViews C, int zone_only) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y, k = blockIdx.z;
-  if (i >= a.cnx || j >= a.cny) return;
-  if (zone_only && imin(imin(i, a.cnx - 1 - i), imin(j, a.cny - 1 - j)) >= a.nzone) return;
+__device__ __forceinline__ void interp_point(const NestArgs& a, const NestViews& P, const NestViews& C, int i, int j,
+                                             int k) {
   const double xp = ((double)(a.i0 + i) + 0.5) * a.inv - 0.5;
   const double yp = ((double)(a.j0 + j) + 0.5) * a.inv - 0.5;
   const int ip = (int)floor(xp), jp = (int)floor(yp);
@@ -57,6 +53,22 @@ __global__ void k_interp(const __grid_constant__ NestArgs a, const __grid_consta
     at(C, q, i, j, k) = lerpd(lerpd(at(P, q, i0, j0, kp), at(P, q, i1, j0, kp), wx),
                               lerpd(at(P, q, i0, j1, kp), at(P, q, i1, j1, kp), wx), wy);
   }
+}
+__global__ void k_interp(const __grid_constant__ NestArgs a, const __grid_constant__ NestViews P,
+                         const __grid_constant__ NestViews C) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y, k = blockIdx.z;
+  if (i >= a.cnx || j >= a.cny) return;
+  interp_point(a, P, C, i, j, k);
+}
+// only the points of the Davies zone (the ones k_lateral reads), one thread
+// per (frame column, level)
+__global__ void k_interp_zone(const __grid_constant__ NestArgs a, const __grid_constant__ NestViews P,
+                              const __grid_constant__ NestViews C, int nframe) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x, k = blockIdx.z;
+  if (e >= nframe) return;
+  int i, j;
+  frame_column(e, a.cnx, a.cny, a.nzone, i, j);
+  interp_point(a, P, C, i, j, k);
 }
 
 __global__ void k_restrict(const __grid_constant__ NestArgs a, const __grid_constant__ NestViews C,
@@ -167,7 +179,7 @@ int run_dev(Op op, const vibe_nest_placement* p, int nvars, const int* stagger, 
     }
     const dim3 b(32, 8);
     if (op == INTERP)
-      k_interp<<<dim3((cnx + 31) / 32, (cny + 7) / 8, cnz), b, 0, s>>>(a, A, B, 0);
+      k_interp<<<dim3((cnx + 31) / 32, (cny + 7) / 8, cnz), b, 0, s>>>(a, A, B);
     else if (op == RESTRICT) {
       if (p->iext > 0 && p->jext > 0)
         k_restrict<<<dim3((p->iext + 31) / 32, (p->jext + 7) / 8, pnz), b, 0, s>>>(a, A, B);
@@ -278,8 +290,11 @@ int nest_model_layout(int op, const vibe_nest_placement* p, int nvars, int pnx, 
       }
     }
     const dim3 b(32, 8);
-    if (op == 0)
-      k_interp<<<dim3((cnx + 31) / 32, (cny + 7) / 8, cnz), b, 0, s>>>(a, A, B, zone_only ? 1 : 0);
+    if (op == 0 && zone_only) {
+      const int nf = frame_count(cnx, cny, a.nzone);
+      k_interp_zone<<<dim3((nf + 127) / 128, 1, cnz), 128, 0, s>>>(a, A, B, nf);
+    } else if (op == 0)
+      k_interp<<<dim3((cnx + 31) / 32, (cny + 7) / 8, cnz), b, 0, s>>>(a, A, B);
     else if (op == 1) {
       if (p->iext > 0 && p->jext > 0)
         k_restrict<<<dim3((p->iext + 31) / 32, (p->jext + 7) / 8, pnz), b, 0, s>>>(a, A, B);

@@ -160,6 +160,11 @@ void mixed_to_working(const Dims& d, const Tab& t, double* const* s, const WS& w
 // within frame points of the lateral edge (min(i, nx-1-i, j, ny-1-j) < frame)
 void mixed_to_working_region(const Dims& d, const Tab& t, double* const* s, const WS& w, int ia, int ja, int ni,
                              int nj, int frame, cudaStream_t stream);
+// a nest's Davies relaxation of its FP64 state s toward the boundary buffer
+// bnd (first nvars fields, the weights davies[0..nzone)) fused with the FP32
+// working copy of the points it changes; -1 on bad arguments
+int mixed_nest_relax(const Dims& d, const Tab& t, double* const* s, const double* const* bnd, int nvars,
+                     const double* davies, int nzone, const WS& w, cudaStream_t stream);
 
 // ---- tangent-linear and adjoint of the slow tendency (step_tlad.cu) ----
 // base, pert, out, bar_*: 12 fields each, model layout (plane * (nz+1)

@@ -2685,6 +2685,49 @@ void mixed_unpack_f32(const Dims& d, int nsx, int nsy, int nsz, int ni, int nj, 
   k_mx_unpack_f32<<<1024, 256, 0, stream>>>(d, nsx, nsy, nsz, ni, nj, nk, src, dst);
 }
 
+namespace {
+struct DaviesW {
+  double a[64];
+};
+// A nest's Davies relaxation toward its boundary buffer (apply_lateral_boundary,
+// nest.cpp:107-124: c = (1 - alpha(d)) c + alpha(d) b on the points within
+// nzone of the lateral edge, d their distance to it) and, at the same points,
+// the FP32 working copy of the relaxed state. One thread per (frame column,
+// level); the products and the sum rounded one by one as the reference
+// computes them (no fused multiply-add).
+__global__ void k_mx_nest_relax(const __grid_constant__ Dims d, const __grid_constant__ Tab t,
+                                const __grid_constant__ MS64 s, const __grid_constant__ CS64 bnd, int nvars,
+                                const __grid_constant__ DaviesW dw, int nzone, int nframe,
+                                const __grid_constant__ WS w) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x, k = blockIdx.z;
+  if (e >= nframe) return;
+  int i, j;
+  frame_column(e, d.nx, d.ny, nzone, i, j);
+  const double alpha = dw.a[imin(imin(i, d.nx - 1 - i), imin(j, d.ny - 1 - j))];
+  const size_t c = IX(i, j, k);
+  for (int q = 0; q < nvars; ++q) {
+    const double v = s.f[q][c];
+    s.f[q][c] = __dadd_rn(__dmul_rn(__dsub_rn(1.0, alpha), v), __dmul_rn(alpha, bnd.f[q][c]));
+  }
+  CS64 r;
+  for (int q = 0; q < NSPECIES; ++q) r.f[q] = s.f[q];
+  to_working_point(d, t, r, w, i, j, k);
+}
+}  // namespace
+
+int mixed_nest_relax(const Dims& d, const Tab& t, double* const* s, const double* const* bnd, int nvars,
+                     const double* davies, int nzone, const WS& w, cudaStream_t stream) {
+  if (nzone < 1 || nzone > 64 || nvars < 1 || nvars > NSPECIES) return -1;
+  DaviesW dw{};
+  for (int q = 0; q < nzone; ++q) dw.a[q] = davies[q];
+  MS64 sm = ms64(s);
+  CS64 bm;
+  for (int q = 0; q < NSPECIES; ++q) bm.f[q] = q < nvars ? bnd[q] : nullptr;
+  const int nf = frame_count(d.nx, d.ny, nzone);
+  k_mx_nest_relax<<<dim3((nf + 127) / 128, 1, d.nz), 128, 0, stream>>>(d, t, sm, bm, nvars, dw, nzone, nf, w);
+  return 0;
+}
+
 void mixed_to_working_region(const Dims& d, const Tab& t, double* const* s, const WS& w, int ia, int ja, int ni,
                              int nj, int frame, cudaStream_t stream) {
   const int a0 = imax(ia, 0), b0 = imax(ja, 0);

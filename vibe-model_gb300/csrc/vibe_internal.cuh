@@ -76,6 +76,37 @@ __host__ __device__ inline int iclamp(int v, int lo, int hi) { return v < lo ? l
 __host__ __device__ inline int imin(int a, int b) { return (b < a) ? b : a; }
 __host__ __device__ inline int imax(int a, int b) { return (a < b) ? b : a; }
 __host__ __device__ inline double dmax(double a, double b) { return (a < b) ? b : a; }
+
+// The lateral frame of an nx x ny cell grid: the columns within f points of
+// its edge (min(i, nx-1-i, j, ny-1-j) < f), numbered bottom rows, top rows,
+// then the left and right ends of the rows between. frame_count gives how
+// many, frame_column the e-th one.
+__host__ __device__ inline void frame_shape(int nx, int ny, int f, int& rb, int& rt, int& cl, int& cr) {
+  rb = imin(f, ny);
+  rt = imin(f, ny - rb);
+  const int mid = ny - rb - rt;
+  cl = mid > 0 ? imin(f, nx) : 0;
+  cr = mid > 0 ? imin(f, nx - cl) : 0;
+}
+__host__ __device__ inline int frame_count(int nx, int ny, int f) {
+  int rb, rt, cl, cr;
+  frame_shape(nx, ny, f, rb, rt, cl, cr);
+  return (rb + rt) * nx + (ny - rb - rt) * (cl + cr);
+}
+__host__ __device__ inline void frame_column(int e, int nx, int ny, int f, int& i, int& j) {
+  int rb, rt, cl, cr;
+  frame_shape(nx, ny, f, rb, rt, cl, cr);
+  const int nrow = (rb + rt) * nx;
+  if (e < nrow) {
+    const int r = e / nx;
+    i = e - r * nx;
+    j = r < rb ? r : ny - rt + (r - rb);
+  } else {
+    const int e2 = e - nrow, w = cl + cr, r = e2 / w, c = e2 - r * w;
+    j = rb + r;
+    i = c < cl ? c : nx - cr + (c - cl);
+  }
+}
 __host__ __device__ inline float fmaxr(float a, float b) { return (a < b) ? b : a; }
 
 // Error word bits written by kernels, read by the host once per step.
