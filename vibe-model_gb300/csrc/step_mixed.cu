@@ -317,7 +317,7 @@ __device__ __forceinline__ void stage_body(const Dims& d, const Tab& t, const Fl
                                            const WS& win, const WS& w0, const WS& wout, const WS& rout, float dts,
                                            int kchunk, unsigned* err, int bx, int by, int bz) {
   __shared__ __align__(128) float sbuf[kStageRing][kBuf];
-  __shared__ __align__(128) float sQm[R3 * TW];  // moisture species beyond qv (plain loads)
+  __shared__ __align__(128) float sQm[R3 * TW], sQm2[R3 * TW];  // a pair of moisture species beyond qv (plain loads)
   __shared__ float sFx[2][TY * (TX + 1)], sFy[2][(TY + 1) * TX];  // theta' / qv (or one moisture species)
   __shared__ __align__(8) unsigned long long sbar[kStageRing];
   // the flags, fixed at compile time for the kSpec composition
@@ -594,15 +594,15 @@ __device__ __forceinline__ void stage_body(const Dims& d, const Tab& t, const Fl
     // loaded in upwind order by choosing the addresses; x and y faces share
     // one code path with the stencil stride chosen per face. Same face values
     // as hflux up to rounding.
-    auto hflux_pair = [&]() {
+    auto hflux_pair = [&](const float* A, const float* B) {  // species A and B (theta', qv or a moisture pair)
       // one x and one y face pair per thread: its cell's left and lower
       // faces; the top row's y faces go to warp 0 and the right column's x
       // faces to lanes 0..7 of warp 1 as a third (no warp diverges on it)
       auto face = [&](int off, int st, float vel, bool valid, float* d0, float* d1) {
         const int sp = vel >= 0.f ? st : -st;  // upwind order
-        const F2 a0 = mk2(sT[off - 2 * sp], sQ[off - 2 * sp]), a1 = mk2(sT[off - sp], sQ[off - sp]);
-        const F2 a2 = mk2(sT[off], sQ[off]), a3 = mk2(sT[off + sp], sQ[off + sp]);
-        const F2 a4 = mk2(sT[off + 2 * sp], sQ[off + 2 * sp]);
+        const F2 a0 = mk2(A[off - 2 * sp], B[off - 2 * sp]), a1 = mk2(A[off - sp], B[off - sp]);
+        const F2 a2 = mk2(A[off], B[off]), a3 = mk2(A[off + sp], B[off + sp]);
+        const F2 a4 = mk2(A[off + 2 * sp], B[off + 2 * sp]);
         float Ft, Fq;
         un2(weno_flux2(a0, a1, a2, a3, a4, vel), Ft, Fq);
         *d0 = valid ? Ft : 0.f;
@@ -661,7 +661,7 @@ __device__ __forceinline__ void stage_body(const Dims& d, const Tab& t, const Fl
     const float tshift = (k > 0) ? -t.t0d[6 * (k - 1) + 4] : 0.f;
     float ftT = 0.f, fbT = 0.f, ftQ = 0.f, fbQ = 0.f;  // vertical face fluxes of theta' and qv
     if (f_weno) {
-      hflux_pair();
+      hflux_pair(sT, sQ);
       if (cell) {  // the top face's pair, carried up as the next level's bottom face
         const F2 z1 = mk2(wT[1] + sh[1], wQ[1]), z2 = mk2(wT[2] + sh[2], wQ[2]);
         const F2 z4 = mk2(wT[4] + sh[4], wQ[4]), z5 = mk2(wT[5] + sh[5], wQ[5]);
@@ -681,26 +681,37 @@ __device__ __forceinline__ void stage_body(const Dims& d, const Tab& t, const Fl
     scalar(THETA, sT, 0, ftT, fbT, wT[2] + sh[2], wT[4] + sh[4]);
     scalar(QV, sQ, 1, ftQ, fbQ, wQ[2], wQ[4]);
     if (f_moist) {
-      for (int q = QC; q <= QG; ++q) {
-        __syncthreads();  // sQm and the flux slots are no longer read
-        load_box3(sQm, win.f[q] + (unsigned)k * pl, P, i0, j0, nx - 1, ny - 1);
+      // the moisture species in pairs (qc qr, qi qs, and qg with itself),
+      // each pair's faces reconstructed as one f32x2 pair like theta' and qv
+      for (int qa = QC; qa <= QG; qa += 2) {
+        const int qb = (qa + 1 <= QG) ? qa + 1 : qa;
+        __syncthreads();  // sQm, sQm2 and the flux slots are no longer read
+        load_box3(sQm, win.f[qa] + (unsigned)k * pl, P, i0, j0, nx - 1, ny - 1);
+        if (qb != qa) load_box3(sQm2, win.f[qb] + (unsigned)k * pl, P, i0, j0, nx - 1, ny - 1);
         __syncthreads();
+        const float* const QB = (qb != qa) ? sQm2 : sQm;
         if (f_weno) {
-          hflux(sQm, 0);
+          hflux_pair(sQm, QB);
           __syncthreads();
         }
-        float z[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-        float ft = 0.f, fb = 0.f;
+        float za[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f}, zb[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+        float fta = 0.f, fba = 0.f, ftb = 0.f, fbb = 0.f;
         if (cell) {
 #pragma unroll
-          for (int m = 0; m < 6; ++m) z[m] = win.f[q][(unsigned)iclamp(k + m - 3, 0, nz - 1) * pl + colc];
+          for (int m = 0; m < 6; ++m) {
+            const unsigned o = (unsigned)iclamp(k + m - 3, 0, nz - 1) * pl + colc;
+            za[m] = win.f[qa][o];
+            zb[m] = win.f[qb][o];
+          }
           if (f_weno) {
-            const float qc = sQm[o3];
-            ft = weno_face_f(z[1], z[2], qc, z[4], z[5], wt);
-            fb = weno_face_f(z[0], z[1], z[2], qc, z[4], wk);
+            const F2 z1 = mk2(za[1], zb[1]), z2 = mk2(za[2], zb[2]), z4 = mk2(za[4], zb[4]);
+            const F2 qc2 = mk2(sQm[o3], QB[o3]);
+            un2(weno_vflux2(z1, z2, qc2, z4, mk2(za[5], zb[5]), wt), fta, ftb);
+            un2(weno_vflux2(mk2(za[0], zb[0]), z1, z2, qc2, z4, wk), fba, fbb);
           }
         }
-        scalar(q, sQm, 0, ft, fb, z[2], z[4]);
+        scalar(qa, sQm, 0, fta, fba, za[2], za[4]);
+        if (qb != qa) scalar(qb, QB, 1, ftb, fbb, zb[2], zb[4]);
       }
     }
     // slide the column registers up one level
