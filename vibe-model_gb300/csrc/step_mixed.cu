@@ -1977,6 +1977,18 @@ __device__ __forceinline__ void hevi_tma_body(const Dims& d, const Tab& t, const
     if (two) *reinterpret_cast<float2*>(p) = make_float2(a, c);
     else *p = a;
   };
+  // L2 policies: the outputs stream out (the next substep reads them a whole
+  // launch later), the parked pi' of the forward sweep is read back by this
+  // block's backward sweep
+  unsigned long long pol_first, pol_last;
+  asm("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(pol_first));
+  asm("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(pol_last));
+  auto st2p = [&](float* p, float a, float c, unsigned long long pol) {
+    if (two)
+      asm volatile("st.global.L2::cache_hint.v2.f32 [%0], {%1, %2}, %3;" ::"l"(p), "f"(a), "f"(c), "l"(pol) : "memory");
+    else
+      asm volatile("st.global.L2::cache_hint.f32 [%0], %1, %2;" ::"l"(p), "f"(a), "l"(pol) : "memory");
+  };
   if (!level_ready(0)) return;
   float pk[2], wk[2], wtk[2], dpp[2] = {0.f, 0.f};
   {
@@ -2048,17 +2060,17 @@ __device__ __forceinline__ void hevi_tma_body(const Dims& d, const Tab& t, const
       rsv[c] = r0v[c] + dtau * S;
     }
     if (active) {
-      st2(Uo + o, u0[0], u0[1]);
-      st2(Vo + o, v0[0], v0[1]);
+      st2p(Uo + o, u0[0], u0[1], pol_first);
+      st2p(Vo + o, v0[0], v0[1], pol_first);
       if (two) {
         if (i + 1 == d.nx - 1) Uo[o + 2] = u1[1];  // face nx
       } else {
         Uo[o + 1] = u1[0];
       }
       if (last_j) st2(Vo + o + vn, v1[0], v1[1]);
-      st2(Po + o, dpk[0], dpk[1]);
-      st2(Ro + o, rsv[0], rsv[1]);
-      st2(Wo + o + pl, wtk1[0], wtk1[1]);
+      st2p(Po + o, dpk[0], dpk[1], pol_last);
+      st2p(Ro + o, rsv[0], rsv[1], pol_first);
+      st2p(Wo + o + pl, wtk1[0], wtk1[1], pol_first);
     }
 #pragma unroll
     for (int c = 0; c < 2; ++c) {
@@ -2119,7 +2131,7 @@ __device__ __forceinline__ void hevi_tma_body(const Dims& d, const Tab& t, const
       float xk[2];
 #pragma unroll
       for (int c = 0; c < 2; ++c) xk[c] = (k >= 0) ? (c == 0 ? fd.x : fd.y) - s_lc[k] * xu[c] : 0.f;
-      if (active) st2(Po + (size_t)kk * pl, xu[0], xu[1]);
+      if (active) st2p(Po + (size_t)kk * pl, xu[0], xu[1], pol_first);
       xu[0] = xk[0];
       xu[1] = xk[1];
       continue;
