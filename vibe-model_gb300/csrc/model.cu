@@ -2194,7 +2194,7 @@ int relax_nest(vibe_gb300_nested* n, int c, int parity) {
 void to_working_box(vibe_gb300_nested* n, int c, int parity) {
   vibe_gb300_model* m = n->parents[n->parent_of[c]];
   const vibe_nest_placement& q = n->pl_restrict[c];
-  mixed_to_working_region(m->d, m->tab, m->S[parity], working_targets(m, m->W0), q.i0, q.j0, q.iext, q.jext, 0,
+  mixed_to_working_region(m->d, m->tab, m->S[parity], working_targets(m, m->W0), q.i0, q.j0, q.iext, q.jext,
                           n->stream);
   ++n->launches;
 }

@@ -156,10 +156,9 @@ void mixed_unpack_f32(const Dims& d, int nsx, int nsy, int nsz, int ni, int nj, 
                       cudaStream_t stream);
 void mixed_to_working(const Dims& d, const Tab& t, double* const* s, const WS& w, cudaStream_t stream);
 // the same conversion on the columns of the box [ia, ia + ni) x [ja, ja + nj)
-// (clipped to the grid), and there, when frame > 0, only on the columns
-// within frame points of the lateral edge (min(i, nx-1-i, j, ny-1-j) < frame)
+// (clipped to the grid)
 void mixed_to_working_region(const Dims& d, const Tab& t, double* const* s, const WS& w, int ia, int ja, int ni,
-                             int nj, int frame, cudaStream_t stream);
+                             int nj, cudaStream_t stream);
 // a nest's Davies relaxation of its FP64 state s toward the boundary buffer
 // bnd (first nvars fields, the weights davies[0..nzone)) fused with the FP32
 // working copy of the points it changes; -1 on bad arguments

@@ -1276,15 +1276,14 @@ __global__ void k_mx_to_working(const __grid_constant__ Dims d, const __grid_con
                                 const __grid_constant__ CS64 s, const __grid_constant__ WS w) {
   to_working_body(d, t, s, w, blockIdx.x, blockIdx.y, blockIdx.z);
 }
-// the columns of a box, or of the lateral frame within it (frame > 0)
+// the columns of a box [ia, ib) x [ja, jb)
 __global__ void k_mx_to_working_region(const __grid_constant__ Dims d, const __grid_constant__ Tab t,
                                        const __grid_constant__ CS64 s, const __grid_constant__ WS w, int ia, int ja,
-                                       int ib, int jb, int frame) {
+                                       int ib, int jb) {
   const int i = ia + blockIdx.x * blockDim.x + threadIdx.x;
   const int j = ja + blockIdx.y * blockDim.y + threadIdx.y;
   const int k = blockIdx.z;
   if (i >= ib || j >= jb || k > d.nz) return;
-  if (frame > 0 && imin(imin(i, d.nx - 1 - i), imin(j, d.ny - 1 - j)) >= frame) return;
   to_working_point(d, t, s, w, i, j, k);
 }
 
@@ -2752,13 +2751,12 @@ int mixed_nest_relax(const Dims& d, const Tab& t, double* const* s, const double
 }
 
 void mixed_to_working_region(const Dims& d, const Tab& t, double* const* s, const WS& w, int ia, int ja, int ni,
-                             int nj, int frame, cudaStream_t stream) {
+                             int nj, cudaStream_t stream) {
   const int a0 = imax(ia, 0), b0 = imax(ja, 0);
   const int a1 = imin(ia + ni, d.nx + 1), b1 = imin(ja + nj, d.ny + 1);
   if (a1 <= a0 || b1 <= b0) return;
   const dim3 b(32, 4);
-  k_mx_to_working_region<<<g3(a1 - a0, b1 - b0, d.nz + 1, b), b, 0, stream>>>(d, t, cs64(s), w, a0, b0, a1, b1,
-                                                                              frame);
+  k_mx_to_working_region<<<g3(a1 - a0, b1 - b0, d.nz + 1, b), b, 0, stream>>>(d, t, cs64(s), w, a0, b0, a1, b1);
 }
 
 void mixed_to_working(const Dims& d, const Tab& t, double* const* s, const WS& w, cudaStream_t stream) {
