@@ -559,11 +559,12 @@ __device__ __forceinline__ void stage_body(const Dims& d, const Tab& t, const Fl
     const bool vert = (k + 2 < nz || k >= 2);
     const float* sh = t.t0d + 6 * k;  // theta0(clamp(k+m)) - theta0(k), m = -3..2
     const float divh = (sU[o1 + 1] - sU[o1]) * t.dx_inv + (sV[o1 + TW] - sV[o1]) * t.dy_inv;
-    // one species: Q = its box at level k; z0..z5 = its column at k-3..k+2
-    // (z3 unused: the box holds it); fc = carried flux, updated. With WENO,
-    // the horizontal face fluxes of a species are first computed into
-    // sFx[slot] / sFy[slot] by hflux (all threads), and after one barrier
-    // scalar reads them; theta' and qv share that barrier pair.
+    // A species' box at level k is Q. With WENO its horizontal face fluxes
+    // are first computed into sFx[0][slot] / sFy[0][slot] by all threads
+    // (hflux for one species, hflux_pair for two as an f32x2 pair: slots 0
+    // and 1), and after one barrier `scalar` reads them with the vertical
+    // face fluxes; theta' and qv share that barrier, as do the two species of
+    // a moisture pair.
     auto hflux = [&](const float* Q, int slot) {
 #pragma unroll
       for (int e = 0; e < 2; ++e) {
