@@ -560,7 +560,7 @@ __device__ __forceinline__ void stage_body(const Dims& d, const Tab& t, const Fl
     const float* sh = t.t0d + 6 * k;  // theta0(clamp(k+m)) - theta0(k), m = -3..2
     const float divh = (sU[o1 + 1] - sU[o1]) * t.dx_inv + (sV[o1 + TW] - sV[o1]) * t.dy_inv;
     // A species' box at level k is Q. With WENO its horizontal face fluxes
-    // are first computed into sFx[0][slot] / sFy[0][slot] by all threads
+    // are first computed into sFx[slot] / sFy[slot] by all threads
     // (hflux for one species, hflux_pair for two as an f32x2 pair: slots 0
     // and 1), and after one barrier `scalar` reads them with the vertical
     // face fluxes; theta' and qv share that barrier, as do the two species of
