@@ -318,7 +318,7 @@ __device__ __forceinline__ void stage_body(const Dims& d, const Tab& t, const Fl
                                            int kchunk, unsigned* err, int bx, int by, int bz) {
   __shared__ __align__(128) float sbuf[kStageRing][kBuf];
   __shared__ __align__(128) float sQm[R3 * TW], sQm2[R3 * TW];  // a pair of moisture species beyond qv (plain loads)
-  __shared__ float sFx[2][TY * (TX + 1)], sFy[2][(TY + 1) * TX];  // theta' / qv (or one moisture species)
+  __shared__ float sFx[2][TY * (TX + 1)], sFy[2][(TY + 1) * TX];  // theta' / qv (or a moisture pair)
   __shared__ __align__(8) unsigned long long sbar[kStageRing];
   // the flags, fixed at compile time for the kSpec composition
   const bool f_weno = kSpec || fl.weno_scalars, f_adv = kSpec || fl.weno_advective;
