@@ -2190,11 +2190,15 @@ __global__ void __launch_bounds__(128, 7) k_mx_hevi_tmad(const __grid_constant__
 // and marches up the levels, reading w~(k+1) (and correcting it) before it
 // writes w(k+1), so no other thread's read races a write (pi' itself is not
 // changed; the u/v updates read it across columns).
+// Each thread marches two column positions, blockDim.x apart in i (so each
+// load instruction stays coalesced), as two independent chains: half the
+// threads, all resident at once at 512 x 512, twice the loads in flight each.
+constexpr int kFixPos = 2;
 __device__ __forceinline__ void fix_body(const Dims& d, const Tab& t, const Flags& fl, const WS& s, float dtau,
                                          int bx, int by) {
-  const int i = bx * blockDim.x + threadIdx.x;
+  const int i0 = bx * blockDim.x * kFixPos + threadIdx.x;
   const int j = by * blockDim.y + threadIdx.y;
-  if (i > d.nx || j > d.ny) return;
+  if (i0 > d.nx || j > d.ny) return;
   const int nz = d.nz;
   const float* __restrict__ pn = s.f[PI];
   float* __restrict__ su = s.f[U];
@@ -2202,61 +2206,83 @@ __device__ __forceinline__ void fix_body(const Dims& d, const Tab& t, const Flag
   float* __restrict__ sw = s.f[W];
   float* __restrict__ sr = s.f[RHO];
   const float cp = (float)kCp, b = (float)fl.hevi_beta, cb = dtau * b * cp, db = dtau * b;
-  const bool du = j < d.ny, dv = i < d.nx, cell = du && dv;
-  // (indices clamped into the grid; each is used only where it is in range;
-  // 32-bit offsets: a field has < 2^32 elements, checked when the model is made)
-  const int ic = imin(i, d.nx - 1), jc = imin(j, d.ny - 1);
-  const int ip = ic, im = imax(i - 1, 0), jp = jc, jm = imax(j - 1, 0);
   const unsigned pl = (unsigned)d.plane, P = (unsigned)d.P;
-  const unsigned cf = j * P + i;                    // u face (j < ny), v face (i < nx)
-  const unsigned ue = jc * P + ip, uw = jc * P + im;  // pi' beside the u face
-  const unsigned vn = jp * P + ic, vs = jm * P + ic;  // pi' beside the v face
-  const unsigned cc = jc * P + ic;                  // the cell (i, j) when cell
+  // per position (indices clamped into the grid; each is used only where it
+  // is in range; 32-bit offsets: a field has < 2^32 elements, checked when
+  // the model is made)
+  bool du[kFixPos], dv[kFixPos], cell[kFixPos];
+  unsigned cf[kFixPos], ue[kFixPos], uw[kFixPos], vn[kFixPos], vs[kFixPos], cc[kFixPos];
+#pragma unroll
+  for (int c = 0; c < kFixPos; ++c) {
+    const int i = i0 + c * (int)blockDim.x;
+    const bool in = i <= d.nx;
+    du[c] = in && j < d.ny;
+    dv[c] = in && i < d.nx;
+    cell[c] = du[c] && dv[c];
+    const int ii = imin(i, d.nx);
+    const int ic = imin(ii, d.nx - 1), jc = imin(j, d.ny - 1);
+    const int ip = ic, im = imax(ii - 1, 0), jp = jc, jm = imax(j - 1, 0);
+    cf[c] = j * P + ii;                            // u face (j < ny), v face (i < nx)
+    ue[c] = jc * P + ip, uw[c] = jc * P + im;      // pi' beside the u face
+    vn[c] = jp * P + ic, vs[c] = jm * P + ic;      // pi' beside the v face
+    cc[c] = jc * P + ic;                           // the cell (i, j) when cell
+  }
   // a level's inputs, loaded one level ahead so that their latency overlaps
   // the level below's arithmetic and stores
   struct Lv {
     float uc, ue, uw, vc, vn, vs, rc, wn, pn;
   };
-  auto load = [&](int k) {
+  auto load = [&](int k, int c) {
     const unsigned o = (unsigned)k * pl;
     Lv L = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-    if (du) {
-      L.uc = su[cf + o];
-      L.ue = pn[ue + o];
-      L.uw = pn[uw + o];
+    if (du[c]) {
+      L.uc = su[cf[c] + o];
+      L.ue = pn[ue[c] + o];
+      L.uw = pn[uw[c] + o];
     }
-    if (dv) {
-      L.vc = sv[cf + o];
-      L.vn = pn[vn + o];
-      L.vs = pn[vs + o];
+    if (dv[c]) {
+      L.vc = sv[cf[c] + o];
+      L.vn = pn[vn[c] + o];
+      L.vs = pn[vs[c] + o];
     }
-    if (cell) {
-      L.rc = sr[cc + o];
-      L.wn = sw[cc + o + pl];                       // w~(k+1) (w has nz+1 faces)
-      if (k + 1 < nz) L.pn = pn[cc + o + pl];       // pi'(k+1)
+    if (cell[c]) {
+      L.rc = sr[cc[c] + o];
+      L.wn = sw[cc[c] + o + pl];                     // w~(k+1) (w has nz+1 faces)
+      if (k + 1 < nz) L.pn = pn[cc[c] + o + pl];     // pi'(k+1)
     }
     return L;
   };
-  float pk = cell ? pn[cc] : 0.f, wk = cell ? sw[cc] : 0.f;  // pi'(k), w(k) (w(0) = w~(0))
-  Lv cur = load(0);
+  float pk[kFixPos], wk[kFixPos];  // pi'(k), w(k) (w(0) = w~(0))
+  Lv cur[kFixPos];
+#pragma unroll
+  for (int c = 0; c < kFixPos; ++c) {
+    pk[c] = cell[c] ? pn[cc[c]] : 0.f;
+    wk[c] = cell[c] ? sw[cc[c]] : 0.f;
+    cur[c] = load(0, c);
+  }
   for (int k = 0; k < nz; ++k) {
-    const Lv nxt = (k + 1 < nz) ? load(k + 1) : cur;
+    Lv nxt[kFixPos];
+#pragma unroll
+    for (int c = 0; c < kFixPos; ++c) nxt[c] = (k + 1 < nz) ? load(k + 1, c) : cur[c];
     const unsigned o = (unsigned)k * pl;
-    if (du) su[cf + o] = cur.uc + dtau * (-cp * t.t0c[k] * (cur.ue - cur.uw) * t.dx_inv);
-    if (dv) sv[cf + o] = cur.vc + dtau * (-cp * t.t0c[k] * (cur.vn - cur.vs) * t.dy_inv);
-    if (cell) {
-      const unsigned c = cc + o;
-      const float pk1 = cur.pn;
-      const float wk1 = defer_fix_w(t, nz, cb, cur.wn, pk1, pk, k + 1);
-      sr[c] = defer_fix_rho(t, db, cur.rc, wk, wk1, k);
-      if (k >= 1) sw[c] = wk;  // faces 1 .. nz-1 (w(0) and w(nz) keep w~)
-      wk = wk1;
-      pk = pk1;
+#pragma unroll
+    for (int c = 0; c < kFixPos; ++c) {
+      if (du[c]) su[cf[c] + o] = cur[c].uc + dtau * (-cp * t.t0c[k] * (cur[c].ue - cur[c].uw) * t.dx_inv);
+      if (dv[c]) sv[cf[c] + o] = cur[c].vc + dtau * (-cp * t.t0c[k] * (cur[c].vn - cur[c].vs) * t.dy_inv);
+      if (cell[c]) {
+        const unsigned q = cc[c] + o;
+        const float pk1 = cur[c].pn;
+        const float wk1 = defer_fix_w(t, nz, cb, cur[c].wn, pk1, pk[c], k + 1);
+        sr[q] = defer_fix_rho(t, db, cur[c].rc, wk[c], wk1, k);
+        if (k >= 1) sw[q] = wk[c];  // faces 1 .. nz-1 (w(0) and w(nz) keep w~)
+        wk[c] = wk1;
+        pk[c] = pk1;
+      }
+      cur[c] = nxt[c];
     }
-    cur = nxt;
   }
 }
-__global__ void k_mx_fix(const __grid_constant__ Dims d, const __grid_constant__ Tab t,
+__global__ void __launch_bounds__(128, 8) k_mx_fix(const __grid_constant__ Dims d, const __grid_constant__ Tab t,
                          const __grid_constant__ Flags fl, const __grid_constant__ WS s, float dtau) {
   fix_body(d, t, fl, s, dtau, blockIdx.x, blockIdx.y);
 }
@@ -2680,7 +2706,7 @@ bool mixed_hevi_defers(const Dims& d) { return hevi_tma_variant(d) == 5; }
 
 void mixed_uv_fix(const Dims& d, const Tab& t, const Flags& fl, const WS& s, float dtau, cudaStream_t stream) {
   const dim3 b(32, 4);
-  k_mx_fix<<<g3(d.nx + 1, d.ny + 1, 1, b), b, 0, stream>>>(d, t, fl, s, dtau);
+  k_mx_fix<<<g3((d.nx + 1 + kFixPos - 1) / kFixPos, d.ny + 1, 1, b), b, 0, stream>>>(d, t, fl, s, dtau);
 }
 
 int mixed_hevi_substep(const Dims& d, const Tab& t, const Flags& fl, const WS& win, const WS& wout, float dtau,
@@ -2862,7 +2888,7 @@ __global__ void k_b_uv(const UvArgs* __restrict__ A, const int* __restrict__ sta
   const int l = (int)blockIdx.x - start[dom];
   fb_mom_body(a.d, a.t, a.win, a.wout, a.dtau, 0, l % a.gx, (l / a.gx) % a.gy, l / (a.gx * a.gy));
 }
-__global__ void k_b_fix(const UvArgs* __restrict__ A, const int* __restrict__ start, int nd) {
+__global__ void __launch_bounds__(128, 8) k_b_fix(const UvArgs* __restrict__ A, const int* __restrict__ start, int nd) {
   const int dom = find_domain(start, nd);
   const UvArgs& a = A[dom];
   const int l = (int)blockIdx.x - start[dom];
@@ -3009,7 +3035,7 @@ MixedBatch* mixed_batch_build(const std::vector<MixedDomain>& doms, const Flags&
       a.win = ws_from(sub_out(m, n_sub - 1));
       a.wout = a.win;
       a.dtau = dtau;
-      a.gx = ceil_div(m.d.nx + 1, 32);
+      a.gx = ceil_div(m.d.nx + 1, b->defer ? 32 * kFixPos : 32);  // (the fix-up: kFixPos positions per thread)
       a.gy = ceil_div(m.d.ny + 1, 4);
       a.gz = b->defer ? 1 : m.d.nz;  // the deferred fix-up marches the levels
       start[q] = ub;
