@@ -49,7 +49,8 @@ typedef struct CUstream_st *vibe_stream_t; /* == cudaStream_t */
  * entries (a[k-1] is row k's sub-diagonal) and may be NULL (= 0). ws (n) is
  * caller workspace, as in the reference; its contents on return are
  * unspecified. Returns VIBE_C_OK, VIBE_C_ERR_SINGULAR on a zero pivot,
- * VIBE_C_ERR_BAD_ARG, or VIBE_C_ERR_DEVICE. */
+ * VIBE_C_ERR_BAD_ARG, or VIBE_C_ERR_DEVICE; x is written only on VIBE_C_OK
+ * (as the reference, which returns before it writes x). */
 int vibe_tridiagonal_solve_f64(const double *a, const double *b, const double *c,
                                const double *d, int n, double *x, double *ws);
 
@@ -59,15 +60,19 @@ void vibe_weno5_reconstruct_f64(double qm2, double qm1, double q0, double q1,
                                 double q2, double *q_left, double *q_right);
 
 /* Replaces c_kernels.h:77-78. Bilinear sample of a halo'd FieldT-layout
- * array at fractional cell index (xi, yj), level k, clamped to the interior.
- * Returns 0 for NULL f or nz <= 0. */
+ * array at fractional cell index (xi, yj), level k, clamped to the interior
+ * in the reference's order (up to 0, then down to n-1: a grid without
+ * interior points reads its last halo point). Returns 0 for NULL f or
+ * nz <= 0; NaN (vibe_c_last_error() says why) for halo < 0 or a plane
+ * narrower than halo + 1, where the reference reads outside the plane. */
 double vibe_bilinear_f64(const double *f, int halo, int nsx, int nsy, int nz,
                          double xi, double yj, int k);
 
 /* Replaces c_kernels.h:89-92. Max over cells of
  * dt*(|u|/dx + |v|/dy + |w|/max(dzeta[k]*(z_top - zs), 1)); also the max wind
  * speed and the min dz (0 when none). zs may be NULL (flat). Returns 0 when
- * u, v, w or dzeta is NULL. */
+ * u, v, w or dzeta is NULL (outputs untouched), and 0 with both outputs 0 on
+ * a grid with nx, ny or nz <= 0 (no cells). */
 double vibe_cfl_scan_f64(const double *u, const double *v, const double *w,
                          const double *dzeta, const double *zs, int nx, int ny,
                          int nz, double dx, double dy, double z_top, double dt,
@@ -81,7 +86,8 @@ double vibe_neumaier_sum_f64(const double *x, size_t n);
 
 /* Replaces c_kernels.h:113-117. Second-order flux-form advection on
  * collocated, halo-free, i-fastest arrays, periodic in x and y, zero vertical
- * flux on the first and last level. Silently returns on NULL arguments. */
+ * flux on the first and last level. Silently returns on NULL arguments and on
+ * a grid with nx, ny or nz <= 0 (dqdt untouched). */
 void vibe_advect_scalar_flux_f64(const double *q, const double *rho,
                                  const double *u, const double *v, const double *w,
                                  const double *dzeta, const double *zs, int nx,
@@ -133,7 +139,8 @@ int vibe_tridiagonal_solve_batched_f64_dev_noalloc(const double *a, const double
                                                    const double *c, const double *d,
                                                    int n, int n_sys, double *x,
                                                    int *status, vibe_stream_t stream);
-/* Host-pointer batched form; returns the first non-zero per-system code. */
+/* Host-pointer batched form; returns the first non-zero per-system code and
+ * writes x only for the systems that solved. */
 int vibe_tridiagonal_solve_batched_f64(const double *a, const double *b,
                                        const double *c, const double *d, int n,
                                        int n_sys, double *x);
@@ -141,6 +148,9 @@ int vibe_tridiagonal_solve_batched_f64(const double *a, const double *b,
 int vibe_weno5_reconstruct_batched_f64_dev(const double *q, size_t n,
                                            double *q_left, double *q_right,
                                            vibe_stream_t stream);
+/* The CFL scan and the flux advection on device pointers: VIBE_C_ERR_BAD_ARG
+ * for a negative dimension; a grid with a zero dimension gives (0, 0, 0) in
+ * out3 and leaves dqdt untouched. n = 0 sums to 0. */
 int vibe_cfl_scan_f64_dev(const double *u, const double *v, const double *w,
                           const double *dzeta, const double *zs, int nx, int ny,
                           int nz, double dx, double dy, double z_top, double dt,

@@ -2273,9 +2273,13 @@ double vo_bilinear(const double *f, int halo, int nsx, int nsy, int nz, double x
   if (k >= nz) k = nz - 1;
   const int i0 = (int)floor(xi), j0 = (int)floor(yj);
   const double wx = xi - (double)i0, wy = yj - (double)j0;
-  int ia = i0, ib = i0 + 1, ja = j0, jb = j0 + 1;
-  ia = iclamp(ia, 0, nxi - 1); ib = iclamp(ib, 0, nxi - 1);
-  ja = iclamp(ja, 0, nyi - 1); jb = iclamp(jb, 0, nyi - 1);
+  /* c_kernels.c:128-135 clamps up to 0 first and then down to n-1 (with
+   * n <= 0 the index ends at n-1, a halo point) */
+  int ia = i0 < 0 ? 0 : i0, ib = i0 + 1 < 0 ? 0 : i0 + 1, ja = j0 < 0 ? 0 : j0, jb = j0 + 1 < 0 ? 0 : j0 + 1;
+  if (ia > nxi - 1) ia = nxi - 1;
+  if (ib > nxi - 1) ib = nxi - 1;
+  if (ja > nyi - 1) ja = nyi - 1;
+  if (jb > nyi - 1) jb = nyi - 1;
 #define F_AT(I, J) f[(((size_t)(k + halo) * (size_t)nsy + (size_t)((J) + halo)) * (size_t)nsx) + (size_t)((I) + halo)]
   const double q00 = F_AT(ia, ja), q10 = F_AT(ib, ja), q01 = F_AT(ia, jb), q11 = F_AT(ib, jb);
 #undef F_AT

@@ -563,3 +563,23 @@ def test_kessler_coupling_in_rk3_step(oc):
     dry = oc.Model(small(oc, qv_surface=0.0), "port")
     for t in oc.kessler_tendency(dry, k, 1.0):
         assert not np.any(t)
+
+
+# ---- C-ABI edge cases (NULL arguments, empty and negative grids, a grid
+# without interior points, one-row systems) -----------------------------------
+def test_oracle_c_abi_edge_cases(oc):
+    import cabi_edge_cases as ce
+    out = ce.run_cases(ce.oracle_table(oc.PORT_SO))
+    assert out[0] == 0 and out[1][0] == 1.5  # one row: d / b
+    assert out[2] == 1 and out[3][0] == -7.0  # zero one-row pivot: singular, x untouched
+    assert out[4] == 2 and out[5][0] == -7.0  # n = 0: bad argument
+    assert out[6] == 0 and list(out[7]) == [0.5, 0.75, -0.625]  # a, c NULL: diagonal
+    assert out[8] == -7.0  # WENO5 with a NULL output writes nothing
+    assert out[9] == out[10] == out[11] == 0.0  # bilinear: NULL f, nz <= 0
+    assert all(np.all(a == 7.0) for a in out[-4:])  # flux: dqdt untouched
+
+
+@need_ref
+def test_c_abi_edge_cases_port_is_bit_exact_to_reference(oc):
+    import cabi_edge_cases as ce
+    ce.compare(ce.run_cases(ce.oracle_table(oc.PORT_SO)), ce.run_cases(ce.reference_table(oc.REF_SO)))

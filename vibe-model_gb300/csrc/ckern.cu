@@ -326,8 +326,11 @@ __global__ void k_bilinear(const T* __restrict__ plane, int halo, int nsx, int n
   const int nxi = nsx - 2 * halo, nyi = nsy - 2 * halo;
   const int i0 = (int)floor(xi), j0 = (int)floor(yj);
   const T wx = xi - (T)i0, wy = yj - (T)j0;
-  const int ia = vgb::iclamp(i0, 0, nxi - 1), ib = vgb::iclamp(i0 + 1, 0, nxi - 1);
-  const int ja = vgb::iclamp(j0, 0, nyi - 1), jb = vgb::iclamp(j0 + 1, 0, nyi - 1);
+  // the reference's clamp order (c_kernels.c:128-135): up to 0 first, then
+  // down to n-1, so a grid without interior points reads its last halo point
+  auto clamp = [](int v, int n) { v = v < 0 ? 0 : v; return v > n - 1 ? n - 1 : v; };
+  const int ia = clamp(i0, nxi), ib = clamp(i0 + 1, nxi);
+  const int ja = clamp(j0, nyi), jb = clamp(j0 + 1, nyi);
   auto at = [&](int i, int j) { return plane[(size_t)(j + halo) * nsx + (size_t)(i + halo)]; };
   const T q00 = at(ia, ja), q10 = at(ib, ja), q01 = at(ia, jb), q11 = at(ib, jb);
   *out = (q00 + wx * (q10 - q00)) + wy * ((q01 + wx * (q11 - q01)) - (q00 + wx * (q10 - q00)));
@@ -565,7 +568,11 @@ int thomas_batched_host(const T* a, const T* b, const T* c, const T* d, int n, i
   HostCall hc;
   const int ia = hc.add(a, no * e, HostCall::kIn), ib = hc.add(b, nn * e, HostCall::kIn);
   const int ic = hc.add(c, no * e, HostCall::kIn), id = hc.add(d, nn * e, HostCall::kIn);
-  const int ix = hc.add(x, nn * e, HostCall::kOut), is = hc.add(nullptr, (size_t)n_sys * sizeof(int), HostCall::kOut);
+  // x comes back through the staging buffer and is copied out only for the
+  // systems that solved: a failed system's x stays as it was, as in the
+  // reference, which returns before it writes x (c_kernels.c:26,34,40)
+  const int ix = hc.add(nullptr, nn * e, HostCall::kOut);
+  const int is = hc.add(nullptr, (size_t)n_sys * sizeof(int), HostCall::kOut);
   const int iw = hc.add(nullptr, thomas_work(n, n_sys) * e, HostCall::kScratch);
   if (!hc.commit()) return VIBE_C_ERR_DEVICE;
   int rc = thomas_launch<T>(hc.dev<T>(ia), hc.dev<T>(ib), hc.dev<T>(ic), hc.dev<T>(id), n, n_sys, hc.dev<T>(ix),
@@ -573,9 +580,14 @@ int thomas_batched_host(const T* a, const T* b, const T* c, const T* d, int n, i
   if (!hc.finish()) return VIBE_C_ERR_DEVICE;
   if (rc) return rc;
   const int* sv = (const int*)hc.host(is);
-  for (int q = 0; q < n_sys; ++q)
-    if (sv[q] != VIBE_C_OK) return sv[q];
-  return VIBE_C_OK;
+  const T* xv = (const T*)hc.host(ix);
+  for (int q = 0; q < n_sys; ++q) {
+    if (sv[q] == VIBE_C_OK)
+      std::memcpy(x + (size_t)q * n, xv + (size_t)q * n, (size_t)n * e);
+    else if (rc == VIBE_C_OK)
+      rc = sv[q];
+  }
+  return rc;
 }
 
 template <typename T>
@@ -605,6 +617,10 @@ void weno_host(T qm2, T qm1, T q0, T q1, T q2, T* q_left, T* q_right) {
 template <typename T>
 T bilinear_host(const T* f, int halo, int nsx, int nsy, int nz, T xi, T yj, int k) {
   if (f == nullptr || nz <= 0) return (T)0;
+  if (halo < 0 || nsx < halo + 1 || nsy < halo + 1) {  // the clamped point would lie outside the plane
+    g_cerr = "bilinear: halo < 0 or a plane narrower than halo + 1";
+    return (T)NAN;
+  }
   if (k < 0) k = 0;
   if (k >= nz) k = nz - 1;
   const size_t plane = (size_t)nsx * nsy, e = sizeof(T);
@@ -644,9 +660,13 @@ template <typename T>
 T cfl_host(const T* u, const T* v, const T* w, const T* dzeta, const T* zs, int nx, int ny, int nz, T dx, T dy, T z_top,
            T dt, T* max_wind_out, T* min_dz_out) {
   if (u == nullptr || v == nullptr || w == nullptr || dzeta == nullptr) return (T)0;
+  if (nx <= 0 || ny <= 0 || nz <= 0) {  // no cells: the reference's loops run zero times
+    if (max_wind_out) *max_wind_out = (T)0;
+    if (min_dz_out) *min_dz_out = (T)0;
+    return (T)0;
+  }
   const size_t e = sizeof(T);
-  const size_t n = (size_t)(nx > 0 ? nx : 0) * (ny > 0 ? ny : 0) * (nz > 0 ? nz : 0);
-  const size_t nzp = (size_t)(nz > 0 ? nz : 0), nxy = (size_t)(nx > 0 ? nx : 0) * (ny > 0 ? ny : 0);
+  const size_t n = (size_t)nx * ny * nz, nzp = (size_t)nz, nxy = (size_t)nx * ny;
   T r[3] = {(T)NAN, (T)NAN, (T)NAN};
   HostCall hc;
   const int iu = hc.add(u, n * e, HostCall::kIn), iv = hc.add(v, n * e, HostCall::kIn),
@@ -698,7 +718,7 @@ T neu_host(const T* x, size_t n) {
 template <typename T>
 int flux_dev(const T* q, const T* rho, const T* u, const T* v, const T* w, const T* dzeta, const T* zs, int nx, int ny,
              int nz, T dx, T dy, T z_top, T* dqdt, vibe_stream_t stream) {
-  if (!q || !rho || !u || !v || !w || !dzeta || !dqdt) return VIBE_C_ERR_BAD_ARG;
+  if (!q || !rho || !u || !v || !w || !dzeta || !dqdt || nx < 0 || ny < 0 || nz < 0) return VIBE_C_ERR_BAD_ARG;
   const size_t n = (size_t)nx * ny * nz;
   if (n == 0) return VIBE_C_OK;
   const int blocks = (int)((n + 255) / 256 < 65535 ? (n + 255) / 256 : 65535);
@@ -712,8 +732,8 @@ void flux_host(const T* q, const T* rho, const T* u, const T* v, const T* w, con
   if (q == nullptr || rho == nullptr || u == nullptr || v == nullptr || w == nullptr || dzeta == nullptr ||
       dqdt == nullptr)
     return;
+  if (nx <= 0 || ny <= 0 || nz <= 0) return;  // no cells: the reference's loops run zero times
   const size_t n = (size_t)nx * ny * nz, e = sizeof(T);
-  if (n == 0) return;
   HostCall hc;
   const int iq = hc.add(q, n * e, HostCall::kIn), ir = hc.add(rho, n * e, HostCall::kIn),
             iu = hc.add(u, n * e, HostCall::kIn), iv = hc.add(v, n * e, HostCall::kIn),
