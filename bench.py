@@ -234,6 +234,88 @@ def nest_leg(vg, torch, warmup, steps=4):
 WIN = dict(nx=192, ny=192, nz=50, dx=3000.0, dt=15.0, n_steps=120, every=10, tl_sub=12)
 
 
+def ckernels_leg(vg, torch, reps=10, warmup=3):
+    """The C-ABI kernels (include/vibe_c_kernels.h, device-pointer forms) on
+    inputs larger than L2, each timed with CUDA events on the calling stream
+    over `reps` calls after `warmup`: algorithmic bytes (every input read once,
+    every output written once) per call over the call's time."""
+    import ctypes
+    vp, i32, f64, sz = ctypes.c_void_p, ctypes.c_int, ctypes.c_double, ctypes.c_size_t
+    lib = ctypes.CDLL(vg.lib._name)  # a handle of its own: its argument types stay here
+    sigs = {"vibe_tridiagonal_solve_batched_f64_dev": [vp] * 4 + [i32, i32, vp, vp, vp],
+            "vibe_weno5_reconstruct_batched_f64_dev": [vp, sz, vp, vp, vp],
+            "vibe_cfl_scan_f64_dev": [vp] * 5 + [i32] * 3 + [f64] * 4 + [vp, vp],
+            "vibe_neumaier_sum_f64_dev": [vp, sz, vp, vp],
+            "vibe_advect_scalar_flux_f64_dev": [vp] * 7 + [i32] * 3 + [f64] * 3 + [vp, vp]}
+    fn = {}
+    for name, args in sigs.items():
+        f = getattr(lib, name)
+        f.restype, f.argtypes = i32, args
+        fn[name] = f
+    dev = torch.device("cuda", torch.cuda.current_device())
+    st = torch.cuda.Stream(dev)
+    h = st.cuda_stream
+    peak, kind = measured_peak()
+    gen = torch.Generator(device=dev).manual_seed(5)
+    rnd = lambda *shape: torch.rand(*shape, dtype=torch.float64, device=dev, generator=gen)  # noqa: E731
+
+    def timed(call, nbytes, what):
+        for _ in range(warmup):
+            assert call() == 0, what
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize(dev)
+        e0.record(st)
+        for _ in range(reps):
+            call()
+        e1.record(st)
+        torch.cuda.synchronize(dev)
+        ms = e0.elapsed_time(e1) / reps
+        gbs = nbytes / (ms * 1e-3) / 1e9
+        return {"workload": what, "ms": ms, "bytes": nbytes, "gbs": gbs, "frac": gbs / peak}
+
+    out = {"peak_gbs": peak, "peak_kind": kind, "reps": reps}
+    nx, ny, nz = NX, NY, NZ
+    with torch.cuda.stream(st):
+        for n, n_sys in ((NZ, nx * ny), (200, 65536)):  # a column of the workload; a tall system (warp per system)
+            a, c = -rnd(n_sys, n - 1), -rnd(n_sys, n - 1)
+            b, d = 4.0 + rnd(n_sys, n), rnd(n_sys, n)
+            x = torch.empty_like(b)
+            f = fn["vibe_tridiagonal_solve_batched_f64_dev"]
+            key = "thomas_batched_n%d" % n
+            out[key] = timed(lambda: f(a.data_ptr(), b.data_ptr(), c.data_ptr(), d.data_ptr(), n, n_sys,
+                                       x.data_ptr(), None, h),
+                             8 * (2 * (n - 1) + 3 * n) * n_sys, "%d systems of %d rows" % (n_sys, n))
+            del a, b, c, d, x
+        nf = 16 * 1024 * 1024
+        q, ql, qr = rnd(5 * nf), torch.empty(nf, dtype=torch.float64, device=dev), \
+            torch.empty(nf, dtype=torch.float64, device=dev)
+        f = fn["vibe_weno5_reconstruct_batched_f64_dev"]
+        out["weno5_batched"] = timed(lambda: f(q.data_ptr(), nf, ql.data_ptr(), qr.data_ptr(), h), 56 * nf,
+                                     "%d stencils" % nf)
+        del q, ql, qr
+        n = nx * ny * nz
+        u, v, w = 20.0 * rnd(n) - 10.0, 20.0 * rnd(n) - 10.0, rnd(n) - 0.5
+        dz, zs = 0.01 + 0.01 * rnd(nz), 500.0 * rnd(nx * ny)
+        o3 = torch.empty(3, dtype=torch.float64, device=dev)
+        f = fn["vibe_cfl_scan_f64_dev"]
+        out["cfl_scan"] = timed(lambda: f(u.data_ptr(), v.data_ptr(), w.data_ptr(), dz.data_ptr(), zs.data_ptr(),
+                                          nx, ny, nz, 1000.0, 1000.0, 20000.0, 6.0, o3.data_ptr(), h),
+                                24 * n + 8 * (nx * ny + nz), "%dx%dx%d cells" % (nx, ny, nz))
+        qq, rho, dq = rnd(n), 1.0 + rnd(n), torch.empty(n, dtype=torch.float64, device=dev)
+        f = fn["vibe_advect_scalar_flux_f64_dev"]
+        out["advect_scalar_flux"] = timed(
+            lambda: f(qq.data_ptr(), rho.data_ptr(), u.data_ptr(), v.data_ptr(), w.data_ptr(), dz.data_ptr(),
+                      zs.data_ptr(), nx, ny, nz, 1000.0, 1000.0, 20000.0, dq.data_ptr(), h),
+            48 * n + 8 * (nx * ny + nz), "%dx%dx%d cells" % (nx, ny, nz))
+        del u, v, w, qq, rho, dq
+        ns = 64 * 1024 * 1024
+        xs, s = rnd(ns), torch.empty(1, dtype=torch.float64, device=dev)
+        f = fn["vibe_neumaier_sum_f64_dev"]
+        out["neumaier_sum"] = timed(lambda: f(xs.data_ptr(), ns, s.data_ptr(), h), 8 * ns, "%d doubles" % ns)
+        del xs
+    return out
+
+
 def window_leg(vg, torch):
     case = {k: v for k, v in CASE.items() if k not in ("dx", "dy", "nz", "zeta_stretch", "hevi_beta")}
     s = vg.Setup.defaults(nx=WIN["nx"], ny=WIN["ny"], nz=WIN["nz"], dx=WIN["dx"], dy=WIN["dx"], zeta_stretch=1.0,
@@ -660,9 +742,11 @@ def main():
     ap.add_argument("--no-window", action="store_true", help="skip the TL/AD assimilation-window leg")
     ap.add_argument("--no-tune", action="store_true", help="skip the autotuner (built-in launch shapes)")
     ap.add_argument("--no-physics", action="store_true", help="skip the Kessler physics-coupling leg")
-    ap.add_argument("--only", choices=["all", "mixed", "fp64", "physics", "nest", "si", "window"], default="all",
+    ap.add_argument("--no-ckernels", action="store_true", help="skip the C-ABI kernel leg")
+    ap.add_argument("--only", choices=["all", "mixed", "fp64", "physics", "nest", "si", "window", "ckernels"],
+                    default="all",
                     help="mixed / fp64: time that path only (no e2e, no other legs); physics / nest / si / "
-                         "window: that leg only")
+                         "window / ckernels: that leg only")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -705,6 +789,10 @@ def main():
         return
     if args.only == "window":
         print(json.dumps({"only": "window", "assimilation_window": window_leg(vg, torch)}))
+        ranks.close()
+        return
+    if args.only == "ckernels":
+        print(json.dumps({"only": "ckernels", "c_abi_kernels": ckernels_leg(vg, torch)}))
         ranks.close()
         return
     setup = case_setup(vg.Setup, args.nx, args.ny)
@@ -827,6 +915,12 @@ def main():
     nest = nest_leg(vg, torch, args.warmup) if not args.no_nest else None
     window = window_leg(vg, torch) if not args.no_window else None
     physics = physics_leg(vg, torch) if not args.no_physics else None
+    ckern = None
+    if not args.no_ckernels:
+        try:
+            ckern = ckernels_leg(vg, torch)
+        except Exception as e:  # a side leg: its failure must not cost the headline line
+            ckern = {"error": repr(e)}
 
     value = whole_job_rate(world, cells, args.steps, ms_mx)
     value64 = whole_job_rate(world, cells, k64, ms_64)
@@ -900,6 +994,8 @@ def main():
         line["assimilation_window"] = window
     if physics is not None:
         line["physics_coupling"] = physics
+    if ckern is not None:
+        line["c_abi_kernels"] = ckern
     if cpu is not None:
         line["cpu_baseline"] = cpu
         line["mixed_vs_oracle_error"] = oracle_errors(vg, 128, 128, oracle_record)
