@@ -427,19 +427,34 @@ template <typename T>
 __global__ void k_cfl_partial(const T* __restrict__ u, const T* __restrict__ v, const T* __restrict__ w,
                               const T* __restrict__ dzeta, const T* __restrict__ zs, int nx, int ny, int nz, T dx, T dy,
                               T z_top, T dt, T* __restrict__ partials) {
-  const size_t n = (size_t)nx * ny * nz, nxy = (size_t)nx * ny;
-  T worst = 0, mw = 0, mdz = (T)1e30;
-  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x) {
-    const int k = (int)(e / nxy);
-    const size_t col = e % nxy;
-    const T uu = u[e], vv = v[e], ww = w[e];
-    const T scale = zs ? (z_top - zs[col]) : z_top;
-    T dz = dzeta[k] * scale;
-    if (dz < (T)1) dz = (T)1;
-    mdz = fmin(mdz, dz);
-    mw = fmax(mw, sqrt(uu * uu + vv * vv + ww * ww));
-    worst = fmax(worst, dt * (fabs(uu) / dx + fabs(vv) / dy + fabs(ww) / dz));
+  const size_t n = (size_t)nx * ny * nz, nxy = (size_t)nx * ny;  // (no negative dimension reaches here)
+  // the largest squared speed, one square root at the end: a correctly
+  // rounded square root is monotone, so the maximum of the roots is the root
+  // of the maximum, bit for bit
+  T worst = 0, mw2 = 0, mdz = (T)1e30;
+  const size_t S = (size_t)gridDim.x * blockDim.x;
+  size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (e < n) {
+    // the cell's level and column, stepped along with e (no division per cell)
+    size_t k = e / nxy, col = e - k * nxy;
+    const size_t sk = S / nxy, sc = S - sk * nxy;
+    for (; e < n; e += S) {
+      const T uu = u[e], vv = v[e], ww = w[e];
+      const T scale = zs ? (z_top - zs[col]) : z_top;
+      T dz = dzeta[k] * scale;
+      if (dz < (T)1) dz = (T)1;
+      mdz = fmin(mdz, dz);
+      mw2 = fmax(mw2, uu * uu + vv * vv + ww * ww);
+      worst = fmax(worst, dt * (fabs(uu) / dx + fabs(vv) / dy + fabs(ww) / dz));
+      col += sc;
+      k += sk;
+      if (col >= nxy) {
+        col -= nxy;
+        ++k;
+      }
+    }
   }
+  T mw = sqrt(mw2);
   max3_block(worst, mw, mdz);
   if (threadIdx.x == 0) {
     partials[3 * blockIdx.x] = worst;
